@@ -1,0 +1,1304 @@
+// Test infrastructure: CPU oracle for the batched rigid-body dynamics path.
+//
+// This header is a plain-C++ restatement (no Eigen) of the reference algorithms
+// that the GPU kernels must reproduce.  It is used only by the tests, by the
+// smoke check and by the CPU baseline leg of the benchmark; the product path
+// never links it.  Every function names the reference file:line it follows.
+//
+// Parity status: the reference (Pinocchio 3.7.0) cannot be compiled in this
+// environment (Eigen and Boost are absent), and its tests hold no golden
+// vectors.  The oracle is therefore pinned by the reference's own identity
+// tests (ABA∘RNEA round trip, M·a + nle = tau, CRBA vs RNEA columns,
+// Minv·M = I, UDU^T = M, finite-difference derivative checks, batch == serial)
+// and by analytic known-answer cases.  Against reference *outputs* it is
+// "parity unpinned".
+//
+// Scalar T may be double, long double, float, or the FLOP-counting scalar
+// FlopScalar (flop_scalar.hpp).  Storage conventions:
+//   * SE3: rotation R row-major (R[3*r+c]) and translation t.
+//   * Motion / Force 6-vectors: [linear(0:3); angular(3:6)]
+//     (reference spatial/force-tpl.hpp:27, motion-tpl.hpp).
+//   * Inertia: mass m, lever c (COM), rotational inertia about the COM as a
+//     packed symmetric [xx, xy, yy, xz, yz, zz] (spatial/symmetric3.hpp:46-49).
+//   * 6x6 matrices row-major; 6 x nv sets column-major (column k at 6*k);
+//     nv x nv matrices row-major (the reference's RowMatrixXs,
+//     multibody/data.hpp:401-416).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace orc {
+
+enum JointType { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4 };
+enum Convention { LOCAL = 0, WORLD = 1 };  // reference multibody/fwd.hpp:73-81
+
+// ---------------------------------------------------------------------------
+// scalar helpers (overloaded for every scalar type the oracle is built for)
+// ---------------------------------------------------------------------------
+inline double o_sqrt(double x) { return std::sqrt(x); }
+inline long double o_sqrt(long double x) { return std::sqrt(x); }
+inline float o_sqrt(float x) { return std::sqrt(x); }
+inline void o_sincos(double a, double* s, double* c) { *s = std::sin(a); *c = std::cos(a); }
+inline void o_sincos(long double a, long double* s, long double* c) { *s = std::sin(a); *c = std::cos(a); }
+inline void o_sincos(float a, float* s, float* c) { *s = std::sin(a); *c = std::cos(a); }
+template <class T> inline T o_max(const T& a, const T& b) { return (a < b) ? b : a; }
+template <class T> inline T o_eps() { return std::numeric_limits<T>::epsilon(); }
+
+// ---------------------------------------------------------------------------
+// Model description (double storage) and the tree tables of DataTpl
+// ---------------------------------------------------------------------------
+struct Model {
+  int njoints = 0, nq = 0, nv = 0;
+  std::vector<int> parents, jtype, idx_q, idx_v, nqs, nvs;
+  std::vector<double> placement;  // 12 per joint: R (row-major 9), t (3)
+  std::vector<double> inertia;    // 10 per joint: m, c[3], I[6]
+  std::vector<double> armature;   // nv
+  double gravity[6] = {0, 0, -9.81, 0, 0, 0};
+  // derived tables (multibody/data.hxx:195-306)
+  std::vector<int> lastChild, nvSubtree, parents_fromRow, nvSubtree_fromRow;
+
+  static int joint_nq(int jt) { return jt == JT_FF ? 7 : (jt == JT_NONE ? 0 : 1); }
+  static int joint_nv(int jt) { return jt == JT_FF ? 6 : (jt == JT_NONE ? 0 : 1); }
+
+  // Validates the description and fills the derived tables.
+  // lastChild / nvSubtree: data.hxx:195-225 (no mimic joints).
+  // parents_fromRow / nvSubtree_fromRow: data.hxx:250-306.
+  void finalize() {
+    if (njoints < 1) throw std::invalid_argument("njoints must be >= 1");
+    nqs.assign(njoints, 0);
+    nvs.assign(njoints, 0);
+    idx_q.assign(njoints, 0);
+    idx_v.assign(njoints, 0);
+    int cq = 0, cv = 0;
+    for (int i = 0; i < njoints; ++i) {
+      if (i == 0) {
+        if (jtype[0] != JT_NONE) throw std::invalid_argument("joint 0 must be the universe");
+        continue;
+      }
+      if (jtype[i] < JT_RX || jtype[i] > JT_FF) throw std::invalid_argument("unsupported joint type");
+      if (parents[i] < 0 || parents[i] >= i) throw std::invalid_argument("parents[i] must be < i");
+      nqs[i] = joint_nq(jtype[i]);
+      nvs[i] = joint_nv(jtype[i]);
+      idx_q[i] = cq;
+      idx_v[i] = cv;
+      cq += nqs[i];
+      cv += nvs[i];
+    }
+    nq = cq;
+    nv = cv;
+    if ((int)armature.size() != nv) armature.assign(nv, 0.0);
+    lastChild.assign(njoints, -1);
+    nvSubtree.assign(njoints, 0);
+    for (int i = njoints - 1; i >= 0; --i) {
+      if (lastChild[i] == -1) lastChild[i] = i;
+      const int parent = i > 0 ? parents[i] : 0;
+      lastChild[parent] = std::max(lastChild[i], lastChild[parent]);
+      const int lc = lastChild[i];
+      nvSubtree[i] = idx_v[lc] + nvs[lc] - idx_v[i];
+    }
+    parents_fromRow.assign(nv, -1);
+    nvSubtree_fromRow.assign(nv, 0);
+    for (int j = 1; j < njoints; ++j) {
+      const int parent = parents[j];
+      const int iv = idx_v[j];
+      parents_fromRow[iv] = parent > 0 ? idx_v[parent] + nvs[parent] - 1 : -1;
+      nvSubtree_fromRow[iv] = nvSubtree[j];
+      for (int row = 1; row < nvs[j]; ++row) {
+        parents_fromRow[iv + row] = iv + row - 1;
+        nvSubtree_fromRow[iv + row] = nvSubtree[j] - row;
+      }
+    }
+    // CRBA requires compact (depth-first) subtrees: crba.hxx:573-595.
+    for (int i = 1; i < njoints; ++i) {
+      for (int k = i + 1; k <= lastChild[i]; ++k) {
+        int a = k;
+        while (a > i) a = parents[a];
+        if (a != i) throw std::invalid_argument("joints are not in depth-first order");
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// spatial algebra (restated from the reference spatial/ headers)
+// ---------------------------------------------------------------------------
+template <class T> struct SE3 { T R[9]; T t[3]; };
+template <class T> struct Vec6 { T v[6]; };  // motion or force, [lin; ang]
+template <class T> struct Iner { T m; T c[3]; T I[6]; };
+template <class T> struct Mat6 { T a[36]; };
+
+template <class T> inline void cross3(const T* a, const T* b, T* o) {
+  T x = a[1] * b[2] - a[2] * b[1];
+  T y = a[2] * b[0] - a[0] * b[2];
+  T z = a[0] * b[1] - a[1] * b[0];
+  o[0] = x; o[1] = y; o[2] = z;
+}
+template <class T> inline void matvec(const T* R, const T* x, T* o) {
+  T a = R[0] * x[0] + R[1] * x[1] + R[2] * x[2];
+  T b = R[3] * x[0] + R[4] * x[1] + R[5] * x[2];
+  T c = R[6] * x[0] + R[7] * x[1] + R[8] * x[2];
+  o[0] = a; o[1] = b; o[2] = c;
+}
+template <class T> inline void matTvec(const T* R, const T* x, T* o) {
+  T a = R[0] * x[0] + R[3] * x[1] + R[6] * x[2];
+  T b = R[1] * x[0] + R[4] * x[1] + R[7] * x[2];
+  T c = R[2] * x[0] + R[5] * x[1] + R[8] * x[2];
+  o[0] = a; o[1] = b; o[2] = c;
+}
+template <class T> inline void matmul3(const T* A, const T* B, T* C) {  // C = A B
+  T tmp[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      tmp[3 * r + c] = A[3 * r + 0] * B[0 + c] + A[3 * r + 1] * B[3 + c] + A[3 * r + 2] * B[6 + c];
+  for (int k = 0; k < 9; ++k) C[k] = tmp[k];
+}
+template <class T> inline void matmul3_ABt(const T* A, const T* B, T* C) {  // C = A B^T
+  T tmp[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      tmp[3 * r + c] = A[3 * r + 0] * B[3 * c + 0] + A[3 * r + 1] * B[3 * c + 1] + A[3 * r + 2] * B[3 * c + 2];
+  for (int k = 0; k < 9; ++k) C[k] = tmp[k];
+}
+
+// SE3 composition A*B (spatial/se3-tpl.hpp:314-330).
+template <class T> inline SE3<T> se3_mul(const SE3<T>& A, const SE3<T>& B) {
+  SE3<T> C;
+  matmul3(A.R, B.R, C.R);
+  T rt[3];
+  matvec(A.R, B.t, rt);
+  for (int k = 0; k < 3; ++k) C.t[k] = A.t[k] + rt[k];
+  return C;
+}
+// Motion M.act(m): spatial/motion-dense.hpp:259-263.
+template <class T> inline Vec6<T> act_motion(const SE3<T>& M, const Vec6<T>& m) {
+  Vec6<T> o;
+  matvec(M.R, m.v + 3, o.v + 3);
+  T rl[3], txw[3];
+  matvec(M.R, m.v, rl);
+  cross3(M.t, o.v + 3, txw);
+  for (int k = 0; k < 3; ++k) o.v[k] = rl[k] + txw[k];
+  return o;
+}
+// Motion M.actInv(m): spatial/motion-dense.hpp:274-279.
+template <class T> inline Vec6<T> actinv_motion(const SE3<T>& M, const Vec6<T>& m) {
+  Vec6<T> o;
+  T txw[3], d[3];
+  cross3(M.t, m.v + 3, txw);
+  for (int k = 0; k < 3; ++k) d[k] = m.v[k] - txw[k];
+  matTvec(M.R, d, o.v);
+  matTvec(M.R, m.v + 3, o.v + 3);
+  return o;
+}
+// Force M.act(f): spatial/force-dense.hpp:214-219.
+template <class T> inline Vec6<T> act_force(const SE3<T>& M, const Vec6<T>& f) {
+  Vec6<T> o;
+  matvec(M.R, f.v, o.v);
+  matvec(M.R, f.v + 3, o.v + 3);
+  T txf[3];
+  cross3(M.t, o.v, txf);
+  for (int k = 0; k < 3; ++k) o.v[3 + k] += txf[k];
+  return o;
+}
+// Motion cross v ^ w (spatial/motion-dense.hpp:217-227): w.motionAction(v).
+template <class T> inline Vec6<T> cross_motion(const Vec6<T>& v, const Vec6<T>& w) {
+  Vec6<T> o;
+  T a[3], b[3];
+  cross3(v.v, w.v + 3, a);
+  cross3(v.v + 3, w.v, b);
+  for (int k = 0; k < 3; ++k) o.v[k] = a[k] + b[k];
+  cross3(v.v + 3, w.v + 3, o.v + 3);
+  return o;
+}
+// Force cross v.cross(f) (spatial/force-dense.hpp:178-182): f.motionAction(v).
+template <class T> inline Vec6<T> cross_force(const Vec6<T>& v, const Vec6<T>& f) {
+  Vec6<T> o;
+  cross3(v.v + 3, f.v, o.v);
+  T a[3], b[3];
+  cross3(v.v + 3, f.v + 3, a);
+  cross3(v.v, f.v, b);
+  for (int k = 0; k < 3; ++k) o.v[3 + k] = a[k] + b[k];
+  return o;
+}
+template <class T> inline Vec6<T> add6(const Vec6<T>& a, const Vec6<T>& b) {
+  Vec6<T> o;
+  for (int k = 0; k < 6; ++k) o.v[k] = a.v[k] + b.v[k];
+  return o;
+}
+template <class T> inline Vec6<T> zero6() {
+  Vec6<T> o;
+  for (int k = 0; k < 6; ++k) o.v[k] = T(0);
+  return o;
+}
+
+// Symmetric3 right multiplication (spatial/symmetric3.hpp:490-499).
+template <class T> inline void sym3_mul(const T* S, const T* x, T* o) {
+  T a = S[0] * x[0] + S[1] * x[1] + S[3] * x[2];
+  T b = S[1] * x[0] + S[2] * x[1] + S[4] * x[2];
+  T c = S[3] * x[0] + S[4] * x[1] + S[5] * x[2];
+  o[0] = a; o[1] = b; o[2] = c;
+}
+// Symmetric3 R*S*R^T via the L-decomposition (spatial/symmetric3.hpp:552-600).
+template <class T> inline void sym3_rotate(const T* d, const T* R, T* out) {
+  const T L00 = d[0] - d[5], L01 = d[1];
+  const T L10 = d[1], L11 = d[2] - d[5];
+  const T L20 = T(2) * d[3], L21 = d[4] + d[4];
+  // Y = R.block<2,3>(1,0) * L
+  const T Y00 = R[3] * L00 + R[4] * L10 + R[5] * L20;
+  const T Y01 = R[3] * L01 + R[4] * L11 + R[5] * L21;
+  const T Y10 = R[6] * L00 + R[7] * L10 + R[8] * L20;
+  const T Y11 = R[6] * L01 + R[7] * L11 + R[8] * L21;
+  T s[6];
+  s[1] = Y00 * R[0] + Y01 * R[1];
+  s[2] = Y00 * R[3] + Y01 * R[4];
+  s[3] = Y10 * R[0] + Y11 * R[1];
+  s[4] = Y10 * R[3] + Y11 * R[4];
+  s[5] = Y10 * R[6] + Y11 * R[7];
+  const T r0 = -R[0] * d[4] + R[1] * d[3];
+  const T r1 = -R[3] * d[4] + R[4] * d[3];
+  const T r2 = -R[6] * d[4] + R[7] * d[3];
+  s[0] = L00 + L11 - s[2] - s[5];
+  s[0] += d[5];
+  s[1] += r2;
+  s[2] += d[5];
+  s[3] -= r1;
+  s[4] += r0;
+  s[5] += d[5];
+  for (int k = 0; k < 6; ++k) out[k] = s[k];
+}
+
+// Inertia * motion (spatial/inertia.hpp:729-735).
+template <class T> inline Vec6<T> iner_mul(const Iner<T>& Y, const Vec6<T>& v) {
+  Vec6<T> f;
+  T cxw[3];
+  cross3(Y.c, v.v + 3, cxw);
+  for (int k = 0; k < 3; ++k) f.v[k] = Y.m * (v.v[k] - cxw[k]);
+  sym3_mul(Y.I, v.v + 3, f.v + 3);
+  T cxf[3];
+  cross3(Y.c, f.v, cxf);
+  for (int k = 0; k < 3; ++k) f.v[3 + k] += cxf[k];
+  return f;
+}
+// M.act(Y) (spatial/inertia.hpp:873-880).
+template <class T> inline Iner<T> iner_act(const SE3<T>& M, const Iner<T>& Y) {
+  Iner<T> o;
+  o.m = Y.m;
+  T rc[3];
+  matvec(M.R, Y.c, rc);
+  for (int k = 0; k < 3; ++k) o.c[k] = M.t[k] + rc[k];
+  sym3_rotate(Y.I, M.R, o.I);
+  return o;
+}
+// Ya += Yb (spatial/inertia.hpp:659-673).
+template <class T> inline void iner_add(Iner<T>& Ya, const Iner<T>& Yb) {
+  const T eps = o_eps<T>();
+  const T mab = Ya.m + Yb.m;
+  const T mab_inv = T(1) / o_max(mab, eps);
+  T AB[3];
+  for (int k = 0; k < 3; ++k) AB[k] = Ya.c[k] - Yb.c[k];
+  const T sa = Ya.m * mab_inv, sb = Yb.m * mab_inv;
+  for (int k = 0; k < 3; ++k) Ya.c[k] *= sa;
+  for (int k = 0; k < 3; ++k) Ya.c[k] += sb * Yb.c[k];
+  for (int k = 0; k < 6; ++k) Ya.I[k] += Yb.I[k];
+  const T al = Ya.m * Yb.m * mab_inv;
+  const T x = AB[0], y = AB[1], z = AB[2];
+  Ya.I[0] += al * (y * y + z * z);
+  Ya.I[1] -= al * x * y;
+  Ya.I[2] += al * (x * x + z * z);
+  Ya.I[3] -= al * x * z;
+  Ya.I[4] -= al * y * z;
+  Ya.I[5] += al * (x * x + y * y);
+  Ya.m = mab;
+}
+// (I - m [c]x^2) packed (Symmetric3 operator-(AlphaSkewSquare), symmetric3.hpp:252-259).
+template <class T> inline void sym3_minus_mskewsq(const T* I, T m, const T* c, T* o) {
+  const T x = c[0], y = c[1], z = c[2];
+  o[0] = I[0] + m * (y * y + z * z);
+  o[1] = I[1] - m * x * y;
+  o[2] = I[2] + m * (x * x + z * z);
+  o[3] = I[3] - m * x * z;
+  o[4] = I[4] - m * y * z;
+  o[5] = I[5] + m * (x * x + y * y);
+}
+template <class T> inline void sym3_full(const T* s, T* M) {  // packed -> 3x3
+  M[0] = s[0]; M[1] = s[1]; M[2] = s[3];
+  M[3] = s[1]; M[4] = s[2]; M[5] = s[4];
+  M[6] = s[3]; M[7] = s[4]; M[8] = s[5];
+}
+// Y.matrix() (spatial/inertia.hpp:481-491).
+template <class T> inline Mat6<T> iner_matrix(const Iner<T>& Y) {
+  Mat6<T> M;
+  for (int k = 0; k < 36; ++k) M.a[k] = T(0);
+  for (int k = 0; k < 3; ++k) M.a[6 * k + k] = Y.m;
+  // ANGULAR,LINEAR = alphaSkew(m, c) (spatial/skew.hpp:134-150)
+  T S[9];
+  S[0] = T(0);
+  S[1] = -Y.c[2] * Y.m;
+  S[2] = Y.c[1] * Y.m;
+  S[3] = -S[1];
+  S[4] = T(0);
+  S[5] = -Y.c[0] * Y.m;
+  S[6] = -S[2];
+  S[7] = -S[5];
+  S[8] = T(0);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      M.a[6 * (3 + r) + c] = S[3 * r + c];
+      M.a[6 * r + 3 + c] = -S[3 * r + c];
+    }
+  T p[6], F[9];
+  sym3_minus_mskewsq(Y.I, Y.m, Y.c, p);
+  sym3_full(p, F);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) M.a[6 * (3 + r) + 3 + c] = F[3 * r + c];
+  return M;
+}
+template <class T> inline void skew3(const T* v, T* M) {
+  M[0] = T(0); M[1] = -v[2]; M[2] = v[1];
+  M[3] = v[2]; M[4] = T(0); M[5] = -v[0];
+  M[6] = -v[1]; M[7] = v[0]; M[8] = T(0);
+}
+// skewSquare(u, v) = v u^T - (u.v) I (spatial/skew.hpp:181-200).
+template <class T> inline void skewsq3(const T* u, const T* v, T* C) {
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) C[3 * r + c] = v[r] * u[c];
+  const T d = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+  C[0] -= d; C[4] -= d; C[8] -= d;
+}
+// Y.variation(v) (spatial/inertia.hpp:750-770).
+template <class T> inline Mat6<T> iner_variation(const Iner<T>& Y, const Vec6<T>& v) {
+  Mat6<T> res;
+  T mvl[3], mva[3];
+  for (int k = 0; k < 3; ++k) { mvl[k] = v.v[k] * Y.m; mva[k] = v.v[3 + k] * Y.m; }
+  T A[9], B[9], C[9], Bla[9];
+  skew3(mvl, A);
+  skewsq3(mva, Y.c, B);
+  skewsq3(Y.c, mva, C);
+  for (int k = 0; k < 9; ++k) Bla[k] = -A[k] - B[k] + C[k];  // LINEAR,ANGULAR block
+  T D1[9], D2[9], Daa[9];
+  skewsq3(mvl, Y.c, D1);
+  skewsq3(Y.c, mvl, D2);
+  for (int k = 0; k < 9; ++k) Daa[k] = -D1[k] - D2[k];
+  T p[6], Ll[9];
+  sym3_minus_mskewsq(Y.I, Y.m, Y.c, p);
+  sym3_full(p, Ll);
+  T Sw[9], P[9];
+  skew3(v.v + 3, Sw);
+  matmul3(Ll, Sw, P);
+  for (int k = 0; k < 9; ++k) Daa[k] -= P[k];
+  // cross(v.ang, Ll): rows = v x (columns) (spatial/skew.hpp:228-245)
+  const T* w = v.v + 3;
+  for (int c = 0; c < 3; ++c) {
+    Daa[0 * 3 + c] += w[1] * Ll[6 + c] - w[2] * Ll[3 + c];
+    Daa[1 * 3 + c] += w[2] * Ll[0 + c] - w[0] * Ll[6 + c];
+    Daa[2 * 3 + c] += w[0] * Ll[3 + c] - w[1] * Ll[0 + c];
+  }
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      res.a[6 * r + c] = T(0);
+      res.a[6 * r + 3 + c] = Bla[3 * r + c];
+      res.a[6 * (3 + r) + c] = Bla[3 * c + r];
+      res.a[6 * (3 + r) + 3 + c] = Daa[3 * r + c];
+    }
+  return res;
+}
+// addForceCrossMatrix (algorithm/rnea-derivatives.hxx:358-367).
+template <class T> inline void add_force_cross_matrix(const Vec6<T>& f, Mat6<T>& M) {
+  auto add_skew = [&](const T* v, int r0, int c0) {  // spatial/skew.hpp:68-82
+    M.a[6 * (r0 + 0) + c0 + 1] -= v[2];
+    M.a[6 * (r0 + 0) + c0 + 2] += v[1];
+    M.a[6 * (r0 + 1) + c0 + 0] += v[2];
+    M.a[6 * (r0 + 1) + c0 + 2] -= v[0];
+    M.a[6 * (r0 + 2) + c0 + 0] -= v[1];
+    M.a[6 * (r0 + 2) + c0 + 1] += v[0];
+  };
+  T nl[3] = {-f.v[0], -f.v[1], -f.v[2]};
+  T na[3] = {-f.v[3], -f.v[4], -f.v[5]};
+  add_skew(nl, 0, 3);
+  add_skew(nl, 3, 0);
+  add_skew(na, 3, 3);
+}
+template <class T> inline Vec6<T> mat6_vec(const Mat6<T>& M, const T* x) {
+  Vec6<T> o;
+  for (int r = 0; r < 6; ++r) {
+    T s = M.a[6 * r] * x[0];
+    for (int c = 1; c < 6; ++c) s += M.a[6 * r + c] * x[c];
+    o.v[r] = s;
+  }
+  return o;
+}
+// SE3actOn(M, I) for a 6x6 matrix (algorithm/aba.hxx:22-76).
+template <class T> inline Mat6<T> se3_act_on(const SE3<T>& M, const Mat6<T>& I) {
+  T Ai[9], Bi[9], Di[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      Ai[3 * r + c] = I.a[6 * r + c];
+      Bi[3 * r + c] = I.a[6 * r + 3 + c];
+      Di[3 * r + c] = I.a[6 * (3 + r) + 3 + c];
+    }
+  const T* R = M.R;
+  const T* t = M.t;
+  T Ao[9], Bo[9], Co[9], Do[9];
+  matmul3(R, Ai, Do);
+  matmul3_ABt(Do, R, Ao);
+  matmul3(R, Bi, Do);
+  matmul3_ABt(Do, R, Bo);
+  matmul3(R, Di, Co);
+  matmul3_ABt(Co, R, Do);
+  for (int k = 0; k < 3; ++k) {  // Do.row(k) += t x Bo.col(k)
+    T col[3] = {Bo[k], Bo[3 + k], Bo[6 + k]}, o[3];
+    cross3(t, col, o);
+    for (int c = 0; c < 3; ++c) Do[3 * k + c] += o[c];
+  }
+  for (int k = 0; k < 3; ++k) {  // Co.col(k) = t x Ao.col(k)
+    T col[3] = {Ao[k], Ao[3 + k], Ao[6 + k]}, o[3];
+    cross3(t, col, o);
+    for (int r = 0; r < 3; ++r) Co[3 * r + k] = o[r];
+  }
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) Co[3 * r + c] += Bo[3 * c + r];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) Bo[3 * r + c] = Co[3 * c + r];
+  for (int k = 0; k < 3; ++k) {  // Do.col(k) += t x Bo.col(k)
+    T col[3] = {Bo[k], Bo[3 + k], Bo[6 + k]}, o[3];
+    cross3(t, col, o);
+    for (int r = 0; r < 3; ++r) Do[3 * r + k] += o[r];
+  }
+  Mat6<T> res;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      res.a[6 * r + c] = Ao[3 * r + c];
+      res.a[6 * r + 3 + c] = Bo[3 * r + c];
+      res.a[6 * (3 + r) + c] = Co[3 * r + c];
+      res.a[6 * (3 + r) + 3 + c] = Do[3 * r + c];
+    }
+  return res;
+}
+
+// Inverse of a small SPD matrix through an unblocked LLT followed by two
+// triangular solves on the identity, as PerformStYSInversion does
+// (multibody/joint/joint-common-operations.hpp:20-33 with Eigen 3.4 LLT).
+template <class T> inline void llt_inverse(int n, const T* A, T* Ainv) {
+  T L[36];
+  for (int k = 0; k < n * n; ++k) L[k] = A[k];
+  for (int k = 0; k < n; ++k) {
+    T x = L[n * k + k];
+    for (int j = 0; j < k; ++j) x -= L[n * k + j] * L[n * k + j];
+    x = o_sqrt(x);
+    L[n * k + k] = x;
+    for (int i = k + 1; i < n; ++i) {
+      T s = L[n * i + k];
+      for (int j = 0; j < k; ++j) s -= L[n * i + j] * L[n * k + j];
+      L[n * i + k] = s / x;
+    }
+  }
+  for (int c = 0; c < n; ++c) {
+    T y[6];
+    for (int i = 0; i < n; ++i) {  // L y = e_c
+      T s = (i == c) ? T(1) : T(0);
+      for (int j = 0; j < i; ++j) s -= L[n * i + j] * y[j];
+      y[i] = s / L[n * i + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {  // L^T x = y
+      T s = y[i];
+      for (int j = i + 1; j < n; ++j) s -= L[n * j + i] * y[j];
+      y[i] = s / L[n * i + i];
+    }
+    for (int i = 0; i < n; ++i) Ainv[n * i + c] = y[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// joint models: revolute about x/y/z and free-flyer
+// ---------------------------------------------------------------------------
+template <class T> inline SE3<T> placement_of(const Model& m, int i) {
+  SE3<T> M;
+  for (int k = 0; k < 9; ++k) M.R[k] = T(m.placement[12 * i + k]);
+  for (int k = 0; k < 3; ++k) M.t[k] = T(m.placement[12 * i + 9 + k]);
+  return M;
+}
+template <class T> inline Iner<T> inertia_of(const Model& m, int i) {
+  Iner<T> Y;
+  Y.m = T(m.inertia[10 * i]);
+  for (int k = 0; k < 3; ++k) Y.c[k] = T(m.inertia[10 * i + 1 + k]);
+  for (int k = 0; k < 6; ++k) Y.I[k] = T(m.inertia[10 * i + 4 + k]);
+  return Y;
+}
+// Joint transform M(q).
+//  * revolute: TransformRevoluteTpl::_setRotation (joint-revolute.hpp:213-235),
+//    angle through SINCOS (math/sincos.hpp:27-55); calc at joint-revolute.hpp:811-821.
+//  * free-flyer: translation q[0:3], rotation = Eigen Quaternion::matrix()
+//    of (x,y,z,w) = q[3:7], not normalised (joint-free-flyer.hpp:333-375).
+template <class T> inline SE3<T> joint_transform(int jt, const T* q) {
+  SE3<T> M;
+  for (int k = 0; k < 9; ++k) M.R[k] = T(0);
+  for (int k = 0; k < 3; ++k) M.t[k] = T(0);
+  if (jt == JT_FF) {
+    const T x = q[3], y = q[4], z = q[5], w = q[6];
+    const T tx = T(2) * x, ty = T(2) * y, tz = T(2) * z;
+    const T twx = tx * w, twy = ty * w, twz = tz * w;
+    const T txx = tx * x, txy = ty * x, txz = tz * x;
+    const T tyy = ty * y, tyz = tz * y, tzz = tz * z;
+    M.R[0] = T(1) - (tyy + tzz); M.R[1] = txy - twz; M.R[2] = txz + twy;
+    M.R[3] = txy + twz; M.R[4] = T(1) - (txx + tzz); M.R[5] = tyz - twx;
+    M.R[6] = txz - twy; M.R[7] = tyz + twx; M.R[8] = T(1) - (txx + tyy);
+    for (int k = 0; k < 3; ++k) M.t[k] = q[k];
+    return M;
+  }
+  T s, c;
+  o_sincos(q[0], &s, &c);
+  for (int k = 0; k < 3; ++k) M.R[4 * k] = T(1);
+  if (jt == JT_RX) { M.R[4] = c; M.R[5] = -s; M.R[7] = s; M.R[8] = c; }
+  if (jt == JT_RY) { M.R[0] = c; M.R[2] = s; M.R[6] = -s; M.R[8] = c; }
+  if (jt == JT_RZ) { M.R[0] = c; M.R[1] = -s; M.R[3] = s; M.R[4] = c; }
+  return M;
+}
+inline int rev_axis(int jt) { return jt - JT_RX; }
+// Column k of the joint motion subspace S (local frame).
+template <class T> inline Vec6<T> S_col(int jt, int k) {
+  Vec6<T> s = zero6<T>();
+  if (jt == JT_FF) s.v[k] = T(1);
+  else s.v[3 + rev_axis(jt)] = T(1);
+  return s;
+}
+// Joint velocity vJ = S * qdot_j.
+template <class T> inline Vec6<T> joint_velocity(int jt, const T* v) {
+  Vec6<T> o = zero6<T>();
+  if (jt == JT_FF) for (int k = 0; k < 6; ++k) o.v[k] = v[k];
+  else o.v[3 + rev_axis(jt)] = v[0];
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Data workspace (the subset of DataTpl the hot-path algorithms use)
+// ---------------------------------------------------------------------------
+template <class T> struct Data {
+  int nj, nv;
+  std::vector<SE3<T>> liMi, oMi;
+  std::vector<Vec6<T>> v, a, a_gf, f, h, ov, oa, oa_gf, oh, of;
+  std::vector<Iner<T>> Ycrb, oYcrb, oinertias;
+  std::vector<Mat6<T>> Yaba, doYcrb;
+  std::vector<std::vector<T>> Ujoint, Dinvjoint, UDinvjoint;  // 6 x nvj, nvj x nvj, 6 x nvj
+  std::vector<T> J, dJ, dVdq, dAdq, dAdv, dFdq, dFdv, dFda, SDinv;  // 6 x nv col-major
+  std::vector<std::vector<T>> Fcrb;                                  // nj x (6 x nv)
+  std::vector<T> tau, ddq, u;
+  std::vector<T> M, Minv, dtau_dq, dtau_dv, ddq_dq, ddq_dv;  // nv x nv row-major
+  std::vector<T> U, D, Dinv, tmp;                            // Cholesky
+  explicit Data(const Model& m) : nj(m.njoints), nv(m.nv) {
+    liMi.resize(nj); oMi.resize(nj);
+    for (auto* vec : {&v, &a, &a_gf, &f, &h, &ov, &oa, &oa_gf, &oh, &of}) vec->assign(nj, zero6<T>());
+    Ycrb.resize(nj); oYcrb.resize(nj); oinertias.resize(nj);
+    Yaba.resize(nj); doYcrb.resize(nj);
+    Ujoint.assign(nj, std::vector<T>(36, T(0)));
+    Dinvjoint.assign(nj, std::vector<T>(36, T(0)));
+    UDinvjoint.assign(nj, std::vector<T>(36, T(0)));
+    for (auto* mat : {&J, &dJ, &dVdq, &dAdq, &dAdv, &dFdq, &dFdv, &dFda, &SDinv}) mat->assign(6 * nv, T(0));
+    Fcrb.assign(nj, std::vector<T>(6 * nv, T(0)));
+    tau.assign(nv, T(0)); ddq.assign(nv, T(0)); u.assign(nv, T(0));
+    for (auto* mat : {&M, &Minv, &dtau_dq, &dtau_dv, &ddq_dq, &ddq_dv}) mat->assign((size_t)nv * nv, T(0));
+    U.assign((size_t)nv * nv, T(0));
+    for (int k = 0; k < nv; ++k) U[(size_t)k * nv + k] = T(1);
+    D.assign(nv, T(0)); Dinv.assign(nv, T(0)); tmp.assign(nv, T(0));
+  }
+};
+
+template <class T> inline Vec6<T> col6(const std::vector<T>& X, int k) {
+  Vec6<T> o;
+  for (int r = 0; r < 6; ++r) o.v[r] = X[6 * k + r];
+  return o;
+}
+template <class T> inline void set_col6(std::vector<T>& X, int k, const Vec6<T>& c) {
+  for (int r = 0; r < 6; ++r) X[6 * k + r] = c.v[r];
+}
+template <class T> inline T dot6(const Vec6<T>& a, const Vec6<T>& b) {
+  T s = a.v[0] * b.v[0];
+  for (int k = 1; k < 6; ++k) s += a.v[k] * b.v[k];
+  return s;
+}
+template <class T> inline T dot6p(const T* a, const T* b) {
+  T s = a[0] * b[0];
+  for (int k = 1; k < 6; ++k) s += a[k] * b[k];
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// RNEA (algorithm/rnea.hxx:24-161)
+// ---------------------------------------------------------------------------
+template <class T>
+void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
+  std::fill(d.tau.begin(), d.tau.end(), T(0));
+  d.v[0] = zero6<T>();
+  for (int k = 0; k < 6; ++k) d.a_gf[0].v[k] = -T(m.gravity[k]);
+  for (int i = 1; i < m.njoints; ++i) {  // RneaForwardStep (rnea.hxx:24-80)
+    const int p = m.parents[i], jt = m.jtype[i];
+    const int iq = m.idx_q[i], iv = m.idx_v[i];
+    const SE3<T> jM = joint_transform<T>(jt, q + iq);
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
+    const Vec6<T> vJ = joint_velocity<T>(jt, v + iv);
+    d.v[i] = vJ;
+    if (p > 0) d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
+    d.a_gf[i] = cross_motion(d.v[i], vJ);  // c() = 0 for these joints
+    d.a_gf[i] = add6(d.a_gf[i], joint_velocity<T>(jt, a + iv));
+    d.a_gf[i] = add6(d.a_gf[i], actinv_motion(d.liMi[i], d.a_gf[p]));
+    const Iner<T> Y = inertia_of<T>(m, i);
+    d.h[i] = iner_mul(Y, d.v[i]);
+    d.f[i] = iner_mul(Y, d.a_gf[i]);
+    d.f[i] = add6(d.f[i], cross_force(d.v[i], d.h[i]));
+  }
+  for (int i = m.njoints - 1; i > 0; --i) {  // RneaBackwardStep (rnea.hxx:83-108)
+    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i];
+    for (int k = 0; k < m.nvs[i]; ++k) d.tau[iv + k] += dot6(S_col<T>(jt, k), d.f[i]);
+    if (p > 0) d.f[p] = add6(d.f[p], act_force(d.liMi[i], d.f[i]));
+  }
+  for (int k = 0; k < m.nv; ++k) d.tau[k] += T(m.armature[k]) * a[k];  // rnea.hxx:158
+}
+
+// ---------------------------------------------------------------------------
+// ABA, LOCAL convention (algorithm/aba.hxx:360-540)
+// ---------------------------------------------------------------------------
+template <class T>
+void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau) {
+  d.v[0] = zero6<T>();
+  for (int k = 0; k < 6; ++k) d.a_gf[0].v[k] = -T(m.gravity[k]);
+  d.f[0] = zero6<T>();
+  for (int k = 0; k < m.nv; ++k) d.u[k] = tau[k];
+  for (int i = 1; i < m.njoints; ++i) {  // AbaLocalConventionForwardStep1 (aba.hxx:360-399)
+    const int p = m.parents[i], jt = m.jtype[i];
+    const SE3<T> jM = joint_transform<T>(jt, q + m.idx_q[i]);
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
+    const Vec6<T> vJ = joint_velocity<T>(jt, v + m.idx_v[i]);
+    d.v[i] = vJ;
+    if (p > 0) d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
+    d.a_gf[i] = cross_motion(d.v[i], vJ);
+    const Iner<T> Y = inertia_of<T>(m, i);
+    d.Yaba[i] = iner_matrix(Y);
+    d.h[i] = iner_mul(Y, d.v[i]);
+    d.f[i] = cross_force(d.v[i], d.h[i]);
+  }
+  for (int i = m.njoints - 1; i > 0; --i) {  // AbaLocalConventionBackwardStep (aba.hxx:402-434)
+    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    Mat6<T>& Ia = d.Yaba[i];
+    for (int k = 0; k < nvj; ++k) d.u[iv + k] -= dot6(S_col<T>(jt, k), d.f[i]);
+    std::vector<T>& U = d.Ujoint[i];
+    std::vector<T>& Dinv = d.Dinvjoint[i];
+    std::vector<T>& UDinv = d.UDinvjoint[i];
+    if (jt == JT_FF) {  // JointModelFreeFlyer::calc_aba (joint-free-flyer.hpp:377-391)
+      T StU[36];
+      for (int k = 0; k < 36; ++k) { U[k] = Ia.a[k]; StU[k] = Ia.a[k]; }
+      for (int k = 0; k < 6; ++k) StU[7 * k] += T(m.armature[iv + k]);
+      llt_inverse(6, StU, Dinv.data());
+      for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) {
+          T s = Ia.a[6 * r] * Dinv[c];
+          for (int k = 1; k < 6; ++k) s += Ia.a[6 * r + k] * Dinv[6 * k + c];
+          UDinv[6 * r + c] = s;
+        }
+      if (p > 0)
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c) {
+            T s = UDinv[6 * r] * U[6 * c];
+            for (int k = 1; k < 6; ++k) s += UDinv[6 * r + k] * U[6 * c + k];
+            Ia.a[6 * r + c] -= s;
+          }
+    } else {  // JointModelRevolute::calc_aba (joint-revolute.hpp:823-834)
+      const int ax = 3 + rev_axis(jt);
+      for (int r = 0; r < 6; ++r) U[r] = Ia.a[6 * r + ax];
+      Dinv[0] = T(1) / (Ia.a[6 * ax + ax] + T(m.armature[iv]));
+      for (int r = 0; r < 6; ++r) UDinv[r] = U[r] * Dinv[0];
+      if (p > 0)
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c) Ia.a[6 * r + c] -= UDinv[r] * U[c];
+    }
+    if (p > 0) {
+      Vec6<T> pa = mat6_vec(Ia, d.a_gf[i].v);
+      for (int r = 0; r < 6; ++r) {
+        T s = T(0);
+        for (int k = 0; k < nvj; ++k) s += UDinv[r * nvj + k] * d.u[iv + k];
+        pa.v[r] += s;
+      }
+      d.f[i] = add6(d.f[i], pa);
+      const Mat6<T> Ip = se3_act_on(d.liMi[i], Ia);
+      for (int k = 0; k < 36; ++k) d.Yaba[p].a[k] += Ip.a[k];
+      d.f[p] = add6(d.f[p], act_force(d.liMi[i], d.f[i]));
+    }
+  }
+  for (int i = 1; i < m.njoints; ++i) {  // AbaLocalConventionForwardStep2 (aba.hxx:437-468)
+    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    d.a_gf[i] = add6(d.a_gf[i], actinv_motion(d.liMi[i], d.a_gf[p]));
+    const std::vector<T>& Dinv = d.Dinvjoint[i];
+    const std::vector<T>& UDinv = d.UDinvjoint[i];
+    for (int k = 0; k < nvj; ++k) {
+      T s = T(0);
+      for (int c = 0; c < nvj; ++c) s += Dinv[k * nvj + c] * d.u[iv + c];
+      T w = T(0);
+      for (int r = 0; r < 6; ++r) w += UDinv[r * nvj + k] * d.a_gf[i].v[r];
+      d.ddq[iv + k] = s - w;
+    }
+    for (int k = 0; k < nvj; ++k) {
+      const Vec6<T> s = S_col<T>(jt, k);
+      for (int r = 0; r < 6; ++r) d.a_gf[i].v[r] += s.v[r] * d.ddq[iv + k];
+    }
+  }
+}
+
+// Shared by the WORLD ABA and the ABA derivatives: the WORLD backward step
+// (aba.hxx:142-193 / aba-derivatives.hxx:87-171 Schur part).
+template <class T>
+void world_schur(const Model& m, Data<T>& d, int i) {
+  const int iv = m.idx_v[i], nvj = m.nvs[i];
+  Mat6<T>& Ia = d.Yaba[i];
+  std::vector<T>& U = d.Ujoint[i];
+  std::vector<T>& Dinv = d.Dinvjoint[i];
+  std::vector<T>& UDinv = d.UDinvjoint[i];
+  for (int k = 0; k < nvj; ++k) d.u[iv + k] -= dot6(col6(d.J, iv + k), d.of[i]);
+  for (int k = 0; k < nvj; ++k) {  // U = Ia * Jcols (6 x nvj, row-major)
+    const Vec6<T> jc = col6(d.J, iv + k);
+    const Vec6<T> uc = mat6_vec(Ia, jc.v);
+    for (int r = 0; r < 6; ++r) U[r * nvj + k] = uc.v[r];
+  }
+  T StU[36];
+  for (int r = 0; r < nvj; ++r)
+    for (int c = 0; c < nvj; ++c) {
+      const Vec6<T> jr = col6(d.J, iv + r);
+      T s = jr.v[0] * U[0 * nvj + c];
+      for (int k = 1; k < 6; ++k) s += jr.v[k] * U[k * nvj + c];
+      StU[r * nvj + c] = s;
+    }
+  for (int k = 0; k < nvj; ++k) StU[k * nvj + k] += T(m.armature[iv + k]);
+  llt_inverse(nvj, StU, Dinv.data());
+  for (int r = 0; r < 6; ++r)
+    for (int c = 0; c < nvj; ++c) {
+      T s = U[r * nvj] * Dinv[c];
+      for (int k = 1; k < nvj; ++k) s += U[r * nvj + k] * Dinv[k * nvj + c];
+      UDinv[r * nvj + c] = s;
+    }
+}
+template <class T>
+void world_schur_update(const Model& m, Data<T>& d, int i) {
+  const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
+  Mat6<T>& Ia = d.Yaba[i];
+  const std::vector<T>& U = d.Ujoint[i];
+  const std::vector<T>& UDinv = d.UDinvjoint[i];
+  for (int r = 0; r < 6; ++r)
+    for (int c = 0; c < 6; ++c) {
+      T s = UDinv[r * nvj] * U[c * nvj];
+      for (int k = 1; k < nvj; ++k) s += UDinv[r * nvj + k] * U[c * nvj + k];
+      Ia.a[6 * r + c] -= s;
+    }
+  Vec6<T> pa = mat6_vec(Ia, d.oa_gf[i].v);
+  for (int r = 0; r < 6; ++r) {
+    T s = T(0);
+    for (int k = 0; k < nvj; ++k) s += UDinv[r * nvj + k] * d.u[iv + k];
+    pa.v[r] += s;
+  }
+  d.of[i] = add6(d.of[i], pa);
+  for (int k = 0; k < 36; ++k) d.Yaba[p].a[k] += Ia.a[k];
+  d.of[p] = add6(d.of[p], d.of[i]);
+}
+
+// World-frame forward kinematics shared by the WORLD ABA and the ABA
+// derivatives (aba.hxx:85-139, aba-derivatives.hxx:22-80).
+template <class T>
+void world_forward1(const Model& m, Data<T>& d, const T* q, const T* v, int i) {
+  const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i];
+  const SE3<T> jM = joint_transform<T>(jt, q + m.idx_q[i]);
+  d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
+  d.oMi[i] = (p > 0) ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
+  for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(jt, k)));
+  d.ov[i] = act_motion(d.oMi[i], joint_velocity<T>(jt, v + iv));
+  if (p > 0) d.ov[i] = add6(d.ov[i], d.ov[p]);
+  d.oa_gf[i] = zero6<T>();  // oMi.act(c()) with c() = 0
+  if (p > 0) d.oa_gf[i] = add6(d.oa_gf[i], cross_motion(d.ov[p], d.ov[i]));
+  d.oinertias[i] = d.oYcrb[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
+  d.Yaba[i] = iner_matrix(d.oYcrb[i]);
+  d.oh[i] = iner_mul(d.oYcrb[i], d.ov[i]);
+  d.of[i] = cross_force(d.ov[i], d.oh[i]);
+}
+
+// ---------------------------------------------------------------------------
+// ABA, WORLD convention (algorithm/aba.hxx:85-293); abaInParallel uses it
+// (algorithm/parallel/aba.hpp:82).
+// ---------------------------------------------------------------------------
+template <class T>
+void aba_world(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau) {
+  for (int k = 0; k < 6; ++k) d.oa_gf[0].v[k] = -T(m.gravity[k]);
+  d.of[0] = zero6<T>();
+  for (int k = 0; k < m.nv; ++k) d.u[k] = tau[k];
+  for (int i = 1; i < m.njoints; ++i) world_forward1(m, d, q, v, i);
+  for (int i = m.njoints - 1; i > 0; --i) {
+    world_schur(m, d, i);
+    if (m.parents[i] > 0) world_schur_update(m, d, i);
+  }
+  for (int i = 1; i < m.njoints; ++i) {  // AbaWorldConventionForwardStep2 (aba.hxx:196-232)
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    d.oa_gf[i] = add6(d.oa_gf[i], d.oa_gf[p]);
+    const std::vector<T>& Dinv = d.Dinvjoint[i];
+    const std::vector<T>& UDinv = d.UDinvjoint[i];
+    for (int k = 0; k < nvj; ++k) {
+      T s = T(0);
+      for (int c = 0; c < nvj; ++c) s += Dinv[k * nvj + c] * d.u[iv + c];
+      T w = T(0);
+      for (int r = 0; r < 6; ++r) w += UDinv[r * nvj + k] * d.oa_gf[i].v[r];
+      d.ddq[iv + k] = s - w;
+    }
+    for (int r = 0; r < 6; ++r) {
+      T s = T(0);
+      for (int k = 0; k < nvj; ++k) s += d.J[6 * (iv + k) + r] * d.ddq[iv + k];
+      d.oa_gf[i].v[r] += s;
+    }
+  }
+}
+
+template <class T>
+void aba(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, int conv) {
+  if (conv == WORLD) aba_world(m, d, q, v, tau);
+  else aba_local(m, d, q, v, tau);
+}
+
+// ---------------------------------------------------------------------------
+// CRBA (algorithm/crba.hxx): LOCAL 224-339 + 454-491, WORLD 25-110 + 498-548.
+// Fills the upper triangle of M (row-major) and adds the armature.
+// ---------------------------------------------------------------------------
+template <class T>
+void crba(const Model& m, Data<T>& d, const T* q, int conv) {
+  const int nv = m.nv;
+  if (conv == LOCAL) {
+    for (int i = 1; i < m.njoints; ++i) {
+      d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m.jtype[i], q + m.idx_q[i]));
+      d.Ycrb[i] = inertia_of<T>(m, i);
+    }
+    for (int i = m.njoints - 1; i > 0; --i) {
+      const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
+      const int nst = m.nvSubtree[i];
+      std::vector<T>& Fi = d.Fcrb[i];
+      for (int k = 0; k < nvj; ++k) set_col6(Fi, iv + k, iner_mul(d.Ycrb[i], S_col<T>(jt, k)));
+      for (int r = 0; r < nvj; ++r)
+        for (int c = iv; c < iv + nst; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(S_col<T>(jt, r), col6(Fi, c));
+      if (p > 0) {
+        iner_add(d.Ycrb[p], iner_act(d.liMi[i], d.Ycrb[i]));
+        for (int c = iv; c < iv + nst; ++c) set_col6(d.Fcrb[p], c, act_force(d.liMi[i], col6(Fi, c)));
+      }
+    }
+  } else {
+    Iner<T> Y0;
+    Y0.m = T(0);
+    for (int k = 0; k < 3; ++k) Y0.c[k] = T(0);
+    for (int k = 0; k < 6; ++k) Y0.I[k] = T(0);
+    d.oYcrb[0] = Y0;
+    for (int i = 1; i < m.njoints; ++i) {
+      const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i];
+      d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(jt, q + m.idx_q[i]));
+      d.oMi[i] = (p > 0) ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
+      for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(jt, k)));
+      d.oYcrb[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
+    }
+    std::vector<T>& Ag = d.dFda;  // plays the role of data.Ag
+    for (int i = m.njoints - 1; i > 0; --i) {
+      const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i], nst = m.nvSubtree[i];
+      for (int k = 0; k < nvj; ++k) set_col6(Ag, iv + k, iner_mul(d.oYcrb[i], col6(d.J, iv + k)));
+      for (int r = 0; r < nvj; ++r)
+        for (int c = iv; c < iv + nst; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(Ag, c));
+      iner_add(d.oYcrb[p], d.oYcrb[i]);
+    }
+  }
+  for (int k = 0; k < nv; ++k) d.M[(size_t)k * nv + k] += T(m.armature[k]);
+}
+
+// ---------------------------------------------------------------------------
+// Tree-sparse U D U^T factorisation of M (algorithm/cholesky.hxx:18-62).
+// Reads the upper triangle of d.M; writes d.U (unit upper, row-major), d.D, d.Dinv.
+// ---------------------------------------------------------------------------
+template <class T>
+void cholesky_decompose(const Model& m, Data<T>& d) {
+  const int nv = m.nv;
+  auto Mij = [&](int i, int j) { return d.M[(size_t)i * nv + j]; };
+  auto Uij = [&](int i, int j) -> T& { return d.U[(size_t)i * nv + j]; };
+  for (int j = nv - 1; j >= 0; --j) {
+    const int NVT = m.nvSubtree_fromRow[j] - 1;
+    for (int k = 0; k < NVT; ++k) d.tmp[k] = Uij(j, j + 1 + k) * d.D[j + 1 + k];
+    T s = T(0);
+    for (int k = 0; k < NVT; ++k) s += Uij(j, j + 1 + k) * d.tmp[k];
+    d.D[j] = Mij(j, j) - s;
+    d.Dinv[j] = T(1) / d.D[j];
+    for (int ii = m.parents_fromRow[j]; ii >= 0; ii = m.parents_fromRow[ii]) {
+      T w = T(0);
+      for (int k = 0; k < NVT; ++k) w += Uij(ii, j + 1 + k) * d.tmp[k];
+      Uij(ii, j) = (Mij(ii, j) - w) * d.Dinv[j];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RNEA derivatives (algorithm/rnea-derivatives.hxx:242-541).
+// Outputs d.dtau_dq, d.dtau_dv (row-major), d.M (upper triangle + armature), d.tau.
+// ---------------------------------------------------------------------------
+template <class T>
+void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
+  const int nv = m.nv;
+  if (m.gravity[3] != 0.0 || m.gravity[4] != 0.0 || m.gravity[5] != 0.0)
+    throw std::invalid_argument("The gravity must be a pure force vector, no angular part");
+  for (int k = 0; k < 6; ++k) d.oa_gf[0].v[k] = -T(m.gravity[k]);
+  Vec6<T> g;
+  for (int k = 0; k < 6; ++k) g.v[k] = T(m.gravity[k]);
+  for (int i = 1; i < m.njoints; ++i) {  // ComputeRNEADerivativesForwardStep (hxx:242-352)
+    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    const SE3<T> jM = joint_transform<T>(jt, q + m.idx_q[i]);
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
+    const Vec6<T> vJ = joint_velocity<T>(jt, v + iv);
+    d.v[i] = vJ;
+    if (p > 0) {
+      d.oMi[i] = se3_mul(d.oMi[p], d.liMi[i]);
+      d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
+    } else {
+      d.oMi[i] = d.liMi[i];
+    }
+    d.a[i] = add6(joint_velocity<T>(jt, a + iv), cross_motion(d.v[i], vJ));
+    if (p > 0) d.a[i] = add6(d.a[i], actinv_motion(d.liMi[i], d.a[p]));
+    d.oYcrb[i] = d.oinertias[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
+    d.ov[i] = act_motion(d.oMi[i], d.v[i]);
+    d.oa[i] = act_motion(d.oMi[i], d.a[i]);
+    for (int k = 0; k < 6; ++k) d.oa_gf[i].v[k] = d.oa[i].v[k] - g.v[k];
+    d.oh[i] = iner_mul(d.oYcrb[i], d.ov[i]);
+    d.of[i] = add6(iner_mul(d.oYcrb[i], d.oa_gf[i]), cross_force(d.ov[i], d.oh[i]));
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      const Vec6<T> Jc = act_motion(d.oMi[i], S_col<T>(jt, k));
+      set_col6(d.J, c, Jc);
+      const Vec6<T> dJc = cross_motion(d.ov[i], Jc);
+      set_col6(d.dJ, c, dJc);
+      Vec6<T> dAdq = cross_motion(d.oa_gf[p], Jc);
+      Vec6<T> dAdv = dJc;
+      if (p > 0) {
+        const Vec6<T> dVdq = cross_motion(d.ov[p], Jc);
+        set_col6(d.dVdq, c, dVdq);
+        dAdq = add6(dAdq, cross_motion(d.ov[p], dVdq));
+        dAdv = add6(dAdv, dVdq);
+      } else {
+        set_col6(d.dVdq, c, zero6<T>());
+      }
+      set_col6(d.dAdq, c, dAdq);
+      set_col6(d.dAdv, c, dAdv);
+    }
+    d.doYcrb[i] = iner_variation(d.oYcrb[i], d.ov[i]);
+    add_force_cross_matrix(d.oh[i], d.doYcrb[i]);
+  }
+  std::vector<T>& dYtJ = d.Fcrb[0];
+  for (int i = m.njoints - 1; i > 0; --i) {  // ComputeRNEADerivativesBackwardStep (hxx:361-460)
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    const int nst = m.nvSubtree[i], ivp = iv + nvj, nstp = nst - nvj;
+    for (int k = 0; k < nvj; ++k) d.tau[iv + k] = dot6(col6(d.J, iv + k), d.of[i]);
+    for (int k = 0; k < nvj; ++k) set_col6(d.dFda, iv + k, iner_mul(d.oYcrb[i], col6(d.J, iv + k)));
+    for (int r = 0; r < nvj; ++r)
+      for (int c = iv; c < iv + nst; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFda, c));
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      Vec6<T> dFdq;
+      if (p > 0) dFdq = add6(mat6_vec(d.doYcrb[i], col6(d.dVdq, c).v), iner_mul(d.oYcrb[i], col6(d.dAdq, c)));
+      else dFdq = iner_mul(d.oYcrb[i], col6(d.dAdq, c));
+      set_col6(d.dFdq, c, dFdq);
+    }
+    for (int k = 0; k < nvj; ++k) {  // dYtJ_cols^T = J_cols^T doYcrb
+      const Vec6<T> Jc = col6(d.J, iv + k);
+      Vec6<T> row;
+      for (int c = 0; c < 6; ++c) {
+        T s = Jc.v[0] * d.doYcrb[i].a[c];
+        for (int r = 1; r < 6; ++r) s += Jc.v[r] * d.doYcrb[i].a[6 * r + c];
+        row.v[c] = s;
+      }
+      set_col6(dYtJ, iv + k, row);
+    }
+    for (int r = ivp; r < ivp + nstp; ++r)
+      for (int k = 0; k < nvj; ++k) {
+        const int c = iv + k;
+        d.dtau_dq[(size_t)r * nv + c] = dot6(col6(d.dFda, r), col6(d.dAdq, c)) + dot6(col6(dYtJ, r), col6(d.dVdq, c));
+      }
+    for (int r = 0; r < nvj; ++r)
+      for (int c = iv; c < iv + nst; ++c)
+        d.dtau_dq[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFdq, c));
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      set_col6(d.dFdq, c, add6(col6(d.dFdq, c), cross_force(col6(d.J, c), d.of[i])));
+    }
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      set_col6(d.dFdv, c, add6(mat6_vec(d.doYcrb[i], col6(d.J, c).v), iner_mul(d.oYcrb[i], col6(d.dAdv, c))));
+    }
+    for (int r = ivp; r < ivp + nstp; ++r)
+      for (int k = 0; k < nvj; ++k) {
+        const int c = iv + k;
+        d.dtau_dv[(size_t)r * nv + c] = dot6(col6(d.dFda, r), col6(d.dAdv, c)) + dot6(col6(dYtJ, r), col6(d.J, c));
+      }
+    for (int r = 0; r < nvj; ++r)
+      for (int c = iv; c < iv + nst; ++c)
+        d.dtau_dv[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFdv, c));
+    if (p > 0) {
+      iner_add(d.oYcrb[p], d.oYcrb[i]);
+      for (int k = 0; k < 36; ++k) d.doYcrb[p].a[k] += d.doYcrb[i].a[k];
+      d.of[p] = add6(d.of[p], d.of[i]);
+    }
+  }
+  for (int k = 0; k < nv; ++k) {  // restore dAdq (hxx:530-535)
+    T w[3];
+    cross3(g.v, &d.J[6 * k + 3], w);
+    for (int r = 0; r < 3; ++r) d.dAdq[6 * k + r] += w[r];
+  }
+  for (int k = 0; k < nv; ++k) d.tau[k] += T(m.armature[k]) * a[k];
+  for (int k = 0; k < nv; ++k) d.M[(size_t)k * nv + k] += T(m.armature[k]);
+}
+
+// ---------------------------------------------------------------------------
+// ABA derivatives (algorithm/aba-derivatives.hxx:22-453).
+// Outputs d.ddq, d.ddq_dq, d.ddq_dv, d.Minv (full symmetric; row-major).
+// ---------------------------------------------------------------------------
+template <class T>
+void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau) {
+  const int nv = m.nv;
+  if (m.gravity[3] != 0.0 || m.gravity[4] != 0.0 || m.gravity[5] != 0.0)
+    throw std::invalid_argument("The gravity must be a pure force vector, no angular part");
+  Vec6<T> g;
+  for (int k = 0; k < 6; ++k) g.v[k] = T(m.gravity[k]);
+  for (int k = 0; k < 6; ++k) d.oa_gf[0].v[k] = -g.v[k];
+  for (int k = 0; k < nv; ++k) d.u[k] = tau[k];
+  std::vector<T>& Minv = d.Minv;
+  for (int r = 0; r < nv; ++r)
+    for (int c = r; c < nv; ++c) Minv[(size_t)r * nv + c] = T(0);
+  for (int i = 1; i < m.njoints; ++i) world_forward1(m, d, q, v, i);  // ForwardStep1 (22-80)
+  std::vector<T>& Fcrb = d.Fcrb[0];
+  std::fill(Fcrb.begin(), Fcrb.end(), T(0));
+  for (int i = m.njoints - 1; i > 0; --i) {  // BackwardStep1 (87-171)
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i], nst = m.nvSubtree[i];
+    world_schur(m, d, i);
+    const std::vector<T>& U = d.Ujoint[i];
+    const std::vector<T>& Dinv = d.Dinvjoint[i];
+    for (int r = 0; r < nvj; ++r)
+      for (int c = 0; c < nvj; ++c) Minv[(size_t)(iv + r) * nv + iv + c] = Dinv[r * nvj + c];
+    const int nch = nst - nvj;
+    if (nch > 0) {
+      for (int k = 0; k < nvj; ++k)  // SDinv_cols = J_cols * Dinv
+        for (int r = 0; r < 6; ++r) {
+          T s = d.J[6 * iv + r] * Dinv[k];
+          for (int j = 1; j < nvj; ++j) s += d.J[6 * (iv + j) + r] * Dinv[j * nvj + k];
+          d.SDinv[6 * (iv + k) + r] = s;
+        }
+      for (int r = 0; r < nvj; ++r)
+        for (int c = iv + nvj; c < iv + nst; ++c)
+          Minv[(size_t)(iv + r) * nv + c] = -dot6p(&d.SDinv[6 * (iv + r)], &Fcrb[6 * c]);
+      if (p > 0)
+        for (int c = iv; c < iv + nst; ++c)
+          for (int r = 0; r < 6; ++r) {
+            T s = U[r * nvj] * Minv[(size_t)iv * nv + c];
+            for (int k = 1; k < nvj; ++k) s += U[r * nvj + k] * Minv[(size_t)(iv + k) * nv + c];
+            Fcrb[6 * c + r] += s;
+          }
+    } else {
+      for (int c = iv; c < iv + nst; ++c)
+        for (int r = 0; r < 6; ++r) {
+          T s = U[r * nvj] * Minv[(size_t)iv * nv + c];
+          for (int k = 1; k < nvj; ++k) s += U[r * nvj + k] * Minv[(size_t)(iv + k) * nv + c];
+          Fcrb[6 * c + r] = s;
+        }
+    }
+    if (p > 0) world_schur_update(m, d, i);
+  }
+  for (int i = 1; i < m.njoints; ++i) {  // ForwardStep2 (178-270)
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    const std::vector<T>& Dinv = d.Dinvjoint[i];
+    const std::vector<T>& UDinv = d.UDinvjoint[i];
+    d.oa_gf[i] = add6(d.oa_gf[i], d.oa_gf[p]);
+    for (int k = 0; k < nvj; ++k) {
+      T s = T(0);
+      for (int c = 0; c < nvj; ++c) s += Dinv[k * nvj + c] * d.u[iv + c];
+      T w = T(0);
+      for (int r = 0; r < 6; ++r) w += UDinv[r * nvj + k] * d.oa_gf[i].v[r];
+      d.ddq[iv + k] = s - w;
+    }
+    for (int r = 0; r < 6; ++r) {
+      T s = T(0);
+      for (int k = 0; k < nvj; ++k) s += d.J[6 * (iv + k) + r] * d.ddq[iv + k];
+      d.oa_gf[i].v[r] += s;
+    }
+    for (int k = 0; k < 6; ++k) d.oa[i].v[k] = d.oa_gf[i].v[k] + g.v[k];
+    d.of[i] = add6(iner_mul(d.oYcrb[i], d.oa_gf[i]), cross_force(d.ov[i], d.oh[i]));
+    if (p > 0)
+      for (int r = 0; r < nvj; ++r)
+        for (int c = iv; c < nv; ++c) {
+          T s = UDinv[0 * nvj + r] * d.Fcrb[p][6 * c];
+          for (int k = 1; k < 6; ++k) s += UDinv[k * nvj + r] * d.Fcrb[p][6 * c + k];
+          Minv[(size_t)(iv + r) * nv + c] -= s;
+        }
+    for (int c = iv; c < nv; ++c)
+      for (int r = 0; r < 6; ++r) {
+        T s = d.J[6 * iv + r] * Minv[(size_t)iv * nv + c];
+        for (int k = 1; k < nvj; ++k) s += d.J[6 * (iv + k) + r] * Minv[(size_t)(iv + k) * nv + c];
+        if (p > 0) s += d.Fcrb[p][6 * c + r];
+        d.Fcrb[i][6 * c + r] = s;
+      }
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      const Vec6<T> Jc = col6(d.J, c);
+      const Vec6<T> dJc = cross_motion(d.ov[i], Jc);
+      set_col6(d.dJ, c, dJc);
+      Vec6<T> dAdq = cross_motion(d.oa_gf[p], Jc);
+      Vec6<T> dAdv = dJc;
+      if (p > 0) {
+        const Vec6<T> dVdq = cross_motion(d.ov[p], Jc);
+        set_col6(d.dVdq, c, dVdq);
+        dAdq = add6(dAdq, cross_motion(d.ov[p], dVdq));
+        dAdv = add6(dAdv, dVdq);
+      } else {
+        set_col6(d.dVdq, c, zero6<T>());
+      }
+      set_col6(d.dAdq, c, dAdq);
+      set_col6(d.dAdv, c, dAdv);
+    }
+    d.doYcrb[i] = iner_variation(d.oYcrb[i], d.ov[i]);
+    add_force_cross_matrix(d.oh[i], d.doYcrb[i]);
+  }
+  for (int i = m.njoints - 1; i > 0; --i) {  // BackwardStep2 (273-368)
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i], nst = m.nvSubtree[i];
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      set_col6(d.dFdv, c, add6(iner_mul(d.oYcrb[i], col6(d.dAdv, c)), mat6_vec(d.doYcrb[i], col6(d.J, c).v)));
+    }
+    for (int r = 0; r < nvj; ++r)
+      for (int c = iv; c < iv + nst; ++c)
+        d.dtau_dv[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFdv, c));
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      Vec6<T> dFdq = iner_mul(d.oYcrb[i], col6(d.dAdq, c));
+      if (p > 0) dFdq = add6(dFdq, mat6_vec(d.doYcrb[i], col6(d.dVdq, c).v));
+      set_col6(d.dFdq, c, dFdq);
+    }
+    for (int r = 0; r < nvj; ++r)
+      for (int c = iv; c < iv + nst; ++c)
+        d.dtau_dq[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFdq, c));
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      set_col6(d.dFdq, c, add6(col6(d.dFdq, c), cross_force(col6(d.J, c), d.of[i])));
+    }
+    for (int k = 0; k < nvj; ++k) set_col6(d.dFda, iv + k, iner_mul(d.oYcrb[i], col6(d.J, iv + k)));
+    if (p > 0) {
+      for (int r = 0; r < nvj; ++r)
+        for (int j = m.parents_fromRow[iv]; j >= 0; j = m.parents_fromRow[j])
+          d.dtau_dq[(size_t)(iv + r) * nv + j] = dot6(col6(d.dFda, iv + r), col6(d.dAdq, j));
+      for (int r = 0; r < nvj; ++r)
+        for (int j = m.parents_fromRow[iv]; j >= 0; j = m.parents_fromRow[j])
+          d.dtau_dv[(size_t)(iv + r) * nv + j] = dot6(col6(d.dFda, iv + r), col6(d.dAdv, j));
+      for (int r = 0; r < nvj; ++r) {
+        const Vec6<T> Jc = col6(d.J, iv + r);
+        T StdY[6];
+        for (int c = 0; c < 6; ++c) {
+          T s = Jc.v[0] * d.doYcrb[i].a[c];
+          for (int k = 1; k < 6; ++k) s += Jc.v[k] * d.doYcrb[i].a[6 * k + c];
+          StdY[c] = s;
+        }
+        for (int j = m.parents_fromRow[iv]; j >= 0; j = m.parents_fromRow[j])
+          d.dtau_dq[(size_t)(iv + r) * nv + j] += dot6p(StdY, &d.dVdq[6 * j]);
+        for (int j = m.parents_fromRow[iv]; j >= 0; j = m.parents_fromRow[j])
+          d.dtau_dv[(size_t)(iv + r) * nv + j] += dot6p(StdY, &d.J[6 * j]);
+      }
+    }
+    if (p > 0) {
+      iner_add(d.oYcrb[p], d.oYcrb[i]);
+      for (int k = 0; k < 36; ++k) d.doYcrb[p].a[k] += d.doYcrb[i].a[k];
+      d.of[p] = add6(d.of[p], d.of[i]);
+    }
+    for (int k = 0; k < nvj; ++k) {
+      T w[3];
+      cross3(g.v, &d.J[6 * (iv + k) + 3], w);
+      for (int r = 0; r < 3; ++r) d.dAdq[6 * (iv + k) + r] += w[r];
+    }
+  }
+  for (int r = 1; r < nv; ++r)  // symmetrise (hxx:448-449)
+    for (int c = 0; c < r; ++c) Minv[(size_t)r * nv + c] = Minv[(size_t)c * nv + r];
+  for (int r = 0; r < nv; ++r)  // ddq_dq = -Minv dtau_dq, ddq_dv = -Minv dtau_dv (hxx:451-452)
+    for (int c = 0; c < nv; ++c) {
+      T s1 = T(0), s2 = T(0);
+      for (int k = 0; k < nv; ++k) {
+        s1 += Minv[(size_t)r * nv + k] * d.dtau_dq[(size_t)k * nv + c];
+        s2 += Minv[(size_t)r * nv + k] * d.dtau_dv[(size_t)k * nv + c];
+      }
+      d.ddq_dq[(size_t)r * nv + c] = -s1;
+      d.ddq_dv[(size_t)r * nv + c] = -s2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// integrate(q, v) for the supported joints: free-flyer through the SE(3)
+// exponential (multibody/liegroup/special-euclidean.hpp:660-699,
+// spatial/explog-quaternion.hpp:20-147, math/quaternion.hpp:90-111); revolute
+// joints are a vector space (q + v).
+// ---------------------------------------------------------------------------
+template <class T>
+void integrate(const Model& m, const T* q, const T* v, T* qout) {
+  for (int i = 1; i < m.njoints; ++i) {
+    const int iq = m.idx_q[i], iv = m.idx_v[i];
+    if (m.jtype[i] != JT_FF) {
+      qout[iq] = q[iq] + v[iv];
+      continue;
+    }
+    const T* w = v + iv + 3;
+    const T* lv = v + iv;
+    const T eps = o_eps<T>();
+    // exp6 translation part
+    const T t2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2] + eps * eps;
+    const T t = o_sqrt(t2);
+    T st, ct;
+    o_sincos(t, &st, &ct);
+    const T inv_t2 = T(1) / t2;
+    const T ts_prec = T(std::pow((double)eps, 1.0 / 4.0));
+    T alpha_wxv, alpha_w2;
+    if (t < ts_prec) {
+      alpha_wxv = T(0.5) - t2 / T(24);
+      alpha_w2 = T(1) / T(6) - t2 / T(120);
+    } else {
+      alpha_wxv = (T(1) - ct) * inv_t2;
+      alpha_w2 = (t - st) * inv_t2 / t;
+    }
+    T wxv[3], wxwxv[3], trans[3];
+    cross3(w, lv, wxv);
+    cross3(w, wxv, wxwxv);
+    for (int k = 0; k < 3; ++k) trans[k] = lv[k] + alpha_wxv * wxv[k] + alpha_w2 * wxwxv[k];
+    // exp3 quaternion part
+    const T s2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    const T th = o_sqrt(s2 + eps * eps);
+    T e[4];  // x, y, z, w
+    if (s2 > ts_prec) {  // AngleAxis(th, w/th) -> quaternion
+      T sh, ch;
+      o_sincos(T(0.5) * th, &sh, &ch);
+      for (int k = 0; k < 3; ++k) e[k] = sh * (w[k] / th);
+      e[3] = ch;
+    } else {
+      const T t2_2 = s2 / T(4);
+      const T c = T(0.5) * (T(1) - t2_2 / T(6) + t2_2 * t2_2 / T(120));
+      for (int k = 0; k < 3; ++k) e[k] = c * w[k];
+      e[3] = T(1) - t2_2 / T(2) + t2_2 * t2_2 / T(24);
+    }
+    const T* qq = q + iq + 3;  // x, y, z, w
+    // quat * trans (Eigen _transformVector: uv = 2 (u x v); v + w uv + u x uv)
+    T uv[3], uxuv[3];
+    cross3(qq, trans, uv);
+    for (int k = 0; k < 3; ++k) uv[k] += uv[k];
+    cross3(qq, uv, uxuv);
+    for (int k = 0; k < 3; ++k) qout[iq + k] = trans[k] + qq[3] * uv[k] + uxuv[k] + q[iq + k];
+    // res = quat * quat1 (Hamilton product)
+    T r[4];
+    r[3] = qq[3] * e[3] - qq[0] * e[0] - qq[1] * e[1] - qq[2] * e[2];
+    r[0] = qq[3] * e[0] + qq[0] * e[3] + qq[1] * e[2] - qq[2] * e[1];
+    r[1] = qq[3] * e[1] + qq[1] * e[3] + qq[2] * e[0] - qq[0] * e[2];
+    r[2] = qq[3] * e[2] + qq[2] * e[3] + qq[0] * e[1] - qq[1] * e[0];
+    const T dp = r[0] * qq[0] + r[1] * qq[1] + r[2] * qq[2] + r[3] * qq[3];
+    if (dp < T(0))
+      for (int k = 0; k < 4; ++k) r[k] = -r[k];
+    const T N2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+    const T alpha = (T(3) - N2) / T(2);
+    for (int k = 0; k < 4; ++k) qout[iq + 3 + k] = r[k] * alpha;
+  }
+}
+
+}  // namespace orc

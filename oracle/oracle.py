@@ -1,0 +1,160 @@
+"""Test infrastructure: ctypes front-end of the CPU oracle (liboracle.so).
+
+Only the tests, the smoke check and the CPU-baseline leg of the benchmark use
+this module; the product path never imports it.  ``build()`` compiles the
+library from ``oracle_capi.cpp`` with the Makefile beside this file.
+
+All batch arrays are numpy float64 of shape (batch, n) -- one instance per
+row, i.e. the reference's column-major ``n x batch`` matrices.  Matrix outputs
+have shape (batch, nv, nv) (row-major per instance).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+LOCAL, WORLD = 0, 1
+F_RNEA, F_ABA_LOCAL, F_ABA_WORLD, F_CRBA_LOCAL, F_CRBA_WORLD, F_CHOL, F_RNEA_D, F_ABA_D, F_INTEGRATE = range(9)
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "oracle.hpp", "flop_scalar.hpp")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "all"], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_model_new.restype = C.c_void_p
+        L.orc_model_new.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_model_free.argtypes = [C.c_void_p]
+        L.orc_model_dims.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.orc_model_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+        vp = C.c_void_p
+        L.orc_rnea.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, C.c_int]
+        L.orc_aba.argtypes = [vp, C.c_int, C.c_int, C.c_long, vp, vp, vp, vp, C.c_int]
+        L.orc_crba.argtypes = [vp, C.c_int, C.c_int, C.c_long, vp, vp, C.c_int]
+        L.orc_cholesky.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
+        L.orc_rnea_derivatives.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_aba_derivatives.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
+        L.orc_count_flops.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class OracleModel:
+    """The oracle's copy of a flattened model (from ``Model.tables()``)."""
+
+    def __init__(self, model):
+        L = lib()
+        t = model.tables()
+        self._keep = t
+        h = L.orc_model_new(
+            int(len(t["parents"])), _ptr(t["parents"]), _ptr(t["jtype"]), _ptr(t["placement"]), _ptr(t["inertia"]),
+            _ptr(t["armature"]), int(len(t["armature"])), _ptr(t["gravity"]),
+        )
+        if not h:
+            raise ValueError(L.orc_last_error().decode())
+        self.h = C.c_void_p(h)
+        nq, nv = C.c_int(), C.c_int()
+        L.orc_model_dims(self.h, C.byref(nq), C.byref(nv))
+        self.nq, self.nv = nq.value, nv.value
+        self.model = model
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_model_free(self.h)
+            self.h = None
+
+    def _check(self, rc):
+        if rc != 0:
+            raise ValueError(lib().orc_last_error().decode())
+
+    # all methods: prec 0 = double, 1 = long double; nthreads 0 = all cores
+    def rnea(self, q, v, a, prec=0, nthreads=0):
+        q, v, a = _c(q), _c(v), _c(a)
+        tau = np.empty((q.shape[0], self.nv))
+        self._check(lib().orc_rnea(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(a), _ptr(tau), nthreads))
+        return tau
+
+    def aba(self, q, v, tau, convention=LOCAL, prec=0, nthreads=0):
+        q, v, tau = _c(q), _c(v), _c(tau)
+        ddq = np.empty((q.shape[0], self.nv))
+        self._check(lib().orc_aba(self.h, prec, convention, q.shape[0], _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), nthreads))
+        return ddq
+
+    def crba(self, q, convention=LOCAL, prec=0, nthreads=0):
+        """Upper triangle of M (lower part zero), as the reference's crba leaves it."""
+        q = _c(q)
+        M = np.empty((q.shape[0], self.nv, self.nv))
+        self._check(lib().orc_crba(self.h, prec, convention, q.shape[0], _ptr(q), _ptr(M), nthreads))
+        return M
+
+    def cholesky(self, M, prec=0, nthreads=0):
+        M = _c(M)
+        U = np.empty_like(M)
+        D = np.empty((M.shape[0], self.nv))
+        self._check(lib().orc_cholesky(self.h, prec, M.shape[0], _ptr(M), _ptr(U), _ptr(D), nthreads))
+        return U, D
+
+    def rnea_derivatives(self, q, v, a, prec=0, nthreads=0):
+        """(tau, dtau_dq, dtau_dv, M upper)."""
+        q, v, a = _c(q), _c(v), _c(a)
+        B, nv = q.shape[0], self.nv
+        tau = np.empty((B, nv))
+        dq, dv, M = (np.empty((B, nv, nv)) for _ in range(3))
+        self._check(lib().orc_rnea_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(tau), _ptr(dq), _ptr(dv), _ptr(M), nthreads))
+        return tau, dq, dv, M
+
+    def aba_derivatives(self, q, v, tau, prec=0, nthreads=0):
+        """(ddq, ddq_dq, ddq_dv, Minv)."""
+        q, v, tau = _c(q), _c(v), _c(tau)
+        B, nv = q.shape[0], self.nv
+        ddq = np.empty((B, nv))
+        dq, dv, Minv = (np.empty((B, nv, nv)) for _ in range(3))
+        self._check(lib().orc_aba_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), _ptr(dq), _ptr(dv), _ptr(Minv), nthreads))
+        return ddq, dq, dv, Minv
+
+    def integrate(self, q, v, prec=0, nthreads=0):
+        q, v = _c(q), _c(v)
+        out = np.empty_like(q)
+        self._check(lib().orc_integrate(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(out), nthreads))
+        return out
+
+    def count_flops(self, func, q, v=None, x=None):
+        """(ops, sincos pairs) of one evaluation at a single instance."""
+        q = _c(q).reshape(-1)
+        v = None if v is None else _c(v).reshape(-1)
+        x = None if x is None else _c(x).reshape(-1)
+        ops, sc = C.c_double(), C.c_double()
+        self._check(lib().orc_count_flops(self.h, func, _ptr(q), _ptr(v), _ptr(x), C.byref(ops), C.byref(sc)))
+        return ops.value, sc.value
+
+
+def symmetrize_upper(M):
+    """make_symmetric on the upper triangle (reference bindings/python/algorithm/expose-crba.cpp:22)."""
+    U = np.triu(M)
+    return U + np.swapaxes(np.triu(M, 1), -1, -2)

@@ -1,0 +1,262 @@
+// Test infrastructure: C entry points of the CPU oracle (liboracle.so).
+//
+// Batch drivers mirror the reference's OpenMP batch entry points
+// rneaInParallel / abaInParallel (algorithm/parallel/rnea.hpp:39-84,
+// algorithm/parallel/aba.hpp:40-84): `#pragma omp parallel for
+// schedule(static)` over instances, one thread-private Data per thread.
+// Batch arrays are instance-contiguous (the reference's column-major
+// nq x batch / nv x batch matrices): instance b of q starts at q + b*nq.
+// Matrix outputs are nv x nv row-major per instance.
+// Precision argument: 0 = double, 1 = long double (inputs and outputs stay double).
+#include <omp.h>
+
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+
+#include "oracle.hpp"
+#include "flop_scalar.hpp"
+
+namespace orc {
+thread_local long long FlopCounter::ops = 0;
+thread_local long long FlopCounter::sincos = 0;
+}  // namespace orc
+
+using orc::Model;
+
+namespace {
+thread_local std::string g_err;
+
+template <class T>
+struct Buf {  // converts one instance's double inputs to T
+  std::vector<T> x;
+  void load(const double* p, int n) {
+    x.resize(n);
+    for (int k = 0; k < n; ++k) x[k] = T(p[k]);
+  }
+};
+template <class T> inline void store(const std::vector<T>& src, double* dst, size_t n) {
+  for (size_t k = 0; k < n; ++k) dst[k] = (double)src[k];
+}
+
+enum Func { F_RNEA = 0, F_ABA_LOCAL, F_ABA_WORLD, F_CRBA_LOCAL, F_CRBA_WORLD, F_CHOL, F_RNEA_D, F_ABA_D, F_INTEGRATE };
+
+template <class T>
+void run_one(const Model& m, orc::Data<T>& d, int func, const double* q, const double* v, const double* x,
+             double* o1, double* o2, double* o3, double* o4) {
+  Buf<T> bq, bv, bx;
+  const int nq = m.nq, nv = m.nv;
+  const size_t nn = (size_t)nv * nv;
+  bq.load(q, nq);
+  if (v) bv.load(v, nv);
+  if (x) bx.load(x, nv);
+  switch (func) {
+    case F_RNEA:
+      orc::rnea(m, d, bq.x.data(), bv.x.data(), bx.x.data());
+      store(d.tau, o1, nv);
+      break;
+    case F_ABA_LOCAL:
+    case F_ABA_WORLD:
+      orc::aba(m, d, bq.x.data(), bv.x.data(), bx.x.data(), func == F_ABA_WORLD ? orc::WORLD : orc::LOCAL);
+      store(d.ddq, o1, nv);
+      break;
+    case F_CRBA_LOCAL:
+    case F_CRBA_WORLD:
+      std::fill(d.M.begin(), d.M.end(), T(0));
+      orc::crba(m, d, bq.x.data(), func == F_CRBA_WORLD ? orc::WORLD : orc::LOCAL);
+      store(d.M, o1, nn);
+      break;
+    case F_CHOL: {  // q holds an nv x nv row-major M (upper triangle read)
+      Buf<T> bm;
+      bm.load(q, (int)nn);
+      d.M = bm.x;
+      std::fill(d.U.begin(), d.U.end(), T(0));
+      for (int k = 0; k < nv; ++k) d.U[(size_t)k * nv + k] = T(1);
+      orc::cholesky_decompose(m, d);
+      store(d.U, o1, nn);
+      store(d.D, o2, nv);
+      break;
+    }
+    case F_RNEA_D:
+      std::fill(d.M.begin(), d.M.end(), T(0));
+      std::fill(d.dtau_dq.begin(), d.dtau_dq.end(), T(0));
+      std::fill(d.dtau_dv.begin(), d.dtau_dv.end(), T(0));
+      orc::rnea_derivatives(m, d, bq.x.data(), bv.x.data(), bx.x.data());
+      if (o1) store(d.tau, o1, nv);
+      if (o2) store(d.dtau_dq, o2, nn);
+      if (o3) store(d.dtau_dv, o3, nn);
+      if (o4) store(d.M, o4, nn);
+      break;
+    case F_ABA_D:
+      std::fill(d.dtau_dq.begin(), d.dtau_dq.end(), T(0));
+      std::fill(d.dtau_dv.begin(), d.dtau_dv.end(), T(0));
+      orc::aba_derivatives(m, d, bq.x.data(), bv.x.data(), bx.x.data());
+      if (o1) store(d.ddq, o1, nv);
+      if (o2) store(d.ddq_dq, o2, nn);
+      if (o3) store(d.ddq_dv, o3, nn);
+      if (o4) store(d.Minv, o4, nn);
+      break;
+    case F_INTEGRATE: {
+      std::vector<T> out(nq);
+      orc::integrate(m, bq.x.data(), bv.x.data(), out.data());
+      store(out, o1, nq);
+      break;
+    }
+    default:
+      throw std::invalid_argument("unknown function");
+  }
+}
+
+int in_stride(int func, const Model& m, int which) {  // per-instance input lengths
+  if (which == 0) return func == F_CHOL ? m.nv * m.nv : m.nq;
+  return m.nv;
+}
+int out_stride(int func, const Model& m, int which) {
+  const int nn = m.nv * m.nv;
+  switch (func) {
+    case F_CRBA_LOCAL: case F_CRBA_WORLD: return nn;
+    case F_CHOL: return which == 0 ? nn : m.nv;
+    case F_RNEA_D: case F_ABA_D: return which == 0 ? m.nv : nn;
+    case F_INTEGRATE: return m.nq;
+    default: return m.nv;
+  }
+}
+
+template <class T>
+int run_batch(const Model& m, int func, long B, const double* q, const double* v, const double* x, double* o1,
+              double* o2, double* o3, double* o4, int nthreads) {
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  omp_set_dynamic(0);  // set_default_omp_options (algorithm/parallel/omp.hpp:12-16)
+  omp_set_num_threads(nthreads);
+  const int sq = in_stride(func, m, 0), sv = in_stride(func, m, 1);
+  const int s1 = out_stride(func, m, 0), s2 = out_stride(func, m, 1), s3 = out_stride(func, m, 2),
+            s4 = out_stride(func, m, 3);
+  std::vector<std::unique_ptr<orc::Data<T>>> datas(nthreads);  // the ModelPool's per-thread Data
+  for (int t = 0; t < nthreads; ++t) datas[t].reset(new orc::Data<T>(m));
+  bool failed = false;
+  std::string msg;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    try {
+      run_one<T>(m, *datas[omp_get_thread_num()], func, q + (size_t)b * sq, v ? v + (size_t)b * sv : nullptr,
+                 x ? x + (size_t)b * sv : nullptr, o1 ? o1 + (size_t)b * s1 : nullptr,
+                 o2 ? o2 + (size_t)b * s2 : nullptr, o3 ? o3 + (size_t)b * s3 : nullptr,
+                 o4 ? o4 + (size_t)b * s4 : nullptr);
+    } catch (const std::exception& e) {
+#pragma omp critical
+      {
+        failed = true;
+        msg = e.what();
+      }
+    }
+  }
+  if (failed) {
+    g_err = msg;
+    return -1;
+  }
+  return 0;
+}
+
+int dispatch(void* h, int prec, int func, long B, const double* q, const double* v, const double* x, double* o1,
+             double* o2, double* o3, double* o4, int nthreads) {
+  if (!h) { g_err = "null model"; return -1; }
+  const Model& m = *static_cast<Model*>(h);
+  if (prec == 0) return run_batch<double>(m, func, B, q, v, x, o1, o2, o3, o4, nthreads);
+  if (prec == 1) return run_batch<long double>(m, func, B, q, v, x, o1, o2, o3, o4, nthreads);
+  g_err = "unknown precision";
+  return -1;
+}
+}  // namespace
+
+extern "C" {
+
+const char* orc_last_error() { return g_err.c_str(); }
+
+void* orc_model_new(int njoints, const int* parents, const int* jtype, const double* placement,
+                    const double* inertia, const double* armature, int nv_armature, const double* gravity) {
+  try {
+    auto* m = new Model();
+    m->njoints = njoints;
+    m->parents.assign(parents, parents + njoints);
+    m->jtype.assign(jtype, jtype + njoints);
+    m->placement.assign(placement, placement + 12 * njoints);
+    m->inertia.assign(inertia, inertia + 10 * njoints);
+    if (armature) m->armature.assign(armature, armature + nv_armature);
+    if (gravity) std::memcpy(m->gravity, gravity, 6 * sizeof(double));
+    m->finalize();
+    return m;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+
+void orc_model_free(void* h) { delete static_cast<Model*>(h); }
+
+int orc_model_dims(void* h, int* nq, int* nv) {
+  const Model& m = *static_cast<Model*>(h);
+  *nq = m.nq;
+  *nv = m.nv;
+  return 0;
+}
+
+// Copies the tree tables: idx_q, idx_v, nvSubtree (njoints each) and
+// parents_fromRow, nvSubtree_fromRow (nv each).
+int orc_model_tables(void* h, int* idx_q, int* idx_v, int* nvSubtree, int* parents_fromRow, int* nvSubtree_fromRow) {
+  const Model& m = *static_cast<Model*>(h);
+  for (int i = 0; i < m.njoints; ++i) { idx_q[i] = m.idx_q[i]; idx_v[i] = m.idx_v[i]; nvSubtree[i] = m.nvSubtree[i]; }
+  for (int k = 0; k < m.nv; ++k) { parents_fromRow[k] = m.parents_fromRow[k]; nvSubtree_fromRow[k] = m.nvSubtree_fromRow[k]; }
+  return 0;
+}
+
+int orc_rnea(void* h, int prec, long B, const double* q, const double* v, const double* a, double* tau, int nt) {
+  return dispatch(h, prec, F_RNEA, B, q, v, a, tau, nullptr, nullptr, nullptr, nt);
+}
+int orc_aba(void* h, int prec, int conv, long B, const double* q, const double* v, const double* tau, double* ddq,
+            int nt) {
+  return dispatch(h, prec, conv == orc::WORLD ? F_ABA_WORLD : F_ABA_LOCAL, B, q, v, tau, ddq, nullptr, nullptr,
+                  nullptr, nt);
+}
+int orc_crba(void* h, int prec, int conv, long B, const double* q, double* M, int nt) {
+  return dispatch(h, prec, conv == orc::WORLD ? F_CRBA_WORLD : F_CRBA_LOCAL, B, q, nullptr, nullptr, M, nullptr,
+                  nullptr, nullptr, nt);
+}
+int orc_cholesky(void* h, int prec, long B, const double* M, double* U, double* D, int nt) {
+  return dispatch(h, prec, F_CHOL, B, M, nullptr, nullptr, U, D, nullptr, nullptr, nt);
+}
+int orc_rnea_derivatives(void* h, int prec, long B, const double* q, const double* v, const double* a, double* tau,
+                         double* dtau_dq, double* dtau_dv, double* M, int nt) {
+  return dispatch(h, prec, F_RNEA_D, B, q, v, a, tau, dtau_dq, dtau_dv, M, nt);
+}
+int orc_aba_derivatives(void* h, int prec, long B, const double* q, const double* v, const double* tau, double* ddq,
+                        double* ddq_dq, double* ddq_dv, double* Minv, int nt) {
+  return dispatch(h, prec, F_ABA_D, B, q, v, tau, ddq, ddq_dq, ddq_dv, Minv, nt);
+}
+int orc_integrate(void* h, int prec, long B, const double* q, const double* v, double* qout, int nt) {
+  return dispatch(h, prec, F_INTEGRATE, B, q, v, nullptr, qout, nullptr, nullptr, nullptr, nt);
+}
+
+// Counts the floating-point operations of one evaluation of `func` at the
+// given instance (q, v, x); returns {ops, sincos pairs}.
+int orc_count_flops(void* h, int func, const double* q, const double* v, const double* x, double* ops,
+                    double* sincos) {
+  try {
+    const Model& m = *static_cast<Model*>(h);
+    orc::Data<orc::FlopScalar> d(m);
+    std::vector<double> o1((size_t)m.nv * m.nv + m.nq), o2((size_t)m.nv * m.nv), o3((size_t)m.nv * m.nv),
+        o4((size_t)m.nv * m.nv);
+    orc::FlopCounter::ops = 0;
+    orc::FlopCounter::sincos = 0;
+    run_one<orc::FlopScalar>(m, d, func, q, v, x, o1.data(), o2.data(), o3.data(), o4.data());
+    *ops = (double)orc::FlopCounter::ops;
+    *sincos = (double)orc::FlopCounter::sincos;
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+}  // extern "C"

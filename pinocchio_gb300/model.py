@@ -1,0 +1,233 @@
+"""Kinematic-tree model description, shaped like the reference's ``pin.Model``.
+
+The reference builds a ``ModelTpl`` joint by joint with ``addJoint`` and
+``appendBodyToJoint`` (reference multibody/model.hxx:61-170); joints are stored
+in insertion order with ``parents[i] < i`` and the configuration / velocity
+indices ``idx_q`` / ``idx_v`` are cumulative in that order.  This module keeps
+that construction API for the joint types on the batched dynamics path
+(revolute about the unit x, y or z axis and the free-flyer) and flattens the
+tree into the plain tables the C ABI takes:
+
+* ``parents`` (int32, njoints), ``jtype`` (int32, njoints; 0 = universe,
+  1/2/3 = RX/RY/RZ, 4 = free-flyer),
+* ``placement`` (njoints x 12: rotation row-major, then translation),
+* ``inertia`` (njoints x 10: mass, lever (COM), rotational inertia about the COM
+  packed as [xx, xy, yy, xz, yz, zz] -- reference spatial/symmetric3.hpp:46-49),
+* ``armature`` (nv) and ``gravity`` (6, [linear; angular]).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF = 0, 1, 2, 3, 4
+_JT_NQ = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 7}
+_JT_NV = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 6}
+
+
+class Convention:
+    """Frame convention of ABA / CRBA (reference multibody/fwd.hpp:73-81)."""
+
+    LOCAL = 0
+    WORLD = 1
+
+
+class JointModel:
+    jtype = JT_NONE
+
+    @property
+    def nq(self) -> int:
+        return _JT_NQ[self.jtype]
+
+    @property
+    def nv(self) -> int:
+        return _JT_NV[self.jtype]
+
+
+class JointModelRX(JointModel):
+    jtype = JT_RX
+
+
+class JointModelRY(JointModel):
+    jtype = JT_RY
+
+
+class JointModelRZ(JointModel):
+    jtype = JT_RZ
+
+
+class JointModelFreeFlyer(JointModel):
+    jtype = JT_FF
+
+
+class SE3:
+    """Rigid transform (R, t)."""
+
+    def __init__(self, rotation=None, translation=None):
+        self.rotation = np.eye(3) if rotation is None else np.asarray(rotation, dtype=np.float64).reshape(3, 3)
+        self.translation = np.zeros(3) if translation is None else np.asarray(translation, dtype=np.float64).reshape(3)
+
+    @staticmethod
+    def Identity() -> "SE3":
+        return SE3()
+
+    def act_point(self, p):
+        return self.rotation @ p + self.translation
+
+
+class Inertia:
+    """Spatial inertia (mass, lever, rotational inertia about the COM)."""
+
+    def __init__(self, mass: float, lever, inertia):
+        self.mass = float(mass)
+        self.lever = np.asarray(lever, dtype=np.float64).reshape(3)
+        inertia = np.asarray(inertia, dtype=np.float64)
+        if inertia.shape == (3, 3):
+            inertia = np.array([inertia[0, 0], inertia[1, 0], inertia[1, 1], inertia[2, 0], inertia[2, 1], inertia[2, 2]])
+        self.inertia = inertia.reshape(6)
+
+    @staticmethod
+    def Zero() -> "Inertia":
+        return Inertia(0.0, np.zeros(3), np.zeros(6))
+
+    def matrix3(self):
+        s = self.inertia
+        return np.array([[s[0], s[1], s[3]], [s[1], s[2], s[4]], [s[3], s[4], s[5]]])
+
+    def se3_action(self, M: SE3) -> "Inertia":
+        """M.act(Y) (reference spatial/inertia.hpp:873-880)."""
+        R = M.rotation
+        return Inertia(self.mass, M.translation + R @ self.lever, R @ self.matrix3() @ R.T)
+
+    def __add__(self, other: "Inertia") -> "Inertia":
+        """Y_a + Y_b (reference spatial/inertia.hpp:641-657)."""
+        mab = self.mass + other.mass
+        inv = 1.0 / max(mab, np.finfo(np.float64).eps)
+        c = (self.mass * self.lever + other.mass * other.lever) * inv
+        ab = self.lever - other.lever
+        skew_sq = np.outer(ab, ab) - ab.dot(ab) * np.eye(3)
+        return Inertia(mab, c, self.matrix3() + other.matrix3() - (self.mass * other.mass * inv) * skew_sq)
+
+
+class Model:
+    """Flattened kinematic tree; joint 0 is the universe."""
+
+    def __init__(self):
+        self.names = ["universe"]
+        self.parents = [0]
+        self.jtypes = [JT_NONE]
+        self.jointPlacements = [SE3.Identity()]
+        self.inertias = [Inertia.Zero()]
+        self.armature = np.zeros(0)
+        self.gravity = np.array([0.0, 0.0, -9.81, 0.0, 0.0, 0.0])
+        self.name = ""
+
+    # -- construction (reference multibody/model.hxx:61-170) -------------------------------
+    def addJoint(self, parent_id: int, joint: JointModel, placement: SE3, name: str = "") -> int:
+        if not 0 <= parent_id < self.njoints:
+            raise ValueError("parent joint index out of range")
+        self.parents.append(int(parent_id))
+        self.jtypes.append(int(joint.jtype))
+        self.jointPlacements.append(placement)
+        self.inertias.append(Inertia.Zero())
+        self.names.append(name or f"joint_{self.njoints - 1}")
+        self.armature = np.concatenate([self.armature, np.zeros(joint.nv)])
+        return self.njoints - 1
+
+    def appendBodyToJoint(self, joint_id: int, inertia: Inertia, placement: SE3 | None = None) -> None:
+        placed = inertia if placement is None else inertia.se3_action(placement)
+        cur = self.inertias[joint_id]
+        self.inertias[joint_id] = placed if cur.mass == 0.0 and not cur.inertia.any() else cur + placed
+
+    # -- sizes ----------------------------------------------------------------------------
+    @property
+    def njoints(self) -> int:
+        return len(self.parents)
+
+    @property
+    def nqs(self):
+        return [_JT_NQ[j] for j in self.jtypes]
+
+    @property
+    def nvs(self):
+        return [_JT_NV[j] for j in self.jtypes]
+
+    @property
+    def idx_qs(self):
+        return list(np.concatenate([[0], np.cumsum(self.nqs)[:-1]]).astype(int))
+
+    @property
+    def idx_vs(self):
+        return list(np.concatenate([[0], np.cumsum(self.nvs)[:-1]]).astype(int))
+
+    @property
+    def nq(self) -> int:
+        return int(sum(self.nqs))
+
+    @property
+    def nv(self) -> int:
+        return int(sum(self.nvs))
+
+    def has_free_flyer(self) -> bool:
+        return JT_FF in self.jtypes
+
+    # -- flattening for the C ABI ----------------------------------------------------------
+    def tables(self) -> dict:
+        nj = self.njoints
+        placement = np.zeros((nj, 12))
+        inertia = np.zeros((nj, 10))
+        for i in range(nj):
+            placement[i, :9] = self.jointPlacements[i].rotation.reshape(9)
+            placement[i, 9:] = self.jointPlacements[i].translation
+            Y = self.inertias[i]
+            inertia[i, 0] = Y.mass
+            inertia[i, 1:4] = Y.lever
+            inertia[i, 4:] = Y.inertia
+        return dict(
+            parents=np.ascontiguousarray(self.parents, dtype=np.int32),
+            jtype=np.ascontiguousarray(self.jtypes, dtype=np.int32),
+            placement=np.ascontiguousarray(placement),
+            inertia=np.ascontiguousarray(inertia),
+            armature=np.ascontiguousarray(self.armature, dtype=np.float64),
+            gravity=np.ascontiguousarray(self.gravity, dtype=np.float64),
+        )
+
+    def subtree_tables(self) -> dict:
+        """nvSubtree, parents_fromRow, nvSubtree_fromRow (reference multibody/data.hxx:195-306)."""
+        nj, nvs, idx_v = self.njoints, self.nvs, self.idx_vs
+        last = [-1] * nj
+        nvsub = [0] * nj
+        for i in range(nj - 1, -1, -1):
+            if last[i] == -1:
+                last[i] = i
+            p = self.parents[i] if i > 0 else 0
+            last[p] = max(last[i], last[p])
+            nvsub[i] = idx_v[last[i]] + nvs[last[i]] - idx_v[i]
+        pfr = [-1] * self.nv
+        nsfr = [0] * self.nv
+        for j in range(1, nj):
+            p = self.parents[j]
+            iv = idx_v[j]
+            pfr[iv] = idx_v[p] + nvs[p] - 1 if p > 0 else -1
+            nsfr[iv] = nvsub[j]
+            for r in range(1, nvs[j]):
+                pfr[iv + r] = iv + r - 1
+                nsfr[iv + r] = nvsub[j] - r
+        return dict(lastChild=last, nvSubtree=nvsub, parents_fromRow=pfr, nvSubtree_fromRow=nsfr)
+
+    def check_depth_first(self) -> None:
+        """Compact-subtree condition the CRBA needs (reference algorithm/crba.hxx:573-595)."""
+        last = self.subtree_tables()["lastChild"]
+        for i in range(1, self.njoints):
+            for k in range(i + 1, last[i] + 1):
+                a = k
+                while a > i:
+                    a = self.parents[a]
+                if a != i:
+                    raise ValueError("joints are not in depth-first order")
+
+    def neutral(self) -> np.ndarray:
+        q = np.zeros(self.nq)
+        for i, (jt, iq) in enumerate(zip(self.jtypes, self.idx_qs)):
+            if jt == JT_FF:
+                q[iq + 6] = 1.0
+        return q

@@ -1,0 +1,215 @@
+"""Seeded synthetic models and inputs for the batched dynamics workloads.
+
+The reference builds its test robots with ``buildModels::humanoidRandom`` and
+``manipulator`` (reference multibody/sample-models.hxx:20-308) from unseeded
+``Inertia::Random`` / ``SE3::Random`` draws.  The workloads here need
+reproducible models, so every generator takes an explicit seed and draws from
+numpy's PCG64 (``np.random.default_rng(seed)``):
+
+* joint placement: rotation from a uniform random unit quaternion (normalised
+  4-D Gaussian), translation U[-0.3, 0.3]^3 m;
+* link inertia: mass U[0.5, 5] kg (or the range given), COM U[-0.1, 0.1]^3 m,
+  rotational inertia R diag(U[0.01, 0.1]^3) R^T with R a uniform random rotation;
+* revolute axes uniform over the unit x / y / z axes.
+
+Workloads:
+  ``manipulator6r``  6 revolute joints in series (nq = nv = 6);
+  ``humanoid32``     free-flyer root, two torso revolute joints, four limbs of
+                     six revolute joints hanging off the torso (nq 33, nv 32);
+  ``random_tree``    seeded trees with 0-3 children per node (optional free-flyer root);
+  ``chain``          a revolute serial chain (100 links, masses U[0.1, 1] kg).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .model import (
+    JT_FF,
+    Inertia,
+    JointModelFreeFlyer,
+    JointModelRX,
+    JointModelRY,
+    JointModelRZ,
+    Model,
+    SE3,
+)
+
+_REVOLUTE = (JointModelRX, JointModelRY, JointModelRZ)
+
+
+def quat_to_matrix(x, y, z, w) -> np.ndarray:
+    return np.array(
+        [
+            [1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+            [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+            [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)],
+        ]
+    )
+
+
+def random_unit_quaternion(rng: np.random.Generator, n: int | None = None) -> np.ndarray:
+    """Uniform unit quaternion(s) (x, y, z, w): a normalised 4-D Gaussian."""
+    g = rng.standard_normal((4,) if n is None else (n, 4))
+    return g / np.linalg.norm(g, axis=-1, keepdims=True)
+
+
+def random_rotation(rng: np.random.Generator) -> np.ndarray:
+    return quat_to_matrix(*random_unit_quaternion(rng))
+
+
+def random_placement(rng: np.random.Generator) -> SE3:
+    R = random_rotation(rng)
+    t = rng.uniform(-0.3, 0.3, 3)
+    return SE3(R, t)
+
+
+def random_inertia(rng: np.random.Generator, mass_range=(0.5, 5.0)) -> Inertia:
+    m = rng.uniform(*mass_range)
+    c = rng.uniform(-0.1, 0.1, 3)
+    R = random_rotation(rng)
+    I = R @ np.diag(rng.uniform(0.01, 0.1, 3)) @ R.T
+    I = 0.5 * (I + I.T)
+    return Inertia(m, c, I)
+
+
+def _random_revolute(rng: np.random.Generator):
+    return _REVOLUTE[int(rng.integers(0, 3))]()
+
+
+def _add_link(model: Model, rng, parent: int, joint, name: str, mass_range=(0.5, 5.0)) -> int:
+    jid = model.addJoint(parent, joint, random_placement(rng), name)
+    model.appendBodyToJoint(jid, random_inertia(rng, mass_range))
+    return jid
+
+
+def manipulator6r(seed: int = 0) -> Model:
+    """6-revolute serial manipulator (nq = nv = 6)."""
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = "manipulator6r"
+    parent = 0
+    for k in range(6):
+        parent = _add_link(model, rng, parent, _random_revolute(rng), f"j{k + 1}")
+    return model
+
+
+def humanoid32(seed: int = 1) -> Model:
+    """Free-flyer + 2 torso revolute joints + 4 limbs x 6 revolute joints (nq 33, nv 32)."""
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = "humanoid32"
+    root = _add_link(model, rng, 0, JointModelFreeFlyer(), "root")
+    t1 = _add_link(model, rng, root, _random_revolute(rng), "torso1")
+    t2 = _add_link(model, rng, t1, _random_revolute(rng), "torso2")
+    for limb in range(4):
+        parent = t2
+        for k in range(6):
+            parent = _add_link(model, rng, parent, _random_revolute(rng), f"limb{limb}_{k}")
+    return model
+
+
+def random_tree(nv: int, free_flyer: bool, seed: int, max_children: int = 3) -> Model:
+    """Seeded tree with 0..max_children children per node and exactly ``nv`` dofs.
+
+    The tree is grown breadth-first (each node draws its number of children),
+    then emitted in depth-first order so that ``parents[i] < i`` and every
+    subtree is a contiguous joint range, as the reference requires.
+    """
+    rng = np.random.default_rng(seed)
+    n_rev = nv - (6 if free_flyer else 0)
+    if n_rev < 1:
+        raise ValueError("tree needs at least one revolute joint")
+    children: dict[int, list[int]] = {0: []}  # node 0 = root joint (FF or first revolute)
+    n_nodes = 1 if free_flyer else 1
+    rev_left = n_rev - (0 if free_flyer else 1)
+    frontier = [0]
+    while rev_left > 0:
+        nxt = []
+        for node in frontier:
+            if rev_left == 0:
+                break
+            k = int(rng.integers(0, max_children + 1))
+            if node == 0 and k == 0:
+                k = 1
+            k = min(k, rev_left)
+            for _ in range(k):
+                children[node].append(n_nodes)
+                children[n_nodes] = []
+                nxt.append(n_nodes)
+                n_nodes += 1
+                rev_left -= 1
+        if not nxt:  # every frontier node drew zero children: force one
+            node = frontier[int(rng.integers(0, len(frontier)))]
+            children[node].append(n_nodes)
+            children[n_nodes] = []
+            nxt.append(n_nodes)
+            n_nodes += 1
+            rev_left -= 1
+        frontier = nxt
+    model = Model()
+    model.name = f"tree{nv}{'ff' if free_flyer else ''}"
+
+    def emit(node: int, parent_jid: int):
+        if node == 0 and free_flyer:
+            joint = JointModelFreeFlyer()
+        else:
+            joint = _random_revolute(rng)
+        jid = _add_link(model, rng, parent_jid, joint, f"n{node}")
+        for ch in children[node]:
+            emit(ch, jid)
+
+    emit(0, 0)
+    assert model.nv == nv, (model.nv, nv)
+    return model
+
+
+def chain(n: int = 100, seed: int = 4, mass_range=(0.1, 1.0)) -> Model:
+    """Revolute serial chain of ``n`` links."""
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = f"chain{n}"
+    parent = 0
+    for k in range(n):
+        parent = _add_link(model, rng, parent, _random_revolute(rng), f"l{k}", mass_range)
+    return model
+
+
+def heterogeneous_trees(seed: int = 3):
+    """The four trees of the heterogeneous batch: nv 7, 12, 32 (FF), 60 (FF)."""
+    return [
+        random_tree(7, False, seed * 100 + 7),
+        random_tree(12, False, seed * 100 + 12),
+        random_tree(32, True, seed * 100 + 32),
+        random_tree(60, True, seed * 100 + 60),
+    ]
+
+
+# ---------------------------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------------------------
+def random_configurations(model: Model, batch: int, rng: np.random.Generator) -> np.ndarray:
+    """q of shape (batch, nq): FF position N(0,1), uniform unit quaternion; joints U[-pi, pi]."""
+    q = np.empty((batch, model.nq))
+    for jt, iq in zip(model.jtypes[1:], model.idx_qs[1:]):
+        if jt == JT_FF:
+            q[:, iq : iq + 3] = rng.standard_normal((batch, 3))
+            q[:, iq + 3 : iq + 7] = random_unit_quaternion(rng, batch)
+        else:
+            q[:, iq] = rng.uniform(-np.pi, np.pi, batch)
+    return q
+
+
+def random_inputs(model: Model, batch: int, seed: int, v_scale=1.0, x_scale=1.0):
+    """(q, v, x) with v ~ N(0, v_scale^2), x ~ N(0, x_scale^2); arrays are (batch, n)."""
+    rng = np.random.default_rng(seed)
+    q = random_configurations(model, batch, rng)
+    v = v_scale * rng.standard_normal((batch, model.nv))
+    x = x_scale * rng.standard_normal((batch, model.nv))
+    return q, v, x
+
+
+WORKLOADS = {
+    "manipulator6r": manipulator6r,
+    "humanoid32": humanoid32,
+    "chain100": lambda seed=4: chain(100, seed),
+}
