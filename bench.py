@@ -1,0 +1,471 @@
+"""Benchmark of the batched dynamics hot path on one GB300 (sm_103a).
+
+Workload (the headline configuration): the 32-dof synthetic humanoid
+(free-flyer + 2 torso + 4 limbs x 6 revolute joints, nq 33, nv 32), batch
+65536 configurations per GPU (q: random unit quaternion, base N(0,1), joints
+U[-pi, pi]; v ~ N(0,1); tau ~ N(0,10)).  One step = ABA (ddq) + ABA
+derivatives (ddq_dq, ddq_dv, Minv) of the whole batch.  ``value`` is
+configurations per second of the mixed-precision kernels (FP32 sweeps, FP64
+Schur complement), inputs resident in HBM; the plain FP64 kernels are timed
+beside it (``fp64``) and both are checked against the FP64 oracle on a
+sample.  ``e2e`` is the same step through the public API with the inputs in
+pinned host memory and the outputs copied back to host memory every step.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the instances shard with no exchange step): ``value`` sums all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ABA/RNEA/derivative evals/s, 1 GB300: mixed vs FP64 plain at ≤1e-5 rel err"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--batch", type=int, default=65536)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        import torch
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+# ------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5,
+                ).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 5 + k and s[5 + k].lower() == "active"})
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(self.samples),
+        }
+
+
+# ------------------------------------------------------------------------------------------
+# reference arm: the reference's CPU algorithm (the oracle port) on all host cores
+# ------------------------------------------------------------------------------------------
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle.oracle import WORLD, OracleModel
+    from pinocchio_gb300 import sample_models as sm
+
+    model = sm.humanoid32(1)
+    om = OracleModel(model)
+    cores = os.cpu_count() or 1
+    sample = min(args.batch, 4096)
+    q, v, x = sm.random_inputs(model, sample, 0)
+    tau = 10.0 * x
+    for _ in range(max(1, args.warmup)):
+        om.aba(q[:256], v[:256], tau[:256], WORLD, nthreads=cores)
+        om.aba_derivatives(q[:256], v[:256], tau[:256], nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        om.aba(q, v, tau, WORLD, nthreads=cores)
+        om.aba_derivatives(q, v, tau, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    rate = sample / t
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": rate,
+        "unit": "evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t * args.batch / sample,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded humanoid32 model and inputs)",
+        "config": {
+            "workload": f"humanoid32 nv=32 ABA(WORLD)+computeABADerivatives, batch {args.batch}",
+            "batch": args.batch,
+            "parallelism": "openmp static over instances (rneaInParallel/abaInParallel structure)",
+        },
+        "cpu_baseline": {
+            "value": rate,
+            "unit": "evals/s",
+            "cores": cores,
+            "kind": "port",
+            "sample": f"{sample} configurations per step, ABA + ABA derivatives, FP64, {cores} OpenMP threads",
+        },
+        "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------------
+def fp64_peak_tflops(torch):
+    """Measured FP64 throughput of this GPU: a cuBLAS DGEMM (4096^3), best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2.0 * n**3 / best / 1e12
+
+
+def run_ours(args, world, rank, local, dist):
+    import torch
+
+    import pinocchio_gb300 as pg
+    from pinocchio_gb300 import _capi
+    from pinocchio_gb300 import sample_models as sm
+
+    torch.cuda.set_device(local)
+    B = args.batch
+    model = sm.humanoid32(1)
+    nq, nv = model.nq, model.nv
+    nrot = 4  # input copies rotated across steps: 4 x 51 MB > 129 MB L2
+    host = [sm.random_inputs(model, B, 100 * rank + r) for r in range(nrot)]
+    dev = [(torch.from_numpy(q).cuda(), torch.from_numpy(v).cuda(), torch.from_numpy(10.0 * x).cuda()) for q, v, x in host]
+    stream = torch.cuda.current_stream()
+    L = _capi.lib()
+    import ctypes
+
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    outs = {
+        "ddq": torch.empty((B, nv), dtype=torch.float64, device="cuda"),
+        "ddq_dq": torch.empty((B, nv, nv), dtype=torch.float64, device="cuda"),
+        "ddq_dv": torch.empty((B, nv, nv), dtype=torch.float64, device="cuda"),
+        "Minv": torch.empty((B, nv, nv), dtype=torch.float64, device="cuda"),
+        "ddq2": torch.empty((B, nv), dtype=torch.float64, device="cuda"),
+    }
+    data = {p: pg.createData(model, p) for p in ("fp64", "mixed")}
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    PREC = {"fp64": _capi.GB_FP64, "mixed": _capi.GB_MIXED}
+
+    def step(prec, k):
+        q, v, tau = dev[k % nrot]
+        h = data[prec].dev.h
+        _capi.check(L.gb_aba(h, PREC[prec], _capi.GB_LOCAL, _capi.GB_LAYOUT_INSTANCE, B, P(q), P(v), P(tau), P(outs["ddq"]), sp))
+        _capi.check(
+            L.gb_aba_derivatives(
+                h, PREC[prec], _capi.GB_LAYOUT_INSTANCE, B, P(q), P(v), P(tau), P(outs["ddq_dq"]), P(outs["ddq_dv"]),
+                P(outs["Minv"]), P(outs["ddq2"]), sp,
+            )
+        )
+
+    def timed(prec, steps, warmup, sampler=None):
+        for k in range(warmup):
+            step(prec, k)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ctx = sampler if sampler is not None else _Null()
+        with ctx:
+            s.record(stream)
+            for k in range(steps):
+                step(prec, k)
+            e.record(stream)
+            torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / steps
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # per-kernel times (dominant kernel for the roofline) with events on the launching stream
+    def kernel_times(prec, reps=5):
+        q, v, tau = dev[0]
+        h = data[prec].dev.h
+        res = {}
+        for name in ("aba", "aba_derivatives"):
+            for _ in range(2):
+                step(prec, 0)
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            for _ in range(reps):
+                if name == "aba":
+                    _capi.check(L.gb_aba(h, PREC[prec], _capi.GB_LOCAL, _capi.GB_LAYOUT_INSTANCE, B, P(q), P(v), P(tau), P(outs["ddq"]), sp))
+                else:
+                    _capi.check(
+                        L.gb_aba_derivatives(
+                            h, PREC[prec], _capi.GB_LAYOUT_INSTANCE, B, P(q), P(v), P(tau), P(outs["ddq_dq"]),
+                            P(outs["ddq_dv"]), P(outs["Minv"]), P(outs["ddq2"]), sp,
+                        )
+                    )
+            e.record(stream)
+            torch.cuda.synchronize()
+            res[name] = s.elapsed_time(e) / reps
+        return res
+
+    sampler = ClockSampler(local)
+    ms_fp64 = timed("fp64", args.steps, args.warmup)
+    ms_mixed = timed("mixed", args.steps, args.warmup, sampler)
+    clocks = sampler.summary()
+    kt_mixed = kernel_times("mixed")
+    kt_fp64 = kernel_times("fp64")
+
+    # accuracy of the mixed and FP64 outputs against the FP64 oracle on a sample (rank 0)
+    acc = {}
+    if rank == 0:
+        from oracle.oracle import OracleModel
+
+        om = OracleModel(model)
+        ns = 512
+        q, v, x = host[0]
+        ref = om.aba_derivatives(q[:ns], v[:ns], 10.0 * x[:ns])
+        for prec in ("mixed", "fp64"):
+            step(prec, 0)
+            torch.cuda.synchronize()
+            got = [outs["ddq2"][:ns], outs["ddq_dq"][:ns], outs["ddq_dv"][:ns], outs["Minv"][:ns]]
+            errs = []
+            for g, r in zip(got, ref):
+                g = g.cpu().numpy().reshape(ns, -1)
+                r = r.reshape(ns, -1)
+                e = np.linalg.norm(g - r, axis=1) / np.linalg.norm(r, axis=1)
+                errs.append((float(e.max()), float(np.median(e))))
+            acc[prec] = {k: {"max": m, "median": md} for k, (m, md) in zip(("ddq", "ddq_dq", "ddq_dv", "Minv"), errs)}
+
+    # end to end through the public API: pinned host inputs -> device -> kernels -> pinned host outputs
+    e2e = None
+    if not args.no_e2e:
+        hq = [torch.from_numpy(q).pin_memory() for q, _, _ in host[:2]]
+        hv = [torch.from_numpy(v).pin_memory() for _, v, _ in host[:2]]
+        ht = [torch.from_numpy(10.0 * x).pin_memory() for _, _, x in host[:2]]
+        ho = {k: torch.empty(t.shape, dtype=t.dtype).pin_memory() for k, t in outs.items() if k != "ddq2"}
+        dq_, dv_, dt_ = (torch.empty_like(dev[0][i]) for i in range(3))
+        d = data["mixed"]
+
+        def e2e_step(k):
+            dq_.copy_(hq[k % 2], non_blocking=True)
+            dv_.copy_(hv[k % 2], non_blocking=True)
+            dt_.copy_(ht[k % 2], non_blocking=True)
+            outs["ddq"] = pg.aba(model, d, dq_, dv_, dt_)
+            a, b, c = pg.computeABADerivatives(model, d, dq_, dv_, dt_)
+            ho["ddq"].copy_(outs["ddq"], non_blocking=True)
+            ho["ddq_dq"].copy_(a, non_blocking=True)
+            ho["ddq_dv"].copy_(b, non_blocking=True)
+            ho["Minv"].copy_(c, non_blocking=True)
+
+        for k in range(args.warmup):
+            e2e_step(k)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            e2e_step(k)
+        torch.cuda.synchronize()
+        t_e2e = (time.perf_counter() - t0) / args.steps
+        if dist:
+            t = torch.tensor([t_e2e], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        h2d = B * (nq + 2 * nv) * 8
+        d2h = B * (nv + 3 * nv * nv) * 8
+        e2e = {"value": world * B / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel call (mixed): HBM bytes it must move per launch
+    peaks = {}
+    if os.path.exists(PEAKS_PATH):
+        peaks = json.load(open(PEAKS_PATH))
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or FALLBACK_HBM_GBS
+    dom = max(kt_mixed, key=kt_mixed.get)
+    alg_bytes = {
+        "aba": B * (nq + 3 * nv) * 8,  # q, v, tau in; ddq out
+        "aba_derivatives": B * (nq + 2 * nv + nv + 3 * nv * nv) * 8,  # q, v, tau in; ddq, ddq_dq, ddq_dv, Minv out
+    }[dom]
+    achieved = alg_bytes / (kt_mixed[dom] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom)
+    flops = {"aba": 26417.0, "aba_derivatives": 214728.0}  # oracle FLOP counts per evaluation (humanoid32)
+    fp64_tf = fp64_peak_tflops(torch)
+    value = world * B / (ms_mixed * 1e-3)
+    value_fp64 = world * B / (ms_fp64 * 1e-3)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64 (mixed: FP32 sweeps, FP64 Schur complement / pivots / accumulation)",
+        "data": "synthetic (seeded humanoid32 model and inputs)",
+        "config": {
+            "workload": f"humanoid32 nv=32 ABA + computeABADerivatives, batch {B} per GPU",
+            "batch": B,
+            "precision": "mixed",
+            "parallelism": f"replicas x{world} (instances shard, no exchange step)",
+            "l2": "inputs rotate over 4 copies (4 x 51 MB) and every step writes 1.6 GB of outputs (> 129 MB L2)",
+        },
+        "fp64": {"value": value_fp64, "unit": "evals/s", "ms_per_step": ms_fp64},
+        "mixed_over_fp64": value / value_fp64,
+        "accuracy_vs_fp64_oracle": acc,
+        "kernel_ms": {"mixed": kt_mixed, "fp64": kt_fp64},
+        "roofline": {
+            "bound": "hbm",
+            "kernel": f"gb_{dom} (mixed)",
+            "achieved": achieved,
+            "peak": hbm_peak,
+            "unit": "GB/s",
+            "frac": achieved / hbm_peak,
+            "peak_source": peak_src,
+            "traffic": traffic,
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "fp64_pipe": {
+                "fp64_kernel_tflops": flops[dom] * B / (kt_fp64[dom] * 1e-3) / 1e12,
+                "measured_dgemm_tflops": fp64_tf,
+                "note": "FP64 kernels: oracle-counted FLOPs / kernel time vs a measured cuBLAS DGEMM",
+            },
+        },
+        "clocks": clocks,
+        "gpu_launches": args.steps * 3,
+        "e2e": e2e,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(model, args)
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(model, args):
+    """The oracle port (FP64, OpenMP over instances) on this host's cores, bounded sample."""
+    from oracle.oracle import WORLD, OracleModel
+    from pinocchio_gb300 import sample_models as sm
+
+    om = OracleModel(model)
+    cores = os.cpu_count() or 1
+    sample = 4096
+    q, v, x = sm.random_inputs(model, sample, 3)
+    tau = 10.0 * x
+    om.aba(q[:256], v[:256], tau[:256], WORLD, nthreads=cores)
+    om.aba_derivatives(q[:256], v[:256], tau[:256], nthreads=cores)
+    reps, t = 0, 0.0
+    while reps < 3 or (t < 10.0 and reps < 50):
+        t0 = time.perf_counter()
+        om.aba(q, v, tau, WORLD, nthreads=cores)
+        om.aba_derivatives(q, v, tau, nthreads=cores)
+        t += time.perf_counter() - t0
+        reps += 1
+    return {
+        "value": sample * reps / t,
+        "unit": "evals/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{sample} configurations x {reps} repetitions of ABA(WORLD) + ABA derivatives, FP64",
+    }
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local, dist)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

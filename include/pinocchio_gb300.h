@@ -1,0 +1,141 @@
+/*
+ * pinocchio_gb300 -- C ABI of the GB300 batched rigid-body dynamics engine.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (GB_OK == 0) and never throws.  On failure gb_last_error()
+ * returns a message (thread-local).  Nothing here falls back to the CPU: a
+ * call without a usable CUDA device returns GB_ERR_CUDA.
+ *
+ * Batch layouts (argument `layout`):
+ *   GB_LAYOUT_INSTANCE -- the reference's layout: an Eigen column-major
+ *       n x batch matrix, one column per instance (instance b of a vector of
+ *       length n starts at p + b*n).  Matrix outputs are nv x nv row-major
+ *       per instance (the reference's RowMatrixXs, multibody/data.hpp:401-416),
+ *       instance b at p + b*nv*nv.
+ *   GB_LAYOUT_SOA -- structure of arrays: element k of every instance is
+ *       contiguous (element k of instance b at p + k*batch + b; matrix entry
+ *       (r, c) of instance b at p + (r*nv + c)*batch + b).
+ * All arrays passed to gb_rnea ... gb_integrate are device (or managed)
+ * memory; the *_in_parallel entry points take host memory, as the reference's
+ * rneaInParallel / abaInParallel do.
+ */
+#ifndef PINOCCHIO_GB300_H
+#define PINOCCHIO_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; mirror the reference's std::invalid_argument cases
+ * (include/pinocchio/macros.hpp:162-223) plus device failures */
+enum {
+  GB_OK = 0,
+  GB_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative batch, bad enum    */
+  GB_ERR_SIZE = 2,             /* size mismatch (PINOCCHIO_CHECK_ARGUMENT_SIZE) */
+  GB_ERR_UNSUPPORTED = 3,      /* joint type / tree shape not supported      */
+  GB_ERR_GRAVITY = 4,          /* derivatives need gravity.angular() == 0    */
+  GB_ERR_POOL = 5,             /* pool empty or num_threads > pool size      */
+  GB_ERR_CUDA = 6,             /* CUDA runtime error (message has details)   */
+  GB_ERR_NUMERIC = 7           /* a kernel saw a non-positive pivot / NaN    */
+};
+
+enum { GB_FP64 = 0, GB_MIXED = 1 };               /* arithmetic of the kernels  */
+enum { GB_LOCAL = 0, GB_WORLD = 1 };              /* reference multibody/fwd.hpp:73-81 */
+enum { GB_LAYOUT_INSTANCE = 0, GB_LAYOUT_SOA = 1 };
+enum { GB_JOINT_NONE = 0, GB_JOINT_RX = 1, GB_JOINT_RY = 2, GB_JOINT_RZ = 3, GB_JOINT_FREEFLYER = 4 };
+enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
+
+typedef struct gb_model gb_model;
+typedef struct gb_pool gb_pool;
+
+/* Flattened kinematic tree.  Joint 0 is the universe (jtype GB_JOINT_NONE).
+ * parents[i] < i and joints are in depth-first order, as ModelTpl builds them
+ * (reference multibody/model.hxx:61-170, algorithm/crba.hxx:573-595).
+ * placement: njoints x 12 (rotation row-major, then translation) -- jointPlacements.
+ * inertia:   njoints x 10 (mass, lever[3], inertia about the COM packed
+ *            [xx, xy, yy, xz, yz, zz]) -- inertias (spatial/symmetric3.hpp:46-49).
+ * armature:  nv values (may be NULL for zeros); gravity: 6 values [lin; ang]
+ *            (may be NULL for (0, 0, -9.81, 0, 0, 0), multibody/model.hxx:40). */
+typedef struct {
+  int njoints;
+  const int* parents;
+  const int* jtype;
+  const double* placement;
+  const double* inertia;
+  const double* armature;
+  int nv_armature;
+  const double* gravity;
+} gb_model_desc;
+
+/* Replaces building a ModelTpl + DataTpl (multibody/model.hpp:98-220,
+ * multibody/data.hxx:20-340): validates the tree, derives nvSubtree /
+ * parents_fromRow, and uploads the level tables to the current device. */
+int gb_model_create(const gb_model_desc* desc, gb_model** out);
+int gb_model_destroy(gb_model* model);
+int gb_model_dims(const gb_model* model, int* nq, int* nv, int* njoints);
+const char* gb_last_error(void);
+
+/* tau = rnea(model, data, q, v, a) for every instance
+ * (reference algorithm/rnea.hxx:117-161, public rnea.hxx:766). */
+int gb_rnea(const gb_model* model, int precision, int layout, long batch, const double* q, const double* v,
+            const double* a, double* tau, void* stream);
+
+/* ddq = aba(model, data, q, v, tau, convention) for every instance
+ * (reference algorithm/aba.hxx:933-948; WORLD 242-293, LOCAL 486-540). */
+int gb_aba(const gb_model* model, int precision, int convention, int layout, long batch, const double* q,
+           const double* v, const double* tau, double* ddq, void* stream);
+
+/* M = crba(model, data, q, convention) (reference algorithm/crba.hxx:602-617),
+ * upper triangle (GB_MATRIX_UPPER, the lower part is written as zero) or full
+ * symmetric.  When U and D are non-NULL the tree-sparse factorisation
+ * M = U diag(D) U^T of cholesky::decompose (algorithm/cholesky.hxx:18-62) is
+ * computed in FP64 in the same launch (U unit upper, row-major per instance). */
+int gb_crba(const gb_model* model, int precision, int convention, int matrix_mode, int layout, long batch,
+            const double* q, double* M, double* U, double* D, void* stream);
+
+/* computeRNEADerivatives(model, data, q, v, a) -> (dtau_dq, dtau_dv, M)
+ * (reference algorithm/rnea-derivatives.hxx:472-541, public 708-790).  M is
+ * dtau/da (upper or symmetric, see matrix_mode).  tau may be NULL. */
+int gb_rnea_derivatives(const gb_model* model, int precision, int matrix_mode, int layout, long batch,
+                        const double* q, const double* v, const double* a, double* dtau_dq, double* dtau_dv,
+                        double* M, double* tau, void* stream);
+
+/* computeABADerivatives(model, data, q, v, tau) -> (ddq_dq, ddq_dv, Minv)
+ * (reference algorithm/aba-derivatives.hxx:380-453, public 910-1051).  Minv
+ * is returned symmetric.  ddq may be NULL. */
+int gb_aba_derivatives(const gb_model* model, int precision, int layout, long batch, const double* q,
+                       const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
+                       double* ddq, void* stream);
+
+/* qout = integrate(model, q, v) (reference algorithm/joint-configuration.hpp:41-80;
+ * free-flyer: multibody/liegroup/special-euclidean.hpp:660-699), always FP64. */
+int gb_integrate(const gb_model* model, int layout, long batch, const double* q, const double* v, double* qout,
+                 void* stream);
+
+/* ModelPool (reference multibody/pool/model.hpp:19-165): `size` nominal
+ * per-thread slots; the GPU needs one model copy only, the size is kept for
+ * the reference's num_threads <= pool.size() check. */
+int gb_pool_create(const gb_model* model, long size, gb_pool** out);
+int gb_pool_destroy(gb_pool* pool);
+int gb_pool_size(const gb_pool* pool, long* size);
+int gb_pool_set_precision(gb_pool* pool, int precision);
+
+/* rneaInParallel(num_threads, pool, q, v, a, tau)
+ * (reference algorithm/parallel/rnea.hpp:39-84).  q: nq x batch, v, a, tau:
+ * nv x batch, column-major HOST arrays.  num_threads must be in
+ * [1, pool size]; the GPU runs the whole batch in one launch. */
+int gb_rnea_in_parallel(long num_threads, gb_pool* pool, long batch, const double* q, const double* v,
+                        const double* a, double* tau);
+
+/* abaInParallel(num_threads, pool, q, v, tau, a) (reference
+ * algorithm/parallel/aba.hpp:40-84; WORLD convention as at line 82). */
+int gb_aba_in_parallel(long num_threads, gb_pool* pool, long batch, const double* q, const double* v,
+                       const double* tau, double* a);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PINOCCHIO_GB300_H */

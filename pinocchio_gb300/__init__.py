@@ -1,0 +1,39 @@
+"""pinocchio_gb300 -- batched rigid-body dynamics on one NVIDIA GB300 (sm_103a).
+
+A drop-in for the batched dynamics path of Pinocchio: RNEA, ABA, CRBA (+ tree
+Cholesky), the analytical RNEA / ABA derivatives and the rneaInParallel /
+abaInParallel batch entry points, computed by hand-written CUDA kernels
+behind the C ABI of ``include/pinocchio_gb300.h``.
+"""
+from .model import (  # noqa: F401
+    Convention,
+    Inertia,
+    JointModelFreeFlyer,
+    JointModelRX,
+    JointModelRY,
+    JointModelRZ,
+    Model,
+    SE3,
+)
+from . import sample_models  # noqa: F401
+from .api import (  # noqa: F401
+    Data,
+    ModelPool,
+    aba,
+    abaInParallel,
+    computeABADerivatives,
+    computeRNEADerivatives,
+    crba,
+    crbaCholesky,
+    createData,
+    integrate,
+    rnea,
+    rneaInParallel,
+)
+
+
+def build(force: bool = False) -> str:
+    """Compile the CUDA library in-tree (nvcc, sm_103a)."""
+    from . import _build
+
+    return _build.build(force=force)

@@ -1,0 +1,121 @@
+"""ctypes binding of the C ABI (``include/pinocchio_gb300.h``) exported by ``libpinocchio_gb300.so``.
+
+The library is built in-tree by ``pinocchio_gb300._build``; importing this
+module never compiles anything.  ``lib()`` raises if the library is missing:
+there is no CPU fallback behind the ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+GB_OK = 0
+GB_ERR_INVALID_ARGUMENT, GB_ERR_SIZE, GB_ERR_UNSUPPORTED, GB_ERR_GRAVITY, GB_ERR_POOL, GB_ERR_CUDA, GB_ERR_NUMERIC = range(1, 8)
+GB_FP64, GB_MIXED = 0, 1
+GB_LOCAL, GB_WORLD = 0, 1
+GB_LAYOUT_INSTANCE, GB_LAYOUT_SOA = 0, 1
+GB_MATRIX_UPPER, GB_MATRIX_SYMMETRIC = 0, 1
+
+# every symbol declared in include/pinocchio_gb300.h, in declaration order
+EXPORTS = (
+    "gb_model_create",
+    "gb_model_destroy",
+    "gb_model_dims",
+    "gb_last_error",
+    "gb_rnea",
+    "gb_aba",
+    "gb_crba",
+    "gb_rnea_derivatives",
+    "gb_aba_derivatives",
+    "gb_integrate",
+    "gb_pool_create",
+    "gb_pool_destroy",
+    "gb_pool_size",
+    "gb_pool_set_precision",
+    "gb_rnea_in_parallel",
+    "gb_aba_in_parallel",
+)
+
+
+class GBError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [
+        ("njoints", C.c_int),
+        ("parents", C.c_void_p),
+        ("jtype", C.c_void_p),
+        ("placement", C.c_void_p),
+        ("inertia", C.c_void_p),
+        ("armature", C.c_void_p),
+        ("nv_armature", C.c_int),
+        ("gravity", C.c_void_p),
+    ]
+
+
+def make_desc(tables: dict) -> tuple[ModelDesc, dict]:
+    """A gb_model_desc over the arrays of ``Model.tables()`` (kept alive by the returned dict)."""
+    keep = {k: np.ascontiguousarray(v) for k, v in tables.items()}
+    d = ModelDesc()
+    d.njoints = len(keep["parents"])
+    d.parents = keep["parents"].ctypes.data
+    d.jtype = keep["jtype"].ctypes.data
+    d.placement = keep["placement"].ctypes.data
+    d.inertia = keep["inertia"].ctypes.data
+    d.armature = keep["armature"].ctypes.data if len(keep["armature"]) else None
+    d.nv_armature = len(keep["armature"])
+    d.gravity = keep["gravity"].ctypes.data
+    return d, keep
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """The loaded library; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"{path} is missing: build the CUDA library first (python -c 'import __graft_entry__ as g; g.build()')"
+            )
+        L = C.CDLL(path)
+        vp, i, l = C.c_void_p, C.c_int, C.c_long
+        L.gb_last_error.restype = C.c_char_p
+        L.gb_model_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(vp)]
+        L.gb_model_destroy.argtypes = [vp]
+        L.gb_model_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
+        L.gb_rnea.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp]
+        L.gb_aba.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp]
+        L.gb_crba.argtypes = [vp, i, i, i, i, l, vp, vp, vp, vp, vp]
+        L.gb_rnea_derivatives.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_aba_derivatives.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
+        L.gb_pool_create.argtypes = [vp, l, C.POINTER(vp)]
+        L.gb_pool_destroy.argtypes = [vp]
+        L.gb_pool_size.argtypes = [vp, C.POINTER(l)]
+        L.gb_pool_set_precision.argtypes = [vp, i]
+        L.gb_rnea_in_parallel.argtypes = [l, vp, l, vp, vp, vp, vp]
+        L.gb_aba_in_parallel.argtypes = [l, vp, l, vp, vp, vp, vp]
+        for name in EXPORTS:
+            if name != "gb_last_error":
+                getattr(L, name).restype = i
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != GB_OK:
+        raise GBError(rc, lib().gb_last_error().decode())

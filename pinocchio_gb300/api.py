@@ -1,0 +1,290 @@
+"""Python front end mirroring the reference's ``pin.*`` entry points for the batched dynamics path.
+
+Reference signatures (bindings/python/algorithm/...):
+  ``pin.rnea(model, data, q, v, a)``, ``pin.aba(model, data, q, v, tau, convention=LOCAL)``,
+  ``pin.crba(model, data, q, convention=LOCAL)`` (symmetrised, expose-crba.cpp:22),
+  ``pin.computeRNEADerivatives(model, data, q, v, a) -> (dtau_dq, dtau_dv, M)``,
+  ``pin.computeABADerivatives(model, data, q, v, tau) -> (ddq_dq, ddq_dv, Minv)``,
+  ``pin.ModelPool(model, size)``, ``pin.rneaInParallel(num_threads, pool, q, v, a)``,
+  ``pin.abaInParallel(num_threads, pool, q, v, tau)``, ``pin.integrate(model, q, v)``.
+
+Here every single-configuration function also takes a batch: a torch CUDA
+tensor of shape (batch, n) (one configuration per row, i.e. the reference's
+column-major n x batch layout) or a 1-D vector.  numpy inputs are copied to the
+device and the result is returned as numpy.  The ``*InParallel`` functions
+take numpy arrays of shape (n, batch) exactly as the reference does and go
+through the host-memory C entry points.  ``data.precision`` selects the FP64
+("fp64", default) or mixed-precision ("mixed") kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from .model import Convention, Model
+
+_PREC = {"fp64": _capi.GB_FP64, "mixed": _capi.GB_MIXED}
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class DeviceModel:
+    """The C ABI's gb_model for one Model (uploaded to the current CUDA device)."""
+
+    def __init__(self, model: Model):
+        self.desc, self._keep = _capi.make_desc(model.tables())
+        h = C.c_void_p()
+        _capi.check(_capi.lib().gb_model_create(C.byref(self.desc), C.byref(h)))
+        self.h = h
+        self.nq, self.nv, self.njoints = model.nq, model.nv, model.njoints
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.gb_model_destroy(h)
+            self.h = None
+
+
+class Data:
+    """Per-model workspace handle (the reference's DataTpl role): holds the device model."""
+
+    def __init__(self, model: Model, precision: str = "fp64"):
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.model = model
+        self.precision = precision
+        self.dev = DeviceModel(model)
+        # outputs of the last call, as the reference keeps them in data
+        self.tau = self.ddq = self.M = self.Minv = None
+        self.dtau_dq = self.dtau_dv = self.ddq_dq = self.ddq_dv = None
+
+
+def createData(model: Model, precision: str = "fp64") -> Data:
+    return Data(model, precision)
+
+
+Model.createData = lambda self, precision="fp64": Data(self, precision)  # pin: model.createData()
+
+
+def _stream_ptr():
+    return C.c_void_p(_torch().cuda.current_stream().cuda_stream)
+
+
+def _as_batch(x, n: int, name: str):
+    """(tensor (B, n) float64 contiguous on CUDA, was_numpy, was_vector)."""
+    torch = _torch()
+    was_np = isinstance(x, np.ndarray)
+    t = torch.as_tensor(x, dtype=torch.float64)
+    vec = t.dim() == 1
+    if vec:
+        t = t.unsqueeze(0)
+    if t.dim() != 2 or t.shape[1] != n:
+        raise ValueError(f"{name} must have shape (batch, {n}) or ({n},), got {tuple(t.shape)}")
+    if not t.is_cuda:
+        t = t.cuda()
+    return t.contiguous(), was_np, vec
+
+
+def _ret(t, was_np, vec):
+    if vec:
+        t = t[0]
+    return t.cpu().numpy() if was_np else t
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def rnea(model: Model, data: Data, q, v, a):
+    """tau = RNEA(q, v, a) (reference algorithm/rnea.hxx:117-161)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    at = _as_batch(a, model.nv, "a")[0]
+    B = qt.shape[0]
+    tau = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_rnea(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at), _ptr(tau), _stream_ptr()
+        )
+    )
+    data.tau = tau
+    return _ret(tau, was_np, vec)
+
+
+def aba(model: Model, data: Data, q, v, tau, convention: int = Convention.LOCAL):
+    """ddq = ABA(q, v, tau) (reference algorithm/aba.hxx:933-948)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    tt = _as_batch(tau, model.nv, "tau")[0]
+    B = qt.shape[0]
+    ddq = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_aba(
+            data.dev.h, _PREC[data.precision], int(convention), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt),
+            _ptr(ddq), _stream_ptr(),
+        )
+    )
+    data.ddq = ddq
+    return _ret(ddq, was_np, vec)
+
+
+def crba(model: Model, data: Data, q, convention: int = Convention.LOCAL, symmetric: bool = True):
+    """M(q), symmetrised as the Python binding returns it (reference bindings/python/algorithm/expose-crba.cpp:22)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    B, nv = qt.shape[0], model.nv
+    M = _torch().empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
+    mode = _capi.GB_MATRIX_SYMMETRIC if symmetric else _capi.GB_MATRIX_UPPER
+    _capi.check(
+        _capi.lib().gb_crba(
+            data.dev.h, _PREC[data.precision], int(convention), mode, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(M), None, None,
+            _stream_ptr(),
+        )
+    )
+    data.M = M
+    return _ret(M, was_np, vec)
+
+
+def crbaCholesky(model: Model, data: Data, q):
+    """(M, U, D) with M = U diag(D) U^T, the cholesky::decompose factorisation (reference algorithm/cholesky.hxx:18-62), FP64."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    B, nv = qt.shape[0], model.nv
+    torch = _torch()
+    M = torch.empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
+    U = torch.empty_like(M)
+    D = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_crba(
+            data.dev.h, _PREC[data.precision], Convention.LOCAL, _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt),
+            _ptr(M), _ptr(U), _ptr(D), _stream_ptr(),
+        )
+    )
+    return tuple(_ret(t, was_np, vec) for t in (M, U, D))
+
+
+def computeRNEADerivatives(model: Model, data: Data, q, v, a):
+    """(dtau_dq, dtau_dv, M) (reference algorithm/rnea-derivatives.hxx:472-541, M symmetrised as the binding does)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    at = _as_batch(a, model.nv, "a")[0]
+    B, nv = qt.shape[0], model.nv
+    torch = _torch()
+    dq = torch.empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
+    dv = torch.empty_like(dq)
+    M = torch.empty_like(dq)
+    tau = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_rnea_derivatives(
+            data.dev.h, _PREC[data.precision], _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at),
+            _ptr(dq), _ptr(dv), _ptr(M), _ptr(tau), _stream_ptr(),
+        )
+    )
+    data.dtau_dq, data.dtau_dv, data.M, data.tau = dq, dv, M, tau
+    return tuple(_ret(t, was_np, vec) for t in (dq, dv, M))
+
+
+def computeABADerivatives(model: Model, data: Data, q, v, tau):
+    """(ddq_dq, ddq_dv, Minv) (reference algorithm/aba-derivatives.hxx:380-453)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    tt = _as_batch(tau, model.nv, "tau")[0]
+    B, nv = qt.shape[0], model.nv
+    torch = _torch()
+    dq = torch.empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
+    dv = torch.empty_like(dq)
+    Minv = torch.empty_like(dq)
+    ddq = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_aba_derivatives(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt), _ptr(dq), _ptr(dv),
+            _ptr(Minv), _ptr(ddq), _stream_ptr(),
+        )
+    )
+    data.ddq_dq, data.ddq_dv, data.Minv, data.ddq = dq, dv, Minv, ddq
+    return tuple(_ret(t, was_np, vec) for t in (dq, dv, Minv))
+
+
+def integrate(model: Model, q, v, data: Data | None = None):
+    """q (+) v on the configuration manifold (reference algorithm/joint-configuration.hpp:41-80), FP64."""
+    data = data or Data(model)
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    out = _torch().empty_like(qt)
+    _capi.check(
+        _capi.lib().gb_integrate(data.dev.h, _capi.GB_LAYOUT_INSTANCE, qt.shape[0], _ptr(qt), _ptr(vt), _ptr(out), _stream_ptr())
+    )
+    return _ret(out, was_np, vec)
+
+
+class ModelPool:
+    """ModelPool(model, size) (reference multibody/pool/model.hpp:19-165)."""
+
+    def __init__(self, model: Model, size: int | None = None, precision: str = "fp64"):
+        import os
+
+        self.model = model
+        self._dev = DeviceModel(model)
+        size = os.cpu_count() if size is None else int(size)
+        h = C.c_void_p()
+        _capi.check(_capi.lib().gb_pool_create(self._dev.h, size, C.byref(h)))
+        self.h = h
+        self.set_precision(precision)
+
+    def set_precision(self, precision: str) -> None:
+        _capi.check(_capi.lib().gb_pool_set_precision(self.h, _PREC[precision]))
+
+    def size(self) -> int:
+        n = C.c_long()
+        _capi.check(_capi.lib().gb_pool_size(self.h, C.byref(n)))
+        return n.value
+
+    def getModel(self, index: int = 0) -> Model:
+        if not 0 <= index < self.size():
+            raise ValueError("Index greater than the size of the model vector.")
+        return self.model
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.gb_pool_destroy(h)
+            self.h = None
+
+
+def _colmajor(x, rows: int, name: str):
+    a = np.asarray(x, dtype=np.float64)
+    if a.ndim == 1:
+        a = a.reshape(rows, 1)
+    if a.ndim != 2 or a.shape[0] != rows:
+        raise ValueError(f"{name} must have {rows} rows (one column per configuration), got {a.shape}")
+    return np.asfortranarray(a)
+
+
+def _in_parallel(fn, num_threads, pool, x1, x2, x3, out, names):
+    m = pool.model
+    q = _colmajor(x1, m.nq, names[0])
+    v = _colmajor(x2, m.nv, names[1])
+    x = _colmajor(x3, m.nv, names[2])
+    B = q.shape[1]
+    if v.shape[1] != B or x.shape[1] != B:
+        raise ValueError("all inputs must have the same number of columns")
+    res = np.empty((m.nv, B), order="F") if out is None else out
+    if res.shape != (m.nv, B) or not res.flags.f_contiguous or res.dtype != np.float64:
+        raise ValueError(f"output must be a Fortran-ordered float64 array of shape ({m.nv}, {B})")
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    _capi.check(fn(int(num_threads), pool.h, B, p(q), p(v), p(x), p(res)))
+    return res
+
+
+def rneaInParallel(num_threads: int, pool: ModelPool, q, v, a, tau=None):
+    """Batch RNEA over columns (reference algorithm/parallel/rnea.hpp:39-84)."""
+    return _in_parallel(_capi.lib().gb_rnea_in_parallel, num_threads, pool, q, v, a, tau, ("q", "v", "a"))
+
+
+def abaInParallel(num_threads: int, pool: ModelPool, q, v, tau, a=None):
+    """Batch ABA over columns, WORLD convention (reference algorithm/parallel/aba.hpp:40-84)."""
+    return _in_parallel(_capi.lib().gb_aba_in_parallel, num_threads, pool, q, v, tau, a, ("q", "v", "tau"))

@@ -1,0 +1,236 @@
+// C ABI of the engine: model flattening / validation, argument checks, the
+// ModelPool-shaped batch entry points.  No entry point computes on the CPU.
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "gb_internal.h"
+
+namespace {
+thread_local std::string g_err;
+}  // namespace
+
+namespace gbi {
+
+int set_error(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+int cuda_error(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return GB_OK;
+  return set_error(GB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+int check_ptr(const void* p, const char* name) {
+  if (p == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, std::string(name) + " is NULL");
+  if (reinterpret_cast<uintptr_t>(p) % alignof(double) != 0)
+    return set_error(GB_ERR_INVALID_ARGUMENT, std::string(name) + " is not 8-byte aligned");
+  return GB_OK;
+}
+int check_common(const gb_model* m, int precision, int layout, long batch) {
+  if (m == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
+  if (precision != GB_FP64 && precision != GB_MIXED) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (layout != GB_LAYOUT_INSTANCE && layout != GB_LAYOUT_SOA)
+    return set_error(GB_ERR_INVALID_ARGUMENT, "unknown layout");
+  if (batch < 0) return set_error(GB_ERR_SIZE, "batch must be >= 0");
+  return GB_OK;
+}
+
+}  // namespace gbi
+
+using gbi::set_error;
+
+extern "C" {
+
+const char* gb_last_error(void) { return g_err.c_str(); }
+
+int gb_model_create(const gb_model_desc* desc, gb_model** out) {
+  if (out == nullptr || desc == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, "desc/out is NULL");
+  *out = nullptr;
+  if (!desc->parents || !desc->jtype || !desc->placement || !desc->inertia)
+    return set_error(GB_ERR_INVALID_ARGUMENT, "model tables must not be NULL");
+  gb_model* M = new (std::nothrow) gb_model();
+  if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "out of host memory");
+  std::string err;
+  int rc = gbm::build_model(M, desc, &err);
+  if (rc != GB_OK) {
+    delete M;
+    return set_error(rc, err);
+  }
+  cudaError_t e = cudaGetDevice(&M->device);
+  if (e == cudaSuccess) e = cudaMalloc(&M->d_blob, M->blob_bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(M->d_blob, M->blob.data(), M->blob_bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (M->d_blob) cudaFree(M->d_blob);
+    delete M;
+    return gbi::cuda_error(e, "gb_model_create");
+  }
+  *out = M;
+  return GB_OK;
+}
+
+int gb_model_destroy(gb_model* M) {
+  if (!M) return GB_OK;
+  if (M->d_blob) cudaFree(M->d_blob);
+  delete M;
+  return GB_OK;
+}
+
+int gb_model_dims(const gb_model* M, int* nq, int* nv, int* nj) {
+  if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
+  if (nq) *nq = M->nq;
+  if (nv) *nv = M->nv;
+  if (nj) *nj = M->nj;
+  return GB_OK;
+}
+
+#define GB_TRY(x)               \
+  do {                          \
+    const int rc__ = (x);       \
+    if (rc__ != GB_OK) return rc__; \
+  } while (0)
+
+int gb_rnea(const gb_model* M, int precision, int layout, long B, const double* q, const double* v, const double* a,
+            double* tau, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(a, "a"));
+  GB_TRY(gbi::check_ptr(tau, "tau"));
+  return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
+                          gbi::arr(a, layout, B, M->nv), gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
+}
+
+int gb_aba(const gb_model* M, int precision, int convention, int layout, long B, const double* q, const double* v,
+           const double* tau, double* ddq, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (convention != GB_LOCAL && convention != GB_WORLD) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown convention");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  GB_TRY(gbi::check_ptr(ddq, "ddq"));
+  return gbi::launch_aba(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
+                         gbi::arr(tau, layout, B, M->nv), gbi::arr(ddq, layout, B, M->nv), (cudaStream_t)stream);
+}
+
+int gb_crba(const gb_model* M, int precision, int convention, int matrix_mode, int layout, long B, const double* q,
+            double* Mout, double* U, double* D, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (convention != GB_LOCAL && convention != GB_WORLD) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown convention");
+  if (matrix_mode != GB_MATRIX_UPPER && matrix_mode != GB_MATRIX_SYMMETRIC)
+    return set_error(GB_ERR_INVALID_ARGUMENT, "unknown matrix mode");
+  if ((U == nullptr) != (D == nullptr)) return set_error(GB_ERR_INVALID_ARGUMENT, "U and D must both be set or both NULL");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(Mout, "M"));
+  if (U) { GB_TRY(gbi::check_ptr(U, "U")); GB_TRY(gbi::check_ptr(D, "D")); }
+  const long nn = (long)M->nv * M->nv;
+  return gbi::launch_crba(M, precision, matrix_mode == GB_MATRIX_SYMMETRIC, B, gbi::arr(q, layout, B, M->nq),
+                          gbi::arr(Mout, layout, B, nn), gbi::arr(U, layout, B, nn), gbi::arr(D, layout, B, M->nv),
+                          (cudaStream_t)stream);
+}
+
+int gb_integrate(const gb_model* M, int layout, long B, const double* q, const double* v, double* qout, void* stream) {
+  GB_TRY(gbi::check_common(M, GB_FP64, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(qout, "qout"));
+  return gbi::launch_integrate(M, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
+                               gbi::arr(qout, layout, B, M->nq), (cudaStream_t)stream);
+}
+
+// ---- ModelPool and the *InParallel entry points ------------------------------------------
+int gb_pool_create(const gb_model* M, long size, gb_pool** out) {
+  if (!M || !out) return set_error(GB_ERR_INVALID_ARGUMENT, "model/out is NULL");
+  *out = nullptr;
+  if (size <= 0) return set_error(GB_ERR_POOL, "The pool should have at least one element");
+  gb_pool* P = new (std::nothrow) gb_pool();
+  if (!P) return set_error(GB_ERR_INVALID_ARGUMENT, "out of host memory");
+  P->model = M;
+  P->size = size;
+  cudaError_t e = cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete P;
+    return gbi::cuda_error(e, "gb_pool_create");
+  }
+  *out = P;
+  return GB_OK;
+}
+int gb_pool_destroy(gb_pool* P) {
+  if (!P) return GB_OK;
+  if (P->d_buf) cudaFree(P->d_buf);
+  if (P->stream) cudaStreamDestroy(P->stream);
+  delete P;
+  return GB_OK;
+}
+int gb_pool_size(const gb_pool* P, long* size) {
+  if (!P || !size) return set_error(GB_ERR_INVALID_ARGUMENT, "pool/size is NULL");
+  *size = P->size;
+  return GB_OK;
+}
+int gb_pool_set_precision(gb_pool* P, int precision) {
+  if (!P) return set_error(GB_ERR_INVALID_ARGUMENT, "pool is NULL");
+  if (precision != GB_FP64 && precision != GB_MIXED) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown precision");
+  P->precision = precision;
+  return GB_OK;
+}
+
+static int pool_buffers(gb_pool* P, size_t bytes) {
+  if (bytes <= P->d_bytes) return GB_OK;
+  if (P->d_buf) cudaFree(P->d_buf);
+  P->d_buf = nullptr;
+  P->d_bytes = 0;
+  cudaError_t e = cudaMalloc(&P->d_buf, bytes);
+  if (e != cudaSuccess) return gbi::cuda_error(e, "pool buffers");
+  P->d_bytes = bytes;
+  return GB_OK;
+}
+
+// checks of algorithm/parallel/{rnea,aba}.hpp:53-69
+static int parallel_checks(long num_threads, gb_pool* P, long B) {
+  if (!P) return set_error(GB_ERR_INVALID_ARGUMENT, "pool is NULL");
+  if (P->size <= 0) return set_error(GB_ERR_POOL, "The pool should have at least one element");
+  if (num_threads > P->size) return set_error(GB_ERR_POOL, "The pool is too small");
+  if (num_threads < 1) return set_error(GB_ERR_POOL, "num_threads must be >= 1");
+  if (B < 0) return set_error(GB_ERR_SIZE, "batch must be >= 0");
+  return GB_OK;
+}
+
+typedef int (*launch3_fn)(const gb_model*, int, long, gbi::Arr, gbi::Arr, gbi::Arr, gbi::Arr, cudaStream_t);
+
+static int in_parallel(gb_pool* P, long B, const double* q, const double* v, const double* x, double* out,
+                       launch3_fn fn) {
+  const gb_model* M = P->model;
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(x, "x"));
+  GB_TRY(gbi::check_ptr(out, "out"));
+  const size_t nq = M->nq, nv = M->nv;
+  const size_t bytes = sizeof(double) * (size_t)B * (nq + 3 * nv);
+  GB_TRY(pool_buffers(P, bytes));
+  double* dq = P->d_buf;
+  double* dv = dq + (size_t)B * nq;
+  double* dx = dv + (size_t)B * nv;
+  double* dout = dx + (size_t)B * nv;
+  cudaStream_t st = P->stream;
+  cudaError_t e = cudaMemcpyAsync(dq, q, sizeof(double) * B * nq, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, sizeof(double) * B * nv, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, sizeof(double) * B * nv, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return gbi::cuda_error(e, "host-to-device copy");
+  GB_TRY(fn(M, P->precision, B, gbi::arr(dq, GB_LAYOUT_INSTANCE, B, nq), gbi::arr(dv, GB_LAYOUT_INSTANCE, B, nv),
+            gbi::arr(dx, GB_LAYOUT_INSTANCE, B, nv), gbi::arr(dout, GB_LAYOUT_INSTANCE, B, nv), st));
+  e = cudaMemcpyAsync(out, dout, sizeof(double) * B * nv, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return gbi::cuda_error(e, "device-to-host copy");
+}
+
+int gb_rnea_in_parallel(long num_threads, gb_pool* P, long B, const double* q, const double* v, const double* a,
+                        double* tau) {
+  GB_TRY(parallel_checks(num_threads, P, B));
+  return in_parallel(P, B, q, v, a, tau, gbi::launch_rnea);
+}
+
+int gb_aba_in_parallel(long num_threads, gb_pool* P, long B, const double* q, const double* v, const double* tau,
+                       double* a) {
+  GB_TRY(parallel_checks(num_threads, P, B));
+  return in_parallel(P, B, q, v, tau, a, gbi::launch_aba);
+}
+
+}  // extern "C"

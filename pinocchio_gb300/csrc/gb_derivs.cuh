@@ -1,0 +1,906 @@
+// Per-instance analytical derivatives (one thread = one configuration), host/device.
+//
+// computeRNEADerivatives (reference algorithm/rnea-derivatives.hxx:242-541) and
+// the sweeps of computeABADerivatives (reference algorithm/aba-derivatives.hxx:22-453).
+// Besides the per-joint arrays, these algorithms need 6 x nv column sets
+// (J, dVdq, dAdq, dAdv, dFda, dFdq, dFdv, ...) and, for ABA, the Fcrb blocks of
+// the Minv recursion: they live in a workspace laid out structure-of-arrays
+// over the batch (element e of instance b at ws[e * batch + b]), so that the
+// threads of a warp touch consecutive addresses.
+//
+// Kinematics run in a world frame as in the reference's derivative passes;
+// the forward velocity / acceleration recursions are written directly in that
+// frame (ov_i = ov_p + oMi.act(vJ)), which is the same quantity as the
+// reference's local-then-transform evaluation up to rounding.  The frame of
+// each root subtree is translated to its root joint (see world_forward).
+#pragma once
+
+#include "gb_dfloat.cuh"
+#include "gb_dyn.cuh"
+
+namespace gb {
+template <> GB_HD dfloat eps_of<dfloat>() { return dfloat(1.1920929e-07f); }
+}  // namespace gb
+
+namespace gb {
+
+template <class T> struct Ws {
+  T* p;
+  long st;
+  GB_HD T& operator[](long e) const { return p[e * st]; }
+};
+template <class T> GB_HD void ld6(const Ws<T>& w, long e, T* x) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) x[k] = w[e + k];
+}
+template <class T, class U> GB_HD void st6(const Ws<T>& w, long e, const U* x) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) w[e + k] = T(x[k]);
+}
+template <class T> GB_HD T dot6(const T* a, const T* b) {
+  T s = a[0] * b[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) s += a[k] * b[k];
+  return s;
+}
+
+// Element offsets of the per-instance workspace.
+// "K" arrays are the world-frame forward kinematics (root-origin frame): oMi,
+// ov, oa, oh, of, the link inertias oY and the joint columns J.  "C" arrays are
+// the derivative column sets and the composite quantities of the backward
+// pass.  The RNEA derivatives keep everything in region S (scalar S).  The
+// ABA derivatives keep K and the Schur / Minv data in region SS (FP64) and C
+// in region S: their first two sweeps feed the Schur complement and Minv,
+// whose conditioning (cond(M) ~ 1e3-1e4 on the humanoid) would amplify FP32
+// kinematics beyond 1e-5 in ddq_dq.
+struct DerivLayout {
+  // K (per joint / per dof)
+  int oM, ov, oa, oh, of, oY, J;
+  // C (per joint: composite inertia, its variation, force; per dof: column sets)
+  int coY, doY, cof, cJ, dVdq, dAdq, dAdv, dFda, dFdq, dFdv, dYtJ;
+  int dtq, dtv;  // nv x nv (ABA only: dtau_dq, dtau_dv feeding -Minv * dtau)
+  int nS;
+  // region SS (ABA only): K + Schur / Minv data
+  int Ia, U, UD, Dinv, u, F0, Fslot, nslot;
+  int nSS;
+};
+
+// Fills the layout for a model; `aba` selects the ABA-derivative arrangement.
+inline DerivLayout make_deriv_layout(int nj, int nv, int nslot, bool aba) {
+  DerivLayout L;
+  int oS = 0, oSS = 0;
+  auto takeS = [&](int n) { const int r = oS; oS += n; return r; };
+  auto takeSS = [&](int n) { const int r = oSS; oSS += n; return r; };
+  auto takeK = [&](int n) { return aba ? takeSS(n) : takeS(n); };
+  L.oM = takeK(12 * nj); L.ov = takeK(6 * nj); L.oa = takeK(6 * nj); L.oh = takeK(6 * nj); L.of = takeK(6 * nj);
+  L.oY = takeK(10 * nj); L.J = takeK(6 * nv);
+  L.coY = aba ? takeS(10 * nj) : L.oY;
+  L.cof = aba ? takeS(6 * nj) : L.of;
+  L.cJ = aba ? takeS(6 * nv) : L.J;
+  L.doY = takeS(36 * nj);
+  L.dVdq = takeS(6 * nv); L.dAdq = takeS(6 * nv); L.dAdv = takeS(6 * nv);
+  L.dFda = takeS(6 * nv); L.dFdq = takeS(6 * nv); L.dFdv = takeS(6 * nv); L.dYtJ = takeS(6 * nv);
+  L.dtq = aba ? takeS(nv * nv) : 0;
+  L.dtv = aba ? takeS(nv * nv) : 0;
+  L.nS = oS;
+  L.Ia = aba ? takeSS(21 * nj) : 0;
+  L.U = aba ? takeSS(6 * nv) : 0;
+  L.UD = aba ? takeSS(6 * nv) : 0;
+  L.Dinv = aba ? takeSS(6 * nv) : 0;
+  L.u = aba ? takeSS(nv) : 0;
+  L.F0 = aba ? takeSS(6 * nv) : 0;
+  L.nslot = nslot;
+  L.Fslot = aba ? takeSS(6 * nv * nslot) : 0;
+  L.nSS = oSS;
+  return L;
+}
+
+template <class S> GB_HD void ld_iner(const Ws<S>& w, long e, Iner<S>& Y) {
+  Y.m = w[e];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) Y.c[k] = w[e + 1 + k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) Y.I[k] = w[e + 4 + k];
+}
+template <class S> GB_HD void st_iner(const Ws<S>& w, long e, const Iner<S>& Y) {
+  w[e] = Y.m;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[e + 1 + k] = Y.c[k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) w[e + 4 + k] = Y.I[k];
+}
+template <class S> GB_HD void ld_x3(const Ws<S>& w, long e, X3<S>& X) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) X.R[k] = w[e + k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) X.t[k] = w[e + 9 + k];
+}
+template <class S> GB_HD void st_x3(const Ws<S>& w, long e, const X3<S>& X) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) w[e + k] = X.R[k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[e + 9 + k] = X.t[k];
+}
+// y = M x for a full row-major 6x6 stored at e
+template <class S> GB_HD void mat6_mv(const Ws<S>& w, long e, const S* x, S* y) {
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    S s = w[e + 6 * r] * x[0];
+#pragma unroll
+    for (int k = 1; k < 6; ++k) s += w[e + 6 * r + k] * x[k];
+    y[r] = s;
+  }
+}
+// y = M^T x
+template <class S> GB_HD void mat6_tmv(const Ws<S>& w, long e, const S* x, S* y) {
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    S s = w[e + c] * x[0];
+#pragma unroll
+    for (int k = 1; k < 6; ++k) s += w[e + 6 * k + c] * x[k];
+    y[c] = s;
+  }
+}
+
+// Y.variation(v) + the force-cross matrix of h (reference spatial/inertia.hpp:750-770,
+// algorithm/rnea-derivatives.hxx:358-367), written row-major into M[36].
+template <class S> GB_HD void variation_plus_fcross(const Iner<S>& Y, const S* v, const S* h, S* M) {
+  const S m = Y.m;
+  const S mvl[3] = {v[0] * m, v[1] * m, v[2] * m};
+  const S mva[3] = {v[3] * m, v[4] * m, v[5] * m};
+  const S* c = Y.c;
+  // skewSquare(u, w) = w u^T - (u.w) I
+  auto skewsq = [](const S* u, const S* w, S* C) {
+    const S d = u[0] * w[0] + u[1] * w[1] + u[2] * w[2];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) C[3 * r + cc] = w[r] * u[cc] - (r == cc ? d : S(0));
+  };
+  S B1[9], B2[9], Bla[9];
+  skewsq(mva, c, B1);
+  skewsq(c, mva, B2);
+  // -skew(mv.lin) - skewSquare(mv.ang, c) + skewSquare(c, mv.ang)
+  Bla[0] = -B1[0] + B2[0];          Bla[1] = mvl[2] - B1[1] + B2[1];  Bla[2] = -mvl[1] - B1[2] + B2[2];
+  Bla[3] = -mvl[2] - B1[3] + B2[3]; Bla[4] = -B1[4] + B2[4];          Bla[5] = mvl[0] - B1[5] + B2[5];
+  Bla[6] = mvl[1] - B1[6] + B2[6];  Bla[7] = -mvl[0] - B1[7] + B2[7]; Bla[8] = -B1[8] + B2[8];
+  S D1[9], D2[9], Daa[9];
+  skewsq(mvl, c, D1);
+  skewsq(c, mvl, D2);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Daa[k] = -D1[k] - D2[k];
+  const S x = c[0], y = c[1], z = c[2];
+  const S L[9] = {Y.I[0] + m * (y * y + z * z), Y.I[1] - m * x * y, Y.I[3] - m * x * z,
+                  Y.I[1] - m * x * y,           Y.I[2] + m * (x * x + z * z), Y.I[4] - m * y * z,
+                  Y.I[3] - m * x * z,           Y.I[4] - m * y * z, Y.I[5] + m * (x * x + y * y)};
+  const S* w = v + 3;
+  // Daa -= L skew(w) ; Daa += skew(w) L
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    Daa[3 * r + 0] -= L[3 * r + 1] * w[2] - L[3 * r + 2] * w[1];
+    Daa[3 * r + 1] -= L[3 * r + 2] * w[0] - L[3 * r + 0] * w[2];
+    Daa[3 * r + 2] -= L[3 * r + 0] * w[1] - L[3 * r + 1] * w[0];
+  }
+#pragma unroll
+  for (int cc = 0; cc < 3; ++cc) {
+    Daa[0 + cc] += w[1] * L[6 + cc] - w[2] * L[3 + cc];
+    Daa[3 + cc] += w[2] * L[0 + cc] - w[0] * L[6 + cc];
+    Daa[6 + cc] += w[0] * L[3 + cc] - w[1] * L[0 + cc];
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      M[6 * r + cc] = S(0);
+      M[6 * r + 3 + cc] = Bla[3 * r + cc];
+      M[6 * (3 + r) + cc] = Bla[3 * cc + r];
+      M[6 * (3 + r) + 3 + cc] = Daa[3 * r + cc];
+    }
+  // force-cross matrix of h: addSkew(-h.lin) on (lin,ang) and (ang,lin), addSkew(-h.ang) on (ang,ang)
+  auto add_skew = [&](const S* u, int r0, int c0) {
+    M[6 * (r0 + 0) + c0 + 1] += u[2];
+    M[6 * (r0 + 0) + c0 + 2] -= u[1];
+    M[6 * (r0 + 1) + c0 + 0] -= u[2];
+    M[6 * (r0 + 1) + c0 + 2] += u[0];
+    M[6 * (r0 + 2) + c0 + 0] += u[1];
+    M[6 * (r0 + 2) + c0 + 1] -= u[0];
+  };
+  add_skew(h, 0, 3);
+  add_skew(h, 3, 0);
+  add_skew(h + 3, 3, 3);
+}
+
+// world-frame joint columns J = oMi.act(S)
+template <class S> GB_HD void joint_columns(int jt, const X3<S>& O, S (*Jc)[6]) {
+  if (jt == JT_FF) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const S w[3] = {O.R[k], O.R[3 + k], O.R[6 + k]};
+      S tw[3];
+      cross3(O.t, w, tw);
+      Jc[k][0] = w[0]; Jc[k][1] = w[1]; Jc[k][2] = w[2]; Jc[k][3] = S(0); Jc[k][4] = S(0); Jc[k][5] = S(0);
+      Jc[3 + k][0] = tw[0]; Jc[3 + k][1] = tw[1]; Jc[3 + k][2] = tw[2];
+      Jc[3 + k][3] = w[0]; Jc[3 + k][4] = w[1]; Jc[3 + k][5] = w[2];
+    }
+  } else {
+    const int ax = jt - JT_RX;
+    const S w[3] = {O.R[ax], O.R[3 + ax], O.R[6 + ax]};
+    S tw[3];
+    cross3(O.t, w, tw);
+    Jc[0][0] = tw[0]; Jc[0][1] = tw[1]; Jc[0][2] = tw[2]; Jc[0][3] = w[0]; Jc[0][4] = w[1]; Jc[0][5] = w[2];
+  }
+}
+
+// motion cross v ^ w on raw 6-arrays
+template <class S> GB_HD void mcross(const S* v, const S* w, S* o) {
+  M6<S> a, b, c;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { a.v[k] = v[k]; b.v[k] = w[k]; }
+  cross_motion(a, b, c);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) o[k] = c.v[k];
+}
+template <class S> GB_HD void fcross(const S* v, const S* f, S* o) {
+  M6<S> a, b, c;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { a.v[k] = v[k]; b.v[k] = f[k]; }
+  cross_force(a, b, c);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) o[k] = c.v[k];
+}
+template <class S> GB_HD void imul(const Iner<S>& Y, const S* v, S* f) {
+  M6<S> a, b;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.v[k] = v[k];
+  iner_mul(Y, a, b);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) f[k] = b.v[k];
+}
+
+// The world-frame forward pass shared by both derivative algorithms: oMi, ov,
+// oa_gf, link inertia oY, oh, of, J, and for `with_derivs` the column sets
+// dVdq / dAdq / dAdv and doYcrb.  `acc` selects the RNEA form (joint
+// accelerations a given: oa_gf is the full acceleration minus gravity) or the
+// ABA form (oa_gf holds only the velocity-product bias ov_p x ov_i, and of the
+// gyroscopic force).
+template <class S>
+GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
+                         const In* acc, bool with_derivs) {
+  const S* g = ModelScalar<S>::grav(m);
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    const int nvj = jt == JT_FF ? 6 : 1;
+    X3<S> X, O;
+    joint_transform(m, i, q, X);
+    if (p > 0) {
+      X3<S> Op;
+      ld_x3(w, L.oM + 12 * p, Op);
+      compose(Op, X, O);
+    } else {
+      // The inertial frame of a root subtree is placed at its root joint: every
+      // output is a joint-space quantity, invariant to a translation of that
+      // frame, and world-frame inertias then carry no parallel-axis terms from a
+      // distant floating base (which FP32 rounding would amplify).
+      O = X;
+      O.t[0] = O.t[1] = O.t[2] = S(0);
+    }
+    st_x3(w, L.oM + 12 * i, O);
+    S Jc[6][6];
+    joint_columns(jt, O, Jc);
+    for (int k = 0; k < nvj; ++k) st6(w, L.J + 6 * (iv + k), Jc[k]);
+    // ov_i = ov_p + oMi.act(vJ)
+    S ovJ[6] = {0, 0, 0, 0, 0, 0}, ov[6], ovp[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < nvj; ++k) {
+      const S vk = S(v[iv + k]);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) ovJ[r] += Jc[k][r] * vk;
+    }
+    if (p > 0) ld6(w, L.ov + 6 * p, ovp);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) ov[r] = ovp[r] + ovJ[r];
+    st6(w, L.ov + 6 * i, ov);
+    S oa[6];
+    if (acc) {
+      // oa_gf_i = oa_gf_p + oMi.act(S a) + ov_i x oMi.act(vJ)   (oa_gf_0 = -g)
+      S oap[6], vx[6];
+      if (p > 0) ld6(w, L.oa + 6 * p, oap);
+      else
+#pragma unroll
+        for (int r = 0; r < 6; ++r) oap[r] = -g[r];
+      mcross(ov, ovJ, vx);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) oa[r] = oap[r] + vx[r];
+      for (int k = 0; k < nvj; ++k) {
+        const S ak = S((*acc)[iv + k]);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * ak;
+      }
+    } else {
+      // velocity-product bias ov_p x ov_i (aba.hxx:126-128)
+      if (p > 0) mcross(ovp, ov, oa);
+      else
+#pragma unroll
+        for (int r = 0; r < 6; ++r) oa[r] = S(0);
+    }
+    st6(w, L.oa + 6 * i, oa);
+    Iner<S> Y, oY;
+    load_inertia(m, i, Y);
+    iner_act(O, Y, oY);
+    st_iner(w, L.oY + 10 * i, oY);
+    S oh[6], of[6], t6[6];
+    imul(oY, ov, oh);
+    fcross(ov, oh, t6);
+    if (acc) {
+      imul(oY, oa, of);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) of[r] += t6[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 6; ++r) of[r] = t6[r];
+    }
+    st6(w, L.oh + 6 * i, oh);
+    st6(w, L.of + 6 * i, of);
+    if (!with_derivs) continue;
+    S oap[6];
+    if (p > 0) ld6(w, L.oa + 6 * p, oap);
+    else
+#pragma unroll
+      for (int r = 0; r < 6; ++r) oap[r] = -g[r];
+    for (int k = 0; k < nvj; ++k) {
+      S dJ[6], dAdq[6], dAdv[6], dVdq[6];
+      mcross(ov, Jc[k], dJ);
+      mcross(oap, Jc[k], dAdq);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) dAdv[r] = dJ[r];
+      if (p > 0) {
+        mcross(ovp, Jc[k], dVdq);
+        S t[6];
+        mcross(ovp, dVdq, t);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) { dAdq[r] += t[r]; dAdv[r] += dVdq[r]; }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 6; ++r) dVdq[r] = S(0);
+      }
+      st6(w, L.dVdq + 6 * (iv + k), dVdq);
+      st6(w, L.dAdq + 6 * (iv + k), dAdq);
+      st6(w, L.dAdv + 6 * (iv + k), dAdv);
+    }
+    S dY[36];
+    variation_plus_fcross(oY, ov, oh, dY);
+#pragma unroll
+    for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// computeRNEADerivatives (rnea-derivatives.hxx:472-541).  Writes dtau_dq, dtau_dv, M (=dtau/da,
+// upper or symmetric) and optionally tau; every other matrix entry is written as zero.
+// ------------------------------------------------------------------------------------------
+template <class S>
+GB_HD void rnea_derivs_one(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
+                           const In& a, const Out& dq, const Out& dv, const Out& Mo, const Out* tau, bool symmetric) {
+  const int nv = m.nv;
+  world_forward(m, L, w, q, v, &a, true);
+  for (int r = 0; r < nv * nv; ++r) { dq[r] = 0.0; dv[r] = 0.0; Mo[r] = 0.0; }
+  const S eps = eps_of<S>();
+  for (int i = m.nj - 1; i > 0; --i) {  // ComputeRNEADerivativesBackwardStep (hxx:361-460)
+    const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
+    Iner<S> oY;
+    ld_iner(w, L.oY + 10 * i, oY);
+    S of[6];
+    ld6(w, L.of + 6 * i, of);
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      S Jc[6], dFda[6], t[6], dFdq[6], dFdv[6], dYtJ[6], x[6];
+      ld6(w, L.J + 6 * c, Jc);
+      if (tau) (*tau)[c] = double(dot6(Jc, of) + m.arm_d[c] * 0.0);
+      imul(oY, Jc, dFda);
+      st6(w, L.dFda + 6 * c, dFda);
+      ld6(w, L.dAdq + 6 * c, x);
+      imul(oY, x, dFdq);
+      if (p > 0) {
+        ld6(w, L.dVdq + 6 * c, x);
+        mat6_mv(w, L.doY + 36 * i, x, t);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) dFdq[r] = t[r] + dFdq[r];
+      }
+      st6(w, L.dFdq + 6 * c, dFdq);
+      mat6_tmv(w, L.doY + 36 * i, Jc, dYtJ);
+      st6(w, L.dYtJ + 6 * c, dYtJ);
+      ld6(w, L.dAdv + 6 * c, x);
+      imul(oY, x, dFdv);
+      mat6_mv(w, L.doY + 36 * i, Jc, t);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) dFdv[r] = t[r] + dFdv[r];
+      st6(w, L.dFdv + 6 * c, dFdv);
+    }
+    // row blocks: M(i, subtree), dtau_dq(i, subtree), dtau_dv(i, subtree)
+    for (int r = 0; r < nvj; ++r) {
+      S Jr[6];
+      ld6(w, L.J + 6 * (iv + r), Jr);
+      for (int c = iv; c < iv + nst; ++c) {
+        S x[6];
+        ld6(w, L.dFda + 6 * c, x);
+        const S mval = dot6(Jr, x);
+        Mo[(iv + r) * nv + c] = double(mval);
+        if (symmetric) Mo[c * nv + iv + r] = double(mval);
+        ld6(w, L.dFdq + 6 * c, x);
+        dq[(iv + r) * nv + c] = double(dot6(Jr, x));
+        ld6(w, L.dFdv + 6 * c, x);
+        dv[(iv + r) * nv + c] = double(dot6(Jr, x));
+      }
+    }
+    // column blocks below the joint: dtau_d*(subtree+, i)
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      S dAdq[6], dVdq[6], dAdv[6], Jc[6];
+      ld6(w, L.dAdq + 6 * c, dAdq);
+      ld6(w, L.dVdq + 6 * c, dVdq);
+      ld6(w, L.dAdv + 6 * c, dAdv);
+      ld6(w, L.J + 6 * c, Jc);
+      for (int r = iv + nvj; r < iv + nst; ++r) {
+        S fa[6], yt[6];
+        ld6(w, L.dFda + 6 * r, fa);
+        ld6(w, L.dYtJ + 6 * r, yt);
+        dq[r * nv + c] = double(dot6(fa, dAdq) + dot6(yt, dVdq));
+        dv[r * nv + c] = double(dot6(fa, dAdv) + dot6(yt, Jc));
+      }
+      // dFdq += J x* of (kept for the ancestors' rows)
+      S x[6], t[6];
+      ld6(w, L.dFdq + 6 * c, x);
+      fcross(Jc, of, t);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) x[r] += t[r];
+      st6(w, L.dFdq + 6 * c, x);
+    }
+    if (p > 0) {
+      Iner<S> oYp;
+      ld_iner(w, L.oY + 10 * p, oYp);
+      iner_add(oYp, oY, eps);
+      st_iner(w, L.oY + 10 * p, oYp);
+      for (int k = 0; k < 36; ++k) w[L.doY + 36 * p + k] += w[L.doY + 36 * i + k];
+      S ofp[6];
+      ld6(w, L.of + 6 * p, ofp);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) ofp[r] += of[r];
+      st6(w, L.of + 6 * p, ofp);
+    }
+  }
+  for (int k = 0; k < nv; ++k) {
+    Mo[k * nv + k] += m.arm_d[k];
+    if (tau) (*tau)[k] += m.arm_d[k] * a[k];
+  }
+}
+
+// ---- translations of the reference point (world orientation kept) --------------------------
+// motion about P -> about P + d: (v - d x w, w)
+template <class S> GB_HD void shift_motion(const S* m, const S* d, S* o) {
+  S dxw[3];
+  cross3(d, m + 3, dxw);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { o[k] = m[k] - dxw[k]; o[3 + k] = m[3 + k]; }
+}
+// force about C -> about C - r (i.e. r = C - P for the new point P): (f, n + r x f)
+template <class S> GB_HD void shift_force(const S* f, const S* r, S* o) {
+  S rxf[3];
+  cross3(r, f, rxf);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { o[k] = f[k]; o[3 + k] = f[3 + k] + rxf[k]; }
+}
+// force about the origin -> about point t: (f, n - t x f)
+template <class S> GB_HD void shift_force_from_origin(const S* f, const S* t, S* o) {
+  S txf[3];
+  cross3(t, f, txf);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { o[k] = f[k]; o[3 + k] = f[3 + k] - txf[k]; }
+}
+// a motion->force operator M (row-major 6x6) about point C re-expressed about
+// P with r = C - P:  [[A, B - A R], [C + R A, D + R B - C R - R A R]], R = [r]x
+template <class S> GB_HD void shift_operator(const S* M, const S* r, S* O) {
+  S A[9], B[9], C[9], D[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      A[3 * a + b] = M[6 * a + b]; B[3 * a + b] = M[6 * a + 3 + b];
+      C[3 * a + b] = M[6 * (3 + a) + b]; D[3 * a + b] = M[6 * (3 + a) + 3 + b];
+    }
+  // X R for a 3x3 X: (X R)(a, b) = sum_k X(a,k) R(k,b), R = [[0,-r2,r1],[r2,0,-r0],[-r1,r0,0]]
+  auto mulR = [&](const S* X, S* Y) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      Y[3 * a + 0] = X[3 * a + 1] * r[2] - X[3 * a + 2] * r[1];
+      Y[3 * a + 1] = X[3 * a + 2] * r[0] - X[3 * a + 0] * r[2];
+      Y[3 * a + 2] = X[3 * a + 0] * r[1] - X[3 * a + 1] * r[0];
+    }
+  };
+  // R X: rows r x (columns of X)
+  auto Rmul = [&](const S* X, S* Y) {
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      Y[0 + b] = r[1] * X[6 + b] - r[2] * X[3 + b];
+      Y[3 + b] = r[2] * X[0 + b] - r[0] * X[6 + b];
+      Y[6 + b] = r[0] * X[3 + b] - r[1] * X[0 + b];
+    }
+  };
+  S AR[9], RA[9], RB[9], CR[9], RAR[9];
+  mulR(A, AR);
+  Rmul(A, RA);
+  Rmul(B, RB);
+  mulR(C, CR);
+  mulR(RA, RAR);
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const int k = 3 * a + b;
+      O[6 * a + b] = A[k];
+      O[6 * a + 3 + b] = B[k] - AR[k];
+      O[6 * (3 + a) + b] = C[k] + RA[k];
+      O[6 * (3 + a) + 3 + b] = D[k] + RB[k] - CR[k] - RAR[k];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// The four sweeps of computeABADerivatives (aba-derivatives.hxx:380-449): writes ddq,
+// the symmetric Minv, and dtau_dq / dtau_dv (at (q, v, ddq)) into the workspace;
+// the products -Minv dtau_dq, -Minv dtau_dv are a separate batched kernel.
+// `slot[i]` is the Fcrb slot of joint i (a last child reuses its parent's slot).
+//
+// Passes 1-2 (kinematics, Schur complement, Minv) and the velocity /
+// acceleration recursion of pass 3 run in SS.  The column sets of pass 3 and
+// the backward pass 4 run in S in floating origins: every quantity of joint i
+// is expressed about joint i's position t_i (world orientation), so that no
+// FP32 value carries the lever arm of a distant origin; contributions move
+// between joints by translation (shift_motion / shift_force / shift_operator).
+// ------------------------------------------------------------------------------------------
+template <class S, class SS>
+GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
+                             const Ws<SS>& z, const In& q, const In& v, const In& tau, const Out& Minv,
+                             const Out* ddq_out) {
+  const int nv = m.nv;
+  const double* arm = m.arm_d;
+  const S eps = eps_of<S>();
+  // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), in SS
+  world_forward<SS>(m, L, z, q, v, nullptr, false);
+  for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix()
+    Iner<SS> oY;
+    ld_iner(z, L.oY + 10 * i, oY);
+    Sym6<SS> I6;
+    iner_to_sym6(oY, I6);
+    for (int k = 0; k < 6; ++k) { z[L.Ia + 21 * i + k] = I6.A[k]; z[L.Ia + 21 * i + 15 + k] = I6.D[k]; }
+    for (int k = 0; k < 9; ++k) z[L.Ia + 21 * i + 6 + k] = I6.B[k];
+  }
+  for (int r = 0; r < nv * nv; ++r) Minv[r] = 0.0;
+  for (int k = 0; k < nv; ++k) z[L.u + k] = SS(tau[k]);
+  for (int k = 0; k < 6 * nv; ++k) z[L.F0 + k] = SS(0);
+  auto ld_sym = [&](int i, Sym6<SS>& I6) {
+    for (int k = 0; k < 6; ++k) { I6.A[k] = z[L.Ia + 21 * i + k]; I6.D[k] = z[L.Ia + 21 * i + 15 + k]; }
+    for (int k = 0; k < 9; ++k) I6.B[k] = z[L.Ia + 21 * i + 6 + k];
+  };
+  auto st_sym = [&](int i, const Sym6<SS>& I6) {
+    for (int k = 0; k < 6; ++k) { z[L.Ia + 21 * i + k] = I6.A[k]; z[L.Ia + 21 * i + 15 + k] = I6.D[k]; }
+    for (int k = 0; k < 9; ++k) z[L.Ia + 21 * i + 6 + k] = I6.B[k];
+  };
+  // ---- pass 2: ComputeABADerivativesBackwardStep1 (hxx:87-171), in SS
+  for (int i = m.nj - 1; i > 0; --i) {
+    const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
+    Sym6<SS> Ia;
+    ld_sym(i, Ia);
+    SS of[6];
+    ld6(z, L.of + 6 * i, of);
+    SS Jc[6][6], U[6][6];  // per joint dof k: J column, U column
+    for (int k = 0; k < nvj; ++k) {
+      ld6(z, L.J + 6 * (iv + k), Jc[k]);
+      z[L.u + iv + k] -= dot6(Jc[k], of);
+      sym6_mv(Ia, Jc[k], U[k]);
+    }
+    SS StU[36], Dinv[36];
+    for (int r = 0; r < nvj; ++r)
+      for (int c = 0; c < nvj; ++c) StU[r * nvj + c] = dot6(Jc[r], U[c]);
+    for (int k = 0; k < nvj; ++k) StU[k * nvj + k] += SS(arm[iv + k]);
+    if (nvj == 6) llt_inverse<SS, 6>(StU, Dinv);
+    else Dinv[0] = SS(1) / StU[0];
+    SS UD[6][6];  // UDinv columns
+    for (int k = 0; k < nvj; ++k)
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        SS s = U[0][r] * Dinv[k];
+        for (int j = 1; j < nvj; ++j) s += U[j][r] * Dinv[j * nvj + k];
+        UD[k][r] = s;
+      }
+    for (int k = 0; k < nvj; ++k) {
+      st6(z, L.U + 6 * (iv + k), U[k]);
+      st6(z, L.UD + 6 * (iv + k), UD[k]);
+      for (int c = 0; c < nvj; ++c) z[L.Dinv + 6 * (iv + k) + c] = Dinv[k * nvj + c];
+    }
+    for (int r = 0; r < nvj; ++r)
+      for (int c = 0; c < nvj; ++c) Minv[(iv + r) * nv + iv + c] = double(Dinv[r * nvj + c]);
+    const int nch = nst - nvj;
+    if (nch > 0) {
+      SS SD[6][6];  // SDinv columns = J Dinv
+      for (int k = 0; k < nvj; ++k)
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          SS s = Jc[0][r] * Dinv[k];
+          for (int j = 1; j < nvj; ++j) s += Jc[j][r] * Dinv[j * nvj + k];
+          SD[k][r] = s;
+        }
+      for (int c = iv + nvj; c < iv + nst; ++c) {
+        SS F[6];
+        ld6(z, L.F0 + 6 * c, F);
+        for (int r = 0; r < nvj; ++r) Minv[(iv + r) * nv + c] = double(-dot6(SD[r], F));
+      }
+    }
+    if (!(nch > 0 && p == 0)) {  // leaf: F = U Minv_rows; inner joint with a parent: F += U Minv_rows
+      for (int c = iv; c < iv + nst; ++c) {
+        SS F[6] = {0, 0, 0, 0, 0, 0};
+        if (nch > 0) ld6(z, L.F0 + 6 * c, F);
+        for (int k = 0; k < nvj; ++k) {
+          const SS mk = SS(Minv[(iv + k) * nv + c]);
+#pragma unroll
+          for (int r = 0; r < 6; ++r) F[r] += U[k][r] * mk;
+        }
+        st6(z, L.F0 + 6 * c, F);
+      }
+    }
+    if (p > 0) {
+      // Ia -= UDinv U^T ; pa = of + Ia oa_gf + UDinv u ; accumulate into the parent
+      for (int k = 0; k < nvj; ++k) sym6_rank1_sub(Ia, U[k], UD[k]);
+      SS oa[6], pa[6];
+      ld6(z, L.oa + 6 * i, oa);
+      sym6_mv(Ia, oa, pa);
+      for (int k = 0; k < nvj; ++k) {
+        const SS uk = z[L.u + iv + k];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) pa[r] += UD[k][r] * uk;
+      }
+      SS ofp[6];
+      ld6(z, L.of + 6 * p, ofp);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) ofp[r] += of[r] + pa[r];
+      st6(z, L.of + 6 * p, ofp);
+      Sym6<SS> Ip;
+      ld_sym(p, Ip);
+      sym6_add(Ip, Ia);
+      st_sym(p, Ip);
+    }
+  }
+  // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
+  // velocity / acceleration recursion runs in SS in floating origins and
+  // replaces ov / oa in K; the column sets, link inertia, momentum, force and
+  // inertia variation of joint i are written to C in S about t_i.
+  const SS* gs = ModelScalar<SS>::grav(m);
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], iv = m.idx_v[i];
+    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
+    SS ti[3];
+    for (int k = 0; k < 3; ++k) ti[k] = z[L.oM + 12 * i + 9 + k];
+    SS ovp[6] = {0, 0, 0, 0, 0, 0}, oap[6];
+    if (p > 0) {
+      SS r[3], x[6];
+      for (int k = 0; k < 3; ++k) r[k] = ti[k] - z[L.oM + 12 * p + 9 + k];
+      ld6(z, L.ov + 6 * p, x);
+      shift_motion(x, r, ovp);
+      ld6(z, L.oa + 6 * p, x);
+      shift_motion(x, r, oap);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) oap[k] = -gs[k];  // uniform field: invariant to the shift
+    }
+    // joint columns about t_i: a revolute axis passes through t_i; the root free-flyer sits at the origin
+    SS Jo[6][6], Jc[6][6];
+    for (int k = 0; k < nvj; ++k) {
+      ld6(z, L.J + 6 * (iv + k), Jo[k]);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) Jc[k][r] = Jo[k][r];
+    }
+    if (nvj == 1) Jc[0][0] = Jc[0][1] = Jc[0][2] = SS(0);
+    SS ov[6], oa[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) ov[k] = ovp[k];
+    for (int k = 0; k < nvj; ++k) {
+      const SS vk = SS(v[iv + k]);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) ov[r] += Jc[k][r] * vk;
+    }
+    mcross(ovp, ov, oa);  // velocity-product bias (aba.hxx:126-128) + the parent's acceleration
+#pragma unroll
+    for (int k = 0; k < 6; ++k) oa[k] += oap[k];
+    SS dd[6];
+    for (int k = 0; k < nvj; ++k) {
+      SS s = SS(0);
+      for (int c = 0; c < nvj; ++c) s += z[L.Dinv + 6 * (iv + k) + c] * z[L.u + iv + c];
+      SS ud[6], udi[6];
+      ld6(z, L.UD + 6 * (iv + k), ud);
+      shift_force_from_origin(ud, ti, udi);  // UDinv (a force about the root origin) about t_i
+      dd[k] = s - dot6(udi, oa);
+      if (ddq_out) (*ddq_out)[iv + k] = double(dd[k]);
+    }
+    for (int k = 0; k < nvj; ++k)
+#pragma unroll
+      for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * dd[k];
+    st6(z, L.ov + 6 * i, ov);
+    st6(z, L.oa + 6 * i, oa);
+    // Minv rows of the joint: -= UDinv^T Fcrb[parent]; Fcrb[i] = J Minv_rows (+ Fcrb[parent])
+    // (root-origin frame, SS)
+    const long Fi = L.Fslot + 6L * nv * slot[i];
+    const long Fp = p > 0 ? L.Fslot + 6L * nv * slot[p] : -1;
+    for (int c = iv; c < nv; ++c) {
+      SS Fpc[6];
+      if (p > 0) {
+        ld6(z, Fp + 6 * c, Fpc);
+        for (int k = 0; k < nvj; ++k) {
+          SS ud[6];
+          ld6(z, L.UD + 6 * (iv + k), ud);
+          Minv[(iv + k) * nv + c] -= double(dot6(ud, Fpc));
+        }
+      }
+      SS Fn[6];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) Fn[r] = p > 0 ? Fpc[r] : SS(0);
+      for (int k = 0; k < nvj; ++k) {
+        const SS mk = SS(Minv[(iv + k) * nv + c]);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) Fn[r] += Jo[k][r] * mk;
+      }
+      st6(z, Fi + 6 * c, Fn);
+    }
+    // C quantities about t_i in S
+    S ovs[6], ovps[6], oaps[6], oas[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { ovs[k] = S(ov[k]); ovps[k] = S(ovp[k]); oaps[k] = S(oap[k]); oas[k] = S(oa[k]); }
+    for (int k = 0; k < nvj; ++k) {
+      S J[6], dJ[6], dAdq[6], dAdv[6], dVdq[6];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) J[r] = S(Jc[k][r]);
+      mcross(ovs, J, dJ);
+      mcross(oaps, J, dAdq);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) dAdv[r] = dJ[r];
+      if (p > 0) {
+        mcross(ovps, J, dVdq);
+        S t[6];
+        mcross(ovps, dVdq, t);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) { dAdq[r] += t[r]; dAdv[r] += dVdq[r]; }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 6; ++r) dVdq[r] = S(0);
+      }
+      st6(w, L.cJ + 6 * (iv + k), J);
+      st6(w, L.dVdq + 6 * (iv + k), dVdq);
+      st6(w, L.dAdq + 6 * (iv + k), dAdq);
+      st6(w, L.dAdv + 6 * (iv + k), dAdv);
+    }
+    Iner<SS> oYd;
+    ld_iner(z, L.oY + 10 * i, oYd);
+    Iner<S> oY;
+    oY.m = S(oYd.m);
+    for (int k = 0; k < 3; ++k) oY.c[k] = S(oYd.c[k] - ti[k]);
+    for (int k = 0; k < 6; ++k) oY.I[k] = S(oYd.I[k]);
+    st_iner(w, L.coY + 10 * i, oY);
+    S oh[6], of[6], t6[6];
+    imul(oY, ovs, oh);
+    imul(oY, oas, of);
+    fcross(ovs, oh, t6);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) of[k] += t6[k];
+    st6(w, L.cof + 6 * i, of);
+    S dY[36];
+    variation_plus_fcross(oY, ovs, oh, dY);
+#pragma unroll
+    for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
+  }
+  // ---- pass 4: ComputeABADerivativesBackwardStep2 (hxx:273-368), in S, floating
+  // origins: a joint's composite oY / doY / of are about its own position; a
+  // child adds its contributions moved to the parent's position.
+  for (int k = 0; k < nv * nv; ++k) { w[L.dtq + k] = S(0); w[L.dtv + k] = S(0); }
+  auto offset = [&](int a, int b, S* d) {  // t_a - t_b, formed in SS
+    for (int k = 0; k < 3; ++k) d[k] = S(z[L.oM + 12 * a + 9 + k] - z[L.oM + 12 * b + 9 + k]);
+  };
+  for (int i = m.nj - 1; i > 0; --i) {
+    const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
+    Iner<S> oY;
+    ld_iner(w, L.coY + 10 * i, oY);
+    S of[6];
+    ld6(w, L.cof + 6 * i, of);
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      S Jc[6], x[6], t[6], dFdv[6], dFdq[6], dFda[6];
+      ld6(w, L.cJ + 6 * c, Jc);
+      ld6(w, L.dAdv + 6 * c, x);
+      imul(oY, x, dFdv);
+      mat6_mv(w, L.doY + 36 * i, Jc, t);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) dFdv[r] += t[r];
+      st6(w, L.dFdv + 6 * c, dFdv);
+      ld6(w, L.dAdq + 6 * c, x);
+      imul(oY, x, dFdq);
+      if (p > 0) {
+        ld6(w, L.dVdq + 6 * c, x);
+        mat6_mv(w, L.doY + 36 * i, x, t);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) dFdq[r] += t[r];
+      }
+      st6(w, L.dFdq + 6 * c, dFdq);
+      imul(oY, Jc, dFda);
+      st6(w, L.dFda + 6 * c, dFda);
+    }
+    // row block: dtau(i, subtree) = J_i^T dF_c, with dF_c moved from its joint's position to t_i
+    for (int r = 0; r < nvj; ++r) {
+      S Jr[6];
+      ld6(w, L.cJ + 6 * (iv + r), Jr);
+      for (int c = iv; c < iv + nst; ++c) {
+        S d[3], x[6], y[6];
+        offset(m.dof_joint[c], i, d);
+        ld6(w, L.dFdv + 6 * c, x);
+        shift_force(x, d, y);
+        w[L.dtv + (iv + r) * nv + c] = dot6(Jr, y);
+        ld6(w, L.dFdq + 6 * c, x);
+        shift_force(x, d, y);
+        w[L.dtq + (iv + r) * nv + c] = dot6(Jr, y);
+      }
+    }
+    for (int k = 0; k < nvj; ++k) {
+      const int c = iv + k;
+      S Jc[6], x[6], t[6];
+      ld6(w, L.cJ + 6 * c, Jc);
+      ld6(w, L.dFdq + 6 * c, x);
+      fcross(Jc, of, t);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) x[r] += t[r];
+      st6(w, L.dFdq + 6 * c, x);
+    }
+    if (p > 0) {
+      // ancestor columns: motion quantities of ancestor j moved from t_j to t_i
+      for (int r = 0; r < nvj; ++r) {
+        S fa[6], Jr[6], StdY[6];
+        ld6(w, L.dFda + 6 * (iv + r), fa);
+        ld6(w, L.cJ + 6 * (iv + r), Jr);
+        mat6_tmv(w, L.doY + 36 * i, Jr, StdY);
+        for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j]) {
+          S d[3], x[6], y[6], xs[6], ys[6];
+          offset(i, m.dof_joint[j], d);
+          ld6(w, L.dAdq + 6 * j, x);
+          ld6(w, L.dVdq + 6 * j, y);
+          shift_motion(x, d, xs);
+          shift_motion(y, d, ys);
+          w[L.dtq + (iv + r) * nv + j] = dot6(fa, xs) + dot6(StdY, ys);
+          ld6(w, L.dAdv + 6 * j, x);
+          ld6(w, L.cJ + 6 * j, y);
+          shift_motion(x, d, xs);
+          shift_motion(y, d, ys);
+          w[L.dtv + (iv + r) * nv + j] = dot6(fa, xs) + dot6(StdY, ys);
+        }
+      }
+      // accumulate into the parent, moved from t_i to t_p
+      S rr[3];
+      offset(i, p, rr);
+      Iner<S> oYp, oYs = oY;
+      ld_iner(w, L.coY + 10 * p, oYp);
+      for (int k = 0; k < 3; ++k) oYs.c[k] += rr[k];
+      iner_add(oYp, oYs, eps);
+      st_iner(w, L.coY + 10 * p, oYp);
+      S Mi[36], Ms[36];
+      for (int k = 0; k < 36; ++k) Mi[k] = w[L.doY + 36 * i + k];
+      shift_operator(Mi, rr, Ms);
+      for (int k = 0; k < 36; ++k) w[L.doY + 36 * p + k] += Ms[k];
+      S ofs[6], ofp[6];
+      shift_force(of, rr, ofs);
+      ld6(w, L.cof + 6 * p, ofp);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) ofp[r] += ofs[r];
+      st6(w, L.cof + 6 * p, ofp);
+    }
+  }
+  // symmetrise Minv (hxx:448-449)
+  for (int r = 1; r < nv; ++r)
+    for (int c = 0; c < r; ++c) Minv[r * nv + c] = Minv[c * nv + r];
+}
+
+}  // namespace gb

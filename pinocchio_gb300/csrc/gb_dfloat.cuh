@@ -1,0 +1,82 @@
+// Double-float scalar: an unevaluated sum hi + lo of two FP32 values, with
+// error-free transformations (Knuth's TwoSum; TwoProduct through a fused
+// multiply-add), giving about 48 significand bits from FP32 instructions.
+// On GB300 FP32 issues at many times the FP64 rate, so the FP32 derivative
+// passes use it where plain FP32 rounding, amplified by the conditioning of
+// the mass matrix, would exceed the 1e-5 mixed-precision bar.
+//
+// The operations follow Dekker (1971) and Knuth (TAOCP vol. 2, 4.2.2);
+// division is one Newton-style correction of the FP32 quotient.
+#pragma once
+
+#include "gb_spatial.cuh"
+
+namespace gb {
+
+GB_HD float gb_fmaf(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+
+struct dfloat {
+  float hi, lo;
+  GB_HD dfloat() : hi(0.f), lo(0.f) {}
+  GB_HD dfloat(float x) : hi(x), lo(0.f) {}  // NOLINT: implicit from float / literals
+  GB_HD dfloat(int x) : hi(float(x)), lo(0.f) {}  // NOLINT
+  GB_HD explicit dfloat(double x) : hi(float(x)), lo(float(x - double(float(x)))) {}
+  GB_HD dfloat(float h, float l, int) : hi(h), lo(l) {}
+  GB_HD explicit operator float() const { return hi + lo; }
+  GB_HD explicit operator double() const { return double(hi) + double(lo); }
+};
+
+// s + e = a + b exactly (Knuth TwoSum)
+GB_HD void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// s + e = a + b exactly, |a| >= |b| (Dekker FastTwoSum)
+GB_HD void fast_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  e = b - (s - a);
+}
+
+GB_HD dfloat operator+(dfloat a, dfloat b) {
+  float s, e, t, f;
+  two_sum(a.hi, b.hi, s, e);
+  two_sum(a.lo, b.lo, t, f);
+  e += t;
+  fast_two_sum(s, e, s, e);
+  e += f;
+  fast_two_sum(s, e, s, e);
+  return dfloat(s, e, 0);
+}
+GB_HD dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo, 0); }
+GB_HD dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+GB_HD dfloat operator*(dfloat a, dfloat b) {
+  const float p = a.hi * b.hi;
+  float e = gb_fmaf(a.hi, b.hi, -p);
+  e = gb_fmaf(a.hi, b.lo, e);
+  e = gb_fmaf(a.lo, b.hi, e);
+  float s;
+  fast_two_sum(p, e, s, e);
+  return dfloat(s, e, 0);
+}
+GB_HD dfloat operator/(dfloat a, dfloat b) {
+  const float q1 = a.hi / b.hi;
+  const dfloat r = a - b * dfloat(q1);
+  const float q2 = r.hi / b.hi;
+  float s, e;
+  fast_two_sum(q1, q2, s, e);
+  return dfloat(s, e, 0);
+}
+GB_HD dfloat& operator+=(dfloat& a, dfloat b) { a = a + b; return a; }
+GB_HD dfloat& operator-=(dfloat& a, dfloat b) { a = a - b; return a; }
+GB_HD dfloat& operator*=(dfloat& a, dfloat b) { a = a * b; return a; }
+GB_HD bool operator>(dfloat a, dfloat b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+GB_HD bool operator<(dfloat a, dfloat b) { return b > a; }
+
+}  // namespace gb

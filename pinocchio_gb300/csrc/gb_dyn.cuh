@@ -1,0 +1,424 @@
+// Per-instance dynamics sweeps (one thread = one configuration), host/device.
+//
+// Template parameters:
+//   S   -- scalar of the kinematic sweeps and spatial transforms
+//          (double for the FP64 kernels, float for the mixed kernels);
+//   SS  -- scalar of the articulated-inertia Schur complement
+//          Ia - U D^-1 U^T, its D^-1 pivots and its accumulation into the
+//          parent (double in both precisions);
+//   CAP -- compile-time capacity (>= njoints and >= nv) of the per-joint
+//          local arrays.
+//
+// The algorithms are the reference's (file:line on each function) written
+// for the GPU: revolute joints use their axis-aligned motion subspace
+// directly (U is a column of Ia, D a diagonal entry), articulated inertias
+// are kept as block-symmetric 6x6 (21 entries), and the free-flyer is only
+// allowed as the root joint (parent = universe), which every supported
+// model satisfies and the host checks.
+#pragma once
+
+#include "gb_model.cuh"
+
+namespace gb {
+
+GB_HD void ssincos(double x, double* s, double* c) { sincos(x, s, c); }
+GB_HD void ssincos(float x, float* s, float* c) { sincosf(x, s, c); }
+
+// strided view of one instance's vector / matrix in the batch arrays
+struct In {
+  const double* p;
+  long es;
+  GB_HD double operator[](int k) const { return p[(long)k * es]; }
+};
+struct Out {
+  double* p;
+  long es;
+  GB_HD double& operator[](int k) const { return p[(long)k * es]; }
+};
+
+template <class S> GB_HD S eps_of();
+template <> GB_HD double eps_of<double>() { return 2.220446049250313e-16; }
+template <> GB_HD float eps_of<float>() { return 1.1920929e-07f; }
+
+// liMi = jointPlacements[i] * M_joint(q)   (rnea.hxx:60, joint calc:
+// revolute joint-revolute.hpp:811-821, free-flyer joint-free-flyer.hpp:333-375)
+template <class S> GB_HD void joint_transform(const MView& m, int i, const In& q, X3<S>& X) {
+  const S* P = ModelScalar<S>::place(m, i);
+  const int jt = m.jtype[i], iq = m.idx_q[i];
+  if (jt == JT_FF) {
+    X3<S> Pl, J;
+    load_placement(m, i, Pl);
+    quat_matrix(S(q[iq + 3]), S(q[iq + 4]), S(q[iq + 5]), S(q[iq + 6]), J.R);
+    J.t[0] = S(q[iq]); J.t[1] = S(q[iq + 1]); J.t[2] = S(q[iq + 2]);
+    compose(Pl, J, X);
+  } else {
+    S s, c;
+    ssincos(S(q[iq]), &s, &c);
+    compose_axis(P, P + 9, jt - JT_RX, c, s, X);
+  }
+}
+// S * x for the joint (x = one value per dof)
+template <class S> GB_HD void joint_motion(int jt, const In& x, int iv, M6<S>& o) {
+  if (jt == JT_FF) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o.v[k] = S(x[iv + k]);
+  } else {
+    zero(o);
+    o.v[3 + jt - JT_RX] = S(x[iv]);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// RNEA (reference algorithm/rnea.hxx:24-161)
+// ------------------------------------------------------------------------------------------
+template <class S, int CAP>
+GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const Out& tau) {
+  X3<S> X[CAP];
+  M6<S> vel[CAP], acc[CAP], f[CAP];
+  const S* g = ModelScalar<S>::grav(m);
+  const S* arm = ModelScalar<S>::arm(m);
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    joint_transform(m, i, q, X[i]);
+    M6<S> vJ, aJ, t, ap;
+    joint_motion(jt, v, iv, vJ);
+    joint_motion(jt, a, iv, aJ);
+    if (p > 0) {
+      actinv_motion(X[i], vel[p], t);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) vel[i].v[k] = vJ.v[k] + t.v[k];
+      actinv_motion(X[i], acc[p], ap);
+    } else {
+      vel[i] = vJ;
+      M6<S> mg;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) mg.v[k] = -g[k];
+      actinv_motion(X[i], mg, ap);
+    }
+    cross_motion(vel[i], vJ, t);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[i].v[k] = (t.v[k] + aJ.v[k]) + ap.v[k];
+    Iner<S> Y;
+    load_inertia(m, i, Y);
+    M6<S> h, fa, fx;
+    iner_mul(Y, vel[i], h);
+    iner_mul(Y, acc[i], fa);
+    cross_force(vel[i], h, fx);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[i].v[k] = fa.v[k] + fx.v[k];
+  }
+  for (int i = m.nj - 1; i > 0; --i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    if (jt == JT_FF) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) tau[iv + k] = double(f[i].v[k] + arm[iv + k] * S(a[iv + k]));
+    } else {
+      tau[iv] = double(f[i].v[3 + jt - JT_RX] + arm[iv] * S(a[iv]));
+    }
+    if (p > 0) {
+      M6<S> fp;
+      act_force(X[i], f[i], fp);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f[p].v[k] += fp.v[k];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// ABA, LOCAL convention (reference algorithm/aba.hxx:360-540); the revolute
+// calc_aba is joint-revolute.hpp:823-834, the free-flyer one
+// joint-free-flyer.hpp:377-391 with the LLT inverse of
+// joint-common-operations.hpp:20-33.
+// ------------------------------------------------------------------------------------------
+template <class S, class SS, int CAP>
+GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, const Out& ddq) {
+  X3<S> X[CAP];
+  M6<S> vel[CAP], c[CAP], f[CAP];
+  Sym6<SS> Ia[CAP];
+  SS UD[CAP][6];
+  SS Dv[CAP], uu[CAP];
+  SS D6[36], UD6[36], u6[6];
+  const S* g = ModelScalar<S>::grav(m);
+  const double* arm = m.arm_d;
+  // pass 1 (AbaLocalConventionForwardStep1, aba.hxx:360-399)
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    joint_transform(m, i, q, X[i]);
+    M6<S> vJ, t;
+    joint_motion(jt, v, iv, vJ);
+    if (p > 0) {
+      actinv_motion(X[i], vel[p], t);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) vel[i].v[k] = vJ.v[k] + t.v[k];
+    } else {
+      vel[i] = vJ;
+    }
+    cross_motion(vel[i], vJ, c[i]);
+    Iner<S> Y;
+    load_inertia(m, i, Y);
+    iner_to_sym6(Y, Ia[i]);
+    M6<S> h;
+    iner_mul(Y, vel[i], h);
+    cross_force(vel[i], h, f[i]);
+  }
+  // pass 2 (AbaLocalConventionBackwardStep, aba.hxx:402-434)
+  for (int i = m.nj - 1; i > 0; --i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    if (jt == JT_FF) {  // root only: no parent update
+      SS StU[36], Ifull[36];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        SS col[6];
+        sym6_col(Ia[i], k, col);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) Ifull[6 * r + k] = col[r];
+      }
+#pragma unroll
+      for (int k = 0; k < 36; ++k) StU[k] = Ifull[k];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        StU[7 * k] += SS(arm[iv + k]);
+        u6[k] = SS(tau[iv + k]) - SS(f[i].v[k]);
+      }
+      llt_inverse<SS, 6>(StU, D6);
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 6; ++cc) {
+          SS s = Ifull[6 * r] * D6[cc];
+#pragma unroll
+          for (int k = 1; k < 6; ++k) s += Ifull[6 * r + k] * D6[6 * k + cc];
+          UD6[6 * r + cc] = s;
+        }
+      continue;
+    }
+    const int ax = jt - JT_RX;
+    const SS u = SS(tau[iv]) - SS(f[i].v[3 + ax]);
+    SS U[6];
+    sym6_col(Ia[i], 3 + ax, U);
+    const SS Dinv = SS(1) / (U[3 + ax] + SS(arm[iv]));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) UD[i][k] = U[k] * Dinv;
+    Dv[i] = Dinv;
+    uu[i] = u;
+    if (p > 0) {
+      sym6_rank1_sub(Ia[i], U, UD[i]);
+      Sym6<S> Iaf, Ip;
+      sym6_convert(Ia[i], Iaf);
+      S t6[6];
+      sym6_mv(Iaf, c[i].v, t6);
+      M6<S> pa, fp;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) pa.v[k] = f[i].v[k] + (t6[k] + S(UD[i][k] * u));
+      sym6_transform(Iaf, X[i], Ip);
+      sym6_add(Ia[p], Ip);
+      act_force(X[i], pa, fp);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f[p].v[k] += fp.v[k];
+    }
+  }
+  // pass 3 (AbaLocalConventionForwardStep2, aba.hxx:437-468)
+  M6<S> acc[CAP];
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    M6<S> a;
+    if (p > 0) {
+      actinv_motion(X[i], acc[p], a);
+    } else {
+      M6<S> mg;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) mg.v[k] = -g[k];
+      actinv_motion(X[i], mg, a);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a.v[k] += c[i].v[k];
+    if (jt == JT_FF) {
+      SS dd[6];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        SS s = D6[6 * r] * u6[0];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) s += D6[6 * r + k] * u6[k];
+        SS w = UD6[r] * SS(a.v[0]);
+#pragma unroll
+        for (int k = 1; k < 6; ++k) w += UD6[6 * k + r] * SS(a.v[k]);
+        dd[r] = s - w;
+        ddq[iv + r] = double(dd[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < 6; ++r) a.v[r] += S(dd[r]);
+    } else {
+      const int ax = jt - JT_RX;
+      SS w = UD[i][0] * SS(a.v[0]);
+#pragma unroll
+      for (int k = 1; k < 6; ++k) w += UD[i][k] * SS(a.v[k]);
+      const SS dd = Dv[i] * uu[i] - w;
+      ddq[iv] = double(dd);
+      a.v[3 + ax] += S(dd);
+    }
+    acc[i] = a;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// CRBA, WORLD convention (reference algorithm/crba.hxx:25-110, 498-548), writes
+// M (upper or symmetric; every other entry zero) and adds the armature; then
+// optionally the tree-sparse U D U^T factorisation of cholesky::decompose
+// (reference algorithm/cholesky.hxx:18-62) in FP64.
+// ------------------------------------------------------------------------------------------
+template <class S, int CAP>
+GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, const Out* U, const Out* D) {
+  const int nv = m.nv;
+  X3<S> oM[CAP];
+  Iner<S> Yc[CAP];
+  S J[CAP][6], Ag[CAP][6];
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    X3<S> X;
+    joint_transform(m, i, q, X);
+    if (p > 0) {
+      compose(oM[p], X, oM[i]);
+    } else {  // frame of the root subtree at its root joint (M is invariant to it)
+      oM[i] = X;
+      oM[i].t[0] = oM[i].t[1] = oM[i].t[2] = S(0);
+    }
+    const X3<S>& O = oM[i];
+    if (jt == JT_FF) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        S w[3] = {O.R[k], O.R[3 + k], O.R[6 + k]}, tw[3];
+        J[iv + k][0] = w[0]; J[iv + k][1] = w[1]; J[iv + k][2] = w[2];
+        J[iv + k][3] = S(0); J[iv + k][4] = S(0); J[iv + k][5] = S(0);
+        cross3(O.t, w, tw);
+        J[iv + 3 + k][0] = tw[0]; J[iv + 3 + k][1] = tw[1]; J[iv + 3 + k][2] = tw[2];
+        J[iv + 3 + k][3] = w[0]; J[iv + 3 + k][4] = w[1]; J[iv + 3 + k][5] = w[2];
+      }
+    } else {
+      const int ax = jt - JT_RX;
+      S w[3] = {O.R[ax], O.R[3 + ax], O.R[6 + ax]}, tw[3];
+      cross3(O.t, w, tw);
+      J[iv][0] = tw[0]; J[iv][1] = tw[1]; J[iv][2] = tw[2];
+      J[iv][3] = w[0]; J[iv][4] = w[1]; J[iv][5] = w[2];
+    }
+    Iner<S> Y;
+    load_inertia(m, i, Y);
+    iner_act(O, Y, Yc[i]);
+  }
+  for (int r = 0; r < nv; ++r)
+    for (int cidx = 0; cidx < nv; ++cidx) M[r * nv + cidx] = 0.0;
+  const S eps = eps_of<S>();
+  for (int i = m.nj - 1; i > 0; --i) {
+    const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+    const int nvj = (m.jtype[i] == JT_FF) ? 6 : 1;
+    for (int k = 0; k < nvj; ++k) {
+      M6<S> jc, ag;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) jc.v[r] = J[iv + k][r];
+      iner_mul(Yc[i], jc, ag);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) Ag[iv + k][r] = ag.v[r];
+    }
+    for (int r = 0; r < nvj; ++r)
+      for (int cidx = iv; cidx < iv + nst; ++cidx) {
+        S s = J[iv + r][0] * Ag[cidx][0];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) s += J[iv + r][k] * Ag[cidx][k];
+        M[(iv + r) * nv + cidx] = double(s);
+        if (symmetric) M[cidx * nv + iv + r] = double(s);
+      }
+    if (p > 0) iner_add(Yc[p], Yc[i], eps);
+  }
+  for (int k = 0; k < nv; ++k) M[k * nv + k] += m.arm_d[k];
+  if (U == nullptr) return;
+  // cholesky::decompose (cholesky.hxx:46-59), FP64 on the just-written M
+  const Out& Uo = *U;
+  const Out& Do = *D;
+  for (int r = 0; r < nv; ++r)
+    for (int cidx = 0; cidx < nv; ++cidx) Uo[r * nv + cidx] = (r == cidx) ? 1.0 : 0.0;
+  for (int j = nv - 1; j >= 0; --j) {
+    const int NVT = m.nsfr[j] - 1;
+    double s = 0.0;
+    for (int k = 0; k < NVT; ++k) {
+      const double ujk = Uo[j * nv + j + 1 + k];
+      s += ujk * (ujk * Do[j + 1 + k]);
+    }
+    const double Dj = M[j * nv + j] - s;
+    Do[j] = Dj;
+    const double Dinv = 1.0 / Dj;
+    for (int ii = m.pfr[j]; ii >= 0; ii = m.pfr[ii]) {
+      double w = 0.0;
+      for (int k = 0; k < NVT; ++k) w += Uo[ii * nv + j + 1 + k] * (Uo[j * nv + j + 1 + k] * Do[j + 1 + k]);
+      Uo[ii * nv + j] = (M[ii * nv + j] - w) * Dinv;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// integrate(q, v): revolute joints q + v; free-flyer through the SE(3)
+// exponential with the quaternion renormalised to first order (reference
+// multibody/liegroup/special-euclidean.hpp:660-699, spatial/explog-quaternion.hpp:20-147,
+// math/quaternion.hpp:90-111).  Always FP64.
+// ------------------------------------------------------------------------------------------
+GB_HD void integrate_one(const MView& m, const In& q, const In& v, const Out& qo) {
+  const double eps = eps_of<double>();
+  const double ts_prec = 1.2207031250000000e-04;  // eps^(1/4): Taylor switch of exp3 / exp6
+  for (int i = 1; i < m.nj; ++i) {
+    const int iq = m.idx_q[i], iv = m.idx_v[i];
+    if (m.jtype[i] != JT_FF) {
+      qo[iq] = q[iq] + v[iv];
+      continue;
+    }
+    const double lv[3] = {v[iv], v[iv + 1], v[iv + 2]};
+    const double w[3] = {v[iv + 3], v[iv + 4], v[iv + 5]};
+    const double t2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2] + eps * eps;
+    const double t = sqrt(t2);
+    double st, ct;
+    sincos(t, &st, &ct);
+    const double inv_t2 = 1.0 / t2;
+    double a_wxv, a_w2;
+    if (t < ts_prec) {
+      a_wxv = 0.5 - t2 / 24.0;
+      a_w2 = 1.0 / 6.0 - t2 / 120.0;
+    } else {
+      a_wxv = (1.0 - ct) * inv_t2;
+      a_w2 = (t - st) * inv_t2 / t;
+    }
+    double wxv[3], wxwxv[3], tr[3];
+    cross3(w, lv, wxv);
+    cross3(w, wxv, wxwxv);
+    for (int k = 0; k < 3; ++k) tr[k] = lv[k] + a_wxv * wxv[k] + a_w2 * wxwxv[k];
+    const double s2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    const double th = sqrt(s2 + eps * eps);
+    double e[4];
+    if (s2 > ts_prec) {
+      double sh, ch;
+      sincos(0.5 * th, &sh, &ch);
+      for (int k = 0; k < 3; ++k) e[k] = sh * (w[k] / th);
+      e[3] = ch;
+    } else {
+      const double t22 = s2 / 4.0;
+      const double cc = 0.5 * (1.0 - t22 / 6.0 + t22 * t22 / 120.0);
+      for (int k = 0; k < 3; ++k) e[k] = cc * w[k];
+      e[3] = 1.0 - t22 / 2.0 + t22 * t22 / 24.0;
+    }
+    const double qq[4] = {q[iq + 3], q[iq + 4], q[iq + 5], q[iq + 6]};
+    double uv[3], uxuv[3];
+    cross3(qq, tr, uv);
+    for (int k = 0; k < 3; ++k) uv[k] += uv[k];
+    cross3(qq, uv, uxuv);
+    for (int k = 0; k < 3; ++k) qo[iq + k] = tr[k] + qq[3] * uv[k] + uxuv[k] + q[iq + k];
+    double r[4];
+    r[3] = qq[3] * e[3] - qq[0] * e[0] - qq[1] * e[1] - qq[2] * e[2];
+    r[0] = qq[3] * e[0] + qq[0] * e[3] + qq[1] * e[2] - qq[2] * e[1];
+    r[1] = qq[3] * e[1] + qq[1] * e[3] + qq[2] * e[0] - qq[0] * e[2];
+    r[2] = qq[3] * e[2] + qq[2] * e[3] + qq[0] * e[1] - qq[1] * e[0];
+    const double dp = r[0] * qq[0] + r[1] * qq[1] + r[2] * qq[2] + r[3] * qq[3];
+    if (dp < 0.0)
+      for (int k = 0; k < 4; ++k) r[k] = -r[k];
+    const double N2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+    const double alpha = (3.0 - N2) / 2.0;
+    for (int k = 0; k < 4; ++k) qo[iq + 3 + k] = r[k] * alpha;
+  }
+}
+
+}  // namespace gb

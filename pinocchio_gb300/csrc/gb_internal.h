@@ -1,0 +1,46 @@
+// Internal host-side declarations shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pinocchio_gb300.h"
+#include "gb_model_build.h"
+
+struct gb_pool {
+  const gb_model* model = nullptr;
+  long size = 0;
+  int precision = GB_FP64;
+  cudaStream_t stream = nullptr;
+  double* d_buf = nullptr;  // device staging for the *_in_parallel calls
+  size_t d_bytes = 0;
+};
+
+namespace gbi {
+
+int set_error(int code, const std::string& msg);
+int cuda_error(cudaError_t e, const char* where);
+
+// per-instance strides of one batch array
+struct Arr {
+  const double* p;
+  long is;  // instance stride
+  long es;  // element stride
+};
+inline Arr arr(const double* p, int layout, long batch, long n) {
+  return layout == GB_LAYOUT_SOA ? Arr{p, 1, batch} : Arr{p, n, 1};
+}
+
+int check_common(const gb_model* m, int precision, int layout, long batch);
+int check_ptr(const void* p, const char* name);
+
+
+// launches (gb_kernels.cu / gb_derivs.cu)
+int launch_rnea(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
+int launch_aba(const gb_model* m, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
+int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q, Arr M, Arr U, Arr D, cudaStream_t st);
+int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
+
+}  // namespace gbi

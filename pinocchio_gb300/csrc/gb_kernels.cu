@@ -1,0 +1,133 @@
+// Batched sweep kernels: RNEA, ABA, CRBA (+ FP64 Cholesky), integrate.
+//
+// One thread evaluates one configuration; a CTA of kThreads threads first
+// copies the model blob (joint tables, placements, inertias) from global to
+// shared memory with 16-byte loads, then every thread walks the tree reading
+// the tables as broadcasts.  Per-joint state lives in thread-local arrays of
+// the model's capacity class.
+#include "gb_dyn.cuh"
+#include "gb_internal.h"
+
+namespace gbi {
+namespace {
+
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ gb::MView stage_model(const unsigned char* __restrict__ blob, int bytes,
+                                                 unsigned char* smem) {
+  const uint4* src = reinterpret_cast<const uint4*>(blob);
+  uint4* dst = reinterpret_cast<uint4*>(smem);
+  for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  return gb::make_view(smem);
+}
+
+__device__ __forceinline__ gb::In in_at(const Arr& a, long b) { return gb::In{a.p + b * a.is, a.es}; }
+__device__ __forceinline__ gb::Out out_at(const Arr& a, long b) {
+  return gb::Out{const_cast<double*>(a.p) + b * a.is, a.es};
+}
+
+template <class S, int CAP>
+__global__ void __launch_bounds__(kThreads) k_rnea(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr a,
+                                                   Arr tau) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  gb::rnea_one<S, CAP>(m, in_at(q, b), in_at(v, b), in_at(a, b), out_at(tau, b));
+}
+
+template <class S, class SS, int CAP>
+__global__ void __launch_bounds__(kThreads) k_aba(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr tau,
+                                                  Arr ddq) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  gb::aba_one<S, SS, CAP>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b));
+}
+
+template <class S, int CAP>
+__global__ void __launch_bounds__(kThreads) k_crba(const unsigned char* blob, int bytes, long B, bool symmetric, Arr q,
+                                                   Arr M, Arr U, Arr D) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const gb::Out Uo = out_at(U, b), Do = out_at(D, b);
+  gb::crba_one<S, CAP>(m, in_at(q, b), out_at(M, b), symmetric, U.p ? &Uo : nullptr, U.p ? &Do : nullptr);
+}
+
+__global__ void __launch_bounds__(kThreads) k_integrate(const unsigned char* blob, int bytes, long B, Arr q, Arr v,
+                                                        Arr qo) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  gb::integrate_one(m, in_at(q, b), in_at(v, b), out_at(qo, b));
+}
+
+template <class K>
+int launch_common(const gb_model* M, long B, cudaStream_t st, K kernel, const char* name) {
+  static_assert(sizeof(K) > 0, "");
+  const int bytes = M->blob_bytes;
+  if (bytes > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return cuda_error(e, name);
+  }
+  (void)st;
+  return GB_OK;
+}
+
+#define GB_LAUNCH(kernel, ...)                                                              \
+  do {                                                                                      \
+    const int rc__ = launch_common(M, B, st, kernel, #kernel);                              \
+    if (rc__ != GB_OK) return rc__;                                                         \
+    const long grid__ = (B + kThreads - 1) / kThreads;                                      \
+    kernel<<<(unsigned)grid__, kThreads, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, __VA_ARGS__); \
+    return cuda_error(cudaGetLastError(), #kernel);                                         \
+  } while (0)
+
+#define GB_CAP_SWITCH(CAPV, BODY)           \
+  switch (CAPV) {                           \
+    case 8: { constexpr int C = 8; BODY; }   \
+    case 16: { constexpr int C = 16; BODY; } \
+    case 32: { constexpr int C = 32; BODY; } \
+    case 64: { constexpr int C = 64; BODY; } \
+    case 128: { constexpr int C = 128; BODY; } \
+    default: return set_error(GB_ERR_UNSUPPORTED, "model too large"); \
+  }
+
+}  // namespace
+
+int launch_rnea(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st) {
+  if (precision == GB_FP64) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_rnea<double, C>), q, v, a, tau));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_rnea<float, C>), q, v, a, tau));
+  }
+}
+
+int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st) {
+  if (precision == GB_FP64) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C>), q, v, tau, ddq));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<float, double, C>), q, v, tau, ddq));
+  }
+}
+
+int launch_crba(const gb_model* M, int precision, bool symmetric, long B, Arr q, Arr Mo, Arr U, Arr D,
+                cudaStream_t st) {
+  // the factorisation is FP64 in both precisions, and so is the M it factorises
+  if (precision == GB_FP64 || U.p != nullptr) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_crba<double, C>), symmetric, q, Mo, U, D));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_crba<float, C>), symmetric, q, Mo, U, D));
+  }
+}
+
+int launch_integrate(const gb_model* M, long B, Arr q, Arr v, Arr qo, cudaStream_t st) {
+  GB_LAUNCH(k_integrate, q, v, qo);
+}
+
+}  // namespace gbi

@@ -1,0 +1,95 @@
+// Flattened model tables: the byte blob that is uploaded once per model and
+// copied into shared memory by every CTA, and the view the kernels read.
+//
+// The blob replaces ModelTpl + the tree tables of DataTpl that the hot path
+// reads (reference multibody/model.hpp:98-220, multibody/data.hxx:195-306):
+// per joint parent / type / idx_q / idx_v / nvSubtree / depth, placements and
+// inertias (FP64 and FP32 copies), per dof armature / parents_fromRow /
+// nvSubtree_fromRow, and for the batched products -Minv*X the per-column list
+// of rows that can be non-zero (ancestor and subtree dofs), and the Fcrb
+// slot of every joint for the Minv recursion of the ABA derivatives.
+#pragma once
+
+#include "gb_spatial.cuh"
+
+namespace gb {
+
+enum { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4 };
+
+struct BlobHeader {
+  int nj, nq, nv, bytes;
+  int max_depth, has_ff, n_rel, nslot;
+  int o_parent, o_jtype, o_idxq, o_idxv, o_nvsub, o_depth, o_pfr, o_nsfr;
+  int o_place_d, o_iner_d, o_arm_d, o_place_f, o_iner_f, o_arm_f, o_rel_off, o_rel_list;
+  int o_slot, o_dofj, pad2, pad3;
+  double grav_d[6];
+  float grav_f[6];
+  float padf[2];
+};
+static_assert(sizeof(BlobHeader) % 16 == 0, "blob header must keep 16-byte alignment");
+
+struct MView {
+  int nj, nq, nv, max_depth, has_ff, nslot;
+  const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint;
+  const double *place_d, *iner_d, *arm_d, *grav_d;
+  const float *place_f, *iner_f, *arm_f, *grav_f;
+};
+
+GB_HD MView make_view(const unsigned char* base) {
+  const BlobHeader* h = reinterpret_cast<const BlobHeader*>(base);
+  MView m;
+  m.nj = h->nj; m.nq = h->nq; m.nv = h->nv; m.max_depth = h->max_depth; m.has_ff = h->has_ff; m.nslot = h->nslot;
+  m.parent = reinterpret_cast<const int*>(base + h->o_parent);
+  m.jtype = reinterpret_cast<const int*>(base + h->o_jtype);
+  m.idx_q = reinterpret_cast<const int*>(base + h->o_idxq);
+  m.idx_v = reinterpret_cast<const int*>(base + h->o_idxv);
+  m.nvsub = reinterpret_cast<const int*>(base + h->o_nvsub);
+  m.depth = reinterpret_cast<const int*>(base + h->o_depth);
+  m.pfr = reinterpret_cast<const int*>(base + h->o_pfr);
+  m.nsfr = reinterpret_cast<const int*>(base + h->o_nsfr);
+  m.rel_off = reinterpret_cast<const int*>(base + h->o_rel_off);
+  m.rel_list = reinterpret_cast<const int*>(base + h->o_rel_list);
+  m.slot = reinterpret_cast<const int*>(base + h->o_slot);
+  m.dof_joint = reinterpret_cast<const int*>(base + h->o_dofj);
+  m.place_d = reinterpret_cast<const double*>(base + h->o_place_d);
+  m.iner_d = reinterpret_cast<const double*>(base + h->o_iner_d);
+  m.arm_d = reinterpret_cast<const double*>(base + h->o_arm_d);
+  m.place_f = reinterpret_cast<const float*>(base + h->o_place_f);
+  m.iner_f = reinterpret_cast<const float*>(base + h->o_iner_f);
+  m.arm_f = reinterpret_cast<const float*>(base + h->o_arm_f);
+  m.grav_d = h->grav_d;
+  m.grav_f = h->grav_f;
+  return m;
+}
+
+template <class S> struct ModelScalar;
+template <> struct ModelScalar<double> {
+  GB_HD static const double* place(const MView& m, int i) { return m.place_d + 12 * i; }
+  GB_HD static const double* iner(const MView& m, int i) { return m.iner_d + 10 * i; }
+  GB_HD static const double* arm(const MView& m) { return m.arm_d; }
+  GB_HD static const double* grav(const MView& m) { return m.grav_d; }
+};
+template <> struct ModelScalar<float> {
+  GB_HD static const float* place(const MView& m, int i) { return m.place_f + 12 * i; }
+  GB_HD static const float* iner(const MView& m, int i) { return m.iner_f + 10 * i; }
+  GB_HD static const float* arm(const MView& m) { return m.arm_f; }
+  GB_HD static const float* grav(const MView& m) { return m.grav_f; }
+};
+
+template <class S> GB_HD void load_placement(const MView& m, int i, X3<S>& P) {
+  const S* p = ModelScalar<S>::place(m, i);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) P.R[k] = p[k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) P.t[k] = p[9 + k];
+}
+template <class S> GB_HD void load_inertia(const MView& m, int i, Iner<S>& Y) {
+  const S* p = ModelScalar<S>::iner(m, i);
+  Y.m = p[0];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) Y.c[k] = p[1 + k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) Y.I[k] = p[4 + k];
+}
+
+}  // namespace gb

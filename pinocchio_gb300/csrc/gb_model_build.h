@@ -1,0 +1,162 @@
+// Host-side flattening of a kinematic tree into the tables and the device
+// blob of gb_model.cuh.  Pure C++ (no CUDA runtime), shared by the C ABI and
+// by the host build of the kernels used in the CPU tests.
+#pragma once
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pinocchio_gb300.h"
+#include "gb_model.cuh"
+
+struct gb_model {
+  int nj = 0, nq = 0, nv = 0, cap = 0, max_depth = 0;
+  int device = 0;
+  std::vector<int> parents, jtype, idx_q, idx_v, nvs, nvsub, depth, pfr, nsfr, rel_off, rel_list, slot;
+  int nslot = 0;
+  std::vector<double> placement, inertia, armature;
+  double gravity[6];
+  std::vector<unsigned char> blob;  // host copy of the device blob
+  unsigned char* d_blob = nullptr;  // device copy (owned by the C ABI)
+  int blob_bytes = 0;
+};
+
+namespace gbm {
+
+inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+// capacity class used to instantiate the kernels (>= njoints and >= nv)
+inline int cap_class(int n) { return n <= 8 ? 8 : n <= 16 ? 16 : n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 0; }
+
+// Builds the tree tables of DataTpl (reference multibody/data.hxx:195-306) and
+// the device blob.
+inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
+  auto set_error = [&](int code, const std::string& msg) { *err = msg; return code; };
+  const int nj = d->njoints;
+  if (nj < 2) return set_error(GB_ERR_SIZE, "model needs at least one joint besides the universe");
+  M->nj = nj;
+  M->parents.assign(d->parents, d->parents + nj);
+  M->jtype.assign(d->jtype, d->jtype + nj);
+  M->placement.assign(d->placement, d->placement + 12 * nj);
+  M->inertia.assign(d->inertia, d->inertia + 10 * nj);
+  const double g0[6] = {0, 0, -9.81, 0, 0, 0};
+  std::memcpy(M->gravity, d->gravity ? d->gravity : g0, sizeof(g0));
+  if (M->jtype[0] != GB_JOINT_NONE) return set_error(GB_ERR_UNSUPPORTED, "joint 0 must be the universe");
+  M->idx_q.assign(nj, 0);
+  M->idx_v.assign(nj, 0);
+  M->nvs.assign(nj, 0);
+  M->depth.assign(nj, 0);
+  int nq = 0, nv = 0, nff = 0;
+  for (int i = 1; i < nj; ++i) {
+    const int jt = M->jtype[i], p = M->parents[i];
+    if (jt < GB_JOINT_RX || jt > GB_JOINT_FREEFLYER)
+      return set_error(GB_ERR_UNSUPPORTED, "joint " + std::to_string(i) + ": unsupported joint type");
+    if (p < 0 || p >= i) return set_error(GB_ERR_INVALID_ARGUMENT, "parents[i] must satisfy 0 <= parents[i] < i");
+    if (jt == GB_JOINT_FREEFLYER) {
+      ++nff;
+      if (i != 1 || p != 0)
+        return set_error(GB_ERR_UNSUPPORTED, "a free-flyer is supported only as the root joint (joint 1, parent 0)");
+    }
+    M->idx_q[i] = nq;
+    M->idx_v[i] = nv;
+    M->nvs[i] = jt == GB_JOINT_FREEFLYER ? 6 : 1;
+    nq += jt == GB_JOINT_FREEFLYER ? 7 : 1;
+    nv += M->nvs[i];
+    M->depth[i] = M->depth[p] + 1;
+    M->max_depth = std::max(M->max_depth, M->depth[i]);
+    if (M->inertia[10 * i] < 0.0) return set_error(GB_ERR_INVALID_ARGUMENT, "negative link mass");
+  }
+  M->nq = nq;
+  M->nv = nv;
+  if (d->armature && d->nv_armature != nv) return set_error(GB_ERR_SIZE, "armature must have nv entries");
+  M->armature.assign(nv, 0.0);
+  if (d->armature) M->armature.assign(d->armature, d->armature + nv);
+  M->cap = cap_class(std::max(nj, nv));
+  if (M->cap == 0) return set_error(GB_ERR_UNSUPPORTED, "models are limited to 128 joints and 128 dofs");
+  // lastChild / nvSubtree (data.hxx:195-225)
+  std::vector<int> last(nj, -1);
+  M->nvsub.assign(nj, 0);
+  for (int i = nj - 1; i >= 0; --i) {
+    if (last[i] == -1) last[i] = i;
+    const int p = i > 0 ? M->parents[i] : 0;
+    last[p] = std::max(last[i], last[p]);
+    M->nvsub[i] = M->idx_v[last[i]] + M->nvs[last[i]] - M->idx_v[i];
+  }
+  for (int i = 1; i < nj; ++i)  // compact subtrees (crba.hxx:573-595)
+    for (int k = i + 1; k <= last[i]; ++k) {
+      int a = k;
+      while (a > i) a = M->parents[a];
+      if (a != i) return set_error(GB_ERR_UNSUPPORTED, "joints are not in depth-first order");
+    }
+  // parents_fromRow / nvSubtree_fromRow (data.hxx:250-306)
+  M->pfr.assign(nv, -1);
+  M->nsfr.assign(nv, 0);
+  for (int j = 1; j < nj; ++j) {
+    const int p = M->parents[j], iv = M->idx_v[j];
+    M->pfr[iv] = p > 0 ? M->idx_v[p] + M->nvs[p] - 1 : -1;
+    M->nsfr[iv] = M->nvsub[j];
+    for (int r = 1; r < M->nvs[j]; ++r) {
+      M->pfr[iv + r] = iv + r - 1;
+      M->nsfr[iv + r] = M->nvsub[j] - r;
+    }
+  }
+  // rows that can be non-zero in column c of dtau/dq: ancestors of c and its subtree
+  M->rel_off.assign(nv + 1, 0);
+  M->rel_list.clear();
+  for (int c = 0; c < nv; ++c) {
+    std::vector<int> rows;
+    for (int a = M->pfr[c]; a >= 0; a = M->pfr[a]) rows.push_back(a);
+    std::sort(rows.begin(), rows.end());
+    for (int k = c; k < c + M->nsfr[c]; ++k) rows.push_back(k);
+    M->rel_off[c] = (int)M->rel_list.size();
+    M->rel_list.insert(M->rel_list.end(), rows.begin(), rows.end());
+  }
+  M->rel_off[nv] = (int)M->rel_list.size();
+  // Fcrb slots of the Minv recursion: the last child of a joint (in depth-first
+  // order) overwrites its parent's block in place, any other child takes the next slot.
+  std::vector<int> last_child(nj, -1);
+  for (int i = 1; i < nj; ++i) last_child[M->parents[i]] = i;
+  M->slot.assign(nj, 0);
+  M->nslot = 1;
+  for (int i = 1; i < nj; ++i) {
+    const int p = M->parents[i];
+    M->slot[i] = (last_child[p] == i) ? M->slot[p] : M->slot[p] + 1;
+    M->nslot = std::max(M->nslot, M->slot[i] + 1);
+  }
+  // blob
+  gb::BlobHeader h;
+  std::memset(&h, 0, sizeof(h));
+  h.nj = nj; h.nq = nq; h.nv = nv; h.max_depth = M->max_depth; h.has_ff = nff; h.n_rel = (int)M->rel_list.size(); h.nslot = M->nslot;
+  size_t off = sizeof(gb::BlobHeader);
+  auto take = [&](size_t bytes) { const size_t o = off; off = align16(off + bytes); return (int)o; };
+  h.o_parent = take(4 * nj); h.o_jtype = take(4 * nj); h.o_idxq = take(4 * nj); h.o_idxv = take(4 * nj);
+  h.o_nvsub = take(4 * nj); h.o_depth = take(4 * nj); h.o_pfr = take(4 * nv); h.o_nsfr = take(4 * nv);
+  h.o_rel_off = take(4 * (nv + 1)); h.o_rel_list = take(4 * M->rel_list.size() + 4); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv);
+  h.o_place_d = take(8 * 12 * nj); h.o_iner_d = take(8 * 10 * nj); h.o_arm_d = take(8 * nv);
+  h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
+  h.bytes = (int)off;
+  for (int k = 0; k < 6; ++k) { h.grav_d[k] = M->gravity[k]; h.grav_f[k] = (float)M->gravity[k]; }
+  M->blob.assign(off, 0);
+  unsigned char* b = M->blob.data();
+  std::memcpy(b, &h, sizeof(h));
+  auto put_i = [&](int o, const std::vector<int>& v) { if (!v.empty()) std::memcpy(b + o, v.data(), 4 * v.size()); };
+  auto put_d = [&](int o, const std::vector<double>& v) { if (!v.empty()) std::memcpy(b + o, v.data(), 8 * v.size()); };
+  auto put_f = [&](int o, const std::vector<double>& v) {
+    for (size_t k = 0; k < v.size(); ++k) reinterpret_cast<float*>(b + o)[k] = (float)v[k];
+  };
+  put_i(h.o_parent, M->parents); put_i(h.o_jtype, M->jtype); put_i(h.o_idxq, M->idx_q); put_i(h.o_idxv, M->idx_v);
+  put_i(h.o_nvsub, M->nvsub); put_i(h.o_depth, M->depth); put_i(h.o_pfr, M->pfr); put_i(h.o_nsfr, M->nsfr);
+  put_i(h.o_rel_off, M->rel_off); put_i(h.o_rel_list, M->rel_list); put_i(h.o_slot, M->slot);
+  std::vector<int> dofj(nv, 0);
+  for (int i = 1; i < nj; ++i)
+    for (int r = 0; r < M->nvs[i]; ++r) dofj[M->idx_v[i] + r] = i;
+  put_i(h.o_dofj, dofj);
+  put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);
+  put_f(h.o_place_f, M->placement); put_f(h.o_iner_f, M->inertia); put_f(h.o_arm_f, M->armature);
+  M->blob_bytes = (int)off;
+  return GB_OK;
+}
+
+
+}  // namespace gbm

@@ -1,0 +1,158 @@
+// Test infrastructure: host (CPU) build of the per-instance kernel code in
+// pinocchio_gb300/csrc/gb_dyn.cuh, so that the kernel arithmetic -- including
+// the mixed-precision split -- can be checked against the oracle without a
+// GPU.  The product never links this file.
+#define _GNU_SOURCE 1
+#include <math.h>
+
+#include <string>
+
+#include "../../pinocchio_gb300/csrc/gb_dyn.cuh"
+#include "../../pinocchio_gb300/csrc/gb_model_build.h"
+
+namespace {
+thread_local std::string g_err;
+gb::In in_at(const double* p, long b, long n) { return gb::In{p + b * n, 1}; }
+gb::Out out_at(double* p, long b, long n) { return gb::Out{p + b * n, 1}; }
+}  // namespace
+
+extern "C" {
+const char* hs_last_error() { return g_err.c_str(); }
+
+void* hs_model_new(const gb_model_desc* d) {
+  gb_model* M = new gb_model();
+  if (gbm::build_model(M, d, &g_err) != GB_OK) {
+    delete M;
+    return nullptr;
+  }
+  return M;
+}
+void hs_model_free(void* h) { delete static_cast<gb_model*>(h); }
+
+#define HS_DISPATCH(CAPV, CALL)                                            \
+  switch (CAPV) {                                                          \
+    case 8: { constexpr int C = 8; CALL; break; }                          \
+    case 16: { constexpr int C = 16; CALL; break; }                        \
+    case 32: { constexpr int C = 32; CALL; break; }                        \
+    case 64: { constexpr int C = 64; CALL; break; }                        \
+    default: { constexpr int C = 128; CALL; break; }                       \
+  }
+
+int hs_rnea(void* h, int mixed, long B, const double* q, const double* v, const double* a, double* tau) {
+  const gb_model* M = static_cast<gb_model*>(h);
+  const gb::MView m = gb::make_view(M->blob.data());
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    if (mixed) { HS_DISPATCH(M->cap, (gb::rnea_one<float, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv), out_at(tau, b, m.nv)))); }
+    else { HS_DISPATCH(M->cap, (gb::rnea_one<double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv), out_at(tau, b, m.nv)))); }
+  }
+  return 0;
+}
+int hs_aba(void* h, int mixed, long B, const double* q, const double* v, const double* tau, double* ddq) {
+  const gb_model* M = static_cast<gb_model*>(h);
+  const gb::MView m = gb::make_view(M->blob.data());
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    if (mixed) { HS_DISPATCH(M->cap, (gb::aba_one<float, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv)))); }
+    else { HS_DISPATCH(M->cap, (gb::aba_one<double, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv)))); }
+  }
+  return 0;
+}
+int hs_crba(void* h, int mixed, int symmetric, long B, const double* q, double* Mo, double* U, double* D) {
+  const gb_model* M = static_cast<gb_model*>(h);
+  const gb::MView m = gb::make_view(M->blob.data());
+  const long nn = (long)m.nv * m.nv;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    const gb::Out Uo = U ? out_at(U, b, nn) : gb::Out{nullptr, 1};
+    const gb::Out Do = D ? out_at(D, b, m.nv) : gb::Out{nullptr, 1};
+    if (mixed) { HS_DISPATCH(M->cap, (gb::crba_one<float, C>(m, in_at(q, b, m.nq), out_at(Mo, b, nn), symmetric != 0, U ? &Uo : nullptr, U ? &Do : nullptr))); }
+    else { HS_DISPATCH(M->cap, (gb::crba_one<double, C>(m, in_at(q, b, m.nq), out_at(Mo, b, nn), symmetric != 0, U ? &Uo : nullptr, U ? &Do : nullptr))); }
+  }
+  return 0;
+}
+int hs_integrate(void* h, long B, const double* q, const double* v, double* qo) {
+  const gb_model* M = static_cast<gb_model*>(h);
+  const gb::MView m = gb::make_view(M->blob.data());
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) gb::integrate_one(m, in_at(q, b, m.nq), in_at(v, b, m.nv), out_at(qo, b, m.nq));
+  return 0;
+}
+}
+
+// ---- derivatives (host build of gb_derivs.cuh; the workspace is per instance, stride 1) ----
+#include "../../pinocchio_gb300/csrc/gb_derivs.cuh"
+#include <vector>
+
+extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const double* q, const double* v, const double* a,
+                   double* dq, double* dv, double* Mo, double* tau) {
+  const gb_model* M = static_cast<gb_model*>(h);
+  const gb::MView m = gb::make_view(M->blob.data());
+  const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, false);
+  const long nn = (long)m.nv * m.nv;
+#pragma omp parallel
+  {
+    std::vector<double> wd(L.nS);
+    std::vector<float> wf(L.nS);
+#pragma omp for schedule(static)
+    for (long b = 0; b < B; ++b) {
+      const gb::Out to = out_at(tau, b, m.nv);
+      if (mixed)
+        gb::rnea_derivs_one<float>(m, L, gb::Ws<float>{wf.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
+                                   out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0);
+      else
+        gb::rnea_derivs_one<double>(m, L, gb::Ws<double>{wd.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
+                                    out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0);
+    }
+  }
+  return 0;
+}
+
+template <class S> struct ProductScalar { typedef S type; };
+template <> struct ProductScalar<gb::dfloat> { typedef float type; };
+
+template <class S>
+static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const double* q, const double* v,
+                            const double* tau, double* dq, double* dv, double* Minv, double* ddq,
+                            std::vector<S>& wS, std::vector<double>& wSS) {
+  const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
+  const int nv = m.nv;
+  const long nn = (long)nv * nv;
+  const gb::Out dd = out_at(ddq, b, nv);
+  gb::aba_derivs_sweeps<S, double>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<double>{wSS.data(), 1},
+                                   in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv), out_at(Minv, b, nn), &dd);
+  // -Minv * dtau restricted to the structurally non-zero rows, as the device kernel does
+  const double* Mi = Minv + b * nn;
+  for (int mm = 0; mm < 2; ++mm) {
+    const S* X = wS.data() + (mm == 0 ? L.dtq : L.dtv);
+    double* O = (mm == 0 ? dq : dv) + b * nn;
+    for (int c = 0; c < nv; ++c)
+      for (int r = 0; r < nv; ++r) {
+        typedef typename ProductScalar<S>::type P;
+        P acc = P(0);
+        for (int kk = M->rel_off[c]; kk < M->rel_off[c + 1]; ++kk) {
+          const int k = M->rel_list[kk];
+          acc += P(Mi[k * nv + r]) * P(X[k * nv + c]);
+        }
+        O[r * nv + c] = -double(acc);
+      }
+  }
+}
+
+extern "C" int hs_aba_derivs(void* h, int mixed, long B, const double* q, const double* v, const double* tau, double* dq,
+                  double* dv, double* Minv, double* ddq) {
+  const gb_model* M = static_cast<gb_model*>(h);
+  const gb::MView m = gb::make_view(M->blob.data());
+  const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
+#pragma omp parallel
+  {
+    std::vector<double> wd(L.nS), wss(L.nSS);
+    std::vector<gb::dfloat> wf(L.nS);
+#pragma omp for schedule(static)
+    for (long b = 0; b < B; ++b) {
+      if (mixed) aba_derivs_host<gb::dfloat>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wss);
+      else aba_derivs_host<double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wss);
+    }
+  }
+  return 0;
+}

@@ -1,0 +1,130 @@
+"""GPU parity of the batched analytical derivatives through the C ABI:
+computeRNEADerivatives -> (dtau_dq, dtau_dv, M) and computeABADerivatives ->
+(ddq_dq, ddq_dv, Minv), FP64 against the oracle at 1e-12 (the ill-conditioned
+100-link chain at 1e-10), mixed precision at 1e-5, central finite differences
+(step 1e-6 in the tangent space), both layouts and the identities the
+reference's tests use (unittest/aba-derivatives.cpp:96-100: Minv = M^-1)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pinocchio_gb300 as pg
+from oracle.oracle import OracleModel, symmetrize_upper
+from pinocchio_gb300 import _capi
+from pinocchio_gb300 import sample_models as sm
+from util import FP64_TOL, MIXED_TOL, MODELS, rel_err
+
+pytestmark = pytest.mark.gpu
+
+# the mixed-precision bar applies to the BASELINE models; the 100-link chain is
+# the FP64 stress test (its Minv condition number amplifies FP32 rounding)
+MIXED_MODELS = [n for n in MODELS if n != "chain100"]
+
+
+def fp64_tol(name):
+    return 1e-10 if name == "chain100" else FP64_TOL
+
+
+@pytest.fixture(scope="module", params=list(MODELS))
+def case(request):
+    import torch
+
+    model = MODELS[request.param]()
+    q, v, x = sm.random_inputs(model, 517, 41)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    return request.param, model, OracleModel(model), q, v, x, dev
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_rnea_derivatives(case, precision):
+    name, model, om, q, v, a, dev = case
+    if precision == "mixed" and name not in MIXED_MODELS:
+        pytest.skip("FP64 stress model")
+    data = pg.createData(model, precision)
+    dq, dv, M = (t.cpu().numpy() for t in pg.computeRNEADerivatives(model, data, dev(q), dev(v), dev(a)))
+    tau_o, dq_o, dv_o, M_o = om.rnea_derivatives(q, v, a)
+    tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
+    assert rel_err(dq, dq_o) < tol
+    assert rel_err(dv, dv_o) < tol
+    assert rel_err(M, symmetrize_upper(M_o)) < tol
+    assert rel_err(data.tau.cpu().numpy(), tau_o) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_aba_derivatives(case, precision):
+    name, model, om, q, v, x, dev = case
+    if precision == "mixed" and name not in MIXED_MODELS:
+        pytest.skip("FP64 stress model")
+    tau = 10.0 * x
+    data = pg.createData(model, precision)
+    dq, dv, Minv = (t.cpu().numpy() for t in pg.computeABADerivatives(model, data, dev(q), dev(v), dev(tau)))
+    ddq_o, dq_o, dv_o, Minv_o = om.aba_derivatives(q, v, tau)
+    tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
+    assert rel_err(data.ddq.cpu().numpy(), ddq_o) < tol
+    assert rel_err(Minv, Minv_o) < tol
+    assert rel_err(dq, dq_o) < tol
+    assert rel_err(dv, dv_o) < tol
+    assert np.array_equal(Minv, np.swapaxes(Minv, 1, 2))
+
+
+def test_minv_is_inverse_of_crba(case):
+    name, model, om, q, v, x, dev = case
+    data = pg.createData(model)
+    _, _, Minv = pg.computeABADerivatives(model, data, dev(q), dev(v), dev(x))
+    M = pg.crba(model, data, dev(q))
+    eye = np.broadcast_to(np.eye(model.nv), (q.shape[0], model.nv, model.nv))
+    assert rel_err((Minv @ M).cpu().numpy(), eye) < (1e-8 if name == "chain100" else 1e-11)
+
+
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12"])
+def test_derivatives_vs_central_fd_on_gpu(name):
+    import torch
+
+    model = MODELS[name]()
+    data = pg.createData(model)
+    q, v, x = sm.random_inputs(model, 16, 3)
+    tau = 10.0 * x
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    dq, dv, Minv = (t.cpu().numpy() for t in pg.computeABADerivatives(model, data, dev(q), dev(v), dev(tau)))
+    h = 1e-6
+    fdq, fdv, fdt = np.zeros_like(dq), np.zeros_like(dq), np.zeros_like(dq)
+    qd, vd, td = dev(q), dev(v), dev(tau)
+    for k in range(model.nv):
+        e = torch.zeros((16, model.nv), dtype=torch.float64, device="cuda")
+        e[:, k] = h
+        qp, qm = pg.integrate(model, qd, e), pg.integrate(model, qd, -e)
+        fdq[:, :, k] = ((pg.aba(model, data, qp, vd, td) - pg.aba(model, data, qm, vd, td)) / (2 * h)).cpu().numpy()
+        fdv[:, :, k] = ((pg.aba(model, data, qd, vd + e, td) - pg.aba(model, data, qd, vd - e, td)) / (2 * h)).cpu().numpy()
+        fdt[:, :, k] = ((pg.aba(model, data, qd, vd, td + e) - pg.aba(model, data, qd, vd, td - e)) / (2 * h)).cpu().numpy()
+    assert rel_err(dq, fdq) < 1e-6
+    assert rel_err(dv, fdv) < 1e-6
+    assert rel_err(Minv, fdt) < 1e-6
+
+
+def test_soa_layout_derivatives(case):
+    import torch
+
+    name, model, om, q, v, x, dev = case
+    data = pg.createData(model)
+    B, nv = q.shape[0], model.nv
+    ref = [t.clone() for t in pg.computeABADerivatives(model, data, dev(q), dev(v), dev(x))]
+    qs, vs, ts = (dev(t.T) for t in (q, v, x))
+    outs = [torch.empty((nv * nv, B), dtype=torch.float64, device="cuda") for _ in range(3)]
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    _capi.check(
+        _capi.lib().gb_aba_derivatives(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, p(qs), p(vs), p(ts),
+                                       p(outs[0]), p(outs[1]), p(outs[2]), None, None)
+    )
+    torch.cuda.synchronize()
+    for o, r in zip(outs, ref):
+        assert torch.equal(o.T.reshape(B, nv, nv), r)
+
+
+def test_gravity_with_angular_part_is_rejected():
+    model = MODELS["manipulator6r"]()
+    model.gravity = np.array([0, 0, -9.81, 0.1, 0, 0])
+    data = pg.createData(model)
+    with pytest.raises(_capi.GBError) as err:
+        pg.computeABADerivatives(model, data, np.zeros((2, 6)), np.zeros((2, 6)), np.zeros((2, 6)))
+    assert err.value.code == _capi.GB_ERR_GRAVITY

@@ -1,0 +1,179 @@
+"""The CPU oracle against the reference's own identity tests and analytic known answers.
+
+The reference's hot-path tests pin no numbers; they check identities, which are
+restated here against the oracle (reference file:line on each test):
+  ABA o RNEA round trip (unittest/aba.cpp:124-184), tau = M a + nle (unittest/aba.cpp:229-263),
+  CRBA vs RNEA columns (unittest/crba.cpp:67-130), U D U^T = M (unittest/cholesky.cpp:31-100),
+  Minv M = I (unittest/aba-derivatives.cpp:96-100), derivatives vs finite differences
+  (unittest/rnea-derivatives.cpp:113-314, unittest/aba-derivatives.cpp:23-155),
+  batch == serial bit-exact (unittest/parallel-aba.cpp:21-55, unittest/parallel-rnea.cpp:78-112).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import LOCAL, WORLD, OracleModel, symmetrize_upper
+from pinocchio_gb300 import model as gm
+from pinocchio_gb300 import sample_models as sm
+from util import MODELS, rel_err
+
+CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100"]
+
+
+@pytest.fixture(scope="module", params=CPU_MODELS)
+def case(request):
+    model = MODELS[request.param]()
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, 16, 11)
+    return request.param, model, om, q, v, a
+
+
+def test_aba_rnea_roundtrip(case):
+    name, model, om, q, v, a = case
+    tau = om.rnea(q, v, a)
+    tol = 1e-10 if name == "chain100" else 1e-12
+    for conv in (LOCAL, WORLD):
+        assert rel_err(om.aba(q, v, tau, conv), a) < tol
+
+
+def test_mass_matrix_and_nle(case):
+    name, model, om, q, v, a = case
+    tau = om.rnea(q, v, a)
+    nle = om.rnea(q, v, np.zeros_like(a))
+    M = symmetrize_upper(om.crba(q))
+    assert rel_err(np.einsum("bij,bj->bi", M, a) + nle, tau) < 1e-12
+
+
+def test_crba_columns_and_conventions(case):
+    name, model, om, q, v, a = case
+    M = symmetrize_upper(om.crba(q, LOCAL))
+    assert rel_err(symmetrize_upper(om.crba(q, WORLD)), M) < 1e-12
+    # block-upper triangle only, as crba leaves it: rows of joint i, columns of its subtree
+    joint_of = np.repeat(np.arange(model.njoints), model.nvs)
+    lower_other = np.tril(np.ones((model.nv, model.nv), bool), -1) & (joint_of[:, None] != joint_of[None, :])
+    assert np.all(om.crba(q)[:, lower_other] == 0.0)
+    zero = np.zeros_like(v)
+    g = om.rnea(q, zero, zero)
+    for j in range(0, model.nv, max(1, model.nv // 5)):
+        e = np.zeros_like(v)
+        e[:, j] = 1.0
+        # the difference cancels the (much larger) gravity torque: allow its rounding
+        assert rel_err(om.rnea(q, zero, e) - g, M[:, :, j]) < 1e-10
+
+
+def test_cholesky(case):
+    name, model, om, q, v, a = case
+    Mu = om.crba(q)
+    U, D = om.cholesky(Mu)
+    M = symmetrize_upper(Mu)
+    assert np.allclose(np.diagonal(U, axis1=1, axis2=2), 1.0) and np.all(np.tril(U, -1) == 0)
+    assert rel_err(np.einsum("bij,bj,bkj->bik", U, D, U), M) < 1e-12
+
+
+def test_aba_derivatives_consistency(case):
+    name, model, om, q, v, a = case
+    tau = om.rnea(q, v, a)
+    ddq, ddq_dq, ddq_dv, Minv = om.aba_derivatives(q, v, tau)
+    M = symmetrize_upper(om.crba(q))
+    eye = np.broadcast_to(np.eye(model.nv), M.shape)
+    tol = 1e-9 if name == "chain100" else 1e-12
+    assert rel_err(np.einsum("bij,bjk->bik", Minv, M), eye) < tol
+    assert np.array_equal(Minv, np.swapaxes(Minv, 1, 2))
+    # ddq_dq = -Minv dtau_dq(q, v, ddq) with the RNEA derivatives (aba-derivatives.hxx:451-452)
+    _, dtau_dq, dtau_dv, _ = om.rnea_derivatives(q, v, ddq)
+    assert rel_err(-np.einsum("bij,bjk->bik", Minv, dtau_dq), ddq_dq) < 1e-11
+    assert rel_err(-np.einsum("bij,bjk->bik", Minv, dtau_dv), ddq_dv) < 1e-11
+
+
+def _fd(f, x0, h, k, integrate=None):
+    e = np.zeros((x0.shape[0], integrate[1] if integrate else x0.shape[1]))
+    e[:, k] = h
+    if integrate:
+        return (f(integrate[0](x0, e)) - f(integrate[0](x0, -e))) / (2 * h)
+    return (f(x0 + e) - f(x0 - e)) / (2 * h)
+
+
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12"])
+def test_derivatives_vs_central_fd(name):
+    model = MODELS[name]()
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, 4, 5)
+    tau = om.rnea(q, v, a)
+    _, dq, dv, _ = om.rnea_derivatives(q, v, a)
+    _, adq, adv, Minv = om.aba_derivatives(q, v, tau)
+    h = 1e-6  # central differences in the tangent space, step 1e-6
+    fd = {k: np.zeros_like(dq) for k in ("rq", "rv", "aq", "av", "at")}
+    for k in range(model.nv):
+        fd["rq"][:, :, k] = _fd(lambda x: om.rnea(x, v, a), q, h, k, (om.integrate, model.nv))
+        fd["rv"][:, :, k] = _fd(lambda x: om.rnea(q, x, a), v, h, k)
+        fd["aq"][:, :, k] = _fd(lambda x: om.aba(x, v, tau), q, h, k, (om.integrate, model.nv))
+        fd["av"][:, :, k] = _fd(lambda x: om.aba(q, x, tau), v, h, k)
+        fd["at"][:, :, k] = _fd(lambda x: om.aba(q, v, x), tau, h, k)
+    assert rel_err(dq, fd["rq"]) < 1e-6
+    assert rel_err(dv, fd["rv"]) < 1e-6
+    assert rel_err(adq, fd["aq"]) < 1e-6
+    assert rel_err(adv, fd["av"]) < 1e-6
+    assert rel_err(Minv, fd["at"]) < 1e-6
+
+
+def test_batch_equals_serial():
+    model = MODELS["humanoid32"]()
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, 64, 3)
+    tau_b = om.rnea(q, v, a, nthreads=4)
+    ddq_b = om.aba(q, v, tau_b, WORLD, nthreads=4)
+    for b in range(0, 64, 7):
+        assert np.array_equal(om.rnea(q[b : b + 1], v[b : b + 1], a[b : b + 1], nthreads=1)[0], tau_b[b])
+        assert np.array_equal(om.aba(q[b : b + 1], v[b : b + 1], tau_b[b : b + 1], WORLD, nthreads=1)[0], ddq_b[b])
+
+
+def test_long_double_agrees():
+    model = MODELS["humanoid32"]()
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, 8, 4)
+    tau = om.rnea(q, v, a)
+    assert rel_err(om.rnea(q, v, a, prec=1), tau) < 1e-14
+    assert rel_err(om.aba(q, v, tau, WORLD, prec=1), om.aba(q, v, tau, WORLD)) < 1e-12
+
+
+# ---- analytic known answers --------------------------------------------------------------
+def pendulum(m=2.0, L=0.7, Ixx=0.05):
+    """One revolute joint about x, COM hanging at (0, 0, -L)."""
+    model = gm.Model()
+    j = model.addJoint(0, gm.JointModelRX(), gm.SE3.Identity(), "pivot")
+    model.appendBodyToJoint(j, gm.Inertia(m, [0, 0, -L], np.diag([Ixx, 0.03, 0.04])))
+    return model
+
+
+def test_kat_pendulum():
+    m, L, Ixx, g = 2.0, 0.7, 0.05, 9.81
+    om = OracleModel(pendulum(m, L, Ixx))
+    rng = np.random.default_rng(0)
+    q = rng.uniform(-np.pi, np.pi, (32, 1))
+    v = rng.standard_normal((32, 1))
+    a = rng.standard_normal((32, 1))
+    tau = (Ixx + m * L * L) * a + m * g * L * np.sin(q)
+    assert rel_err(om.rnea(q, v, a), tau) < 1e-13
+    assert rel_err(om.aba(q, v, tau), a) < 1e-13
+    assert rel_err(symmetrize_upper(om.crba(q))[:, 0, 0][:, None], np.full((32, 1), Ixx + m * L * L)) < 1e-14
+
+
+def free_body(m=3.0, I=(0.2, 0.3, 0.4)):
+    model = gm.Model()
+    j = model.addJoint(0, gm.JointModelFreeFlyer(), gm.SE3.Identity(), "base")
+    model.appendBodyToJoint(j, gm.Inertia(m, [0, 0, 0], np.diag(I)))
+    return model
+
+
+def test_kat_free_body_newton_euler():
+    m, I = 3.0, np.diag([0.2, 0.3, 0.4])
+    model = free_body(m, np.diag(I))
+    om = OracleModel(model)
+    q, v, _ = sm.random_inputs(model, 32, 9)
+    ddq = om.aba(q, v, np.zeros((32, 6)))
+    g = np.array([0.0, 0.0, -9.81])
+    for b in range(32):
+        R = sm.quat_to_matrix(*q[b, 3:7])
+        lin, w = v[b, :3], v[b, 3:]
+        exp_lin = R.T @ g - np.cross(w, lin)
+        exp_ang = np.linalg.solve(I, -np.cross(w, I @ w))
+        assert np.allclose(ddq[b], np.concatenate([exp_lin, exp_ang]), rtol=1e-13, atol=1e-13)

@@ -1,0 +1,36 @@
+"""Shared helpers of the tests: error metrics and the workload models."""
+import numpy as np
+
+from pinocchio_gb300 import sample_models as sm
+
+
+def rel_err(x, ref):
+    """Max over instances of ||x - ref|| / ||ref|| (Frobenius per instance), the
+    isApprox-style relative error the reference's tests use."""
+    x = np.asarray(x, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    x = x.reshape(x.shape[0], -1)
+    ref = ref.reshape(ref.shape[0], -1)
+    den = np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+    return float((np.linalg.norm(x - ref, axis=1) / den).max())
+
+
+def med_rel_err(x, ref):
+    x = np.asarray(x, dtype=np.float64).reshape(len(x), -1)
+    ref = np.asarray(ref, dtype=np.float64).reshape(len(ref), -1)
+    return float(np.median(np.linalg.norm(x - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)))
+
+
+MODELS = {
+    "manipulator6r": lambda: sm.manipulator6r(0),
+    "humanoid32": lambda: sm.humanoid32(1),
+    "tree7": lambda: sm.random_tree(7, False, 307),
+    "tree12": lambda: sm.random_tree(12, False, 312),
+    "tree32ff": lambda: sm.random_tree(32, True, 332),
+    "tree60ff": lambda: sm.random_tree(60, True, 360),
+    "chain100": lambda: sm.chain(100, 4),
+}
+# FP64 parity bar of the batched kernels against the FP64 oracle (relative, per instance)
+FP64_TOL = 1e-12
+# mixed-precision bar (max relative error against the FP64 oracle)
+MIXED_TOL = 1e-5
