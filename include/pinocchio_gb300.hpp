@@ -1,0 +1,154 @@
+// C++ facade over the C ABI with the argument shapes of the reference's batched
+// dynamics entry points:
+//   rneaInParallel(num_threads, pool, q, v, a, tau)   (algorithm/parallel/rnea.hpp:39-84)
+//   abaInParallel(num_threads, pool, q, v, tau, a)    (algorithm/parallel/aba.hpp:40-84)
+// and, for device-resident batches, rnea / aba / crba / computeRNEADerivatives /
+// computeABADerivatives over (batch, n) device arrays.
+//
+// Matrix arguments are any type with rows(), cols() and data() over contiguous
+// column-major double storage -- Eigen::MatrixXd satisfies this, so a caller of
+// the reference passes the same objects.  Errors are thrown as
+// std::invalid_argument (size / pool errors, as PINOCCHIO_CHECK_ARGUMENT_SIZE
+// does, include/pinocchio/macros.hpp:162-223) or std::runtime_error (device errors).
+#ifndef PINOCCHIO_GB300_HPP
+#define PINOCCHIO_GB300_HPP
+
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pinocchio_gb300.h"
+
+namespace pinocchio_gb300 {
+
+inline void check(int rc) {
+  if (rc == GB_OK) return;
+  const std::string msg = gb_last_error();
+  if (rc == GB_ERR_SIZE || rc == GB_ERR_POOL || rc == GB_ERR_INVALID_ARGUMENT || rc == GB_ERR_GRAVITY ||
+      rc == GB_ERR_UNSUPPORTED)
+    throw std::invalid_argument(msg);
+  throw std::runtime_error(msg);
+}
+
+// A flattened kinematic tree (the ModelTpl tables the batched path reads).
+struct ModelTables {
+  std::vector<int> parents, jtype;  // joint 0 = universe (GB_JOINT_NONE)
+  std::vector<double> placement;    // njoints x 12
+  std::vector<double> inertia;      // njoints x 10
+  std::vector<double> armature;     // nv
+  double gravity[6] = {0, 0, -9.81, 0, 0, 0};
+};
+
+class Model {
+ public:
+  explicit Model(const ModelTables& t) {
+    gb_model_desc d;
+    d.njoints = static_cast<int>(t.parents.size());
+    d.parents = t.parents.data();
+    d.jtype = t.jtype.data();
+    d.placement = t.placement.data();
+    d.inertia = t.inertia.data();
+    d.armature = t.armature.empty() ? nullptr : t.armature.data();
+    d.nv_armature = static_cast<int>(t.armature.size());
+    d.gravity = t.gravity;
+    gb_model* m = nullptr;
+    check(gb_model_create(&d, &m));
+    handle_.reset(m, [](gb_model* p) { gb_model_destroy(p); });
+    check(gb_model_dims(m, &nq, &nv, &njoints));
+  }
+  gb_model* get() const { return handle_.get(); }
+  int nq = 0, nv = 0, njoints = 0;
+
+ private:
+  std::shared_ptr<gb_model> handle_;
+};
+
+// ModelPool(model, size) (multibody/pool/model.hpp:19-165).
+class ModelPool {
+ public:
+  ModelPool(const Model& model, long size) : model_(model) {
+    gb_pool* p = nullptr;
+    check(gb_pool_create(model.get(), size, &p));
+    handle_.reset(p, [](gb_pool* q) { gb_pool_destroy(q); });
+  }
+  long size() const {
+    long s = 0;
+    check(gb_pool_size(handle_.get(), &s));
+    return s;
+  }
+  void setPrecision(int precision) { check(gb_pool_set_precision(handle_.get(), precision)); }
+  const Model& getModel() const { return model_; }
+  gb_pool* get() const { return handle_.get(); }
+
+ private:
+  Model model_;
+  std::shared_ptr<gb_pool> handle_;
+};
+
+namespace detail {
+template <class M> void check_rows(const M& x, long rows, const char* name) {
+  if (static_cast<long>(x.rows()) != rows)
+    throw std::invalid_argument(std::string("wrong number of rows for ") + name);
+}
+}  // namespace detail
+
+// q: nq x batch, v, a: nv x batch, tau: nv x batch (written), column-major host storage.
+template <class MQ, class MV, class MA, class MT>
+void rneaInParallel(std::size_t num_threads, ModelPool& pool, const MQ& q, const MV& v, const MA& a, MT& tau) {
+  const Model& m = pool.getModel();
+  detail::check_rows(q, m.nq, "q");
+  detail::check_rows(v, m.nv, "v");
+  detail::check_rows(a, m.nv, "a");
+  detail::check_rows(tau, m.nv, "tau");
+  if (q.cols() != v.cols() || q.cols() != a.cols() || q.cols() != tau.cols())
+    throw std::invalid_argument("all batch matrices must have the same number of columns");
+  check(gb_rnea_in_parallel(static_cast<long>(num_threads), pool.get(), static_cast<long>(q.cols()), q.data(),
+                            v.data(), a.data(), tau.data()));
+}
+
+// q: nq x batch, v, tau: nv x batch, a: nv x batch (written); WORLD convention as the reference.
+template <class MQ, class MV, class MT, class MA>
+void abaInParallel(std::size_t num_threads, ModelPool& pool, const MQ& q, const MV& v, const MT& tau, MA& a) {
+  const Model& m = pool.getModel();
+  detail::check_rows(q, m.nq, "q");
+  detail::check_rows(v, m.nv, "v");
+  detail::check_rows(tau, m.nv, "tau");
+  detail::check_rows(a, m.nv, "a");
+  if (q.cols() != v.cols() || q.cols() != tau.cols() || q.cols() != a.cols())
+    throw std::invalid_argument("all batch matrices must have the same number of columns");
+  check(gb_aba_in_parallel(static_cast<long>(num_threads), pool.get(), static_cast<long>(q.cols()), q.data(),
+                           v.data(), tau.data(), a.data()));
+}
+
+// ---- device-resident batches (pointers to device memory, GB_LAYOUT_INSTANCE) -------------------
+inline void rnea(const Model& m, int precision, long batch, const double* q, const double* v, const double* a,
+                 double* tau, void* stream = nullptr) {
+  check(gb_rnea(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, a, tau, stream));
+}
+inline void aba(const Model& m, int precision, long batch, const double* q, const double* v, const double* tau,
+                double* ddq, int convention = GB_LOCAL, void* stream = nullptr) {
+  check(gb_aba(m.get(), precision, convention, GB_LAYOUT_INSTANCE, batch, q, v, tau, ddq, stream));
+}
+inline void crba(const Model& m, int precision, long batch, const double* q, double* M, int convention = GB_LOCAL,
+                 void* stream = nullptr) {
+  check(gb_crba(m.get(), precision, convention, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, batch, q, M, nullptr, nullptr,
+                stream));
+}
+inline void computeRNEADerivatives(const Model& m, int precision, long batch, const double* q, const double* v,
+                                   const double* a, double* dtau_dq, double* dtau_dv, double* M,
+                                   void* stream = nullptr) {
+  check(gb_rnea_derivatives(m.get(), precision, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, batch, q, v, a, dtau_dq, dtau_dv,
+                            M, nullptr, stream));
+}
+inline void computeABADerivatives(const Model& m, int precision, long batch, const double* q, const double* v,
+                                  const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
+                                  void* stream = nullptr) {
+  check(gb_aba_derivatives(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, tau, ddq_dq, ddq_dv, Minv, nullptr,
+                           stream));
+}
+
+}  // namespace pinocchio_gb300
+
+#endif  // PINOCCHIO_GB300_HPP

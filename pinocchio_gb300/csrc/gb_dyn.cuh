@@ -129,47 +129,103 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
 // calc_aba is joint-revolute.hpp:823-834, the free-flyer one
 // joint-free-flyer.hpp:377-391 with the LLT inverse of
 // joint-common-operations.hpp:20-33.
+//
+// Per joint only what crosses passes is stored: the velocity, the joint
+// transform (FP64 kernels) or its sine / cosine (mixed kernels, which rebuild
+// the transform in FP32), UDinv and Dinv*u.  The articulated inertia, the bias
+// force and the acceleration travel in registers from a joint to its first
+// child (forward) / from a first child to its parent (backward); only joints
+// with two or more children keep them in a branch slot.
 // ------------------------------------------------------------------------------------------
 template <class S, class SS, int CAP>
 GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, const Out& ddq) {
-  X3<S> X[CAP];
-  M6<S> vel[CAP], c[CAP], f[CAP];
-  Sym6<SS> Ia[CAP];
-  SS UD[CAP][6];
-  SS Dv[CAP], uu[CAP];
+  constexpr bool kStoreX = sizeof(S) == sizeof(double);
+  constexpr int NB = CAP / 2 + 1;
+  M6<S> vel[CAP];
+  X3<S> Xs[kStoreX ? CAP : 1];
+  S cs[kStoreX ? 1 : CAP][2];
+  X3<S> Xff;  // root free-flyer transform
+  S UDs[CAP][6];
+  SS du[CAP];
   SS D6[36], UD6[36], u6[6];
+  Sym6<SS> Islot[NB];
+  M6<S> fslot[NB], aslot[NB];
   const S* g = ModelScalar<S>::grav(m);
   const double* arm = m.arm_d;
-  // pass 1 (AbaLocalConventionForwardStep1, aba.hxx:360-399)
+  auto transform = [&](int i, X3<S>& X) {
+    if (kStoreX) {
+      X = Xs[i];
+    } else if (m.jtype[i] == JT_FF) {
+      X = Xff;
+    } else {
+      const S* P = ModelScalar<S>::place(m, i);
+      compose_axis(P, P + 9, m.jtype[i] - JT_RX, cs[i][1], cs[i][0], X);
+    }
+  };
+  // pass 1 (AbaLocalConventionForwardStep1, aba.hxx:360-399): transforms and velocities
   for (int i = 1; i < m.nj; ++i) {
     const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
-    joint_transform(m, i, q, X[i]);
+    X3<S> X;
+    if (jt == JT_FF) {
+      joint_transform(m, i, q, X);
+      Xff = X;
+    } else {
+      S sn, cn;
+      ssincos(S(q[m.idx_q[i]]), &sn, &cn);
+      const S* P = ModelScalar<S>::place(m, i);
+      compose_axis(P, P + 9, jt - JT_RX, cn, sn, X);
+      if (!kStoreX) { cs[i][0] = sn; cs[i][1] = cn; }
+    }
+    if (kStoreX) Xs[kStoreX ? i : 0] = X;
     M6<S> vJ, t;
     joint_motion(jt, v, iv, vJ);
     if (p > 0) {
-      actinv_motion(X[i], vel[p], t);
+      actinv_motion(X, vel[p], t);
 #pragma unroll
       for (int k = 0; k < 6; ++k) vel[i].v[k] = vJ.v[k] + t.v[k];
     } else {
       vel[i] = vJ;
     }
-    cross_motion(vel[i], vJ, c[i]);
-    Iner<S> Y;
-    load_inertia(m, i, Y);
-    iner_to_sym6(Y, Ia[i]);
-    M6<S> h;
-    iner_mul(Y, vel[i], h);
-    cross_force(vel[i], h, f[i]);
+  }
+  for (int b = 0; b < m.nbranch; ++b) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { Islot[b].A[k] = SS(0); Islot[b].D[k] = SS(0); fslot[b].v[k] = S(0); }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Islot[b].B[k] = SS(0);
   }
   // pass 2 (AbaLocalConventionBackwardStep, aba.hxx:402-434)
+  Sym6<SS> Icar;
+  M6<S> fcar;
   for (int i = m.nj - 1; i > 0; --i) {
     const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    X3<S> X;
+    transform(i, X);
+    Iner<S> Y;
+    load_inertia(m, i, Y);
+    Sym6<SS> Ia;
+    iner_to_sym6(Y, Ia);
+    M6<S> vJ, c, h, f;
+    joint_motion(jt, v, iv, vJ);
+    cross_motion(vel[i], vJ, c);
+    iner_mul(Y, vel[i], h);
+    cross_force(vel[i], h, f);
+    if (i + 1 < m.nj && m.parent[i + 1] == i) {  // first child's contribution, carried
+      sym6_add(Ia, Icar);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f.v[k] += fcar.v[k];
+    }
+    const int bs = m.bslot[i];
+    if (bs >= 0) {  // the other children's contributions
+      sym6_add(Ia, Islot[bs]);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f.v[k] += fslot[bs].v[k];
+    }
     if (jt == JT_FF) {  // root only: no parent update
       SS StU[36], Ifull[36];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         SS col[6];
-        sym6_col(Ia[i], k, col);
+        sym6_col(Ia, k, col);
 #pragma unroll
         for (int r = 0; r < 6; ++r) Ifull[6 * r + k] = col[r];
       }
@@ -178,7 +234,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         StU[7 * k] += SS(arm[iv + k]);
-        u6[k] = SS(tau[iv + k]) - SS(f[i].v[k]);
+        u6[k] = SS(tau[iv + k]) - SS(f.v[k]);
       }
       llt_inverse<SS, 6>(StU, D6);
 #pragma unroll
@@ -193,45 +249,56 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       continue;
     }
     const int ax = jt - JT_RX;
-    const SS u = SS(tau[iv]) - SS(f[i].v[3 + ax]);
-    SS U[6];
-    sym6_col(Ia[i], 3 + ax, U);
+    const SS u = SS(tau[iv]) - SS(f.v[3 + ax]);
+    SS U[6], UD[6];
+    sym6_col(Ia, 3 + ax, U);
     const SS Dinv = SS(1) / (U[3 + ax] + SS(arm[iv]));
 #pragma unroll
-    for (int k = 0; k < 6; ++k) UD[i][k] = U[k] * Dinv;
-    Dv[i] = Dinv;
-    uu[i] = u;
+    for (int k = 0; k < 6; ++k) {
+      UD[k] = U[k] * Dinv;
+      UDs[i][k] = S(UD[k]);
+    }
+    du[i] = Dinv * u;
     if (p > 0) {
-      sym6_rank1_sub(Ia[i], U, UD[i]);
+      sym6_rank1_sub(Ia, U, UD);
       Sym6<S> Iaf, Ip;
-      sym6_convert(Ia[i], Iaf);
+      sym6_convert(Ia, Iaf);
       S t6[6];
-      sym6_mv(Iaf, c[i].v, t6);
+      sym6_mv(Iaf, c.v, t6);
       M6<S> pa, fp;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) pa.v[k] = f[i].v[k] + (t6[k] + S(UD[i][k] * u));
-      sym6_transform(Iaf, X[i], Ip);
-      sym6_add(Ia[p], Ip);
-      act_force(X[i], pa, fp);
+      for (int k = 0; k < 6; ++k) pa.v[k] = f.v[k] + (t6[k] + S(UD[k] * u));
+      sym6_transform(Iaf, X, Ip);
+      act_force(X, pa, fp);
+      if (p == i - 1) {  // i is the first child of p: processed next
+        sym6_convert(Ip, Icar);
+        fcar = fp;
+      } else {
+        const int pb = m.bslot[p];
+        sym6_add(Islot[pb], Ip);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) f[p].v[k] += fp.v[k];
+        for (int k = 0; k < 6; ++k) fslot[pb].v[k] += fp.v[k];
+      }
     }
   }
   // pass 3 (AbaLocalConventionForwardStep2, aba.hxx:437-468)
-  M6<S> acc[CAP];
+  M6<S> acar;
   for (int i = 1; i < m.nj; ++i) {
     const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
-    M6<S> a;
-    if (p > 0) {
-      actinv_motion(X[i], acc[p], a);
+    X3<S> X;
+    transform(i, X);
+    M6<S> ap, a, vJ, c;
+    if (p == 0) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) ap.v[k] = -g[k];
     } else {
-      M6<S> mg;
-#pragma unroll
-      for (int k = 0; k < 6; ++k) mg.v[k] = -g[k];
-      actinv_motion(X[i], mg, a);
+      ap = (p == i - 1) ? acar : aslot[m.bslot[p]];
     }
+    actinv_motion(X, ap, a);
+    joint_motion(jt, v, iv, vJ);
+    cross_motion(vel[i], vJ, c);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) a.v[k] += c[i].v[k];
+    for (int k = 0; k < 6; ++k) a.v[k] += c.v[k];
     if (jt == JT_FF) {
       SS dd[6];
 #pragma unroll
@@ -249,14 +316,16 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       for (int r = 0; r < 6; ++r) a.v[r] += S(dd[r]);
     } else {
       const int ax = jt - JT_RX;
-      SS w = UD[i][0] * SS(a.v[0]);
+      SS w = SS(UDs[i][0]) * SS(a.v[0]);
 #pragma unroll
-      for (int k = 1; k < 6; ++k) w += UD[i][k] * SS(a.v[k]);
-      const SS dd = Dv[i] * uu[i] - w;
+      for (int k = 1; k < 6; ++k) w += SS(UDs[i][k]) * SS(a.v[k]);
+      const SS dd = du[i] - w;
       ddq[iv] = double(dd);
       a.v[3 + ax] += S(dd);
     }
-    acc[i] = a;
+    const int bs = m.bslot[i];
+    if (bs >= 0) aslot[bs] = a;
+    acar = a;
   }
 }
 

@@ -7,7 +7,10 @@
 // inertias (FP64 and FP32 copies), per dof armature / parents_fromRow /
 // nvSubtree_fromRow, and for the batched products -Minv*X the per-column list
 // of rows that can be non-zero (ancestor and subtree dofs), and the Fcrb
-// slot of every joint for the Minv recursion of the ABA derivatives.
+// slot of every joint for the Minv recursion of the ABA derivatives, and the
+// branch slot of every joint with two or more children (-1 otherwise): the
+// sweeps carry a joint's accumulators in registers to its first child / from
+// its first child and keep them in a branch slot only where the tree forks.
 #pragma once
 
 #include "gb_spatial.cuh"
@@ -21,7 +24,7 @@ struct BlobHeader {
   int max_depth, has_ff, n_rel, nslot;
   int o_parent, o_jtype, o_idxq, o_idxv, o_nvsub, o_depth, o_pfr, o_nsfr;
   int o_place_d, o_iner_d, o_arm_d, o_place_f, o_iner_f, o_arm_f, o_rel_off, o_rel_list;
-  int o_slot, o_dofj, pad2, pad3;
+  int o_slot, o_dofj, o_bslot, nbranch;
   double grav_d[6];
   float grav_f[6];
   float padf[2];
@@ -30,7 +33,8 @@ static_assert(sizeof(BlobHeader) % 16 == 0, "blob header must keep 16-byte align
 
 struct MView {
   int nj, nq, nv, max_depth, has_ff, nslot;
-  const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint;
+  const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint, *bslot;
+  int nbranch;
   const double *place_d, *iner_d, *arm_d, *grav_d;
   const float *place_f, *iner_f, *arm_f, *grav_f;
 };
@@ -51,6 +55,8 @@ GB_HD MView make_view(const unsigned char* base) {
   m.rel_list = reinterpret_cast<const int*>(base + h->o_rel_list);
   m.slot = reinterpret_cast<const int*>(base + h->o_slot);
   m.dof_joint = reinterpret_cast<const int*>(base + h->o_dofj);
+  m.bslot = reinterpret_cast<const int*>(base + h->o_bslot);
+  m.nbranch = h->nbranch;
   m.place_d = reinterpret_cast<const double*>(base + h->o_place_d);
   m.iner_d = reinterpret_cast<const double*>(base + h->o_iner_d);
   m.arm_d = reinterpret_cast<const double*>(base + h->o_arm_d);

@@ -132,7 +132,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   auto take = [&](size_t bytes) { const size_t o = off; off = align16(off + bytes); return (int)o; };
   h.o_parent = take(4 * nj); h.o_jtype = take(4 * nj); h.o_idxq = take(4 * nj); h.o_idxv = take(4 * nj);
   h.o_nvsub = take(4 * nj); h.o_depth = take(4 * nj); h.o_pfr = take(4 * nv); h.o_nsfr = take(4 * nv);
-  h.o_rel_off = take(4 * (nv + 1)); h.o_rel_list = take(4 * M->rel_list.size() + 4); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv);
+  h.o_rel_off = take(4 * (nv + 1)); h.o_rel_list = take(4 * M->rel_list.size() + 4); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv); h.o_bslot = take(4 * nj);
   h.o_place_d = take(8 * 12 * nj); h.o_iner_d = take(8 * 10 * nj); h.o_arm_d = take(8 * nv);
   h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
   h.bytes = (int)off;
@@ -152,6 +152,15 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   for (int i = 1; i < nj; ++i)
     for (int r = 0; r < M->nvs[i]; ++r) dofj[M->idx_v[i] + r] = i;
   put_i(h.o_dofj, dofj);
+  // branch slots: joints with two or more children
+  std::vector<int> nchild(nj, 0), bslot(nj, -1);
+  for (int i = 1; i < nj; ++i) ++nchild[M->parents[i]];
+  int nb = 0;
+  for (int i = 1; i < nj; ++i)
+    if (nchild[i] >= 2) bslot[i] = nb++;
+  h.nbranch = nb;
+  std::memcpy(b, &h, sizeof(h));
+  put_i(h.o_bslot, bslot);
   put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);
   put_f(h.o_place_f, M->placement); put_f(h.o_iner_f, M->inertia); put_f(h.o_arm_f, M->armature);
   M->blob_bytes = (int)off;

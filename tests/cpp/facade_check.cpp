@@ -1,0 +1,59 @@
+// Test program for the C++ facade (include/pinocchio_gb300.hpp): builds a
+// 3-joint chain, runs rneaInParallel / abaInParallel on host column-major
+// matrices and prints the max |ABA(RNEA(a)) - a|.  A minimal column-major
+// matrix type stands in for Eigen::MatrixXd (same rows/cols/data interface).
+#include <cmath>
+#include <cstdio>
+#include <stdexcept>
+#include <vector>
+
+#include "../../include/pinocchio_gb300.hpp"
+
+struct Mat {
+  long r, c;
+  std::vector<double> d;
+  Mat(long rows, long cols) : r(rows), c(cols), d(rows * cols, 0.0) {}
+  long rows() const { return r; }
+  long cols() const { return c; }
+  const double* data() const { return d.data(); }
+  double* data() { return d.data(); }
+};
+
+int main() {
+  pinocchio_gb300::ModelTables t;
+  t.parents = {0, 0, 1, 2};
+  t.jtype = {GB_JOINT_NONE, GB_JOINT_RZ, GB_JOINT_RY, GB_JOINT_RX};
+  t.placement.assign(4 * 12, 0.0);
+  t.inertia.assign(4 * 10, 0.0);
+  for (int i = 0; i < 4; ++i) {
+    double* P = &t.placement[12 * i];
+    P[0] = P[4] = P[8] = 1.0;
+    P[11] = i > 0 ? 0.25 : 0.0;
+    double* Y = &t.inertia[10 * i];
+    if (i > 0) { Y[0] = 1.0 + i; Y[3] = 0.1; Y[4] = 0.02; Y[6] = 0.03; Y[9] = 0.04; }
+  }
+  try {
+    pinocchio_gb300::Model model(t);
+    pinocchio_gb300::ModelPool pool(model, 4);
+    const long B = 257;
+    Mat q(model.nq, B), v(model.nv, B), a(model.nv, B), tau(model.nv, B), a2(model.nv, B);
+    for (long k = 0; k < model.nq * B; ++k) q.d[k] = std::sin(0.37 * k);
+    for (long k = 0; k < model.nv * B; ++k) { v.d[k] = std::cos(0.11 * k); a.d[k] = std::sin(0.23 * k + 1.0); }
+    pinocchio_gb300::rneaInParallel(4, pool, q, v, a, tau);
+    pinocchio_gb300::abaInParallel(4, pool, q, v, tau, a2);
+    double err = 0.0;
+    for (long k = 0; k < model.nv * B; ++k) err = std::fmax(err, std::fabs(a2.d[k] - a.d[k]));
+    std::printf("roundtrip_max_abs_err %.3e\n", err);
+    try {
+      pinocchio_gb300::rneaInParallel(5, pool, q, v, a, tau);
+      std::printf("expected an exception\n");
+      return 2;
+    } catch (const std::invalid_argument& e) {
+      std::printf("pool_check_ok %s\n", e.what());
+    }
+    return err < 1e-10 ? 0 : 1;
+  } catch (const std::exception& e) {
+    std::printf("error %s\n", e.what());
+    return 3;
+  }
+}
