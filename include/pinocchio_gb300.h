@@ -109,6 +109,21 @@ int gb_aba_derivatives(const gb_model* model, int precision, int layout, long ba
                        const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                        double* ddq, void* stream);
 
+/* The batched ABA derivatives of gb_aba_derivatives, computed without any
+ * device allocation: no counterpart in the reference (whose algorithms never
+ * allocate on their own).  For callers that must not allocate -- real-time
+ * control loops, code running while a stream is captured into a CUDA graph,
+ * plugins whose host application owns every device allocation -- the
+ * workspace is a fixed 64 MiB device array inside the library (held by every
+ * GPU that loads it until exit) instead of a cudaMallocAsync block.  Batches
+ * whose workspace exceeds it (~1000 configurations of the 32-dof humanoid) are
+ * rejected with GB_ERR_SIZE.  The first call on a device resolves the array's
+ * address, so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+int gb_aba_derivatives_noalloc(const gb_model* model, int precision, int layout, long batch, const double* q,
+                               const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
+                               double* ddq, void* stream);
+
 /* qout = integrate(model, q, v) (reference algorithm/joint-configuration.hpp:41-80;
  * free-flyer: multibody/liegroup/special-euclidean.hpp:660-699), always FP64. */
 int gb_integrate(const gb_model* model, int layout, long batch, const double* q, const double* v, double* qout,

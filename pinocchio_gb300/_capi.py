@@ -31,6 +31,7 @@ EXPORTS = (
     "gb_crba",
     "gb_rnea_derivatives",
     "gb_aba_derivatives",
+    "gb_aba_derivatives_noalloc",
     "gb_integrate",
     "gb_pool_create",
     "gb_pool_destroy",
@@ -102,6 +103,7 @@ def lib():
         L.gb_crba.argtypes = [vp, i, i, i, i, l, vp, vp, vp, vp, vp]
         L.gb_rnea_derivatives.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_aba_derivatives_noalloc.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
         L.gb_pool_create.argtypes = [vp, l, C.POINTER(vp)]
         L.gb_pool_destroy.argtypes = [vp]

@@ -235,6 +235,42 @@ int check_gravity(const gb_model* M) {
 }
 
 }  // namespace
+
+// The ABA-derivative kernels on a workspace the caller provides (no allocation):
+// bytes needed per configuration, and the launch itself.
+size_t aba_derivs_workspace_bytes(const gb_model* M, int precision) {
+  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
+  const size_t s = precision == GB_FP64 ? sizeof(double) : sizeof(gb::dfloat);
+  return sizeof(double) * (size_t)L.nSS + s * (size_t)L.nS;
+}
+
+int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
+                                   Arr Minv, Arr ddq, void* ws, cudaStream_t st) {
+  if (check_gravity(M) != GB_OK) return GB_ERR_GRAVITY;
+  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
+  const long grid = (B + kThreads - 1) / kThreads;
+  const size_t bSS = sizeof(double) * (size_t)L.nSS * B;
+  double* wsSS = static_cast<double*>(ws);
+  if (precision == GB_FP64) {
+    double* wsS = reinterpret_cast<double*>(static_cast<char*>(ws) + bSS);
+    int rc = blob_smem(M, (const void*)k_aba_derivs_sweeps<double, double>, "k_aba_derivs_sweeps");
+    if (rc != GB_OK) return rc;
+    k_aba_derivs_sweeps<double, double><<<(unsigned)grid, kThreads, M->blob_bytes, st>>>(
+        M->d_blob, M->blob_bytes, B, L, wsS, wsSS, q, v, tau, Minv, ddq);
+    rc = cuda_error(cudaGetLastError(), "k_aba_derivs_sweeps");
+    if (rc != GB_OK) return rc;
+    return launch_minv_products<double, double>(M, B, Minv, wsS, L, dq, dv, st);
+  }
+  gb::dfloat* wsS = reinterpret_cast<gb::dfloat*>(static_cast<char*>(ws) + bSS);
+  int rc = blob_smem(M, (const void*)k_aba_derivs_sweeps<gb::dfloat, double>, "k_aba_derivs_sweeps");
+  if (rc != GB_OK) return rc;
+  k_aba_derivs_sweeps<gb::dfloat, double><<<(unsigned)grid, kThreads, M->blob_bytes, st>>>(
+      M->d_blob, M->blob_bytes, B, L, wsS, wsSS, q, v, tau, Minv, ddq);
+  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_sweeps");
+  if (rc != GB_OK) return rc;
+  return launch_minv_products<float, gb::dfloat>(M, B, Minv, wsS, L, dq, dv, st);
+}
+
 }  // namespace gbi
 
 #define GB_TRY(x)                   \
