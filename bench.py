@@ -44,6 +44,9 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--only", choices=["rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives"], default=None,
+                   help="time one batched call on the humanoid (for profiling), print its timing and exit")
+    p.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     return p.parse_args()
 
 
@@ -455,8 +458,46 @@ class _Null:
         return False
 
 
+def run_only(args):
+    """Warm-up + timed repetitions of one batched call (used for ncu captures)."""
+    import ctypes
+
+    import torch
+
+    import pinocchio_gb300 as pg
+    from pinocchio_gb300 import sample_models as sm
+
+    model = sm.humanoid32(1)
+    B = args.batch
+    q, v, x = sm.random_inputs(model, B, 0)
+    qd, vd, xd = (torch.from_numpy(a).cuda() for a in (q, v, 10.0 * x))
+    data = pg.createData(model, args.precision)
+    fn = {
+        "rnea": lambda: pg.rnea(model, data, qd, vd, xd),
+        "aba": lambda: pg.aba(model, data, qd, vd, xd),
+        "crba": lambda: pg.crba(model, data, qd),
+        "rnea_derivatives": lambda: pg.computeRNEADerivatives(model, data, qd, vd, xd),
+        "aba_derivatives": lambda: pg.computeABADerivatives(model, data, qd, vd, xd),
+    }[args.only]
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.steps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / max(1, args.steps)
+    print(json.dumps({"only": args.only, "precision": args.precision, "batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}))
+    del ctypes
+
+
 def main():
     args = parse()
+    if args.only:
+        run_only(args)
+        return
     world, rank, local, dist = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -46,6 +46,8 @@ enum { GB_LOCAL = 0, GB_WORLD = 1 };              /* reference multibody/fwd.hpp
 enum { GB_LAYOUT_INSTANCE = 0, GB_LAYOUT_SOA = 1 };
 enum { GB_JOINT_NONE = 0, GB_JOINT_RX = 1, GB_JOINT_RY = 2, GB_JOINT_RZ = 3, GB_JOINT_FREEFLYER = 4 };
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
+/* functions of a heterogeneous batch task / of a launch setting */
+enum { GB_FUNC_RNEA = 0, GB_FUNC_ABA = 1, GB_FUNC_CRBA = 2, GB_FUNC_RNEA_DERIVATIVES = 3, GB_FUNC_ABA_DERIVATIVES = 4 };
 
 typedef struct gb_model gb_model;
 typedef struct gb_pool gb_pool;
@@ -128,6 +130,30 @@ int gb_aba_derivatives_noalloc(const gb_model* model, int precision, int layout,
  * free-flyer: multibody/liegroup/special-euclidean.hpp:660-699), always FP64. */
 int gb_integrate(const gb_model* model, int layout, long batch, const double* q, const double* v, double* qout,
                  void* stream);
+
+/* One task of a heterogeneous batch: `batch` configurations of `model`,
+ * GB_LAYOUT_INSTANCE device arrays; function GB_FUNC_RNEA (x = a, out = tau)
+ * or GB_FUNC_ABA (x = tau, out = ddq, LOCAL convention). */
+typedef struct {
+  const gb_model* model;
+  int function;
+  long batch;
+  const double* q;
+  const double* v;
+  const double* x;
+  double* out;
+} gb_task;
+
+/* Many configurations over several models in one persistent launch: the
+ * batch of rneaInParallel / abaInParallel (algorithm/parallel/{rnea,aba}.hpp)
+ * generalised to several models.  At most 16 tasks; threads_per_block 0
+ * selects the default (128).  The launch allocates nothing, so it can be
+ * captured in a CUDA graph. */
+int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, int threads_per_block, void* stream);
+
+/* Launch setting chosen by the autotuner for one model and function:
+ * configurations per CTA (32, 64, 96 or 128; default 128). */
+int gb_model_set_launch(gb_model* model, int function, int threads_per_block);
 
 /* ModelPool (reference multibody/pool/model.hpp:19-165): `size` nominal
  * per-thread slots; the GPU needs one model copy only, the size is kept for

@@ -19,6 +19,7 @@ GB_FP64, GB_MIXED = 0, 1
 GB_LOCAL, GB_WORLD = 0, 1
 GB_LAYOUT_INSTANCE, GB_LAYOUT_SOA = 0, 1
 GB_MATRIX_UPPER, GB_MATRIX_SYMMETRIC = 0, 1
+GB_FUNC_RNEA, GB_FUNC_ABA, GB_FUNC_CRBA, GB_FUNC_RNEA_DERIVATIVES, GB_FUNC_ABA_DERIVATIVES = range(5)
 
 # every symbol declared in include/pinocchio_gb300.h, in declaration order
 EXPORTS = (
@@ -33,6 +34,8 @@ EXPORTS = (
     "gb_aba_derivatives",
     "gb_aba_derivatives_noalloc",
     "gb_integrate",
+    "gb_batch_multi",
+    "gb_model_set_launch",
     "gb_pool_create",
     "gb_pool_destroy",
     "gb_pool_size",
@@ -46,6 +49,18 @@ class GBError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"[{code}] {msg}")
         self.code = code
+
+
+class Task(C.Structure):
+    _fields_ = [
+        ("model", C.c_void_p),
+        ("function", C.c_int),
+        ("batch", C.c_long),
+        ("q", C.c_void_p),
+        ("v", C.c_void_p),
+        ("x", C.c_void_p),
+        ("out", C.c_void_p),
+    ]
 
 
 class ModelDesc(C.Structure):
@@ -105,6 +120,8 @@ def lib():
         L.gb_aba_derivatives.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives_noalloc.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
+        L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]
+        L.gb_model_set_launch.argtypes = [vp, i, i]
         L.gb_pool_create.argtypes = [vp, l, C.POINTER(vp)]
         L.gb_pool_destroy.argtypes = [vp]
         L.gb_pool_size.argtypes = [vp, C.POINTER(l)]

@@ -288,3 +288,64 @@ def rneaInParallel(num_threads: int, pool: ModelPool, q, v, a, tau=None):
 def abaInParallel(num_threads: int, pool: ModelPool, q, v, tau, a=None):
     """Batch ABA over columns, WORLD convention (reference algorithm/parallel/aba.hpp:40-84)."""
     return _in_parallel(_capi.lib().gb_aba_in_parallel, num_threads, pool, q, v, tau, a, ("q", "v", "tau"))
+
+
+# ------------------------------------------------------------------------------------------
+# heterogeneous batch: several models, RNEA / ABA tasks, one persistent launch
+# ------------------------------------------------------------------------------------------
+_FUNC = {"rnea": _capi.GB_FUNC_RNEA, "aba": _capi.GB_FUNC_ABA}
+
+
+class MultiBatch:
+    """RNEA / ABA tasks over several models evaluated by one persistent launch (gb_batch_multi).
+
+    ``tasks`` is a list of ``(data, function, q, v, x)`` with ``function`` in
+    {"rnea", "aba"} and CUDA float64 tensors of shape (batch, nq) / (batch, nv);
+    outputs are allocated once.  ``run()`` launches on the current stream;
+    ``capture()`` records the launch into a CUDA graph that ``replay()`` re-runs
+    (the launch allocates nothing).
+    """
+
+    def __init__(self, tasks, precision: str = "fp64", threads_per_block: int = 0):
+        torch = _torch()
+        if len(tasks) > 16:
+            raise ValueError("at most 16 tasks per launch")
+        self.precision = precision
+        self.threads_per_block = int(threads_per_block)
+        self._keep = []
+        self.outputs = []
+        arr = (_capi.Task * len(tasks))()
+        for k, (data, function, q, v, x) in enumerate(tasks):
+            m = data.model
+            q, v, x = (t.contiguous() for t in (q, v, x))
+            out = torch.empty((q.shape[0], m.nv), dtype=torch.float64, device=q.device)
+            self._keep += [q, v, x, out, data]
+            self.outputs.append(out)
+            arr[k].model = data.dev.h.value
+            arr[k].function = _FUNC[function]
+            arr[k].batch = q.shape[0]
+            arr[k].q, arr[k].v, arr[k].x, arr[k].out = (t.data_ptr() for t in (q, v, x, out))
+        self._tasks = arr
+        self._graph = None
+
+    def run(self):
+        _capi.check(
+            _capi.lib().gb_batch_multi(self._tasks, len(self._tasks), _PREC[self.precision], self.threads_per_block, _stream_ptr())
+        )
+        return self.outputs
+
+    def capture(self):
+        torch = _torch()
+        self.run()  # warm-up outside the capture (sets kernel attributes)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run()
+        self._graph = g
+        return g
+
+    def replay(self):
+        if self._graph is None:
+            self.capture()
+        self._graph.replay()
+        return self.outputs

@@ -1,0 +1,119 @@
+"""Launch autotuner: picks, per model and function, the configurations per CTA.
+
+Every batched entry point evaluates one configuration per thread; the free
+launch parameter is how many configurations share a CTA (and so the model
+tables staged in its shared memory): small CTAs spread a small batch over
+more SMs, large ones amortise the staging.  ``tune`` times the candidates with
+CUDA events on the given batch, applies the fastest with
+``gb_model_set_launch`` and records it in a JSON cache (keyed by GPU name,
+model tables, function, precision and batch size) so that later processes
+reuse it without timing again.  The heterogeneous launch is tuned the same
+way over its threads_per_block argument (``tune_multi``).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+
+import numpy as np
+
+from . import _capi, api
+from . import sample_models as sm
+
+CANDIDATES = (32, 64, 96, 128)
+CACHE_PATH = os.environ.get(
+    "PINOCCHIO_GB300_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "pinocchio_gb300", "autotune.json")
+)
+_FUNCS = {
+    "rnea": _capi.GB_FUNC_RNEA,
+    "aba": _capi.GB_FUNC_ABA,
+    "crba": _capi.GB_FUNC_CRBA,
+    "rnea_derivatives": _capi.GB_FUNC_RNEA_DERIVATIVES,
+    "aba_derivatives": _capi.GB_FUNC_ABA_DERIVATIVES,
+}
+
+
+def model_key(model) -> str:
+    h = hashlib.sha1()
+    for k, v in sorted(model.tables().items()):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(v).tobytes())
+    return h.hexdigest()[:16]
+
+
+def _load():
+    try:
+        return json.load(open(CACHE_PATH))
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(cache):
+    try:
+        os.makedirs(os.path.dirname(CACHE_PATH), exist_ok=True)
+        json.dump(cache, open(CACHE_PATH, "w"), indent=1, sort_keys=True)
+    except OSError:
+        pass
+
+
+def _time(fn, reps=5):
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives"), batch=16384,
+         candidates=CANDIDATES, use_cache=True):
+    """Tune ``data``'s device model; returns {function: (threads_per_block, ms)}."""
+    import torch
+
+    dev = torch.cuda.get_device_name()
+    key = f"{dev}|{model_key(model)}|{data.precision}|{batch}"
+    cache = _load() if use_cache else {}
+    q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, batch, 0))
+    calls = {
+        "rnea": lambda: api.rnea(model, data, q, v, x),
+        "aba": lambda: api.aba(model, data, q, v, x),
+        "crba": lambda: api.crba(model, data, q),
+        "rnea_derivatives": lambda: api.computeRNEADerivatives(model, data, q, v, x),
+        "aba_derivatives": lambda: api.computeABADerivatives(model, data, q, v, x),
+    }
+    result = {}
+    for f in functions:
+        ck = f"{key}|{f}"
+        if ck in cache:
+            tpb, ms = cache[ck]
+        else:
+            best = None
+            for tpb in candidates:
+                _capi.check(_capi.lib().gb_model_set_launch(data.dev.h, _FUNCS[f], tpb))
+                ms = _time(calls[f])
+                if best is None or ms < best[1]:
+                    best = (tpb, ms)
+            tpb, ms = best
+            cache[ck] = [tpb, ms]
+        _capi.check(_capi.lib().gb_model_set_launch(data.dev.h, _FUNCS[f], int(tpb)))
+        result[f] = (int(tpb), float(ms))
+    if use_cache:
+        _save(cache)
+    return result
+
+
+def tune_multi(tasks, precision="fp64", candidates=(64, 128, 256)):
+    """Best threads_per_block for a heterogeneous batch (MultiBatch); returns (tpb, ms)."""
+    best = None
+    for tpb in candidates:
+        mb = api.MultiBatch(tasks, precision, tpb)
+        ms = _time(mb.run)
+        if best is None or ms < best[1]:
+            best = (tpb, ms)
+    return best

@@ -137,6 +137,15 @@ int gb_integrate(const gb_model* M, int layout, long B, const double* q, const d
                                gbi::arr(qout, layout, B, M->nq), (cudaStream_t)stream);
 }
 
+int gb_model_set_launch(gb_model* M, int function, int threads_per_block) {
+  if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
+  if (function < GB_FUNC_RNEA || function > GB_FUNC_ABA_DERIVATIVES) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown function");
+  if (threads_per_block != 32 && threads_per_block != 64 && threads_per_block != 96 && threads_per_block != 128)
+    return set_error(GB_ERR_INVALID_ARGUMENT, "threads_per_block must be 32, 64, 96 or 128");
+  M->tpb[function] = threads_per_block;
+  return GB_OK;
+}
+
 // ---- ModelPool and the *InParallel entry points ------------------------------------------
 int gb_pool_create(const gb_model* M, long size, gb_pool** out) {
   if (!M || !out) return set_error(GB_ERR_INVALID_ARGUMENT, "model/out is NULL");

@@ -44,36 +44,68 @@ __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* b
                          tau.p ? &to : nullptr, symmetric);
 }
 
+// The ABA-derivative sweeps as three kernels (passes 1-2, pass 3, pass 4), so
+// that each keeps fewer values live than one fused kernel would (register use
+// bounds the number of resident warps).  The workspace carries everything
+// between them.
 template <class S, class SS>
-__global__ void __launch_bounds__(kThreads) k_aba_derivs_sweeps(const unsigned char* blob, int bytes, long B,
-                                                                gb::DerivLayout L, S* wsS, SS* wsSS, Arr q, Arr v,
-                                                                Arr tau, Arr Minv, Arr ddq) {
+__global__ void __launch_bounds__(kThreads) k_aba_derivs_pass12(const unsigned char* blob, int bytes, long B,
+                                                                gb::DerivLayout L, SS* wsSS, Arr q, Arr v, Arr tau,
+                                                                Arr Minv) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
-  const gb::Ws<S> w{wsS + b, B};
-  const gb::Ws<SS> z{wsSS + b, B};
+  gb::aba_derivs_pass12<S, SS>(m, L, gb::Ws<SS>{wsSS + b, B}, in_at(q, b), in_at(v, b), in_at(tau, b),
+                               out_at(Minv, b));
+}
+
+template <class S, class SS>
+__global__ void __launch_bounds__(kThreads) k_aba_derivs_pass3(const unsigned char* blob, int bytes, long B,
+                                                               gb::DerivLayout L, S* wsS, SS* wsSS, Arr v, Arr Minv,
+                                                               Arr ddq) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
   const gb::Out dd = out_at(ddq, b);
-  gb::aba_derivs_sweeps<S, SS>(m, L, m.slot, w, z, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(Minv, b),
-                               ddq.p ? &dd : nullptr);
+  gb::aba_derivs_pass3<S, SS>(m, L, m.slot, gb::Ws<S>{wsS + b, B}, gb::Ws<SS>{wsSS + b, B}, in_at(v, b),
+                              out_at(Minv, b), ddq.p ? &dd : nullptr);
+}
+
+template <class S, class SS, class P>
+__global__ void __launch_bounds__(kThreads) k_aba_derivs_pass4(const unsigned char* blob, int bytes, long B,
+                                                               gb::DerivLayout L, S* wsS, SS* wsSS, P* wsP,
+                                                               Arr Minv) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  gb::aba_derivs_pass4<S, SS, P>(m, L, gb::Ws<S>{wsS + b, B}, gb::Ws<SS>{wsSS + b, B}, gb::Ws<P>{wsP + b, B},
+                                 out_at(Minv, b));
 }
 
 // out_m = -Minv * X_m for the two matrices X_0 = dtau_dq, X_1 = dtau_dv of G
-// consecutive configurations per iteration.  smem: Minv[G][nv*nv] then
-// X[G][NM][nv*nv] (scalar S).  NM = number of the two products done per pass.
+// consecutive configurations per iteration.  smem: Minv[G][nv*nv], then
+// X[G][NM][nv*nv] (scalar S), then the column-group tables.  NM = number of the
+// two products done per pass.  A warp owns one (configuration, matrix, column
+// group); its lanes own rows (lane + 32*chunk); for every row k that can be
+// non-zero in the group's columns it loads one Minv row segment (lane-contiguous,
+// Minv symmetric) and the group's <= 8 entries of X's row k (broadcast) and does
+// up to 8 FMAs per lane.  The result overwrites the group's columns of X in place.
 template <class S, class W>
 __global__ void k_minv_products(const unsigned char* blob, int bytes, long B, int G, int m0, int NM, Arr Minv,
                                 const W* ws, long dtq, long dtv, Arr out0, Arr out1) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(blob);
-  // the model blob is only needed for rel_off / rel_list: read them from global (L1-cached)
-  const int nv = h->nv;
-  const int* rel_off = reinterpret_cast<const int*>(blob + h->o_rel_off);
-  const int* rel_list = reinterpret_cast<const int*>(blob + h->o_rel_list);
+  const int nv = h->nv, ng = h->ngroup, nrel = h->n_grp_rel;
   const int nn = nv * nv;
   S* sM = reinterpret_cast<S*>(smem_raw);
   S* sX = sM + (long)G * nn;
+  int* sgrp = reinterpret_cast<int*>(sX + (long)G * NM * nn);
+  int* srel = sgrp + 4 * ng;
+  for (int t = threadIdx.x; t < 4 * ng; t += blockDim.x) sgrp[t] = reinterpret_cast<const int*>(blob + h->o_grp)[t];
+  for (int t = threadIdx.x; t < nrel; t += blockDim.x) srel[t] = reinterpret_cast<const int*>(blob + h->o_grp_rel)[t];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nwarps = blockDim.x / 32;
   for (long b0 = (long)blockIdx.x * G; b0 < B; b0 += (long)gridDim.x * G) {
     const int g_here = (int)min((long)G, B - b0);
@@ -91,32 +123,44 @@ __global__ void k_minv_products(const unsigned char* blob, int bytes, long B, in
       }
     }
     __syncthreads();
-    for (int task = warp; task < g_here * NM; task += nwarps) {
-      const int g = task / NM, mm = task % NM;
+    const int ntask = g_here * NM * ng;
+    for (int task = warp; task < ntask; task += nwarps) {
+      const int g = task / (NM * ng), rem = task % (NM * ng), mm = rem / ng, gi = rem % ng;
+      const int c0 = sgrp[4 * gi], nc = sgrp[4 * gi + 1], k0 = sgrp[4 * gi + 2], k1 = sgrp[4 * gi + 3];
       const S* Mg = sM + g * nn;
       S* X = sX + (g * NM + mm) * nn;
-      for (int c = 0; c < nv; ++c) {
-        const int k0 = rel_off[c], k1 = rel_off[c + 1];
-        S acc[4] = {S(0), S(0), S(0), S(0)};  // rows lane, lane+32, lane+64, lane+96 (nv <= 128)
-        for (int kk = k0; kk < k1; ++kk) {
-          const int k = rel_list[kk];
-          const S x = X[k * nv + c];
-          const S* Mk = Mg + k * nv;  // Minv symmetric: Minv(r, k) = Minv(k, r)
+      S acc[4][8];
 #pragma unroll
-          for (int ch = 0; ch < 4; ++ch) {
-            const int r = ch * 32 + lane;
-            if (r < nv) acc[ch] += Mk[r] * x;
-          }
-        }
-        __syncwarp();
-        // column c of X is no longer read: store the result column there
+      for (int ch = 0; ch < 4; ++ch)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[ch][c] = S(0);
+      for (int kk = k0; kk < k1; ++kk) {
+        const int k = srel[kk];
+        const S* Xk = X + k * nv + c0;
+        S x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = c < nc ? Xk[c] : S(0);
+        const S* Mk = Mg + k * nv;
 #pragma unroll
         for (int ch = 0; ch < 4; ++ch) {
           const int r = ch * 32 + lane;
-          if (r < nv) X[r * nv + c] = -acc[ch];
+          if (ch * 32 < nv) {
+            const S mr = r < nv ? Mk[r] : S(0);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[ch][c] += mr * x[c];
+          }
         }
-        __syncwarp();
       }
+      __syncwarp();
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const int r = ch * 32 + lane;
+        if (r < nv)
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            if (c < nc) X[r * nv + c0 + c] = -acc[ch][c];
+      }
+      __syncwarp();
     }
     __syncthreads();
     for (int mm = 0; mm < NM; ++mm) {
@@ -166,7 +210,7 @@ template <class S, class W>
 int launch_minv_products(const gb_model* M, long B, Arr Minv, const W* ws, const gb::DerivLayout& L, Arr o0, Arr o1,
                          cudaStream_t st) {
   const long nn = (long)M->nv * M->nv;
-  const long budget = 200 * 1024;
+  const long budget = 190 * 1024;
   int NM = 2;
   long G = budget / (nn * (long)sizeof(S) * (1 + NM));
   if (G < 1) {
@@ -175,8 +219,10 @@ int launch_minv_products(const gb_model* M, long B, Arr Minv, const W* ws, const
   }
   if (G < 1) return set_error(GB_ERR_UNSUPPORTED, "nv too large for the Minv products");
   G = std::min<long>(G, 16);
-  const int threads = 32 * (int)std::min<long>(G * NM, 16);
-  const size_t smem = (size_t)G * nn * sizeof(S) * (1 + NM);
+  const int ngroup = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->ngroup;
+  const int nrel = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->n_grp_rel;
+  const int threads = 32 * (int)std::min<long>(G * NM * ngroup, 16);
+  const size_t smem = (size_t)G * nn * sizeof(S) * (1 + NM) + sizeof(int) * (4 * ngroup + nrel);
   cudaError_t e = cudaFuncSetAttribute(k_minv_products<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "k_minv_products");
   const long grid = std::min<long>((B + G - 1) / G, 152L * 8);
@@ -198,34 +244,60 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   if (rc != GB_OK) return rc;
   rc = blob_smem(M, (const void*)k_rnea_derivs<S>, "k_rnea_derivs");
   if (rc != GB_OK) return rc;
-  const long grid = (B + kThreads - 1) / kThreads;
-  k_rnea_derivs<S><<<(unsigned)grid, kThreads, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L,
+  const int tpb = M->tpb[GB_FUNC_RNEA_DERIVATIVES];
+  const long grid = (B + tpb - 1) / tpb;
+  k_rnea_derivs<S><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L,
                                                                    static_cast<S*>(ws.p), symmetric, q, v, a, dq, dv,
                                                                    Mo, tau);
   return cuda_error(cudaGetLastError(), "k_rnea_derivs");
 }
 
-// S: scalar of the FP32-side derivative passes (dfloat in the mixed kernels),
-// SS: scalar of kinematics / Schur / Minv, P: scalar of the -Minv dtau products
+// Workspace of the ABA derivatives: region SS (FP64: kinematics, Schur, Minv
+// data), region S (the derivative column passes: dfloat in the mixed kernels)
+// and region P (dtau_dq, dtau_dv in the scalar of the -Minv*dtau products).
+template <class S, class SS, class P>
+size_t aba_ws_bytes(const gb::DerivLayout& L, long B) {
+  return (sizeof(SS) * (size_t)L.nSS + sizeof(S) * (size_t)L.nS + sizeof(P) * (size_t)L.nP) * (size_t)B;
+}
+
+template <class S, class SS, class P>
+int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq, void* ws,
+                         cudaStream_t st) {
+  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
+  SS* wsSS = static_cast<SS*>(ws);
+  S* wsS = reinterpret_cast<S*>(static_cast<char*>(ws) + sizeof(SS) * (size_t)L.nSS * B);
+  P* wsP = reinterpret_cast<P*>(reinterpret_cast<char*>(wsS) + sizeof(S) * (size_t)L.nS * B);
+  const int tpb = M->tpb[GB_FUNC_ABA_DERIVATIVES];
+  const long grid = (B + tpb - 1) / tpb;
+  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<S, SS>, "k_aba_derivs_pass12");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, SS>, "k_aba_derivs_pass3");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, SS, P>, "k_aba_derivs_pass4");
+  if (rc != GB_OK) return rc;
+  k_aba_derivs_pass12<S, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsSS, q, v,
+                                                                             tau, Minv);
+  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
+  if (rc != GB_OK) return rc;
+  k_aba_derivs_pass3<S, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS, wsSS,
+                                                                            v, Minv, ddq);
+  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass3");
+  if (rc != GB_OK) return rc;
+  k_aba_derivs_pass4<S, SS, P><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
+                                                                               wsSS, wsP, Minv);
+  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass4");
+  if (rc != GB_OK) return rc;
+  return launch_minv_products<P, P>(M, B, Minv, wsP, L, dq, dv, st);
+}
+
+// S: scalar of the column passes (dfloat in the mixed kernels), SS: scalar of
+// kinematics / Schur / Minv, P: scalar of the -Minv dtau products
 template <class S, class SS, class P>
 int run_aba_derivs(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq,
                    cudaStream_t st) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  const size_t bSS = sizeof(SS) * (size_t)L.nSS * B;
-  const size_t bS = sizeof(S) * (size_t)L.nS * B;
   Workspace ws;
-  int rc = ws_alloc(ws, bSS + bS, st);
+  int rc = ws_alloc(ws, aba_ws_bytes<S, SS, P>(L, B), st);
   if (rc != GB_OK) return rc;
-  SS* wsSS = static_cast<SS*>(ws.p);
-  S* wsS = reinterpret_cast<S*>(static_cast<char*>(ws.p) + bSS);
-  rc = blob_smem(M, (const void*)k_aba_derivs_sweeps<S, SS>, "k_aba_derivs_sweeps");
-  if (rc != GB_OK) return rc;
-  const long grid = (B + kThreads - 1) / kThreads;
-  k_aba_derivs_sweeps<S, SS><<<(unsigned)grid, kThreads, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
-                                                                             wsSS, q, v, tau, Minv, ddq);
-  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_sweeps");
-  if (rc != GB_OK) return rc;
-  return launch_minv_products<P, S>(M, B, Minv, wsS, L, dq, dv, st);
+  return launch_aba_derivs_ws<S, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st);
 }
 
 int check_gravity(const gb_model* M) {
@@ -240,35 +312,14 @@ int check_gravity(const gb_model* M) {
 // bytes needed per configuration, and the launch itself.
 size_t aba_derivs_workspace_bytes(const gb_model* M, int precision) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  const size_t s = precision == GB_FP64 ? sizeof(double) : sizeof(gb::dfloat);
-  return sizeof(double) * (size_t)L.nSS + s * (size_t)L.nS;
+  return precision == GB_FP64 ? aba_ws_bytes<double, double, double>(L, 1) : aba_ws_bytes<gb::dfloat, double, float>(L, 1);
 }
 
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
                                    Arr Minv, Arr ddq, void* ws, cudaStream_t st) {
   if (check_gravity(M) != GB_OK) return GB_ERR_GRAVITY;
-  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  const long grid = (B + kThreads - 1) / kThreads;
-  const size_t bSS = sizeof(double) * (size_t)L.nSS * B;
-  double* wsSS = static_cast<double*>(ws);
-  if (precision == GB_FP64) {
-    double* wsS = reinterpret_cast<double*>(static_cast<char*>(ws) + bSS);
-    int rc = blob_smem(M, (const void*)k_aba_derivs_sweeps<double, double>, "k_aba_derivs_sweeps");
-    if (rc != GB_OK) return rc;
-    k_aba_derivs_sweeps<double, double><<<(unsigned)grid, kThreads, M->blob_bytes, st>>>(
-        M->d_blob, M->blob_bytes, B, L, wsS, wsSS, q, v, tau, Minv, ddq);
-    rc = cuda_error(cudaGetLastError(), "k_aba_derivs_sweeps");
-    if (rc != GB_OK) return rc;
-    return launch_minv_products<double, double>(M, B, Minv, wsS, L, dq, dv, st);
-  }
-  gb::dfloat* wsS = reinterpret_cast<gb::dfloat*>(static_cast<char*>(ws) + bSS);
-  int rc = blob_smem(M, (const void*)k_aba_derivs_sweeps<gb::dfloat, double>, "k_aba_derivs_sweeps");
-  if (rc != GB_OK) return rc;
-  k_aba_derivs_sweeps<gb::dfloat, double><<<(unsigned)grid, kThreads, M->blob_bytes, st>>>(
-      M->d_blob, M->blob_bytes, B, L, wsS, wsSS, q, v, tau, Minv, ddq);
-  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_sweeps");
-  if (rc != GB_OK) return rc;
-  return launch_minv_products<float, gb::dfloat>(M, B, Minv, wsS, L, dq, dv, st);
+  if (precision == GB_FP64) return launch_aba_derivs_ws<double, double, double>(M, B, q, v, tau, dq, dv, Minv, ddq, ws, st);
+  return launch_aba_derivs_ws<gb::dfloat, double, float>(M, B, q, v, tau, dq, dv, Minv, ddq, ws, st);
 }
 
 }  // namespace gbi

@@ -58,8 +58,8 @@ struct DerivLayout {
   int oM, ov, oa, oh, of, oY, J;
   // C (per joint: composite inertia, its variation, force; per dof: column sets)
   int coY, doY, cof, cJ, dVdq, dAdq, dAdv, dFda, dFdq, dFdv, dYtJ;
-  int dtq, dtv;  // nv x nv (ABA only: dtau_dq, dtau_dv feeding -Minv * dtau)
-  int nS;
+  int dtq, dtv;  // nv x nv in region P (ABA only: dtau_dq, dtau_dv feeding -Minv * dtau)
+  int nS, nP;
   // region SS (ABA only): K + Schur / Minv data
   int Ia, U, UD, Dinv, u, F0, Fslot, nslot;
   int nSS;
@@ -80,9 +80,10 @@ inline DerivLayout make_deriv_layout(int nj, int nv, int nslot, bool aba) {
   L.doY = takeS(36 * nj);
   L.dVdq = takeS(6 * nv); L.dAdq = takeS(6 * nv); L.dAdv = takeS(6 * nv);
   L.dFda = takeS(6 * nv); L.dFdq = takeS(6 * nv); L.dFdv = takeS(6 * nv); L.dYtJ = takeS(6 * nv);
-  L.dtq = aba ? takeS(nv * nv) : 0;
-  L.dtv = aba ? takeS(nv * nv) : 0;
   L.nS = oS;
+  L.dtq = 0;
+  L.dtv = aba ? nv * nv : 0;
+  L.nP = aba ? 2 * nv * nv : 0;
   L.Ia = aba ? takeSS(21 * nj) : 0;
   L.U = aba ? takeSS(6 * nv) : 0;
   L.UD = aba ? takeSS(6 * nv) : 0;
@@ -557,12 +558,10 @@ template <class S> GB_HD void shift_operator(const S* M, const S* r, S* O) {
 // between joints by translation (shift_motion / shift_force / shift_operator).
 // ------------------------------------------------------------------------------------------
 template <class S, class SS>
-GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                             const Ws<SS>& z, const In& q, const In& v, const In& tau, const Out& Minv,
-                             const Out* ddq_out) {
+GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<SS>& z, const In& q, const In& v,
+                             const In& tau, const Out& Minv) {
   const int nv = m.nv;
   const double* arm = m.arm_d;
-  const S eps = eps_of<S>();
   // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), in SS
   world_forward<SS>(m, L, z, q, v, nullptr, false);
   for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix()
@@ -669,6 +668,12 @@ GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* sl
       st_sym(p, Ip);
     }
   }
+}
+
+template <class S, class SS>
+GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
+                            const Ws<SS>& z, const In& v, const Out& Minv, const Out* ddq_out) {
+  const int nv = m.nv;
   // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
   // velocity / acceleration recursion runs in SS in floating origins and
   // replaces ov / oa in K; the column sets, link inertia, momentum, force and
@@ -795,10 +800,18 @@ GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* sl
 #pragma unroll
     for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
   }
+}
+
+// P: scalar of the dtau matrices handed to the -Minv*dtau products
+template <class S, class SS, class P>
+GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<SS>& z, const Ws<P>& wp,
+                            const Out& Minv) {
+  const int nv = m.nv;
+  const S eps = eps_of<S>();
   // ---- pass 4: ComputeABADerivativesBackwardStep2 (hxx:273-368), in S, floating
   // origins: a joint's composite oY / doY / of are about its own position; a
   // child adds its contributions moved to the parent's position.
-  for (int k = 0; k < nv * nv; ++k) { w[L.dtq + k] = S(0); w[L.dtv + k] = S(0); }
+  for (int k = 0; k < nv * nv; ++k) { wp[L.dtq + k] = P(0); wp[L.dtv + k] = P(0); }
   auto offset = [&](int a, int b, S* d) {  // t_a - t_b, formed in SS
     for (int k = 0; k < 3; ++k) d[k] = S(z[L.oM + 12 * a + 9 + k] - z[L.oM + 12 * b + 9 + k]);
   };
@@ -840,10 +853,10 @@ GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* sl
         offset(m.dof_joint[c], i, d);
         ld6(w, L.dFdv + 6 * c, x);
         shift_force(x, d, y);
-        w[L.dtv + (iv + r) * nv + c] = dot6(Jr, y);
+        wp[L.dtv + (iv + r) * nv + c] = P(dot6(Jr, y));
         ld6(w, L.dFdq + 6 * c, x);
         shift_force(x, d, y);
-        w[L.dtq + (iv + r) * nv + c] = dot6(Jr, y);
+        wp[L.dtq + (iv + r) * nv + c] = P(dot6(Jr, y));
       }
     }
     for (int k = 0; k < nvj; ++k) {
@@ -870,12 +883,12 @@ GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* sl
           ld6(w, L.dVdq + 6 * j, y);
           shift_motion(x, d, xs);
           shift_motion(y, d, ys);
-          w[L.dtq + (iv + r) * nv + j] = dot6(fa, xs) + dot6(StdY, ys);
+          wp[L.dtq + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
           ld6(w, L.dAdv + 6 * j, x);
           ld6(w, L.cJ + 6 * j, y);
           shift_motion(x, d, xs);
           shift_motion(y, d, ys);
-          w[L.dtv + (iv + r) * nv + j] = dot6(fa, xs) + dot6(StdY, ys);
+          wp[L.dtv + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
         }
       }
       // accumulate into the parent, moved from t_i to t_p
@@ -901,6 +914,15 @@ GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* sl
   // symmetrise Minv (hxx:448-449)
   for (int r = 1; r < nv; ++r)
     for (int c = 0; c < r; ++c) Minv[r * nv + c] = Minv[c * nv + r];
+}
+
+template <class S, class SS, class P>
+GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
+                             const Ws<SS>& z, const Ws<P>& wp, const In& q, const In& v, const In& tau,
+                             const Out& Minv, const Out* ddq_out) {
+  aba_derivs_pass12<S, SS>(m, L, z, q, v, tau, Minv);
+  aba_derivs_pass3<S, SS>(m, L, slot, w, z, v, Minv, ddq_out);
+  aba_derivs_pass4<S, SS, P>(m, L, w, z, wp, Minv);
 }
 
 }  // namespace gb

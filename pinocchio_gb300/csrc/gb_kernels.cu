@@ -83,8 +83,9 @@ int launch_common(const gb_model* M, long B, cudaStream_t st, K kernel, const ch
   do {                                                                                      \
     const int rc__ = launch_common(M, B, st, kernel, #kernel);                              \
     if (rc__ != GB_OK) return rc__;                                                         \
-    const long grid__ = (B + kThreads - 1) / kThreads;                                      \
-    kernel<<<(unsigned)grid__, kThreads, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, __VA_ARGS__); \
+    const int tpb__ = M->tpb[GB_FUNC_ID];                                                   \
+    const long grid__ = (B + tpb__ - 1) / tpb__;                                            \
+    kernel<<<(unsigned)grid__, tpb__, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, __VA_ARGS__); \
     return cuda_error(cudaGetLastError(), #kernel);                                         \
   } while (0)
 
@@ -101,6 +102,7 @@ int launch_common(const gb_model* M, long B, cudaStream_t st, K kernel, const ch
 }  // namespace
 
 int launch_rnea(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_RNEA;
   if (precision == GB_FP64) {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_rnea<double, C>), q, v, a, tau));
   } else {
@@ -109,6 +111,7 @@ int launch_rnea(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, A
 }
 
 int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_ABA;
   if (precision == GB_FP64) {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C>), q, v, tau, ddq));
   } else {
@@ -118,6 +121,7 @@ int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, 
 
 int launch_crba(const gb_model* M, int precision, bool symmetric, long B, Arr q, Arr Mo, Arr U, Arr D,
                 cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_CRBA;
   // the factorisation is FP64 in both precisions, and so is the M it factorises
   if (precision == GB_FP64 || U.p != nullptr) {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_crba<double, C>), symmetric, q, Mo, U, D));
@@ -127,6 +131,7 @@ int launch_crba(const gb_model* M, int precision, bool symmetric, long B, Arr q,
 }
 
 int launch_integrate(const gb_model* M, long B, Arr q, Arr v, Arr qo, cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_RNEA;
   GB_LAUNCH(k_integrate, q, v, qo);
 }
 

@@ -25,6 +25,7 @@ struct BlobHeader {
   int o_parent, o_jtype, o_idxq, o_idxv, o_nvsub, o_depth, o_pfr, o_nsfr;
   int o_place_d, o_iner_d, o_arm_d, o_place_f, o_iner_f, o_arm_f, o_rel_off, o_rel_list;
   int o_slot, o_dofj, o_bslot, nbranch;
+  int o_grp, ngroup, o_grp_rel, n_grp_rel;
   double grav_d[6];
   float grav_f[6];
   float padf[2];
@@ -33,8 +34,8 @@ static_assert(sizeof(BlobHeader) % 16 == 0, "blob header must keep 16-byte align
 
 struct MView {
   int nj, nq, nv, max_depth, has_ff, nslot;
-  const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint, *bslot;
-  int nbranch;
+  const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint, *bslot, *grp, *grp_rel;
+  int nbranch, ngroup;
   const double *place_d, *iner_d, *arm_d, *grav_d;
   const float *place_f, *iner_f, *arm_f, *grav_f;
 };
@@ -57,6 +58,9 @@ GB_HD MView make_view(const unsigned char* base) {
   m.dof_joint = reinterpret_cast<const int*>(base + h->o_dofj);
   m.bslot = reinterpret_cast<const int*>(base + h->o_bslot);
   m.nbranch = h->nbranch;
+  m.grp = reinterpret_cast<const int*>(base + h->o_grp);
+  m.grp_rel = reinterpret_cast<const int*>(base + h->o_grp_rel);
+  m.ngroup = h->ngroup;
   m.place_d = reinterpret_cast<const double*>(base + h->o_place_d);
   m.iner_d = reinterpret_cast<const double*>(base + h->o_iner_d);
   m.arm_d = reinterpret_cast<const double*>(base + h->o_arm_d);

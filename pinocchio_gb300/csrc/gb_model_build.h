@@ -16,6 +16,7 @@ struct gb_model {
   int device = 0;
   std::vector<int> parents, jtype, idx_q, idx_v, nvs, nvsub, depth, pfr, nsfr, rel_off, rel_list, slot;
   int nslot = 0;
+  int tpb[8] = {128, 128, 128, 128, 128, 128, 128, 128};  // configurations per CTA, per GB_FUNC_*
   std::vector<double> placement, inertia, armature;
   double gravity[6];
   std::vector<unsigned char> blob;  // host copy of the device blob
@@ -133,6 +134,20 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.o_parent = take(4 * nj); h.o_jtype = take(4 * nj); h.o_idxq = take(4 * nj); h.o_idxv = take(4 * nj);
   h.o_nvsub = take(4 * nj); h.o_depth = take(4 * nj); h.o_pfr = take(4 * nv); h.o_nsfr = take(4 * nv);
   h.o_rel_off = take(4 * (nv + 1)); h.o_rel_list = take(4 * M->rel_list.size() + 4); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv); h.o_bslot = take(4 * nj);
+  // column groups of the -Minv*dtau products (filled below)
+  std::vector<int> grp, grp_rel;
+  for (int c = 0; c < nv;) {
+    int e = c + 1;
+    auto rows_of = [&](int col) { return std::vector<int>(M->rel_list.begin() + M->rel_off[col], M->rel_list.begin() + M->rel_off[col + 1]); };
+    const std::vector<int> rc = rows_of(c);
+    while (e < nv && e - c < 8 && rows_of(e) == rc) ++e;
+    grp.push_back(c); grp.push_back(e - c); grp.push_back((int)grp_rel.size());
+    grp_rel.insert(grp_rel.end(), rc.begin(), rc.end());
+    grp.push_back((int)grp_rel.size());
+    c = e;
+  }
+  h.ngroup = (int)grp.size() / 4; h.n_grp_rel = (int)grp_rel.size();
+  h.o_grp = take(4 * grp.size()); h.o_grp_rel = take(4 * grp_rel.size() + 4);
   h.o_place_d = take(8 * 12 * nj); h.o_iner_d = take(8 * 10 * nj); h.o_arm_d = take(8 * nv);
   h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
   h.bytes = (int)off;
@@ -161,6 +176,8 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.nbranch = nb;
   std::memcpy(b, &h, sizeof(h));
   put_i(h.o_bslot, bslot);
+  put_i(h.o_grp, grp);
+  put_i(h.o_grp_rel, grp_rel);
   put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);
   put_f(h.o_place_f, M->placement); put_f(h.o_iner_f, M->inertia); put_f(h.o_arm_f, M->armature);
   M->blob_bytes = (int)off;

@@ -115,24 +115,26 @@ template <class S>
 static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const double* q, const double* v,
                             const double* tau, double* dq, double* dv, double* Minv, double* ddq,
                             std::vector<S>& wS, std::vector<double>& wSS) {
+  typedef typename ProductScalar<S>::type P;
   const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
   const int nv = m.nv;
   const long nn = (long)nv * nv;
+  std::vector<P> wP(L.nP);
   const gb::Out dd = out_at(ddq, b, nv);
-  gb::aba_derivs_sweeps<S, double>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<double>{wSS.data(), 1},
-                                   in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv), out_at(Minv, b, nn), &dd);
+  gb::aba_derivs_sweeps<S, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<double>{wSS.data(), 1},
+                                      gb::Ws<P>{wP.data(), 1}, in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv),
+                                      out_at(Minv, b, nn), &dd);
   // -Minv * dtau restricted to the structurally non-zero rows, as the device kernel does
   const double* Mi = Minv + b * nn;
   for (int mm = 0; mm < 2; ++mm) {
-    const S* X = wS.data() + (mm == 0 ? L.dtq : L.dtv);
+    const P* X = wP.data() + (mm == 0 ? L.dtq : L.dtv);
     double* O = (mm == 0 ? dq : dv) + b * nn;
     for (int c = 0; c < nv; ++c)
       for (int r = 0; r < nv; ++r) {
-        typedef typename ProductScalar<S>::type P;
         P acc = P(0);
         for (int kk = M->rel_off[c]; kk < M->rel_off[c + 1]; ++kk) {
           const int k = M->rel_list[kk];
-          acc += P(Mi[k * nv + r]) * P(X[k * nv + c]);
+          acc += P(Mi[k * nv + r]) * X[k * nv + c];
         }
         O[r * nv + c] = -double(acc);
       }

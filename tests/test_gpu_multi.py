@@ -1,0 +1,75 @@
+"""GPU tests of the heterogeneous single-launch batch (RNEA + ABA tasks over the
+four seeded random trees, nv 7 / 12 / 32 (free-flyer) / 60 (free-flyer),
+instances split 40/30/20/10 %), its CUDA-graph capture, and the autotuner."""
+import numpy as np
+import pytest
+
+import pinocchio_gb300 as pg
+from oracle.oracle import LOCAL, OracleModel
+from pinocchio_gb300 import api, autotune
+from pinocchio_gb300 import sample_models as sm
+from util import FP64_TOL, MIXED_TOL, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _tasks(precision, total=4000, seed=0):
+    import torch
+
+    models = sm.heterogeneous_trees(3)
+    shares = (0.4, 0.3, 0.2, 0.1)
+    tasks, ref = [], []
+    for k, (model, share) in enumerate(zip(models, shares)):
+        B = int(total * share)
+        q, v, x = sm.random_inputs(model, B, seed + k)
+        data = pg.createData(model, precision)
+        d = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+        tasks.append((data, "aba", d(q), d(v), d(10.0 * x)))
+        tasks.append((data, "rnea", d(q), d(v), d(x)))
+        ref.append((model, q, v, x))
+    return tasks, ref
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_multi_matches_oracle_and_single_model_calls(precision, tol):
+    import torch
+
+    tasks, ref = _tasks(precision)
+    mb = api.MultiBatch(tasks, precision)
+    outs = [o.cpu().numpy() for o in mb.run()]
+    for k, (model, q, v, x) in enumerate(ref):
+        om = OracleModel(model)
+        assert rel_err(outs[2 * k], om.aba(q, v, 10.0 * x, LOCAL)) < tol
+        assert rel_err(outs[2 * k + 1], om.rnea(q, v, x)) < tol
+        data = tasks[2 * k][0]
+        single = pg.aba(model, data, torch.from_numpy(q).cuda(), torch.from_numpy(v).cuda(), torch.from_numpy(10.0 * x).cuda())
+        assert np.array_equal(single.cpu().numpy(), outs[2 * k])  # same per-instance code
+
+
+def test_multi_graph_replay():
+    tasks, ref = _tasks("mixed", 2000, 7)
+    mb = api.MultiBatch(tasks, "mixed", 64)
+    first = [o.clone() for o in mb.run()]
+    for o in mb.outputs:
+        o.zero_()
+    mb.capture()
+    for o in mb.outputs:
+        o.zero_()
+    mb.replay()
+    for a, b in zip(first, mb.outputs):
+        assert bool((a == b).all())
+
+
+def test_autotuner_keeps_results(tmp_path, monkeypatch):
+    import torch
+
+    monkeypatch.setattr(autotune, "CACHE_PATH", str(tmp_path / "tune.json"))
+    model = sm.humanoid32(1)
+    data = pg.createData(model, "mixed")
+    q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 3000, 2))
+    before = pg.aba(model, data, q, v, x).clone()
+    res = autotune.tune(model, data, functions=("aba", "rnea"), batch=4096)
+    assert set(res) == {"aba", "rnea"} and all(t in autotune.CANDIDATES for t, _ in res.values())
+    assert torch.equal(pg.aba(model, data, q, v, x), before)
+    again = autotune.tune(model, data, functions=("aba", "rnea"), batch=4096)  # served from the cache
+    assert again == {k: (t, ms) for k, (t, ms) in res.items()}
