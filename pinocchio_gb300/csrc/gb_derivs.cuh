@@ -43,6 +43,13 @@ template <class T> GB_HD T dot6(const T* a, const T* b) {
   for (int k = 1; k < 6; ++k) s += a[k] * b[k];
   return s;
 }
+GB_HD dfloat dot6(const dfloat* a, const dfloat* b) {
+  dacc d;
+  d.first(a[0], b[0]);
+#pragma unroll
+  for (int k = 1; k < 6; ++k) d.add(a[k], b[k]);
+  return d.result();
+}
 
 // Element offsets of the per-instance workspace.
 // "K" arrays are the world-frame forward kinematics (root-origin frame): oMi,
@@ -60,18 +67,24 @@ struct DerivLayout {
   int coY, doY, cof, cJ, dVdq, dAdq, dAdv, dFda, dFdq, dFdv, dYtJ;
   int dtq, dtv;  // nv x nv in region P (ABA only: dtau_dq, dtau_dv feeding -Minv * dtau)
   int nS, nP;
-  // region SS (ABA only): K + Schur / Minv data
-  int Ia, U, UD, Dinv, u, F0, Fslot, nslot;
-  int nSS;
+  // ABA only: region SS (articulated inertias and the bias u of the Schur
+  // complement) and region K (kinematics, the Fcrb columns of the Minv
+  // recursion, Minv itself as a packed upper triangle, U Dinv and Dinv u)
+  int Ia, u, F0, Fslot, nslot, Mi, UD, Du;
+  int nSS, nK;
 };
+
+// index of (r, c), r <= c, in a packed row-major upper triangle of an nv x nv matrix
+GB_HD int upk(int nv, int r, int c) { return r * nv - (r * (r - 1)) / 2 + (c - r); }
 
 // Fills the layout for a model; `aba` selects the ABA-derivative arrangement.
 inline DerivLayout make_deriv_layout(int nj, int nv, int nslot, bool aba) {
   DerivLayout L;
-  int oS = 0, oSS = 0;
+  int oS = 0, oSS = 0, oK = 0;
   auto takeS = [&](int n) { const int r = oS; oS += n; return r; };
   auto takeSS = [&](int n) { const int r = oSS; oSS += n; return r; };
-  auto takeK = [&](int n) { return aba ? takeSS(n) : takeS(n); };
+  auto takeKr = [&](int n) { const int r = oK; oK += n; return r; };
+  auto takeK = [&](int n) { return aba ? takeKr(n) : takeS(n); };
   L.oM = takeK(12 * nj); L.ov = takeK(6 * nj); L.oa = takeK(6 * nj); L.oh = takeK(6 * nj); L.of = takeK(6 * nj);
   L.oY = takeK(10 * nj); L.J = takeK(6 * nv);
   L.coY = aba ? takeS(10 * nj) : L.oY;
@@ -79,23 +92,43 @@ inline DerivLayout make_deriv_layout(int nj, int nv, int nslot, bool aba) {
   L.cJ = aba ? takeS(6 * nv) : L.J;
   L.doY = takeS(36 * nj);
   L.dVdq = takeS(6 * nv); L.dAdq = takeS(6 * nv); L.dAdv = takeS(6 * nv);
-  L.dFda = takeS(6 * nv); L.dFdq = takeS(6 * nv); L.dFdv = takeS(6 * nv); L.dYtJ = takeS(6 * nv);
+  L.dFda = takeS(6 * nv); L.dFdq = takeS(6 * nv); L.dFdv = takeS(6 * nv); L.dYtJ = aba ? 0 : takeS(6 * nv);
   L.nS = oS;
   L.dtq = 0;
   L.dtv = aba ? nv * nv : 0;
   L.nP = aba ? 2 * nv * nv : 0;
   L.Ia = aba ? takeSS(21 * nj) : 0;
-  L.U = aba ? takeSS(6 * nv) : 0;
-  L.UD = aba ? takeSS(6 * nv) : 0;
-  L.Dinv = aba ? takeSS(6 * nv) : 0;
   L.u = aba ? takeSS(nv) : 0;
-  L.F0 = aba ? takeSS(6 * nv) : 0;
+  L.F0 = aba ? takeKr(6 * nv) : 0;
   L.nslot = nslot;
-  L.Fslot = aba ? takeSS(6 * nv * nslot) : 0;
+  L.Fslot = aba ? takeKr(6 * nv * nslot) : 0;
+  L.Mi = aba ? takeKr(nv * (nv + 1) / 2) : 0;
+  L.UD = aba ? takeKr(6 * nv) : 0;
+  L.Du = aba ? takeKr(nv) : 0;
   L.nSS = oSS;
+  L.nK = oK;
   return L;
 }
 
+// load 6 values stored as S into the compute scalar T
+template <class T, class S> GB_HD void ldc6(const Ws<S>& w, long e, T* x) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) x[k] = T(w[e + k]);
+}
+template <class T, class S> GB_HD void ldc_iner(const Ws<S>& w, long e, Iner<T>& Y) {
+  Y.m = T(w[e]);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) Y.c[k] = T(w[e + 1 + k]);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) Y.I[k] = T(w[e + 4 + k]);
+}
+template <class T, class S> GB_HD void stc_iner(const Ws<S>& w, long e, const Iner<T>& Y) {
+  w[e] = S(Y.m);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[e + 1 + k] = S(Y.c[k]);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) w[e + 4 + k] = S(Y.I[k]);
+}
 template <class S> GB_HD void ld_iner(const Ws<S>& w, long e, Iner<S>& Y) {
   Y.m = w[e];
 #pragma unroll
@@ -123,23 +156,23 @@ template <class S> GB_HD void st_x3(const Ws<S>& w, long e, const X3<S>& X) {
   for (int k = 0; k < 3; ++k) w[e + 9 + k] = X.t[k];
 }
 // y = M x for a full row-major 6x6 stored at e
-template <class S> GB_HD void mat6_mv(const Ws<S>& w, long e, const S* x, S* y) {
+template <class T, class S> GB_HD void mat6_mv(const Ws<S>& w, long e, const T* x, T* y) {
 #pragma unroll
   for (int r = 0; r < 6; ++r) {
-    S s = w[e + 6 * r] * x[0];
+    T row[6];
 #pragma unroll
-    for (int k = 1; k < 6; ++k) s += w[e + 6 * r + k] * x[k];
-    y[r] = s;
+    for (int k = 0; k < 6; ++k) row[k] = T(w[e + 6 * r + k]);
+    y[r] = dot6(row, x);
   }
 }
 // y = M^T x
-template <class S> GB_HD void mat6_tmv(const Ws<S>& w, long e, const S* x, S* y) {
+template <class T, class S> GB_HD void mat6_tmv(const Ws<S>& w, long e, const T* x, T* y) {
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
-    S s = w[e + c] * x[0];
+    T col[6];
 #pragma unroll
-    for (int k = 1; k < 6; ++k) s += w[e + 6 * k + c] * x[k];
-    y[c] = s;
+    for (int k = 0; k < 6; ++k) col[k] = T(w[e + 6 * k + c]);
+    y[c] = dot6(col, x);
   }
 }
 
@@ -212,8 +245,8 @@ template <class S> GB_HD void variation_plus_fcross(const Iner<S>& Y, const S* v
 }
 
 // world-frame joint columns J = oMi.act(S)
-template <class S> GB_HD void joint_columns(int jt, const X3<S>& O, S (*Jc)[6]) {
-  if (jt == JT_FF) {
+template <int NVJ, class S> GB_HD void joint_columns(int jt, const X3<S>& O, S (*Jc)[6]) {
+  if constexpr (NVJ == 6) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const S w[3] = {O.R[k], O.R[3 + k], O.R[6 + k]};
@@ -224,8 +257,8 @@ template <class S> GB_HD void joint_columns(int jt, const X3<S>& O, S (*Jc)[6]) 
       Jc[3 + k][3] = w[0]; Jc[3 + k][4] = w[1]; Jc[3 + k][5] = w[2];
     }
   } else {
-    const int ax = jt - JT_RX;
-    const S w[3] = {O.R[ax], O.R[3 + ax], O.R[6 + ax]};
+    S w[3];
+    axis_column(O, jt - JT_RX, w);
     S tw[3];
     cross3(O.t, w, tw);
     Jc[0][0] = tw[0]; Jc[0][1] = tw[1]; Jc[0][2] = tw[2]; Jc[0][3] = w[0]; Jc[0][4] = w[1]; Jc[0][5] = w[2];
@@ -264,113 +297,125 @@ template <class S> GB_HD void imul(const Iner<S>& Y, const S* v, S* f) {
 // accelerations a given: oa_gf is the full acceleration minus gravity) or the
 // ABA form (oa_gf holds only the velocity-product bias ov_p x ov_i, and of the
 // gyroscopic force).
-template <class S>
-GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
-                         const In* acc, bool with_derivs) {
-  const S* g = ModelScalar<S>::grav(m);
-  for (int i = 1; i < m.nj; ++i) {
-    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
-    const int nvj = jt == JT_FF ? 6 : 1;
-    X3<S> X, O;
-    joint_transform(m, i, q, X);
-    if (p > 0) {
-      X3<S> Op;
-      ld_x3(w, L.oM + 12 * p, Op);
-      compose(Op, X, O);
-    } else {
-      // The inertial frame of a root subtree is placed at its root joint: every
-      // output is a joint-space quantity, invariant to a translation of that
-      // frame, and world-frame inertias then carry no parallel-axis terms from a
-      // distant floating base (which FP32 rounding would amplify).
-      O = X;
-      O.t[0] = O.t[1] = O.t[2] = S(0);
-    }
-    st_x3(w, L.oM + 12 * i, O);
-    S Jc[6][6];
-    joint_columns(jt, O, Jc);
-    for (int k = 0; k < nvj; ++k) st6(w, L.J + 6 * (iv + k), Jc[k]);
-    // ov_i = ov_p + oMi.act(vJ)
-    S ovJ[6] = {0, 0, 0, 0, 0, 0}, ov[6], ovp[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < nvj; ++k) {
-      const S vk = S(v[iv + k]);
+// One joint of the world-frame forward pass (NVJ: its degrees of freedom).
+template <int NVJ, class S>
+GB_HD void world_forward_joint(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
+                               const In* acc, bool with_derivs, const S* g, int i) {
+  const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+  X3<S> X, O;
+  joint_transform(m, i, q, X);
+  if (p > 0) {
+    X3<S> Op;
+    ld_x3(w, L.oM + 12 * p, Op);
+    compose(Op, X, O);
+  } else {
+    // The inertial frame of a root subtree is placed at its root joint: every
+    // output is a joint-space quantity, invariant to a translation of that
+    // frame, and world-frame inertias then carry no parallel-axis terms from a
+    // distant floating base (which FP32 rounding would amplify).
+    O = X;
+    O.t[0] = O.t[1] = O.t[2] = S(0);
+  }
+  st_x3(w, L.oM + 12 * i, O);
+  S Jc[NVJ][6];
+  joint_columns<NVJ>(jt, O, Jc);
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) st6(w, L.J + 6 * (iv + k), Jc[k]);
+  // ov_i = ov_p + oMi.act(vJ)
+  S ovJ[6] = {0, 0, 0, 0, 0, 0}, ov[6], ovp[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    const S vk = S(v[iv + k]);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) ovJ[r] += Jc[k][r] * vk;
-    }
-    if (p > 0) ld6(w, L.ov + 6 * p, ovp);
+    for (int r = 0; r < 6; ++r) ovJ[r] += Jc[k][r] * vk;
+  }
+  if (p > 0) ld6(w, L.ov + 6 * p, ovp);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) ov[r] = ovp[r] + ovJ[r];
-    st6(w, L.ov + 6 * i, ov);
-    S oa[6];
-    if (acc) {
-      // oa_gf_i = oa_gf_p + oMi.act(S a) + ov_i x oMi.act(vJ)   (oa_gf_0 = -g)
-      S oap[6], vx[6];
-      if (p > 0) ld6(w, L.oa + 6 * p, oap);
-      else
-#pragma unroll
-        for (int r = 0; r < 6; ++r) oap[r] = -g[r];
-      mcross(ov, ovJ, vx);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) oa[r] = oap[r] + vx[r];
-      for (int k = 0; k < nvj; ++k) {
-        const S ak = S((*acc)[iv + k]);
-#pragma unroll
-        for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * ak;
-      }
-    } else {
-      // velocity-product bias ov_p x ov_i (aba.hxx:126-128)
-      if (p > 0) mcross(ovp, ov, oa);
-      else
-#pragma unroll
-        for (int r = 0; r < 6; ++r) oa[r] = S(0);
-    }
-    st6(w, L.oa + 6 * i, oa);
-    Iner<S> Y, oY;
-    load_inertia(m, i, Y);
-    iner_act(O, Y, oY);
-    st_iner(w, L.oY + 10 * i, oY);
-    S oh[6], of[6], t6[6];
-    imul(oY, ov, oh);
-    fcross(ov, oh, t6);
-    if (acc) {
-      imul(oY, oa, of);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) of[r] += t6[r];
-    } else {
-#pragma unroll
-      for (int r = 0; r < 6; ++r) of[r] = t6[r];
-    }
-    st6(w, L.oh + 6 * i, oh);
-    st6(w, L.of + 6 * i, of);
-    if (!with_derivs) continue;
-    S oap[6];
+  for (int r = 0; r < 6; ++r) ov[r] = ovp[r] + ovJ[r];
+  st6(w, L.ov + 6 * i, ov);
+  S oa[6];
+  if (acc) {
+    // oa_gf_i = oa_gf_p + oMi.act(S a) + ov_i x oMi.act(vJ)   (oa_gf_0 = -g)
+    S oap[6], vx[6];
     if (p > 0) ld6(w, L.oa + 6 * p, oap);
     else
 #pragma unroll
       for (int r = 0; r < 6; ++r) oap[r] = -g[r];
-    for (int k = 0; k < nvj; ++k) {
-      S dJ[6], dAdq[6], dAdv[6], dVdq[6];
-      mcross(ov, Jc[k], dJ);
-      mcross(oap, Jc[k], dAdq);
+    mcross(ov, ovJ, vx);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) dAdv[r] = dJ[r];
-      if (p > 0) {
-        mcross(ovp, Jc[k], dVdq);
-        S t[6];
-        mcross(ovp, dVdq, t);
+    for (int r = 0; r < 6; ++r) oa[r] = oap[r] + vx[r];
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+      const S ak = S((*acc)[iv + k]);
 #pragma unroll
-        for (int r = 0; r < 6; ++r) { dAdq[r] += t[r]; dAdv[r] += dVdq[r]; }
-      } else {
-#pragma unroll
-        for (int r = 0; r < 6; ++r) dVdq[r] = S(0);
-      }
-      st6(w, L.dVdq + 6 * (iv + k), dVdq);
-      st6(w, L.dAdq + 6 * (iv + k), dAdq);
-      st6(w, L.dAdv + 6 * (iv + k), dAdv);
+      for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * ak;
     }
-    S dY[36];
-    variation_plus_fcross(oY, ov, oh, dY);
+  } else {
+    // velocity-product bias ov_p x ov_i (aba.hxx:126-128)
+    if (p > 0) mcross(ovp, ov, oa);
+    else
 #pragma unroll
-    for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
+      for (int r = 0; r < 6; ++r) oa[r] = S(0);
+  }
+  st6(w, L.oa + 6 * i, oa);
+  Iner<S> Y, oY;
+  load_inertia(m, i, Y);
+  iner_act(O, Y, oY);
+  st_iner(w, L.oY + 10 * i, oY);
+  S oh[6], of[6], t6[6];
+  imul(oY, ov, oh);
+  fcross(ov, oh, t6);
+  if (acc) {
+    imul(oY, oa, of);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) of[r] += t6[r];
+  } else {
+#pragma unroll
+    for (int r = 0; r < 6; ++r) of[r] = t6[r];
+  }
+  st6(w, L.oh + 6 * i, oh);
+  st6(w, L.of + 6 * i, of);
+  if (!with_derivs) return;
+  S oap[6];
+  if (p > 0) ld6(w, L.oa + 6 * p, oap);
+  else
+#pragma unroll
+    for (int r = 0; r < 6; ++r) oap[r] = -g[r];
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    S dJ[6], dAdq[6], dAdv[6], dVdq[6];
+    mcross(ov, Jc[k], dJ);
+    mcross(oap, Jc[k], dAdq);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) dAdv[r] = dJ[r];
+    if (p > 0) {
+      mcross(ovp, Jc[k], dVdq);
+      S t[6];
+      mcross(ovp, dVdq, t);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) { dAdq[r] += t[r]; dAdv[r] += dVdq[r]; }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 6; ++r) dVdq[r] = S(0);
+    }
+    st6(w, L.dVdq + 6 * (iv + k), dVdq);
+    st6(w, L.dAdq + 6 * (iv + k), dAdq);
+    st6(w, L.dAdv + 6 * (iv + k), dAdv);
+  }
+  S dY[36];
+  variation_plus_fcross(oY, ov, oh, dY);
+#pragma unroll
+  for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
+}
+
+template <class S>
+GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
+                         const In* acc, bool with_derivs) {
+  const S* g = ModelScalar<S>::grav(m);
+#pragma unroll 1
+  for (int i = 1; i < m.nj; ++i) {
+    if (m.jtype[i] == JT_FF) world_forward_joint<6, S>(m, L, w, q, v, acc, with_derivs, g, i);
+    else world_forward_joint<1, S>(m, L, w, q, v, acc, with_derivs, g, i);
   }
 }
 
@@ -498,431 +543,572 @@ template <class S> GB_HD void shift_force_from_origin(const S* f, const S* t, S*
   for (int k = 0; k < 3; ++k) { o[k] = f[k]; o[3 + k] = f[3 + k] - txf[k]; }
 }
 // a motion->force operator M (row-major 6x6) about point C re-expressed about
-// P with r = C - P:  [[A, B - A R], [C + R A, D + R B - C R - R A R]], R = [r]x
-template <class S> GB_HD void shift_operator(const S* M, const S* r, S* O) {
-  S A[9], B[9], C[9], D[9];
+// P with r = C - P:  [[A, B - A R], [C + R A, D + R B - C R - R A R]], R = [r]x,
+// added to the operator stored at `dst` (both row-major in the workspace).
+// Row a of X R is x_a x r (x_a = row a of X); column b of R X is r x (column b
+// of X).  The blocks are streamed so that at most three 3x3 blocks are live.
+template <class T, class S> GB_HD void shift_operator_add(const Ws<S>& w, long src, long dst, const T* r) {
+  auto ld3x3 = [&](int r0, int c0, T* X) {
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      A[3 * a + b] = M[6 * a + b]; B[3 * a + b] = M[6 * a + 3 + b];
-      C[3 * a + b] = M[6 * (3 + a) + b]; D[3 * a + b] = M[6 * (3 + a) + 3 + b];
-    }
-  // X R for a 3x3 X: (X R)(a, b) = sum_k X(a,k) R(k,b), R = [[0,-r2,r1],[r2,0,-r0],[-r1,r0,0]]
-  auto mulR = [&](const S* X, S* Y) {
+      for (int b = 0; b < 3; ++b) X[3 * a + b] = T(w[src + 6 * (r0 + a) + c0 + b]);
+  };
+  auto add3x3 = [&](int r0, int c0, const T* X) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) w[dst + 6 * (r0 + a) + c0 + b] = S(T(w[dst + 6 * (r0 + a) + c0 + b]) + X[3 * a + b]);
+  };
+  auto mulR = [&](const T* X, T* Y) {  // X R
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      Y[3 * a + 0] = X[3 * a + 1] * r[2] - X[3 * a + 2] * r[1];
-      Y[3 * a + 1] = X[3 * a + 2] * r[0] - X[3 * a + 0] * r[2];
-      Y[3 * a + 2] = X[3 * a + 0] * r[1] - X[3 * a + 1] * r[0];
+      Y[3 * a + 0] = dot2(X[3 * a + 1], r[2], -X[3 * a + 2], r[1]);
+      Y[3 * a + 1] = dot2(X[3 * a + 2], r[0], -X[3 * a + 0], r[2]);
+      Y[3 * a + 2] = dot2(X[3 * a + 0], r[1], -X[3 * a + 1], r[0]);
     }
   };
-  // R X: rows r x (columns of X)
-  auto Rmul = [&](const S* X, S* Y) {
+  auto Rmul = [&](const T* X, T* Y) {  // R X
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      Y[0 + b] = r[1] * X[6 + b] - r[2] * X[3 + b];
-      Y[3 + b] = r[2] * X[0 + b] - r[0] * X[6 + b];
-      Y[6 + b] = r[0] * X[3 + b] - r[1] * X[0 + b];
+      Y[0 + b] = dot2(r[1], X[6 + b], -r[2], X[3 + b]);
+      Y[3 + b] = dot2(r[2], X[0 + b], -r[0], X[6 + b]);
+      Y[6 + b] = dot2(r[0], X[3 + b], -r[1], X[0 + b]);
     }
   };
-  S AR[9], RA[9], RB[9], CR[9], RAR[9];
-  mulR(A, AR);
-  Rmul(A, RA);
-  Rmul(B, RB);
-  mulR(C, CR);
-  mulR(RA, RAR);
+  T X[9], Y[9], Dacc[9];
+  // A: top-left unchanged; B - A R; C + R A; -R A R into the D block
+  ld3x3(0, 0, X);
+  add3x3(0, 0, X);
+  mulR(X, Y);
+  ld3x3(0, 3, Dacc);
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+  for (int k = 0; k < 9; ++k) Dacc[k] -= Y[k];
+  add3x3(0, 3, Dacc);
+  Rmul(X, Y);
+  ld3x3(3, 0, Dacc);
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const int k = 3 * a + b;
-      O[6 * a + b] = A[k];
-      O[6 * a + 3 + b] = B[k] - AR[k];
-      O[6 * (3 + a) + b] = C[k] + RA[k];
-      O[6 * (3 + a) + 3 + b] = D[k] + RB[k] - CR[k] - RAR[k];
-    }
+  for (int k = 0; k < 9; ++k) Dacc[k] += Y[k];
+  add3x3(3, 0, Dacc);
+  mulR(Y, X);  // R A R
+  ld3x3(3, 3, Dacc);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Dacc[k] -= X[k];
+  ld3x3(0, 3, X);  // + R B
+  Rmul(X, Y);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Dacc[k] += Y[k];
+  ld3x3(3, 0, X);  // - C R
+  mulR(X, Y);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Dacc[k] -= Y[k];
+  add3x3(3, 3, Dacc);
 }
 
 // ------------------------------------------------------------------------------------------
-// The four sweeps of computeABADerivatives (aba-derivatives.hxx:380-449): writes ddq,
-// the symmetric Minv, and dtau_dq / dtau_dv (at (q, v, ddq)) into the workspace;
-// the products -Minv dtau_dq, -Minv dtau_dv are a separate batched kernel.
+// The four sweeps of computeABADerivatives (aba-derivatives.hxx:380-449): ddq,
+// Minv (packed upper triangle, workspace region K) and dtau_dq / dtau_dv (at
+// (q, v, ddq), region P); the products -Minv dtau_dq, -Minv dtau_dv and the
+// symmetric Minv output are written by a separate batched kernel.
 // `slot[i]` is the Fcrb slot of joint i (a last child reuses its parent's slot).
 //
-// Passes 1-2 (kinematics, Schur complement, Minv) and the velocity /
-// acceleration recursion of pass 3 run in SS.  The column sets of pass 3 and
-// the backward pass 4 run in S in floating origins: every quantity of joint i
-// is expressed about joint i's position t_i (world orientation), so that no
-// FP32 value carries the lever arm of a distant origin; contributions move
-// between joints by translation (shift_motion / shift_force / shift_operator).
+// Scalar types: SS for the Schur complement Ia - U Dinv U^T with Dinv and the
+// bias u (pass 2); K for the kinematics of pass 1, Minv and its Fcrb columns,
+// U Dinv, Dinv u and the velocity / acceleration recursion of pass 3; T for
+// the column sets of pass 3 and the backward pass 4, stored between the
+// passes as S; P for dtau_dq / dtau_dv.  The quantities of passes 3-4 are in
+// floating origins: every quantity of joint i is expressed about joint i's
+// position t_i (world orientation), so that no reduced-precision value
+// carries the lever arm of a distant origin; contributions move between
+// joints by translation (shift_motion / shift_force / shift_operator_add).
 // ------------------------------------------------------------------------------------------
-template <class S, class SS>
-GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<SS>& z, const In& q, const In& v,
-                             const In& tau, const Out& Minv) {
+template <class SS> GB_HD void ld_sym6(const Ws<SS>& zs, long e, Sym6<SS>& I6) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { I6.A[k] = zs[e + k]; I6.D[k] = zs[e + 15 + k]; }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) I6.B[k] = zs[e + 6 + k];
+}
+template <class SS> GB_HD void st_sym6(const Ws<SS>& zs, long e, const Sym6<SS>& I6) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { zs[e + k] = I6.A[k]; zs[e + 15 + k] = I6.D[k]; }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) zs[e + 6 + k] = I6.B[k];
+}
+
+// Minv(r, c) from the packed upper triangle (symmetric)
+template <class K> GB_HD K minv_at(const DerivLayout& L, const Ws<K>& zk, int nv, int r, int c) {
+  return r <= c ? zk[L.Mi + upk(nv, r, c)] : zk[L.Mi + upk(nv, c, r)];
+}
+
+// One joint of pass 2 (ComputeABADerivativesBackwardStep1, hxx:87-171) with
+// NVJ degrees of freedom: the Schur complement in SS, the Minv rows and Fcrb
+// columns in K.  Minv rows of the joint: the diagonal block Dinv and the
+// columns of its subtree (-SDinv^T Fcrb); the columns right of the subtree are
+// first written by pass 3.
+template <int NVJ, class K, class SS>
+GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs, int i) {
   const int nv = m.nv;
-  const double* arm = m.arm_d;
-  // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), in SS
-  world_forward<SS>(m, L, z, q, v, nullptr, false);
-  for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix()
-    Iner<SS> oY;
-    ld_iner(z, L.oY + 10 * i, oY);
-    Sym6<SS> I6;
-    iner_to_sym6(oY, I6);
-    for (int k = 0; k < 6; ++k) { z[L.Ia + 21 * i + k] = I6.A[k]; z[L.Ia + 21 * i + 15 + k] = I6.D[k]; }
-    for (int k = 0; k < 9; ++k) z[L.Ia + 21 * i + 6 + k] = I6.B[k];
+  const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+  Sym6<SS> Ia;
+  ld_sym6(zs, L.Ia + 21 * i, Ia);
+  K of[6];
+  ld6(zk, L.of + 6 * i, of);
+  K Jk[NVJ][6];
+  SS U[NVJ][6];  // per joint dof k: U column
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    ld6(zk, L.J + 6 * (iv + k), Jk[k]);
+    SS Jc[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) Jc[r] = SS(Jk[k][r]);
+    zs[L.u + iv + k] -= SS(dot6(Jk[k], of));
+    sym6_mv(Ia, Jc, U[k]);
   }
-  for (int r = 0; r < nv * nv; ++r) Minv[r] = 0.0;
-  for (int k = 0; k < nv; ++k) z[L.u + k] = SS(tau[k]);
-  for (int k = 0; k < 6 * nv; ++k) z[L.F0 + k] = SS(0);
-  auto ld_sym = [&](int i, Sym6<SS>& I6) {
-    for (int k = 0; k < 6; ++k) { I6.A[k] = z[L.Ia + 21 * i + k]; I6.D[k] = z[L.Ia + 21 * i + 15 + k]; }
-    for (int k = 0; k < 9; ++k) I6.B[k] = z[L.Ia + 21 * i + 6 + k];
-  };
-  auto st_sym = [&](int i, const Sym6<SS>& I6) {
-    for (int k = 0; k < 6; ++k) { z[L.Ia + 21 * i + k] = I6.A[k]; z[L.Ia + 21 * i + 15 + k] = I6.D[k]; }
-    for (int k = 0; k < 9; ++k) z[L.Ia + 21 * i + 6 + k] = I6.B[k];
-  };
-  // ---- pass 2: ComputeABADerivativesBackwardStep1 (hxx:87-171), in SS
-  for (int i = m.nj - 1; i > 0; --i) {
-    const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
-    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
-    Sym6<SS> Ia;
-    ld_sym(i, Ia);
-    SS of[6];
-    ld6(z, L.of + 6 * i, of);
-    SS Jc[6][6], U[6][6];  // per joint dof k: J column, U column
-    for (int k = 0; k < nvj; ++k) {
-      ld6(z, L.J + 6 * (iv + k), Jc[k]);
-      z[L.u + iv + k] -= dot6(Jc[k], of);
-      sym6_mv(Ia, Jc[k], U[k]);
-    }
-    SS StU[36], Dinv[36];
-    for (int r = 0; r < nvj; ++r)
-      for (int c = 0; c < nvj; ++c) StU[r * nvj + c] = dot6(Jc[r], U[c]);
-    for (int k = 0; k < nvj; ++k) StU[k * nvj + k] += SS(arm[iv + k]);
-    if (nvj == 6) llt_inverse<SS, 6>(StU, Dinv);
+  SS Dinv[NVJ * NVJ];
+  {
+    SS StU[NVJ * NVJ];
+#pragma unroll 1
+    for (int r = 0; r < NVJ; ++r)
+#pragma unroll 1
+      for (int c = 0; c < NVJ; ++c) {
+        SS d = SS(Jk[r][0]) * U[c][0];
+#pragma unroll
+        for (int e = 1; e < 6; ++e) d += SS(Jk[r][e]) * U[c][e];
+        StU[r * NVJ + c] = d;
+      }
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) StU[k * NVJ + k] += SS(m.arm_d[iv + k]);
+    if constexpr (NVJ == 6) llt_inverse<SS, 6>(StU, Dinv);
     else Dinv[0] = SS(1) / StU[0];
-    SS UD[6][6];  // UDinv columns
-    for (int k = 0; k < nvj; ++k)
+  }
+  SS UD[NVJ][6];  // UDinv columns
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k)
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      SS sum = U[0][r] * Dinv[k];
+#pragma unroll 1
+      for (int j = 1; j < NVJ; ++j) sum += U[j][r] * Dinv[j * NVJ + k];
+      UD[k][r] = sum;
+    }
+  // U Dinv and Dinv u (u is final here: every child has been folded in) for pass 3, in K
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    st6(zk, L.UD + 6 * (iv + k), UD[k]);
+    SS du = SS(0);
+#pragma unroll 1
+    for (int c = 0; c < NVJ; ++c) du += Dinv[k * NVJ + c] * zs[L.u + iv + c];
+    zk[L.Du + iv + k] = K(du);
+  }
+#pragma unroll 1
+  for (int r = 0; r < NVJ; ++r)
+#pragma unroll 1
+    for (int c = r; c < NVJ; ++c) zk[L.Mi + upk(nv, iv + r, iv + c)] = K(Dinv[r * NVJ + c]);
+  const int nch = nst - NVJ;
+  if (nch > 0) {
+    K SD[NVJ][6];  // SDinv columns = J Dinv
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k)
 #pragma unroll
       for (int r = 0; r < 6; ++r) {
-        SS s = U[0][r] * Dinv[k];
-        for (int j = 1; j < nvj; ++j) s += U[j][r] * Dinv[j * nvj + k];
-        UD[k][r] = s;
+        K sum = Jk[0][r] * K(Dinv[k]);
+#pragma unroll 1
+        for (int j = 1; j < NVJ; ++j) sum += Jk[j][r] * K(Dinv[j * NVJ + k]);
+        SD[k][r] = sum;
       }
-    for (int k = 0; k < nvj; ++k) {
-      st6(z, L.U + 6 * (iv + k), U[k]);
-      st6(z, L.UD + 6 * (iv + k), UD[k]);
-      for (int c = 0; c < nvj; ++c) z[L.Dinv + 6 * (iv + k) + c] = Dinv[k * nvj + c];
+#pragma unroll 1
+    for (int c = iv + NVJ; c < iv + nst; ++c) {
+      K F[6];
+      ld6(zk, L.F0 + 6 * c, F);
+#pragma unroll 1
+      for (int r = 0; r < NVJ; ++r) zk[L.Mi + upk(nv, iv + r, c)] = -dot6(SD[r], F);
     }
-    for (int r = 0; r < nvj; ++r)
-      for (int c = 0; c < nvj; ++c) Minv[(iv + r) * nv + iv + c] = double(Dinv[r * nvj + c]);
-    const int nch = nst - nvj;
-    if (nch > 0) {
-      SS SD[6][6];  // SDinv columns = J Dinv
-      for (int k = 0; k < nvj; ++k)
+  }
+  if (!(nch > 0 && p == 0)) {  // leaf: F = U Minv_rows; inner joint with a parent: F += U Minv_rows
+    K Uk[NVJ][6];
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k)
 #pragma unroll
-        for (int r = 0; r < 6; ++r) {
-          SS s = Jc[0][r] * Dinv[k];
-          for (int j = 1; j < nvj; ++j) s += Jc[j][r] * Dinv[j * nvj + k];
-          SD[k][r] = s;
-        }
-      for (int c = iv + nvj; c < iv + nst; ++c) {
-        SS F[6];
-        ld6(z, L.F0 + 6 * c, F);
-        for (int r = 0; r < nvj; ++r) Minv[(iv + r) * nv + c] = double(-dot6(SD[r], F));
-      }
-    }
-    if (!(nch > 0 && p == 0)) {  // leaf: F = U Minv_rows; inner joint with a parent: F += U Minv_rows
-      for (int c = iv; c < iv + nst; ++c) {
-        SS F[6] = {0, 0, 0, 0, 0, 0};
-        if (nch > 0) ld6(z, L.F0 + 6 * c, F);
-        for (int k = 0; k < nvj; ++k) {
-          const SS mk = SS(Minv[(iv + k) * nv + c]);
+      for (int r = 0; r < 6; ++r) Uk[k][r] = K(U[k][r]);
+#pragma unroll 1
+    for (int c = iv; c < iv + nst; ++c) {
+      K F[6] = {K(0), K(0), K(0), K(0), K(0), K(0)};
+      if (nch > 0) ld6(zk, L.F0 + 6 * c, F);
+#pragma unroll 1
+      for (int k = 0; k < NVJ; ++k) {
+        const K mk = minv_at(L, zk, nv, iv + k, c);
 #pragma unroll
-          for (int r = 0; r < 6; ++r) F[r] += U[k][r] * mk;
-        }
-        st6(z, L.F0 + 6 * c, F);
+        for (int r = 0; r < 6; ++r) F[r] += Uk[k][r] * mk;
       }
+      st6(zk, L.F0 + 6 * c, F);
     }
-    if (p > 0) {
-      // Ia -= UDinv U^T ; pa = of + Ia oa_gf + UDinv u ; accumulate into the parent
-      for (int k = 0; k < nvj; ++k) sym6_rank1_sub(Ia, U[k], UD[k]);
-      SS oa[6], pa[6];
-      ld6(z, L.oa + 6 * i, oa);
+  }
+  if (p > 0) {
+    // Ia -= UDinv U^T ; pa = of + Ia oa_gf + UDinv u ; accumulate into the parent
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) sym6_rank1_sub(Ia, U[k], UD[k]);
+    SS pa[6];
+    {
+      K oak[6];
+      SS oa[6];
+      ld6(zk, L.oa + 6 * i, oak);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) oa[r] = SS(oak[r]);
       sym6_mv(Ia, oa, pa);
-      for (int k = 0; k < nvj; ++k) {
-        const SS uk = z[L.u + iv + k];
-#pragma unroll
-        for (int r = 0; r < 6; ++r) pa[r] += UD[k][r] * uk;
-      }
-      SS ofp[6];
-      ld6(z, L.of + 6 * p, ofp);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) ofp[r] += of[r] + pa[r];
-      st6(z, L.of + 6 * p, ofp);
-      Sym6<SS> Ip;
-      ld_sym(p, Ip);
-      sym6_add(Ip, Ia);
-      st_sym(p, Ip);
     }
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
+      const SS uk = zs[L.u + iv + k];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) pa[r] += UD[k][r] * uk;
+    }
+    K ofp[6];
+    ld6(zk, L.of + 6 * p, ofp);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) ofp[r] += of[r] + K(pa[r]);
+    st6(zk, L.of + 6 * p, ofp);
+    Sym6<SS> Ip;
+    ld_sym6(zs, L.Ia + 21 * p, Ip);
+    sym6_add(Ip, Ia);
+    st_sym6(zs, L.Ia + 21 * p, Ip);
   }
 }
 
-template <class S, class SS>
-GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                            const Ws<SS>& z, const In& v, const Out& Minv, const Out* ddq_out) {
+template <class K, class SS>
+GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs, const In& q,
+                             const In& v, const In& tau) {
   const int nv = m.nv;
-  // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
-  // velocity / acceleration recursion runs in SS in floating origins and
-  // replaces ov / oa in K; the column sets, link inertia, momentum, force and
-  // inertia variation of joint i are written to C in S about t_i.
-  const SS* gs = ModelScalar<SS>::grav(m);
-  for (int i = 1; i < m.nj; ++i) {
-    const int p = m.parent[i], iv = m.idx_v[i];
-    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
-    SS ti[3];
-    for (int k = 0; k < 3; ++k) ti[k] = z[L.oM + 12 * i + 9 + k];
-    SS ovp[6] = {0, 0, 0, 0, 0, 0}, oap[6];
+  // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K
+  world_forward<K>(m, L, zk, q, v, nullptr, false);
+#pragma unroll 1
+  for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix(), formed in SS
+    Iner<K> oY;
+    ld_iner(zk, L.oY + 10 * i, oY);
+    Sym6<SS> I6;
+    iner_to_sym6(oY, I6);
+    st_sym6(zs, L.Ia + 21 * i, I6);
+  }
+  for (int k = 0; k < nv; ++k) zs[L.u + k] = SS(tau[k]);
+  for (int k = 0; k < 6 * nv; ++k) zk[L.F0 + k] = K(0);
+  // ---- pass 2: ComputeABADerivativesBackwardStep1 (hxx:87-171)
+#pragma unroll 1
+  for (int i = m.nj - 1; i > 0; --i) {
+    if (m.jtype[i] == JT_FF) aba_derivs_pass2_joint<6, K, SS>(m, L, zk, zs, i);
+    else aba_derivs_pass2_joint<1, K, SS>(m, L, zk, zs, i);
+  }
+}
+
+// One joint of pass 3 (ComputeABADerivativesForwardStep2, hxx:178-270) with NVJ
+// degrees of freedom.
+template <int NVJ, class S, class T, class K>
+GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
+                                  const Ws<K>& zk, const In& v, const Out* ddq_out, const K* gk, int i) {
+  const int nv = m.nv;
+  const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+  K ti[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ti[k] = zk[L.oM + 12 * i + 9 + k];
+  K ovp[6] = {K(0), K(0), K(0), K(0), K(0), K(0)}, oap[6];
+  if (p > 0) {
+    K r[3], x[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = ti[k] - zk[L.oM + 12 * p + 9 + k];
+    ld6(zk, L.ov + 6 * p, x);
+    shift_motion(x, r, ovp);
+    ld6(zk, L.oa + 6 * p, x);
+    shift_motion(x, r, oap);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) oap[k] = -gk[k];  // uniform field: invariant to the shift
+  }
+  // joint columns about t_i: a revolute axis passes through t_i; the root free-flyer sits at the origin
+  K Jo[NVJ][6], Jc[NVJ][6];
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    ld6(zk, L.J + 6 * (iv + k), Jo[k]);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) Jc[k][r] = Jo[k][r];
+  }
+  if constexpr (NVJ == 1) Jc[0][0] = Jc[0][1] = Jc[0][2] = K(0);
+  K ov[6], oa[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) ov[k] = ovp[k];
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    const K vk = K(v[iv + k]);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) ov[r] += Jc[k][r] * vk;
+  }
+  mcross(ovp, ov, oa);  // velocity-product bias (aba.hxx:126-128) + the parent's acceleration
+#pragma unroll
+  for (int k = 0; k < 6; ++k) oa[k] += oap[k];
+  K dd[NVJ];
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    K ud[6], udi[6];
+    ld6(zk, L.UD + 6 * (iv + k), ud);
+    shift_force_from_origin(ud, ti, udi);  // UDinv (a force about the root origin) about t_i
+    dd[k] = zk[L.Du + iv + k] - dot6(udi, oa);
+    if (ddq_out) (*ddq_out)[iv + k] = double(dd[k]);
+  }
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k)
+#pragma unroll
+    for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * dd[k];
+  st6(zk, L.ov + 6 * i, ov);
+  st6(zk, L.oa + 6 * i, oa);
+  // Minv rows of the joint: -= UDinv^T Fcrb[parent] (columns right of the
+  // subtree start from zero); Fcrb[i] = J Minv_rows (+ Fcrb[parent]).  A
+  // free-flyer is a root joint (no parent), so the updated rows are revolute.
+  const long Fi = L.Fslot + 6L * nv * slot[i];
+  const long Fp = p > 0 ? L.Fslot + 6L * nv * slot[p] : -1;
+  if (p > 0) {
+    K udk[6];
+    ld6(zk, L.UD + 6 * iv, udk);
+#pragma unroll 1
+    for (int c = iv; c < nv; ++c) {
+      K Fpc[6];
+      ld6(zk, Fp + 6 * c, Fpc);
+      const long e = L.Mi + upk(nv, iv, c);
+      const K mk = (c < iv + nst ? zk[e] : K(0)) - dot6(udk, Fpc);
+      zk[e] = mk;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) Fpc[r] += Jo[0][r] * mk;
+      st6(zk, Fi + 6 * c, Fpc);
+    }
+  } else {  // a root joint: its rows are final; zero right of its subtree (another root's)
+#pragma unroll 1
+    for (int c = iv; c < nv; ++c) {
+      K Fn[6] = {K(0), K(0), K(0), K(0), K(0), K(0)};
+      if (c < iv + nst) {
+#pragma unroll 1
+        for (int k = 0; k < NVJ; ++k) {
+          const K mk = minv_at(L, zk, nv, iv + k, c);
+#pragma unroll
+          for (int r = 0; r < 6; ++r) Fn[r] += Jo[k][r] * mk;
+        }
+      } else {
+#pragma unroll 1
+        for (int k = 0; k < NVJ; ++k) zk[L.Mi + upk(nv, iv + k, c)] = K(0);
+      }
+      st6(zk, Fi + 6 * c, Fn);
+    }
+  }
+  // C quantities about t_i, computed in T and stored as S
+  T ovs[6], ovps[6], oaps[6], oas[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { ovs[k] = T(ov[k]); ovps[k] = T(ovp[k]); oaps[k] = T(oap[k]); oas[k] = T(oa[k]); }
+#pragma unroll 1
+  for (int k = 0; k < NVJ; ++k) {
+    T J[6], dJ[6], dAdq[6], dAdv[6], dVdq[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) J[r] = T(Jc[k][r]);
+    mcross(ovs, J, dJ);
+    mcross(oaps, J, dAdq);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) dAdv[r] = dJ[r];
     if (p > 0) {
-      SS r[3], x[6];
-      for (int k = 0; k < 3; ++k) r[k] = ti[k] - z[L.oM + 12 * p + 9 + k];
-      ld6(z, L.ov + 6 * p, x);
-      shift_motion(x, r, ovp);
-      ld6(z, L.oa + 6 * p, x);
-      shift_motion(x, r, oap);
+      mcross(ovps, J, dVdq);
+      T t[6];
+      mcross(ovps, dVdq, t);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) { dAdq[r] += t[r]; dAdv[r] += dVdq[r]; }
     } else {
 #pragma unroll
-      for (int k = 0; k < 6; ++k) oap[k] = -gs[k];  // uniform field: invariant to the shift
+      for (int r = 0; r < 6; ++r) dVdq[r] = T(0);
     }
-    // joint columns about t_i: a revolute axis passes through t_i; the root free-flyer sits at the origin
-    SS Jo[6][6], Jc[6][6];
-    for (int k = 0; k < nvj; ++k) {
-      ld6(z, L.J + 6 * (iv + k), Jo[k]);
+    st6(w, L.cJ + 6 * (iv + k), J);
+    st6(w, L.dVdq + 6 * (iv + k), dVdq);
+    st6(w, L.dAdq + 6 * (iv + k), dAdq);
+    st6(w, L.dAdv + 6 * (iv + k), dAdv);
+  }
+  Iner<T> oY;
+  {
+    Iner<K> oYd;
+    ld_iner(zk, L.oY + 10 * i, oYd);
+    oY.m = T(oYd.m);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) Jc[k][r] = Jo[k][r];
-    }
-    if (nvj == 1) Jc[0][0] = Jc[0][1] = Jc[0][2] = SS(0);
-    SS ov[6], oa[6];
+    for (int k = 0; k < 3; ++k) oY.c[k] = T(oYd.c[k] - ti[k]);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) ov[k] = ovp[k];
-    for (int k = 0; k < nvj; ++k) {
-      const SS vk = SS(v[iv + k]);
+    for (int k = 0; k < 6; ++k) oY.I[k] = T(oYd.I[k]);
+  }
+  stc_iner(w, L.coY + 10 * i, oY);
+  T oh[6], of[6], t6[6];
+  imul(oY, ovs, oh);
+  imul(oY, oas, of);
+  fcross(ovs, oh, t6);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) ov[r] += Jc[k][r] * vk;
-    }
-    mcross(ovp, ov, oa);  // velocity-product bias (aba.hxx:126-128) + the parent's acceleration
+  for (int k = 0; k < 6; ++k) of[k] += t6[k];
+  st6(w, L.cof + 6 * i, of);
+  T dY[36];
+  variation_plus_fcross(oY, ovs, oh, dY);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) oa[k] += oap[k];
-    SS dd[6];
-    for (int k = 0; k < nvj; ++k) {
-      SS s = SS(0);
-      for (int c = 0; c < nvj; ++c) s += z[L.Dinv + 6 * (iv + k) + c] * z[L.u + iv + c];
-      SS ud[6], udi[6];
-      ld6(z, L.UD + 6 * (iv + k), ud);
-      shift_force_from_origin(ud, ti, udi);  // UDinv (a force about the root origin) about t_i
-      dd[k] = s - dot6(udi, oa);
-      if (ddq_out) (*ddq_out)[iv + k] = double(dd[k]);
-    }
-    for (int k = 0; k < nvj; ++k)
-#pragma unroll
-      for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * dd[k];
-    st6(z, L.ov + 6 * i, ov);
-    st6(z, L.oa + 6 * i, oa);
-    // Minv rows of the joint: -= UDinv^T Fcrb[parent]; Fcrb[i] = J Minv_rows (+ Fcrb[parent])
-    // (root-origin frame, SS)
-    const long Fi = L.Fslot + 6L * nv * slot[i];
-    const long Fp = p > 0 ? L.Fslot + 6L * nv * slot[p] : -1;
-    for (int c = iv; c < nv; ++c) {
-      SS Fpc[6];
-      if (p > 0) {
-        ld6(z, Fp + 6 * c, Fpc);
-        for (int k = 0; k < nvj; ++k) {
-          SS ud[6];
-          ld6(z, L.UD + 6 * (iv + k), ud);
-          Minv[(iv + k) * nv + c] -= double(dot6(ud, Fpc));
-        }
-      }
-      SS Fn[6];
-#pragma unroll
-      for (int r = 0; r < 6; ++r) Fn[r] = p > 0 ? Fpc[r] : SS(0);
-      for (int k = 0; k < nvj; ++k) {
-        const SS mk = SS(Minv[(iv + k) * nv + c]);
-#pragma unroll
-        for (int r = 0; r < 6; ++r) Fn[r] += Jo[k][r] * mk;
-      }
-      st6(z, Fi + 6 * c, Fn);
-    }
-    // C quantities about t_i in S
-    S ovs[6], ovps[6], oaps[6], oas[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) { ovs[k] = S(ov[k]); ovps[k] = S(ovp[k]); oaps[k] = S(oap[k]); oas[k] = S(oa[k]); }
-    for (int k = 0; k < nvj; ++k) {
-      S J[6], dJ[6], dAdq[6], dAdv[6], dVdq[6];
-#pragma unroll
-      for (int r = 0; r < 6; ++r) J[r] = S(Jc[k][r]);
-      mcross(ovs, J, dJ);
-      mcross(oaps, J, dAdq);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) dAdv[r] = dJ[r];
-      if (p > 0) {
-        mcross(ovps, J, dVdq);
-        S t[6];
-        mcross(ovps, dVdq, t);
-#pragma unroll
-        for (int r = 0; r < 6; ++r) { dAdq[r] += t[r]; dAdv[r] += dVdq[r]; }
-      } else {
-#pragma unroll
-        for (int r = 0; r < 6; ++r) dVdq[r] = S(0);
-      }
-      st6(w, L.cJ + 6 * (iv + k), J);
-      st6(w, L.dVdq + 6 * (iv + k), dVdq);
-      st6(w, L.dAdq + 6 * (iv + k), dAdq);
-      st6(w, L.dAdv + 6 * (iv + k), dAdv);
-    }
-    Iner<SS> oYd;
-    ld_iner(z, L.oY + 10 * i, oYd);
-    Iner<S> oY;
-    oY.m = S(oYd.m);
-    for (int k = 0; k < 3; ++k) oY.c[k] = S(oYd.c[k] - ti[k]);
-    for (int k = 0; k < 6; ++k) oY.I[k] = S(oYd.I[k]);
-    st_iner(w, L.coY + 10 * i, oY);
-    S oh[6], of[6], t6[6];
-    imul(oY, ovs, oh);
-    imul(oY, oas, of);
-    fcross(ovs, oh, t6);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) of[k] += t6[k];
-    st6(w, L.cof + 6 * i, of);
-    S dY[36];
-    variation_plus_fcross(oY, ovs, oh, dY);
-#pragma unroll
-    for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
+  for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = S(dY[k]);
+}
+
+template <class S, class T, class K>
+GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
+                            const Ws<K>& zk, const In& v, const Out* ddq_out) {
+  // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
+  // velocity / acceleration recursion runs in K in floating origins and
+  // replaces ov / oa in K; the column sets, link inertia, momentum, force and
+  // inertia variation of joint i are computed in T about t_i and stored as S.
+  const K* gk = ModelScalar<K>::grav(m);
+#pragma unroll 1
+  for (int i = 1; i < m.nj; ++i) {
+    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K>(m, L, slot, w, zk, v, ddq_out, gk, i);
+    else aba_derivs_pass3_joint<1, S, T, K>(m, L, slot, w, zk, v, ddq_out, gk, i);
   }
 }
 
-// P: scalar of the dtau matrices handed to the -Minv*dtau products
-template <class S, class SS, class P>
-GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<SS>& z, const Ws<P>& wp,
-                            const Out& Minv) {
+// t_a - t_b (joint positions), formed in K and rounded to T
+template <class T, class K>
+GB_HD void joint_offset(const DerivLayout& L, const Ws<K>& zk, int a, int b, T* d) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = T(zk[L.oM + 12 * a + 9 + k] - zk[L.oM + 12 * b + 9 + k]);
+}
+
+// One joint of pass 4 with NVJ degrees of freedom (1: revolute, 6: the root
+// free-flyer, whose parent is the universe), so that every per-dof loop has a
+// compile-time bound and the per-dof arrays stay in registers.
+template <int NVJ, class S, class T, class K, class P>
+GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<K>& zk,
+                                  const Ws<P>& wp, int i, T eps) {
   const int nv = m.nv;
-  const S eps = eps_of<S>();
-  // ---- pass 4: ComputeABADerivativesBackwardStep2 (hxx:273-368), in S, floating
-  // origins: a joint's composite oY / doY / of are about its own position; a
-  // child adds its contributions moved to the parent's position.
-  for (int k = 0; k < nv * nv; ++k) { wp[L.dtq + k] = P(0); wp[L.dtv + k] = P(0); }
-  auto offset = [&](int a, int b, S* d) {  // t_a - t_b, formed in SS
-    for (int k = 0; k < 3; ++k) d[k] = S(z[L.oM + 12 * a + 9 + k] - z[L.oM + 12 * b + 9 + k]);
-  };
-  for (int i = m.nj - 1; i > 0; --i) {
-    const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
-    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
-    Iner<S> oY;
-    ld_iner(w, L.coY + 10 * i, oY);
-    S of[6];
-    ld6(w, L.cof + 6 * i, of);
-    for (int k = 0; k < nvj; ++k) {
+  const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+  {
+    Iner<T> oY;
+    ldc_iner(w, L.coY + 10 * i, oY);
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
       const int c = iv + k;
-      S Jc[6], x[6], t[6], dFdv[6], dFdq[6], dFda[6];
-      ld6(w, L.cJ + 6 * c, Jc);
-      ld6(w, L.dAdv + 6 * c, x);
-      imul(oY, x, dFdv);
+      T Jc[6], x[6], t[6], y[6];
+      ldc6(w, L.cJ + 6 * c, Jc);
+      ldc6(w, L.dAdv + 6 * c, x);
+      imul(oY, x, y);
       mat6_mv(w, L.doY + 36 * i, Jc, t);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) dFdv[r] += t[r];
-      st6(w, L.dFdv + 6 * c, dFdv);
-      ld6(w, L.dAdq + 6 * c, x);
-      imul(oY, x, dFdq);
+      for (int r = 0; r < 6; ++r) y[r] += t[r];
+      st6(w, L.dFdv + 6 * c, y);  // dFdv
+      ldc6(w, L.dAdq + 6 * c, x);
+      imul(oY, x, y);
       if (p > 0) {
-        ld6(w, L.dVdq + 6 * c, x);
+        ldc6(w, L.dVdq + 6 * c, x);
         mat6_mv(w, L.doY + 36 * i, x, t);
 #pragma unroll
-        for (int r = 0; r < 6; ++r) dFdq[r] += t[r];
+        for (int r = 0; r < 6; ++r) y[r] += t[r];
       }
-      st6(w, L.dFdq + 6 * c, dFdq);
-      imul(oY, Jc, dFda);
-      st6(w, L.dFda + 6 * c, dFda);
+      st6(w, L.dFdq + 6 * c, y);  // dFdq
+      imul(oY, Jc, y);
+      st6(w, L.dFda + 6 * c, y);  // dFda
     }
-    // row block: dtau(i, subtree) = J_i^T dF_c, with dF_c moved from its joint's position to t_i
-    for (int r = 0; r < nvj; ++r) {
-      S Jr[6];
-      ld6(w, L.cJ + 6 * (iv + r), Jr);
-      for (int c = iv; c < iv + nst; ++c) {
-        S d[3], x[6], y[6];
-        offset(m.dof_joint[c], i, d);
-        ld6(w, L.dFdv + 6 * c, x);
-        shift_force(x, d, y);
-        wp[L.dtv + (iv + r) * nv + c] = P(dot6(Jr, y));
-        ld6(w, L.dFdq + 6 * c, x);
-        shift_force(x, d, y);
-        wp[L.dtq + (iv + r) * nv + c] = P(dot6(Jr, y));
-      }
+  }
+  // row block: dtau(i, subtree) = J_i^T dF_c, with dF_c moved from its joint's position to t_i
+#pragma unroll 1
+  for (int r = 0; r < NVJ; ++r) {
+    T Jr[6];
+    ldc6(w, L.cJ + 6 * (iv + r), Jr);
+#pragma unroll 1
+    for (int c = iv; c < iv + nst; ++c) {
+      T d[3], x[6], y[6];
+      joint_offset(L, zk, m.dof_joint[c], i, d);
+      ldc6(w, L.dFdv + 6 * c, x);
+      shift_force(x, d, y);
+      wp[L.dtv + (iv + r) * nv + c] = P(dot6(Jr, y));
+      ldc6(w, L.dFdq + 6 * c, x);
+      shift_force(x, d, y);
+      wp[L.dtq + (iv + r) * nv + c] = P(dot6(Jr, y));
     }
-    for (int k = 0; k < nvj; ++k) {
+  }
+  {
+    T of[6];
+    ldc6(w, L.cof + 6 * i, of);
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
       const int c = iv + k;
-      S Jc[6], x[6], t[6];
-      ld6(w, L.cJ + 6 * c, Jc);
-      ld6(w, L.dFdq + 6 * c, x);
+      T Jc[6], x[6], t[6];
+      ldc6(w, L.cJ + 6 * c, Jc);
+      ldc6(w, L.dFdq + 6 * c, x);
       fcross(Jc, of, t);
 #pragma unroll
       for (int r = 0; r < 6; ++r) x[r] += t[r];
       st6(w, L.dFdq + 6 * c, x);
     }
-    if (p > 0) {
-      // ancestor columns: motion quantities of ancestor j moved from t_j to t_i
-      for (int r = 0; r < nvj; ++r) {
-        S fa[6], Jr[6], StdY[6];
-        ld6(w, L.dFda + 6 * (iv + r), fa);
-        ld6(w, L.cJ + 6 * (iv + r), Jr);
-        mat6_tmv(w, L.doY + 36 * i, Jr, StdY);
-        for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j]) {
-          S d[3], x[6], y[6], xs[6], ys[6];
-          offset(i, m.dof_joint[j], d);
-          ld6(w, L.dAdq + 6 * j, x);
-          ld6(w, L.dVdq + 6 * j, y);
-          shift_motion(x, d, xs);
-          shift_motion(y, d, ys);
-          wp[L.dtq + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
-          ld6(w, L.dAdv + 6 * j, x);
-          ld6(w, L.cJ + 6 * j, y);
-          shift_motion(x, d, xs);
-          shift_motion(y, d, ys);
-          wp[L.dtv + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
-        }
-      }
-      // accumulate into the parent, moved from t_i to t_p
-      S rr[3];
-      offset(i, p, rr);
-      Iner<S> oYp, oYs = oY;
-      ld_iner(w, L.coY + 10 * p, oYp);
-      for (int k = 0; k < 3; ++k) oYs.c[k] += rr[k];
-      iner_add(oYp, oYs, eps);
-      st_iner(w, L.coY + 10 * p, oYp);
-      S Mi[36], Ms[36];
-      for (int k = 0; k < 36; ++k) Mi[k] = w[L.doY + 36 * i + k];
-      shift_operator(Mi, rr, Ms);
-      for (int k = 0; k < 36; ++k) w[L.doY + 36 * p + k] += Ms[k];
-      S ofs[6], ofp[6];
-      shift_force(of, rr, ofs);
-      ld6(w, L.cof + 6 * p, ofp);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) ofp[r] += ofs[r];
-      st6(w, L.cof + 6 * p, ofp);
+  }
+  if (NVJ == 6 || p == 0) return;  // a free-flyer is a root joint: nothing above it
+  // ancestor columns: motion quantities of ancestor j moved from t_j to t_i
+#pragma unroll 1
+  for (int r = 0; r < NVJ; ++r) {
+    T fa[6], StdY[6];
+    {
+      T Jr[6];
+      ldc6(w, L.dFda + 6 * (iv + r), fa);
+      ldc6(w, L.cJ + 6 * (iv + r), Jr);
+      mat6_tmv(w, L.doY + 36 * i, Jr, StdY);
+    }
+#pragma unroll 1
+    for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j]) {
+      T d[3], x[6], y[6], xs[6], ys[6];
+      joint_offset(L, zk, i, m.dof_joint[j], d);
+      ldc6(w, L.dAdq + 6 * j, x);
+      ldc6(w, L.dVdq + 6 * j, y);
+      shift_motion(x, d, xs);
+      shift_motion(y, d, ys);
+      wp[L.dtq + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
+      ldc6(w, L.dAdv + 6 * j, x);
+      ldc6(w, L.cJ + 6 * j, y);
+      shift_motion(x, d, xs);
+      shift_motion(y, d, ys);
+      wp[L.dtv + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
     }
   }
-  // symmetrise Minv (hxx:448-449)
-  for (int r = 1; r < nv; ++r)
-    for (int c = 0; c < r; ++c) Minv[r * nv + c] = Minv[c * nv + r];
+  // accumulate into the parent, moved from t_i to t_p
+  T rr[3];
+  joint_offset(L, zk, i, p, rr);
+  {
+    Iner<T> oYp, oYs;
+    ldc_iner(w, L.coY + 10 * i, oYs);
+    ldc_iner(w, L.coY + 10 * p, oYp);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) oYs.c[k] += rr[k];
+    iner_add(oYp, oYs, eps);
+    stc_iner(w, L.coY + 10 * p, oYp);
+  }
+  shift_operator_add(w, L.doY + 36 * i, L.doY + 36 * p, rr);
+  {
+    T of[6], ofs[6], ofp[6];
+    ldc6(w, L.cof + 6 * i, of);
+    shift_force(of, rr, ofs);
+    ldc6(w, L.cof + 6 * p, ofp);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) ofp[r] += ofs[r];
+    st6(w, L.cof + 6 * p, ofp);
+  }
 }
 
-template <class S, class SS, class P>
+// ---- pass 4: ComputeABADerivativesBackwardStep2 (hxx:273-368), in T, floating
+// origins: a joint's composite oY / doY / of are about its own position; a
+// child adds its contributions moved to the parent's position.  Only the
+// structurally non-zero entries of dtau_dq / dtau_dv (row k of column c for k
+// an ancestor of c or in its subtree) are written: the products read no other.
+template <class S, class T, class K, class P>
+GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<K>& zk,
+                            const Ws<P>& wp) {
+  const T eps = eps_of<T>();
+#pragma unroll 1
+  for (int i = m.nj - 1; i > 0; --i) {
+    if (m.jtype[i] == JT_FF) aba_derivs_pass4_joint<6, S, T, K, P>(m, L, w, zk, wp, i, eps);
+    else aba_derivs_pass4_joint<1, S, T, K, P>(m, L, w, zk, wp, i, eps);
+  }
+}
+
+template <class S, class T, class K, class SS, class P>
 GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                             const Ws<SS>& z, const Ws<P>& wp, const In& q, const In& v, const In& tau,
-                             const Out& Minv, const Out* ddq_out) {
-  aba_derivs_pass12<S, SS>(m, L, z, q, v, tau, Minv);
-  aba_derivs_pass3<S, SS>(m, L, slot, w, z, v, Minv, ddq_out);
-  aba_derivs_pass4<S, SS, P>(m, L, w, z, wp, Minv);
+                             const Ws<K>& zk, const Ws<SS>& zs, const Ws<P>& wp, const In& q, const In& v,
+                             const In& tau, const Out* ddq_out) {
+  aba_derivs_pass12<K, SS>(m, L, zk, zs, q, v, tau);
+  aba_derivs_pass3<S, T, K>(m, L, slot, w, zk, v, ddq_out);
+  aba_derivs_pass4<S, T, K, P>(m, L, w, zk, wp);
 }
 
 }  // namespace gb

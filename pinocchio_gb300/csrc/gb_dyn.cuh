@@ -23,6 +23,13 @@ namespace gb {
 
 GB_HD void ssincos(double x, double* s, double* c) { sincos(x, s, c); }
 GB_HD void ssincos(float x, float* s, float* c) { sincosf(x, s, c); }
+// double-float angle: sine and cosine through FP64 (one sincos per revolute joint)
+GB_HD void ssincos(dfloat x, dfloat* s, dfloat* c) {
+  double sd, cd;
+  sincos(double(x), &sd, &cd);
+  *s = dfloat(sd);
+  *c = dfloat(cd);
+}
 
 // strided view of one instance's vector / matrix in the batch arrays
 struct In {
@@ -203,7 +210,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
     Iner<S> Y;
     load_inertia(m, i, Y);
     Sym6<SS> Ia;
-    iner_to_sym6(Y, Ia);
+    load_sym6(m, i, Ia);
     M6<S> vJ, c, h, f;
     joint_motion(jt, v, iv, vJ);
     cross_motion(vel[i], vJ, c);
@@ -316,10 +323,10 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       for (int r = 0; r < 6; ++r) a.v[r] += S(dd[r]);
     } else {
       const int ax = jt - JT_RX;
-      SS w = SS(UDs[i][0]) * SS(a.v[0]);
+      S w = UDs[i][0] * a.v[0];
 #pragma unroll
-      for (int k = 1; k < 6; ++k) w += SS(UDs[i][k]) * SS(a.v[k]);
-      const SS dd = du[i] - w;
+      for (int k = 1; k < 6; ++k) w += UDs[i][k] * a.v[k];
+      const SS dd = du[i] - SS(w);
       ddq[iv] = double(dd);
       a.v[3 + ax] += S(dd);
     }

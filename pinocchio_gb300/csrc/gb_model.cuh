@@ -4,7 +4,8 @@
 // The blob replaces ModelTpl + the tree tables of DataTpl that the hot path
 // reads (reference multibody/model.hpp:98-220, multibody/data.hxx:195-306):
 // per joint parent / type / idx_q / idx_v / nvSubtree / depth, placements and
-// inertias (FP64 and FP32 copies), per dof armature / parents_fromRow /
+// inertias (FP64, FP32 and double-float copies, also as 6x6 block-symmetric
+// matrices), per dof armature / parents_fromRow /
 // nvSubtree_fromRow, and for the batched products -Minv*X the per-column list
 // of rows that can be non-zero (ancestor and subtree dofs), and the Fcrb
 // slot of every joint for the Minv recursion of the ABA derivatives, and the
@@ -13,6 +14,7 @@
 // its first child and keep them in a branch slot only where the tree forks.
 #pragma once
 
+#include "gb_dfloat.cuh"
 #include "gb_spatial.cuh"
 
 namespace gb {
@@ -26,9 +28,12 @@ struct BlobHeader {
   int o_place_d, o_iner_d, o_arm_d, o_place_f, o_iner_f, o_arm_f, o_rel_off, o_rel_list;
   int o_slot, o_dofj, o_bslot, nbranch;
   int o_grp, ngroup, o_grp_rel, n_grp_rel;
+  int o_i6_d, o_i6_f, o_place_df, o_iner_df;
+  int o_arm_df, pad6, pad7, pad8;
   double grav_d[6];
   float grav_f[6];
   float padf[2];
+  dfloat grav_df[6];
 };
 static_assert(sizeof(BlobHeader) % 16 == 0, "blob header must keep 16-byte alignment");
 
@@ -36,8 +41,9 @@ struct MView {
   int nj, nq, nv, max_depth, has_ff, nslot;
   const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint, *bslot, *grp, *grp_rel;
   int nbranch, ngroup;
-  const double *place_d, *iner_d, *arm_d, *grav_d;
-  const float *place_f, *iner_f, *arm_f, *grav_f;
+  const double *place_d, *iner_d, *arm_d, *grav_d, *i6_d;
+  const float *place_f, *iner_f, *arm_f, *grav_f, *i6_f;
+  const dfloat *place_df, *iner_df, *arm_df, *grav_df;
 };
 
 GB_HD MView make_view(const unsigned char* base) {
@@ -67,6 +73,12 @@ GB_HD MView make_view(const unsigned char* base) {
   m.place_f = reinterpret_cast<const float*>(base + h->o_place_f);
   m.iner_f = reinterpret_cast<const float*>(base + h->o_iner_f);
   m.arm_f = reinterpret_cast<const float*>(base + h->o_arm_f);
+  m.i6_d = reinterpret_cast<const double*>(base + h->o_i6_d);
+  m.i6_f = reinterpret_cast<const float*>(base + h->o_i6_f);
+  m.place_df = reinterpret_cast<const dfloat*>(base + h->o_place_df);
+  m.iner_df = reinterpret_cast<const dfloat*>(base + h->o_iner_df);
+  m.arm_df = reinterpret_cast<const dfloat*>(base + h->o_arm_df);
+  m.grav_df = h->grav_df;
   m.grav_d = h->grav_d;
   m.grav_f = h->grav_f;
   return m;
@@ -74,16 +86,25 @@ GB_HD MView make_view(const unsigned char* base) {
 
 template <class S> struct ModelScalar;
 template <> struct ModelScalar<double> {
+  GB_HD static const double* i6(const MView& m, int i) { return m.i6_d + 21 * i; }
   GB_HD static const double* place(const MView& m, int i) { return m.place_d + 12 * i; }
   GB_HD static const double* iner(const MView& m, int i) { return m.iner_d + 10 * i; }
   GB_HD static const double* arm(const MView& m) { return m.arm_d; }
   GB_HD static const double* grav(const MView& m) { return m.grav_d; }
 };
 template <> struct ModelScalar<float> {
+  GB_HD static const float* i6(const MView& m, int i) { return m.i6_f + 21 * i; }
   GB_HD static const float* place(const MView& m, int i) { return m.place_f + 12 * i; }
   GB_HD static const float* iner(const MView& m, int i) { return m.iner_f + 10 * i; }
   GB_HD static const float* arm(const MView& m) { return m.arm_f; }
   GB_HD static const float* grav(const MView& m) { return m.grav_f; }
+};
+
+template <> struct ModelScalar<dfloat> {
+  GB_HD static const dfloat* place(const MView& m, int i) { return m.place_df + 12 * i; }
+  GB_HD static const dfloat* iner(const MView& m, int i) { return m.iner_df + 10 * i; }
+  GB_HD static const dfloat* arm(const MView& m) { return m.arm_df; }
+  GB_HD static const dfloat* grav(const MView& m) { return m.grav_df; }
 };
 
 template <class S> GB_HD void load_placement(const MView& m, int i, X3<S>& P) {
@@ -92,6 +113,14 @@ template <class S> GB_HD void load_placement(const MView& m, int i, X3<S>& P) {
   for (int k = 0; k < 9; ++k) P.R[k] = p[k];
 #pragma unroll
   for (int k = 0; k < 3; ++k) P.t[k] = p[9 + k];
+}
+// the link's spatial inertia Y.matrix() in block-symmetric form (A, B, D), formed once on the host
+template <class S> GB_HD void load_sym6(const MView& m, int i, Sym6<S>& I) {
+  const S* p = ModelScalar<S>::i6(m, i);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { I.A[k] = p[k]; I.D[k] = p[15 + k]; }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) I.B[k] = p[6 + k];
 }
 template <class S> GB_HD void load_inertia(const MView& m, int i, Iner<S>& Y) {
   const S* p = ModelScalar<S>::iner(m, i);

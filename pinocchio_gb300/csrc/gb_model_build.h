@@ -150,8 +150,14 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.o_grp = take(4 * grp.size()); h.o_grp_rel = take(4 * grp_rel.size() + 4);
   h.o_place_d = take(8 * 12 * nj); h.o_iner_d = take(8 * 10 * nj); h.o_arm_d = take(8 * nv);
   h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
+  h.o_i6_d = take(8 * 21 * nj); h.o_i6_f = take(4 * 21 * nj);
+  h.o_place_df = take(8 * 12 * nj); h.o_iner_df = take(8 * 10 * nj); h.o_arm_df = take(8 * nv);
   h.bytes = (int)off;
-  for (int k = 0; k < 6; ++k) { h.grav_d[k] = M->gravity[k]; h.grav_f[k] = (float)M->gravity[k]; }
+  for (int k = 0; k < 6; ++k) {
+    h.grav_d[k] = M->gravity[k];
+    h.grav_f[k] = (float)M->gravity[k];
+    h.grav_df[k] = gb::dfloat(M->gravity[k]);
+  }
   M->blob.assign(off, 0);
   unsigned char* b = M->blob.data();
   std::memcpy(b, &h, sizeof(h));
@@ -180,6 +186,25 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   put_i(h.o_grp_rel, grp_rel);
   put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);
   put_f(h.o_place_f, M->placement); put_f(h.o_iner_f, M->inertia); put_f(h.o_arm_f, M->armature);
+  {  // Y.matrix() per link (reference spatial/inertia.hpp:481-491), block-symmetric A, B, D
+    std::vector<double> i6(21 * (size_t)nj, 0.0);
+    for (int i = 0; i < nj; ++i) {
+      gb::Iner<double> Y;
+      Y.m = M->inertia[10 * i];
+      for (int k = 0; k < 3; ++k) Y.c[k] = M->inertia[10 * i + 1 + k];
+      for (int k = 0; k < 6; ++k) Y.I[k] = M->inertia[10 * i + 4 + k];
+      gb::Sym6<double> S6;
+      gb::iner_to_sym6(Y, S6);
+      for (int k = 0; k < 6; ++k) { i6[21 * i + k] = S6.A[k]; i6[21 * i + 15 + k] = S6.D[k]; }
+      for (int k = 0; k < 9; ++k) i6[21 * i + 6 + k] = S6.B[k];
+    }
+    put_d(h.o_i6_d, i6);
+    put_f(h.o_i6_f, i6);
+  }
+  auto put_df = [&](int o, const std::vector<double>& v) {
+    for (size_t k = 0; k < v.size(); ++k) reinterpret_cast<gb::dfloat*>(b + o)[k] = gb::dfloat(v[k]);
+  };
+  put_df(h.o_place_df, M->placement); put_df(h.o_iner_df, M->inertia); put_df(h.o_arm_df, M->armature);
   M->blob_bytes = (int)off;
   return GB_OK;
 }

@@ -27,34 +27,47 @@ template <class S> GB_HD S sqr(S x) { return x * x; }
 
 template <class S> struct M6 { S v[6]; };   // motion or force
 template <class S> struct X3 { S R[9]; S t[3]; };
+
+// column `ax` (0, 1, 2) of a rotation, chosen by selects rather than a
+// run-time array index (which would move the matrix to local memory)
+template <class S> GB_HD void axis_column(const X3<S>& O, int ax, S* w) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[k] = ax == 0 ? O.R[3 * k] : (ax == 1 ? O.R[3 * k + 1] : O.R[3 * k + 2]);
+}
+// x[ax] of a 3-vector by selects
+template <class S> GB_HD S pick3(const S* x, int ax) { return ax == 0 ? x[0] : (ax == 1 ? x[1] : x[2]); }
 template <class S> struct Sym6 { S A[6]; S B[9]; S D[6]; };
 
 template <class S> GB_HD void zero(M6<S>& m) {
 #pragma unroll
   for (int k = 0; k < 6; ++k) m.v[k] = S(0);
 }
+// Short dot products.  The double-float scalar overloads them with one
+// compensated accumulation per dot product instead of a normalised sum per term.
+template <class S> GB_HD S dot2(S a0, S b0, S a1, S b1) { return a0 * b0 + a1 * b1; }
+template <class S> GB_HD S dot3(S a0, S b0, S a1, S b1, S a2, S b2) { return a0 * b0 + a1 * b1 + a2 * b2; }
 template <class S> GB_HD void cross3(const S* a, const S* b, S* o) {
-  const S x = a[1] * b[2] - a[2] * b[1];
-  const S y = a[2] * b[0] - a[0] * b[2];
-  const S z = a[0] * b[1] - a[1] * b[0];
+  const S x = dot2(a[1], b[2], -a[2], b[1]);
+  const S y = dot2(a[2], b[0], -a[0], b[2]);
+  const S z = dot2(a[0], b[1], -a[1], b[0]);
   o[0] = x; o[1] = y; o[2] = z;
 }
 template <class S> GB_HD void mv3(const S* R, const S* x, S* o) {
-  const S a = R[0] * x[0] + R[1] * x[1] + R[2] * x[2];
-  const S b = R[3] * x[0] + R[4] * x[1] + R[5] * x[2];
-  const S c = R[6] * x[0] + R[7] * x[1] + R[8] * x[2];
+  const S a = dot3(R[0], x[0], R[1], x[1], R[2], x[2]);
+  const S b = dot3(R[3], x[0], R[4], x[1], R[5], x[2]);
+  const S c = dot3(R[6], x[0], R[7], x[1], R[8], x[2]);
   o[0] = a; o[1] = b; o[2] = c;
 }
 template <class S> GB_HD void mtv3(const S* R, const S* x, S* o) {
-  const S a = R[0] * x[0] + R[3] * x[1] + R[6] * x[2];
-  const S b = R[1] * x[0] + R[4] * x[1] + R[7] * x[2];
-  const S c = R[2] * x[0] + R[5] * x[1] + R[8] * x[2];
+  const S a = dot3(R[0], x[0], R[3], x[1], R[6], x[2]);
+  const S b = dot3(R[1], x[0], R[4], x[1], R[7], x[2]);
+  const S c = dot3(R[2], x[0], R[5], x[1], R[8], x[2]);
   o[0] = a; o[1] = b; o[2] = c;
 }
 template <class S> GB_HD void sym3_mv(const S* s, const S* x, S* o) {
-  const S a = s[0] * x[0] + s[1] * x[1] + s[3] * x[2];
-  const S b = s[1] * x[0] + s[2] * x[1] + s[4] * x[2];
-  const S c = s[3] * x[0] + s[4] * x[1] + s[5] * x[2];
+  const S a = dot3(s[0], x[0], s[1], x[1], s[3], x[2]);
+  const S b = dot3(s[1], x[0], s[2], x[1], s[4], x[2]);
+  const S c = dot3(s[3], x[0], s[4], x[1], s[5], x[2]);
   o[0] = a; o[1] = b; o[2] = c;
 }
 
@@ -90,7 +103,7 @@ template <class S> GB_HD void compose(const X3<S>& A, const X3<S>& B, X3<S>& C) 
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) R[3 * r + c] = A.R[3 * r] * B.R[c] + A.R[3 * r + 1] * B.R[3 + c] + A.R[3 * r + 2] * B.R[6 + c];
+    for (int c = 0; c < 3; ++c) R[3 * r + c] = dot3(A.R[3 * r], B.R[c], A.R[3 * r + 1], B.R[3 + c], A.R[3 * r + 2], B.R[6 + c]);
   mv3(A.R, B.t, t);
 #pragma unroll
   for (int k = 0; k < 9; ++k) C.R[k] = R[k];
@@ -162,18 +175,18 @@ template <class S> GB_HD void sym3_rotate(const S* d, const S* R, S* out) {
   const S L00 = d[0] - d[5], L01 = d[1];
   const S L10 = d[1], L11 = d[2] - d[5];
   const S L20 = S(2) * d[3], L21 = d[4] + d[4];
-  const S Y00 = R[3] * L00 + R[4] * L10 + R[5] * L20;
-  const S Y01 = R[3] * L01 + R[4] * L11 + R[5] * L21;
-  const S Y10 = R[6] * L00 + R[7] * L10 + R[8] * L20;
-  const S Y11 = R[6] * L01 + R[7] * L11 + R[8] * L21;
-  S s1 = Y00 * R[0] + Y01 * R[1];
-  S s2 = Y00 * R[3] + Y01 * R[4];
-  S s3v = Y10 * R[0] + Y11 * R[1];
-  S s4 = Y10 * R[3] + Y11 * R[4];
-  S s5 = Y10 * R[6] + Y11 * R[7];
-  const S r0 = -R[0] * d[4] + R[1] * d[3];
-  const S r1 = -R[3] * d[4] + R[4] * d[3];
-  const S r2 = -R[6] * d[4] + R[7] * d[3];
+  const S Y00 = dot3(R[3], L00, R[4], L10, R[5], L20);
+  const S Y01 = dot3(R[3], L01, R[4], L11, R[5], L21);
+  const S Y10 = dot3(R[6], L00, R[7], L10, R[8], L20);
+  const S Y11 = dot3(R[6], L01, R[7], L11, R[8], L21);
+  S s1 = dot2(Y00, R[0], Y01, R[1]);
+  S s2 = dot2(Y00, R[3], Y01, R[4]);
+  S s3v = dot2(Y10, R[0], Y11, R[1]);
+  S s4 = dot2(Y10, R[3], Y11, R[4]);
+  S s5 = dot2(Y10, R[6], Y11, R[7]);
+  const S r0 = dot2(-R[0], d[4], R[1], d[3]);
+  const S r1 = dot2(-R[3], d[4], R[4], d[3]);
+  const S r2 = dot2(-R[6], d[4], R[7], d[3]);
   S s0 = L00 + L11 - s2 - s5;
   out[0] = s0 + d[5];
   out[1] = s1 + r2;

@@ -14,6 +14,9 @@ namespace {
 thread_local std::string g_err;
 gb::In in_at(const double* p, long b, long n) { return gb::In{p + b * n, 1}; }
 gb::Out out_at(double* p, long b, long n) { return gb::Out{p + b * n, 1}; }
+double to_double(double x) { return x; }
+double to_double(float x) { return x; }
+double to_double(gb::dfloat x) { return double(x.hi) + double(x.lo); }
 }  // namespace
 
 extern "C" {
@@ -108,24 +111,30 @@ extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const d
   return 0;
 }
 
-template <class S> struct ProductScalar { typedef S type; };
-template <> struct ProductScalar<gb::dfloat> { typedef float type; };
-
-template <class S>
+// Mirrors the device: sweeps with S (column-set storage), T (column-set
+// arithmetic), K (kinematics, Minv), SS = double (Schur), P (dtau); then the
+// product kernel, which writes Minv from the packed K copy and forms
+// -Minv * dtau in P over the structurally non-zero rows.
+template <class S, class T, class K, class P>
 static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const double* q, const double* v,
                             const double* tau, double* dq, double* dv, double* Minv, double* ddq,
-                            std::vector<S>& wS, std::vector<double>& wSS) {
-  typedef typename ProductScalar<S>::type P;
+                            std::vector<S>& wS, std::vector<K>& wK, std::vector<double>& wSS) {
   const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
   const int nv = m.nv;
   const long nn = (long)nv * nv;
   std::vector<P> wP(L.nP);
   const gb::Out dd = out_at(ddq, b, nv);
-  gb::aba_derivs_sweeps<S, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<double>{wSS.data(), 1},
-                                      gb::Ws<P>{wP.data(), 1}, in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv),
-                                      out_at(Minv, b, nn), &dd);
-  // -Minv * dtau restricted to the structurally non-zero rows, as the device kernel does
-  const double* Mi = Minv + b * nn;
+  gb::aba_derivs_sweeps<S, T, K, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
+                                            gb::Ws<double>{wSS.data(), 1}, gb::Ws<P>{wP.data(), 1},
+                                            in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv), &dd);
+  double* Mi = Minv + b * nn;
+  std::vector<P> Mp(nn);
+  for (int r = 0; r < nv; ++r)
+    for (int c = 0; c < nv; ++c) {
+      const K x = wK[L.Mi + (r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r))];
+      Mi[r * nv + c] = to_double(x);
+      Mp[r * nv + c] = P(x);
+    }
   for (int mm = 0; mm < 2; ++mm) {
     const P* X = wP.data() + (mm == 0 ? L.dtq : L.dtv);
     double* O = (mm == 0 ? dq : dv) + b * nn;
@@ -134,7 +143,7 @@ static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const
         P acc = P(0);
         for (int kk = M->rel_off[c]; kk < M->rel_off[c + 1]; ++kk) {
           const int k = M->rel_list[kk];
-          acc += P(Mi[k * nv + r]) * X[k * nv + c];
+          acc += Mp[k * nv + r] * X[k * nv + c];
         }
         O[r * nv + c] = -double(acc);
       }
@@ -148,12 +157,14 @@ extern "C" int hs_aba_derivs(void* h, int mixed, long B, const double* q, const 
   const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
 #pragma omp parallel
   {
-    std::vector<double> wd(L.nS), wss(L.nSS);
-    std::vector<gb::dfloat> wf(L.nS);
+    std::vector<double> wd(L.nS), wdk(L.nK), wss(L.nSS);
+    std::vector<float> wf(L.nS);
+    std::vector<gb::dfloat> wfk(L.nK);
 #pragma omp for schedule(static)
     for (long b = 0; b < B; ++b) {
-      if (mixed) aba_derivs_host<gb::dfloat>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wss);
-      else aba_derivs_host<double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wss);
+      if (mixed)
+        aba_derivs_host<float, gb::dfloat, gb::dfloat, float>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wfk, wss);
+      else aba_derivs_host<double, double, double, double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wdk, wss);
     }
   }
   return 0;
