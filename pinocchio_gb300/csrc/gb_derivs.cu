@@ -88,22 +88,9 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
   gb::aba_derivs_pass4<S, T, K, P>(m, L, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, gb::Ws<P>{wsP + b, B});
 }
 
-// Exact FP32 -> FP64 conversion with integer instructions (the hardware
-// conversion issues on the FP64 pipe); zero, subnormal, infinite and NaN
-// inputs take the hardware path.
-__device__ __forceinline__ double f2d(float x) {
-  const unsigned u = __float_as_uint(x);
-  const unsigned ex = (u >> 23) & 0xffu;
-  if (ex == 0u || ex == 0xffu) {
-    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    return (double)x;
-  }
-  const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-  return __hiloint2double((int)hi, (int)(u << 29));
-}
 __device__ __forceinline__ double to_double(double x) { return x; }
-__device__ __forceinline__ double to_double(float x) { return f2d(x); }
-__device__ __forceinline__ double to_double(gb::dfloat x) { return f2d(x.hi) + f2d(x.lo); }
+__device__ __forceinline__ double to_double(float x) { return gb::widen(x); }
+__device__ __forceinline__ double to_double(gb::dfloat x) { return double(x); }
 
 // Minv and out_m = -Minv * X_m for the two matrices X_0 = dtau_dq, X_1 = dtau_dv
 // of G consecutive configurations per iteration (G a power of two).  smem:
@@ -284,7 +271,10 @@ int launch_minv_products_n(const gb_model* M, long B, const KM* wsMi, Arr Minv, 
     const long region = std::max(G * npk * (long)sizeof(KM), G * NM * nn * (long)sizeof(S));
     return G * nn * (long)sizeof(S) + ((region + 15) & ~15L) + (long)sizeof(int) * (4 * ngroup + nrel);
   };
-  const long budget = 100 * 1024;  // two CTAs per SM
+#ifndef GB_MINV_SMEM_KB
+#define GB_MINV_SMEM_KB 100
+#endif
+  const long budget = GB_MINV_SMEM_KB * 1024;  // shared memory per CTA (100 KB: two CTAs per SM)
   int NM = 2, lgG = 3;
   while (lgG > 0 && smem_of(1L << lgG, NM) > budget) --lgG;
   if (smem_of(1L << lgG, NM) > budget) NM = 1;
@@ -333,8 +323,9 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
 // Workspace of the ABA derivatives: region SS (articulated inertias and u:
 // FP64), region K (kinematics, Fcrb columns, Minv, U Dinv, Dinv u, velocity /
 // acceleration), region S (the derivative column sets stored between passes 3
-// and 4, computed in T) and region P (dtau_dq, dtau_dv in the scalar of the
-// -Minv*dtau products).  The mixed kernels use K = T = dfloat, S = P = float.
+// and 4: computed in T3 by pass 3 and in T by pass 4) and region P (dtau_dq,
+// dtau_dv in the scalar of the -Minv*dtau products).  The mixed kernels use
+// K = T = dfloat, S = T3 = P = float.
 template <class S, class T, class K, class SS, class P>
 size_t aba_ws_bytes(const gb::DerivLayout& L, long B) {
   return (sizeof(SS) * (size_t)L.nSS + sizeof(K) * (size_t)L.nK + sizeof(S) * (size_t)L.nS +
@@ -342,7 +333,7 @@ size_t aba_ws_bytes(const gb::DerivLayout& L, long B) {
          (size_t)B;
 }
 
-template <class S, class T, class K, class SS, class P>
+template <class S, class T3, class T, class K, class SS, class P>
 int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq, void* ws,
                          cudaStream_t st) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
@@ -353,15 +344,15 @@ int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr d
   const int tpb = M->tpb[GB_FUNC_ABA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
   int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS>, "k_aba_derivs_pass12");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T, K>, "k_aba_derivs_pass3");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T3, K>, "k_aba_derivs_pass3");
   if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, T, K, P>, "k_aba_derivs_pass4");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass12<K, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK, wsSS,
                                                                              q, v, tau);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass3<S, T, K><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS, wsK,
-                                                                              v, ddq);
+  k_aba_derivs_pass3<S, T3, K><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
+                                                                               wsK, v, ddq);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass3");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass4<S, T, K, P><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
@@ -371,14 +362,14 @@ int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr d
   return launch_minv_products<P, P, K>(M, B, wsK + (long)L.Mi * B, Minv, wsP, L, dq, dv, st);
 }
 
-template <class S, class T, class K, class SS, class P>
+template <class S, class T3, class T, class K, class SS, class P>
 int run_aba_derivs(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq,
                    cudaStream_t st) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   Workspace ws;
   int rc = ws_alloc(ws, aba_ws_bytes<S, T, K, SS, P>(L, B), st);
   if (rc != GB_OK) return rc;
-  return launch_aba_derivs_ws<S, T, K, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st);
+  return launch_aba_derivs_ws<S, T3, T, K, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st);
 }
 
 int check_gravity(const gb_model* M) {
@@ -401,9 +392,10 @@ int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr
                                    Arr Minv, Arr ddq, void* ws, cudaStream_t st) {
   if (check_gravity(M) != GB_OK) return GB_ERR_GRAVITY;
   if (precision == GB_FP64)
-    return launch_aba_derivs_ws<double, double, double, double, double>(M, B, q, v, tau, dq, dv, Minv, ddq, ws, st);
-  return launch_aba_derivs_ws<float, gb::dfloat, gb::dfloat, double, float>(M, B, q, v, tau, dq, dv, Minv, ddq, ws,
-                                                                           st);
+    return launch_aba_derivs_ws<double, double, double, double, double, double>(M, B, q, v, tau, dq, dv, Minv, ddq,
+                                                                                ws, st);
+  return launch_aba_derivs_ws<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, q, v, tau, dq, dv, Minv, ddq,
+                                                                                  ws, st);
 }
 
 }  // namespace gbi
@@ -453,8 +445,10 @@ int gb_aba_derivatives(const gb_model* M, int precision, int layout, long B, con
   const gbi::Arr Add = arr(ddq, layout, B, M->nv);
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == GB_FP64)
-    return gbi::run_aba_derivs<double, double, double, double, double>(M, B, Aq, Av, At, Adq, Adv, AMi, Add, st);
-  return gbi::run_aba_derivs<float, gb::dfloat, gb::dfloat, double, float>(M, B, Aq, Av, At, Adq, Adv, AMi, Add, st);
+    return gbi::run_aba_derivs<double, double, double, double, double, double>(M, B, Aq, Av, At, Adq, Adv, AMi, Add,
+                                                                               st);
+  return gbi::run_aba_derivs<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, Aq, Av, At, Adq, Adv, AMi,
+                                                                                 Add, st);
 }
 
 }  // extern "C"

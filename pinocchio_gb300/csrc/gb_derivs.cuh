@@ -1102,12 +1102,13 @@ GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w
   }
 }
 
-template <class S, class T, class K, class SS, class P>
+// T3: arithmetic of the column sets in pass 3; T: arithmetic of pass 4
+template <class S, class T3, class T, class K, class SS, class P>
 GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                              const Ws<K>& zk, const Ws<SS>& zs, const Ws<P>& wp, const In& q, const In& v,
                              const In& tau, const Out* ddq_out) {
   aba_derivs_pass12<K, SS>(m, L, zk, zs, q, v, tau);
-  aba_derivs_pass3<S, T, K>(m, L, slot, w, zk, v, ddq_out);
+  aba_derivs_pass3<S, T3, K>(m, L, slot, w, zk, v, ddq_out);
   aba_derivs_pass4<S, T, K, P>(m, L, w, zk, wp);
 }
 

@@ -29,10 +29,10 @@ struct alignas(8) dfloat {
   GB_HD dfloat() : hi(0.f), lo(0.f) {}
   GB_HD dfloat(float x) : hi(x), lo(0.f) {}  // NOLINT: implicit from float / literals
   GB_HD dfloat(int x) : hi(float(x)), lo(0.f) {}  // NOLINT
-  GB_HD explicit dfloat(double x) : hi(float(x)), lo(float(x - double(float(x)))) {}
+  GB_HD explicit dfloat(double x) : hi(narrow(x)), lo(narrow(x - widen(hi))) {}
   GB_HD dfloat(float h, float l, int) : hi(h), lo(l) {}
   GB_HD explicit operator float() const { return hi + lo; }
-  GB_HD explicit operator double() const { return double(hi) + double(lo); }
+  GB_HD explicit operator double() const { return widen(hi) + widen(lo); }
 };
 
 // s + e = a + b exactly (Knuth TwoSum)

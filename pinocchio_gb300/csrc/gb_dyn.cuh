@@ -70,8 +70,11 @@ template <class S> GB_HD void joint_motion(int jt, const In& x, int iv, M6<S>& o
 #pragma unroll
     for (int k = 0; k < 6; ++k) o.v[k] = S(x[iv + k]);
   } else {
-    zero(o);
-    o.v[3 + jt - JT_RX] = S(x[iv]);
+    const S val = S(x[iv]);
+    o.v[0] = o.v[1] = o.v[2] = S(0);
+    o.v[3] = jt == JT_RX ? val : S(0);
+    o.v[4] = jt == JT_RY ? val : S(0);
+    o.v[5] = jt == JT_RZ ? val : S(0);
   }
 }
 
@@ -241,7 +244,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         StU[7 * k] += SS(arm[iv + k]);
-        u6[k] = SS(tau[iv + k]) - SS(f.v[k]);
+        u6[k] = SS(tau[iv + k]) - cvt<SS>(f.v[k]);
       }
       llt_inverse<SS, 6>(StU, D6);
 #pragma unroll
@@ -256,14 +259,14 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       continue;
     }
     const int ax = jt - JT_RX;
-    const SS u = SS(tau[iv]) - SS(f.v[3 + ax]);
+    const SS u = SS(tau[iv]) - cvt<SS>(pick3(f.v + 3, ax));
     SS U[6], UD[6];
     sym6_col(Ia, 3 + ax, U);
-    const SS Dinv = SS(1) / (U[3 + ax] + SS(arm[iv]));
+    const SS Dinv = SS(1) / (pick3(U + 3, ax) + SS(arm[iv]));
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       UD[k] = U[k] * Dinv;
-      UDs[i][k] = S(UD[k]);
+      UDs[i][k] = cvt<S>(UD[k]);
     }
     du[i] = Dinv * u;
     if (p > 0) {
@@ -274,7 +277,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       sym6_mv(Iaf, c.v, t6);
       M6<S> pa, fp;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) pa.v[k] = f.v[k] + (t6[k] + S(UD[k] * u));
+      for (int k = 0; k < 6; ++k) pa.v[k] = f.v[k] + (t6[k] + cvt<S>(UD[k] * u));
       sym6_transform(Iaf, X, Ip);
       act_force(X, pa, fp);
       if (p == i - 1) {  // i is the first child of p: processed next
@@ -313,22 +316,25 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
         SS s = D6[6 * r] * u6[0];
 #pragma unroll
         for (int k = 1; k < 6; ++k) s += D6[6 * r + k] * u6[k];
-        SS w = UD6[r] * SS(a.v[0]);
+        SS w = UD6[r] * cvt<SS>(a.v[0]);
 #pragma unroll
-        for (int k = 1; k < 6; ++k) w += UD6[6 * k + r] * SS(a.v[k]);
+        for (int k = 1; k < 6; ++k) w += UD6[6 * k + r] * cvt<SS>(a.v[k]);
         dd[r] = s - w;
         ddq[iv + r] = double(dd[r]);
       }
 #pragma unroll
-      for (int r = 0; r < 6; ++r) a.v[r] += S(dd[r]);
+      for (int r = 0; r < 6; ++r) a.v[r] += cvt<S>(dd[r]);
     } else {
       const int ax = jt - JT_RX;
       S w = UDs[i][0] * a.v[0];
 #pragma unroll
       for (int k = 1; k < 6; ++k) w += UDs[i][k] * a.v[k];
-      const SS dd = du[i] - SS(w);
+      const SS dd = du[i] - cvt<SS>(w);
       ddq[iv] = double(dd);
-      a.v[3 + ax] += S(dd);
+      const S dds = cvt<S>(dd);
+      a.v[3] += ax == 0 ? dds : S(0);
+      a.v[4] += ax == 1 ? dds : S(0);
+      a.v[5] += ax == 2 ? dds : S(0);
     }
     const int bs = m.bslot[i];
     if (bs >= 0) aslot[bs] = a;
@@ -371,7 +377,8 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
       }
     } else {
       const int ax = jt - JT_RX;
-      S w[3] = {O.R[ax], O.R[3 + ax], O.R[6 + ax]}, tw[3];
+      S w[3], tw[3];
+      axis_column(O, ax, w);
       cross3(O.t, w, tw);
       J[iv][0] = tw[0]; J[iv][1] = tw[1]; J[iv][2] = tw[2];
       J[iv][3] = w[0]; J[iv][4] = w[1]; J[iv][5] = w[2];

@@ -18,6 +18,50 @@
 
 namespace gb {
 
+// FP32 <-> FP64 conversions.  On the device the hardware conversions issue on
+// the FP64 pipe (a small fraction of the FP32 rate on GB300), so the exact
+// FP32 -> FP64 widening and the round-to-nearest-even FP64 -> FP32 narrowing
+// are done with integer instructions on the bit patterns (IEEE 754 binary32 /
+// binary64 layouts); zero takes the integer path too, and subnormal, infinite,
+// NaN and out-of-range values the hardware path.
+GB_HD double widen(float x) {
+#if defined(__CUDA_ARCH__)
+  const unsigned u = __float_as_uint(x);
+  const unsigned ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) {
+    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)x;
+  }
+  const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+#else
+  return (double)x;
+#endif
+}
+GB_HD float narrow(double x) {
+#if defined(__CUDA_ARCH__)
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  if (ex < 897u || ex > 1150u) {  // outside the normal FP32 range (or zero)
+    if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return (float)x;
+  }
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of the 52 fraction bits
+  const unsigned rest = lo & 0x1fffffffu;                      // the 29 bits dropped
+  unsigned r = (hi & 0x80000000u) | ((ex - 896u) << 23) | mant;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (mant & 1u))) r += 1u;  // carries into the exponent
+  return __uint_as_float(r);
+#else
+  return (float)x;
+#endif
+}
+
+// T(x) with the integer conversions between FP32 and FP64
+template <class T, class U> GB_HD T cvt(U x) { return T(x); }
+template <> GB_HD double cvt<double, float>(float x) { return widen(x); }
+template <> GB_HD float cvt<float, double>(double x) { return narrow(x); }
+
+
 // packed symmetric 3x3 index (xx, xy, yy, xz, yz, zz)
 GB_HD constexpr int s3(int r, int c) {
   return (r == 0 && c == 0) ? 0 : (r + c == 1) ? 1 : (r == 1 && c == 1) ? 2 : (r + c == 2) ? 3 : (r + c == 3) ? 4 : 5;
@@ -283,9 +327,9 @@ template <class S, class T> GB_HD void sym6_add(Sym6<S>& a, const Sym6<T>& b) {
 }
 template <class S, class T> GB_HD void sym6_convert(const Sym6<T>& b, Sym6<S>& a) {
 #pragma unroll
-  for (int k = 0; k < 6; ++k) { a.A[k] = S(b.A[k]); a.D[k] = S(b.D[k]); }
+  for (int k = 0; k < 6; ++k) { a.A[k] = cvt<S>(b.A[k]); a.D[k] = cvt<S>(b.D[k]); }
 #pragma unroll
-  for (int k = 0; k < 9; ++k) a.B[k] = S(b.B[k]);
+  for (int k = 0; k < 9; ++k) a.B[k] = cvt<S>(b.B[k]);
 }
 // R S R^T for a packed symmetric 3x3, straightforward two-stage product
 template <class S> GB_HD void sym3_rrt(const S* s, const S* R, S* o) {

@@ -111,11 +111,11 @@ extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const d
   return 0;
 }
 
-// Mirrors the device: sweeps with S (column-set storage), T (column-set
-// arithmetic), K (kinematics, Minv), SS = double (Schur), P (dtau); then the
-// product kernel, which writes Minv from the packed K copy and forms
-// -Minv * dtau in P over the structurally non-zero rows.
-template <class S, class T, class K, class P>
+// Mirrors the device: sweeps with S (column-set storage), T3 / T (column-set
+// arithmetic of passes 3 / 4), K (kinematics, Minv), SS = double (Schur), P
+// (dtau); then the product kernel, which writes Minv from the packed K copy
+// and forms -Minv * dtau in P over the structurally non-zero rows.
+template <class S, class T3, class T, class K, class P>
 static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const double* q, const double* v,
                             const double* tau, double* dq, double* dv, double* Minv, double* ddq,
                             std::vector<S>& wS, std::vector<K>& wK, std::vector<double>& wSS) {
@@ -124,7 +124,7 @@ static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const
   const long nn = (long)nv * nv;
   std::vector<P> wP(L.nP);
   const gb::Out dd = out_at(ddq, b, nv);
-  gb::aba_derivs_sweeps<S, T, K, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
+  gb::aba_derivs_sweeps<S, T3, T, K, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
                                             gb::Ws<double>{wSS.data(), 1}, gb::Ws<P>{wP.data(), 1},
                                             in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv), &dd);
   double* Mi = Minv + b * nn;
@@ -163,8 +163,8 @@ extern "C" int hs_aba_derivs(void* h, int mixed, long B, const double* q, const 
 #pragma omp for schedule(static)
     for (long b = 0; b < B; ++b) {
       if (mixed)
-        aba_derivs_host<float, gb::dfloat, gb::dfloat, float>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wfk, wss);
-      else aba_derivs_host<double, double, double, double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wdk, wss);
+        aba_derivs_host<float, float, gb::dfloat, gb::dfloat, float>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wfk, wss);
+      else aba_derivs_host<double, double, double, double, double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wdk, wss);
     }
   }
   return 0;
