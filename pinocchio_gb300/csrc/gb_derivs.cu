@@ -53,29 +53,39 @@ __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* b
 // that each keeps fewer values live than one fused kernel would (register use
 // bounds the number of resident warps).  The workspace carries everything
 // between them.
+// Blocked workspace layout of the arrays the product kernel reads (Minv,
+// dtau_dq, dtau_dv): configurations in blocks of kBlk, element e of
+// configuration b at ((b / kBlk) * n + e) * kBlk + b % kBlk for an array of n
+// elements -- a warp of the sweep kernels still accesses whole 32-byte
+// segments, and one block is contiguous for the product kernel.
+constexpr int kBlk = 8;
+template <class T> __device__ __forceinline__ gb::Ws<T> blocked(T* base, long n, long b) {
+  return gb::Ws<T>{base + (b / kBlk) * n * kBlk + (b % kBlk), kBlk};
+}
+
 template <class K, class SS>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
-    k_aba_derivs_pass12(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, SS* wsSS, Arr q,
-                        Arr v, Arr tau) {
+    k_aba_derivs_pass12(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, SS* wsSS, K* wsMB,
+                        int npk, Arr q, Arr v, Arr tau) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
-  gb::aba_derivs_pass12<K, SS>(m, L, gb::Ws<K>{wsK + b, B}, gb::Ws<SS>{wsSS + b, B}, in_at(q, b), in_at(v, b),
-                               in_at(tau, b));
+  gb::aba_derivs_pass12<K, SS>(m, L, gb::Ws<K>{wsK + b, B}, gb::Ws<SS>{wsSS + b, B}, blocked(wsMB, npk, b),
+                               in_at(q, b), in_at(v, b), in_at(tau, b));
 }
 
 template <class S, class T, class K>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
-    k_aba_derivs_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, Arr v,
-                       Arr ddq) {
+    k_aba_derivs_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, K* wsMB,
+                       int npk, Arr v, Arr ddq) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
   const gb::Out dd = out_at(ddq, b);
-  gb::aba_derivs_pass3<S, T, K>(m, L, m.slot, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, in_at(v, b),
-                                ddq.p ? &dd : nullptr);
+  gb::aba_derivs_pass3<S, T, K>(m, L, m.slot, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, blocked(wsMB, npk, b),
+                                in_at(v, b), ddq.p ? &dd : nullptr);
 }
 
 template <class S, class T, class K, class P>
@@ -85,144 +95,134 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
-  gb::aba_derivs_pass4<S, T, K, P>(m, L, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, gb::Ws<P>{wsP + b, B});
+  gb::aba_derivs_pass4<S, T, K, P>(m, L, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, blocked(wsP, L.nP, b));
 }
 
 __device__ __forceinline__ double to_double(double x) { return x; }
 __device__ __forceinline__ double to_double(float x) { return gb::widen(x); }
 __device__ __forceinline__ double to_double(gb::dfloat x) { return double(x); }
 
-// Minv and out_m = -Minv * X_m for the two matrices X_0 = dtau_dq, X_1 = dtau_dv
-// of G consecutive configurations per iteration (G a power of two).  smem:
-// Minv[G][nv*nv] (scalar S), then a region that first holds the packed upper
-// Minv of the workspace (scalar KM) and then X[G][NM][nv*nv] (scalar S), then
-// the column-group tables.  NM = number of the two products done per launch;
-// the launch with m0 == 0 also writes the symmetric Minv output.  A warp owns
-// one (configuration, matrix, column group); its lanes own rows (lane +
-// 32*chunk, NCH chunks); for every row k that can be non-zero in the group's
-// columns it loads one Minv row segment (lane-contiguous, Minv symmetric) and
-// the group's <= 8 entries of X's row k (broadcast) and does up to 8 FMAs per
-// lane.  With the instance layout each lane writes its row segment straight to
-// the output; with the SoA layout the result goes back to X and is stored with
-// the configurations contiguous.
-template <int NCH, class S, class W, class KM>
-__global__ void __launch_bounds__(512)
-    k_minv_products(const unsigned char* blob, long B, int lgG, int m0, int NM, const KM* wsMi, Arr Minv,
-                    const W* ws, long dtq, long dtv, Arr out0, Arr out1) {
+
+// Minv and out_m = -Minv * X_m for the two matrices X_0 = dtau_dq, X_1 = dtau_dv.
+// A CTA iteration takes Gs = 2^lgG (<= kBlk) configurations of one block; shared
+// memory holds them interleaved ([element][configuration]): the full Minv
+// (scalar S), then a region that first holds the packed upper Minv (scalar KM)
+// and then X for NM of the two matrices (scalar S), then the column-group
+// tables.  The launch with m0 == 0 also writes the symmetric Minv output.  A
+// warp task is (matrix, column group, 64 / Gs rows); lane = (row pair,
+// config), so the Minv and X reads are conflict-free; for every row k that
+// can be non-zero in the group's columns a lane loads two Minv entries and the
+// group's <= 8 entries of X's row k and does 16 FMAs; each lane writes its two
+// row segments.
+template <int LG, class S, class W, class KM>
+__global__ void __launch_bounds__(512, 2)
+    k_minv_products(const unsigned char* blob, long B, int m0, int NM, const KM* wsMi, Arr Minv, const W* wsP, long nP,
+                    long dtq, long dtv, Arr out0, Arr out1) {
+  constexpr int Gs = 1 << LG, R = 32 >> LG;  // configurations per iteration, rows per warp task
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(blob);
   const int nv = h->nv, ng = h->ngroup, nrel = h->n_grp_rel;
   const int nn = nv * nv, npk = nv * (nv + 1) / 2;
-  const int G = 1 << lgG;
   S* sM = reinterpret_cast<S*>(smem_raw);
-  unsigned char* region = reinterpret_cast<unsigned char*>(sM + (long)G * nn);
+  unsigned char* region = reinterpret_cast<unsigned char*>(sM + (long)nn * Gs);
   S* sX = reinterpret_cast<S*>(region);
   KM* sK = reinterpret_cast<KM*>(region);
-  const size_t region_bytes = max((size_t)G * npk * sizeof(KM), (size_t)G * NM * nn * sizeof(S));
+  const size_t region_bytes = max((size_t)npk * Gs * sizeof(KM), ((size_t)NM * nn + 8) * Gs * sizeof(S));
   int* sgrp = reinterpret_cast<int*>(region + ((region_bytes + 15) & ~(size_t)15));
   int* srel = sgrp + 4 * ng;
   for (int t = threadIdx.x; t < 4 * ng; t += blockDim.x) sgrp[t] = reinterpret_cast<const int*>(blob + h->o_grp)[t];
   for (int t = threadIdx.x; t < nrel; t += blockDim.x) srel[t] = reinterpret_cast<const int*>(blob + h->o_grp_rel)[t];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nwarps = blockDim.x / 32;
+  const int lr = lane >> LG, lg = lane & (Gs - 1);  // lane's row in the task, lane's configuration
+  const long nblk = (B + kBlk - 1) / kBlk, nit = nblk << (3 - LG);
   double* Mo = const_cast<double*>(Minv.p);
-  for (long b0 = (long)blockIdx.x * G; b0 < B; b0 += (long)gridDim.x * G) {
-    const int g_here = (int)min((long)G, B - b0);
+  const int nrc = (nv + R - 1) / R;        // row chunks of the Minv expansion
+  const int nrt = (nv + 2 * R - 1) / (2 * R);  // row chunks of the products: two rows per lane
+  const int rowstride = nv * Gs;           // between rows k of one matrix in shared memory
+  for (long it = blockIdx.x; it < nit; it += gridDim.x) {
+    const long blk = it >> (3 - LG);
+    const int g0 = (int)(it & ((kBlk >> LG) - 1)) << LG;
+    const long b0 = blk * kBlk + g0;
+    if (b0 >= B) continue;
+    const int g_here = (int)min((long)Gs, B - b0);
     __syncthreads();
-    // packed upper Minv of the workspace (SoA over the batch)
-    for (int t = threadIdx.x; t < (npk << lgG); t += blockDim.x) {
-      const int g = t & (G - 1), e = t >> lgG;
-      if (g < g_here) sK[g * npk + e] = wsMi[(long)e * B + b0 + g];
+    // packed upper Minv of the iteration's configurations (contiguous when Gs == kBlk)
+    {
+      const KM* src = wsMi + blk * (long)npk * kBlk + g0;
+      auto at = [&](int t) { return Gs == kBlk ? src[t] : src[(long)(t >> LG) * kBlk + (t & (Gs - 1))]; };
+      const int n = npk << LG, step = blockDim.x;
+      int t = threadIdx.x;
+      for (; t + 3 * step < n; t += 4 * step) {  // four loads in flight per thread
+        const KM a0 = at(t), a1 = at(t + step), a2 = at(t + 2 * step), a3 = at(t + 3 * step);
+        sK[t] = a0; sK[t + step] = a1; sK[t + 2 * step] = a2; sK[t + 3 * step] = a3;
+      }
+      for (; t < n; t += step) sK[t] = at(t);
     }
     __syncthreads();
-    // full symmetric Minv: S copy for the products, FP64 output (launch m0 == 0)
-    if (Minv.es == 1) {
-      for (int g = 0; g < g_here; ++g) {
-        double* dst = Mo + (b0 + g) * Minv.is;
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-          const int r = e / nv, c = e - r * nv;
-          const KM x = sK[g * npk + (r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r))];
-          sM[g * nn + e] = S(x);
-          if (m0 == 0) dst[e] = to_double(x);
-        }
-      }
-    } else {
-      for (int t = threadIdx.x; t < (nn << lgG); t += blockDim.x) {
-        const int g = t & (G - 1), e = t >> lgG;
-        if (g >= g_here) continue;
-        const int r = e / nv, c = e - r * nv;
-        const KM x = sK[g * npk + (r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r))];
-        sM[g * nn + e] = S(x);
-        if (m0 == 0) Mo[(b0 + g) + (long)e * Minv.es] = to_double(x);
-      }
+    // full symmetric Minv: S copy for the products, FP64 output (launch m0 == 0).
+    // A warp covers (row r, 32 / Gs columns) x Gs configurations.
+    for (int rc = warp; rc < nv * nrc; rc += nwarps) {
+      const int r = rc / nrc, c = (rc - r * nrc) * R + lr;
+      if (c >= nv) continue;
+      const KM x = sK[(r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r)) * Gs + lg];
+      sM[(r * nv + c) * Gs + lg] = S(x);
+      if (m0 == 0 && lg < g_here) Mo[(b0 + lg) * Minv.is + (long)(r * nv + c) * Minv.es] = to_double(x);
     }
     __syncthreads();
-    // the dtau matrices (workspace, SoA over the batch)
+    // the dtau matrices
     for (int mm = 0; mm < NM; ++mm) {
-      const W* src = ws + ((m0 + mm) == 0 ? dtq : dtv) * B + b0;
-      for (int t = threadIdx.x; t < (nn << lgG); t += blockDim.x) {
-        const int g = t & (G - 1), e = t >> lgG;
-        if (g < g_here) sX[(g * NM + mm) * nn + e] = S(src[(long)e * B + g]);
+      const W* src = wsP + blk * nP * kBlk + ((m0 + mm) == 0 ? dtq : dtv) * kBlk + g0;
+      S* dst = sX + (long)mm * nn * Gs;
+      auto at = [&](int t) { return S(Gs == kBlk ? src[t] : src[(long)(t >> LG) * kBlk + (t & (Gs - 1))]); };
+      const int n = nn << LG, step = blockDim.x;
+      int t = threadIdx.x;
+      for (; t + 3 * step < n; t += 4 * step) {
+        const S a0 = at(t), a1 = at(t + step), a2 = at(t + 2 * step), a3 = at(t + 3 * step);
+        dst[t] = a0; dst[t + step] = a1; dst[t + 2 * step] = a2; dst[t + 3 * step] = a3;
       }
+      for (; t < n; t += step) dst[t] = at(t);
     }
     __syncthreads();
-    const int ntask = g_here * NM * ng;
+    const int ntask = NM * ng * nrt;
     for (int task = warp; task < ntask; task += nwarps) {
-      const int g = task / (NM * ng), rem = task - g * (NM * ng), mm = rem / ng, gi = rem - mm * ng;
+      const int mm = task / (ng * nrt), rem = task - mm * (ng * nrt), gi = rem / nrt, rch = rem - gi * nrt;
+      const int r0 = rch * 2 * R + lr, r1 = r0 + R;
       const int c0 = sgrp[4 * gi], nc = sgrp[4 * gi + 1], k0 = sgrp[4 * gi + 2], k1 = sgrp[4 * gi + 3];
-      const S* Mg = sM + g * nn;
-      S* X = sX + (g * NM + mm) * nn;
-      S acc[NCH][8];
+      const S* Xg = sX + ((long)mm * nn + c0) * Gs + lg;
+      const S* M0 = sM + (r0 < nv ? r0 : 0) * Gs + lg;
+      const S* M1 = sM + (r1 < nv ? r1 : 0) * Gs + lg;
+      S acc0[8], acc1[8];
 #pragma unroll
-      for (int ch = 0; ch < NCH; ++ch)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[ch][c] = S(0);
+      for (int c = 0; c < 8; ++c) acc0[c] = acc1[c] = S(0);
+#pragma unroll 2
       for (int kk = k0; kk < k1; ++kk) {
-        const int k = srel[kk];
-        const S* Xk = X + k * nv + c0;
-        S x[8];
+        const int ko = srel[kk] * rowstride;
+        const S m0v = M0[ko], m1v = M1[ko];  // Minv(k, r) = Minv(r, k)
+        const S* Xk = Xg + ko;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) x[c] = c < nc ? Xk[c] : S(0);
-        const S* Mk = Mg + k * nv;
-#pragma unroll
-        for (int ch = 0; ch < NCH; ++ch) {
-          const int r = ch * 32 + lane;
-          const S mr = r < nv ? Mk[r] : S(0);
-#pragma unroll
-          for (int c = 0; c < 8; ++c) acc[ch][c] += mr * x[c];
+        for (int c = 0; c < 8; ++c) {  // past the group: padded, not stored
+          const S x = Xk[c * Gs];
+          acc0[c] += m0v * x;
+          acc1[c] += m1v * x;
         }
       }
+      if (lg >= g_here) continue;
       const Arr& o = (m0 + mm) == 0 ? out0 : out1;
-      if (o.es == 1) {
-        double* op = const_cast<double*>(o.p) + (b0 + g) * o.is + c0;
+      double* ob = const_cast<double*>(o.p) + (b0 + lg) * o.is + (long)c0 * o.es;
 #pragma unroll
-        for (int ch = 0; ch < NCH; ++ch) {
-          const int r = ch * 32 + lane;
-          if (r < nv)
+      for (int h2 = 0; h2 < 2; ++h2) {
+        const int r = h2 == 0 ? r0 : r1;
+        if (r >= nv) continue;
+        double* op = ob + (long)r * nv * o.es;
+        if (o.es == 1) {
 #pragma unroll
-            for (int c = 0; c < 8; ++c)
-              if (c < nc) op[r * nv + c] = -to_double(acc[ch][c]);
+          for (int c = 0; c < 8; ++c)
+            if (c < nc) op[c] = -to_double(h2 == 0 ? acc0[c] : acc1[c]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            if (c < nc) op[c * o.es] = -to_double(h2 == 0 ? acc0[c] : acc1[c]);
         }
-      } else {
-        __syncwarp();
-#pragma unroll
-        for (int ch = 0; ch < NCH; ++ch) {
-          const int r = ch * 32 + lane;
-          if (r < nv)
-#pragma unroll
-            for (int c = 0; c < 8; ++c)
-              if (c < nc) X[r * nv + c0 + c] = -acc[ch][c];
-        }
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    for (int mm = 0; mm < NM; ++mm) {
-      const Arr& o = (m0 + mm) == 0 ? out0 : out1;
-      if (o.es == 1) continue;
-      double* op = const_cast<double*>(o.p) + b0;
-      for (int t = threadIdx.x; t < (nn << lgG); t += blockDim.x) {
-        const int g = t & (G - 1), e = t >> lgG;
-        if (g < g_here) op[(long)e * o.es + g] = to_double(sX[(g * NM + mm) * nn + e]);
       }
     }
   }
@@ -261,15 +261,15 @@ int ws_alloc(Workspace& w, size_t bytes, cudaStream_t st) {
 
 // S: scalar of the products (smem, FMA); W: scalar of the dtau matrices in the
 // workspace; KM: scalar of the packed Minv in the workspace
-template <int NCH, class S, class W, class KM>
-int launch_minv_products_n(const gb_model* M, long B, const KM* wsMi, Arr Minv, const W* ws, const gb::DerivLayout& L,
-                           Arr o0, Arr o1, cudaStream_t st) {
+template <class S, class W, class KM>
+int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, const W* wsP,
+                         const gb::DerivLayout& L, Arr o0, Arr o1, cudaStream_t st) {
   const long nn = (long)M->nv * M->nv, npk = (long)M->nv * (M->nv + 1) / 2;
   const int ngroup = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->ngroup;
   const int nrel = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->n_grp_rel;
   auto smem_of = [&](long G, int NM) {
-    const long region = std::max(G * npk * (long)sizeof(KM), G * NM * nn * (long)sizeof(S));
-    return G * nn * (long)sizeof(S) + ((region + 15) & ~15L) + (long)sizeof(int) * (4 * ngroup + nrel);
+    const long region = std::max(npk * G * (long)sizeof(KM), (NM * nn + 8) * G * (long)sizeof(S));
+    return nn * G * (long)sizeof(S) + ((region + 15) & ~15L) + (long)sizeof(int) * (4 * ngroup + nrel);
   };
 #ifndef GB_MINV_SMEM_KB
 #define GB_MINV_SMEM_KB 100
@@ -280,27 +280,26 @@ int launch_minv_products_n(const gb_model* M, long B, const KM* wsMi, Arr Minv, 
   if (smem_of(1L << lgG, NM) > budget) NM = 1;
   if (smem_of(1L << lgG, NM) > 220 * 1024) return set_error(GB_ERR_UNSUPPORTED, "nv too large for the Minv products");
   const long G = 1L << lgG;
-  const int threads = 32 * (int)std::min<long>(G * NM * ngroup, 16);
   const size_t smem = (size_t)smem_of(G, NM);
-  cudaError_t e =
-      cudaFuncSetAttribute(k_minv_products<NCH, S, W, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const void* kern = lgG == 3 ? (const void*)k_minv_products<3, S, W, KM>
+                   : lgG == 2 ? (const void*)k_minv_products<2, S, W, KM>
+                   : lgG == 1 ? (const void*)k_minv_products<1, S, W, KM>
+                              : (const void*)k_minv_products<0, S, W, KM>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "k_minv_products");
-  const long grid = std::min<long>((B + G - 1) / G, 152L * 2 * 8);
+  const long nit = ((B + kBlk - 1) / kBlk) * (kBlk / G);
+  const long grid = std::min<long>(nit, 152L * 2 * 8);
   for (int m0 = 0; m0 < 2; m0 += NM) {
-    k_minv_products<NCH, S, W, KM><<<(unsigned)grid, threads, smem, st>>>(M->d_blob, B, lgG, m0, NM, wsMi, Minv, ws,
-                                                                           L.dtq, L.dtv, o0, o1);
+    const unsigned char* bl = M->d_blob;
+    const long nP = L.nP, dtq = L.dtq, dtv = L.dtv;
+    if (lgG == 3) k_minv_products<3, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
+    else if (lgG == 2) k_minv_products<2, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
+    else if (lgG == 1) k_minv_products<1, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
+    else k_minv_products<0, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
     const int rc = cuda_error(cudaGetLastError(), "k_minv_products");
     if (rc != GB_OK) return rc;
   }
   return GB_OK;
-}
-
-template <class S, class W, class KM>
-int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, const W* ws, const gb::DerivLayout& L,
-                         Arr o0, Arr o1, cudaStream_t st) {
-  if (M->nv <= 32) return launch_minv_products_n<1, S, W, KM>(M, B, wsMi, Minv, ws, L, o0, o1, st);
-  if (M->nv <= 64) return launch_minv_products_n<2, S, W, KM>(M, B, wsMi, Minv, ws, L, o0, o1, st);
-  return launch_minv_products_n<4, S, W, KM>(M, B, wsMi, Minv, ws, L, o0, o1, st);
 }
 
 template <class S>
@@ -320,27 +319,42 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   return cuda_error(cudaGetLastError(), "k_rnea_derivs");
 }
 
-// Workspace of the ABA derivatives: region SS (articulated inertias and u:
-// FP64), region K (kinematics, Fcrb columns, Minv, U Dinv, Dinv u, velocity /
-// acceleration), region S (the derivative column sets stored between passes 3
-// and 4: computed in T3 by pass 3 and in T by pass 4) and region P (dtau_dq,
-// dtau_dv in the scalar of the -Minv*dtau products).  The mixed kernels use
-// K = T = dfloat, S = T3 = P = float.
-template <class S, class T, class K, class SS, class P>
-size_t aba_ws_bytes(const gb::DerivLayout& L, long B) {
-  return (sizeof(SS) * (size_t)L.nSS + sizeof(K) * (size_t)L.nK + sizeof(S) * (size_t)L.nS +
-          sizeof(P) * (size_t)L.nP) *
-         (size_t)B;
+// Workspace of the ABA derivatives, regions 256-byte aligned: SS (articulated
+// inertias and u: FP64), K (kinematics, Fcrb columns, U Dinv, Dinv u, velocity
+// / acceleration), S (the derivative column sets stored between passes 3 and
+// 4: computed in T3 by pass 3 and in T by pass 4) -- these three [element]
+// [configuration] -- and, in the blocked layout the product kernel reads, MB
+// (the packed upper Minv, scalar K) and P (dtau_dq, dtau_dv in the scalar of
+// the -Minv*dtau products).  The mixed kernels use K = T = dfloat and
+// S = T3 = P = float.
+struct AbaWs {
+  size_t oK, oS, oMB, oP, bytes;
+};
+template <class S, class K, class SS, class P>
+AbaWs aba_ws_layout(const gb::DerivLayout& L, int nv, long B) {
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t Bp = (size_t)((B + kBlk - 1) / kBlk) * kBlk;
+  AbaWs w;
+  w.oK = up(sizeof(SS) * (size_t)L.nSS * B);
+  w.oS = w.oK + up(sizeof(K) * (size_t)L.nK * B);
+  w.oMB = w.oS + up(sizeof(S) * (size_t)L.nS * B);
+  w.oP = w.oMB + up(sizeof(K) * (size_t)nv * (nv + 1) / 2 * Bp);
+  w.bytes = w.oP + up(sizeof(P) * (size_t)L.nP * Bp);
+  return w;
 }
 
 template <class S, class T3, class T, class K, class SS, class P>
 int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq, void* ws,
                          cudaStream_t st) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  SS* wsSS = static_cast<SS*>(ws);
-  K* wsK = reinterpret_cast<K*>(static_cast<char*>(ws) + sizeof(SS) * (size_t)L.nSS * B);
-  S* wsS = reinterpret_cast<S*>(reinterpret_cast<char*>(wsK) + sizeof(K) * (size_t)L.nK * B);
-  P* wsP = reinterpret_cast<P*>(reinterpret_cast<char*>(wsS) + sizeof(S) * (size_t)L.nS * B);
+  const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, B);
+  char* base = static_cast<char*>(ws);
+  SS* wsSS = reinterpret_cast<SS*>(base);
+  K* wsK = reinterpret_cast<K*>(base + W.oK);
+  S* wsS = reinterpret_cast<S*>(base + W.oS);
+  K* wsMB = reinterpret_cast<K*>(base + W.oMB);
+  P* wsP = reinterpret_cast<P*>(base + W.oP);
+  const int npk = M->nv * (M->nv + 1) / 2;
   const int tpb = M->tpb[GB_FUNC_ABA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
   int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS>, "k_aba_derivs_pass12");
@@ -348,18 +362,18 @@ int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr d
   if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, T, K, P>, "k_aba_derivs_pass4");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass12<K, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK, wsSS,
-                                                                             q, v, tau);
+                                                                             wsMB, npk, q, v, tau);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass3<S, T3, K><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
-                                                                               wsK, v, ddq);
+                                                                               wsK, wsMB, npk, v, ddq);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass3");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass4<S, T, K, P><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
                                                                                  wsK, wsP);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass4");
   if (rc != GB_OK) return rc;
-  return launch_minv_products<P, P, K>(M, B, wsK + (long)L.Mi * B, Minv, wsP, L, dq, dv, st);
+  return launch_minv_products<P, P, K>(M, B, wsMB, Minv, wsP, L, dq, dv, st);
 }
 
 template <class S, class T3, class T, class K, class SS, class P>
@@ -367,7 +381,7 @@ int run_aba_derivs(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr
                    cudaStream_t st) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   Workspace ws;
-  int rc = ws_alloc(ws, aba_ws_bytes<S, T, K, SS, P>(L, B), st);
+  int rc = ws_alloc(ws, aba_ws_layout<S, K, SS, P>(L, M->nv, B).bytes, st);
   if (rc != GB_OK) return rc;
   return launch_aba_derivs_ws<S, T3, T, K, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st);
 }
@@ -381,11 +395,11 @@ int check_gravity(const gb_model* M) {
 }  // namespace
 
 // The ABA-derivative kernels on a workspace the caller provides (no allocation):
-// bytes needed per configuration, and the launch itself.
-size_t aba_derivs_workspace_bytes(const gb_model* M, int precision) {
+// total bytes needed for a batch, and the launch itself.
+size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  return precision == GB_FP64 ? aba_ws_bytes<double, double, double, double, double>(L, 1)
-                              : aba_ws_bytes<float, gb::dfloat, gb::dfloat, double, float>(L, 1);
+  return precision == GB_FP64 ? aba_ws_layout<double, double, double, double>(L, M->nv, B).bytes
+                              : aba_ws_layout<float, gb::dfloat, double, float>(L, M->nv, B).bytes;
 }
 
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,

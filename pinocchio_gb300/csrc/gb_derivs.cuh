@@ -50,6 +50,17 @@ GB_HD dfloat dot6(const dfloat* a, const dfloat* b) {
   for (int k = 1; k < 6; ++k) d.add(a[k], b[k]);
   return d.result();
 }
+// a . x + b . y for 6-vectors (one compensated accumulation for double-float)
+template <class T> GB_HD T dot6x2(const T* a, const T* x, const T* b, const T* y) { return dot6(a, x) + dot6(b, y); }
+GB_HD dfloat dot6x2(const dfloat* a, const dfloat* x, const dfloat* b, const dfloat* y) {
+  dacc d;
+  d.first(a[0], x[0]);
+#pragma unroll
+  for (int k = 1; k < 6; ++k) d.add(a[k], x[k]);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d.add(b[k], y[k]);
+  return d.result();
+}
 
 // Element offsets of the per-instance workspace.
 // "K" arrays are the world-frame forward kinematics (root-origin frame): oMi,
@@ -69,8 +80,9 @@ struct DerivLayout {
   int nS, nP;
   // ABA only: region SS (articulated inertias and the bias u of the Schur
   // complement) and region K (kinematics, the Fcrb columns of the Minv
-  // recursion, Minv itself as a packed upper triangle, U Dinv and Dinv u)
-  int Ia, u, F0, Fslot, nslot, Mi, UD, Du;
+  // recursion, U Dinv and Dinv u); Minv itself (a packed upper triangle of
+  // nv (nv + 1) / 2 values in K) has a region of its own
+  int Ia, u, F0, Fslot, nslot, UD, Du;
   int nSS, nK;
 };
 
@@ -102,7 +114,6 @@ inline DerivLayout make_deriv_layout(int nj, int nv, int nslot, bool aba) {
   L.F0 = aba ? takeKr(6 * nv) : 0;
   L.nslot = nslot;
   L.Fslot = aba ? takeKr(6 * nv * nslot) : 0;
-  L.Mi = aba ? takeKr(nv * (nv + 1) / 2) : 0;
   L.UD = aba ? takeKr(6 * nv) : 0;
   L.Du = aba ? takeKr(nv) : 0;
   L.nSS = oSS;
@@ -607,8 +618,8 @@ template <class T, class S> GB_HD void shift_operator_add(const Ws<S>& w, long s
 
 // ------------------------------------------------------------------------------------------
 // The four sweeps of computeABADerivatives (aba-derivatives.hxx:380-449): ddq,
-// Minv (packed upper triangle, workspace region K) and dtau_dq / dtau_dv (at
-// (q, v, ddq), region P); the products -Minv dtau_dq, -Minv dtau_dv and the
+// Minv (packed upper triangle, workspace zm) and dtau_dq / dtau_dv (at
+// (q, v, ddq), workspace wp); the products -Minv dtau_dq, -Minv dtau_dv and the
 // symmetric Minv output are written by a separate batched kernel.
 // `slot[i]` is the Fcrb slot of joint i (a last child reuses its parent's slot).
 //
@@ -636,8 +647,8 @@ template <class SS> GB_HD void st_sym6(const Ws<SS>& zs, long e, const Sym6<SS>&
 }
 
 // Minv(r, c) from the packed upper triangle (symmetric)
-template <class K> GB_HD K minv_at(const DerivLayout& L, const Ws<K>& zk, int nv, int r, int c) {
-  return r <= c ? zk[L.Mi + upk(nv, r, c)] : zk[L.Mi + upk(nv, c, r)];
+template <class K> GB_HD K minv_at(const Ws<K>& zm, int nv, int r, int c) {
+  return r <= c ? zm[upk(nv, r, c)] : zm[upk(nv, c, r)];
 }
 
 // One joint of pass 2 (ComputeABADerivativesBackwardStep1, hxx:87-171) with
@@ -646,7 +657,8 @@ template <class K> GB_HD K minv_at(const DerivLayout& L, const Ws<K>& zk, int nv
 // columns of its subtree (-SDinv^T Fcrb); the columns right of the subtree are
 // first written by pass 3.
 template <int NVJ, class K, class SS>
-GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs, int i) {
+GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
+                                  const Ws<K>& zm, int i) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
   Sym6<SS> Ia;
@@ -703,7 +715,7 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
 #pragma unroll 1
   for (int r = 0; r < NVJ; ++r)
 #pragma unroll 1
-    for (int c = r; c < NVJ; ++c) zk[L.Mi + upk(nv, iv + r, iv + c)] = K(Dinv[r * NVJ + c]);
+    for (int c = r; c < NVJ; ++c) zm[upk(nv, iv + r, iv + c)] = K(Dinv[r * NVJ + c]);
   const int nch = nst - NVJ;
   if (nch > 0) {
     K SD[NVJ][6];  // SDinv columns = J Dinv
@@ -721,7 +733,7 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
       K F[6];
       ld6(zk, L.F0 + 6 * c, F);
 #pragma unroll 1
-      for (int r = 0; r < NVJ; ++r) zk[L.Mi + upk(nv, iv + r, c)] = -dot6(SD[r], F);
+      for (int r = 0; r < NVJ; ++r) zm[upk(nv, iv + r, c)] = -dot6(SD[r], F);
     }
   }
   if (!(nch > 0 && p == 0)) {  // leaf: F = U Minv_rows; inner joint with a parent: F += U Minv_rows
@@ -736,7 +748,7 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
       if (nch > 0) ld6(zk, L.F0 + 6 * c, F);
 #pragma unroll 1
       for (int k = 0; k < NVJ; ++k) {
-        const K mk = minv_at(L, zk, nv, iv + k, c);
+        const K mk = minv_at(zm, nv, iv + k, c);
 #pragma unroll
         for (int r = 0; r < 6; ++r) F[r] += Uk[k][r] * mk;
       }
@@ -775,8 +787,8 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
 }
 
 template <class K, class SS>
-GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs, const In& q,
-                             const In& v, const In& tau) {
+GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
+                             const Ws<K>& zm, const In& q, const In& v, const In& tau) {
   const int nv = m.nv;
   // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K
   world_forward<K>(m, L, zk, q, v, nullptr, false);
@@ -793,8 +805,8 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
   // ---- pass 2: ComputeABADerivativesBackwardStep1 (hxx:87-171)
 #pragma unroll 1
   for (int i = m.nj - 1; i > 0; --i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass2_joint<6, K, SS>(m, L, zk, zs, i);
-    else aba_derivs_pass2_joint<1, K, SS>(m, L, zk, zs, i);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass2_joint<6, K, SS>(m, L, zk, zs, zm, i);
+    else aba_derivs_pass2_joint<1, K, SS>(m, L, zk, zs, zm, i);
   }
 }
 
@@ -802,7 +814,8 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
 // degrees of freedom.
 template <int NVJ, class S, class T, class K>
 GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                                  const Ws<K>& zk, const In& v, const Out* ddq_out, const K* gk, int i) {
+                                  const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out, const K* gk,
+                                  int i) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
   K ti[3];
@@ -869,9 +882,9 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     for (int c = iv; c < nv; ++c) {
       K Fpc[6];
       ld6(zk, Fp + 6 * c, Fpc);
-      const long e = L.Mi + upk(nv, iv, c);
-      const K mk = (c < iv + nst ? zk[e] : K(0)) - dot6(udk, Fpc);
-      zk[e] = mk;
+      const long e = upk(nv, iv, c);
+      const K mk = (c < iv + nst ? zm[e] : K(0)) - dot6(udk, Fpc);
+      zm[e] = mk;
 #pragma unroll
       for (int r = 0; r < 6; ++r) Fpc[r] += Jo[0][r] * mk;
       st6(zk, Fi + 6 * c, Fpc);
@@ -883,13 +896,13 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
       if (c < iv + nst) {
 #pragma unroll 1
         for (int k = 0; k < NVJ; ++k) {
-          const K mk = minv_at(L, zk, nv, iv + k, c);
+          const K mk = minv_at(zm, nv, iv + k, c);
 #pragma unroll
           for (int r = 0; r < 6; ++r) Fn[r] += Jo[k][r] * mk;
         }
       } else {
 #pragma unroll 1
-        for (int k = 0; k < NVJ; ++k) zk[L.Mi + upk(nv, iv + k, c)] = K(0);
+        for (int k = 0; k < NVJ; ++k) zm[upk(nv, iv + k, c)] = K(0);
       }
       st6(zk, Fi + 6 * c, Fn);
     }
@@ -948,7 +961,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
 
 template <class S, class T, class K>
 GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                            const Ws<K>& zk, const In& v, const Out* ddq_out) {
+                            const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out) {
   // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
   // velocity / acceleration recursion runs in K in floating origins and
   // replaces ov / oa in K; the column sets, link inertia, momentum, force and
@@ -956,8 +969,8 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
   const K* gk = ModelScalar<K>::grav(m);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K>(m, L, slot, w, zk, v, ddq_out, gk, i);
-    else aba_derivs_pass3_joint<1, S, T, K>(m, L, slot, w, zk, v, ddq_out, gk, i);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
+    else aba_derivs_pass3_joint<1, S, T, K>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
   }
 }
 
@@ -1003,21 +1016,23 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
       st6(w, L.dFda + 6 * c, y);  // dFda
     }
   }
-  // row block: dtau(i, subtree) = J_i^T dF_c, with dF_c moved from its joint's position to t_i
+  // row block: dtau(i, subtree) = J_i^T dF_c, with dF_c moved from its joint's
+  // position to t_i: J . (f_lin, f_ang + d x f_lin) = (J_lin + J_ang x d, J_ang) . f
 #pragma unroll 1
   for (int r = 0; r < NVJ; ++r) {
     T Jr[6];
     ldc6(w, L.cJ + 6 * (iv + r), Jr);
 #pragma unroll 1
     for (int c = iv; c < iv + nst; ++c) {
-      T d[3], x[6], y[6];
+      T d[3], u[6], x[6];
       joint_offset(L, zk, m.dof_joint[c], i, d);
+      cross3(Jr + 3, d, u);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { u[k] += Jr[k]; u[3 + k] = Jr[3 + k]; }
       ldc6(w, L.dFdv + 6 * c, x);
-      shift_force(x, d, y);
-      wp[L.dtv + (iv + r) * nv + c] = P(dot6(Jr, y));
+      wp[L.dtv + (iv + r) * nv + c] = P(dot6(u, x));
       ldc6(w, L.dFdq + 6 * c, x);
-      shift_force(x, d, y);
-      wp[L.dtq + (iv + r) * nv + c] = P(dot6(Jr, y));
+      wp[L.dtq + (iv + r) * nv + c] = P(dot6(u, x));
     }
   }
   {
@@ -1046,20 +1061,27 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
       ldc6(w, L.cJ + 6 * (iv + r), Jr);
       mat6_tmv(w, L.doY + 36 * i, Jr, StdY);
     }
+    // f . (m_lin - d x m_ang, m_ang) = (f_lin, f_ang - f_lin x d) . m for the
+    // motion m of ancestor j moved from t_j to t_i (d = t_i - t_j)
 #pragma unroll 1
     for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j]) {
-      T d[3], x[6], y[6], xs[6], ys[6];
+      T d[3], fs[6], Ss[6], x[6], y[6];
       joint_offset(L, zk, i, m.dof_joint[j], d);
+      cross3(fa, d, fs + 3);
+      cross3(StdY, d, Ss + 3);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        fs[k] = fa[k];
+        fs[3 + k] = fa[3 + k] - fs[3 + k];
+        Ss[k] = StdY[k];
+        Ss[3 + k] = StdY[3 + k] - Ss[3 + k];
+      }
       ldc6(w, L.dAdq + 6 * j, x);
       ldc6(w, L.dVdq + 6 * j, y);
-      shift_motion(x, d, xs);
-      shift_motion(y, d, ys);
-      wp[L.dtq + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
+      wp[L.dtq + (iv + r) * nv + j] = P(dot6x2(fs, x, Ss, y));
       ldc6(w, L.dAdv + 6 * j, x);
       ldc6(w, L.cJ + 6 * j, y);
-      shift_motion(x, d, xs);
-      shift_motion(y, d, ys);
-      wp[L.dtv + (iv + r) * nv + j] = P(dot6(fa, xs) + dot6(StdY, ys));
+      wp[L.dtv + (iv + r) * nv + j] = P(dot6x2(fs, x, Ss, y));
     }
   }
   // accumulate into the parent, moved from t_i to t_p
@@ -1105,10 +1127,10 @@ GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w
 // T3: arithmetic of the column sets in pass 3; T: arithmetic of pass 4
 template <class S, class T3, class T, class K, class SS, class P>
 GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                             const Ws<K>& zk, const Ws<SS>& zs, const Ws<P>& wp, const In& q, const In& v,
-                             const In& tau, const Out* ddq_out) {
-  aba_derivs_pass12<K, SS>(m, L, zk, zs, q, v, tau);
-  aba_derivs_pass3<S, T3, K>(m, L, slot, w, zk, v, ddq_out);
+                             const Ws<K>& zk, const Ws<SS>& zs, const Ws<K>& zm, const Ws<P>& wp, const In& q,
+                             const In& v, const In& tau, const Out* ddq_out) {
+  aba_derivs_pass12<K, SS>(m, L, zk, zs, zm, q, v, tau);
+  aba_derivs_pass3<S, T3, K>(m, L, slot, w, zk, zm, v, ddq_out);
   aba_derivs_pass4<S, T, K, P>(m, L, w, zk, wp);
 }
 

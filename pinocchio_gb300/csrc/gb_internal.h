@@ -42,7 +42,7 @@ int launch_rnea(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, A
 int launch_aba(const gb_model* m, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
 int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q, Arr M, Arr U, Arr D, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
-size_t aba_derivs_workspace_bytes(const gb_model* M, int precision);
+size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B);
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
                                    Arr Minv, Arr ddq, void* ws, cudaStream_t st);
 

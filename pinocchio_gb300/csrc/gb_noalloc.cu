@@ -66,7 +66,7 @@ int gb_aba_derivatives_noalloc(const gb_model* M, int precision, int layout, lon
   int rc = gbi::check_common(M, precision, layout, B);
   if (rc != GB_OK) return rc;
   if (B == 0) return GB_OK;
-  const size_t need = gbi::aba_derivs_workspace_bytes(M, precision) * (size_t)B;
+  const size_t need = gbi::aba_derivs_workspace_bytes(M, precision, B);
   if (need > kNoAllocScratchBytes)
     return gbi::set_error(GB_ERR_SIZE, "gb_aba_derivatives_noalloc: batch " + std::to_string(B) + " needs " +
                                            std::to_string(need) + " bytes of workspace, the fixed scratch holds " +

@@ -124,14 +124,16 @@ static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const
   const long nn = (long)nv * nv;
   std::vector<P> wP(L.nP);
   const gb::Out dd = out_at(ddq, b, nv);
+  std::vector<K> wM(nv * (nv + 1) / 2);
   gb::aba_derivs_sweeps<S, T3, T, K, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
-                                            gb::Ws<double>{wSS.data(), 1}, gb::Ws<P>{wP.data(), 1},
-                                            in_at(q, b, m.nq), in_at(v, b, nv), in_at(tau, b, nv), &dd);
+                                                gb::Ws<double>{wSS.data(), 1}, gb::Ws<K>{wM.data(), 1},
+                                                gb::Ws<P>{wP.data(), 1}, in_at(q, b, m.nq), in_at(v, b, nv),
+                                                in_at(tau, b, nv), &dd);
   double* Mi = Minv + b * nn;
   std::vector<P> Mp(nn);
   for (int r = 0; r < nv; ++r)
     for (int c = 0; c < nv; ++c) {
-      const K x = wK[L.Mi + (r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r))];
+      const K x = wM[r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r)];
       Mi[r * nv + c] = to_double(x);
       Mp[r * nv + c] = P(x);
     }
