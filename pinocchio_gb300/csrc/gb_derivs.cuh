@@ -553,67 +553,64 @@ template <class S> GB_HD void shift_force_from_origin(const S* f, const S* t, S*
 #pragma unroll
   for (int k = 0; k < 3; ++k) { o[k] = f[k]; o[3 + k] = f[3 + k] - txf[k]; }
 }
-// a motion->force operator M (row-major 6x6) about point C re-expressed about
-// P with r = C - P:  [[A, B - A R], [C + R A, D + R B - C R - R A R]], R = [r]x,
-// added to the operator stored at `dst` (both row-major in the workspace).
-// Row a of X R is x_a x r (x_a = row a of X); column b of R X is r x (column b
-// of X).  The blocks are streamed so that at most three 3x3 blocks are live.
-template <class T, class S> GB_HD void shift_operator_add(const Ws<S>& w, long src, long dst, const T* r) {
-  auto ld3x3 = [&](int r0, int c0, T* X) {
+// The composite inertia variation doY = sum over the subtree of shifted
+// (Y.variation(v) + force-cross(h)) has a zero linear-linear block: each
+// link's term does (its lin-lin block is zero) and a shift keeps that block.
+// The operators below read and write only the other three blocks B (lin-ang),
+// C (ang-lin) and D (ang-ang) of such a row-major 6x6.
+template <class T, class S> GB_HD void op0_mv(const Ws<S>& w, long e, const T* x, T* y) {  // y = M x
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+  for (int r = 0; r < 3; ++r) {
+    y[r] = dot3(T(w[e + 6 * r + 3]), x[3], T(w[e + 6 * r + 4]), x[4], T(w[e + 6 * r + 5]), x[5]);
+    T row[6];
 #pragma unroll
-      for (int b = 0; b < 3; ++b) X[3 * a + b] = T(w[src + 6 * (r0 + a) + c0 + b]);
-  };
-  auto add3x3 = [&](int r0, int c0, const T* X) {
+    for (int k = 0; k < 6; ++k) row[k] = T(w[e + 6 * (3 + r) + k]);
+    y[3 + r] = dot6(row, x);
+  }
+}
+template <class T, class S> GB_HD void op0_tmv(const Ws<S>& w, long e, const T* x, T* y) {  // y = M^T x
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+  for (int c = 0; c < 3; ++c) {
+    y[c] = dot3(T(w[e + 18 + c]), x[3], T(w[e + 24 + c]), x[4], T(w[e + 30 + c]), x[5]);
+    T col[6];
 #pragma unroll
-      for (int b = 0; b < 3; ++b) w[dst + 6 * (r0 + a) + c0 + b] = S(T(w[dst + 6 * (r0 + a) + c0 + b]) + X[3 * a + b]);
-  };
-  auto mulR = [&](const T* X, T* Y) {  // X R
+    for (int k = 0; k < 6; ++k) col[k] = T(w[e + 6 * k + 3 + c]);
+    y[3 + c] = dot6(col, x);
+  }
+}
+// dst += the operator at src (about C) re-expressed about P, r = C - P:
+// [[0, B], [C, D + R B - C R]], R = [r]x
+template <class T, class S> GB_HD void op0_shift_add(const Ws<S>& w, long src, long dst, const T* r) {
+  T Bm[9], Cm[9], Dacc[9];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      Y[3 * a + 0] = dot2(X[3 * a + 1], r[2], -X[3 * a + 2], r[1]);
-      Y[3 * a + 1] = dot2(X[3 * a + 2], r[0], -X[3 * a + 0], r[2]);
-      Y[3 * a + 2] = dot2(X[3 * a + 0], r[1], -X[3 * a + 1], r[0]);
-    }
-  };
-  auto Rmul = [&](const T* X, T* Y) {  // R X
+  for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      Y[0 + b] = dot2(r[1], X[6 + b], -r[2], X[3 + b]);
-      Y[3 + b] = dot2(r[2], X[0 + b], -r[0], X[6 + b]);
-      Y[6 + b] = dot2(r[0], X[3 + b], -r[1], X[0 + b]);
+      Bm[3 * a + b] = T(w[src + 6 * a + 3 + b]);
+      Cm[3 * a + b] = T(w[src + 6 * (3 + a) + b]);
+      Dacc[3 * a + b] = T(w[src + 6 * (3 + a) + 3 + b]);
     }
-  };
-  T X[9], Y[9], Dacc[9];
-  // A: top-left unchanged; B - A R; C + R A; -R A R into the D block
-  ld3x3(0, 0, X);
-  add3x3(0, 0, X);
-  mulR(X, Y);
-  ld3x3(0, 3, Dacc);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Dacc[k] -= Y[k];
-  add3x3(0, 3, Dacc);
-  Rmul(X, Y);
-  ld3x3(3, 0, Dacc);
+  for (int b = 0; b < 3; ++b) {  // + R B (column b: r x B_b) and - C R (row a: C_a x r)
+    Dacc[0 + b] += dot2(r[1], Bm[6 + b], -r[2], Bm[3 + b]);
+    Dacc[3 + b] += dot2(r[2], Bm[0 + b], -r[0], Bm[6 + b]);
+    Dacc[6 + b] += dot2(r[0], Bm[3 + b], -r[1], Bm[0 + b]);
+  }
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Dacc[k] += Y[k];
-  add3x3(3, 0, Dacc);
-  mulR(Y, X);  // R A R
-  ld3x3(3, 3, Dacc);
+  for (int a = 0; a < 3; ++a) {
+    Dacc[3 * a + 0] -= dot2(Cm[3 * a + 1], r[2], -Cm[3 * a + 2], r[1]);
+    Dacc[3 * a + 1] -= dot2(Cm[3 * a + 2], r[0], -Cm[3 * a + 0], r[2]);
+    Dacc[3 * a + 2] -= dot2(Cm[3 * a + 0], r[1], -Cm[3 * a + 1], r[0]);
+  }
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Dacc[k] -= X[k];
-  ld3x3(0, 3, X);  // + R B
-  Rmul(X, Y);
+  for (int a = 0; a < 3; ++a)
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Dacc[k] += Y[k];
-  ld3x3(3, 0, X);  // - C R
-  mulR(X, Y);
-#pragma unroll
-  for (int k = 0; k < 9; ++k) Dacc[k] -= Y[k];
-  add3x3(3, 3, Dacc);
+    for (int b = 0; b < 3; ++b) {
+      const long eb = dst + 6 * a + 3 + b, ec = dst + 6 * (3 + a) + b, ed = dst + 6 * (3 + a) + 3 + b;
+      w[eb] = S(T(w[eb]) + Bm[3 * a + b]);
+      w[ec] = S(T(w[ec]) + Cm[3 * a + b]);
+      w[ed] = S(T(w[ed]) + Dacc[3 * a + b]);
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -631,7 +628,7 @@ template <class T, class S> GB_HD void shift_operator_add(const Ws<S>& w, long s
 // floating origins: every quantity of joint i is expressed about joint i's
 // position t_i (world orientation), so that no reduced-precision value
 // carries the lever arm of a distant origin; contributions move between
-// joints by translation (shift_motion / shift_force / shift_operator_add).
+// joints by translation (shift_motion / shift_force / op0_shift_add).
 // ------------------------------------------------------------------------------------------
 template <class SS> GB_HD void ld_sym6(const Ws<SS>& zs, long e, Sym6<SS>& I6) {
 #pragma unroll
@@ -956,7 +953,8 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   T dY[36];
   variation_plus_fcross(oY, ovs, oh, dY);
 #pragma unroll
-  for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = S(dY[k]);
+  for (int k = 0; k < 36; ++k)
+    if (k >= 18 || k % 6 >= 3) w[L.doY + 36 * i + k] = S(dY[k]);  // the lin-lin block is zero
 }
 
 template <class S, class T, class K>
@@ -999,7 +997,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
       ldc6(w, L.cJ + 6 * c, Jc);
       ldc6(w, L.dAdv + 6 * c, x);
       imul(oY, x, y);
-      mat6_mv(w, L.doY + 36 * i, Jc, t);
+      op0_mv(w, L.doY + 36 * i, Jc, t);
 #pragma unroll
       for (int r = 0; r < 6; ++r) y[r] += t[r];
       st6(w, L.dFdv + 6 * c, y);  // dFdv
@@ -1007,7 +1005,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
       imul(oY, x, y);
       if (p > 0) {
         ldc6(w, L.dVdq + 6 * c, x);
-        mat6_mv(w, L.doY + 36 * i, x, t);
+        op0_mv(w, L.doY + 36 * i, x, t);
 #pragma unroll
         for (int r = 0; r < 6; ++r) y[r] += t[r];
       }
@@ -1059,7 +1057,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
       T Jr[6];
       ldc6(w, L.dFda + 6 * (iv + r), fa);
       ldc6(w, L.cJ + 6 * (iv + r), Jr);
-      mat6_tmv(w, L.doY + 36 * i, Jr, StdY);
+      op0_tmv(w, L.doY + 36 * i, Jr, StdY);
     }
     // f . (m_lin - d x m_ang, m_ang) = (f_lin, f_ang - f_lin x d) . m for the
     // motion m of ancestor j moved from t_j to t_i (d = t_i - t_j)
@@ -1096,7 +1094,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
     iner_add(oYp, oYs, eps);
     stc_iner(w, L.coY + 10 * p, oYp);
   }
-  shift_operator_add(w, L.doY + 36 * i, L.doY + 36 * p, rr);
+  op0_shift_add(w, L.doY + 36 * i, L.doY + 36 * p, rr);
   {
     T of[6], ofs[6], ofp[6];
     ldc6(w, L.cof + 6 * i, of);
