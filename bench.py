@@ -10,6 +10,10 @@ Schur complement), inputs resident in HBM; the plain FP64 kernels are timed
 beside it (``fp64``) and both are checked against the FP64 oracle on a
 sample.  ``e2e`` is the same step through the public API with the inputs in
 pinned host memory and the outputs copied back to host memory every step.
+Beside the headline the line carries (unless --no-extra) the evals/s of every
+batched function per precision (``functions``), the heterogeneous
+single-launch batch over four trees (``heterogeneous``) and the differentiable
+rollout on the 100-link chain (``rollout``).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU
@@ -38,12 +42,14 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--batch", type=int, default=65536)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the per-function, heterogeneous-batch and rollout measurements")
     p.add_argument("--only", choices=["rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives"], default=None,
                    help="time one batched call on the humanoid (for profiling), print its timing and exit")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
@@ -194,6 +200,99 @@ def fp64_peak_tflops(torch):
     return 2.0 * n**3 / best / 1e12
 
 
+def _time_call(torch, fn, reps=5, warmup=2):
+    """Milliseconds per call of fn (CUDA events on the current stream, after warm-up)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def measure_functions(torch, pg, sm):
+    """evals/s of every batched function on the humanoid, per precision: RNEA / ABA /
+    CRBA (+ tree Cholesky) at batch 65536, the two derivative algorithms at batch 16384."""
+    model = sm.humanoid32(1)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        data = pg.createData(model, prec)
+        res = {}
+        for fname, B in (("rnea", 65536), ("aba", 65536), ("crba", 65536), ("crba_cholesky", 65536),
+                         ("rnea_derivatives", 16384), ("aba_derivatives", 16384)):
+            q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
+            fn = {
+                "rnea": lambda: pg.rnea(model, data, q, v, x),
+                "aba": lambda: pg.aba(model, data, q, v, 10.0 * x),
+                "crba": lambda: pg.crba(model, data, q),
+                "crba_cholesky": lambda: pg.crbaCholesky(model, data, q),
+                "rnea_derivatives": lambda: pg.computeRNEADerivatives(model, data, q, v, x),
+                "aba_derivatives": lambda: pg.computeABADerivatives(model, data, q, v, 10.0 * x),
+            }[fname]
+            ms = _time_call(torch, fn)
+            res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}
+            del q, v, x
+        out[prec] = res
+    return out
+
+
+def measure_heterogeneous(torch, pg, sm, total=100000):
+    """RNEA + ABA over the four seeded trees (nv 7 / 12 / 32 FF / 60 FF, instances 40/30/20/10 %)
+    in one persistent launch captured in a CUDA graph; threads per block from the autotuner."""
+    from pinocchio_gb300 import api, autotune
+
+    models = sm.heterogeneous_trees(3)
+    out = {"instances": total, "trees_nv": [m.nv for m in models], "split": [0.4, 0.3, 0.2, 0.1]}
+    for prec in ("fp64", "mixed"):
+        tasks = []
+        for k, (model, share) in enumerate(zip(models, (0.4, 0.3, 0.2, 0.1))):
+            B = int(total * share)
+            q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 20 + k))
+            data = pg.createData(model, prec)
+            tasks.append((data, "aba", q, v, 10.0 * x))
+            tasks.append((data, "rnea", q, v, x))
+        tpb, _ = autotune.tune_multi(tasks, prec)
+        mb = api.MultiBatch(tasks, prec, tpb)
+        mb.capture()
+        ms = _time_call(torch, mb.replay, reps=20, warmup=3)
+        evals = 2 * sum(int(total * s) for s in (0.4, 0.3, 0.2, 0.1))
+        out[prec] = {"ms_per_launch": ms, "evals_per_s": evals / ms * 1e3, "threads_per_block": tpb,
+                     "evals_per_launch": evals}
+    return out
+
+
+def measure_rollout(torch, pg, sm, B=8192, T=64, n=100):
+    """Differentiable rollout: T semi-implicit Euler steps (dt 1e-3) of ABA on the n-link chain,
+    batch B, loss ||q_T||^2, backward through the ABA-derivative kernels with checkpoints every 8 steps."""
+    from pinocchio_gb300 import autograd
+
+    model = sm.chain(n, 4, (0.1, 1.0))
+    rng = np.random.default_rng(5)
+    d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    q0 = d(rng.uniform(-np.pi, np.pi, (B, n)))
+    v0 = d(0.1 * rng.standard_normal((B, n)))
+    taus = d(rng.standard_normal((T, B, n)))
+    out = {"batch": B, "steps": T, "nv": n, "checkpoint_every": 8}
+    for prec in ("fp64", "mixed"):
+        data = pg.createData(model, prec)
+
+        def once():
+            q0.grad = v0.grad = taus.grad = None
+            for t in (q0, v0, taus):
+                t.requires_grad_()
+            qT, _ = autograd.rollout(model, data, q0, v0, taus, dt=1e-3, checkpoint_every=8)
+            (qT**2).sum().backward()
+
+        ms = _time_call(torch, once, reps=2, warmup=1)
+        out[prec] = {"ms_per_rollout": ms, "trajectories_per_s": B / ms * 1e3,
+                     "aba_evals_per_s": B * T / ms * 1e3}
+    return out
+
+
 def run_ours(args, world, rank, local, dist):
     import torch
 
@@ -283,9 +382,10 @@ def run_ours(args, world, rank, local, dist):
             res[name] = s.elapsed_time(e) / reps
         return res
 
-    sampler = ClockSampler(local)
-    ms_fp64 = timed("fp64", args.steps, args.warmup)
-    ms_mixed = timed("mixed", args.steps, args.warmup, sampler)
+    sampler = ClockSampler(local)  # samples clocks over both timed regions
+    with sampler:
+        ms_fp64 = timed("fp64", args.steps, args.warmup)
+        ms_mixed = timed("mixed", args.steps, args.warmup)
     clocks = sampler.summary()
     kt_mixed = kernel_times("mixed")
     kt_fp64 = kernel_times("fp64")
@@ -365,10 +465,13 @@ def run_ours(args, world, rank, local, dist):
         "aba_derivatives": B * (nq + 2 * nv + nv + 3 * nv * nv) * 8,  # q, v, tau in; ddq, ddq_dq, ddq_dv, Minv out
     }[dom]
     achieved = alg_bytes / (kt_mixed[dom] * 1e-3) / 1e9
+    # DRAM bytes of one call (sum over its kernels) from an ncu capture, scaled to this batch
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(dom)
+        t = json.load(open(tpath)).get(f"{dom}_mixed")
+        if t:
+            traffic = t["dram_bytes"] * B / t["batch"]
     flops = {"aba": 26417.0, "aba_derivatives": 214728.0}  # oracle FLOP counts per evaluation (humanoid32)
     fp64_tf = fp64_peak_tflops(torch)
     value = world * B / (ms_mixed * 1e-3)
@@ -399,7 +502,7 @@ def run_ours(args, world, rank, local, dist):
         "kernel_ms": {"mixed": kt_mixed, "fp64": kt_fp64},
         "roofline": {
             "bound": "hbm",
-            "kernel": f"gb_{dom} (mixed)",
+            "kernel": f"gb_{dom} (mixed; one call = {'1 kernel' if dom == 'aba' else '3 sweep kernels + 1 product kernel'})",
             "achieved": achieved,
             "peak": hbm_peak,
             "unit": "GB/s",
@@ -414,9 +517,14 @@ def run_ours(args, world, rank, local, dist):
             },
         },
         "clocks": clocks,
-        "gpu_launches": args.steps * 3,
+        # per step: gb_aba (1 kernel) + gb_aba_derivatives (3 sweep kernels + 1 product kernel)
+        "gpu_launches": args.steps * (1 + 4),
         "e2e": e2e,
     }
+    if not args.no_extra:
+        line["functions"] = measure_functions(torch, pg, sm)
+        line["heterogeneous"] = measure_heterogeneous(torch, pg, sm)
+        line["rollout"] = measure_rollout(torch, pg, sm)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(model, args)
     print(json.dumps(line), flush=True)
