@@ -111,6 +111,17 @@ int gb_aba_derivatives(const gb_model* model, int precision, int layout, long ba
                        const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                        double* ddq, void* stream);
 
+/* Vector-Jacobian products of the forward dynamics, for reverse-mode
+ * differentiation (no counterpart in the reference, whose callers form the
+ * full Jacobians of computeABADerivatives, aba-derivatives.hxx:380-453, and
+ * multiply): for an incoming gradient g on ddq, tau_bar = Minv g,
+ * q_bar = ddq_dq^T g and v_bar = ddq_dv^T g, from the same sweeps as
+ * gb_aba_derivatives but O(nv^2) per instance instead of the O(nv^3) products.
+ * g, q_bar, v_bar, tau_bar (and the optional ddq) are nv x batch in `layout`. */
+int gb_aba_derivatives_vjp(const gb_model* model, int precision, int layout, long batch, const double* q,
+                           const double* v, const double* tau, const double* g, double* q_bar, double* v_bar,
+                           double* tau_bar, double* ddq, void* stream);
+
 /* The batched ABA derivatives of gb_aba_derivatives, computed without any
  * device allocation: no counterpart in the reference (whose algorithms never
  * allocate on their own).  For callers that must not allocate -- real-time

@@ -20,6 +20,7 @@ from .api import (  # noqa: F401
     Data,
     ModelPool,
     aba,
+    abaDerivativesVJP,
     abaInParallel,
     computeABADerivatives,
     computeRNEADerivatives,

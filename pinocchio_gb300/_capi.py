@@ -32,6 +32,7 @@ EXPORTS = (
     "gb_crba",
     "gb_rnea_derivatives",
     "gb_aba_derivatives",
+    "gb_aba_derivatives_vjp",
     "gb_aba_derivatives_noalloc",
     "gb_integrate",
     "gb_batch_multi",
@@ -118,6 +119,7 @@ def lib():
         L.gb_crba.argtypes = [vp, i, i, i, i, l, vp, vp, vp, vp, vp]
         L.gb_rnea_derivatives.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_aba_derivatives_vjp.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives_noalloc.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]

@@ -209,6 +209,24 @@ def computeABADerivatives(model: Model, data: Data, q, v, tau):
     return tuple(_ret(t, was_np, vec) for t in (dq, dv, Minv))
 
 
+def abaDerivativesVJP(model: Model, data: Data, q, v, tau, g):
+    """(q_bar, v_bar, tau_bar) = (ddq_dq^T g, ddq_dv^T g, Minv g) for a gradient g on ddq, without
+    forming the Jacobians (gb_aba_derivatives_vjp; used by the autograd wrapper)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    tt = _as_batch(tau, model.nv, "tau")[0]
+    gt = _as_batch(g, model.nv, "g")[0]
+    torch = _torch()
+    qb, vb, tb = (torch.empty_like(vt) for _ in range(3))
+    _capi.check(
+        _capi.lib().gb_aba_derivatives_vjp(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, qt.shape[0], _ptr(qt), _ptr(vt), _ptr(tt),
+            _ptr(gt), _ptr(qb), _ptr(vb), _ptr(tb), None, _stream_ptr(),
+        )
+    )
+    return tuple(_ret(t, was_np, vec) for t in (qb, vb, tb))
+
+
 def integrate(model: Model, q, v, data: Data | None = None):
     """q (+) v on the configuration manifold (reference algorithm/joint-configuration.hpp:41-80), FP64."""
     data = data or Data(model)

@@ -5,6 +5,8 @@ derivatives (backward) of the C ABI in a ``torch.autograd.Function``: for an
 incoming gradient g on ddq, the vector-Jacobian products are
 ``q_bar = ddq_dq^T g``, ``v_bar = ddq_dv^T g`` and ``tau_bar = Minv g`` (Minv is
 symmetric), with the Jacobians of reference algorithm/aba-derivatives.hxx:380-453.
+The backward calls gb_aba_derivatives_vjp, which applies them without forming
+the nv x nv Jacobians (O(nv^2) per instance instead of the O(nv^3) products).
 
 ``rollout`` integrates ``v <- v + dt * ABA(q, v, tau_k)``, ``q <- q + dt * v``
 (semi-implicit Euler) for all time steps and, with ``checkpoint_every = k``,
@@ -34,11 +36,7 @@ class ABAFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         q, v, tau = ctx.saved_tensors
-        ddq_dq, ddq_dv, Minv = api.computeABADerivatives(ctx.model, ctx.data, q, v, tau)
-        g = g.contiguous()
-        q_bar = torch.bmm(g.unsqueeze(1), ddq_dq).squeeze(1)
-        v_bar = torch.bmm(g.unsqueeze(1), ddq_dv).squeeze(1)
-        tau_bar = torch.bmm(Minv, g.unsqueeze(2)).squeeze(2)
+        q_bar, v_bar, tau_bar = api.abaDerivativesVJP(ctx.model, ctx.data, q, v, tau, g.contiguous())
         return q_bar, v_bar, tau_bar, None, None
 
 

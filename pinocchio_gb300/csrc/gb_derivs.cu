@@ -343,9 +343,9 @@ AbaWs aba_ws_layout(const gb::DerivLayout& L, int nv, long B) {
   return w;
 }
 
+// The three sweep kernels of the ABA derivatives on a workspace laid out by aba_ws_layout.
 template <class S, class T3, class T, class K, class SS, class P>
-int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq, void* ws,
-                         cudaStream_t st) {
+int launch_aba_sweeps(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq, void* ws, cudaStream_t st) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, B);
   char* base = static_cast<char*>(ws);
@@ -371,9 +371,92 @@ int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr d
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass4<S, T, K, P><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
                                                                                  wsK, wsP);
-  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass4");
+  return cuda_error(cudaGetLastError(), "k_aba_derivs_pass4");
+}
+
+template <class S, class T3, class T, class K, class SS, class P>
+int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq, void* ws,
+                         cudaStream_t st) {
+  int rc = launch_aba_sweeps<S, T3, T, K, SS, P>(M, B, q, v, tau, ddq, ws, st);
   if (rc != GB_OK) return rc;
-  return launch_minv_products<P, P, K>(M, B, wsMB, Minv, wsP, L, dq, dv, st);
+  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
+  const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, B);
+  char* base = static_cast<char*>(ws);
+  return launch_minv_products<P, P, K>(M, B, reinterpret_cast<K*>(base + W.oMB), Minv,
+                                       reinterpret_cast<P*>(base + W.oP), L, dq, dv, st);
+}
+
+// Vector-Jacobian products of the forward dynamics for an incoming gradient g on
+// ddq: tau_bar = Minv g, q_bar = ddq_dq^T g = -dtau_dq^T (Minv g), v_bar =
+// -dtau_dv^T (Minv g) (Minv symmetric) -- O(nv^2) per configuration from the
+// workspace of the sweeps, instead of the O(nv^3) products.  A warp per
+// configuration: lanes over rows of Minv g, then over columns of dtau.
+template <class A, class W, class KM>
+__global__ void __launch_bounds__(256)
+    k_aba_vjp(const unsigned char* blob, long B, const KM* wsMB, const W* wsP, long nP, long dtq, long dtv, Arr g,
+              Arr qb, Arr vb, Arr tb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(blob);
+  const int nv = h->nv, nrel = h->n_rel, npk = nv * (nv + 1) / 2;
+  int* srel_off = reinterpret_cast<int*>(smem_raw);
+  int* srel = srel_off + (nv + 1);
+  A* sw = reinterpret_cast<A*>(smem_raw + (((size_t)(nv + 1 + nrel) * sizeof(int) + 15) & ~(size_t)15));
+  for (int t = threadIdx.x; t <= nv; t += blockDim.x) srel_off[t] = reinterpret_cast<const int*>(blob + h->o_rel_off)[t];
+  for (int t = threadIdx.x; t < nrel; t += blockDim.x) srel[t] = reinterpret_cast<const int*>(blob + h->o_rel_list)[t];
+  __syncthreads();
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nwarps = blockDim.x / 32;
+  A* gs = sw + (long)warp * 2 * nv;
+  A* ys = gs + nv;
+  for (long b = (long)blockIdx.x * nwarps + warp; b < B; b += (long)gridDim.x * nwarps) {
+    for (int j = lane; j < nv; j += 32) gs[j] = A(g.p[b * g.is + (long)j * g.es]);
+    __syncwarp();
+    const KM* Mb = wsMB + (b / kBlk) * (long)npk * kBlk + (b % kBlk);
+    for (int k = lane; k < nv; k += 32) {
+      A acc = A(0);
+      for (int j = 0; j < nv; ++j) acc += A(Mb[(long)(k <= j ? gb::upk(nv, k, j) : gb::upk(nv, j, k)) * kBlk]) * gs[j];
+      ys[k] = acc;
+      const_cast<double*>(tb.p)[b * tb.is + (long)k * tb.es] = to_double(acc);
+    }
+    __syncwarp();
+    const W* Pb = wsP + (b / kBlk) * nP * kBlk + (b % kBlk);
+    for (int c = lane; c < nv; c += 32) {
+      A aq = A(0), av = A(0);
+      for (int kk = srel_off[c]; kk < srel_off[c + 1]; ++kk) {
+        const int k = srel[kk];
+        const A y = ys[k];
+        aq += A(Pb[(dtq + (long)k * nv + c) * kBlk]) * y;
+        av += A(Pb[(dtv + (long)k * nv + c) * kBlk]) * y;
+      }
+      const_cast<double*>(qb.p)[b * qb.is + (long)c * qb.es] = -to_double(aq);
+      const_cast<double*>(vb.p)[b * vb.is + (long)c * vb.es] = -to_double(av);
+    }
+    __syncwarp();
+  }
+}
+
+template <class S, class T3, class T, class K, class SS, class P>
+int run_aba_vjp(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr g, Arr qb, Arr vb, Arr tb, Arr ddq,
+                cudaStream_t st) {
+  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
+  const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, B);
+  Workspace ws;
+  int rc = ws_alloc(ws, W.bytes, st);
+  if (rc != GB_OK) return rc;
+  rc = launch_aba_sweeps<S, T3, T, K, SS, P>(M, B, q, v, tau, ddq, ws.p, st);
+  if (rc != GB_OK) return rc;
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  constexpr int threads = 256;
+  // accumulated in K (Minv is stored in K; dtau is rounded to P)
+  const size_t smem = (((size_t)(M->nv + 1 + h->n_rel) * sizeof(int) + 15) & ~(size_t)15) +
+                      (size_t)(threads / 32) * 2 * M->nv * sizeof(K);
+  cudaError_t e = cudaFuncSetAttribute(k_aba_vjp<K, P, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_error(e, "k_aba_vjp");
+  const long grid = std::min<long>((B + 7) / 8, 152L * 8 * 4);
+  char* base = static_cast<char*>(ws.p);
+  k_aba_vjp<K, P, K><<<(unsigned)grid, threads, smem, st>>>(M->d_blob, B, reinterpret_cast<K*>(base + W.oMB),
+                                                             reinterpret_cast<P*>(base + W.oP), L.nP, L.dtq, L.dtv, g,
+                                                             qb, vb, tb);
+  return cuda_error(cudaGetLastError(), "k_aba_vjp");
 }
 
 template <class S, class T3, class T, class K, class SS, class P>
@@ -463,6 +546,29 @@ int gb_aba_derivatives(const gb_model* M, int precision, int layout, long B, con
                                                                                st);
   return gbi::run_aba_derivs<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, Aq, Av, At, Adq, Adv, AMi,
                                                                                  Add, st);
+}
+
+int gb_aba_derivatives_vjp(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                           const double* tau, const double* g, double* q_bar, double* v_bar, double* tau_bar,
+                           double* ddq, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_gravity(M));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  GB_TRY(gbi::check_ptr(g, "g")); GB_TRY(gbi::check_ptr(q_bar, "q_bar")); GB_TRY(gbi::check_ptr(v_bar, "v_bar"));
+  GB_TRY(gbi::check_ptr(tau_bar, "tau_bar"));
+  if (ddq) GB_TRY(gbi::check_ptr(ddq, "ddq"));
+  using gbi::arr;
+  const gbi::Arr Aq = arr(q, layout, B, M->nq), Av = arr(v, layout, B, M->nv), At = arr(tau, layout, B, M->nv);
+  const gbi::Arr Ag = arr(g, layout, B, M->nv), Aqb = arr(q_bar, layout, B, M->nv), Avb = arr(v_bar, layout, B, M->nv);
+  const gbi::Arr Atb = arr(tau_bar, layout, B, M->nv), Add = arr(ddq, layout, B, M->nv);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == GB_FP64)
+    return gbi::run_aba_vjp<double, double, double, double, double, double>(M, B, Aq, Av, At, Ag, Aqb, Avb, Atb, Add,
+                                                                            st);
+  // dtau kept in double-float: a projection g^T ddq_dq cancels more than the Jacobian entries do
+  return gbi::run_aba_vjp<float, float, gb::dfloat, gb::dfloat, double, gb::dfloat>(M, B, Aq, Av, At, Ag, Aqb, Avb,
+                                                                                   Atb, Add, st);
 }
 
 }  // extern "C"

@@ -128,3 +128,20 @@ def test_gravity_with_angular_part_is_rejected():
     with pytest.raises(_capi.GBError) as err:
         pg.computeABADerivatives(model, data, np.zeros((2, 6)), np.zeros((2, 6)), np.zeros((2, 6)))
     assert err.value.code == _capi.GB_ERR_GRAVITY
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_aba_derivatives_vjp(case, precision):
+    """gb_aba_derivatives_vjp == g^T of the oracle's Jacobians (and Minv g)."""
+    name, model, om, q, v, x, dev = case
+    if precision == "mixed" and name not in MIXED_MODELS:
+        pytest.skip("mixed-precision bar applies to the BASELINE models")
+    tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
+    tau = 10.0 * x
+    g = np.random.default_rng(5).standard_normal((q.shape[0], model.nv))
+    data = pg.createData(model, precision)
+    qb, vb, tb = (a.cpu().numpy() for a in pg.abaDerivativesVJP(model, data, dev(q), dev(v), dev(tau), dev(g)))
+    _, dq, dv, Minv = om.aba_derivatives(q, v, tau)
+    assert rel_err(qb, np.einsum("bk,bkc->bc", g, dq)) < tol
+    assert rel_err(vb, np.einsum("bk,bkc->bc", g, dv)) < tol
+    assert rel_err(tb, np.einsum("bkc,bc->bk", Minv, g)) < tol
