@@ -129,7 +129,8 @@ int gb_aba_derivatives_vjp(const gb_model* model, int precision, int layout, lon
  * plugins whose host application owns every device allocation -- the
  * workspace is a fixed 64 MiB device array inside the library (held by every
  * GPU that loads it until exit) instead of a cudaMallocAsync block.  Batches
- * whose workspace exceeds it (~1000 configurations of the 32-dof humanoid) are
+ * whose workspace exceeds it (~1000 FP64 / ~1400 mixed configurations of the
+ * 32-dof humanoid) are
  * rejected with GB_ERR_SIZE.  The first call on a device resolves the array's
  * address, so make it before any stream capture.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller. */

@@ -11,8 +11,8 @@
 // The array is kNoAllocScratchBytes (64 MiB) and is held by every GPU that
 // loads this library until the process exits.  A call needs a fixed number of
 // workspace bytes per configuration (about 66 KB for the 32-dof humanoid in
-// FP64, i.e. up to ~1000 configurations per
-// call; the error message of a rejected call states both figures); larger
+// FP64, 47 KB mixed, i.e. up to ~1000 / ~1400 configurations per call; the
+// error message of a rejected call states both figures); larger
 // batches are rejected with GB_ERR_SIZE.  Every call shares the
 // array: calls whose kernels overlap on the GPU (different streams, or other
 // host threads) race on it and must be serialised by the caller.  The kernels
