@@ -37,19 +37,6 @@ template <class T, class U> GB_HD void st6(const Ws<T>& w, long e, const U* x) {
 #pragma unroll
   for (int k = 0; k < 6; ++k) w[e + k] = T(x[k]);
 }
-template <class T> GB_HD T dot6(const T* a, const T* b) {
-  T s = a[0] * b[0];
-#pragma unroll
-  for (int k = 1; k < 6; ++k) s += a[k] * b[k];
-  return s;
-}
-GB_HD dfloat dot6(const dfloat* a, const dfloat* b) {
-  dacc d;
-  d.first(a[0], b[0]);
-#pragma unroll
-  for (int k = 1; k < 6; ++k) d.add(a[k], b[k]);
-  return d.result();
-}
 // a . x + b . y for 6-vectors (one compensated accumulation for double-float)
 template <class T> GB_HD T dot6x2(const T* a, const T* x, const T* b, const T* y) { return dot6(a, x) + dot6(b, y); }
 GB_HD dfloat dot6x2(const dfloat* a, const dfloat* x, const dfloat* b, const dfloat* y) {
@@ -701,9 +688,12 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
       UD[k][r] = sum;
     }
   // U Dinv and Dinv u (u is final here: every child has been folded in) for pass 3, in K
+  K UDk[NVJ][6];
 #pragma unroll 1
   for (int k = 0; k < NVJ; ++k) {
-    st6(zk, L.UD + 6 * (iv + k), UD[k]);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) UDk[k][r] = K(UD[k][r]);
+    st6(zk, L.UD + 6 * (iv + k), UDk[k]);
     SS du = SS(0);
 #pragma unroll 1
     for (int c = 0; c < NVJ; ++c) du += Dinv[k * NVJ + c] * zs[L.u + iv + c];
@@ -753,28 +743,28 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
     }
   }
   if (p > 0) {
-    // Ia -= UDinv U^T ; pa = of + Ia oa_gf + UDinv u ; accumulate into the parent
+    // Ia -= UDinv U^T (SS); the bias pa = of + Ia oa_gf + UDinv u, accumulated
+    // into the parent, is not part of the Schur complement: formed in K
 #pragma unroll 1
     for (int k = 0; k < NVJ; ++k) sym6_rank1_sub(Ia, U[k], UD[k]);
-    SS pa[6];
+    K pa[6];
     {
       K oak[6];
-      SS oa[6];
+      Sym6<K> Iak;
+      sym6_convert(Ia, Iak);
       ld6(zk, L.oa + 6 * i, oak);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) oa[r] = SS(oak[r]);
-      sym6_mv(Ia, oa, pa);
+      sym6_mv(Iak, oak, pa);
     }
 #pragma unroll 1
     for (int k = 0; k < NVJ; ++k) {
-      const SS uk = zs[L.u + iv + k];
+      const K uk = K(zs[L.u + iv + k]);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) pa[r] += UD[k][r] * uk;
+      for (int r = 0; r < 6; ++r) pa[r] += UDk[k][r] * uk;
     }
     K ofp[6];
     ld6(zk, L.of + 6 * p, ofp);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) ofp[r] += of[r] + K(pa[r]);
+    for (int r = 0; r < 6; ++r) ofp[r] += of[r] + pa[r];
     st6(zk, L.of + 6 * p, ofp);
     Sym6<SS> Ip;
     ld_sym6(zs, L.Ia + 21 * p, Ip);
@@ -790,11 +780,13 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
   // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K
   world_forward<K>(m, L, zk, q, v, nullptr, false);
 #pragma unroll 1
-  for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix(), formed in SS
+  for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix(), formed in K and stored in SS
     Iner<K> oY;
     ld_iner(zk, L.oY + 10 * i, oY);
+    Sym6<K> Ik;
+    iner_to_sym6(oY, Ik);
     Sym6<SS> I6;
-    iner_to_sym6(oY, I6);
+    sym6_convert(Ik, I6);
     st_sym6(zs, L.Ia + 21 * i, I6);
   }
   for (int k = 0; k < nv; ++k) zs[L.u + k] = SS(tau[k]);

@@ -118,6 +118,13 @@ GB_HD dfloat dot3(dfloat a0, dfloat b0, dfloat a1, dfloat b1, dfloat a2, dfloat 
   d.add(a2, b2);
   return d.result();
 }
+GB_HD dfloat dot6(const dfloat* a, const dfloat* b) {
+  dacc d;
+  d.first(a[0], b[0]);
+#pragma unroll
+  for (int k = 1; k < 6; ++k) d.add(a[k], b[k]);
+  return d.result();
+}
 GB_HD dfloat& operator+=(dfloat& a, dfloat b) { a = a + b; return a; }
 GB_HD dfloat& operator-=(dfloat& a, dfloat b) { a = a - b; return a; }
 GB_HD dfloat& operator*=(dfloat& a, dfloat b) { a = a * b; return a; }

@@ -12,6 +12,10 @@ namespace gbi {
 namespace {
 
 constexpr int kThreads = 128;
+// resident CTAs of kThreads per SM the ABA kernel is compiled for (caps registers per thread)
+#ifndef GB_ABA_MINB
+#define GB_ABA_MINB 4
+#endif
 
 __device__ __forceinline__ gb::MView stage_model(const unsigned char* __restrict__ blob, int bytes,
                                                  unsigned char* smem) {
@@ -38,7 +42,7 @@ __global__ void __launch_bounds__(kThreads) k_rnea(const unsigned char* blob, in
 }
 
 template <class S, class SS, int CAP>
-__global__ void __launch_bounds__(kThreads) k_aba(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr tau,
+__global__ void __launch_bounds__(kThreads, GB_ABA_MINB) k_aba(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr tau,
                                                   Arr ddq) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);

@@ -89,6 +89,12 @@ template <class S> GB_HD void zero(M6<S>& m) {
 // Short dot products.  The double-float scalar overloads them with one
 // compensated accumulation per dot product instead of a normalised sum per term.
 template <class S> GB_HD S dot2(S a0, S b0, S a1, S b1) { return a0 * b0 + a1 * b1; }
+template <class T> GB_HD T dot6(const T* a, const T* b) {
+  T s = a[0] * b[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) s += a[k] * b[k];
+  return s;
+}
 template <class S> GB_HD S dot3(S a0, S b0, S a1, S b1, S a2, S b2) { return a0 * b0 + a1 * b1 + a2 * b2; }
 template <class S> GB_HD void cross3(const S* a, const S* b, S* o) {
   const S x = dot2(a[1], b[2], -a[2], b[1]);
@@ -289,13 +295,15 @@ template <class S, class T> GB_HD void iner_to_sym6(const Iner<S>& Y, Sym6<T>& M
 }
 // f = I x for a block-symmetric 6x6
 template <class S, class X> GB_HD void sym6_mv(const Sym6<S>& I, const X* x, S* f) {
-  const S l0 = S(x[0]), l1 = S(x[1]), l2 = S(x[2]), a0 = S(x[3]), a1 = S(x[4]), a2 = S(x[5]);
-  f[0] = I.A[0] * l0 + I.A[1] * l1 + I.A[3] * l2 + I.B[0] * a0 + I.B[1] * a1 + I.B[2] * a2;
-  f[1] = I.A[1] * l0 + I.A[2] * l1 + I.A[4] * l2 + I.B[3] * a0 + I.B[4] * a1 + I.B[5] * a2;
-  f[2] = I.A[3] * l0 + I.A[4] * l1 + I.A[5] * l2 + I.B[6] * a0 + I.B[7] * a1 + I.B[8] * a2;
-  f[3] = I.B[0] * l0 + I.B[3] * l1 + I.B[6] * l2 + I.D[0] * a0 + I.D[1] * a1 + I.D[3] * a2;
-  f[4] = I.B[1] * l0 + I.B[4] * l1 + I.B[7] * l2 + I.D[1] * a0 + I.D[2] * a1 + I.D[4] * a2;
-  f[5] = I.B[2] * l0 + I.B[5] * l1 + I.B[8] * l2 + I.D[3] * a0 + I.D[4] * a1 + I.D[5] * a2;
+  const S xv[6] = {S(x[0]), S(x[1]), S(x[2]), S(x[3]), S(x[4]), S(x[5])};
+  const S r0[6] = {I.A[0], I.A[1], I.A[3], I.B[0], I.B[1], I.B[2]};
+  const S r1[6] = {I.A[1], I.A[2], I.A[4], I.B[3], I.B[4], I.B[5]};
+  const S r2[6] = {I.A[3], I.A[4], I.A[5], I.B[6], I.B[7], I.B[8]};
+  const S r3[6] = {I.B[0], I.B[3], I.B[6], I.D[0], I.D[1], I.D[3]};
+  const S r4[6] = {I.B[1], I.B[4], I.B[7], I.D[1], I.D[2], I.D[4]};
+  const S r5[6] = {I.B[2], I.B[5], I.B[8], I.D[3], I.D[4], I.D[5]};
+  f[0] = dot6(r0, xv); f[1] = dot6(r1, xv); f[2] = dot6(r2, xv);
+  f[3] = dot6(r3, xv); f[4] = dot6(r4, xv); f[5] = dot6(r5, xv);
 }
 // column k (0..5) of a block-symmetric 6x6
 template <class S> GB_HD void sym6_col(const Sym6<S>& I, int k, S* u) {
