@@ -964,12 +964,11 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
   }
 }
 
-// t_a - t_b (joint positions), formed in K and rounded to T
-template <class T, class K>
-GB_HD void joint_offset(const DerivLayout& L, const Ws<K>& zk, int a, int b, T* d) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) d[k] = T(zk[L.oM + 12 * a + 9 + k] - zk[L.oM + 12 * b + 9 + k]);
-}
+// unroll factor of the row-block loop of pass 4 (independent iterations: more loads in flight)
+#ifndef GB_P4_UNROLL
+#define GB_P4_UNROLL 1
+#endif
+constexpr int kRowBlockUnroll = GB_P4_UNROLL;
 
 // One joint of pass 4 with NVJ degrees of freedom (1: revolute, 6: the root
 // free-flyer, whose parent is the universe), so that every per-dof loop has a
@@ -979,6 +978,13 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
                                   const Ws<P>& wp, int i, T eps) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
+  K ti[3];  // t_i, loaded once (the dtau stores would otherwise force reloads)
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ti[k] = zk[L.oM + 12 * i + 9 + k];
+  auto offset_from = [&](int a, T* d) {  // t_a - t_i
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = T(zk[L.oM + 12 * a + 9 + k] - ti[k]);
+  };
   {
     Iner<T> oY;
     ldc_iner(w, L.coY + 10 * i, oY);
@@ -1012,10 +1018,10 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
   for (int r = 0; r < NVJ; ++r) {
     T Jr[6];
     ldc6(w, L.cJ + 6 * (iv + r), Jr);
-#pragma unroll 1
+#pragma unroll (kRowBlockUnroll)
     for (int c = iv; c < iv + nst; ++c) {
       T d[3], u[6], x[6];
-      joint_offset(L, zk, m.dof_joint[c], i, d);
+      offset_from(m.dof_joint[c], d);
       cross3(Jr + 3, d, u);
 #pragma unroll
       for (int k = 0; k < 3; ++k) { u[k] += Jr[k]; u[3 + k] = Jr[3 + k]; }
@@ -1056,7 +1062,9 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
 #pragma unroll 1
     for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j]) {
       T d[3], fs[6], Ss[6], x[6], y[6];
-      joint_offset(L, zk, i, m.dof_joint[j], d);
+      offset_from(m.dof_joint[j], d);  // t_j - t_i
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d[k] = -d[k];  // t_i - t_j
       cross3(fa, d, fs + 3);
       cross3(StdY, d, Ss + 3);
 #pragma unroll
@@ -1076,7 +1084,9 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
   }
   // accumulate into the parent, moved from t_i to t_p
   T rr[3];
-  joint_offset(L, zk, i, p, rr);
+  offset_from(p, rr);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) rr[k] = -rr[k];  // t_i - t_p
   {
     Iner<T> oYp, oYs;
     ldc_iner(w, L.coY + 10 * i, oYs);
