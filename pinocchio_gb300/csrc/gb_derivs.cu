@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* b
   const gb::Ws<S> w{ws + b, B};
   const gb::Out to = out_at(tau, b);
   gb::rnea_derivs_one<S>(m, L, w, in_at(q, b), in_at(v, b), in_at(a, b), out_at(dq, b), out_at(dv, b), out_at(Mo, b),
-                         tau.p ? &to : nullptr, symmetric);
+                         tau.p ? &to : nullptr, symmetric, true);
 }
 
 // The ABA-derivative sweeps as three kernels (passes 1-2, pass 3, pass 4), so
@@ -311,6 +311,12 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   if (rc != GB_OK) return rc;
   rc = blob_smem(M, (const void*)k_rnea_derivs<S>, "k_rnea_derivs");
   if (rc != GB_OK) return rc;
+  // the three matrices are cleared with full-bandwidth memsets; the kernel writes their non-zero entries
+  const size_t nn = (size_t)M->nv * M->nv * sizeof(double) * (size_t)B;
+  for (const Arr* a : {&dq, &dv, &Mo}) {
+    rc = cuda_error(cudaMemsetAsync(const_cast<double*>(a->p), 0, nn, st), "cudaMemsetAsync");
+    if (rc != GB_OK) return rc;
+  }
   const int tpb = M->tpb[GB_FUNC_RNEA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
   k_rnea_derivs<S><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L,

@@ -423,10 +423,12 @@ GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, c
 // ------------------------------------------------------------------------------------------
 template <class S>
 GB_HD void rnea_derivs_one(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
-                           const In& a, const Out& dq, const Out& dv, const Out& Mo, const Out* tau, bool symmetric) {
+                           const In& a, const Out& dq, const Out& dv, const Out& Mo, const Out* tau, bool symmetric,
+                           bool zeroed) {
   const int nv = m.nv;
   world_forward(m, L, w, q, v, &a, true);
-  for (int r = 0; r < nv * nv; ++r) { dq[r] = 0.0; dv[r] = 0.0; Mo[r] = 0.0; }
+  if (!zeroed)  // otherwise the outputs arrive zero-filled: only non-zero entries are written
+    for (int r = 0; r < nv * nv; ++r) { dq[r] = 0.0; dv[r] = 0.0; Mo[r] = 0.0; }
   const S eps = eps_of<S>();
   for (int i = m.nj - 1; i > 0; --i) {  // ComputeRNEADerivativesBackwardStep (hxx:361-460)
     const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];

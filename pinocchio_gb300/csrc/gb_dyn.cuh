@@ -349,7 +349,10 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 // (reference algorithm/cholesky.hxx:18-62) in FP64.
 // ------------------------------------------------------------------------------------------
 template <class S, int CAP>
-GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, const Out* U, const Out* D) {
+// `zeroed`: M (and U) arrive zero-filled (the device launcher clears them with
+// one bandwidth-bound memset), so only the structurally non-zero entries are written.
+GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, const Out* U, const Out* D,
+                    bool zeroed) {
   const int nv = m.nv;
   X3<S> oM[CAP];
   Iner<S> Yc[CAP];
@@ -387,8 +390,9 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
     load_inertia(m, i, Y);
     iner_act(O, Y, Yc[i]);
   }
-  for (int r = 0; r < nv; ++r)
-    for (int cidx = 0; cidx < nv; ++cidx) M[r * nv + cidx] = 0.0;
+  if (!zeroed)
+    for (int r = 0; r < nv; ++r)
+      for (int cidx = 0; cidx < nv; ++cidx) M[r * nv + cidx] = 0.0;
   const S eps = eps_of<S>();
   for (int i = m.nj - 1; i > 0; --i) {
     const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
@@ -416,8 +420,11 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
   // cholesky::decompose (cholesky.hxx:46-59), FP64 on the just-written M
   const Out& Uo = *U;
   const Out& Do = *D;
-  for (int r = 0; r < nv; ++r)
-    for (int cidx = 0; cidx < nv; ++cidx) Uo[r * nv + cidx] = (r == cidx) ? 1.0 : 0.0;
+  if (zeroed)
+    for (int r = 0; r < nv; ++r) Uo[r * nv + r] = 1.0;
+  else
+    for (int r = 0; r < nv; ++r)
+      for (int cidx = 0; cidx < nv; ++cidx) Uo[r * nv + cidx] = (r == cidx) ? 1.0 : 0.0;
   for (int j = nv - 1; j >= 0; --j) {
     const int NVT = m.nsfr[j] - 1;
     double s = 0.0;

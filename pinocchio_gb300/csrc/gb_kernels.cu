@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kThreads) k_crba(const unsigned char* blob, in
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
   const gb::Out Uo = out_at(U, b), Do = out_at(D, b);
-  gb::crba_one<S, CAP>(m, in_at(q, b), out_at(M, b), symmetric, U.p ? &Uo : nullptr, U.p ? &Do : nullptr);
+  gb::crba_one<S, CAP>(m, in_at(q, b), out_at(M, b), symmetric, U.p ? &Uo : nullptr, U.p ? &Do : nullptr, true);
 }
 
 __global__ void __launch_bounds__(kThreads) k_integrate(const unsigned char* blob, int bytes, long B, Arr q, Arr v,
@@ -126,6 +126,11 @@ int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, 
 int launch_crba(const gb_model* M, int precision, bool symmetric, long B, Arr q, Arr Mo, Arr U, Arr D,
                 cudaStream_t st) {
   constexpr int GB_FUNC_ID = GB_FUNC_CRBA;
+  // M and U are cleared here with full-bandwidth memsets; the kernel writes their non-zero entries
+  const size_t nn = (size_t)M->nv * M->nv * sizeof(double) * (size_t)B;
+  int rc = cuda_error(cudaMemsetAsync(const_cast<double*>(Mo.p), 0, nn, st), "cudaMemsetAsync(M)");
+  if (rc == GB_OK && U.p) rc = cuda_error(cudaMemsetAsync(const_cast<double*>(U.p), 0, nn, st), "cudaMemsetAsync(U)");
+  if (rc != GB_OK) return rc;
   // the factorisation is FP64 in both precisions, and so is the M it factorises
   if (precision == GB_FP64 || U.p != nullptr) {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_crba<double, C>), symmetric, q, Mo, U, D));

@@ -69,8 +69,8 @@ int hs_crba(void* h, int mixed, int symmetric, long B, const double* q, double* 
   for (long b = 0; b < B; ++b) {
     const gb::Out Uo = U ? out_at(U, b, nn) : gb::Out{nullptr, 1};
     const gb::Out Do = D ? out_at(D, b, m.nv) : gb::Out{nullptr, 1};
-    if (mixed) { HS_DISPATCH(M->cap, (gb::crba_one<float, C>(m, in_at(q, b, m.nq), out_at(Mo, b, nn), symmetric != 0, U ? &Uo : nullptr, U ? &Do : nullptr))); }
-    else { HS_DISPATCH(M->cap, (gb::crba_one<double, C>(m, in_at(q, b, m.nq), out_at(Mo, b, nn), symmetric != 0, U ? &Uo : nullptr, U ? &Do : nullptr))); }
+    if (mixed) { HS_DISPATCH(M->cap, (gb::crba_one<float, C>(m, in_at(q, b, m.nq), out_at(Mo, b, nn), symmetric != 0, U ? &Uo : nullptr, U ? &Do : nullptr, false))); }
+    else { HS_DISPATCH(M->cap, (gb::crba_one<double, C>(m, in_at(q, b, m.nq), out_at(Mo, b, nn), symmetric != 0, U ? &Uo : nullptr, U ? &Do : nullptr, false))); }
   }
   return 0;
 }
@@ -102,10 +102,10 @@ extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const d
       const gb::Out to = out_at(tau, b, m.nv);
       if (mixed)
         gb::rnea_derivs_one<float>(m, L, gb::Ws<float>{wf.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
-                                   out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0);
+                                   out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false);
       else
         gb::rnea_derivs_one<double>(m, L, gb::Ws<double>{wd.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
-                                    out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0);
+                                    out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false);
     }
   }
   return 0;
