@@ -22,18 +22,18 @@ namespace gb {
 // the FP64 pipe (a small fraction of the FP32 rate on GB300), so the exact
 // FP32 -> FP64 widening and the round-to-nearest-even FP64 -> FP32 narrowing
 // are done with integer instructions on the bit patterns (IEEE 754 binary32 /
-// binary64 layouts); zero takes the integer path too, and subnormal, infinite,
-// NaN and out-of-range values the hardware path.
+// binary64 layouts), branch-free: zero, infinity and NaN map exactly; values
+// below the normal FP32 range (subnormal inputs of widen, results of narrow
+// smaller than 2^-126) become a signed zero, a change below 1.2e-38.
 GB_HD double widen(float x) {
 #if defined(__CUDA_ARCH__)
   const unsigned u = __float_as_uint(x);
   const unsigned ex = (u >> 23) & 0xffu;
-  if (ex == 0u || ex == 0xffu) {
-    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    return (double)x;
-  }
-  const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-  return __hiloint2double((int)hi, (int)(u << 29));
+  const unsigned mant = (u & 0x7fffffu) >> 3;
+  const unsigned ex64 = ex == 0u ? 0u : (ex == 0xffu ? 0x7ffu : ex + 896u);
+  const unsigned hi = (u & 0x80000000u) | (ex64 << 20) | (ex == 0u ? 0u : mant);
+  const unsigned lo = ex == 0u ? 0u : (u << 29);
+  return __hiloint2double((int)hi, (int)lo);
 #else
   return (double)x;
 #endif
@@ -41,21 +41,20 @@ GB_HD double widen(float x) {
 GB_HD float narrow(double x) {
 #if defined(__CUDA_ARCH__)
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
   const unsigned ex = (hi >> 20) & 0x7ffu;
-  if (ex < 897u || ex > 1150u) {  // outside the normal FP32 range (or zero)
-    if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-    return (float)x;
-  }
   const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of the 52 fraction bits
   const unsigned rest = lo & 0x1fffffffu;                      // the 29 bits dropped
-  unsigned r = (hi & 0x80000000u) | ((ex - 896u) << 23) | mant;
-  if (rest > 0x10000000u || (rest == 0x10000000u && (mant & 1u))) r += 1u;  // carries into the exponent
+  unsigned r = sign | (((ex - 896u) & 0xffu) << 23) | mant;
+  r += (rest > 0x10000000u || (rest == 0x10000000u && (mant & 1u))) ? 1u : 0u;  // carries into the exponent
+  const bool nan = ex == 0x7ffu && (((hi & 0xfffffu) | lo) != 0u);
+  r = ex < 897u ? sign : r;                                                        // zero / below FP32's range
+  r = ex > 1150u ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u)) : r;              // overflow, inf, NaN
   return __uint_as_float(r);
 #else
   return (float)x;
 #endif
 }
-
 // T(x) with the integer conversions between FP32 and FP64
 template <class T, class U> GB_HD T cvt(U x) { return T(x); }
 template <> GB_HD double cvt<double, float>(float x) { return widen(x); }
