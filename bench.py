@@ -216,14 +216,16 @@ def _time_call(torch, fn, reps=5, warmup=2):
 
 def measure_functions(torch, pg, sm):
     """evals/s of every batched function on the humanoid, per precision: RNEA / ABA /
-    CRBA (+ tree Cholesky) at batch 65536, the two derivative algorithms at batch 16384."""
+    CRBA (+ tree Cholesky) / computeMinverse / nonLinearEffects / generalized gravity at
+    batch 65536, the two derivative algorithms at batch 16384."""
     model = sm.humanoid32(1)
     out = {}
     for prec in ("fp64", "mixed"):
         data = pg.createData(model, prec)
         res = {}
         for fname, B in (("rnea", 65536), ("aba", 65536), ("crba", 65536), ("crba_cholesky", 65536),
-                         ("rnea_derivatives", 16384), ("aba_derivatives", 16384)):
+                         ("rnea_derivatives", 16384), ("aba_derivatives", 16384), ("compute_minverse", 65536),
+                         ("nonlinear_effects", 65536), ("generalized_gravity", 65536)):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
             fn = {
                 "rnea": lambda: pg.rnea(model, data, q, v, x),
@@ -232,6 +234,9 @@ def measure_functions(torch, pg, sm):
                 "crba_cholesky": lambda: pg.crbaCholesky(model, data, q),
                 "rnea_derivatives": lambda: pg.computeRNEADerivatives(model, data, q, v, x),
                 "aba_derivatives": lambda: pg.computeABADerivatives(model, data, q, v, 10.0 * x),
+                "compute_minverse": lambda: pg.computeMinverse(model, data, q),
+                "nonlinear_effects": lambda: pg.nonLinearEffects(model, data, q, v),
+                "generalized_gravity": lambda: pg.computeGeneralizedGravity(model, data, q),
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}

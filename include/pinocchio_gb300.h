@@ -84,6 +84,16 @@ const char* gb_last_error(void);
 int gb_rnea(const gb_model* model, int precision, int layout, long batch, const double* q, const double* v,
             const double* a, double* tau, void* stream);
 
+/* nle = nonLinearEffects(model, data, q, v) = C(q, v) v + g(q)
+ * (reference algorithm/rnea.hxx:221-336, public rnea.hpp:105-109, rnea.hxx:801-808). */
+int gb_nonlinear_effects(const gb_model* model, int precision, int layout, long batch, const double* q,
+                         const double* v, double* nle, void* stream);
+
+/* g = computeGeneralizedGravity(model, data, q)
+ * (reference algorithm/rnea.hxx:346-446, public rnea.hpp:133-136, rnea.hxx:816-822). */
+int gb_generalized_gravity(const gb_model* model, int precision, int layout, long batch, const double* q, double* g,
+                           void* stream);
+
 /* ddq = aba(model, data, q, v, tau, convention) for every instance
  * (reference algorithm/aba.hxx:933-948; WORLD 242-293, LOCAL 486-540). */
 int gb_aba(const gb_model* model, int precision, int convention, int layout, long batch, const double* q,
@@ -110,6 +120,14 @@ int gb_rnea_derivatives(const gb_model* model, int precision, int matrix_mode, i
 int gb_aba_derivatives(const gb_model* model, int precision, int layout, long batch, const double* q,
                        const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                        double* ddq, void* stream);
+
+/* Minv = computeMinverse(model, data, q) (reference algorithm/aba.hxx:838-880,
+ * public aba.hpp:101-109): the reference fills the upper triangle
+ * (GB_MATRIX_UPPER, the lower part written as zero); GB_MATRIX_SYMMETRIC gives
+ * the symmetric matrix its Python binding returns.  Passes 1-2 of the ABA
+ * derivatives without velocity terms and the Minv recursion. */
+int gb_compute_minverse(const gb_model* model, int precision, int matrix_mode, int layout, long batch,
+                        const double* q, double* Minv, void* stream);
 
 /* Vector-Jacobian products of the forward dynamics, for reverse-mode
  * differentiation (no counterpart in the reference, whose callers form the

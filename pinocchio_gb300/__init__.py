@@ -23,11 +23,14 @@ from .api import (  # noqa: F401
     abaDerivativesVJP,
     abaInParallel,
     computeABADerivatives,
+    computeGeneralizedGravity,
+    computeMinverse,
     computeRNEADerivatives,
     crba,
     crbaCholesky,
     createData,
     integrate,
+    nonLinearEffects,
     rnea,
     rneaInParallel,
 )

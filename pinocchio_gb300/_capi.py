@@ -28,10 +28,13 @@ EXPORTS = (
     "gb_model_dims",
     "gb_last_error",
     "gb_rnea",
+    "gb_nonlinear_effects",
+    "gb_generalized_gravity",
     "gb_aba",
     "gb_crba",
     "gb_rnea_derivatives",
     "gb_aba_derivatives",
+    "gb_compute_minverse",
     "gb_aba_derivatives_vjp",
     "gb_aba_derivatives_noalloc",
     "gb_integrate",
@@ -115,10 +118,13 @@ def lib():
         L.gb_model_destroy.argtypes = [vp]
         L.gb_model_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
         L.gb_rnea.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp]
+        L.gb_nonlinear_effects.argtypes = [vp, i, i, l, vp, vp, vp, vp]
+        L.gb_generalized_gravity.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_aba.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp]
         L.gb_crba.argtypes = [vp, i, i, i, i, l, vp, vp, vp, vp, vp]
         L.gb_rnea_derivatives.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_compute_minverse.argtypes = [vp, i, i, i, l, vp, vp, vp]
         L.gb_aba_derivatives_vjp.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives_noalloc.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]

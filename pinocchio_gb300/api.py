@@ -117,6 +117,49 @@ def rnea(model: Model, data: Data, q, v, a):
     return _ret(tau, was_np, vec)
 
 
+def nonLinearEffects(model: Model, data: Data, q, v):
+    """nle = C(q, v) v + g(q) (reference algorithm/rnea.hxx:221-336, 801-808)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    out = _torch().empty((qt.shape[0], model.nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_nonlinear_effects(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, qt.shape[0], _ptr(qt), _ptr(vt), _ptr(out), _stream_ptr()
+        )
+    )
+    data.nle = out
+    return _ret(out, was_np, vec)
+
+
+def computeGeneralizedGravity(model: Model, data: Data, q):
+    """g(q) (reference algorithm/rnea.hxx:346-446, 816-822)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    out = _torch().empty((qt.shape[0], model.nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_generalized_gravity(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, qt.shape[0], _ptr(qt), _ptr(out), _stream_ptr()
+        )
+    )
+    data.g = out
+    return _ret(out, was_np, vec)
+
+
+def computeMinverse(model: Model, data: Data, q, symmetric: bool = True):
+    """Minv(q) (reference algorithm/aba.hxx:838-880), symmetrised as the Python binding returns it
+    (bindings/python/algorithm/expose-aba.cpp:17-23); ``symmetric=False`` gives the C++ upper triangle."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    nv = model.nv
+    out = _torch().empty((qt.shape[0], nv, nv), dtype=qt.dtype, device=qt.device)
+    mode = _capi.GB_MATRIX_SYMMETRIC if symmetric else _capi.GB_MATRIX_UPPER
+    _capi.check(
+        _capi.lib().gb_compute_minverse(
+            data.dev.h, _PREC[data.precision], mode, _capi.GB_LAYOUT_INSTANCE, qt.shape[0], _ptr(qt), _ptr(out), _stream_ptr()
+        )
+    )
+    data.Minv = out
+    return _ret(out, was_np, vec)
+
+
 def aba(model: Model, data: Data, q, v, tau, convention: int = Convention.LOCAL):
     """ddq = ABA(q, v, tau) (reference algorithm/aba.hxx:933-948)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")

@@ -102,6 +102,32 @@ int gb_rnea(const gb_model* M, int precision, int layout, long B, const double* 
                           gbi::arr(a, layout, B, M->nv), gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
 }
 
+// nonLinearEffects = rnea(q, v, 0) and computeGeneralizedGravity = rnea(q, 0, 0)
+// (reference algorithm/rnea.hxx:221-336, 346-446): the RNEA kernel reading a zero vector
+// (16 zero bytes of the model blob, stride 0) for the absent arguments.
+static gbi::Arr zero_arr(const gb_model* M) {
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  return gbi::Arr{reinterpret_cast<const double*>(M->d_blob + h->o_zero), 0, 0};
+}
+
+int gb_nonlinear_effects(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                         double* nle, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(nle, "nle"));
+  return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv), zero_arr(M),
+                          gbi::arr(nle, layout, B, M->nv), (cudaStream_t)stream);
+}
+
+int gb_generalized_gravity(const gb_model* M, int precision, int layout, long B, const double* q, double* g,
+                           void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(g, "g"));
+  return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), zero_arr(M), zero_arr(M),
+                          gbi::arr(g, layout, B, M->nv), (cudaStream_t)stream);
+}
+
 int gb_aba(const gb_model* M, int precision, int convention, int layout, long B, const double* q, const double* v,
            const double* tau, double* ddq, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));

@@ -88,6 +88,18 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
                                 in_at(v, b), ddq.p ? &dd : nullptr);
 }
 
+// the Minv recursion of computeMinverse (pass 3 without velocities and column sets)
+template <class K>
+__global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
+    k_minverse_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, K* wsMB, int npk) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  gb::aba_derivs_pass3<K, K, K, true>(m, L, m.slot, gb::Ws<K>{wsK + b, B}, gb::Ws<K>{wsK + b, B},
+                                      blocked(wsMB, npk, b), gb::In{nullptr, 0}, nullptr);
+}
+
 template <class S, class T, class K, class P>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_aba_derivs_pass4(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, P* wsP) {
@@ -116,8 +128,8 @@ __device__ __forceinline__ double to_double(gb::dfloat x) { return double(x); }
 // row segments.
 template <int LG, class S, class W, class KM>
 __global__ void __launch_bounds__(512, 2)
-    k_minv_products(const unsigned char* blob, long B, int m0, int NM, const KM* wsMi, Arr Minv, const W* wsP, long nP,
-                    long dtq, long dtv, Arr out0, Arr out1) {
+    k_minv_products(const unsigned char* blob, long B, int m0, int NM, const KM* wsMi, Arr Minv, bool minv_upper,
+                    const W* wsP, long nP, long dtq, long dtv, Arr out0, Arr out1) {
   constexpr int Gs = 1 << LG, R = 32 >> LG;  // configurations per iteration, rows per warp task
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(blob);
@@ -166,9 +178,11 @@ __global__ void __launch_bounds__(512, 2)
       if (c >= nv) continue;
       const KM x = sK[(r <= c ? gb::upk(nv, r, c) : gb::upk(nv, c, r)) * Gs + lg];
       sM[(r * nv + c) * Gs + lg] = S(x);
-      if (m0 == 0 && lg < g_here) Mo[(b0 + lg) * Minv.is + (long)(r * nv + c) * Minv.es] = to_double(x);
+      if (m0 == 0 && lg < g_here)
+        Mo[(b0 + lg) * Minv.is + (long)(r * nv + c) * Minv.es] = (minv_upper && r > c) ? 0.0 : to_double(x);
     }
     __syncthreads();
+    if (NM == 0) continue;  // Minv only
     // the dtau matrices
     for (int mm = 0; mm < NM; ++mm) {
       const W* src = wsP + blk * nP * kBlk + ((m0 + mm) == 0 ? dtq : dtv) * kBlk + g0;
@@ -261,9 +275,11 @@ int ws_alloc(Workspace& w, size_t bytes, cudaStream_t st) {
 
 // S: scalar of the products (smem, FMA); W: scalar of the dtau matrices in the
 // workspace; KM: scalar of the packed Minv in the workspace
+// products == false: only the Minv output (symmetric, or upper with zeros below when minv_upper)
 template <class S, class W, class KM>
 int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, const W* wsP,
-                         const gb::DerivLayout& L, Arr o0, Arr o1, cudaStream_t st) {
+                         const gb::DerivLayout& L, Arr o0, Arr o1, cudaStream_t st, bool products = true,
+                         bool minv_upper = false) {
   const long nn = (long)M->nv * M->nv, npk = (long)M->nv * (M->nv + 1) / 2;
   const int ngroup = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->ngroup;
   const int nrel = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->n_grp_rel;
@@ -275,9 +291,9 @@ int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, co
 #define GB_MINV_SMEM_KB 100
 #endif
   const long budget = GB_MINV_SMEM_KB * 1024;  // shared memory per CTA (100 KB: two CTAs per SM)
-  int NM = 2, lgG = 3;
+  int NM = products ? 2 : 0, lgG = 3;
   while (lgG > 0 && smem_of(1L << lgG, NM) > budget) --lgG;
-  if (smem_of(1L << lgG, NM) > budget) NM = 1;
+  if (products && smem_of(1L << lgG, NM) > budget) NM = 1;
   if (smem_of(1L << lgG, NM) > 220 * 1024) return set_error(GB_ERR_UNSUPPORTED, "nv too large for the Minv products");
   const long G = 1L << lgG;
   const size_t smem = (size_t)smem_of(G, NM);
@@ -289,13 +305,14 @@ int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, co
   if (e != cudaSuccess) return cuda_error(e, "k_minv_products");
   const long nit = ((B + kBlk - 1) / kBlk) * (kBlk / G);
   const long grid = std::min<long>(nit, 152L * 2 * 8);
-  for (int m0 = 0; m0 < 2; m0 += NM) {
+  for (int m0 = 0; m0 < 2; m0 += (NM > 0 ? NM : 2)) {
     const unsigned char* bl = M->d_blob;
     const long nP = L.nP, dtq = L.dtq, dtv = L.dtv;
-    if (lgG == 3) k_minv_products<3, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
-    else if (lgG == 2) k_minv_products<2, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
-    else if (lgG == 1) k_minv_products<1, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
-    else k_minv_products<0, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, wsP, nP, dtq, dtv, o0, o1);
+    const bool up = minv_upper;
+    if (lgG == 3) k_minv_products<3, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, up, wsP, nP, dtq, dtv, o0, o1);
+    else if (lgG == 2) k_minv_products<2, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, up, wsP, nP, dtq, dtv, o0, o1);
+    else if (lgG == 1) k_minv_products<1, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, up, wsP, nP, dtq, dtv, o0, o1);
+    else k_minv_products<0, S, W, KM><<<(unsigned)grid, 512, smem, st>>>(bl, B, m0, NM, wsMi, Minv, up, wsP, nP, dtq, dtv, o0, o1);
     const int rc = cuda_error(cudaGetLastError(), "k_minv_products");
     if (rc != GB_OK) return rc;
   }
@@ -440,6 +457,40 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// computeMinverse (reference algorithm/aba.hxx:838-880): passes 1-2 with zero
+// velocity and torque (the bias terms vanish; Minv does not depend on them),
+// the Minv recursion of pass 3, and the Minv output of the product kernel.
+template <class K, class SS>
+int run_minverse(const gb_model* M, long B, Arr q, Arr Minv, bool upper, cudaStream_t st) {
+  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
+  const AbaWs W = aba_ws_layout<K, K, SS, K>(L, M->nv, B);
+  Workspace ws;
+  int rc = ws_alloc(ws, W.oP, st);  // no dtau region
+  if (rc != GB_OK) return rc;
+  char* base = static_cast<char*>(ws.p);
+  K* wsK = reinterpret_cast<K*>(base + W.oK);
+  K* wsMB = reinterpret_cast<K*>(base + W.oMB);
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  const Arr zero{reinterpret_cast<const double*>(M->d_blob + h->o_zero), 0, 0};
+  const int npk = M->nv * (M->nv + 1) / 2;
+  const int tpb = M->tpb[GB_FUNC_ABA_DERIVATIVES];
+  const long grid = (B + tpb - 1) / tpb;
+  rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS>, "k_aba_derivs_pass12");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_minverse_pass3<K>, "k_minverse_pass3");
+  if (rc != GB_OK) return rc;
+  k_aba_derivs_pass12<K, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK,
+                                                                             reinterpret_cast<SS*>(base), wsMB, npk, q,
+                                                                             zero, zero);
+  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
+  if (rc != GB_OK) return rc;
+  k_minverse_pass3<K><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK, wsMB, npk);
+  rc = cuda_error(cudaGetLastError(), "k_minverse_pass3");
+  if (rc != GB_OK) return rc;
+  const Arr none{nullptr, 0, 0};
+  return launch_minv_products<K, K, K>(M, B, wsMB, Minv, static_cast<const K*>(nullptr), L, none, none, st, false,
+                                       upper);
+}
+
 template <class S, class T3, class T, class K, class SS, class P>
 int run_aba_vjp(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr g, Arr qb, Arr vb, Arr tb, Arr ddq,
                 cudaStream_t st) {
@@ -552,6 +603,20 @@ int gb_aba_derivatives(const gb_model* M, int precision, int layout, long B, con
                                                                                st);
   return gbi::run_aba_derivs<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, Aq, Av, At, Adq, Adv, AMi,
                                                                                  Add, st);
+}
+
+int gb_compute_minverse(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
+                        double* Minv, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (matrix_mode != GB_MATRIX_UPPER && matrix_mode != GB_MATRIX_SYMMETRIC)
+    return gbi::set_error(GB_ERR_INVALID_ARGUMENT, "unknown matrix mode");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(Minv, "Minv"));
+  const gbi::Arr Aq = gbi::arr(q, layout, B, M->nq), AMi = gbi::arr(Minv, layout, B, (long)M->nv * M->nv);
+  const bool upper = matrix_mode == GB_MATRIX_UPPER;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == GB_FP64) return gbi::run_minverse<double, double>(M, B, Aq, AMi, upper, st);
+  return gbi::run_minverse<gb::dfloat, double>(M, B, Aq, AMi, upper, st);
 }
 
 int gb_aba_derivatives_vjp(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,

@@ -803,7 +803,9 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
 
 // One joint of pass 3 (ComputeABADerivativesForwardStep2, hxx:178-270) with NVJ
 // degrees of freedom.
-template <int NVJ, class S, class T, class K>
+// MINV: the Minv recursion only (computeMinverse's ComputeMinverseForwardStep2,
+// aba.hxx:789-836): no velocity / acceleration recursion, no column sets.
+template <int NVJ, class S, class T, class K, bool MINV = false>
 GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                                   const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out, const K* gk,
                                   int i) {
@@ -812,19 +814,6 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   K ti[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) ti[k] = zk[L.oM + 12 * i + 9 + k];
-  K ovp[6] = {K(0), K(0), K(0), K(0), K(0), K(0)}, oap[6];
-  if (p > 0) {
-    K r[3], x[6];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) r[k] = ti[k] - zk[L.oM + 12 * p + 9 + k];
-    ld6(zk, L.ov + 6 * p, x);
-    shift_motion(x, r, ovp);
-    ld6(zk, L.oa + 6 * p, x);
-    shift_motion(x, r, oap);
-  } else {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) oap[k] = -gk[k];  // uniform field: invariant to the shift
-  }
   // joint columns about t_i: a revolute axis passes through t_i; the root free-flyer sits at the origin
   K Jo[NVJ][6], Jc[NVJ][6];
 #pragma unroll 1
@@ -834,33 +823,47 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     for (int r = 0; r < 6; ++r) Jc[k][r] = Jo[k][r];
   }
   if constexpr (NVJ == 1) Jc[0][0] = Jc[0][1] = Jc[0][2] = K(0);
-  K ov[6], oa[6];
+  K ovp[6] = {K(0), K(0), K(0), K(0), K(0), K(0)}, oap[6], ov[6], oa[6];
+  if constexpr (!MINV) {
+    if (p > 0) {
+      K r[3], x[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) ov[k] = ovp[k];
+      for (int k = 0; k < 3; ++k) r[k] = ti[k] - zk[L.oM + 12 * p + 9 + k];
+      ld6(zk, L.ov + 6 * p, x);
+      shift_motion(x, r, ovp);
+      ld6(zk, L.oa + 6 * p, x);
+      shift_motion(x, r, oap);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) oap[k] = -gk[k];  // uniform field: invariant to the shift
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) ov[k] = ovp[k];
 #pragma unroll 1
-  for (int k = 0; k < NVJ; ++k) {
-    const K vk = K(v[iv + k]);
+    for (int k = 0; k < NVJ; ++k) {
+      const K vk = K(v[iv + k]);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) ov[r] += Jc[k][r] * vk;
+      for (int r = 0; r < 6; ++r) ov[r] += Jc[k][r] * vk;
+    }
+    mcross(ovp, ov, oa);  // velocity-product bias (aba.hxx:126-128) + the parent's acceleration
+#pragma unroll
+    for (int k = 0; k < 6; ++k) oa[k] += oap[k];
+    K dd[NVJ];
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
+      K ud[6], udi[6];
+      ld6(zk, L.UD + 6 * (iv + k), ud);
+      shift_force_from_origin(ud, ti, udi);  // UDinv (a force about the root origin) about t_i
+      dd[k] = zk[L.Du + iv + k] - dot6(udi, oa);
+      if (ddq_out) (*ddq_out)[iv + k] = double(dd[k]);
+    }
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k)
+#pragma unroll
+      for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * dd[k];
+    st6(zk, L.ov + 6 * i, ov);
+    st6(zk, L.oa + 6 * i, oa);
   }
-  mcross(ovp, ov, oa);  // velocity-product bias (aba.hxx:126-128) + the parent's acceleration
-#pragma unroll
-  for (int k = 0; k < 6; ++k) oa[k] += oap[k];
-  K dd[NVJ];
-#pragma unroll 1
-  for (int k = 0; k < NVJ; ++k) {
-    K ud[6], udi[6];
-    ld6(zk, L.UD + 6 * (iv + k), ud);
-    shift_force_from_origin(ud, ti, udi);  // UDinv (a force about the root origin) about t_i
-    dd[k] = zk[L.Du + iv + k] - dot6(udi, oa);
-    if (ddq_out) (*ddq_out)[iv + k] = double(dd[k]);
-  }
-#pragma unroll 1
-  for (int k = 0; k < NVJ; ++k)
-#pragma unroll
-    for (int r = 0; r < 6; ++r) oa[r] += Jc[k][r] * dd[k];
-  st6(zk, L.ov + 6 * i, ov);
-  st6(zk, L.oa + 6 * i, oa);
   // Minv rows of the joint: -= UDinv^T Fcrb[parent] (columns right of the
   // subtree start from zero); Fcrb[i] = J Minv_rows (+ Fcrb[parent]).  A
   // free-flyer is a root joint (no parent), so the updated rows are revolute.
@@ -898,6 +901,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
       st6(zk, Fi + 6 * c, Fn);
     }
   }
+  if constexpr (MINV) return;
   // C quantities about t_i, computed in T and stored as S
   T ovs[6], ovps[6], oaps[6], oas[6];
 #pragma unroll
@@ -951,7 +955,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     if (k >= 18 || k % 6 >= 3) w[L.doY + 36 * i + k] = S(dY[k]);  // the lin-lin block is zero
 }
 
-template <class S, class T, class K>
+template <class S, class T, class K, bool MINV = false>
 GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                             const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out) {
   // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
@@ -961,8 +965,8 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
   const K* gk = ModelScalar<K>::grav(m);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
-    else aba_derivs_pass3_joint<1, S, T, K>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
+    else aba_derivs_pass3_joint<1, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
   }
 }
 

@@ -29,7 +29,7 @@ struct BlobHeader {
   int o_slot, o_dofj, o_bslot, nbranch;
   int o_grp, ngroup, o_grp_rel, n_grp_rel;
   int o_i6_d, o_i6_f, o_place_df, o_iner_df;
-  int o_arm_df, pad6, pad7, pad8;
+  int o_arm_df, o_zero, pad7, pad8;  // o_zero: 16 zero bytes (a zero vector with stride 0)
   double grav_d[6];
   float grav_f[6];
   float padf[2];

@@ -152,6 +152,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
   h.o_i6_d = take(8 * 21 * nj); h.o_i6_f = take(4 * 21 * nj);
   h.o_place_df = take(8 * 12 * nj); h.o_iner_df = take(8 * 10 * nj); h.o_arm_df = take(8 * nv);
+  h.o_zero = take(16);
   h.bytes = (int)off;
   for (int k = 0; k < 6; ++k) {
     h.grav_d[k] = M->gravity[k];

@@ -1,0 +1,97 @@
+"""The neighbours of the path through the C ABI:
+computeMinverse (reference algorithm/aba.hxx:838-880) against the oracle's
+Minv and M^-1, nonLinearEffects and computeGeneralizedGravity (rnea.hxx:221-446)
+against the oracle's RNEA with zero acceleration / zero velocity; FP64 at 1e-12
+and mixed precision at 1e-5, both output modes, both layouts."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pinocchio_gb300 as pg
+from oracle.oracle import LOCAL, OracleModel, symmetrize_upper
+from pinocchio_gb300 import _capi
+from pinocchio_gb300 import sample_models as sm
+from util import FP64_TOL, MIXED_TOL, MODELS, rel_err
+
+pytestmark = pytest.mark.gpu
+MIXED_MODELS = [n for n in MODELS if n != "chain100"]
+
+
+@pytest.fixture(scope="module", params=list(MODELS))
+def case(request):
+    import torch
+
+    model = MODELS[request.param]()
+    q, v, x = sm.random_inputs(model, 301, 77)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    return request.param, model, OracleModel(model), q, v, x, dev
+
+
+def _tol(name, precision):
+    if precision == "mixed":
+        return MIXED_TOL
+    return 1e-10 if name == "chain100" else FP64_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_compute_minverse(case, precision):
+    name, model, om, q, v, x, dev = case
+    if precision == "mixed" and name not in MIXED_MODELS:
+        pytest.skip("mixed-precision bar applies to the BASELINE models")
+    tol = _tol(name, precision)
+    data = pg.createData(model, precision)
+    Mi = pg.computeMinverse(model, data, dev(q)).cpu().numpy()
+    _, _, _, Mref = om.aba_derivatives(q, v, 10.0 * x)
+    assert rel_err(Mi, Mref) < tol
+    Mi_up = pg.computeMinverse(model, data, dev(q), symmetric=False).cpu().numpy()
+    assert rel_err(Mi_up, np.triu(Mref)) < tol
+    assert np.all(np.tril(Mi_up, -1) == 0.0)
+    if precision == "fp64":  # Minv M = I (unittest/aba-derivatives.cpp:96-100)
+        M = symmetrize_upper(om.crba(q, LOCAL))
+        eye = np.broadcast_to(np.eye(model.nv), M.shape)
+        assert np.abs(np.einsum("bij,bjk->bik", Mi, M) - eye).max() < (1e-8 if name == "chain100" else 1e-11)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nonlinear_effects_and_gravity(case, precision):
+    name, model, om, q, v, x, dev = case
+    tol = _tol(name, precision)
+    if precision == "mixed":
+        tol = 1e-5
+    data = pg.createData(model, precision)
+    nle = pg.nonLinearEffects(model, data, dev(q), dev(v)).cpu().numpy()
+    g = pg.computeGeneralizedGravity(model, data, dev(q)).cpu().numpy()
+    zero = np.zeros_like(v)
+    assert rel_err(nle, om.rnea(q, v, zero)) < tol
+    assert rel_err(g, om.rnea(q, zero, zero)) < tol
+
+
+def test_soa_layout_minverse_and_gravity():
+    import torch
+
+    model = sm.humanoid32(1)
+    om = OracleModel(model)
+    q, v, x = sm.random_inputs(model, 77, 3)
+    data = pg.createData(model)
+    B, nv = q.shape[0], model.nv
+    qs = torch.from_numpy(np.ascontiguousarray(q.T)).cuda()  # SoA: element-major
+    Mi = torch.empty((nv * nv, B), dtype=torch.float64, device="cuda")
+    g = torch.empty((nv, B), dtype=torch.float64, device="cuda")
+    L = _capi.lib()
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    _capi.check(L.gb_compute_minverse(data.dev.h, _capi.GB_FP64, _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_SOA, B, P(qs), P(Mi), None))
+    _capi.check(L.gb_generalized_gravity(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, P(qs), P(g), None))
+    torch.cuda.synchronize()
+    _, _, _, Mref = om.aba_derivatives(q, v, x)
+    assert rel_err(Mi.cpu().numpy().T.reshape(B, nv, nv), Mref) < FP64_TOL
+    assert rel_err(g.cpu().numpy().T, om.rnea(q, np.zeros_like(v), np.zeros_like(v))) < FP64_TOL
+
+
+def test_empty_batch_and_errors():
+    model = sm.manipulator6r(0)
+    data = pg.createData(model)
+    L = _capi.lib()
+    assert L.gb_compute_minverse(data.dev.h, _capi.GB_FP64, _capi.GB_MATRIX_UPPER, _capi.GB_LAYOUT_INSTANCE, 0, None, None, None) == 0
+    assert L.gb_compute_minverse(data.dev.h, _capi.GB_FP64, 7, _capi.GB_LAYOUT_INSTANCE, 1, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_nonlinear_effects(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, 3, None, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
