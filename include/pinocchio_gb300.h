@@ -185,6 +185,15 @@ int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, int threads_
  * configurations per CTA (32, 64, 96 or 128; default 128). */
 int gb_model_set_launch(gb_model* model, int function, int threads_per_block);
 
+/* Layout of one model's function chosen by the autotuner: one thread per
+ * configuration (GB_INSTANCE_PER_THREAD, the default) or one warp per
+ * configuration (GB_INSTANCE_PER_WARP: the joints of one tree level in
+ * parallel, for batches too small to fill the GPU; RNEA and ABA, including
+ * nonLinearEffects / generalized gravity and the *_in_parallel entry points).
+ * Both layouts give identical results. */
+enum { GB_INSTANCE_PER_THREAD = 0, GB_INSTANCE_PER_WARP = 1 };
+int gb_model_set_layout(gb_model* model, int function, int layout);
+
 /* ModelPool (reference multibody/pool/model.hpp:19-165): `size` nominal
  * per-thread slots; the GPU needs one model copy only, the size is kept for
  * the reference's num_threads <= pool.size() check. */

@@ -20,6 +20,7 @@ GB_LOCAL, GB_WORLD = 0, 1
 GB_LAYOUT_INSTANCE, GB_LAYOUT_SOA = 0, 1
 GB_MATRIX_UPPER, GB_MATRIX_SYMMETRIC = 0, 1
 GB_FUNC_RNEA, GB_FUNC_ABA, GB_FUNC_CRBA, GB_FUNC_RNEA_DERIVATIVES, GB_FUNC_ABA_DERIVATIVES = range(5)
+GB_INSTANCE_PER_THREAD, GB_INSTANCE_PER_WARP = 0, 1
 
 # every symbol declared in include/pinocchio_gb300.h, in declaration order
 EXPORTS = (
@@ -40,6 +41,7 @@ EXPORTS = (
     "gb_integrate",
     "gb_batch_multi",
     "gb_model_set_launch",
+    "gb_model_set_layout",
     "gb_pool_create",
     "gb_pool_destroy",
     "gb_pool_size",
@@ -130,6 +132,7 @@ def lib():
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]
         L.gb_model_set_launch.argtypes = [vp, i, i]
+        L.gb_model_set_layout.argtypes = [vp, i, i]
         L.gb_pool_create.argtypes = [vp, l, C.POINTER(vp)]
         L.gb_pool_destroy.argtypes = [vp]
         L.gb_pool_size.argtypes = [vp, C.POINTER(l)]

@@ -1,14 +1,18 @@
-"""Launch autotuner: picks, per model and function, the configurations per CTA.
+"""Launch autotuner: picks, per model and function, the layout and the
+configurations per CTA.
 
-Every batched entry point evaluates one configuration per thread; the free
-launch parameter is how many configurations share a CTA (and so the model
-tables staged in its shared memory): small CTAs spread a small batch over
-more SMs, large ones amortise the staging.  ``tune`` times the candidates with
-CUDA events on the given batch, applies the fastest with
-``gb_model_set_launch`` and records it in a JSON cache (keyed by GPU name,
-model tables, function, precision and batch size) so that later processes
-reuse it without timing again.  The heterogeneous launch is tuned the same
-way over its threads_per_block argument (``tune_multi``).
+Every batched entry point evaluates one configuration per thread by default;
+RNEA and ABA (and the functions built on them) also have a warp-per-instance
+layout, where the 32 lanes of a warp evaluate one configuration with the joints
+of a tree level in parallel (``gb_model_set_layout``): it wins when the batch is
+too small to fill the GPU one thread per configuration.  For the thread layout
+the free parameter is how many configurations share a CTA (and so the model
+tables staged in its shared memory): small CTAs spread a small batch over more
+SMs, large ones amortise the staging.  ``tune`` times the candidates with CUDA
+events on the given batch, applies the fastest and records it in a JSON cache
+(keyed by GPU name, model tables, function, precision and batch size) so that
+later processes reuse it without timing again.  The heterogeneous launch is
+tuned over its threads_per_block argument (``tune_multi``).
 """
 from __future__ import annotations
 
@@ -21,7 +25,8 @@ import numpy as np
 from . import _capi, api
 from . import sample_models as sm
 
-CANDIDATES = (32, 64, 96, 128)
+CANDIDATES = (32, 64, 96, 128)  # configurations per CTA, one thread each
+WARP = "warp"  # one warp per configuration (RNEA, ABA)
 CACHE_PATH = os.environ.get(
     "PINOCCHIO_GB300_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "pinocchio_gb300", "autotune.json")
 )
@@ -73,7 +78,7 @@ def _time(fn, reps=5):
 
 def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives"), batch=16384,
          candidates=CANDIDATES, use_cache=True):
-    """Tune ``data``'s device model; returns {function: (threads_per_block, ms)}."""
+    """Tune ``data``'s device model; returns {function: (threads_per_block or WARP, ms)}."""
     import torch
 
     dev = torch.cuda.get_device_name()
@@ -87,22 +92,31 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
         "rnea_derivatives": lambda: api.computeRNEADerivatives(model, data, q, v, x),
         "aba_derivatives": lambda: api.computeABADerivatives(model, data, q, v, x),
     }
+    def apply(f, setting):
+        L = _capi.lib()
+        if setting == WARP:
+            _capi.check(L.gb_model_set_layout(data.dev.h, _FUNCS[f], _capi.GB_INSTANCE_PER_WARP))
+        else:
+            _capi.check(L.gb_model_set_layout(data.dev.h, _FUNCS[f], _capi.GB_INSTANCE_PER_THREAD))
+            _capi.check(L.gb_model_set_launch(data.dev.h, _FUNCS[f], int(setting)))
+
     result = {}
     for f in functions:
         ck = f"{key}|{f}"
         if ck in cache:
-            tpb, ms = cache[ck]
+            setting, ms = cache[ck]
         else:
             best = None
-            for tpb in candidates:
-                _capi.check(_capi.lib().gb_model_set_launch(data.dev.h, _FUNCS[f], tpb))
+            settings = list(candidates) + ([WARP] if f in ("rnea", "aba") else [])
+            for st in settings:
+                apply(f, st)
                 ms = _time(calls[f])
                 if best is None or ms < best[1]:
-                    best = (tpb, ms)
-            tpb, ms = best
-            cache[ck] = [tpb, ms]
-        _capi.check(_capi.lib().gb_model_set_launch(data.dev.h, _FUNCS[f], int(tpb)))
-        result[f] = (int(tpb), float(ms))
+                    best = (st, ms)
+            setting, ms = best
+            cache[ck] = [setting, ms]
+        apply(f, setting)
+        result[f] = (setting if setting == WARP else int(setting), float(ms))
     if use_cache:
         _save(cache)
     return result

@@ -172,6 +172,17 @@ int gb_model_set_launch(gb_model* M, int function, int threads_per_block) {
   return GB_OK;
 }
 
+int gb_model_set_layout(gb_model* M, int function, int layout) {
+  if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
+  if (function < GB_FUNC_RNEA || function > GB_FUNC_ABA_DERIVATIVES) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown function");
+  if (layout != GB_INSTANCE_PER_THREAD && layout != GB_INSTANCE_PER_WARP)
+    return set_error(GB_ERR_INVALID_ARGUMENT, "unknown layout");
+  if (layout == GB_INSTANCE_PER_WARP && function != GB_FUNC_RNEA && function != GB_FUNC_ABA)
+    return set_error(GB_ERR_UNSUPPORTED, "the warp-per-instance layout exists for RNEA and ABA only");
+  M->layout[function] = layout;
+  return GB_OK;
+}
+
 // ---- ModelPool and the *InParallel entry points ------------------------------------------
 int gb_pool_create(const gb_model* M, long size, gb_pool** out) {
   if (!M || !out) return set_error(GB_ERR_INVALID_ARGUMENT, "model/out is NULL");

@@ -17,6 +17,7 @@ struct gb_model {
   std::vector<int> parents, jtype, idx_q, idx_v, nvs, nvsub, depth, pfr, nsfr, rel_off, rel_list, slot;
   int nslot = 0;
   int tpb[8] = {128, 128, 128, 128, 128, 128, 128, 128};  // configurations per CTA, per GB_FUNC_*
+  int layout[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // GB_INSTANCE_PER_THREAD / _PER_WARP, per GB_FUNC_*
   std::vector<double> placement, inertia, armature;
   double gravity[6];
   std::vector<unsigned char> blob;  // host copy of the device blob

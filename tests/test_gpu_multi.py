@@ -69,7 +69,53 @@ def test_autotuner_keeps_results(tmp_path, monkeypatch):
     q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 3000, 2))
     before = pg.aba(model, data, q, v, x).clone()
     res = autotune.tune(model, data, functions=("aba", "rnea"), batch=4096)
-    assert set(res) == {"aba", "rnea"} and all(t in autotune.CANDIDATES for t, _ in res.values())
+    assert set(res) == {"aba", "rnea"} and all(t in autotune.CANDIDATES or t == autotune.WARP for t, _ in res.values())
     assert torch.equal(pg.aba(model, data, q, v, x), before)
     again = autotune.tune(model, data, functions=("aba", "rnea"), batch=4096)  # served from the cache
     assert again == {k: (t, ms) for k, (t, ms) in res.items()}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100"])
+def test_warp_layout_matches_thread_layout_bitwise(name, precision):
+    """The warp-per-instance layout (gb_model_set_layout) gives the thread layout's
+    results for RNEA, ABA, nonLinearEffects and gravity -- the same bits in FP64,
+    FP32 rounding in the mixed kernels (the compiler may contract their FP32
+    multiply-adds differently in the two kernels) -- and matches the oracle."""
+    import torch
+
+    from util import MODELS
+
+    model = MODELS[name]()
+    q, v, x = sm.random_inputs(model, 203, 9)
+    d = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    data = pg.createData(model, precision)
+    L = pg._capi.lib()
+    outs = {}
+    for layout in (pg._capi.GB_INSTANCE_PER_THREAD, pg._capi.GB_INSTANCE_PER_WARP):
+        for f in (pg._capi.GB_FUNC_RNEA, pg._capi.GB_FUNC_ABA):
+            pg._capi.check(L.gb_model_set_layout(data.dev.h, f, layout))
+        outs[layout] = [
+            pg.rnea(model, data, d(q), d(v), d(x)).cpu().numpy(),
+            pg.aba(model, data, d(q), d(v), d(10.0 * x)).cpu().numpy(),
+            pg.nonLinearEffects(model, data, d(q), d(v)).cpu().numpy(),
+            pg.computeGeneralizedGravity(model, data, d(q)).cpu().numpy(),
+        ]
+    for k, (a, b) in enumerate(zip(outs[0], outs[1])):
+        if precision == "fp64":
+            assert np.array_equal(a, b), k
+        else:
+            assert rel_err(b, a) < 1e-6, (k, rel_err(b, a))
+    om = OracleModel(model)
+    tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else MIXED_TOL
+    if precision == "fp64" or name != "chain100":
+        assert rel_err(outs[1][0], om.rnea(q, v, x)) < tol
+        assert rel_err(outs[1][1], om.aba(q, v, 10.0 * x, LOCAL)) < tol
+
+
+def test_layout_setting_errors():
+    model = sm.manipulator6r(0)
+    data = pg.createData(model)
+    L = pg._capi.lib()
+    assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_CRBA, pg._capi.GB_INSTANCE_PER_WARP) == pg._capi.GB_ERR_UNSUPPORTED
+    assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_RNEA, 5) == pg._capi.GB_ERR_INVALID_ARGUMENT
