@@ -79,6 +79,14 @@ int gb_model_destroy(gb_model* model);
 int gb_model_dims(const gb_model* model, int* nq, int* nv, int* njoints);
 const char* gb_last_error(void);
 
+/* Diagnostic without a reference counterpart: how many warps of the pipelined
+ * kernels (asynchronous bulk copies and producer / consumer barriers, each
+ * wait limited to 2 s) gave up waiting since the library was loaded, or since
+ * the last reset (reset != 0 clears the count after reading it).  Non-zero
+ * means some outputs of those calls were not written.  Synchronises the
+ * device. */
+int gb_pipeline_timeouts(unsigned int* count, int reset);
+
 /* tau = rnea(model, data, q, v, a) for every instance
  * (reference algorithm/rnea.hxx:117-161, public rnea.hxx:766). */
 int gb_rnea(const gb_model* model, int precision, int layout, long batch, const double* q, const double* v,

@@ -10,6 +10,11 @@
 // and for every column c the warp loops only over the rows k that can be
 // non-zero in column c of dtau (ancestors and subtree of c) -- the reference
 // multiplies the dense matrices.
+#include <algorithm>
+#include <type_traits>
+#include <vector>
+
+#include "gb_async.cuh"
 #include "gb_derivs.cuh"
 #include "gb_internal.h"
 
@@ -242,6 +247,247 @@ __global__ void __launch_bounds__(512, 2)
   }
 }
 
+// The mixed-precision products as a warp-specialised pipeline: one persistent
+// CTA per SM walks the blocks of kBlk configurations with two stages.
+//  - Producer warps (GB_PROD_PWARPS): for block j they wait until stage j % 2
+//    is free, let the TMA unit copy both dtau matrices of the block (FP32,
+//    already in the [element][configuration] order the FMA loop reads) into
+//    the stage with one bulk copy completing on full_x, read the packed upper
+//    Minv (double-float) with coalesced loads, write the FP64 Minv output and
+//    the full FP32 Minv of the stage, and arrive on full_m.
+//  - Consumer warps (GB_PROD_CWARPS): wait on full_x and full_m, run the
+//    column-group products of k_minv_products with four output rows per lane
+//    (Minv kept as [k][row / 4][configuration][row % 4]: one 16-byte load gives
+//    a lane its four Minv(k, row), each X(k, c) read feeds four FMAs), write the
+//    outputs and arrive on empty.  Warp tasks (matrix, column group, 16 rows)
+//    are assigned in longest-processing-time order (ProdPlan).
+// The producers fill block j + 1 while the consumers work on block j; no CTA-wide
+// barrier after the start.  Every wait gives up after kPipeWaitNs (counted in
+// g_pipe_timeouts).  Same FP32 products and summation order as k_minv_products:
+// the outputs are bit-identical to k_minv_products<3, float, float, dfloat>.
+#ifndef GB_PROD_CWARPS
+#define GB_PROD_CWARPS 12
+#endif
+#ifndef GB_PROD_PWARPS
+#define GB_PROD_PWARPS 4
+#endif
+constexpr int kProdMaxWarps = 32, kProdMaxTasks = 256, kProdRows = 16;  // rows per task (4 per lane)
+struct ProdPlan {
+  unsigned short woff[kProdMaxWarps + 1];  // consumer warp w runs task[woff[w] .. woff[w+1])
+  unsigned short task[kProdMaxTasks];      // matrix | group << 1 | row chunk << 8
+};
+__device__ unsigned int g_pipe_timeouts = 0;  // warps whose pipeline wait gave up (gb_pipeline_timeouts)
+constexpr unsigned long long kPipeWaitNs = 2000000000ull;
+
+struct PipeSmem {
+  size_t oK, oX0, oX1, oM0, oM1, oT, bytes;
+};
+__host__ __device__ __forceinline__ PipeSmem pipe_smem(int nv, int ng, int nrel) {
+  const size_t nn = (size_t)nv * nv, npk = (size_t)nv * (nv + 1) / 2;
+  PipeSmem p;
+  p.oK = 64;  // seven mbarriers first
+  p.oX0 = p.oK + ((npk * kBlk * sizeof(gb::dfloat) + 15) & ~(size_t)15);
+  p.oX1 = p.oX0 + 2 * nn * kBlk * sizeof(float);
+  p.oM0 = p.oX1 + 2 * nn * kBlk * sizeof(float);
+  p.oM1 = p.oM0 + nn * kBlk * sizeof(float);
+  p.oT = p.oM1 + nn * kBlk * sizeof(float);
+  p.bytes = p.oT + sizeof(int) * (4 * (size_t)ng + nrel);
+  return p;
+}
+
+__global__ void __launch_bounds__((GB_PROD_CWARPS + GB_PROD_PWARPS) * 32, 1)
+    k_minv_products_pipe(const unsigned char* blob, long B, const gb::dfloat* wsMi, Arr Minv, bool minv_upper,
+                         const float* wsP, long nP, Arr out0, Arr out1, const __grid_constant__ ProdPlan plan) {
+  constexpr int Gs = kBlk, CW = GB_PROD_CWARPS, PW = GB_PROD_PWARPS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(blob);
+  const int nv = h->nv, ng = h->ngroup, nrel = h->n_grp_rel;
+  const int nn = nv * nv, npk = nv * (nv + 1) / 2;
+  const PipeSmem P = pipe_smem(nv, ng, nrel);
+  uint64_t* full_x = reinterpret_cast<uint64_t*>(smem_raw);  // [2]: the stage's dtau copy landed
+  uint64_t* full_m = full_x + 2;                             // [2]: the stage's FP32 Minv is written
+  uint64_t* empty = full_x + 4;                              // [2]: the consumers are done with the stage
+  uint64_t* full_k = full_x + 6;                             // the packed Minv copy landed (one buffer)
+  gb::dfloat* sK = reinterpret_cast<gb::dfloat*>(smem_raw + P.oK);
+  float* const sX0 = reinterpret_cast<float*>(smem_raw + P.oX0);
+  float* const sX1 = reinterpret_cast<float*>(smem_raw + P.oX1);
+  float* const sM0 = reinterpret_cast<float*>(smem_raw + P.oM0);
+  float* const sM1 = reinterpret_cast<float*>(smem_raw + P.oM1);
+  int* sgrp = reinterpret_cast<int*>(smem_raw + P.oT);
+  int* srel = sgrp + 4 * ng;
+  const uint32_t bytesX = 2u * nn * Gs * sizeof(float), bytesK = (uint32_t)npk * Gs * sizeof(gb::dfloat);
+  const long nblk = (B + kBlk - 1) / kBlk;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      gb::mbar_init(&full_x[s], 1);
+      gb::mbar_init(&full_m[s], PW * 32);
+      gb::mbar_init(&empty[s], CW * 32);
+    }
+    gb::mbar_init(full_k, 1);
+    gb::fence_mbar_init();
+  }
+  for (int t = threadIdx.x; t < 4 * ng; t += blockDim.x) sgrp[t] = reinterpret_cast<const int*>(blob + h->o_grp)[t];
+  for (int t = threadIdx.x; t < nrel; t += blockDim.x) srel[t] = reinterpret_cast<const int*>(blob + h->o_grp_rel)[t];
+  __syncthreads();
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int lg = lane & (Gs - 1);
+  auto give_up = [&]() {
+    if (lane == 0) atomicAdd(&g_pipe_timeouts, 1u);
+  };
+  if (warp >= CW) {  // ---------------- producers
+    const int pt = threadIdx.x - CW * 32, pw = warp - CW, lr = lane >> 3;
+    double* Mo = const_cast<double*>(Minv.p);
+    auto load_minv = [&](long blk) {
+      gb::mbar_arrive_expect_tx(full_k, bytesK);
+      gb::bulk_load(sK, wsMi + blk * (long)npk * Gs, bytesK, full_k);
+    };
+    if (pt == 0 && blockIdx.x < nblk) load_minv(blockIdx.x);
+    int j = 0;
+    for (long blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++j) {
+      const int s = j & 1;
+      const uint32_t n = (uint32_t)(j >> 1);
+      bool ok = j < 2 || gb::mbar_wait(&empty[s], (n - 1) & 1u, kPipeWaitNs);
+      ok = gb::named_bar_all(1, PW * 32, ok);  // the same decision in every producer thread
+      if (ok && pt == 0) {
+        gb::fence_proxy_async();
+        gb::mbar_arrive_expect_tx(&full_x[s], bytesX);
+        gb::bulk_load(s ? sX1 : sX0, wsP + blk * nP * Gs, bytesX, &full_x[s]);
+      }
+      const bool issued_x = ok;
+      ok = gb::named_bar_all(1, PW * 32, ok && gb::mbar_wait(full_k, (uint32_t)j & 1u, kPipeWaitNs));
+      if (!ok) {
+        if (pt == 0) {  // let the copies this thread issued finish before leaving
+          gb::mbar_wait(full_k, (uint32_t)j & 1u, kPipeWaitNs);
+          if (issued_x) gb::mbar_wait(&full_x[s], n & 1u, kPipeWaitNs);
+          if (j >= 1) gb::mbar_wait(&full_x[s ^ 1], ((uint32_t)(j - 1) >> 1) & 1u, kPipeWaitNs);
+        }
+        give_up();
+        return;
+      }
+      float* sM = s ? sM1 : sM0;
+      const long b0 = blk * kBlk;
+      const int g_here = (int)min((long)Gs, B - b0);
+      double* ob = Mo + (b0 + lg) * Minv.is;
+      // one packed entry (a <= b) per lane step; producer warp t takes rows t, nv - 1 - t, t + PW, ...
+      for (int t = pw; 2 * t < nv; t += PW) {
+#pragma unroll 1
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int a = h2 == 0 ? t : nv - 1 - t;
+          if (h2 == 1 && a == t) break;
+          const int pa = a * nv - (a * (a - 1)) / 2 - a;  // upk(a, b) = pa + b for b >= a
+          for (int b = a + lr; b < nv; b += 4) {
+            const gb::dfloat x = sK[(pa + b) * Gs + lg];
+            const float xf = float(x);
+            sM[(a * nv + b) * Gs + lg] = xf;
+            sM[(b * nv + a) * Gs + lg] = xf;
+            if (lg < g_here) {
+              const double xd = to_double(x);
+              ob[(long)(a * nv + b) * Minv.es] = xd;
+              ob[(long)(b * nv + a) * Minv.es] = minv_upper && b > a ? 0.0 : xd;
+            }
+          }
+        }
+      }
+      gb::named_bar(1, PW * 32);  // all producers are done with sK
+      const long nxt = blk + gridDim.x;
+      if (pt == 0 && nxt < nblk) {
+        gb::fence_proxy_async();
+        load_minv(nxt);
+      }
+      gb::mbar_arrive(&full_m[s]);
+    }
+    return;
+  }
+  // ---------------- consumers
+  // lane = (configuration quad cq, column c_l, row r_l): configurations 4 cq .. 4 cq + 3, columns c_l and
+  // c_l + 4 of the group, rows r_l + 4 i (i < 4) of the task's 16; every shared load is 16 bytes (four
+  // configurations) and the 32 lanes' addresses fall in distinct banks
+  const int cq = lane >> 4, cl = (lane >> 2) & 3, rl = lane & 3;
+  int j = 0;
+  for (long blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++j) {
+    const int s = j & 1;
+    const uint32_t par = (uint32_t)(j >> 1) & 1u;
+    if (!gb::mbar_wait(&full_x[s], par, kPipeWaitNs) || !gb::mbar_wait(&full_m[s], par, kPipeWaitNs)) {
+      give_up();
+      return;
+    }
+    const long b0 = blk * kBlk;
+    const int g_here = (int)min((long)Gs, B - b0);
+    const float* sX = s ? sX1 : sX0;
+    const float* sM = s ? sM1 : sM0;
+    for (int p = plan.woff[warp]; p < plan.woff[warp + 1]; ++p) {
+      const int task = plan.task[p];
+      const int mm = task & 1, gi = (task >> 1) & 127, rch = task >> 8;
+      const int c0 = sgrp[4 * gi], nc = sgrp[4 * gi + 1], k0 = sgrp[4 * gi + 2], k1 = sgrp[4 * gi + 3];
+      const int r0 = rch * kProdRows + rl;  // the lane's rows: r0 + 4 i
+      const float* Xg = sX + ((long)mm * nn + c0 + cl) * Gs + 4 * cq;
+      const float* Mr[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Mr[i] = sM + min(r0 + 4 * i, nv - 1) * Gs + 4 * cq;  // rows past nv: not stored
+      float acc[4][2][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc)
+#pragma unroll
+          for (int g = 0; g < 4; ++g) acc[i][cc][g] = 0.f;
+#pragma unroll 2
+      for (int kk = k0; kk < k1; ++kk) {
+        const int kb = srel[kk] * nv * Gs;
+        const float4 x0 = *reinterpret_cast<const float4*>(Xg + kb);  // X(k, c_l), X(k, c_l + 4): past the group
+        const float4 x1 = *reinterpret_cast<const float4*>(Xg + kb + 4 * Gs);  // padded, not stored
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float4 m = *reinterpret_cast<const float4*>(Mr[i] + kb);  // Minv(k, r) = Minv(r, k)
+          acc[i][0][0] += m.x * x0.x; acc[i][0][1] += m.y * x0.y; acc[i][0][2] += m.z * x0.z; acc[i][0][3] += m.w * x0.w;
+          acc[i][1][0] += m.x * x1.x; acc[i][1][1] += m.y * x1.y; acc[i][1][2] += m.z * x1.z; acc[i][1][3] += m.w * x1.w;
+        }
+      }
+      const Arr& o = mm == 0 ? out0 : out1;
+      double* ob = const_cast<double*>(o.p) + (b0 + 4 * cq) * o.is + (long)(c0 + cl) * o.es;
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        if (4 * cq + g >= g_here) break;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = r0 + 4 * i;
+          if (r >= nv) break;
+          double* op = ob + g * o.is + (long)r * nv * o.es;
+          if (cl < nc) op[0] = to_double(-acc[i][0][g]);
+          if (cl + 4 < nc) op[4 * o.es] = to_double(-acc[i][1][g]);
+        }
+      }
+    }
+    gb::mbar_arrive(&empty[s]);
+  }
+}
+
+// Longest-processing-time assignment of the product tasks to nwarps warps.
+bool make_prod_plan(const gb_model* M, int nwarps, ProdPlan& plan) {
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  const int* grp = reinterpret_cast<const int*>(M->blob.data() + h->o_grp);
+  const int ng = h->ngroup, nrt = (M->nv + kProdRows - 1) / kProdRows, nt = 2 * ng * nrt;
+  if (nt > kProdMaxTasks || nwarps > kProdMaxWarps || ng > 127 || nrt > 127) return false;
+  std::vector<std::pair<int, int>> tasks;  // (cost, task)
+  for (int mm = 0; mm < 2; ++mm)
+    for (int gi = 0; gi < ng; ++gi)
+      for (int rch = 0; rch < nrt; ++rch) tasks.push_back({grp[4 * gi + 3] - grp[4 * gi + 2] + 2, mm | gi << 1 | rch << 8});
+  std::stable_sort(tasks.begin(), tasks.end(), [](auto a, auto b) { return a.first > b.first; });
+  std::vector<long> load(nwarps, 0);
+  std::vector<std::vector<int>> per(nwarps);
+  for (const auto& ct : tasks) {
+    const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[w] += ct.first;
+    per[w].push_back(ct.second);
+  }
+  int p = 0;
+  for (int w = 0; w <= kProdMaxWarps; ++w) {
+    plan.woff[w] = (unsigned short)p;
+    if (w < nwarps) for (int t : per[w]) plan.task[p++] = (unsigned short)t;
+  }
+  return true;
+}
+
 int blob_smem(const gb_model* M, const void* kernel, const char* name) {
   if (M->blob_bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, M->blob_bytes);
@@ -273,6 +519,35 @@ int ws_alloc(Workspace& w, size_t bytes, cudaStream_t st) {
   return cuda_error(cudaMallocAsync(&w.p, bytes, st), "workspace allocation");
 }
 
+#ifndef GB_PROD_PIPE
+#define GB_PROD_PIPE 1
+#endif
+// the pipelined mixed products when the two stages fit in one CTA's shared
+// memory (nv <= 32); used == false leaves the call to k_minv_products
+int launch_products_pipe(const gb_model* M, long B, const gb::dfloat* wsMi, Arr Minv, bool minv_upper,
+                         const float* wsP, long nP, Arr o0, Arr o1, cudaStream_t st, bool& used) {
+  used = false;
+  if (!GB_PROD_PIPE) return GB_OK;
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  const PipeSmem P = pipe_smem(M->nv, h->ngroup, h->n_grp_rel);
+  int dev = 0, optin = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_error(e, "k_minv_products_pipe");
+  if (P.bytes > (size_t)optin) return GB_OK;
+  ProdPlan plan;  // a few dozen tasks: rebuilt per call
+  if (!make_prod_plan(M, GB_PROD_CWARPS, plan)) return GB_OK;
+  e = cudaFuncSetAttribute(k_minv_products_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.bytes);
+  if (e != cudaSuccess) return cuda_error(e, "k_minv_products_pipe");
+  const long nblk = (B + kBlk - 1) / kBlk;
+  const long grid = std::min<long>(nblk, nsm);
+  k_minv_products_pipe<<<(unsigned)grid, (GB_PROD_CWARPS + GB_PROD_PWARPS) * 32, P.bytes, st>>>(M->d_blob, B, wsMi, Minv, minv_upper, wsP,
+                                                                          nP, o0, o1, plan);
+  used = true;
+  return cuda_error(cudaGetLastError(), "k_minv_products_pipe");
+}
+
 // S: scalar of the products (smem, FMA); W: scalar of the dtau matrices in the
 // workspace; KM: scalar of the packed Minv in the workspace
 // products == false: only the Minv output (symmetric, or upper with zeros below when minv_upper)
@@ -280,6 +555,14 @@ template <class S, class W, class KM>
 int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, const W* wsP,
                          const gb::DerivLayout& L, Arr o0, Arr o1, cudaStream_t st, bool products = true,
                          bool minv_upper = false) {
+  if constexpr (std::is_same<S, float>::value && std::is_same<W, float>::value &&
+                std::is_same<KM, gb::dfloat>::value) {
+    if (products) {
+      bool used = false;
+      const int rc = launch_products_pipe(M, B, wsMi, Minv, minv_upper, wsP, L.nP, o0, o1, st, used);
+      if (rc != GB_OK || used) return rc;
+    }
+  }
   const long nn = (long)M->nv * M->nv, npk = (long)M->nv * (M->nv + 1) / 2;
   const int ngroup = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->ngroup;
   const int nrel = reinterpret_cast<const gb::BlobHeader*>(M->blob.data())->n_grp_rel;
@@ -561,6 +844,17 @@ int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr
   } while (0)
 
 extern "C" {
+
+int gb_pipeline_timeouts(unsigned int* count, int reset) {
+  if (count == nullptr) return gbi::set_error(GB_ERR_INVALID_ARGUMENT, "count is NULL");
+  GB_TRY(gbi::cuda_error(cudaDeviceSynchronize(), "gb_pipeline_timeouts"));
+  GB_TRY(gbi::cuda_error(cudaMemcpyFromSymbol(count, gbi::g_pipe_timeouts, sizeof(unsigned int)), "gb_pipeline_timeouts"));
+  if (reset) {
+    const unsigned int zero = 0;
+    GB_TRY(gbi::cuda_error(cudaMemcpyToSymbol(gbi::g_pipe_timeouts, &zero, sizeof(unsigned int)), "gb_pipeline_timeouts"));
+  }
+  return GB_OK;
+}
 
 int gb_rnea_derivatives(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
                         const double* v, const double* a, double* dtau_dq, double* dtau_dv, double* Mo, double* tau,

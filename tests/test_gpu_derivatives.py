@@ -145,3 +145,38 @@ def test_aba_derivatives_vjp(case, precision):
     assert rel_err(qb, np.einsum("bk,bkc->bc", g, dq)) < tol
     assert rel_err(vb, np.einsum("bk,bkc->bc", g, dv)) < tol
     assert rel_err(tb, np.einsum("bkc,bc->bk", Minv, g)) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_aba_derivatives_large_batch_matches_slices(precision):
+    """A batch large enough that every CTA of the product kernel walks several
+    blocks (both pipeline stages, many barrier phases) gives, bit for bit, the
+    results of the same configurations computed in small batches; the SOA
+    layout gives the same bits as the instance layout; no pipeline wait gave up."""
+    import torch
+
+    model = MODELS["humanoid32"]()
+    B, nv = 3001, model.nv
+    q, v, x = sm.random_inputs(model, B, 77)
+    tau = 10.0 * x
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    data = pg.createData(model, precision)
+    full = [t.clone() for t in pg.computeABADerivatives(model, data, dev(q), dev(v), dev(tau))]
+    for lo, hi in ((0, 41), (1500, 1517), (B - 9, B)):
+        part = pg.computeABADerivatives(model, data, dev(q[lo:hi]), dev(v[lo:hi]), dev(tau[lo:hi]))
+        for f, p in zip(full, part):
+            assert torch.equal(f[lo:hi], p)
+    qs, vs, ts = (dev(t.T) for t in (q, v, tau))
+    outs = [torch.empty((nv * nv, B), dtype=torch.float64, device="cuda") for _ in range(3)]
+    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    prec = _capi.GB_FP64 if precision == "fp64" else _capi.GB_MIXED
+    _capi.check(
+        _capi.lib().gb_aba_derivatives(data.dev.h, prec, _capi.GB_LAYOUT_SOA, B, ptr(qs), ptr(vs), ptr(ts),
+                                       ptr(outs[0]), ptr(outs[1]), ptr(outs[2]), None, None)
+    )
+    torch.cuda.synchronize()
+    for o, r in zip(outs, full):
+        assert torch.equal(o.T.reshape(B, nv, nv), r)
+    n = C.c_uint(7)
+    _capi.check(_capi.lib().gb_pipeline_timeouts(C.byref(n), 0))
+    assert n.value == 0
