@@ -282,8 +282,12 @@ def measure_rollout(torch, pg, sm, B=8192, T=64, n=100):
     v0 = d(0.1 * rng.standard_normal((B, n)))
     taus = d(rng.standard_normal((T, B, n)))
     out = {"batch": B, "steps": T, "nv": n, "checkpoint_every": 8}
+    from pinocchio_gb300 import autotune
+
     for prec in ("fp64", "mixed"):
         data = pg.createData(model, prec)
+        # layout per function for this model and batch (the deep chain favours a warp per trajectory)
+        tuned = autotune.tune(model, data, functions=("aba", "aba_derivatives"), batch=B, use_cache=False)
 
         def once():
             q0.grad = v0.grad = taus.grad = None
@@ -294,7 +298,8 @@ def measure_rollout(torch, pg, sm, B=8192, T=64, n=100):
 
         ms = _time_call(torch, once, reps=2, warmup=1)
         out[prec] = {"ms_per_rollout": ms, "trajectories_per_s": B / ms * 1e3,
-                     "aba_evals_per_s": B * T / ms * 1e3}
+                     "aba_evals_per_s": B * T / ms * 1e3,
+                     "layouts": {f: (t if isinstance(t, str) else f"thread x{t}") for f, (t, _) in tuned.items()}}
     return out
 
 

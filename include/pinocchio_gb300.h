@@ -195,11 +195,20 @@ int gb_model_set_launch(gb_model* model, int function, int threads_per_block);
 
 /* Layout of one model's function chosen by the autotuner: one thread per
  * configuration (GB_INSTANCE_PER_THREAD, the default) or one warp per
- * configuration (GB_INSTANCE_PER_WARP: the joints of one tree level in
- * parallel, for batches too small to fill the GPU; RNEA and ABA, including
- * nonLinearEffects / generalized gravity and the *_in_parallel entry points).
- * Both layouts give identical results. */
-enum { GB_INSTANCE_PER_THREAD = 0, GB_INSTANCE_PER_WARP = 1 };
+ * configuration (GB_INSTANCE_PER_WARP), for batches too small to fill the GPU.
+ * RNEA and ABA (including nonLinearEffects / generalized gravity and the
+ * *_in_parallel entry points): the warp's lanes take the joints of one tree
+ * level in parallel.  ABA derivatives (and computeMinverse, the VJP): a team of
+ * 4, 8 or 32 lanes per configuration (GB_INSTANCE_PER_4_LANES, _8_LANES,
+ * GB_INSTANCE_PER_WARP) splits the loops over matrix columns of every joint
+ * (subtree, ancestor and Minv-row columns), for deep trees at small batches.
+ * FP64 results are identical in every layout. */
+enum {
+  GB_INSTANCE_PER_THREAD = 0,
+  GB_INSTANCE_PER_WARP = 1,
+  GB_INSTANCE_PER_4_LANES = 2,
+  GB_INSTANCE_PER_8_LANES = 3
+};
 int gb_model_set_layout(gb_model* model, int function, int layout);
 
 /* ModelPool (reference multibody/pool/model.hpp:19-165): `size` nominal

@@ -2,10 +2,14 @@
 configurations per CTA.
 
 Every batched entry point evaluates one configuration per thread by default;
-RNEA and ABA (and the functions built on them) also have a warp-per-instance
-layout, where the 32 lanes of a warp evaluate one configuration with the joints
-of a tree level in parallel (``gb_model_set_layout``): it wins when the batch is
-too small to fill the GPU one thread per configuration.  For the thread layout
+RNEA, ABA (and the functions built on them) and the ABA derivatives also have a
+warp-per-instance layout (``gb_model_set_layout``): for RNEA and ABA the 32
+lanes of a warp evaluate one configuration with the joints of a tree level in
+parallel; for the ABA derivatives a team of 4, 8 or 32 lanes splits the loops
+over matrix columns (subtree, ancestor and Minv-row columns of every joint)
+while every lane repeats the per-joint work, which pays on deep trees such as
+the 100-link chain at small batches.  They win when the batch is too small to
+fill the GPU one thread per configuration.  For the thread layout
 the free parameter is how many configurations share a CTA (and so the model
 tables staged in its shared memory): small CTAs spread a small batch over more
 SMs, large ones amortise the staging.  ``tune`` times the candidates with CUDA
@@ -26,7 +30,10 @@ from . import _capi, api
 from . import sample_models as sm
 
 CANDIDATES = (32, 64, 96, 128)  # configurations per CTA, one thread each
-WARP = "warp"  # one warp per configuration (RNEA, ABA)
+WARP = "warp"  # one warp per configuration (RNEA, ABA, ABA derivatives)
+LANES4, LANES8 = "lanes4", "lanes8"  # a team of 4 or 8 lanes per configuration (ABA derivatives)
+_LAYOUT = {WARP: _capi.GB_INSTANCE_PER_WARP, LANES4: _capi.GB_INSTANCE_PER_4_LANES,
+           LANES8: _capi.GB_INSTANCE_PER_8_LANES}
 CACHE_PATH = os.environ.get(
     "PINOCCHIO_GB300_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "pinocchio_gb300", "autotune.json")
 )
@@ -94,8 +101,8 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
     }
     def apply(f, setting):
         L = _capi.lib()
-        if setting == WARP:
-            _capi.check(L.gb_model_set_layout(data.dev.h, _FUNCS[f], _capi.GB_INSTANCE_PER_WARP))
+        if setting in _LAYOUT:
+            _capi.check(L.gb_model_set_layout(data.dev.h, _FUNCS[f], _LAYOUT[setting]))
         else:
             _capi.check(L.gb_model_set_layout(data.dev.h, _FUNCS[f], _capi.GB_INSTANCE_PER_THREAD))
             _capi.check(L.gb_model_set_launch(data.dev.h, _FUNCS[f], int(setting)))
@@ -108,6 +115,8 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
         else:
             best = None
             settings = list(candidates) + ([WARP] if f in ("rnea", "aba") else [])
+            if f == "aba_derivatives":
+                settings += [LANES4, LANES8, WARP]
             for st in settings:
                 apply(f, st)
                 ms = _time(calls[f])
@@ -116,7 +125,7 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
             setting, ms = best
             cache[ck] = [setting, ms]
         apply(f, setting)
-        result[f] = (setting if setting == WARP else int(setting), float(ms))
+        result[f] = (setting if setting in _LAYOUT else int(setting), float(ms))
     if use_cache:
         _save(cache)
     return result

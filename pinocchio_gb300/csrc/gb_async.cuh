@@ -66,7 +66,10 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 }
 
 // wait until the barrier's phase with the given parity has completed; gives up
-// (returns false) after limit_ns nanoseconds
+// (returns false) after limit_ns nanoseconds.  Each try_wait may suspend the
+// thread for up to kSuspendNs until the phase completes, so waiting warps do
+// not take issue slots from working ones.
+constexpr uint32_t kSuspendNs = 100000;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
   const uint32_t a = smem_u32(bar);
   uint64_t t0 = 0;
@@ -74,10 +77,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(kSuspendNs)
         : "memory");
     if (done) return true;
     if (k == 0) t0 = global_ns();

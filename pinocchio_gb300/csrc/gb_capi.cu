@@ -175,10 +175,13 @@ int gb_model_set_launch(gb_model* M, int function, int threads_per_block) {
 int gb_model_set_layout(gb_model* M, int function, int layout) {
   if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
   if (function < GB_FUNC_RNEA || function > GB_FUNC_ABA_DERIVATIVES) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown function");
-  if (layout != GB_INSTANCE_PER_THREAD && layout != GB_INSTANCE_PER_WARP)
+  if (layout < GB_INSTANCE_PER_THREAD || layout > GB_INSTANCE_PER_8_LANES)
     return set_error(GB_ERR_INVALID_ARGUMENT, "unknown layout");
-  if (layout == GB_INSTANCE_PER_WARP && function != GB_FUNC_RNEA && function != GB_FUNC_ABA)
-    return set_error(GB_ERR_UNSUPPORTED, "the warp-per-instance layout exists for RNEA and ABA only");
+  if (layout == GB_INSTANCE_PER_WARP && function != GB_FUNC_RNEA && function != GB_FUNC_ABA &&
+      function != GB_FUNC_ABA_DERIVATIVES)
+    return set_error(GB_ERR_UNSUPPORTED, "the warp-per-instance layout exists for RNEA, ABA and the ABA derivatives");
+  if ((layout == GB_INSTANCE_PER_4_LANES || layout == GB_INSTANCE_PER_8_LANES) && function != GB_FUNC_ABA_DERIVATIVES)
+    return set_error(GB_ERR_UNSUPPORTED, "lane teams of 4 or 8 exist for the ABA derivatives only");
   M->layout[function] = layout;
   return GB_OK;
 }

@@ -15,30 +15,10 @@
 #include <vector>
 
 #include "gb_async.cuh"
-#include "gb_derivs.cuh"
-#include "gb_internal.h"
+#include "gb_sweeps.cuh"
 
 namespace gbi {
 namespace {
-
-constexpr int kThreads = 128;
-// resident CTAs of kThreads per SM the derivative sweeps are compiled for (caps registers per thread)
-#ifndef GB_DERIV_MINB
-#define GB_DERIV_MINB 4
-#endif
-
-__device__ __forceinline__ gb::MView stage_model(const unsigned char* __restrict__ blob, int bytes,
-                                                 unsigned char* smem) {
-  const uint4* src = reinterpret_cast<const uint4*>(blob);
-  uint4* dst = reinterpret_cast<uint4*>(smem);
-  for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x) dst[k] = src[k];
-  __syncthreads();
-  return gb::make_view(smem);
-}
-__device__ __forceinline__ gb::In in_at(const Arr& a, long b) { return gb::In{a.p + b * a.is, a.es}; }
-__device__ __forceinline__ gb::Out out_at(const Arr& a, long b) {
-  return gb::Out{const_cast<double*>(a.p) + b * a.is, a.es};
-}
 
 template <class S>
 __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* blob, int bytes, long B,
@@ -52,67 +32,6 @@ __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* b
   const gb::Out to = out_at(tau, b);
   gb::rnea_derivs_one<S>(m, L, w, in_at(q, b), in_at(v, b), in_at(a, b), out_at(dq, b), out_at(dv, b), out_at(Mo, b),
                          tau.p ? &to : nullptr, symmetric, true);
-}
-
-// The ABA-derivative sweeps as three kernels (passes 1-2, pass 3, pass 4), so
-// that each keeps fewer values live than one fused kernel would (register use
-// bounds the number of resident warps).  The workspace carries everything
-// between them.
-// Blocked workspace layout of the arrays the product kernel reads (Minv,
-// dtau_dq, dtau_dv): configurations in blocks of kBlk, element e of
-// configuration b at ((b / kBlk) * n + e) * kBlk + b % kBlk for an array of n
-// elements -- a warp of the sweep kernels still accesses whole 32-byte
-// segments, and one block is contiguous for the product kernel.
-constexpr int kBlk = 8;
-template <class T> __device__ __forceinline__ gb::Ws<T> blocked(T* base, long n, long b) {
-  return gb::Ws<T>{base + (b / kBlk) * n * kBlk + (b % kBlk), kBlk};
-}
-
-template <class K, class SS>
-__global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
-    k_aba_derivs_pass12(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, SS* wsSS, K* wsMB,
-                        int npk, Arr q, Arr v, Arr tau) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const gb::MView m = stage_model(blob, bytes, smem);
-  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  gb::aba_derivs_pass12<K, SS>(m, L, gb::Ws<K>{wsK + b, B}, gb::Ws<SS>{wsSS + b, B}, blocked(wsMB, npk, b),
-                               in_at(q, b), in_at(v, b), in_at(tau, b));
-}
-
-template <class S, class T, class K>
-__global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
-    k_aba_derivs_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, K* wsMB,
-                       int npk, Arr v, Arr ddq) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const gb::MView m = stage_model(blob, bytes, smem);
-  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  const gb::Out dd = out_at(ddq, b);
-  gb::aba_derivs_pass3<S, T, K>(m, L, m.slot, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, blocked(wsMB, npk, b),
-                                in_at(v, b), ddq.p ? &dd : nullptr);
-}
-
-// the Minv recursion of computeMinverse (pass 3 without velocities and column sets)
-template <class K>
-__global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
-    k_minverse_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, K* wsMB, int npk) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const gb::MView m = stage_model(blob, bytes, smem);
-  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  gb::aba_derivs_pass3<K, K, K, true>(m, L, m.slot, gb::Ws<K>{wsK + b, B}, gb::Ws<K>{wsK + b, B},
-                                      blocked(wsMB, npk, b), gb::In{nullptr, 0}, nullptr);
-}
-
-template <class S, class T, class K, class P>
-__global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
-    k_aba_derivs_pass4(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, P* wsP) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const gb::MView m = stage_model(blob, bytes, smem);
-  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  gb::aba_derivs_pass4<S, T, K, P>(m, L, gb::Ws<S>{wsS + b, B}, gb::Ws<K>{wsK + b, B}, blocked(wsP, L.nP, b));
 }
 
 __device__ __forceinline__ double to_double(double x) { return x; }
@@ -445,16 +364,28 @@ __global__ void __launch_bounds__((GB_PROD_CWARPS + GB_PROD_PWARPS) * 32, 1)
       }
       const Arr& o = mm == 0 ? out0 : out1;
       double* ob = const_cast<double*>(o.p) + (b0 + 4 * cq) * o.is + (long)(c0 + cl) * o.es;
+      const bool st0 = cl < nc, st1 = cl + 4 < nc;
+      if (o.es == 1 && g_here == Gs && r0 + 12 < nv) {  // the common case: predicated stores only
 #pragma unroll
-      for (int g = 0; g < 4; ++g) {
-        if (4 * cq + g >= g_here) break;
+        for (int g = 0; g < 4; ++g)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int r = r0 + 4 * i;
-          if (r >= nv) break;
-          double* op = ob + g * o.is + (long)r * nv * o.es;
-          if (cl < nc) op[0] = to_double(-acc[i][0][g]);
-          if (cl + 4 < nc) op[4 * o.es] = to_double(-acc[i][1][g]);
+          for (int i = 0; i < 4; ++i) {
+            double* op = ob + g * o.is + (r0 + 4 * i) * nv;
+            if (st0) op[0] = to_double(-acc[i][0][g]);
+            if (st1) op[4] = to_double(-acc[i][1][g]);
+          }
+      } else {
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          if (4 * cq + g >= g_here) break;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int r = r0 + 4 * i;
+            if (r >= nv) break;
+            double* op = ob + g * o.is + (long)r * nv * o.es;
+            if (st0) op[0] = to_double(-acc[i][0][g]);
+            if (st1) op[4 * o.es] = to_double(-acc[i][1][g]);
+          }
         }
       }
     }
@@ -486,14 +417,6 @@ bool make_prod_plan(const gb_model* M, int nwarps, ProdPlan& plan) {
     if (w < nwarps) for (int t : per[w]) plan.task[p++] = (unsigned short)t;
   }
   return true;
-}
-
-int blob_smem(const gb_model* M, const void* kernel, const char* name) {
-  if (M->blob_bytes > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, M->blob_bytes);
-    if (e != cudaSuccess) return cuda_error(e, name);
-  }
-  return GB_OK;
 }
 
 // workspace: stream-ordered allocation from the device's default memory pool
@@ -619,65 +542,20 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   }
   const int tpb = M->tpb[GB_FUNC_RNEA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
-  k_rnea_derivs<S><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L,
+  k_rnea_derivs<S><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
                                                                    static_cast<S*>(ws.p), symmetric, q, v, a, dq, dv,
                                                                    Mo, tau);
   return cuda_error(cudaGetLastError(), "k_rnea_derivs");
 }
 
-// Workspace of the ABA derivatives, regions 256-byte aligned: SS (articulated
-// inertias and u: FP64), K (kinematics, Fcrb columns, U Dinv, Dinv u, velocity
-// / acceleration), S (the derivative column sets stored between passes 3 and
-// 4: computed in T3 by pass 3 and in T by pass 4) -- these three [element]
-// [configuration] -- and, in the blocked layout the product kernel reads, MB
-// (the packed upper Minv, scalar K) and P (dtau_dq, dtau_dv in the scalar of
-// the -Minv*dtau products).  The mixed kernels use K = T = dfloat and
-// S = T3 = P = float.
-struct AbaWs {
-  size_t oK, oS, oMB, oP, bytes;
-};
-template <class S, class K, class SS, class P>
-AbaWs aba_ws_layout(const gb::DerivLayout& L, int nv, long B) {
-  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const size_t Bp = (size_t)((B + kBlk - 1) / kBlk) * kBlk;
-  AbaWs w;
-  w.oK = up(sizeof(SS) * (size_t)L.nSS * B);
-  w.oS = w.oK + up(sizeof(K) * (size_t)L.nK * B);
-  w.oMB = w.oS + up(sizeof(S) * (size_t)L.nS * B);
-  w.oP = w.oMB + up(sizeof(K) * (size_t)nv * (nv + 1) / 2 * Bp);
-  w.bytes = w.oP + up(sizeof(P) * (size_t)L.nP * Bp);
-  return w;
-}
-
-// The three sweep kernels of the ABA derivatives on a workspace laid out by aba_ws_layout.
+// The three sweep kernels of the ABA derivatives on a workspace laid out by
+// aba_ws_layout, in the model's layout (gb_sweeps_t*.cu, one translation unit
+// per team size).
 template <class S, class T3, class T, class K, class SS, class P>
 int launch_aba_sweeps(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq, void* ws, cudaStream_t st) {
-  const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, B);
-  char* base = static_cast<char*>(ws);
-  SS* wsSS = reinterpret_cast<SS*>(base);
-  K* wsK = reinterpret_cast<K*>(base + W.oK);
-  S* wsS = reinterpret_cast<S*>(base + W.oS);
-  K* wsMB = reinterpret_cast<K*>(base + W.oMB);
-  P* wsP = reinterpret_cast<P*>(base + W.oP);
-  const int npk = M->nv * (M->nv + 1) / 2;
-  const int tpb = M->tpb[GB_FUNC_ABA_DERIVATIVES];
-  const long grid = (B + tpb - 1) / tpb;
-  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS>, "k_aba_derivs_pass12");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T3, K>, "k_aba_derivs_pass3");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, T, K, P>, "k_aba_derivs_pass4");
-  if (rc != GB_OK) return rc;
-  k_aba_derivs_pass12<K, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK, wsSS,
-                                                                             wsMB, npk, q, v, tau);
-  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
-  if (rc != GB_OK) return rc;
-  k_aba_derivs_pass3<S, T3, K><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
-                                                                               wsK, wsMB, npk, v, ddq);
-  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass3");
-  if (rc != GB_OK) return rc;
-  k_aba_derivs_pass4<S, T, K, P><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsS,
-                                                                                 wsK, wsP);
-  return cuda_error(cudaGetLastError(), "k_aba_derivs_pass4");
+  constexpr bool f64 = std::is_same<K, double>::value, vjp = std::is_same<P, gb::dfloat>::value;
+  const SweepCall c{f64 ? kSweepFp64 : vjp ? kSweepMixedVjp : kSweepMixed, M, B, q, v, tau, ddq, ws, st};
+  return sweeps_team(c);
 }
 
 template <class S, class T3, class T, class K, class SS, class P>
@@ -750,24 +628,12 @@ int run_minverse(const gb_model* M, long B, Arr q, Arr Minv, bool upper, cudaStr
   Workspace ws;
   int rc = ws_alloc(ws, W.oP, st);  // no dtau region
   if (rc != GB_OK) return rc;
-  char* base = static_cast<char*>(ws.p);
-  K* wsK = reinterpret_cast<K*>(base + W.oK);
-  K* wsMB = reinterpret_cast<K*>(base + W.oMB);
+  K* wsMB = reinterpret_cast<K*>(static_cast<char*>(ws.p) + W.oMB);
   const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
   const Arr zero{reinterpret_cast<const double*>(M->d_blob + h->o_zero), 0, 0};
-  const int npk = M->nv * (M->nv + 1) / 2;
-  const int tpb = M->tpb[GB_FUNC_ABA_DERIVATIVES];
-  const long grid = (B + tpb - 1) / tpb;
-  rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS>, "k_aba_derivs_pass12");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_minverse_pass3<K>, "k_minverse_pass3");
-  if (rc != GB_OK) return rc;
-  k_aba_derivs_pass12<K, SS><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK,
-                                                                             reinterpret_cast<SS*>(base), wsMB, npk, q,
-                                                                             zero, zero);
-  rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
-  if (rc != GB_OK) return rc;
-  k_minverse_pass3<K><<<(unsigned)grid, tpb, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, L, wsK, wsMB, npk);
-  rc = cuda_error(cudaGetLastError(), "k_minverse_pass3");
+  const SweepCall c{std::is_same<K, double>::value ? kMinvFp64 : kMinvMixed, M, B, q, zero, zero, Arr{nullptr, 0, 0},
+                    ws.p, st};
+  rc = sweeps_team(c);
   if (rc != GB_OK) return rc;
   const Arr none{nullptr, 0, 0};
   return launch_minv_products<K, K, K>(M, B, wsMB, Minv, static_cast<const K*>(nullptr), L, none, none, st, false,
@@ -816,6 +682,15 @@ int check_gravity(const gb_model* M) {
 }
 
 }  // namespace
+
+int sweeps_team(const SweepCall& c) {
+  switch (c.M->layout[GB_FUNC_ABA_DERIVATIVES]) {
+    case GB_INSTANCE_PER_WARP: return sweeps_t32(c);
+    case GB_INSTANCE_PER_8_LANES: return sweeps_t8(c);
+    case GB_INSTANCE_PER_4_LANES: return sweeps_t4(c);
+    default: return sweeps_t1(c);
+  }
+}
 
 // The ABA-derivative kernels on a workspace the caller provides (no allocation):
 // total bytes needed for a batch, and the launch itself.

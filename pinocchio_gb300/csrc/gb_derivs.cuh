@@ -29,6 +29,34 @@ template <class T> struct Ws {
   long st;
   GB_HD T& operator[](long e) const { return p[e * st]; }
 };
+// Who runs one configuration's sweeps.  Solo: one thread (every loop serial).
+// LaneTeam<TS>: TS consecutive lanes of a warp; every lane runs the per-joint
+// work (same values), the loops over matrix columns are split by column (rank
+// c % TS owns column c in every pass, so a column's workspace entries are
+// written and read by one lane), and sync() orders the team's workspace
+// accesses where one lane's store could otherwise overtake another lane's load
+// of the same entry (before the stores of a read-modify-write, at the end of
+// every joint).
+struct Solo {
+  static constexpr int size = 1;
+  GB_HD int first(int c0) const { return c0; }  // the first column >= c0 this member owns
+  GB_HD bool owns(int idx) const { return true; }
+  GB_HD void sync() const {}
+};
+#if defined(__CUDACC__)
+template <int TS> struct LaneTeam {
+  static_assert(TS > 1 && TS <= 32 && (TS & (TS - 1)) == 0, "a team is a power-of-two group of lanes");
+  static constexpr int size = TS;
+  int rank;
+  unsigned mask;  // the team's lanes
+  __device__ explicit LaneTeam(int lane)
+      : rank(lane & (TS - 1)), mask(TS == 32 ? 0xffffffffu : ((1u << TS) - 1u) << (lane & ~(TS - 1))) {}
+  __device__ int first(int c0) const { return c0 + ((rank - c0) & (TS - 1)); }
+  __device__ bool owns(int idx) const { return (idx & (TS - 1)) == rank; }
+  __device__ void sync() const { __syncwarp(mask); }
+};
+#endif
+
 template <class T> GB_HD void ld6(const Ws<T>& w, long e, T* x) {
 #pragma unroll
   for (int k = 0; k < 6; ++k) x[k] = w[e + k];
@@ -569,7 +597,8 @@ template <class T, class S> GB_HD void op0_tmv(const Ws<S>& w, long e, const T* 
 }
 // dst += the operator at src (about C) re-expressed about P, r = C - P:
 // [[0, B], [C, D + R B - C R]], R = [r]x
-template <class T, class S> GB_HD void op0_shift_add(const Ws<S>& w, long src, long dst, const T* r) {
+template <class T, class S, class Team = Solo>
+GB_HD void op0_shift_add(const Ws<S>& w, long src, long dst, const T* r, const Team& tm = Team()) {
   T Bm[9], Cm[9], Dacc[9];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -591,15 +620,35 @@ template <class T, class S> GB_HD void op0_shift_add(const Ws<S>& w, long src, l
     Dacc[3 * a + 1] -= dot2(Cm[3 * a + 2], r[0], -Cm[3 * a + 0], r[2]);
     Dacc[3 * a + 2] -= dot2(Cm[3 * a + 0], r[1], -Cm[3 * a + 1], r[0]);
   }
+  if constexpr (Team::size > 1) {  // every lane loads before any lane stores
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const long eb = dst + 6 * a + 3 + b, ec = dst + 6 * (3 + a) + b, ed = dst + 6 * (3 + a) + 3 + b;
-      w[eb] = S(T(w[eb]) + Bm[3 * a + b]);
-      w[ec] = S(T(w[ec]) + Cm[3 * a + b]);
-      w[ed] = S(T(w[ed]) + Dacc[3 * a + b]);
-    }
+      for (int b = 0; b < 3; ++b) {
+        Bm[3 * a + b] = T(w[dst + 6 * a + 3 + b]) + Bm[3 * a + b];
+        Cm[3 * a + b] = T(w[dst + 6 * (3 + a) + b]) + Cm[3 * a + b];
+        Dacc[3 * a + b] = T(w[dst + 6 * (3 + a) + 3 + b]) + Dacc[3 * a + b];
+      }
+    tm.sync();
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        w[dst + 6 * a + 3 + b] = S(Bm[3 * a + b]);
+        w[dst + 6 * (3 + a) + b] = S(Cm[3 * a + b]);
+        w[dst + 6 * (3 + a) + 3 + b] = S(Dacc[3 * a + b]);
+      }
+  } else {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const long eb = dst + 6 * a + 3 + b, ec = dst + 6 * (3 + a) + b, ed = dst + 6 * (3 + a) + 3 + b;
+        w[eb] = S(T(w[eb]) + Bm[3 * a + b]);
+        w[ec] = S(T(w[ec]) + Cm[3 * a + b]);
+        w[ed] = S(T(w[ed]) + Dacc[3 * a + b]);
+      }
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -642,9 +691,9 @@ template <class K> GB_HD K minv_at(const Ws<K>& zm, int nv, int r, int c) {
 // columns in K.  Minv rows of the joint: the diagonal block Dinv and the
 // columns of its subtree (-SDinv^T Fcrb); the columns right of the subtree are
 // first written by pass 3.
-template <int NVJ, class K, class SS>
+template <int NVJ, class K, class SS, class Team = Solo>
 GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
-                                  const Ws<K>& zm, int i) {
+                                  const Ws<K>& zm, int i, const Team& tm = Team()) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
   Sym6<SS> Ia;
@@ -659,7 +708,9 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
     SS Jc[6];
 #pragma unroll
     for (int r = 0; r < 6; ++r) Jc[r] = SS(Jk[k][r]);
-    zs[L.u + iv + k] -= SS(dot6(Jk[k], of));
+    const SS uk = zs[L.u + iv + k] - SS(dot6(Jk[k], of));
+    tm.sync();
+    zs[L.u + iv + k] = uk;
     sym6_mv(Ia, Jc, U[k]);
   }
   SS Dinv[NVJ * NVJ];
@@ -718,7 +769,7 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
         SD[k][r] = sum;
       }
 #pragma unroll 1
-    for (int c = iv + NVJ; c < iv + nst; ++c) {
+    for (int c = tm.first(iv + NVJ); c < iv + nst; c += Team::size) {
       K F[6];
       ld6(zk, L.F0 + 6 * c, F);
 #pragma unroll 1
@@ -732,7 +783,7 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
 #pragma unroll
       for (int r = 0; r < 6; ++r) Uk[k][r] = K(U[k][r]);
 #pragma unroll 1
-    for (int c = iv; c < iv + nst; ++c) {
+    for (int c = tm.first(iv); c < iv + nst; c += Team::size) {
       K F[6] = {K(0), K(0), K(0), K(0), K(0), K(0)};
       if (nch > 0) ld6(zk, L.F0 + 6 * c, F);
 #pragma unroll 1
@@ -767,17 +818,18 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
     ld6(zk, L.of + 6 * p, ofp);
 #pragma unroll
     for (int r = 0; r < 6; ++r) ofp[r] += of[r] + pa[r];
-    st6(zk, L.of + 6 * p, ofp);
     Sym6<SS> Ip;
     ld_sym6(zs, L.Ia + 21 * p, Ip);
     sym6_add(Ip, Ia);
+    tm.sync();
+    st6(zk, L.of + 6 * p, ofp);
     st_sym6(zs, L.Ia + 21 * p, Ip);
   }
 }
 
-template <class K, class SS>
+template <class K, class SS, class Team = Solo>
 GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
-                             const Ws<K>& zm, const In& q, const In& v, const In& tau) {
+                             const Ws<K>& zm, const In& q, const In& v, const In& tau, const Team& tm = Team()) {
   const int nv = m.nv;
   // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K
   world_forward<K>(m, L, zk, q, v, nullptr, false);
@@ -792,12 +844,14 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
     st_sym6(zs, L.Ia + 21 * i, I6);
   }
   for (int k = 0; k < nv; ++k) zs[L.u + k] = SS(tau[k]);
-  for (int k = 0; k < 6 * nv; ++k) zk[L.F0 + k] = K(0);
+  for (int c = tm.first(0); c < nv; c += Team::size)
+    for (int r = 0; r < 6; ++r) zk[L.F0 + 6 * c + r] = K(0);
   // ---- pass 2: ComputeABADerivativesBackwardStep1 (hxx:87-171)
 #pragma unroll 1
   for (int i = m.nj - 1; i > 0; --i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass2_joint<6, K, SS>(m, L, zk, zs, zm, i);
-    else aba_derivs_pass2_joint<1, K, SS>(m, L, zk, zs, zm, i);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass2_joint<6, K, SS>(m, L, zk, zs, zm, i, tm);
+    else aba_derivs_pass2_joint<1, K, SS>(m, L, zk, zs, zm, i, tm);
+    tm.sync();
   }
 }
 
@@ -805,10 +859,10 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
 // degrees of freedom.
 // MINV: the Minv recursion only (computeMinverse's ComputeMinverseForwardStep2,
 // aba.hxx:789-836): no velocity / acceleration recursion, no column sets.
-template <int NVJ, class S, class T, class K, bool MINV = false>
+template <int NVJ, class S, class T, class K, bool MINV = false, class Team = Solo>
 GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                                   const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out, const K* gk,
-                                  int i) {
+                                  int i, const Team& tm = Team()) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
   K ti[3];
@@ -873,7 +927,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     K udk[6];
     ld6(zk, L.UD + 6 * iv, udk);
 #pragma unroll 1
-    for (int c = iv; c < nv; ++c) {
+    for (int c = tm.first(iv); c < nv; c += Team::size) {
       K Fpc[6];
       ld6(zk, Fp + 6 * c, Fpc);
       const long e = upk(nv, iv, c);
@@ -885,7 +939,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     }
   } else {  // a root joint: its rows are final; zero right of its subtree (another root's)
 #pragma unroll 1
-    for (int c = iv; c < nv; ++c) {
+    for (int c = tm.first(iv); c < nv; c += Team::size) {
       K Fn[6] = {K(0), K(0), K(0), K(0), K(0), K(0)};
       if (c < iv + nst) {
 #pragma unroll 1
@@ -955,9 +1009,10 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     if (k >= 18 || k % 6 >= 3) w[L.doY + 36 * i + k] = S(dY[k]);  // the lin-lin block is zero
 }
 
-template <class S, class T, class K, bool MINV = false>
+template <class S, class T, class K, bool MINV = false, class Team = Solo>
 GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                            const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out) {
+                            const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out,
+                            const Team& tm = Team()) {
   // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
   // velocity / acceleration recursion runs in K in floating origins and
   // replaces ov / oa in K; the column sets, link inertia, momentum, force and
@@ -965,8 +1020,8 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
   const K* gk = ModelScalar<K>::grav(m);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
-    else aba_derivs_pass3_joint<1, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i, tm);
+    else aba_derivs_pass3_joint<1, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i, tm);
   }
 }
 
@@ -979,9 +1034,9 @@ constexpr int kRowBlockUnroll = GB_P4_UNROLL;
 // One joint of pass 4 with NVJ degrees of freedom (1: revolute, 6: the root
 // free-flyer, whose parent is the universe), so that every per-dof loop has a
 // compile-time bound and the per-dof arrays stay in registers.
-template <int NVJ, class S, class T, class K, class P>
+template <int NVJ, class S, class T, class K, class P, class Team = Solo>
 GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<K>& zk,
-                                  const Ws<P>& wp, int i, T eps) {
+                                  const Ws<P>& wp, int i, T eps, const Team& tm = Team()) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
   K ti[3];  // t_i, loaded once (the dtau stores would otherwise force reloads)
@@ -1025,7 +1080,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
     T Jr[6];
     ldc6(w, L.cJ + 6 * (iv + r), Jr);
 #pragma unroll (kRowBlockUnroll)
-    for (int c = iv; c < iv + nst; ++c) {
+    for (int c = tm.first(iv); c < iv + nst; c += Team::size) {
       T d[3], u[6], x[6];
       offset_from(m.dof_joint[c], d);
       cross3(Jr + 3, d, u);
@@ -1049,6 +1104,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
       fcross(Jc, of, t);
 #pragma unroll
       for (int r = 0; r < 6; ++r) x[r] += t[r];
+      tm.sync();  // the row block's readers of dFdq (column owners) are done
       st6(w, L.dFdq + 6 * c, x);
     }
   }
@@ -1065,8 +1121,10 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
     }
     // f . (m_lin - d x m_ang, m_ang) = (f_lin, f_ang - f_lin x d) . m for the
     // motion m of ancestor j moved from t_j to t_i (d = t_i - t_j)
+    int idx = 0;
 #pragma unroll 1
-    for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j]) {
+    for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j], ++idx) {
+      if (!tm.owns(idx)) continue;
       T d[3], fs[6], Ss[6], x[6], y[6];
       offset_from(m.dof_joint[j], d);  // t_j - t_i
 #pragma unroll
@@ -1100,9 +1158,10 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
 #pragma unroll
     for (int k = 0; k < 3; ++k) oYs.c[k] += rr[k];
     iner_add(oYp, oYs, eps);
+    tm.sync();
     stc_iner(w, L.coY + 10 * p, oYp);
   }
-  op0_shift_add(w, L.doY + 36 * i, L.doY + 36 * p, rr);
+  op0_shift_add(w, L.doY + 36 * i, L.doY + 36 * p, rr, tm);
   {
     T of[6], ofs[6], ofp[6];
     ldc6(w, L.cof + 6 * i, of);
@@ -1110,6 +1169,7 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
     ldc6(w, L.cof + 6 * p, ofp);
 #pragma unroll
     for (int r = 0; r < 6; ++r) ofp[r] += ofs[r];
+    tm.sync();
     st6(w, L.cof + 6 * p, ofp);
   }
 }
@@ -1119,14 +1179,15 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
 // child adds its contributions moved to the parent's position.  Only the
 // structurally non-zero entries of dtau_dq / dtau_dv (row k of column c for k
 // an ancestor of c or in its subtree) are written: the products read no other.
-template <class S, class T, class K, class P>
+template <class S, class T, class K, class P, class Team = Solo>
 GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<K>& zk,
-                            const Ws<P>& wp) {
+                            const Ws<P>& wp, const Team& tm = Team()) {
   const T eps = eps_of<T>();
 #pragma unroll 1
   for (int i = m.nj - 1; i > 0; --i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass4_joint<6, S, T, K, P>(m, L, w, zk, wp, i, eps);
-    else aba_derivs_pass4_joint<1, S, T, K, P>(m, L, w, zk, wp, i, eps);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass4_joint<6, S, T, K, P>(m, L, w, zk, wp, i, eps, tm);
+    else aba_derivs_pass4_joint<1, S, T, K, P>(m, L, w, zk, wp, i, eps, tm);
+    tm.sync();
   }
 }
 

@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(const unsigned char* blo
 template <class K>
 int launch_common(const gb_model* M, long B, cudaStream_t st, K kernel, const char* name) {
   static_assert(sizeof(K) > 0, "");
-  const int bytes = M->blob_bytes;
+  const int bytes = M->stage_bytes;
   if (bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return cuda_error(e, name);
@@ -89,7 +89,7 @@ int launch_common(const gb_model* M, long B, cudaStream_t st, K kernel, const ch
     if (rc__ != GB_OK) return rc__;                                                         \
     const int tpb__ = M->tpb[GB_FUNC_ID];                                                   \
     const long grid__ = (B + tpb__ - 1) / tpb__;                                            \
-    kernel<<<(unsigned)grid__, tpb__, M->blob_bytes, st>>>(M->d_blob, M->blob_bytes, B, __VA_ARGS__); \
+    kernel<<<(unsigned)grid__, tpb__, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, __VA_ARGS__); \
     return cuda_error(cudaGetLastError(), #kernel);                                         \
   } while (0)
 

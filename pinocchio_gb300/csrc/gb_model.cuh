@@ -28,8 +28,9 @@ struct BlobHeader {
   int o_place_d, o_iner_d, o_arm_d, o_place_f, o_iner_f, o_arm_f, o_rel_off, o_rel_list;
   int o_slot, o_dofj, o_bslot, nbranch;
   int o_grp, ngroup, o_grp_rel, n_grp_rel;
+  int stage_bytes;  // [0, stage_bytes): what the per-instance kernels stage (rel_list and the groups lie beyond)
   int o_i6_d, o_i6_f, o_place_df, o_iner_df;
-  int o_arm_df, o_zero, pad7, pad8;  // o_zero: 16 zero bytes (a zero vector with stride 0)
+  int o_arm_df, o_zero, pad8;  // o_zero: 16 zero bytes (a zero vector with stride 0)
   double grav_d[6];
   float grav_f[6];
   float padf[2];

@@ -23,6 +23,7 @@ struct gb_model {
   std::vector<unsigned char> blob;  // host copy of the device blob
   unsigned char* d_blob = nullptr;  // device copy (owned by the C ABI)
   int blob_bytes = 0;
+  int stage_bytes = 0;  // prefix of the blob the per-instance kernels copy into shared memory
 };
 
 namespace gbm {
@@ -134,7 +135,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   auto take = [&](size_t bytes) { const size_t o = off; off = align16(off + bytes); return (int)o; };
   h.o_parent = take(4 * nj); h.o_jtype = take(4 * nj); h.o_idxq = take(4 * nj); h.o_idxv = take(4 * nj);
   h.o_nvsub = take(4 * nj); h.o_depth = take(4 * nj); h.o_pfr = take(4 * nv); h.o_nsfr = take(4 * nv);
-  h.o_rel_off = take(4 * (nv + 1)); h.o_rel_list = take(4 * M->rel_list.size() + 4); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv); h.o_bslot = take(4 * nj);
+  h.o_rel_off = take(4 * (nv + 1)); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv); h.o_bslot = take(4 * nj);
   // column groups of the -Minv*dtau products (filled below)
   std::vector<int> grp, grp_rel;
   for (int c = 0; c < nv;) {
@@ -148,12 +149,17 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
     c = e;
   }
   h.ngroup = (int)grp.size() / 4; h.n_grp_rel = (int)grp_rel.size();
-  h.o_grp = take(4 * grp.size()); h.o_grp_rel = take(4 * grp_rel.size() + 4);
   h.o_place_d = take(8 * 12 * nj); h.o_iner_d = take(8 * 10 * nj); h.o_arm_d = take(8 * nv);
   h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
   h.o_i6_d = take(8 * 21 * nj); h.o_i6_f = take(4 * 21 * nj);
   h.o_place_df = take(8 * 12 * nj); h.o_iner_df = take(8 * 10 * nj); h.o_arm_df = take(8 * nv);
   h.o_zero = take(16);
+  // the per-instance kernels stage [0, stage_bytes) in shared memory; the row
+  // lists below (O(nv^2) for deep trees) are read from global memory by the
+  // product and VJP kernels only
+  h.stage_bytes = (int)off;
+  h.o_rel_list = take(4 * M->rel_list.size() + 4);
+  h.o_grp = take(4 * grp.size()); h.o_grp_rel = take(4 * grp_rel.size() + 4);
   h.bytes = (int)off;
   for (int k = 0; k < 6; ++k) {
     h.grav_d[k] = M->gravity[k];
@@ -208,6 +214,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   };
   put_df(h.o_place_df, M->placement); put_df(h.o_iner_df, M->inertia); put_df(h.o_arm_df, M->armature);
   M->blob_bytes = (int)off;
+  M->stage_bytes = h.stage_bytes;
   return GB_OK;
 }
 

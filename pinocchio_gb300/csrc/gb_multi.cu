@@ -118,7 +118,7 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
     if (t.batch == 0) continue;
     DevTask& d = tab.t[tab.ntasks++];
     d.blob = t.model->d_blob;
-    d.blob_bytes = t.model->blob_bytes;
+    d.blob_bytes = t.model->stage_bytes;
     d.function = t.function;
     d.batch = t.batch;
     d.tile_begin = tab.ntiles;
@@ -126,7 +126,7 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
     d.nq = t.model->nq; d.nv = t.model->nv;
     tab.ntiles += (t.batch + tile - 1) / tile;
     cap = std::max(cap, t.model->cap);
-    max_blob = std::max(max_blob, t.model->blob_bytes);
+    max_blob = std::max(max_blob, t.model->stage_bytes);
   }
   if (tab.ntasks == 0) return GB_OK;
   cudaStream_t st = (cudaStream_t)stream;

@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_aba_warp(const unsigned char* 
 template <class Kern>
 int warp_launch_shape(const gb_model* M, size_t per_warp, Kern kernel, const char* name, int* nw, size_t* smem) {
   const size_t limit = 200 * 1024;
-  const size_t blob = align16((size_t)M->blob_bytes);
+  const size_t blob = align16((size_t)M->stage_bytes);
   if (blob + per_warp > limit) return set_error(GB_ERR_UNSUPPORTED, std::string(name) + ": model too large for the warp layout");
   *nw = (int)std::min<size_t>(kWarpThreads / 32, (limit - blob) / per_warp);
   *smem = blob + (size_t)(*nw) * per_warp;
@@ -356,7 +356,7 @@ int launch_rnea_warp_t(const gb_model* M, long B, Arr q, Arr v, Arr a, Arr tau, 
   int rc = warp_launch_shape(M, per_warp, k_rnea_warp<S>, "k_rnea_warp", &nw, &smem);
   if (rc != GB_OK) return rc;
   const long grid = std::min<long>((B + nw - 1) / nw, 152L * 16);
-  k_rnea_warp<S><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->blob_bytes, B, q, v, a, tau);
+  k_rnea_warp<S><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, a, tau);
   return cuda_error(cudaGetLastError(), "k_rnea_warp");
 }
 
@@ -369,7 +369,7 @@ int launch_aba_warp_t(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq,
   int rc = warp_launch_shape(M, per_warp, k_aba_warp<S, SS>, "k_aba_warp", &nw, &smem);
   if (rc != GB_OK) return rc;
   const long grid = std::min<long>((B + nw - 1) / nw, 152L * 16);
-  k_aba_warp<S, SS><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->blob_bytes, B, q, v, tau, ddq);
+  k_aba_warp<S, SS><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, tau, ddq);
   return cuda_error(cudaGetLastError(), "k_aba_warp");
 }
 

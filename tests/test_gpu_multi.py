@@ -119,3 +119,66 @@ def test_layout_setting_errors():
     L = pg._capi.lib()
     assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_CRBA, pg._capi.GB_INSTANCE_PER_WARP) == pg._capi.GB_ERR_UNSUPPORTED
     assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_RNEA, 5) == pg._capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_ABA, pg._capi.GB_INSTANCE_PER_8_LANES) == pg._capi.GB_ERR_UNSUPPORTED
+    assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_ABA_DERIVATIVES, pg._capi.GB_INSTANCE_PER_4_LANES) == pg._capi.GB_OK
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100"])
+def test_team_layouts_aba_derivatives(name, precision):
+    """The ABA derivatives with a team of 4, 8 or 32 lanes per configuration
+    (the lanes split the column loops of the sweeps) give the thread layout's
+    ddq_dq, ddq_dv, Minv, ddq, VJP and computeMinverse: the same bits in FP64,
+    FP32 rounding in the mixed kernels."""
+    import torch
+
+    from util import MODELS
+
+    model = MODELS[name]()
+    q, v, x = sm.random_inputs(model, 77, 4)
+    tau = 10.0 * x
+    g = np.random.default_rng(2).standard_normal((77, model.nv))
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    data = pg.createData(model, precision)
+    L = pg._capi.lib()
+    outs = {}
+    layouts = (pg._capi.GB_INSTANCE_PER_THREAD, pg._capi.GB_INSTANCE_PER_4_LANES, pg._capi.GB_INSTANCE_PER_8_LANES,
+               pg._capi.GB_INSTANCE_PER_WARP)
+    for layout in layouts:
+        pg._capi.check(L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_ABA_DERIVATIVES, layout))
+        res = [t.cpu().numpy() for t in pg.computeABADerivatives(model, data, d(q), d(v), d(tau))]
+        res.append(data.ddq.cpu().numpy())
+        res += [t.cpu().numpy() for t in pg.abaDerivativesVJP(model, data, d(q), d(v), d(tau), d(g))]
+        res.append(pg.computeMinverse(model, data, d(q)).cpu().numpy())
+        outs[layout] = res
+    for layout in layouts[1:]:
+        for k, (a, b) in enumerate(zip(outs[layouts[0]], outs[layout])):
+            if precision == "fp64":
+                assert np.array_equal(a, b), (layout, k)
+            else:
+                assert rel_err(b, a) < 1e-6, (layout, k, rel_err(b, a))
+    if precision == "fp64" or name != "chain100":
+        ddq_o, dq_o, dv_o, Minv_o = OracleModel(model).aba_derivatives(q, v, tau)
+        tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else MIXED_TOL
+        w = outs[pg._capi.GB_INSTANCE_PER_WARP]
+        assert rel_err(w[0], dq_o) < tol and rel_err(w[1], dv_o) < tol and rel_err(w[2], Minv_o) < tol
+        assert rel_err(w[3], ddq_o) < tol
+
+
+def test_autotuner_chooses_a_derivative_layout(tmp_path, monkeypatch):
+    """tune() also times the lane-team layouts of the ABA derivatives; whatever it
+    picks, the FP64 results keep their bits."""
+    import torch
+
+    from util import MODELS
+
+    monkeypatch.setattr(autotune, "CACHE_PATH", str(tmp_path / "tune.json"))
+    model = MODELS["chain100"]()
+    data = pg.createData(model)
+    q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 256, 3))
+    before = [t.clone() for t in pg.computeABADerivatives(model, data, q, v, x)]
+    res = autotune.tune(model, data, functions=("aba_derivatives",), batch=256, use_cache=False)
+    setting = res["aba_derivatives"][0]
+    assert setting in autotune.CANDIDATES or setting in (autotune.LANES4, autotune.LANES8, autotune.WARP)
+    for a, b in zip(before, pg.computeABADerivatives(model, data, q, v, x)):
+        assert torch.equal(a, b)
