@@ -33,26 +33,33 @@ template <class T> struct Ws {
 // LaneTeam<TS>: TS consecutive lanes of a warp; every lane runs the per-joint
 // work (same values), the loops over matrix columns are split by column (rank
 // c % TS owns column c in every pass, so a column's workspace entries are
-// written and read by one lane), and sync() orders the team's workspace
+// written and read by one lane; a walk up the ancestors gives every lane every
+// TS-th one), and sync() orders the team's workspace
 // accesses where one lane's store could otherwise overtake another lane's load
 // of the same entry (before the stores of a read-modify-write, at the end of
 // every joint).
 struct Solo {
   static constexpr int size = 1;
+  GB_HD int rank() const { return 0; }
   GB_HD int first(int c0) const { return c0; }  // the first column >= c0 this member owns
-  GB_HD bool owns(int idx) const { return true; }
+  GB_HD int advance(const int* next, int j) const { return next[j]; }  // size steps along a chain
   GB_HD void sync() const {}
 };
 #if defined(__CUDACC__)
 template <int TS> struct LaneTeam {
   static_assert(TS > 1 && TS <= 32 && (TS & (TS - 1)) == 0, "a team is a power-of-two group of lanes");
   static constexpr int size = TS;
-  int rank;
+  int r;
   unsigned mask;  // the team's lanes
   __device__ explicit LaneTeam(int lane)
-      : rank(lane & (TS - 1)), mask(TS == 32 ? 0xffffffffu : ((1u << TS) - 1u) << (lane & ~(TS - 1))) {}
-  __device__ int first(int c0) const { return c0 + ((rank - c0) & (TS - 1)); }
-  __device__ bool owns(int idx) const { return (idx & (TS - 1)) == rank; }
+      : r(lane & (TS - 1)), mask(TS == 32 ? 0xffffffffu : ((1u << TS) - 1u) << (lane & ~(TS - 1))) {}
+  __device__ int rank() const { return r; }
+  __device__ int first(int c0) const { return c0 + ((r - c0) & (TS - 1)); }
+  __device__ int advance(const int* next, int j) const {
+#pragma unroll 1
+    for (int s = 0; s < TS && j >= 0; ++s) j = next[j];
+    return j;
+  }
   __device__ void sync() const { __syncwarp(mask); }
 };
 #endif
@@ -690,72 +697,77 @@ template <class K> GB_HD K minv_at(const Ws<K>& zm, int nv, int r, int c) {
 // NVJ degrees of freedom: the Schur complement in SS, the Minv rows and Fcrb
 // columns in K.  Minv rows of the joint: the diagonal block Dinv and the
 // columns of its subtree (-SDinv^T Fcrb); the columns right of the subtree are
-// first written by pass 3.
+// first written by pass 3.  In a lane team every lane runs the per-joint work
+// (one lane and shuffles measured slower: the work is latency-bound, not
+// FP64-throughput-bound) and the column loops are split over the team.
 template <int NVJ, class K, class SS, class Team = Solo>
 GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
                                   const Ws<K>& zm, int i, const Team& tm = Team()) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
-  Sym6<SS> Ia;
-  ld_sym6(zs, L.Ia + 21 * i, Ia);
-  K of[6];
-  ld6(zk, L.of + 6 * i, of);
   K Jk[NVJ][6];
-  SS U[NVJ][6];  // per joint dof k: U column
 #pragma unroll 1
-  for (int k = 0; k < NVJ; ++k) {
-    ld6(zk, L.J + 6 * (iv + k), Jk[k]);
-    SS Jc[6];
-#pragma unroll
-    for (int r = 0; r < 6; ++r) Jc[r] = SS(Jk[k][r]);
-    const SS uk = zs[L.u + iv + k] - SS(dot6(Jk[k], of));
-    tm.sync();
-    zs[L.u + iv + k] = uk;
-    sym6_mv(Ia, Jc, U[k]);
-  }
+  for (int k = 0; k < NVJ; ++k) ld6(zk, L.J + 6 * (iv + k), Jk[k]);
+  Sym6<SS> Ia;
+  SS U[NVJ][6];  // per joint dof k: U column
   SS Dinv[NVJ * NVJ];
+  SS UD[NVJ][6];  // UDinv columns
+  K UDk[NVJ][6];
   {
-    SS StU[NVJ * NVJ];
+    ld_sym6(zs, L.Ia + 21 * i, Ia);
+    K of[6];
+    ld6(zk, L.of + 6 * i, of);
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
+      SS Jc[6];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) Jc[r] = SS(Jk[k][r]);
+      const SS uk = zs[L.u + iv + k] - SS(dot6(Jk[k], of));
+      tm.sync();  // every lane has read u before any lane writes it
+      zs[L.u + iv + k] = uk;
+      sym6_mv(Ia, Jc, U[k]);
+    }
+    {
+      SS StU[NVJ * NVJ];
+#pragma unroll 1
+      for (int r = 0; r < NVJ; ++r)
+#pragma unroll 1
+        for (int c = 0; c < NVJ; ++c) {
+          SS d = SS(Jk[r][0]) * U[c][0];
+#pragma unroll
+          for (int e = 1; e < 6; ++e) d += SS(Jk[r][e]) * U[c][e];
+          StU[r * NVJ + c] = d;
+        }
+#pragma unroll 1
+      for (int k = 0; k < NVJ; ++k) StU[k * NVJ + k] += SS(m.arm_d[iv + k]);
+      if constexpr (NVJ == 6) llt_inverse<SS, 6>(StU, Dinv);
+      else Dinv[0] = SS(1) / StU[0];
+    }
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k)
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        SS sum = U[0][r] * Dinv[k];
+#pragma unroll 1
+        for (int j = 1; j < NVJ; ++j) sum += U[j][r] * Dinv[j * NVJ + k];
+        UD[k][r] = sum;
+      }
+    // U Dinv and Dinv u (u is final here: every child has been folded in) for pass 3, in K
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
+#pragma unroll
+      for (int r = 0; r < 6; ++r) UDk[k][r] = K(UD[k][r]);
+      st6(zk, L.UD + 6 * (iv + k), UDk[k]);
+      SS du = SS(0);
+#pragma unroll 1
+      for (int c = 0; c < NVJ; ++c) du += Dinv[k * NVJ + c] * zs[L.u + iv + c];
+      zk[L.Du + iv + k] = K(du);
+    }
 #pragma unroll 1
     for (int r = 0; r < NVJ; ++r)
 #pragma unroll 1
-      for (int c = 0; c < NVJ; ++c) {
-        SS d = SS(Jk[r][0]) * U[c][0];
-#pragma unroll
-        for (int e = 1; e < 6; ++e) d += SS(Jk[r][e]) * U[c][e];
-        StU[r * NVJ + c] = d;
-      }
-#pragma unroll 1
-    for (int k = 0; k < NVJ; ++k) StU[k * NVJ + k] += SS(m.arm_d[iv + k]);
-    if constexpr (NVJ == 6) llt_inverse<SS, 6>(StU, Dinv);
-    else Dinv[0] = SS(1) / StU[0];
+      for (int c = r; c < NVJ; ++c) zm[upk(nv, iv + r, iv + c)] = K(Dinv[r * NVJ + c]);
   }
-  SS UD[NVJ][6];  // UDinv columns
-#pragma unroll 1
-  for (int k = 0; k < NVJ; ++k)
-#pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      SS sum = U[0][r] * Dinv[k];
-#pragma unroll 1
-      for (int j = 1; j < NVJ; ++j) sum += U[j][r] * Dinv[j * NVJ + k];
-      UD[k][r] = sum;
-    }
-  // U Dinv and Dinv u (u is final here: every child has been folded in) for pass 3, in K
-  K UDk[NVJ][6];
-#pragma unroll 1
-  for (int k = 0; k < NVJ; ++k) {
-#pragma unroll
-    for (int r = 0; r < 6; ++r) UDk[k][r] = K(UD[k][r]);
-    st6(zk, L.UD + 6 * (iv + k), UDk[k]);
-    SS du = SS(0);
-#pragma unroll 1
-    for (int c = 0; c < NVJ; ++c) du += Dinv[k * NVJ + c] * zs[L.u + iv + c];
-    zk[L.Du + iv + k] = K(du);
-  }
-#pragma unroll 1
-  for (int r = 0; r < NVJ; ++r)
-#pragma unroll 1
-    for (int c = r; c < NVJ; ++c) zm[upk(nv, iv + r, iv + c)] = K(Dinv[r * NVJ + c]);
   const int nch = nst - NVJ;
   if (nch > 0) {
     K SD[NVJ][6];  // SDinv columns = J Dinv
@@ -814,14 +826,15 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
 #pragma unroll
       for (int r = 0; r < 6; ++r) pa[r] += UDk[k][r] * uk;
     }
-    K ofp[6];
+    K of[6], ofp[6];
+    ld6(zk, L.of + 6 * i, of);
     ld6(zk, L.of + 6 * p, ofp);
 #pragma unroll
     for (int r = 0; r < 6; ++r) ofp[r] += of[r] + pa[r];
     Sym6<SS> Ip;
     ld_sym6(zs, L.Ia + 21 * p, Ip);
     sym6_add(Ip, Ia);
-    tm.sync();
+    tm.sync();  // every lane has read the parent's entries before any lane writes them
     st6(zk, L.of + 6 * p, ofp);
     st_sym6(zs, L.Ia + 21 * p, Ip);
   }
@@ -1121,10 +1134,13 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
     }
     // f . (m_lin - d x m_ang, m_ang) = (f_lin, f_ang - f_lin x d) . m for the
     // motion m of ancestor j moved from t_j to t_i (d = t_i - t_j)
-    int idx = 0;
+    // a team's lanes take every size-th ancestor in rounds (the body runs once per
+    // round for the whole team)
+    int j = m.pfr[iv];
 #pragma unroll 1
-    for (int j = m.pfr[iv]; j >= 0; j = m.pfr[j], ++idx) {
-      if (!tm.owns(idx)) continue;
+    for (int s = 0; s < tm.rank() && j >= 0; ++s) j = m.pfr[j];
+#pragma unroll 1
+    for (; j >= 0; j = tm.advance(m.pfr, j)) {
       T d[3], fs[6], Ss[6], x[6], y[6];
       offset_from(m.dof_joint[j], d);  // t_j - t_i
 #pragma unroll
