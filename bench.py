@@ -247,17 +247,20 @@ def measure_functions(torch, pg, sm):
 
 def measure_heterogeneous(torch, pg, sm, total=100000):
     """RNEA + ABA over the four seeded trees (nv 7 / 12 / 32 FF / 60 FF, instances 40/30/20/10 %)
-    in one persistent launch captured in a CUDA graph; threads per block from the autotuner."""
+    in one persistent launch captured in a CUDA graph; the autotuner picks the layout per tree (on
+    the tree's own batch) and then the launch's threads per block."""
     from pinocchio_gb300 import api, autotune
 
     models = sm.heterogeneous_trees(3)
     out = {"instances": total, "trees_nv": [m.nv for m in models], "split": [0.4, 0.3, 0.2, 0.1]}
     for prec in ("fp64", "mixed"):
-        tasks = []
+        tasks, layouts = [], []
         for k, (model, share) in enumerate(zip(models, (0.4, 0.3, 0.2, 0.1))):
             B = int(total * share)
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 20 + k))
             data = pg.createData(model, prec)
+            tuned = autotune.tune(model, data, functions=("rnea", "aba"), batch=B, use_cache=False)
+            layouts.append({f: ("warp" if t == autotune.WARP else "thread") for f, (t, _) in tuned.items()})
             tasks.append((data, "aba", q, v, 10.0 * x))
             tasks.append((data, "rnea", q, v, x))
         tpb, _ = autotune.tune_multi(tasks, prec)
@@ -266,7 +269,7 @@ def measure_heterogeneous(torch, pg, sm, total=100000):
         ms = _time_call(torch, mb.replay, reps=20, warmup=3)
         evals = 2 * sum(int(total * s) for s in (0.4, 0.3, 0.2, 0.1))
         out[prec] = {"ms_per_launch": ms, "evals_per_s": evals / ms * 1e3, "threads_per_block": tpb,
-                     "evals_per_launch": evals}
+                     "evals_per_launch": evals, "layouts": layouts}
     return out
 
 

@@ -46,6 +46,33 @@ def test_multi_matches_oracle_and_single_model_calls(precision, tol):
         assert np.array_equal(single.cpu().numpy(), outs[2 * k])  # same per-instance code
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_multi_per_tree_layouts(precision, tol):
+    """Tasks of the same launch in different layouts (the autotuner's choice per
+    tree, gb_model_set_layout): warp-layout trees give their single-model calls'
+    results (same bits in FP64) and the oracle's."""
+    import torch
+
+    tasks, ref = _tasks(precision, 1200, 5)
+    L = pg._capi.lib()
+    for k in (0, 2):  # nv 7 and 32 (free-flyer) trees: one warp per configuration
+        for f in (pg._capi.GB_FUNC_RNEA, pg._capi.GB_FUNC_ABA):
+            pg._capi.check(L.gb_model_set_layout(tasks[2 * k][0].dev.h, f, pg._capi.GB_INSTANCE_PER_WARP))
+    outs = [o.cpu().numpy() for o in api.MultiBatch(tasks, precision).run()]
+    d = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    for k, (model, q, v, x) in enumerate(ref):
+        om = OracleModel(model)
+        assert rel_err(outs[2 * k], om.aba(q, v, 10.0 * x, LOCAL)) < tol
+        assert rel_err(outs[2 * k + 1], om.rnea(q, v, x)) < tol
+        data = tasks[2 * k][0]
+        single = [pg.aba(model, data, d(q), d(v), d(10.0 * x)).cpu().numpy(), pg.rnea(model, data, d(q), d(v), d(x)).cpu().numpy()]
+        for a, b in zip(single, outs[2 * k : 2 * k + 2]):
+            if precision == "fp64":
+                assert np.array_equal(a, b)
+            else:
+                assert rel_err(b, a) < 1e-6
+
+
 def test_multi_graph_replay():
     tasks, ref = _tasks("mixed", 2000, 7)
     mb = api.MultiBatch(tasks, "mixed", 64)
