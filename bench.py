@@ -216,8 +216,9 @@ def _time_call(torch, fn, reps=5, warmup=2):
 
 def measure_functions(torch, pg, sm):
     """evals/s of every batched function on the humanoid, per precision: RNEA / ABA /
-    CRBA (+ tree Cholesky) / computeMinverse / nonLinearEffects / generalized gravity at
-    batch 65536, the two derivative algorithms at batch 16384."""
+    CRBA (+ tree Cholesky) / computeMinverse / nonLinearEffects / generalized gravity /
+    forwardKinematics (q, v, a) / computeJointJacobians at batch 65536, the two derivative
+    algorithms at batch 16384."""
     model = sm.humanoid32(1)
     out = {}
     for prec in ("fp64", "mixed"):
@@ -225,7 +226,8 @@ def measure_functions(torch, pg, sm):
         res = {}
         for fname, B in (("rnea", 65536), ("aba", 65536), ("crba", 65536), ("crba_cholesky", 65536),
                          ("rnea_derivatives", 16384), ("aba_derivatives", 16384), ("compute_minverse", 65536),
-                         ("nonlinear_effects", 65536), ("generalized_gravity", 65536)):
+                         ("nonlinear_effects", 65536), ("generalized_gravity", 65536),
+                         ("forward_kinematics", 65536), ("joint_jacobians", 65536)):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
             fn = {
                 "rnea": lambda: pg.rnea(model, data, q, v, x),
@@ -237,6 +239,8 @@ def measure_functions(torch, pg, sm):
                 "compute_minverse": lambda: pg.computeMinverse(model, data, q),
                 "nonlinear_effects": lambda: pg.nonLinearEffects(model, data, q, v),
                 "generalized_gravity": lambda: pg.computeGeneralizedGravity(model, data, q),
+                "forward_kinematics": lambda: pg.forwardKinematics(model, data, q, v, x),
+                "joint_jacobians": lambda: pg.computeJointJacobians(model, data, q),
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}

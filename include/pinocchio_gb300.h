@@ -164,6 +164,22 @@ int gb_aba_derivatives_noalloc(const gb_model* model, int precision, int layout,
                                const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                                double* ddq, void* stream);
 
+/* forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272):
+ * per instance, for every joint i = 0 .. njoints-1 (joint 0 the universe:
+ * identity, zero), oMi[12 i ..] = the world placement (rotation row-major, then
+ * translation); with v, vout[6 i ..] = data.v[i], the joint-frame spatial
+ * velocity [linear; angular]; with v and a, aout[6 i ..] = data.a[i], the
+ * joint-frame spatial acceleration (no gravity).  v, a, vout, aout may be NULL
+ * (an output needs its input). */
+int gb_forward_kinematics(const gb_model* model, int precision, int layout, long batch, const double* q,
+                          const double* v, const double* a, double* oMi, double* vout, double* aout, void* stream);
+
+/* J = computeJointJacobians(model, data, q) (reference algorithm/jacobian.hxx:17-95):
+ * data.J, 6 x nv column-major per instance (column k = [linear; angular] of
+ * the motion subspace of dof k, in the world frame about the world origin). */
+int gb_compute_joint_jacobians(const gb_model* model, int precision, int layout, long batch, const double* q,
+                               double* J, void* stream);
+
 /* qout = integrate(model, q, v) (reference algorithm/joint-configuration.hpp:41-80;
  * free-flyer: multibody/liegroup/special-euclidean.hpp:660-699), always FP64. */
 int gb_integrate(const gb_model* model, int layout, long batch, const double* q, const double* v, double* qout,

@@ -1229,6 +1229,45 @@ void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T
 }
 
 // ---------------------------------------------------------------------------
+// forwardKinematics (algorithm/kinematics.hxx: ForwardKinematicZeroStep
+// 42-77 with q, FirstStep 105-178 with q and v, SecondStep 188-272 with q, v
+// and a): liMi, oMi, and the joint-frame spatial velocities / accelerations
+// (no gravity: data.a[0] = 0).
+// ---------------------------------------------------------------------------
+template <class T>
+void forward_kinematics(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
+  d.v[0] = zero6<T>();
+  d.a[0] = zero6<T>();
+  for (int i = 1; i < m.njoints; ++i) {
+    const int p = m.parents[i], jt = m.jtype[i], iq = m.idx_q[i], iv = m.idx_v[i];
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(jt, q + iq));
+    d.oMi[i] = p > 0 ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
+    if (!v) continue;
+    const Vec6<T> vJ = joint_velocity<T>(jt, v + iv);
+    d.v[i] = vJ;
+    if (p > 0) d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
+    if (!a) continue;
+    // S a + c + v_i x vJ (c = 0 for these joints), then + liMi.actInv(a_parent)
+    d.a[i] = add6(joint_velocity<T>(jt, a + iv), cross_motion(d.v[i], vJ));
+    d.a[i] = add6(d.a[i], actinv_motion(d.liMi[i], d.a[p]));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// computeJointJacobians (algorithm/jacobian.hxx:17-95): oMi and
+// J = [oMi.act(S_i)] columns, 6 x nv column-major, about the world origin.
+// ---------------------------------------------------------------------------
+template <class T>
+void joint_jacobians(const Model& m, Data<T>& d, const T* q) {
+  for (int i = 1; i < m.njoints; ++i) {
+    const int p = m.parents[i], jt = m.jtype[i], iq = m.idx_q[i], iv = m.idx_v[i];
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(jt, q + iq));
+    d.oMi[i] = p > 0 ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
+    for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(jt, k)));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // integrate(q, v) for the supported joints: free-flyer through the SE(3)
 // exponential (multibody/liegroup/special-euclidean.hpp:660-699,
 // spatial/explog-quaternion.hpp:20-147, math/quaternion.hpp:90-111); revolute

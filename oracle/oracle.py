@@ -52,6 +52,8 @@ def lib():
         L.orc_rnea_derivatives.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_aba_derivatives.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
+        L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_joint_jacobians.argtypes = [vp, C.c_int, C.c_long, vp, vp, C.c_int]
         L.orc_count_flops.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
     return _lib
@@ -82,6 +84,7 @@ class OracleModel:
         nq, nv = C.c_int(), C.c_int()
         L.orc_model_dims(self.h, C.byref(nq), C.byref(nv))
         self.nq, self.nv = nq.value, nv.value
+        self.njoints = int(len(t["parents"]))
         self.model = model
 
     def __del__(self):
@@ -143,6 +146,27 @@ class OracleModel:
         out = np.empty_like(q)
         self._check(lib().orc_integrate(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(out), nthreads))
         return out
+
+    def forward_kinematics(self, q, v=None, a=None, prec=0, nthreads=0):
+        """(oMi (B, njoints, 12): R row-major then t; v (B, njoints, 6) or None; a (B, njoints, 6) or None),
+        joint 0 the identity / zero -- data.oMi, data.v, data.a after forwardKinematics(q[, v[, a]])."""
+        q = _c(q)
+        B, nj = q.shape[0], self.njoints
+        v = None if v is None else _c(v)
+        a = None if (a is None or v is None) else _c(a)
+        oMi = np.empty((B, nj, 12))
+        vi = np.empty((B, nj, 6)) if v is not None else None
+        ai = np.empty((B, nj, 6)) if a is not None else None
+        self._check(lib().orc_forward_kinematics(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(oMi), _ptr(vi),
+                                                 _ptr(ai), nthreads))
+        return oMi, vi, ai
+
+    def joint_jacobians(self, q, prec=0, nthreads=0):
+        """data.J after computeJointJacobians(q): (B, nv, 6), column k of the 6 x nv matrix per row."""
+        q = _c(q)
+        J = np.empty((q.shape[0], self.nv, 6))
+        self._check(lib().orc_joint_jacobians(self.h, prec, q.shape[0], _ptr(q), _ptr(J), nthreads))
+        return J
 
     def count_flops(self, func, q, v=None, x=None):
         """(ops, sincos pairs) of one evaluation at a single instance."""

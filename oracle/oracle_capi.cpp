@@ -41,7 +41,19 @@ template <class T> inline void store(const std::vector<T>& src, double* dst, siz
   for (size_t k = 0; k < n; ++k) dst[k] = (double)src[k];
 }
 
-enum Func { F_RNEA = 0, F_ABA_LOCAL, F_ABA_WORLD, F_CRBA_LOCAL, F_CRBA_WORLD, F_CHOL, F_RNEA_D, F_ABA_D, F_INTEGRATE };
+enum Func { F_RNEA = 0, F_ABA_LOCAL, F_ABA_WORLD, F_CRBA_LOCAL, F_CRBA_WORLD, F_CHOL, F_RNEA_D, F_ABA_D, F_INTEGRATE,
+            F_FK, F_JAC };
+
+template <class T> void store_placements(const orc::Data<T>& d, int nj, double* o) {  // joint 0: identity
+  for (int i = 0; i < nj; ++i)
+    for (int k = 0; k < 12; ++k)
+      o[12 * i + k] = i == 0 ? ((k == 0 || k == 4 || k == 8) ? 1.0 : 0.0)
+                             : (double)(k < 9 ? d.oMi[i].R[k] : d.oMi[i].t[k - 9]);
+}
+template <class T> void store_motions(const std::vector<orc::Vec6<T>>& x, int nj, double* o) {
+  for (int i = 0; i < nj; ++i)
+    for (int k = 0; k < 6; ++k) o[6 * i + k] = (double)x[i].v[k];
+}
 
 template <class T>
 void run_one(const Model& m, orc::Data<T>& d, int func, const double* q, const double* v, const double* x,
@@ -98,6 +110,16 @@ void run_one(const Model& m, orc::Data<T>& d, int func, const double* q, const d
       if (o3) store(d.ddq_dv, o3, nn);
       if (o4) store(d.Minv, o4, nn);
       break;
+    case F_FK:
+      orc::forward_kinematics(m, d, bq.x.data(), v ? bv.x.data() : nullptr, (v && x) ? bx.x.data() : nullptr);
+      store_placements(d, m.njoints, o1);
+      if (o2) store_motions(d.v, m.njoints, o2);
+      if (o3) store_motions(d.a, m.njoints, o3);
+      break;
+    case F_JAC:
+      orc::joint_jacobians(m, d, bq.x.data());
+      store(d.J, o1, (size_t)6 * nv);
+      break;
     case F_INTEGRATE: {
       std::vector<T> out(nq);
       orc::integrate(m, bq.x.data(), bv.x.data(), out.data());
@@ -120,6 +142,8 @@ int out_stride(int func, const Model& m, int which) {
     case F_CHOL: return which == 0 ? nn : m.nv;
     case F_RNEA_D: case F_ABA_D: return which == 0 ? m.nv : nn;
     case F_INTEGRATE: return m.nq;
+    case F_FK: return which == 0 ? 12 * m.njoints : 6 * m.njoints;
+    case F_JAC: return 6 * m.nv;
     default: return m.nv;
   }
 }
@@ -233,6 +257,13 @@ int orc_rnea_derivatives(void* h, int prec, long B, const double* q, const doubl
 int orc_aba_derivatives(void* h, int prec, long B, const double* q, const double* v, const double* tau, double* ddq,
                         double* ddq_dq, double* ddq_dv, double* Minv, int nt) {
   return dispatch(h, prec, F_ABA_D, B, q, v, tau, ddq, ddq_dq, ddq_dv, Minv, nt);
+}
+int orc_forward_kinematics(void* h, int prec, long B, const double* q, const double* v, const double* a, double* oMi,
+                           double* vi, double* ai, int nt) {
+  return dispatch(h, prec, F_FK, B, q, v, a, oMi, vi, ai, nullptr, nt);
+}
+int orc_joint_jacobians(void* h, int prec, long B, const double* q, double* J, int nt) {
+  return dispatch(h, prec, F_JAC, B, q, nullptr, nullptr, J, nullptr, nullptr, nullptr, nt);
 }
 int orc_integrate(void* h, int prec, long B, const double* q, const double* v, double* qout, int nt) {
   return dispatch(h, prec, F_INTEGRATE, B, q, v, nullptr, qout, nullptr, nullptr, nullptr, nt);

@@ -24,11 +24,13 @@ from .api import (  # noqa: F401
     abaInParallel,
     computeABADerivatives,
     computeGeneralizedGravity,
+    computeJointJacobians,
     computeMinverse,
     computeRNEADerivatives,
     crba,
     crbaCholesky,
     createData,
+    forwardKinematics,
     integrate,
     nonLinearEffects,
     rnea,

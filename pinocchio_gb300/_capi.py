@@ -39,6 +39,8 @@ EXPORTS = (
     "gb_compute_minverse",
     "gb_aba_derivatives_vjp",
     "gb_aba_derivatives_noalloc",
+    "gb_forward_kinematics",
+    "gb_compute_joint_jacobians",
     "gb_integrate",
     "gb_batch_multi",
     "gb_model_set_launch",
@@ -132,6 +134,8 @@ def lib():
         L.gb_aba_derivatives_vjp.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives_noalloc.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
+        L.gb_forward_kinematics.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_compute_joint_jacobians.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]
         L.gb_model_set_launch.argtypes = [vp, i, i]
         L.gb_model_set_layout.argtypes = [vp, i, i]

@@ -6,7 +6,8 @@ Reference signatures (bindings/python/algorithm/...):
   ``pin.computeRNEADerivatives(model, data, q, v, a) -> (dtau_dq, dtau_dv, M)``,
   ``pin.computeABADerivatives(model, data, q, v, tau) -> (ddq_dq, ddq_dv, Minv)``,
   ``pin.ModelPool(model, size)``, ``pin.rneaInParallel(num_threads, pool, q, v, a)``,
-  ``pin.abaInParallel(num_threads, pool, q, v, tau)``, ``pin.integrate(model, q, v)``.
+  ``pin.abaInParallel(num_threads, pool, q, v, tau)``, ``pin.integrate(model, q, v)``,
+  ``pin.forwardKinematics(model, data, q[, v[, a]])``, ``pin.computeJointJacobians(model, data, q)``.
 
 Here every single-configuration function also takes a batch: a torch CUDA
 tensor of shape (batch, n) (one configuration per row, i.e. the reference's
@@ -142,6 +143,49 @@ def computeGeneralizedGravity(model: Model, data: Data, q):
     )
     data.g = out
     return _ret(out, was_np, vec)
+
+
+def forwardKinematics(model: Model, data: Data, q, v=None, a=None):
+    """forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272).
+
+    Fills and returns ``(data.oMi, data.v, data.a)``: oMi (batch, njoints, 12) world placements
+    (rotation row-major, then translation; joint 0 the identity), v and a (batch, njoints, 6) the
+    joint-frame spatial velocities and accelerations ([linear; angular], no gravity), or None
+    when v (a) is not given."""
+    torch = _torch()
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    if a is not None and v is None:
+        raise ValueError("forwardKinematics: an acceleration needs a velocity")
+    vt = None if v is None else _as_batch(v, model.nv, "v")[0]
+    at = None if a is None else _as_batch(a, model.nv, "a")[0]
+    B, nj = qt.shape[0], model.njoints
+    oMi = torch.empty((B, nj, 12), dtype=qt.dtype, device=qt.device)
+    vo = None if vt is None else torch.empty((B, nj, 6), dtype=qt.dtype, device=qt.device)
+    ao = None if at is None else torch.empty((B, nj, 6), dtype=qt.dtype, device=qt.device)
+    p = lambda t: None if t is None else _ptr(t)  # noqa: E731
+    _capi.check(
+        _capi.lib().gb_forward_kinematics(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), p(vt), p(at), _ptr(oMi), p(vo),
+            p(ao), _stream_ptr()
+        )
+    )
+    data.oMi, data.v, data.a = oMi, vo, ao
+    return tuple(None if t is None else _ret(t, was_np, vec) for t in (oMi, vo, ao))
+
+
+def computeJointJacobians(model: Model, data: Data, q):
+    """data.J = computeJointJacobians(model, data, q) (reference algorithm/jacobian.hxx:17-95):
+    (batch, 6, nv), column k the world-frame motion subspace of dof k about the world origin."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    B, nv = qt.shape[0], model.nv
+    Jc = _torch().empty((B, nv, 6), dtype=qt.dtype, device=qt.device)  # column-major 6 x nv
+    _capi.check(
+        _capi.lib().gb_compute_joint_jacobians(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(Jc), _stream_ptr()
+        )
+    )
+    data.J = Jc.transpose(1, 2)
+    return _ret(data.J, was_np, vec)
 
 
 def computeMinverse(model: Model, data: Data, q, symmetric: bool = True):

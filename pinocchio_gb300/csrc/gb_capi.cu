@@ -128,6 +128,32 @@ int gb_generalized_gravity(const gb_model* M, int precision, int layout, long B,
                           gbi::arr(g, layout, B, M->nv), (cudaStream_t)stream);
 }
 
+int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                          const double* a, double* oMi, double* vout, double* aout, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (a && !v) return set_error(GB_ERR_INVALID_ARGUMENT, "an acceleration needs a velocity");
+  if ((vout && !v) || (aout && !a)) return set_error(GB_ERR_INVALID_ARGUMENT, "velocity / acceleration output without input");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(oMi, "oMi"));
+  if (v) GB_TRY(gbi::check_ptr(v, "v"));
+  if (a) GB_TRY(gbi::check_ptr(a, "a"));
+  if (vout) GB_TRY(gbi::check_ptr(vout, "v output"));
+  if (aout) GB_TRY(gbi::check_ptr(aout, "a output"));
+  const long nj = M->nj;
+  return gbi::launch_fk(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
+                        gbi::arr(a, layout, B, M->nv), gbi::arr(oMi, layout, B, 12 * nj),
+                        gbi::arr(vout, layout, B, 6 * nj), gbi::arr(aout, layout, B, 6 * nj), (cudaStream_t)stream);
+}
+
+int gb_compute_joint_jacobians(const gb_model* M, int precision, int layout, long B, const double* q, double* J,
+                               void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(J, "J"));
+  return gbi::launch_jacobians(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(J, layout, B, 6L * M->nv),
+                               (cudaStream_t)stream);
+}
+
 int gb_aba(const gb_model* M, int precision, int convention, int layout, long B, const double* q, const double* v,
            const double* tau, double* ddq, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));

@@ -444,6 +444,90 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
 }
 
 // ------------------------------------------------------------------------------------------
+// forwardKinematics (reference algorithm/kinematics.hxx: ZeroStep 42-77, FirstStep 105-178,
+// SecondStep 188-272): oMi (R row-major, then t; joint 0 the identity) and, when v (and a)
+// are given, the joint-frame spatial velocities (and accelerations, without gravity).
+// computeJointJacobians (reference algorithm/jacobian.hxx:17-95): J = [oMi.act(S_i)],
+// 6 x nv column-major about the world origin.
+// ------------------------------------------------------------------------------------------
+template <class S>
+GB_HD void store_placement(const Out& o, int i, const X3<S>& X) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o[12 * i + k] = double(X.R[k]);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) o[12 * i + 9 + k] = double(X.t[k]);
+}
+template <class S, int CAP>
+GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const Out& oMi, const Out* vo,
+                  const Out* ao) {
+  X3<S> oM[CAP];
+  M6<S> vel[CAP], acc[CAP];
+  {
+    X3<S> I;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) I.R[k] = (k == 0 || k == 4 || k == 8) ? S(1) : S(0);
+    I.t[0] = I.t[1] = I.t[2] = S(0);
+    store_placement(oMi, 0, I);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      if (vo) (*vo)[k] = 0.0;
+      if (ao) (*ao)[k] = 0.0;
+    }
+  }
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    X3<S> X;
+    joint_transform(m, i, q, X);
+    if (p > 0) compose(oM[p], X, oM[i]);
+    else oM[i] = X;
+    store_placement(oMi, i, oM[i]);
+    if (!v) continue;
+    M6<S> vJ, t;
+    joint_motion(jt, *v, iv, vJ);
+    if (p > 0) {
+      actinv_motion(X, vel[p], t);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) vel[i].v[k] = vJ.v[k] + t.v[k];
+    } else {
+      vel[i] = vJ;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) (*vo)[6 * i + k] = double(vel[i].v[k]);
+    if (!a) continue;
+    M6<S> aJ, ap;
+    joint_motion(jt, *a, iv, aJ);
+    cross_motion(vel[i], vJ, t);
+    if (p > 0) actinv_motion(X, acc[p], ap);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[i].v[k] = p > 0 ? (aJ.v[k] + t.v[k]) + ap.v[k] : aJ.v[k] + t.v[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) (*ao)[6 * i + k] = double(acc[i].v[k]);
+  }
+}
+template <class S, int CAP>
+GB_HD void jacobians_one(const MView& m, const In& q, const Out& J) {
+  X3<S> oM[CAP];
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+    X3<S> X;
+    joint_transform(m, i, q, X);
+    if (p > 0) compose(oM[p], X, oM[i]);
+    else oM[i] = X;
+    const int nvj = jt == JT_FF ? 6 : 1;
+    for (int k = 0; k < nvj; ++k) {
+      M6<S> sk, c;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) sk.v[r] = S(0);
+      if (jt == JT_FF) sk.v[k] = S(1);
+      else sk.v[3 + jt - JT_RX] = S(1);
+      act_motion(oM[i], sk, c);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) J[6 * (iv + k) + r] = double(c.v[r]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 // integrate(q, v): revolute joints q + v; free-flyer through the SE(3)
 // exponential with the quaternion renormalised to first order (reference
 // multibody/liegroup/special-euclidean.hpp:660-699, spatial/explog-quaternion.hpp:20-147,

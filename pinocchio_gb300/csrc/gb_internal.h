@@ -45,6 +45,8 @@ int launch_rnea_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr
 int launch_aba_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
 int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q, Arr M, Arr U, Arr D, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
+int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
+int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);
 size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B);
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
                                    Arr Minv, Arr ddq, void* ws, cudaStream_t st);

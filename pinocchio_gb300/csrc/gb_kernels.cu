@@ -1,4 +1,5 @@
-// Batched sweep kernels: RNEA, ABA, CRBA (+ FP64 Cholesky), integrate.
+// Batched sweep kernels: RNEA, ABA, CRBA (+ FP64 Cholesky), forward kinematics,
+// joint Jacobians, integrate.
 //
 // One thread evaluates one configuration; a CTA of kThreads threads first
 // copies the model blob (joint tables, placements, inertias) from global to
@@ -60,6 +61,28 @@ __global__ void __launch_bounds__(kThreads) k_crba(const unsigned char* blob, in
   if (b >= B) return;
   const gb::Out Uo = out_at(U, b), Do = out_at(D, b);
   gb::crba_one<S, CAP>(m, in_at(q, b), out_at(M, b), symmetric, U.p ? &Uo : nullptr, U.p ? &Do : nullptr, true);
+}
+
+template <class S, int CAP>
+__global__ void __launch_bounds__(kThreads) k_fk(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr a,
+                                                 Arr oMi, Arr vo, Arr ao) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const gb::In qi = in_at(q, b), vi = in_at(v, b), ai = in_at(a, b);
+  const gb::Out vout = out_at(vo, b), aout = out_at(ao, b);
+  gb::fk_one<S, CAP>(m, qi, v.p ? &vi : nullptr, a.p ? &ai : nullptr, out_at(oMi, b), vo.p ? &vout : nullptr,
+                     ao.p ? &aout : nullptr);
+}
+
+template <class S, int CAP>
+__global__ void __launch_bounds__(kThreads) k_jacobians(const unsigned char* blob, int bytes, long B, Arr q, Arr J) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  gb::jacobians_one<S, CAP>(m, in_at(q, b), out_at(J, b));
 }
 
 __global__ void __launch_bounds__(kThreads) k_integrate(const unsigned char* blob, int bytes, long B, Arr q, Arr v,
@@ -138,6 +161,24 @@ int launch_crba(const gb_model* M, int precision, bool symmetric, long B, Arr q,
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_crba<double, C>), symmetric, q, Mo, U, D));
   } else {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_crba<float, C>), symmetric, q, Mo, U, D));
+  }
+}
+
+int launch_fk(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_RNEA;
+  if (precision == GB_FP64) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_fk<double, C>), q, v, a, oMi, vo, ao));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_fk<float, C>), q, v, a, oMi, vo, ao));
+  }
+}
+
+int launch_jacobians(const gb_model* M, int precision, long B, Arr q, Arr J, cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_RNEA;
+  if (precision == GB_FP64) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_jacobians<double, C>), q, J));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_jacobians<float, C>), q, J));
   }
 }
 

@@ -17,7 +17,7 @@ from util import FP64_TOL, MIXED_TOL, MODELS, rel_err
 
 pytestmark = pytest.mark.gpu
 
-# the mixed-precision bar applies to the BASELINE models; the 100-link chain is
+# the mixed-precision bar applies to the benchmark models; the 100-link chain is
 # the FP64 stress test (its Minv condition number amplifies FP32 rounding)
 MIXED_MODELS = [n for n in MODELS if n != "chain100"]
 
@@ -135,7 +135,7 @@ def test_aba_derivatives_vjp(case, precision):
     """gb_aba_derivatives_vjp == g^T of the oracle's Jacobians (and Minv g)."""
     name, model, om, q, v, x, dev = case
     if precision == "mixed" and name not in MIXED_MODELS:
-        pytest.skip("mixed-precision bar applies to the BASELINE models")
+        pytest.skip("the mixed-precision bar applies to the benchmark models")
     tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
     tau = 10.0 * x
     g = np.random.default_rng(5).standard_normal((q.shape[0], model.nv))

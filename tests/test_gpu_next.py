@@ -1,8 +1,10 @@
-"""The neighbours of the path (SURVEY 8(f) next rows) through the C ABI:
+"""The neighbours of the path through the C ABI:
 computeMinverse (reference algorithm/aba.hxx:838-880) against the oracle's
 Minv and M^-1, nonLinearEffects and computeGeneralizedGravity (rnea.hxx:221-446)
-against the oracle's RNEA with zero acceleration / zero velocity; FP64 at 1e-12
-and mixed precision at 1e-5, both output modes, both layouts."""
+against the oracle's RNEA with zero acceleration / zero velocity,
+forwardKinematics (kinematics.hxx:42-272) and computeJointJacobians
+(jacobian.hxx:17-95) against the oracle's; FP64 at 1e-12 and mixed precision
+at 1e-5, both output modes, both layouts."""
 import ctypes as C
 
 import numpy as np
@@ -38,7 +40,7 @@ def _tol(name, precision):
 def test_compute_minverse(case, precision):
     name, model, om, q, v, x, dev = case
     if precision == "mixed" and name not in MIXED_MODELS:
-        pytest.skip("mixed-precision bar applies to the BASELINE models")
+        pytest.skip("the mixed-precision bar applies to the benchmark models")
     tol = _tol(name, precision)
     data = pg.createData(model, precision)
     Mi = pg.computeMinverse(model, data, dev(q)).cpu().numpy()
@@ -95,3 +97,64 @@ def test_empty_batch_and_errors():
     assert L.gb_compute_minverse(data.dev.h, _capi.GB_FP64, _capi.GB_MATRIX_UPPER, _capi.GB_LAYOUT_INSTANCE, 0, None, None, None) == 0
     assert L.gb_compute_minverse(data.dev.h, _capi.GB_FP64, 7, _capi.GB_LAYOUT_INSTANCE, 1, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
     assert L.gb_nonlinear_effects(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, 3, None, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_forward_kinematics(case, precision):
+    """forwardKinematics (reference algorithm/kinematics.hxx:42-272): placements,
+    joint-frame velocities and accelerations against the oracle; the q-only and
+    (q, v) forms; the SOA layout gives the same bits."""
+    import torch
+
+    name, model, om, q, v, x, dev = case
+    tol = _tol(name, precision)
+    data = pg.createData(model, precision)
+    oMi, vi, ai = (t.cpu().numpy() for t in pg.forwardKinematics(model, data, dev(q), dev(v), dev(x)))
+    o_r, v_r, a_r = om.forward_kinematics(q, v, x)
+    assert rel_err(oMi, o_r) < tol
+    assert rel_err(vi, v_r) < tol
+    assert rel_err(ai, a_r) < tol
+    o2, v2, a2 = pg.forwardKinematics(model, data, dev(q), dev(v))
+    assert np.array_equal(o2.cpu().numpy(), oMi) and np.array_equal(v2.cpu().numpy(), vi) and a2 is None
+    o3, v3, a3 = pg.forwardKinematics(model, data, dev(q))
+    assert np.array_equal(o3.cpu().numpy(), oMi) and v3 is None and a3 is None
+    B, nj = q.shape[0], model.njoints
+    outs = [torch.empty((n, B), dtype=torch.float64, device="cuda") for n in (12 * nj, 6 * nj, 6 * nj)]
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    qs, vs, xs = (dev(np.ascontiguousarray(t.T)) for t in (q, v, x))
+    _capi.check(
+        _capi.lib().gb_forward_kinematics(data.dev.h, _capi.GB_FP64 if precision == "fp64" else _capi.GB_MIXED,
+                                          _capi.GB_LAYOUT_SOA, B, p(qs), p(vs), p(xs), p(outs[0]), p(outs[1]),
+                                          p(outs[2]), None)
+    )
+    torch.cuda.synchronize()
+    for o, r in zip(outs, (oMi, vi, ai)):
+        assert np.array_equal(o.cpu().numpy().T.reshape(r.shape), r)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_compute_joint_jacobians(case, precision):
+    """computeJointJacobians (reference algorithm/jacobian.hxx:17-95) against the
+    oracle; J v equals the world-frame velocity of the last joint."""
+    name, model, om, q, v, x, dev = case
+    tol = _tol(name, precision)
+    data = pg.createData(model, precision)
+    J = pg.computeJointJacobians(model, data, dev(q)).cpu().numpy()  # (B, 6, nv)
+    assert J.shape == (q.shape[0], 6, model.nv)
+    assert rel_err(J, np.swapaxes(om.joint_jacobians(q), 1, 2)) < tol
+
+
+def test_forward_kinematics_errors():
+    model = MODELS["manipulator6r"]()
+    data = pg.createData(model)
+    L = _capi.lib()
+    z = np.zeros((2, 12 * model.njoints))
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    q = np.zeros((2, model.nq))
+    # an acceleration without a velocity, an output without its input
+    assert L.gb_forward_kinematics(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, 2, p(q), None, p(q), p(z), None,
+                                   None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_forward_kinematics(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, 2, p(q), None, None, p(z), p(z),
+                                   None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_forward_kinematics(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, 0, None, None, None, None, None,
+                                   None, None) == _capi.GB_OK

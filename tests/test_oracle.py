@@ -177,3 +177,65 @@ def test_kat_free_body_newton_euler():
         exp_lin = R.T @ g - np.cross(w, lin)
         exp_ang = np.linalg.solve(I, -np.cross(w, I @ w))
         assert np.allclose(ddq[b], np.concatenate([exp_lin, exp_ang]), rtol=1e-13, atol=1e-13)
+
+
+def _act_motion(M, m6):
+    """oMi.act(m) for M = (R row-major, t) (reference spatial/se3-tpl.hpp:265-280)."""
+    R = M[..., :9].reshape(M.shape[:-1] + (3, 3))
+    t = M[..., 9:]
+    w = np.einsum("...ij,...j->...i", R, m6[..., 3:])
+    lin = np.einsum("...ij,...j->...i", R, m6[..., :3]) + np.cross(t, w)
+    return np.concatenate([lin, w], axis=-1)
+
+
+def _support(model):
+    """dofs of joint i and of its ancestors, per joint (the columns of data.J that move joint i)."""
+    t = model.tables()
+    parents = t["parents"]
+    nvs = [0] + [6 if jt == gm.JT_FF else 1 for jt in t["jtype"][1:]]
+    idx_v = np.concatenate([[0], np.cumsum(nvs)])[: len(parents)]
+    out = []
+    for i in range(len(parents)):
+        dofs, j = [], i
+        while j > 0:
+            dofs += list(range(idx_v[j], idx_v[j] + nvs[j]))
+            j = parents[j]
+        out.append(sorted(dofs))
+    return out
+
+
+def test_forward_kinematics_and_jacobians_agree(case):
+    """computeJointJacobians against forwardKinematics (unittest/jacobian.cpp:19-60:
+    J v is the world-frame spatial velocity of each joint), joint 0 the identity,
+    and the long-double oracle."""
+    name, model, om, q, v, a = case
+    oMi, vi, ai = om.forward_kinematics(q, v, a)
+    J = om.joint_jacobians(q)  # (B, nv, 6)
+    for i, dofs in enumerate(_support(model)):
+        world = _act_motion(oMi[:, i], vi[:, i])
+        Jv = np.einsum("bkr,bk->br", J[:, dofs], v[:, dofs]) if dofs else np.zeros_like(world)
+        assert rel_err(Jv, world) < 1e-12, i
+    assert np.array_equal(oMi[:, 0], np.tile(np.eye(3).reshape(-1).tolist() + [0, 0, 0], (len(q), 1)))
+    assert not vi[:, 0].any() and not ai[:, 0].any()
+    oMl, vl, al = om.forward_kinematics(q, v, a, prec=1)
+    Jl = om.joint_jacobians(q, prec=1)
+    for x, y in ((oMi, oMl), (vi, vl), (ai, al), (J, Jl)):
+        assert rel_err(x, y) < 1e-12
+    # placement-only and velocity-only calls fill the same placements / velocities
+    o2, v2, a2 = om.forward_kinematics(q, v)
+    assert np.array_equal(o2, oMi) and np.array_equal(v2, vi) and a2 is None
+    assert np.array_equal(om.forward_kinematics(q)[0], oMi)
+
+
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12"])
+def test_forward_kinematics_acceleration_vs_fd(name):
+    """data.a[i] is the time derivative of the joint-frame velocity data.v[i]
+    along (q + dt v, v + dt a): central differences, step 1e-6."""
+    model = MODELS[name]()
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, 4, 21)
+    _, _, ai = om.forward_kinematics(q, v, a)
+    h = 1e-6
+    vp = om.forward_kinematics(om.integrate(q, h * v), v + h * a)[1]
+    vm = om.forward_kinematics(om.integrate(q, -h * v), v - h * a)[1]
+    assert rel_err((vp - vm) / (2 * h), ai) < 1e-6
