@@ -148,6 +148,27 @@ inline void computeABADerivatives(const Model& m, int precision, long batch, con
   check(gb_aba_derivatives(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, tau, ddq_dq, ddq_dv, Minv, nullptr,
                            stream));
 }
+inline void computeMinverse(const Model& m, int precision, long batch, const double* q, double* Minv,
+                            void* stream = nullptr) {
+  check(gb_compute_minverse(m.get(), precision, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, batch, q, Minv, stream));
+}
+inline void nonLinearEffects(const Model& m, int precision, long batch, const double* q, const double* v, double* nle,
+                             void* stream = nullptr) {
+  check(gb_nonlinear_effects(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, nle, stream));
+}
+inline void computeGeneralizedGravity(const Model& m, int precision, long batch, const double* q, double* g,
+                                      void* stream = nullptr) {
+  check(gb_generalized_gravity(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, g, stream));
+}
+// v, a, v_out, a_out may be null (placements only, or placements and velocities)
+inline void forwardKinematics(const Model& m, int precision, long batch, const double* q, const double* v,
+                              const double* a, double* oMi, double* v_out, double* a_out, void* stream = nullptr) {
+  check(gb_forward_kinematics(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, a, oMi, v_out, a_out, stream));
+}
+inline void computeJointJacobians(const Model& m, int precision, long batch, const double* q, double* J,
+                                  void* stream = nullptr) {
+  check(gb_compute_joint_jacobians(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, J, stream));
+}
 
 }  // namespace pinocchio_gb300
 
