@@ -16,6 +16,7 @@ from .model import (  # noqa: F401
     SE3,
 )
 from . import sample_models  # noqa: F401
+from .urdf import buildModelFromUrdf, buildModelFromXML, load_model, save_model  # noqa: F401
 from .api import (  # noqa: F401
     Data,
     ModelPool,

@@ -1,0 +1,189 @@
+"""URDF -> Model, and the Model's on-disk format.
+
+``buildModelFromUrdf(path, root_joint=None)`` / ``buildModelFromXML(xml, root_joint=None)`` follow
+the reference's URDF parser (src/parsers/urdf/model.cpp, src/parsers/urdf/model.hxx): the tree is
+walked depth first from the root link, children in file order; every moving joint becomes a joint of
+the model, placed relative to its parent joint by the chain of URDF origins (through any fixed
+joints in between); every link becomes a body appended to the joint that moves it (its inertial
+frame placed in that joint's frame); a fixed joint adds no degree of freedom and merges its child
+link into the parent body (reference: fixed joints become frames, their bodies are appended to the
+parent joint).  ``root_joint=JointModelFreeFlyer()`` puts a free-flyer between the universe and the
+root link, as the reference's ``buildModel(filename, root_joint, model)`` does.
+
+The batched kernels support revolute joints about a coordinate axis: ``revolute`` and ``continuous``
+joints with axis +-x, +-y or +-z.  A negative axis is taken by a fixed half-turn F of the joint frame
+(F maps the axis to its opposite), so that the joint keeps the file's angle sign: the model's frame
+of that joint is the URDF joint frame times F, the link hung from it is placed by F^-1, and every
+joint-space quantity (q, v, tau, M, the derivatives) is the reference's.  Other joint types
+(prismatic, planar, floating inside the tree) and axes off the coordinate axes raise ValueError.
+
+``save_model`` / ``load_model`` write and read the flattened tables (``Model.tables()`` plus the joint
+names) as one ``.npz`` file: the on-disk format of a model (the reference serialises ModelTpl with
+boost archives, serialization/model.hpp).
+"""
+from __future__ import annotations
+
+import xml.etree.ElementTree as ET
+
+import numpy as np
+
+from .model import JT_FF, JT_NONE, JT_RX, JT_RY, JT_RZ, Inertia, JointModel, JointModelFreeFlyer, Model, SE3
+
+
+def _floats(text, n, default):
+    if text is None:
+        return np.array(default, dtype=np.float64)
+    vals = [float(x) for x in text.split()]
+    if len(vals) != n:
+        raise ValueError(f"expected {n} numbers, got {text!r}")
+    return np.array(vals)
+
+
+def _rpy(rpy):
+    """Rotation of URDF roll-pitch-yaw angles: Rz(yaw) Ry(pitch) Rx(roll)."""
+    r, p, y = rpy
+    cr, sr, cp, sp, cy, sy = np.cos(r), np.sin(r), np.cos(p), np.sin(p), np.cos(y), np.sin(y)
+    Rx = np.array([[1, 0, 0], [0, cr, -sr], [0, sr, cr]])
+    Ry = np.array([[cp, 0, sp], [0, 1, 0], [-sp, 0, cp]])
+    Rz = np.array([[cy, -sy, 0], [sy, cy, 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx
+
+
+def _origin(elem):
+    o = None if elem is None else elem.find("origin")
+    if o is None:
+        return SE3.Identity()
+    return SE3(_rpy(_floats(o.get("rpy"), 3, [0, 0, 0])), _floats(o.get("xyz"), 3, [0, 0, 0]))
+
+
+def _mul(A: SE3, B: SE3) -> SE3:
+    return SE3(A.rotation @ B.rotation, A.rotation @ B.translation + A.translation)
+
+
+def _link_inertia(link) -> Inertia:
+    """The link's inertia in the link frame (inertial origin applied)."""
+    inertial = link.find("inertial")
+    if inertial is None:
+        return Inertia.Zero()
+    mass_el = inertial.find("mass")
+    mass = float(mass_el.get("value")) if mass_el is not None else 0.0
+    it = inertial.find("inertia")
+    I = np.zeros((3, 3))
+    if it is not None:
+        g = lambda k: float(it.get(k, "0"))  # noqa: E731
+        I = np.array([[g("ixx"), g("ixy"), g("ixz")], [g("ixy"), g("iyy"), g("iyz")], [g("ixz"), g("iyz"), g("izz")]])
+    return Inertia(mass, np.zeros(3), I).se3_action(_origin(inertial))
+
+
+# the half-turn that maps a coordinate axis to its opposite: about z for x and y, about x for z
+_FLIP = {0: np.diag([-1.0, -1.0, 1.0]), 1: np.diag([-1.0, -1.0, 1.0]), 2: np.diag([1.0, -1.0, -1.0])}
+_AXIS_JT = {0: JT_RX, 1: JT_RY, 2: JT_RZ}
+
+
+class _Revolute(JointModel):
+    def __init__(self, jtype):
+        self.jtype = jtype
+
+
+def _axis_joint(joint):
+    """(jtype, F) for a revolute joint's axis; F the frame flip (None for a positive axis)."""
+    ax = _floats(None if joint.find("axis") is None else joint.find("axis").get("xyz"), 3, [1, 0, 0])
+    n = np.linalg.norm(ax)
+    if n == 0:
+        raise ValueError(f"joint {joint.get('name')!r}: zero axis")
+    ax = ax / n
+    k = int(np.argmax(np.abs(ax)))
+    if abs(abs(ax[k]) - 1.0) > 1e-12:
+        raise ValueError(f"joint {joint.get('name')!r}: axis {ax} is not a coordinate axis (unsupported)")
+    return _AXIS_JT[k], (None if ax[k] > 0 else _FLIP[k])
+
+
+def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
+    """Model of a URDF document (reference pinocchio::urdf::buildModelFromXML)."""
+    robot = ET.fromstring(xml)
+    if robot.tag != "robot":
+        raise ValueError("not a URDF document: the root element must be <robot>")
+    links = {l.get("name"): l for l in robot.findall("link")}
+    joints = robot.findall("joint")
+    children: dict[str, list] = {name: [] for name in links}
+    is_child = set()
+    for j in joints:
+        parent, child = j.find("parent").get("link"), j.find("child").get("link")
+        if parent not in links or child not in links:
+            raise ValueError(f"joint {j.get('name')!r} refers to an unknown link")
+        children[parent].append(j)
+        is_child.add(child)
+    roots = [name for name in links if name not in is_child]
+    if len(roots) != 1:
+        raise ValueError(f"a URDF tree has one root link, found {roots}")
+    model = Model()
+    model.name = robot.get("name", "")
+    if root_joint is not None:
+        if root_joint.jtype != JT_FF:
+            raise ValueError("root_joint: only JointModelFreeFlyer is supported")
+        frame = (model.addJoint(0, JointModelFreeFlyer(), SE3.Identity(), "root_joint"), SE3.Identity())
+    else:
+        frame = (0, SE3.Identity())
+
+    def append(joint_id, link_name, placement):
+        Y = _link_inertia(links[link_name])
+        if joint_id > 0 and (Y.mass > 0.0 or Y.inertia.any()):
+            model.appendBodyToJoint(joint_id, Y, placement)
+
+    append(frame[0], roots[0], frame[1])
+
+    def visit(link_name, frame):  # depth first, children in file order (the reference's recursion)
+        joint_id, link_in_joint = frame
+        for j in children[link_name]:
+            child = j.find("child").get("link")
+            Pj = _mul(link_in_joint, _origin(j))
+            jt = j.get("type")
+            if jt == "fixed":
+                append(joint_id, child, Pj)
+                visit(child, (joint_id, Pj))
+            elif jt in ("revolute", "continuous"):
+                jtype, F = _axis_joint(j)
+                placement = Pj if F is None else SE3(Pj.rotation @ F, Pj.translation)
+                new_id = model.addJoint(joint_id, _Revolute(jtype), placement, j.get("name"))
+                child_in_joint = SE3.Identity() if F is None else SE3(F.T, np.zeros(3))
+                append(new_id, child, child_in_joint)
+                visit(child, (new_id, child_in_joint))
+            else:
+                raise ValueError(f"joint {j.get('name')!r}: type {jt!r} is not supported by the batched kernels")
+
+    visit(roots[0], frame)
+    model.check_depth_first()
+    return model
+
+
+def buildModelFromUrdf(path: str, root_joint: JointModel | None = None) -> Model:
+    """Model of a URDF file (reference pinocchio::urdf::buildModel(filename[, root_joint], model))."""
+    with open(path, "r", encoding="utf-8") as f:
+        return buildModelFromXML(f.read(), root_joint)
+
+
+def save_model(model: Model, path: str) -> None:
+    """Writes the model's tables and joint names to ``path`` (.npz)."""
+    t = model.tables()
+    np.savez(path, names=np.array(model.names), name=np.array(model.name), **t)
+
+
+def load_model(path: str) -> Model:
+    """Reads a model written by ``save_model``."""
+    with np.load(path, allow_pickle=False) as z:
+        parents, jtype = z["parents"], z["jtype"]
+        placement, inertia = z["placement"], z["inertia"]
+        names = [str(n) for n in z["names"]]
+        model = Model()
+        model.name = str(z["name"])
+        for i in range(1, len(parents)):
+            jt = int(jtype[i])
+            joint = JointModelFreeFlyer() if jt == JT_FF else _Revolute(jt)
+            if jt == JT_NONE:
+                raise ValueError("joint type 0 (universe) below the root")
+            P = SE3(placement[i, :9].reshape(3, 3), placement[i, 9:])
+            model.addJoint(int(parents[i]), joint, P, names[i])
+            model.inertias[i] = Inertia(inertia[i, 0], inertia[i, 1:4], inertia[i, 4:])
+        model.armature = np.array(z["armature"], dtype=np.float64)
+        model.gravity = np.array(z["gravity"], dtype=np.float64)
+    return model

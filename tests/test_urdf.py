@@ -1,0 +1,161 @@
+"""URDF loading (reference src/parsers/urdf/model.cpp: depth-first walk from the
+root link, moving joints placed through any fixed joints, links appended as
+bodies to the joint that moves them, fixed joints merged into the parent body,
+an optional free-flyer root joint) and the model's on-disk format, checked on
+the CPU against models built with the construction API and through the oracle."""
+import numpy as np
+import pytest
+
+import pinocchio_gb300 as pg
+from oracle.oracle import OracleModel
+from pinocchio_gb300 import model as gm
+from pinocchio_gb300 import sample_models as sm
+from util import MODELS, rel_err
+
+_AX = {gm.JT_RX: "1 0 0", gm.JT_RY: "0 1 0", gm.JT_RZ: "0 0 1"}
+
+
+def _rpy_of(R):
+    """roll, pitch, yaw with R = Rz(yaw) Ry(pitch) Rx(roll)."""
+    pitch = np.arcsin(-np.clip(R[2, 0], -1.0, 1.0))
+    roll = np.arctan2(R[2, 1], R[2, 2])
+    yaw = np.arctan2(R[1, 0], R[0, 0])
+    return roll, pitch, yaw
+
+
+def _f(x):
+    return repr(float(x))
+
+
+def _origin(P):
+    r, p, y = _rpy_of(P.rotation)
+    t = P.translation
+    return f'<origin xyz="{_f(t[0])} {_f(t[1])} {_f(t[2])}" rpy="{_f(r)} {_f(p)} {_f(y)}"/>'
+
+
+def _inertial(Y):
+    I = Y.matrix3()
+    c = Y.lever
+    return (f'<inertial><origin xyz="{_f(c[0])} {_f(c[1])} {_f(c[2])}"/><mass value="{_f(Y.mass)}"/>'
+            f'<inertia ixx="{_f(I[0, 0])}" ixy="{_f(I[0, 1])}" ixz="{_f(I[0, 2])}" iyy="{_f(I[1, 1])}" '
+            f'iyz="{_f(I[1, 2])}" izz="{_f(I[2, 2])}"/></inertial>')
+
+
+def to_urdf(model, skip_free_flyer=True):
+    """URDF of a revolute-joint model (the root free-flyer, if any, left to root_joint)."""
+    out = ['<robot name="exported">', '<link name="base"/>']
+    link_of = {0: "base"}
+    for i in range(1, model.njoints):
+        if model.jtypes[i] == gm.JT_FF:
+            assert skip_free_flyer and model.parents[i] == 0
+            link_of[i] = "base"
+            out[1] = f'<link name="base">{_inertial(model.inertias[i])}</link>'
+            continue
+        link_of[i] = f"link{i}"
+        out.append(f'<link name="link{i}">{_inertial(model.inertias[i])}</link>')
+        out.append(f'<joint name="{model.names[i]}" type="revolute"><parent link="{link_of[model.parents[i]]}"/>'
+                   f'<child link="link{i}"/>{_origin(model.jointPlacements[i])}<axis xyz="{_AX[model.jtypes[i]]}"/>'
+                   f'<limit lower="-3" upper="3" effort="1" velocity="1"/></joint>')
+    out.append("</robot>")
+    return "\n".join(out)
+
+
+@pytest.mark.parametrize("name", ["manipulator6r", "tree12", "chain100"])
+def test_urdf_round_trip(name):
+    model = MODELS[name]()
+    back = pg.buildModelFromXML(to_urdf(model))
+    a, b = model.tables(), back.tables()
+    assert np.array_equal(a["parents"], b["parents"]) and np.array_equal(a["jtype"], b["jtype"])
+    assert np.abs(a["placement"] - b["placement"]).max() < 1e-12
+    assert np.abs(a["inertia"] - b["inertia"]).max() < 1e-12
+
+
+def test_urdf_free_flyer_root():
+    model = MODELS["humanoid32"]()  # the free-flyer sits at the root with its own placement
+    back = pg.buildModelFromXML(to_urdf(model), root_joint=pg.JointModelFreeFlyer())
+    a, b = model.tables(), back.tables()
+    assert np.array_equal(a["parents"], b["parents"]) and np.array_equal(a["jtype"], b["jtype"])
+    assert np.abs(a["placement"][2:] - b["placement"][2:]).max() < 1e-12  # joints below the root
+    assert np.abs(a["inertia"] - b["inertia"]).max() < 1e-12
+    om, ob = OracleModel(model), OracleModel(back)
+    q, v, x = sm.random_inputs(model, 8, 3)
+    # the root placement only re-expresses the free-flyer's q: joint-space dynamics in the root frame agree
+    assert rel_err(om.crba(q)[:, 6:, 6:], ob.crba(q)[:, 6:, 6:]) < 1e-12
+
+
+_TWO_LINK = """<robot name="two">
+  <link name="base"/>
+  <link name="upper"><inertial><origin xyz="0.1 0 -0.2" rpy="0.1 0.2 0.3"/><mass value="1.5"/>
+    <inertia ixx="0.02" ixy="0.001" ixz="0" iyy="0.03" iyz="0.002" izz="0.01"/></inertial></link>
+  <link name="tool"><inertial><origin xyz="0 0.05 0"/><mass value="0.4"/>
+    <inertia ixx="0.001" ixy="0" ixz="0" iyy="0.002" iyz="0" izz="0.003"/></inertial></link>
+  <link name="lower"><inertial><origin xyz="0 0 -0.25"/><mass value="0.8"/>
+    <inertia ixx="0.01" ixy="0" ixz="0" iyy="0.01" iyz="0" izz="0.004"/></inertial></link>
+  <joint name="shoulder" type="continuous"><parent link="base"/><child link="upper"/>
+    <origin xyz="0 0 1" rpy="0 0 0.4"/><axis xyz="0 AXIS"/></joint>
+  <joint name="mount" type="fixed"><parent link="upper"/><child link="tool"/>
+    <origin xyz="0.05 0 -0.1" rpy="0.3 0 0"/></joint>
+  <joint name="elbow" type="revolute"><parent link="tool"/><child link="lower"/>
+    <origin xyz="0 0.02 -0.3" rpy="0 0.5 0"/><axis xyz="1 0 0"/>
+    <limit lower="-2" upper="2" effort="1" velocity="1"/></joint>
+</robot>"""
+
+
+def test_urdf_fixed_joint_and_negative_axis():
+    """A fixed joint merges its link into the parent body and carries its origin to
+    the next joint; an axis -z gives the +z joint's dynamics with that joint's
+    coordinate negated (tau_-(q, v, a) = D tau_+(D q, D v, D a), D = diag(-1, 1))."""
+    plus = pg.buildModelFromXML(_TWO_LINK.replace("AXIS", "0 1"))
+    minus = pg.buildModelFromXML(_TWO_LINK.replace("AXIS", "0 -1"))
+    assert plus.njoints == 3 and plus.jtypes[1:] == [gm.JT_RZ, gm.JT_RX]
+    assert abs(plus.inertias[1].mass - 1.9) < 1e-15  # upper + tool
+    rng = np.random.default_rng(1)
+    q, v, a = (rng.standard_normal((16, 2)) for _ in range(3))
+    D = np.array([-1.0, 1.0])
+    tp = OracleModel(plus).rnea(q * D, v * D, a * D)
+    tm = OracleModel(minus).rnea(q, v, a)
+    assert rel_err(tm, tp * D) < 1e-12
+    # the same tree from the construction API: the tool merged into the shoulder body
+    m = pg.Model()
+    j1 = m.addJoint(0, pg.JointModelRZ(), pg.SE3(gm_rz(0.4), [0, 0, 1]), "shoulder")
+    upper = pg.Inertia(1.5, [0, 0, 0], [[0.02, 0.001, 0], [0.001, 0.03, 0.002], [0, 0.002, 0.01]])
+    m.appendBodyToJoint(j1, upper, pg.SE3(rpy(0.1, 0.2, 0.3), [0.1, 0, -0.2]))
+    mount = pg.SE3(rpy(0.3, 0, 0), [0.05, 0, -0.1])
+    m.appendBodyToJoint(j1, pg.Inertia(0.4, [0, 0.05, 0], np.diag([0.001, 0.002, 0.003])), mount)
+    elbow = pg.SE3(mount.rotation @ rpy(0, 0.5, 0), mount.rotation @ np.array([0, 0.02, -0.3]) + mount.translation)
+    j2 = m.addJoint(j1, pg.JointModelRX(), elbow, "elbow")
+    m.appendBodyToJoint(j2, pg.Inertia(0.8, [0, 0, -0.25], np.diag([0.01, 0.01, 0.004])))
+    assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(plus).rnea(q, v, a)) < 1e-12
+
+
+def rpy(r, p, y):
+    cr, sr, cp, sp, cy, sy = np.cos(r), np.sin(r), np.cos(p), np.sin(p), np.cos(y), np.sin(y)
+    return (np.array([[cy, -sy, 0], [sy, cy, 0], [0, 0, 1]]) @ np.array([[cp, 0, sp], [0, 1, 0], [-sp, 0, cp]])
+            @ np.array([[1, 0, 0], [0, cr, -sr], [0, sr, cr]]))
+
+
+def gm_rz(t):
+    return rpy(0, 0, t)
+
+
+@pytest.mark.parametrize("bad,msg", [
+    ('<joint name="s" type="prismatic"><parent link="a"/><child link="b"/><axis xyz="1 0 0"/></joint>', "not supported"),
+    ('<joint name="s" type="revolute"><parent link="a"/><child link="b"/><axis xyz="1 1 0"/></joint>', "coordinate axis"),
+])
+def test_urdf_unsupported(bad, msg):
+    xml = f'<robot name="x"><link name="a"/><link name="b"/>{bad}</robot>'
+    with pytest.raises(ValueError, match=msg):
+        pg.buildModelFromXML(xml)
+
+
+def test_urdf_file_and_model_file(tmp_path):
+    model = MODELS["tree12"]()
+    path = tmp_path / "tree.urdf"
+    path.write_text(to_urdf(model))
+    loaded = pg.buildModelFromUrdf(str(path))
+    npz = tmp_path / "tree.npz"
+    pg.save_model(loaded, str(npz))
+    back = pg.load_model(str(npz))
+    for k, v in loaded.tables().items():
+        assert np.array_equal(v, back.tables()[k]), k
+    assert back.names == loaded.names
