@@ -264,7 +264,7 @@ def measure_heterogeneous(torch, pg, sm, total=100000):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 20 + k))
             data = pg.createData(model, prec)
             tuned = autotune.tune(model, data, functions=("rnea", "aba"), batch=B, use_cache=False)
-            layouts.append({f: ("warp" if t == autotune.WARP else "thread") for f, (t, _) in tuned.items()})
+            layouts.append({f: (t if isinstance(t, str) else "thread") for f, (t, _) in tuned.items()})
             tasks.append((data, "aba", q, v, 10.0 * x))
             tasks.append((data, "rnea", q, v, x))
         tpb, _ = autotune.tune_multi(tasks, prec)

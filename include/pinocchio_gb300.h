@@ -218,12 +218,16 @@ int gb_model_set_launch(gb_model* model, int function, int threads_per_block);
  * 4, 8 or 32 lanes per configuration (GB_INSTANCE_PER_4_LANES, _8_LANES,
  * GB_INSTANCE_PER_WARP) splits the loops over matrix columns of every joint
  * (subtree, ancestor and Minv-row columns), for deep trees at small batches.
+ * RNEA and ABA also: one lane per branch (GB_INSTANCE_PER_BRANCH: a team of 4-32
+ * lanes per configuration, one lane per chain of joints, chains of one level
+ * of the chain tree in parallel).
  * FP64 results are identical in every layout. */
 enum {
   GB_INSTANCE_PER_THREAD = 0,
   GB_INSTANCE_PER_WARP = 1,
   GB_INSTANCE_PER_4_LANES = 2,
-  GB_INSTANCE_PER_8_LANES = 3
+  GB_INSTANCE_PER_8_LANES = 3,
+  GB_INSTANCE_PER_BRANCH = 4
 };
 int gb_model_set_layout(gb_model* model, int function, int layout);
 

@@ -21,6 +21,7 @@ GB_LAYOUT_INSTANCE, GB_LAYOUT_SOA = 0, 1
 GB_MATRIX_UPPER, GB_MATRIX_SYMMETRIC = 0, 1
 GB_FUNC_RNEA, GB_FUNC_ABA, GB_FUNC_CRBA, GB_FUNC_RNEA_DERIVATIVES, GB_FUNC_ABA_DERIVATIVES = range(5)
 GB_INSTANCE_PER_THREAD, GB_INSTANCE_PER_WARP, GB_INSTANCE_PER_4_LANES, GB_INSTANCE_PER_8_LANES = 0, 1, 2, 3
+GB_INSTANCE_PER_BRANCH = 4
 
 # every symbol declared in include/pinocchio_gb300.h, in declaration order
 EXPORTS = (

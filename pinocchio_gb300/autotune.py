@@ -5,7 +5,8 @@ Every batched entry point evaluates one configuration per thread by default;
 RNEA, ABA (and the functions built on them) and the ABA derivatives also have a
 warp-per-instance layout (``gb_model_set_layout``): for RNEA and ABA the 32
 lanes of a warp evaluate one configuration with the joints of a tree level in
-parallel; for the ABA derivatives a team of 4, 8 or 32 lanes splits the loops
+parallel, and a lane-per-branch layout gives each chain of the tree a lane (a
+team of 4-32 lanes per configuration, several configurations per warp); for the ABA derivatives a team of 4, 8 or 32 lanes splits the loops
 over matrix columns (subtree, ancestor and Minv-row columns of every joint)
 while every lane repeats the per-joint work, which pays on deep trees such as
 the 100-link chain at small batches.  They win when the batch is too small to
@@ -32,8 +33,9 @@ from . import sample_models as sm
 CANDIDATES = (32, 64, 96, 128)  # configurations per CTA, one thread each
 WARP = "warp"  # one warp per configuration (RNEA, ABA, ABA derivatives)
 LANES4, LANES8 = "lanes4", "lanes8"  # a team of 4 or 8 lanes per configuration (ABA derivatives)
+BRANCH = "branch"  # one lane per chain of the tree (RNEA, ABA)
 _LAYOUT = {WARP: _capi.GB_INSTANCE_PER_WARP, LANES4: _capi.GB_INSTANCE_PER_4_LANES,
-           LANES8: _capi.GB_INSTANCE_PER_8_LANES}
+           LANES8: _capi.GB_INSTANCE_PER_8_LANES, BRANCH: _capi.GB_INSTANCE_PER_BRANCH}
 CACHE_PATH = os.environ.get(
     "PINOCCHIO_GB300_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "pinocchio_gb300", "autotune.json")
 )
@@ -114,7 +116,7 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
             setting, ms = cache[ck]
         else:
             best = None
-            settings = list(candidates) + ([WARP] if f in ("rnea", "aba") else [])
+            settings = list(candidates) + ([WARP, BRANCH] if f in ("rnea", "aba") else [])
             if f == "aba_derivatives":
                 settings += [LANES4, LANES8, WARP]
             for st in settings:

@@ -201,8 +201,10 @@ int gb_model_set_launch(gb_model* M, int function, int threads_per_block) {
 int gb_model_set_layout(gb_model* M, int function, int layout) {
   if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
   if (function < GB_FUNC_RNEA || function > GB_FUNC_ABA_DERIVATIVES) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown function");
-  if (layout < GB_INSTANCE_PER_THREAD || layout > GB_INSTANCE_PER_8_LANES)
+  if (layout < GB_INSTANCE_PER_THREAD || layout > GB_INSTANCE_PER_BRANCH)
     return set_error(GB_ERR_INVALID_ARGUMENT, "unknown layout");
+  if (layout == GB_INSTANCE_PER_BRANCH && function != GB_FUNC_RNEA && function != GB_FUNC_ABA)
+    return set_error(GB_ERR_UNSUPPORTED, "the lane-per-branch layout exists for RNEA and ABA");
   if (layout == GB_INSTANCE_PER_WARP && function != GB_FUNC_RNEA && function != GB_FUNC_ABA &&
       function != GB_FUNC_ABA_DERIVATIVES)
     return set_error(GB_ERR_UNSUPPORTED, "the warp-per-instance layout exists for RNEA, ABA and the ABA derivatives");

@@ -43,6 +43,9 @@ int launch_aba(const gb_model* m, int precision, long B, Arr q, Arr v, Arr tau, 
 // warp-per-instance layout (gb_warp.cu)
 int launch_rnea_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
 int launch_aba_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
+// lane-per-branch layout (gb_warp.cu)
+int launch_rnea_branch(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
+int launch_aba_branch(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
 int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q, Arr M, Arr U, Arr D, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);

@@ -131,6 +131,7 @@ int launch_common(const gb_model* M, long B, cudaStream_t st, K kernel, const ch
 int launch_rnea(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st) {
   constexpr int GB_FUNC_ID = GB_FUNC_RNEA;
   if (M->layout[GB_FUNC_ID] == GB_INSTANCE_PER_WARP) return launch_rnea_warp(M, precision, B, q, v, a, tau, st);
+  if (M->layout[GB_FUNC_ID] == GB_INSTANCE_PER_BRANCH) return launch_rnea_branch(M, precision, B, q, v, a, tau, st);
   if (precision == GB_FP64) {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_rnea<double, C>), q, v, a, tau));
   } else {
@@ -141,6 +142,7 @@ int launch_rnea(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, A
 int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st) {
   constexpr int GB_FUNC_ID = GB_FUNC_ABA;
   if (M->layout[GB_FUNC_ID] == GB_INSTANCE_PER_WARP) return launch_aba_warp(M, precision, B, q, v, tau, ddq, st);
+  if (M->layout[GB_FUNC_ID] == GB_INSTANCE_PER_BRANCH) return launch_aba_branch(M, precision, B, q, v, tau, ddq, st);
   if (precision == GB_FP64) {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C>), q, v, tau, ddq));
   } else {

@@ -31,6 +31,9 @@ struct BlobHeader {
   int stage_bytes;  // [0, stage_bytes): what the per-instance kernels stage (rel_list and the groups lie beyond)
   int o_i6_d, o_i6_f, o_place_df, o_iner_df;
   int o_arm_df, o_zero, pad8;  // o_zero: 16 zero bytes (a zero vector with stride 0)
+  // chains: maximal runs of joints each the only child of the previous one (consecutive in the
+  // depth-first order); chain c holds joints chain[3c] .. chain[3c+1] at chain level chain[3c+2]
+  int o_chain, nchain, nclevel, chain_team;
   double grav_d[6];
   float grav_f[6];
   float padf[2];
@@ -42,6 +45,8 @@ struct MView {
   int nj, nq, nv, max_depth, has_ff, nslot;
   const int *parent, *jtype, *idx_q, *idx_v, *nvsub, *depth, *pfr, *nsfr, *rel_off, *rel_list, *slot, *dof_joint, *bslot, *grp, *grp_rel;
   int nbranch, ngroup;
+  const int* chain;  // (first joint, last joint, level) per chain
+  int nchain, nclevel;
   const double *place_d, *iner_d, *arm_d, *grav_d, *i6_d;
   const float *place_f, *iner_f, *arm_f, *grav_f, *i6_f;
   const dfloat *place_df, *iner_df, *arm_df, *grav_df;
@@ -68,6 +73,9 @@ GB_HD MView make_view(const unsigned char* base) {
   m.grp = reinterpret_cast<const int*>(base + h->o_grp);
   m.grp_rel = reinterpret_cast<const int*>(base + h->o_grp_rel);
   m.ngroup = h->ngroup;
+  m.chain = reinterpret_cast<const int*>(base + h->o_chain);
+  m.nchain = h->nchain;
+  m.nclevel = h->nclevel;
   m.place_d = reinterpret_cast<const double*>(base + h->o_place_d);
   m.iner_d = reinterpret_cast<const double*>(base + h->o_iner_d);
   m.arm_d = reinterpret_cast<const double*>(base + h->o_arm_d);

@@ -24,6 +24,7 @@ struct gb_model {
   unsigned char* d_blob = nullptr;  // device copy (owned by the C ABI)
   int blob_bytes = 0;
   int stage_bytes = 0;  // prefix of the blob the per-instance kernels copy into shared memory
+  int chain_team = 4;   // lanes per configuration of the lane-per-branch layout
 };
 
 namespace gbm {
@@ -136,6 +137,35 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.o_parent = take(4 * nj); h.o_jtype = take(4 * nj); h.o_idxq = take(4 * nj); h.o_idxv = take(4 * nj);
   h.o_nvsub = take(4 * nj); h.o_depth = take(4 * nj); h.o_pfr = take(4 * nv); h.o_nsfr = take(4 * nv);
   h.o_rel_off = take(4 * (nv + 1)); h.o_slot = take(4 * nj); h.o_dofj = take(4 * nv); h.o_bslot = take(4 * nj);
+  // chains of the lane-per-branch layout
+  std::vector<int> chain;
+  {
+    std::vector<int> nch(nj, 0), chain_of(nj, -1);
+    for (int i = 1; i < nj; ++i) ++nch[M->parents[i]];
+    int nclevel = 0;
+    for (int i = 1; i < nj; ++i) {
+      const int p = M->parents[i];
+      if (p > 0 && nch[p] == 1) {  // continues the parent's chain (i == p + 1 in depth-first order)
+        chain_of[i] = chain_of[p];
+        chain[3 * chain_of[i] + 1] = i;
+      } else {
+        chain_of[i] = (int)chain.size() / 3;
+        const int level = p > 0 ? chain[3 * chain_of[p] + 2] + 1 : 0;
+        chain.insert(chain.end(), {i, i, level});
+        nclevel = std::max(nclevel, level + 1);
+      }
+    }
+    h.nchain = (int)chain.size() / 3;
+    h.nclevel = nclevel;
+    std::vector<int> per_level(std::max(nclevel, 1), 0);
+    for (int c = 0; c < h.nchain; ++c) ++per_level[chain[3 * c + 2]];
+    const int widest = *std::max_element(per_level.begin(), per_level.end());
+    int ts = 4;  // lanes per configuration: the widest chain level, in powers of two from 4 to 32
+    while (ts < widest && ts < 32) ts *= 2;
+    h.chain_team = ts;
+    M->chain_team = ts;
+  }
+  h.o_chain = take(4 * chain.size() + 4);
   // column groups of the -Minv*dtau products (filled below)
   std::vector<int> grp, grp_rel;
   for (int c = 0; c < nv;) {
@@ -190,6 +220,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.nbranch = nb;
   std::memcpy(b, &h, sizeof(h));
   put_i(h.o_bslot, bslot);
+  put_i(h.o_chain, chain);
   put_i(h.o_grp, grp);
   put_i(h.o_grp_rel, grp_rel);
   put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);

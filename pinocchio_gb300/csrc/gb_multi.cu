@@ -69,11 +69,11 @@ __global__ void k_multi(TaskTable tab, int tile, int blob_region, int warp_regio
       const gb::In x = warp::w_in(Arr{T.x, T.nv, 1}, b);
       const gb::Out o = warp::w_out(Arr{T.out, T.nv, 1}, b);
       if (T.function == GB_FUNC_RNEA) {
-        warp::rnea_warp_one<S>(m, q, v, x, o, reinterpret_cast<S*>(region), lane);
+        warp::rnea_warp_one<S>(m, q, v, x, o, reinterpret_cast<S*>(region), warp::LevelSched{lane});
       } else {
         const size_t per_s = warp::align16(sizeof(S) * warp::aba_words_s<S, SS>() * (size_t)m.nj);
         warp::aba_warp_one<S, SS>(m, q, v, x, o, reinterpret_cast<S*>(region), reinterpret_cast<SS*>(region + per_s),
-                                  lane);
+                                  warp::LevelSched{lane});
       }
       __syncwarp();
       continue;

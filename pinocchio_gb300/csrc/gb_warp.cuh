@@ -24,12 +24,53 @@ __device__ __forceinline__ gb::Out w_out(const Arr& a, long b) {
 }
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+// Who evaluates which joint when.  LevelSched: a warp per configuration, lane j
+// takes joints j, j + 32, ...; one step per tree depth (all joints of a depth at
+// once).  BranchSched<TS>: a team of TS lanes per configuration, one lane per
+// chain (a maximal run of joints each the only child of the previous one); one
+// step per chain level, each lane walking its chain joint by joint (down the
+// chain in the forward passes, up in the backward ones).  In both, a joint's
+// parent and children are done in an earlier step or earlier by the same lane,
+// and the per-joint code is the same.
+struct LevelSched {
+  int lane;
+  __device__ int steps(const gb::MView& m) const { return m.max_depth; }
+  template <class F> __device__ void all(const gb::MView& m, F f) const {
+    for (int i = 1 + lane; i < m.nj; i += 32) f(i);
+  }
+  template <class F> __device__ void down(const gb::MView& m, int step, F f) const {
+    for (int i = 1 + lane; i < m.nj; i += 32)
+      if (m.depth[i] == step) f(i);
+  }
+  template <class F> __device__ void up(const gb::MView& m, int step, F f) const { down(m, step, f); }
+  __device__ void sync() const { __syncwarp(); }
+};
+template <int TS> struct BranchSched {
+  int rank;
+  unsigned mask;  // the team's lanes
+  __device__ int steps(const gb::MView& m) const { return m.nclevel; }
+  template <class F> __device__ void all(const gb::MView& m, F f) const {
+    for (int i = 1 + rank; i < m.nj; i += TS) f(i);
+  }
+  template <class F> __device__ void down(const gb::MView& m, int step, F f) const {
+    for (int c = rank; c < m.nchain; c += TS)
+      if (m.chain[3 * c + 2] == step - 1)
+        for (int i = m.chain[3 * c]; i <= m.chain[3 * c + 1]; ++i) f(i);
+  }
+  template <class F> __device__ void up(const gb::MView& m, int step, F f) const {
+    for (int c = rank; c < m.nchain; c += TS)
+      if (m.chain[3 * c + 2] == step - 1)
+        for (int i = m.chain[3 * c + 1]; i >= m.chain[3 * c]; --i) f(i);
+  }
+  __device__ void sync() const { __syncwarp(mask); }
+};
+
 // shared-memory scalars per joint of one warp's region
 template <class S> constexpr int rnea_words() { return 12 + 6 * 4; }  // X, vel, acc, f, child force
 
-template <class S>
+template <class S, class Sched>
 __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In& v, const gb::In& a,
-                              const gb::Out& tau, S* ws, int lane) {
+                              const gb::Out& tau, S* ws, const Sched& sc) {
   using namespace gb;
   const int nj = m.nj;
   X3<S>* X = reinterpret_cast<X3<S>*>(ws);
@@ -39,11 +80,10 @@ __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In&
   M6<S>* cf = f + nj;
   const S* g = ModelScalar<S>::grav(m);
   const S* arm = ModelScalar<S>::arm(m);
-  for (int i = 1 + lane; i < nj; i += 32) joint_transform(m, i, q, X[i]);
-  __syncwarp();
-  for (int d = 1; d <= m.max_depth; ++d) {  // forward, level by level (rnea_one's first loop)
-    for (int i = 1 + lane; i < nj; i += 32) {
-      if (m.depth[i] != d) continue;
+  sc.all(m, [&](int i) { joint_transform(m, i, q, X[i]); });
+  sc.sync();
+  for (int d = 1; d <= sc.steps(m); ++d) {  // forward (rnea_one's first loop)
+    sc.down(m, d, [&](int i) {
       const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
       M6<S> vJ, aJ, t, ap, vi, ai;
       joint_motion(jt, v, iv, vJ);
@@ -73,12 +113,11 @@ __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In&
       for (int k = 0; k < 6; ++k) f[i].v[k] = fa.v[k] + fx.v[k];
       vel[i] = vi;
       acc[i] = ai;
-    }
-    __syncwarp();
+    });
+    sc.sync();
   }
-  for (int d = m.max_depth; d >= 1; --d) {  // backward: children folded in by decreasing index
-    for (int i = 1 + lane; i < nj; i += 32) {
-      if (m.depth[i] != d) continue;
+  for (int d = sc.steps(m); d >= 1; --d) {  // backward: children folded in by decreasing index
+    sc.up(m, d, [&](int i) {
       const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
       M6<S> fi = f[i];
       for (int c = nj - 1; c > i; --c)
@@ -92,17 +131,17 @@ __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In&
         tau[iv] = double(pick3(fi.v + 3, jt - JT_RX) + arm[iv] * S(a[iv]));
       }
       if (p > 0) act_force(X[i], fi, cf[i]);
-    }
-    __syncwarp();
+    });
+    sc.sync();
   }
 }
 
 // per joint: X (12 S), vel (6), child inertia (21), child force (6), UDinv (6), acc (6) in S; du in SS
 template <class S, class SS> constexpr int aba_words_s() { return 12 + 6 + 21 + 6 + 6 + 6; }
 
-template <class S, class SS>
+template <class S, class SS, class Sched>
 __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& v, const gb::In& tau,
-                             const gb::Out& ddq, S* ws, SS* wss, int lane) {
+                             const gb::Out& ddq, S* ws, SS* wss, const Sched& sc) {
   using namespace gb;
   const int nj = m.nj;
   X3<S>* X = reinterpret_cast<X3<S>*>(ws);
@@ -118,7 +157,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
   const S* g = ModelScalar<S>::grav(m);
   const double* arm = m.arm_d;
   // pass 1 (AbaLocalConventionForwardStep1, aba.hxx:360-399)
-  for (int i = 1 + lane; i < nj; i += 32) {
+  sc.all(m, [&](int i) {
     if (m.jtype[i] == JT_FF) {
       joint_transform(m, i, q, X[i]);
     } else {
@@ -127,11 +166,10 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
       const S* P = ModelScalar<S>::place(m, i);
       compose_axis(P, P + 9, m.jtype[i] - JT_RX, cn, sn, X[i]);
     }
-  }
-  __syncwarp();
-  for (int d = 1; d <= m.max_depth; ++d) {
-    for (int i = 1 + lane; i < nj; i += 32) {
-      if (m.depth[i] != d) continue;
+  });
+  sc.sync();
+  for (int d = 1; d <= sc.steps(m); ++d) {
+    sc.down(m, d, [&](int i) {
       const int p = m.parent[i];
       M6<S> vJ, t;
       joint_motion(m.jtype[i], v, m.idx_v[i], vJ);
@@ -142,13 +180,12 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
       } else {
         vel[i] = vJ;
       }
-    }
-    __syncwarp();
+    });
+    sc.sync();
   }
   // pass 2 (AbaLocalConventionBackwardStep, aba.hxx:402-434), deepest level first
-  for (int d = m.max_depth; d >= 1; --d) {
-    for (int i = 1 + lane; i < nj; i += 32) {
-      if (m.depth[i] != d) continue;
+  for (int d = sc.steps(m); d >= 1; --d) {
+    sc.up(m, d, [&](int i) {
       const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
       Iner<S> Y;
       load_inertia(m, i, Y);
@@ -212,7 +249,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
             for (int k = 1; k < 6; ++k) s += Ifull[6 * r + k] * D[6 * k + cc];
             UD6[6 * r + cc] = s;
           }
-        continue;
+        return;
       }
       const int ax = jt - JT_RX;
       const SS u = SS(tau[iv]) - cvt<SS>(pick3(f.v + 3, ax));
@@ -237,13 +274,12 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
         sym6_transform(Iaf, X[i], cI[i]);
         act_force(X[i], pa, cf[i]);
       }
-    }
-    __syncwarp();
+    });
+    sc.sync();
   }
   // pass 3 (AbaLocalConventionForwardStep2, aba.hxx:437-468)
-  for (int d = 1; d <= m.max_depth; ++d) {
-    for (int i = 1 + lane; i < nj; i += 32) {
-      if (m.depth[i] != d) continue;
+  for (int d = 1; d <= sc.steps(m); ++d) {
+    sc.down(m, d, [&](int i) {
       const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
       M6<S> ap, a, vJ, c;
       if (p == 0) {
@@ -285,8 +321,8 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
         a.v[5] += ax == 2 ? dds : S(0);
       }
       acc[i] = a;
-    }
-    __syncwarp();
+    });
+    sc.sync();
   }
 }
 

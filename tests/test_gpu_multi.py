@@ -96,7 +96,7 @@ def test_autotuner_keeps_results(tmp_path, monkeypatch):
     q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 3000, 2))
     before = pg.aba(model, data, q, v, x).clone()
     res = autotune.tune(model, data, functions=("aba", "rnea"), batch=4096)
-    assert set(res) == {"aba", "rnea"} and all(t in autotune.CANDIDATES or t == autotune.WARP for t, _ in res.values())
+    assert set(res) == {"aba", "rnea"} and all(t in autotune.CANDIDATES or t in (autotune.WARP, autotune.BRANCH) for t, _ in res.values())
     assert torch.equal(pg.aba(model, data, q, v, x), before)
     again = autotune.tune(model, data, functions=("aba", "rnea"), batch=4096)  # served from the cache
     assert again == {k: (t, ms) for k, (t, ms) in res.items()}
@@ -105,8 +105,8 @@ def test_autotuner_keeps_results(tmp_path, monkeypatch):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100"])
 def test_warp_layout_matches_thread_layout_bitwise(name, precision):
-    """The warp-per-instance layout (gb_model_set_layout) gives the thread layout's
-    results for RNEA, ABA, nonLinearEffects and gravity -- the same bits in FP64,
+    """The warp-per-instance and lane-per-branch layouts (gb_model_set_layout) give
+    the thread layout's results for RNEA, ABA, nonLinearEffects and gravity -- the same bits in FP64,
     FP32 rounding in the mixed kernels (the compiler may contract their FP32
     multiply-adds differently in the two kernels) -- and matches the oracle."""
     import torch
@@ -119,7 +119,8 @@ def test_warp_layout_matches_thread_layout_bitwise(name, precision):
     data = pg.createData(model, precision)
     L = pg._capi.lib()
     outs = {}
-    for layout in (pg._capi.GB_INSTANCE_PER_THREAD, pg._capi.GB_INSTANCE_PER_WARP):
+    layouts = (pg._capi.GB_INSTANCE_PER_THREAD, pg._capi.GB_INSTANCE_PER_WARP, pg._capi.GB_INSTANCE_PER_BRANCH)
+    for layout in layouts:
         for f in (pg._capi.GB_FUNC_RNEA, pg._capi.GB_FUNC_ABA):
             pg._capi.check(L.gb_model_set_layout(data.dev.h, f, layout))
         outs[layout] = [
@@ -128,16 +129,18 @@ def test_warp_layout_matches_thread_layout_bitwise(name, precision):
             pg.nonLinearEffects(model, data, d(q), d(v)).cpu().numpy(),
             pg.computeGeneralizedGravity(model, data, d(q)).cpu().numpy(),
         ]
-    for k, (a, b) in enumerate(zip(outs[0], outs[1])):
-        if precision == "fp64":
-            assert np.array_equal(a, b), k
-        else:
-            assert rel_err(b, a) < 1e-6, (k, rel_err(b, a))
+    for layout in layouts[1:]:
+        for k, (a, b) in enumerate(zip(outs[layouts[0]], outs[layout])):
+            if precision == "fp64":
+                assert np.array_equal(a, b), (layout, k)
+            else:
+                assert rel_err(b, a) < 1e-6, (layout, k, rel_err(b, a))
     om = OracleModel(model)
     tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else MIXED_TOL
     if precision == "fp64" or name != "chain100":
-        assert rel_err(outs[1][0], om.rnea(q, v, x)) < tol
-        assert rel_err(outs[1][1], om.aba(q, v, 10.0 * x, LOCAL)) < tol
+        for layout in layouts[1:]:
+            assert rel_err(outs[layout][0], om.rnea(q, v, x)) < tol
+            assert rel_err(outs[layout][1], om.aba(q, v, 10.0 * x, LOCAL)) < tol
 
 
 def test_layout_setting_errors():
@@ -147,6 +150,7 @@ def test_layout_setting_errors():
     assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_CRBA, pg._capi.GB_INSTANCE_PER_WARP) == pg._capi.GB_ERR_UNSUPPORTED
     assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_RNEA, 5) == pg._capi.GB_ERR_INVALID_ARGUMENT
     assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_ABA, pg._capi.GB_INSTANCE_PER_8_LANES) == pg._capi.GB_ERR_UNSUPPORTED
+    assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_CRBA, pg._capi.GB_INSTANCE_PER_BRANCH) == pg._capi.GB_ERR_UNSUPPORTED
     assert L.gb_model_set_layout(data.dev.h, pg._capi.GB_FUNC_ABA_DERIVATIVES, pg._capi.GB_INSTANCE_PER_4_LANES) == pg._capi.GB_OK
 
 
