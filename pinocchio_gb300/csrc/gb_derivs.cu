@@ -429,17 +429,7 @@ struct Workspace {
 };
 int ws_alloc(Workspace& w, size_t bytes, cudaStream_t st) {
   w.st = st;
-  static bool pool_tuned = false;
-  if (!pool_tuned) {  // keep freed blocks in the pool: repeated calls reuse them
-    int dev = 0;
-    cudaMemPool_t pool;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-      unsigned long long thr = ~0ull;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    }
-    pool_tuned = true;
-  }
-  return cuda_error(cudaMallocAsync(&w.p, bytes, st), "workspace allocation");
+  return scratch_alloc(&w.p, bytes, st);
 }
 
 #ifndef GB_PROD_PIPE
@@ -534,18 +524,34 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   if (rc != GB_OK) return rc;
   rc = blob_smem(M, (const void*)k_rnea_derivs<S>, "k_rnea_derivs");
   if (rc != GB_OK) return rc;
+  // instance-layout matrices of a large batch are written coalesced into an SOA scratch, then transposed
+  const long nn = (long)M->nv * M->nv;
+  const bool staged = dq.es == 1 && B >= kSoaStagingMin;
+  Workspace soa;
+  Arr mats[3] = {dq, dv, Mo};
+  if (staged) {
+    rc = ws_alloc(soa, sizeof(double) * 3 * (size_t)nn * B, st);
+    if (rc != GB_OK) return rc;
+    for (int k = 0; k < 3; ++k) mats[k] = Arr{static_cast<double*>(soa.p) + (size_t)k * nn * B, 1, B};
+  }
   // the three matrices are cleared with full-bandwidth memsets; the kernel writes their non-zero entries
-  const size_t nn = (size_t)M->nv * M->nv * sizeof(double) * (size_t)B;
-  for (const Arr* a : {&dq, &dv, &Mo}) {
-    rc = cuda_error(cudaMemsetAsync(const_cast<double*>(a->p), 0, nn, st), "cudaMemsetAsync");
+  for (const Arr& a : mats) {
+    rc = cuda_error(cudaMemsetAsync(const_cast<double*>(a.p), 0, sizeof(double) * (size_t)nn * B, st), "cudaMemsetAsync");
     if (rc != GB_OK) return rc;
   }
   const int tpb = M->tpb[GB_FUNC_RNEA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
   k_rnea_derivs<S><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
-                                                                   static_cast<S*>(ws.p), symmetric, q, v, a, dq, dv,
-                                                                   Mo, tau);
-  return cuda_error(cudaGetLastError(), "k_rnea_derivs");
+                                                                   static_cast<S*>(ws.p), symmetric, q, v, a, mats[0],
+                                                                   mats[1], mats[2], tau);
+  rc = cuda_error(cudaGetLastError(), "k_rnea_derivs");
+  if (rc != GB_OK || !staged) return rc;
+  const Arr outs[3] = {dq, dv, Mo};
+  for (int k = 0; k < 3; ++k) {
+    rc = launch_soa_to_instance(mats[k].p, B, nn, outs[k], st);
+    if (rc != GB_OK) return rc;
+  }
+  return GB_OK;
 }
 
 // The three sweep kernels of the ABA derivatives on a workspace laid out by

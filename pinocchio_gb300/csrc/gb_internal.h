@@ -51,6 +51,13 @@ int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);
 size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B);
+// device scratch from the stream-ordered pool, and the SOA -> instance transpose (gb_util.cu):
+// src holds n elements x B configurations ([element][configuration]), dst an instance-layout array
+int scratch_alloc(void** p, size_t bytes, cudaStream_t st);
+void scratch_free(void* p, cudaStream_t st);
+int launch_soa_to_instance(const double* src, long B, long n, Arr dst, cudaStream_t st);
+// batches from which the matrix outputs of the per-thread kernels go through an SOA scratch
+constexpr long kSoaStagingMin = 1024;
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
                                    Arr Minv, Arr ddq, void* ws, cudaStream_t st);
 

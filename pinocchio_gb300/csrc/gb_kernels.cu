@@ -153,6 +153,20 @@ int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, 
 int launch_crba(const gb_model* M, int precision, bool symmetric, long B, Arr q, Arr Mo, Arr U, Arr D,
                 cudaStream_t st) {
   constexpr int GB_FUNC_ID = GB_FUNC_CRBA;
+  // instance-layout matrices of a large batch are written coalesced into an SOA scratch, then transposed
+  if (Mo.es == 1 && B >= kSoaStagingMin) {
+    const long nn = (long)M->nv * M->nv;
+    void* scratch = nullptr;
+    int rc = scratch_alloc(&scratch, sizeof(double) * (U.p ? 2 : 1) * (size_t)nn * B, st);
+    if (rc != GB_OK) return rc;
+    double* ms = static_cast<double*>(scratch);
+    const Arr Ms{ms, 1, B}, Us{U.p ? ms + (size_t)nn * B : nullptr, 1, B};
+    rc = launch_crba(M, precision, symmetric, B, q, Ms, Us, D, st);
+    if (rc == GB_OK) rc = launch_soa_to_instance(Ms.p, B, nn, Mo, st);
+    if (rc == GB_OK && U.p) rc = launch_soa_to_instance(Us.p, B, nn, U, st);
+    scratch_free(scratch, st);
+    return rc;
+  }
   // M and U are cleared here with full-bandwidth memsets; the kernel writes their non-zero entries
   const size_t nn = (size_t)M->nv * M->nv * sizeof(double) * (size_t)B;
   int rc = cuda_error(cudaMemsetAsync(const_cast<double*>(Mo.p), 0, nn, st), "cudaMemsetAsync(M)");

@@ -180,3 +180,46 @@ def test_aba_derivatives_large_batch_matches_slices(precision):
     n = C.c_uint(7)
     _capi.check(_capi.lib().gb_pipeline_timeouts(C.byref(n), 0))
     assert n.value == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_staged_matrix_outputs_match_soa(precision):
+    """From 1024 configurations the instance-layout matrices of computeRNEADerivatives
+    and of the CRBA (with its Cholesky factors) are written into an SOA scratch and
+    transposed: the same bits as the SOA layout the kernels write directly, and as a
+    small batch of the same configurations."""
+    import torch
+
+    model = MODELS["humanoid32"]()
+    B, nv = 1500, model.nv
+    q, v, a = sm.random_inputs(model, B, 19)
+    dev = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()  # noqa: E731
+    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    data = pg.createData(model, precision)
+    prec = _capi.GB_FP64 if precision == "fp64" else _capi.GB_MIXED
+    L = _capi.lib()
+    inst = [torch.empty((B, nv, nv), dtype=torch.float64, device="cuda") for _ in range(3)]
+    soa = [torch.empty((nv * nv, B), dtype=torch.float64, device="cuda") for _ in range(3)]
+    qi, vi, ai = dev(q), dev(v), dev(a)  # kept alive until the kernels have run
+    qs, vs, as_ = dev(q.T), dev(v.T), dev(a.T)
+    _capi.check(L.gb_rnea_derivatives(data.dev.h, prec, _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_INSTANCE, B,
+                                      ptr(qi), ptr(vi), ptr(ai), ptr(inst[0]), ptr(inst[1]), ptr(inst[2]), None, None))
+    _capi.check(L.gb_rnea_derivatives(data.dev.h, prec, _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_SOA, B,
+                                      ptr(qs), ptr(vs), ptr(as_), ptr(soa[0]), ptr(soa[1]), ptr(soa[2]), None, None))
+    small = pg.computeRNEADerivatives(model, data, dev(q[:37]), dev(v[:37]), dev(a[:37]))
+    torch.cuda.synchronize()
+    for i, s, sm_ in zip(inst, soa, small):
+        assert torch.equal(i, s.T.reshape(B, nv, nv))
+        assert torch.equal(i[:37], sm_)
+    Mi, Ui = (torch.empty((B, nv, nv), dtype=torch.float64, device="cuda") for _ in range(2))
+    Di = torch.empty((B, nv), dtype=torch.float64, device="cuda")
+    Ms, Us = (torch.empty((nv * nv, B), dtype=torch.float64, device="cuda") for _ in range(2))
+    Ds = torch.empty((nv, B), dtype=torch.float64, device="cuda")
+    for lay, qq, outs in ((_capi.GB_LAYOUT_INSTANCE, qi, (Mi, Ui, Di)), (_capi.GB_LAYOUT_SOA, qs, (Ms, Us, Ds))):
+        _capi.check(L.gb_crba(data.dev.h, prec, _capi.GB_LOCAL, _capi.GB_MATRIX_UPPER, lay, B, ptr(qq), ptr(outs[0]),
+                              ptr(outs[1]), ptr(outs[2]), None))
+    torch.cuda.synchronize()
+    assert torch.equal(Mi, Ms.T.reshape(B, nv, nv)) and torch.equal(Ui, Us.T.reshape(B, nv, nv))
+    assert torch.equal(Di, Ds.T)
+    _, _, _, M_o = OracleModel(model).rnea_derivatives(q[:64], v[:64], a[:64])
+    assert rel_err(Mi[:64].cpu().numpy(), M_o) < (FP64_TOL if precision == "fp64" else MIXED_TOL)
