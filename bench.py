@@ -337,6 +337,12 @@ def run_ours(args, world, rank, local, dist):
         "ddq2": torch.empty((B, nv), dtype=torch.float64, device="cuda"),
     }
     data = {p: pg.createData(model, p) for p in ("fp64", "mixed")}
+    # both precisions run in the launch settings the autotuner finds best at this batch, so that the
+    # plain FP64 kernels are compared at their best
+    from pinocchio_gb300 import autotune
+
+    tuned = {p: autotune.tune(model, data[p], functions=("aba", "aba_derivatives"), batch=B, use_cache=False)
+             for p in ("fp64", "mixed")}
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     PREC = {"fp64": _capi.GB_FP64, "mixed": _capi.GB_MIXED}
 
@@ -512,6 +518,8 @@ def run_ours(args, world, rank, local, dist):
             "precision": "mixed",
             "parallelism": f"replicas x{world} (instances shard, no exchange step)",
             "l2": "inputs rotate over 4 copies (4 x 51 MB) and every step writes 1.6 GB of outputs (> 129 MB L2)",
+            "launch_settings": {p: {f: (t if isinstance(t, str) else f"thread x{t}") for f, (t, _) in tuned[p].items()}
+                                for p in tuned},
         },
         "fp64": {"value": value_fp64, "unit": "evals/s", "ms_per_step": ms_fp64},
         "mixed_over_fp64": value / value_fp64,

@@ -86,6 +86,10 @@ const char* gb_last_error(void);
  * means some outputs of those calls were not written.  Synchronises the
  * device. */
 int gb_pipeline_timeouts(unsigned int* count, int reset);
+/* Exercises that failure path without a fault: one warp waits limit_us
+ * microseconds (1..100000) on a barrier nothing arrives on and records one
+ * timeout in the count above; the context stays usable. */
+int gb_pipeline_wait_selftest(unsigned int limit_us, void* stream);
 
 /* tau = rnea(model, data, q, v, a) for every instance
  * (reference algorithm/rnea.hxx:117-161, public rnea.hxx:766). */

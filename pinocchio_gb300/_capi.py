@@ -30,6 +30,7 @@ EXPORTS = (
     "gb_model_dims",
     "gb_last_error",
     "gb_pipeline_timeouts",
+    "gb_pipeline_wait_selftest",
     "gb_rnea",
     "gb_nonlinear_effects",
     "gb_generalized_gravity",
@@ -124,6 +125,7 @@ def lib():
         L.gb_model_destroy.argtypes = [vp]
         L.gb_model_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
         L.gb_pipeline_timeouts.argtypes = [C.POINTER(C.c_uint), i]
+        L.gb_pipeline_wait_selftest.argtypes = [C.c_uint, vp]
         L.gb_rnea.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp]
         L.gb_nonlinear_effects.argtypes = [vp, i, i, l, vp, vp, vp, vp]
         L.gb_generalized_gravity.argtypes = [vp, i, i, l, vp, vp, vp]

@@ -393,6 +393,20 @@ __global__ void __launch_bounds__((GB_PROD_CWARPS + GB_PROD_PWARPS) * 32, 1)
   }
 }
 
+// The bounded wait's failure path, exercised without a fault: one warp waits on an
+// mbarrier that nothing arrives on, gives up after limit_ns and records the timeout
+// exactly as the pipeline's warps do.
+__global__ void k_wait_selftest(unsigned long long limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    gb::mbar_init(&bar, 1);
+    gb::fence_mbar_init();
+  }
+  __syncwarp();
+  const bool ok = gb::mbar_wait(&bar, 0u, limit_ns);
+  if (!__any_sync(0xffffffffu, ok) && threadIdx.x == 0) atomicAdd(&g_pipe_timeouts, 1u);
+}
+
 // Longest-processing-time assignment of the product tasks to nwarps warps.
 bool make_prod_plan(const gb_model* M, int nwarps, ProdPlan& plan) {
   const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
@@ -735,6 +749,12 @@ int gb_pipeline_timeouts(unsigned int* count, int reset) {
     GB_TRY(gbi::cuda_error(cudaMemcpyToSymbol(gbi::g_pipe_timeouts, &zero, sizeof(unsigned int)), "gb_pipeline_timeouts"));
   }
   return GB_OK;
+}
+
+int gb_pipeline_wait_selftest(unsigned int limit_us, void* stream) {
+  if (limit_us == 0 || limit_us > 100000) return gbi::set_error(GB_ERR_INVALID_ARGUMENT, "limit_us must be in 1..100000");
+  gbi::k_wait_selftest<<<1, 32, 0, (cudaStream_t)stream>>>(1000ull * limit_us);
+  return gbi::cuda_error(cudaGetLastError(), "k_wait_selftest");
 }
 
 int gb_rnea_derivatives(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,

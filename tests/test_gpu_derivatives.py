@@ -223,3 +223,27 @@ def test_staged_matrix_outputs_match_soa(precision):
     assert torch.equal(Di, Ds.T)
     _, _, _, M_o = OracleModel(model).rnea_derivatives(q[:64], v[:64], a[:64])
     assert rel_err(Mi[:64].cpu().numpy(), M_o) < (FP64_TOL if precision == "fp64" else MIXED_TOL)
+
+
+def test_pipeline_wait_timeout_is_reported_and_recoverable():
+    """The bounded mbarrier wait of the pipelined kernels gives up, records the
+    timeout (gb_pipeline_timeouts) and leaves the context usable: a barrier that
+    nothing arrives on, waited on for 2 ms."""
+    import torch
+
+    L = _capi.lib()
+    n = C.c_uint(0)
+    _capi.check(L.gb_pipeline_timeouts(C.byref(n), 1))  # read and reset
+    _capi.check(L.gb_pipeline_wait_selftest(2000, None))
+    _capi.check(L.gb_pipeline_timeouts(C.byref(n), 1))
+    assert n.value == 1
+    assert L.gb_pipeline_wait_selftest(0, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    model = MODELS["humanoid32"]()
+    q, v, x = sm.random_inputs(model, 64, 2)
+    data = pg.createData(model, "mixed")
+    dev = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    dq, dv, Minv = (t.cpu().numpy() for t in pg.computeABADerivatives(model, data, dev(q), dev(v), dev(10.0 * x)))
+    _, dq_o, _, _ = OracleModel(model).aba_derivatives(q, v, 10.0 * x)
+    assert rel_err(dq, dq_o) < MIXED_TOL
+    _capi.check(L.gb_pipeline_timeouts(C.byref(n), 0))
+    assert n.value == 0
