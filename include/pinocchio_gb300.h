@@ -44,7 +44,19 @@ enum {
 enum { GB_FP64 = 0, GB_MIXED = 1 };               /* arithmetic of the kernels  */
 enum { GB_LOCAL = 0, GB_WORLD = 1 };              /* reference multibody/fwd.hpp:73-81 */
 enum { GB_LAYOUT_INSTANCE = 0, GB_LAYOUT_SOA = 1 };
-enum { GB_JOINT_NONE = 0, GB_JOINT_RX = 1, GB_JOINT_RY = 2, GB_JOINT_RZ = 3, GB_JOINT_FREEFLYER = 4 };
+/* joint types: revolute about x / y / z (JointModelRX/RY/RZ, multibody/joint/joint-revolute.hpp),
+ * the free-flyer (JointModelFreeFlyer, joint-free-flyer.hpp; root joint only), prismatic along
+ * x / y / z (JointModelPX/PY/PZ, joint-prismatic.hpp) */
+enum {
+  GB_JOINT_NONE = 0,
+  GB_JOINT_RX = 1,
+  GB_JOINT_RY = 2,
+  GB_JOINT_RZ = 3,
+  GB_JOINT_FREEFLYER = 4,
+  GB_JOINT_PX = 5,
+  GB_JOINT_PY = 6,
+  GB_JOINT_PZ = 7
+};
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
 /* functions of a heterogeneous batch task / of a launch setting */
 enum { GB_FUNC_RNEA = 0, GB_FUNC_ABA = 1, GB_FUNC_CRBA = 2, GB_FUNC_RNEA_DERIVATIVES = 3, GB_FUNC_ABA_DERIVATIVES = 4 };

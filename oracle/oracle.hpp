@@ -35,7 +35,7 @@
 
 namespace orc {
 
-enum JointType { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4 };
+enum JointType { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7 };
 enum Convention { LOCAL = 0, WORLD = 1 };  // reference multibody/fwd.hpp:73-81
 
 // ---------------------------------------------------------------------------
@@ -81,7 +81,7 @@ struct Model {
         if (jtype[0] != JT_NONE) throw std::invalid_argument("joint 0 must be the universe");
         continue;
       }
-      if (jtype[i] < JT_RX || jtype[i] > JT_FF) throw std::invalid_argument("unsupported joint type");
+      if (jtype[i] < JT_RX || jtype[i] > JT_PZ) throw std::invalid_argument("unsupported joint type");
       if (parents[i] < 0 || parents[i] >= i) throw std::invalid_argument("parents[i] must be < i");
       nqs[i] = joint_nq(jtype[i]);
       nvs[i] = joint_nv(jtype[i]);
@@ -532,6 +532,8 @@ template <class T> inline Iner<T> inertia_of(const Model& m, int i) {
 // Joint transform M(q).
 //  * revolute: TransformRevoluteTpl::_setRotation (joint-revolute.hpp:213-235),
 //    angle through SINCOS (math/sincos.hpp:27-55); calc at joint-revolute.hpp:811-821.
+//  * prismatic: translation q[0] along the axis, identity rotation
+//    (TransformPrismaticTpl, joint-prismatic.hpp:232-284; calc at 700-704).
 //  * free-flyer: translation q[0:3], rotation = Eigen Quaternion::matrix()
 //    of (x,y,z,w) = q[3:7], not normalised (joint-free-flyer.hpp:333-375).
 template <class T> inline SE3<T> joint_transform(int jt, const T* q) {
@@ -550,27 +552,34 @@ template <class T> inline SE3<T> joint_transform(int jt, const T* q) {
     for (int k = 0; k < 3; ++k) M.t[k] = q[k];
     return M;
   }
+  for (int k = 0; k < 3; ++k) M.R[4 * k] = T(1);
+  if (jt >= JT_PX) {
+    M.t[jt - JT_PX] = q[0];
+    return M;
+  }
   T s, c;
   o_sincos(q[0], &s, &c);
-  for (int k = 0; k < 3; ++k) M.R[4 * k] = T(1);
   if (jt == JT_RX) { M.R[4] = c; M.R[5] = -s; M.R[7] = s; M.R[8] = c; }
   if (jt == JT_RY) { M.R[0] = c; M.R[2] = s; M.R[6] = -s; M.R[8] = c; }
   if (jt == JT_RZ) { M.R[0] = c; M.R[1] = -s; M.R[3] = s; M.R[4] = c; }
   return M;
 }
-inline int rev_axis(int jt) { return jt - JT_RX; }
+// The motion-subspace entry of a one-dof joint: the angular axis 3 + a of a
+// revolute joint (SpatialAxis<ANGULAR + axis>, joint-revolute.hpp:429-543), the
+// linear axis a of a prismatic one (SpatialAxis<LINEAR + axis>, joint-prismatic.hpp:353-461).
+inline int motion_index(int jt) { return jt >= JT_PX ? jt - JT_PX : 3 + (jt - JT_RX); }
 // Column k of the joint motion subspace S (local frame).
 template <class T> inline Vec6<T> S_col(int jt, int k) {
   Vec6<T> s = zero6<T>();
   if (jt == JT_FF) s.v[k] = T(1);
-  else s.v[3 + rev_axis(jt)] = T(1);
+  else s.v[motion_index(jt)] = T(1);
   return s;
 }
 // Joint velocity vJ = S * qdot_j.
 template <class T> inline Vec6<T> joint_velocity(int jt, const T* v) {
   Vec6<T> o = zero6<T>();
   if (jt == JT_FF) for (int k = 0; k < 6; ++k) o.v[k] = v[k];
-  else o.v[3 + rev_axis(jt)] = v[0];
+  else o.v[motion_index(jt)] = v[0];
   return o;
 }
 
@@ -705,8 +714,8 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
             for (int k = 1; k < 6; ++k) s += UDinv[6 * r + k] * U[6 * c + k];
             Ia.a[6 * r + c] -= s;
           }
-    } else {  // JointModelRevolute::calc_aba (joint-revolute.hpp:823-834)
-      const int ax = 3 + rev_axis(jt);
+    } else {  // JointModelRevolute::calc_aba (joint-revolute.hpp:823-834), prismatic (joint-prismatic.hpp:728-740)
+      const int ax = motion_index(jt);
       for (int r = 0; r < 6; ++r) U[r] = Ia.a[6 * r + ax];
       Dinv[0] = T(1) / (Ia.a[6 * ax + ax] + T(m.armature[iv]));
       for (int r = 0; r < 6; ++r) UDinv[r] = U[r] * Dinv[0];
@@ -1271,7 +1280,7 @@ void joint_jacobians(const Model& m, Data<T>& d, const T* q) {
 // integrate(q, v) for the supported joints: free-flyer through the SE(3)
 // exponential (multibody/liegroup/special-euclidean.hpp:660-699,
 // spatial/explog-quaternion.hpp:20-147, math/quaternion.hpp:90-111); revolute
-// joints are a vector space (q + v).
+// and prismatic joints are a vector space (q + v).
 // ---------------------------------------------------------------------------
 template <class T>
 void integrate(const Model& m, const T* q, const T* v, T* qout) {

@@ -12,7 +12,7 @@ the nv x nv Jacobians (O(nv^2) per instance instead of the O(nv^3) products).
 (semi-implicit Euler) for all time steps and, with ``checkpoint_every = k``,
 stores only every k-th state for the backward pass and recomputes the steps
 inside a segment (torch.utils.checkpoint).  The wrapper supports models whose
-configuration space is a vector space (revolute joints only, nq == nv), as the
+configuration space is a vector space (revolute and prismatic joints, nq == nv), as the
 100-link chain of the rollout workload is.
 """
 from __future__ import annotations
@@ -43,7 +43,7 @@ class ABAFunction(torch.autograd.Function):
 def aba(model: Model, data: api.Data, q, v, tau):
     """Differentiable batched ABA (q, v, tau: (batch, nv) CUDA float64 tensors)."""
     if model.nq != model.nv:
-        raise ValueError("the autograd wrapper needs a vector-space configuration (revolute joints, nq == nv)")
+        raise ValueError("the autograd wrapper needs a vector-space configuration (revolute / prismatic joints, nq == nv)")
     return ABAFunction.apply(q, v, tau, model, data)
 
 

@@ -291,10 +291,14 @@ template <int NVJ, class S> GB_HD void joint_columns(int jt, const X3<S>& O, S (
     }
   } else {
     S w[3];
-    axis_column(O, jt - JT_RX, w);
-    S tw[3];
-    cross3(O.t, w, tw);
-    Jc[0][0] = tw[0]; Jc[0][1] = tw[1]; Jc[0][2] = tw[2]; Jc[0][3] = w[0]; Jc[0][4] = w[1]; Jc[0][5] = w[2];
+    axis_column(O, jt_axis(jt), w);
+    if (jt_slides(jt)) {  // prismatic: (R e_axis, 0)
+      Jc[0][0] = w[0]; Jc[0][1] = w[1]; Jc[0][2] = w[2]; Jc[0][3] = S(0); Jc[0][4] = S(0); Jc[0][5] = S(0);
+    } else {  // revolute: (t x R e_axis, R e_axis)
+      S tw[3];
+      cross3(O.t, w, tw);
+      Jc[0][0] = tw[0]; Jc[0][1] = tw[1]; Jc[0][2] = tw[2]; Jc[0][3] = w[0]; Jc[0][4] = w[1]; Jc[0][5] = w[2];
+    }
   }
 }
 
@@ -881,7 +885,8 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   K ti[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) ti[k] = zk[L.oM + 12 * i + 9 + k];
-  // joint columns about t_i: a revolute axis passes through t_i; the root free-flyer sits at the origin
+  // joint columns about t_i: a revolute axis passes through t_i, a prismatic column has no
+  // angular part (the same about every point); the root free-flyer sits at the origin
   K Jo[NVJ][6], Jc[NVJ][6];
 #pragma unroll 1
   for (int k = 0; k < NVJ; ++k) {
@@ -889,7 +894,8 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
 #pragma unroll
     for (int r = 0; r < 6; ++r) Jc[k][r] = Jo[k][r];
   }
-  if constexpr (NVJ == 1) Jc[0][0] = Jc[0][1] = Jc[0][2] = K(0);
+  if constexpr (NVJ == 1)
+    if (!jt_slides(m.jtype[i])) Jc[0][0] = Jc[0][1] = Jc[0][2] = K(0);
   K ovp[6] = {K(0), K(0), K(0), K(0), K(0), K(0)}, oap[6], ov[6], oa[6];
   if constexpr (!MINV) {
     if (p > 0) {
@@ -933,7 +939,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   }
   // Minv rows of the joint: -= UDinv^T Fcrb[parent] (columns right of the
   // subtree start from zero); Fcrb[i] = J Minv_rows (+ Fcrb[parent]).  A
-  // free-flyer is a root joint (no parent), so the updated rows are revolute.
+  // free-flyer is a root joint (no parent), so the updated rows are one-dof joints'.
   const long Fi = L.Fslot + 6L * nv * slot[i];
   const long Fp = p > 0 ? L.Fslot + 6L * nv * slot[p] : -1;
   if (p > 0) {
@@ -1044,7 +1050,7 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
 #endif
 constexpr int kRowBlockUnroll = GB_P4_UNROLL;
 
-// One joint of pass 4 with NVJ degrees of freedom (1: revolute, 6: the root
+// One joint of pass 4 with NVJ degrees of freedom (1: revolute or prismatic, 6: the root
 // free-flyer, whose parent is the universe), so that every per-dof loop has a
 // compile-time bound and the per-dof arrays stay in registers.
 template <int NVJ, class S, class T, class K, class P, class Team = Solo>

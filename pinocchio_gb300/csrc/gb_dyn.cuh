@@ -47,8 +47,25 @@ template <class S> GB_HD S eps_of();
 template <> GB_HD double eps_of<double>() { return 2.220446049250313e-16; }
 template <> GB_HD float eps_of<float>() { return 1.1920929e-07f; }
 
+// The configuration parameters of a one-dof joint: (sin, cos) of a revolute
+// angle, (displacement, 1) of a prismatic joint.
+template <class S> GB_HD void joint_params(int jt, S x, S* s, S* c) {
+  if (jt_slides(jt)) {
+    *s = x;
+    *c = S(1);
+  } else {
+    ssincos(x, s, c);
+  }
+}
+// liMi = placement * M_joint of a one-dof joint from its parameters
+template <class S> GB_HD void compose_joint(const S* PR, const S* Pt, int jt, S c, S s, X3<S>& X) {
+  if (jt_slides(jt)) compose_slide(PR, Pt, jt_axis(jt), s, X);
+  else compose_axis(PR, Pt, jt_axis(jt), c, s, X);
+}
+
 // liMi = jointPlacements[i] * M_joint(q)   (rnea.hxx:60, joint calc:
-// revolute joint-revolute.hpp:811-821, free-flyer joint-free-flyer.hpp:333-375)
+// revolute joint-revolute.hpp:811-821, prismatic joint-prismatic.hpp:700-704,
+// free-flyer joint-free-flyer.hpp:333-375)
 template <class S> GB_HD void joint_transform(const MView& m, int i, const In& q, X3<S>& X) {
   const S* P = ModelScalar<S>::place(m, i);
   const int jt = m.jtype[i], iq = m.idx_q[i];
@@ -60,8 +77,8 @@ template <class S> GB_HD void joint_transform(const MView& m, int i, const In& q
     compose(Pl, J, X);
   } else {
     S s, c;
-    ssincos(S(q[iq]), &s, &c);
-    compose_axis(P, P + 9, jt - JT_RX, c, s, X);
+    joint_params(jt, S(q[iq]), &s, &c);
+    compose_joint(P, P + 9, jt, c, s, X);
   }
 }
 // S * x for the joint (x = one value per dof)
@@ -71,10 +88,9 @@ template <class S> GB_HD void joint_motion(int jt, const In& x, int iv, M6<S>& o
     for (int k = 0; k < 6; ++k) o.v[k] = S(x[iv + k]);
   } else {
     const S val = S(x[iv]);
-    o.v[0] = o.v[1] = o.v[2] = S(0);
-    o.v[3] = jt == JT_RX ? val : S(0);
-    o.v[4] = jt == JT_RY ? val : S(0);
-    o.v[5] = jt == JT_RZ ? val : S(0);
+    const int k0 = jt_sidx(jt);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o.v[k] = k == k0 ? val : S(0);
   }
 }
 
@@ -123,7 +139,7 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
 #pragma unroll
       for (int k = 0; k < 6; ++k) tau[iv + k] = double(f[i].v[k] + arm[iv + k] * S(a[iv + k]));
     } else {
-      tau[iv] = double(f[i].v[3 + jt - JT_RX] + arm[iv] * S(a[iv]));
+      tau[iv] = double(pick6(f[i].v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
     }
     if (p > 0) {
       M6<S> fp;
@@ -169,7 +185,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       X = Xff;
     } else {
       const S* P = ModelScalar<S>::place(m, i);
-      compose_axis(P, P + 9, m.jtype[i] - JT_RX, cs[i][1], cs[i][0], X);
+      compose_joint(P, P + 9, m.jtype[i], cs[i][1], cs[i][0], X);
     }
   };
   // pass 1 (AbaLocalConventionForwardStep1, aba.hxx:360-399): transforms and velocities
@@ -181,9 +197,9 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       Xff = X;
     } else {
       S sn, cn;
-      ssincos(S(q[m.idx_q[i]]), &sn, &cn);
+      joint_params(jt, S(q[m.idx_q[i]]), &sn, &cn);
       const S* P = ModelScalar<S>::place(m, i);
-      compose_axis(P, P + 9, jt - JT_RX, cn, sn, X);
+      compose_joint(P, P + 9, jt, cn, sn, X);
       if (!kStoreX) { cs[i][0] = sn; cs[i][1] = cn; }
     }
     if (kStoreX) Xs[kStoreX ? i : 0] = X;
@@ -258,11 +274,12 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
         }
       continue;
     }
-    const int ax = jt - JT_RX;
-    const SS u = SS(tau[iv]) - cvt<SS>(pick3(f.v + 3, ax));
+    // revolute calc_aba (joint-revolute.hpp:823-834), prismatic (joint-prismatic.hpp:728-740)
+    const int sx = jt_sidx(jt);
+    const SS u = SS(tau[iv]) - cvt<SS>(pick6(f.v, sx));
     SS U[6], UD[6];
-    sym6_col(Ia, 3 + ax, U);
-    const SS Dinv = SS(1) / (pick3(U + 3, ax) + SS(arm[iv]));
+    sym6_col(Ia, sx, U);
+    const SS Dinv = SS(1) / (pick6(U, sx) + SS(arm[iv]));
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       UD[k] = U[k] * Dinv;
@@ -325,16 +342,12 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 #pragma unroll
       for (int r = 0; r < 6; ++r) a.v[r] += cvt<S>(dd[r]);
     } else {
-      const int ax = jt - JT_RX;
       S w = UDs[i][0] * a.v[0];
 #pragma unroll
       for (int k = 1; k < 6; ++k) w += UDs[i][k] * a.v[k];
       const SS dd = du[i] - cvt<SS>(w);
       ddq[iv] = double(dd);
-      const S dds = cvt<S>(dd);
-      a.v[3] += ax == 0 ? dds : S(0);
-      a.v[4] += ax == 1 ? dds : S(0);
-      a.v[5] += ax == 2 ? dds : S(0);
+      add_at6(a.v, jt_sidx(jt), cvt<S>(dd));
     }
     const int bs = m.bslot[i];
     if (bs >= 0) aslot[bs] = a;
@@ -379,12 +392,16 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
         J[iv + 3 + k][3] = w[0]; J[iv + 3 + k][4] = w[1]; J[iv + 3 + k][5] = w[2];
       }
     } else {
-      const int ax = jt - JT_RX;
       S w[3], tw[3];
-      axis_column(O, ax, w);
-      cross3(O.t, w, tw);
-      J[iv][0] = tw[0]; J[iv][1] = tw[1]; J[iv][2] = tw[2];
-      J[iv][3] = w[0]; J[iv][4] = w[1]; J[iv][5] = w[2];
+      axis_column(O, jt_axis(jt), w);
+      if (jt_slides(jt)) {  // (R e_axis, 0)
+        J[iv][0] = w[0]; J[iv][1] = w[1]; J[iv][2] = w[2];
+        J[iv][3] = S(0); J[iv][4] = S(0); J[iv][5] = S(0);
+      } else {  // (t x R e_axis, R e_axis)
+        cross3(O.t, w, tw);
+        J[iv][0] = tw[0]; J[iv][1] = tw[1]; J[iv][2] = tw[2];
+        J[iv][3] = w[0]; J[iv][4] = w[1]; J[iv][5] = w[2];
+      }
     }
     Iner<S> Y;
     load_inertia(m, i, Y);
@@ -518,8 +535,7 @@ GB_HD void jacobians_one(const MView& m, const In& q, const Out& J) {
       M6<S> sk, c;
 #pragma unroll
       for (int r = 0; r < 6; ++r) sk.v[r] = S(0);
-      if (jt == JT_FF) sk.v[k] = S(1);
-      else sk.v[3 + jt - JT_RX] = S(1);
+      sk.v[jt == JT_FF ? k : jt_sidx(jt)] = S(1);
       act_motion(oM[i], sk, c);
 #pragma unroll
       for (int r = 0; r < 6; ++r) J[6 * (iv + k) + r] = double(c.v[r]);
@@ -528,7 +544,7 @@ GB_HD void jacobians_one(const MView& m, const In& q, const Out& J) {
 }
 
 // ------------------------------------------------------------------------------------------
-// integrate(q, v): revolute joints q + v; free-flyer through the SE(3)
+// integrate(q, v): revolute and prismatic joints q + v; free-flyer through the SE(3)
 // exponential with the quaternion renormalised to first order (reference
 // multibody/liegroup/special-euclidean.hpp:660-699, spatial/explog-quaternion.hpp:20-147,
 // math/quaternion.hpp:90-111).  Always FP64.

@@ -19,7 +19,14 @@
 
 namespace gb {
 
-enum { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4 };
+enum { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7 };
+
+// One-dof joints (revolute RX/RY/RZ, prismatic PX/PY/PZ): the coordinate axis,
+// whether the joint slides along it, and its entry of the motion subspace S
+// (3 + axis, angular, for a revolute joint; axis, linear, for a prismatic one).
+GB_HD bool jt_slides(int jt) { return jt >= JT_PX; }
+GB_HD int jt_axis(int jt) { return jt >= JT_PX ? jt - JT_PX : jt - JT_RX; }
+GB_HD int jt_sidx(int jt) { return jt >= JT_PX ? jt - JT_PX : jt + 2; }
 
 struct BlobHeader {
   int nj, nq, nv, bytes;

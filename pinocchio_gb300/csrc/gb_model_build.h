@@ -54,7 +54,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   int nq = 0, nv = 0, nff = 0;
   for (int i = 1; i < nj; ++i) {
     const int jt = M->jtype[i], p = M->parents[i];
-    if (jt < GB_JOINT_RX || jt > GB_JOINT_FREEFLYER)
+    if (jt < GB_JOINT_RX || jt > GB_JOINT_PZ)
       return set_error(GB_ERR_UNSUPPORTED, "joint " + std::to_string(i) + ": unsupported joint type");
     if (p < 0 || p >= i) return set_error(GB_ERR_INVALID_ARGUMENT, "parents[i] must satisfy 0 <= parents[i] < i");
     if (jt == GB_JOINT_FREEFLYER) {

@@ -79,6 +79,13 @@ template <class S> GB_HD void axis_column(const X3<S>& O, int ax, S* w) {
 }
 // x[ax] of a 3-vector by selects
 template <class S> GB_HD S pick3(const S* x, int ax) { return ax == 0 ? x[0] : (ax == 1 ? x[1] : x[2]); }
+// x[k] of a 6-vector by selects
+template <class S> GB_HD S pick6(const S* x, int k) { return k < 3 ? pick3(x, k) : pick3(x + 3, k - 3); }
+// x[k] += a for a run-time k, by selects
+template <class S> GB_HD void add_at6(S* x, int k, S a) {
+#pragma unroll
+  for (int r = 0; r < 6; ++r) x[r] += r == k ? a : S(0);
+}
 template <class S> struct Sym6 { S A[6]; S B[9]; S D[6]; };
 
 template <class S> GB_HD void zero(M6<S>& m) {
@@ -133,6 +140,17 @@ template <class S> GB_HD void compose_axis(const S* PR, const S* Pt, int axis, S
     out.R[3 * r + i] = c * pi + s * pj;
     out.R[3 * r + j] = c * pj - s * pi;
     out.t[r] = Pt[r];
+  }
+}
+// Translation of a joint along a unit axis, composed on the right of a placement:
+// liMi = placement * (I, d e_axis)  (prismatic joint, reference joint-prismatic.hpp:232-284,
+// calc 700-704).
+template <class S> GB_HD void compose_slide(const S* PR, const S* Pt, int axis, S d, X3<S>& out) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) out.R[3 * r + k] = PR[3 * r + k];
+    out.t[r] = Pt[r] + PR[3 * r + axis] * d;
   }
 }
 // Free-flyer joint transform from (x, y, z, qx, qy, qz, qw) composed after a

@@ -128,7 +128,7 @@ __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In&
 #pragma unroll
         for (int k = 0; k < 6; ++k) tau[iv + k] = double(fi.v[k] + arm[iv + k] * S(a[iv + k]));
       } else {
-        tau[iv] = double(pick3(fi.v + 3, jt - JT_RX) + arm[iv] * S(a[iv]));
+        tau[iv] = double(pick6(fi.v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
       }
       if (p > 0) act_force(X[i], fi, cf[i]);
     });
@@ -162,9 +162,9 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
       joint_transform(m, i, q, X[i]);
     } else {
       S sn, cn;
-      ssincos(S(q[m.idx_q[i]]), &sn, &cn);
+      joint_params(m.jtype[i], S(q[m.idx_q[i]]), &sn, &cn);
       const S* P = ModelScalar<S>::place(m, i);
-      compose_axis(P, P + 9, m.jtype[i] - JT_RX, cn, sn, X[i]);
+      compose_joint(P, P + 9, m.jtype[i], cn, sn, X[i]);
     }
   });
   sc.sync();
@@ -251,11 +251,11 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
           }
         return;
       }
-      const int ax = jt - JT_RX;
-      const SS u = SS(tau[iv]) - cvt<SS>(pick3(f.v + 3, ax));
+      const int sx = jt_sidx(jt);
+      const SS u = SS(tau[iv]) - cvt<SS>(pick6(f.v, sx));
       SS U[6], UD[6];
-      sym6_col(Ia, 3 + ax, U);
-      const SS Dinv = SS(1) / (pick3(U + 3, ax) + SS(arm[iv]));
+      sym6_col(Ia, sx, U);
+      const SS Dinv = SS(1) / (pick6(U, sx) + SS(arm[iv]));
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         UD[k] = U[k] * Dinv;
@@ -309,16 +309,12 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
 #pragma unroll
         for (int r = 0; r < 6; ++r) a.v[r] += cvt<S>(dd[r]);
       } else {
-        const int ax = jt - JT_RX;
         S w = UDs[i].v[0] * a.v[0];
 #pragma unroll
         for (int k = 1; k < 6; ++k) w += UDs[i].v[k] * a.v[k];
         const SS dd = du[i] - cvt<SS>(w);
         ddq[iv] = double(dd);
-        const S dds = cvt<S>(dd);
-        a.v[3] += ax == 0 ? dds : S(0);
-        a.v[4] += ax == 1 ? dds : S(0);
-        a.v[5] += ax == 2 ? dds : S(0);
+        add_at6(a.v, jt_sidx(jt), cvt<S>(dd));
       }
       acc[i] = a;
     });

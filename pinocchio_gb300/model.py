@@ -5,11 +5,11 @@ The reference builds a ``ModelTpl`` joint by joint with ``addJoint`` and
 in insertion order with ``parents[i] < i`` and the configuration / velocity
 indices ``idx_q`` / ``idx_v`` are cumulative in that order.  This module keeps
 that construction API for the joint types on the batched dynamics path
-(revolute about the unit x, y or z axis and the free-flyer) and flattens the
-tree into the plain tables the C ABI takes:
+(revolute about the unit x, y or z axis, prismatic along it, and the free-flyer)
+and flattens the tree into the plain tables the C ABI takes:
 
 * ``parents`` (int32, njoints), ``jtype`` (int32, njoints; 0 = universe,
-  1/2/3 = RX/RY/RZ, 4 = free-flyer),
+  1/2/3 = RX/RY/RZ, 4 = free-flyer, 5/6/7 = PX/PY/PZ),
 * ``placement`` (njoints x 12: rotation row-major, then translation),
 * ``inertia`` (njoints x 10: mass, lever (COM), rotational inertia about the COM
   packed as [xx, xy, yy, xz, yz, zz] -- reference spatial/symmetric3.hpp:46-49),
@@ -19,9 +19,10 @@ from __future__ import annotations
 
 import numpy as np
 
-JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF = 0, 1, 2, 3, 4
-_JT_NQ = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 7}
-_JT_NV = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 6}
+JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ = 0, 1, 2, 3, 4, 5, 6, 7
+_JT_NQ = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 7, JT_PX: 1, JT_PY: 1, JT_PZ: 1}
+_JT_NV = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 6, JT_PX: 1, JT_PY: 1, JT_PZ: 1}
+PRISMATIC = (JT_PX, JT_PY, JT_PZ)
 
 
 class Convention:
@@ -57,6 +58,18 @@ class JointModelRZ(JointModel):
 
 class JointModelFreeFlyer(JointModel):
     jtype = JT_FF
+
+
+class JointModelPX(JointModel):
+    jtype = JT_PX
+
+
+class JointModelPY(JointModel):
+    jtype = JT_PY
+
+
+class JointModelPZ(JointModel):
+    jtype = JT_PZ
 
 
 class SE3:

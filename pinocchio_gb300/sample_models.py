@@ -10,14 +10,16 @@ numpy's PCG64 (``np.random.default_rng(seed)``):
   4-D Gaussian), translation U[-0.3, 0.3]^3 m;
 * link inertia: mass U[0.5, 5] kg (or the range given), COM U[-0.1, 0.1]^3 m,
   rotational inertia R diag(U[0.01, 0.1]^3) R^T with R a uniform random rotation;
-* revolute axes uniform over the unit x / y / z axes.
+* revolute axes uniform over the unit x / y / z axes; in ``mixed_tree`` each
+  one-dof joint is one of RX, RY, RZ, PX, PY, PZ, uniformly.
 
 Workloads:
   ``manipulator6r``  6 revolute joints in series (nq = nv = 6);
   ``humanoid32``     free-flyer root, two torso revolute joints, four limbs of
                      six revolute joints hanging off the torso (nq 33, nv 32);
   ``random_tree``    seeded trees with 0-3 children per node (optional free-flyer root);
-  ``chain``          a revolute serial chain (100 links, masses U[0.1, 1] kg).
+  ``chain``          a revolute serial chain (100 links, masses U[0.1, 1] kg);
+  ``mixed_tree``     a ``random_tree`` of revolute and prismatic joints.
 """
 from __future__ import annotations
 
@@ -25,8 +27,12 @@ import numpy as np
 
 from .model import (
     JT_FF,
+    PRISMATIC,
     Inertia,
     JointModelFreeFlyer,
+    JointModelPX,
+    JointModelPY,
+    JointModelPZ,
     JointModelRX,
     JointModelRY,
     JointModelRZ,
@@ -35,6 +41,7 @@ from .model import (
 )
 
 _REVOLUTE = (JointModelRX, JointModelRY, JointModelRZ)
+_ONE_DOF = _REVOLUTE + (JointModelPX, JointModelPY, JointModelPZ)
 
 
 def quat_to_matrix(x, y, z, w) -> np.ndarray:
@@ -76,6 +83,10 @@ def _random_revolute(rng: np.random.Generator):
     return _REVOLUTE[int(rng.integers(0, 3))]()
 
 
+def _random_one_dof(rng: np.random.Generator):
+    return _ONE_DOF[int(rng.integers(0, 6))]()
+
+
 def _add_link(model: Model, rng, parent: int, joint, name: str, mass_range=(0.5, 5.0)) -> int:
     jid = model.addJoint(parent, joint, random_placement(rng), name)
     model.appendBodyToJoint(jid, random_inertia(rng, mass_range))
@@ -108,7 +119,7 @@ def humanoid32(seed: int = 1) -> Model:
     return model
 
 
-def random_tree(nv: int, free_flyer: bool, seed: int, max_children: int = 3) -> Model:
+def random_tree(nv: int, free_flyer: bool, seed: int, max_children: int = 3, joint=_random_revolute) -> Model:
     """Seeded tree with 0..max_children children per node and exactly ``nv`` dofs.
 
     The tree is grown breadth-first (each node draws its number of children),
@@ -150,16 +161,20 @@ def random_tree(nv: int, free_flyer: bool, seed: int, max_children: int = 3) -> 
     model.name = f"tree{nv}{'ff' if free_flyer else ''}"
 
     def emit(node: int, parent_jid: int):
-        if node == 0 and free_flyer:
-            joint = JointModelFreeFlyer()
-        else:
-            joint = _random_revolute(rng)
-        jid = _add_link(model, rng, parent_jid, joint, f"n{node}")
+        jm = JointModelFreeFlyer() if node == 0 and free_flyer else joint(rng)
+        jid = _add_link(model, rng, parent_jid, jm, f"n{node}")
         for ch in children[node]:
             emit(ch, jid)
 
     emit(0, 0)
     assert model.nv == nv, (model.nv, nv)
+    return model
+
+
+def mixed_tree(nv: int = 24, free_flyer: bool = True, seed: int = 5) -> Model:
+    """``random_tree`` whose one-dof joints are revolute or prismatic (x / y / z), uniformly."""
+    model = random_tree(nv, free_flyer, seed, joint=_random_one_dof)
+    model.name = f"mixedtree{nv}{'ff' if free_flyer else ''}"
     return model
 
 
@@ -188,12 +203,15 @@ def heterogeneous_trees(seed: int = 3):
 # inputs
 # ---------------------------------------------------------------------------------------------
 def random_configurations(model: Model, batch: int, rng: np.random.Generator) -> np.ndarray:
-    """q of shape (batch, nq): FF position N(0,1), uniform unit quaternion; joints U[-pi, pi]."""
+    """q of shape (batch, nq): FF position N(0,1), uniform unit quaternion; revolute angles
+    U[-pi, pi]; prismatic displacements U[-0.5, 0.5] m."""
     q = np.empty((batch, model.nq))
     for jt, iq in zip(model.jtypes[1:], model.idx_qs[1:]):
         if jt == JT_FF:
             q[:, iq : iq + 3] = rng.standard_normal((batch, 3))
             q[:, iq + 3 : iq + 7] = random_unit_quaternion(rng, batch)
+        elif jt in PRISMATIC:
+            q[:, iq] = rng.uniform(-0.5, 0.5, batch)
         else:
             q[:, iq] = rng.uniform(-np.pi, np.pi, batch)
     return q

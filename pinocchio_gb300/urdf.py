@@ -10,12 +10,13 @@ link into the parent body (reference: fixed joints become frames, their bodies a
 parent joint).  ``root_joint=JointModelFreeFlyer()`` puts a free-flyer between the universe and the
 root link, as the reference's ``buildModel(filename, root_joint, model)`` does.
 
-The batched kernels support revolute joints about a coordinate axis: ``revolute`` and ``continuous``
-joints with axis +-x, +-y or +-z.  A negative axis is taken by a fixed half-turn F of the joint frame
-(F maps the axis to its opposite), so that the joint keeps the file's angle sign: the model's frame
-of that joint is the URDF joint frame times F, the link hung from it is placed by F^-1, and every
-joint-space quantity (q, v, tau, M, the derivatives) is the reference's.  Other joint types
-(prismatic, planar, floating inside the tree) and axes off the coordinate axes raise ValueError.
+The batched kernels support one-dof joints along a coordinate axis: ``revolute`` and ``continuous``
+joints (JointModelRX/RY/RZ) and ``prismatic`` joints (JointModelPX/PY/PZ) with axis +-x, +-y or +-z.
+A negative axis is taken by a fixed half-turn F of the joint frame (F maps the axis to its
+opposite), so that the joint keeps the file's sign of q: the model's frame of that joint is the URDF
+joint frame times F, the link hung from it is placed by F^-1, and every joint-space quantity (q, v,
+tau, M, the derivatives) is the reference's.  Other joint types (planar, floating inside the tree)
+and axes off the coordinate axes raise ValueError.
 
 ``save_model`` / ``load_model`` write and read the flattened tables (``Model.tables()`` plus the joint
 names) as one ``.npz`` file: the on-disk format of a model (the reference serialises ModelTpl with
@@ -27,7 +28,21 @@ import xml.etree.ElementTree as ET
 
 import numpy as np
 
-from .model import JT_FF, JT_NONE, JT_RX, JT_RY, JT_RZ, Inertia, JointModel, JointModelFreeFlyer, Model, SE3
+from .model import (
+    JT_FF,
+    JT_NONE,
+    JT_PX,
+    JT_PY,
+    JT_PZ,
+    JT_RX,
+    JT_RY,
+    JT_RZ,
+    Inertia,
+    JointModel,
+    JointModelFreeFlyer,
+    Model,
+    SE3,
+)
 
 
 def _floats(text, n, default):
@@ -77,16 +92,16 @@ def _link_inertia(link) -> Inertia:
 
 # the half-turn that maps a coordinate axis to its opposite: about z for x and y, about x for z
 _FLIP = {0: np.diag([-1.0, -1.0, 1.0]), 1: np.diag([-1.0, -1.0, 1.0]), 2: np.diag([1.0, -1.0, -1.0])}
-_AXIS_JT = {0: JT_RX, 1: JT_RY, 2: JT_RZ}
+_AXIS_JT = {"revolute": (JT_RX, JT_RY, JT_RZ), "continuous": (JT_RX, JT_RY, JT_RZ), "prismatic": (JT_PX, JT_PY, JT_PZ)}
 
 
-class _Revolute(JointModel):
+class _OneDof(JointModel):
     def __init__(self, jtype):
         self.jtype = jtype
 
 
 def _axis_joint(joint):
-    """(jtype, F) for a revolute joint's axis; F the frame flip (None for a positive axis)."""
+    """(jtype, F) for a one-dof joint's axis; F the frame flip (None for a positive axis)."""
     ax = _floats(None if joint.find("axis") is None else joint.find("axis").get("xyz"), 3, [1, 0, 0])
     n = np.linalg.norm(ax)
     if n == 0:
@@ -95,7 +110,7 @@ def _axis_joint(joint):
     k = int(np.argmax(np.abs(ax)))
     if abs(abs(ax[k]) - 1.0) > 1e-12:
         raise ValueError(f"joint {joint.get('name')!r}: axis {ax} is not a coordinate axis (unsupported)")
-    return _AXIS_JT[k], (None if ax[k] > 0 else _FLIP[k])
+    return _AXIS_JT[joint.get("type")][k], (None if ax[k] > 0 else _FLIP[k])
 
 
 def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
@@ -141,10 +156,10 @@ def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
             if jt == "fixed":
                 append(joint_id, child, Pj)
                 visit(child, (joint_id, Pj))
-            elif jt in ("revolute", "continuous"):
+            elif jt in _AXIS_JT:
                 jtype, F = _axis_joint(j)
                 placement = Pj if F is None else SE3(Pj.rotation @ F, Pj.translation)
-                new_id = model.addJoint(joint_id, _Revolute(jtype), placement, j.get("name"))
+                new_id = model.addJoint(joint_id, _OneDof(jtype), placement, j.get("name"))
                 child_in_joint = SE3.Identity() if F is None else SE3(F.T, np.zeros(3))
                 append(new_id, child, child_in_joint)
                 visit(child, (new_id, child_in_joint))
@@ -178,7 +193,7 @@ def load_model(path: str) -> Model:
         model.name = str(z["name"])
         for i in range(1, len(parents)):
             jt = int(jtype[i])
-            joint = JointModelFreeFlyer() if jt == JT_FF else _Revolute(jt)
+            joint = JointModelFreeFlyer() if jt == JT_FF else _OneDof(jt)
             if jt == JT_NONE:
                 raise ValueError("joint type 0 (universe) below the root")
             P = SE3(placement[i, :9].reshape(3, 3), placement[i, 9:])

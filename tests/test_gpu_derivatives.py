@@ -77,7 +77,7 @@ def test_minv_is_inverse_of_crba(case):
     assert rel_err((Minv @ M).cpu().numpy(), eye) < (1e-8 if name == "chain100" else 1e-11)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff"])
 def test_derivatives_vs_central_fd_on_gpu(name):
     import torch
 

@@ -103,7 +103,7 @@ def test_autotuner_keeps_results(tmp_path, monkeypatch):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100", "mixedtree24ff"])
 def test_warp_layout_matches_thread_layout_bitwise(name, precision):
     """The warp-per-instance and lane-per-branch layouts (gb_model_set_layout) give
     the thread layout's results for RNEA, ABA, nonLinearEffects and gravity -- the same bits in FP64,
@@ -155,7 +155,7 @@ def test_layout_setting_errors():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100", "mixedtree24ff"])
 def test_team_layouts_aba_derivatives(name, precision):
     """The ABA derivatives with a team of 4, 8 or 32 lanes per configuration
     (the lanes split the column loops of the sweeps) give the thread layout's

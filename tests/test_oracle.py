@@ -16,7 +16,7 @@ from pinocchio_gb300 import model as gm
 from pinocchio_gb300 import sample_models as sm
 from util import MODELS, rel_err
 
-CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100"]
+CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100", "mixedtree12", "mixedtree24ff"]
 
 
 @pytest.fixture(scope="module", params=CPU_MODELS)
@@ -92,7 +92,7 @@ def _fd(f, x0, h, k, integrate=None):
     return (f(x0 + e) - f(x0 - e)) / (2 * h)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff"])
 def test_derivatives_vs_central_fd(name):
     model = MODELS[name]()
     om = OracleModel(model)
@@ -155,6 +155,48 @@ def test_kat_pendulum():
     assert rel_err(om.rnea(q, v, a), tau) < 1e-13
     assert rel_err(om.aba(q, v, tau), a) < 1e-13
     assert rel_err(symmetrize_upper(om.crba(q))[:, 0, 0][:, None], np.full((32, 1), Ixx + m * L * L)) < 1e-14
+
+
+def cart_pole(M=1.5, m=0.4, L=0.6, I=(0.02, 0.03, 0.01)):
+    """A cart sliding along x (prismatic) carrying a pendulum about y, COM at (0, 0, -L)."""
+    model = gm.Model()
+    cart = model.addJoint(0, gm.JointModelPX(), gm.SE3.Identity(), "cart")
+    model.appendBodyToJoint(cart, gm.Inertia(M, [0, 0, 0], np.diag([0.1, 0.2, 0.3])))
+    pole = model.addJoint(cart, gm.JointModelRY(), gm.SE3.Identity(), "pole")
+    model.appendBodyToJoint(pole, gm.Inertia(m, [0, 0, -L], np.diag(I)))
+    return model
+
+
+def test_kat_cart_pole():
+    """Lagrange's equations of the cart-pole: with x_c = x - L sin t, z_c = -L cos t,
+    tau_x = (M+m) x'' - m L cos t t'' + m L sin t t'^2,
+    tau_t = -m L cos t x'' + (m L^2 + Iyy) t'' + m g L sin t."""
+    M, m, L, Iyy, g = 1.5, 0.4, 0.6, 0.03, 9.81
+    om = OracleModel(cart_pole(M, m, L))
+    rng = np.random.default_rng(3)
+    q = np.stack([rng.uniform(-0.5, 0.5, 32), rng.uniform(-np.pi, np.pi, 32)], axis=1)
+    v, a = rng.standard_normal((32, 2)), rng.standard_normal((32, 2))
+    s, c = np.sin(q[:, 1]), np.cos(q[:, 1])
+    tau = np.stack([(M + m) * a[:, 0] - m * L * c * a[:, 1] + m * L * s * v[:, 1] ** 2,
+                    -m * L * c * a[:, 0] + (m * L * L + Iyy) * a[:, 1] + m * g * L * s], axis=1)
+    assert rel_err(om.rnea(q, v, a), tau) < 1e-13
+    assert rel_err(om.aba(q, v, tau), a) < 1e-12
+    Mq = symmetrize_upper(om.crba(q))
+    assert np.allclose(Mq[:, 0, 0], M + m, rtol=1e-14) and np.allclose(Mq[:, 1, 1], m * L * L + Iyy, rtol=1e-14)
+    assert np.allclose(Mq[:, 0, 1], -m * L * c, rtol=1e-13, atol=1e-15)
+
+
+def test_kat_prismatic_slide():
+    """A body on a slide (no rotation): tau = m (a + 9.81 e_z . axis), the axis in the world."""
+    rng = np.random.default_rng(4)
+    for joint, k in ((gm.JointModelPZ(), 2), (gm.JointModelPX(), 0), (gm.JointModelPY(), 1)):
+        model = gm.Model()
+        R = sm.random_rotation(rng)
+        j = model.addJoint(0, joint, gm.SE3(R, [0.1, -0.2, 0.3]), "slide")
+        model.appendBodyToJoint(j, gm.Inertia(2.5, [0.05, 0.0, -0.1], np.diag([0.01, 0.02, 0.03])))
+        q, v, a = (rng.standard_normal((8, 1)) for _ in range(3))
+        tau = 2.5 * (a + 9.81 * R[2, k])
+        assert rel_err(OracleModel(model).rnea(q, v, a), tau) < 1e-13
 
 
 def free_body(m=3.0, I=(0.2, 0.3, 0.4)):
@@ -227,7 +269,7 @@ def test_forward_kinematics_and_jacobians_agree(case):
     assert np.array_equal(om.forward_kinematics(q)[0], oMi)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff"])
 def test_forward_kinematics_acceleration_vs_fd(name):
     """data.a[i] is the time derivative of the joint-frame velocity data.v[i]
     along (q + dt v, v + dt a): central differences, step 1e-6."""

@@ -12,7 +12,7 @@ from pinocchio_gb300 import model as gm
 from pinocchio_gb300 import sample_models as sm
 from util import MODELS, rel_err
 
-_AX = {gm.JT_RX: "1 0 0", gm.JT_RY: "0 1 0", gm.JT_RZ: "0 0 1"}
+_AX = {gm.JT_RX: "1 0 0", gm.JT_RY: "0 1 0", gm.JT_RZ: "0 0 1", gm.JT_PX: "1 0 0", gm.JT_PY: "0 1 0", gm.JT_PZ: "0 0 1"}
 
 
 def _rpy_of(R):
@@ -42,7 +42,7 @@ def _inertial(Y):
 
 
 def to_urdf(model, skip_free_flyer=True):
-    """URDF of a revolute-joint model (the root free-flyer, if any, left to root_joint)."""
+    """URDF of a model of one-dof joints (the root free-flyer, if any, left to root_joint)."""
     out = ['<robot name="exported">', '<link name="base"/>']
     link_of = {0: "base"}
     for i in range(1, model.njoints):
@@ -53,14 +53,15 @@ def to_urdf(model, skip_free_flyer=True):
             continue
         link_of[i] = f"link{i}"
         out.append(f'<link name="link{i}">{_inertial(model.inertias[i])}</link>')
-        out.append(f'<joint name="{model.names[i]}" type="revolute"><parent link="{link_of[model.parents[i]]}"/>'
+        kind = "prismatic" if model.jtypes[i] in gm.PRISMATIC else "revolute"
+        out.append(f'<joint name="{model.names[i]}" type="{kind}"><parent link="{link_of[model.parents[i]]}"/>'
                    f'<child link="link{i}"/>{_origin(model.jointPlacements[i])}<axis xyz="{_AX[model.jtypes[i]]}"/>'
                    f'<limit lower="-3" upper="3" effort="1" velocity="1"/></joint>')
     out.append("</robot>")
     return "\n".join(out)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "tree12", "chain100"])
+@pytest.mark.parametrize("name", ["manipulator6r", "tree12", "chain100", "mixedtree12"])
 def test_urdf_round_trip(name):
     model = MODELS[name]()
     back = pg.buildModelFromXML(to_urdf(model))
@@ -128,6 +129,31 @@ def test_urdf_fixed_joint_and_negative_axis():
     assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(plus).rnea(q, v, a)) < 1e-12
 
 
+def test_urdf_prismatic_negative_axis():
+    """A prismatic joint along -x gives the +x joint's dynamics with its coordinate negated."""
+    doc = """<robot name="slide">
+  <link name="base"/>
+  <link name="cart"><inertial><origin xyz="0.1 0 0.05"/><mass value="2.0"/>
+    <inertia ixx="0.02" ixy="0" ixz="0" iyy="0.03" iyz="0" izz="0.04"/></inertial></link>
+  <link name="pole"><inertial><origin xyz="0 0 -0.4"/><mass value="0.5"/>
+    <inertia ixx="0.01" ixy="0" ixz="0" iyy="0.01" iyz="0" izz="0.002"/></inertial></link>
+  <joint name="rail" type="prismatic"><parent link="base"/><child link="cart"/>
+    <origin xyz="0 0 0.3" rpy="0 0 0.2"/><axis xyz="AXIS"/>
+    <limit lower="-1" upper="1" effort="1" velocity="1"/></joint>
+  <joint name="hinge" type="continuous"><parent link="cart"/><child link="pole"/>
+    <origin xyz="0.1 0 0"/><axis xyz="0 1 0"/></joint>
+</robot>"""
+    plus = pg.buildModelFromXML(doc.replace("AXIS", "1 0 0"))
+    minus = pg.buildModelFromXML(doc.replace("AXIS", "-1 0 0"))
+    assert plus.jtypes[1:] == [gm.JT_PX, gm.JT_RY] and minus.jtypes[1:] == [gm.JT_PX, gm.JT_RY]
+    rng = np.random.default_rng(2)
+    q, v, a = (rng.standard_normal((16, 2)) for _ in range(3))
+    D = np.array([-1.0, 1.0])
+    tp = OracleModel(plus).rnea(q * D, v * D, a * D)
+    tm = OracleModel(minus).rnea(q, v, a)
+    assert rel_err(tm, tp * D) < 1e-12
+
+
 def rpy(r, p, y):
     cr, sr, cp, sp, cy, sy = np.cos(r), np.sin(r), np.cos(p), np.sin(p), np.cos(y), np.sin(y)
     return (np.array([[cy, -sy, 0], [sy, cy, 0], [0, 0, 1]]) @ np.array([[cp, 0, sp], [0, 1, 0], [-sp, 0, cp]])
@@ -139,7 +165,9 @@ def gm_rz(t):
 
 
 @pytest.mark.parametrize("bad,msg", [
-    ('<joint name="s" type="prismatic"><parent link="a"/><child link="b"/><axis xyz="1 0 0"/></joint>', "not supported"),
+    ('<joint name="s" type="planar"><parent link="a"/><child link="b"/><axis xyz="1 0 0"/></joint>', "not supported"),
+    ('<joint name="s" type="prismatic"><parent link="a"/><child link="b"/><axis xyz="0 0.6 0.8"/></joint>',
+     "coordinate axis"),
     ('<joint name="s" type="revolute"><parent link="a"/><child link="b"/><axis xyz="1 1 0"/></joint>', "coordinate axis"),
 ])
 def test_urdf_unsupported(bad, msg):

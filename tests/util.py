@@ -29,6 +29,8 @@ MODELS = {
     "tree32ff": lambda: sm.random_tree(32, True, 332),
     "tree60ff": lambda: sm.random_tree(60, True, 360),
     "chain100": lambda: sm.chain(100, 4),
+    "mixedtree12": lambda: sm.mixed_tree(12, False, 6),
+    "mixedtree24ff": lambda: sm.mixed_tree(24, True, 5),
 }
 # FP64 parity bar of the batched kernels against the FP64 oracle (relative, per instance)
 FP64_TOL = 1e-12
