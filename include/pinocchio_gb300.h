@@ -46,7 +46,9 @@ enum { GB_LOCAL = 0, GB_WORLD = 1 };              /* reference multibody/fwd.hpp
 enum { GB_LAYOUT_INSTANCE = 0, GB_LAYOUT_SOA = 1 };
 /* joint types: revolute about x / y / z (JointModelRX/RY/RZ, multibody/joint/joint-revolute.hpp),
  * the free-flyer (JointModelFreeFlyer, joint-free-flyer.hpp; root joint only), prismatic along
- * x / y / z (JointModelPX/PY/PZ, joint-prismatic.hpp) */
+ * x / y / z (JointModelPX/PY/PZ, joint-prismatic.hpp), revolute about / prismatic along a unit
+ * axis of the joint frame (JointModelRevoluteUnaligned, joint-revolute-unaligned.hpp;
+ * JointModelPrismaticUnaligned, joint-prismatic-unaligned.hpp) given by gb_model_desc.axis */
 enum {
   GB_JOINT_NONE = 0,
   GB_JOINT_RX = 1,
@@ -55,7 +57,9 @@ enum {
   GB_JOINT_FREEFLYER = 4,
   GB_JOINT_PX = 5,
   GB_JOINT_PY = 6,
-  GB_JOINT_PZ = 7
+  GB_JOINT_PZ = 7,
+  GB_JOINT_REVOLUTE_UNALIGNED = 8,
+  GB_JOINT_PRISMATIC_UNALIGNED = 9
 };
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
 /* functions of a heterogeneous batch task / of a launch setting */
@@ -71,7 +75,9 @@ typedef struct gb_pool gb_pool;
  * inertia:   njoints x 10 (mass, lever[3], inertia about the COM packed
  *            [xx, xy, yy, xz, yz, zz]) -- inertias (spatial/symmetric3.hpp:46-49).
  * armature:  nv values (may be NULL for zeros); gravity: 6 values [lin; ang]
- *            (may be NULL for (0, 0, -9.81, 0, 0, 0), multibody/model.hxx:40). */
+ *            (may be NULL for (0, 0, -9.81, 0, 0, 0), multibody/model.hxx:40).
+ * axis:      njoints x 3, the axis of each unaligned joint (normalised on creation; the
+ *            entries of other joints are ignored); may be NULL when there is none. */
 typedef struct {
   int njoints;
   const int* parents;
@@ -81,6 +87,7 @@ typedef struct {
   const double* armature;
   int nv_armature;
   const double* gravity;
+  const double* axis;
 } gb_model_desc;
 
 /* Replaces building a ModelTpl + DataTpl (multibody/model.hpp:98-220,

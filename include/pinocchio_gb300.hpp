@@ -39,12 +39,13 @@ struct ModelTables {
   std::vector<double> inertia;      // njoints x 10
   std::vector<double> armature;     // nv
   double gravity[6] = {0, 0, -9.81, 0, 0, 0};
+  std::vector<double> axis;         // njoints x 3: axes of the unaligned joints (empty: none)
 };
 
 class Model {
  public:
   explicit Model(const ModelTables& t) {
-    gb_model_desc d;
+    gb_model_desc d{};
     d.njoints = static_cast<int>(t.parents.size());
     d.parents = t.parents.data();
     d.jtype = t.jtype.data();
@@ -53,6 +54,7 @@ class Model {
     d.armature = t.armature.empty() ? nullptr : t.armature.data();
     d.nv_armature = static_cast<int>(t.armature.size());
     d.gravity = t.gravity;
+    d.axis = t.axis.empty() ? nullptr : t.axis.data();
     gb_model* m = nullptr;
     check(gb_model_create(&d, &m));
     handle_.reset(m, [](gb_model* p) { gb_model_destroy(p); });

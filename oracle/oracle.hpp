@@ -35,7 +35,11 @@
 
 namespace orc {
 
-enum JointType { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7 };
+enum JointType {
+  JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7,
+  JT_RU = 8,  // JointModelRevoluteUnaligned (multibody/joint/joint-revolute-unaligned.hpp)
+  JT_PU = 9   // JointModelPrismaticUnaligned (multibody/joint/joint-prismatic-unaligned.hpp)
+};
 enum Convention { LOCAL = 0, WORLD = 1 };  // reference multibody/fwd.hpp:73-81
 
 // ---------------------------------------------------------------------------
@@ -59,6 +63,7 @@ struct Model {
   std::vector<double> placement;  // 12 per joint: R (row-major 9), t (3)
   std::vector<double> inertia;    // 10 per joint: m, c[3], I[6]
   std::vector<double> armature;   // nv
+  std::vector<double> axis;       // 3 per joint: the unit axis of a JT_RU / JT_PU joint
   double gravity[6] = {0, 0, -9.81, 0, 0, 0};
   // derived tables (multibody/data.hxx:195-306)
   std::vector<int> lastChild, nvSubtree, parents_fromRow, nvSubtree_fromRow;
@@ -81,7 +86,14 @@ struct Model {
         if (jtype[0] != JT_NONE) throw std::invalid_argument("joint 0 must be the universe");
         continue;
       }
-      if (jtype[i] < JT_RX || jtype[i] > JT_PZ) throw std::invalid_argument("unsupported joint type");
+      if (jtype[i] < JT_RX || jtype[i] > JT_PU) throw std::invalid_argument("unsupported joint type");
+      if (jtype[i] == JT_RU || jtype[i] == JT_PU) {
+        if ((int)axis.size() != 3 * njoints) throw std::invalid_argument("unaligned joints need the axis table");
+        const double n = std::sqrt(axis[3 * i] * axis[3 * i] + axis[3 * i + 1] * axis[3 * i + 1] +
+                                   axis[3 * i + 2] * axis[3 * i + 2]);
+        if (!(n > 0.0)) throw std::invalid_argument("zero joint axis");
+        for (int k = 0; k < 3; ++k) axis[3 * i + k] /= n;
+      }
       if (parents[i] < 0 || parents[i] >= i) throw std::invalid_argument("parents[i] must be < i");
       nqs[i] = joint_nq(jtype[i]);
       nvs[i] = joint_nv(jtype[i]);
@@ -583,6 +595,50 @@ template <class T> inline Vec6<T> joint_velocity(int jt, const T* v) {
   return o;
 }
 
+// Joint i of a model, unaligned joints included.
+//  * revolute unaligned: M = (toRotationMatrix(axis, q), 0) (joint-revolute-unaligned.hpp:668-673;
+//    math/rotation.hpp:26-73, the Eigen AngleAxis formula), S = (0, axis);
+//  * prismatic unaligned: M = (I, axis q) (joint-prismatic-unaligned.hpp:643-647), S = (axis, 0).
+inline bool unaligned(int jt) { return jt == JT_RU || jt == JT_PU; }
+template <class T> inline SE3<T> joint_transform(const Model& m, int i, const T* q) {
+  const int jt = m.jtype[i];
+  if (!unaligned(jt)) return joint_transform<T>(jt, q);
+  const T a[3] = {T(m.axis[3 * i]), T(m.axis[3 * i + 1]), T(m.axis[3 * i + 2])};
+  SE3<T> M;
+  for (int k = 0; k < 9; ++k) M.R[k] = T(0);
+  for (int k = 0; k < 3; ++k) M.t[k] = T(0);
+  if (jt == JT_PU) {
+    for (int k = 0; k < 3; ++k) { M.R[4 * k] = T(1); M.t[k] = a[k] * q[0]; }
+    return M;
+  }
+  T s, c;
+  o_sincos(q[0], &s, &c);
+  const T sa[3] = {s * a[0], s * a[1], s * a[2]};
+  const T ca[3] = {(T(1) - c) * a[0], (T(1) - c) * a[1], (T(1) - c) * a[2]};
+  T t = ca[0] * a[1];
+  M.R[1] = t - sa[2]; M.R[3] = t + sa[2];
+  t = ca[0] * a[2];
+  M.R[2] = t + sa[1]; M.R[6] = t - sa[1];
+  t = ca[1] * a[2];
+  M.R[5] = t - sa[0]; M.R[7] = t + sa[0];
+  for (int k = 0; k < 3; ++k) M.R[4 * k] = ca[k] * a[k] + c;
+  return M;
+}
+template <class T> inline Vec6<T> S_col(const Model& m, int i, int k) {
+  const int jt = m.jtype[i];
+  if (!unaligned(jt)) return S_col<T>(jt, k);
+  Vec6<T> s = zero6<T>();
+  const int o = jt == JT_RU ? 3 : 0;
+  for (int r = 0; r < 3; ++r) s.v[o + r] = T(m.axis[3 * i + r]);
+  return s;
+}
+template <class T> inline Vec6<T> joint_velocity(const Model& m, int i, const T* v) {
+  if (!unaligned(m.jtype[i])) return joint_velocity<T>(m.jtype[i], v);
+  Vec6<T> s = S_col<T>(m, i, 0);
+  for (int r = 0; r < 6; ++r) s.v[r] *= v[0];
+  return s;
+}
+
 // ---------------------------------------------------------------------------
 // Data workspace (the subset of DataTpl the hot-path algorithms use)
 // ---------------------------------------------------------------------------
@@ -644,15 +700,15 @@ void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
   d.v[0] = zero6<T>();
   for (int k = 0; k < 6; ++k) d.a_gf[0].v[k] = -T(m.gravity[k]);
   for (int i = 1; i < m.njoints; ++i) {  // RneaForwardStep (rnea.hxx:24-80)
-    const int p = m.parents[i], jt = m.jtype[i];
+    const int p = m.parents[i];
     const int iq = m.idx_q[i], iv = m.idx_v[i];
-    const SE3<T> jM = joint_transform<T>(jt, q + iq);
+    const SE3<T> jM = joint_transform<T>(m, i, q + iq);
     d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
-    const Vec6<T> vJ = joint_velocity<T>(jt, v + iv);
+    const Vec6<T> vJ = joint_velocity<T>(m, i, v + iv);
     d.v[i] = vJ;
     if (p > 0) d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
     d.a_gf[i] = cross_motion(d.v[i], vJ);  // c() = 0 for these joints
-    d.a_gf[i] = add6(d.a_gf[i], joint_velocity<T>(jt, a + iv));
+    d.a_gf[i] = add6(d.a_gf[i], joint_velocity<T>(m, i, a + iv));
     d.a_gf[i] = add6(d.a_gf[i], actinv_motion(d.liMi[i], d.a_gf[p]));
     const Iner<T> Y = inertia_of<T>(m, i);
     d.h[i] = iner_mul(Y, d.v[i]);
@@ -660,8 +716,8 @@ void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
     d.f[i] = add6(d.f[i], cross_force(d.v[i], d.h[i]));
   }
   for (int i = m.njoints - 1; i > 0; --i) {  // RneaBackwardStep (rnea.hxx:83-108)
-    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i];
-    for (int k = 0; k < m.nvs[i]; ++k) d.tau[iv + k] += dot6(S_col<T>(jt, k), d.f[i]);
+    const int p = m.parents[i], iv = m.idx_v[i];
+    for (int k = 0; k < m.nvs[i]; ++k) d.tau[iv + k] += dot6(S_col<T>(m, i, k), d.f[i]);
     if (p > 0) d.f[p] = add6(d.f[p], act_force(d.liMi[i], d.f[i]));
   }
   for (int k = 0; k < m.nv; ++k) d.tau[k] += T(m.armature[k]) * a[k];  // rnea.hxx:158
@@ -677,10 +733,10 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
   d.f[0] = zero6<T>();
   for (int k = 0; k < m.nv; ++k) d.u[k] = tau[k];
   for (int i = 1; i < m.njoints; ++i) {  // AbaLocalConventionForwardStep1 (aba.hxx:360-399)
-    const int p = m.parents[i], jt = m.jtype[i];
-    const SE3<T> jM = joint_transform<T>(jt, q + m.idx_q[i]);
+    const int p = m.parents[i];
+    const SE3<T> jM = joint_transform<T>(m, i, q + m.idx_q[i]);
     d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
-    const Vec6<T> vJ = joint_velocity<T>(jt, v + m.idx_v[i]);
+    const Vec6<T> vJ = joint_velocity<T>(m, i, v + m.idx_v[i]);
     d.v[i] = vJ;
     if (p > 0) d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
     d.a_gf[i] = cross_motion(d.v[i], vJ);
@@ -692,7 +748,7 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
   for (int i = m.njoints - 1; i > 0; --i) {  // AbaLocalConventionBackwardStep (aba.hxx:402-434)
     const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
     Mat6<T>& Ia = d.Yaba[i];
-    for (int k = 0; k < nvj; ++k) d.u[iv + k] -= dot6(S_col<T>(jt, k), d.f[i]);
+    for (int k = 0; k < nvj; ++k) d.u[iv + k] -= dot6(S_col<T>(m, i, k), d.f[i]);
     std::vector<T>& U = d.Ujoint[i];
     std::vector<T>& Dinv = d.Dinvjoint[i];
     std::vector<T>& UDinv = d.UDinvjoint[i];
@@ -714,6 +770,17 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
             for (int k = 1; k < 6; ++k) s += UDinv[6 * r + k] * U[6 * c + k];
             Ia.a[6 * r + c] -= s;
           }
+    } else if (unaligned(jt)) {  // calc_aba of joint-revolute-unaligned.hpp:695-707 /
+                                 // joint-prismatic-unaligned.hpp:671-683: U = I S, Dinv = 1 / (S.U + armature)
+      const int o = jt == JT_RU ? 3 : 0;
+      T a[3];
+      for (int k = 0; k < 3; ++k) a[k] = T(m.axis[3 * i + k]);
+      for (int r = 0; r < 6; ++r) U[r] = Ia.a[6 * r + o] * a[0] + Ia.a[6 * r + o + 1] * a[1] + Ia.a[6 * r + o + 2] * a[2];
+      Dinv[0] = T(1) / ((a[0] * U[o] + a[1] * U[o + 1] + a[2] * U[o + 2]) + T(m.armature[iv]));
+      for (int r = 0; r < 6; ++r) UDinv[r] = U[r] * Dinv[0];
+      if (p > 0)
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c) Ia.a[6 * r + c] -= UDinv[r] * U[c];
     } else {  // JointModelRevolute::calc_aba (joint-revolute.hpp:823-834), prismatic (joint-prismatic.hpp:728-740)
       const int ax = motion_index(jt);
       for (int r = 0; r < 6; ++r) U[r] = Ia.a[6 * r + ax];
@@ -737,7 +804,7 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
     }
   }
   for (int i = 1; i < m.njoints; ++i) {  // AbaLocalConventionForwardStep2 (aba.hxx:437-468)
-    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
     d.a_gf[i] = add6(d.a_gf[i], actinv_motion(d.liMi[i], d.a_gf[p]));
     const std::vector<T>& Dinv = d.Dinvjoint[i];
     const std::vector<T>& UDinv = d.UDinvjoint[i];
@@ -749,7 +816,7 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
       d.ddq[iv + k] = s - w;
     }
     for (int k = 0; k < nvj; ++k) {
-      const Vec6<T> s = S_col<T>(jt, k);
+      const Vec6<T> s = S_col<T>(m, i, k);
       for (int r = 0; r < 6; ++r) d.a_gf[i].v[r] += s.v[r] * d.ddq[iv + k];
     }
   }
@@ -814,12 +881,12 @@ void world_schur_update(const Model& m, Data<T>& d, int i) {
 // derivatives (aba.hxx:85-139, aba-derivatives.hxx:22-80).
 template <class T>
 void world_forward1(const Model& m, Data<T>& d, const T* q, const T* v, int i) {
-  const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i];
-  const SE3<T> jM = joint_transform<T>(jt, q + m.idx_q[i]);
+  const int p = m.parents[i], iv = m.idx_v[i];
+  const SE3<T> jM = joint_transform<T>(m, i, q + m.idx_q[i]);
   d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
   d.oMi[i] = (p > 0) ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
-  for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(jt, k)));
-  d.ov[i] = act_motion(d.oMi[i], joint_velocity<T>(jt, v + iv));
+  for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(m, i, k)));
+  d.ov[i] = act_motion(d.oMi[i], joint_velocity<T>(m, i, v + iv));
   if (p > 0) d.ov[i] = add6(d.ov[i], d.ov[p]);
   d.oa_gf[i] = zero6<T>();  // oMi.act(c()) with c() = 0
   if (p > 0) d.oa_gf[i] = add6(d.oa_gf[i], cross_motion(d.ov[p], d.ov[i]));
@@ -878,16 +945,16 @@ void crba(const Model& m, Data<T>& d, const T* q, int conv) {
   const int nv = m.nv;
   if (conv == LOCAL) {
     for (int i = 1; i < m.njoints; ++i) {
-      d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m.jtype[i], q + m.idx_q[i]));
+      d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m, i, q + m.idx_q[i]));
       d.Ycrb[i] = inertia_of<T>(m, i);
     }
     for (int i = m.njoints - 1; i > 0; --i) {
-      const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
+      const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
       const int nst = m.nvSubtree[i];
       std::vector<T>& Fi = d.Fcrb[i];
-      for (int k = 0; k < nvj; ++k) set_col6(Fi, iv + k, iner_mul(d.Ycrb[i], S_col<T>(jt, k)));
+      for (int k = 0; k < nvj; ++k) set_col6(Fi, iv + k, iner_mul(d.Ycrb[i], S_col<T>(m, i, k)));
       for (int r = 0; r < nvj; ++r)
-        for (int c = iv; c < iv + nst; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(S_col<T>(jt, r), col6(Fi, c));
+        for (int c = iv; c < iv + nst; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(S_col<T>(m, i, r), col6(Fi, c));
       if (p > 0) {
         iner_add(d.Ycrb[p], iner_act(d.liMi[i], d.Ycrb[i]));
         for (int c = iv; c < iv + nst; ++c) set_col6(d.Fcrb[p], c, act_force(d.liMi[i], col6(Fi, c)));
@@ -900,10 +967,10 @@ void crba(const Model& m, Data<T>& d, const T* q, int conv) {
     for (int k = 0; k < 6; ++k) Y0.I[k] = T(0);
     d.oYcrb[0] = Y0;
     for (int i = 1; i < m.njoints; ++i) {
-      const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i];
-      d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(jt, q + m.idx_q[i]));
+      const int p = m.parents[i], iv = m.idx_v[i];
+      d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m, i, q + m.idx_q[i]));
       d.oMi[i] = (p > 0) ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
-      for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(jt, k)));
+      for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(m, i, k)));
       d.oYcrb[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
     }
     std::vector<T>& Ag = d.dFda;  // plays the role of data.Ag
@@ -955,10 +1022,10 @@ void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const 
   Vec6<T> g;
   for (int k = 0; k < 6; ++k) g.v[k] = T(m.gravity[k]);
   for (int i = 1; i < m.njoints; ++i) {  // ComputeRNEADerivativesForwardStep (hxx:242-352)
-    const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
-    const SE3<T> jM = joint_transform<T>(jt, q + m.idx_q[i]);
+    const int p = m.parents[i], iv = m.idx_v[i], nvj = m.nvs[i];
+    const SE3<T> jM = joint_transform<T>(m, i, q + m.idx_q[i]);
     d.liMi[i] = se3_mul(placement_of<T>(m, i), jM);
-    const Vec6<T> vJ = joint_velocity<T>(jt, v + iv);
+    const Vec6<T> vJ = joint_velocity<T>(m, i, v + iv);
     d.v[i] = vJ;
     if (p > 0) {
       d.oMi[i] = se3_mul(d.oMi[p], d.liMi[i]);
@@ -966,7 +1033,7 @@ void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const 
     } else {
       d.oMi[i] = d.liMi[i];
     }
-    d.a[i] = add6(joint_velocity<T>(jt, a + iv), cross_motion(d.v[i], vJ));
+    d.a[i] = add6(joint_velocity<T>(m, i, a + iv), cross_motion(d.v[i], vJ));
     if (p > 0) d.a[i] = add6(d.a[i], actinv_motion(d.liMi[i], d.a[p]));
     d.oYcrb[i] = d.oinertias[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
     d.ov[i] = act_motion(d.oMi[i], d.v[i]);
@@ -976,7 +1043,7 @@ void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const 
     d.of[i] = add6(iner_mul(d.oYcrb[i], d.oa_gf[i]), cross_force(d.ov[i], d.oh[i]));
     for (int k = 0; k < nvj; ++k) {
       const int c = iv + k;
-      const Vec6<T> Jc = act_motion(d.oMi[i], S_col<T>(jt, k));
+      const Vec6<T> Jc = act_motion(d.oMi[i], S_col<T>(m, i, k));
       set_col6(d.J, c, Jc);
       const Vec6<T> dJc = cross_motion(d.ov[i], Jc);
       set_col6(d.dJ, c, dJc);
@@ -1248,16 +1315,16 @@ void forward_kinematics(const Model& m, Data<T>& d, const T* q, const T* v, cons
   d.v[0] = zero6<T>();
   d.a[0] = zero6<T>();
   for (int i = 1; i < m.njoints; ++i) {
-    const int p = m.parents[i], jt = m.jtype[i], iq = m.idx_q[i], iv = m.idx_v[i];
-    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(jt, q + iq));
+    const int p = m.parents[i], iq = m.idx_q[i], iv = m.idx_v[i];
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m, i, q + iq));
     d.oMi[i] = p > 0 ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
     if (!v) continue;
-    const Vec6<T> vJ = joint_velocity<T>(jt, v + iv);
+    const Vec6<T> vJ = joint_velocity<T>(m, i, v + iv);
     d.v[i] = vJ;
     if (p > 0) d.v[i] = add6(d.v[i], actinv_motion(d.liMi[i], d.v[p]));
     if (!a) continue;
     // S a + c + v_i x vJ (c = 0 for these joints), then + liMi.actInv(a_parent)
-    d.a[i] = add6(joint_velocity<T>(jt, a + iv), cross_motion(d.v[i], vJ));
+    d.a[i] = add6(joint_velocity<T>(m, i, a + iv), cross_motion(d.v[i], vJ));
     d.a[i] = add6(d.a[i], actinv_motion(d.liMi[i], d.a[p]));
   }
 }
@@ -1269,10 +1336,10 @@ void forward_kinematics(const Model& m, Data<T>& d, const T* q, const T* v, cons
 template <class T>
 void joint_jacobians(const Model& m, Data<T>& d, const T* q) {
   for (int i = 1; i < m.njoints; ++i) {
-    const int p = m.parents[i], jt = m.jtype[i], iq = m.idx_q[i], iv = m.idx_v[i];
-    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(jt, q + iq));
+    const int p = m.parents[i], iq = m.idx_q[i], iv = m.idx_v[i];
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m, i, q + iq));
     d.oMi[i] = p > 0 ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
-    for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(jt, k)));
+    for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(m, i, k)));
   }
 }
 

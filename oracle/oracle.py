@@ -40,7 +40,8 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.orc_last_error.restype = C.c_char_p
         L.orc_model_new.restype = C.c_void_p
-        L.orc_model_new.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_model_new.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_void_p, C.c_void_p]
         L.orc_model_free.argtypes = [C.c_void_p]
         L.orc_model_dims.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.orc_model_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 5
@@ -76,7 +77,7 @@ class OracleModel:
         self._keep = t
         h = L.orc_model_new(
             int(len(t["parents"])), _ptr(t["parents"]), _ptr(t["jtype"]), _ptr(t["placement"]), _ptr(t["inertia"]),
-            _ptr(t["armature"]), int(len(t["armature"])), _ptr(t["gravity"]),
+            _ptr(t["armature"]), int(len(t["armature"])), _ptr(t["gravity"]), _ptr(t.get("axis")),
         )
         if not h:
             raise ValueError(L.orc_last_error().decode())

@@ -199,10 +199,12 @@ extern "C" {
 const char* orc_last_error() { return g_err.c_str(); }
 
 void* orc_model_new(int njoints, const int* parents, const int* jtype, const double* placement,
-                    const double* inertia, const double* armature, int nv_armature, const double* gravity) {
+                    const double* inertia, const double* armature, int nv_armature, const double* gravity,
+                    const double* axis) {
   try {
-    auto* m = new Model();
+    std::unique_ptr<Model> m(new Model());
     m->njoints = njoints;
+    if (axis) m->axis.assign(axis, axis + 3 * njoints);
     m->parents.assign(parents, parents + njoints);
     m->jtype.assign(jtype, jtype + njoints);
     m->placement.assign(placement, placement + 12 * njoints);
@@ -210,7 +212,7 @@ void* orc_model_new(int njoints, const int* parents, const int* jtype, const dou
     if (armature) m->armature.assign(armature, armature + nv_armature);
     if (gravity) std::memcpy(m->gravity, gravity, 6 * sizeof(double));
     m->finalize();
-    return m;
+    return m.release();
   } catch (const std::exception& e) {
     g_err = e.what();
     return nullptr;

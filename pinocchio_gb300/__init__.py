@@ -9,6 +9,11 @@ from .model import (  # noqa: F401
     Convention,
     Inertia,
     JointModelFreeFlyer,
+    JointModelPrismaticUnaligned,
+    JointModelPX,
+    JointModelPY,
+    JointModelPZ,
+    JointModelRevoluteUnaligned,
     JointModelRX,
     JointModelRY,
     JointModelRZ,

@@ -84,6 +84,7 @@ class ModelDesc(C.Structure):
         ("armature", C.c_void_p),
         ("nv_armature", C.c_int),
         ("gravity", C.c_void_p),
+        ("axis", C.c_void_p),
     ]
 
 
@@ -99,6 +100,7 @@ def make_desc(tables: dict) -> tuple[ModelDesc, dict]:
     d.armature = keep["armature"].ctypes.data if len(keep["armature"]) else None
     d.nv_armature = len(keep["armature"])
     d.gravity = keep["gravity"].ctypes.data
+    d.axis = keep["axis"].ctypes.data if "axis" in keep else None
     return d, keep
 
 

@@ -474,6 +474,41 @@ GB_HD void store_placement(const Out& o, int i, const X3<S>& X) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) o[12 * i + 9 + k] = double(X.t[k]);
 }
+// The frame of an unaligned joint i is frame_i F_i inside the kernels (the model
+// build folds the axis into the placements): the outputs map back with
+// oMi = oMi' F^T and a joint-frame motion m = F m'.
+template <class S>
+GB_HD void store_placement_fixed(const MView& m, const Out& o, int i, const X3<S>& X) {
+  if (!m.fix_d) {
+    store_placement(o, i, X);
+    return;
+  }
+  const double* F = m.fix_d + 9 * i;
+  X3<S> Y;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      Y.R[3 * r + c] = X.R[3 * r] * S(F[3 * c]) + X.R[3 * r + 1] * S(F[3 * c + 1]) + X.R[3 * r + 2] * S(F[3 * c + 2]);
+    Y.t[r] = X.t[r];
+  }
+  store_placement(o, i, Y);
+}
+template <class S>
+GB_HD void store_motion_fixed(const MView& m, const Out& o, int i, const M6<S>& x) {
+  if (!m.fix_d) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[6 * i + k] = double(x.v[k]);
+    return;
+  }
+  const double* F = m.fix_d + 9 * i;
+#pragma unroll
+  for (int h = 0; h < 6; h += 3)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      o[6 * i + h + r] =
+          double(S(F[3 * r]) * x.v[h] + S(F[3 * r + 1]) * x.v[h + 1] + S(F[3 * r + 2]) * x.v[h + 2]);
+}
 template <class S, int CAP>
 GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const Out& oMi, const Out* vo,
                   const Out* ao) {
@@ -497,7 +532,7 @@ GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const O
     joint_transform(m, i, q, X);
     if (p > 0) compose(oM[p], X, oM[i]);
     else oM[i] = X;
-    store_placement(oMi, i, oM[i]);
+    store_placement_fixed(m, oMi, i, oM[i]);
     if (!v) continue;
     M6<S> vJ, t;
     joint_motion(jt, *v, iv, vJ);
@@ -508,8 +543,7 @@ GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const O
     } else {
       vel[i] = vJ;
     }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) (*vo)[6 * i + k] = double(vel[i].v[k]);
+    store_motion_fixed(m, *vo, i, vel[i]);
     if (!a) continue;
     M6<S> aJ, ap;
     joint_motion(jt, *a, iv, aJ);
@@ -517,8 +551,7 @@ GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const O
     if (p > 0) actinv_motion(X, acc[p], ap);
 #pragma unroll
     for (int k = 0; k < 6; ++k) acc[i].v[k] = p > 0 ? (aJ.v[k] + t.v[k]) + ap.v[k] : aJ.v[k] + t.v[k];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) (*ao)[6 * i + k] = double(acc[i].v[k]);
+    store_motion_fixed(m, *ao, i, acc[i]);
   }
 }
 template <class S, int CAP>

@@ -37,7 +37,8 @@ struct BlobHeader {
   int o_grp, ngroup, o_grp_rel, n_grp_rel;
   int stage_bytes;  // [0, stage_bytes): what the per-instance kernels stage (rel_list and the groups lie beyond)
   int o_i6_d, o_i6_f, o_place_df, o_iner_df;
-  int o_arm_df, o_zero, pad8;  // o_zero: 16 zero bytes (a zero vector with stride 0)
+  int o_arm_df, o_zero;  // o_zero: 16 zero bytes (a zero vector with stride 0)
+  int o_fix;             // 9 doubles per joint: F of an unaligned joint's frame (0: no such joint)
   // chains: maximal runs of joints each the only child of the previous one (consecutive in the
   // depth-first order); chain c holds joints chain[3c] .. chain[3c+1] at chain level chain[3c+2]
   int o_chain, nchain, nclevel, chain_team;
@@ -57,6 +58,7 @@ struct MView {
   const double *place_d, *iner_d, *arm_d, *grav_d, *i6_d;
   const float *place_f, *iner_f, *arm_f, *grav_f, *i6_f;
   const dfloat *place_df, *iner_df, *arm_df, *grav_df;
+  const double* fix_d;  // nullptr when no joint is unaligned
 };
 
 GB_HD MView make_view(const unsigned char* base) {
@@ -95,6 +97,7 @@ GB_HD MView make_view(const unsigned char* base) {
   m.iner_df = reinterpret_cast<const dfloat*>(base + h->o_iner_df);
   m.arm_df = reinterpret_cast<const dfloat*>(base + h->o_arm_df);
   m.grav_df = h->grav_df;
+  m.fix_d = h->o_fix ? reinterpret_cast<const double*>(base + h->o_fix) : nullptr;
   m.grav_d = h->grav_d;
   m.grav_f = h->grav_f;
   return m;

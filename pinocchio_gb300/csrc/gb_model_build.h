@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -19,6 +20,9 @@ struct gb_model {
   int tpb[8] = {128, 128, 128, 128, 128, 128, 128, 128};  // configurations per CTA, per GB_FUNC_*
   int layout[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // GB_INSTANCE_PER_THREAD / _PER_WARP, per GB_FUNC_*
   std::vector<double> placement, inertia, armature;
+  // per joint, the rotation F of an unaligned joint's frame (identity otherwise); has_fix: any
+  std::vector<double> fix;
+  bool has_fix = false;
   double gravity[6];
   std::vector<unsigned char> blob;  // host copy of the device blob
   unsigned char* d_blob = nullptr;  // device copy (owned by the C ABI)
@@ -32,6 +36,81 @@ namespace gbm {
 inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 // capacity class used to instantiate the kernels (>= njoints and >= nv)
 inline int cap_class(int n) { return n <= 8 ? 8 : n <= 16 ? 16 : n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 0; }
+
+// A rotation F with F e_z = a (a unit): the smallest rotation taking e_z to a
+// (Rodrigues' formula about e_z x a) when a_z >= 0; otherwise the half-turn
+// about x composed with the smallest rotation taking e_z to diag(1,-1,-1) a.
+inline void rotation_to_axis(const double* a, double* F) {
+  const double s = a[2] >= 0.0 ? 1.0 : -1.0;
+  const double b0 = a[0], b1 = s * a[1], c = s * a[2];  // b = diag(1, s, s) a, b_z >= 0
+  const double k = 1.0 / (1.0 + c);
+  const double G[9] = {1.0 - k * b0 * b0, -k * b0 * b1, b0, -k * b0 * b1, 1.0 - k * b1 * b1, b1, -b0, -b1, c};
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) F[3 * r + q] = (r == 0 ? 1.0 : s) * G[3 * r + q];
+}
+
+// Unaligned joints (JointModelRevoluteUnaligned / JointModelPrismaticUnaligned,
+// reference multibody/joint/joint-revolute-unaligned.hpp:611-735 and
+// joint-prismatic-unaligned.hpp:586-711) become z-axis joints of a rotated frame:
+// with F e_z = a, rotation about (translation along) a in frame i is rotation
+// about (along) z in frame i' = frame i * F.  So jointPlacement_i <- jointPlacement_i F,
+// and the body of joint i and the placements of its children are expressed in
+// frame i' (F^T on the left).  Every joint-space quantity is unchanged; forward
+// kinematics maps its frame-i' outputs back to frame i (the blob's fix table).
+inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err) {
+  const int nj = M->nj;
+  M->fix.assign(9 * (size_t)nj, 0.0);
+  for (int i = 0; i < nj; ++i) M->fix[9 * i] = M->fix[9 * i + 4] = M->fix[9 * i + 8] = 1.0;
+  M->has_fix = false;
+  for (int i = 1; i < nj; ++i) {
+    const int jt = M->jtype[i];
+    if (jt != GB_JOINT_REVOLUTE_UNALIGNED && jt != GB_JOINT_PRISMATIC_UNALIGNED) continue;
+    if (!d->axis) {
+      *err = "unaligned joints need gb_model_desc.axis";
+      return GB_ERR_INVALID_ARGUMENT;
+    }
+    double a[3] = {d->axis[3 * i], d->axis[3 * i + 1], d->axis[3 * i + 2]};
+    const double n = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (!(n > 0.0) || !std::isfinite(n)) {
+      *err = "joint " + std::to_string(i) + ": the axis must be finite and non-zero";
+      return GB_ERR_INVALID_ARGUMENT;
+    }
+    for (double& x : a) x /= n;
+    double F[9];
+    rotation_to_axis(a, F);
+    M->jtype[i] = jt == GB_JOINT_REVOLUTE_UNALIGNED ? GB_JOINT_RZ : GB_JOINT_PZ;
+    double* P = &M->placement[12 * (size_t)i];  // R <- R F
+    double R[9];
+    std::memcpy(R, P, sizeof(R));
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) P[3 * r + q] = R[3 * r] * F[q] + R[3 * r + 1] * F[3 + q] + R[3 * r + 2] * F[6 + q];
+    double* Y = &M->inertia[10 * (size_t)i];  // lever <- F^T c, I <- F^T I F
+    const double c[3] = {Y[1], Y[2], Y[3]};
+    const double I[9] = {Y[4], Y[5], Y[7], Y[5], Y[6], Y[8], Y[7], Y[8], Y[9]};
+    double FI[9], J[9];
+    for (int r = 0; r < 3; ++r) {
+      Y[1 + r] = F[r] * c[0] + F[3 + r] * c[1] + F[6 + r] * c[2];
+      for (int q = 0; q < 3; ++q) FI[3 * r + q] = F[r] * I[q] + F[3 + r] * I[3 + q] + F[6 + r] * I[6 + q];
+    }
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) J[3 * r + q] = FI[3 * r] * F[q] + FI[3 * r + 1] * F[3 + q] + FI[3 * r + 2] * F[6 + q];
+    Y[4] = J[0]; Y[5] = 0.5 * (J[1] + J[3]); Y[6] = J[4];
+    Y[7] = 0.5 * (J[2] + J[6]); Y[8] = 0.5 * (J[5] + J[7]); Y[9] = J[8];
+    for (int j = i + 1; j < nj; ++j) {  // children: placement <- F^T placement
+      if (M->parents[j] != i) continue;
+      double* Q = &M->placement[12 * (size_t)j];
+      double Rq[12];
+      std::memcpy(Rq, Q, sizeof(Rq));
+      for (int r = 0; r < 3; ++r) {
+        for (int q = 0; q < 3; ++q) Q[3 * r + q] = F[r] * Rq[q] + F[3 + r] * Rq[3 + q] + F[6 + r] * Rq[6 + q];
+        Q[9 + r] = F[r] * Rq[9] + F[3 + r] * Rq[10] + F[6 + r] * Rq[11];
+      }
+    }
+    std::memcpy(&M->fix[9 * (size_t)i], F, sizeof(F));
+    M->has_fix = true;
+  }
+  return GB_OK;
+}
 
 // Builds the tree tables of DataTpl (reference multibody/data.hxx:195-306) and
 // the device blob.
@@ -54,7 +133,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   int nq = 0, nv = 0, nff = 0;
   for (int i = 1; i < nj; ++i) {
     const int jt = M->jtype[i], p = M->parents[i];
-    if (jt < GB_JOINT_RX || jt > GB_JOINT_PZ)
+    if (jt < GB_JOINT_RX || jt > GB_JOINT_PRISMATIC_UNALIGNED)
       return set_error(GB_ERR_UNSUPPORTED, "joint " + std::to_string(i) + ": unsupported joint type");
     if (p < 0 || p >= i) return set_error(GB_ERR_INVALID_ARGUMENT, "parents[i] must satisfy 0 <= parents[i] < i");
     if (jt == GB_JOINT_FREEFLYER) {
@@ -73,6 +152,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   }
   M->nq = nq;
   M->nv = nv;
+  if (int rc = fold_unaligned(M, d, err)) return rc;
   if (d->armature && d->nv_armature != nv) return set_error(GB_ERR_SIZE, "armature must have nv entries");
   M->armature.assign(nv, 0.0);
   if (d->armature) M->armature.assign(d->armature, d->armature + nv);
@@ -183,6 +263,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.o_place_f = take(4 * 12 * nj); h.o_iner_f = take(4 * 10 * nj); h.o_arm_f = take(4 * nv);
   h.o_i6_d = take(8 * 21 * nj); h.o_i6_f = take(4 * 21 * nj);
   h.o_place_df = take(8 * 12 * nj); h.o_iner_df = take(8 * 10 * nj); h.o_arm_df = take(8 * nv);
+  h.o_fix = M->has_fix ? take(8 * 9 * nj) : 0;  // frame fixes of forward kinematics
   h.o_zero = take(16);
   // the per-instance kernels stage [0, stage_bytes) in shared memory; the row
   // lists below (O(nv^2) for deep trees) are read from global memory by the
@@ -224,6 +305,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   put_i(h.o_grp, grp);
   put_i(h.o_grp_rel, grp_rel);
   put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);
+  if (M->has_fix) put_d(h.o_fix, M->fix);
   put_f(h.o_place_f, M->placement); put_f(h.o_iner_f, M->inertia); put_f(h.o_arm_f, M->armature);
   {  // Y.matrix() per link (reference spatial/inertia.hpp:481-491), block-symmetric A, B, D
     std::vector<double> i6(21 * (size_t)nj, 0.0);

@@ -5,11 +5,13 @@ The reference builds a ``ModelTpl`` joint by joint with ``addJoint`` and
 in insertion order with ``parents[i] < i`` and the configuration / velocity
 indices ``idx_q`` / ``idx_v`` are cumulative in that order.  This module keeps
 that construction API for the joint types on the batched dynamics path
-(revolute about the unit x, y or z axis, prismatic along it, and the free-flyer)
-and flattens the tree into the plain tables the C ABI takes:
+(revolute about the unit x, y or z axis or any unit axis, prismatic along one, and the
+free-flyer) and flattens the tree into the plain tables the C ABI takes:
 
 * ``parents`` (int32, njoints), ``jtype`` (int32, njoints; 0 = universe,
-  1/2/3 = RX/RY/RZ, 4 = free-flyer, 5/6/7 = PX/PY/PZ),
+  1/2/3 = RX/RY/RZ, 4 = free-flyer, 5/6/7 = PX/PY/PZ, 8 = revolute unaligned,
+  9 = prismatic unaligned),
+* ``axis`` (njoints x 3: the unit axis of an unaligned joint, zero otherwise),
 * ``placement`` (njoints x 12: rotation row-major, then translation),
 * ``inertia`` (njoints x 10: mass, lever (COM), rotational inertia about the COM
   packed as [xx, xy, yy, xz, yz, zz] -- reference spatial/symmetric3.hpp:46-49),
@@ -19,10 +21,10 @@ from __future__ import annotations
 
 import numpy as np
 
-JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ = 0, 1, 2, 3, 4, 5, 6, 7
-_JT_NQ = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 7, JT_PX: 1, JT_PY: 1, JT_PZ: 1}
-_JT_NV = {JT_NONE: 0, JT_RX: 1, JT_RY: 1, JT_RZ: 1, JT_FF: 6, JT_PX: 1, JT_PY: 1, JT_PZ: 1}
-PRISMATIC = (JT_PX, JT_PY, JT_PZ)
+JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU = range(10)
+_JT_NQ = {JT_NONE: 0, JT_FF: 7, **{j: 1 for j in (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)}}
+_JT_NV = {JT_NONE: 0, JT_FF: 6, **{j: 1 for j in (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)}}
+PRISMATIC = (JT_PX, JT_PY, JT_PZ, JT_PU)
 
 
 class Convention:
@@ -34,6 +36,7 @@ class Convention:
 
 class JointModel:
     jtype = JT_NONE
+    axis = None
 
     @property
     def nq(self) -> int:
@@ -70,6 +73,32 @@ class JointModelPY(JointModel):
 
 class JointModelPZ(JointModel):
     jtype = JT_PZ
+
+
+def _unit(axis) -> np.ndarray:
+    a = np.asarray(axis, dtype=np.float64).reshape(3)
+    n = float(np.linalg.norm(a))
+    if not n > 0.0:
+        raise ValueError("joint axis must be non-zero")
+    return a / n
+
+
+class JointModelRevoluteUnaligned(JointModel):
+    """Revolute joint about a unit axis of its frame (reference JointModelRevoluteUnalignedTpl)."""
+
+    jtype = JT_RU
+
+    def __init__(self, axis):
+        self.axis = _unit(axis)
+
+
+class JointModelPrismaticUnaligned(JointModel):
+    """Prismatic joint along a unit axis of its frame (reference JointModelPrismaticUnalignedTpl)."""
+
+    jtype = JT_PU
+
+    def __init__(self, axis):
+        self.axis = _unit(axis)
 
 
 class SE3:
@@ -129,6 +158,7 @@ class Model:
         self.parents = [0]
         self.jtypes = [JT_NONE]
         self.jointPlacements = [SE3.Identity()]
+        self.axes = [np.zeros(3)]
         self.inertias = [Inertia.Zero()]
         self.armature = np.zeros(0)
         self.gravity = np.array([0.0, 0.0, -9.81, 0.0, 0.0, 0.0])
@@ -141,6 +171,7 @@ class Model:
         self.parents.append(int(parent_id))
         self.jtypes.append(int(joint.jtype))
         self.jointPlacements.append(placement)
+        self.axes.append(np.zeros(3) if joint.axis is None else np.array(joint.axis, dtype=np.float64))
         self.inertias.append(Inertia.Zero())
         self.names.append(name or f"joint_{self.njoints - 1}")
         self.armature = np.concatenate([self.armature, np.zeros(joint.nv)])
@@ -202,6 +233,7 @@ class Model:
             inertia=np.ascontiguousarray(inertia),
             armature=np.ascontiguousarray(self.armature, dtype=np.float64),
             gravity=np.ascontiguousarray(self.gravity, dtype=np.float64),
+            axis=np.ascontiguousarray(np.array(self.axes, dtype=np.float64).reshape(nj, 3)),
         )
 
     def subtree_tables(self) -> dict:

@@ -19,7 +19,9 @@ Workloads:
                      six revolute joints hanging off the torso (nq 33, nv 32);
   ``random_tree``    seeded trees with 0-3 children per node (optional free-flyer root);
   ``chain``          a revolute serial chain (100 links, masses U[0.1, 1] kg);
-  ``mixed_tree``     a ``random_tree`` of revolute and prismatic joints.
+  ``mixed_tree``     a ``random_tree`` of revolute and prismatic joints;
+  ``unaligned_tree`` a ``random_tree`` whose joints are, uniformly, aligned revolute,
+                     aligned prismatic, or revolute / prismatic about a random unit axis.
 """
 from __future__ import annotations
 
@@ -33,6 +35,8 @@ from .model import (
     JointModelPX,
     JointModelPY,
     JointModelPZ,
+    JointModelPrismaticUnaligned,
+    JointModelRevoluteUnaligned,
     JointModelRX,
     JointModelRY,
     JointModelRZ,
@@ -85,6 +89,16 @@ def _random_revolute(rng: np.random.Generator):
 
 def _random_one_dof(rng: np.random.Generator):
     return _ONE_DOF[int(rng.integers(0, 6))]()
+
+
+def _random_any_axis(rng: np.random.Generator):
+    k = int(rng.integers(0, 4))
+    if k == 0:
+        return _random_revolute(rng)
+    if k == 1:
+        return _ONE_DOF[3 + int(rng.integers(0, 3))]()
+    axis = rng.standard_normal(3)
+    return (JointModelRevoluteUnaligned if k == 2 else JointModelPrismaticUnaligned)(axis / np.linalg.norm(axis))
 
 
 def _add_link(model: Model, rng, parent: int, joint, name: str, mass_range=(0.5, 5.0)) -> int:
@@ -175,6 +189,13 @@ def mixed_tree(nv: int = 24, free_flyer: bool = True, seed: int = 5) -> Model:
     """``random_tree`` whose one-dof joints are revolute or prismatic (x / y / z), uniformly."""
     model = random_tree(nv, free_flyer, seed, joint=_random_one_dof)
     model.name = f"mixedtree{nv}{'ff' if free_flyer else ''}"
+    return model
+
+
+def unaligned_tree(nv: int = 14, free_flyer: bool = False, seed: int = 7) -> Model:
+    """``random_tree`` with aligned and unaligned revolute / prismatic joints."""
+    model = random_tree(nv, free_flyer, seed, joint=_random_any_axis)
+    model.name = f"unalignedtree{nv}{'ff' if free_flyer else ''}"
     return model
 
 

@@ -10,13 +10,14 @@ link into the parent body (reference: fixed joints become frames, their bodies a
 parent joint).  ``root_joint=JointModelFreeFlyer()`` puts a free-flyer between the universe and the
 root link, as the reference's ``buildModel(filename, root_joint, model)`` does.
 
-The batched kernels support one-dof joints along a coordinate axis: ``revolute`` and ``continuous``
-joints (JointModelRX/RY/RZ) and ``prismatic`` joints (JointModelPX/PY/PZ) with axis +-x, +-y or +-z.
-A negative axis is taken by a fixed half-turn F of the joint frame (F maps the axis to its
-opposite), so that the joint keeps the file's sign of q: the model's frame of that joint is the URDF
-joint frame times F, the link hung from it is placed by F^-1, and every joint-space quantity (q, v,
-tau, M, the derivatives) is the reference's.  Other joint types (planar, floating inside the tree)
-and axes off the coordinate axes raise ValueError.
+Joint axes map as in the reference (UrdfVisitor::addJoint and extractCartesianAxis,
+include/pinocchio/parsers/urdf/model.hxx:438-576): an axis equal to the unit x, y or z axis (to a
+relative 1e-12) gives JointModelRX/RY/RZ (``revolute``, ``continuous``) or JointModelPX/PY/PZ
+(``prismatic``); any other axis, negative ones included, gives JointModelRevoluteUnaligned /
+JointModelPrismaticUnaligned with the normalised axis.  One difference: the reference makes a
+``continuous`` joint a JointModelRevoluteUnbounded (nq = 2, q = (cos, sin)); here it is the bounded
+revolute joint (nq = 1, q = the angle), with the same dynamics in the angle.  Other joint types
+(planar, floating inside the tree) raise ValueError.
 
 ``save_model`` / ``load_model`` write and read the flattened tables (``Model.tables()`` plus the joint
 names) as one ``.npz`` file: the on-disk format of a model (the reference serialises ModelTpl with
@@ -31,15 +32,19 @@ import numpy as np
 from .model import (
     JT_FF,
     JT_NONE,
+    JT_PU,
     JT_PX,
     JT_PY,
     JT_PZ,
+    JT_RU,
     JT_RX,
     JT_RY,
     JT_RZ,
     Inertia,
     JointModel,
     JointModelFreeFlyer,
+    JointModelPrismaticUnaligned,
+    JointModelRevoluteUnaligned,
     Model,
     SE3,
 )
@@ -90,9 +95,9 @@ def _link_inertia(link) -> Inertia:
     return Inertia(mass, np.zeros(3), I).se3_action(_origin(inertial))
 
 
-# the half-turn that maps a coordinate axis to its opposite: about z for x and y, about x for z
-_FLIP = {0: np.diag([-1.0, -1.0, 1.0]), 1: np.diag([-1.0, -1.0, 1.0]), 2: np.diag([1.0, -1.0, -1.0])}
 _AXIS_JT = {"revolute": (JT_RX, JT_RY, JT_RZ), "continuous": (JT_RX, JT_RY, JT_RZ), "prismatic": (JT_PX, JT_PY, JT_PZ)}
+_UNALIGNED = {"revolute": JointModelRevoluteUnaligned, "continuous": JointModelRevoluteUnaligned,
+              "prismatic": JointModelPrismaticUnaligned}
 
 
 class _OneDof(JointModel):
@@ -100,17 +105,20 @@ class _OneDof(JointModel):
         self.jtype = jtype
 
 
-def _axis_joint(joint):
-    """(jtype, F) for a one-dof joint's axis; F the frame flip (None for a positive axis)."""
+def _axis_joint(joint) -> JointModel:
+    """The joint model of a one-dof URDF joint from its axis (reference extractCartesianAxis:
+    Eigen isApprox against the unit axes, precision 1e-12)."""
     ax = _floats(None if joint.find("axis") is None else joint.find("axis").get("xyz"), 3, [1, 0, 0])
-    n = np.linalg.norm(ax)
+    n = float(np.linalg.norm(ax))
     if n == 0:
         raise ValueError(f"joint {joint.get('name')!r}: zero axis")
-    ax = ax / n
-    k = int(np.argmax(np.abs(ax)))
-    if abs(abs(ax[k]) - 1.0) > 1e-12:
-        raise ValueError(f"joint {joint.get('name')!r}: axis {ax} is not a coordinate axis (unsupported)")
-    return _AXIS_JT[joint.get("type")][k], (None if ax[k] > 0 else _FLIP[k])
+    kind = joint.get("type")
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1.0
+        if np.linalg.norm(ax - e) <= 1e-12 * min(n, 1.0):
+            return _OneDof(_AXIS_JT[kind][k])
+    return _UNALIGNED[kind](ax / n)
 
 
 def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
@@ -157,12 +165,9 @@ def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
                 append(joint_id, child, Pj)
                 visit(child, (joint_id, Pj))
             elif jt in _AXIS_JT:
-                jtype, F = _axis_joint(j)
-                placement = Pj if F is None else SE3(Pj.rotation @ F, Pj.translation)
-                new_id = model.addJoint(joint_id, _OneDof(jtype), placement, j.get("name"))
-                child_in_joint = SE3.Identity() if F is None else SE3(F.T, np.zeros(3))
-                append(new_id, child, child_in_joint)
-                visit(child, (new_id, child_in_joint))
+                new_id = model.addJoint(joint_id, _axis_joint(j), Pj, j.get("name"))
+                append(new_id, child, SE3.Identity())
+                visit(child, (new_id, SE3.Identity()))
             else:
                 raise ValueError(f"joint {j.get('name')!r}: type {jt!r} is not supported by the batched kernels")
 
@@ -188,12 +193,20 @@ def load_model(path: str) -> Model:
     with np.load(path, allow_pickle=False) as z:
         parents, jtype = z["parents"], z["jtype"]
         placement, inertia = z["placement"], z["inertia"]
+        axis = z["axis"] if "axis" in z.files else np.zeros((len(parents), 3))
         names = [str(n) for n in z["names"]]
         model = Model()
         model.name = str(z["name"])
         for i in range(1, len(parents)):
             jt = int(jtype[i])
-            joint = JointModelFreeFlyer() if jt == JT_FF else _OneDof(jt)
+            if jt == JT_FF:
+                joint = JointModelFreeFlyer()
+            elif jt == JT_RU:
+                joint = JointModelRevoluteUnaligned(axis[i])
+            elif jt == JT_PU:
+                joint = JointModelPrismaticUnaligned(axis[i])
+            else:
+                joint = _OneDof(jt)
             if jt == JT_NONE:
                 raise ValueError("joint type 0 (universe) below the root")
             P = SE3(placement[i, :9].reshape(3, 3), placement[i, 9:])

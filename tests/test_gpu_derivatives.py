@@ -13,7 +13,7 @@ import pinocchio_gb300 as pg
 from oracle.oracle import OracleModel, symmetrize_upper
 from pinocchio_gb300 import _capi
 from pinocchio_gb300 import sample_models as sm
-from util import FP64_TOL, MIXED_TOL, MODELS, rel_err
+from util import FP64_TOL, MIXED_TOL, MODELS, mixed_tol, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -44,7 +44,7 @@ def test_rnea_derivatives(case, precision):
     data = pg.createData(model, precision)
     dq, dv, M = (t.cpu().numpy() for t in pg.computeRNEADerivatives(model, data, dev(q), dev(v), dev(a)))
     tau_o, dq_o, dv_o, M_o = om.rnea_derivatives(q, v, a)
-    tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
+    tol = fp64_tol(name) if precision == "fp64" else mixed_tol(name)
     assert rel_err(dq, dq_o) < tol
     assert rel_err(dv, dv_o) < tol
     assert rel_err(M, symmetrize_upper(M_o)) < tol
@@ -60,7 +60,7 @@ def test_aba_derivatives(case, precision):
     data = pg.createData(model, precision)
     dq, dv, Minv = (t.cpu().numpy() for t in pg.computeABADerivatives(model, data, dev(q), dev(v), dev(tau)))
     ddq_o, dq_o, dv_o, Minv_o = om.aba_derivatives(q, v, tau)
-    tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
+    tol = fp64_tol(name) if precision == "fp64" else mixed_tol(name)
     assert rel_err(data.ddq.cpu().numpy(), ddq_o) < tol
     assert rel_err(Minv, Minv_o) < tol
     assert rel_err(dq, dq_o) < tol
@@ -136,7 +136,7 @@ def test_aba_derivatives_vjp(case, precision):
     name, model, om, q, v, x, dev = case
     if precision == "mixed" and name not in MIXED_MODELS:
         pytest.skip("the mixed-precision bar applies to the benchmark models")
-    tol = fp64_tol(name) if precision == "fp64" else MIXED_TOL
+    tol = fp64_tol(name) if precision == "fp64" else mixed_tol(name)
     tau = 10.0 * x
     g = np.random.default_rng(5).standard_normal((q.shape[0], model.nv))
     data = pg.createData(model, precision)

@@ -13,7 +13,7 @@ import pinocchio_gb300 as pg
 from pinocchio_gb300 import _capi
 from oracle.oracle import LOCAL, WORLD, OracleModel, symmetrize_upper
 from pinocchio_gb300 import sample_models as sm
-from util import FP64_TOL, MIXED_TOL, MODELS, rel_err
+from util import FP64_TOL, MODELS, mixed_tol, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -33,7 +33,7 @@ def test_rnea(case, precision):
     name, model, om, q, v, a, dev = case
     data = pg.createData(model, precision)
     tau = pg.rnea(model, data, dev(q), dev(v), dev(a)).cpu().numpy()
-    assert rel_err(tau, om.rnea(q, v, a)) < (FP64_TOL if precision == "fp64" else MIXED_TOL)
+    assert rel_err(tau, om.rnea(q, v, a)) < (FP64_TOL if precision == "fp64" else mixed_tol(name))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -43,7 +43,7 @@ def test_aba(case, precision, convention):
     tau = 10.0 * x
     data = pg.createData(model, precision)
     ddq = pg.aba(model, data, dev(q), dev(v), dev(tau), convention).cpu().numpy()
-    assert rel_err(ddq, om.aba(q, v, tau, convention)) < (FP64_TOL if precision == "fp64" else MIXED_TOL)
+    assert rel_err(ddq, om.aba(q, v, tau, convention)) < (FP64_TOL if precision == "fp64" else mixed_tol(name))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -52,7 +52,7 @@ def test_crba(case, precision):
     data = pg.createData(model, precision)
     Mref = om.crba(q)
     M = pg.crba(model, data, dev(q)).cpu().numpy()
-    assert rel_err(M, symmetrize_upper(Mref)) < (FP64_TOL if precision == "fp64" else MIXED_TOL)
+    assert rel_err(M, symmetrize_upper(Mref)) < (FP64_TOL if precision == "fp64" else mixed_tol(name))
     Mu = pg.crba(model, data, dev(q), symmetric=False).cpu().numpy()
     if precision == "fp64":
         # block-upper output: every entry outside the joint-diagonal blocks and below the diagonal is zero

@@ -8,7 +8,7 @@ import pinocchio_gb300 as pg
 from oracle.oracle import LOCAL, OracleModel
 from pinocchio_gb300 import api, autotune
 from pinocchio_gb300 import sample_models as sm
-from util import FP64_TOL, MIXED_TOL, rel_err
+from util import FP64_TOL, MIXED_TOL, mixed_tol, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -136,7 +136,7 @@ def test_warp_layout_matches_thread_layout_bitwise(name, precision):
             else:
                 assert rel_err(b, a) < 1e-6, (layout, k, rel_err(b, a))
     om = OracleModel(model)
-    tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else MIXED_TOL
+    tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else mixed_tol(name)
     if precision == "fp64" or name != "chain100":
         for layout in layouts[1:]:
             assert rel_err(outs[layout][0], om.rnea(q, v, x)) < tol
@@ -190,7 +190,7 @@ def test_team_layouts_aba_derivatives(name, precision):
                 assert rel_err(b, a) < 1e-6, (layout, k, rel_err(b, a))
     if precision == "fp64" or name != "chain100":
         ddq_o, dq_o, dv_o, Minv_o = OracleModel(model).aba_derivatives(q, v, tau)
-        tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else MIXED_TOL
+        tol = (1e-10 if name == "chain100" else FP64_TOL) if precision == "fp64" else mixed_tol(name)
         w = outs[pg._capi.GB_INSTANCE_PER_WARP]
         assert rel_err(w[0], dq_o) < tol and rel_err(w[1], dv_o) < tol and rel_err(w[2], Minv_o) < tol
         assert rel_err(w[3], ddq_o) < tol

@@ -14,7 +14,7 @@ import pinocchio_gb300 as pg
 from oracle.oracle import LOCAL, OracleModel, symmetrize_upper
 from pinocchio_gb300 import _capi
 from pinocchio_gb300 import sample_models as sm
-from util import FP64_TOL, MIXED_TOL, MODELS, rel_err
+from util import FP64_TOL, MODELS, mixed_tol, rel_err
 
 pytestmark = pytest.mark.gpu
 MIXED_MODELS = [n for n in MODELS if n != "chain100"]
@@ -32,7 +32,7 @@ def case(request):
 
 def _tol(name, precision):
     if precision == "mixed":
-        return MIXED_TOL
+        return mixed_tol(name)
     return 1e-10 if name == "chain100" else FP64_TOL
 
 

@@ -16,7 +16,8 @@ from pinocchio_gb300 import model as gm
 from pinocchio_gb300 import sample_models as sm
 from util import MODELS, rel_err
 
-CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100", "mixedtree12", "mixedtree24ff"]
+CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100", "mixedtree12", "mixedtree24ff",
+              "unaligned14", "unaligned20ff"]
 
 
 @pytest.fixture(scope="module", params=CPU_MODELS)
@@ -92,7 +93,7 @@ def _fd(f, x0, h, k, integrate=None):
     return (f(x0 + e) - f(x0 - e)) / (2 * h)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff"])
 def test_derivatives_vs_central_fd(name):
     model = MODELS[name]()
     om = OracleModel(model)
@@ -199,6 +200,49 @@ def test_kat_prismatic_slide():
         assert rel_err(OracleModel(model).rnea(q, v, a), tau) < 1e-13
 
 
+def _rebuild(model, joint_of):
+    """The same tree with joint i replaced by joint_of(i, jtype)."""
+    out = gm.Model()
+    for i in range(1, model.njoints):
+        out.addJoint(model.parents[i], joint_of(i, model.jtypes[i]), model.jointPlacements[i], model.names[i])
+        out.inertias[i] = model.inertias[i]
+    return out
+
+
+def test_unaligned_joints_on_coordinate_axes():
+    """A revolute / prismatic unaligned joint about +e_k is JointModelR{X,Y,Z} / P{X,Y,Z};
+    about -e_k it is that joint with its coordinate negated."""
+    model = MODELS["mixedtree12"]()
+    rng = np.random.default_rng(5)
+    q, v, a = sm.random_inputs(model, 16, 6)
+    ref = OracleModel(model)
+    axis_of = lambda jt: np.eye(3)[(jt - gm.JT_PX) if jt in gm.PRISMATIC else (jt - gm.JT_RX)]  # noqa: E731
+    kind = lambda jt: gm.JointModelPrismaticUnaligned if jt in gm.PRISMATIC else gm.JointModelRevoluteUnaligned  # noqa: E731
+    plus = OracleModel(_rebuild(model, lambda i, jt: kind(jt)(axis_of(jt))))
+    assert rel_err(plus.rnea(q, v, a), ref.rnea(q, v, a)) < 1e-14
+    assert rel_err(plus.aba(q, v, a), ref.aba(q, v, a)) < 1e-13
+    D = np.where(rng.random(model.nv) < 0.5, -1.0, 1.0)  # flip a random subset of the joints
+    flip = OracleModel(_rebuild(model, lambda i, jt: kind(jt)(D[model.idx_vs[i]] * axis_of(jt))))
+    assert rel_err(flip.rnea(q * D, v * D, a * D), ref.rnea(q, v, a) * D) < 1e-13
+
+
+def test_kat_tilted_pendulum():
+    """A point mass m at distance L from an axis a tilted by b from the vertical (COM
+    perpendicular to a, down-slope at q = 0): tau = m L^2 q'' + m g L sin(b) sin q."""
+    m, L, b, g = 1.3, 0.8, 0.6, 9.81
+    a = np.array([np.sin(b), 0.0, np.cos(b)])  # tilted about y
+    c = L * np.array([np.cos(b), 0.0, -np.sin(b)])  # perpendicular to a, down-slope
+    model = gm.Model()
+    j = model.addJoint(0, gm.JointModelRevoluteUnaligned(a), gm.SE3.Identity(), "pivot")
+    model.appendBodyToJoint(j, gm.Inertia(m, c, np.zeros((3, 3))))
+    om = OracleModel(model)
+    rng = np.random.default_rng(7)
+    q, v, acc = rng.uniform(-np.pi, np.pi, (16, 1)), rng.standard_normal((16, 1)), rng.standard_normal((16, 1))
+    tau = m * L * L * acc + m * g * L * np.sin(b) * np.sin(q)
+    assert rel_err(om.rnea(q, v, acc), tau) < 1e-13
+    assert rel_err(om.aba(q, v, tau), acc) < 1e-12
+
+
 def free_body(m=3.0, I=(0.2, 0.3, 0.4)):
     model = gm.Model()
     j = model.addJoint(0, gm.JointModelFreeFlyer(), gm.SE3.Identity(), "base")
@@ -269,7 +313,7 @@ def test_forward_kinematics_and_jacobians_agree(case):
     assert np.array_equal(om.forward_kinematics(q)[0], oMi)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff"])
 def test_forward_kinematics_acceleration_vs_fd(name):
     """data.a[i] is the time derivative of the joint-frame velocity data.v[i]
     along (q + dt v, v + dt a): central differences, step 1e-6."""

@@ -15,6 +15,12 @@ from util import MODELS, rel_err
 _AX = {gm.JT_RX: "1 0 0", gm.JT_RY: "0 1 0", gm.JT_RZ: "0 0 1", gm.JT_PX: "1 0 0", gm.JT_PY: "0 1 0", gm.JT_PZ: "0 0 1"}
 
 
+def _axis_text(model, i):
+    if model.jtypes[i] in (gm.JT_RU, gm.JT_PU):
+        return " ".join(_f(x) for x in model.axes[i])
+    return _AX[model.jtypes[i]]
+
+
 def _rpy_of(R):
     """roll, pitch, yaw with R = Rz(yaw) Ry(pitch) Rx(roll)."""
     pitch = np.arcsin(-np.clip(R[2, 0], -1.0, 1.0))
@@ -55,13 +61,13 @@ def to_urdf(model, skip_free_flyer=True):
         out.append(f'<link name="link{i}">{_inertial(model.inertias[i])}</link>')
         kind = "prismatic" if model.jtypes[i] in gm.PRISMATIC else "revolute"
         out.append(f'<joint name="{model.names[i]}" type="{kind}"><parent link="{link_of[model.parents[i]]}"/>'
-                   f'<child link="link{i}"/>{_origin(model.jointPlacements[i])}<axis xyz="{_AX[model.jtypes[i]]}"/>'
+                   f'<child link="link{i}"/>{_origin(model.jointPlacements[i])}<axis xyz="{_axis_text(model, i)}"/>'
                    f'<limit lower="-3" upper="3" effort="1" velocity="1"/></joint>')
     out.append("</robot>")
     return "\n".join(out)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "tree12", "chain100", "mixedtree12"])
+@pytest.mark.parametrize("name", ["manipulator6r", "tree12", "chain100", "mixedtree12", "unaligned14"])
 def test_urdf_round_trip(name):
     model = MODELS[name]()
     back = pg.buildModelFromXML(to_urdf(model))
@@ -69,6 +75,7 @@ def test_urdf_round_trip(name):
     assert np.array_equal(a["parents"], b["parents"]) and np.array_equal(a["jtype"], b["jtype"])
     assert np.abs(a["placement"] - b["placement"]).max() < 1e-12
     assert np.abs(a["inertia"] - b["inertia"]).max() < 1e-12
+    assert np.abs(a["axis"] - b["axis"]).max() < 1e-15
 
 
 def test_urdf_free_flyer_root():
@@ -145,7 +152,7 @@ def test_urdf_prismatic_negative_axis():
 </robot>"""
     plus = pg.buildModelFromXML(doc.replace("AXIS", "1 0 0"))
     minus = pg.buildModelFromXML(doc.replace("AXIS", "-1 0 0"))
-    assert plus.jtypes[1:] == [gm.JT_PX, gm.JT_RY] and minus.jtypes[1:] == [gm.JT_PX, gm.JT_RY]
+    assert plus.jtypes[1:] == [gm.JT_PX, gm.JT_RY] and minus.jtypes[1:] == [gm.JT_PU, gm.JT_RY]
     rng = np.random.default_rng(2)
     q, v, a = (rng.standard_normal((16, 2)) for _ in range(3))
     D = np.array([-1.0, 1.0])
@@ -166,9 +173,8 @@ def gm_rz(t):
 
 @pytest.mark.parametrize("bad,msg", [
     ('<joint name="s" type="planar"><parent link="a"/><child link="b"/><axis xyz="1 0 0"/></joint>', "not supported"),
-    ('<joint name="s" type="prismatic"><parent link="a"/><child link="b"/><axis xyz="0 0.6 0.8"/></joint>',
-     "coordinate axis"),
-    ('<joint name="s" type="revolute"><parent link="a"/><child link="b"/><axis xyz="1 1 0"/></joint>', "coordinate axis"),
+    ('<joint name="s" type="floating"><parent link="a"/><child link="b"/></joint>', "not supported"),
+    ('<joint name="s" type="revolute"><parent link="a"/><child link="b"/><axis xyz="0 0 0"/></joint>', "zero axis"),
 ])
 def test_urdf_unsupported(bad, msg):
     xml = f'<robot name="x"><link name="a"/><link name="b"/>{bad}</robot>'
@@ -176,8 +182,26 @@ def test_urdf_unsupported(bad, msg):
         pg.buildModelFromXML(xml)
 
 
-def test_urdf_file_and_model_file(tmp_path):
-    model = MODELS["tree12"]()
+@pytest.mark.parametrize("kind", ["revolute", "prismatic"])
+def test_urdf_unaligned_axis(kind):
+    """An axis off the unit axes (negative ones included) gives the unaligned joint with the
+    normalised axis, as the reference's extractCartesianAxis; an axis equal to a unit axis
+    up to 1e-12 (relative) gives the aligned joint."""
+    doc = f"""<robot name="u"><link name="a"/><link name="b"><inertial><mass value="1"/>
+      <inertia ixx="0.1" ixy="0" ixz="0" iyy="0.1" iyz="0" izz="0.1"/></inertial></link>
+      <joint name="s" type="{kind}"><parent link="a"/><child link="b"/><axis xyz="AXIS"/></joint></robot>"""
+    m = pg.buildModelFromXML(doc.replace("AXIS", "0 3 4"))
+    assert m.jtypes[1] == (gm.JT_PU if kind == "prismatic" else gm.JT_RU)
+    assert np.allclose(m.axes[1], [0, 0.6, 0.8], rtol=0, atol=1e-16)
+    m = pg.buildModelFromXML(doc.replace("AXIS", "0 0 -1"))
+    assert m.jtypes[1] == (gm.JT_PU if kind == "prismatic" else gm.JT_RU)
+    m = pg.buildModelFromXML(doc.replace("AXIS", "0 1e-14 1"))
+    assert m.jtypes[1] == (gm.JT_PZ if kind == "prismatic" else gm.JT_RZ)
+
+
+@pytest.mark.parametrize("name", ["tree12", "unaligned14"])
+def test_urdf_file_and_model_file(tmp_path, name):
+    model = MODELS[name]()
     path = tmp_path / "tree.urdf"
     path.write_text(to_urdf(model))
     loaded = pg.buildModelFromUrdf(str(path))
