@@ -125,10 +125,35 @@ int gb_nonlinear_effects(const gb_model* model, int precision, int layout, long 
 int gb_generalized_gravity(const gb_model* model, int precision, int layout, long batch, const double* q, double* g,
                            void* stream);
 
+/* External forces.  fext holds, per instance, njoints x 6 values: the force
+ * [linear; angular] applied to joint i, expressed in joint i's own frame, as
+ * the reference's container::aligned_vector<Force> fext of size model.njoints
+ * (joint 0's entries are not read); in `layout` like the other arrays (an
+ * instance's 6 * njoints values contiguous, or value-major with stride batch).
+ * These calls run one thread per configuration whatever layout the model has. */
+
+/* tau = rnea(model, data, q, v, a, fext) (reference algorithm/rnea.hxx:164-218,
+ * public rnea.hpp:74-79, rnea.hxx:784-793): f_i -= fext_i after the forward
+ * step of joint i. */
+int gb_rnea_fext(const gb_model* model, int precision, int layout, long batch, const double* q, const double* v,
+                 const double* a, const double* fext, double* tau, void* stream);
+
+/* tau = computeStaticTorque(model, data, q, fext) = the generalized gravity minus
+ * the joint torques of fext (reference algorithm/rnea.hxx:448-489, public
+ * rnea.hpp:159-167, rnea.hxx:828-837). */
+int gb_static_torque(const gb_model* model, int precision, int layout, long batch, const double* q,
+                     const double* fext, double* tau, void* stream);
+
 /* ddq = aba(model, data, q, v, tau, convention) for every instance
  * (reference algorithm/aba.hxx:933-948; WORLD 242-293, LOCAL 486-540). */
 int gb_aba(const gb_model* model, int precision, int convention, int layout, long batch, const double* q,
            const double* v, const double* tau, double* ddq, void* stream);
+
+/* ddq = aba(model, data, q, v, tau, fext, convention) (reference
+ * algorithm/aba.hxx:958-973; WORLD 296-357, LOCAL 543-605): the bias force of
+ * joint i is v_i x* (I_i v_i) - fext_i. */
+int gb_aba_fext(const gb_model* model, int precision, int convention, int layout, long batch, const double* q,
+                const double* v, const double* tau, const double* fext, double* ddq, void* stream);
 
 /* M = crba(model, data, q, convention) (reference algorithm/crba.hxx:602-617),
  * upper triangle (GB_MATRIX_UPPER, the lower part is written as zero) or full
@@ -145,12 +170,27 @@ int gb_rnea_derivatives(const gb_model* model, int precision, int matrix_mode, i
                         const double* q, const double* v, const double* a, double* dtau_dq, double* dtau_dv,
                         double* M, double* tau, void* stream);
 
+/* computeRNEADerivatives(model, data, q, v, a, fext) (reference
+ * algorithm/rnea-derivatives.hxx:550-633, public 728-750, 772-790): the world
+ * force of joint i is reduced by oMi.act(fext_i) before the backward sweep. */
+int gb_rnea_derivatives_fext(const gb_model* model, int precision, int matrix_mode, int layout, long batch,
+                             const double* q, const double* v, const double* a, const double* fext, double* dtau_dq,
+                             double* dtau_dv, double* M, double* tau, void* stream);
+
 /* computeABADerivatives(model, data, q, v, tau) -> (ddq_dq, ddq_dv, Minv)
  * (reference algorithm/aba-derivatives.hxx:380-453, public 910-1051).  Minv
  * is returned symmetric.  ddq may be NULL. */
 int gb_aba_derivatives(const gb_model* model, int precision, int layout, long batch, const double* q,
                        const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                        double* ddq, void* stream);
+
+/* computeABADerivatives(model, data, q, v, tau, fext) (reference
+ * algorithm/aba-derivatives.hxx:463-541, public 930-950, 978-990): oMi.act(fext_i)
+ * is subtracted from the world force of joint i after the first and the
+ * second forward sweep. */
+int gb_aba_derivatives_fext(const gb_model* model, int precision, int layout, long batch, const double* q,
+                            const double* v, const double* tau, const double* fext, double* ddq_dq,
+                            double* ddq_dv, double* Minv, double* ddq, void* stream);
 
 /* Minv = computeMinverse(model, data, q) (reference algorithm/aba.hxx:838-880,
  * public aba.hpp:101-109): the reference fills the upper triangle

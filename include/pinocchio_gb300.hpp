@@ -150,6 +150,39 @@ inline void computeABADerivatives(const Model& m, int precision, long batch, con
   check(gb_aba_derivatives(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, tau, ddq_dq, ddq_dv, Minv, nullptr,
                            stream));
 }
+
+// ---- external forces: the reference's fext overloads (rnea.hxx:164-218, 448-489;
+// aba.hxx:958-973; rnea-derivatives.hxx:550-633; aba-derivatives.hxx:463-541).
+// `data` holds batch x njoints x 6 doubles on the device: per configuration, the
+// force [linear; angular] on each joint in that joint's frame (joint 0 not read).
+// A distinct type keeps these overloads apart from the ones without forces.
+struct ExternalForces {
+  const double* data;
+};
+inline void rnea(const Model& m, int precision, long batch, const double* q, const double* v, const double* a,
+                 ExternalForces fext, double* tau, void* stream = nullptr) {
+  check(gb_rnea_fext(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, a, fext.data, tau, stream));
+}
+inline void computeStaticTorque(const Model& m, int precision, long batch, const double* q, ExternalForces fext,
+                                double* tau, void* stream = nullptr) {
+  check(gb_static_torque(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, fext.data, tau, stream));
+}
+inline void aba(const Model& m, int precision, long batch, const double* q, const double* v, const double* tau,
+                ExternalForces fext, double* ddq, int convention = GB_LOCAL, void* stream = nullptr) {
+  check(gb_aba_fext(m.get(), precision, convention, GB_LAYOUT_INSTANCE, batch, q, v, tau, fext.data, ddq, stream));
+}
+inline void computeRNEADerivatives(const Model& m, int precision, long batch, const double* q, const double* v,
+                                   const double* a, ExternalForces fext, double* dtau_dq, double* dtau_dv, double* M,
+                                   void* stream = nullptr) {
+  check(gb_rnea_derivatives_fext(m.get(), precision, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, batch, q, v, a, fext.data,
+                                 dtau_dq, dtau_dv, M, nullptr, stream));
+}
+inline void computeABADerivatives(const Model& m, int precision, long batch, const double* q, const double* v,
+                                  const double* tau, ExternalForces fext, double* ddq_dq, double* ddq_dv, double* Minv,
+                                  void* stream = nullptr) {
+  check(gb_aba_derivatives_fext(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, tau, fext.data, ddq_dq, ddq_dv,
+                                Minv, nullptr, stream));
+}
 inline void computeMinverse(const Model& m, int precision, long batch, const double* q, double* Minv,
                             void* stream = nullptr) {
   check(gb_compute_minverse(m.get(), precision, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, batch, q, Minv, stream));

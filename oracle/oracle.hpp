@@ -691,11 +691,28 @@ template <class T> inline T dot6p(const T* a, const T* b) {
   return s;
 }
 
+// External forces: fext holds njoints x 6 values [linear; angular], the force on
+// joint i expressed in joint i's frame (the reference's aligned_vector<Force> of
+// size njoints, algorithm/rnea.hpp:60-79); NULL for none.  f -= fext_i
+// (joint frame) or f -= oMi.act(fext_i) (world frame).
+template <class T> inline void sub_fext_local(const T* fext, int i, Vec6<T>& f) {
+  if (!fext) return;
+  for (int k = 0; k < 6; ++k) f.v[k] -= fext[6 * i + k];
+}
+template <class T> inline void sub_fext_world(const T* fext, int i, const SE3<T>& oMi, Vec6<T>& f) {
+  if (!fext) return;
+  Vec6<T> fl;
+  for (int k = 0; k < 6; ++k) fl.v[k] = fext[6 * i + k];
+  const Vec6<T> fw = act_force(oMi, fl);
+  for (int k = 0; k < 6; ++k) f.v[k] -= fw.v[k];
+}
+
 // ---------------------------------------------------------------------------
-// RNEA (algorithm/rnea.hxx:24-161)
+// RNEA (algorithm/rnea.hxx:24-161); with fext rnea.hxx:164-218 (f_i -= fext_i,
+// line 205)
 // ---------------------------------------------------------------------------
 template <class T>
-void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
+void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a, const T* fext = nullptr) {
   std::fill(d.tau.begin(), d.tau.end(), T(0));
   d.v[0] = zero6<T>();
   for (int k = 0; k < 6; ++k) d.a_gf[0].v[k] = -T(m.gravity[k]);
@@ -714,6 +731,7 @@ void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
     d.h[i] = iner_mul(Y, d.v[i]);
     d.f[i] = iner_mul(Y, d.a_gf[i]);
     d.f[i] = add6(d.f[i], cross_force(d.v[i], d.h[i]));
+    sub_fext_local(fext, i, d.f[i]);
   }
   for (int i = m.njoints - 1; i > 0; --i) {  // RneaBackwardStep (rnea.hxx:83-108)
     const int p = m.parents[i], iv = m.idx_v[i];
@@ -726,8 +744,9 @@ void rnea(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
 // ---------------------------------------------------------------------------
 // ABA, LOCAL convention (algorithm/aba.hxx:360-540)
 // ---------------------------------------------------------------------------
+// with fext: aba.hxx:543-605 (f_i -= fext_i after the forward step, line 584)
 template <class T>
-void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau) {
+void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, const T* fext = nullptr) {
   d.v[0] = zero6<T>();
   for (int k = 0; k < 6; ++k) d.a_gf[0].v[k] = -T(m.gravity[k]);
   d.f[0] = zero6<T>();
@@ -744,6 +763,7 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
     d.Yaba[i] = iner_matrix(Y);
     d.h[i] = iner_mul(Y, d.v[i]);
     d.f[i] = cross_force(d.v[i], d.h[i]);
+    sub_fext_local(fext, i, d.f[i]);
   }
   for (int i = m.njoints - 1; i > 0; --i) {  // AbaLocalConventionBackwardStep (aba.hxx:402-434)
     const int p = m.parents[i], jt = m.jtype[i], iv = m.idx_v[i], nvj = m.nvs[i];
@@ -900,12 +920,16 @@ void world_forward1(const Model& m, Data<T>& d, const T* q, const T* v, int i) {
 // ABA, WORLD convention (algorithm/aba.hxx:85-293); abaInParallel uses it
 // (algorithm/parallel/aba.hpp:82).
 // ---------------------------------------------------------------------------
+// with fext: aba.hxx:296-352 (of_i -= oMi.act(fext_i) after the forward step, line 336)
 template <class T>
-void aba_world(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau) {
+void aba_world(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, const T* fext = nullptr) {
   for (int k = 0; k < 6; ++k) d.oa_gf[0].v[k] = -T(m.gravity[k]);
   d.of[0] = zero6<T>();
   for (int k = 0; k < m.nv; ++k) d.u[k] = tau[k];
-  for (int i = 1; i < m.njoints; ++i) world_forward1(m, d, q, v, i);
+  for (int i = 1; i < m.njoints; ++i) {
+    world_forward1(m, d, q, v, i);
+    sub_fext_world(fext, i, d.oMi[i], d.of[i]);
+  }
   for (int i = m.njoints - 1; i > 0; --i) {
     world_schur(m, d, i);
     if (m.parents[i] > 0) world_schur_update(m, d, i);
@@ -931,9 +955,9 @@ void aba_world(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau)
 }
 
 template <class T>
-void aba(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, int conv) {
-  if (conv == WORLD) aba_world(m, d, q, v, tau);
-  else aba_local(m, d, q, v, tau);
+void aba(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, int conv, const T* fext = nullptr) {
+  if (conv == WORLD) aba_world(m, d, q, v, tau, fext);
+  else aba_local(m, d, q, v, tau, fext);
 }
 
 // ---------------------------------------------------------------------------
@@ -1014,7 +1038,8 @@ void cholesky_decompose(const Model& m, Data<T>& d) {
 // Outputs d.dtau_dq, d.dtau_dv (row-major), d.M (upper triangle + armature), d.tau.
 // ---------------------------------------------------------------------------
 template <class T>
-void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
+// with fext: rnea-derivatives.hxx:550-633 (of_i -= oMi.act(fext_i) after the forward step, line 596)
+void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* a, const T* fext = nullptr) {
   const int nv = m.nv;
   if (m.gravity[3] != 0.0 || m.gravity[4] != 0.0 || m.gravity[5] != 0.0)
     throw std::invalid_argument("The gravity must be a pure force vector, no angular part");
@@ -1041,6 +1066,7 @@ void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const 
     for (int k = 0; k < 6; ++k) d.oa_gf[i].v[k] = d.oa[i].v[k] - g.v[k];
     d.oh[i] = iner_mul(d.oYcrb[i], d.ov[i]);
     d.of[i] = add6(iner_mul(d.oYcrb[i], d.oa_gf[i]), cross_force(d.ov[i], d.oh[i]));
+    sub_fext_world(fext, i, d.oMi[i], d.of[i]);
     for (int k = 0; k < nvj; ++k) {
       const int c = iv + k;
       const Vec6<T> Jc = act_motion(d.oMi[i], S_col<T>(m, i, k));
@@ -1131,8 +1157,10 @@ void rnea_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const 
 // ABA derivatives (algorithm/aba-derivatives.hxx:22-453).
 // Outputs d.ddq, d.ddq_dq, d.ddq_dv, d.Minv (full symmetric; row-major).
 // ---------------------------------------------------------------------------
+// with fext: aba-derivatives.hxx:463-541 (of_i -= oMi.act(fext_i) after forward
+// steps 1 and 2, lines 513 and 529)
 template <class T>
-void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau) {
+void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, const T* fext = nullptr) {
   const int nv = m.nv;
   if (m.gravity[3] != 0.0 || m.gravity[4] != 0.0 || m.gravity[5] != 0.0)
     throw std::invalid_argument("The gravity must be a pure force vector, no angular part");
@@ -1143,7 +1171,10 @@ void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T
   std::vector<T>& Minv = d.Minv;
   for (int r = 0; r < nv; ++r)
     for (int c = r; c < nv; ++c) Minv[(size_t)r * nv + c] = T(0);
-  for (int i = 1; i < m.njoints; ++i) world_forward1(m, d, q, v, i);  // ForwardStep1 (22-80)
+  for (int i = 1; i < m.njoints; ++i) {  // ForwardStep1 (22-80)
+    world_forward1(m, d, q, v, i);
+    sub_fext_world(fext, i, d.oMi[i], d.of[i]);
+  }
   std::vector<T>& Fcrb = d.Fcrb[0];
   std::fill(Fcrb.begin(), Fcrb.end(), T(0));
   for (int i = m.njoints - 1; i > 0; --i) {  // BackwardStep1 (87-171)
@@ -1200,6 +1231,7 @@ void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T
     }
     for (int k = 0; k < 6; ++k) d.oa[i].v[k] = d.oa_gf[i].v[k] + g.v[k];
     d.of[i] = add6(iner_mul(d.oYcrb[i], d.oa_gf[i]), cross_force(d.ov[i], d.oh[i]));
+    sub_fext_world(fext, i, d.oMi[i], d.of[i]);
     if (p > 0)
       for (int r = 0; r < nvj; ++r)
         for (int c = iv; c < nv; ++c) {

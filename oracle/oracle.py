@@ -52,6 +52,10 @@ def lib():
         L.orc_cholesky.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_rnea_derivatives.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_aba_derivatives.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_rnea_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_aba_fext.argtypes = [vp, C.c_int, C.c_int, C.c_long, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_rnea_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_aba_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_joint_jacobians.argtypes = [vp, C.c_int, C.c_long, vp, vp, C.c_int]
@@ -97,17 +101,33 @@ class OracleModel:
         if rc != 0:
             raise ValueError(lib().orc_last_error().decode())
 
-    # all methods: prec 0 = double, 1 = long double; nthreads 0 = all cores
-    def rnea(self, q, v, a, prec=0, nthreads=0):
+    # all methods: prec 0 = double, 1 = long double; nthreads 0 = all cores.
+    # fext (rnea, aba and the derivatives): external forces, (B, njoints, 6) [linear;
+    # angular] in the joint frames, or None.
+    def _fext(self, fext, B):
+        f = _c(fext).reshape(B, -1)
+        if f.shape[1] != 6 * self.njoints:
+            raise ValueError("fext must hold njoints x 6 values per instance")
+        return f
+
+    def rnea(self, q, v, a, prec=0, nthreads=0, fext=None):
         q, v, a = _c(q), _c(v), _c(a)
         tau = np.empty((q.shape[0], self.nv))
-        self._check(lib().orc_rnea(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(a), _ptr(tau), nthreads))
+        if fext is None:
+            self._check(lib().orc_rnea(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(a), _ptr(tau), nthreads))
+        else:
+            f = self._fext(fext, q.shape[0])
+            self._check(lib().orc_rnea_fext(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(a), _ptr(f), _ptr(tau), nthreads))
         return tau
 
-    def aba(self, q, v, tau, convention=LOCAL, prec=0, nthreads=0):
+    def aba(self, q, v, tau, convention=LOCAL, prec=0, nthreads=0, fext=None):
         q, v, tau = _c(q), _c(v), _c(tau)
         ddq = np.empty((q.shape[0], self.nv))
-        self._check(lib().orc_aba(self.h, prec, convention, q.shape[0], _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), nthreads))
+        if fext is None:
+            self._check(lib().orc_aba(self.h, prec, convention, q.shape[0], _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), nthreads))
+        else:
+            f = self._fext(fext, q.shape[0])
+            self._check(lib().orc_aba_fext(self.h, prec, convention, q.shape[0], _ptr(q), _ptr(v), _ptr(tau), _ptr(f), _ptr(ddq), nthreads))
         return ddq
 
     def crba(self, q, convention=LOCAL, prec=0, nthreads=0):
@@ -124,22 +144,30 @@ class OracleModel:
         self._check(lib().orc_cholesky(self.h, prec, M.shape[0], _ptr(M), _ptr(U), _ptr(D), nthreads))
         return U, D
 
-    def rnea_derivatives(self, q, v, a, prec=0, nthreads=0):
+    def rnea_derivatives(self, q, v, a, prec=0, nthreads=0, fext=None):
         """(tau, dtau_dq, dtau_dv, M upper)."""
         q, v, a = _c(q), _c(v), _c(a)
         B, nv = q.shape[0], self.nv
         tau = np.empty((B, nv))
         dq, dv, M = (np.empty((B, nv, nv)) for _ in range(3))
-        self._check(lib().orc_rnea_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(tau), _ptr(dq), _ptr(dv), _ptr(M), nthreads))
+        if fext is None:
+            self._check(lib().orc_rnea_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(tau), _ptr(dq), _ptr(dv), _ptr(M), nthreads))
+        else:
+            f = self._fext(fext, B)
+            self._check(lib().orc_rnea_derivatives_fext(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(f), _ptr(tau), _ptr(dq), _ptr(dv), _ptr(M), nthreads))
         return tau, dq, dv, M
 
-    def aba_derivatives(self, q, v, tau, prec=0, nthreads=0):
+    def aba_derivatives(self, q, v, tau, prec=0, nthreads=0, fext=None):
         """(ddq, ddq_dq, ddq_dv, Minv)."""
         q, v, tau = _c(q), _c(v), _c(tau)
         B, nv = q.shape[0], self.nv
         ddq = np.empty((B, nv))
         dq, dv, Minv = (np.empty((B, nv, nv)) for _ in range(3))
-        self._check(lib().orc_aba_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), _ptr(dq), _ptr(dv), _ptr(Minv), nthreads))
+        if fext is None:
+            self._check(lib().orc_aba_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), _ptr(dq), _ptr(dv), _ptr(Minv), nthreads))
+        else:
+            f = self._fext(fext, B)
+            self._check(lib().orc_aba_derivatives_fext(self.h, prec, B, _ptr(q), _ptr(v), _ptr(tau), _ptr(f), _ptr(ddq), _ptr(dq), _ptr(dv), _ptr(Minv), nthreads))
         return ddq, dq, dv, Minv
 
     def integrate(self, q, v, prec=0, nthreads=0):

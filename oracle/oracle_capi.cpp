@@ -57,21 +57,23 @@ template <class T> void store_motions(const std::vector<orc::Vec6<T>>& x, int nj
 
 template <class T>
 void run_one(const Model& m, orc::Data<T>& d, int func, const double* q, const double* v, const double* x,
-             double* o1, double* o2, double* o3, double* o4) {
-  Buf<T> bq, bv, bx;
+             double* o1, double* o2, double* o3, double* o4, const double* fe = nullptr) {
+  Buf<T> bq, bv, bx, bf;
   const int nq = m.nq, nv = m.nv;
   const size_t nn = (size_t)nv * nv;
   bq.load(q, nq);
   if (v) bv.load(v, nv);
   if (x) bx.load(x, nv);
+  if (fe) bf.load(fe, 6 * m.njoints);
+  const T* fext = fe ? bf.x.data() : nullptr;  // external forces (njoints x 6, joint frames)
   switch (func) {
     case F_RNEA:
-      orc::rnea(m, d, bq.x.data(), bv.x.data(), bx.x.data());
+      orc::rnea(m, d, bq.x.data(), bv.x.data(), bx.x.data(), fext);
       store(d.tau, o1, nv);
       break;
     case F_ABA_LOCAL:
     case F_ABA_WORLD:
-      orc::aba(m, d, bq.x.data(), bv.x.data(), bx.x.data(), func == F_ABA_WORLD ? orc::WORLD : orc::LOCAL);
+      orc::aba(m, d, bq.x.data(), bv.x.data(), bx.x.data(), func == F_ABA_WORLD ? orc::WORLD : orc::LOCAL, fext);
       store(d.ddq, o1, nv);
       break;
     case F_CRBA_LOCAL:
@@ -95,7 +97,7 @@ void run_one(const Model& m, orc::Data<T>& d, int func, const double* q, const d
       std::fill(d.M.begin(), d.M.end(), T(0));
       std::fill(d.dtau_dq.begin(), d.dtau_dq.end(), T(0));
       std::fill(d.dtau_dv.begin(), d.dtau_dv.end(), T(0));
-      orc::rnea_derivatives(m, d, bq.x.data(), bv.x.data(), bx.x.data());
+      orc::rnea_derivatives(m, d, bq.x.data(), bv.x.data(), bx.x.data(), fext);
       if (o1) store(d.tau, o1, nv);
       if (o2) store(d.dtau_dq, o2, nn);
       if (o3) store(d.dtau_dv, o3, nn);
@@ -104,7 +106,7 @@ void run_one(const Model& m, orc::Data<T>& d, int func, const double* q, const d
     case F_ABA_D:
       std::fill(d.dtau_dq.begin(), d.dtau_dq.end(), T(0));
       std::fill(d.dtau_dv.begin(), d.dtau_dv.end(), T(0));
-      orc::aba_derivatives(m, d, bq.x.data(), bv.x.data(), bx.x.data());
+      orc::aba_derivatives(m, d, bq.x.data(), bv.x.data(), bx.x.data(), fext);
       if (o1) store(d.ddq, o1, nv);
       if (o2) store(d.ddq_dq, o2, nn);
       if (o3) store(d.ddq_dv, o3, nn);
@@ -150,7 +152,7 @@ int out_stride(int func, const Model& m, int which) {
 
 template <class T>
 int run_batch(const Model& m, int func, long B, const double* q, const double* v, const double* x, double* o1,
-              double* o2, double* o3, double* o4, int nthreads) {
+              double* o2, double* o3, double* o4, int nthreads, const double* fe) {
   if (nthreads <= 0) nthreads = omp_get_max_threads();
   omp_set_dynamic(0);  // set_default_omp_options (algorithm/parallel/omp.hpp:12-16)
   omp_set_num_threads(nthreads);
@@ -167,7 +169,7 @@ int run_batch(const Model& m, int func, long B, const double* q, const double* v
       run_one<T>(m, *datas[omp_get_thread_num()], func, q + (size_t)b * sq, v ? v + (size_t)b * sv : nullptr,
                  x ? x + (size_t)b * sv : nullptr, o1 ? o1 + (size_t)b * s1 : nullptr,
                  o2 ? o2 + (size_t)b * s2 : nullptr, o3 ? o3 + (size_t)b * s3 : nullptr,
-                 o4 ? o4 + (size_t)b * s4 : nullptr);
+                 o4 ? o4 + (size_t)b * s4 : nullptr, fe ? fe + (size_t)b * 6 * m.njoints : nullptr);
     } catch (const std::exception& e) {
 #pragma omp critical
       {
@@ -184,11 +186,11 @@ int run_batch(const Model& m, int func, long B, const double* q, const double* v
 }
 
 int dispatch(void* h, int prec, int func, long B, const double* q, const double* v, const double* x, double* o1,
-             double* o2, double* o3, double* o4, int nthreads) {
+             double* o2, double* o3, double* o4, int nthreads, const double* fe = nullptr) {
   if (!h) { g_err = "null model"; return -1; }
   const Model& m = *static_cast<Model*>(h);
-  if (prec == 0) return run_batch<double>(m, func, B, q, v, x, o1, o2, o3, o4, nthreads);
-  if (prec == 1) return run_batch<long double>(m, func, B, q, v, x, o1, o2, o3, o4, nthreads);
+  if (prec == 0) return run_batch<double>(m, func, B, q, v, x, o1, o2, o3, o4, nthreads, fe);
+  if (prec == 1) return run_batch<long double>(m, func, B, q, v, x, o1, o2, o3, o4, nthreads, fe);
   g_err = "unknown precision";
   return -1;
 }
@@ -260,6 +262,28 @@ int orc_aba_derivatives(void* h, int prec, long B, const double* q, const double
                         double* ddq_dq, double* ddq_dv, double* Minv, int nt) {
   return dispatch(h, prec, F_ABA_D, B, q, v, tau, ddq, ddq_dq, ddq_dv, Minv, nt);
 }
+// With external forces fext (njoints x 6 per instance, [linear; angular] in the
+// joint frames): rnea / aba / computeRNEADerivatives / computeABADerivatives of
+// the reference's fext overloads (algorithm/rnea.hxx:164-218, aba.hxx:296-352 and
+// 543-605, rnea-derivatives.hxx:550-633, aba-derivatives.hxx:463-541).
+int orc_rnea_fext(void* h, int prec, long B, const double* q, const double* v, const double* a, const double* fext,
+                  double* tau, int nt) {
+  return dispatch(h, prec, F_RNEA, B, q, v, a, tau, nullptr, nullptr, nullptr, nt, fext);
+}
+int orc_aba_fext(void* h, int prec, int conv, long B, const double* q, const double* v, const double* tau,
+                 const double* fext, double* ddq, int nt) {
+  return dispatch(h, prec, conv == orc::WORLD ? F_ABA_WORLD : F_ABA_LOCAL, B, q, v, tau, ddq, nullptr, nullptr,
+                  nullptr, nt, fext);
+}
+int orc_rnea_derivatives_fext(void* h, int prec, long B, const double* q, const double* v, const double* a,
+                              const double* fext, double* tau, double* dtau_dq, double* dtau_dv, double* M, int nt) {
+  return dispatch(h, prec, F_RNEA_D, B, q, v, a, tau, dtau_dq, dtau_dv, M, nt, fext);
+}
+int orc_aba_derivatives_fext(void* h, int prec, long B, const double* q, const double* v, const double* tau,
+                             const double* fext, double* ddq, double* ddq_dq, double* ddq_dv, double* Minv, int nt) {
+  return dispatch(h, prec, F_ABA_D, B, q, v, tau, ddq, ddq_dq, ddq_dv, Minv, nt, fext);
+}
+
 int orc_forward_kinematics(void* h, int prec, long B, const double* q, const double* v, const double* a, double* oMi,
                            double* vi, double* ai, int nt) {
   return dispatch(h, prec, F_FK, B, q, v, a, oMi, vi, ai, nullptr, nt);

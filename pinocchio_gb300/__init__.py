@@ -33,6 +33,7 @@ from .api import (  # noqa: F401
     computeJointJacobians,
     computeMinverse,
     computeRNEADerivatives,
+    computeStaticTorque,
     crba,
     crbaCholesky,
     createData,

@@ -34,10 +34,15 @@ EXPORTS = (
     "gb_rnea",
     "gb_nonlinear_effects",
     "gb_generalized_gravity",
+    "gb_rnea_fext",
+    "gb_static_torque",
     "gb_aba",
+    "gb_aba_fext",
     "gb_crba",
     "gb_rnea_derivatives",
+    "gb_rnea_derivatives_fext",
     "gb_aba_derivatives",
+    "gb_aba_derivatives_fext",
     "gb_compute_minverse",
     "gb_aba_derivatives_vjp",
     "gb_aba_derivatives_noalloc",
@@ -132,6 +137,11 @@ def lib():
         L.gb_nonlinear_effects.argtypes = [vp, i, i, l, vp, vp, vp, vp]
         L.gb_generalized_gravity.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_aba.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp]
+        L.gb_rnea_fext.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp]
+        L.gb_static_torque.argtypes = [vp, i, i, l, vp, vp, vp, vp]
+        L.gb_aba_fext.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp]
+        L.gb_rnea_derivatives_fext.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gb_aba_derivatives_fext.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_crba.argtypes = [vp, i, i, i, i, l, vp, vp, vp, vp, vp]
         L.gb_rnea_derivatives.argtypes = [vp, i, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]

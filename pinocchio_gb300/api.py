@@ -102,20 +102,70 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-def rnea(model: Model, data: Data, q, v, a):
-    """tau = RNEA(q, v, a) (reference algorithm/rnea.hxx:117-161)."""
+def _fext(model: Model, fext, B: int):
+    """External forces as the reference's Python bindings take them (a list of njoints
+    forces, each [linear; angular] in its joint's frame, expressed in the local frame of
+    the joints: bindings/python/algorithm/expose-rnea.cpp:38-46): an array (njoints, 6)
+    shared by the batch or (B, njoints, 6) per configuration, or a list of njoints 6-vectors
+    (objects with .vector, as pin.Force has, are accepted).  Returns a (B, njoints * 6)
+    float64 CUDA tensor."""
+    torch = _torch()
+    if isinstance(fext, (list, tuple)):
+        fext = [np.asarray(getattr(f, "vector", f), dtype=np.float64).reshape(6) for f in fext]
+    t = torch.as_tensor(np.asarray(fext) if isinstance(fext, list) else fext, dtype=torch.float64)
+    if t.dim() == 2:
+        t = t.unsqueeze(0).expand(B, -1, -1)
+    if t.dim() != 3 or t.shape[1] != model.njoints or t.shape[2] != 6:
+        raise ValueError(f"fext must have shape ({model.njoints}, 6) or (batch, {model.njoints}, 6), got {tuple(t.shape)}")
+    if t.shape[0] != B:
+        raise ValueError(f"fext holds {t.shape[0]} configurations, the batch {B}")
+    if not t.is_cuda:
+        t = t.cuda()
+    return t.reshape(B, -1).contiguous()
+
+
+def rnea(model: Model, data: Data, q, v, a, fext=None):
+    """tau = RNEA(q, v, a) (reference algorithm/rnea.hxx:117-161); with external forces
+    fext (njoints forces in the joint frames) rnea(model, data, q, v, a, fext)
+    (rnea.hxx:164-218)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     at = _as_batch(a, model.nv, "a")[0]
     B = qt.shape[0]
     tau = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
-    _capi.check(
-        _capi.lib().gb_rnea(
-            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at), _ptr(tau), _stream_ptr()
+    if fext is None:
+        _capi.check(
+            _capi.lib().gb_rnea(
+                data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at), _ptr(tau), _stream_ptr()
+            )
         )
-    )
+    else:
+        ft = _fext(model, fext, B)
+        _capi.check(
+            _capi.lib().gb_rnea_fext(
+                data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at), _ptr(ft), _ptr(tau),
+                _stream_ptr(),
+            )
+        )
     data.tau = tau
     return _ret(tau, was_np, vec)
+
+
+def computeStaticTorque(model: Model, data: Data, q, fext):
+    """tau = g(q) - sum_i J_i^T fext_i, the joint torques that hold the configuration
+    against gravity and the external forces (reference algorithm/rnea.hxx:448-489,
+    binding expose-rnea.cpp:76-86)."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    B = qt.shape[0]
+    ft = _fext(model, fext, B)
+    out = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_static_torque(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(ft), _ptr(out), _stream_ptr()
+        )
+    )
+    data.tau = out
+    return _ret(out, was_np, vec)
 
 
 def nonLinearEffects(model: Model, data: Data, q, v):
@@ -204,19 +254,39 @@ def computeMinverse(model: Model, data: Data, q, symmetric: bool = True):
     return _ret(out, was_np, vec)
 
 
-def aba(model: Model, data: Data, q, v, tau, convention: int = Convention.LOCAL):
-    """ddq = ABA(q, v, tau) (reference algorithm/aba.hxx:933-948)."""
+def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = None, fext=None):
+    """ddq = ABA(q, v, tau) (reference algorithm/aba.hxx:933-948), called as the
+    reference's binding is: aba(model, data, q, v, tau[, convention]) or
+    aba(model, data, q, v, tau, fext[, convention]) with external forces in the
+    joint frames (aba.hxx:958-973, expose-aba.cpp:60-82)."""
+    if len(args) > 2:
+        raise TypeError("aba takes at most fext and convention after tau")
+    for x in args:
+        if isinstance(x, (int, np.integer)) and not isinstance(x, bool):
+            convention = int(x)
+        else:
+            fext = x
+    convention = Convention.LOCAL if convention is None else convention
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     tt = _as_batch(tau, model.nv, "tau")[0]
     B = qt.shape[0]
     ddq = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
-    _capi.check(
-        _capi.lib().gb_aba(
-            data.dev.h, _PREC[data.precision], int(convention), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt),
-            _ptr(ddq), _stream_ptr(),
+    if fext is None:
+        _capi.check(
+            _capi.lib().gb_aba(
+                data.dev.h, _PREC[data.precision], int(convention), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt),
+                _ptr(ddq), _stream_ptr(),
+            )
         )
-    )
+    else:
+        ft = _fext(model, fext, B)
+        _capi.check(
+            _capi.lib().gb_aba_fext(
+                data.dev.h, _PREC[data.precision], int(convention), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt),
+                _ptr(ft), _ptr(ddq), _stream_ptr(),
+            )
+        )
     data.ddq = ddq
     return _ret(ddq, was_np, vec)
 
@@ -254,8 +324,9 @@ def crbaCholesky(model: Model, data: Data, q):
     return tuple(_ret(t, was_np, vec) for t in (M, U, D))
 
 
-def computeRNEADerivatives(model: Model, data: Data, q, v, a):
-    """(dtau_dq, dtau_dv, M) (reference algorithm/rnea-derivatives.hxx:472-541, M symmetrised as the binding does)."""
+def computeRNEADerivatives(model: Model, data: Data, q, v, a, fext=None):
+    """(dtau_dq, dtau_dv, M) (reference algorithm/rnea-derivatives.hxx:472-541, M symmetrised as the binding does);
+    with external forces fext in the joint frames, rnea-derivatives.hxx:550-633."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     at = _as_batch(a, model.nv, "a")[0]
@@ -265,18 +336,26 @@ def computeRNEADerivatives(model: Model, data: Data, q, v, a):
     dv = torch.empty_like(dq)
     M = torch.empty_like(dq)
     tau = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
-    _capi.check(
-        _capi.lib().gb_rnea_derivatives(
-            data.dev.h, _PREC[data.precision], _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at),
-            _ptr(dq), _ptr(dv), _ptr(M), _ptr(tau), _stream_ptr(),
+    prec, h = _PREC[data.precision], data.dev.h
+    if fext is None:
+        rc = _capi.lib().gb_rnea_derivatives(
+            h, prec, _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at), _ptr(dq), _ptr(dv),
+            _ptr(M), _ptr(tau), _stream_ptr(),
         )
-    )
+    else:
+        ft = _fext(model, fext, B)
+        rc = _capi.lib().gb_rnea_derivatives_fext(
+            h, prec, _capi.GB_MATRIX_SYMMETRIC, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(at), _ptr(ft), _ptr(dq),
+            _ptr(dv), _ptr(M), _ptr(tau), _stream_ptr(),
+        )
+    _capi.check(rc)
     data.dtau_dq, data.dtau_dv, data.M, data.tau = dq, dv, M, tau
     return tuple(_ret(t, was_np, vec) for t in (dq, dv, M))
 
 
-def computeABADerivatives(model: Model, data: Data, q, v, tau):
-    """(ddq_dq, ddq_dv, Minv) (reference algorithm/aba-derivatives.hxx:380-453)."""
+def computeABADerivatives(model: Model, data: Data, q, v, tau, fext=None):
+    """(ddq_dq, ddq_dv, Minv) (reference algorithm/aba-derivatives.hxx:380-453); with external
+    forces fext in the joint frames, aba-derivatives.hxx:463-541."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     tt = _as_batch(tau, model.nv, "tau")[0]
@@ -286,12 +365,19 @@ def computeABADerivatives(model: Model, data: Data, q, v, tau):
     dv = torch.empty_like(dq)
     Minv = torch.empty_like(dq)
     ddq = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
-    _capi.check(
-        _capi.lib().gb_aba_derivatives(
-            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt), _ptr(dq), _ptr(dv),
-            _ptr(Minv), _ptr(ddq), _stream_ptr(),
+    prec, h = _PREC[data.precision], data.dev.h
+    if fext is None:
+        rc = _capi.lib().gb_aba_derivatives(
+            h, prec, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt), _ptr(dq), _ptr(dv), _ptr(Minv), _ptr(ddq),
+            _stream_ptr(),
         )
-    )
+    else:
+        ft = _fext(model, fext, B)
+        rc = _capi.lib().gb_aba_derivatives_fext(
+            h, prec, _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt), _ptr(tt), _ptr(ft), _ptr(dq), _ptr(dv), _ptr(Minv),
+            _ptr(ddq), _stream_ptr(),
+        )
+    _capi.check(rc)
     data.ddq_dq, data.ddq_dv, data.Minv, data.ddq = dq, dv, Minv, ddq
     return tuple(_ret(t, was_np, vec) for t in (dq, dv, Minv))
 

@@ -102,6 +102,17 @@ int gb_rnea(const gb_model* M, int precision, int layout, long B, const double* 
                           gbi::arr(a, layout, B, M->nv), gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
 }
 
+int gb_rnea_fext(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                 const double* a, const double* fext, double* tau, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(a, "a"));
+  GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  return gbi::launch_rnea_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
+                               gbi::arr(a, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj),
+                               gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
+}
+
 // nonLinearEffects = rnea(q, v, 0) and computeGeneralizedGravity = rnea(q, 0, 0)
 // (reference algorithm/rnea.hxx:221-336, 346-446): the RNEA kernel reading a zero vector
 // (16 zero bytes of the model blob, stride 0) for the absent arguments.
@@ -126,6 +137,16 @@ int gb_generalized_gravity(const gb_model* M, int precision, int layout, long B,
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(g, "g"));
   return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), zero_arr(M), zero_arr(M),
                           gbi::arr(g, layout, B, M->nv), (cudaStream_t)stream);
+}
+
+int gb_static_torque(const gb_model* M, int precision, int layout, long B, const double* q, const double* fext,
+                     double* tau, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  return gbi::launch_rnea_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), zero_arr(M), zero_arr(M),
+                               gbi::arr(fext, layout, B, 6L * M->nj), gbi::arr(tau, layout, B, M->nv),
+                               (cudaStream_t)stream);
 }
 
 int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
@@ -163,6 +184,18 @@ int gb_aba(const gb_model* M, int precision, int convention, int layout, long B,
   GB_TRY(gbi::check_ptr(ddq, "ddq"));
   return gbi::launch_aba(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
                          gbi::arr(tau, layout, B, M->nv), gbi::arr(ddq, layout, B, M->nv), (cudaStream_t)stream);
+}
+
+int gb_aba_fext(const gb_model* M, int precision, int convention, int layout, long B, const double* q,
+                const double* v, const double* tau, const double* fext, double* ddq, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (convention != GB_LOCAL && convention != GB_WORLD) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown convention");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(ddq, "ddq"));
+  return gbi::launch_aba_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
+                              gbi::arr(tau, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj),
+                              gbi::arr(ddq, layout, B, M->nv), (cudaStream_t)stream);
 }
 
 int gb_crba(const gb_model* M, int precision, int convention, int matrix_mode, int layout, long B, const double* q,

@@ -20,18 +20,20 @@
 namespace gbi {
 namespace {
 
-template <class S>
+// FE: with external forces (fext, njoints x 6 per configuration in the joint frames)
+template <class S, bool FE = false>
 __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* blob, int bytes, long B,
                                                           gb::DerivLayout L, S* ws, bool symmetric, Arr q, Arr v,
-                                                          Arr a, Arr dq, Arr dv, Arr Mo, Arr tau) {
+                                                          Arr a, Arr dq, Arr dv, Arr Mo, Arr tau, Arr fext) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
   const gb::Ws<S> w{ws + b, B};
   const gb::Out to = out_at(tau, b);
+  const gb::In fe = in_at(fext, b);
   gb::rnea_derivs_one<S>(m, L, w, in_at(q, b), in_at(v, b), in_at(a, b), out_at(dq, b), out_at(dv, b), out_at(Mo, b),
-                         tau.p ? &to : nullptr, symmetric, true);
+                         tau.p ? &to : nullptr, symmetric, true, FE ? &fe : nullptr);
 }
 
 __device__ __forceinline__ double to_double(double x) { return x; }
@@ -529,14 +531,14 @@ int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, co
   return GB_OK;
 }
 
-template <class S>
+template <class S, bool FE = false>
 int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr a, Arr dq, Arr dv, Arr Mo, Arr tau,
-                    cudaStream_t st) {
+                    cudaStream_t st, Arr fext = Arr{nullptr, 0, 0}) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, false);
   Workspace ws;
   int rc = ws_alloc(ws, sizeof(S) * (size_t)L.nS * B, st);
   if (rc != GB_OK) return rc;
-  rc = blob_smem(M, (const void*)k_rnea_derivs<S>, "k_rnea_derivs");
+  rc = blob_smem(M, (const void*)k_rnea_derivs<S, FE>, "k_rnea_derivs");
   if (rc != GB_OK) return rc;
   // instance-layout matrices of a large batch are written coalesced into an SOA scratch, then transposed
   const long nn = (long)M->nv * M->nv;
@@ -555,9 +557,9 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   }
   const int tpb = M->tpb[GB_FUNC_RNEA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
-  k_rnea_derivs<S><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
-                                                                   static_cast<S*>(ws.p), symmetric, q, v, a, mats[0],
-                                                                   mats[1], mats[2], tau);
+  k_rnea_derivs<S, FE><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
+                                                                       static_cast<S*>(ws.p), symmetric, q, v, a,
+                                                                       mats[0], mats[1], mats[2], tau, fext);
   rc = cuda_error(cudaGetLastError(), "k_rnea_derivs");
   if (rc != GB_OK || !staged) return rc;
   const Arr outs[3] = {dq, dv, Mo};
@@ -571,17 +573,19 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
 // The three sweep kernels of the ABA derivatives on a workspace laid out by
 // aba_ws_layout, in the model's layout (gb_sweeps_t*.cu, one translation unit
 // per team size).
+// With external forces (fext.p set) the sweeps run one thread per configuration.
 template <class S, class T3, class T, class K, class SS, class P>
-int launch_aba_sweeps(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq, void* ws, cudaStream_t st) {
+int launch_aba_sweeps(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq, void* ws, cudaStream_t st,
+                      Arr fext = Arr{nullptr, 0, 0}) {
   constexpr bool f64 = std::is_same<K, double>::value, vjp = std::is_same<P, gb::dfloat>::value;
-  const SweepCall c{f64 ? kSweepFp64 : vjp ? kSweepMixedVjp : kSweepMixed, M, B, q, v, tau, ddq, ws, st};
-  return sweeps_team(c);
+  const SweepCall c{f64 ? kSweepFp64 : vjp ? kSweepMixedVjp : kSweepMixed, M, B, q, v, tau, ddq, ws, st, fext};
+  return fext.p ? sweeps_t1(c) : sweeps_team(c);
 }
 
 template <class S, class T3, class T, class K, class SS, class P>
 int launch_aba_derivs_ws(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq, void* ws,
-                         cudaStream_t st) {
-  int rc = launch_aba_sweeps<S, T3, T, K, SS, P>(M, B, q, v, tau, ddq, ws, st);
+                         cudaStream_t st, Arr fext = Arr{nullptr, 0, 0}) {
+  int rc = launch_aba_sweeps<S, T3, T, K, SS, P>(M, B, q, v, tau, ddq, ws, st, fext);
   if (rc != GB_OK) return rc;
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, B);
@@ -687,12 +691,12 @@ int run_aba_vjp(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr g, Arr qb,
 
 template <class S, class T3, class T, class K, class SS, class P>
 int run_aba_derivs(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv, Arr Minv, Arr ddq,
-                   cudaStream_t st) {
+                   cudaStream_t st, Arr fext = Arr{nullptr, 0, 0}) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   Workspace ws;
   int rc = ws_alloc(ws, aba_ws_layout<S, K, SS, P>(L, M->nv, B).bytes, st);
   if (rc != GB_OK) return rc;
-  return launch_aba_derivs_ws<S, T3, T, K, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st);
+  return launch_aba_derivs_ws<S, T3, T, K, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st, fext);
 }
 
 int check_gravity(const gb_model* M) {
@@ -757,9 +761,13 @@ int gb_pipeline_wait_selftest(unsigned int limit_us, void* stream) {
   return gbi::cuda_error(cudaGetLastError(), "k_wait_selftest");
 }
 
-int gb_rnea_derivatives(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
-                        const double* v, const double* a, double* dtau_dq, double* dtau_dv, double* Mo, double* tau,
-                        void* stream) {
+}  // extern "C"
+
+namespace gbi {
+namespace {
+int rnea_derivs_entry(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
+                      const double* v, const double* a, const double* fext, double* dtau_dq, double* dtau_dv,
+                      double* Mo, double* tau, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));
   if (matrix_mode != GB_MATRIX_UPPER && matrix_mode != GB_MATRIX_SYMMETRIC)
     return gbi::set_error(GB_ERR_INVALID_ARGUMENT, "unknown matrix mode");
@@ -768,6 +776,7 @@ int gb_rnea_derivatives(const gb_model* M, int precision, int matrix_mode, int l
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(a, "a"));
   GB_TRY(gbi::check_ptr(dtau_dq, "dtau_dq")); GB_TRY(gbi::check_ptr(dtau_dv, "dtau_dv")); GB_TRY(gbi::check_ptr(Mo, "M"));
   if (tau) GB_TRY(gbi::check_ptr(tau, "tau"));
+  if (fext) GB_TRY(gbi::check_ptr(fext, "fext"));
   const long nn = (long)M->nv * M->nv;
   using gbi::arr;
   const gbi::Arr Aq = arr(q, layout, B, M->nq), Av = arr(v, layout, B, M->nv), Aa = arr(a, layout, B, M->nv);
@@ -775,29 +784,68 @@ int gb_rnea_derivatives(const gb_model* M, int precision, int matrix_mode, int l
   const gbi::Arr At = arr(tau, layout, B, M->nv);
   const bool sym = matrix_mode == GB_MATRIX_SYMMETRIC;
   cudaStream_t st = (cudaStream_t)stream;
+  if (fext) {
+    const gbi::Arr Af = arr(fext, layout, B, 6L * M->nj);
+    if (precision == GB_FP64) return gbi::run_rnea_derivs<double, true>(M, B, sym, Aq, Av, Aa, Adq, Adv, AM, At, st, Af);
+    return gbi::run_rnea_derivs<float, true>(M, B, sym, Aq, Av, Aa, Adq, Adv, AM, At, st, Af);
+  }
   if (precision == GB_FP64) return gbi::run_rnea_derivs<double>(M, B, sym, Aq, Av, Aa, Adq, Adv, AM, At, st);
   return gbi::run_rnea_derivs<float>(M, B, sym, Aq, Av, Aa, Adq, Adv, AM, At, st);
 }
 
-int gb_aba_derivatives(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
-                       const double* tau, double* ddq_dq, double* ddq_dv, double* Minv, double* ddq, void* stream) {
+int aba_derivs_entry(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                     const double* tau, const double* fext, double* ddq_dq, double* ddq_dv, double* Minv, double* ddq,
+                     void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));
   GB_TRY(gbi::check_gravity(M));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
   GB_TRY(gbi::check_ptr(ddq_dq, "ddq_dq")); GB_TRY(gbi::check_ptr(ddq_dv, "ddq_dv")); GB_TRY(gbi::check_ptr(Minv, "Minv"));
   if (ddq) GB_TRY(gbi::check_ptr(ddq, "ddq"));
+  if (fext) GB_TRY(gbi::check_ptr(fext, "fext"));
   const long nn = (long)M->nv * M->nv;
   using gbi::arr;
   const gbi::Arr Aq = arr(q, layout, B, M->nq), Av = arr(v, layout, B, M->nv), At = arr(tau, layout, B, M->nv);
   const gbi::Arr Adq = arr(ddq_dq, layout, B, nn), Adv = arr(ddq_dv, layout, B, nn), AMi = arr(Minv, layout, B, nn);
   const gbi::Arr Add = arr(ddq, layout, B, M->nv);
+  const gbi::Arr Af = fext ? arr(fext, layout, B, 6L * M->nj) : gbi::Arr{nullptr, 0, 0};
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == GB_FP64)
     return gbi::run_aba_derivs<double, double, double, double, double, double>(M, B, Aq, Av, At, Adq, Adv, AMi, Add,
-                                                                               st);
+                                                                               st, Af);
   return gbi::run_aba_derivs<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, Aq, Av, At, Adq, Adv, AMi,
-                                                                                 Add, st);
+                                                                                 Add, st, Af);
+}
+}  // namespace
+}  // namespace gbi
+
+extern "C" {
+
+int gb_rnea_derivatives(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
+                        const double* v, const double* a, double* dtau_dq, double* dtau_dv, double* Mo, double* tau,
+                        void* stream) {
+  return gbi::rnea_derivs_entry(M, precision, matrix_mode, layout, B, q, v, a, nullptr, dtau_dq, dtau_dv, Mo, tau,
+                                stream);
+}
+
+int gb_rnea_derivatives_fext(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
+                             const double* v, const double* a, const double* fext, double* dtau_dq, double* dtau_dv,
+                             double* Mo, double* tau, void* stream) {
+  if (!fext) return gbi::set_error(GB_ERR_INVALID_ARGUMENT, "fext is NULL");
+  return gbi::rnea_derivs_entry(M, precision, matrix_mode, layout, B, q, v, a, fext, dtau_dq, dtau_dv, Mo, tau,
+                                stream);
+}
+
+int gb_aba_derivatives(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                       const double* tau, double* ddq_dq, double* ddq_dv, double* Minv, double* ddq, void* stream) {
+  return gbi::aba_derivs_entry(M, precision, layout, B, q, v, tau, nullptr, ddq_dq, ddq_dv, Minv, ddq, stream);
+}
+
+int gb_aba_derivatives_fext(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
+                            const double* tau, const double* fext, double* ddq_dq, double* ddq_dv, double* Minv,
+                            double* ddq, void* stream) {
+  if (!fext) return gbi::set_error(GB_ERR_INVALID_ARGUMENT, "fext is NULL");
+  return gbi::aba_derivs_entry(M, precision, layout, B, q, v, tau, fext, ddq_dq, ddq_dv, Minv, ddq, stream);
 }
 
 int gb_compute_minverse(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,

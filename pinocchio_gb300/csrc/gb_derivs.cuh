@@ -337,7 +337,7 @@ template <class S> GB_HD void imul(const Iner<S>& Y, const S* v, S* f) {
 // One joint of the world-frame forward pass (NVJ: its degrees of freedom).
 template <int NVJ, class S>
 GB_HD void world_forward_joint(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
-                               const In* acc, bool with_derivs, const S* g, int i) {
+                               const In* acc, bool with_derivs, const S* g, int i, const In* fext) {
   const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
   X3<S> X, O;
   joint_transform(m, i, q, X);
@@ -410,6 +410,13 @@ GB_HD void world_forward_joint(const MView& m, const DerivLayout& L, const Ws<S>
 #pragma unroll
     for (int r = 0; r < 6; ++r) of[r] = t6[r];
   }
+  if (fext) {  // of -= oMi.act(fext_i) (rnea-derivatives.hxx:596, aba-derivatives.hxx:513)
+    M6<S> fe, fw;
+    load_fext(m, *fext, i, fe.v);
+    act_force(O, fe, fw);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) of[r] -= fw.v[r];
+  }
   st6(w, L.oh + 6 * i, oh);
   st6(w, L.of + 6 * i, of);
   if (!with_derivs) return;
@@ -447,12 +454,12 @@ GB_HD void world_forward_joint(const MView& m, const DerivLayout& L, const Ws<S>
 
 template <class S>
 GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
-                         const In* acc, bool with_derivs) {
+                         const In* acc, bool with_derivs, const In* fext = nullptr) {
   const S* g = ModelScalar<S>::grav(m);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
-    if (m.jtype[i] == JT_FF) world_forward_joint<6, S>(m, L, w, q, v, acc, with_derivs, g, i);
-    else world_forward_joint<1, S>(m, L, w, q, v, acc, with_derivs, g, i);
+    if (m.jtype[i] == JT_FF) world_forward_joint<6, S>(m, L, w, q, v, acc, with_derivs, g, i, fext);
+    else world_forward_joint<1, S>(m, L, w, q, v, acc, with_derivs, g, i, fext);
   }
 }
 
@@ -463,9 +470,9 @@ GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, c
 template <class S>
 GB_HD void rnea_derivs_one(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
                            const In& a, const Out& dq, const Out& dv, const Out& Mo, const Out* tau, bool symmetric,
-                           bool zeroed) {
+                           bool zeroed, const In* fext = nullptr) {
   const int nv = m.nv;
-  world_forward(m, L, w, q, v, &a, true);
+  world_forward(m, L, w, q, v, &a, true, fext);
   if (!zeroed)  // otherwise the outputs arrive zero-filled: only non-zero entries are written
     for (int r = 0; r < nv * nv; ++r) { dq[r] = 0.0; dv[r] = 0.0; Mo[r] = 0.0; }
   const S eps = eps_of<S>();
@@ -846,10 +853,12 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
 
 template <class K, class SS, class Team = Solo>
 GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
-                             const Ws<K>& zm, const In& q, const In& v, const In& tau, const Team& tm = Team()) {
+                             const Ws<K>& zm, const In& q, const In& v, const In& tau, const In* fext,
+                             const Team& tm = Team()) {
   const int nv = m.nv;
-  // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K
-  world_forward<K>(m, L, zk, q, v, nullptr, false);
+  // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K;
+  // external forces enter the bias force (hxx:513)
+  world_forward<K>(m, L, zk, q, v, nullptr, false, fext);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix(), formed in K and stored in SS
     Iner<K> oY;
@@ -879,7 +888,7 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
 template <int NVJ, class S, class T, class K, bool MINV = false, class Team = Solo>
 GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                                   const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out, const K* gk,
-                                  int i, const Team& tm = Team()) {
+                                  const In* fext, int i, const Team& tm = Team()) {
   const int nv = m.nv;
   const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
   K ti[3];
@@ -1020,6 +1029,16 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   fcross(ovs, oh, t6);
 #pragma unroll
   for (int k = 0; k < 6; ++k) of[k] += t6[k];
+  if (fext) {  // of -= oMi.act(fext_i) (hxx:529), about t_i: the rotation part only
+    K R[9], fe[6];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = zk[L.oM + 12 * i + k];
+    load_fext(m, *fext, i, fe);
+#pragma unroll
+    for (int h = 0; h < 6; h += 3)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) of[h + r] -= T(R[3 * r] * fe[h] + R[3 * r + 1] * fe[h + 1] + R[3 * r + 2] * fe[h + 2]);
+  }
   st6(w, L.cof + 6 * i, of);
   T dY[36];
   variation_plus_fcross(oY, ovs, oh, dY);
@@ -1030,7 +1049,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
 
 template <class S, class T, class K, bool MINV = false, class Team = Solo>
 GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
-                            const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out,
+                            const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out, const In* fext,
                             const Team& tm = Team()) {
   // ---- pass 3: ComputeABADerivativesForwardStep2 (hxx:178-270).  The
   // velocity / acceleration recursion runs in K in floating origins and
@@ -1039,8 +1058,8 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
   const K* gk = ModelScalar<K>::grav(m);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
-    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i, tm);
-    else aba_derivs_pass3_joint<1, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, i, tm);
+    if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, fext, i, tm);
+    else aba_derivs_pass3_joint<1, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, fext, i, tm);
   }
 }
 
@@ -1217,9 +1236,9 @@ GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w
 template <class S, class T3, class T, class K, class SS, class P>
 GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                              const Ws<K>& zk, const Ws<SS>& zs, const Ws<K>& zm, const Ws<P>& wp, const In& q,
-                             const In& v, const In& tau, const Out* ddq_out) {
-  aba_derivs_pass12<K, SS>(m, L, zk, zs, zm, q, v, tau);
-  aba_derivs_pass3<S, T3, K>(m, L, slot, w, zk, zm, v, ddq_out);
+                             const In& v, const In& tau, const Out* ddq_out, const In* fext = nullptr) {
+  aba_derivs_pass12<K, SS>(m, L, zk, zs, zm, q, v, tau, fext);
+  aba_derivs_pass3<S, T3, K>(m, L, slot, w, zk, zm, v, ddq_out, fext);
   aba_derivs_pass4<S, T, K, P>(m, L, w, zk, wp);
 }
 

@@ -94,11 +94,32 @@ template <class S> GB_HD void joint_motion(int jt, const In& x, int iv, M6<S>& o
   }
 }
 
+// External force on joint i as the reference takes it: a force [linear; angular]
+// expressed in the joint's own frame (fext[i], algorithm/rnea.hpp:60-79); fe
+// holds njoints x 6 values per configuration, joint 0's are not read.  Inside the
+// kernels an unaligned joint's frame is the joint frame turned by F (a rotation
+// about the same origin, folded in at model build): f' = F^T f.
+template <class S> GB_HD void load_fext(const MView& m, const In& fe, int i, S* f) {
+  if (!m.fix_d) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[k] = S(fe[6 * i + k]);
+    return;
+  }
+  const double* F = m.fix_d + 9 * i;
+#pragma unroll
+  for (int h = 0; h < 6; h += 3)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      f[h + r] = S(F[r] * fe[6 * i + h] + F[3 + r] * fe[6 * i + h + 1] + F[6 + r] * fe[6 * i + h + 2]);
+}
+
 // ------------------------------------------------------------------------------------------
-// RNEA (reference algorithm/rnea.hxx:24-161)
+// RNEA (reference algorithm/rnea.hxx:24-161); with external forces fext
+// (rnea.hxx:170-215: f_i -= fext_i after the forward step of joint i).
 // ------------------------------------------------------------------------------------------
 template <class S, int CAP>
-GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const Out& tau) {
+GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const Out& tau,
+                    const In* fext = nullptr) {
   X3<S> X[CAP];
   M6<S> vel[CAP], acc[CAP], f[CAP];
   const S* g = ModelScalar<S>::grav(m);
@@ -132,6 +153,12 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
     cross_force(vel[i], h, fx);
 #pragma unroll
     for (int k = 0; k < 6; ++k) f[i].v[k] = fa.v[k] + fx.v[k];
+    if (fext) {
+      S fe[6];
+      load_fext(m, *fext, i, fe);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f[i].v[k] -= fe[k];
+    }
   }
   for (int i = m.nj - 1; i > 0; --i) {
     const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
@@ -163,8 +190,12 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
 // child (forward) / from a first child to its parent (backward); only joints
 // with two or more children keep them in a branch slot.
 // ------------------------------------------------------------------------------------------
+//
+// With external forces fext (aba.hxx:550-590): the bias force of joint i is
+// v_i x* (I_i v_i) - fext_i.
 template <class S, class SS, int CAP>
-GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, const Out& ddq) {
+GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, const Out& ddq,
+                   const In* fext = nullptr) {
   constexpr bool kStoreX = sizeof(S) == sizeof(double);
   constexpr int NB = CAP / 2 + 1;
   M6<S> vel[CAP];
@@ -235,6 +266,12 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
     cross_motion(vel[i], vJ, c);
     iner_mul(Y, vel[i], h);
     cross_force(vel[i], h, f);
+    if (fext) {
+      S fe[6];
+      load_fext(m, *fext, i, fe);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f.v[k] -= fe[k];
+    }
     if (i + 1 < m.nj && m.parent[i + 1] == i) {  // first child's contribution, carried
       sym6_add(Ia, Icar);
 #pragma unroll

@@ -40,6 +40,9 @@ int check_ptr(const void* p, const char* name);
 // launches (gb_kernels.cu / gb_derivs.cu)
 int launch_rnea(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
 int launch_aba(const gb_model* m, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
+// with external forces (njoints x 6 per configuration): one thread per configuration
+int launch_rnea_fext(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr fext, Arr tau, cudaStream_t st);
+int launch_aba_fext(const gb_model* m, int precision, long B, Arr q, Arr v, Arr tau, Arr fext, Arr ddq, cudaStream_t st);
 // warp-per-instance layout (gb_warp.cu)
 int launch_rnea_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
 int launch_aba_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);

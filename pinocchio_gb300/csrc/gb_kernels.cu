@@ -52,6 +52,30 @@ __global__ void __launch_bounds__(kThreads, GB_ABA_MINB) k_aba(const unsigned ch
   gb::aba_one<S, SS, CAP>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b));
 }
 
+// RNEA / ABA with external forces fext (njoints x 6 per configuration, in the
+// joint frames): one thread per configuration, whatever layout the model has.
+template <class S, int CAP>
+__global__ void __launch_bounds__(kThreads) k_rnea_fext(const unsigned char* blob, int bytes, long B, Arr q, Arr v,
+                                                        Arr a, Arr fext, Arr tau) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const gb::In fe = in_at(fext, b);
+  gb::rnea_one<S, CAP>(m, in_at(q, b), in_at(v, b), in_at(a, b), out_at(tau, b), &fe);
+}
+
+template <class S, class SS, int CAP>
+__global__ void __launch_bounds__(kThreads, GB_ABA_MINB) k_aba_fext(const unsigned char* blob, int bytes, long B,
+                                                                    Arr q, Arr v, Arr tau, Arr fext, Arr ddq) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const gb::In fe = in_at(fext, b);
+  gb::aba_one<S, SS, CAP>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b), &fe);
+}
+
 template <class S, int CAP>
 __global__ void __launch_bounds__(kThreads) k_crba(const unsigned char* blob, int bytes, long B, bool symmetric, Arr q,
                                                    Arr M, Arr U, Arr D) {
@@ -147,6 +171,26 @@ int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, 
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C>), q, v, tau, ddq));
   } else {
     GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<float, double, C>), q, v, tau, ddq));
+  }
+}
+
+int launch_rnea_fext(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr fext, Arr tau,
+                     cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_RNEA;
+  if (precision == GB_FP64) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_rnea_fext<double, C>), q, v, a, fext, tau));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_rnea_fext<float, C>), q, v, a, fext, tau));
+  }
+}
+
+int launch_aba_fext(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr fext, Arr ddq,
+                    cudaStream_t st) {
+  constexpr int GB_FUNC_ID = GB_FUNC_ABA;
+  if (precision == GB_FP64) {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<double, double, C>), q, v, tau, fext, ddq));
+  } else {
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<float, double, C>), q, v, tau, fext, ddq));
   }
 }
 

@@ -22,6 +22,7 @@ struct SweepCall {
   Arr q, v, tau, ddq;  // computeMinverse: v = tau = a zero vector
   void* ws;
   cudaStream_t st;
+  Arr fext;  // external forces (njoints x 6 per configuration, joint frames) or p == nullptr
 };
 int sweeps_team(const SweepCall& c);  // dispatches on the model's layout
 int sweeps_t1(const SweepCall& c);
@@ -79,29 +80,34 @@ template <int TS> __device__ __forceinline__ long sweep_config() {
     else fn(__VA_ARGS__, gb::LaneTeam<TS>((int)(threadIdx.x & 31))); \
   } while (0)
 
-template <class K, class SS, int TS>
+// FE: with external forces (read from fext; otherwise fext is not touched)
+template <class K, class SS, int TS, bool FE = false>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_aba_derivs_pass12(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, SS* wsSS, K* wsMB,
-                        int npk, Arr q, Arr v, Arr tau) {
+                        int npk, Arr q, Arr v, Arr tau, Arr fext) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = sweep_config<TS>();
   if (b >= B) return;
+  const gb::In fe = in_at(fext, b);
   GB_SWEEP_CALL((gb::aba_derivs_pass12<K, SS>), m, L, gb::Ws<K>{wsK + b, B},
-                gb::Ws<SS>{wsSS + b, B}, blocked(wsMB, npk, b), in_at(q, b), in_at(v, b), in_at(tau, b));
+                gb::Ws<SS>{wsSS + b, B}, blocked(wsMB, npk, b), in_at(q, b), in_at(v, b), in_at(tau, b),
+                FE ? &fe : nullptr);
 }
 
-template <class S, class T, class K, int TS>
+template <class S, class T, class K, int TS, bool FE = false>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_aba_derivs_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, K* wsMB,
-                       int npk, Arr v, Arr ddq) {
+                       int npk, Arr v, Arr ddq, Arr fext) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = sweep_config<TS>();
   if (b >= B) return;
   const gb::Out dd = out_at(ddq, b);
+  const gb::In fe = in_at(fext, b);
   GB_SWEEP_CALL((gb::aba_derivs_pass3<S, T, K, false>), m, L, m.slot, gb::Ws<S>{wsS + b, B},
-                gb::Ws<K>{wsK + b, B}, blocked(wsMB, npk, b), in_at(v, b), ddq.p ? &dd : nullptr);
+                gb::Ws<K>{wsK + b, B}, blocked(wsMB, npk, b), in_at(v, b), ddq.p ? &dd : nullptr,
+                FE ? &fe : nullptr);
 }
 
 // the Minv recursion of computeMinverse (pass 3 without velocities and column sets)
@@ -114,7 +120,7 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
   if (b >= B) return;
   const gb::Ws<K> zk = gb::Ws<K>{wsK + b, B};
   GB_SWEEP_CALL((gb::aba_derivs_pass3<K, K, K, true>), m, L, m.slot, zk, zk, blocked(wsMB, npk, b),
-                gb::In{nullptr, 0}, nullptr);
+                gb::In{nullptr, 0}, nullptr, nullptr);
 }
 
 template <class S, class T, class K, class P, int TS>
@@ -167,22 +173,22 @@ template <int TS> void sweep_grid(const gb_model* M, long B, int& tpb, long& gri
   grid = (B + per - 1) / per;
 }
 
-template <class S, class T3, class T, class K, class SS, class P, int TS>
+template <class S, class T3, class T, class K, class SS, class P, int TS, bool FE = false>
 int launch_sweeps_as(const gb_model* M, long B, const gb::DerivLayout& L, Arr q, Arr v, Arr tau, Arr ddq, SS* wsSS,
-                     K* wsK, S* wsS, K* wsMB, P* wsP, int npk, cudaStream_t st) {
+                     K* wsK, S* wsS, K* wsMB, P* wsP, int npk, cudaStream_t st, Arr fext) {
   int tpb;
   long grid;
   sweep_grid<TS>(M, B, tpb, grid);
-  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS, TS>, "k_aba_derivs_pass12");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T3, K, TS>, "k_aba_derivs_pass3");
+  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS, TS, FE>, "k_aba_derivs_pass12");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T3, K, TS, FE>, "k_aba_derivs_pass3");
   if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, T, K, P, TS>, "k_aba_derivs_pass4");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass12<K, SS, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L, wsK,
-                                                                                   wsSS, wsMB, npk, q, v, tau);
+  k_aba_derivs_pass12<K, SS, TS, FE><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
+      M->d_blob, M->stage_bytes, B, L, wsK, wsSS, wsMB, npk, q, v, tau, fext);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass3<S, T3, K, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
-                                                                                     wsS, wsK, wsMB, npk, v, ddq);
+  k_aba_derivs_pass3<S, T3, K, TS, FE><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
+      M->d_blob, M->stage_bytes, B, L, wsS, wsK, wsMB, npk, v, ddq, fext);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass3");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass4<S, T, K, P, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
@@ -200,7 +206,8 @@ int minverse_sweeps_as(const gb_model* M, long B, const gb::DerivLayout& L, Arr 
   if (rc == GB_OK) rc = blob_smem(M, (const void*)k_minverse_pass3<K, TS>, "k_minverse_pass3");
   if (rc != GB_OK) return rc;
   k_aba_derivs_pass12<K, SS, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L, wsK,
-                                                                                   wsSS, wsMB, npk, q, zero, zero);
+                                                                                   wsSS, wsMB, npk, q, zero, zero,
+                                                                                   Arr{nullptr, 0, 0});
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
   if (rc != GB_OK) return rc;
   k_minverse_pass3<K, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L, wsK, wsMB,
@@ -208,16 +215,16 @@ int minverse_sweeps_as(const gb_model* M, long B, const gb::DerivLayout& L, Arr 
   return cuda_error(cudaGetLastError(), "k_minverse_pass3");
 }
 
-template <class S, class T3, class T, class K, class SS, class P, int TS>
+template <class S, class T3, class T, class K, class SS, class P, int TS, bool FE = false>
 int aba_sweeps_on(const SweepCall& c) {
   const gb_model* M = c.M;
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, c.B);
   char* base = static_cast<char*>(c.ws);
-  return launch_sweeps_as<S, T3, T, K, SS, P, TS>(
+  return launch_sweeps_as<S, T3, T, K, SS, P, TS, FE>(
       M, c.B, L, c.q, c.v, c.tau, c.ddq, reinterpret_cast<SS*>(base), reinterpret_cast<K*>(base + W.oK),
       reinterpret_cast<S*>(base + W.oS), reinterpret_cast<K*>(base + W.oMB), reinterpret_cast<P*>(base + W.oP),
-      M->nv * (M->nv + 1) / 2, c.st);
+      M->nv * (M->nv + 1) / 2, c.st, c.fext);
 }
 
 template <class K, class SS, int TS>
@@ -235,6 +242,13 @@ int minverse_sweeps_on(const SweepCall& c) {
 template <int TS>
 int sweeps_for(const SweepCall& c) {
   using gb::dfloat;
+  if (c.fext.p) {  // external forces: one thread per configuration, ddq and the derivatives
+    if constexpr (TS == 1) {
+      if (c.kind == kSweepFp64) return aba_sweeps_on<double, double, double, double, double, double, 1, true>(c);
+      if (c.kind == kSweepMixed) return aba_sweeps_on<float, float, dfloat, dfloat, double, float, 1, true>(c);
+    }
+    return set_error(GB_ERR_INVALID_ARGUMENT, "external forces: unsupported sweep variant");
+  }
   switch (c.kind) {
     case kSweepFp64: return aba_sweeps_on<double, double, double, double, double, double, TS>(c);
     case kSweepMixed: return aba_sweeps_on<float, float, dfloat, dfloat, double, float, TS>(c);

@@ -19,6 +19,22 @@ struct Mat {
   double* data() { return d.data(); }
 };
 
+// Overload resolution of the external-force calls next to the plain ones (compiled,
+// not run: these take device pointers).
+[[maybe_unused]] static void fext_overloads_resolve(const pinocchio_gb300::Model& m, double* q, double* x, double* f,
+                                                    double* o1, double* o2, double* o3) {
+  const pinocchio_gb300::ExternalForces fe{f};
+  pinocchio_gb300::rnea(m, GB_FP64, 1, q, x, x, o1);
+  pinocchio_gb300::rnea(m, GB_FP64, 1, q, x, x, fe, o1);
+  pinocchio_gb300::computeStaticTorque(m, GB_MIXED, 1, q, fe, o1);
+  pinocchio_gb300::aba(m, GB_FP64, 1, q, x, x, o1, GB_WORLD);
+  pinocchio_gb300::aba(m, GB_FP64, 1, q, x, x, fe, o1, GB_WORLD);
+  pinocchio_gb300::computeRNEADerivatives(m, GB_FP64, 1, q, x, x, o1, o2, o3);
+  pinocchio_gb300::computeRNEADerivatives(m, GB_FP64, 1, q, x, x, fe, o1, o2, o3);
+  pinocchio_gb300::computeABADerivatives(m, GB_MIXED, 1, q, x, x, o1, o2, o3);
+  pinocchio_gb300::computeABADerivatives(m, GB_MIXED, 1, q, x, x, fe, o1, o2, o3);
+}
+
 int main() {
   pinocchio_gb300::ModelTables t;
   t.parents = {0, 0, 1, 2};

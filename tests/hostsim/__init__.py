@@ -32,12 +32,12 @@ def lib():
         L.hs_model_new.restype = vp
         L.hs_model_new.argtypes = [C.POINTER(ModelDesc)]
         L.hs_model_free.argtypes = [vp]
-        L.hs_rnea.argtypes = [vp, i, l, vp, vp, vp, vp]
-        L.hs_aba.argtypes = [vp, i, l, vp, vp, vp, vp]
+        L.hs_rnea.argtypes = [vp, i, l, vp, vp, vp, vp, vp]
+        L.hs_aba.argtypes = [vp, i, l, vp, vp, vp, vp, vp]
         L.hs_crba.argtypes = [vp, i, i, l, vp, vp, vp, vp]
         L.hs_integrate.argtypes = [vp, l, vp, vp, vp]
-        L.hs_rnea_derivs.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp]
-        L.hs_aba_derivs.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
+        L.hs_rnea_derivs.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.hs_aba_derivs.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -63,16 +63,19 @@ class HostSim:
         if getattr(self, "h", None) and _lib is not None:
             _lib.hs_model_free(self.h)
 
-    def rnea(self, q, v, a, mixed=False):
+    # fext: external forces (B, njoints, 6) in the joint frames, or None
+    def rnea(self, q, v, a, mixed=False, fext=None):
         q, v, a = _c(q), _c(v), _c(a)
         tau = np.empty((q.shape[0], self.nv))
-        lib().hs_rnea(self.h, int(mixed), q.shape[0], _p(q), _p(v), _p(a), _p(tau))
+        f = None if fext is None else _c(fext)
+        lib().hs_rnea(self.h, int(mixed), q.shape[0], _p(q), _p(v), _p(a), _p(tau), _p(f))
         return tau
 
-    def aba(self, q, v, tau, mixed=False):
+    def aba(self, q, v, tau, mixed=False, fext=None):
         q, v, tau = _c(q), _c(v), _c(tau)
         ddq = np.empty((q.shape[0], self.nv))
-        lib().hs_aba(self.h, int(mixed), q.shape[0], _p(q), _p(v), _p(tau), _p(ddq))
+        f = None if fext is None else _c(fext)
+        lib().hs_aba(self.h, int(mixed), q.shape[0], _p(q), _p(v), _p(tau), _p(ddq), _p(f))
         return ddq
 
     def crba(self, q, mixed=False, symmetric=False, cholesky=False):
@@ -90,18 +93,20 @@ class HostSim:
         lib().hs_integrate(self.h, q.shape[0], _p(q), _p(v), _p(out))
         return out
 
-    def rnea_derivatives(self, q, v, a, mixed=False, symmetric=True):
+    def rnea_derivatives(self, q, v, a, mixed=False, symmetric=True, fext=None):
         q, v, a = _c(q), _c(v), _c(a)
         B, nv = q.shape[0], self.nv
         dq, dv, M = (np.empty((B, nv, nv)) for _ in range(3))
         tau = np.empty((B, nv))
-        lib().hs_rnea_derivs(self.h, int(mixed), int(symmetric), B, _p(q), _p(v), _p(a), _p(dq), _p(dv), _p(M), _p(tau))
+        f = None if fext is None else _c(fext)
+        lib().hs_rnea_derivs(self.h, int(mixed), int(symmetric), B, _p(q), _p(v), _p(a), _p(dq), _p(dv), _p(M), _p(tau), _p(f))
         return tau, dq, dv, M
 
-    def aba_derivatives(self, q, v, tau, mixed=False):
+    def aba_derivatives(self, q, v, tau, mixed=False, fext=None):
         q, v, tau = _c(q), _c(v), _c(tau)
         B, nv = q.shape[0], self.nv
         dq, dv, Minv = (np.empty((B, nv, nv)) for _ in range(3))
         ddq = np.empty((B, nv))
-        lib().hs_aba_derivs(self.h, int(mixed), B, _p(q), _p(v), _p(tau), _p(dq), _p(dv), _p(Minv), _p(ddq))
+        f = None if fext is None else _c(fext)
+        lib().hs_aba_derivs(self.h, int(mixed), B, _p(q), _p(v), _p(tau), _p(dq), _p(dv), _p(Minv), _p(ddq), _p(f))
         return ddq, dq, dv, Minv

@@ -41,23 +41,30 @@ void hs_model_free(void* h) { delete static_cast<gb_model*>(h); }
     default: { constexpr int C = 128; CALL; break; }                       \
   }
 
-int hs_rnea(void* h, int mixed, long B, const double* q, const double* v, const double* a, double* tau) {
+// fext: external forces (njoints x 6 per instance) or NULL
+int hs_rnea(void* h, int mixed, long B, const double* q, const double* v, const double* a, double* tau,
+            const double* fext) {
   const gb_model* M = static_cast<gb_model*>(h);
   const gb::MView m = gb::make_view(M->blob.data());
 #pragma omp parallel for schedule(static)
   for (long b = 0; b < B; ++b) {
-    if (mixed) { HS_DISPATCH(M->cap, (gb::rnea_one<float, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv), out_at(tau, b, m.nv)))); }
-    else { HS_DISPATCH(M->cap, (gb::rnea_one<double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv), out_at(tau, b, m.nv)))); }
+    const gb::In fe = in_at(fext, b, 6L * m.nj);
+    const gb::In* fp = fext ? &fe : nullptr;
+    if (mixed) { HS_DISPATCH(M->cap, (gb::rnea_one<float, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv), out_at(tau, b, m.nv), fp))); }
+    else { HS_DISPATCH(M->cap, (gb::rnea_one<double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv), out_at(tau, b, m.nv), fp))); }
   }
   return 0;
 }
-int hs_aba(void* h, int mixed, long B, const double* q, const double* v, const double* tau, double* ddq) {
+int hs_aba(void* h, int mixed, long B, const double* q, const double* v, const double* tau, double* ddq,
+           const double* fext) {
   const gb_model* M = static_cast<gb_model*>(h);
   const gb::MView m = gb::make_view(M->blob.data());
 #pragma omp parallel for schedule(static)
   for (long b = 0; b < B; ++b) {
-    if (mixed) { HS_DISPATCH(M->cap, (gb::aba_one<float, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv)))); }
-    else { HS_DISPATCH(M->cap, (gb::aba_one<double, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv)))); }
+    const gb::In fe = in_at(fext, b, 6L * m.nj);
+    const gb::In* fp = fext ? &fe : nullptr;
+    if (mixed) { HS_DISPATCH(M->cap, (gb::aba_one<float, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv), fp))); }
+    else { HS_DISPATCH(M->cap, (gb::aba_one<double, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv), fp))); }
   }
   return 0;
 }
@@ -88,7 +95,7 @@ int hs_integrate(void* h, long B, const double* q, const double* v, double* qo) 
 #include <vector>
 
 extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const double* q, const double* v, const double* a,
-                   double* dq, double* dv, double* Mo, double* tau) {
+                   double* dq, double* dv, double* Mo, double* tau, const double* fext) {
   const gb_model* M = static_cast<gb_model*>(h);
   const gb::MView m = gb::make_view(M->blob.data());
   const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, false);
@@ -100,12 +107,14 @@ extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const d
 #pragma omp for schedule(static)
     for (long b = 0; b < B; ++b) {
       const gb::Out to = out_at(tau, b, m.nv);
+      const gb::In fe = in_at(fext, b, 6L * m.nj);
+      const gb::In* fp = fext ? &fe : nullptr;
       if (mixed)
         gb::rnea_derivs_one<float>(m, L, gb::Ws<float>{wf.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
-                                   out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false);
+                                   out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false, fp);
       else
         gb::rnea_derivs_one<double>(m, L, gb::Ws<double>{wd.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
-                                    out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false);
+                                    out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false, fp);
     }
   }
   return 0;
@@ -118,17 +127,18 @@ extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const d
 template <class S, class T3, class T, class K, class P>
 static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const double* q, const double* v,
                             const double* tau, double* dq, double* dv, double* Minv, double* ddq,
-                            std::vector<S>& wS, std::vector<K>& wK, std::vector<double>& wSS) {
+                            std::vector<S>& wS, std::vector<K>& wK, std::vector<double>& wSS, const double* fext) {
   const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
   const int nv = m.nv;
   const long nn = (long)nv * nv;
   std::vector<P> wP(L.nP);
   const gb::Out dd = out_at(ddq, b, nv);
+  const gb::In fe = in_at(fext, b, 6L * m.nj);
   std::vector<K> wM(nv * (nv + 1) / 2);
   gb::aba_derivs_sweeps<S, T3, T, K, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
                                                 gb::Ws<double>{wSS.data(), 1}, gb::Ws<K>{wM.data(), 1},
                                                 gb::Ws<P>{wP.data(), 1}, in_at(q, b, m.nq), in_at(v, b, nv),
-                                                in_at(tau, b, nv), &dd);
+                                                in_at(tau, b, nv), &dd, fext ? &fe : nullptr);
   double* Mi = Minv + b * nn;
   std::vector<P> Mp(nn);
   for (int r = 0; r < nv; ++r)
@@ -153,7 +163,7 @@ static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const
 }
 
 extern "C" int hs_aba_derivs(void* h, int mixed, long B, const double* q, const double* v, const double* tau, double* dq,
-                  double* dv, double* Minv, double* ddq) {
+                  double* dv, double* Minv, double* ddq, const double* fext) {
   const gb_model* M = static_cast<gb_model*>(h);
   const gb::MView m = gb::make_view(M->blob.data());
   const gb::DerivLayout L = gb::make_deriv_layout(m.nj, m.nv, M->nslot, true);
@@ -165,8 +175,10 @@ extern "C" int hs_aba_derivs(void* h, int mixed, long B, const double* q, const 
 #pragma omp for schedule(static)
     for (long b = 0; b < B; ++b) {
       if (mixed)
-        aba_derivs_host<float, float, gb::dfloat, gb::dfloat, float>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wfk, wss);
-      else aba_derivs_host<double, double, double, double, double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wdk, wss);
+        aba_derivs_host<float, float, gb::dfloat, gb::dfloat, float>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wf, wfk, wss,
+                                                                     fext);
+      else aba_derivs_host<double, double, double, double, double>(M, m, b, q, v, tau, dq, dv, Minv, ddq, wd, wdk, wss,
+                                                                   fext);
     }
   }
   return 0;

@@ -40,6 +40,14 @@ def test_invalid_arguments_are_rejected_on_the_host(L):
     assert b"model" in L.gb_last_error()
     out = C.c_void_p()
     assert L.gb_model_create(None, C.byref(out)) == _capi.GB_ERR_INVALID_ARGUMENT
+    # the external-force entry points check their arguments the same way, and require fext
+    assert L.gb_rnea_fext(None, 0, 0, 1, None, None, None, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_aba_fext(None, 0, 0, 0, 1, None, None, None, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_static_torque(None, 0, 0, 1, None, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_rnea_derivatives_fext(None, 0, 0, 0, 1, *([None] * 9)) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert b"fext" in L.gb_last_error()
+    assert L.gb_aba_derivatives_fext(None, 0, 0, 1, *([None] * 9)) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert b"fext" in L.gb_last_error()
 
 
 def _create(L, model_tables):
