@@ -218,7 +218,8 @@ def measure_functions(torch, pg, sm):
     """evals/s of every batched function on the humanoid, per precision: RNEA / ABA /
     CRBA (+ tree Cholesky) / computeMinverse / nonLinearEffects / generalized gravity /
     forwardKinematics (q, v, a) / computeJointJacobians at batch 65536, the two derivative
-    algorithms at batch 16384."""
+    algorithms at batch 16384; RNEA, ABA and the ABA derivatives with external forces on
+    every joint (the fext overloads) at the same batches."""
     model = sm.humanoid32(1)
     out = {}
     for prec in ("fp64", "mixed"):
@@ -227,8 +228,10 @@ def measure_functions(torch, pg, sm):
         for fname, B in (("rnea", 65536), ("aba", 65536), ("crba", 65536), ("crba_cholesky", 65536),
                          ("rnea_derivatives", 16384), ("aba_derivatives", 16384), ("compute_minverse", 65536),
                          ("nonlinear_effects", 65536), ("generalized_gravity", 65536),
-                         ("forward_kinematics", 65536), ("joint_jacobians", 65536)):
+                         ("forward_kinematics", 65536), ("joint_jacobians", 65536), ("rnea_fext", 65536),
+                         ("aba_fext", 65536), ("aba_derivatives_fext", 16384)):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
+            f = torch.randn((B, model.njoints, 6), dtype=torch.float64, device="cuda")
             fn = {
                 "rnea": lambda: pg.rnea(model, data, q, v, x),
                 "aba": lambda: pg.aba(model, data, q, v, 10.0 * x),
@@ -241,10 +244,13 @@ def measure_functions(torch, pg, sm):
                 "generalized_gravity": lambda: pg.computeGeneralizedGravity(model, data, q),
                 "forward_kinematics": lambda: pg.forwardKinematics(model, data, q, v, x),
                 "joint_jacobians": lambda: pg.computeJointJacobians(model, data, q),
+                "rnea_fext": lambda: pg.rnea(model, data, q, v, x, f),
+                "aba_fext": lambda: pg.aba(model, data, q, v, 10.0 * x, f),
+                "aba_derivatives_fext": lambda: pg.computeABADerivatives(model, data, q, v, 10.0 * x, f),
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}
-            del q, v, x
+            del q, v, x, f
         out[prec] = res
     return out
 

@@ -34,6 +34,7 @@ from .api import (  # noqa: F401
     computeMinverse,
     computeRNEADerivatives,
     computeStaticTorque,
+    computeStaticTorqueDerivatives,
     crba,
     crbaCholesky,
     createData,

@@ -254,6 +254,16 @@ def computeMinverse(model: Model, data: Data, q, symmetric: bool = True):
     return _ret(out, was_np, vec)
 
 
+def computeStaticTorqueDerivatives(model: Model, data: Data, q, fext):
+    """d(computeStaticTorque)/dq (reference algorithm/rnea-derivatives.hxx:185-233, public
+    686-697): the RNEA derivative sweeps with external forces at zero velocity and
+    acceleration, of which the q-derivative is returned."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    z = _torch().zeros((qt.shape[0], model.nv), dtype=qt.dtype, device=qt.device)
+    dq = computeRNEADerivatives(model, data, qt, z, z, fext)[0]
+    return _ret(dq, was_np, vec)
+
+
 def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = None, fext=None):
     """ddq = ABA(q, v, tau) (reference algorithm/aba.hxx:933-948), called as the
     reference's binding is: aba(model, data, q, v, tau[, convention]) or

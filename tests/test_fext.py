@@ -152,3 +152,18 @@ def test_kernel_code_with_fext_on_host(name):
     for mixed, t in ((False, 1e-12), (True, tol)):
         for x, y in zip(hs.aba_derivatives(q, v, tau, mixed=mixed, fext=fext), ref):
             assert rel_err(x, y) < t
+
+
+def test_static_torque_derivatives_vs_central_fd():
+    """d/dq of rnea(q, 0, 0, fext), which computeStaticTorqueDerivatives returns
+    (rnea-derivatives.hxx:185-233), against central differences"""
+    model = MODELS["unaligned20ff"]()
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, 3, 31)
+    fext = random_fext(om.njoints, 3, 32)
+    z = np.zeros_like(v)
+    dq = om.rnea_derivatives(q, z, z, fext=fext)[1]
+    fd = np.zeros_like(dq)
+    for k in range(model.nv):
+        fd[:, :, k] = _fd(lambda x: om.rnea(x, z, z, fext=fext), q, 1e-6, k, (om.integrate, model.nv))
+    assert rel_err(dq, fd) < 1e-6

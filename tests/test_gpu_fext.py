@@ -91,21 +91,21 @@ def test_soa_layout_with_fext(case):
     name, model, om, q, v, x, fext, dev = case
     data = pg.createData(model)
     B, nv = q.shape[0], model.nv
-    f2 = fext.reshape(B, -1)
+    tau = 10.0 * x
+    # the value-major copies stay referenced until the kernels have run
+    qs, vs, xs, ts, fs = (dev(np.ascontiguousarray(t.T)) for t in (q, v, x, tau, fext.reshape(B, -1)))
     p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
-    T = lambda t: dev(np.ascontiguousarray(t.T))  # noqa: E731
     ref_tau = pg.rnea(model, data, dev(q), dev(v), dev(x), dev(fext))
     out = torch.empty((nv, B), dtype=torch.float64, device="cuda")
-    _capi.check(_capi.lib().gb_rnea_fext(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, p(T(q)), p(T(v)), p(T(x)),
-                                         p(T(f2)), p(out), None))
+    _capi.check(_capi.lib().gb_rnea_fext(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, p(qs), p(vs), p(xs), p(fs),
+                                         p(out), None))
     torch.cuda.synchronize()
     assert torch.equal(out.T, ref_tau)
-    tau = 10.0 * x
     ref = pg.computeABADerivatives(model, data, dev(q), dev(v), dev(tau), dev(fext))
     mats = [torch.empty((nv * nv, B), dtype=torch.float64, device="cuda") for _ in range(3)]
     ddq = torch.empty((nv, B), dtype=torch.float64, device="cuda")
-    _capi.check(_capi.lib().gb_aba_derivatives_fext(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, p(T(q)), p(T(v)),
-                                                    p(T(tau)), p(T(f2)), *(p(m) for m in mats), p(ddq), None))
+    _capi.check(_capi.lib().gb_aba_derivatives_fext(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, p(qs), p(vs),
+                                                    p(ts), p(fs), *(p(m) for m in mats), p(ddq), None))
     torch.cuda.synchronize()
     for m, r in zip(mats, ref):
         assert torch.equal(m.T.reshape(B, nv, nv), r)
@@ -120,6 +120,19 @@ def test_fext_arguments_are_checked(case):
     B = q.shape[0]
     p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
     out = dev(np.zeros((B, model.nv)))
-    rc = _capi.lib().gb_rnea_fext(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, B, p(dev(q)), p(dev(v)), p(dev(x)),
-                                  None, p(out), None)
+    qd, vd, xd = dev(q), dev(v), dev(x)
+    rc = _capi.lib().gb_rnea_fext(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, B, p(qd), p(vd), p(xd), None,
+                                  p(out), None)
     assert rc == _capi.GB_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_static_torque_derivatives(case, precision):
+    """computeStaticTorqueDerivatives (rnea-derivatives.hxx:185-233) against the oracle's
+    RNEA derivatives at zero velocity and acceleration with the same forces"""
+    name, model, om, q, v, x, fext, dev = case
+    data = pg.createData(model, precision)
+    z = np.zeros_like(v)
+    ref = om.rnea_derivatives(q, z, z, fext=fext)[1]
+    got = pg.computeStaticTorqueDerivatives(model, data, dev(q), dev(fext)).cpu().numpy()
+    assert rel_err(got, ref) < _tol(name, precision)
