@@ -227,6 +227,31 @@ int gb_aba_derivatives_noalloc(const gb_model* model, int precision, int layout,
                                const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                                double* ddq, void* stream);
 
+/* Contact dynamics with a given constraint Jacobian.  J holds, per instance, an
+ * nc x nv row-major matrix (nc * nv values in `layout`); gamma, lambda_c and
+ * impulse_c nc values (they, and J, may be NULL when nc == 0).  M = U D U^T comes
+ * from the CRBA with the FP64 tree factorisation, the rest is FP64 in both
+ * precisions except the bias forces (FP32 sweeps in GB_MIXED).  As in the
+ * reference, J M^-1 J^T + inv_damping I must be positive definite (a rank-deficient
+ * J needs inv_damping > 0); otherwise the outputs are NaN.  inv_damping < 0 is
+ * rejected, nc is limited to 0..1024.
+ *
+ * forwardDynamics(model, data, q, v, tau, J, gamma, inv_damping) (reference
+ * algorithm/contact-dynamics.hxx:81-165, contact-dynamics.hpp:60-74, deprecated there):
+ * ddq and lambda_c with M ddq + nle = tau + J^T lambda_c and
+ * J ddq + gamma = -inv_damping lambda_c. */
+int gb_forward_dynamics(const gb_model* model, int precision, int layout, long batch, int nc, const double* q,
+                        const double* v, const double* tau, const double* J, const double* gamma,
+                        double inv_damping, double* ddq, double* lambda_c, void* stream);
+
+/* impulseDynamics(model, data, q, v_before, J, r_coeff, inv_damping) (reference
+ * algorithm/contact-dynamics.hxx:255-327, contact-dynamics.hpp:230-248, deprecated there):
+ * dq_after and impulse_c with M (dq_after - v_before) = J^T impulse_c and
+ * J dq_after = -r_coeff J v_before - inv_damping impulse_c. */
+int gb_impulse_dynamics(const gb_model* model, int precision, int layout, long batch, int nc, const double* q,
+                        const double* v_before, const double* J, double r_coeff, double inv_damping,
+                        double* dq_after, double* impulse_c, void* stream);
+
 /* forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272):
  * per instance, for every joint i = 0 .. njoints-1 (joint 0 the universe:
  * identity, zero), oMi[12 i ..] = the world placement (rotation row-major, then

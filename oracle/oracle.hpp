@@ -1342,6 +1342,141 @@ void aba_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T
 // and a): liMi, oMi, and the joint-frame spatial velocities / accelerations
 // (no gravity: data.a[0] = 0).
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Tree-sparse solves with M = U D U^T (algorithm/cholesky.hxx): Uiv (210-235,
+// v <- U^-1 v), Utiv (275-296, v <- U^-T v) and solve (483-505, v <- M^-1 v).
+// ---------------------------------------------------------------------------
+template <class T>
+void chol_Uiv(const Model& m, const Data<T>& d, T* v, int stride = 1) {
+  const int nv = m.nv;
+  for (int k = nv - 2; k >= 0; --k) {
+    const int n = m.nvSubtree_fromRow[k] - 1;
+    T s = T(0);
+    for (int j = 0; j < n; ++j) s += d.U[(size_t)k * nv + k + 1 + j] * v[(size_t)(k + 1 + j) * stride];
+    v[(size_t)k * stride] -= s;
+  }
+}
+template <class T>
+void chol_Utiv(const Model& m, const Data<T>& d, T* v) {
+  const int nv = m.nv;
+  for (int k = 0; k < nv - 1; ++k) {
+    const int n = m.nvSubtree_fromRow[k] - 1;
+    for (int j = 0; j < n; ++j) v[k + 1 + j] -= d.U[(size_t)k * nv + k + 1 + j] * v[k];
+  }
+}
+template <class T>
+void chol_solve(const Model& m, const Data<T>& d, T* v) {
+  chol_Uiv(m, d, v);
+  for (int k = 0; k < m.nv; ++k) v[k] *= d.Dinv[k];
+  chol_Utiv(m, d, v);
+}
+
+// In-place LLT of an n x n row-major SPD matrix (lower factor L, G = L L^T) and
+// the solve G x = b (Eigen LLT, Cholesky-Banachiewicz order; the reference's
+// PerformCholeskyCompute / PerformCholeskySolveInPlace, contact-dynamics.hxx:19-80).
+template <class T>
+void llt_factor_solve(int n, T* G, T* b) {
+  for (int j = 0; j < n; ++j) {
+    T s = G[(size_t)j * n + j];
+    for (int k = 0; k < j; ++k) s -= G[(size_t)j * n + k] * G[(size_t)j * n + k];
+    const T ljj = o_sqrt(s);
+    G[(size_t)j * n + j] = ljj;
+    for (int i = j + 1; i < n; ++i) {
+      T t = G[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) t -= G[(size_t)i * n + k] * G[(size_t)j * n + k];
+      G[(size_t)i * n + j] = t / ljj;
+    }
+  }
+  for (int i = 0; i < n; ++i) {  // L y = b
+    T t = b[i];
+    for (int k = 0; k < i; ++k) t -= G[(size_t)i * n + k] * b[k];
+    b[i] = t / G[(size_t)i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {  // L^T x = y
+    T t = b[i];
+    for (int k = i + 1; k < n; ++k) t -= G[(size_t)k * n + i] * b[k];
+    b[i] = t / G[(size_t)i * n + i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Contact dynamics with a given constraint Jacobian (algorithm/contact-dynamics.hxx):
+// forwardDynamics(q, v, tau, J, gamma, inv_damping) (81-165) and
+// impulseDynamics(q, v_before, J, r_coeff, inv_damping) (255-327).  J is nc x nv
+// row-major.  Outputs: d.ddq (or the velocity after impact) in `out` and the
+// multipliers (lambda_c / impulse_c) in `lam`.
+// ---------------------------------------------------------------------------
+template <class T>
+void contact_common(const Model& m, Data<T>& d, const T* q, int nc, const T* J, T inv_damping,
+                    std::vector<T>& G) {
+  const int nv = m.nv;
+  std::fill(d.M.begin(), d.M.end(), T(0));
+  crba(m, d, q, WORLD);
+  std::fill(d.U.begin(), d.U.end(), T(0));
+  for (int k = 0; k < nv; ++k) d.U[(size_t)k * nv + k] = T(1);
+  cholesky_decompose(m, d);
+  // sDUiJt = D^-1/2 U^-1 J^T (nv x nc, row-major), JMinvJt = sDUiJt^T sDUiJt + inv_damping I
+  std::vector<T> Y((size_t)nv * nc);
+  for (int r = 0; r < nv; ++r)
+    for (int c = 0; c < nc; ++c) Y[(size_t)r * nc + c] = J[(size_t)c * nv + r];
+  for (int c = 0; c < nc; ++c) chol_Uiv(m, d, Y.data() + c, nc);
+  for (int r = 0; r < nv; ++r) {
+    const T sd = o_sqrt(d.D[r]);
+    for (int c = 0; c < nc; ++c) Y[(size_t)r * nc + c] /= sd;
+  }
+  G.assign((size_t)nc * nc, T(0));
+  for (int i = 0; i < nc; ++i)
+    for (int j = 0; j < nc; ++j) {
+      T s = T(0);
+      for (int r = 0; r < nv; ++r) s += Y[(size_t)r * nc + i] * Y[(size_t)r * nc + j];
+      G[(size_t)i * nc + j] = s + (i == j ? inv_damping : T(0));
+    }
+}
+template <class T>
+void forward_dynamics_contact(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, int nc, const T* J,
+                              const T* gamma, T inv_damping, T* out, T* lam) {
+  const int nv = m.nv;
+  std::vector<T> G;
+  contact_common(m, d, q, nc, J, inv_damping, G);
+  std::vector<T> zero(nv, T(0)), r(nv);
+  rnea(m, d, q, v, zero.data());  // nle = C(q, v) v + g (computeAllTerms)
+  for (int k = 0; k < nv; ++k) r[k] = tau[k] - d.tau[k];
+  chol_solve(m, d, r.data());  // torque_residual = M^-1 (tau - nle)
+  for (int c = 0; c < nc; ++c) {  // lambda = -J torque_residual - gamma
+    T s = T(0);
+    for (int k = 0; k < nv; ++k) s += J[(size_t)c * nv + k] * r[k];
+    lam[c] = -s - gamma[c];
+  }
+  llt_factor_solve(nc, G.data(), lam);
+  for (int k = 0; k < nv; ++k) {  // a = M^-1 J^T lambda + torque_residual
+    T s = T(0);
+    for (int c = 0; c < nc; ++c) s += J[(size_t)c * nv + k] * lam[c];
+    out[k] = s;
+  }
+  chol_solve(m, d, out);
+  for (int k = 0; k < nv; ++k) out[k] += r[k];
+}
+template <class T>
+void impulse_dynamics_contact(const Model& m, Data<T>& d, const T* q, const T* v_before, int nc, const T* J,
+                              T r_coeff, T inv_damping, T* out, T* lam) {
+  const int nv = m.nv;
+  std::vector<T> G;
+  contact_common(m, d, q, nc, J, inv_damping, G);
+  for (int c = 0; c < nc; ++c) {  // impulse = -(1 + r_coeff) J v_before
+    T s = T(0);
+    for (int k = 0; k < nv; ++k) s += J[(size_t)c * nv + k] * v_before[k];
+    lam[c] = (-r_coeff - T(1)) * s;
+  }
+  llt_factor_solve(nc, G.data(), lam);
+  for (int k = 0; k < nv; ++k) {
+    T s = T(0);
+    for (int c = 0; c < nc; ++c) s += J[(size_t)c * nv + k] * lam[c];
+    out[k] = s;
+  }
+  chol_solve(m, d, out);
+  for (int k = 0; k < nv; ++k) out[k] += v_before[k];
+}
+
 template <class T>
 void forward_kinematics(const Model& m, Data<T>& d, const T* q, const T* v, const T* a) {
   d.v[0] = zero6<T>();

@@ -56,6 +56,8 @@ def lib():
         L.orc_aba_fext.argtypes = [vp, C.c_int, C.c_int, C.c_long, vp, vp, vp, vp, vp, C.c_int]
         L.orc_rnea_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_aba_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_forward_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, vp, C.c_double, vp, vp, C.c_int]
+        L.orc_impulse_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_joint_jacobians.argtypes = [vp, C.c_int, C.c_long, vp, vp, C.c_int]
@@ -169,6 +171,24 @@ class OracleModel:
             f = self._fext(fext, B)
             self._check(lib().orc_aba_derivatives_fext(self.h, prec, B, _ptr(q), _ptr(v), _ptr(tau), _ptr(f), _ptr(ddq), _ptr(dq), _ptr(dv), _ptr(Minv), nthreads))
         return ddq, dq, dv, Minv
+
+    def forward_dynamics(self, q, v, tau, J, gamma, inv_damping=0.0, prec=0, nthreads=0):
+        """(ddq, lambda_c) of forwardDynamics with the constraint Jacobian J (B, nc, nv) and drift gamma (B, nc)."""
+        q, v, tau, J, gamma = _c(q), _c(v), _c(tau), _c(J), _c(gamma)
+        B, nc = q.shape[0], J.shape[1]
+        ddq, lam = np.empty((B, self.nv)), np.empty((B, nc))
+        self._check(lib().orc_forward_dynamics(self.h, prec, B, nc, _ptr(q), _ptr(v), _ptr(tau), _ptr(J), _ptr(gamma),
+                                               float(inv_damping), _ptr(ddq), _ptr(lam), nthreads))
+        return ddq, lam
+
+    def impulse_dynamics(self, q, v_before, J, r_coeff=0.0, inv_damping=0.0, prec=0, nthreads=0):
+        """(dq_after, impulse_c) of impulseDynamics with the constraint Jacobian J (B, nc, nv)."""
+        q, v, J = _c(q), _c(v_before), _c(J)
+        B, nc = q.shape[0], J.shape[1]
+        out, lam = np.empty((B, self.nv)), np.empty((B, nc))
+        self._check(lib().orc_impulse_dynamics(self.h, prec, B, nc, _ptr(q), _ptr(v), _ptr(J), float(r_coeff),
+                                               float(inv_damping), _ptr(out), _ptr(lam), nthreads))
+        return out, lam
 
     def integrate(self, q, v, prec=0, nthreads=0):
         q, v = _c(q), _c(v)

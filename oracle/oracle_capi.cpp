@@ -284,6 +284,61 @@ int orc_aba_derivatives_fext(void* h, int prec, long B, const double* q, const d
   return dispatch(h, prec, F_ABA_D, B, q, v, tau, ddq, ddq_dq, ddq_dv, Minv, nt, fext);
 }
 
+// Contact dynamics with a given constraint Jacobian (algorithm/contact-dynamics.hxx:81-165,
+// 255-327): per instance J is nc x nv row-major, gamma nc values; out = ddq (or the
+// velocity after impact), lam = the multipliers.  prec 0 = double, 1 = long double.
+}  // extern "C"
+namespace {
+template <class T>
+int contact_batch(const Model& m, bool impulse, long B, int nc, const double* q, const double* v, const double* x,
+                  const double* J, const double* gamma, double r_coeff, double inv_damping, double* out, double* lam,
+                  int nthreads) {
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  omp_set_dynamic(0);
+  omp_set_num_threads(nthreads);
+  std::vector<std::unique_ptr<orc::Data<T>>> datas(nthreads);
+  for (int t = 0; t < nthreads; ++t) datas[t].reset(new orc::Data<T>(m));
+  const int nq = m.nq, nv = m.nv;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    orc::Data<T>& d = *datas[omp_get_thread_num()];
+    Buf<T> bq, bv, bx, bJ, bg;
+    bq.load(q + (size_t)b * nq, nq);
+    bv.load(v + (size_t)b * nv, nv);
+    bJ.load(J + (size_t)b * nc * nv, nc * nv);
+    std::vector<T> o(nv), l(nc);
+    if (impulse) {
+      orc::impulse_dynamics_contact(m, d, bq.x.data(), bv.x.data(), nc, bJ.x.data(), T(r_coeff), T(inv_damping),
+                                    o.data(), l.data());
+    } else {
+      bx.load(x + (size_t)b * nv, nv);
+      bg.load(gamma + (size_t)b * nc, nc);
+      orc::forward_dynamics_contact(m, d, bq.x.data(), bv.x.data(), bx.x.data(), nc, bJ.x.data(), bg.x.data(),
+                                    T(inv_damping), o.data(), l.data());
+    }
+    store(o, out + (size_t)b * nv, nv);
+    store(l, lam + (size_t)b * nc, nc);
+  }
+  return 0;
+}
+}  // namespace
+extern "C" {
+int orc_forward_dynamics(void* h, int prec, long B, int nc, const double* q, const double* v, const double* tau,
+                         const double* J, const double* gamma, double inv_damping, double* ddq, double* lambda_c,
+                         int nt) {
+  const Model& m = *static_cast<Model*>(h);
+  return prec == 1 ? contact_batch<long double>(m, false, B, nc, q, v, tau, J, gamma, 0.0, inv_damping, ddq, lambda_c, nt)
+                   : contact_batch<double>(m, false, B, nc, q, v, tau, J, gamma, 0.0, inv_damping, ddq, lambda_c, nt);
+}
+int orc_impulse_dynamics(void* h, int prec, long B, int nc, const double* q, const double* v_before, const double* J,
+                         double r_coeff, double inv_damping, double* dq_after, double* impulse_c, int nt) {
+  const Model& m = *static_cast<Model*>(h);
+  return prec == 1 ? contact_batch<long double>(m, true, B, nc, q, v_before, nullptr, J, nullptr, r_coeff, inv_damping,
+                                                dq_after, impulse_c, nt)
+                   : contact_batch<double>(m, true, B, nc, q, v_before, nullptr, J, nullptr, r_coeff, inv_damping,
+                                           dq_after, impulse_c, nt);
+}
+
 int orc_forward_kinematics(void* h, int prec, long B, const double* q, const double* v, const double* a, double* oMi,
                            double* vi, double* ai, int nt) {
   return dispatch(h, prec, F_FK, B, q, v, a, oMi, vi, ai, nullptr, nt);

@@ -38,7 +38,9 @@ from .api import (  # noqa: F401
     crba,
     crbaCholesky,
     createData,
+    forwardDynamics,
     forwardKinematics,
+    impulseDynamics,
     integrate,
     nonLinearEffects,
     rnea,

@@ -46,6 +46,8 @@ EXPORTS = (
     "gb_compute_minverse",
     "gb_aba_derivatives_vjp",
     "gb_aba_derivatives_noalloc",
+    "gb_forward_dynamics",
+    "gb_impulse_dynamics",
     "gb_forward_kinematics",
     "gb_compute_joint_jacobians",
     "gb_integrate",
@@ -149,6 +151,8 @@ def lib():
         L.gb_aba_derivatives_vjp.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_aba_derivatives_noalloc.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp, vp]
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
+        L.gb_forward_dynamics.argtypes = [vp, i, i, l, i, vp, vp, vp, vp, vp, C.c_double, vp, vp, vp]
+        L.gb_impulse_dynamics.argtypes = [vp, i, i, l, i, vp, vp, vp, C.c_double, C.c_double, vp, vp, vp]
         L.gb_forward_kinematics.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.gb_compute_joint_jacobians.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]

@@ -301,6 +301,65 @@ def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = Non
     return _ret(ddq, was_np, vec)
 
 
+def _constraint(x, B: int, shape: tuple, name: str):
+    """A per-configuration constraint array (B, *shape), or one (shape) shared by the batch,
+    as a contiguous float64 CUDA tensor."""
+    torch = _torch()
+    t = torch.as_tensor(x, dtype=torch.float64)
+    if t.dim() == len(shape):
+        t = t.unsqueeze(0).expand(B, *shape)
+    if tuple(t.shape) != (B, *shape):
+        raise ValueError(f"{name} must have shape {shape} or (batch, *{shape}), got {tuple(t.shape)}")
+    if not t.is_cuda:
+        t = t.cuda()
+    return t.contiguous()
+
+
+def forwardDynamics(model: Model, data: Data, q, v, tau, J, gamma, inv_damping: float = 0.0):
+    """ddq of the dynamics under the constraints J ddq + gamma = 0 (J: (nc, nv) or (batch, nc, nv),
+    gamma: (nc,) or (batch, nc)), with the multipliers in data.lambda_c (reference
+    algorithm/contact-dynamics.hxx:81-165): M ddq + nle = tau + J^T lambda_c."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    tt = _as_batch(tau, model.nv, "tau")[0]
+    B = qt.shape[0]
+    Jt = _torch().as_tensor(J)
+    nc = int(Jt.shape[-2])
+    Jt = _constraint(J, B, (nc, model.nv), "J")
+    gt = _constraint(gamma, B, (nc,), "gamma")
+    ddq = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    lam = _torch().empty((B, nc), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_forward_dynamics(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, nc, _ptr(qt), _ptr(vt), _ptr(tt), _ptr(Jt),
+            _ptr(gt), float(inv_damping), _ptr(ddq), _ptr(lam), _stream_ptr(),
+        )
+    )
+    data.ddq, data.lambda_c = ddq, _ret(lam, was_np, vec)
+    return _ret(ddq, was_np, vec)
+
+
+def impulseDynamics(model: Model, data: Data, q, v_before, J, r_coeff: float = 0.0, inv_damping: float = 0.0):
+    """The velocity after an impact on the constraints J (restitution r_coeff), with the
+    impulses in data.impulse_c (reference algorithm/contact-dynamics.hxx:255-327):
+    M (dq_after - v_before) = J^T impulse_c, J dq_after = -r_coeff J v_before."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v_before, model.nv, "v_before")[0]
+    B = qt.shape[0]
+    nc = int(_torch().as_tensor(J).shape[-2])
+    Jt = _constraint(J, B, (nc, model.nv), "J")
+    out = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    imp = _torch().empty((B, nc), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_impulse_dynamics(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, nc, _ptr(qt), _ptr(vt), _ptr(Jt),
+            float(r_coeff), float(inv_damping), _ptr(out), _ptr(imp), _stream_ptr(),
+        )
+    )
+    data.dq_after, data.impulse_c = out, _ret(imp, was_np, vec)
+    return _ret(out, was_np, vec)
+
+
 def crba(model: Model, data: Data, q, convention: int = Convention.LOCAL, symmetric: bool = True):
     """M(q), symmetrised as the Python binding returns it (reference bindings/python/algorithm/expose-crba.cpp:22)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")

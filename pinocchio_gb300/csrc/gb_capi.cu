@@ -149,6 +149,47 @@ int gb_static_torque(const gb_model* M, int precision, int layout, long B, const
                                (cudaStream_t)stream);
 }
 
+// forwardDynamics / impulseDynamics with a constraint Jacobian: J is nc x nv
+// row-major per configuration (nc * nv values in `layout`), gamma / lambda nc values.
+static int contact_entry(const gb_model* M, int precision, int layout, long B, int nc, bool impulse,
+                         const double* q, const double* v, const double* tau, const double* J, const double* gamma,
+                         double r_coeff, double inv_damping, double* out, double* lam, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (nc < 0 || nc > 1024) return set_error(GB_ERR_SIZE, "the number of constraint rows must be in 0..1024");
+  if (!(inv_damping >= 0.0)) return set_error(GB_ERR_INVALID_ARGUMENT, "mu must be positive.");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, impulse ? "v_before" : "v"));
+  GB_TRY(gbi::check_ptr(out, impulse ? "dq_after" : "ddq"));
+  if (!impulse) GB_TRY(gbi::check_ptr(tau, "tau"));
+  if (nc > 0) {
+    GB_TRY(gbi::check_ptr(J, "J"));
+    GB_TRY(gbi::check_ptr(lam, impulse ? "impulse_c" : "lambda_c"));
+    if (!impulse) GB_TRY(gbi::check_ptr(gamma, "gamma"));
+  }
+  const gbi::Arr none{nullptr, 0, 0};
+  const long nv = M->nv;
+  return gbi::launch_contact(M, precision, impulse, B, nc, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, nv),
+                             gbi::arr(impulse ? v : tau, layout, B, nv),
+                             nc > 0 ? gbi::arr(J, layout, B, (long)nc * nv) : none,
+                             nc > 0 && !impulse ? gbi::arr(gamma, layout, B, nc) : none, r_coeff, inv_damping,
+                             gbi::arr(out, layout, B, nv), nc > 0 ? gbi::arr(lam, layout, B, nc) : none,
+                             (cudaStream_t)stream);
+}
+
+int gb_forward_dynamics(const gb_model* M, int precision, int layout, long B, int nc, const double* q, const double* v,
+                        const double* tau, const double* J, const double* gamma, double inv_damping, double* ddq,
+                        double* lambda_c, void* stream) {
+  return contact_entry(M, precision, layout, B, nc, false, q, v, tau, J, gamma, 0.0, inv_damping, ddq, lambda_c,
+                       stream);
+}
+
+int gb_impulse_dynamics(const gb_model* M, int precision, int layout, long B, int nc, const double* q,
+                        const double* v_before, const double* J, double r_coeff, double inv_damping, double* dq_after,
+                        double* impulse_c, void* stream) {
+  return contact_entry(M, precision, layout, B, nc, true, q, v_before, nullptr, J, nullptr, r_coeff, inv_damping,
+                       dq_after, impulse_c, stream);
+}
+
 int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                           const double* a, double* oMi, double* vout, double* aout, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));

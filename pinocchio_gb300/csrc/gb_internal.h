@@ -50,6 +50,9 @@ int launch_aba_warp(const gb_model* M, int precision, long B, Arr q, Arr v, Arr 
 int launch_rnea_branch(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
 int launch_aba_branch(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr ddq, cudaStream_t st);
 int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q, Arr M, Arr U, Arr D, cudaStream_t st);
+// forwardDynamics / impulseDynamics with a given constraint Jacobian (gb_contact.cu)
+int launch_contact(const gb_model* m, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
+                   Arr gamma, double r_coeff, double inv_damping, Arr out, Arr lam, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);

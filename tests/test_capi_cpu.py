@@ -48,6 +48,9 @@ def test_invalid_arguments_are_rejected_on_the_host(L):
     assert b"fext" in L.gb_last_error()
     assert L.gb_aba_derivatives_fext(None, 0, 0, 1, *([None] * 9)) == _capi.GB_ERR_INVALID_ARGUMENT
     assert b"fext" in L.gb_last_error()
+    assert L.gb_forward_dynamics(None, 0, 0, 1, 2, *([None] * 5), 0.0, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_impulse_dynamics(None, 0, 0, 1, 2, None, None, None, 0.0, 0.0, None, None, None) == \
+        _capi.GB_ERR_INVALID_ARGUMENT
 
 
 def _create(L, model_tables):
