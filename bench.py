@@ -219,7 +219,8 @@ def measure_functions(torch, pg, sm):
     CRBA (+ tree Cholesky) / computeMinverse / nonLinearEffects / generalized gravity /
     forwardKinematics (q, v, a) / computeJointJacobians at batch 65536, the two derivative
     algorithms at batch 16384; RNEA, ABA and the ABA derivatives with external forces on
-    every joint (the fext overloads) at the same batches."""
+    every joint (the fext overloads) at the same batches; forwardDynamics with 12 constraint
+    rows (two 6-D contacts) at batch 65536."""
     model = sm.humanoid32(1)
     out = {}
     for prec in ("fp64", "mixed"):
@@ -229,9 +230,11 @@ def measure_functions(torch, pg, sm):
                          ("rnea_derivatives", 16384), ("aba_derivatives", 16384), ("compute_minverse", 65536),
                          ("nonlinear_effects", 65536), ("generalized_gravity", 65536),
                          ("forward_kinematics", 65536), ("joint_jacobians", 65536), ("rnea_fext", 65536),
-                         ("aba_fext", 65536), ("aba_derivatives_fext", 16384)):
+                         ("aba_fext", 65536), ("aba_derivatives_fext", 16384), ("forward_dynamics_12rows", 65536)):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
             f = torch.randn((B, model.njoints, 6), dtype=torch.float64, device="cuda")
+            Jc = torch.randn((B, 12, model.nv), dtype=torch.float64, device="cuda") if fname.startswith("forward_dyn") else None
+            gc = torch.randn((B, 12), dtype=torch.float64, device="cuda") if Jc is not None else None
             fn = {
                 "rnea": lambda: pg.rnea(model, data, q, v, x),
                 "aba": lambda: pg.aba(model, data, q, v, 10.0 * x),
@@ -247,10 +250,11 @@ def measure_functions(torch, pg, sm):
                 "rnea_fext": lambda: pg.rnea(model, data, q, v, x, f),
                 "aba_fext": lambda: pg.aba(model, data, q, v, 10.0 * x, f),
                 "aba_derivatives_fext": lambda: pg.computeABADerivatives(model, data, q, v, 10.0 * x, f),
+                "forward_dynamics_12rows": lambda: pg.forwardDynamics(model, data, q, v, 10.0 * x, Jc, gc),
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}
-            del q, v, x, f
+            del q, v, x, f, Jc, gc
         out[prec] = res
     return out
 

@@ -183,6 +183,21 @@ inline void computeABADerivatives(const Model& m, int precision, long batch, con
   check(gb_aba_derivatives_fext(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, v, tau, fext.data, ddq_dq, ddq_dv,
                                 Minv, nullptr, stream));
 }
+
+// ---- contact dynamics with a constraint Jacobian J (nc x nv row-major per configuration, device
+// memory): forwardDynamics (contact-dynamics.hxx:81-165) and impulseDynamics (255-327)
+inline void forwardDynamics(const Model& m, int precision, long batch, const double* q, const double* v,
+                            const double* tau, int nc, const double* J, const double* gamma, double* ddq,
+                            double* lambda_c, double inv_damping = 0.0, void* stream = nullptr) {
+  check(gb_forward_dynamics(m.get(), precision, GB_LAYOUT_INSTANCE, batch, nc, q, v, tau, J, gamma, inv_damping, ddq,
+                            lambda_c, stream));
+}
+inline void impulseDynamics(const Model& m, int precision, long batch, const double* q, const double* v_before, int nc,
+                            const double* J, double* dq_after, double* impulse_c, double r_coeff = 0.0,
+                            double inv_damping = 0.0, void* stream = nullptr) {
+  check(gb_impulse_dynamics(m.get(), precision, GB_LAYOUT_INSTANCE, batch, nc, q, v_before, J, r_coeff, inv_damping,
+                            dq_after, impulse_c, stream));
+}
 inline void computeMinverse(const Model& m, int precision, long batch, const double* q, double* Minv,
                             void* stream = nullptr) {
   check(gb_compute_minverse(m.get(), precision, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, batch, q, Minv, stream));
