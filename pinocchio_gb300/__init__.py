@@ -22,6 +22,7 @@ from .model import (  # noqa: F401
 )
 from . import sample_models  # noqa: F401
 from .urdf import buildModelFromUrdf, buildModelFromXML, load_model, save_model  # noqa: F401
+from .mjcf import buildModelFromMJCF, buildModelFromMJCFXML  # noqa: F401
 from .api import (  # noqa: F401
     Data,
     ModelPool,

@@ -1,0 +1,142 @@
+"""The MJCF loader (a subset of the reference's src/parsers/mjcf/mjcf-graph.cpp) on the CPU:
+documents against the same trees built with the construction API (tables equal, and the
+oracle's dynamics equal), the orientation forms (quat / axisangle / euler, degrees and
+radians), welded bodies, joint positions inside a body, armature, and the features outside
+the subset raising ValueError."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleModel
+from pinocchio_gb300 import model as gm
+from pinocchio_gb300 import sample_models as sm
+from pinocchio_gb300.mjcf import buildModelFromMJCF, buildModelFromMJCFXML
+from util import rel_err
+
+DOC = """<mujoco model="walker">
+  <compiler angle="radian"/>
+  <worldbody>
+    <body name="base" pos="0 0 1">
+      <freejoint name="root"/>
+      <inertial pos="0.01 0 0.02" mass="5" diaginertia="0.1 0.2 0.3"/>
+      <body name="torso" pos="0 0 0.3" quat="0.9238795325112867 0 0.3826834323650898 0">
+        <joint name="waist" type="hinge" axis="0 0 1" armature="0.05"/>
+        <inertial pos="0 0 0.1" quat="1 0 0 0" mass="2" diaginertia="0.02 0.03 0.04"/>
+        <body name="head" pos="0 0 0.25">
+          <inertial pos="0 0 0.05" mass="0.8" fullinertia="0.01 0.012 0.009 0.001 0 0.0005"/>
+        </body>
+        <body name="arm" pos="0.2 0 0.1" axisangle="1 0 0 0.3">
+          <joint name="shoulder" type="hinge" axis="0 1 1" pos="0 0 0.05"/>
+          <inertial pos="0 0 -0.1" mass="1" diaginertia="0.01 0.01 0.002"/>
+          <body name="forearm" pos="0 0 -0.25" euler="0.1 0.2 0.3">
+            <joint name="elbow" type="hinge" axis="1 0 0"/>
+            <inertial pos="0 0 -0.1" mass="0.6" diaginertia="0.005 0.005 0.001"/>
+          </body>
+        </body>
+      </body>
+      <body name="leg" pos="0 -0.1 -0.1">
+        <joint name="hip" type="slide" axis="0 0 -1"/>
+        <inertial pos="0 0 -0.2" mass="1.5" diaginertia="0.02 0.02 0.003"/>
+        <body name="shin" pos="0 0 -0.4">
+          <joint name="knee" type="hinge" axis="0 1 0"/>
+          <inertial pos="0 0 -0.2" mass="1" diaginertia="0.01 0.01 0.002"/>
+        </body>
+      </body>
+    </body>
+  </worldbody>
+</mujoco>"""
+
+
+def _rot(axis, angle):
+    a = np.asarray(axis, dtype=float) / np.linalg.norm(axis)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * K @ K
+
+
+def _Y(mass, pos, I, R=np.eye(3)):
+    return gm.Inertia(mass, np.zeros(3), R @ I @ R.T).se3_action(gm.SE3(np.eye(3), pos))
+
+
+def reference_walker():
+    """The same tree through the construction API (addJoint / appendBodyToJoint)."""
+    m = gm.Model()
+    base = m.addJoint(0, gm.JointModelFreeFlyer(), gm.SE3(np.eye(3), [0, 0, 1]), "root")
+    m.appendBodyToJoint(base, _Y(5, [0.01, 0, 0.02], np.diag([0.1, 0.2, 0.3])))
+    Rt = _rot([0, 1, 0], np.pi / 4)
+    waist = m.addJoint(base, gm.JointModelRZ(), gm.SE3(Rt, [0, 0, 0.3]), "waist")
+    m.armature[m.idx_vs[waist]] = 0.05
+    m.appendBodyToJoint(waist, _Y(2, [0, 0, 0.1], np.diag([0.02, 0.03, 0.04])))
+    Ih = np.array([[0.01, 0.001, 0], [0.001, 0.012, 0.0005], [0, 0.0005, 0.009]])
+    m.appendBodyToJoint(waist, _Y(0.8, [0, 0, 0.05], Ih), gm.SE3(np.eye(3), [0, 0, 0.25]))
+    Ra = _rot([1, 0, 0], 0.3)
+    sh = m.addJoint(waist, gm.JointModelRevoluteUnaligned(np.array([0, 1, 1]) / np.sqrt(2)),
+                    gm.SE3(Ra, [0.2, 0, 0.1] + Ra @ [0, 0, 0.05]), "shoulder")
+    m.appendBodyToJoint(sh, _Y(1, [0, 0, -0.1], np.diag([0.01, 0.01, 0.002])), gm.SE3(np.eye(3), [0, 0, -0.05]))
+    Re = _rot([1, 0, 0], 0.1) @ _rot([0, 1, 0], 0.2) @ _rot([0, 0, 1], 0.3)
+    el = m.addJoint(sh, gm.JointModelRX(), gm.SE3(Re, [0, 0, -0.3]), "elbow")
+    m.appendBodyToJoint(el, _Y(0.6, [0, 0, -0.1], np.diag([0.005, 0.005, 0.001])))
+    hip = m.addJoint(base, gm.JointModelPrismaticUnaligned(np.array([0, 0, -1.0])), gm.SE3(np.eye(3), [0, -0.1, -0.1]), "hip")
+    m.appendBodyToJoint(hip, _Y(1.5, [0, 0, -0.2], np.diag([0.02, 0.02, 0.003])))
+    kn = m.addJoint(hip, gm.JointModelRY(), gm.SE3(np.eye(3), [0, 0, -0.4]), "knee")
+    m.appendBodyToJoint(kn, _Y(1, [0, 0, -0.2], np.diag([0.01, 0.01, 0.002])))
+    return m
+
+
+def _same(a, b, tol=1e-12):
+    ta, tb = a.tables(), b.tables()
+    assert ta.keys() == tb.keys()
+    for k in ta:
+        assert np.allclose(ta[k], tb[k], rtol=0, atol=tol), k
+
+
+def test_walker_matches_construction_api(tmp_path):
+    m = buildModelFromMJCFXML(DOC)
+    ref = reference_walker()
+    assert m.names[1:] == ["root", "waist", "shoulder", "elbow", "hip", "knee"]
+    _same(m, ref)
+    p = tmp_path / "walker.xml"
+    p.write_text(DOC)
+    _same(buildModelFromMJCF(str(p)), ref)
+    om, oref = OracleModel(m), OracleModel(ref)
+    q, v, a = sm.random_inputs(m, 8, 3)
+    assert rel_err(om.rnea(q, v, a), oref.rnea(q, v, a)) < 1e-13
+
+
+def test_orientation_forms_and_units():
+    def doc(compiler, attr):
+        return f"""<mujoco>{compiler}<worldbody>
+          <body name="a" {attr}><joint type="hinge" axis="1 0 0"/>
+            <inertial pos="0.1 0 0" mass="1" diaginertia="0.1 0.2 0.3"/></body>
+        </worldbody></mujoco>"""
+    c = np.cos(np.pi / 6 / 2)
+    s = np.sin(np.pi / 6 / 2)
+    forms = [doc("", f'quat="{c} 0 0 {s}"'), doc("", 'axisangle="0 0 1 30"'), doc("", 'euler="0 0 30"'),
+             doc('<compiler angle="radian"/>', f'axisangle="0 0 1 {np.pi / 6}"'),
+             doc('<compiler eulerseq="zyx"/>', 'euler="30 0 0"')]
+    models = [buildModelFromMJCFXML(x) for x in forms]
+    for m in models[1:]:
+        _same(m, models[0])
+    R = models[0].tables()["placement"][1, :9].reshape(3, 3)
+    assert np.allclose(R, _rot([0, 0, 1], np.pi / 6), atol=1e-12)
+
+
+@pytest.mark.parametrize("snippet, msg", [
+    ('<default><joint damping="1"/></default><worldbody/>', "default"),
+    ('<worldbody><body name="a"><joint type="ball"/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "ball"),
+    ('<worldbody><body name="a"><joint/><joint type="slide"/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "several"),
+    ('<worldbody><body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody>', "geom"),
+    ('<worldbody><body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/>'
+     '<body name="b"><freejoint/><inertial mass="1" diaginertia="1 1 1"/></body></body></worldbody>', "free"),
+    ('<worldbody><body name="a" zaxis="0 1 0"><joint/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "zaxis"),
+    ('<worldbody><body name="a" childclass="x"><joint/></body></worldbody>', "class"),
+])
+def test_outside_the_subset_raises(snippet, msg):
+    with pytest.raises(ValueError, match=msg):
+        buildModelFromMJCFXML(f"<mujoco>{snippet}</mujoco>")
+    with pytest.raises(ValueError, match="mujoco"):
+        buildModelFromMJCFXML("<robot/>")
+
+
+def test_geoms_ignored_when_inertia_not_from_geoms():
+    m = buildModelFromMJCFXML("""<mujoco><compiler inertiafromgeom="false"/><worldbody>
+      <body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody></mujoco>""")
+    assert m.nv == 1 and m.inertias[1].mass == 0.0
