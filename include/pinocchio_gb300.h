@@ -252,6 +252,13 @@ int gb_impulse_dynamics(const gb_model* model, int precision, int layout, long b
                         const double* v_before, const double* J, double r_coeff, double inv_damping,
                         double* dq_after, double* impulse_c, void* stream);
 
+/* computeKKTContactDynamicMatrixInverse(model, data, q, J, KKTMatrix_inv, inv_damping)
+ * (reference algorithm/contact-dynamics.hxx:166-225, contact-dynamics.hpp:150-163):
+ * K = [[M, J^T], [J, -inv_damping I]]^-1, (nv + nc) x (nv + nc) row-major per instance,
+ * FP64 in both precisions. */
+int gb_kkt_contact_inverse(const gb_model* model, int precision, int layout, long batch, int nc, const double* q,
+                           const double* J, double inv_damping, double* K, void* stream);
+
 /* forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272):
  * per instance, for every joint i = 0 .. njoints-1 (joint 0 the universe:
  * identity, zero), oMi[12 i ..] = the world placement (rotation row-major, then

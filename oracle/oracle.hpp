@@ -1432,6 +1432,56 @@ void contact_common(const Model& m, Data<T>& d, const T* q, int nc, const T* J, 
       G[(size_t)i * nc + j] = s + (i == j ? inv_damping : T(0));
     }
 }
+// computeKKTContactDynamicMatrixInverse(q, J, inv_damping) (contact-dynamics.hxx:166-225):
+// the inverse of [[M, J^T], [J, -inv_damping I]], n = nv + nc, row-major in `K`, from the
+// factorisations: bottomRight = -(J M^-1 J^T + mu I)^-1, topLeft = M^-1, bottomLeft = J M^-1,
+// topRight = bottomLeft^T (-bottomRight), topLeft -= topRight bottomLeft, bottomLeft = topRight^T.
+template <class T>
+void kkt_inverse_contact(const Model& m, Data<T>& d, const T* q, int nc, const T* J, T inv_damping, T* K) {
+  const int nv = m.nv, n = nv + nc;
+  std::vector<T> G;
+  contact_common(m, d, q, nc, J, inv_damping, G);
+  auto at = [&](int r, int c) -> T& { return K[(size_t)r * n + c]; };
+  std::vector<T> col(nv);
+  for (int c = 0; c < nv; ++c) {  // topLeft = M^-1
+    for (int k = 0; k < nv; ++k) col[k] = T(k == c);
+    chol_solve(m, d, col.data());
+    for (int k = 0; k < nv; ++k) at(k, c) = col[k];
+  }
+  std::vector<T> BR((size_t)nc * nc), BL((size_t)nc * nv), TR((size_t)nv * nc);
+  for (int j = 0; j < nc; ++j) {  // bottomRight = -G^-1, column by column
+    std::vector<T> Gc(G), e(nc, T(0));
+    e[j] = T(-1);
+    llt_factor_solve(nc, Gc.data(), e.data());
+    for (int i = 0; i < nc; ++i) BR[(size_t)i * nc + j] = e[i];
+  }
+  for (int i = 0; i < nc; ++i)  // bottomLeft = J topLeft
+    for (int c = 0; c < nv; ++c) {
+      T s = T(0);
+      for (int k = 0; k < nv; ++k) s += J[(size_t)i * nv + k] * at(k, c);
+      BL[(size_t)i * nv + c] = s;
+    }
+  for (int r = 0; r < nv; ++r)  // topRight = bottomLeft^T (-bottomRight)
+    for (int j = 0; j < nc; ++j) {
+      T s = T(0);
+      for (int i = 0; i < nc; ++i) s += BL[(size_t)i * nv + r] * -BR[(size_t)i * nc + j];
+      TR[(size_t)r * nc + j] = s;
+    }
+  for (int r = 0; r < nv; ++r)  // topLeft -= topRight bottomLeft
+    for (int c = 0; c < nv; ++c) {
+      T s = T(0);
+      for (int j = 0; j < nc; ++j) s += TR[(size_t)r * nc + j] * BL[(size_t)j * nv + c];
+      at(r, c) -= s;
+    }
+  for (int r = 0; r < nv; ++r)
+    for (int j = 0; j < nc; ++j) {
+      at(r, nv + j) = TR[(size_t)r * nc + j];
+      at(nv + j, r) = TR[(size_t)r * nc + j];
+    }
+  for (int i = 0; i < nc; ++i)
+    for (int j = 0; j < nc; ++j) at(nv + i, nv + j) = BR[(size_t)i * nc + j];
+}
+
 template <class T>
 void forward_dynamics_contact(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau, int nc, const T* J,
                               const T* gamma, T inv_damping, T* out, T* lam) {

@@ -57,6 +57,7 @@ def lib():
         L.orc_rnea_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_aba_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_forward_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, vp, C.c_double, vp, vp, C.c_int]
+        L.orc_kkt_inverse.argtypes = [vp, C.c_long, C.c_int, vp, vp, C.c_double, vp]
         L.orc_impulse_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
@@ -180,6 +181,14 @@ class OracleModel:
         self._check(lib().orc_forward_dynamics(self.h, prec, B, nc, _ptr(q), _ptr(v), _ptr(tau), _ptr(J), _ptr(gamma),
                                                float(inv_damping), _ptr(ddq), _ptr(lam), nthreads))
         return ddq, lam
+
+    def kkt_inverse(self, q, J, inv_damping=0.0):
+        """computeKKTContactDynamicMatrixInverse: (B, nv + nc, nv + nc), FP64."""
+        q, J = _c(q), _c(J)
+        B, nc = q.shape[0], J.shape[1]
+        K = np.empty((B, self.nv + nc, self.nv + nc))
+        self._check(lib().orc_kkt_inverse(self.h, B, nc, _ptr(q), _ptr(J), float(inv_damping), _ptr(K)))
+        return K
 
     def impulse_dynamics(self, q, v_before, J, r_coeff=0.0, inv_damping=0.0, prec=0, nthreads=0):
         """(dq_after, impulse_c) of impulseDynamics with the constraint Jacobian J (B, nc, nv)."""

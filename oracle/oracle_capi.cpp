@@ -330,6 +330,16 @@ int orc_forward_dynamics(void* h, int prec, long B, int nc, const double* q, con
   return prec == 1 ? contact_batch<long double>(m, false, B, nc, q, v, tau, J, gamma, 0.0, inv_damping, ddq, lambda_c, nt)
                    : contact_batch<double>(m, false, B, nc, q, v, tau, J, gamma, 0.0, inv_damping, ddq, lambda_c, nt);
 }
+// computeKKTContactDynamicMatrixInverse (contact-dynamics.hxx:166-225), double only:
+// K holds (nv + nc)^2 values per instance, row-major.
+int orc_kkt_inverse(void* h, long B, int nc, const double* q, const double* J, double inv_damping, double* K) {
+  const Model& m = *static_cast<Model*>(h);
+  orc::Data<double> d(m);
+  const size_t n = (size_t)m.nv + nc;
+  for (long b = 0; b < B; ++b)
+    orc::kkt_inverse_contact(m, d, q + (size_t)b * m.nq, nc, J + (size_t)b * nc * m.nv, inv_damping, K + (size_t)b * n * n);
+  return 0;
+}
 int orc_impulse_dynamics(void* h, int prec, long B, int nc, const double* q, const double* v_before, const double* J,
                          double r_coeff, double inv_damping, double* dq_after, double* impulse_c, int nt) {
   const Model& m = *static_cast<Model*>(h);

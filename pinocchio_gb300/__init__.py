@@ -32,6 +32,7 @@ from .api import (  # noqa: F401
     computeABADerivatives,
     computeGeneralizedGravity,
     computeJointJacobians,
+    computeKKTContactDynamicMatrixInverse,
     computeMinverse,
     computeRNEADerivatives,
     computeStaticTorque,

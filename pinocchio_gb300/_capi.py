@@ -48,6 +48,7 @@ EXPORTS = (
     "gb_aba_derivatives_noalloc",
     "gb_forward_dynamics",
     "gb_impulse_dynamics",
+    "gb_kkt_contact_inverse",
     "gb_forward_kinematics",
     "gb_compute_joint_jacobians",
     "gb_integrate",
@@ -153,6 +154,7 @@ def lib():
         L.gb_integrate.argtypes = [vp, i, l, vp, vp, vp, vp]
         L.gb_forward_dynamics.argtypes = [vp, i, i, l, i, vp, vp, vp, vp, vp, C.c_double, vp, vp, vp]
         L.gb_impulse_dynamics.argtypes = [vp, i, i, l, i, vp, vp, vp, C.c_double, C.c_double, vp, vp, vp]
+        L.gb_kkt_contact_inverse.argtypes = [vp, i, i, l, i, vp, vp, C.c_double, vp, vp]
         L.gb_forward_kinematics.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.gb_compute_joint_jacobians.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]

@@ -360,6 +360,24 @@ def impulseDynamics(model: Model, data: Data, q, v_before, J, r_coeff: float = 0
     return _ret(out, was_np, vec)
 
 
+def computeKKTContactDynamicMatrixInverse(model: Model, data: Data, q, J, inv_damping: float = 0.0):
+    """[[M, J^T], [J, -inv_damping I]]^-1, shape (batch, nv + nc, nv + nc) (reference
+    algorithm/contact-dynamics.hxx:166-225), FP64."""
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    B = qt.shape[0]
+    nc = int(_torch().as_tensor(J).shape[-2])
+    Jt = _constraint(J, B, (nc, model.nv), "J")
+    n = model.nv + nc
+    K = _torch().empty((B, n, n), dtype=qt.dtype, device=qt.device)
+    _capi.check(
+        _capi.lib().gb_kkt_contact_inverse(
+            data.dev.h, _PREC[data.precision], _capi.GB_LAYOUT_INSTANCE, B, nc, _ptr(qt), _ptr(Jt), float(inv_damping),
+            _ptr(K), _stream_ptr(),
+        )
+    )
+    return _ret(K, was_np, vec)
+
+
 def crba(model: Model, data: Data, q, convention: int = Convention.LOCAL, symmetric: bool = True):
     """M(q), symmetrised as the Python binding returns it (reference bindings/python/algorithm/expose-crba.cpp:22)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")

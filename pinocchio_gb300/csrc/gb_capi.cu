@@ -190,6 +190,20 @@ int gb_impulse_dynamics(const gb_model* M, int precision, int layout, long B, in
                        dq_after, impulse_c, stream);
 }
 
+int gb_kkt_contact_inverse(const gb_model* M, int precision, int layout, long B, int nc, const double* q,
+                           const double* J, double inv_damping, double* K, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (nc < 0 || nc > 1024) return set_error(GB_ERR_SIZE, "the number of constraint rows must be in 0..1024");
+  if (!(inv_damping >= 0.0)) return set_error(GB_ERR_INVALID_ARGUMENT, "mu must be positive.");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(K, "KKTMatrix_inv"));
+  if (nc > 0) GB_TRY(gbi::check_ptr(J, "J"));
+  const long nv = M->nv, n = nv + nc;
+  return gbi::launch_kkt_inverse(M, B, nc, gbi::arr(q, layout, B, M->nq),
+                                 nc > 0 ? gbi::arr(J, layout, B, (long)nc * nv) : gbi::Arr{nullptr, 0, 0}, inv_damping,
+                                 gbi::arr(K, layout, B, n * n), (cudaStream_t)stream);
+}
+
 int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                           const double* a, double* oMi, double* vout, double* aout, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));

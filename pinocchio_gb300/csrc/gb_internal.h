@@ -53,6 +53,7 @@ int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q,
 // forwardDynamics / impulseDynamics with a given constraint Jacobian (gb_contact.cu)
 int launch_contact(const gb_model* m, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
                    Arr gamma, double r_coeff, double inv_damping, Arr out, Arr lam, cudaStream_t st);
+int launch_kkt_inverse(const gb_model* m, long B, int nc, Arr q, Arr J, double inv_damping, Arr K, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);

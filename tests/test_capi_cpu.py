@@ -51,6 +51,7 @@ def test_invalid_arguments_are_rejected_on_the_host(L):
     assert L.gb_forward_dynamics(None, 0, 0, 1, 2, *([None] * 5), 0.0, None, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
     assert L.gb_impulse_dynamics(None, 0, 0, 1, 2, None, None, None, 0.0, 0.0, None, None, None) == \
         _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_kkt_contact_inverse(None, 0, 0, 1, 2, None, None, 0.0, None, None) == _capi.GB_ERR_INVALID_ARGUMENT
 
 
 def _create(L, model_tables):

@@ -93,3 +93,15 @@ def test_impulse_dynamics_identities(case):
         assert rel_err(imp, np.linalg.solve(JMJ, (-(1 + r) * Jv)[..., None])[..., 0]) < 1e-10
         assert np.abs(np.einsum("bij,bj->bi", M, out - v) - np.einsum("bck,bc->bk", J, imp)).max() < 1e-10 * np.abs(v).max()
         assert np.abs(np.einsum("bck,bk->bc", J, out) + r * Jv).max() < 1e-10 * np.abs(v).max()
+
+
+@pytest.mark.parametrize("mu", [0.0, 1e-3])
+def test_kkt_inverse(case, mu):
+    """computeKKTContactDynamicMatrixInverse against the dense inverse of [[M, J^T], [J, -mu I]]
+    (unittest/contact-dynamics.cpp:94-134)"""
+    name, model, om, q, v, tau, J, gamma = case
+    K = om.kkt_inverse(q, J, mu)
+    M, _, _ = _dense(model, om, q, v)
+    nc = J.shape[1]
+    KKT = np.block([[M, J.transpose(0, 2, 1)], [J, np.broadcast_to(-mu * np.eye(nc), (len(q), nc, nc))]])
+    assert rel_err(K, np.linalg.inv(KKT)) < 1e-9

@@ -107,3 +107,13 @@ def test_contact_arguments_are_checked(case):
         _capi.GB_ERR_INVALID_ARGUMENT
     assert L.gb_impulse_dynamics(h, 0, 0, B, nc, p(qd), p(vd), p(Jd), 0.0, 0.0, p(out), None, None) == \
         _capi.GB_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("mu", [0.0, 1e-3])
+def test_kkt_inverse(case, mu):
+    """computeKKTContactDynamicMatrixInverse against the oracle's (contact-dynamics.hxx:166-225),
+    at 1e-10: its blocks carry (J M^-1 J^T)^-1, whose conditioning widens the FP64 bar further"""
+    name, model, om, q, v, tau, J, gamma, dev = case
+    data = pg.createData(model)
+    K = pg.computeKKTContactDynamicMatrixInverse(model, data, dev(q), dev(J), mu).cpu().numpy()
+    assert rel_err(K, om.kkt_inverse(q, J, mu)) < 1e-10
