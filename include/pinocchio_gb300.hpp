@@ -192,6 +192,11 @@ inline void forwardDynamics(const Model& m, int precision, long batch, const dou
   check(gb_forward_dynamics(m.get(), precision, GB_LAYOUT_INSTANCE, batch, nc, q, v, tau, J, gamma, inv_damping, ddq,
                             lambda_c, stream));
 }
+inline void computeKKTContactDynamicMatrixInverse(const Model& m, long batch, const double* q, int nc, const double* J,
+                                                  double* KKTMatrix_inv, double inv_damping = 0.0,
+                                                  void* stream = nullptr) {
+  check(gb_kkt_contact_inverse(m.get(), GB_FP64, GB_LAYOUT_INSTANCE, batch, nc, q, J, inv_damping, KKTMatrix_inv, stream));
+}
 inline void impulseDynamics(const Model& m, int precision, long batch, const double* q, const double* v_before, int nc,
                             const double* J, double* dq_after, double* impulse_c, double r_coeff = 0.0,
                             double inv_damping = 0.0, void* stream = nullptr) {

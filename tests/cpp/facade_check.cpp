@@ -35,6 +35,7 @@ struct Mat {
   pinocchio_gb300::computeABADerivatives(m, GB_MIXED, 1, q, x, x, fe, o1, o2, o3);
   pinocchio_gb300::forwardDynamics(m, GB_FP64, 1, q, x, x, 2, f, f, o1, o2);
   pinocchio_gb300::impulseDynamics(m, GB_FP64, 1, q, x, 2, f, o1, o2, 0.5);
+  pinocchio_gb300::computeKKTContactDynamicMatrixInverse(m, 1, q, 2, f, o1, 1e-6);
 }
 
 int main() {
