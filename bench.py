@@ -124,29 +124,100 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------
 # reference arm: the reference's CPU algorithm (the oracle port) on all host cores
 # ------------------------------------------------------------------------------------------
+def _omp_env():
+    """Thread binding of the OpenMP batch drivers (OMP_PROC_BIND=true, as the CPU baseline of
+    rneaInParallel / abaInParallel is specified); set before the oracle's OpenMP runtime loads."""
+    os.environ.setdefault("OMP_PROC_BIND", "true")
+    return {"OMP_PROC_BIND": os.environ.get("OMP_PROC_BIND"), "OMP_PLACES": os.environ.get("OMP_PLACES")}
+
+
+def _cpu_model_name():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
+
+
+def _cpu_step(om, q, v, tau, outs, nthreads):
+    """One CPU step of the headline workload: ABA (WORLD, as abaInParallel) + ABA derivatives."""
+    from oracle.oracle import WORLD
+
+    om.aba(q, v, tau, WORLD, nthreads=nthreads, out=outs[0])
+    om.aba_derivatives(q, v, tau, nthreads=nthreads, out=outs[1:])
+
+
+def _cpu_outs(B, nv):
+    outs = [np.empty((B, nv)), np.empty((B, nv)), np.empty((B, nv, nv)), np.empty((B, nv, nv)), np.empty((B, nv, nv))]
+    for o in outs:
+        o.fill(0.0)  # touch the pages once, outside any timed region
+    return outs
+
+
+def cpu_single_thread(om, model, sample=1024, reps=3):
+    """ABA + ABA derivatives on one thread, on a bounded sample (evals/s)."""
+    from pinocchio_gb300 import sample_models as sm
+
+    q, v, x = sm.random_inputs(model, sample, 3)
+    tau = 10.0 * x
+    outs = _cpu_outs(sample, model.nv)
+    _cpu_step(om, q[:64], v[:64], tau[:64], [o[:64] for o in outs], 1)
+    t = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _cpu_step(om, q, v, tau, outs, 1)
+        t.append(time.perf_counter() - t0)
+    return {"value": sample / float(np.median(t)), "unit": "evals/s", "cores": 1,
+            "sample": f"{sample} configurations x {reps} repetitions, ABA(WORLD) + ABA derivatives, FP64, 1 thread"}
+
+
+def cpu_rnea_c0(cores, B=4096):
+    """rneaInParallel on the 6R manipulator (batch 4096, FP64): all cores and one thread (evals/s)."""
+    from oracle.oracle import OracleModel
+    from pinocchio_gb300 import sample_models as sm
+
+    model = sm.manipulator6r(0)
+    om = OracleModel(model)
+    q, v, a = sm.random_inputs(model, B, 0)
+    out = np.zeros((B, model.nv))
+    res = {"workload": f"manipulator6r nv=6 RNEA, batch {B}, FP64"}
+    for name, nt, reps in (("all_cores", cores, 200), ("single_thread", 1, 20)):
+        om.rnea(q, v, a, nthreads=nt, out=out)
+        t = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            om.rnea(q, v, a, nthreads=nt, out=out)
+            t.append(time.perf_counter() - t0)
+        res[name] = {"value": B / float(np.median(t)), "unit": "evals/s", "cores": nt,
+                     "ms_per_call": 1e3 * float(np.median(t))}
+    return res
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    from oracle.oracle import WORLD, OracleModel
+    env = _omp_env()
+    from oracle.oracle import OracleModel
     from pinocchio_gb300 import sample_models as sm
 
     model = sm.humanoid32(1)
     om = OracleModel(model)
     cores = os.cpu_count() or 1
-    sample = min(args.batch, 4096)
-    q, v, x = sm.random_inputs(model, sample, 0)
+    B = args.batch
+    q, v, x = sm.random_inputs(model, B, 0)
     tau = 10.0 * x
+    outs = _cpu_outs(B, model.nv)
     for _ in range(max(1, args.warmup)):
-        om.aba(q[:256], v[:256], tau[:256], WORLD, nthreads=cores)
-        om.aba_derivatives(q[:256], v[:256], tau[:256], nthreads=cores)
+        _cpu_step(om, q, v, tau, outs, cores)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        om.aba(q, v, tau, WORLD, nthreads=cores)
-        om.aba_derivatives(q, v, tau, nthreads=cores)
+        _cpu_step(om, q, v, tau, outs, cores)
         times.append(time.perf_counter() - t0)
     t = float(np.median(times))
-    rate = sample / t
+    rate = B / t
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -155,15 +226,15 @@ def run_reference(args, world, rank):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 * t * args.batch / sample,
+        "ms_per_step": 1e3 * t,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded humanoid32 model and inputs)",
         "config": {
-            "workload": f"humanoid32 nv=32 ABA(WORLD)+computeABADerivatives, batch {args.batch}",
-            "batch": args.batch,
+            "workload": f"humanoid32 nv=32 ABA(WORLD)+computeABADerivatives, batch {B}",
+            "batch": B,
             "parallelism": "openmp static over instances (rneaInParallel/abaInParallel structure)",
         },
         "cpu_baseline": {
@@ -171,8 +242,13 @@ def run_reference(args, world, rank):
             "unit": "evals/s",
             "cores": cores,
             "kind": "port",
-            "sample": f"{sample} configurations per step, ABA + ABA derivatives, FP64, {cores} OpenMP threads",
+            "sample": f"the whole batch of {B} configurations every step (median of {args.steps} steps), ABA(WORLD) + "
+                      f"ABA derivatives, FP64, {cores} OpenMP threads, outputs preallocated",
+            "cpu": _cpu_model_name(),
+            "omp": env,
+            "single_thread": cpu_single_thread(om, model),
         },
+        "rnea_in_parallel_c0": cpu_rnea_c0(cores),
         "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -320,6 +396,157 @@ def measure_rollout(torch, pg, sm, B=8192, T=64, n=100):
     return out
 
 
+def measure_e2e(torch, pg, model, host, B, args, dist, world):
+    """The headline step through the public API (``pg.aba`` + ``pg.computeABADerivatives``) with
+    the inputs in pinned host memory and every output copied back to pinned host memory, each
+    step.  Outputs are double-buffered: step k's device-to-host copies run on a copy stream
+    while step k + 1's kernels run on the compute stream (two output sets on the device and on
+    the host).  Beside it, the copy floor: the same bytes moved by plain pinned copies alone."""
+    nq, nv = model.nq, model.nv
+    h2d = B * (nq + 2 * nv) * 8
+    d2h = B * (nv + 3 * nv * nv) * 8
+    hq = [torch.from_numpy(q).pin_memory() for q, _, _ in host[:2]]
+    hv = [torch.from_numpy(v).pin_memory() for _, v, _ in host[:2]]
+    ht = [torch.from_numpy(10.0 * x).pin_memory() for _, _, x in host[:2]]
+    shapes = {"ddq": (B, nv), "ddq_dq": (B, nv, nv), "ddq_dv": (B, nv, nv), "Minv": (B, nv, nv)}
+    ho = [{k: torch.empty(sh, dtype=torch.float64).pin_memory() for k, sh in shapes.items()} for _ in range(2)]
+    d = pg.createData(model, "mixed")
+    from pinocchio_gb300 import autotune
+
+    autotune.tune(model, d, functions=("aba", "aba_derivatives"), batch=B, use_cache=False)
+    comp = torch.cuda.current_stream()
+    copy = torch.cuda.Stream()
+    din = [tuple(torch.empty(t.shape, dtype=torch.float64, device="cuda") for t in (hq[0], hv[0], ht[0]))
+           for _ in range(2)]
+    done = [torch.cuda.Event() for _ in range(2)]  # the step's kernels finished (outputs ready)
+    freed = [torch.cuda.Event() for _ in range(2)]  # the step's outputs are on the host
+    keep = [None, None]
+
+    def e2e_step(k):
+        s = k % 2
+        q, v, t = din[s]
+        comp.wait_event(freed[s])  # the inputs / outputs of step k - 2 are no longer in use
+        q.copy_(hq[s], non_blocking=True)
+        v.copy_(hv[s], non_blocking=True)
+        t.copy_(ht[s], non_blocking=True)
+        ddq = pg.aba(model, d, q, v, t)
+        dq, dv, Mi = pg.computeABADerivatives(model, d, q, v, t)
+        done[s].record(comp)
+        with torch.cuda.stream(copy):
+            copy.wait_event(done[s])
+            for name, src in (("ddq", ddq), ("ddq_dq", dq), ("ddq_dv", dv), ("Minv", Mi)):
+                src.record_stream(copy)
+                ho[s][name].copy_(src, non_blocking=True)
+            freed[s].record(copy)
+        keep[s] = (ddq, dq, dv, Mi)
+
+    for k in range(args.warmup):
+        e2e_step(k)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_step(k)
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    # a host read of the result of the last step (what a caller consumes)
+    checksum = float(ho[(args.steps - 1) % 2]["ddq"][0, 0])
+    # copy floor: the step's bytes moved by pinned copies alone (one stream, CUDA events)
+    src = [keep[0][1], keep[0][2], keep[0][3], keep[0][0]]
+    dst = [ho[0]["ddq_dq"], ho[0]["ddq_dv"], ho[0]["Minv"], ho[0]["ddq"]]
+
+    def copies():
+        for a, b in zip(dst, src):
+            a.copy_(b, non_blocking=True)
+        for a, b in zip(din[0], (hq[0], hv[0], ht[0])):
+            a.copy_(b, non_blocking=True)
+
+    ms_copy = _time_call(torch, copies, reps=5, warmup=1)
+    del keep
+    floor = world * B / (ms_copy * 1e-3)
+    return {"value": world * B / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": 1e3 * t_e2e,
+            "copy_floor": {"value": floor, "unit": "evals/s", "ms_per_step": ms_copy,
+                           "d2h_gbs": d2h / (ms_copy * 1e-3) / 1e9,
+                           "note": "the same H2D + D2H bytes as pinned copies alone on one stream (no kernels)"},
+            "fraction_of_copy_floor": (world * B / t_e2e) / floor,
+            "overlap": "outputs double-buffered: step k's D2H copies on a copy stream overlap step k+1's kernels",
+            "host_checksum": checksum}
+
+
+def dtau_structural_nonzeros(model):
+    """Entries of dtau_dq that can be non-zero: row k of column c with k's joint an ancestor of (or)
+    c's joint or in its subtree -- the rows the -Minv * dtau product kernels loop over."""
+    par = model.parents
+    jv = [j for j, n in enumerate(model.nvs) for _ in range(n)]
+
+    def anc(j):
+        out = set()
+        while j > 0:
+            out.add(j)
+            j = par[j]
+        return out
+
+    A = [anc(j) for j in range(model.njoints)]
+    return sum(1 for c in jv for k in jv if k in A[c] or c in A[k])
+
+
+def measure_soa(torch, L, _capi, data, dev, B, nq, nv, PREC, sp, P, reps=10):
+    """The headline step with GB_LAYOUT_SOA inputs and outputs (element k of every configuration
+    contiguous), both precisions, CUDA events: ms per step."""
+    q, v, tau = (t.t().contiguous() for t in dev[0])  # (n, B): SOA
+    o = {"ddq": torch.empty((nv, B), dtype=torch.float64, device="cuda"),
+         "dq": torch.empty((nv * nv, B), dtype=torch.float64, device="cuda"),
+         "dv": torch.empty((nv * nv, B), dtype=torch.float64, device="cuda"),
+         "Mi": torch.empty((nv * nv, B), dtype=torch.float64, device="cuda"),
+         "ddq2": torch.empty((nv, B), dtype=torch.float64, device="cuda")}
+    res = {}
+    for prec in ("mixed", "fp64"):
+        h = data[prec].dev.h
+
+        def fn():
+            _capi.check(L.gb_aba(h, PREC[prec], _capi.GB_LOCAL, _capi.GB_LAYOUT_SOA, B, P(q), P(v), P(tau),
+                                 P(o["ddq"]), sp))
+            _capi.check(L.gb_aba_derivatives(h, PREC[prec], _capi.GB_LAYOUT_SOA, B, P(q), P(v), P(tau), P(o["dq"]),
+                                             P(o["dv"]), P(o["Mi"]), P(o["ddq2"]), sp))
+
+        ms = _time_call(torch, fn, reps=reps, warmup=2)
+        res[prec] = {"ms_per_step": ms, "evals_per_s": B / ms * 1e3}
+    res["note"] = "same step with SOA inputs/outputs (coalesced loads of q, v, tau); the headline uses the reference's layout"
+    return res
+
+
+def measure_c0(torch, pg, sm, B=4096):
+    """rneaInParallel's workload (6R manipulator, batch 4096): the batched RNEA kernel on device-resident
+    inputs (CUDA events) per precision, and rneaInParallel itself through the host-array entry point
+    (wall clock, copies and synchronisation included)."""
+    model = sm.manipulator6r(0)
+    q, v, a = sm.random_inputs(model, B, 0)
+    qd, vd, ad = (torch.from_numpy(x).cuda() for x in (q, v, a))
+    out = {"workload": f"manipulator6r nv=6 RNEA, batch {B}"}
+    for prec in ("fp64", "mixed"):
+        data = pg.createData(model, prec)
+        ms = _time_call(torch, lambda: pg.rnea(model, data, qd, vd, ad), reps=50, warmup=5)
+        out[prec] = {"ms": ms, "evals_per_s": B / ms * 1e3}
+    pool = pg.ModelPool(model, 4)
+    qc, vc, ac = (np.asfortranarray(x.T) for x in (q, v, a))
+    tau = np.empty((model.nv, B), order="F")
+    for _ in range(5):
+        pg.rneaInParallel(4, pool, qc, vc, ac, tau)
+    t = []
+    for _ in range(50):
+        t0 = time.perf_counter()
+        pg.rneaInParallel(4, pool, qc, vc, ac, tau)
+        t.append(time.perf_counter() - t0)
+    out["rneaInParallel_host_arrays_fp64"] = {"ms": 1e3 * float(np.median(t)), "evals_per_s": B / float(np.median(t))}
+    return out
+
+
 def run_ours(args, world, rank, local, dist):
     import torch
 
@@ -422,6 +649,7 @@ def run_ours(args, world, rank, local, dist):
     clocks = sampler.summary()
     kt_mixed = kernel_times("mixed")
     kt_fp64 = kernel_times("fp64")
+    soa_ms = measure_soa(torch, L, _capi, data, dev, B, nq, nv, PREC, sp, P)
 
     # accuracy of the mixed and FP64 outputs against the FP64 oracle on a sample (rank 0)
     acc = {}
@@ -429,59 +657,33 @@ def run_ours(args, world, rank, local, dist):
         from oracle.oracle import OracleModel
 
         om = OracleModel(model)
-        ns = 512
+        # a sample strided over the whole batch (first and last configuration included), so that every
+        # part of the grid and of the persistent product pipeline is checked
+        idx = np.unique(np.linspace(0, B - 1, min(B, 2048)).astype(np.int64))
+        ns = len(idx)
         q, v, x = host[0]
-        ref = om.aba_derivatives(q[:ns], v[:ns], 10.0 * x[:ns])
+        ref = om.aba_derivatives(q[idx], v[idx], 10.0 * x[idx])
+        ref_aba = om.aba(q[idx], v[idx], 10.0 * x[idx])
+        tidx = torch.from_numpy(idx).cuda()
         for prec in ("mixed", "fp64"):
             step(prec, 0)
             torch.cuda.synchronize()
-            got = [outs["ddq2"][:ns], outs["ddq_dq"][:ns], outs["ddq_dv"][:ns], outs["Minv"][:ns]]
+            got = [outs["ddq2"][tidx], outs["ddq_dq"][tidx], outs["ddq_dv"][tidx], outs["Minv"][tidx], outs["ddq"][tidx]]
+            ref_all = list(ref) + [ref_aba]
             errs = []
-            for g, r in zip(got, ref):
+            for g, r in zip(got, ref_all):
                 g = g.cpu().numpy().reshape(ns, -1)
                 r = r.reshape(ns, -1)
                 e = np.linalg.norm(g - r, axis=1) / np.linalg.norm(r, axis=1)
                 errs.append((float(e.max()), float(np.median(e))))
-            acc[prec] = {k: {"max": m, "median": md} for k, (m, md) in zip(("ddq", "ddq_dq", "ddq_dv", "Minv"), errs)}
+            acc[prec] = {k: {"max": m, "median": md} for k, (m, md) in
+                         zip(("ddq", "ddq_dq", "ddq_dv", "Minv", "aba_ddq"), errs)}
+            acc[prec]["sample"] = f"{ns} configurations strided over the batch of {B} (first and last included)"
 
     # end to end through the public API: pinned host inputs -> device -> kernels -> pinned host outputs
     e2e = None
     if not args.no_e2e:
-        hq = [torch.from_numpy(q).pin_memory() for q, _, _ in host[:2]]
-        hv = [torch.from_numpy(v).pin_memory() for _, v, _ in host[:2]]
-        ht = [torch.from_numpy(10.0 * x).pin_memory() for _, _, x in host[:2]]
-        ho = {k: torch.empty(t.shape, dtype=t.dtype).pin_memory() for k, t in outs.items() if k != "ddq2"}
-        dq_, dv_, dt_ = (torch.empty_like(dev[0][i]) for i in range(3))
-        d = data["mixed"]
-
-        def e2e_step(k):
-            dq_.copy_(hq[k % 2], non_blocking=True)
-            dv_.copy_(hv[k % 2], non_blocking=True)
-            dt_.copy_(ht[k % 2], non_blocking=True)
-            outs["ddq"] = pg.aba(model, d, dq_, dv_, dt_)
-            a, b, c = pg.computeABADerivatives(model, d, dq_, dv_, dt_)
-            ho["ddq"].copy_(outs["ddq"], non_blocking=True)
-            ho["ddq_dq"].copy_(a, non_blocking=True)
-            ho["ddq_dv"].copy_(b, non_blocking=True)
-            ho["Minv"].copy_(c, non_blocking=True)
-
-        for k in range(args.warmup):
-            e2e_step(k)
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            e2e_step(k)
-        torch.cuda.synchronize()
-        t_e2e = (time.perf_counter() - t0) / args.steps
-        if dist:
-            t = torch.tensor([t_e2e], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            t_e2e = float(t.item())
-        h2d = B * (nq + 2 * nv) * 8
-        d2h = B * (nv + 3 * nv * nv) * 8
-        e2e = {"value": world * B / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        e2e = measure_e2e(torch, pg, model, host, B, args, dist, world)
 
     if rank != 0:
         return
@@ -505,7 +707,13 @@ def run_ours(args, world, rank, local, dist):
         t = json.load(open(tpath)).get(f"{dom}_mixed")
         if t:
             traffic = t["dram_bytes"] * B / t["batch"]
-    flops = {"aba": 26417.0, "aba_derivatives": 214728.0}  # oracle FLOP counts per evaluation (humanoid32)
+    # FLOPs per evaluation (humanoid32): the oracle's FLOP-counting scalar over the reference's passes
+    # (+, -, *, / = 1 each), with the two dense -Minv * dtau products (4 nv^3) replaced by the products
+    # the kernels execute: only the rows of dtau that can be non-zero (4 nv nnz)
+    nnz = dtau_structural_nonzeros(model)
+    flops_oracle = {"aba": 26417.0, "aba_derivatives": 214728.0}
+    flops = {"aba": flops_oracle["aba"],
+             "aba_derivatives": flops_oracle["aba_derivatives"] - 4.0 * nv**3 + 4.0 * nv * nnz}
     fp64_tf = fp64_peak_tflops(torch)
     value = world * B / (ms_mixed * 1e-3)
     value_fp64 = world * B / (ms_fp64 * 1e-3)
@@ -545,10 +753,16 @@ def run_ours(args, world, rank, local, dist):
             "peak_source": peak_src,
             "traffic": traffic,
             "algorithmic_bytes_per_launch": alg_bytes,
+            "limiter": ("latency (mixed: few warps per SM at this batch, long-scoreboard stalls on workspace "
+                        "loads, FP64 Schur complement in the first sweep); FP64 pipe (fp64 kernels)"),
             "fp64_pipe": {
                 "fp64_kernel_tflops": flops[dom] * B / (kt_fp64[dom] * 1e-3) / 1e12,
                 "measured_dgemm_tflops": fp64_tf,
-                "note": "FP64 kernels: oracle-counted FLOPs / kernel time vs a measured cuBLAS DGEMM",
+                "frac": flops[dom] * B / (kt_fp64[dom] * 1e-3) / 1e12 / fp64_tf,
+                "flops_per_eval": flops[dom],
+                "dtau_structural_nonzeros": nnz,
+                "note": "FP64 kernels: FLOPs the kernels execute (oracle-counted sweeps + the sparse products) / "
+                        "kernel time vs a measured cuBLAS DGEMM",
             },
         },
         "clocks": clocks,
@@ -556,7 +770,9 @@ def run_ours(args, world, rank, local, dist):
         "gpu_launches": args.steps * (1 + 4),
         "e2e": e2e,
     }
+    line["layout_soa"] = soa_ms
     if not args.no_extra:
+        line["rnea_in_parallel_c0"] = measure_c0(torch, pg, sm)
         line["functions"] = measure_functions(torch, pg, sm)
         line["heterogeneous"] = measure_heterogeneous(torch, pg, sm)
         line["rollout"] = measure_rollout(torch, pg, sm)
@@ -567,29 +783,33 @@ def run_ours(args, world, rank, local, dist):
 
 def cpu_baseline(model, args):
     """The oracle port (FP64, OpenMP over instances) on this host's cores, bounded sample."""
-    from oracle.oracle import WORLD, OracleModel
+    env = _omp_env()
+    from oracle.oracle import OracleModel
     from pinocchio_gb300 import sample_models as sm
 
     om = OracleModel(model)
     cores = os.cpu_count() or 1
-    sample = 4096
+    sample = 8192
     q, v, x = sm.random_inputs(model, sample, 3)
     tau = 10.0 * x
-    om.aba(q[:256], v[:256], tau[:256], WORLD, nthreads=cores)
-    om.aba_derivatives(q[:256], v[:256], tau[:256], nthreads=cores)
-    reps, t = 0, 0.0
-    while reps < 3 or (t < 10.0 and reps < 50):
+    outs = _cpu_outs(sample, model.nv)
+    _cpu_step(om, q, v, tau, outs, cores)
+    t = []
+    while len(t) < 3 or (sum(t) < 10.0 and len(t) < 50):
         t0 = time.perf_counter()
-        om.aba(q, v, tau, WORLD, nthreads=cores)
-        om.aba_derivatives(q, v, tau, nthreads=cores)
-        t += time.perf_counter() - t0
-        reps += 1
+        _cpu_step(om, q, v, tau, outs, cores)
+        t.append(time.perf_counter() - t0)
     return {
-        "value": sample * reps / t,
+        "value": sample / float(np.median(t)),
         "unit": "evals/s",
         "cores": cores,
         "kind": "port",
-        "sample": f"{sample} configurations x {reps} repetitions of ABA(WORLD) + ABA derivatives, FP64",
+        "sample": f"{sample} configurations x {len(t)} repetitions (median) of ABA(WORLD) + ABA derivatives, FP64, "
+                  "outputs preallocated",
+        "cpu": _cpu_model_name(),
+        "omp": env,
+        "single_thread": cpu_single_thread(om, model),
+        "rnea_in_parallel_c0": cpu_rnea_c0(cores),
     }
 
 

@@ -98,6 +98,26 @@ int gb_model_destroy(gb_model* model);
 int gb_model_dims(const gb_model* model, int* nq, int* nv, int* njoints);
 const char* gb_last_error(void);
 
+/* Numeric status of a model's kernels (bits of *flags), replacing the checks the
+ * reference makes with assertions and exceptions around its factorisations
+ * (PINOCCHIO_CHECK_INPUT_ARGUMENT / assert, include/pinocchio/macros.hpp:162-223;
+ * the LLT of PerformStYSInversion, multibody/joint/joint-common-operations.hpp:20-45):
+ *   GB_NUMERIC_PIVOT     -- a pivot of a factorisation was not > 0 (or NaN): the
+ *                           joint-space inertia StU + armature of an ABA step, a pivot of
+ *                           the 6x6 LLT of a free-flyer, D of the tree Cholesky of the
+ *                           CRBA, a pivot of the contact solves (singular or indefinite
+ *                           inertia, or NaN inputs);
+ *   GB_NUMERIC_NONFINITE -- an output (tau of RNEA, ddq of ABA / the ABA derivatives)
+ *                           was NaN or infinite.
+ * The kernels OR the bits into a word of the model's device memory; the affected
+ * outputs are then NaN or infinite, as the reference's would be.  This call
+ * synchronises the device, fills *flags (0: nothing seen since the model was
+ * created or the last reset; reset != 0 clears the word after reading it) and
+ * returns GB_ERR_NUMERIC with a message naming the failures when *flags != 0,
+ * GB_OK otherwise. */
+enum { GB_NUMERIC_PIVOT = 1, GB_NUMERIC_NONFINITE = 2 };
+int gb_numeric_status(const gb_model* model, unsigned int* flags, int reset);
+
 /* Diagnostic without a reference counterpart: how many warps of the pipelined
  * kernels (asynchronous bulk copies and producer / consumer barriers, each
  * wait limited to 2 s) gave up waiting since the library was loaded, or since
@@ -179,7 +199,11 @@ int gb_rnea_derivatives_fext(const gb_model* model, int precision, int matrix_mo
 
 /* computeABADerivatives(model, data, q, v, tau) -> (ddq_dq, ddq_dv, Minv)
  * (reference algorithm/aba-derivatives.hxx:380-453, public 910-1051).  Minv
- * is returned symmetric.  ddq may be NULL. */
+ * is returned symmetric.  ddq may be NULL.  In GB_MIXED (nv <= 32) the
+ * -Minv * dtau products run in a pipelined kernel whose barrier waits are
+ * bounded (2 s each): a wait that gives up leaves those outputs unwritten and
+ * is reported only by gb_pipeline_timeouts (the call itself has returned
+ * GB_OK), so a caller that needs the guarantee polls it after the call. */
 int gb_aba_derivatives(const gb_model* model, int precision, int layout, long batch, const double* q,
                        const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                        double* ddq, void* stream);
@@ -214,15 +238,16 @@ int gb_aba_derivatives_vjp(const gb_model* model, int precision, int layout, lon
 /* The batched ABA derivatives of gb_aba_derivatives, computed without any
  * device allocation: no counterpart in the reference (whose algorithms never
  * allocate on their own).  For callers that must not allocate -- real-time
- * control loops, code running while a stream is captured into a CUDA graph,
- * plugins whose host application owns every device allocation -- the
- * workspace is a fixed 64 MiB device array inside the library (held by every
- * GPU that loads it until exit) instead of a cudaMallocAsync block.  Batches
- * whose workspace exceeds it (~1000 FP64 / ~1400 mixed configurations of the
- * 32-dof humanoid) are
- * rejected with GB_ERR_SIZE.  The first call on a device resolves the array's
- * address, so make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * control loops whose cycle must not wait on an allocator, plugins whose host
+ * application owns every device allocation and its budget -- the workspace is
+ * a fixed 64 MiB device array inside the library (held by every GPU that loads
+ * it until exit) instead of a cudaMallocAsync block.  Batches whose workspace
+ * exceeds it (~1000 FP64 / ~1400 mixed configurations of the 32-dof humanoid)
+ * are rejected with GB_ERR_SIZE.  The first call on a device resolves the
+ * array's address, so make it before any stream capture; the address is kept
+ * for the process, so do not call this after a cudaDeviceReset.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller. */
 int gb_aba_derivatives_noalloc(const gb_model* model, int precision, int layout, long batch, const double* q,
                                const double* v, const double* tau, double* ddq_dq, double* ddq_dv, double* Minv,
                                double* ddq, void* stream);

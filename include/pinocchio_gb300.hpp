@@ -2,8 +2,16 @@
 // dynamics entry points:
 //   rneaInParallel(num_threads, pool, q, v, a, tau)   (algorithm/parallel/rnea.hpp:39-84)
 //   abaInParallel(num_threads, pool, q, v, tau, a)    (algorithm/parallel/aba.hpp:40-84)
-// and, for device-resident batches, rnea / aba / crba / computeRNEADerivatives /
-// computeABADerivatives over (batch, n) device arrays.
+// the reference's single calls with their signatures, over a device-batched Data
+// (one column of q, v, a, tau per configuration; a vector is a batch of one):
+//   rnea(model, data, q, v, a)                    -> data.tau   (algorithm/rnea.hpp:37-42)
+//   aba(model, data, q, v, tau, convention)       -> data.ddq   (algorithm/aba.hpp:41-47)
+//   crba(model, data, q, convention)              -> data.M     (algorithm/crba.hpp:47-51)
+//   computeRNEADerivatives(model, data, q, v, a)  -> data.dtau_dq, dtau_dv, M
+//                                                    (algorithm/rnea-derivatives.hpp:120-260)
+//   computeABADerivatives(model, data, q, v, tau) -> data.ddq_dq, ddq_dv, Minv, ddq
+//                                                    (algorithm/aba-derivatives.hpp:52-310)
+// and, for device-resident batches, the same functions over raw (batch, n) device arrays.
 //
 // Matrix arguments are any type with rows(), cols() and data() over contiguous
 // column-major double storage -- Eigen::MatrixXd satisfies this, so a caller of
@@ -18,6 +26,8 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "pinocchio_gb300.h"
 
@@ -223,6 +233,189 @@ inline void forwardKinematics(const Model& m, int precision, long batch, const d
 inline void computeJointJacobians(const Model& m, int precision, long batch, const double* q, double* J,
                                   void* stream = nullptr) {
   check(gb_compute_joint_jacobians(m.get(), precision, GB_LAYOUT_INSTANCE, batch, q, J, stream));
+}
+
+// ---- the reference's single-call signatures over a device-batched Data -------------------------
+inline void check_cuda(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// A column-major rows x cols matrix of doubles in device memory (owned).  Batched
+// outputs hold one configuration per column: a vector output is n x batch, a matrix
+// output (nv x nv per configuration, row-major as the reference's RowMatrixXs) is
+// (nv * nv) x batch.
+class DeviceMatrix {
+ public:
+  DeviceMatrix() = default;
+  DeviceMatrix(const DeviceMatrix&) = delete;
+  DeviceMatrix& operator=(const DeviceMatrix&) = delete;
+  ~DeviceMatrix() {
+    if (p_) cudaFree(p_);
+  }
+  long rows() const { return r_; }
+  long cols() const { return c_; }
+  double* data() { return p_; }
+  const double* data() const { return p_; }
+  // sets the size, reallocating only when it grows
+  void resize(long rows, long cols) {
+    const size_t n = static_cast<size_t>(rows) * static_cast<size_t>(cols);
+    if (n > cap_) {
+      if (p_) cudaFree(p_);
+      p_ = nullptr;
+      cap_ = 0;
+      check_cuda(cudaMalloc(&p_, sizeof(double) * (n > 0 ? n : 1)), "DeviceMatrix");
+      cap_ = n;
+    }
+    r_ = rows;
+    c_ = cols;
+  }
+  // copies into any host matrix with the same rows / cols and contiguous column-major data()
+  template <class M> void copyToHost(M& out, void* stream = nullptr) const {
+    if (static_cast<long>(out.rows()) != r_ || static_cast<long>(out.cols()) != c_)
+      throw std::invalid_argument("copyToHost: the destination has the wrong size");
+    check_cuda(cudaMemcpyAsync(out.data(), p_, sizeof(double) * r_ * c_, cudaMemcpyDeviceToHost,
+                               static_cast<cudaStream_t>(stream)),
+               "copyToHost");
+    check_cuda(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "copyToHost");
+  }
+
+ private:
+  double* p_ = nullptr;
+  long r_ = 0, c_ = 0;
+  size_t cap_ = 0;
+};
+
+// The device-batched counterpart of DataTpl (multibody/data.hpp): the precision and
+// stream of the calls and the outputs the reference keeps in data, for a batch of
+// configurations.  The batch size is the number of columns of q in each call.
+class Data {
+ public:
+  explicit Data(const Model& model, int precision = GB_FP64, void* stream = nullptr)
+      : nq(model.nq), nv(model.nv), precision(precision), stream(stream) {}
+  int nq, nv;
+  int precision;
+  void* stream;
+  DeviceMatrix tau, ddq, M, dtau_dq, dtau_dv, ddq_dq, ddq_dv, Minv;
+
+  // a device pointer to the n x batch input x: x itself when it lives in device (or
+  // managed) memory, else a copy in the input slot
+  template <class X> const double* input(int slot, const X& x, long n, long batch, const char* name) {
+    if (static_cast<long>(x.rows()) != n)
+      throw std::invalid_argument(std::string("wrong number of rows for ") + name);
+    if (static_cast<long>(x.cols()) != batch)
+      throw std::invalid_argument(std::string("wrong number of columns for ") + name);
+    const double* p = x.data();
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) == cudaSuccess &&
+        (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged))
+      return p;
+    (void)cudaGetLastError();  // an unregistered host pointer may leave an error behind
+    staged_[slot].resize(n, batch);
+    check_cuda(cudaMemcpyAsync(staged_[slot].data(), p, sizeof(double) * n * batch, cudaMemcpyHostToDevice,
+                               static_cast<cudaStream_t>(stream)),
+               "input copy");
+    return staged_[slot].data();
+  }
+
+ private:
+  DeviceMatrix staged_[3];
+};
+
+// tau = RNEA(q, v, a) of every column (algorithm/rnea.hpp:37-42): data.tau (nv x batch)
+template <class MQ, class MV, class MA>
+const DeviceMatrix& rnea(const Model& m, Data& data, const MQ& q, const MV& v, const MA& a) {
+  const long B = static_cast<long>(q.cols());
+  const double* Q = data.input(0, q, m.nq, B, "q");
+  const double* V = data.input(1, v, m.nv, B, "v");
+  const double* A = data.input(2, a, m.nv, B, "a");
+  data.tau.resize(m.nv, B);
+  check(gb_rnea(m.get(), data.precision, GB_LAYOUT_INSTANCE, B, Q, V, A, data.tau.data(), data.stream));
+  return data.tau;
+}
+
+// ddq = ABA(q, v, tau) of every column (algorithm/aba.hpp:41-47): data.ddq (nv x batch)
+template <class MQ, class MV, class MT>
+const DeviceMatrix& aba(const Model& m, Data& data, const MQ& q, const MV& v, const MT& tau,
+                        int convention = GB_LOCAL) {
+  const long B = static_cast<long>(q.cols());
+  const double* Q = data.input(0, q, m.nq, B, "q");
+  const double* V = data.input(1, v, m.nv, B, "v");
+  const double* T = data.input(2, tau, m.nv, B, "tau");
+  data.ddq.resize(m.nv, B);
+  check(gb_aba(m.get(), data.precision, convention, GB_LAYOUT_INSTANCE, B, Q, V, T, data.ddq.data(), data.stream));
+  return data.ddq;
+}
+
+// M(q) of every column, upper triangle (algorithm/crba.hpp:47-51): data.M ((nv * nv) x batch)
+template <class MQ>
+const DeviceMatrix& crba(const Model& m, Data& data, const MQ& q, int convention = GB_LOCAL) {
+  const long B = static_cast<long>(q.cols());
+  const double* Q = data.input(0, q, m.nq, B, "q");
+  data.M.resize(static_cast<long>(m.nv) * m.nv, B);
+  check(gb_crba(m.get(), data.precision, convention, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, B, Q, data.M.data(), nullptr,
+                nullptr, data.stream));
+  return data.M;
+}
+
+// dtau/dq, dtau/dv and M (upper) of every column (algorithm/rnea-derivatives.hpp:120-260):
+// data.dtau_dq, data.dtau_dv, data.M ((nv * nv) x batch each) and data.tau
+template <class MQ, class MV, class MA>
+void computeRNEADerivatives(const Model& m, Data& data, const MQ& q, const MV& v, const MA& a) {
+  const long B = static_cast<long>(q.cols());
+  const double* Q = data.input(0, q, m.nq, B, "q");
+  const double* V = data.input(1, v, m.nv, B, "v");
+  const double* A = data.input(2, a, m.nv, B, "a");
+  const long nn = static_cast<long>(m.nv) * m.nv;
+  data.dtau_dq.resize(nn, B);
+  data.dtau_dv.resize(nn, B);
+  data.M.resize(nn, B);
+  data.tau.resize(m.nv, B);
+  check(gb_rnea_derivatives(m.get(), data.precision, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, B, Q, V, A,
+                            data.dtau_dq.data(), data.dtau_dv.data(), data.M.data(), data.tau.data(), data.stream));
+}
+
+// ddq/dq, ddq/dv and Minv of every column (algorithm/aba-derivatives.hpp:52-310):
+// data.ddq_dq, data.ddq_dv, data.Minv ((nv * nv) x batch each, Minv symmetric) and data.ddq
+template <class MQ, class MV, class MT>
+void computeABADerivatives(const Model& m, Data& data, const MQ& q, const MV& v, const MT& tau) {
+  const long B = static_cast<long>(q.cols());
+  const double* Q = data.input(0, q, m.nq, B, "q");
+  const double* V = data.input(1, v, m.nv, B, "v");
+  const double* T = data.input(2, tau, m.nv, B, "tau");
+  const long nn = static_cast<long>(m.nv) * m.nv;
+  data.ddq_dq.resize(nn, B);
+  data.ddq_dv.resize(nn, B);
+  data.Minv.resize(nn, B);
+  data.ddq.resize(m.nv, B);
+  check(gb_aba_derivatives(m.get(), data.precision, GB_LAYOUT_INSTANCE, B, Q, V, T, data.ddq_dq.data(),
+                           data.ddq_dv.data(), data.Minv.data(), data.ddq.data(), data.stream));
+}
+
+// The overloads writing into caller matrices (aba-derivatives.hpp:99-130): each output is
+// (nv * nv) x batch (one row-major nv x nv matrix per column), in device or host memory.
+template <class MQ, class MV, class MT, class M1, class M2, class M3>
+void computeABADerivatives(const Model& m, Data& data, const MQ& q, const MV& v, const MT& tau, M1& ddq_dq,
+                           M2& ddq_dv, M3& dtau) {
+  computeABADerivatives(m, data, q, v, tau);
+  const long nn = static_cast<long>(m.nv) * m.nv;
+  auto out = [&](const DeviceMatrix& src, auto& dst, const char* name) {
+    if (static_cast<long>(dst.rows()) != nn || static_cast<long>(dst.cols()) != src.cols())
+      throw std::invalid_argument(std::string("wrong size for ") + name);
+    check_cuda(cudaMemcpyAsync(dst.data(), src.data(), sizeof(double) * nn * src.cols(), cudaMemcpyDefault,
+                               static_cast<cudaStream_t>(data.stream)),
+               name);
+  };
+  out(data.ddq_dq, ddq_dq, "ddq_dq");
+  out(data.ddq_dv, ddq_dv, "ddq_dv");
+  out(data.Minv, dtau, "Minv");
+  check_cuda(cudaStreamSynchronize(static_cast<cudaStream_t>(data.stream)), "computeABADerivatives");
+}
+
+// Throws std::runtime_error when the model's kernels recorded a numeric failure
+// (gb_numeric_status: a pivot that was not > 0, or a non-finite output); clears the record.
+inline void checkNumeric(const Model& m) {
+  unsigned int flags = 0;
+  check(gb_numeric_status(m.get(), &flags, 1));
 }
 
 }  // namespace pinocchio_gb300

@@ -75,6 +75,15 @@ def _c(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _out(o, shape):
+    """A caller-provided output array (C-contiguous float64 of ``shape``) or a new one."""
+    if o is None:
+        return np.empty(shape)
+    if o.shape != tuple(shape) or o.dtype != np.float64 or not o.flags.c_contiguous:
+        raise ValueError(f"output must be a C-contiguous float64 array of shape {tuple(shape)}")
+    return o
+
+
 class OracleModel:
     """The oracle's copy of a flattened model (from ``Model.tables()``)."""
 
@@ -113,9 +122,9 @@ class OracleModel:
             raise ValueError("fext must hold njoints x 6 values per instance")
         return f
 
-    def rnea(self, q, v, a, prec=0, nthreads=0, fext=None):
+    def rnea(self, q, v, a, prec=0, nthreads=0, fext=None, out=None):
         q, v, a = _c(q), _c(v), _c(a)
-        tau = np.empty((q.shape[0], self.nv))
+        tau = _out(out, (q.shape[0], self.nv))
         if fext is None:
             self._check(lib().orc_rnea(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(a), _ptr(tau), nthreads))
         else:
@@ -123,9 +132,9 @@ class OracleModel:
             self._check(lib().orc_rnea_fext(self.h, prec, q.shape[0], _ptr(q), _ptr(v), _ptr(a), _ptr(f), _ptr(tau), nthreads))
         return tau
 
-    def aba(self, q, v, tau, convention=LOCAL, prec=0, nthreads=0, fext=None):
+    def aba(self, q, v, tau, convention=LOCAL, prec=0, nthreads=0, fext=None, out=None):
         q, v, tau = _c(q), _c(v), _c(tau)
-        ddq = np.empty((q.shape[0], self.nv))
+        ddq = _out(out, (q.shape[0], self.nv))
         if fext is None:
             self._check(lib().orc_aba(self.h, prec, convention, q.shape[0], _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), nthreads))
         else:
@@ -160,12 +169,15 @@ class OracleModel:
             self._check(lib().orc_rnea_derivatives_fext(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(f), _ptr(tau), _ptr(dq), _ptr(dv), _ptr(M), nthreads))
         return tau, dq, dv, M
 
-    def aba_derivatives(self, q, v, tau, prec=0, nthreads=0, fext=None):
-        """(ddq, ddq_dq, ddq_dv, Minv)."""
+    def aba_derivatives(self, q, v, tau, prec=0, nthreads=0, fext=None, out=None):
+        """(ddq, ddq_dq, ddq_dv, Minv); ``out``: the four arrays to write (reused across calls)."""
         q, v, tau = _c(q), _c(v), _c(tau)
         B, nv = q.shape[0], self.nv
-        ddq = np.empty((B, nv))
-        dq, dv, Minv = (np.empty((B, nv, nv)) for _ in range(3))
+        if out is None:
+            ddq = np.empty((B, nv))
+            dq, dv, Minv = (np.empty((B, nv, nv)) for _ in range(3))
+        else:
+            ddq, dq, dv, Minv = (_out(o, shp) for o, shp in zip(out, ((B, nv),) + ((B, nv, nv),) * 3))
         if fext is None:
             self._check(lib().orc_aba_derivatives(self.h, prec, B, _ptr(q), _ptr(v), _ptr(tau), _ptr(ddq), _ptr(dq), _ptr(dv), _ptr(Minv), nthreads))
         else:
@@ -240,3 +252,30 @@ def symmetrize_upper(M):
     """make_symmetric on the upper triangle (reference bindings/python/algorithm/expose-crba.cpp:22)."""
     U = np.triu(M)
     return U + np.swapaxes(np.triu(M, 1), -1, -2)
+
+
+def rollout_with_gradients(om, q0, v0, taus, dt=1e-3, nthreads=0):
+    """FP64 reference of the differentiable rollout: semi-implicit Euler
+    v_{k+1} = v_k + dt ABA(q_k, v_k, tau_k), q_{k+1} = q_k + dt v_{k+1} (vector-space
+    configurations, nq == nv), loss ||q_T||^2 per trajectory summed; the gradients of the
+    loss with respect to q0, v0 and every tau_k by the adjoint recursion over the oracle's
+    analytical ABA derivatives (ddq_dq, ddq_dv, Minv).  Returns (q_T, v_T, g_q0, g_v0, g_taus)."""
+    q, v = _c(q0).copy(), _c(v0).copy()
+    T = taus.shape[0]
+    states = []
+    for k in range(T):
+        states.append((q, v))
+        v = v + dt * om.aba(q, v, taus[k], LOCAL, nthreads=nthreads)
+        q = q + dt * v
+    qT, vT = q, v
+    lq, lv = 2.0 * qT, np.zeros_like(vT)
+    gt = np.empty_like(_c(taus))
+    for k in range(T - 1, -1, -1):
+        qk, vk = states[k]
+        lv = lv + dt * lq  # q_{k+1} = q_k + dt v_{k+1}
+        g = dt * lv  # adjoint of ddq_k
+        _, dq, dv, Minv = om.aba_derivatives(qk, vk, taus[k], nthreads=nthreads)
+        lq = lq + np.einsum("bk,bkc->bc", g, dq)
+        lv = lv + np.einsum("bk,bkc->bc", g, dv)
+        gt[k] = np.einsum("bkc,bk->bc", Minv, g)
+    return qT, vT, lq, lv, gt

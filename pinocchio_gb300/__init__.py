@@ -29,6 +29,7 @@ from .api import (  # noqa: F401
     aba,
     abaDerivativesVJP,
     abaInParallel,
+    checkNumeric,
     computeABADerivatives,
     computeGeneralizedGravity,
     computeJointJacobians,
@@ -44,6 +45,7 @@ from .api import (  # noqa: F401
     forwardKinematics,
     impulseDynamics,
     integrate,
+    numericStatus,
     nonLinearEffects,
     rnea,
     rneaInParallel,

@@ -22,6 +22,7 @@ GB_MATRIX_UPPER, GB_MATRIX_SYMMETRIC = 0, 1
 GB_FUNC_RNEA, GB_FUNC_ABA, GB_FUNC_CRBA, GB_FUNC_RNEA_DERIVATIVES, GB_FUNC_ABA_DERIVATIVES = range(5)
 GB_INSTANCE_PER_THREAD, GB_INSTANCE_PER_WARP, GB_INSTANCE_PER_4_LANES, GB_INSTANCE_PER_8_LANES = 0, 1, 2, 3
 GB_INSTANCE_PER_BRANCH = 4
+GB_NUMERIC_PIVOT, GB_NUMERIC_NONFINITE = 1, 2
 
 # every symbol declared in include/pinocchio_gb300.h, in declaration order
 EXPORTS = (
@@ -29,6 +30,7 @@ EXPORTS = (
     "gb_model_destroy",
     "gb_model_dims",
     "gb_last_error",
+    "gb_numeric_status",
     "gb_pipeline_timeouts",
     "gb_pipeline_wait_selftest",
     "gb_rnea",
@@ -135,6 +137,7 @@ def lib():
         L.gb_model_destroy.argtypes = [vp]
         L.gb_model_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
         L.gb_pipeline_timeouts.argtypes = [C.POINTER(C.c_uint), i]
+        L.gb_numeric_status.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.gb_pipeline_wait_selftest.argtypes = [C.c_uint, vp]
         L.gb_rnea.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp]
         L.gb_nonlinear_effects.argtypes = [vp, i, i, l, vp, vp, vp, vp]

@@ -73,6 +73,26 @@ def createData(model: Model, precision: str = "fp64") -> Data:
 Model.createData = lambda self, precision="fp64": Data(self, precision)  # pin: model.createData()
 
 
+def numericStatus(data: Data, reset: bool = True) -> int:
+    """The numeric status bits the kernels recorded for this model since it was created or
+    last reset (``_capi.GB_NUMERIC_PIVOT``: a factorisation pivot was not > 0, i.e. a
+    singular or indefinite inertia or NaN inputs; ``_capi.GB_NUMERIC_NONFINITE``: an output
+    was NaN or infinite).  Synchronises the device; 0 means nothing was seen."""
+    flags = C.c_uint(0)
+    rc = _capi.lib().gb_numeric_status(data.dev.h, C.byref(flags), int(bool(reset)))
+    if rc not in (_capi.GB_OK, _capi.GB_ERR_NUMERIC):
+        _capi.check(rc)
+    return int(flags.value)
+
+
+def checkNumeric(data: Data, reset: bool = True) -> None:
+    """Raises ``GBError`` (code GB_ERR_NUMERIC) when the kernels of this model recorded a
+    numeric failure (see ``numericStatus``); the reference raises or asserts at the same
+    points of its factorisations."""
+    flags = C.c_uint(0)
+    _capi.check(_capi.lib().gb_numeric_status(data.dev.h, C.byref(flags), int(bool(reset))))
+
+
 def _stream_ptr():
     return C.c_void_p(_torch().cuda.current_stream().cuda_stream)
 

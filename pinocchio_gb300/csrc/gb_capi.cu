@@ -60,12 +60,20 @@ int gb_model_create(const gb_model_desc* desc, gb_model** out) {
     return set_error(rc, err);
   }
   cudaError_t e = cudaGetDevice(&M->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&M->sm_count, cudaDevAttrMultiProcessorCount, M->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&M->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, M->device);
   if (e == cudaSuccess) e = cudaMalloc(&M->d_blob, M->blob_bytes);
   if (e == cudaSuccess) e = cudaMemcpy(M->d_blob, M->blob.data(), M->blob_bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     if (M->d_blob) cudaFree(M->d_blob);
     delete M;
     return gbi::cuda_error(e, "gb_model_create");
+  }
+  rc = gbi::prepare_model_launches(M);
+  if (rc != GB_OK) {
+    cudaFree(M->d_blob);
+    delete M;
+    return rc;
   }
   *out = M;
   return GB_OK;
@@ -76,6 +84,23 @@ int gb_model_destroy(gb_model* M) {
   if (M->d_blob) cudaFree(M->d_blob);
   delete M;
   return GB_OK;
+}
+
+int gb_numeric_status(const gb_model* M, unsigned int* flags, int reset) {
+  if (!M || !flags) return set_error(GB_ERR_INVALID_ARGUMENT, "model/flags is NULL");
+  static_assert(GB_NUMERIC_PIVOT == gb::NUM_PIVOT && GB_NUMERIC_NONFINITE == gb::NUM_NONFINITE, "status bits");
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  unsigned* word = reinterpret_cast<unsigned*>(M->d_blob + h->o_status);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(flags, word, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && reset) e = cudaMemset(word, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return gbi::cuda_error(e, "gb_numeric_status");
+  if (*flags == 0) return GB_OK;
+  std::string msg = "numeric failure in a kernel:";
+  if (*flags & GB_NUMERIC_PIVOT) msg += " a pivot was not positive (singular or indefinite inertia, or NaN input);";
+  if (*flags & GB_NUMERIC_NONFINITE) msg += " an output was NaN or infinite;";
+  return set_error(GB_ERR_NUMERIC, msg);
 }
 
 int gb_model_dims(const gb_model* M, int* nq, int* nv, int* nj) {

@@ -24,7 +24,9 @@ __device__ __forceinline__ gb::MView stage_model(const unsigned char* __restrict
   uint4* dst = reinterpret_cast<uint4*>(smem);
   for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x) dst[k] = src[k];
   __syncthreads();
-  return gb::make_view(smem);
+  gb::MView m = gb::make_view(smem);
+  gb::attach_status(m, blob);
+  return m;
 }
 
 // One configuration's view of an [element][configuration] scratch array.
@@ -71,6 +73,7 @@ __device__ void delassus_llt(const gb::MView& m, const Col& U, const Col& D, con
     for (int c = 0; c < nc; ++c) Y[(long)r * nc + c] = Ji[c * nv + r];
   for (int c = 0; c < nc; ++c) chol_uiv(m, U, Col{Y.p + (long)c * B, B}, nc);
   for (int r = 0; r < nv; ++r) {
+    gb::check_pivot(m, D[r]);
     const double sd = sqrt(D[r]);
     for (int c = 0; c < nc; ++c) Y[(long)r * nc + c] /= sd;
   }
@@ -83,6 +86,7 @@ __device__ void delassus_llt(const gb::MView& m, const Col& U, const Col& D, con
   for (int j = 0; j < nc; ++j) {
     double s = G[(long)j * nc + j];
     for (int k = 0; k < j; ++k) s -= G[(long)j * nc + k] * G[(long)j * nc + k];
+    gb::check_pivot(m, s);
     const double ljj = sqrt(s);
     G[(long)j * nc + j] = ljj;
     for (int i = j + 1; i < nc; ++i) {

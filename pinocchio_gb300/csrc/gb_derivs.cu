@@ -197,6 +197,9 @@ struct ProdPlan {
   unsigned short woff[kProdMaxWarps + 1];  // consumer warp w runs task[woff[w] .. woff[w+1])
   unsigned short task[kProdMaxTasks];      // matrix | group << 1 | row chunk << 8
 };
+static_assert(sizeof(ProdPlan::woff) == sizeof(gb_model::prod_woff) &&
+                  sizeof(ProdPlan::task) == sizeof(gb_model::prod_task),
+              "the model caches the product plan");
 __device__ unsigned int g_pipe_timeouts = 0;  // warps whose pipeline wait gave up (gb_pipeline_timeouts)
 constexpr unsigned long long kPipeWaitNs = 2000000000ull;
 
@@ -456,21 +459,14 @@ int ws_alloc(Workspace& w, size_t bytes, cudaStream_t st) {
 int launch_products_pipe(const gb_model* M, long B, const gb::dfloat* wsMi, Arr Minv, bool minv_upper,
                          const float* wsP, long nP, Arr o0, Arr o1, cudaStream_t st, bool& used) {
   used = false;
-  if (!GB_PROD_PIPE) return GB_OK;
+  if (!GB_PROD_PIPE || !M->prod_plan_ok) return GB_OK;  // plan and shared-memory size: set at model creation
   const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
   const PipeSmem P = pipe_smem(M->nv, h->ngroup, h->n_grp_rel);
-  int dev = 0, optin = 0, nsm = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return cuda_error(e, "k_minv_products_pipe");
-  if (P.bytes > (size_t)optin) return GB_OK;
-  ProdPlan plan;  // a few dozen tasks: rebuilt per call
-  if (!make_prod_plan(M, GB_PROD_CWARPS, plan)) return GB_OK;
-  e = cudaFuncSetAttribute(k_minv_products_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.bytes);
-  if (e != cudaSuccess) return cuda_error(e, "k_minv_products_pipe");
+  ProdPlan plan;
+  std::copy(M->prod_woff, M->prod_woff + kProdMaxWarps + 1, plan.woff);
+  std::copy(M->prod_task, M->prod_task + kProdMaxTasks, plan.task);
   const long nblk = (B + kBlk - 1) / kBlk;
-  const long grid = std::min<long>(nblk, nsm);
+  const long grid = std::min<long>(nblk, M->sm_count);
   k_minv_products_pipe<<<(unsigned)grid, (GB_PROD_CWARPS + GB_PROD_PWARPS) * 32, P.bytes, st>>>(M->d_blob, B, wsMi, Minv, minv_upper, wsP,
                                                                           nP, o0, o1, plan);
   used = true;
@@ -516,7 +512,7 @@ int launch_minv_products(const gb_model* M, long B, const KM* wsMi, Arr Minv, co
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "k_minv_products");
   const long nit = ((B + kBlk - 1) / kBlk) * (kBlk / G);
-  const long grid = std::min<long>(nit, 152L * 2 * 8);
+  const long grid = std::min<long>(nit, (long)M->sm_count * 2 * 8);
   for (int m0 = 0; m0 < 2; m0 += (NM > 0 ? NM : 2)) {
     const unsigned char* bl = M->d_blob;
     const long nP = L.nP, dtq = L.dtq, dtv = L.dtv;
@@ -681,7 +677,7 @@ int run_aba_vjp(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr g, Arr qb,
                       (size_t)(threads / 32) * 2 * M->nv * sizeof(K);
   cudaError_t e = cudaFuncSetAttribute(k_aba_vjp<K, P, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "k_aba_vjp");
-  const long grid = std::min<long>((B + 7) / 8, 152L * 8 * 4);
+  const long grid = std::min<long>((B + 7) / 8, (long)M->sm_count * 8 * 4);
   char* base = static_cast<char*>(ws.p);
   k_aba_vjp<K, P, K><<<(unsigned)grid, threads, smem, st>>>(M->d_blob, B, reinterpret_cast<K*>(base + W.oMB),
                                                              reinterpret_cast<P*>(base + W.oP), L.nP, L.dtq, L.dtv, g,
@@ -706,6 +702,24 @@ int check_gravity(const gb_model* M) {
 }
 
 }  // namespace
+
+// Per-model launch preparation (at creation, on the model's device): the warp-task plan
+// of the pipelined product kernel and its shared-memory size, when the two stages fit.
+int prepare_model_launches(gb_model* M) {
+  M->prod_plan_ok = false;
+  const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+  const PipeSmem P = pipe_smem(M->nv, h->ngroup, h->n_grp_rel);
+  if (P.bytes > (size_t)M->smem_optin) return GB_OK;
+  ProdPlan plan;
+  if (!make_prod_plan(M, GB_PROD_CWARPS, plan)) return GB_OK;
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_minv_products_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.bytes);
+  if (e != cudaSuccess) return cuda_error(e, "k_minv_products_pipe");
+  std::copy(plan.woff, plan.woff + kProdMaxWarps + 1, M->prod_woff);
+  std::copy(plan.task, plan.task + kProdMaxTasks, M->prod_task);
+  M->prod_plan_ok = true;
+  return GB_OK;
+}
 
 int sweeps_team(const SweepCall& c) {
   switch (c.M->layout[GB_FUNC_ABA_DERIVATIVES]) {

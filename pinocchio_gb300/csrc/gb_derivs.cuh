@@ -751,8 +751,12 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
         }
 #pragma unroll 1
       for (int k = 0; k < NVJ; ++k) StU[k * NVJ + k] += SS(m.arm_d[iv + k]);
-      if constexpr (NVJ == 6) llt_inverse<SS, 6>(StU, Dinv);
-      else Dinv[0] = SS(1) / StU[0];
+      if constexpr (NVJ == 6) {
+        if (!llt_inverse<SS, 6>(StU, Dinv)) flag_numeric(m, NUM_PIVOT);
+      } else {
+        check_pivot(m, StU[0]);
+        Dinv[0] = SS(1) / StU[0];
+      }
     }
 #pragma unroll 1
     for (int k = 0; k < NVJ; ++k)
@@ -937,7 +941,11 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
       ld6(zk, L.UD + 6 * (iv + k), ud);
       shift_force_from_origin(ud, ti, udi);  // UDinv (a force about the root origin) about t_i
       dd[k] = zk[L.Du + iv + k] - dot6(udi, oa);
-      if (ddq_out) (*ddq_out)[iv + k] = double(dd[k]);
+      if (ddq_out) {
+        const double x = double(dd[k]);
+        if (!finite_value(x)) flag_numeric(m, NUM_NONFINITE);
+        (*ddq_out)[iv + k] = x;
+      }
     }
 #pragma unroll 1
     for (int k = 0; k < NVJ; ++k)

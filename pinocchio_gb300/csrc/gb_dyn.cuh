@@ -23,12 +23,59 @@ namespace gb {
 
 GB_HD void ssincos(double x, double* s, double* c) { sincos(x, s, c); }
 GB_HD void ssincos(float x, float* s, float* c) { sincosf(x, s, c); }
-// double-float angle: sine and cosine through FP64 (one sincos per revolute joint)
+// double-float angle: sine and cosine through FP64 (the reference for sincos_df below)
 GB_HD void ssincos(dfloat x, dfloat* s, dfloat* c) {
   double sd, cd;
   sincos(double(x), &sd, &cd);
   *s = dfloat(sd);
   *c = dfloat(cd);
+}
+
+// 1 / n!, folded at compile time
+constexpr double inv_fact(int n) { return n <= 1 ? 1.0 : inv_fact(n - 1) / n; }
+// a double-float constant from an FP64 value known at compile time
+#define GB_DF_CONST(x) dfloat(float(x), float((x) - double(float(x))), 0)
+
+// Sine and cosine of an FP64 angle as double-floats with three FP64 operations: the
+// Cody-Waite reduction r = x - k pi/2 (k the nearest integer to x 2/pi, found in FP32;
+// pi/2 in two FP64 parts, two fused multiply-adds) and the split of r into a double-float.
+// The rest runs on the FP32 pipe: the Taylor series of sin and cos on |r| <= pi/4 (the
+// quotient can be off by one near a quadrant boundary, which only widens the interval a
+// little), Horner steps in double-float for the terms above ~1e-9 and plain FP32 for the
+// smaller ones, whose rounding stays below 1e-16; truncation after r^17 / 17! and
+// r^16 / 16! leaves < 1e-17.  The quadrant (k mod 4) then selects +-sin / +-cos.
+GB_HD void sincos_df(double x, dfloat* s, dfloat* c) {
+  constexpr double kPio2Hi = 1.5707963267948966, kPio2Lo = 6.123233995736766e-17;  // pi/2 = hi + lo
+  const float kf = rintf(narrow(x) * 0.636619772f);
+  const double kd = widen(kf);
+#if defined(__CUDA_ARCH__)
+  const double r = __fma_rn(-kd, kPio2Lo, __fma_rn(-kd, kPio2Hi, x));
+#else
+  const double r = fma(-kd, kPio2Lo, fma(-kd, kPio2Hi, x));
+#endif
+  const dfloat rd(r);
+  const dfloat z = rd * rd;
+  const float zf = z.hi;
+  // sin r = r + r z (-1/3! + z (1/5! + z (-1/7! + z (1/9! + z T(z))))), T in FP32
+  const float ts = float(-inv_fact(11)) +
+                   zf * (float(inv_fact(13)) + zf * (float(-inv_fact(15)) + zf * float(inv_fact(17))));
+  dfloat hs = GB_DF_CONST(inv_fact(9)) + z * dfloat(ts);
+  hs = GB_DF_CONST(-inv_fact(7)) + z * hs;
+  hs = GB_DF_CONST(inv_fact(5)) + z * hs;
+  hs = GB_DF_CONST(-inv_fact(3)) + z * hs;
+  const dfloat sn = rd + (rd * z) * hs;
+  // cos r = 1 + z (-1/2 + z (1/4! + z (-1/6! + z (1/8! + z (-1/10! + z U(z)))))), U in FP32
+  const float uc = float(inv_fact(12)) + zf * (float(-inv_fact(14)) + zf * float(inv_fact(16)));
+  dfloat hc = GB_DF_CONST(-inv_fact(10)) + z * dfloat(uc);
+  hc = GB_DF_CONST(inv_fact(8)) + z * hc;
+  hc = GB_DF_CONST(-inv_fact(6)) + z * hc;
+  hc = GB_DF_CONST(inv_fact(4)) + z * hc;
+  hc = dfloat(-0.5f) + z * hc;
+  const dfloat cs = dfloat(1.0f) + z * hc;
+  const int q = (int)kf & 3;
+  const dfloat a = (q & 1) ? cs : sn, b = (q & 1) ? sn : cs;  // sin, cos of x up to signs
+  *s = (q & 2) ? -a : a;
+  *c = ((q + 1) & 2) ? -b : b;
 }
 
 // strided view of one instance's vector / matrix in the batch arrays
@@ -57,6 +104,17 @@ template <class S> GB_HD void joint_params(int jt, S x, S* s, S* c) {
     ssincos(x, s, c);
   }
 }
+// joint_params from the FP64 configuration value; a double-float revolute angle
+// takes sincos_df (no FP64 sincos)
+template <class S> GB_HD void joint_params_q(int jt, double x, S* s, S* c) { joint_params(jt, S(x), s, c); }
+template <> GB_HD void joint_params_q<dfloat>(int jt, double x, dfloat* s, dfloat* c) {
+  if (jt_slides(jt)) {
+    *s = dfloat(x);
+    *c = dfloat(1.0f);
+  } else {
+    sincos_df(x, s, c);
+  }
+}
 // liMi = placement * M_joint of a one-dof joint from its parameters
 template <class S> GB_HD void compose_joint(const S* PR, const S* Pt, int jt, S c, S s, X3<S>& X) {
   if (jt_slides(jt)) compose_slide(PR, Pt, jt_axis(jt), s, X);
@@ -77,7 +135,7 @@ template <class S> GB_HD void joint_transform(const MView& m, int i, const In& q
     compose(Pl, J, X);
   } else {
     S s, c;
-    joint_params(jt, S(q[iq]), &s, &c);
+    joint_params_q(jt, q[iq], &s, &c);
     compose_joint(P, P + 9, jt, c, s, X);
   }
 }
@@ -164,9 +222,15 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
     const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
     if (jt == JT_FF) {
 #pragma unroll
-      for (int k = 0; k < 6; ++k) tau[iv + k] = double(f[i].v[k] + arm[iv + k] * S(a[iv + k]));
+      for (int k = 0; k < 6; ++k) {
+        const double t = double(f[i].v[k] + arm[iv + k] * S(a[iv + k]));
+        if (!finite_value(t)) flag_numeric(m, NUM_NONFINITE);
+        tau[iv + k] = t;
+      }
     } else {
-      tau[iv] = double(pick6(f[i].v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
+      const double t = double(pick6(f[i].v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
+      if (!finite_value(t)) flag_numeric(m, NUM_NONFINITE);
+      tau[iv] = t;
     }
     if (p > 0) {
       M6<S> fp;
@@ -228,7 +292,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       Xff = X;
     } else {
       S sn, cn;
-      joint_params(jt, S(q[m.idx_q[i]]), &sn, &cn);
+      joint_params_q(jt, q[m.idx_q[i]], &sn, &cn);
       const S* P = ModelScalar<S>::place(m, i);
       compose_joint(P, P + 9, jt, cn, sn, X);
       if (!kStoreX) { cs[i][0] = sn; cs[i][1] = cn; }
@@ -299,7 +363,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
         StU[7 * k] += SS(arm[iv + k]);
         u6[k] = SS(tau[iv + k]) - cvt<SS>(f.v[k]);
       }
-      llt_inverse<SS, 6>(StU, D6);
+      if (!llt_inverse<SS, 6>(StU, D6)) flag_numeric(m, NUM_PIVOT);
 #pragma unroll
       for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -316,7 +380,9 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
     const SS u = SS(tau[iv]) - cvt<SS>(pick6(f.v, sx));
     SS U[6], UD[6];
     sym6_col(Ia, sx, U);
-    const SS Dinv = SS(1) / (pick6(U, sx) + SS(arm[iv]));
+    const SS Dpiv = pick6(U, sx) + SS(arm[iv]);
+    check_pivot(m, Dpiv);
+    const SS Dinv = SS(1) / Dpiv;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       UD[k] = U[k] * Dinv;
@@ -374,6 +440,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 #pragma unroll
         for (int k = 1; k < 6; ++k) w += UD6[6 * k + r] * cvt<SS>(a.v[k]);
         dd[r] = s - w;
+        if (!finite_value(dd[r])) flag_numeric(m, NUM_NONFINITE);
         ddq[iv + r] = double(dd[r]);
       }
 #pragma unroll
@@ -383,6 +450,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 #pragma unroll
       for (int k = 1; k < 6; ++k) w += UDs[i][k] * a.v[k];
       const SS dd = du[i] - cvt<SS>(w);
+      if (!finite_value(dd)) flag_numeric(m, NUM_NONFINITE);
       ddq[iv] = double(dd);
       add_at6(a.v, jt_sidx(jt), cvt<S>(dd));
     }
@@ -488,6 +556,7 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
     }
     const double Dj = M[j * nv + j] - s;
     Do[j] = Dj;
+    check_pivot(m, Dj);
     const double Dinv = 1.0 / Dj;
     for (int ii = m.pfr[j]; ii >= 0; ii = m.pfr[ii]) {
       double w = 0.0;

@@ -58,6 +58,8 @@ int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);
 size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B);
+// per-model launch preparation at creation (gb_derivs.cu)
+int prepare_model_launches(gb_model* M);
 // device scratch from the stream-ordered pool, and the SOA -> instance transpose (gb_util.cu):
 // src holds n elements x B configurations ([element][configuration]), dst an instance-layout array
 int scratch_alloc(void** p, size_t bytes, cudaStream_t st);

@@ -42,6 +42,9 @@ struct BlobHeader {
   // chains: maximal runs of joints each the only child of the previous one (consecutive in the
   // depth-first order); chain c holds joints chain[3c] .. chain[3c+1] at chain level chain[3c+2]
   int o_chain, nchain, nclevel, chain_team;
+  // o_status: the model's numeric status word (GB_NUMERIC_* bits, atomicOr from the kernels), in
+  // global memory beyond the staged prefix
+  int o_status, pad_status[3];
   double grav_d[6];
   float grav_f[6];
   float padf[2];
@@ -59,7 +62,31 @@ struct MView {
   const float *place_f, *iner_f, *arm_f, *grav_f, *i6_f;
   const dfloat *place_df, *iner_df, *arm_df, *grav_df;
   const double* fix_d;  // nullptr when no joint is unaligned
+  unsigned* status;     // the status word in the global copy of the blob (nullptr: not recorded)
 };
+
+// Numeric failures seen by a kernel (bits of the model's status word, read by gb_numeric_status):
+// a pivot of a factorisation that is not > 0 (or NaN): singular or indefinite articulated /
+// joint-space inertia; a non-finite output.
+enum { NUM_PIVOT = 1u, NUM_NONFINITE = 2u };
+GB_HD void flag_numeric(const MView& m, unsigned bits) {
+#if defined(__CUDA_ARCH__)
+  if (m.status) atomicOr(m.status, bits);
+#else
+  (void)m;
+  (void)bits;
+#endif
+}
+// a pivot d of a factorisation (flagged unless d > 0)
+template <class S> GB_HD void check_pivot(const MView& m, S d) {
+  if (!(d > S(0))) flag_numeric(m, NUM_PIVOT);
+}
+GB_HD bool finite_value(double x) { return x - x == 0.0; }  // false for NaN and +-inf
+// the status word of a blob staged from `global_blob` (the view was made from the staged copy)
+GB_HD void attach_status(MView& m, const unsigned char* global_blob) {
+  const BlobHeader* h = reinterpret_cast<const BlobHeader*>(global_blob);
+  m.status = reinterpret_cast<unsigned*>(const_cast<unsigned char*>(global_blob) + h->o_status);
+}
 
 GB_HD MView make_view(const unsigned char* base) {
   const BlobHeader* h = reinterpret_cast<const BlobHeader*>(base);
@@ -98,6 +125,7 @@ GB_HD MView make_view(const unsigned char* base) {
   m.arm_df = reinterpret_cast<const dfloat*>(base + h->o_arm_df);
   m.grav_df = h->grav_df;
   m.fix_d = h->o_fix ? reinterpret_cast<const double*>(base + h->o_fix) : nullptr;
+  m.status = nullptr;
   m.grav_d = h->grav_d;
   m.grav_f = h->grav_f;
   return m;

@@ -29,6 +29,14 @@ struct gb_model {
   int blob_bytes = 0;
   int stage_bytes = 0;  // prefix of the blob the per-instance kernels copy into shared memory
   int chain_team = 4;   // lanes per configuration of the lane-per-branch layout
+  // the model's device, read once at creation: multiprocessors (grid sizes of the
+  // persistent kernels) and the opt-in shared memory per block
+  int sm_count = 0, smem_optin = 0;
+  // the warp-task plan of the pipelined -Minv*dtau product kernel (built once per model;
+  // prod_plan_ok false: that kernel does not apply to this model)
+  unsigned short prod_woff[33] = {};
+  unsigned short prod_task[256] = {};
+  bool prod_plan_ok = false;
 };
 
 namespace gbm {
@@ -271,6 +279,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   h.stage_bytes = (int)off;
   h.o_rel_list = take(4 * M->rel_list.size() + 4);
   h.o_grp = take(4 * grp.size()); h.o_grp_rel = take(4 * grp_rel.size() + 4);
+  h.o_status = take(16);  // the numeric status word (zero at creation)
   h.bytes = (int)off;
   for (int k = 0; k < 6; ++k) {
     h.grav_d[k] = M->gravity[k];

@@ -59,7 +59,8 @@ __global__ void k_multi(TaskTable tab, int tile, int blob_region, int warp_regio
       __syncthreads();
       staged = T.blob;
     }
-    const gb::MView m = gb::make_view(smem);
+    gb::MView m = gb::make_view(smem);
+    gb::attach_status(m, T.blob);
     if (T.warp) {  // warp-uniform
       const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const long b = (g - T.tile_begin) * T.per_tile + w;

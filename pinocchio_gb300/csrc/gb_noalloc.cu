@@ -1,11 +1,11 @@
 // gb_aba_derivatives_noalloc: the batched ABA derivatives for callers that must
 // not allocate device memory.
 //
-// Who cannot allocate: real-time control loops (the reference's own algorithms
-// promise not to allocate, and unittest/crba.cpp checks it with Eigen's
-// malloc guard), code that runs while a CUDA stream is being captured into a
-// graph, and plugins hosted by an application that owns every device
-// allocation.  gb_aba_derivatives takes its per-configuration workspace from
+// Who cannot allocate: real-time control loops, whose cycle must not wait on
+// an allocator (the reference's own algorithms promise not to allocate, and
+// unittest/crba.cpp checks it with Eigen's malloc guard), and plugins hosted by
+// an application that owns every device allocation and its budget.
+// gb_aba_derivatives takes its per-configuration workspace from
 // cudaMallocAsync; this entry point instead uses the fixed device array below.
 //
 // The array is kNoAllocScratchBytes (64 MiB) and is held by every GPU that
@@ -39,7 +39,9 @@ void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 // Resolves the device address of the array on the current device, once per
 // device.  This happens inside the first call made on a device, so that first
-// call must come before any stream capture.
+// call must come before any stream capture.  The address is kept for the life
+// of the process: after a cudaDeviceReset the module is loaded again and the
+// array may move, so this entry point must not be used after a device reset.
 int scratch_on_current_device(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -130,17 +130,25 @@ template <class S> GB_HD void sym3_mv(const S* s, const S* x, S* o) {
 // --- rigid transforms ---------------------------------------------------------------------
 // Rotation of a joint about a unit axis, composed on the right of a placement:
 // liMi = placement * (Rax(c, s), 0)  (revolute joint, reference joint-revolute.hpp:213-235).
-template <class S> GB_HD void compose_axis(const S* PR, const S* Pt, int axis, S c, S s, X3<S>& out) {
+template <int AX, class S> GB_HD void compose_axis_ax(const S* PR, const S* Pt, S c, S s, X3<S>& out) {
   // columns i, j rotated: col_i' = c col_i + s col_j ; col_j' = -s col_i + c col_j (i,j cyclic after axis)
-  const int i = (axis + 1) % 3, j = (axis + 2) % 3;
+  constexpr int i = (AX + 1) % 3, j = (AX + 2) % 3;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const S pi = PR[3 * r + i], pj = PR[3 * r + j];
-    out.R[3 * r + axis] = PR[3 * r + axis];
+    out.R[3 * r + AX] = PR[3 * r + AX];
     out.R[3 * r + i] = c * pi + s * pj;
     out.R[3 * r + j] = c * pj - s * pi;
     out.t[r] = Pt[r];
   }
+}
+// The axis is the same for every thread of a warp (all run the same joint): one
+// branch, each case with compile-time indices, so that the transform stays in
+// registers (a run-time index into it would move it to local memory).
+template <class S> GB_HD void compose_axis(const S* PR, const S* Pt, int axis, S c, S s, X3<S>& out) {
+  if (axis == 0) compose_axis_ax<0>(PR, Pt, c, s, out);
+  else if (axis == 1) compose_axis_ax<1>(PR, Pt, c, s, out);
+  else compose_axis_ax<2>(PR, Pt, c, s, out);
 }
 // Translation of a joint along a unit axis, composed on the right of a placement:
 // liMi = placement * (I, d e_axis)  (prismatic joint, reference joint-prismatic.hpp:232-284,
@@ -436,8 +444,10 @@ template <class S> GB_HD void sym6_transform(const Sym6<S>& I, const X3<S>& X, S
 
 // Inverse of a small SPD matrix by an LLT and two triangular solves
 // (the PerformStYSInversion of reference multibody/joint/joint-common-operations.hpp:20-33).
-template <class S, int N> GB_HD void llt_inverse(const S* A, S* Ainv) {
+// Returns false when a pivot is not > 0 (A not positive definite, or NaN).
+template <class S, int N> GB_HD bool llt_inverse(const S* A, S* Ainv) {
   S L[N * N];
+  bool ok = true;
 #pragma unroll
   for (int k = 0; k < N * N; ++k) L[k] = A[k];
 #pragma unroll
@@ -445,6 +455,7 @@ template <class S, int N> GB_HD void llt_inverse(const S* A, S* Ainv) {
     S x = L[N * k + k];
 #pragma unroll
     for (int j = 0; j < k; ++j) x -= L[N * k + j] * L[N * k + j];
+    ok = ok && x > S(0);
     x = sqrt(x);
     L[N * k + k] = x;
     const S ix = S(1) / x;
@@ -476,6 +487,7 @@ template <class S, int N> GB_HD void llt_inverse(const S* A, S* Ainv) {
 #pragma unroll
     for (int i = 0; i < N; ++i) Ainv[N * i + c] = y[i];
   }
+  return ok;
 }
 
 }  // namespace gb

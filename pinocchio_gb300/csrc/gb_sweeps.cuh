@@ -44,7 +44,9 @@ __device__ __forceinline__ gb::MView stage_model(const unsigned char* __restrict
   uint4* dst = reinterpret_cast<uint4*>(smem);
   for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x) dst[k] = src[k];
   __syncthreads();
-  return gb::make_view(smem);
+  gb::MView m = gb::make_view(smem);
+  gb::attach_status(m, blob);
+  return m;
 }
 __device__ __forceinline__ gb::In in_at(const Arr& a, long b) { return gb::In{a.p + b * a.is, a.es}; }
 __device__ __forceinline__ gb::Out out_at(const Arr& a, long b) {

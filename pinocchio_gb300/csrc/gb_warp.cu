@@ -19,7 +19,9 @@ __device__ __forceinline__ gb::MView stage_blob(const unsigned char* __restrict_
   uint4* dst = reinterpret_cast<uint4*>(smem);
   for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x) dst[k] = src[k];
   __syncthreads();
-  return gb::make_view(smem);
+  gb::MView m = gb::make_view(smem);
+  gb::attach_status(m, blob);
+  return m;
 }
 
 template <class S>
@@ -113,7 +115,7 @@ int launch_rnea_branch_t(const gb_model* M, long B, Arr q, Arr v, Arr a, Arr tau
   int rc = branch_launch_shape(M, TS, region, k_rnea_branch<S, TS>, "k_rnea_branch", &threads, &smem);
   if (rc != GB_OK) return rc;
   const int teams = threads / TS;
-  const long grid = std::min<long>((B + teams - 1) / teams, 152L * 16);
+  const long grid = std::min<long>((B + teams - 1) / teams, (long)M->sm_count * 16);
   k_rnea_branch<S, TS><<<(unsigned)grid, threads, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, a, tau, (int)region);
   return cuda_error(cudaGetLastError(), "k_rnea_branch");
 }
@@ -125,7 +127,7 @@ int launch_aba_branch_t(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dd
   int rc = branch_launch_shape(M, TS, region, k_aba_branch<S, SS, TS>, "k_aba_branch", &threads, &smem);
   if (rc != GB_OK) return rc;
   const int teams = threads / TS;
-  const long grid = std::min<long>((B + teams - 1) / teams, 152L * 16);
+  const long grid = std::min<long>((B + teams - 1) / teams, (long)M->sm_count * 16);
   k_aba_branch<S, SS, TS><<<(unsigned)grid, threads, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, tau, ddq,
                                                                   (int)region);
   return cuda_error(cudaGetLastError(), "k_aba_branch");
@@ -153,7 +155,7 @@ int launch_rnea_warp_t(const gb_model* M, long B, Arr q, Arr v, Arr a, Arr tau, 
   const size_t per_warp = rnea_warp_bytes<S>(M->nj);
   int rc = warp_launch_shape(M, per_warp, k_rnea_warp<S>, "k_rnea_warp", &nw, &smem);
   if (rc != GB_OK) return rc;
-  const long grid = std::min<long>((B + nw - 1) / nw, 152L * 16);
+  const long grid = std::min<long>((B + nw - 1) / nw, (long)M->sm_count * 16);
   k_rnea_warp<S><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, a, tau);
   return cuda_error(cudaGetLastError(), "k_rnea_warp");
 }
@@ -165,7 +167,7 @@ int launch_aba_warp_t(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq,
   const size_t per_warp = aba_warp_bytes<S, SS>(M->nj);
   int rc = warp_launch_shape(M, per_warp, k_aba_warp<S, SS>, "k_aba_warp", &nw, &smem);
   if (rc != GB_OK) return rc;
-  const long grid = std::min<long>((B + nw - 1) / nw, 152L * 16);
+  const long grid = std::min<long>((B + nw - 1) / nw, (long)M->sm_count * 16);
   k_aba_warp<S, SS><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, tau, ddq);
   return cuda_error(cudaGetLastError(), "k_aba_warp");
 }

@@ -126,9 +126,15 @@ __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In&
           for (int k = 0; k < 6; ++k) fi.v[k] += cf[c].v[k];
       if (jt == JT_FF) {
 #pragma unroll
-        for (int k = 0; k < 6; ++k) tau[iv + k] = double(fi.v[k] + arm[iv + k] * S(a[iv + k]));
+        for (int k = 0; k < 6; ++k) {
+          const double t = double(fi.v[k] + arm[iv + k] * S(a[iv + k]));
+          if (!gb::finite_value(t)) gb::flag_numeric(m, gb::NUM_NONFINITE);
+          tau[iv + k] = t;
+        }
       } else {
-        tau[iv] = double(pick6(fi.v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
+        const double t = double(pick6(fi.v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
+        if (!gb::finite_value(t)) gb::flag_numeric(m, gb::NUM_NONFINITE);
+        tau[iv] = t;
       }
       if (p > 0) act_force(X[i], fi, cf[i]);
     });
@@ -162,7 +168,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
       joint_transform(m, i, q, X[i]);
     } else {
       S sn, cn;
-      joint_params(m.jtype[i], S(q[m.idx_q[i]]), &sn, &cn);
+      joint_params_q(m.jtype[i], q[m.idx_q[i]], &sn, &cn);
       const S* P = ModelScalar<S>::place(m, i);
       compose_joint(P, P + 9, m.jtype[i], cn, sn, X[i]);
     }
@@ -237,7 +243,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
           StU[7 * k] += SS(arm[iv + k]);
           u6[k] = SS(tau[iv + k]) - cvt<SS>(f.v[k]);
         }
-        llt_inverse<SS, 6>(StU, D);
+        if (!llt_inverse<SS, 6>(StU, D)) gb::flag_numeric(m, gb::NUM_PIVOT);
 #pragma unroll
         for (int k = 0; k < 36; ++k) D6[k] = D[k];
 #pragma unroll
@@ -255,7 +261,9 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
       const SS u = SS(tau[iv]) - cvt<SS>(pick6(f.v, sx));
       SS U[6], UD[6];
       sym6_col(Ia, sx, U);
-      const SS Dinv = SS(1) / (pick6(U, sx) + SS(arm[iv]));
+      const SS Dpiv = pick6(U, sx) + SS(arm[iv]);
+      gb::check_pivot(m, Dpiv);
+      const SS Dinv = SS(1) / Dpiv;
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         UD[k] = U[k] * Dinv;
@@ -304,6 +312,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
 #pragma unroll
           for (int k = 1; k < 6; ++k) w += UD6[6 * k + r] * cvt<SS>(a.v[k]);
           dd[r] = s - w;
+          if (!gb::finite_value(dd[r])) gb::flag_numeric(m, gb::NUM_NONFINITE);
           ddq[iv + r] = double(dd[r]);
         }
 #pragma unroll
@@ -313,6 +322,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
 #pragma unroll
         for (int k = 1; k < 6; ++k) w += UDs[i].v[k] * a.v[k];
         const SS dd = du[i] - cvt<SS>(w);
+        if (!gb::finite_value(dd)) gb::flag_numeric(m, gb::NUM_NONFINITE);
         ddq[iv] = double(dd);
         add_at6(a.v, jt_sidx(jt), cvt<S>(dd));
       }

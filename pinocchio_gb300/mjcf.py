@@ -134,7 +134,7 @@ def buildModelFromMJCFXML(xml: str) -> Model:
     if root.tag != "mujoco":
         raise ValueError("not an MJCF document: the root element must be <mujoco>")
     for el in root.iter():
-        if el.tag in ("default", "include"):
+        if el.tag in ("default", "include", "frame"):
             raise ValueError(f"<{el.tag}> is not supported")
         if el.get("class") is not None or el.get("childclass") is not None:
             raise ValueError(f"<{el.tag}>: class / childclass attributes are not supported")
@@ -145,8 +145,16 @@ def buildModelFromMJCFXML(xml: str) -> Model:
     model = Model()
     model.name = root.get("model", "")
 
+    def check_children(el):
+        # bodies are read as direct <body> children only: a body nested in any other container
+        # would be dropped, so such a container is an error (no model may silently differ)
+        for child in el:
+            if child.tag != "body" and child.find(".//body") is not None:
+                raise ValueError(f"<{child.tag}> inside <{el.tag}> holds bodies: not supported")
+
     def visit(body, frame):
         """frame: (the joint that carries the parent body, the parent body's frame in that joint's frame)."""
+        check_children(body)
         parent_joint, parent_in_joint = frame
         pose = _mul(parent_in_joint, comp.pose(body))
         joints = [("free", j) for j in body.findall("freejoint")] + [(j.get("type", "hinge"), j) for j in body.findall("joint")]
@@ -177,6 +185,7 @@ def buildModelFromMJCFXML(xml: str) -> Model:
         for child in body.findall("body"):
             visit(child, child_frame)
 
+    check_children(world)
     for body in world.findall("body"):
         visit(body, (0, SE3.Identity()))
     if model.njoints > 1 and any(t == JT_FF for t in model.jtypes[2:]):

@@ -1,6 +1,8 @@
 // Test program for the C++ facade (include/pinocchio_gb300.hpp): builds a
 // 3-joint chain, runs rneaInParallel / abaInParallel on host column-major
-// matrices and prints the max |ABA(RNEA(a)) - a|.  A minimal column-major
+// matrices and prints the max |ABA(RNEA(a)) - a|; then the single calls
+// rnea / aba / crba / computeRNEADerivatives / computeABADerivatives over a Data
+// (ABA(RNEA(a)) = a, the ddq of the derivatives, Minv M = I, M of both algorithms).  A minimal column-major
 // matrix type stands in for Eigen::MatrixXd (same rows/cols/data interface).
 #include <cmath>
 #include <cstdio>
@@ -70,7 +72,54 @@ int main() {
     } catch (const std::invalid_argument& e) {
       std::printf("pool_check_ok %s\n", e.what());
     }
-    return err < 1e-10 ? 0 : 1;
+    if (err >= 1e-10) return 1;
+
+    // the reference's single-call signatures over a device-batched Data: host inputs,
+    // a device input (data.tau of a previous call), outputs into caller matrices
+    pinocchio_gb300::Data data(model), data2(model);
+    const pinocchio_gb300::DeviceMatrix& tau_d = pinocchio_gb300::rnea(model, data, q, v, a);
+    Mat tau2(model.nv, B), a3(model.nv, B);
+    tau_d.copyToHost(tau2);
+    double e1 = 0.0;
+    for (long k = 0; k < model.nv * B; ++k) e1 = std::fmax(e1, std::fabs(tau2.d[k] - tau.d[k]));
+    pinocchio_gb300::aba(model, data2, q, v, data.tau).copyToHost(a3);  // device input
+    double e2 = 0.0;
+    for (long k = 0; k < model.nv * B; ++k) e2 = std::fmax(e2, std::fabs(a3.d[k] - a.d[k]));
+    const long nn = static_cast<long>(model.nv) * model.nv;
+    Mat dq(nn, B), dv(nn, B), Minv(nn, B), Mup(nn, B), ddq(model.nv, B);
+    pinocchio_gb300::computeABADerivatives(model, data, q, v, tau2, dq, dv, Minv);
+    data.ddq.copyToHost(ddq);
+    double e3 = 0.0;
+    for (long k = 0; k < model.nv * B; ++k) e3 = std::fmax(e3, std::fabs(ddq.d[k] - a.d[k]));
+    pinocchio_gb300::crba(model, data, q).copyToHost(Mup);
+    double e4 = 0.0;  // Minv * M = I per configuration (M from its upper triangle)
+    const int n = model.nv;
+    for (long b = 0; b < B; ++b) {
+      const double* Mi = &Minv.d[nn * b];
+      const double* Mu = &Mup.d[nn * b];
+      for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) {
+          double s = 0.0;
+          for (int k = 0; k < n; ++k) s += Mi[r * n + k] * (k <= c ? Mu[k * n + c] : Mu[c * n + k]);
+          e4 = std::fmax(e4, std::fabs(s - (r == c ? 1.0 : 0.0)));
+        }
+    }
+    pinocchio_gb300::computeRNEADerivatives(model, data, q, v, a);
+    Mat M2(nn, B);
+    data.M.copyToHost(M2);
+    double e5 = 0.0;
+    for (long k = 0; k < nn * B; ++k) e5 = std::fmax(e5, std::fabs(M2.d[k] - Mup.d[k]));
+    pinocchio_gb300::checkNumeric(model);
+    std::printf("single_calls rnea %.3e aba %.3e ddq %.3e minv_m %.3e M %.3e\n", e1, e2, e3, e4, e5);
+    try {
+      Mat bad(model.nq + 1, B);
+      pinocchio_gb300::rnea(model, data, bad, v, a);
+      std::printf("expected an exception\n");
+      return 4;
+    } catch (const std::invalid_argument& e) {
+      std::printf("size_check_ok %s\n", e.what());
+    }
+    return (e1 < 1e-12 && e2 < 1e-10 && e3 < 1e-10 && e4 < 1e-10 && e5 < 1e-12) ? 0 : 5;
   } catch (const std::exception& e) {
     std::printf("error %s\n", e.what());
     return 3;

@@ -17,7 +17,9 @@ def build_exe(tmp_path):
     _build.build()
     exe = str(tmp_path / "facade_check")
     libdir = os.path.dirname(_build.LIB)
-    cmd = ["g++", "-std=c++17", "-O1", "-o", exe, SRC, f"-L{libdir}", "-lpinocchio_gb300", f"-Wl,-rpath,{libdir}"]
+    cuda = os.path.dirname(os.path.dirname(_build.nvcc()))
+    cmd = ["g++", "-std=c++17", "-O1", "-o", exe, SRC, f"-I{cuda}/include", f"-L{libdir}", "-lpinocchio_gb300",
+           f"-Wl,-rpath,{libdir}", f"-L{cuda}/lib64", "-lcudart", f"-Wl,-rpath,{cuda}/lib64"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return exe
 
@@ -31,3 +33,4 @@ def test_facade_roundtrip_on_gpu(tmp_path):
     r = subprocess.run([build_exe(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "pool_check_ok" in r.stdout
+    assert "single_calls" in r.stdout and "size_check_ok" in r.stdout

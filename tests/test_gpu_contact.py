@@ -117,3 +117,35 @@ def test_kkt_inverse(case, mu):
     data = pg.createData(model)
     K = pg.computeKKTContactDynamicMatrixInverse(model, data, dev(q), dev(J), mu).cpu().numpy()
     assert rel_err(K, om.kkt_inverse(q, J, mu)) < 1e-10
+
+
+def test_kkt_inverse_soa_layout_and_no_constraint_rows(case):
+    """The value-major (SOA) indexing of J and of the KKT inverse gives the bits of the
+    instance layout; with nc == 0 (J may be NULL) the inverse is M^-1 itself, which
+    computeMinverse also returns."""
+    import torch
+
+    name, model, om, q, v, tau, J, gamma, dev = case
+    data = pg.createData(model)
+    B, nv, nc = q.shape[0], model.nv, J.shape[1]
+    n = nv + nc
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    L, h = _capi.lib(), data.dev.h
+    qd, Jd = dev(q), dev(J)
+    K_inst = torch.empty((B, n, n), dtype=torch.float64, device="cuda")
+    _capi.check(L.gb_kkt_contact_inverse(h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, B, nc, p(qd), p(Jd), 1e-3,
+                                         p(K_inst), None))
+    qs, Js = dev(q.T), dev(J.reshape(B, -1).T)
+    K_soa = torch.empty((n * n, B), dtype=torch.float64, device="cuda")
+    _capi.check(L.gb_kkt_contact_inverse(h, _capi.GB_FP64, _capi.GB_LAYOUT_SOA, B, nc, p(qs), p(Js), 1e-3,
+                                         p(K_soa), None))
+    torch.cuda.synchronize()
+    assert torch.equal(K_soa.T.reshape(B, n, n), K_inst)
+    K0 = torch.empty((B, nv, nv), dtype=torch.float64, device="cuda")
+    _capi.check(L.gb_kkt_contact_inverse(h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, B, 0, p(qd), None, 0.0, p(K0),
+                                         None))
+    Minv = pg.computeMinverse(model, data, qd)
+    torch.cuda.synchronize()
+    assert rel_err(K0.cpu().numpy(), Minv.cpu().numpy()) < 1e-12
+    _, _, _, Minv_o = om.aba_derivatives(q, v, tau)
+    assert rel_err(K0.cpu().numpy(), Minv_o) < 1e-11

@@ -128,6 +128,11 @@ def test_orientation_forms_and_units():
      '<body name="b"><freejoint/><inertial mass="1" diaginertia="1 1 1"/></body></body></worldbody>', "free"),
     ('<worldbody><body name="a" zaxis="0 1 0"><joint/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "zaxis"),
     ('<worldbody><body name="a" childclass="x"><joint/></body></worldbody>', "class"),
+    ('<worldbody><body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/>'
+     '<frame pos="0 0 1"><body name="b"><joint/><inertial mass="1" diaginertia="1 1 1"/></body></frame>'
+     '</body></worldbody>', "frame"),
+    ('<worldbody><group><body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/></body></group></worldbody>',
+     "holds bodies"),
 ])
 def test_outside_the_subset_raises(snippet, msg):
     with pytest.raises(ValueError, match=msg):

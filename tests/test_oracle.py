@@ -325,3 +325,34 @@ def test_forward_kinematics_acceleration_vs_fd(name):
     vp = om.forward_kinematics(om.integrate(q, h * v), v + h * a)[1]
     vm = om.forward_kinematics(om.integrate(q, -h * v), v - h * a)[1]
     assert rel_err((vp - vm) / (2 * h), ai) < 1e-6
+
+
+def test_oracle_rollout_gradients_vs_central_differences():
+    """The adjoint recursion of the oracle's rollout (the FP64 reference of the
+    differentiable rollout) against central differences of its own forward rollout."""
+    from oracle.oracle import rollout_with_gradients
+
+    model = sm.chain(6, 2, (0.1, 1.0))
+    om = OracleModel(model)
+    rng = np.random.default_rng(9)
+    B, T, n, dt = 2, 8, model.nv, 1e-2
+    q0 = rng.uniform(-np.pi, np.pi, (B, n))
+    v0 = 0.1 * rng.standard_normal((B, n))
+    taus = rng.standard_normal((T, B, n))
+    _, _, gq, gv, gt = rollout_with_gradients(om, q0, v0, taus, dt)
+
+    def loss(q, v, t):
+        qT = rollout_with_gradients(om, q, v, t, dt)[0]
+        return float((qT**2).sum())
+
+    h = 1e-6
+    for which, (base, grad) in enumerate(((q0, gq), (v0, gv), (taus, gt))):
+        for _ in range(5):
+            idx = tuple(rng.integers(0, s) for s in base.shape)
+            args_p, args_m = [q0, v0, taus], [q0, v0, taus]
+            plus, minus = base.copy(), base.copy()
+            plus[idx] += h
+            minus[idx] -= h
+            args_p[which], args_m[which] = plus, minus
+            fd = (loss(*args_p) - loss(*args_m)) / (2 * h)
+            assert abs(fd - grad[idx]) <= 1e-7 * max(1.0, abs(grad[idx])), (which, idx, fd, grad[idx])
