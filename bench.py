@@ -679,6 +679,21 @@ def run_ours(args, world, rank, local, dist):
             acc[prec] = {k: {"max": m, "median": md} for k, (m, md) in
                          zip(("ddq", "ddq_dq", "ddq_dv", "Minv", "aba_ddq"), errs)}
             acc[prec]["sample"] = f"{ns} configurations strided over the batch of {B} (first and last included)"
+        # the mixed derivatives over every configuration of the batch (chunks of 8192)
+        step("mixed", 0)
+        torch.cuda.synchronize()
+        errs = {k: [] for k in ("ddq_dq", "ddq_dv", "Minv")}
+        for lo in range(0, B, 8192):
+            hi = min(B, lo + 8192)
+            ref = om.aba_derivatives(q[lo:hi], v[lo:hi], 10.0 * x[lo:hi])
+            for k, g, r in (("ddq_dq", outs["ddq_dq"], ref[1]), ("ddq_dv", outs["ddq_dv"], ref[2]),
+                            ("Minv", outs["Minv"], ref[3])):
+                g = g[lo:hi].cpu().numpy().reshape(hi - lo, -1)
+                r = r.reshape(hi - lo, -1)
+                errs[k].append(np.linalg.norm(g - r, axis=1) / np.linalg.norm(r, axis=1))
+        acc["mixed_full_batch"] = {k: {"max": float(np.concatenate(e).max()), "median": float(np.median(np.concatenate(e))),
+                                       "p999": float(np.quantile(np.concatenate(e), 0.999))} for k, e in errs.items()}
+        acc["mixed_full_batch"]["sample"] = f"all {B} configurations"
 
     # end to end through the public API: pinned host inputs -> device -> kernels -> pinned host outputs
     e2e = None

@@ -574,7 +574,9 @@ template <class S, class T3, class T, class K, class SS, class P>
 int launch_aba_sweeps(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr ddq, void* ws, cudaStream_t st,
                       Arr fext = Arr{nullptr, 0, 0}) {
   constexpr bool f64 = std::is_same<K, double>::value, vjp = std::is_same<P, gb::dfloat>::value;
-  const SweepCall c{f64 ? kSweepFp64 : vjp ? kSweepMixedVjp : kSweepMixed, M, B, q, v, tau, ddq, ws, st, fext};
+  constexpr bool df = std::is_same<S, gb::dfloat>::value;  // double-float column sets (deep trees)
+  const SweepCall c{f64 ? kSweepFp64 : df ? kSweepMixedDf : vjp ? kSweepMixedVjp : kSweepMixed, M, B, q, v, tau, ddq,
+                    ws, st, fext};
   return fext.p ? sweeps_t1(c) : sweeps_team(c);
 }
 
@@ -695,6 +697,13 @@ int run_aba_derivs(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr
   return launch_aba_derivs_ws<S, T3, T, K, SS, P>(M, B, q, v, tau, dq, dv, Minv, ddq, ws.p, st, fext);
 }
 
+// The mixed derivative sweeps keep the column sets and dtau in double-float on trees deeper
+// than this: the conditioning of their mass matrix grows with the depth and amplifies the
+// FP32 rounding of the column sets past the 1e-5 bar (measured: the 100-link chain at 2.9e-4
+// with FP32 column sets; the 32-dof humanoid, depth 9, at 9e-6).
+constexpr int kMixedDfDepth = 32;
+bool mixed_df(const gb_model* M) { return M->max_depth > kMixedDfDepth; }
+
 int check_gravity(const gb_model* M) {
   if (M->gravity[3] != 0.0 || M->gravity[4] != 0.0 || M->gravity[5] != 0.0)
     return set_error(GB_ERR_GRAVITY, "The gravity must be a pure force vector, no angular part");
@@ -734,8 +743,9 @@ int sweeps_team(const SweepCall& c) {
 // total bytes needed for a batch, and the launch itself.
 size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B) {
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
-  return precision == GB_FP64 ? aba_ws_layout<double, double, double, double>(L, M->nv, B).bytes
-                              : aba_ws_layout<float, gb::dfloat, double, float>(L, M->nv, B).bytes;
+  if (precision == GB_FP64) return aba_ws_layout<double, double, double, double>(L, M->nv, B).bytes;
+  if (mixed_df(M)) return aba_ws_layout<gb::dfloat, gb::dfloat, double, gb::dfloat>(L, M->nv, B).bytes;
+  return aba_ws_layout<float, gb::dfloat, double, float>(L, M->nv, B).bytes;
 }
 
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
@@ -744,6 +754,9 @@ int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr
   if (precision == GB_FP64)
     return launch_aba_derivs_ws<double, double, double, double, double, double>(M, B, q, v, tau, dq, dv, Minv, ddq,
                                                                                 ws, st);
+  if (mixed_df(M))
+    return launch_aba_derivs_ws<gb::dfloat, gb::dfloat, gb::dfloat, gb::dfloat, double, gb::dfloat>(
+        M, B, q, v, tau, dq, dv, Minv, ddq, ws, st);
   return launch_aba_derivs_ws<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, q, v, tau, dq, dv, Minv, ddq,
                                                                                   ws, st);
 }
@@ -827,6 +840,9 @@ int aba_derivs_entry(const gb_model* M, int precision, int layout, long B, const
   if (precision == GB_FP64)
     return gbi::run_aba_derivs<double, double, double, double, double, double>(M, B, Aq, Av, At, Adq, Adv, AMi, Add,
                                                                                st, Af);
+  if (gbi::mixed_df(M))
+    return gbi::run_aba_derivs<gb::dfloat, gb::dfloat, gb::dfloat, gb::dfloat, double, gb::dfloat>(
+        M, B, Aq, Av, At, Adq, Adv, AMi, Add, st, Af);
   return gbi::run_aba_derivs<float, float, gb::dfloat, gb::dfloat, double, float>(M, B, Aq, Av, At, Adq, Adv, AMi,
                                                                                  Add, st, Af);
 }
@@ -895,6 +911,9 @@ int gb_aba_derivatives_vjp(const gb_model* M, int precision, int layout, long B,
     return gbi::run_aba_vjp<double, double, double, double, double, double>(M, B, Aq, Av, At, Ag, Aqb, Avb, Atb, Add,
                                                                             st);
   // dtau kept in double-float: a projection g^T ddq_dq cancels more than the Jacobian entries do
+  if (gbi::mixed_df(M))
+    return gbi::run_aba_vjp<gb::dfloat, gb::dfloat, gb::dfloat, gb::dfloat, double, gb::dfloat>(
+        M, B, Aq, Av, At, Ag, Aqb, Avb, Atb, Add, st);
   return gbi::run_aba_vjp<float, float, gb::dfloat, gb::dfloat, double, gb::dfloat>(M, B, Aq, Av, At, Ag, Aqb, Avb,
                                                                                    Atb, Add, st);
 }

@@ -44,7 +44,9 @@ struct BlobHeader {
   int o_chain, nchain, nclevel, chain_team;
   // o_status: the model's numeric status word (GB_NUMERIC_* bits, atomicOr from the kernels), in
   // global memory beyond the staged prefix
-  int o_status, pad_status[3];
+  int o_status;
+  int o_child, max_child;  // children of each joint, from the last one down (max_child per joint, -1 padded)
+  int pad_status;
   double grav_d[6];
   float grav_f[6];
   float padf[2];
@@ -63,6 +65,8 @@ struct MView {
   const dfloat *place_df, *iner_df, *arm_df, *grav_df;
   const double* fix_d;  // nullptr when no joint is unaligned
   unsigned* status;     // the status word in the global copy of the blob (nullptr: not recorded)
+  const int* child;     // max_child entries per joint: its children from the last one down, -1 padded
+  int max_child;
 };
 
 // Numeric failures seen by a kernel (bits of the model's status word, read by gb_numeric_status):
@@ -126,6 +130,8 @@ GB_HD MView make_view(const unsigned char* base) {
   m.grav_df = h->grav_df;
   m.fix_d = h->o_fix ? reinterpret_cast<const double*>(base + h->o_fix) : nullptr;
   m.status = nullptr;
+  m.child = reinterpret_cast<const int*>(base + h->o_child);
+  m.max_child = h->max_child;
   m.grav_d = h->grav_d;
   m.grav_f = h->grav_f;
   return m;

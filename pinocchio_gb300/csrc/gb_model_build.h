@@ -254,6 +254,16 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
     M->chain_team = ts;
   }
   h.o_chain = take(4 * chain.size() + 4);
+  // children of each joint from the last one down (the order the RNEA backward sweep folds them)
+  std::vector<std::vector<int>> kids(nj);
+  for (int i = nj - 1; i >= 1; --i) kids[M->parents[i]].push_back(i);
+  int maxc = 1;
+  for (int i = 0; i < nj; ++i) maxc = std::max(maxc, (int)kids[i].size());
+  std::vector<int> child((size_t)nj * maxc, -1);
+  for (int i = 0; i < nj; ++i)
+    for (size_t k = 0; k < kids[i].size(); ++k) child[(size_t)i * maxc + k] = kids[i][k];
+  h.max_child = maxc;
+  h.o_child = take(4 * child.size());
   // column groups of the -Minv*dtau products (filled below)
   std::vector<int> grp, grp_rel;
   for (int c = 0; c < nv;) {
@@ -311,6 +321,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   std::memcpy(b, &h, sizeof(h));
   put_i(h.o_bslot, bslot);
   put_i(h.o_chain, chain);
+  put_i(h.o_child, child);
   put_i(h.o_grp, grp);
   put_i(h.o_grp_rel, grp_rel);
   put_d(h.o_place_d, M->placement); put_d(h.o_iner_d, M->inertia); put_d(h.o_arm_d, M->armature);

@@ -14,7 +14,9 @@
 namespace gbi {
 
 // One sweep launch: what to run (precision and variant), on which workspace.
-enum SweepKind { kSweepFp64, kSweepMixed, kSweepMixedVjp, kMinvFp64, kMinvMixed };
+// kSweepMixedDf: the mixed sweeps with the column sets, pass 3's arithmetic and dtau in
+// double-float (deep trees, whose mass-matrix conditioning amplifies FP32 rounding)
+enum SweepKind { kSweepFp64, kSweepMixed, kSweepMixedVjp, kSweepMixedDf, kMinvFp64, kMinvMixed };
 struct SweepCall {
   SweepKind kind;
   const gb_model* M;
@@ -248,6 +250,7 @@ int sweeps_for(const SweepCall& c) {
     if constexpr (TS == 1) {
       if (c.kind == kSweepFp64) return aba_sweeps_on<double, double, double, double, double, double, 1, true>(c);
       if (c.kind == kSweepMixed) return aba_sweeps_on<float, float, dfloat, dfloat, double, float, 1, true>(c);
+      if (c.kind == kSweepMixedDf) return aba_sweeps_on<dfloat, dfloat, dfloat, dfloat, double, dfloat, 1, true>(c);
     }
     return set_error(GB_ERR_INVALID_ARGUMENT, "external forces: unsupported sweep variant");
   }
@@ -255,6 +258,7 @@ int sweeps_for(const SweepCall& c) {
     case kSweepFp64: return aba_sweeps_on<double, double, double, double, double, double, TS>(c);
     case kSweepMixed: return aba_sweeps_on<float, float, dfloat, dfloat, double, float, TS>(c);
     case kSweepMixedVjp: return aba_sweeps_on<float, float, dfloat, dfloat, double, dfloat, TS>(c);
+    case kSweepMixedDf: return aba_sweeps_on<dfloat, dfloat, dfloat, dfloat, double, dfloat, TS>(c);
     case kMinvFp64: return minverse_sweeps_on<double, double, TS>(c);
     case kMinvMixed: return minverse_sweeps_on<dfloat, double, TS>(c);
   }

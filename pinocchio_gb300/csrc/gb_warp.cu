@@ -12,6 +12,10 @@ namespace {
 using namespace warp;
 
 constexpr int kWarpThreads = 256;  // 8 instances per CTA at most
+// the RNEA warp layout gathers children's forces by warp shuffles (1) or shared memory (0)
+#ifndef GB_WARP_SHFL
+#define GB_WARP_SHFL 0
+#endif
 
 __device__ __forceinline__ gb::MView stage_blob(const unsigned char* __restrict__ blob, int bytes,
                                                 unsigned char* smem) {
@@ -24,7 +28,7 @@ __device__ __forceinline__ gb::MView stage_blob(const unsigned char* __restrict_
   return m;
 }
 
-template <class S>
+template <class S, bool SHFL>
 __global__ void __launch_bounds__(kWarpThreads) k_rnea_warp(const unsigned char* blob, int bytes, long B, Arr q,
                                                              Arr v, Arr a, Arr tau) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -32,7 +36,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_rnea_warp(const unsigned char*
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   S* ws = reinterpret_cast<S*>(smem + align16(bytes)) + (long)warp * rnea_words<S>() * m.nj;
   for (long b = (long)blockIdx.x * nw + warp; b < B; b += (long)gridDim.x * nw) {
-    rnea_warp_one<S>(m, w_in(q, b), w_in(v, b), w_in(a, b), w_out(tau, b), ws, LevelSched{lane});
+    rnea_warp_one<S, LevelSched, SHFL>(m, w_in(q, b), w_in(v, b), w_in(a, b), w_out(tau, b), ws, LevelSched{lane});
     __syncwarp();
   }
 }
@@ -153,10 +157,13 @@ int launch_rnea_warp_t(const gb_model* M, long B, Arr q, Arr v, Arr a, Arr tau, 
   int nw;
   size_t smem;
   const size_t per_warp = rnea_warp_bytes<S>(M->nj);
-  int rc = warp_launch_shape(M, per_warp, k_rnea_warp<S>, "k_rnea_warp", &nw, &smem);
+  const bool shfl = GB_WARP_SHFL && M->nj - 1 <= 32;  // one joint per lane
+  int rc = shfl ? warp_launch_shape(M, per_warp, k_rnea_warp<S, true>, "k_rnea_warp", &nw, &smem)
+                : warp_launch_shape(M, per_warp, k_rnea_warp<S, false>, "k_rnea_warp", &nw, &smem);
   if (rc != GB_OK) return rc;
   const long grid = std::min<long>((B + nw - 1) / nw, (long)M->sm_count * 16);
-  k_rnea_warp<S><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, a, tau);
+  if (shfl) k_rnea_warp<S, true><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, a, tau);
+  else k_rnea_warp<S, false><<<(unsigned)grid, 32 * nw, smem, st>>>(M->d_blob, M->stage_bytes, B, q, v, a, tau);
   return cuda_error(cudaGetLastError(), "k_rnea_warp");
 }
 

@@ -68,7 +68,10 @@ template <int TS> struct BranchSched {
 // shared-memory scalars per joint of one warp's region
 template <class S> constexpr int rnea_words() { return 12 + 6 * 4; }  // X, vel, acc, f, child force
 
-template <class S, class Sched>
+// SHFL (one joint per lane, nj - 1 <= 32, LevelSched): the backward sweep gathers the
+// children's forces with warp shuffles from the lanes that computed them (kept in registers)
+// instead of through shared memory; same children, same order, same bits.
+template <class S, class Sched, bool SHFL = false>
 __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In& v, const gb::In& a,
                               const gb::Out& tau, S* ws, const Sched& sc) {
   using namespace gb;
@@ -115,6 +118,44 @@ __device__ void rnea_warp_one(const gb::MView& m, const gb::In& q, const gb::In&
       acc[i] = ai;
     });
     sc.sync();
+  }
+  if constexpr (SHFL) {
+    const int i = sc.lane + 1;
+    M6<S> mine;  // the joint's force moved to its parent, valid after its level
+#pragma unroll
+    for (int k = 0; k < 6; ++k) mine.v[k] = S(0);
+    for (int d = sc.steps(m); d >= 1; --d) {
+      const bool active = i < nj && m.depth[i] == d;
+      M6<S> fi;
+      if (active) fi = f[i];
+      for (int s = 0; s < m.max_child; ++s) {  // warp-uniform: every lane takes part in the shuffles
+        const int c = active ? m.child[i * m.max_child + s] : -1;
+        const int src = c > 0 ? c - 1 : sc.lane;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          const S x = __shfl_sync(0xffffffffu, mine.v[k], src);
+          if (c > 0) fi.v[k] += x;
+        }
+      }
+      if (active) {
+        const int p = m.parent[i], jt = m.jtype[i], iv = m.idx_v[i];
+        if (jt == JT_FF) {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            const double t = double(fi.v[k] + arm[iv + k] * S(a[iv + k]));
+            if (!gb::finite_value(t)) gb::flag_numeric(m, gb::NUM_NONFINITE);
+            tau[iv + k] = t;
+          }
+        } else {
+          const double t = double(pick6(fi.v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
+          if (!gb::finite_value(t)) gb::flag_numeric(m, gb::NUM_NONFINITE);
+          tau[iv] = t;
+        }
+        if (p > 0) act_force(X[i], fi, mine);
+      }
+      __syncwarp();
+    }
+    return;
   }
   for (int d = sc.steps(m); d >= 1; --d) {  // backward: children folded in by decreasing index
     sc.up(m, d, [&](int i) {
