@@ -48,7 +48,11 @@ enum { GB_LAYOUT_INSTANCE = 0, GB_LAYOUT_SOA = 1 };
  * the free-flyer (JointModelFreeFlyer, joint-free-flyer.hpp; root joint only), prismatic along
  * x / y / z (JointModelPX/PY/PZ, joint-prismatic.hpp), revolute about / prismatic along a unit
  * axis of the joint frame (JointModelRevoluteUnaligned, joint-revolute-unaligned.hpp;
- * JointModelPrismaticUnaligned, joint-prismatic-unaligned.hpp) given by gb_model_desc.axis */
+ * JointModelPrismaticUnaligned, joint-prismatic-unaligned.hpp) given by gb_model_desc.axis,
+ * translation (JointModelTranslation, joint-translation.hpp: nq = nv = 3, anywhere in the tree;
+ * the kernels run it as three prismatic joints along x, y, z with identity placements, which
+ * is the same transform, joint velocity and configuration space).  Per-joint arrays (external
+ * forces, forward-kinematics outputs) are indexed by the caller's joints. */
 enum {
   GB_JOINT_NONE = 0,
   GB_JOINT_RX = 1,
@@ -59,7 +63,10 @@ enum {
   GB_JOINT_PY = 6,
   GB_JOINT_PZ = 7,
   GB_JOINT_REVOLUTE_UNALIGNED = 8,
-  GB_JOINT_PRISMATIC_UNALIGNED = 9
+  GB_JOINT_PRISMATIC_UNALIGNED = 9,
+  GB_JOINT_TRANSLATION = 10, /* JointModelTranslation (joint-translation.hpp): q = v in R^3 */
+  GB_JOINT_SPHERICAL = 11,   /* JointModelSpherical (joint-spherical.hpp): not supported yet */
+  GB_JOINT_PLANAR = 12       /* JointModelPlanar (joint-planar.hpp): not supported yet */
 };
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
 /* functions of a heterogeneous batch task / of a launch setting */

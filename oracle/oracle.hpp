@@ -38,7 +38,10 @@ namespace orc {
 enum JointType {
   JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7,
   JT_RU = 8,  // JointModelRevoluteUnaligned (multibody/joint/joint-revolute-unaligned.hpp)
-  JT_PU = 9   // JointModelPrismaticUnaligned (multibody/joint/joint-prismatic-unaligned.hpp)
+  JT_PU = 9,  // JointModelPrismaticUnaligned (multibody/joint/joint-prismatic-unaligned.hpp)
+  JT_TR = 10,   // JointModelTranslation (multibody/joint/joint-translation.hpp): nq = nv = 3
+  JT_SPH = 11,  // JointModelSpherical (multibody/joint/joint-spherical.hpp): quaternion, nq 4, nv 3
+  JT_PL = 12    // JointModelPlanar (multibody/joint/joint-planar.hpp): (x, y, cos, sin), nq 4, nv 3
 };
 enum Convention { LOCAL = 0, WORLD = 1 };  // reference multibody/fwd.hpp:73-81
 
@@ -68,8 +71,10 @@ struct Model {
   // derived tables (multibody/data.hxx:195-306)
   std::vector<int> lastChild, nvSubtree, parents_fromRow, nvSubtree_fromRow;
 
-  static int joint_nq(int jt) { return jt == JT_FF ? 7 : (jt == JT_NONE ? 0 : 1); }
-  static int joint_nv(int jt) { return jt == JT_FF ? 6 : (jt == JT_NONE ? 0 : 1); }
+  static int joint_nq(int jt) {
+    return jt == JT_FF ? 7 : jt == JT_NONE ? 0 : jt == JT_TR ? 3 : (jt == JT_SPH || jt == JT_PL) ? 4 : 1;
+  }
+  static int joint_nv(int jt) { return jt == JT_FF ? 6 : jt == JT_NONE ? 0 : jt >= JT_TR ? 3 : 1; }
 
   // Validates the description and fills the derived tables.
   // lastChild / nvSubtree: data.hxx:195-225 (no mimic joints).
@@ -86,7 +91,7 @@ struct Model {
         if (jtype[0] != JT_NONE) throw std::invalid_argument("joint 0 must be the universe");
         continue;
       }
-      if (jtype[i] < JT_RX || jtype[i] > JT_PU) throw std::invalid_argument("unsupported joint type");
+      if (jtype[i] < JT_RX || jtype[i] > JT_PL) throw std::invalid_argument("unsupported joint type");
       if (jtype[i] == JT_RU || jtype[i] == JT_PU) {
         if ((int)axis.size() != 3 * njoints) throw std::invalid_argument("unaligned joints need the axis table");
         const double n = std::sqrt(axis[3 * i] * axis[3 * i] + axis[3 * i + 1] * axis[3 * i + 1] +
@@ -548,10 +553,39 @@ template <class T> inline Iner<T> inertia_of(const Model& m, int i) {
 //    (TransformPrismaticTpl, joint-prismatic.hpp:232-284; calc at 700-704).
 //  * free-flyer: translation q[0:3], rotation = Eigen Quaternion::matrix()
 //    of (x,y,z,w) = q[3:7], not normalised (joint-free-flyer.hpp:333-375).
+//  * translation: (I, q[0:3]) (TransformTranslationTpl, joint-translation.hpp; calc);
+//  * spherical: rotation = Quaternion::matrix() of q[0:4] = (x,y,z,w), no translation
+//    (joint-spherical.hpp:504-531);
+//  * planar: rotation about z with (cos, sin) = q[2:4], translation (q[0], q[1], 0)
+//    (joint-planar.hpp:586-609).
+template <class T> inline void quat_rotation(const T* qv, T* R) {
+  const T x = qv[0], y = qv[1], z = qv[2], w = qv[3];
+  const T tx = T(2) * x, ty = T(2) * y, tz = T(2) * z;
+  const T twx = tx * w, twy = ty * w, twz = tz * w;
+  const T txx = tx * x, txy = ty * x, txz = tz * x;
+  const T tyy = ty * y, tyz = tz * y, tzz = tz * z;
+  R[0] = T(1) - (tyy + tzz); R[1] = txy - twz; R[2] = txz + twy;
+  R[3] = txy + twz; R[4] = T(1) - (txx + tzz); R[5] = tyz - twx;
+  R[6] = txz - twy; R[7] = tyz + twx; R[8] = T(1) - (txx + tyy);
+}
 template <class T> inline SE3<T> joint_transform(int jt, const T* q) {
   SE3<T> M;
   for (int k = 0; k < 9; ++k) M.R[k] = T(0);
   for (int k = 0; k < 3; ++k) M.t[k] = T(0);
+  if (jt == JT_TR) {
+    for (int k = 0; k < 3; ++k) { M.R[4 * k] = T(1); M.t[k] = q[k]; }
+    return M;
+  }
+  if (jt == JT_SPH) {
+    quat_rotation(q, M.R);
+    return M;
+  }
+  if (jt == JT_PL) {
+    const T c = q[2], s = q[3];
+    M.R[0] = c; M.R[1] = -s; M.R[3] = s; M.R[4] = c; M.R[8] = T(1);
+    M.t[0] = q[0]; M.t[1] = q[1];
+    return M;
+  }
   if (jt == JT_FF) {
     const T x = q[3], y = q[4], z = q[5], w = q[6];
     const T tx = T(2) * x, ty = T(2) * y, tz = T(2) * z;
@@ -581,9 +615,15 @@ template <class T> inline SE3<T> joint_transform(int jt, const T* q) {
 // linear axis a of a prismatic one (SpatialAxis<LINEAR + axis>, joint-prismatic.hpp:353-461).
 inline int motion_index(int jt) { return jt >= JT_PX ? jt - JT_PX : 3 + (jt - JT_RX); }
 // Column k of the joint motion subspace S (local frame).
+// The three-dof joints have unit columns too: translation the linear axes
+// (JointMotionSubspaceTranslationTpl), spherical the angular axes
+// (JointMotionSubspaceSphericalTpl), planar (vx, vy, wz) (JointMotionSubspacePlanarTpl,
+// joint-planar.hpp:380-470); multi_col gives the spatial index of column k.
+inline int multi_col(int jt, int k) { return jt == JT_TR ? k : jt == JT_SPH ? 3 + k : (k < 2 ? k : 5); }
 template <class T> inline Vec6<T> S_col(int jt, int k) {
   Vec6<T> s = zero6<T>();
   if (jt == JT_FF) s.v[k] = T(1);
+  else if (jt >= JT_TR) s.v[multi_col(jt, k)] = T(1);
   else s.v[motion_index(jt)] = T(1);
   return s;
 }
@@ -591,6 +631,7 @@ template <class T> inline Vec6<T> S_col(int jt, int k) {
 template <class T> inline Vec6<T> joint_velocity(int jt, const T* v) {
   Vec6<T> o = zero6<T>();
   if (jt == JT_FF) for (int k = 0; k < 6; ++k) o.v[k] = v[k];
+  else if (jt >= JT_TR) for (int k = 0; k < 3; ++k) o.v[multi_col(jt, k)] = v[k];
   else o.v[motion_index(jt)] = v[0];
   return o;
 }
@@ -788,6 +829,31 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau,
           for (int c = 0; c < 6; ++c) {
             T s = UDinv[6 * r] * U[6 * c];
             for (int k = 1; k < 6; ++k) s += UDinv[6 * r + k] * U[6 * c + k];
+            Ia.a[6 * r + c] -= s;
+          }
+    } else if (jt >= JT_TR) {  // calc_aba of the three-dof joints with unit columns (translation
+                               // joint-translation.hpp, spherical joint-spherical.hpp:572-586, planar
+                               // joint-planar.hpp:643-661): U = I S, StU = S^T U + armature, LLT inverse
+      int cols[3];
+      for (int k = 0; k < 3; ++k) cols[k] = multi_col(jt, k);
+      T StU[9];
+      for (int r = 0; r < 6; ++r)
+        for (int k = 0; k < 3; ++k) U[r * 3 + k] = Ia.a[6 * r + cols[k]];
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) StU[3 * r + c] = U[cols[r] * 3 + c];
+      for (int k = 0; k < 3; ++k) StU[4 * k] += T(m.armature[iv + k]);
+      llt_inverse(3, StU, Dinv.data());
+      for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 3; ++c) {
+          T s = U[r * 3] * Dinv[c];
+          for (int k = 1; k < 3; ++k) s += U[r * 3 + k] * Dinv[3 * k + c];
+          UDinv[r * 3 + c] = s;
+        }
+      if (p > 0)
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c) {
+            T s = UDinv[r * 3] * U[c * 3];
+            for (int k = 1; k < 3; ++k) s += UDinv[r * 3 + k] * U[c * 3 + k];
             Ia.a[6 * r + c] -= s;
           }
     } else if (unaligned(jt)) {  // calc_aba of joint-revolute-unaligned.hpp:695-707 /
@@ -1566,11 +1632,72 @@ void joint_jacobians(const Model& m, Data<T>& d, const T* q) {
 // spatial/explog-quaternion.hpp:20-147, math/quaternion.hpp:90-111); revolute
 // and prismatic joints are a vector space (q + v).
 // ---------------------------------------------------------------------------
+// exp3 of an angular velocity as a quaternion (x, y, z, w) (spatial/explog-quaternion.hpp:20-60)
+template <class T> void exp3_quat(const T* w, T* e) {
+  const T eps = o_eps<T>();
+  const T ts_prec = T(std::pow((double)eps, 1.0 / 4.0));
+  const T s2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  const T th = o_sqrt(s2 + eps * eps);
+  if (s2 > ts_prec) {  // AngleAxis(th, w/th) -> quaternion
+    T sh, ch;
+    o_sincos(T(0.5) * th, &sh, &ch);
+    for (int k = 0; k < 3; ++k) e[k] = sh * (w[k] / th);
+    e[3] = ch;
+  } else {
+    const T t2_2 = s2 / T(4);
+    const T c = T(0.5) * (T(1) - t2_2 / T(6) + t2_2 * t2_2 / T(120));
+    for (int k = 0; k < 3; ++k) e[k] = c * w[k];
+    e[3] = T(1) - t2_2 / T(2) + t2_2 * t2_2 / T(24);
+  }
+}
+// SO(3): quat * exp3(v), first-order normalised (liegroup/special-orthogonal.hpp:467-481,
+// math/quaternion.hpp:90-111)
+template <class T> void integrate_so3(const T* qq, const T* w, T* out) {
+  T e[4];
+  exp3_quat(w, e);
+  T r[4];
+  r[3] = qq[3] * e[3] - qq[0] * e[0] - qq[1] * e[1] - qq[2] * e[2];
+  r[0] = qq[3] * e[0] + qq[0] * e[3] + qq[1] * e[2] - qq[2] * e[1];
+  r[1] = qq[3] * e[1] + qq[1] * e[3] + qq[2] * e[0] - qq[0] * e[2];
+  r[2] = qq[3] * e[2] + qq[2] * e[3] + qq[0] * e[1] - qq[1] * e[0];
+  const T N2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+  const T alpha = (T(3) - N2) / T(2);
+  for (int k = 0; k < 4; ++k) out[k] = r[k] * alpha;
+}
+// SE(2) on (x, y, cos, sin): exp of (vx, vy, w) in the body frame composed on the right
+// (liegroup/special-euclidean.hpp:61-90, 289-306)
+template <class T> void integrate_se2(const T* q, const T* v, T* out) {
+  const T c0 = q[2], s0 = q[3];
+  T sv, cv;
+  o_sincos(v[2], &sv, &cv);
+  T t[2];
+  const T vc0 = -v[1] - (-v[1] * cv + v[0] * (-sv)), vc1 = v[0] - (-v[1] * sv + v[0] * cv);
+  const T aw = v[2] < T(0) ? -v[2] : v[2];
+  if (aw > T(1e-14)) { t[0] = vc0 / v[2]; t[1] = vc1 / v[2]; }
+  else { t[0] = v[0]; t[1] = v[1]; }
+  out[0] = c0 * t[0] - s0 * t[1] + q[0];
+  out[1] = s0 * t[0] + c0 * t[1] + q[1];
+  out[2] = c0 * cv - s0 * sv;
+  out[3] = s0 * cv + c0 * sv;
+}
+
 template <class T>
 void integrate(const Model& m, const T* q, const T* v, T* qout) {
   for (int i = 1; i < m.njoints; ++i) {
-    const int iq = m.idx_q[i], iv = m.idx_v[i];
-    if (m.jtype[i] != JT_FF) {
+    const int iq = m.idx_q[i], iv = m.idx_v[i], jt = m.jtype[i];
+    if (jt == JT_TR) {
+      for (int k = 0; k < 3; ++k) qout[iq + k] = q[iq + k] + v[iv + k];
+      continue;
+    }
+    if (jt == JT_SPH) {
+      integrate_so3(q + iq, v + iv, qout + iq);
+      continue;
+    }
+    if (jt == JT_PL) {
+      integrate_se2(q + iq, v + iv, qout + iq);
+      continue;
+    }
+    if (jt != JT_FF) {
       qout[iq] = q[iq] + v[iv];
       continue;
     }

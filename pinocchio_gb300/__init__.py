@@ -9,6 +9,7 @@ from .model import (  # noqa: F401
     Convention,
     Inertia,
     JointModelFreeFlyer,
+    JointModelPlanar,
     JointModelPrismaticUnaligned,
     JointModelPX,
     JointModelPY,
@@ -17,6 +18,8 @@ from .model import (  # noqa: F401
     JointModelRX,
     JointModelRY,
     JointModelRZ,
+    JointModelSpherical,
+    JointModelTranslation,
     Model,
     SE3,
 )

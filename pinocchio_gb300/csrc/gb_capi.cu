@@ -107,7 +107,7 @@ int gb_model_dims(const gb_model* M, int* nq, int* nv, int* nj) {
   if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
   if (nq) *nq = M->nq;
   if (nv) *nv = M->nv;
-  if (nj) *nj = M->nj;
+  if (nj) *nj = M->nj_user;
   return GB_OK;
 }
 
@@ -134,7 +134,7 @@ int gb_rnea_fext(const gb_model* M, int precision, int layout, long B, const dou
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(a, "a"));
   GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(tau, "tau"));
   return gbi::launch_rnea_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
-                               gbi::arr(a, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj),
+                               gbi::arr(a, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj_user),
                                gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
 }
 
@@ -170,7 +170,7 @@ int gb_static_torque(const gb_model* M, int precision, int layout, long B, const
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(tau, "tau"));
   return gbi::launch_rnea_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), zero_arr(M), zero_arr(M),
-                               gbi::arr(fext, layout, B, 6L * M->nj), gbi::arr(tau, layout, B, M->nv),
+                               gbi::arr(fext, layout, B, 6L * M->nj_user), gbi::arr(tau, layout, B, M->nv),
                                (cudaStream_t)stream);
 }
 
@@ -240,7 +240,7 @@ int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, 
   if (a) GB_TRY(gbi::check_ptr(a, "a"));
   if (vout) GB_TRY(gbi::check_ptr(vout, "v output"));
   if (aout) GB_TRY(gbi::check_ptr(aout, "a output"));
-  const long nj = M->nj;
+  const long nj = M->nj_user;
   return gbi::launch_fk(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
                         gbi::arr(a, layout, B, M->nv), gbi::arr(oMi, layout, B, 12 * nj),
                         gbi::arr(vout, layout, B, 6 * nj), gbi::arr(aout, layout, B, 6 * nj), (cudaStream_t)stream);
@@ -274,7 +274,7 @@ int gb_aba_fext(const gb_model* M, int precision, int convention, int layout, lo
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
   GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(ddq, "ddq"));
   return gbi::launch_aba_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
-                              gbi::arr(tau, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj),
+                              gbi::arr(tau, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj_user),
                               gbi::arr(ddq, layout, B, M->nv), (cudaStream_t)stream);
 }
 

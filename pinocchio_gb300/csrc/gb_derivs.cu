@@ -812,7 +812,7 @@ int rnea_derivs_entry(const gb_model* M, int precision, int matrix_mode, int lay
   const bool sym = matrix_mode == GB_MATRIX_SYMMETRIC;
   cudaStream_t st = (cudaStream_t)stream;
   if (fext) {
-    const gbi::Arr Af = arr(fext, layout, B, 6L * M->nj);
+    const gbi::Arr Af = arr(fext, layout, B, 6L * M->nj_user);
     if (precision == GB_FP64) return gbi::run_rnea_derivs<double, true>(M, B, sym, Aq, Av, Aa, Adq, Adv, AM, At, st, Af);
     return gbi::run_rnea_derivs<float, true>(M, B, sym, Aq, Av, Aa, Adq, Adv, AM, At, st, Af);
   }
@@ -835,7 +835,7 @@ int aba_derivs_entry(const gb_model* M, int precision, int layout, long B, const
   const gbi::Arr Aq = arr(q, layout, B, M->nq), Av = arr(v, layout, B, M->nv), At = arr(tau, layout, B, M->nv);
   const gbi::Arr Adq = arr(ddq_dq, layout, B, nn), Adv = arr(ddq_dv, layout, B, nn), AMi = arr(Minv, layout, B, nn);
   const gbi::Arr Add = arr(ddq, layout, B, M->nv);
-  const gbi::Arr Af = fext ? arr(fext, layout, B, 6L * M->nj) : gbi::Arr{nullptr, 0, 0};
+  const gbi::Arr Af = fext ? arr(fext, layout, B, 6L * M->nj_user) : gbi::Arr{nullptr, 0, 0};
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == GB_FP64)
     return gbi::run_aba_derivs<double, double, double, double, double, double>(M, B, Aq, Av, At, Adq, Adv, AMi, Add,

@@ -157,10 +157,18 @@ template <class S> GB_HD void joint_motion(int jt, const In& x, int iv, M6<S>& o
 // holds njoints x 6 values per configuration, joint 0's are not read.  Inside the
 // kernels an unaligned joint's frame is the joint frame turned by F (a rotation
 // about the same origin, folded in at model build): f' = F^T f.
+// The forces are per caller joint: an intermediate joint of an expanded translation joint
+// takes none, the last one the caller joint's.
 template <class S> GB_HD void load_fext(const MView& m, const In& fe, int i, S* f) {
+  const int u = m.ujoint[i];
+  if (u < 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[k] = S(0);
+    return;
+  }
   if (!m.fix_d) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) f[k] = S(fe[6 * i + k]);
+    for (int k = 0; k < 6; ++k) f[k] = S(fe[6 * u + k]);
     return;
   }
   const double* F = m.fix_d + 9 * i;
@@ -168,7 +176,7 @@ template <class S> GB_HD void load_fext(const MView& m, const In& fe, int i, S* 
   for (int h = 0; h < 6; h += 3)
 #pragma unroll
     for (int r = 0; r < 3; ++r)
-      f[h + r] = S(F[r] * fe[6 * i + h] + F[3 + r] * fe[6 * i + h + 1] + F[6 + r] * fe[6 * i + h + 2]);
+      f[h + r] = S(F[r] * fe[6 * u + h] + F[3 + r] * fe[6 * u + h + 1] + F[6 + r] * fe[6 * u + h + 2]);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -580,6 +588,17 @@ GB_HD void store_placement(const Out& o, int i, const X3<S>& X) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) o[12 * i + 9 + k] = double(X.t[k]);
 }
+template <class S> GB_HD void store_placement_fixed(const MView& m, const Out& o, int i, const X3<S>& X);
+template <class S> GB_HD void store_motion_fixed(const MView& m, const Out& o, int i, const M6<S>& x);
+// the joint-i output written at slot u of the caller's joints
+template <class S>
+GB_HD void store_placement_fixed_at(const MView& m, const Out& o, int i, int u, const X3<S>& X) {
+  store_placement_fixed(m, Out{o.p + (long)12 * (u - i) * o.es, o.es}, i, X);
+}
+template <class S>
+GB_HD void store_motion_fixed_at(const MView& m, const Out& o, int i, int u, const M6<S>& x) {
+  store_motion_fixed(m, Out{o.p + (long)6 * (u - i) * o.es, o.es}, i, x);
+}
 // The frame of an unaligned joint i is frame_i F_i inside the kernels (the model
 // build folds the axis into the placements): the outputs map back with
 // oMi = oMi' F^T and a joint-frame motion m = F m'.
@@ -638,7 +657,8 @@ GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const O
     joint_transform(m, i, q, X);
     if (p > 0) compose(oM[p], X, oM[i]);
     else oM[i] = X;
-    store_placement_fixed(m, oMi, i, oM[i]);
+    const int u = m.ujoint[i];  // outputs per caller joint (-1: inside an expanded translation joint)
+    if (u > 0) store_placement_fixed_at(m, oMi, i, u, oM[i]);
     if (!v) continue;
     M6<S> vJ, t;
     joint_motion(jt, *v, iv, vJ);
@@ -649,7 +669,7 @@ GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const O
     } else {
       vel[i] = vJ;
     }
-    store_motion_fixed(m, *vo, i, vel[i]);
+    if (u > 0) store_motion_fixed_at(m, *vo, i, u, vel[i]);
     if (!a) continue;
     M6<S> aJ, ap;
     joint_motion(jt, *a, iv, aJ);
@@ -657,7 +677,7 @@ GB_HD void fk_one(const MView& m, const In& q, const In* v, const In* a, const O
     if (p > 0) actinv_motion(X, acc[p], ap);
 #pragma unroll
     for (int k = 0; k < 6; ++k) acc[i].v[k] = p > 0 ? (aJ.v[k] + t.v[k]) + ap.v[k] : aJ.v[k] + t.v[k];
-    store_motion_fixed(m, *ao, i, acc[i]);
+    if (u > 0) store_motion_fixed_at(m, *ao, i, u, acc[i]);
   }
 }
 template <class S, int CAP>

@@ -46,7 +46,7 @@ struct BlobHeader {
   // global memory beyond the staged prefix
   int o_status;
   int o_child, max_child;  // children of each joint, from the last one down (max_child per joint, -1 padded)
-  int pad_status;
+  int o_ujoint;            // per joint: the caller's joint it carries (-1: inside an expanded translation)
   double grav_d[6];
   float grav_f[6];
   float padf[2];
@@ -67,6 +67,7 @@ struct MView {
   unsigned* status;     // the status word in the global copy of the blob (nullptr: not recorded)
   const int* child;     // max_child entries per joint: its children from the last one down, -1 padded
   int max_child;
+  const int* ujoint;    // the caller's joint of each joint (per-joint inputs and outputs), -1: none
 };
 
 // Numeric failures seen by a kernel (bits of the model's status word, read by gb_numeric_status):
@@ -132,6 +133,7 @@ GB_HD MView make_view(const unsigned char* base) {
   m.status = nullptr;
   m.child = reinterpret_cast<const int*>(base + h->o_child);
   m.max_child = h->max_child;
+  m.ujoint = reinterpret_cast<const int*>(base + h->o_ujoint);
   m.grav_d = h->grav_d;
   m.grav_f = h->grav_f;
   return m;

@@ -29,6 +29,10 @@ struct gb_model {
   int blob_bytes = 0;
   int stage_bytes = 0;  // prefix of the blob the per-instance kernels copy into shared memory
   int chain_team = 4;   // lanes per configuration of the lane-per-branch layout
+  // the caller's joints (the reference's model) and, per internal joint, the caller's joint it
+  // carries (-1 for the intermediate joints of an expanded translation joint)
+  int nj_user = 0;
+  std::vector<int> ujoint;
   // the model's device, read once at creation: multiprocessors (grid sizes of the
   // persistent kernels) and the opt-in shared memory per block
   int sm_count = 0, smem_optin = 0;
@@ -120,12 +124,75 @@ inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err)
   return GB_OK;
 }
 
+// Translation joints (JointModelTranslation, reference multibody/joint/joint-translation.hpp:
+// M = (I, q), S = the three linear axes, nq = nv = 3) become three prismatic joints along x,
+// y and z with identity placements between them and the body on the last: the same transform
+// placement * (I, q), the same joint velocity (v, 0) in the same frame, the same q and v, and
+// positive pivots (each prismatic pivot is a translational inertia of the subtree).  The
+// kernels then see only one-dof joints there.  `expanded` is the internal tree; user_of[i] is
+// the caller's joint of internal joint i (-1 for the two intermediate ones), last_of[j] the
+// internal joint carrying the caller's joint j.
+struct ExpandedTree {
+  std::vector<int> parents, jtype, user_of, last_of;
+  std::vector<double> placement, inertia, axis;
+  gb_model_desc desc{};
+};
+inline int expand_translations(const gb_model_desc* d, ExpandedTree& t, std::string* err) {
+  const int nju = d->njoints;
+  t.last_of.assign(nju, 0);
+  static const double kIdentity[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+  static const double kZero[10] = {0};
+  auto push = [&](int parent, int jt, const double* place, const double* iner, const double* ax, int user) {
+    t.parents.push_back(parent);
+    t.jtype.push_back(jt);
+    t.placement.insert(t.placement.end(), place, place + 12);
+    t.inertia.insert(t.inertia.end(), iner, iner + 10);
+    for (int k = 0; k < 3; ++k) t.axis.push_back(ax ? ax[k] : 0.0);
+    t.user_of.push_back(user);
+    return (int)t.parents.size() - 1;
+  };
+  for (int j = 0; j < nju; ++j) {
+    const double* ax = d->axis ? d->axis + 3 * (size_t)j : nullptr;
+    if (j == 0) {
+      t.last_of[0] = push(d->parents[0], d->jtype[0], d->placement, d->inertia, ax, 0);
+      continue;
+    }
+    const int pu = d->parents[j];
+    if (pu < 0 || pu >= j) {
+      *err = "parents[i] must satisfy 0 <= parents[i] < i";
+      return GB_ERR_INVALID_ARGUMENT;
+    }
+    const double* P = d->placement + 12 * (size_t)j;
+    const double* Y = d->inertia + 10 * (size_t)j;
+    if (d->jtype[j] == GB_JOINT_TRANSLATION) {
+      const int a = push(t.last_of[pu], GB_JOINT_PX, P, kZero, nullptr, -1);
+      const int b = push(a, GB_JOINT_PY, kIdentity, kZero, nullptr, -1);
+      t.last_of[j] = push(b, GB_JOINT_PZ, kIdentity, Y, nullptr, j);
+    } else {
+      t.last_of[j] = push(t.last_of[pu], d->jtype[j], P, Y, ax, j);
+    }
+  }
+  t.desc = *d;
+  t.desc.njoints = (int)t.parents.size();
+  t.desc.parents = t.parents.data();
+  t.desc.jtype = t.jtype.data();
+  t.desc.placement = t.placement.data();
+  t.desc.inertia = t.inertia.data();
+  t.desc.axis = d->axis ? t.axis.data() : nullptr;
+  return GB_OK;
+}
+
 // Builds the tree tables of DataTpl (reference multibody/data.hxx:195-306) and
 // the device blob.
-inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
+inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
   auto set_error = [&](int code, const std::string& msg) { *err = msg; return code; };
+  if (du->njoints < 2) return set_error(GB_ERR_SIZE, "model needs at least one joint besides the universe");
+  ExpandedTree tree;
+  if (int rc = expand_translations(du, tree, err)) return rc;
+  const gb_model_desc* d = &tree.desc;
+  M->nj_user = du->njoints;
+  M->ujoint = tree.user_of;
   const int nj = d->njoints;
-  if (nj < 2) return set_error(GB_ERR_SIZE, "model needs at least one joint besides the universe");
   M->nj = nj;
   M->parents.assign(d->parents, d->parents + nj);
   M->jtype.assign(d->jtype, d->jtype + nj);
@@ -141,6 +208,8 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   int nq = 0, nv = 0, nff = 0;
   for (int i = 1; i < nj; ++i) {
     const int jt = M->jtype[i], p = M->parents[i];
+    if (jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR)
+      return set_error(GB_ERR_UNSUPPORTED, "spherical and planar joints are not supported by the batched kernels");
     if (jt < GB_JOINT_RX || jt > GB_JOINT_PRISMATIC_UNALIGNED)
       return set_error(GB_ERR_UNSUPPORTED, "joint " + std::to_string(i) + ": unsupported joint type");
     if (p < 0 || p >= i) return set_error(GB_ERR_INVALID_ARGUMENT, "parents[i] must satisfy 0 <= parents[i] < i");
@@ -254,6 +323,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
     M->chain_team = ts;
   }
   h.o_chain = take(4 * chain.size() + 4);
+  h.o_ujoint = take(4 * (size_t)nj);
   // children of each joint from the last one down (the order the RNEA backward sweep folds them)
   std::vector<std::vector<int>> kids(nj);
   for (int i = nj - 1; i >= 1; --i) kids[M->parents[i]].push_back(i);
@@ -321,6 +391,7 @@ inline int build_model(gb_model* M, const gb_model_desc* d, std::string* err) {
   std::memcpy(b, &h, sizeof(h));
   put_i(h.o_bslot, bslot);
   put_i(h.o_chain, chain);
+  put_i(h.o_ujoint, M->ujoint);
   put_i(h.o_child, child);
   put_i(h.o_grp, grp);
   put_i(h.o_grp_rel, grp_rel);

@@ -21,9 +21,10 @@ from __future__ import annotations
 
 import numpy as np
 
-JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU = range(10)
-_JT_NQ = {JT_NONE: 0, JT_FF: 7, **{j: 1 for j in (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)}}
-_JT_NV = {JT_NONE: 0, JT_FF: 6, **{j: 1 for j in (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)}}
+JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU, JT_TR, JT_SPH, JT_PL = range(13)
+_ONE_DOF = (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)
+_JT_NQ = {JT_NONE: 0, JT_FF: 7, JT_TR: 3, JT_SPH: 4, JT_PL: 4, **{j: 1 for j in _ONE_DOF}}
+_JT_NV = {JT_NONE: 0, JT_FF: 6, JT_TR: 3, JT_SPH: 3, JT_PL: 3, **{j: 1 for j in _ONE_DOF}}
 PRISMATIC = (JT_PX, JT_PY, JT_PZ, JT_PU)
 
 
@@ -73,6 +74,27 @@ class JointModelPY(JointModel):
 
 class JointModelPZ(JointModel):
     jtype = JT_PZ
+
+
+class JointModelTranslation(JointModel):
+    """Translation along the three axes of the joint frame, q = v in R^3 (reference
+    JointModelTranslationTpl, multibody/joint/joint-translation.hpp)."""
+
+    jtype = JT_TR
+
+
+class JointModelSpherical(JointModel):
+    """Rotation with a unit quaternion q = (x, y, z, w), v the angular velocity in the joint
+    frame (reference JointModelSphericalTpl, multibody/joint/joint-spherical.hpp)."""
+
+    jtype = JT_SPH
+
+
+class JointModelPlanar(JointModel):
+    """Motion in the x-y plane: q = (x, y, cos theta, sin theta), v = (vx, vy, wz) in the
+    joint frame (reference JointModelPlanarTpl, multibody/joint/joint-planar.hpp)."""
+
+    jtype = JT_PL
 
 
 def _unit(axis) -> np.ndarray:

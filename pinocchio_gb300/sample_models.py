@@ -29,6 +29,9 @@ import numpy as np
 
 from .model import (
     JT_FF,
+    JT_PL,
+    JT_SPH,
+    JT_TR,
     PRISMATIC,
     Inertia,
     JointModelFreeFlyer,
@@ -40,6 +43,7 @@ from .model import (
     JointModelRX,
     JointModelRY,
     JointModelRZ,
+    JointModelTranslation,
     Model,
     SE3,
 )
@@ -199,6 +203,42 @@ def unaligned_tree(nv: int = 14, free_flyer: bool = False, seed: int = 7) -> Mod
     return model
 
 
+def translation_tree(seed: int = 9) -> Model:
+    """A tree with translation joints (JointModelTranslation) at the root, inside a chain and at
+    a leaf, among revolute and prismatic joints: nv 14."""
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = "translationtree14"
+    root = _add_link(model, rng, 0, JointModelTranslation(), "base")
+    a = _add_link(model, rng, root, _random_revolute(rng), "a1")
+    a = _add_link(model, rng, a, JointModelTranslation(), "a2")
+    a = _add_link(model, rng, a, _random_one_dof(rng), "a3")
+    b = _add_link(model, rng, root, _random_revolute(rng), "b1")
+    b = _add_link(model, rng, b, _random_revolute(rng), "b2")
+    _add_link(model, rng, b, JointModelTranslation(), "b3")
+    _add_link(model, rng, root, _random_one_dof(rng), "c1")
+    return model
+
+
+def multidof_tree(seed: int = 10) -> Model:
+    """A tree with every three-dof joint type: a planar root, a spherical torso, a translation
+    joint and a spherical leaf among revolute joints: nv 16."""
+    from .model import JointModelPlanar, JointModelSpherical
+
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = "multidoftree16"
+    base = _add_link(model, rng, 0, JointModelPlanar(), "base")
+    torso = _add_link(model, rng, base, JointModelSpherical(), "torso")
+    a = _add_link(model, rng, torso, _random_revolute(rng), "a1")
+    a = _add_link(model, rng, a, _random_revolute(rng), "a2")
+    _add_link(model, rng, a, JointModelSpherical(), "a3")
+    b = _add_link(model, rng, torso, JointModelTranslation(), "b1")
+    _add_link(model, rng, b, _random_one_dof(rng), "b2")
+    _add_link(model, rng, base, _random_revolute(rng), "c1")
+    return model
+
+
 def chain(n: int = 100, seed: int = 4, mass_range=(0.1, 1.0)) -> Model:
     """Revolute serial chain of ``n`` links."""
     rng = np.random.default_rng(seed)
@@ -231,6 +271,15 @@ def random_configurations(model: Model, batch: int, rng: np.random.Generator) ->
         if jt == JT_FF:
             q[:, iq : iq + 3] = rng.standard_normal((batch, 3))
             q[:, iq + 3 : iq + 7] = random_unit_quaternion(rng, batch)
+        elif jt == JT_TR:
+            q[:, iq : iq + 3] = rng.uniform(-0.5, 0.5, (batch, 3))
+        elif jt == JT_SPH:
+            q[:, iq : iq + 4] = random_unit_quaternion(rng, batch)
+        elif jt == JT_PL:
+            th = rng.uniform(-np.pi, np.pi, batch)
+            q[:, iq : iq + 2] = rng.uniform(-0.5, 0.5, (batch, 2))
+            q[:, iq + 2] = np.cos(th)
+            q[:, iq + 3] = np.sin(th)
         elif jt in PRISMATIC:
             q[:, iq] = rng.uniform(-0.5, 0.5, batch)
         else:

@@ -18,7 +18,8 @@ from test_fext import random_fext
 from util import FP64_TOL, MODELS, mixed_tol, rel_err
 
 pytestmark = pytest.mark.gpu
-GPU_FEXT_MODELS = ["manipulator6r", "humanoid32", "tree32ff", "mixedtree24ff", "unaligned14", "unaligned20ff"]
+GPU_FEXT_MODELS = ["manipulator6r", "humanoid32", "tree32ff", "mixedtree24ff", "unaligned14", "unaligned20ff",
+                   "translationtree14"]
 
 
 @pytest.fixture(scope="module", params=GPU_FEXT_MODELS)

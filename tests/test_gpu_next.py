@@ -158,3 +158,23 @@ def test_forward_kinematics_errors():
                                    None, None) == _capi.GB_ERR_INVALID_ARGUMENT
     assert L.gb_forward_kinematics(data.dev.h, _capi.GB_FP64, _capi.GB_LAYOUT_INSTANCE, 0, None, None, None, None, None,
                                    None, None) == _capi.GB_OK
+
+
+def test_translation_joints_keep_the_callers_joint_indexing():
+    """A translation joint runs as three prismatic joints inside the kernels; the C ABI still
+    reports the caller's joints, and forwardKinematics writes one placement per caller joint
+    (the oracle computes the translation joint natively)."""
+    import ctypes as C
+
+    from pinocchio_gb300 import _capi
+
+    model = sm.translation_tree(9)
+    data = pg.createData(model)
+    nq, nv, nj = C.c_int(), C.c_int(), C.c_int()
+    _capi.check(_capi.lib().gb_model_dims(data.dev.h, C.byref(nq), C.byref(nv), C.byref(nj)))
+    assert (nq.value, nv.value, nj.value) == (model.nq, model.nv, model.njoints)
+    q, v, a = sm.random_inputs(model, 33, 4)
+    oMi, vi, ai = pg.forwardKinematics(model, data, q, v, a)  # numpy in, numpy out
+    oMo, vo, ao = OracleModel(model).forward_kinematics(q, v, a)
+    assert oMi.shape == oMo.shape
+    assert rel_err(oMi, oMo) < FP64_TOL and rel_err(vi, vo) < FP64_TOL and rel_err(ai, ao) < FP64_TOL

@@ -14,15 +14,15 @@ import pytest
 from oracle.oracle import LOCAL, WORLD, OracleModel, symmetrize_upper
 from pinocchio_gb300 import model as gm
 from pinocchio_gb300 import sample_models as sm
-from util import MODELS, rel_err
+from util import MODELS, ORACLE_ONLY_MODELS, rel_err
 
 CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100", "mixedtree12", "mixedtree24ff",
-              "unaligned14", "unaligned20ff"]
+              "unaligned14", "unaligned20ff", "translationtree14", "multidoftree16"]
 
 
 @pytest.fixture(scope="module", params=CPU_MODELS)
 def case(request):
-    model = MODELS[request.param]()
+    model = {**MODELS, **ORACLE_ONLY_MODELS}[request.param]()
     om = OracleModel(model)
     q, v, a = sm.random_inputs(model, 16, 11)
     return request.param, model, om, q, v, a
@@ -93,9 +93,10 @@ def _fd(f, x0, h, k, integrate=None):
     return (f(x0 + e) - f(x0 - e)) / (2 * h)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff",
+                                  "translationtree14", "multidoftree16"])
 def test_derivatives_vs_central_fd(name):
-    model = MODELS[name]()
+    model = {**MODELS, **ORACLE_ONLY_MODELS}[name]()
     om = OracleModel(model)
     q, v, a = sm.random_inputs(model, 4, 5)
     tau = om.rnea(q, v, a)
@@ -278,7 +279,7 @@ def _support(model):
     """dofs of joint i and of its ancestors, per joint (the columns of data.J that move joint i)."""
     t = model.tables()
     parents = t["parents"]
-    nvs = [0] + [6 if jt == gm.JT_FF else 1 for jt in t["jtype"][1:]]
+    nvs = list(model.nvs)
     idx_v = np.concatenate([[0], np.cumsum(nvs)])[: len(parents)]
     out = []
     for i in range(len(parents)):
@@ -313,11 +314,12 @@ def test_forward_kinematics_and_jacobians_agree(case):
     assert np.array_equal(om.forward_kinematics(q)[0], oMi)
 
 
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff",
+                                  "translationtree14", "multidoftree16"])
 def test_forward_kinematics_acceleration_vs_fd(name):
     """data.a[i] is the time derivative of the joint-frame velocity data.v[i]
     along (q + dt v, v + dt a): central differences, step 1e-6."""
-    model = MODELS[name]()
+    model = {**MODELS, **ORACLE_ONLY_MODELS}[name]()
     om = OracleModel(model)
     q, v, a = sm.random_inputs(model, 4, 21)
     _, _, ai = om.forward_kinematics(q, v, a)
@@ -356,3 +358,23 @@ def test_oracle_rollout_gradients_vs_central_differences():
             args_p[which], args_m[which] = plus, minus
             fd = (loss(*args_p) - loss(*args_m)) / (2 * h)
             assert abs(fd - grad[idx]) <= 1e-7 * max(1.0, abs(grad[idx])), (which, idx, fd, grad[idx])
+
+
+def test_kat_spherical_euler_equations():
+    """A body on a spherical joint with its centre of mass at the joint, no gravity: ABA gives
+    Euler's equations, dw/dt = Ic^-1 (tau - w x Ic w) in the body frame, for any orientation."""
+    rng = np.random.default_rng(3)
+    model = gm.Model()
+    model.gravity = np.zeros(6)
+    j = model.addJoint(0, gm.JointModelSpherical(), gm.SE3(), "ball")
+    A = rng.standard_normal((3, 3))
+    Ic = A @ A.T + 3 * np.eye(3)
+    model.appendBodyToJoint(j, gm.Inertia(2.0, np.zeros(3), Ic))
+    om = OracleModel(model)
+    q = sm.random_unit_quaternion(rng, 8)
+    w = rng.standard_normal((8, 3))
+    tau = rng.standard_normal((8, 3))
+    ddq = om.aba(q, w, tau)
+    ref = np.linalg.solve(Ic, (tau - np.cross(w, w @ Ic.T)).T).T
+    assert rel_err(ddq, ref) < 1e-13
+    assert rel_err(om.rnea(q, w, ddq), tau) < 1e-13
