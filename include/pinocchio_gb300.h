@@ -65,8 +65,12 @@ enum {
   GB_JOINT_REVOLUTE_UNALIGNED = 8,
   GB_JOINT_PRISMATIC_UNALIGNED = 9,
   GB_JOINT_TRANSLATION = 10, /* JointModelTranslation (joint-translation.hpp): q = v in R^3 */
-  GB_JOINT_SPHERICAL = 11,   /* JointModelSpherical (joint-spherical.hpp): not supported yet */
-  GB_JOINT_PLANAR = 12       /* JointModelPlanar (joint-planar.hpp): not supported yet */
+  GB_JOINT_SPHERICAL = 11,   /* JointModelSpherical (joint-spherical.hpp): q = unit quaternion
+                                (x, y, z, w), v = angular velocity in the joint frame */
+  GB_JOINT_PLANAR = 12       /* JointModelPlanar (joint-planar.hpp): q = (x, y, cos t, sin t),
+                                v = (vx, vy, wz) in the joint frame.  Models with spherical or
+                                planar joints run one configuration per thread (gb_model_set_layout
+                                refuses the lane layouts) and are not accepted by gb_batch_multi. */
 };
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
 /* functions of a heterogeneous batch task / of a launch setting */

@@ -29,6 +29,7 @@ import numpy as np
 
 from . import _capi, api
 from . import sample_models as sm
+from .model import JT_PL, JT_SPH
 
 CANDIDATES = (32, 64, 96, 128)  # configurations per CTA, one thread each
 WARP = "warp"  # one warp per configuration (RNEA, ABA, ABA derivatives)
@@ -109,6 +110,7 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
             _capi.check(L.gb_model_set_layout(data.dev.h, _FUNCS[f], _capi.GB_INSTANCE_PER_THREAD))
             _capi.check(L.gb_model_set_launch(data.dev.h, _FUNCS[f], int(setting)))
 
+    three_dof = any(jt in (JT_SPH, JT_PL) for jt in model.jtypes)
     result = {}
     for f in functions:
         ck = f"{key}|{f}"
@@ -116,9 +118,11 @@ def tune(model, data, functions=("rnea", "aba", "crba", "rnea_derivatives", "aba
             setting, ms = cache[ck]
         else:
             best = None
-            settings = list(candidates) + ([WARP, BRANCH] if f in ("rnea", "aba") else [])
-            if f == "aba_derivatives":
-                settings += [LANES4, LANES8, WARP]
+            settings = list(candidates)
+            if not three_dof:  # spherical and planar joints run one configuration per thread
+                settings += [WARP, BRANCH] if f in ("rnea", "aba") else []
+                if f == "aba_derivatives":
+                    settings += [LANES4, LANES8, WARP]
             for st in settings:
                 apply(f, st)
                 ms = _time(calls[f])

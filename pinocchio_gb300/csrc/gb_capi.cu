@@ -316,6 +316,8 @@ int gb_model_set_layout(gb_model* M, int function, int layout) {
   if (function < GB_FUNC_RNEA || function > GB_FUNC_ABA_DERIVATIVES) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown function");
   if (layout < GB_INSTANCE_PER_THREAD || layout > GB_INSTANCE_PER_BRANCH)
     return set_error(GB_ERR_INVALID_ARGUMENT, "unknown layout");
+  if (M->has_three && layout != GB_INSTANCE_PER_THREAD)
+    return set_error(GB_ERR_UNSUPPORTED, "spherical and planar joints run one configuration per thread");
   if (layout == GB_INSTANCE_PER_BRANCH && function != GB_FUNC_RNEA && function != GB_FUNC_ABA)
     return set_error(GB_ERR_UNSUPPORTED, "the lane-per-branch layout exists for RNEA and ABA");
   if (layout == GB_INSTANCE_PER_WARP && function != GB_FUNC_RNEA && function != GB_FUNC_ABA &&

@@ -21,7 +21,7 @@ namespace gbi {
 namespace {
 
 // FE: with external forces (fext, njoints x 6 per configuration in the joint frames)
-template <class S, bool FE = false>
+template <class S, bool FE = false, bool J3 = false>
 __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* blob, int bytes, long B,
                                                           gb::DerivLayout L, S* ws, bool symmetric, Arr q, Arr v,
                                                           Arr a, Arr dq, Arr dv, Arr Mo, Arr tau, Arr fext) {
@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kThreads) k_rnea_derivs(const unsigned char* b
   const gb::Ws<S> w{ws + b, B};
   const gb::Out to = out_at(tau, b);
   const gb::In fe = in_at(fext, b);
-  gb::rnea_derivs_one<S>(m, L, w, in_at(q, b), in_at(v, b), in_at(a, b), out_at(dq, b), out_at(dv, b), out_at(Mo, b),
+  gb::rnea_derivs_one<S, J3>(m, L, w, in_at(q, b), in_at(v, b), in_at(a, b), out_at(dq, b), out_at(dv, b), out_at(Mo, b),
                          tau.p ? &to : nullptr, symmetric, true, FE ? &fe : nullptr);
 }
 
@@ -534,7 +534,8 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   Workspace ws;
   int rc = ws_alloc(ws, sizeof(S) * (size_t)L.nS * B, st);
   if (rc != GB_OK) return rc;
-  rc = blob_smem(M, (const void*)k_rnea_derivs<S, FE>, "k_rnea_derivs");
+  rc = blob_smem(M, M->has_three ? (const void*)k_rnea_derivs<S, FE, true> : (const void*)k_rnea_derivs<S, FE, false>,
+                 "k_rnea_derivs");
   if (rc != GB_OK) return rc;
   // instance-layout matrices of a large batch are written coalesced into an SOA scratch, then transposed
   const long nn = (long)M->nv * M->nv;
@@ -553,7 +554,12 @@ int run_rnea_derivs(const gb_model* M, long B, bool symmetric, Arr q, Arr v, Arr
   }
   const int tpb = M->tpb[GB_FUNC_RNEA_DERIVATIVES];
   const long grid = (B + tpb - 1) / tpb;
-  k_rnea_derivs<S, FE><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
+  if (M->has_three)
+    k_rnea_derivs<S, FE, true><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
+                                                                       static_cast<S*>(ws.p), symmetric, q, v, a,
+                                                                       mats[0], mats[1], mats[2], tau, fext);
+  else
+    k_rnea_derivs<S, FE, false><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
                                                                        static_cast<S*>(ws.p), symmetric, q, v, a,
                                                                        mats[0], mats[1], mats[2], tau, fext);
   rc = cuda_error(cudaGetLastError(), "k_rnea_derivs");
@@ -750,7 +756,7 @@ size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B) {
 
 int launch_aba_derivs_on_workspace(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr dq, Arr dv,
                                    Arr Minv, Arr ddq, void* ws, cudaStream_t st) {
-  if (check_gravity(M) != GB_OK) return GB_ERR_GRAVITY;
+  if (const int rc = check_gravity(M)) return rc;
   if (precision == GB_FP64)
     return launch_aba_derivs_ws<double, double, double, double, double, double>(M, B, q, v, tau, dq, dv, Minv, ddq,
                                                                                 ws, st);

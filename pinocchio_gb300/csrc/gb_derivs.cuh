@@ -289,6 +289,9 @@ template <int NVJ, class S> GB_HD void joint_columns(int jt, const X3<S>& O, S (
       Jc[3 + k][0] = tw[0]; Jc[3 + k][1] = tw[1]; Jc[3 + k][2] = tw[2];
       Jc[3 + k][3] = w[0]; Jc[3 + k][4] = w[1]; Jc[3 + k][5] = w[2];
     }
+  } else if constexpr (NVJ == 3) {  // spherical / planar: unit axes of the joint frame
+#pragma unroll
+    for (int k = 0; k < 3; ++k) world_axis_column(O, jt_col(jt, k), Jc[k]);
   } else {
     S w[3];
     axis_column(O, jt_axis(jt), w);
@@ -452,13 +455,16 @@ GB_HD void world_forward_joint(const MView& m, const DerivLayout& L, const Ws<S>
   for (int k = 0; k < 36; ++k) w[L.doY + 36 * i + k] = dY[k];
 }
 
-template <class S>
+// J3: the model has spherical / planar joints (their three-dof steps are compiled in only then,
+// so that the kernels of the other models keep their registers)
+template <class S, bool J3 = false>
 GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
                          const In* acc, bool with_derivs, const In* fext = nullptr) {
   const S* g = ModelScalar<S>::grav(m);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
     if (m.jtype[i] == JT_FF) world_forward_joint<6, S>(m, L, w, q, v, acc, with_derivs, g, i, fext);
+    else if (J3 && jt_three(m.jtype[i])) world_forward_joint<3, S>(m, L, w, q, v, acc, with_derivs, g, i, fext);
     else world_forward_joint<1, S>(m, L, w, q, v, acc, with_derivs, g, i, fext);
   }
 }
@@ -467,18 +473,18 @@ GB_HD void world_forward(const MView& m, const DerivLayout& L, const Ws<S>& w, c
 // computeRNEADerivatives (rnea-derivatives.hxx:472-541).  Writes dtau_dq, dtau_dv, M (=dtau/da,
 // upper or symmetric) and optionally tau; every other matrix entry is written as zero.
 // ------------------------------------------------------------------------------------------
-template <class S>
+template <class S, bool J3 = false>
 GB_HD void rnea_derivs_one(const MView& m, const DerivLayout& L, const Ws<S>& w, const In& q, const In& v,
                            const In& a, const Out& dq, const Out& dv, const Out& Mo, const Out* tau, bool symmetric,
                            bool zeroed, const In* fext = nullptr) {
   const int nv = m.nv;
-  world_forward(m, L, w, q, v, &a, true, fext);
+  world_forward<S, J3>(m, L, w, q, v, &a, true, fext);
   if (!zeroed)  // otherwise the outputs arrive zero-filled: only non-zero entries are written
     for (int r = 0; r < nv * nv; ++r) { dq[r] = 0.0; dv[r] = 0.0; Mo[r] = 0.0; }
   const S eps = eps_of<S>();
   for (int i = m.nj - 1; i > 0; --i) {  // ComputeRNEADerivativesBackwardStep (hxx:361-460)
     const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
-    const int nvj = m.jtype[i] == JT_FF ? 6 : 1;
+    const int nvj = jt_nv(m.jtype[i]);
     Iner<S> oY;
     ld_iner(w, L.oY + 10 * i, oY);
     S of[6];
@@ -751,8 +757,8 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
         }
 #pragma unroll 1
       for (int k = 0; k < NVJ; ++k) StU[k * NVJ + k] += SS(m.arm_d[iv + k]);
-      if constexpr (NVJ == 6) {
-        if (!llt_inverse<SS, 6>(StU, Dinv)) flag_numeric(m, NUM_PIVOT);
+      if constexpr (NVJ > 1) {
+        if (!llt_inverse<SS, NVJ>(StU, Dinv)) flag_numeric(m, NUM_PIVOT);
       } else {
         check_pivot(m, StU[0]);
         Dinv[0] = SS(1) / StU[0];
@@ -855,14 +861,14 @@ GB_HD void aba_derivs_pass2_joint(const MView& m, const DerivLayout& L, const Ws
   }
 }
 
-template <class K, class SS, class Team = Solo>
+template <class K, class SS, bool J3 = false, class Team = Solo>
 GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& zk, const Ws<SS>& zs,
                              const Ws<K>& zm, const In& q, const In& v, const In& tau, const In* fext,
                              const Team& tm = Team()) {
   const int nv = m.nv;
   // ---- pass 1: ComputeABADerivativesForwardStep1 (hxx:22-80), kinematics in K;
   // external forces enter the bias force (hxx:513)
-  world_forward<K>(m, L, zk, q, v, nullptr, false, fext);
+  world_forward<K, J3>(m, L, zk, q, v, nullptr, false, fext);
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {  // Ia = oYcrb.matrix(), formed in K and stored in SS
     Iner<K> oY;
@@ -880,6 +886,7 @@ GB_HD void aba_derivs_pass12(const MView& m, const DerivLayout& L, const Ws<K>& 
 #pragma unroll 1
   for (int i = m.nj - 1; i > 0; --i) {
     if (m.jtype[i] == JT_FF) aba_derivs_pass2_joint<6, K, SS>(m, L, zk, zs, zm, i, tm);
+    else if (J3 && jt_three(m.jtype[i])) aba_derivs_pass2_joint<3, K, SS>(m, L, zk, zs, zm, i, tm);
     else aba_derivs_pass2_joint<1, K, SS>(m, L, zk, zs, zm, i, tm);
     tm.sync();
   }
@@ -909,6 +916,10 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   }
   if constexpr (NVJ == 1)
     if (!jt_slides(m.jtype[i])) Jc[0][0] = Jc[0][1] = Jc[0][2] = K(0);
+  if constexpr (NVJ == 3)  // angular axes of a spherical / planar joint pass through t_i
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (jt_col(m.jtype[i], k) >= 3) Jc[k][0] = Jc[k][1] = Jc[k][2] = K(0);
   K ovp[6] = {K(0), K(0), K(0), K(0), K(0), K(0)}, oap[6], ov[6], oa[6];
   if constexpr (!MINV) {
     if (p > 0) {
@@ -956,10 +967,56 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
   }
   // Minv rows of the joint: -= UDinv^T Fcrb[parent] (columns right of the
   // subtree start from zero); Fcrb[i] = J Minv_rows (+ Fcrb[parent]).  A
-  // free-flyer is a root joint (no parent), so the updated rows are one-dof joints'.
+  // free-flyer is a root joint (no parent); a spherical / planar joint with a parent
+  // updates its own NVJ x NVJ block first (every lane, all of it, before its columns).
   const long Fi = L.Fslot + 6L * nv * slot[i];
   const long Fp = p > 0 ? L.Fslot + 6L * nv * slot[p] : -1;
-  if (p > 0) {
+  if constexpr (NVJ == 3) {  // (a free-flyer has no parent: only three-dof joints take this)
+   if (p > 0) {
+    K ud[NVJ][6], Fo[NVJ][6], Bn[NVJ][NVJ];
+#pragma unroll 1
+    for (int k = 0; k < NVJ; ++k) {
+      ld6(zk, L.UD + 6 * (iv + k), ud[k]);
+      ld6(zk, Fp + 6 * (iv + k), Fo[k]);
+    }
+#pragma unroll 1
+    for (int r = 0; r < NVJ; ++r)
+#pragma unroll 1
+      for (int c = 0; c < NVJ; ++c) Bn[r][c] = minv_at(zm, nv, iv + r, iv + c) - dot6(ud[r], Fo[c]);
+    tm.sync();  // every lane has read the block before any lane writes it
+#pragma unroll 1
+    for (int c = tm.first(iv); c < iv + NVJ; c += Team::size) {
+      K F[6];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) F[r] = Fo[c - iv][r];
+#pragma unroll 1
+      for (int k = 0; k < NVJ; ++k) {
+        if (iv + k <= c) zm[upk(nv, iv + k, c)] = Bn[k][c - iv];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) F[r] += Jo[k][r] * Bn[k][c - iv];
+      }
+      st6(zk, Fi + 6 * c, F);
+    }
+#pragma unroll 1
+    for (int c = tm.first(iv + NVJ); c < nv; c += Team::size) {
+      K Fpc[6], F[6];
+      ld6(zk, Fp + 6 * c, Fpc);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) F[r] = Fpc[r];
+#pragma unroll 1
+      for (int k = 0; k < NVJ; ++k) {
+        const long e = upk(nv, iv + k, c);
+        const K mk = (c < iv + nst ? zm[e] : K(0)) - dot6(ud[k], Fpc);
+        zm[e] = mk;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) F[r] += Jo[k][r] * mk;
+      }
+      st6(zk, Fi + 6 * c, F);
+    }
+   }
+  }
+  if (NVJ == 3 && p > 0) {
+  } else if (p > 0) {
     K udk[6];
     ld6(zk, L.UD + 6 * iv, udk);
 #pragma unroll 1
@@ -1055,7 +1112,7 @@ GB_HD void aba_derivs_pass3_joint(const MView& m, const DerivLayout& L, const in
     if (k >= 18 || k % 6 >= 3) w[L.doY + 36 * i + k] = S(dY[k]);  // the lin-lin block is zero
 }
 
-template <class S, class T, class K, bool MINV = false, class Team = Solo>
+template <class S, class T, class K, bool MINV = false, bool J3 = false, class Team = Solo>
 GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                             const Ws<K>& zk, const Ws<K>& zm, const In& v, const Out* ddq_out, const In* fext,
                             const Team& tm = Team()) {
@@ -1067,6 +1124,8 @@ GB_HD void aba_derivs_pass3(const MView& m, const DerivLayout& L, const int* slo
 #pragma unroll 1
   for (int i = 1; i < m.nj; ++i) {
     if (m.jtype[i] == JT_FF) aba_derivs_pass3_joint<6, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, fext, i, tm);
+    else if (J3 && jt_three(m.jtype[i]))
+      aba_derivs_pass3_joint<3, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, fext, i, tm);
     else aba_derivs_pass3_joint<1, S, T, K, MINV>(m, L, slot, w, zk, zm, v, ddq_out, gk, fext, i, tm);
   }
 }
@@ -1228,26 +1287,27 @@ GB_HD void aba_derivs_pass4_joint(const MView& m, const DerivLayout& L, const Ws
 // child adds its contributions moved to the parent's position.  Only the
 // structurally non-zero entries of dtau_dq / dtau_dv (row k of column c for k
 // an ancestor of c or in its subtree) are written: the products read no other.
-template <class S, class T, class K, class P, class Team = Solo>
+template <class S, class T, class K, class P, bool J3 = false, class Team = Solo>
 GB_HD void aba_derivs_pass4(const MView& m, const DerivLayout& L, const Ws<S>& w, const Ws<K>& zk,
                             const Ws<P>& wp, const Team& tm = Team()) {
   const T eps = eps_of<T>();
 #pragma unroll 1
   for (int i = m.nj - 1; i > 0; --i) {
     if (m.jtype[i] == JT_FF) aba_derivs_pass4_joint<6, S, T, K, P>(m, L, w, zk, wp, i, eps, tm);
+    else if (J3 && jt_three(m.jtype[i])) aba_derivs_pass4_joint<3, S, T, K, P>(m, L, w, zk, wp, i, eps, tm);
     else aba_derivs_pass4_joint<1, S, T, K, P>(m, L, w, zk, wp, i, eps, tm);
     tm.sync();
   }
 }
 
 // T3: arithmetic of the column sets in pass 3; T: arithmetic of pass 4
-template <class S, class T3, class T, class K, class SS, class P>
+template <class S, class T3, class T, class K, class SS, class P, bool J3 = false>
 GB_HD void aba_derivs_sweeps(const MView& m, const DerivLayout& L, const int* slot, const Ws<S>& w,
                              const Ws<K>& zk, const Ws<SS>& zs, const Ws<K>& zm, const Ws<P>& wp, const In& q,
                              const In& v, const In& tau, const Out* ddq_out, const In* fext = nullptr) {
-  aba_derivs_pass12<K, SS>(m, L, zk, zs, zm, q, v, tau, fext);
-  aba_derivs_pass3<S, T3, K>(m, L, slot, w, zk, zm, v, ddq_out, fext);
-  aba_derivs_pass4<S, T, K, P>(m, L, w, zk, wp);
+  aba_derivs_pass12<K, SS, J3>(m, L, zk, zs, zm, q, v, tau, fext);
+  aba_derivs_pass3<S, T3, K, false, J3>(m, L, slot, w, zk, zm, v, ddq_out, fext);
+  aba_derivs_pass4<S, T, K, P, J3>(m, L, w, zk, wp);
 }
 
 }  // namespace gb

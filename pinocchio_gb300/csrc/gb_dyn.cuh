@@ -123,15 +123,28 @@ template <class S> GB_HD void compose_joint(const S* PR, const S* Pt, int jt, S 
 
 // liMi = jointPlacements[i] * M_joint(q)   (rnea.hxx:60, joint calc:
 // revolute joint-revolute.hpp:811-821, prismatic joint-prismatic.hpp:700-704,
-// free-flyer joint-free-flyer.hpp:333-375)
+// free-flyer joint-free-flyer.hpp:333-375, spherical joint-spherical.hpp:504-531 (the
+// quaternion's matrix, no translation), planar joint-planar.hpp:586-609 (rotation about z
+// with (cos, sin) = q[2:4], translation (q[0], q[1], 0)))
 template <class S> GB_HD void joint_transform(const MView& m, int i, const In& q, X3<S>& X) {
   const S* P = ModelScalar<S>::place(m, i);
   const int jt = m.jtype[i], iq = m.idx_q[i];
-  if (jt == JT_FF) {
+  if (jt == JT_FF || jt_three(jt)) {
     X3<S> Pl, J;
     load_placement(m, i, Pl);
-    quat_matrix(S(q[iq + 3]), S(q[iq + 4]), S(q[iq + 5]), S(q[iq + 6]), J.R);
-    J.t[0] = S(q[iq]); J.t[1] = S(q[iq + 1]); J.t[2] = S(q[iq + 2]);
+    if (jt == JT_FF) {
+      quat_matrix(S(q[iq + 3]), S(q[iq + 4]), S(q[iq + 5]), S(q[iq + 6]), J.R);
+      J.t[0] = S(q[iq]); J.t[1] = S(q[iq + 1]); J.t[2] = S(q[iq + 2]);
+    } else if (jt == JT_SPH) {
+      quat_matrix(S(q[iq]), S(q[iq + 1]), S(q[iq + 2]), S(q[iq + 3]), J.R);
+      J.t[0] = J.t[1] = J.t[2] = S(0);
+    } else {
+      const S c = S(q[iq + 2]), s = S(q[iq + 3]);
+      J.R[0] = c; J.R[1] = -s; J.R[2] = S(0);
+      J.R[3] = s; J.R[4] = c; J.R[5] = S(0);
+      J.R[6] = S(0); J.R[7] = S(0); J.R[8] = S(1);
+      J.t[0] = S(q[iq]); J.t[1] = S(q[iq + 1]); J.t[2] = S(0);
+    }
     compose(Pl, J, X);
   } else {
     S s, c;
@@ -144,6 +157,11 @@ template <class S> GB_HD void joint_motion(int jt, const In& x, int iv, M6<S>& o
   if (jt == JT_FF) {
 #pragma unroll
     for (int k = 0; k < 6; ++k) o.v[k] = S(x[iv + k]);
+  } else if (jt_three(jt)) {
+    const S x0 = S(x[iv]), x1 = S(x[iv + 1]), x2 = S(x[iv + 2]);
+    const int c2 = jt_col(jt, 2), c0 = jt_col(jt, 0);  // spherical 3, 4, 5; planar 0, 1, 5
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o.v[k] = k == c0 ? x0 : k == c0 + 1 ? x1 : k == c2 ? x2 : S(0);
   } else {
     const S val = S(x[iv]);
     const int k0 = jt_sidx(jt);
@@ -236,9 +254,12 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
         tau[iv + k] = t;
       }
     } else {
-      const double t = double(pick6(f[i].v, jt_sidx(jt)) + arm[iv] * S(a[iv]));
-      if (!finite_value(t)) flag_numeric(m, NUM_NONFINITE);
-      tau[iv] = t;
+      const int nvj = jt_nv(jt);
+      for (int k = 0; k < nvj; ++k) {
+        const double t = double(pick6(f[i].v, jt_col(jt, k)) + arm[iv + k] * S(a[iv + k]));
+        if (!finite_value(t)) flag_numeric(m, NUM_NONFINITE);
+        tau[iv + k] = t;
+      }
     }
     if (p > 0) {
       M6<S> fp;
@@ -265,7 +286,9 @@ GB_HD void rnea_one(const MView& m, const In& q, const In& v, const In& a, const
 //
 // With external forces fext (aba.hxx:550-590): the bias force of joint i is
 // v_i x* (I_i v_i) - fext_i.
-template <class S, class SS, int CAP>
+// J3: the model has spherical / planar joints (their three-dof steps are compiled in only
+// then, so that the kernels of the other models keep their registers).
+template <class S, class SS, int CAP, bool J3 = false>
 GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, const Out& ddq,
                    const In* fext = nullptr) {
   constexpr bool kStoreX = sizeof(S) == sizeof(double);
@@ -286,6 +309,8 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       X = Xs[i];
     } else if (m.jtype[i] == JT_FF) {
       X = Xff;
+    } else if (J3 && jt_three(m.jtype[i])) {  // rebuilt from q (spherical / planar)
+      joint_transform(m, i, q, X);
     } else {
       const S* P = ModelScalar<S>::place(m, i);
       compose_joint(P, P + 9, m.jtype[i], cs[i][1], cs[i][0], X);
@@ -298,6 +323,8 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
     if (jt == JT_FF) {
       joint_transform(m, i, q, X);
       Xff = X;
+    } else if (J3 && jt_three(jt)) {
+      joint_transform(m, i, q, X);
     } else {
       S sn, cn;
       joint_params_q(jt, q[m.idx_q[i]], &sn, &cn);
@@ -383,29 +410,15 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
         }
       continue;
     }
-    // revolute calc_aba (joint-revolute.hpp:823-834), prismatic (joint-prismatic.hpp:728-740)
-    const int sx = jt_sidx(jt);
-    const SS u = SS(tau[iv]) - cvt<SS>(pick6(f.v, sx));
-    SS U[6], UD[6];
-    sym6_col(Ia, sx, U);
-    const SS Dpiv = pick6(U, sx) + SS(arm[iv]);
-    check_pivot(m, Dpiv);
-    const SS Dinv = SS(1) / Dpiv;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      UD[k] = U[k] * Dinv;
-      UDs[i][k] = cvt<S>(UD[k]);
-    }
-    du[i] = Dinv * u;
-    if (p > 0) {
-      sym6_rank1_sub(Ia, U, UD);
+    // the Schur-updated Ia and the bias pa = f + Ia c + U Dinv u moved to the parent
+    auto to_parent = [&](const SS* UDu) {
       Sym6<S> Iaf, Ip;
       sym6_convert(Ia, Iaf);
       S t6[6];
       sym6_mv(Iaf, c.v, t6);
       M6<S> pa, fp;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) pa.v[k] = f.v[k] + (t6[k] + cvt<S>(UD[k] * u));
+      for (int k = 0; k < 6; ++k) pa.v[k] = f.v[k] + (t6[k] + cvt<S>(UDu[k]));
       sym6_transform(Iaf, X, Ip);
       act_force(X, pa, fp);
       if (p == i - 1) {  // i is the first child of p: processed next
@@ -417,6 +430,56 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 #pragma unroll
         for (int k = 0; k < 6; ++k) fslot[pb].v[k] += fp.v[k];
       }
+    };
+    if (J3 && jt_three(jt)) {  // calc_aba of the spherical (joint-spherical.hpp:572-586) and planar
+                         // (joint-planar.hpp:643-661) joints: U = Ia S, Dinv = (S^T U + armature)^-1
+      SS U[3][6], UD[3][6], StU[9], D3[9], u3[3];
+      for (int k = 0; k < 3; ++k) {
+        const int col = jt_col(jt, k);
+        sym6_col(Ia, col, U[k]);
+        u3[k] = SS(tau[iv + k]) - cvt<SS>(pick6(f.v, col));
+      }
+      for (int r = 0; r < 3; ++r)
+        for (int cc = 0; cc < 3; ++cc) StU[3 * r + cc] = pick6(U[cc], jt_col(jt, r));
+      for (int k = 0; k < 3; ++k) StU[4 * k] += SS(arm[iv + k]);
+      if (!llt_inverse<SS, 3>(StU, D3)) flag_numeric(m, NUM_PIVOT);
+      for (int k = 0; k < 3; ++k) {
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          UD[k][r] = U[0][r] * D3[k] + U[1][r] * D3[3 + k] + U[2][r] * D3[6 + k];
+          UDs[iv + k][r] = cvt<S>(UD[k][r]);
+        }
+        du[iv + k] = D3[3 * k] * u3[0] + D3[3 * k + 1] * u3[1] + D3[3 * k + 2] * u3[2];
+      }
+      if (p > 0) {
+        SS UDu[6];
+        for (int k = 0; k < 3; ++k) sym6_rank1_sub(Ia, U[k], UD[k]);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) UDu[r] = UD[0][r] * u3[0] + UD[1][r] * u3[1] + UD[2][r] * u3[2];
+        to_parent(UDu);
+      }
+      continue;
+    }
+    // revolute calc_aba (joint-revolute.hpp:823-834), prismatic (joint-prismatic.hpp:728-740)
+    const int sx = jt_sidx(jt);
+    const SS u = SS(tau[iv]) - cvt<SS>(pick6(f.v, sx));
+    SS U[6], UD[6];
+    sym6_col(Ia, sx, U);
+    const SS Dpiv = pick6(U, sx) + SS(arm[iv]);
+    check_pivot(m, Dpiv);
+    const SS Dinv = SS(1) / Dpiv;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      UD[k] = U[k] * Dinv;
+      UDs[iv][k] = cvt<S>(UD[k]);
+    }
+    du[iv] = Dinv * u;
+    if (p > 0) {
+      sym6_rank1_sub(Ia, U, UD);
+      SS UDu[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) UDu[k] = UD[k] * u;
+      to_parent(UDu);
     }
   }
   // pass 3 (AbaLocalConventionForwardStep2, aba.hxx:437-468)
@@ -453,11 +516,22 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       }
 #pragma unroll
       for (int r = 0; r < 6; ++r) a.v[r] += cvt<S>(dd[r]);
-    } else {
-      S w = UDs[i][0] * a.v[0];
+    } else if (J3 && jt_three(jt)) {  // the three dofs from the same a
+      SS dd[3];
+      for (int k = 0; k < 3; ++k) {
+        S w = UDs[iv + k][0] * a.v[0];
 #pragma unroll
-      for (int k = 1; k < 6; ++k) w += UDs[i][k] * a.v[k];
-      const SS dd = du[i] - cvt<SS>(w);
+        for (int r = 1; r < 6; ++r) w += UDs[iv + k][r] * a.v[r];
+        dd[k] = du[iv + k] - cvt<SS>(w);
+        if (!finite_value(dd[k])) flag_numeric(m, NUM_NONFINITE);
+        ddq[iv + k] = double(dd[k]);
+      }
+      for (int k = 0; k < 3; ++k) add_at6(a.v, jt_col(jt, k), cvt<S>(dd[k]));
+    } else {
+      S w = UDs[iv][0] * a.v[0];
+#pragma unroll
+      for (int k = 1; k < 6; ++k) w += UDs[iv][k] * a.v[k];
+      const SS dd = du[iv] - cvt<SS>(w);
       if (!finite_value(dd)) flag_numeric(m, NUM_NONFINITE);
       ddq[iv] = double(dd);
       add_at6(a.v, jt_sidx(jt), cvt<S>(dd));
@@ -474,6 +548,20 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
 // optionally the tree-sparse U D U^T factorisation of cholesky::decompose
 // (reference algorithm/cholesky.hxx:18-62) in FP64.
 // ------------------------------------------------------------------------------------------
+// The world-frame column oMi.act(e_col) of a unit spatial axis col ([linear; angular]) of
+// joint i's frame O: (R e_col, 0) for a linear axis, (t x R e_a, R e_a) for angular axis a.
+template <class S> GB_HD void world_axis_column(const X3<S>& O, int col, S* Jc) {
+  S w[3];
+  axis_column(O, col < 3 ? col : col - 3, w);
+  if (col < 3) {
+    Jc[0] = w[0]; Jc[1] = w[1]; Jc[2] = w[2]; Jc[3] = S(0); Jc[4] = S(0); Jc[5] = S(0);
+  } else {
+    S tw[3];
+    cross3(O.t, w, tw);
+    Jc[0] = tw[0]; Jc[1] = tw[1]; Jc[2] = tw[2]; Jc[3] = w[0]; Jc[4] = w[1]; Jc[5] = w[2];
+  }
+}
+
 template <class S, int CAP>
 // `zeroed`: M (and U) arrive zero-filled (the device launcher clears them with
 // one bandwidth-bound memset), so only the structurally non-zero entries are written.
@@ -505,16 +593,7 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
         J[iv + 3 + k][3] = w[0]; J[iv + 3 + k][4] = w[1]; J[iv + 3 + k][5] = w[2];
       }
     } else {
-      S w[3], tw[3];
-      axis_column(O, jt_axis(jt), w);
-      if (jt_slides(jt)) {  // (R e_axis, 0)
-        J[iv][0] = w[0]; J[iv][1] = w[1]; J[iv][2] = w[2];
-        J[iv][3] = S(0); J[iv][4] = S(0); J[iv][5] = S(0);
-      } else {  // (t x R e_axis, R e_axis)
-        cross3(O.t, w, tw);
-        J[iv][0] = tw[0]; J[iv][1] = tw[1]; J[iv][2] = tw[2];
-        J[iv][3] = w[0]; J[iv][4] = w[1]; J[iv][5] = w[2];
-      }
+      for (int k = 0; k < jt_nv(jt); ++k) world_axis_column(O, jt_col(jt, k), J[iv + k]);
     }
     Iner<S> Y;
     load_inertia(m, i, Y);
@@ -526,7 +605,7 @@ GB_HD void crba_one(const MView& m, const In& q, const Out& M, bool symmetric, c
   const S eps = eps_of<S>();
   for (int i = m.nj - 1; i > 0; --i) {
     const int p = m.parent[i], iv = m.idx_v[i], nst = m.nvsub[i];
-    const int nvj = (m.jtype[i] == JT_FF) ? 6 : 1;
+    const int nvj = jt_nv(m.jtype[i]);
     for (int k = 0; k < nvj; ++k) {
       M6<S> jc, ag;
 #pragma unroll
@@ -689,12 +768,12 @@ GB_HD void jacobians_one(const MView& m, const In& q, const Out& J) {
     joint_transform(m, i, q, X);
     if (p > 0) compose(oM[p], X, oM[i]);
     else oM[i] = X;
-    const int nvj = jt == JT_FF ? 6 : 1;
+    const int nvj = jt_nv(jt);
     for (int k = 0; k < nvj; ++k) {
       M6<S> sk, c;
+      const int col = jt_col(jt, k);
 #pragma unroll
-      for (int r = 0; r < 6; ++r) sk.v[r] = S(0);
-      sk.v[jt == JT_FF ? k : jt_sidx(jt)] = S(1);
+      for (int r = 0; r < 6; ++r) sk.v[r] = r == col ? S(1) : S(0);
       act_motion(oM[i], sk, c);
 #pragma unroll
       for (int r = 0; r < 6; ++r) J[6 * (iv + k) + r] = double(c.v[r]);
@@ -708,11 +787,63 @@ GB_HD void jacobians_one(const MView& m, const In& q, const Out& J) {
 // multibody/liegroup/special-euclidean.hpp:660-699, spatial/explog-quaternion.hpp:20-147,
 // math/quaternion.hpp:90-111).  Always FP64.
 // ------------------------------------------------------------------------------------------
+// exp3 of an angular velocity w as a quaternion (x, y, z, w) (spatial/explog-quaternion.hpp:20-60)
+GB_HD void exp3_quaternion(const double* w, double* e) {
+  const double eps = eps_of<double>();
+  const double ts_prec = 1.2207031250000000e-04;  // eps^(1/4)
+  const double s2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  const double th = sqrt(s2 + eps * eps);
+  if (s2 > ts_prec) {
+    double sh, ch;
+    sincos(0.5 * th, &sh, &ch);
+    for (int k = 0; k < 3; ++k) e[k] = sh * (w[k] / th);
+    e[3] = ch;
+  } else {
+    const double t22 = s2 / 4.0;
+    const double cc = 0.5 * (1.0 - t22 / 6.0 + t22 * t22 / 120.0);
+    for (int k = 0; k < 3; ++k) e[k] = cc * w[k];
+    e[3] = 1.0 - t22 / 2.0 + t22 * t22 / 24.0;
+  }
+}
+// spherical: q * exp3(v), first-order normalised (liegroup/special-orthogonal.hpp:467-481);
+// planar: the SE(2) exponential of (vx, vy, w) in the body frame composed on the right
+// (liegroup/special-euclidean.hpp:61-90, 289-306)
+GB_HD void integrate_three(int jt, const In& q, const In& v, int iq, int iv, const Out& qo) {
+  if (jt == JT_SPH) {
+    const double qq[4] = {q[iq], q[iq + 1], q[iq + 2], q[iq + 3]};
+    const double w[3] = {v[iv], v[iv + 1], v[iv + 2]};
+    double e[4], r[4];
+    exp3_quaternion(w, e);
+    r[3] = qq[3] * e[3] - qq[0] * e[0] - qq[1] * e[1] - qq[2] * e[2];
+    r[0] = qq[3] * e[0] + qq[0] * e[3] + qq[1] * e[2] - qq[2] * e[1];
+    r[1] = qq[3] * e[1] + qq[1] * e[3] + qq[2] * e[0] - qq[0] * e[2];
+    r[2] = qq[3] * e[2] + qq[2] * e[3] + qq[0] * e[1] - qq[1] * e[0];
+    const double alpha = (3.0 - (r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3])) / 2.0;
+    for (int k = 0; k < 4; ++k) qo[iq + k] = r[k] * alpha;
+    return;
+  }
+  const double c0 = q[iq + 2], s0 = q[iq + 3], vx = v[iv], vy = v[iv + 1], w = v[iv + 2];
+  double sv, cv;
+  sincos(w, &sv, &cv);
+  double t0 = vx, t1 = vy;
+  if (fabs(w) > 1e-14) {
+    t0 = (-vy - (-vy * cv + vx * (-sv))) / w;
+    t1 = (vx - (-vy * sv + vx * cv)) / w;
+  }
+  qo[iq] = c0 * t0 - s0 * t1 + q[iq];
+  qo[iq + 1] = s0 * t0 + c0 * t1 + q[iq + 1];
+  qo[iq + 2] = c0 * cv - s0 * sv;
+  qo[iq + 3] = s0 * cv + c0 * sv;
+}
 GB_HD void integrate_one(const MView& m, const In& q, const In& v, const Out& qo) {
   const double eps = eps_of<double>();
   const double ts_prec = 1.2207031250000000e-04;  // eps^(1/4): Taylor switch of exp3 / exp6
   for (int i = 1; i < m.nj; ++i) {
     const int iq = m.idx_q[i], iv = m.idx_v[i];
+    if (jt_three(m.jtype[i])) {
+      integrate_three(m.jtype[i], q, v, iq, iv, qo);
+      continue;
+    }
     if (m.jtype[i] != JT_FF) {
       qo[iq] = q[iq] + v[iv];
       continue;

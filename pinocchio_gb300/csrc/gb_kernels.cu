@@ -44,14 +44,14 @@ __global__ void __launch_bounds__(kThreads) k_rnea(const unsigned char* blob, in
   gb::rnea_one<S, CAP>(m, in_at(q, b), in_at(v, b), in_at(a, b), out_at(tau, b));
 }
 
-template <class S, class SS, int CAP>
+template <class S, class SS, int CAP, bool J3>
 __global__ void __launch_bounds__(kThreads, GB_ABA_MINB) k_aba(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr tau,
                                                   Arr ddq) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
-  gb::aba_one<S, SS, CAP>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b));
+  gb::aba_one<S, SS, CAP, J3>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b));
 }
 
 // RNEA / ABA with external forces fext (njoints x 6 per configuration, in the
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kThreads) k_rnea_fext(const unsigned char* blo
   gb::rnea_one<S, CAP>(m, in_at(q, b), in_at(v, b), in_at(a, b), out_at(tau, b), &fe);
 }
 
-template <class S, class SS, int CAP>
+template <class S, class SS, int CAP, bool J3>
 __global__ void __launch_bounds__(kThreads, GB_ABA_MINB) k_aba_fext(const unsigned char* blob, int bytes, long B,
                                                                     Arr q, Arr v, Arr tau, Arr fext, Arr ddq) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kThreads, GB_ABA_MINB) k_aba_fext(const unsign
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
   const gb::In fe = in_at(fext, b);
-  gb::aba_one<S, SS, CAP>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b), &fe);
+  gb::aba_one<S, SS, CAP, J3>(m, in_at(q, b), in_at(v, b), in_at(tau, b), out_at(ddq, b), &fe);
 }
 
 template <class S, int CAP>
@@ -169,10 +169,17 @@ int launch_aba(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, 
   constexpr int GB_FUNC_ID = GB_FUNC_ABA;
   if (M->layout[GB_FUNC_ID] == GB_INSTANCE_PER_WARP) return launch_aba_warp(M, precision, B, q, v, tau, ddq, st);
   if (M->layout[GB_FUNC_ID] == GB_INSTANCE_PER_BRANCH) return launch_aba_branch(M, precision, B, q, v, tau, ddq, st);
+  if (M->has_three) {  // spherical / planar joints: the kernels with the three-dof steps
+    if (precision == GB_FP64) {
+      GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C, true>), q, v, tau, ddq));
+    } else {
+      GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<float, double, C, true>), q, v, tau, ddq));
+    }
+  }
   if (precision == GB_FP64) {
-    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C>), q, v, tau, ddq));
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<double, double, C, false>), q, v, tau, ddq));
   } else {
-    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<float, double, C>), q, v, tau, ddq));
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba<float, double, C, false>), q, v, tau, ddq));
   }
 }
 
@@ -189,10 +196,17 @@ int launch_rnea_fext(const gb_model* M, int precision, long B, Arr q, Arr v, Arr
 int launch_aba_fext(const gb_model* M, int precision, long B, Arr q, Arr v, Arr tau, Arr fext, Arr ddq,
                     cudaStream_t st) {
   constexpr int GB_FUNC_ID = GB_FUNC_ABA;
+  if (M->has_three) {
+    if (precision == GB_FP64) {
+      GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<double, double, C, true>), q, v, tau, fext, ddq));
+    } else {
+      GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<float, double, C, true>), q, v, tau, fext, ddq));
+    }
+  }
   if (precision == GB_FP64) {
-    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<double, double, C>), q, v, tau, fext, ddq));
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<double, double, C, false>), q, v, tau, fext, ddq));
   } else {
-    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<float, double, C>), q, v, tau, fext, ddq));
+    GB_CAP_SWITCH(M->cap, GB_LAUNCH((k_aba_fext<float, double, C, false>), q, v, tau, fext, ddq));
   }
 }
 

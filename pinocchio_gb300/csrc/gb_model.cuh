@@ -19,14 +19,26 @@
 
 namespace gb {
 
-enum { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7 };
+// JT_SPH / JT_PL: spherical (quaternion q, angular velocity v in the joint frame) and planar
+// ((x, y, cos, sin), (vx, vy, wz) in the joint frame) joints, the C ABI's values
+enum { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7, JT_SPH = 11, JT_PL = 12 };
 
 // One-dof joints (revolute RX/RY/RZ, prismatic PX/PY/PZ): the coordinate axis,
 // whether the joint slides along it, and its entry of the motion subspace S
 // (3 + axis, angular, for a revolute joint; axis, linear, for a prismatic one).
-GB_HD bool jt_slides(int jt) { return jt >= JT_PX; }
+GB_HD bool jt_slides(int jt) { return jt >= JT_PX && jt <= JT_PZ; }
 GB_HD int jt_axis(int jt) { return jt >= JT_PX ? jt - JT_PX : jt - JT_RX; }
 GB_HD int jt_sidx(int jt) { return jt >= JT_PX ? jt - JT_PX : jt + 2; }
+// Every supported joint's motion subspace is made of unit spatial axes of its frame:
+// jt_nv(jt) dofs, dof k along spatial axis jt_col(jt, k) ([linear; angular] index):
+// the free-flyer all six (joint-free-flyer.hpp), the spherical joint the angular three
+// (JointMotionSubspaceSphericalTpl, joint-spherical.hpp), the planar joint vx, vy, wz
+// (JointMotionSubspacePlanarTpl, joint-planar.hpp:380-470), a one-dof joint its axis.
+GB_HD bool jt_three(int jt) { return jt == JT_SPH || jt == JT_PL; }
+GB_HD int jt_nv(int jt) { return jt == JT_FF ? 6 : jt_three(jt) ? 3 : 1; }
+GB_HD int jt_col(int jt, int k) {
+  return jt == JT_FF ? k : jt == JT_SPH ? 3 + k : jt == JT_PL ? (k < 2 ? k : 5) : jt_sidx(jt);
+}
 
 struct BlobHeader {
   int nj, nq, nv, bytes;

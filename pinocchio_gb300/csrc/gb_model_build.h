@@ -33,6 +33,7 @@ struct gb_model {
   // carries (-1 for the intermediate joints of an expanded translation joint)
   int nj_user = 0;
   std::vector<int> ujoint;
+  bool has_three = false;  // spherical or planar joints (three dofs along unit axes of the joint frame)
   // the model's device, read once at creation: multiprocessors (grid sizes of the
   // persistent kernels) and the opt-in shared memory per block
   int sm_count = 0, smem_optin = 0;
@@ -132,6 +133,9 @@ inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err)
 // kernels then see only one-dof joints there.  `expanded` is the internal tree; user_of[i] is
 // the caller's joint of internal joint i (-1 for the two intermediate ones), last_of[j] the
 // internal joint carrying the caller's joint j.
+static_assert((int)GB_JOINT_SPHERICAL == (int)gb::JT_SPH && (int)GB_JOINT_PLANAR == (int)gb::JT_PL &&
+                  (int)GB_JOINT_FREEFLYER == (int)gb::JT_FF,
+              "the kernels use the C ABI's joint codes");
 struct ExpandedTree {
   std::vector<int> parents, jtype, user_of, last_of;
   std::vector<double> placement, inertia, axis;
@@ -208,9 +212,8 @@ inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
   int nq = 0, nv = 0, nff = 0;
   for (int i = 1; i < nj; ++i) {
     const int jt = M->jtype[i], p = M->parents[i];
-    if (jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR)
-      return set_error(GB_ERR_UNSUPPORTED, "spherical and planar joints are not supported by the batched kernels");
-    if (jt < GB_JOINT_RX || jt > GB_JOINT_PRISMATIC_UNALIGNED)
+    const bool three = jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR;
+    if (!three && (jt < GB_JOINT_RX || jt > GB_JOINT_PRISMATIC_UNALIGNED))
       return set_error(GB_ERR_UNSUPPORTED, "joint " + std::to_string(i) + ": unsupported joint type");
     if (p < 0 || p >= i) return set_error(GB_ERR_INVALID_ARGUMENT, "parents[i] must satisfy 0 <= parents[i] < i");
     if (jt == GB_JOINT_FREEFLYER) {
@@ -220,8 +223,9 @@ inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
     }
     M->idx_q[i] = nq;
     M->idx_v[i] = nv;
-    M->nvs[i] = jt == GB_JOINT_FREEFLYER ? 6 : 1;
-    nq += jt == GB_JOINT_FREEFLYER ? 7 : 1;
+    M->nvs[i] = jt == GB_JOINT_FREEFLYER ? 6 : three ? 3 : 1;
+    nq += jt == GB_JOINT_FREEFLYER ? 7 : three ? 4 : 1;
+    M->has_three = M->has_three || three;
     nv += M->nvs[i];
     M->depth[i] = M->depth[p] + 1;
     M->max_depth = std::max(M->max_depth, M->depth[i]);

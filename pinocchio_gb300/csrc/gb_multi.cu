@@ -126,6 +126,9 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
   for (int k = 0; k < ntasks; ++k) {
     const gb_task& t = tasks[k];
     if (t.model == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, "task model is NULL");
+    if (t.model->has_three)
+      return set_error(GB_ERR_UNSUPPORTED, "spherical and planar joints: the heterogeneous launch does not take them "
+                                           "(gb_rnea / gb_aba do)");
     if (t.function != GB_FUNC_RNEA && t.function != GB_FUNC_ABA) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown task function");
     if (t.batch < 0) return set_error(GB_ERR_SIZE, "task batch must be >= 0");
     if (t.batch > 0) {

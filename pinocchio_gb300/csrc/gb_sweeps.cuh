@@ -85,7 +85,8 @@ template <int TS> __device__ __forceinline__ long sweep_config() {
   } while (0)
 
 // FE: with external forces (read from fext; otherwise fext is not touched)
-template <class K, class SS, int TS, bool FE = false>
+// J3: with the three-dof steps of spherical / planar joints (one thread per configuration)
+template <class K, class SS, int TS, bool FE = false, bool J3 = false>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_aba_derivs_pass12(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, SS* wsSS, K* wsMB,
                         int npk, Arr q, Arr v, Arr tau, Arr fext) {
@@ -94,12 +95,12 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
   const long b = sweep_config<TS>();
   if (b >= B) return;
   const gb::In fe = in_at(fext, b);
-  GB_SWEEP_CALL((gb::aba_derivs_pass12<K, SS>), m, L, gb::Ws<K>{wsK + b, B},
+  GB_SWEEP_CALL((gb::aba_derivs_pass12<K, SS, J3>), m, L, gb::Ws<K>{wsK + b, B},
                 gb::Ws<SS>{wsSS + b, B}, blocked(wsMB, npk, b), in_at(q, b), in_at(v, b), in_at(tau, b),
                 FE ? &fe : nullptr);
 }
 
-template <class S, class T, class K, int TS, bool FE = false>
+template <class S, class T, class K, int TS, bool FE = false, bool J3 = false>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_aba_derivs_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, K* wsMB,
                        int npk, Arr v, Arr ddq, Arr fext) {
@@ -109,13 +110,13 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
   if (b >= B) return;
   const gb::Out dd = out_at(ddq, b);
   const gb::In fe = in_at(fext, b);
-  GB_SWEEP_CALL((gb::aba_derivs_pass3<S, T, K, false>), m, L, m.slot, gb::Ws<S>{wsS + b, B},
+  GB_SWEEP_CALL((gb::aba_derivs_pass3<S, T, K, false, J3>), m, L, m.slot, gb::Ws<S>{wsS + b, B},
                 gb::Ws<K>{wsK + b, B}, blocked(wsMB, npk, b), in_at(v, b), ddq.p ? &dd : nullptr,
                 FE ? &fe : nullptr);
 }
 
 // the Minv recursion of computeMinverse (pass 3 without velocities and column sets)
-template <class K, int TS>
+template <class K, int TS, bool J3 = false>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_minverse_pass3(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, K* wsK, K* wsMB, int npk) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -123,18 +124,18 @@ __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
   const long b = sweep_config<TS>();
   if (b >= B) return;
   const gb::Ws<K> zk = gb::Ws<K>{wsK + b, B};
-  GB_SWEEP_CALL((gb::aba_derivs_pass3<K, K, K, true>), m, L, m.slot, zk, zk, blocked(wsMB, npk, b),
+  GB_SWEEP_CALL((gb::aba_derivs_pass3<K, K, K, true, J3>), m, L, m.slot, zk, zk, blocked(wsMB, npk, b),
                 gb::In{nullptr, 0}, nullptr, nullptr);
 }
 
-template <class S, class T, class K, class P, int TS>
+template <class S, class T, class K, class P, int TS, bool J3 = false>
 __global__ void __launch_bounds__(kThreads, GB_DERIV_MINB)
     k_aba_derivs_pass4(const unsigned char* blob, int bytes, long B, gb::DerivLayout L, S* wsS, K* wsK, P* wsP) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = sweep_config<TS>();
   if (b >= B) return;
-  GB_SWEEP_CALL((gb::aba_derivs_pass4<S, T, K, P>), m, L, gb::Ws<S>{wsS + b, B},
+  GB_SWEEP_CALL((gb::aba_derivs_pass4<S, T, K, P, J3>), m, L, gb::Ws<S>{wsS + b, B},
                 gb::Ws<K>{wsK + b, B}, blocked(wsP, L.nP, b));
 }
 
@@ -177,92 +178,100 @@ template <int TS> void sweep_grid(const gb_model* M, long B, int& tpb, long& gri
   grid = (B + per - 1) / per;
 }
 
-template <class S, class T3, class T, class K, class SS, class P, int TS, bool FE = false>
+template <class S, class T3, class T, class K, class SS, class P, int TS, bool FE, bool J3>
 int launch_sweeps_as(const gb_model* M, long B, const gb::DerivLayout& L, Arr q, Arr v, Arr tau, Arr ddq, SS* wsSS,
                      K* wsK, S* wsS, K* wsMB, P* wsP, int npk, cudaStream_t st, Arr fext) {
   int tpb;
   long grid;
   sweep_grid<TS>(M, B, tpb, grid);
-  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS, TS, FE>, "k_aba_derivs_pass12");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T3, K, TS, FE>, "k_aba_derivs_pass3");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, T, K, P, TS>, "k_aba_derivs_pass4");
+  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS, TS, FE, J3>, "k_aba_derivs_pass12");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass3<S, T3, K, TS, FE, J3>, "k_aba_derivs_pass3");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_aba_derivs_pass4<S, T, K, P, TS, J3>, "k_aba_derivs_pass4");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass12<K, SS, TS, FE><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
+  k_aba_derivs_pass12<K, SS, TS, FE, J3><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
       M->d_blob, M->stage_bytes, B, L, wsK, wsSS, wsMB, npk, q, v, tau, fext);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass3<S, T3, K, TS, FE><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
+  k_aba_derivs_pass3<S, T3, K, TS, FE, J3><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
       M->d_blob, M->stage_bytes, B, L, wsS, wsK, wsMB, npk, v, ddq, fext);
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass3");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass4<S, T, K, P, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L,
-                                                                                       wsS, wsK, wsP);
+  k_aba_derivs_pass4<S, T, K, P, TS, J3><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B,
+                                                                                           L, wsS, wsK, wsP);
   return cuda_error(cudaGetLastError(), "k_aba_derivs_pass4");
 }
 
-template <class K, class SS, int TS>
+template <class K, class SS, int TS, bool J3>
 int minverse_sweeps_as(const gb_model* M, long B, const gb::DerivLayout& L, Arr q, Arr zero, SS* wsSS, K* wsK,
                        K* wsMB, int npk, cudaStream_t st) {
   int tpb;
   long grid;
   sweep_grid<TS>(M, B, tpb, grid);
-  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS, TS>, "k_aba_derivs_pass12");
-  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_minverse_pass3<K, TS>, "k_minverse_pass3");
+  int rc = blob_smem(M, (const void*)k_aba_derivs_pass12<K, SS, TS, false, J3>, "k_aba_derivs_pass12");
+  if (rc == GB_OK) rc = blob_smem(M, (const void*)k_minverse_pass3<K, TS, J3>, "k_minverse_pass3");
   if (rc != GB_OK) return rc;
-  k_aba_derivs_pass12<K, SS, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L, wsK,
-                                                                                   wsSS, wsMB, npk, q, zero, zero,
-                                                                                   Arr{nullptr, 0, 0});
+  k_aba_derivs_pass12<K, SS, TS, false, J3><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(
+      M->d_blob, M->stage_bytes, B, L, wsK, wsSS, wsMB, npk, q, zero, zero, Arr{nullptr, 0, 0});
   rc = cuda_error(cudaGetLastError(), "k_aba_derivs_pass12");
   if (rc != GB_OK) return rc;
-  k_minverse_pass3<K, TS><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L, wsK, wsMB,
-                                                                            npk);
+  k_minverse_pass3<K, TS, J3><<<(unsigned)grid, tpb, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, L, wsK,
+                                                                                wsMB, npk);
   return cuda_error(cudaGetLastError(), "k_minverse_pass3");
 }
 
-template <class S, class T3, class T, class K, class SS, class P, int TS, bool FE = false>
+template <class S, class T3, class T, class K, class SS, class P, int TS, bool FE, bool J3>
 int aba_sweeps_on(const SweepCall& c) {
   const gb_model* M = c.M;
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   const AbaWs W = aba_ws_layout<S, K, SS, P>(L, M->nv, c.B);
   char* base = static_cast<char*>(c.ws);
-  return launch_sweeps_as<S, T3, T, K, SS, P, TS, FE>(
+  return launch_sweeps_as<S, T3, T, K, SS, P, TS, FE, J3>(
       M, c.B, L, c.q, c.v, c.tau, c.ddq, reinterpret_cast<SS*>(base), reinterpret_cast<K*>(base + W.oK),
       reinterpret_cast<S*>(base + W.oS), reinterpret_cast<K*>(base + W.oMB), reinterpret_cast<P*>(base + W.oP),
       M->nv * (M->nv + 1) / 2, c.st, c.fext);
 }
 
-template <class K, class SS, int TS>
+template <class K, class SS, int TS, bool J3>
 int minverse_sweeps_on(const SweepCall& c) {
   const gb_model* M = c.M;
   const gb::DerivLayout L = gb::make_deriv_layout(M->nj, M->nv, M->nslot, true);
   const AbaWs W = aba_ws_layout<K, K, SS, K>(L, M->nv, c.B);
   char* base = static_cast<char*>(c.ws);
-  return minverse_sweeps_as<K, SS, TS>(M, c.B, L, c.q, c.v, reinterpret_cast<SS*>(base),
-                                       reinterpret_cast<K*>(base + W.oK), reinterpret_cast<K*>(base + W.oMB),
-                                       M->nv * (M->nv + 1) / 2, c.st);
+  return minverse_sweeps_as<K, SS, TS, J3>(M, c.B, L, c.q, c.v, reinterpret_cast<SS*>(base),
+                                           reinterpret_cast<K*>(base + W.oK), reinterpret_cast<K*>(base + W.oMB),
+                                           M->nv * (M->nv + 1) / 2, c.st);
 }
 
-// the kernels of one team size for every precision and variant
-template <int TS>
-int sweeps_for(const SweepCall& c) {
+// the kernels of one team size (and with or without the three-dof steps) for every precision and variant
+template <int TS, bool J3>
+int sweeps_kinds(const SweepCall& c) {
   using gb::dfloat;
   if (c.fext.p) {  // external forces: one thread per configuration, ddq and the derivatives
     if constexpr (TS == 1) {
-      if (c.kind == kSweepFp64) return aba_sweeps_on<double, double, double, double, double, double, 1, true>(c);
-      if (c.kind == kSweepMixed) return aba_sweeps_on<float, float, dfloat, dfloat, double, float, 1, true>(c);
-      if (c.kind == kSweepMixedDf) return aba_sweeps_on<dfloat, dfloat, dfloat, dfloat, double, dfloat, 1, true>(c);
+      if (c.kind == kSweepFp64) return aba_sweeps_on<double, double, double, double, double, double, 1, true, J3>(c);
+      if (c.kind == kSweepMixed) return aba_sweeps_on<float, float, dfloat, dfloat, double, float, 1, true, J3>(c);
+      if (c.kind == kSweepMixedDf)
+        return aba_sweeps_on<dfloat, dfloat, dfloat, dfloat, double, dfloat, 1, true, J3>(c);
     }
     return set_error(GB_ERR_INVALID_ARGUMENT, "external forces: unsupported sweep variant");
   }
   switch (c.kind) {
-    case kSweepFp64: return aba_sweeps_on<double, double, double, double, double, double, TS>(c);
-    case kSweepMixed: return aba_sweeps_on<float, float, dfloat, dfloat, double, float, TS>(c);
-    case kSweepMixedVjp: return aba_sweeps_on<float, float, dfloat, dfloat, double, dfloat, TS>(c);
-    case kSweepMixedDf: return aba_sweeps_on<dfloat, dfloat, dfloat, dfloat, double, dfloat, TS>(c);
-    case kMinvFp64: return minverse_sweeps_on<double, double, TS>(c);
-    case kMinvMixed: return minverse_sweeps_on<dfloat, double, TS>(c);
+    case kSweepFp64: return aba_sweeps_on<double, double, double, double, double, double, TS, false, J3>(c);
+    case kSweepMixed: return aba_sweeps_on<float, float, dfloat, dfloat, double, float, TS, false, J3>(c);
+    case kSweepMixedVjp: return aba_sweeps_on<float, float, dfloat, dfloat, double, dfloat, TS, false, J3>(c);
+    case kSweepMixedDf: return aba_sweeps_on<dfloat, dfloat, dfloat, dfloat, double, dfloat, TS, false, J3>(c);
+    case kMinvFp64: return minverse_sweeps_on<double, double, TS, J3>(c);
+    case kMinvMixed: return minverse_sweeps_on<dfloat, double, TS, J3>(c);
   }
   return set_error(GB_ERR_INVALID_ARGUMENT, "unknown sweep kind");
+}
+// models with spherical / planar joints run one configuration per thread (the layout setting
+// refuses the others) with the three-dof steps compiled in
+template <int TS>
+int sweeps_for(const SweepCall& c) {
+  if constexpr (TS == 1)
+    if (c.M->has_three) return sweeps_kinds<1, true>(c);
+  return sweeps_kinds<TS, false>(c);
 }
 
 }  // namespace

@@ -8,18 +8,20 @@ children in file order, as MjcfGraph::parseGraph / fillModel do:
   ``body pose * joint pos`` in the frame of its parent body (addSoloJoint, mjcf-graph.cpp:918-971);
   the body's inertia goes to that joint, expressed in the joint frame (``bodyInJoint = joint
   pos^-1``); ``hinge`` -> revolute, ``slide`` -> prismatic (aligned or unaligned by the axis, as the
-  URDF loader maps axes), ``free`` -> the free-flyer (root body only);
+  URDF loader maps axes), ``ball`` -> the spherical joint (mjcf-graph.cpp:946-951), ``free`` -> the
+  free-flyer (root body only);
 * a body without a joint is welded to its parent: its inertia is merged into the parent's joint
   (addFixedJointAndBody);
 * body poses: ``pos`` with ``quat`` (w x y z), ``axisangle`` or ``euler`` (the compiler's
   ``eulerseq``, lowercase: rotating axes) in the compiler's ``angle`` unit, degrees by default
   (MjcfCompiler, mjcf-graph.cpp:102-116, 720-770);
 * ``<inertial pos quat mass diaginertia|fullinertia>`` gives the body's inertia (the principal
-  frame rotated by ``quat``); a joint's ``armature`` becomes the model's armature on its dofs.
+  frame rotated by ``quat``); a joint's ``armature`` becomes the model's armature on each of its
+  dofs (mjcf-graph.cpp:966-970).
 
 Outside the subset (each raises ValueError, so that no model is silently different from the
 reference's): ``<default>`` classes and ``class`` / ``childclass`` attributes, ``<include>``,
-bodies with several joints (the reference's composite joints), ``ball`` joints, free joints below
+bodies with several joints (the reference's composite joints), free joints below
 the root, ``xyaxes`` / ``zaxis`` orientations, uppercase (fixed-axis) Euler sequences, and bodies
 whose inertia MuJoCo would infer from their ``<geom>`` elements (``inertiafromgeom``; a body with
 geoms needs an ``<inertial>`` unless the compiler sets ``inertiafromgeom="false"``).
@@ -30,7 +32,7 @@ import xml.etree.ElementTree as ET
 
 import numpy as np
 
-from .model import JT_FF, Inertia, JointModelFreeFlyer, Model, SE3
+from .model import JT_FF, Inertia, JointModelFreeFlyer, JointModelSpherical, Model, SE3
 from .urdf import _OneDof, _mul, _floats
 from .model import JT_PX, JT_PY, JT_PZ, JT_RX, JT_RY, JT_RZ, JointModelPrismaticUnaligned, JointModelRevoluteUnaligned
 
@@ -114,6 +116,8 @@ def _body_inertia(body, comp: _Compiler) -> Inertia:
 
 def _joint_model(j, comp: _Compiler):
     kind = j.get("type", "hinge")
+    if kind == "ball":
+        return JointModelSpherical()
     if kind not in _ALIGNED:
         raise ValueError(f"joint {j.get('name')!r}: type {kind!r} is not supported by the batched kernels")
     ax = _floats(j.get("axis"), 3, [0, 0, 1])
@@ -177,7 +181,8 @@ def buildModelFromMJCFXML(xml: str) -> Model:
                 jid = model.addJoint(parent_joint, _joint_model(j, comp), _mul(pose, jpos), name)
                 arm = float(j.get("armature", "0"))
                 if arm:
-                    model.armature[model.idx_vs[jid]] = arm
+                    iv = model.idx_vs[jid]
+                    model.armature[iv:iv + model.nvs[jid]] = arm
             body_in_joint = SE3(np.eye(3), -jpos.translation)
             if Y.mass > 0.0 or Y.inertia.any():
                 model.appendBodyToJoint(jid, Y, body_in_joint)

@@ -16,8 +16,11 @@ relative 1e-12) gives JointModelRX/RY/RZ (``revolute``, ``continuous``) or Joint
 (``prismatic``); any other axis, negative ones included, gives JointModelRevoluteUnaligned /
 JointModelPrismaticUnaligned with the normalised axis.  One difference: the reference makes a
 ``continuous`` joint a JointModelRevoluteUnbounded (nq = 2, q = (cos, sin)); here it is the bounded
-revolute joint (nq = 1, q = the angle), with the same dynamics in the angle.  Other joint types
-(planar, floating inside the tree) raise ValueError.
+revolute joint (nq = 1, q = the angle), with the same dynamics in the angle.  ``planar`` gives
+JointModelPlanar (motion in the joint frame's xy plane, the axis ignored, as the reference's
+UrdfVisitor::addJointAndBody, model.hxx:285-290); ``floating`` gives the free-flyer on the root
+link (the kernels run the free-flyer as the root joint only; a ``floating`` joint inside the tree
+raises ValueError).
 
 ``save_model`` / ``load_model`` write and read the flattened tables (``Model.tables()`` plus the joint
 names) as one ``.npz`` file: the on-disk format of a model (the reference serialises ModelTpl with
@@ -43,6 +46,7 @@ from .model import (
     Inertia,
     JointModel,
     JointModelFreeFlyer,
+    JointModelPlanar,
     JointModelPrismaticUnaligned,
     JointModelRevoluteUnaligned,
     Model,
@@ -164,8 +168,9 @@ def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
             if jt == "fixed":
                 append(joint_id, child, Pj)
                 visit(child, (joint_id, Pj))
-            elif jt in _AXIS_JT:
-                new_id = model.addJoint(joint_id, _axis_joint(j), Pj, j.get("name"))
+            elif jt in _AXIS_JT or jt == "planar" or (jt == "floating" and joint_id == 0):
+                jm = _axis_joint(j) if jt in _AXIS_JT else JointModelPlanar() if jt == "planar" else JointModelFreeFlyer()
+                new_id = model.addJoint(joint_id, jm, Pj, j.get("name"))
                 append(new_id, child, SE3.Identity())
                 visit(child, (new_id, SE3.Identity()))
             else:

@@ -63,8 +63,8 @@ int hs_aba(void* h, int mixed, long B, const double* q, const double* v, const d
   for (long b = 0; b < B; ++b) {
     const gb::In fe = in_at(fext, b, 6L * m.nj);
     const gb::In* fp = fext ? &fe : nullptr;
-    if (mixed) { HS_DISPATCH(M->cap, (gb::aba_one<float, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv), fp))); }
-    else { HS_DISPATCH(M->cap, (gb::aba_one<double, double, C>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv), fp))); }
+    if (mixed) { HS_DISPATCH(M->cap, (gb::aba_one<float, double, C, true>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv), fp))); }
+    else { HS_DISPATCH(M->cap, (gb::aba_one<double, double, C, true>(m, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(tau, b, m.nv), out_at(ddq, b, m.nv), fp))); }
   }
   return 0;
 }
@@ -110,10 +110,10 @@ extern "C" int hs_rnea_derivs(void* h, int mixed, int symmetric, long B, const d
       const gb::In fe = in_at(fext, b, 6L * m.nj);
       const gb::In* fp = fext ? &fe : nullptr;
       if (mixed)
-        gb::rnea_derivs_one<float>(m, L, gb::Ws<float>{wf.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
+        gb::rnea_derivs_one<float, true>(m, L, gb::Ws<float>{wf.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
                                    out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false, fp);
       else
-        gb::rnea_derivs_one<double>(m, L, gb::Ws<double>{wd.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
+        gb::rnea_derivs_one<double, true>(m, L, gb::Ws<double>{wd.data(), 1}, in_at(q, b, m.nq), in_at(v, b, m.nv), in_at(a, b, m.nv),
                                     out_at(dq, b, nn), out_at(dv, b, nn), out_at(Mo, b, nn), &to, symmetric != 0, false, fp);
     }
   }
@@ -135,7 +135,7 @@ static void aba_derivs_host(const gb_model* M, const gb::MView& m, long b, const
   const gb::Out dd = out_at(ddq, b, nv);
   const gb::In fe = in_at(fext, b, 6L * m.nj);
   std::vector<K> wM(nv * (nv + 1) / 2);
-  gb::aba_derivs_sweeps<S, T3, T, K, double, P>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
+  gb::aba_derivs_sweeps<S, T3, T, K, double, P, true>(m, L, m.slot, gb::Ws<S>{wS.data(), 1}, gb::Ws<K>{wK.data(), 1},
                                                 gb::Ws<double>{wSS.data(), 1}, gb::Ws<K>{wM.data(), 1},
                                                 gb::Ws<P>{wP.data(), 1}, in_at(q, b, m.nq), in_at(v, b, nv),
                                                 in_at(tau, b, nv), &dd, fext ? &fe : nullptr);

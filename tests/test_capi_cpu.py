@@ -75,13 +75,12 @@ def test_tree_validation(L):
     rc, _ = _create(L, m.tables())
     assert rc == _capi.GB_ERR_UNSUPPORTED
     assert b"depth-first" in L.gb_last_error()
-    # spherical and planar joints are outside the kernels' joint types (the oracle has them)
-    for joint in (gm.JointModelSpherical(), gm.JointModelPlanar()):
-        m = gm.Model()
-        m.addJoint(0, joint, gm.SE3.Identity(), "a")
-        rc, _ = _create(L, m.tables())
-        assert rc == _capi.GB_ERR_UNSUPPORTED
-        assert b"spherical and planar" in L.gb_last_error()
+    # an unknown joint type code
+    t = sm.manipulator6r().tables()
+    t["jtype"] = t["jtype"].copy()
+    t["jtype"][3] = 13
+    rc, _ = _create(L, t)
+    assert rc == _capi.GB_ERR_UNSUPPORTED
     # armature of the wrong size
     t = sm.manipulator6r().tables()
     t["armature"] = np.zeros(3)

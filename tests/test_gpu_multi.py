@@ -213,3 +213,27 @@ def test_autotuner_chooses_a_derivative_layout(tmp_path, monkeypatch):
     assert setting in autotune.CANDIDATES or setting in (autotune.LANES4, autotune.LANES8, autotune.WARP)
     for a, b in zip(before, pg.computeABADerivatives(model, data, q, v, x)):
         assert torch.equal(a, b)
+
+
+def test_three_dof_joints_run_per_thread(tmp_path, monkeypatch):
+    """Models with spherical or planar joints run one configuration per thread: the lane
+    layouts are refused, the autotuner keeps to CTA sizes, and gb_batch_multi refuses them."""
+    import torch
+
+    from util import MODELS
+
+    monkeypatch.setattr(autotune, "CACHE_PATH", str(tmp_path / "tune.json"))
+    model = MODELS["multidoftree16"]()
+    data = pg.createData(model)
+    L = pg._capi.lib()
+    for f, layout in ((pg._capi.GB_FUNC_RNEA, pg._capi.GB_INSTANCE_PER_WARP),
+                      (pg._capi.GB_FUNC_ABA, pg._capi.GB_INSTANCE_PER_BRANCH),
+                      (pg._capi.GB_FUNC_ABA_DERIVATIVES, pg._capi.GB_INSTANCE_PER_4_LANES)):
+        assert L.gb_model_set_layout(data.dev.h, f, layout) == pg._capi.GB_ERR_UNSUPPORTED
+    res = autotune.tune(model, data, batch=256, use_cache=False)
+    assert all(s in autotune.CANDIDATES for s, _ in res.values())
+    q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 64, 5))
+    ddq_o = OracleModel(model).aba(*(t.cpu().numpy() for t in (q, v, x)), LOCAL)
+    assert rel_err(pg.aba(model, data, q, v, x).cpu().numpy(), ddq_o) < FP64_TOL
+    with pytest.raises(pg._capi.GBError):
+        api.MultiBatch([(data, "aba", q, v, x)]).run()

@@ -121,7 +121,6 @@ def test_orientation_forms_and_units():
 
 @pytest.mark.parametrize("snippet, msg", [
     ('<default><joint damping="1"/></default><worldbody/>', "default"),
-    ('<worldbody><body name="a"><joint type="ball"/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "ball"),
     ('<worldbody><body name="a"><joint/><joint type="slide"/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "several"),
     ('<worldbody><body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody>', "geom"),
     ('<worldbody><body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/>'
@@ -145,3 +144,23 @@ def test_geoms_ignored_when_inertia_not_from_geoms():
     m = buildModelFromMJCFXML("""<mujoco><compiler inertiafromgeom="false"/><worldbody>
       <body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody></mujoco>""")
     assert m.nv == 1 and m.inertias[1].mass == 0.0
+
+
+def test_ball_joint():
+    """A ``ball`` joint gives the spherical joint at ``body pose * joint pos`` with the armature on
+    its three dofs (reference mjcf-graph.cpp:946-970); the dynamics match the same model built
+    through the construction API."""
+    m = buildModelFromMJCFXML("""<mujoco><worldbody>
+      <body name="a" pos="0 0 1"><joint type="hinge" axis="0 1 0"/><inertial mass="1" diaginertia="0.1 0.2 0.3"/>
+        <body name="b" pos="0.4 0 0"><joint type="ball" pos="0.1 0 0" armature="0.05"/>
+          <inertial pos="0.2 0 0" mass="2" diaginertia="0.2 0.3 0.4"/></body></body></worldbody></mujoco>""")
+    assert m.jtypes[1:] == [gm.JT_RY, gm.JT_SPH] and m.nq == 5 and m.nv == 4
+    assert np.array_equal(m.armature, [0, 0.05, 0.05, 0.05])
+    ref = gm.Model()
+    j1 = ref.addJoint(0, gm.JointModelRY(), gm.SE3(np.eye(3), np.array([0.0, 0, 1])), "a")
+    ref.appendBodyToJoint(j1, gm.Inertia(1.0, np.zeros(3), np.diag([0.1, 0.2, 0.3])), gm.SE3.Identity())
+    j2 = ref.addJoint(j1, gm.JointModelSpherical(), gm.SE3(np.eye(3), np.array([0.5, 0, 0])), "b")
+    ref.appendBodyToJoint(j2, gm.Inertia(2.0, np.array([0.1, 0, 0]), np.diag([0.2, 0.3, 0.4])), gm.SE3.Identity())
+    ref.armature[1:] = 0.05
+    q, v, a = sm.random_inputs(m, 8, 4)
+    assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(ref).rnea(q, v, a)) < 1e-14

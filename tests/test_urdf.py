@@ -172,8 +172,8 @@ def gm_rz(t):
 
 
 @pytest.mark.parametrize("bad,msg", [
-    ('<joint name="s" type="planar"><parent link="a"/><child link="b"/><axis xyz="1 0 0"/></joint>', "not supported"),
-    ('<joint name="s" type="floating"><parent link="a"/><child link="b"/></joint>', "not supported"),
+    ('<link name="c"/><joint name="r" type="revolute"><parent link="a"/><child link="c"/></joint>'
+     '<joint name="s" type="floating"><parent link="c"/><child link="b"/></joint>', "not supported"),
     ('<joint name="s" type="revolute"><parent link="a"/><child link="b"/><axis xyz="0 0 0"/></joint>', "zero axis"),
 ])
 def test_urdf_unsupported(bad, msg):
@@ -211,3 +211,25 @@ def test_urdf_file_and_model_file(tmp_path, name):
     for k, v in loaded.tables().items():
         assert np.array_equal(v, back.tables()[k]), k
     assert back.names == loaded.names
+
+
+def test_urdf_planar_and_floating():
+    """``planar`` gives the planar joint (the axis ignored), a root ``floating`` joint the
+    free-flyer, as the reference's UrdfVisitor::addJointAndBody (model.hxx:255-296); the
+    dynamics of the loaded model match the same model built through the construction API."""
+    inertial = ('<inertial><origin xyz="0.1 0.2 0.3"/><mass value="2"/>'
+                '<inertia ixx="0.3" ixy="0.01" ixz="0" iyy="0.2" iyz="0.02" izz="0.4"/></inertial>')
+    doc = f"""<robot name="p"><link name="w"/><link name="a">{inertial}</link><link name="b">{inertial}</link>
+      <joint name="f" type="floating"><parent link="w"/><child link="a"/><origin xyz="0 0 1"/></joint>
+      <joint name="s" type="planar"><parent link="a"/><child link="b"/><origin xyz="0.5 0 0"/>
+      <axis xyz="1 0 0"/></joint></robot>"""
+    m = pg.buildModelFromXML(doc)
+    assert m.jtypes[1:] == [gm.JT_FF, gm.JT_PL] and m.nq == 11 and m.nv == 9
+    Y = gm.Inertia(2.0, np.array([0.1, 0.2, 0.3]), np.array([[0.3, 0.01, 0], [0.01, 0.2, 0.02], [0, 0.02, 0.4]]))
+    ref = gm.Model()
+    j1 = ref.addJoint(0, gm.JointModelFreeFlyer(), gm.SE3(np.eye(3), np.array([0.0, 0, 1])), "f")
+    ref.appendBodyToJoint(j1, Y, gm.SE3.Identity())
+    j2 = ref.addJoint(j1, gm.JointModelPlanar(), gm.SE3(np.eye(3), np.array([0.5, 0, 0])), "s")
+    ref.appendBodyToJoint(j2, Y, gm.SE3.Identity())
+    q, v, a = sm.random_inputs(m, 8, 3)
+    assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(ref).rnea(q, v, a)) < 1e-14

@@ -34,9 +34,10 @@ MODELS = {
     "unaligned14": lambda: sm.unaligned_tree(14, False, 7),
     "unaligned20ff": lambda: sm.unaligned_tree(20, True, 8),
     "translationtree14": lambda: sm.translation_tree(9),
+    "multidoftree16": lambda: sm.multidof_tree(10),
 }
-# models the oracle covers beyond the kernels (spherical and planar joints)
-ORACLE_ONLY_MODELS = {"multidoftree16": lambda: sm.multidof_tree(10)}
+# models the oracle covers beyond the kernels (none at present)
+ORACLE_ONLY_MODELS = {}
 # FP64 parity bar of the batched kernels against the FP64 oracle (relative, per instance)
 FP64_TOL = 1e-12
 # mixed-precision bar (max relative error against the FP64 oracle)
@@ -44,7 +45,8 @@ MIXED_TOL = 1e-5
 # the models that cover joint types (prismatic, unaligned axes) rather than a benchmark
 # workload: their FP64 results meet FP64_TOL; their mixed-precision error, which scales with
 # each random model's conditioning, is held to 1e-4
-JOINT_TYPE_MODELS = ("mixedtree12", "mixedtree24ff", "unaligned14", "unaligned20ff", "translationtree14")
+JOINT_TYPE_MODELS = ("mixedtree12", "mixedtree24ff", "unaligned14", "unaligned20ff", "translationtree14",
+                     "multidoftree16")
 
 
 def mixed_tol(name: str) -> float:
