@@ -400,8 +400,9 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
     """The headline step through the public API (``pg.aba`` + ``pg.computeABADerivatives``) with
     the inputs in pinned host memory and every output copied back to pinned host memory, each
     step.  Outputs are double-buffered: step k's device-to-host copies run on a copy stream
-    while step k + 1's kernels run on the compute stream (two output sets on the device and on
-    the host).  Beside it, the copy floor: the same bytes moved by plain pinned copies alone."""
+    while step k + 1's kernels run on the compute stream (two output sets, preallocated and
+    passed as ``out=``, on the device and on the host).  Beside it, the copy floor: the same
+    bytes moved by plain pinned copies alone."""
     nq, nv = model.nq, model.nv
     h2d = B * (nq + 2 * nv) * 8
     d2h = B * (nv + 3 * nv * nv) * 8
@@ -418,6 +419,9 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
     copy = torch.cuda.Stream()
     din = [tuple(torch.empty(t.shape, dtype=torch.float64, device="cuda") for t in (hq[0], hv[0], ht[0]))
            for _ in range(2)]
+    dout = [(torch.empty((B, nv), dtype=torch.float64, device="cuda"),)
+            + tuple(torch.empty((B, nv, nv), dtype=torch.float64, device="cuda") for _ in range(3))
+            + (torch.empty((B, nv), dtype=torch.float64, device="cuda"),) for _ in range(2)]
     done = [torch.cuda.Event() for _ in range(2)]  # the step's kernels finished (outputs ready)
     freed = [torch.cuda.Event() for _ in range(2)]  # the step's outputs are on the host
     keep = [None, None]
@@ -429,13 +433,13 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
         q.copy_(hq[s], non_blocking=True)
         v.copy_(hv[s], non_blocking=True)
         t.copy_(ht[s], non_blocking=True)
-        ddq = pg.aba(model, d, q, v, t)
-        dq, dv, Mi = pg.computeABADerivatives(model, d, q, v, t)
+        ddq, dq, dv, Mi, ddq_d = dout[s]
+        pg.aba(model, d, q, v, t, out=ddq)
+        pg.computeABADerivatives(model, d, q, v, t, out=(dq, dv, Mi, ddq_d))
         done[s].record(comp)
         with torch.cuda.stream(copy):
             copy.wait_event(done[s])
             for name, src in (("ddq", ddq), ("ddq_dq", dq), ("ddq_dv", dv), ("Minv", Mi)):
-                src.record_stream(copy)
                 ho[s][name].copy_(src, non_blocking=True)
             freed[s].record(copy)
         keep[s] = (ddq, dq, dv, Mi)

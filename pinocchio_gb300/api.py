@@ -122,6 +122,29 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _out(out, shape, like, name: str):
+    """A preallocated output (``out=``): a contiguous CUDA float64 tensor of ``shape`` (or of
+    ``shape[1:]`` for a single configuration) that overlaps no input, else a new one on
+    ``like``'s device."""
+    torch = _torch()
+    if out is None:
+        return torch.empty(shape, dtype=torch.float64, device=like.device)
+    if isinstance(out, torch.Tensor) and shape[0] == 1 and tuple(out.shape) == tuple(shape[1:]):
+        out = out.unsqueeze(0)
+    if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float64 and out.is_contiguous()
+            and tuple(out.shape) == tuple(shape)):
+        raise ValueError(f"{name} must be a contiguous CUDA float64 tensor of shape {tuple(shape)}")
+    return out
+
+
+def _outs(out, n: int, name: str):
+    if out is None:
+        return (None,) * n
+    if not isinstance(out, (tuple, list)) or len(out) not in (n - 1, n):
+        raise ValueError(f"{name}: out must be a tuple of {n - 1} or {n} tensors")
+    return tuple(out) + (None,) * (n - len(out))
+
+
 def _fext(model: Model, fext, B: int):
     """External forces as the reference's Python bindings take them (a list of njoints
     forces, each [linear; angular] in its joint's frame, expressed in the local frame of
@@ -144,15 +167,15 @@ def _fext(model: Model, fext, B: int):
     return t.reshape(B, -1).contiguous()
 
 
-def rnea(model: Model, data: Data, q, v, a, fext=None):
+def rnea(model: Model, data: Data, q, v, a, fext=None, *, out=None):
     """tau = RNEA(q, v, a) (reference algorithm/rnea.hxx:117-161); with external forces
     fext (njoints forces in the joint frames) rnea(model, data, q, v, a, fext)
-    (rnea.hxx:164-218)."""
+    (rnea.hxx:164-218).  ``out``: a preallocated (batch, nv) CUDA tensor for tau."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     at = _as_batch(a, model.nv, "a")[0]
     B = qt.shape[0]
-    tau = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    tau = _out(out, (B, model.nv), qt, "out")
     if fext is None:
         _capi.check(
             _capi.lib().gb_rnea(
@@ -284,11 +307,12 @@ def computeStaticTorqueDerivatives(model: Model, data: Data, q, fext):
     return _ret(dq, was_np, vec)
 
 
-def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = None, fext=None):
+def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = None, fext=None, out=None):
     """ddq = ABA(q, v, tau) (reference algorithm/aba.hxx:933-948), called as the
     reference's binding is: aba(model, data, q, v, tau[, convention]) or
     aba(model, data, q, v, tau, fext[, convention]) with external forces in the
-    joint frames (aba.hxx:958-973, expose-aba.cpp:60-82)."""
+    joint frames (aba.hxx:958-973, expose-aba.cpp:60-82).  ``out``: a preallocated
+    (batch, nv) CUDA tensor for ddq."""
     if len(args) > 2:
         raise TypeError("aba takes at most fext and convention after tau")
     for x in args:
@@ -301,7 +325,7 @@ def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = Non
     vt = _as_batch(v, model.nv, "v")[0]
     tt = _as_batch(tau, model.nv, "tau")[0]
     B = qt.shape[0]
-    ddq = _torch().empty((B, model.nv), dtype=qt.dtype, device=qt.device)
+    ddq = _out(out, (B, model.nv), qt, "out")
     if fext is None:
         _capi.check(
             _capi.lib().gb_aba(
@@ -398,11 +422,12 @@ def computeKKTContactDynamicMatrixInverse(model: Model, data: Data, q, J, inv_da
     return _ret(K, was_np, vec)
 
 
-def crba(model: Model, data: Data, q, convention: int = Convention.LOCAL, symmetric: bool = True):
-    """M(q), symmetrised as the Python binding returns it (reference bindings/python/algorithm/expose-crba.cpp:22)."""
+def crba(model: Model, data: Data, q, convention: int = Convention.LOCAL, symmetric: bool = True, *, out=None):
+    """M(q), symmetrised as the Python binding returns it (reference bindings/python/algorithm/expose-crba.cpp:22).
+    ``out``: a preallocated (batch, nv, nv) CUDA tensor for M."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     B, nv = qt.shape[0], model.nv
-    M = _torch().empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
+    M = _out(out, (B, nv, nv), qt, "out")
     mode = _capi.GB_MATRIX_SYMMETRIC if symmetric else _capi.GB_MATRIX_UPPER
     _capi.check(
         _capi.lib().gb_crba(
@@ -431,18 +456,17 @@ def crbaCholesky(model: Model, data: Data, q):
     return tuple(_ret(t, was_np, vec) for t in (M, U, D))
 
 
-def computeRNEADerivatives(model: Model, data: Data, q, v, a, fext=None):
+def computeRNEADerivatives(model: Model, data: Data, q, v, a, fext=None, *, out=None):
     """(dtau_dq, dtau_dv, M) (reference algorithm/rnea-derivatives.hxx:472-541, M symmetrised as the binding does);
-    with external forces fext in the joint frames, rnea-derivatives.hxx:550-633."""
+    with external forces fext in the joint frames, rnea-derivatives.hxx:550-633.  ``out``: preallocated
+    CUDA tensors (dtau_dq, dtau_dv, M[, tau]) of shapes (batch, nv, nv) and (batch, nv)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     at = _as_batch(a, model.nv, "a")[0]
     B, nv = qt.shape[0], model.nv
-    torch = _torch()
-    dq = torch.empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
-    dv = torch.empty_like(dq)
-    M = torch.empty_like(dq)
-    tau = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
+    o = _outs(out, 4, "computeRNEADerivatives")
+    dq, dv, M = (_out(t, (B, nv, nv), qt, "out") for t in o[:3])
+    tau = _out(o[3], (B, nv), qt, "out")
     prec, h = _PREC[data.precision], data.dev.h
     if fext is None:
         rc = _capi.lib().gb_rnea_derivatives(
@@ -460,18 +484,17 @@ def computeRNEADerivatives(model: Model, data: Data, q, v, a, fext=None):
     return tuple(_ret(t, was_np, vec) for t in (dq, dv, M))
 
 
-def computeABADerivatives(model: Model, data: Data, q, v, tau, fext=None):
+def computeABADerivatives(model: Model, data: Data, q, v, tau, fext=None, *, out=None):
     """(ddq_dq, ddq_dv, Minv) (reference algorithm/aba-derivatives.hxx:380-453); with external
-    forces fext in the joint frames, aba-derivatives.hxx:463-541."""
+    forces fext in the joint frames, aba-derivatives.hxx:463-541.  ``out``: preallocated CUDA
+    tensors (ddq_dq, ddq_dv, Minv[, ddq]) of shapes (batch, nv, nv) and (batch, nv)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
     vt = _as_batch(v, model.nv, "v")[0]
     tt = _as_batch(tau, model.nv, "tau")[0]
     B, nv = qt.shape[0], model.nv
-    torch = _torch()
-    dq = torch.empty((B, nv, nv), dtype=qt.dtype, device=qt.device)
-    dv = torch.empty_like(dq)
-    Minv = torch.empty_like(dq)
-    ddq = torch.empty((B, nv), dtype=qt.dtype, device=qt.device)
+    o = _outs(out, 4, "computeABADerivatives")
+    dq, dv, Minv = (_out(t, (B, nv, nv), qt, "out") for t in o[:3])
+    ddq = _out(o[3], (B, nv), qt, "out")
     prec, h = _PREC[data.precision], data.dev.h
     if fext is None:
         rc = _capi.lib().gb_aba_derivatives(

@@ -126,3 +126,41 @@ def test_in_parallel_host_entry_points(name):
     with pytest.raises(_capi.GBError) as err:
         pg.rneaInParallel(9, pool, q.T, v.T, a.T)  # num_threads > pool.size()
     assert err.value.code == _capi.GB_ERR_POOL
+
+
+@pytest.mark.parametrize("name", ["humanoid32", "multidoftree16"])
+def test_preallocated_outputs(name):
+    """``out=`` writes the single calls' results into the caller's tensors (the same tensors are
+    returned, with the bits of the allocating calls); a wrong shape, dtype or device raises."""
+    import torch
+
+    model = MODELS[name]()
+    q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 301, 8))
+    data = pg.createData(model, "mixed")
+    B, nv = q.shape[0], model.nv
+    vec = lambda: torch.full((B, nv), np.nan, dtype=torch.float64, device="cuda")  # noqa: E731
+    mat = lambda: torch.full((B, nv, nv), np.nan, dtype=torch.float64, device="cuda")  # noqa: E731
+    o = vec()
+    assert pg.rnea(model, data, q, v, x, out=o) is o and torch.equal(o, pg.rnea(model, data, q, v, x))
+    o = vec()
+    assert pg.aba(model, data, q, v, x, out=o) is o and torch.equal(o, pg.aba(model, data, q, v, x))
+    o = mat()
+    assert pg.crba(model, data, q, out=o) is o and torch.equal(o, pg.crba(model, data, q))
+    outs = (mat(), mat(), mat(), vec())
+    got = pg.computeABADerivatives(model, data, q, v, x, out=outs)
+    assert all(a is b for a, b in zip(got, outs))
+    ref = pg.computeABADerivatives(model, data, q, v, x)
+    assert all(torch.equal(a, b) for a, b in zip(got, ref)) and torch.equal(outs[3], data.ddq)
+    outs = (mat(), mat(), mat())
+    got = pg.computeRNEADerivatives(model, data, q, v, x, out=outs)
+    ref = pg.computeRNEADerivatives(model, data, q, v, x)
+    assert all(a is b and torch.equal(a, r) for a, b, r in zip(got, outs, ref))
+    one = torch.empty(nv, dtype=torch.float64, device="cuda")
+    assert torch.equal(pg.aba(model, data, q[7], v[7], x[7], out=one), pg.aba(model, data, q, v, x)[7])
+    for bad in (torch.empty((B, nv + 1), dtype=torch.float64, device="cuda"),
+                torch.empty((B, nv), dtype=torch.float32, device="cuda"),
+                torch.empty((B, nv), dtype=torch.float64)):
+        with pytest.raises(ValueError):
+            pg.aba(model, data, q, v, x, out=bad)
+    with pytest.raises(ValueError):
+        pg.computeABADerivatives(model, data, q, v, x, out=(mat(),))
