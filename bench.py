@@ -290,14 +290,55 @@ def _time_call(torch, fn, reps=5, warmup=2):
     return s.elapsed_time(e) / reps
 
 
+def _per_config_rel_err(got, ref):
+    """max and median over configurations of ||got - ref|| / ||ref|| (one row per configuration)."""
+    n = ref.shape[0]
+    g, r = got.reshape(n, -1), ref.reshape(n, -1)
+    e = np.linalg.norm(g - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
+    return float(e.max()), float(np.median(e))
+
+
+def _function_reference(om, fname, q, v, x, f, J, g):
+    """The FP64 oracle's outputs of one benchmarked function, in the order the API returns them."""
+    from oracle.oracle import symmetrize_upper
+
+    t, z = 10.0 * x, np.zeros_like(v)
+    if fname == "crba_cholesky":
+        Mu = om.crba(q)
+        return (symmetrize_upper(Mu),) + tuple(om.cholesky(Mu))
+    if fname == "rnea_derivatives":
+        _, dq, dv, M = om.rnea_derivatives(q, v, x)
+        return dq, dv, symmetrize_upper(M)
+    return {
+        "rnea": lambda: (om.rnea(q, v, x),),
+        "aba": lambda: (om.aba(q, v, t),),
+        "crba": lambda: (symmetrize_upper(om.crba(q)),),
+        "aba_derivatives": lambda: om.aba_derivatives(q, v, t)[1:],
+        "compute_minverse": lambda: (om.aba_derivatives(q, v, t)[3],),
+        "nonlinear_effects": lambda: (om.rnea(q, v, z),),
+        "generalized_gravity": lambda: (om.rnea(q, z, z),),
+        "forward_kinematics": lambda: om.forward_kinematics(q, v, x),
+        "joint_jacobians": lambda: (np.swapaxes(om.joint_jacobians(q), 1, 2),),
+        "rnea_fext": lambda: (om.rnea(q, v, x, fext=f),),
+        "aba_fext": lambda: (om.aba(q, v, t, fext=f),),
+        "aba_derivatives_fext": lambda: om.aba_derivatives(q, v, t, fext=f)[1:],
+        "forward_dynamics_12rows": lambda: (om.forward_dynamics(q, v, t, J, g)[0],),
+    }[fname]()
+
+
 def measure_functions(torch, pg, sm):
     """evals/s of every batched function on the humanoid, per precision: RNEA / ABA /
     CRBA (+ tree Cholesky) / computeMinverse / nonLinearEffects / generalized gravity /
     forwardKinematics (q, v, a) / computeJointJacobians at batch 65536, the two derivative
     algorithms at batch 16384; RNEA, ABA and the ABA derivatives with external forces on
     every joint (the fext overloads) at the same batches; forwardDynamics with 12 constraint
-    rows (two 6-D contacts) at batch 65536."""
+    rows (two 6-D contacts) at batch 65536.  Each function's outputs are checked against the
+    FP64 oracle on 256 configurations strided over its batch: the max and median over those
+    configurations of the relative error of every output."""
+    from oracle.oracle import OracleModel
+
     model = sm.humanoid32(1)
+    om = OracleModel(model)
     out = {}
     for prec in ("fp64", "mixed"):
         data = pg.createData(model, prec)
@@ -330,7 +371,15 @@ def measure_functions(torch, pg, sm):
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}
-            del q, v, x, f, Jc, gc
+            got = fn()
+            got = [t for t in (got if isinstance(got, tuple) else (got,)) if t is not None]
+            idx = torch.from_numpy(np.unique(np.linspace(0, B - 1, 256).astype(np.int64))).cuda()
+            host = lambda t: None if t is None else t[idx].cpu().numpy()  # noqa: E731
+            ref = _function_reference(om, fname, host(q), host(v), host(x), host(f), host(Jc), host(gc))
+            errs = [_per_config_rel_err(host(a), b) for a, b in zip(got, ref)]
+            res[fname]["max_rel_err"] = max(e[0] for e in errs)
+            res[fname]["median_rel_err"] = max(e[1] for e in errs)
+            del q, v, x, f, Jc, gc, got
         out[prec] = res
     return out
 
@@ -366,9 +415,11 @@ def measure_heterogeneous(torch, pg, sm, total=100000):
 def measure_rollout(torch, pg, sm, B=8192, T=64, n=100):
     """Differentiable rollout: T semi-implicit Euler steps (dt 1e-3) of ABA on the n-link chain,
     batch B, loss ||q_T||^2, backward through the ABA-derivative kernels with checkpoints every 8 steps."""
+    from oracle.oracle import OracleModel, rollout_with_gradients
     from pinocchio_gb300 import autograd
 
     model = sm.chain(n, 4, (0.1, 1.0))
+    om = OracleModel(model)
     rng = np.random.default_rng(5)
     d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
     q0 = d(rng.uniform(-np.pi, np.pi, (B, n)))
@@ -393,6 +444,20 @@ def measure_rollout(torch, pg, sm, B=8192, T=64, n=100):
         out[prec] = {"ms_per_rollout": ms, "trajectories_per_s": B / ms * 1e3,
                      "aba_evals_per_s": B * T / ms * 1e3,
                      "layouts": {f: (t if isinstance(t, str) else f"thread x{t}") for f, (t, _) in tuned.items()}}
+        # accuracy: q_T and the three gradients of 16 trajectories strided over the batch against the
+        # FP64 oracle rollout (adjoint recursion over the oracle's ABA derivatives)
+        once()
+        qT, _ = autograd.rollout(model, data, q0.detach(), v0.detach(), taus.detach(), dt=1e-3, checkpoint_every=8)
+        idx = np.unique(np.linspace(0, B - 1, 16).astype(np.int64))
+        ti = torch.from_numpy(idx).cuda()
+        got = [qT[ti], q0.grad[ti], v0.grad[ti], taus.grad[:, ti].transpose(0, 1)]
+        qn, vn, tn = (t.detach().cpu().numpy() for t in (q0[ti], v0[ti], taus[:, ti]))
+        qT_o, _, gq_o, gv_o, gt_o = rollout_with_gradients(om, qn, vn, tn, 1e-3)
+        refs = [qT_o, gq_o, gv_o, gt_o.transpose(1, 0, 2)]
+        out[prec]["accuracy_vs_fp64_oracle"] = {
+            k: dict(zip(("max", "median"), _per_config_rel_err(a.detach().cpu().numpy(), b)))
+            for k, a, b in zip(("q_T", "grad_q0", "grad_v0", "grad_taus"), got, refs)}
+        out[prec]["accuracy_vs_fp64_oracle"]["sample"] = f"{len(idx)} trajectories strided over the batch of {B}"
     return out
 
 

@@ -295,6 +295,65 @@ int gb_impulse_dynamics(const gb_model* model, int precision, int layout, long b
 int gb_kkt_contact_inverse(const gb_model* model, int precision, int layout, long batch, int nc, const double* q,
                            const double* J, double inv_damping, double* K, void* stream);
 
+/* ---- constraintDynamics with rigid constraint models (reference algorithm/constrained-dynamics.hpp:90-110,
+ * constrained-dynamics.hxx:188-520; contact models algorithm/contact-info.hpp:140-230; proximal settings
+ * algorithm/proximal.hpp:22-110) ---------------------------------------------------------------------- */
+enum { GB_CONTACT_3D = 0, GB_CONTACT_6D = 1 };  /* ContactType, contact-info.hpp:19-24 */
+enum { GB_FRAME_WORLD = 0, GB_FRAME_LOCAL = 1, GB_FRAME_LOCAL_WORLD_ALIGNED = 2 };  /* ReferenceFrame, multibody/fwd.hpp:46-56 */
+
+/* RigidConstraintModel(type, model, joint1_id, joint1_placement, joint2_id, joint2_placement,
+ * reference_frame): a point (3 rows) or frame (6 rows) constraint between a frame of joint 1 and a
+ * frame of joint 2 (joint 0: the world), joints indexed as in gb_model_desc, placements R row-major
+ * then t, relative to the joint frames; reference_frame GB_FRAME_LOCAL or
+ * GB_FRAME_LOCAL_WORLD_ALIGNED; the desired contact acceleration and the Baumgarte gains Kp, Kd
+ * (corrector) [linear; angular] (GB_CONTACT_3D reads the first three of each). */
+typedef struct gb_constraint_desc {
+  int type;
+  int reference_frame;
+  int joint1_id;
+  int joint2_id;
+  double joint1_placement[12];
+  double joint2_placement[12];
+  double desired_acceleration[6];
+  double Kp[6];
+  double Kd[6];
+} gb_constraint_desc;
+
+/* ProximalSettings(absolute_accuracy, relative_accuracy, mu, max_iter) (proximal.hpp:22-110). */
+typedef struct gb_proximal_settings {
+  double absolute_accuracy;
+  double relative_accuracy;
+  double mu;
+  int max_iter;
+} gb_proximal_settings;
+
+/* The constraint models of initConstraintDynamics(model, data, contact_models)
+ * (constrained-dynamics.hxx:21-60), uploaded once for all the calls of `model`.  n may be 0.
+ * Rejected: a reference frame other than LOCAL / LOCAL_WORLD_ALIGNED, an unknown type, a joint
+ * index out of range, n outside 0..64. */
+typedef struct gb_constraint_set gb_constraint_set;
+int gb_constraint_set_create(const gb_model* model, int n, const gb_constraint_desc* constraints,
+                             gb_constraint_set** out);
+int gb_constraint_set_destroy(gb_constraint_set* set);
+/* the number of constraint models and the constraint dimension (the length of lambda_c) */
+int gb_constraint_set_dims(const gb_constraint_set* set, int* n, int* constraint_dim);
+
+/* ddq = constraintDynamics(model, data, q, v, tau, contact_models, contact_datas, settings) per
+ * instance: the world-frame kinematics, M and the bias forces nle, the constraint Jacobian rows
+ * and drifts of the set, then the proximal iterations
+ *   lambda_k = (J M^-1 J^T + mu I)^-1 (rhs + mu lambda_{k-1} - J M^-1 (tau - nle)), lambda_0 = 0,
+ * until the reference's absolute or relative residual falls below its accuracy or max_iter
+ * iterations ran; ddq = M^-1 (tau - nle + J^T lambda).  lambda_c holds the constraint_dim
+ * multipliers (data.lambda_c; each constraint's segment is its contact_force in its frame).
+ * Optional outputs: iterations (one int per instance, settings.iter) and residuals (two doubles per
+ * instance, instance-major: absolute_residual, relative_residual).  FP64 after the CRBA in both
+ * precisions except the bias forces (FP32 sweeps in GB_MIXED).  mu = 0 needs full-rank
+ * constraints (otherwise the outputs are NaN and the numeric status is set). */
+int gb_constraint_dynamics(const gb_model* model, int precision, const gb_constraint_set* set,
+                           const gb_proximal_settings* settings, int layout, long batch, const double* q,
+                           const double* v, const double* tau, double* ddq, double* lambda_c, int* iterations,
+                           double* residuals, void* stream);
+
 /* forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272):
  * per instance, for every joint i = 0 .. njoints-1 (joint 0 the universe:
  * identity, zero), oMi[12 i ..] = the world placement (rotation row-major, then

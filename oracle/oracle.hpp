@@ -1760,4 +1760,470 @@ void integrate(const Model& m, const T* q, const T* v, T* qout) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// constraintDynamics with rigid constraint models and the proximal iterations
+// (algorithm/constrained-dynamics.hxx:188-520): the world-frame forward /
+// backward sweeps (ContactAndImpulseDynamicsForwardStep / BackwardStep,
+// constrained-dynamics.hxx:63-186), the contact Cholesky factorisation of the
+// KKT matrix [[-mu I, J], [J^T, M]] (contact-cholesky.hxx:21-330), the contact
+// drifts and Baumgarte corrections, and the proximal loop.
+// ---------------------------------------------------------------------------
+enum ContactType { CONTACT_3D = 0, CONTACT_6D = 1 };                  // contact-info.hpp:19-24
+enum ReferenceFrame { RF_WORLD = 0, RF_LOCAL = 1, RF_LOCAL_WORLD_ALIGNED = 2 };  // multibody/fwd.hpp:46-56
+
+// RigidConstraintModel (contact-info.hpp:140-230): placements R row-major + t; the
+// desired acceleration and the corrector gains are [linear; angular].
+struct ConstraintModel {
+  int type = CONTACT_6D, frame = RF_LOCAL, joint1 = 0, joint2 = 0;
+  double P1[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, P2[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+  double desired_acc[6] = {0, 0, 0, 0, 0, 0}, Kp[6] = {0, 0, 0, 0, 0, 0}, Kd[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<int> s1, s2;  // colwise_joint1_sparsity / colwise_joint2_sparsity
+  int size() const { return type == CONTACT_3D ? 3 : 6; }
+  // RigidConstraintModel::init (contact-info.hpp:712-790): the columns of the joints from
+  // joint1 / joint2 up to (excluding) their common ancestor; for CONTACT_3D also the
+  // common ancestor's support, in both sets
+  void init(const Model& m) {
+    if (frame != RF_LOCAL && frame != RF_LOCAL_WORLD_ALIGNED)
+      throw std::invalid_argument("reference_frame should be LOCAL or LOCAL_WORLD_ALIGNED");
+    if (type != CONTACT_3D && type != CONTACT_6D) throw std::invalid_argument("unknown contact type");
+    if (joint1 < 0 || joint1 >= m.njoints || joint2 < 0 || joint2 >= m.njoints)
+      throw std::invalid_argument("constraint joint index out of range");
+    s1.assign(m.nv, 0);
+    s2.assign(m.nv, 0);
+    int c1 = joint1, c2 = joint2;
+    while (c1 != c2) {
+      if (c1 > c2) {
+        for (int k = 0; k < m.nvs[c1]; ++k) s1[m.idx_v[c1] + k] = 1;
+        c1 = m.parents[c1];
+      } else {
+        for (int k = 0; k < m.nvs[c2]; ++k) s2[m.idx_v[c2] + k] = 1;
+        c2 = m.parents[c2];
+      }
+    }
+    if (type == CONTACT_3D)
+      for (int c = c1; c > 0; c = m.parents[c])
+        for (int k = 0; k < m.nvs[c]; ++k) s1[m.idx_v[c] + k] = s2[m.idx_v[c] + k] = 1;
+  }
+};
+
+inline double o_atan2(double y, double x) { return std::atan2(y, x); }
+inline long double o_atan2(long double y, long double x) { return std::atan2(y, x); }
+
+template <class T> inline SE3<T> se3_from(const double* P) {
+  SE3<T> M;
+  for (int k = 0; k < 9; ++k) M.R[k] = T(P[k]);
+  for (int k = 0; k < 3; ++k) M.t[k] = T(P[9 + k]);
+  return M;
+}
+template <class T> inline SE3<T> se3_actinv(const SE3<T>& A, const SE3<T>& B) {  // A^-1 B
+  SE3<T> o;
+  T d[3];
+  for (int k = 0; k < 3; ++k) d[k] = B.t[k] - A.t[k];
+  matTvec(A.R, d, o.t);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) o.R[3 * r + c] = A.R[r] * B.R[c] + A.R[3 + r] * B.R[3 + c] + A.R[6 + r] * B.R[6 + c];
+  return o;
+}
+
+// log3 of a rotation (the angle-axis vector, angle in [0, pi]; reference spatial/log.hxx:58-170):
+// theta = atan2(|a|, (tr - 1) / 2) with a = unskew(R) = sin(theta) n; w = theta / sin(theta) a away
+// from pi (series of theta / sin(theta) near 0), and near pi the axis from the symmetric part
+// (R + R^T) / 2 - cos(theta) I = (1 - cos(theta)) n n^T, its sign taken from a.
+template <class T> inline void log3(const T* R, T* w, T& theta) {
+  const T a[3] = {(R[7] - R[5]) / T(2), (R[2] - R[6]) / T(2), (R[3] - R[1]) / T(2)};
+  const T s = o_sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  T c = (R[0] + R[4] + R[8] - T(1)) / T(2);
+  c = c > T(1) ? T(1) : c < T(-1) ? T(-1) : c;
+  theta = o_atan2(s, c);
+  if (theta < T(3)) {
+    const T t2 = theta * theta;
+    const T k = s < T(1e-4) ? T(1) + t2 / T(6) + T(7) * t2 * t2 / T(360) : theta / s;
+    for (int i = 0; i < 3; ++i) w[i] = k * a[i];
+    return;
+  }
+  const T omc = T(1) - c;
+  int j = 0;
+  for (int i = 1; i < 3; ++i)
+    if (R[4 * i] > R[4 * j]) j = i;
+  T n[3];
+  n[j] = o_sqrt((R[4 * j] - c) / omc);
+  for (int i = 0; i < 3; ++i)
+    if (i != j) n[i] = (R[3 * i + j] + R[3 * j + i]) / (T(2) * omc * n[j]);
+  const T dp = n[0] * a[0] + n[1] * a[1] + n[2] * a[2];
+  const T sg = dp < T(0) ? T(-1) : T(1);
+  for (int i = 0; i < 3; ++i) w[i] = sg * theta * n[i];
+}
+// log6 of a placement (spatial/log.hxx:189-230): angular = log3(R); linear = alpha p - w x p / 2 +
+// beta (w . p) w, alpha = theta sin / (2 (1 - cos)), beta = 1 / theta^2 - sin / (2 theta (1 - cos)),
+// their series in |unskew(R)|^2 when tr(R) >= 3 - eps^(1/3)
+template <class T> inline Vec6<T> log6(const SE3<T>& M) {
+  T w[3], theta;
+  log3(M.R, w, theta);
+  const T a[3] = {(M.R[7] - M.R[5]) / T(2), (M.R[2] - M.R[6]) / T(2), (M.R[3] - M.R[1]) / T(2)};
+  const T t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+  const T tr = M.R[0] + M.R[4] + M.R[8];
+  T alpha, beta;
+  if (tr >= T(3) - T(std::cbrt(std::numeric_limits<double>::epsilon()))) {
+    alpha = T(1) - t2 / T(12) - t2 * t2 / T(720);
+    beta = T(1) / T(12) + t2 / T(720);
+  } else {
+    T st, ct;
+    o_sincos(theta, &st, &ct);
+    alpha = theta * st / (T(2) * (T(1) - ct));
+    beta = T(1) / (theta * theta) - st / (T(2) * theta * (T(1) - ct));
+  }
+  T wxp[3];
+  cross3(w, M.t, wxp);
+  const T wp = w[0] * M.t[0] + w[1] * M.t[1] + w[2] * M.t[2];
+  Vec6<T> o;
+  for (int k = 0; k < 3; ++k) {
+    o.v[k] = alpha * M.t[k] - T(0.5) * wxp[k] + beta * wp * w[k];
+    o.v[3 + k] = w[k];
+  }
+  return o;
+}
+
+// The contact Cholesky factorisation U D U^T of the KKT matrix (contact-cholesky.hxx:21-330):
+// rows / columns 0..nc-1 the constraints, nc..nc+nv-1 the dofs; U unit upper, row-major.
+template <class T> struct ContactCholesky {
+  int nc = 0, nv = 0, n = 0;
+  std::vector<int> pfr, nsfr;  // parents_fromRow / nv_subtree_fromRow shifted by nc
+  std::vector<T> U, D, Dinv;
+  void allocate(const Model& m, const std::vector<ConstraintModel>& cms) {  // allocate, hxx:21-150
+    nv = m.nv;
+    nc = 0;
+    for (const auto& c : cms) nc += c.size();
+    n = nc + nv;
+    pfr.assign(n, -1);
+    nsfr.assign(n, 0);
+    for (int j = 1; j < m.njoints; ++j) {
+      const int p = m.parents[j], iv = m.idx_v[j];
+      pfr[nc + iv] = p > 0 ? m.idx_v[p] + m.nvs[p] - 1 + nc : -1;
+      nsfr[nc + iv] = m.nvSubtree[j];
+      for (int r = 1; r < m.nvs[j]; ++r) {
+        pfr[nc + iv + r] = nc + iv + r - 1;
+        nsfr[nc + iv + r] = m.nvSubtree[j] - r;
+      }
+    }
+    int row = 0;
+    for (const auto& c : cms) {
+      const int e = std::max(m.idx_v[c.joint1] + m.nvs[c.joint1], m.idx_v[c.joint2] + m.nvs[c.joint2]);
+      for (int k = 0; k < c.size(); ++k, ++row) nsfr[row] = e + (nc - row);
+    }
+    U.assign((size_t)n * n, T(0));
+    for (int k = 0; k < n; ++k) U[(size_t)k * n + k] = T(1);
+    D.assign(n, T(0));
+    Dinv.assign(n, T(0));
+  }
+  T& u(int r, int c) { return U[(size_t)r * n + c]; }
+  // compute (hxx:152-272) after the Jacobian rows are in U's top-right block and M in
+  // D.tail / U's bottom-right block; then updateDamping(mu) (hxx:274-304)
+  void factor(T mu) {
+    std::vector<T> DUt(n);
+    for (int j = nv - 1; j >= 0; --j) {
+      const int jj = nc + j, NVT = nsfr[jj] - 1;
+      for (int k = 0; k < NVT; ++k) DUt[k] = u(jj, jj + 1 + k) * D[jj + 1 + k];
+      T s = T(0);
+      for (int k = 0; k < NVT; ++k) s += u(jj, jj + 1 + k) * DUt[k];
+      D[jj] -= s;
+      Dinv[jj] = T(1) / D[jj];
+      for (int ii = pfr[jj]; ii >= nc; ii = pfr[ii]) {
+        T t = T(0);
+        for (int k = 0; k < NVT; ++k) t += u(ii, jj + 1 + k) * DUt[k];
+        u(ii, jj) = (u(ii, jj) - t) * Dinv[jj];
+      }
+      for (int r = nc - 1; r >= 0; --r) {
+        T t = T(0);
+        for (int k = 0; k < NVT; ++k) t += u(r, jj + 1 + k) * DUt[k];
+        u(r, jj) = (u(r, jj) - t) * Dinv[jj];
+      }
+    }
+    for (int j = nc - 1; j >= 0; --j) {
+      const int sd = n - j - 1;
+      for (int k = 0; k < sd; ++k) DUt[k] = u(j, j + 1 + k) * D[j + 1 + k];
+      T s = T(0);
+      for (int k = 0; k < sd; ++k) s += u(j, j + 1 + k) * DUt[k];
+      D[j] = -mu - s;
+      Dinv[j] = T(1) / D[j];
+      for (int i = j - 1; i >= 0; --i) {
+        T t = T(0);
+        for (int k = 0; k < sd; ++k) t += u(i, j + 1 + k) * DUt[k];
+        u(i, j) = -t * Dinv[j];
+      }
+    }
+  }
+  // solveInPlace (hxx:306-316): Uiv (hxx:512-538), Dinv, Utiv (hxx:570-595)
+  void solve(T* x) {
+    for (int k = n - 2; k >= nc; --k) {
+      T s = T(0);
+      for (int j = 1; j < nsfr[k]; ++j) s += u(k, k + j) * x[k + j];
+      x[k] -= s;
+    }
+    for (int k = nc - 1; k >= 0; --k) {
+      T s = T(0);
+      for (int j = k + 1; j < n; ++j) s += u(k, j) * x[j];
+      x[k] -= s;
+    }
+    for (int k = 0; k < n; ++k) x[k] *= Dinv[k];
+    for (int k = 0; k < nc; ++k)
+      for (int j = k + 1; j < n; ++j) x[j] -= u(k, j) * x[k];
+    for (int k = nc; k <= n - 2; ++k)
+      for (int j = 1; j < nsfr[k]; ++j) x[k + j] -= u(k, k + j) * x[k];
+  }
+  // DelassusCholeskyExpression::applyOnTheRight (contact-cholesky.hpp:536-558):
+  // res = U1 (-D1) U1^T x over the constraint block
+  void delassus_apply(const T* x, T* res) {
+    std::vector<T> t(nc);
+    for (int i = 0; i < nc; ++i) {
+      T s = x[i];
+      for (int k = 0; k < i; ++k) s += u(k, i) * x[k];
+      t[i] = -D[i] * s;
+    }
+    for (int i = 0; i < nc; ++i) {
+      T s = t[i];
+      for (int k = i + 1; k < nc; ++k) s += u(i, k) * t[k];
+      res[i] = s;
+    }
+  }
+};
+
+// The constraint Jacobian rows of one model (RigidConstraintModel::jacobian, contact-info.hpp:551-672)
+// from the world-frame columns d.J, written into the KKT factor's top-right block
+template <class T>
+void constraint_jacobian(const Model& m, const Data<T>& d, const ConstraintModel& c, const SE3<T>& oMc1,
+                         const SE3<T>& oMc2, const SE3<T>& c1Mc2, int row, ContactCholesky<T>& ch) {
+  for (int jj = 0; jj < m.nv; ++jj) {
+    if (!c.s1[jj] && !c.s2[jj]) continue;
+    const int sign = c.s1[jj] != c.s2[jj] ? (c.s1[jj] ? 1 : -1) : 0;
+    const Vec6<T> Jc = col6(d.J, jj);
+    T col[6];
+    if (c.type == CONTACT_3D) {
+      if (c.frame == RF_LOCAL) {
+        if (sign == 0) {
+          const Vec6<T> l1 = actinv_motion(oMc1, Jc), l2 = actinv_motion(oMc2, Jc);
+          T r2[3];
+          matvec(c1Mc2.R, l2.v, r2);
+          for (int k = 0; k < 3; ++k) col[k] = l1.v[k] - r2[k];
+        } else if (sign == 1) {
+          const Vec6<T> l1 = actinv_motion(oMc1, Jc);
+          for (int k = 0; k < 3; ++k) col[k] = l1.v[k];
+        } else {
+          const Vec6<T> l2 = actinv_motion(oMc2, Jc);
+          T r2[3];
+          matvec(c1Mc2.R, l2.v, r2);
+          for (int k = 0; k < 3; ++k) col[k] = -r2[k];
+        }
+      } else {
+        if (sign == 0) {
+          T dpos[3];
+          for (int k = 0; k < 3; ++k) dpos[k] = oMc2.t[k] - oMc1.t[k];
+          cross3(dpos, Jc.v + 3, col);
+        } else {
+          T pxw[3];
+          cross3(sign == 1 ? oMc1.t : oMc2.t, Jc.v + 3, pxw);
+          for (int k = 0; k < 3; ++k) col[k] = (Jc.v[k] - pxw[k]) * T(sign);
+        }
+      }
+    } else {
+      if (c.frame == RF_LOCAL) {
+        const Vec6<T> l1 = actinv_motion(oMc1, Jc);
+        for (int k = 0; k < 6; ++k) col[k] = l1.v[k] * T(sign);
+      } else {
+        T pxw[3];
+        cross3(oMc1.t, Jc.v + 3, pxw);
+        for (int k = 0; k < 3; ++k) {
+          col[k] = (Jc.v[k] - pxw[k]) * T(sign);
+          col[3 + k] = Jc.v[3 + k] * T(sign);
+        }
+      }
+    }
+    for (int k = 0; k < c.size(); ++k) ch.u(row + k, ch.nc + jj) = col[k];
+  }
+}
+
+struct ProximalResult {
+  int iter = 0;
+  double absolute_residual = -1.0, relative_residual = -1.0;
+};
+
+// constraintDynamics (constrained-dynamics.hxx:188-520).  ddq: nv; lambda: the stacked
+// multipliers lambda_c (sum of the constraint sizes); the contact forces are lambda's segments.
+template <class T>
+ProximalResult constraint_dynamics(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau,
+                                   const std::vector<ConstraintModel>& cms, T mu, int max_iter, T abs_acc,
+                                   T rel_acc, T* ddq, T* lambda) {
+  const int nv = m.nv;
+  // ContactAndImpulseDynamicsForwardStep (hxx:63-135) with ContactMode
+  d.ov[0] = zero6<T>();
+  d.oa[0] = zero6<T>();
+  d.of[0] = zero6<T>();
+  d.oYcrb[0] = Iner<T>{T(0), {T(0), T(0), T(0)}, {T(0), T(0), T(0), T(0), T(0), T(0)}};
+  for (int i = 1; i < m.njoints; ++i) {
+    const int p = m.parents[i], iq = m.idx_q[i], iv = m.idx_v[i];
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m, i, q + iq));
+    d.oMi[i] = p > 0 ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
+    d.ov[i] = act_motion(d.oMi[i], joint_velocity<T>(m, i, v + iv));
+    if (p > 0) d.ov[i] = add6(d.ov[i], d.ov[p]);
+    for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(m, i, k)));
+    d.oinertias[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
+    d.oYcrb[i] = d.oinertias[i];
+    d.oh[i] = iner_mul(d.oinertias[i], d.ov[i]);
+    d.oa[i] = zero6<T>();  // oMi.act(c) with c = 0 for these joints
+    if (p > 0) d.oa[i] = add6(add6(d.oa[i], cross_motion(d.ov[p], d.ov[i])), d.oa[p]);
+    for (int k = 0; k < 6; ++k) d.oa_gf[i].v[k] = d.oa[i].v[k] - T(m.gravity[k]);
+    d.of[i] = add6(iner_mul(d.oinertias[i], d.oa_gf[i]), cross_force(d.ov[i], d.oh[i]));
+  }
+  // ContactAndImpulseDynamicsBackwardStep (hxx:137-186): M rows from dFda = oYcrb J, nle = J^T of
+  std::fill(d.M.begin(), d.M.end(), T(0));
+  std::vector<T> nle(nv);
+  for (int i = m.njoints - 1; i > 0; --i) {
+    const int p = m.parents[i], iv = m.idx_v[i], nvi = m.nvs[i];
+    for (int k = 0; k < nvi; ++k) set_col6(d.dFda, iv + k, iner_mul(d.oYcrb[i], col6(d.J, iv + k)));
+    for (int r = 0; r < nvi; ++r)
+      for (int c = iv; c < iv + m.nvSubtree[i]; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFda, c));
+    iner_add(d.oYcrb[p], d.oYcrb[i]);
+    for (int r = 0; r < nvi; ++r) nle[iv + r] = dot6(col6(d.J, iv + r), d.of[i]);
+    d.of[p] = add6(d.of[p], d.of[i]);
+  }
+  for (int k = 0; k < nv; ++k) d.M[(size_t)k * nv + k] += T(m.armature[k]);
+  // contact_chol.compute (contact-cholesky.hxx:152-272)
+  ContactCholesky<T> ch;
+  ch.allocate(m, cms);
+  const int nc = ch.nc;
+  for (int k = 0; k < nv; ++k) {
+    ch.D[nc + k] = d.M[(size_t)k * nv + k];
+    for (int c = k + 1; c < nv; ++c) ch.u(nc + k, nc + c) = d.M[(size_t)k * nv + c];
+  }
+  std::vector<SE3<T>> oMc1(cms.size()), oMc2(cms.size()), c1Mc2(cms.size());
+  int row = 0;
+  for (size_t e = 0; e < cms.size(); ++e) {  // RigidConstraintModel::calc (contact-info.hpp:426-446)
+    const ConstraintModel& c = cms[e];
+    oMc1[e] = c.joint1 > 0 ? se3_mul(d.oMi[c.joint1], se3_from<T>(c.P1)) : se3_from<T>(c.P1);
+    oMc2[e] = c.joint2 > 0 ? se3_mul(d.oMi[c.joint2], se3_from<T>(c.P2)) : se3_from<T>(c.P2);
+    c1Mc2[e] = se3_actinv(oMc1[e], oMc2[e]);
+    constraint_jacobian(m, d, c, oMc1[e], oMc2[e], c1Mc2[e], row, ch);
+    row += c.size();
+  }
+  ch.factor(mu);
+  // the right-hand side: contact drifts and Baumgarte corrections (hxx:282-432)
+  std::vector<T> rhs(nc);
+  row = 0;
+  for (size_t e = 0; e < cms.size(); ++e) {
+    const ConstraintModel& c = cms[e];
+    const int j1 = c.joint1, j2 = c.joint2;
+    const Vec6<T> vc1 = j1 > 0 ? actinv_motion(oMc1[e], d.ov[j1]) : zero6<T>();
+    const Vec6<T> vc2 = j2 > 0 ? actinv_motion(oMc2[e], d.ov[j2]) : zero6<T>();
+    const Vec6<T> vc2_1 = act_motion(c1Mc2[e], vc2);
+    Vec6<T> pe = zero6<T>(), ve = zero6<T>(), ae = zero6<T>(), a1, a2;
+    if (c.type == CONTACT_6D) {
+      const Vec6<T> lg = log6(c1Mc2[e]);
+      for (int k = 0; k < 6; ++k) {
+        pe.v[k] = -lg.v[k];
+        ve.v[k] = vc1.v[k] - vc2_1.v[k];
+      }
+    } else {
+      T r2[3];
+      matvec(c1Mc2[e].R, vc2.v, r2);
+      for (int k = 0; k < 3; ++k) {
+        pe.v[k] = -c1Mc2[e].t[k];
+        ve.v[k] = vc1.v[k] - r2[k];
+      }
+    }
+    bool gains = false;
+    for (int k = 0; k < 6; ++k) gains = gains || c.Kp[k] != 0.0 || c.Kd[k] != 0.0;
+    if (gains)
+      for (int k = 0; k < (c.type == CONTACT_6D ? 6 : 3); ++k) ae.v[k] = -T(c.Kp[k]) * pe.v[k] - T(c.Kd[k]) * ve.v[k];
+    const Vec6<T>& oa1 = d.oa[j1];
+    const Vec6<T>& oa2 = d.oa[j2];
+    const Vec6<T>& ov1 = d.ov[j1];
+    const Vec6<T>& ov2 = d.ov[j2];
+    // the classical acceleration part of a point p: ov.ang x (ov.lin + ov.ang x p)
+    auto point_drift = [](const Vec6<T>& ov, const T* pt, T* o) {
+      T wxp[3], vp[3];
+      cross3(ov.v + 3, pt, wxp);
+      for (int k = 0; k < 3; ++k) vp[k] = ov.v[k] + wxp[k];
+      cross3(ov.v + 3, vp, o);
+    };
+    if (c.frame == RF_LOCAL_WORLD_ALIGNED) {
+      T t[3];
+      cross3(oa1.v + 3, oMc1[e].t, t);
+      for (int k = 0; k < 3; ++k) a1.v[k] = oa1.v[k] + t[k];
+      if (c.type == CONTACT_3D) {
+        point_drift(ov1, oMc1[e].t, t);
+        for (int k = 0; k < 3; ++k) a1.v[k] += t[k];
+      }
+      for (int k = 0; k < 3; ++k) a1.v[3 + k] = oa1.v[3 + k];
+      if (c.type == CONTACT_3D) {
+        T u[3];
+        cross3(oa2.v + 3, oMc2[e].t, t);
+        point_drift(ov2, oMc2[e].t, u);
+        for (int k = 0; k < 3; ++k) {
+          a2.v[k] = oa2.v[k] + t[k] + u[k];
+          a2.v[3 + k] = T(0);
+        }
+      } else {
+        cross3(oa2.v + 3, oMc1[e].t, t);
+        for (int k = 0; k < 3; ++k) {
+          a2.v[k] = oa2.v[k] + t[k];
+          a2.v[3 + k] = oa2.v[3 + k];
+        }
+      }
+      T rl[3], ra[3];
+      matvec(oMc1[e].R, ae.v, rl);
+      matvec(oMc1[e].R, ae.v + 3, ra);
+      for (int k = 0; k < 3; ++k) {
+        ae.v[k] = rl[k];
+        ae.v[3 + k] = ra[k];
+      }
+    } else {
+      a1 = actinv_motion(oMc1[e], oa1);
+      if (c.type == CONTACT_3D) {
+        T t[3];
+        cross3(vc1.v + 3, vc1.v, t);
+        for (int k = 0; k < 3; ++k) {
+          a1.v[k] += t[k];
+          a1.v[3 + k] = T(0);
+        }
+        T u[3], w[3];
+        cross3(oa2.v + 3, oMc2[e].t, t);
+        point_drift(ov2, oMc2[e].t, u);
+        for (int k = 0; k < 3; ++k) w[k] = oa2.v[k] + t[k] + u[k];
+        matTvec(oMc1[e].R, w, a2.v);
+        for (int k = 0; k < 3; ++k) a2.v[3 + k] = T(0);
+      } else {
+        a1 = add6(a1, cross_motion(ve, vc2_1));
+        a2 = actinv_motion(oMc1[e], oa2);
+      }
+    }
+    for (int k = 0; k < c.size(); ++k) rhs[row + k] = -a1.v[k] + a2.v[k] + ae.v[k] + T(c.desired_acc[k]);
+    row += c.size();
+  }
+  // the proximal iterations (hxx:434-486)
+  ProximalResult res;
+  std::vector<T> x(nc + nv), lprox(nc, T(0)), tmp(nc);
+  int it = 0;
+  for (; it < max_iter;) {
+    ++it;
+    for (int k = 0; k < nc; ++k) x[k] = rhs[k] + lprox[k] * mu;
+    for (int k = 0; k < nv; ++k) x[nc + k] = tau[k] - nle[k];
+    ch.solve(x.data());
+    ch.delassus_apply(x.data(), tmp.data());
+    T ar = T(0), rr = T(0);
+    for (int k = 0; k < nc; ++k) {
+      tmp[k] -= mu * x[k] + rhs[k];
+      ar = o_max(ar, tmp[k] < T(0) ? -tmp[k] : tmp[k]);
+      const T dk = x[k] + lprox[k];
+      rr = o_max(rr, dk < T(0) ? -dk : dk);
+    }
+    res.absolute_residual = (double)ar;
+    res.relative_residual = (double)rr;
+    for (int k = 0; k < nc; ++k) lprox[k] = -x[k];
+    if (ar <= abs_acc || rr <= rel_acc) break;
+  }
+  res.iter = it;
+  for (int k = 0; k < nv; ++k) ddq[k] = x[nc + k];
+  for (int k = 0; k < nc; ++k) lambda[k] = -x[k];
+  return res;
+}
+
 }  // namespace orc

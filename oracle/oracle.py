@@ -58,6 +58,8 @@ def lib():
         L.orc_aba_derivatives_fext.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_forward_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, vp, C.c_double, vp, vp, C.c_int]
         L.orc_kkt_inverse.argtypes = [vp, C.c_long, C.c_int, vp, vp, C.c_double, vp]
+        L.orc_constraint_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, C.c_double, C.c_int,
+                                              C.c_double, C.c_double, vp, vp, vp, vp, C.c_int]
         L.orc_impulse_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
@@ -201,6 +203,24 @@ class OracleModel:
         K = np.empty((B, self.nv + nc, self.nv + nc))
         self._check(lib().orc_kkt_inverse(self.h, B, nc, _ptr(q), _ptr(J), float(inv_damping), _ptr(K)))
         return K
+
+    def constraint_dynamics(self, q, v, tau, desc, mu=0.0, max_iter=1, absolute_accuracy=1e-12,
+                            relative_accuracy=1e-12, prec=0, nthreads=0):
+        """constraintDynamics (reference algorithm/constrained-dynamics.hxx:188-520) with the constraint
+        models ``desc`` ((n, 46): type, frame, joint1, joint2, joint1_placement (12), joint2_placement
+        (12), desired acceleration (6), Kp (6), Kd (6)).  Returns (ddq (B, nv), lambda_c (B, nc),
+        iterations (B,), residuals (B, 2): absolute, relative)."""
+        q, v, tau = _c(q), _c(v), _c(tau)
+        desc = _c(np.asarray(desc).reshape(-1, 46))
+        B = q.shape[0]
+        nc = int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
+        ddq, lam = np.empty((B, self.nv)), np.empty((B, nc))
+        iters, res = np.empty(B, dtype=np.int32), np.empty((B, 2))
+        self._check(lib().orc_constraint_dynamics(self.h, prec, B, len(desc), _ptr(desc), _ptr(q), _ptr(v), _ptr(tau),
+                                                  float(mu), int(max_iter), float(absolute_accuracy),
+                                                  float(relative_accuracy), _ptr(ddq), _ptr(lam), _ptr(iters),
+                                                  _ptr(res), nthreads))
+        return ddq, lam, iters, res
 
     def impulse_dynamics(self, q, v_before, J, r_coeff=0.0, inv_damping=0.0, prec=0, nthreads=0):
         """(dq_after, impulse_c) of impulseDynamics with the constraint Jacobian J (B, nc, nv)."""

@@ -340,6 +340,15 @@ int orc_kkt_inverse(void* h, long B, int nc, const double* q, const double* J, d
     orc::kkt_inverse_contact(m, d, q + (size_t)b * m.nq, nc, J + (size_t)b * nc * m.nv, inv_damping, K + (size_t)b * n * n);
   return 0;
 }
+// constraintDynamics with rigid constraint models and the proximal iterations
+// (algorithm/constrained-dynamics.hxx:188-520).  Each constraint model is 46 doubles:
+// type (0 = CONTACT_3D, 1 = CONTACT_6D), reference frame (1 = LOCAL, 2 = LOCAL_WORLD_ALIGNED),
+// joint1, joint2, joint1_placement (R row-major, t), joint2_placement, the desired acceleration,
+// Kp, Kd.  Outputs per instance: ddq (nv), lambda_c (the stacked constraint sizes), the
+// iteration count and (absolute, relative) residuals.  prec 0 = double, 1 = long double.
+int orc_constraint_dynamics(void* h, int prec, long B, int ncontacts, const double* desc, const double* q,
+                            const double* v, const double* tau, double mu, int max_iter, double abs_acc,
+                            double rel_acc, double* ddq, double* lambda_c, int* iters, double* residuals, int nt);
 int orc_impulse_dynamics(void* h, int prec, long B, int nc, const double* q, const double* v_before, const double* J,
                          double r_coeff, double inv_damping, double* dq_after, double* impulse_c, int nt) {
   const Model& m = *static_cast<Model*>(h);
@@ -382,3 +391,73 @@ int orc_count_flops(void* h, int func, const double* q, const double* v, const d
 }
 
 }  // extern "C"
+
+namespace {
+std::vector<orc::ConstraintModel> constraint_models(const Model& m, int n, const double* desc) {
+  std::vector<orc::ConstraintModel> cms(n);
+  for (int e = 0; e < n; ++e) {
+    const double* d = desc + 46 * e;
+    orc::ConstraintModel& c = cms[e];
+    c.type = (int)d[0];
+    c.frame = (int)d[1];
+    c.joint1 = (int)d[2];
+    c.joint2 = (int)d[3];
+    std::memcpy(c.P1, d + 4, sizeof(c.P1));
+    std::memcpy(c.P2, d + 16, sizeof(c.P2));
+    std::memcpy(c.desired_acc, d + 28, sizeof(c.desired_acc));
+    std::memcpy(c.Kp, d + 34, sizeof(c.Kp));
+    std::memcpy(c.Kd, d + 40, sizeof(c.Kd));
+    c.init(m);
+  }
+  return cms;
+}
+template <class T>
+int constraint_batch(const Model& m, long B, const std::vector<orc::ConstraintModel>& cms, const double* q,
+                     const double* v, const double* tau, double mu, int max_iter, double abs_acc, double rel_acc,
+                     double* ddq, double* lam, int* iters, double* residuals, int nthreads) {
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  omp_set_dynamic(0);
+  omp_set_num_threads(nthreads);
+  std::vector<std::unique_ptr<orc::Data<T>>> datas(nthreads);
+  for (int t = 0; t < nthreads; ++t) datas[t].reset(new orc::Data<T>(m));
+  int nc = 0;
+  for (const auto& c : cms) nc += c.size();
+  const int nq = m.nq, nv = m.nv;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    orc::Data<T>& d = *datas[omp_get_thread_num()];
+    Buf<T> bq, bv, bt;
+    bq.load(q + (size_t)b * nq, nq);
+    bv.load(v + (size_t)b * nv, nv);
+    bt.load(tau + (size_t)b * nv, nv);
+    std::vector<T> o(nv), l(nc);
+    const orc::ProximalResult r = orc::constraint_dynamics(m, d, bq.x.data(), bv.x.data(), bt.x.data(), cms, T(mu),
+                                                           max_iter, T(abs_acc), T(rel_acc), o.data(), l.data());
+    store(o, ddq + (size_t)b * nv, nv);
+    store(l, lam + (size_t)b * nc, nc);
+    if (iters) iters[b] = r.iter;
+    if (residuals) {
+      residuals[2 * b] = r.absolute_residual;
+      residuals[2 * b + 1] = r.relative_residual;
+    }
+  }
+  return 0;
+}
+}  // namespace
+extern "C" int orc_constraint_dynamics(void* h, int prec, long B, int ncontacts, const double* desc, const double* q,
+                                       const double* v, const double* tau, double mu, int max_iter, double abs_acc,
+                                       double rel_acc, double* ddq, double* lambda_c, int* iters, double* residuals,
+                                       int nt) {
+  const Model& m = *static_cast<Model*>(h);
+  try {
+    const std::vector<orc::ConstraintModel> cms = constraint_models(m, ncontacts, desc);
+    if (max_iter < 1 || !(mu >= 0.0)) throw std::invalid_argument("max_iter must be >= 1 and mu >= 0");
+    return prec == 1 ? constraint_batch<long double>(m, B, cms, q, v, tau, mu, max_iter, abs_acc, rel_acc, ddq,
+                                                     lambda_c, iters, residuals, nt)
+                     : constraint_batch<double>(m, B, cms, q, v, tau, mu, max_iter, abs_acc, rel_acc, ddq, lambda_c,
+                                                iters, residuals, nt);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}

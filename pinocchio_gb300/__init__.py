@@ -24,6 +24,19 @@ from .model import (  # noqa: F401
     SE3,
 )
 from . import sample_models  # noqa: F401
+from .constraints import (  # noqa: F401
+    CONTACT_3D,
+    CONTACT_6D,
+    LOCAL,
+    LOCAL_WORLD_ALIGNED,
+    WORLD,
+    BaumgarteCorrectorParameters,
+    ContactType,
+    ProximalSettings,
+    ReferenceFrame,
+    RigidConstraintData,
+    RigidConstraintModel,
+)
 from .urdf import buildModelFromUrdf, buildModelFromXML, load_model, save_model  # noqa: F401
 from .mjcf import buildModelFromMJCF, buildModelFromMJCFXML  # noqa: F401
 from .api import (  # noqa: F401
@@ -41,12 +54,14 @@ from .api import (  # noqa: F401
     computeRNEADerivatives,
     computeStaticTorque,
     computeStaticTorqueDerivatives,
+    constraintDynamics,
     crba,
     crbaCholesky,
     createData,
     forwardDynamics,
     forwardKinematics,
     impulseDynamics,
+    initConstraintDynamics,
     integrate,
     numericStatus,
     nonLinearEffects,

@@ -23,6 +23,8 @@ GB_FUNC_RNEA, GB_FUNC_ABA, GB_FUNC_CRBA, GB_FUNC_RNEA_DERIVATIVES, GB_FUNC_ABA_D
 GB_INSTANCE_PER_THREAD, GB_INSTANCE_PER_WARP, GB_INSTANCE_PER_4_LANES, GB_INSTANCE_PER_8_LANES = 0, 1, 2, 3
 GB_INSTANCE_PER_BRANCH = 4
 GB_NUMERIC_PIVOT, GB_NUMERIC_NONFINITE = 1, 2
+GB_CONTACT_3D, GB_CONTACT_6D = 0, 1
+GB_FRAME_WORLD, GB_FRAME_LOCAL, GB_FRAME_LOCAL_WORLD_ALIGNED = 0, 1, 2
 
 # every symbol declared in include/pinocchio_gb300.h, in declaration order
 EXPORTS = (
@@ -51,6 +53,10 @@ EXPORTS = (
     "gb_forward_dynamics",
     "gb_impulse_dynamics",
     "gb_kkt_contact_inverse",
+    "gb_constraint_set_create",
+    "gb_constraint_set_destroy",
+    "gb_constraint_set_dims",
+    "gb_constraint_dynamics",
     "gb_forward_kinematics",
     "gb_compute_joint_jacobians",
     "gb_integrate",
@@ -95,6 +101,33 @@ class ModelDesc(C.Structure):
         ("nv_armature", C.c_int),
         ("gravity", C.c_void_p),
         ("axis", C.c_void_p),
+    ]
+
+
+class ConstraintDesc(C.Structure):
+    """gb_constraint_desc"""
+
+    _fields_ = [
+        ("type", C.c_int),
+        ("reference_frame", C.c_int),
+        ("joint1_id", C.c_int),
+        ("joint2_id", C.c_int),
+        ("joint1_placement", C.c_double * 12),
+        ("joint2_placement", C.c_double * 12),
+        ("desired_acceleration", C.c_double * 6),
+        ("Kp", C.c_double * 6),
+        ("Kd", C.c_double * 6),
+    ]
+
+
+class ProximalSettingsC(C.Structure):
+    """gb_proximal_settings"""
+
+    _fields_ = [
+        ("absolute_accuracy", C.c_double),
+        ("relative_accuracy", C.c_double),
+        ("mu", C.c_double),
+        ("max_iter", C.c_int),
     ]
 
 
@@ -158,6 +191,11 @@ def lib():
         L.gb_forward_dynamics.argtypes = [vp, i, i, l, i, vp, vp, vp, vp, vp, C.c_double, vp, vp, vp]
         L.gb_impulse_dynamics.argtypes = [vp, i, i, l, i, vp, vp, vp, C.c_double, C.c_double, vp, vp, vp]
         L.gb_kkt_contact_inverse.argtypes = [vp, i, i, l, i, vp, vp, C.c_double, vp, vp]
+        L.gb_constraint_set_create.argtypes = [vp, i, C.POINTER(ConstraintDesc), C.POINTER(vp)]
+        L.gb_constraint_set_destroy.argtypes = [vp]
+        L.gb_constraint_set_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+        L.gb_constraint_dynamics.argtypes = [vp, i, vp, C.POINTER(ProximalSettingsC), i, l, vp, vp, vp, vp, vp, vp, vp,
+                                             vp]
         L.gb_forward_kinematics.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.gb_compute_joint_jacobians.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]

@@ -345,6 +345,96 @@ def aba(model: Model, data: Data, q, v, tau, *args, convention: int | None = Non
     return _ret(ddq, was_np, vec)
 
 
+class _ConstraintSet:
+    """The C ABI's gb_constraint_set of a list of RigidConstraintModel (uploaded once)."""
+
+    def __init__(self, data: Data, desc: np.ndarray):
+        self.desc = desc.copy()
+        n = desc.shape[0]
+        arr = (_capi.ConstraintDesc * max(n, 1))()
+        for k, d in enumerate(desc):
+            c = arr[k]
+            c.type, c.reference_frame, c.joint1_id, c.joint2_id = (int(x) for x in d[:4])
+            c.joint1_placement[:] = d[4:16].tolist()
+            c.joint2_placement[:] = d[16:28].tolist()
+            c.desired_acceleration[:] = d[28:34].tolist()
+            c.Kp[:] = d[34:40].tolist()
+            c.Kd[:] = d[40:46].tolist()
+        h = C.c_void_p()
+        _capi.check(_capi.lib().gb_constraint_set_create(data.dev.h, n, arr, C.byref(h)))
+        self.h = h
+        nn, nc = C.c_int(), C.c_int()
+        _capi.check(_capi.lib().gb_constraint_set_dims(h, C.byref(nn), C.byref(nc)))
+        self.n, self.nc = nn.value, nc.value
+        self._data = data  # the set must not outlive its device model
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.gb_constraint_set_destroy(h)
+            self.h = None
+
+
+def initConstraintDynamics(model: Model, data: Data, contact_models) -> None:
+    """initConstraintDynamics(model, data, contact_models) (reference
+    algorithm/constrained-dynamics.hxx:21-60): uploads the constraint models for the calls of
+    constraintDynamics; a later call with different models (or changed gains) uploads them again."""
+    from .constraints import stack_desc
+
+    data.constraint_set = _ConstraintSet(data, stack_desc(contact_models))
+
+
+def constraintDynamics(model: Model, data: Data, q, v, tau, contact_models, contact_datas=None, settings=None, *,
+                       out=None):
+    """ddq = constraintDynamics(model, data, q, v, tau, contact_models, contact_datas[, settings])
+    (reference algorithm/constrained-dynamics.hxx:188-520, constrained-dynamics.hpp:90-110) over a
+    batch: data.lambda_c (batch, constraint_dim) the multipliers, contact_datas[k].contact_force
+    (batch, 6) each constraint's force in its frame, data.constraint_iterations (batch,) and
+    data.constraint_residuals (batch, 2: absolute, relative) per configuration; settings.iter and the
+    residuals become the largest over the batch.  ``out``: a preallocated (batch, nv) tensor for ddq."""
+    from .constraints import ProximalSettings, stack_desc
+
+    torch = _torch()
+    settings = ProximalSettings() if settings is None else settings
+    desc = stack_desc(contact_models)
+    cset = getattr(data, "constraint_set", None)
+    if cset is None or cset.desc.shape != desc.shape or not np.array_equal(cset.desc, desc):
+        initConstraintDynamics(model, data, contact_models)
+        cset = data.constraint_set
+    if contact_datas is not None and len(contact_datas) != len(contact_models):
+        raise ValueError("The contact models and data do not have the same vector size.")
+    qt, was_np, vec = _as_batch(q, model.nq, "q")
+    vt = _as_batch(v, model.nv, "v")[0]
+    tt = _as_batch(tau, model.nv, "tau")[0]
+    B, nc = qt.shape[0], cset.nc
+    ddq = _out(out, (B, model.nv), qt, "out")
+    lam = torch.empty((B, nc), dtype=torch.float64, device=qt.device)
+    iters = torch.empty(B, dtype=torch.int32, device=qt.device)
+    res = torch.empty((B, 2), dtype=torch.float64, device=qt.device)
+    ps = _capi.ProximalSettingsC(float(settings.absolute_accuracy), float(settings.relative_accuracy),
+                                 float(settings.mu), int(settings.max_iter))
+    _capi.check(
+        _capi.lib().gb_constraint_dynamics(
+            data.dev.h, _PREC[data.precision], cset.h, C.byref(ps), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt),
+            _ptr(tt), _ptr(ddq), _ptr(lam) if nc else None, _ptr(iters), _ptr(res), _stream_ptr(),
+        )
+    )
+    data.ddq, data.lambda_c, data.constraint_iterations, data.constraint_residuals = ddq, lam, iters, res
+    if B:
+        settings.iter = int(iters.max().item())
+        settings.absolute_residual = float(res[:, 0].max().item())
+        settings.relative_residual = float(res[:, 1].max().item())
+    if contact_datas is not None:
+        row = 0
+        for cd, cm in zip(contact_datas, contact_models):
+            n = cm.size()
+            f = torch.zeros((B, 6), dtype=torch.float64, device=qt.device)
+            f[:, :n] = lam[:, row : row + n]
+            cd.contact_force = _ret(f, was_np, vec)
+            row += n
+    return _ret(ddq, was_np, vec)
+
+
 def _constraint(x, B: int, shape: tuple, name: str):
     """A per-configuration constraint array (B, *shape), or one (shape) shared by the batch,
     as a contiguous float64 CUDA tensor."""

@@ -229,6 +229,131 @@ int gb_kkt_contact_inverse(const gb_model* M, int precision, int layout, long B,
                                  gbi::arr(K, layout, B, n * n), (cudaStream_t)stream);
 }
 
+int gb_constraint_set_create(const gb_model* M, int n, const gb_constraint_desc* cs, gb_constraint_set** out) {
+  if (!M || !out) return set_error(GB_ERR_INVALID_ARGUMENT, "model/out is NULL");
+  *out = nullptr;
+  if (n < 0 || n > 64) return set_error(GB_ERR_SIZE, "the number of constraint models must be in 0..64");
+  if (n > 0 && !cs) return set_error(GB_ERR_INVALID_ARGUMENT, "constraints is NULL");
+  std::vector<int> internal(M->nj_user, -1);  // the caller's joint -> the internal joint carrying it
+  for (int i = 0; i < M->nj; ++i)
+    if (M->ujoint[i] >= 0) internal[M->ujoint[i]] = i;
+  internal[0] = 0;
+  auto* S = new gb_constraint_set;
+  S->model = M;
+  S->n = n;
+  const int nv = M->nv;
+  S->sparsity.assign((size_t)n * nv, 0);
+  for (int e = 0; e < n; ++e) {
+    const gb_constraint_desc& c = cs[e];
+    std::string bad;
+    if (c.type != GB_CONTACT_3D && c.type != GB_CONTACT_6D) bad = "unknown constraint type";
+    else if (c.reference_frame != GB_FRAME_LOCAL && c.reference_frame != GB_FRAME_LOCAL_WORLD_ALIGNED)
+      bad = "constraintDynamics is only operating from LOCAL or LOCAL_WORLD_ALIGNED reference frames";
+    else if (c.joint1_id < 0 || c.joint1_id >= M->nj_user || c.joint2_id < 0 || c.joint2_id >= M->nj_user)
+      bad = "constraint joint index out of range";
+    if (!bad.empty()) {
+      delete S;
+      return set_error(GB_ERR_INVALID_ARGUMENT, "constraint " + std::to_string(e) + ": " + bad);
+    }
+    gbi::ConstraintDev d{};
+    const int size = c.type == GB_CONTACT_3D ? 3 : 6;
+    d.type = c.type;
+    d.frame = c.reference_frame;
+    d.j1 = internal[c.joint1_id];
+    d.j2 = internal[c.joint2_id];
+    d.row = S->nc;
+    S->nc += size;
+    // placements relative to the internal (folded) frames: the caller's frame i is frame_i' F^T
+    for (int side = 0; side < 2; ++side) {
+      const double* P = side == 0 ? c.joint1_placement : c.joint2_placement;
+      double* Q = side == 0 ? d.P1 : d.P2;
+      const double* F = M->fix.data() + 9 * (side == 0 ? d.j1 : d.j2);
+      for (int r = 0; r < 3; ++r) {
+        for (int col = 0; col < 3; ++col)
+          Q[3 * r + col] = F[r] * P[col] + F[3 + r] * P[3 + col] + F[6 + r] * P[6 + col];
+        Q[9 + r] = F[r] * P[9] + F[3 + r] * P[10] + F[6 + r] * P[11];
+      }
+    }
+    for (int k = 0; k < 6; ++k) {
+      d.des[k] = c.desired_acceleration[k];
+      d.Kp[k] = k < size ? c.Kp[k] : 0.0;
+      d.Kd[k] = k < size ? c.Kd[k] : 0.0;
+      if (d.Kp[k] != 0.0 || d.Kd[k] != 0.0) d.gains = 1;
+    }
+    // the columns each side moves (RigidConstraintModel::init, contact-info.hpp:712-790), on the
+    // internal tree: joints up to the common ancestor, and for a point constraint the ancestor's support
+    signed char* sp = S->sparsity.data() + (size_t)e * nv;
+    auto mark = [&](int j, int bit) {
+      for (int k = 0; k < M->nvs[j]; ++k) sp[M->idx_v[j] + k] |= bit;
+    };
+    int c1 = d.j1, c2 = d.j2;
+    while (c1 != c2) {
+      if (c1 > c2) {
+        mark(c1, 1);
+        c1 = M->parents[c1];
+      } else {
+        mark(c2, 2);
+        c2 = M->parents[c2];
+      }
+    }
+    if (c.type == GB_CONTACT_3D)
+      for (int j = c1; j > 0; j = M->parents[j]) mark(j, 3);
+    S->host.push_back(d);
+  }
+  const size_t bytes = sizeof(gbi::ConstraintDev) * (size_t)n + S->sparsity.size();
+  if (bytes > 0) {
+    std::vector<unsigned char> h(bytes);
+    if (n > 0) std::memcpy(h.data(), S->host.data(), sizeof(gbi::ConstraintDev) * (size_t)n);
+    if (!S->sparsity.empty()) std::memcpy(h.data() + sizeof(gbi::ConstraintDev) * (size_t)n, S->sparsity.data(),
+                                          S->sparsity.size());
+    cudaError_t e = cudaMalloc(&S->d_mem, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(S->d_mem, h.data(), bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      if (S->d_mem) cudaFree(S->d_mem);
+      delete S;
+      return gbi::cuda_error(e, "gb_constraint_set_create");
+    }
+  }
+  *out = S;
+  return GB_OK;
+}
+
+int gb_constraint_set_destroy(gb_constraint_set* S) {
+  if (!S) return GB_OK;
+  if (S->d_mem) cudaFree(S->d_mem);
+  delete S;
+  return GB_OK;
+}
+
+int gb_constraint_set_dims(const gb_constraint_set* S, int* n, int* constraint_dim) {
+  if (!S) return set_error(GB_ERR_INVALID_ARGUMENT, "set is NULL");
+  if (n) *n = S->n;
+  if (constraint_dim) *constraint_dim = S->nc;
+  return GB_OK;
+}
+
+int gb_constraint_dynamics(const gb_model* M, int precision, const gb_constraint_set* S,
+                           const gb_proximal_settings* settings, int layout, long B, const double* q, const double* v,
+                           const double* tau, double* ddq, double* lambda_c, int* iterations, double* residuals,
+                           void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (!S || !settings) return set_error(GB_ERR_INVALID_ARGUMENT, "set/settings is NULL");
+  if (S->model != M) return set_error(GB_ERR_INVALID_ARGUMENT, "the constraint set belongs to another model");
+  if (!(settings->mu >= 0.0)) return set_error(GB_ERR_INVALID_ARGUMENT, "mu has to be positive");
+  if (!(settings->absolute_accuracy >= 0.0) || !(settings->relative_accuracy >= 0.0))
+    return set_error(GB_ERR_INVALID_ARGUMENT, "Accuracy must be positive.");
+  if (settings->max_iter < 1) return set_error(GB_ERR_INVALID_ARGUMENT, "max_iter must be greater or equal to 1");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  GB_TRY(gbi::check_ptr(ddq, "ddq"));
+  if (S->nc > 0) GB_TRY(gbi::check_ptr(lambda_c, "lambda_c"));
+  const long nv = M->nv;
+  return gbi::launch_constraint(M, precision, B, S, *settings, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, nv),
+                                gbi::arr(tau, layout, B, nv), gbi::arr(ddq, layout, B, nv),
+                                S->nc > 0 ? gbi::arr(lambda_c, layout, B, S->nc) : gbi::Arr{nullptr, 0, 0}, iterations,
+                                residuals, (cudaStream_t)stream);
+}
+
 int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                           const double* a, double* oMi, double* vout, double* aout, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));

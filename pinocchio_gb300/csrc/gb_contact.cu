@@ -1,5 +1,6 @@
 // Contact dynamics with a given constraint Jacobian: forwardDynamics and
-// impulseDynamics (reference algorithm/contact-dynamics.hxx:81-165, 255-327).
+// impulseDynamics (reference algorithm/contact-dynamics.hxx:81-165, 255-327); and
+// constraintDynamics with rigid constraint models (constrained-dynamics.hxx:188-520).
 //
 // Three launches per call: the CRBA with its FP64 tree factorisation
 // M = U D U^T (k_crba), the bias forces nle = rnea(q, v, 0) (forward dynamics
@@ -207,6 +208,377 @@ __global__ void __launch_bounds__(kThreads)
   for (int k = 0; k < nv; ++k) o[k] = A[k] + R[k];
 }
 
+
+// ---- constraintDynamics with rigid constraint models (algorithm/constrained-dynamics.hxx:188-520) ----
+// Two more launches after the CRBA and the bias forces: k_constraint_setup (world-frame kinematics,
+// the constraint Jacobian rows and drifts of every constraint model) and k_constraint_solve (the
+// Delassus factorisation and the proximal iterations).  The reference factorises the whole KKT matrix
+// [[-mu I, J], [J^T, M]] (contact-cholesky.hxx:152-304); here M = U D U^T and the Delassus matrix
+// J M^-1 J^T + mu I = L L^T are factorised apart, which gives the same iterates.
+
+using X3d = gb::X3<double>;
+using M6d = gb::M6<double>;
+
+__device__ void load_se3(const double* P, X3d& X) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) X.R[k] = P[k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) X.t[k] = P[9 + k];
+}
+__device__ void se3_actinv(const X3d& A, const X3d& B, X3d& o) {  // A^-1 B
+  double d[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = B.t[k] - A.t[k];
+  gb::mtv3(A.R, d, o.t);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) o.R[3 * r + c] = A.R[r] * B.R[c] + A.R[3 + r] * B.R[3 + c] + A.R[6 + r] * B.R[6 + c];
+}
+// the angle-axis vector of a rotation, angle in [0, pi] (spatial/log.hxx:58-170): theta =
+// atan2(|a|, (tr - 1) / 2) with a = unskew(R) = sin(theta) n; w = theta / sin(theta) a away from pi
+// (a series of theta / sin(theta) near 0), near pi the axis from (R + R^T) / 2 - cos(theta) I =
+// (1 - cos(theta)) n n^T with the sign of a
+__device__ void log3(const double* R, double* w, double& theta) {
+  const double a[3] = {0.5 * (R[7] - R[5]), 0.5 * (R[2] - R[6]), 0.5 * (R[3] - R[1])};
+  const double s = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  const double c = fmin(1.0, fmax(-1.0, 0.5 * (R[0] + R[4] + R[8] - 1.0)));
+  theta = atan2(s, c);
+  if (theta < 3.0) {
+    const double t2 = theta * theta;
+    const double k = s < 1e-4 ? 1.0 + t2 / 6.0 + 7.0 * t2 * t2 / 360.0 : theta / s;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) w[i] = k * a[i];
+    return;
+  }
+  const double omc = 1.0 - c;
+  int j = 0;
+  if (R[4] > R[0]) j = 1;
+  if (R[8] > R[4 * j]) j = 2;
+  double n[3];
+  n[j] = sqrt((R[4 * j] - c) / omc);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (i != j) n[i] = (R[3 * i + j] + R[3 * j + i]) / (2.0 * omc * n[j]);
+  const double sg = n[0] * a[0] + n[1] * a[1] + n[2] * a[2] < 0.0 ? -1.0 : 1.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) w[i] = sg * theta * n[i];
+}
+// log6 of a placement (spatial/log.hxx:189-230): [alpha p - w x p / 2 + beta (w . p) w; w]
+__device__ void log6(const X3d& M, M6d& o) {
+  double w[3], theta;
+  log3(M.R, w, theta);
+  const double a[3] = {0.5 * (M.R[7] - M.R[5]), 0.5 * (M.R[2] - M.R[6]), 0.5 * (M.R[3] - M.R[1])};
+  const double t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+  double alpha, beta;
+  if (M.R[0] + M.R[4] + M.R[8] >= 3.0 - 6.0554544523933395e-06) {  // 3 - eps^(1/3)
+    alpha = 1.0 - t2 / 12.0 - t2 * t2 / 720.0;
+    beta = 1.0 / 12.0 + t2 / 720.0;
+  } else {
+    double st, ct;
+    sincos(theta, &st, &ct);
+    alpha = theta * st / (2.0 * (1.0 - ct));
+    beta = 1.0 / (theta * theta) - st / (2.0 * theta * (1.0 - ct));
+  }
+  double wxp[3];
+  gb::cross3(w, M.t, wxp);
+  const double wp = w[0] * M.t[0] + w[1] * M.t[1] + w[2] * M.t[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    o.v[k] = alpha * M.t[k] - 0.5 * wxp[k] + beta * wp * w[k];
+    o.v[3 + k] = w[k];
+  }
+}
+// ov.ang x (ov.lin + ov.ang x p): the velocity-product part of a point's classical acceleration
+__device__ void point_drift(const M6d& ov, const double* p, double* o) {
+  double wxp[3], vp[3];
+  gb::cross3(ov.v + 3, p, wxp);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) vp[k] = ov.v[k] + wxp[k];
+  gb::cross3(ov.v + 3, vp, o);
+}
+
+// Per configuration: the world placements, velocities and velocity-product accelerations of every
+// joint (ContactAndImpulseDynamicsForwardStep, constrained-dynamics.hxx:63-135), then per constraint
+// model its placements (RigidConstraintModel::calc, contact-info.hpp:426-446), Jacobian rows
+// (RigidConstraintModel::jacobian, contact-info.hpp:551-672) into Js and the right-hand side
+// (-drift_1 + drift_2 + Baumgarte correction + desired acceleration, constrained-dynamics.hxx:282-432)
+// into Rh, both [element][configuration].
+template <int CAP>
+__global__ void __launch_bounds__(kThreads)
+    k_constraint_setup(const unsigned char* blob, int bytes, long B, Arr q, Arr v,
+                       const ConstraintDev* __restrict__ tab, const signed char* __restrict__ sparsity, int ncon,
+                       double* Js, double* Rh) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int nv = m.nv;
+  const gb::In qi{q.p + b * q.is, q.es}, vi{v.p + b * v.is, v.es};
+  X3d oM[CAP];
+  M6d ov[CAP], oa[CAP];
+  gb::zero(ov[0]);
+  gb::zero(oa[0]);
+  for (int i = 1; i < m.nj; ++i) {
+    const int p = m.parent[i];
+    X3d X;
+    gb::joint_transform(m, i, qi, X);
+    if (p > 0) gb::compose(oM[p], X, oM[i]);
+    else oM[i] = X;
+    M6d vJ, w;
+    gb::joint_motion(m.jtype[i], vi, m.idx_v[i], vJ);
+    gb::act_motion(oM[i], vJ, w);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) ov[i].v[k] = w.v[k] + ov[p].v[k];
+    gb::cross_motion(ov[p], ov[i], w);  // zero for a root joint (ov[0] = 0)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) oa[i].v[k] = w.v[k] + oa[p].v[k];
+  }
+  const Col J{Js + b, B}, Rhs{Rh + b, B};
+  for (int e = 0; e < ncon; ++e) {
+    const ConstraintDev& c = tab[e];
+    const int n = c.type == GB_CONTACT_3D ? 3 : 6, j1 = c.j1, j2 = c.j2;
+    X3d P1, P2, oMc1, oMc2, c12;
+    load_se3(c.P1, P1);
+    load_se3(c.P2, P2);
+    if (j1 > 0) gb::compose(oM[j1], P1, oMc1);
+    else oMc1 = P1;
+    if (j2 > 0) gb::compose(oM[j2], P2, oMc2);
+    else oMc2 = P2;
+    se3_actinv(oMc1, oMc2, c12);
+    const bool local = c.frame == GB_FRAME_LOCAL;
+    // Jacobian rows: column jj of the world Jacobian, by the side(s) of the loop it moves
+    for (int jj = 0; jj < nv; ++jj) {
+      const int code = sparsity[(long)e * nv + jj];
+      double col[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      if (code != 0) {
+        const int i = m.dof_joint[jj];
+        M6d Jc;
+        gb::world_axis_column(oM[i], gb::jt_col(m.jtype[i], jj - m.idx_v[i]), Jc.v);
+        const double sign = code == 1 ? 1.0 : code == 2 ? -1.0 : 0.0;
+        if (n == 3) {
+          if (local) {
+            if (code == 3) {
+              M6d l1, l2;
+              double r2[3];
+              gb::actinv_motion(oMc1, Jc, l1);
+              gb::actinv_motion(oMc2, Jc, l2);
+              gb::mv3(c12.R, l2.v, r2);
+#pragma unroll
+              for (int k = 0; k < 3; ++k) col[k] = l1.v[k] - r2[k];
+            } else if (code == 1) {
+              M6d l1;
+              gb::actinv_motion(oMc1, Jc, l1);
+#pragma unroll
+              for (int k = 0; k < 3; ++k) col[k] = l1.v[k];
+            } else {
+              M6d l2;
+              double r2[3];
+              gb::actinv_motion(oMc2, Jc, l2);
+              gb::mv3(c12.R, l2.v, r2);
+#pragma unroll
+              for (int k = 0; k < 3; ++k) col[k] = -r2[k];
+            }
+          } else if (code == 3) {
+            double d[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) d[k] = oMc2.t[k] - oMc1.t[k];
+            gb::cross3(d, Jc.v + 3, col);
+          } else {
+            double pxw[3];
+            gb::cross3(code == 1 ? oMc1.t : oMc2.t, Jc.v + 3, pxw);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) col[k] = (Jc.v[k] - pxw[k]) * sign;
+          }
+        } else if (local) {
+          M6d l1;
+          gb::actinv_motion(oMc1, Jc, l1);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) col[k] = l1.v[k] * sign;
+        } else {
+          double pxw[3];
+          gb::cross3(oMc1.t, Jc.v + 3, pxw);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            col[k] = (Jc.v[k] - pxw[k]) * sign;
+            col[3 + k] = Jc.v[3 + k] * sign;
+          }
+        }
+      }
+      for (int k = 0; k < n; ++k) J[(long)(c.row + k) * nv + jj] = col[k];
+    }
+    // velocities and errors of the constraint (constrained-dynamics.hxx:296-350)
+    M6d vc1, vc2, vc21, pe, ve, ae, a1, a2;
+    gb::zero(vc1);
+    gb::zero(vc2);
+    if (j1 > 0) gb::actinv_motion(oMc1, ov[j1], vc1);
+    if (j2 > 0) gb::actinv_motion(oMc2, ov[j2], vc2);
+    gb::act_motion(c12, vc2, vc21);
+    gb::zero(pe);
+    gb::zero(ve);
+    gb::zero(ae);
+    if (n == 6) {
+      M6d lg;
+      log6(c12, lg);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        pe.v[k] = -lg.v[k];
+        ve.v[k] = vc1.v[k] - vc21.v[k];
+      }
+    } else {
+      double r2[3];
+      gb::mv3(c12.R, vc2.v, r2);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        pe.v[k] = -c12.t[k];
+        ve.v[k] = vc1.v[k] - r2[k];
+      }
+    }
+    if (c.gains)
+      for (int k = 0; k < n; ++k) ae.v[k] = -c.Kp[k] * pe.v[k] - c.Kd[k] * ve.v[k];
+    const M6d& oa1 = oa[j1];
+    const M6d& oa2 = oa[j2];
+    double t[3], u[3];
+    if (!local) {  // LOCAL_WORLD_ALIGNED
+      gb::cross3(oa1.v + 3, oMc1.t, t);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a1.v[k] = oa1.v[k] + t[k];
+      if (n == 3) {
+        point_drift(ov[j1], oMc1.t, t);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a1.v[k] += t[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a1.v[3 + k] = oa1.v[3 + k];
+      if (n == 3) {
+        gb::cross3(oa2.v + 3, oMc2.t, t);
+        point_drift(ov[j2], oMc2.t, u);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          a2.v[k] = oa2.v[k] + t[k] + u[k];
+          a2.v[3 + k] = 0.0;
+        }
+      } else {
+        gb::cross3(oa2.v + 3, oMc1.t, t);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          a2.v[k] = oa2.v[k] + t[k];
+          a2.v[3 + k] = oa2.v[3 + k];
+        }
+      }
+      double rl[3], ra[3];
+      gb::mv3(oMc1.R, ae.v, rl);
+      gb::mv3(oMc1.R, ae.v + 3, ra);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ae.v[k] = rl[k];
+        ae.v[3 + k] = ra[k];
+      }
+    } else {
+      gb::actinv_motion(oMc1, oa1, a1);
+      if (n == 3) {
+        gb::cross3(vc1.v + 3, vc1.v, t);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          a1.v[k] += t[k];
+          a1.v[3 + k] = 0.0;
+        }
+        double w[3];
+        gb::cross3(oa2.v + 3, oMc2.t, t);
+        point_drift(ov[j2], oMc2.t, u);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) w[k] = oa2.v[k] + t[k] + u[k];
+        gb::mtv3(oMc1.R, w, a2.v);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a2.v[3 + k] = 0.0;
+      } else {
+        M6d x;
+        gb::cross_motion(ve, vc21, x);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a1.v[k] += x.v[k];
+        gb::actinv_motion(oMc1, oa2, a2);
+      }
+    }
+    for (int k = 0; k < n; ++k) Rhs[c.row + k] = -a1.v[k] + a2.v[k] + ae.v[k] + c.des[k];
+  }
+}
+
+// The proximal iterations (constrained-dynamics.hxx:434-486) on the factorisations M = U D U^T and
+// J M^-1 J^T + mu I = L L^T: lambda_k = L^-T L^-1 (c0 + mu lambda_{k-1}) with c0 = rhs - J M^-1 (tau -
+// nle); the reference's residuals: absolute ||(J M^-1 J^T) y - rhs||_inf and relative ||y - y_prev||_inf
+// for y = -lambda_k; then ddq = M^-1 (tau - nle + J^T lambda).
+__global__ void __launch_bounds__(kThreads)
+    k_constraint_solve(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
+                       const double* nles, double* Rs, double* Ys, double* Gs, const double* Js, const double* Rh,
+                       double* C0s, double* LPs, double* Ts, Arr tau, gb_proximal_settings s, Arr ddq, Arr lam,
+                       int* iters, double* residuals) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int nv = m.nv;
+  const Col U{const_cast<double*>(Us) + b, B}, D{const_cast<double*>(Ds) + b, B};
+  const Col Y{Ys + b, B}, G{Gs + b, B}, R{Rs + b, B};
+  const Col C0{C0s + b, B}, LP{LPs + b, B}, T{Ts + b, B}, Rhs{const_cast<double*>(Rh) + b, B};
+  const gb::In taui{tau.p + b * tau.is, tau.es}, Ji{Js + b, B};
+  const gb::Out o{const_cast<double*>(ddq.p) + b * ddq.is, ddq.es};
+  const Col nle{const_cast<double*>(nles) + b, B};
+  for (int k = 0; k < nv; ++k) R[k] = taui[k] - nle[k];
+  chol_solve(m, U, D, R);
+  int it = 0;
+  double ar = 0.0, rr = 0.0;
+  const Col L{nc > 0 ? const_cast<double*>(lam.p) + b * lam.is : nullptr, nc > 0 ? lam.es : 0};
+  if (nc > 0) {
+    delassus_llt(m, U, D, Ji, nc, s.mu, Y, G);
+    for (int c = 0; c < nc; ++c) {
+      double t = 0.0;
+      for (int k = 0; k < nv; ++k) t += Ji[c * nv + k] * R[k];
+      C0[c] = Rhs[c] - t;
+      LP[c] = 0.0;
+    }
+    while (it < s.max_iter) {
+      ++it;
+      for (int c = 0; c < nc; ++c) L[c] = C0[c] + s.mu * LP[c];
+      llt_solve(G, nc, L);
+      for (int i = 0; i < nc; ++i) {  // T = L_f^T lambda (L_f the lower factor in G)
+        double t = 0.0;
+        for (int k = i; k < nc; ++k) t += G[(long)k * nc + i] * L[k];
+        T[i] = t;
+      }
+      ar = 0.0;
+      rr = 0.0;
+      for (int i = 0; i < nc; ++i) {
+        double t = 0.0;
+        for (int k = 0; k <= i; ++k) t += G[(long)i * nc + k] * T[k];
+        ar = fmax(ar, fabs(t - s.mu * L[i] + Rhs[i]));
+        rr = fmax(rr, fabs(L[i] - LP[i]));
+      }
+      for (int c = 0; c < nc; ++c) LP[c] = L[c];
+      if (ar <= s.absolute_accuracy || rr <= s.relative_accuracy) break;
+    }
+  } else {
+    it = 1;
+  }
+  if (iters) iters[b] = it;
+  if (residuals) {
+    residuals[2 * b] = ar;
+    residuals[2 * b + 1] = rr;
+  }
+  const Col A{Y.p, B};
+  for (int k = 0; k < nv; ++k) {
+    double t = 0.0;
+    for (int c = 0; c < nc; ++c) t += Ji[c * nv + k] * L[c];
+    A[k] = t;
+  }
+  chol_solve(m, U, D, A);
+  bool finite = true;
+  for (int k = 0; k < nv; ++k) {
+    const double x = A[k] + R[k];
+    finite = finite && gb::finite_value(x);
+    o[k] = x;
+  }
+  if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
+}
 }  // namespace
 
 int launch_contact(const gb_model* M, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
@@ -244,6 +616,65 @@ int launch_contact(const gb_model* M, int precision, bool impulse, long B, int n
                                                                          nles, Rs, Ys, Gs, x, J, gamma, r_coeff,
                                                                          inv_damping, out, lam);
     rc = cuda_error(cudaGetLastError(), "k_contact");
+  }
+  scratch_free(scratch, st);
+  return rc;
+}
+
+int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
+                      const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
+                      double* residuals, cudaStream_t st) {
+  const long nv = M->nv, nn = nv * nv, nc = set->nc;
+  // scratch, [element][configuration]: M, U (nn), D, nle, r (nv), sDUiJt (nv * max(nc, 1)), G (nc * nc),
+  // J (nc * nv), rhs, c0, lambda_prev, tmp (nc)
+  const long ny = nv * (nc > 0 ? nc : 1), ng = nc * nc;
+  void* scratch = nullptr;
+  int rc = scratch_alloc(&scratch, sizeof(double) * (size_t)B * (2 * nn + 3 * nv + ny + ng + nc * nv + 4 * nc), st);
+  if (rc != GB_OK) return rc;
+  double* base = static_cast<double*>(scratch);
+  double *Ms = base, *Us = Ms + nn * B, *Ds = Us + nn * B, *nles = Ds + nv * B, *Rs = nles + nv * B,
+         *Ys = Rs + nv * B, *Gs = Ys + ny * B, *Js = Gs + ng * B, *Rh = Js + nc * nv * B, *C0 = Rh + nc * B,
+         *LP = C0 + nc * B, *Ts = LP + nc * B;
+  const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
+  const signed char* sp = reinterpret_cast<const signed char*>(tab + (set->n > 0 ? set->n : 0));
+  rc = launch_crba(M, GB_FP64, false, B, q, Arr{Ms, 1, B}, Arr{Us, 1, B}, Arr{Ds, 1, B}, st);
+  if (rc == GB_OK) {
+    const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+    const Arr zero{reinterpret_cast<const double*>(M->d_blob + h->o_zero), 0, 0};
+    rc = launch_rnea(M, precision, B, q, v, zero, Arr{nles, 1, B}, st);
+  }
+  const long grid = (B + kThreads - 1) / kThreads;
+  auto opt_in = [&](const void* kern, const char* name) -> int {
+    if (M->stage_bytes <= 48 * 1024) return GB_OK;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M->stage_bytes);
+    return e == cudaSuccess ? GB_OK : cuda_error(e, name);
+  };
+  if (rc == GB_OK && set->n > 0) {
+    switch (M->cap) {
+#define GB_SETUP(C)                                                                                         \
+  case C:                                                                                                   \
+    rc = opt_in((const void*)k_constraint_setup<C>, "k_constraint_setup");                                  \
+    if (rc == GB_OK)                                                                                        \
+      k_constraint_setup<C><<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, q, v, \
+                                                                               tab, sp, set->n, Js, Rh);    \
+    break;
+      GB_SETUP(8)
+      GB_SETUP(16)
+      GB_SETUP(32)
+      GB_SETUP(64)
+      GB_SETUP(128)
+#undef GB_SETUP
+      default:
+        rc = set_error(GB_ERR_UNSUPPORTED, "model too large");
+    }
+    if (rc == GB_OK) rc = cuda_error(cudaGetLastError(), "k_constraint_setup");
+  }
+  if (rc == GB_OK) rc = opt_in((const void*)k_constraint_solve, "k_constraint_solve");
+  if (rc == GB_OK) {
+    k_constraint_solve<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds,
+                                                                        nles, Rs, Ys, Gs, Js, Rh, C0, LP, Ts, tau, s,
+                                                                        ddq, lam, iters, residuals);
+    rc = cuda_error(cudaGetLastError(), "k_constraint_solve");
   }
   scratch_free(scratch, st);
   return rc;

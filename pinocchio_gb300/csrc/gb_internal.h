@@ -20,6 +20,27 @@ struct gb_pool {
 
 namespace gbi {
 
+// One rigid constraint model as the kernels read it (gb_constraint_set): the joints of the
+// internal tree and the placements relative to their (folded) frames; `row` is the first
+// constraint row, `gains` whether any Baumgarte gain is non-zero.
+struct ConstraintDev {
+  int type, frame, j1, j2, row, gains, pad0, pad1;
+  double P1[12], P2[12], des[6], Kp[6], Kd[6];
+};
+
+}  // namespace gbi
+
+struct gb_constraint_set {
+  const gb_model* model = nullptr;
+  int n = 0, nc = 0;
+  std::vector<gbi::ConstraintDev> host;
+  // per constraint and dof: 0 no column, 1 joint 1's side only, 2 joint 2's side only, 3 both
+  std::vector<signed char> sparsity;
+  void* d_mem = nullptr;  // the table, then the sparsity codes
+};
+
+namespace gbi {
+
 int set_error(int code, const std::string& msg);
 int cuda_error(cudaError_t e, const char* where);
 
@@ -54,6 +75,9 @@ int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q,
 int launch_contact(const gb_model* m, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
                    Arr gamma, double r_coeff, double inv_damping, Arr out, Arr lam, cudaStream_t st);
 int launch_kkt_inverse(const gb_model* m, long B, int nc, Arr q, Arr J, double inv_damping, Arr K, cudaStream_t st);
+int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
+                      const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
+                      double* residuals, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);

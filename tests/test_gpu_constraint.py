@@ -1,0 +1,233 @@
+"""GPU parity of constraintDynamics (reference algorithm/constrained-dynamics.hxx:188-520) through the
+C ABI against the oracle: point and frame contacts in LOCAL and LOCAL_WORLD_ALIGNED axes, closed
+loops between two limbs, Baumgarte gains and desired accelerations, the proximal iterations with
+mu > 0 (iteration counts and residuals), a redundant pair of contacts, no constraint (= ABA), both
+precisions and both batch layouts, every joint type, and the argument errors."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pinocchio_gb300 as pg
+from oracle.oracle import LOCAL as CONV_LOCAL
+from oracle.oracle import OracleModel
+from pinocchio_gb300 import _capi
+from pinocchio_gb300 import constraints as cs
+from pinocchio_gb300 import model as gm
+from pinocchio_gb300 import sample_models as sm
+from util import FP64_TOL, MODELS, mixed_tol, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand_se3(rng, scale=0.2):
+    a = rng.standard_normal(3)
+    th = np.linalg.norm(a)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]]) / th
+    return gm.SE3(np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K, scale * rng.standard_normal(3))
+
+
+def _leaves(model):
+    par = set(model.parents[1:])
+    return [j for j in range(1, model.njoints) if j not in par]
+
+
+def _exclusive_dofs(model, leaf):
+    """The dofs between a leaf and its first branching ancestor (only this leaf's constraint moves them)."""
+    nchild = np.bincount(np.asarray(model.parents[1:]), minlength=model.njoints)
+    n, j = 0, leaf
+    while j > 0:
+        n += model.nvs[j]
+        if nchild[model.parents[j]] > 1 or model.parents[j] == 0:
+            break
+        j = model.parents[j]
+    return n
+
+
+def _support(model, j):
+    cols = []
+    while j > 0:
+        cols += list(range(model.idx_vs[j], model.idx_vs[j] + model.nvs[j]))
+        j = model.parents[j]
+    return cols
+
+
+def _constraints(model, seed, gains=False):
+    """Full-rank constraints: per leaf a frame contact (6 rows) when at least 6 dofs serve only that
+    leaf, a point contact (3 rows) when at least 3 do, in alternating LOCAL / LOCAL_WORLD_ALIGNED
+    axes, anchored to random world frames."""
+    rng = np.random.default_rng(seed)
+    cms = []
+    for k, leaf in enumerate(_leaves(model)):
+        n = _exclusive_dofs(model, leaf)
+        if n < 3:
+            continue
+        t = cs.CONTACT_6D if n >= 6 and k % 2 == 0 else cs.CONTACT_3D
+        f = cs.LOCAL if (k // 2) % 2 == 0 else cs.LOCAL_WORLD_ALIGNED
+        cms.append(cs.RigidConstraintModel(t, model, leaf, _rand_se3(rng), 0, _rand_se3(rng, 1.0), f))
+    if not cms:  # no leaf has three dofs of its own: one point contact on the deepest leaf
+        depth = {j: len(_support(model, j)) for j in _leaves(model)}
+        leaf = max(depth, key=depth.get)
+        cms.append(cs.RigidConstraintModel(cs.CONTACT_3D, model, leaf, _rand_se3(rng), 0, _rand_se3(rng, 1.0),
+                                           cs.LOCAL))
+    if gains:
+        for c in cms:
+            c.corrector.Kp[:] = rng.uniform(0.5, 5.0, c.size())
+            c.corrector.Kd[:] = rng.uniform(0.5, 5.0, c.size())
+            c.desired_contact_acceleration[:] = rng.standard_normal(6)
+    return cms
+
+
+def _loop_constraints(model, seed):
+    """The humanoid's limbs: a frame loop between the first two, a point contact on the third, a frame
+    contact on the fourth (15 rows, each limb's six dofs serving one constraint)."""
+    rng = np.random.default_rng(seed)
+    lv = _leaves(model)
+    return [
+        cs.RigidConstraintModel(cs.CONTACT_6D, model, lv[0], _rand_se3(rng), lv[1], _rand_se3(rng), cs.LOCAL),
+        cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[2], _rand_se3(rng), 0, _rand_se3(rng, 1.0),
+                                cs.LOCAL_WORLD_ALIGNED),
+        cs.RigidConstraintModel(cs.CONTACT_6D, model, lv[3], _rand_se3(rng), cs.LOCAL_WORLD_ALIGNED),
+    ]
+
+
+def _fp64_tol(om, q, v, tau, desc, **kw):
+    """The FP64 bar of one case: 30 x the double oracle's own error against the long-double oracle
+    (the KKT solve's conditioning), at least 1e-10."""
+    a = om.constraint_dynamics(q, v, tau, desc, **kw)
+    b = om.constraint_dynamics(q, v, tau, desc, prec=1, **kw)
+    return a, b, max(1e-10, 30 * max(rel_err(a[0], b[0]), rel_err(a[1], b[1]) if a[1].size else 0.0))
+
+
+def _dev(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", list(MODELS) + ["humanoid32-loop"])
+def test_constraint_dynamics_matches_oracle(name, precision):
+    loop = name.endswith("-loop")
+    model = MODELS[name.replace("-loop", "")]()
+    om = OracleModel(model)
+    cms = _loop_constraints(model, 4) if loop else _constraints(model, 3, gains=name in ("humanoid32", "mixedtree24ff"))
+    q, v, x = sm.random_inputs(model, 333, 12)
+    v = 0.3 * v
+    tau = 10 * x
+    data = pg.createData(model, precision)
+    cds = [cs.RigidConstraintData(c) for c in cms]
+    ddq = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(tau), cms, cds).cpu().numpy()
+    lam = data.lambda_c.cpu().numpy()
+    (d_o, l_o, it_o, res_o), (d_ld, l_ld, _, _), tol64 = _fp64_tol(om, q, v, tau, cs.stack_desc(cms))
+    if precision == "fp64":
+        assert rel_err(ddq, d_ld) < tol64
+        assert lam.size == 0 or rel_err(lam, l_ld) < tol64
+    else:
+        tol = max(mixed_tol(name.replace("-loop", "")), 30 * tol64)
+        if name == "chain100":
+            tol = 1e-3
+        assert rel_err(ddq, d_o) < tol
+        assert lam.size == 0 or rel_err(lam, l_o) < tol
+    assert np.array_equal(data.constraint_iterations.cpu().numpy(), it_o)
+    row = 0
+    for cd, c in zip(cds, cms):
+        f = cd.contact_force.cpu().numpy()
+        assert np.array_equal(f[:, : c.size()], lam[:, row : row + c.size()])
+        assert np.all(f[:, c.size():] == 0)
+        row += c.size()
+    assert pg.numericStatus(data) == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_proximal_iterations(precision):
+    """mu > 0: the iteration counts and residuals follow the oracle's proximal loop; a duplicated
+    contact (singular Delassus matrix) gives the single contact's accelerations."""
+    model = sm.humanoid32(1)
+    om = OracleModel(model)
+    cms = _loop_constraints(model, 5)
+    q, v, x = sm.random_inputs(model, 200, 13)
+    data = pg.createData(model, precision)
+    st = pg.ProximalSettings(1e-10, 1e-4, 50)
+    ddq = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms, None, st).cpu().numpy()
+    d_o, l_o, it_o, res_o = om.constraint_dynamics(q, v, 10 * x, cs.stack_desc(cms), mu=1e-4, max_iter=50,
+                                                   absolute_accuracy=1e-10, relative_accuracy=1e-10)
+    it = data.constraint_iterations.cpu().numpy()
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert rel_err(ddq, d_o) < tol
+    assert np.abs(it - it_o).max() <= 1 and it.max() > 1 and st.iter == it.max()
+    res = data.constraint_residuals.cpu().numpy()
+    assert np.all((res[:, 0] <= 1e-10) | (res[:, 1] <= 1e-10) | (it == 50))
+    d1 = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms[:1]).cpu().numpy()
+    st2 = pg.ProximalSettings(1e-12, 1e-6, 300)
+    d2 = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms[:1] * 2, None, st2).cpu().numpy()
+    assert rel_err(d2, d1) < (1e-7 if precision == "fp64" else 1e-5)
+
+
+def test_no_constraint_is_aba_and_layouts():
+    import torch
+
+    model = MODELS["mixedtree24ff"]()
+    q, v, x = sm.random_inputs(model, 257, 14)
+    data = pg.createData(model)
+    ddq = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), []).cpu().numpy()
+    assert rel_err(ddq, OracleModel(model).aba(q, v, 10 * x, CONV_LOCAL)) < FP64_TOL
+    assert data.lambda_c.shape == (257, 0) and torch.all(data.constraint_iterations == 1)
+    # SOA layout: the same bits
+    cms = _constraints(model, 6)
+    assert cms
+    pg.initConstraintDynamics(model, data, cms)
+    ref = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms).cpu().numpy()
+    lam = data.lambda_c.cpu().numpy()
+    B, nv, nc = q.shape[0], model.nv, lam.shape[1]
+    outs = [torch.empty((n, B), dtype=torch.float64, device="cuda") for n in (nv, nc)]
+    ps = _capi.ProximalSettingsC(1e-12, 1e-12, 0.0, 1)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    qs, vs, ts = (_dev(np.ascontiguousarray(t.T)) for t in (q, v, 10 * x))
+    _capi.check(_capi.lib().gb_constraint_dynamics(data.dev.h, _capi.GB_FP64, data.constraint_set.h, C.byref(ps),
+                                                   _capi.GB_LAYOUT_SOA, B, p(qs), p(vs), p(ts), p(outs[0]),
+                                                   p(outs[1]), None, None, None))
+    torch.cuda.synchronize()
+    assert np.array_equal(outs[0].cpu().numpy().T, ref) and np.array_equal(outs[1].cpu().numpy().T, lam)
+
+
+def test_batch_equals_single():
+    model = sm.humanoid32(1)
+    cms = _loop_constraints(model, 8)
+    cms[0].corrector.Kp[:] = 2.0
+    q, v, x = sm.random_inputs(model, 64, 15)
+    data = pg.createData(model)
+    full = pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms).cpu().numpy()
+    for b in (0, 31, 63):
+        one = pg.constraintDynamics(model, data, _dev(q[b]), _dev(v[b]), _dev(10 * x[b]), cms).cpu().numpy()
+        assert np.array_equal(one, full[b])
+
+
+def test_argument_errors():
+    model = sm.humanoid32(1)
+    data = pg.createData(model)
+    other = pg.createData(model)
+    L = _capi.lib()
+    arr = (_capi.ConstraintDesc * 1)()
+    arr[0].type, arr[0].reference_frame, arr[0].joint1_id = _capi.GB_CONTACT_6D, _capi.GB_FRAME_WORLD, 5
+    h = C.c_void_p()
+    assert L.gb_constraint_set_create(data.dev.h, 1, arr, C.byref(h)) == _capi.GB_ERR_INVALID_ARGUMENT
+    arr[0].reference_frame, arr[0].joint1_id = _capi.GB_FRAME_LOCAL, model.njoints
+    assert L.gb_constraint_set_create(data.dev.h, 1, arr, C.byref(h)) == _capi.GB_ERR_INVALID_ARGUMENT
+    arr[0].joint1_id, arr[0].type = 5, 7
+    assert L.gb_constraint_set_create(data.dev.h, 1, arr, C.byref(h)) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_constraint_set_create(data.dev.h, 65, arr, C.byref(h)) == _capi.GB_ERR_SIZE
+    cms = _constraints(model, 9)
+    pg.initConstraintDynamics(model, data, cms)
+    q, v, x = (_dev(a) for a in sm.random_inputs(model, 4, 16))
+    ps = _capi.ProximalSettingsC(1e-12, 1e-12, -1.0, 1)
+    out = _dev(np.zeros((4, model.nv)))
+    lam = _dev(np.zeros((4, data.constraint_set.nc)))
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    args = (_capi.GB_LAYOUT_INSTANCE, 4, p(q), p(v), p(x), p(out), p(lam), None, None, None)
+    assert L.gb_constraint_dynamics(data.dev.h, 0, data.constraint_set.h, C.byref(ps), *args) == _capi.GB_ERR_INVALID_ARGUMENT
+    ps.mu, ps.max_iter = 0.0, 0
+    assert L.gb_constraint_dynamics(data.dev.h, 0, data.constraint_set.h, C.byref(ps), *args) == _capi.GB_ERR_INVALID_ARGUMENT
+    ps.max_iter = 1
+    assert L.gb_constraint_dynamics(other.dev.h, 0, data.constraint_set.h, C.byref(ps), *args) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_constraint_dynamics(data.dev.h, 0, data.constraint_set.h, C.byref(ps), *args) == _capi.GB_OK
