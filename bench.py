@@ -298,7 +298,7 @@ def _per_config_rel_err(got, ref):
     return float(e.max()), float(np.median(e))
 
 
-def _function_reference(om, fname, q, v, x, f, J, g):
+def _function_reference(om, fname, q, v, x, f, J, g, desc=None):
     """The FP64 oracle's outputs of one benchmarked function, in the order the API returns them."""
     from oracle.oracle import symmetrize_upper
 
@@ -323,7 +323,27 @@ def _function_reference(om, fname, q, v, x, f, J, g):
         "aba_fext": lambda: (om.aba(q, v, t, fext=f),),
         "aba_derivatives_fext": lambda: om.aba_derivatives(q, v, t, fext=f)[1:],
         "forward_dynamics_12rows": lambda: (om.forward_dynamics(q, v, t, J, g)[0],),
+        "constraint_dynamics_18rows": lambda: (om.constraint_dynamics(q, v, t, desc)[0],),
     }[fname]()
+
+
+def humanoid_contacts(pg, model):
+    """Four contacts of the humanoid's limbs to world anchors: frame contacts (LOCAL) on the two
+    legs, point contacts (LOCAL_WORLD_ALIGNED) on the two arms -- 18 constraint rows."""
+    rng = np.random.default_rng(17)
+    par = set(model.parents[1:])
+    leaves = [j for j in range(1, model.njoints) if j not in par]
+    out = []
+    for k, leaf in enumerate(leaves[:4]):
+        R, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        R *= np.sign(np.linalg.det(R))
+        P = pg.SE3(R, 0.1 * rng.standard_normal(3))
+        anchor = pg.SE3(np.eye(3), rng.standard_normal(3))
+        if k < 2:
+            out.append(pg.RigidConstraintModel(pg.CONTACT_6D, model, leaf, P, 0, anchor, pg.LOCAL))
+        else:
+            out.append(pg.RigidConstraintModel(pg.CONTACT_3D, model, leaf, P, 0, anchor, pg.LOCAL_WORLD_ALIGNED))
+    return out
 
 
 def measure_functions(torch, pg, sm):
@@ -332,13 +352,17 @@ def measure_functions(torch, pg, sm):
     forwardKinematics (q, v, a) / computeJointJacobians at batch 65536, the two derivative
     algorithms at batch 16384; RNEA, ABA and the ABA derivatives with external forces on
     every joint (the fext overloads) at the same batches; forwardDynamics with 12 constraint
-    rows (two 6-D contacts) at batch 65536.  Each function's outputs are checked against the
+    rows (two 6-D contacts) and constraintDynamics with four contacts (18 rows) at batch 65536.  Each function's outputs are checked against the
     FP64 oracle on 256 configurations strided over its batch: the max and median over those
     configurations of the relative error of every output."""
     from oracle.oracle import OracleModel
 
+    from pinocchio_gb300.constraints import stack_desc
+
     model = sm.humanoid32(1)
     om = OracleModel(model)
+    contacts = humanoid_contacts(pg, model)
+    desc = stack_desc(contacts)
     out = {}
     for prec in ("fp64", "mixed"):
         data = pg.createData(model, prec)
@@ -347,7 +371,8 @@ def measure_functions(torch, pg, sm):
                          ("rnea_derivatives", 16384), ("aba_derivatives", 16384), ("compute_minverse", 65536),
                          ("nonlinear_effects", 65536), ("generalized_gravity", 65536),
                          ("forward_kinematics", 65536), ("joint_jacobians", 65536), ("rnea_fext", 65536),
-                         ("aba_fext", 65536), ("aba_derivatives_fext", 16384), ("forward_dynamics_12rows", 65536)):
+                         ("aba_fext", 65536), ("aba_derivatives_fext", 16384), ("forward_dynamics_12rows", 65536),
+                         ("constraint_dynamics_18rows", 65536)):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
             f = torch.randn((B, model.njoints, 6), dtype=torch.float64, device="cuda")
             Jc = torch.randn((B, 12, model.nv), dtype=torch.float64, device="cuda") if fname.startswith("forward_dyn") else None
@@ -368,6 +393,7 @@ def measure_functions(torch, pg, sm):
                 "aba_fext": lambda: pg.aba(model, data, q, v, 10.0 * x, f),
                 "aba_derivatives_fext": lambda: pg.computeABADerivatives(model, data, q, v, 10.0 * x, f),
                 "forward_dynamics_12rows": lambda: pg.forwardDynamics(model, data, q, v, 10.0 * x, Jc, gc),
+                "constraint_dynamics_18rows": lambda: pg.constraintDynamics(model, data, q, v, 10.0 * x, contacts),
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}
@@ -375,7 +401,7 @@ def measure_functions(torch, pg, sm):
             got = [t for t in (got if isinstance(got, tuple) else (got,)) if t is not None]
             idx = torch.from_numpy(np.unique(np.linspace(0, B - 1, 256).astype(np.int64))).cuda()
             host = lambda t: None if t is None else t[idx].cpu().numpy()  # noqa: E731
-            ref = _function_reference(om, fname, host(q), host(v), host(x), host(f), host(Jc), host(gc))
+            ref = _function_reference(om, fname, host(q), host(v), host(x), host(f), host(Jc), host(gc), desc)
             errs = [_per_config_rel_err(host(a), b) for a, b in zip(got, ref)]
             res[fname]["max_rel_err"] = max(e[0] for e in errs)
             res[fname]["median_rel_err"] = max(e[1] for e in errs)
@@ -466,8 +492,10 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
     the inputs in pinned host memory and every output copied back to pinned host memory, each
     step.  Outputs are double-buffered: step k's device-to-host copies run on a copy stream
     while step k + 1's kernels run on the compute stream (two output sets, preallocated and
-    passed as ``out=``, on the device and on the host).  Beside it, the copy floor: the same
-    bytes moved by plain pinned copies alone."""
+    passed as ``out=``, on the device and on the host).  The compute runs on its own stream:
+    on the legacy default stream the concurrent device-to-host copies fell to ~20 GB/s after a
+    few steps (measured), on a non-default stream they keep the link's rate.  Beside it, the copy
+    floor: the same bytes moved by plain pinned copies alone."""
     nq, nv = model.nq, model.nv
     h2d = B * (nq + 2 * nv) * 8
     d2h = B * (nv + 3 * nv * nv) * 8
@@ -480,7 +508,7 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
     from pinocchio_gb300 import autotune
 
     autotune.tune(model, d, functions=("aba", "aba_derivatives"), batch=B, use_cache=False)
-    comp = torch.cuda.current_stream()
+    comp = torch.cuda.Stream()
     copy = torch.cuda.Stream()
     din = [tuple(torch.empty(t.shape, dtype=torch.float64, device="cuda") for t in (hq[0], hv[0], ht[0]))
            for _ in range(2)]
@@ -494,14 +522,15 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
     def e2e_step(k):
         s = k % 2
         q, v, t = din[s]
-        comp.wait_event(freed[s])  # the inputs / outputs of step k - 2 are no longer in use
-        q.copy_(hq[s], non_blocking=True)
-        v.copy_(hv[s], non_blocking=True)
-        t.copy_(ht[s], non_blocking=True)
         ddq, dq, dv, Mi, ddq_d = dout[s]
-        pg.aba(model, d, q, v, t, out=ddq)
-        pg.computeABADerivatives(model, d, q, v, t, out=(dq, dv, Mi, ddq_d))
-        done[s].record(comp)
+        with torch.cuda.stream(comp):
+            comp.wait_event(freed[s])  # the inputs / outputs of step k - 2 are no longer in use
+            q.copy_(hq[s], non_blocking=True)
+            v.copy_(hv[s], non_blocking=True)
+            t.copy_(ht[s], non_blocking=True)
+            pg.aba(model, d, q, v, t, out=ddq)
+            pg.computeABADerivatives(model, d, q, v, t, out=(dq, dv, Mi, ddq_d))
+            done[s].record(comp)
         with torch.cuda.stream(copy):
             copy.wait_event(done[s])
             for name, src in (("ddq", ddq), ("ddq_dq", dq), ("ddq_dv", dv), ("Minv", Mi)):
