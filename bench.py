@@ -494,7 +494,9 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
     while step k + 1's kernels run on the compute stream (two output sets, preallocated and
     passed as ``out=``, on the device and on the host).  The compute runs on its own stream:
     on the legacy default stream the concurrent device-to-host copies fell to ~20 GB/s after a
-    few steps (measured), on a non-default stream they keep the link's rate.  Beside it, the copy
+    few steps (measured), on a non-default stream they keep the link's rate.  The transfers go
+    through the library's ``copyAsync`` (torch's ``copy_`` with pinned memory stalled the
+    concurrent copies for tens of milliseconds every ~40 steps, measured).  Beside it, the copy
     floor: the same bytes moved by plain pinned copies alone."""
     nq, nv = model.nq, model.nv
     h2d = B * (nq + 2 * nv) * 8
@@ -525,16 +527,15 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
         ddq, dq, dv, Mi, ddq_d = dout[s]
         with torch.cuda.stream(comp):
             comp.wait_event(freed[s])  # the inputs / outputs of step k - 2 are no longer in use
-            q.copy_(hq[s], non_blocking=True)
-            v.copy_(hv[s], non_blocking=True)
-            t.copy_(ht[s], non_blocking=True)
+            for dst, src in ((q, hq[s]), (v, hv[s]), (t, ht[s])):
+                pg.copyAsync(dst, src)
             pg.aba(model, d, q, v, t, out=ddq)
             pg.computeABADerivatives(model, d, q, v, t, out=(dq, dv, Mi, ddq_d))
             done[s].record(comp)
         with torch.cuda.stream(copy):
             copy.wait_event(done[s])
             for name, src in (("ddq", ddq), ("ddq_dq", dq), ("ddq_dv", dv), ("Minv", Mi)):
-                ho[s][name].copy_(src, non_blocking=True)
+                pg.copyAsync(ho[s][name], src)
             freed[s].record(copy)
         keep[s] = (ddq, dq, dv, Mi)
 
@@ -580,7 +581,7 @@ def measure_e2e(torch, pg, model, host, B, args, dist, world):
                 st.wait_event(s0)
                 with torch.cuda.stream(st):
                     for j in range(k, len(pieces), nstreams):
-                        pieces[j][0].copy_(pieces[j][1], non_blocking=True)
+                        pg.copyAsync(pieces[j][0], pieces[j][1])
                 ev = torch.cuda.Event()
                 ev.record(st)
                 ends.append(ev)

@@ -141,6 +141,12 @@ int gb_pipeline_timeouts(unsigned int* count, int reset);
  * timeout in the count above; the context stays usable. */
 int gb_pipeline_wait_selftest(unsigned int limit_us, void* stream);
 
+/* Utility without a reference counterpart: a stream-ordered copy of `bytes` bytes between
+ * host and device memory (any direction; page-locked host memory makes it asynchronous),
+ * for moving a batch's inputs and outputs next to the calls that use them.  bytes == 0 is a
+ * no-op; NULL pointers otherwise are rejected. */
+int gb_memcpy_async(void* dst, const void* src, size_t bytes, void* stream);
+
 /* tau = rnea(model, data, q, v, a) for every instance
  * (reference algorithm/rnea.hxx:117-161, public rnea.hxx:766). */
 int gb_rnea(const gb_model* model, int precision, int layout, long batch, const double* q, const double* v,

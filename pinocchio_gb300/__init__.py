@@ -55,6 +55,7 @@ from .api import (  # noqa: F401
     computeStaticTorque,
     computeStaticTorqueDerivatives,
     constraintDynamics,
+    copyAsync,
     crba,
     crbaCholesky,
     createData,

@@ -35,6 +35,7 @@ EXPORTS = (
     "gb_numeric_status",
     "gb_pipeline_timeouts",
     "gb_pipeline_wait_selftest",
+    "gb_memcpy_async",
     "gb_rnea",
     "gb_nonlinear_effects",
     "gb_generalized_gravity",
@@ -172,6 +173,7 @@ def lib():
         L.gb_pipeline_timeouts.argtypes = [C.POINTER(C.c_uint), i]
         L.gb_numeric_status.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.gb_pipeline_wait_selftest.argtypes = [C.c_uint, vp]
+        L.gb_memcpy_async.argtypes = [vp, vp, C.c_size_t, vp]
         L.gb_rnea.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp]
         L.gb_nonlinear_effects.argtypes = [vp, i, i, l, vp, vp, vp, vp]
         L.gb_generalized_gravity.argtypes = [vp, i, i, l, vp, vp, vp]

@@ -97,6 +97,21 @@ def _stream_ptr():
     return C.c_void_p(_torch().cuda.current_stream().cuda_stream)
 
 
+def copyAsync(dst, src) -> None:
+    """dst <- src on the current CUDA stream through the library's runtime (gb_memcpy_async):
+    tensors of the same number of bytes, contiguous, each on the device or in host memory
+    (page-locked host memory makes the copy asynchronous).  A batch's host inputs and outputs
+    move next to the calls that use them; measured on GB300, torch's own ``copy_`` between
+    pinned host memory and the device stalled for tens of milliseconds every few hundred
+    milliseconds while other work ran, this path does not."""
+    nb = dst.numel() * dst.element_size()
+    if src.numel() * src.element_size() != nb:
+        raise ValueError("copyAsync: dst and src sizes differ")
+    if not (dst.is_contiguous() and src.is_contiguous()):
+        raise ValueError("copyAsync: tensors must be contiguous")
+    _capi.check(_capi.lib().gb_memcpy_async(_ptr(dst), _ptr(src), nb, _stream_ptr()))
+
+
 def _as_batch(x, n: int, name: str):
     """(tensor (B, n) float64 contiguous on CUDA, was_numpy, was_vector)."""
     torch = _torch()

@@ -103,6 +103,12 @@ int gb_numeric_status(const gb_model* M, unsigned int* flags, int reset) {
   return set_error(GB_ERR_NUMERIC, msg);
 }
 
+int gb_memcpy_async(void* dst, const void* src, size_t bytes, void* stream) {
+  if (bytes == 0) return GB_OK;
+  if (!dst || !src) return set_error(GB_ERR_INVALID_ARGUMENT, "dst/src is NULL");
+  return gbi::cuda_error(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, (cudaStream_t)stream), "gb_memcpy_async");
+}
+
 int gb_model_dims(const gb_model* M, int* nq, int* nv, int* nj) {
   if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
   if (nq) *nq = M->nq;

@@ -164,3 +164,22 @@ def test_preallocated_outputs(name):
             pg.aba(model, data, q, v, x, out=bad)
     with pytest.raises(ValueError):
         pg.computeABADerivatives(model, data, q, v, x, out=(mat(),))
+
+
+def test_copy_async_round_trip():
+    """copyAsync (gb_memcpy_async): pinned host -> device -> pinned host on the current stream,
+    the same bytes back; size mismatches and NULL pointers are rejected."""
+    import torch
+
+    src = torch.arange(1 << 20, dtype=torch.float64).pin_memory()
+    dev = torch.empty(1 << 20, dtype=torch.float64, device="cuda")
+    back = torch.empty(1 << 20, dtype=torch.float64).pin_memory()
+    pg.copyAsync(dev, src)
+    pg.copyAsync(back, dev)
+    torch.cuda.synchronize()
+    assert torch.equal(back, src)
+    with pytest.raises(ValueError):
+        pg.copyAsync(back[:10], dev)
+    L = _capi.lib()
+    assert L.gb_memcpy_async(None, C.c_void_p(dev.data_ptr()), 8, None) == _capi.GB_ERR_INVALID_ARGUMENT
+    assert L.gb_memcpy_async(None, None, 0, None) == _capi.GB_OK
