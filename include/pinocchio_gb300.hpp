@@ -21,7 +21,9 @@
 #ifndef PINOCCHIO_GB300_HPP
 #define PINOCCHIO_GB300_HPP
 
+#include <algorithm>
 #include <cstddef>
+#include <cstring>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -285,6 +287,8 @@ class DeviceMatrix {
   size_t cap_ = 0;
 };
 
+class ConstraintSet;
+
 // The device-batched counterpart of DataTpl (multibody/data.hpp): the precision and
 // stream of the calls and the outputs the reference keeps in data, for a batch of
 // configurations.  The batch size is the number of columns of q in each call.
@@ -296,6 +300,8 @@ class Data {
   int precision;
   void* stream;
   DeviceMatrix tau, ddq, M, dtau_dq, dtau_dv, ddq_dq, ddq_dv, Minv;
+  DeviceMatrix lambda_c, prox_residuals;  // constraintDynamics: multipliers, (absolute, relative) residuals
+  std::shared_ptr<ConstraintSet> constraints;  // the models of initConstraintDynamics
 
   // a device pointer to the n x batch input x: x itself when it lives in device (or
   // managed) memory, else a copy in the input slot
@@ -409,6 +415,134 @@ void computeABADerivatives(const Model& m, Data& data, const MQ& q, const MV& v,
   out(data.ddq_dv, ddq_dv, "ddq_dv");
   out(data.Minv, dtau, "Minv");
   check_cuda(cudaStreamSynchronize(static_cast<cudaStream_t>(data.stream)), "computeABADerivatives");
+}
+
+// ---- constraintDynamics (algorithm/constrained-dynamics.hpp:90-110) ---------------------------
+// RigidConstraintModel(type, model, joint1_id, joint1_placement, joint2_id, joint2_placement,
+// reference_frame) (algorithm/contact-info.hpp:236-262) in the flattened gb_constraint_desc form:
+// placements are 12 doubles (R row-major, then t); Kp, Kd and the desired acceleration are public.
+struct RigidConstraintModel : gb_constraint_desc {
+  RigidConstraintModel(int contact_type, const Model& m, int joint1, const double* joint1_placement, int joint2,
+                       const double* joint2_placement, int frame = GB_FRAME_LOCAL)
+      : gb_constraint_desc{} {
+    (void)m;
+    type = contact_type;
+    reference_frame = frame;
+    joint1_id = joint1;
+    joint2_id = joint2;
+    for (int k = 0; k < 12; ++k) {
+      this->joint1_placement[k] = joint1_placement ? joint1_placement[k] : (k == 0 || k == 4 || k == 8 ? 1.0 : 0.0);
+      this->joint2_placement[k] = joint2_placement ? joint2_placement[k] : (k == 0 || k == 4 || k == 8 ? 1.0 : 0.0);
+    }
+  }
+  RigidConstraintModel(int contact_type, const Model& m, int joint1, const double* joint1_placement,
+                       int frame = GB_FRAME_LOCAL)
+      : RigidConstraintModel(contact_type, m, joint1, joint1_placement, 0, nullptr, frame) {}
+  int size() const { return type == GB_CONTACT_3D ? 3 : 6; }
+};
+// RigidConstraintData: after a call, this constraint's rows of data.lambda_c (its force in its frame)
+struct RigidConstraintData {
+  explicit RigidConstraintData(const RigidConstraintModel& c) : size(c.size()) {}
+  int row = 0, size = 0;
+};
+// ProximalSettings (algorithm/proximal.hpp:22-110); after a call, iter and the residuals are the
+// largest over the batch
+struct ProximalSettings {
+  ProximalSettings() = default;
+  ProximalSettings(double accuracy, double mu_, int max_iter_)
+      : absolute_accuracy(accuracy), relative_accuracy(accuracy), mu(mu_), max_iter(max_iter_) {}
+  ProximalSettings(double absolute, double relative, double mu_, int max_iter_)
+      : absolute_accuracy(absolute), relative_accuracy(relative), mu(mu_), max_iter(max_iter_) {}
+  double absolute_accuracy = 1e-12, relative_accuracy = 1e-12, mu = 0.0;
+  int max_iter = 1;
+  int iter = 0;
+  double absolute_residual = -1.0, relative_residual = -1.0;
+};
+
+// The constraint models of initConstraintDynamics on the device (gb_constraint_set), kept in Data
+class ConstraintSet {
+ public:
+  ConstraintSet(const Model& m, const std::vector<RigidConstraintModel>& cms) : descs_(cms.begin(), cms.end()) {
+    check(gb_constraint_set_create(m.get(), static_cast<int>(descs_.size()), descs_.data(), &h_));
+    check(gb_constraint_set_dims(h_, nullptr, &dim_));
+  }
+  ConstraintSet(const ConstraintSet&) = delete;
+  ConstraintSet& operator=(const ConstraintSet&) = delete;
+  ~ConstraintSet() { gb_constraint_set_destroy(h_); }
+  bool same(const std::vector<RigidConstraintModel>& cms) const {
+    if (cms.size() != descs_.size()) return false;
+    for (size_t k = 0; k < cms.size(); ++k)
+      if (std::memcmp(static_cast<const gb_constraint_desc*>(&cms[k]), &descs_[k], sizeof(gb_constraint_desc)) != 0)
+        return false;
+    return true;
+  }
+  const gb_constraint_set* get() const { return h_; }
+  int dim() const { return dim_; }
+
+ private:
+  std::vector<gb_constraint_desc> descs_;
+  gb_constraint_set* h_ = nullptr;
+  int dim_ = 0;
+};
+
+// initConstraintDynamics(model, data, contact_models) (constrained-dynamics.hxx:21-60)
+inline void initConstraintDynamics(const Model& m, Data& data, const std::vector<RigidConstraintModel>& cms) {
+  data.constraints.reset(new ConstraintSet(m, cms));
+}
+
+// ddq = constraintDynamics(model, data, q, v, tau, contact_models, contact_datas, settings) of every
+// column: data.ddq (nv x batch), data.lambda_c (constraint_dim x batch); contact_datas[k] gets its
+// rows; settings.iter and the residuals the largest over the batch (this reads them back: the call
+// synchronises data.stream).
+template <class MQ, class MV, class MT>
+const DeviceMatrix& constraintDynamics(const Model& m, Data& data, const MQ& q, const MV& v, const MT& tau,
+                                       const std::vector<RigidConstraintModel>& contact_models,
+                                       std::vector<RigidConstraintData>& contact_datas, ProximalSettings& settings) {
+  if (contact_models.size() != contact_datas.size())
+    throw std::invalid_argument("The contact models and data do not have the same vector size.");
+  if (!data.constraints || !data.constraints->same(contact_models)) initConstraintDynamics(m, data, contact_models);
+  const long B = static_cast<long>(q.cols());
+  const double* Q = data.input(0, q, m.nq, B, "q");
+  const double* V = data.input(1, v, m.nv, B, "v");
+  const double* T = data.input(2, tau, m.nv, B, "tau");
+  const int nc = data.constraints->dim();
+  data.ddq.resize(m.nv, B);
+  data.lambda_c.resize(nc, B);
+  data.prox_residuals.resize(2, B);
+  std::vector<int> iters(static_cast<size_t>(B > 0 ? B : 1));
+  int* d_iters = nullptr;
+  check_cuda(cudaMalloc(&d_iters, sizeof(int) * iters.size()), "constraintDynamics");
+  const gb_proximal_settings ps{settings.absolute_accuracy, settings.relative_accuracy, settings.mu, settings.max_iter};
+  const int rc = gb_constraint_dynamics(m.get(), data.precision, data.constraints->get(), &ps, GB_LAYOUT_INSTANCE, B,
+                                        Q, V, T, data.ddq.data(), nc > 0 ? data.lambda_c.data() : nullptr, d_iters,
+                                        data.prox_residuals.data(), data.stream);
+  std::vector<double> res(static_cast<size_t>(2 * (B > 0 ? B : 1)));
+  cudaError_t e = cudaSuccess;
+  if (rc == GB_OK && B > 0) {
+    e = cudaMemcpyAsync(iters.data(), d_iters, sizeof(int) * B, cudaMemcpyDeviceToHost,
+                        static_cast<cudaStream_t>(data.stream));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(res.data(), data.prox_residuals.data(), sizeof(double) * 2 * B, cudaMemcpyDeviceToHost,
+                          static_cast<cudaStream_t>(data.stream));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(data.stream));
+  }
+  cudaFree(d_iters);
+  check(rc);
+  check_cuda(e, "constraintDynamics");
+  settings.iter = 0;
+  settings.absolute_residual = settings.relative_residual = 0.0;
+  for (long b = 0; b < B; ++b) {
+    settings.iter = std::max(settings.iter, iters[b]);
+    settings.absolute_residual = std::max(settings.absolute_residual, res[2 * b]);
+    settings.relative_residual = std::max(settings.relative_residual, res[2 * b + 1]);
+  }
+  int row = 0;
+  for (size_t k = 0; k < contact_datas.size(); ++k) {
+    contact_datas[k].row = row;
+    contact_datas[k].size = contact_models[k].size();
+    row += contact_models[k].size();
+  }
+  return data.ddq;
 }
 
 // Throws std::runtime_error when the model's kernels recorded a numeric failure

@@ -111,6 +111,31 @@ int main() {
     for (long k = 0; k < nn * B; ++k) e5 = std::fmax(e5, std::fabs(M2.d[k] - Mup.d[k]));
     pinocchio_gb300::checkNumeric(model);
     std::printf("single_calls rnea %.3e aba %.3e ddq %.3e minv_m %.3e M %.3e\n", e1, e2, e3, e4, e5);
+
+    // constraintDynamics: no constraint gives ABA; a point contact at the chain's tip solved
+    // undamped equals the proximal iterations with mu > 0 run to convergence
+    std::vector<pinocchio_gb300::RigidConstraintModel> none;
+    std::vector<pinocchio_gb300::RigidConstraintData> none_d;
+    pinocchio_gb300::ProximalSettings ps0;
+    Mat a4(model.nv, B), c1(model.nv, B), c2(model.nv, B);
+    pinocchio_gb300::constraintDynamics(model, data, q, v, tau2, none, none_d, ps0).copyToHost(a4);
+    double e6 = 0.0;
+    for (long k = 0; k < model.nv * B; ++k) e6 = std::fmax(e6, std::fabs(a4.d[k] - a.d[k]));
+    const double tip[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0.05, 0.0, 0.1};
+    std::vector<pinocchio_gb300::RigidConstraintModel> cm{
+        pinocchio_gb300::RigidConstraintModel(GB_CONTACT_3D, model, 3, tip, GB_FRAME_LOCAL)};
+    std::vector<pinocchio_gb300::RigidConstraintData> cd{pinocchio_gb300::RigidConstraintData(cm[0])};
+    pinocchio_gb300::constraintDynamics(model, data, q, v, tau2, cm, cd, ps0).copyToHost(c1);
+    pinocchio_gb300::ProximalSettings ps1(1e-12, 1e-6, 200);
+    pinocchio_gb300::constraintDynamics(model, data, q, v, tau2, cm, cd, ps1).copyToHost(c2);
+    double e7 = 0.0, s7 = 0.0;
+    for (long k = 0; k < model.nv * B; ++k) {
+      e7 = std::fmax(e7, std::fabs(c1.d[k] - c2.d[k]));
+      s7 = std::fmax(s7, std::fabs(c1.d[k]));
+    }
+    std::printf("constraint_dynamics aba %.3e prox %.3e iter %d lambda_rows %ld\n", e6, e7 / s7, ps1.iter,
+                data.lambda_c.rows());
+    if (!(e6 < 1e-10 && e7 < 1e-6 * s7 && ps1.iter > 1 && data.lambda_c.rows() == 3 && cd[0].size == 3)) return 6;
     try {
       Mat bad(model.nq + 1, B);
       pinocchio_gb300::rnea(model, data, bad, v, a);
