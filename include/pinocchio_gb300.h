@@ -360,6 +360,22 @@ int gb_constraint_dynamics(const gb_model* model, int precision, const gb_constr
                            const double* v, const double* tau, double* ddq, double* lambda_c, int* iterations,
                            double* residuals, void* stream);
 
+/* computeConstraintDynamicsDerivatives(model, data, contact_models, contact_datas, settings, ddq_dq,
+ * ddq_dv, ddq_dtau, dlambda_dq, dlambda_dv, dlambda_dtau) (reference
+ * algorithm/constrained-dynamics-derivatives.hpp:27-100, hxx:344-1050) after constraintDynamics on the
+ * same inputs, both in one call: ddq and lambda_c as gb_constraint_dynamics, the derivatives of ddq
+ * (nv x nv, row-major per instance) and of lambda_c (constraint_dim x nv) with respect to q (in the
+ * tangent space), v and tau, following the reference's proximal recursion over each instance's
+ * iteration count; iterations may be NULL.  Constraints to the world (joint2_id = 0) without
+ * Baumgarte gains (others: GB_ERR_UNSUPPORTED); gravity without an angular part (GB_ERR_GRAVITY).
+ * The inverse-dynamics derivatives at ddq use the precision's sweeps, the rest is FP64. */
+int gb_constraint_dynamics_derivatives(const gb_model* model, int precision, const gb_constraint_set* set,
+                                       const gb_proximal_settings* settings, int layout, long batch,
+                                       const double* q, const double* v, const double* tau, double* ddq,
+                                       double* lambda_c, double* ddq_dq, double* ddq_dv, double* ddq_dtau,
+                                       double* dlambda_dq, double* dlambda_dv, double* dlambda_dtau,
+                                       int* iterations, void* stream);
+
 /* forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272):
  * per instance, for every joint i = 0 .. njoints-1 (joint 0 the universe:
  * identity, zero), oMi[12 i ..] = the world placement (rotation row-major, then

@@ -2226,4 +2226,338 @@ ProximalResult constraint_dynamics(const Model& m, Data<T>& d, const T* q, const
   return res;
 }
 
+// ---------------------------------------------------------------------------
+// computeConstraintDynamicsDerivatives for constraints to the world (joint2 = 0) without Baumgarte
+// gains (algorithm/constrained-dynamics-derivatives.hxx:344-1050): the inverse dynamics
+// derivatives at (q, v, ddq) with the contact forces as forces on the contact joints
+// (ContactForceContribution, hxx:225-342), the contact frames' acceleration derivatives
+// (getFrameAccelerationDerivatives, frames-derivatives.hxx:85-176, on
+// JointAccelerationDerivativesBackwardStep, kinematics-derivatives.hxx:285-440; for point
+// contacts getPointClassicAccelerationDerivatives, kinematics-derivatives.hxx:700-940), and the
+// assembly with the operational-space inertia and the proximal recursion (hxx:815-1045).
+// Outputs nv x nv (ddq_dq, ddq_dv, ddq_dtau) and nc x nv (dlambda_dq, dlambda_dv, dlambda_dtau),
+// row-major.
+// ---------------------------------------------------------------------------
+template <class T>
+void translate_motion(const T* p, Vec6<T>& m) {  // linear -= p x angular
+  T w[3];
+  cross3(p, m.v + 3, w);
+  for (int k = 0; k < 3; ++k) m.v[k] -= w[k];
+}
+
+// rows 0..5 of a 6 x nv column-major set written column by column: o[6 * col + r]
+template <class T>
+void frame_acceleration_derivatives(const Model& m, const Data<T>& d, int joint, const SE3<T>& P, int rf,
+                                    std::vector<T>& v_dq, std::vector<T>& a_dq, std::vector<T>& a_dv,
+                                    std::vector<T>& a_da) {
+  const int nv = m.nv;
+  for (auto* x : {&v_dq, &a_dq, &a_dv, &a_da}) x->assign(6 * (size_t)nv, T(0));
+  const SE3<T>& oMl = d.oMi[joint];
+  const Vec6<T>& alast = d.oa[joint];
+  for (int i = joint; i > 0; i = m.parents[i]) {  // JointAccelerationDerivativesBackwardStep
+    const int p = m.parents[i];
+    for (int k = 0; k < m.nvs[i]; ++k) {
+      const int c = m.idx_v[i] + k;
+      const Vec6<T> Jc = col6(d.J, c), dJc = col6(d.dJ, c);
+      Vec6<T> da, vdq = zero6<T>(), adq = zero6<T>(), adv;
+      if (rf == RF_LOCAL) {
+        da = actinv_motion(oMl, Jc);
+        Vec6<T> vtmp = zero6<T>();
+        if (p > 0) {
+          vtmp = actinv_motion(oMl, d.ov[p]);
+          vdq = cross_motion(vtmp, da);
+        }
+        for (int r = 0; r < 6; ++r) vtmp.v[r] -= d.v[joint].v[r];
+        adv = add6(cross_motion(vtmp, da), actinv_motion(oMl, dJc));
+        if (p > 0) adq = add6(cross_motion(actinv_motion(oMl, d.oa[p]), da), cross_motion(vtmp, vdq));
+      } else {
+        da = Jc;
+        translate_motion(oMl.t, da);
+        Vec6<T> vtmp, atmp;
+        for (int r = 0; r < 6; ++r) {
+          vtmp.v[r] = (p > 0 ? d.ov[p].v[r] : T(0)) - d.ov[joint].v[r];
+          atmp.v[r] = (p > 0 ? d.oa[p].v[r] : T(0)) - alast.v[r];
+        }
+        T w[3];
+        cross3(vtmp.v + 3, oMl.t, w);
+        for (int r = 0; r < 3; ++r) vtmp.v[r] += w[r];
+        cross3(atmp.v + 3, oMl.t, w);
+        for (int r = 0; r < 3; ++r) atmp.v[r] += w[r];
+        vdq = cross_motion(vtmp, da);
+        adv = dJc;
+        translate_motion(oMl.t, adv);
+        adq = cross_motion(atmp, da);
+        if (p > 0) adq = add6(adq, cross_motion(vtmp, adv));
+        adv = add6(adv, vdq);
+      }
+      set_col6(v_dq, c, vdq);
+      set_col6(a_dq, c, adq);
+      set_col6(a_dv, c, adv);
+      set_col6(a_da, c, da);
+    }
+  }
+  // getFrameAccelerationDerivatives' frame transform (frames-derivatives.hxx:137-172)
+  T trans[3];
+  matvec(oMl.R, P.t, trans);
+  for (int i = joint; i > 0; i = m.parents[i])
+    for (int k = 0; k < m.nvs[i]; ++k) {
+      const int c = m.idx_v[i] + k;
+      for (auto* x : {&v_dq, &a_dq, &a_dv, &a_da}) {
+        Vec6<T> col = col6(*x, c);
+        if (rf == RF_LOCAL_WORLD_ALIGNED) translate_motion(trans, col);
+        else col = actinv_motion(P, col);
+        set_col6(*x, c, col);
+      }
+    }
+}
+
+// PointClassicAccelerationDerivativesBackwardStep over the support of `joint`; 3 x nv outputs
+// (o[3 * col + r])
+template <class T>
+void point_acceleration_derivatives(const Model& m, const Data<T>& d, int joint, const SE3<T>& P, int rf,
+                                    std::vector<T>& v_dq, std::vector<T>& a_dq, std::vector<T>& a_dv,
+                                    std::vector<T>& a_da) {
+  const int nv = m.nv;
+  for (auto* x : {&v_dq, &a_dq, &a_dv, &a_da}) x->assign(3 * (size_t)nv, T(0));
+  const SE3<T> oMp = se3_mul(d.oMi[joint], P);
+  const Vec6<T> vl = actinv_motion(oMp, d.ov[joint]);
+  const Vec6<T> al = actinv_motion(oMp, d.oa[joint]);
+  T pacc[3];
+  cross3(vl.v + 3, vl.v, pacc);
+  for (int r = 0; r < 3; ++r) pacc[r] += al.v[r];
+  auto put = [&](std::vector<T>& x, int c, const T* v3) {
+    for (int r = 0; r < 3; ++r) x[3 * (size_t)c + r] = v3[r];
+  };
+  for (int i = joint; i > 0; i = m.parents[i]) {
+    const int p = m.parents[i];
+    for (int k = 0; k < m.nvs[i]; ++k) {
+      const int c = m.idx_v[i] + k;
+      const Vec6<T> Jc = col6(d.J, c), dJc = col6(d.dJ, c);
+      const Vec6<T> sda = actinv_motion(oMp, Jc);
+      Vec6<T> svdq = zero6<T>(), vtmp = zero6<T>();
+      T vdq[3] = {T(0), T(0), T(0)}, adq[3] = {T(0), T(0), T(0)}, adv[3], t1[3], t2[3];
+      if (p > 0) {
+        vtmp = actinv_motion(oMp, d.ov[p]);
+        svdq = cross_motion(vtmp, sda);
+        for (int r = 0; r < 3; ++r) vdq[r] = svdq.v[r];
+      }
+      for (int r = 0; r < 6; ++r) vtmp.v[r] -= vl.v[r];
+      cross3(vtmp.v + 3, sda.v, t1);
+      cross3(vtmp.v, sda.v + 3, t2);
+      for (int r = 0; r < 3; ++r) adv[r] = t1[r] + t2[r];
+      T dl[3], wxt[3];
+      cross3(dJc.v + 3, oMp.t, wxt);
+      for (int r = 0; r < 3; ++r) dl[r] = dJc.v[r] + wxt[r];
+      matTvec(oMp.R, dl, t1);
+      for (int r = 0; r < 3; ++r) adv[r] += t1[r];
+      cross3(vl.v + 3, sda.v, t1);
+      cross3(vl.v, sda.v + 3, t2);
+      for (int r = 0; r < 3; ++r) adv[r] += t1[r] - t2[r];
+      if (p > 0) {
+        const Vec6<T> atmp = actinv_motion(oMp, d.oa[p]);
+        cross3(atmp.v + 3, sda.v, t1);
+        cross3(atmp.v, sda.v + 3, t2);
+        for (int r = 0; r < 3; ++r) adq[r] = t1[r] + t2[r];
+        cross3(vtmp.v + 3, svdq.v, t1);
+        cross3(vtmp.v, svdq.v + 3, t2);
+        for (int r = 0; r < 3; ++r) adq[r] += t1[r] + t2[r];
+        cross3(vl.v + 3, svdq.v, t1);
+        cross3(vl.v, svdq.v + 3, t2);
+        for (int r = 0; r < 3; ++r) adq[r] += t1[r] - t2[r];
+      }
+      T ada[3] = {sda.v[0], sda.v[1], sda.v[2]};
+      if (rf == RF_LOCAL_WORLD_ALIGNED) {
+        T x[3], y[3];
+        cross3(sda.v + 3, vl.v, x);
+        for (int r = 0; r < 3; ++r) x[r] += vdq[r];
+        matvec(oMp.R, x, vdq);
+        cross3(sda.v + 3, pacc, x);
+        for (int r = 0; r < 3; ++r) x[r] += adq[r];
+        matvec(oMp.R, x, adq);
+        matvec(oMp.R, adv, y);
+        for (int r = 0; r < 3; ++r) adv[r] = y[r];
+        matvec(oMp.R, ada, y);
+        for (int r = 0; r < 3; ++r) ada[r] = y[r];
+      }
+      put(v_dq, c, vdq);
+      put(a_dq, c, adq);
+      put(a_dv, c, adv);
+      put(a_da, c, ada);
+    }
+  }
+}
+
+template <class T>
+ProximalResult constraint_dynamics_derivatives(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau,
+                                               const std::vector<ConstraintModel>& cms, T mu, int max_iter,
+                                               T abs_acc, T rel_acc, T* ddq, T* lambda, T* ddq_dq, T* ddq_dv,
+                                               T* ddq_dtau, T* dl_dq, T* dl_dv, T* dl_dtau) {
+  for (const auto& c : cms) {
+    bool gains = false;
+    for (int k = 0; k < 6; ++k) gains = gains || c.Kp[k] != 0.0 || c.Kd[k] != 0.0;
+    if (c.joint2 != 0 || gains)
+      throw std::invalid_argument("the derivatives take constraints to the world without Baumgarte gains");
+  }
+  const int nv = m.nv;
+  const ProximalResult res = constraint_dynamics(m, d, q, v, tau, cms, mu, max_iter, abs_acc, rel_acc, ddq, lambda);
+  int nc = 0;
+  for (const auto& c : cms) nc += c.size();
+  // the contact forces as forces on the contact joints, in their frames (fext of rnea_derivatives):
+  // ContactForceContribution subtracts them from of[joint1] in the world frame
+  std::vector<T> fext(6 * (size_t)m.njoints, T(0));
+  std::vector<SE3<T>> oMc(cms.size());
+  int row = 0;
+  for (size_t e = 0; e < cms.size(); ++e) {
+    const ConstraintModel& c = cms[e];
+    const SE3<T> P = se3_from<T>(c.P1);
+    oMc[e] = se3_mul(d.oMi[c.joint1], P);
+    Vec6<T> f = zero6<T>();
+    for (int k = 0; k < c.size(); ++k) f.v[k] = lambda[row + k];
+    Vec6<T> fj;
+    if (c.frame == RF_LOCAL) {
+      fj = act_force(P, f);
+    } else {  // world-aligned force at the contact point -> world force about the origin -> joint frame
+      Vec6<T> fw = f;
+      T w[3];
+      cross3(oMc[e].t, f.v, w);
+      for (int r = 0; r < 3; ++r) fw.v[3 + r] += w[r];
+      const SE3<T>& oMi = d.oMi[c.joint1];
+      // oMi^-1 . act(force): linear R^T f, angular R^T (n - t x f)
+      T fl[3], tmp[3], nn[3];
+      matTvec(oMi.R, fw.v, fl);
+      cross3(oMi.t, fw.v, tmp);
+      for (int r = 0; r < 3; ++r) nn[r] = fw.v[3 + r] - tmp[r];
+      matTvec(oMi.R, nn, fj.v + 3);
+      for (int r = 0; r < 3; ++r) fj.v[r] = fl[r];
+    }
+    for (int k = 0; k < 6; ++k) fext[6 * (size_t)c.joint1 + k] += fj.v[k];
+    row += c.size();
+  }
+  rnea_derivatives(m, d, q, v, ddq, fext.data());  // J, dJ, ov, oa at ddq; dtau_dq, dtau_dv
+  std::vector<T> dtq(d.dtau_dq), dtv(d.dtau_dv);
+  // M^-1 (the KKT factor's bottom-right block: M with the armature)
+  crba(m, d, q, LOCAL);
+  std::fill(d.U.begin(), d.U.end(), T(0));
+  for (int k = 0; k < nv; ++k) d.U[(size_t)k * nv + k] = T(1);
+  cholesky_decompose(m, d);
+  std::vector<T> Minv((size_t)nv * nv);
+  for (int c = 0; c < nv; ++c) {
+    std::vector<T> col(nv, T(0));
+    col[c] = T(1);
+    chol_solve(m, d, col.data());
+    for (int r = 0; r < nv; ++r) Minv[(size_t)r * nv + c] = col[r];
+  }
+  // the contact rows: dac_da (= the constraint Jacobian), dac_dq, dac_dv
+  std::vector<T> Jc((size_t)nc * nv, T(0)), Aq((size_t)nc * nv, T(0)), Av((size_t)nc * nv, T(0));
+  row = 0;
+  std::vector<T> vdq, adq, adv, ada;
+  for (size_t e = 0; e < cms.size(); ++e) {
+    const ConstraintModel& c = cms[e];
+    const SE3<T> P = se3_from<T>(c.P1);
+    const int n = c.size();
+    if (c.type == CONTACT_6D) frame_acceleration_derivatives(m, d, c.joint1, P, c.frame, vdq, adq, adv, ada);
+    else point_acceleration_derivatives(m, d, c.joint1, P, c.frame, vdq, adq, adv, ada);
+    const int stride = c.type == CONTACT_6D ? 6 : 3;
+    for (int k = 0; k < n; ++k)
+      for (int col = 0; col < nv; ++col) {
+        Jc[(size_t)(row + k) * nv + col] = ada[(size_t)stride * col + k];
+        Aq[(size_t)(row + k) * nv + col] = adq[(size_t)stride * col + k];
+        Av[(size_t)(row + k) * nv + col] = adv[(size_t)stride * col + k];
+      }
+    row += n;
+  }
+  // JMinv, osim = (J M^-1 J^T + mu I)^-1
+  std::vector<T> JMinv((size_t)nc * nv, T(0)), G((size_t)nc * nc), osim((size_t)nc * nc);
+  for (int r = 0; r < nc; ++r)
+    for (int c = 0; c < nv; ++c) {
+      T s = T(0);
+      for (int k = 0; k < nv; ++k) s += Jc[(size_t)r * nv + k] * Minv[(size_t)k * nv + c];
+      JMinv[(size_t)r * nv + c] = s;
+    }
+  for (int r = 0; r < nc; ++r)
+    for (int c = 0; c < nc; ++c) {
+      T s = T(0);
+      for (int k = 0; k < nv; ++k) s += JMinv[(size_t)r * nv + k] * Jc[(size_t)c * nv + k];
+      G[(size_t)r * nc + c] = s + (r == c ? mu : T(0));
+    }
+  for (int c = 0; c < nc; ++c) {
+    std::vector<T> Gc(G), e(nc, T(0));
+    e[c] = T(1);
+    llt_factor_solve(nc, Gc.data(), e.data());
+    for (int r = 0; r < nc; ++r) osim[(size_t)r * nc + c] = e[r];
+  }
+  // the proximal recursion of a right-hand side R (nc x nv): X_1 = -osim R, X_k = osim (mu X_{k-1} - R)
+  auto prox = [&](const std::vector<T>& R, T* X) {
+    std::vector<T> prev((size_t)nc * nv), t((size_t)nc * nv);
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nv; ++c) {
+        T s = T(0);
+        for (int k = 0; k < nc; ++k) s += osim[(size_t)r * nc + k] * R[(size_t)k * nv + c];
+        X[(size_t)r * nv + c] = -s;
+      }
+    for (int it = 1; it < res.iter; ++it) {
+      for (size_t k = 0; k < prev.size(); ++k) t[k] = mu * X[k] - R[k];
+      for (int r = 0; r < nc; ++r)
+        for (int c = 0; c < nv; ++c) {
+          T s = T(0);
+          for (int k = 0; k < nc; ++k) s += osim[(size_t)r * nc + k] * t[(size_t)k * nv + c];
+          X[(size_t)r * nv + c] = s;
+        }
+    }
+  };
+  prox(JMinv, dl_dtau);
+  for (int r = 0; r < nv; ++r)  // ddq_dtau = M^-1 + JMinv^T dl_dtau
+    for (int c = 0; c < nv; ++c) {
+      T s = Minv[(size_t)r * nv + c];
+      for (int k = 0; k < nc; ++k) s += JMinv[(size_t)k * nv + r] * dl_dtau[(size_t)k * nv + c];
+      ddq_dtau[(size_t)r * nv + c] = s;
+    }
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<T>& dt = pass == 0 ? dtq : dtv;
+    const std::vector<T>& A = pass == 0 ? Aq : Av;
+    T* dl = pass == 0 ? dl_dq : dl_dv;
+    T* out = pass == 0 ? ddq_dq : ddq_dv;
+    std::vector<T> R((size_t)nc * nv);
+    for (int r = 0; r < nc; ++r)  // R = dac_dx - JMinv dtau_dx
+      for (int c = 0; c < nv; ++c) {
+        T s = T(0);
+        for (int k = 0; k < nv; ++k) s += JMinv[(size_t)r * nv + k] * dt[(size_t)k * nv + c];
+        R[(size_t)r * nv + c] = A[(size_t)r * nv + c] - s;
+      }
+    prox(R, dl);
+    for (int r = 0; r < nv; ++r)  // dtau_dx -= J^T dl_dx
+      for (int c = 0; c < nv; ++c) {
+        T s = T(0);
+        for (int k = 0; k < nc; ++k) s += Jc[(size_t)k * nv + r] * dl[(size_t)k * nv + c];
+        dt[(size_t)r * nv + c] -= s;
+      }
+    for (int r = 0; r < nv; ++r)  // ddq_dx = -M^-1 dtau_dx
+      for (int c = 0; c < nv; ++c) {
+        T s = T(0);
+        for (int k = 0; k < nv; ++k) s += Minv[(size_t)r * nv + k] * dt[(size_t)k * nv + c];
+        out[(size_t)r * nv + c] = -s;
+      }
+  }
+  // world-aligned contacts: the force rotates with nothing (hxx:1000-1040)
+  row = 0;
+  for (size_t e = 0; e < cms.size(); ++e) {
+    const ConstraintModel& c = cms[e];
+    if (c.frame == RF_LOCAL_WORLD_ALIGNED) {
+      const int colRef = m.idx_v[c.joint1] + m.nvs[c.joint1] - 1;
+      for (int j = colRef; j >= 0; j = m.parents_fromRow[j]) {
+        const Vec6<T> J = col6(d.J, j);
+        T w[3];
+        cross3(J.v + 3, lambda + row, w);
+        for (int r = 0; r < 3; ++r) dl_dq[(size_t)(row + r) * nv + j] += w[r];
+        if (c.type == CONTACT_6D) {
+          cross3(J.v + 3, lambda + row + 3, w);
+          for (int r = 0; r < 3; ++r) dl_dq[(size_t)(row + 3 + r) * nv + j] += w[r];
+        }
+      }
+    }
+    row += c.size();
+  }
+  return res;
+}
+
 }  // namespace orc

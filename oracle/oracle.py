@@ -60,6 +60,8 @@ def lib():
         L.orc_kkt_inverse.argtypes = [vp, C.c_long, C.c_int, vp, vp, C.c_double, vp]
         L.orc_constraint_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, C.c_double, C.c_int,
                                               C.c_double, C.c_double, vp, vp, vp, vp, C.c_int]
+        L.orc_constraint_dynamics_derivatives.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, C.c_double,
+                                                          C.c_int, C.c_double, C.c_double] + [vp] * 9 + [C.c_int]
         L.orc_impulse_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
@@ -221,6 +223,25 @@ class OracleModel:
                                                   float(relative_accuracy), _ptr(ddq), _ptr(lam), _ptr(iters),
                                                   _ptr(res), nthreads))
         return ddq, lam, iters, res
+
+    def constraint_dynamics_derivatives(self, q, v, tau, desc, mu=0.0, max_iter=1, absolute_accuracy=1e-12,
+                                        relative_accuracy=1e-12, prec=0, nthreads=0):
+        """computeConstraintDynamicsDerivatives (reference algorithm/constrained-dynamics-derivatives.hxx:
+        344-1050) for constraints to the world without Baumgarte gains.  Returns (ddq, lambda_c, ddq_dq,
+        ddq_dv, ddq_dtau (B, nv, nv), dlambda_dq, dlambda_dv, dlambda_dtau (B, nc, nv), iterations)."""
+        q, v, tau = _c(q), _c(v), _c(tau)
+        desc = _c(np.asarray(desc).reshape(-1, 46))
+        B, nv = q.shape[0], self.nv
+        nc = int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
+        ddq, lam = np.empty((B, nv)), np.empty((B, nc))
+        a = [np.empty((B, nv, nv)) for _ in range(3)]
+        lm = [np.empty((B, nc, nv)) for _ in range(3)]
+        iters = np.empty(B, dtype=np.int32)
+        self._check(lib().orc_constraint_dynamics_derivatives(
+            self.h, prec, B, len(desc), _ptr(desc), _ptr(q), _ptr(v), _ptr(tau), float(mu), int(max_iter),
+            float(absolute_accuracy), float(relative_accuracy), _ptr(ddq), _ptr(lam), *(_ptr(x) for x in a),
+            *(_ptr(x) for x in lm), _ptr(iters), nthreads))
+        return (ddq, lam, *a, *lm, iters)
 
     def impulse_dynamics(self, q, v_before, J, r_coeff=0.0, inv_damping=0.0, prec=0, nthreads=0):
         """(dq_after, impulse_c) of impulseDynamics with the constraint Jacobian J (B, nc, nv)."""

@@ -461,3 +461,75 @@ extern "C" int orc_constraint_dynamics(void* h, int prec, long B, int ncontacts,
     return 1;
   }
 }
+
+namespace {
+template <class T>
+int constraint_derivs_batch(const Model& m, long B, const std::vector<orc::ConstraintModel>& cms, const double* q,
+                            const double* v, const double* tau, double mu, int max_iter, double abs_acc,
+                            double rel_acc, double* ddq, double* lam, double* ddq_dq, double* ddq_dv,
+                            double* ddq_dtau, double* dl_dq, double* dl_dv, double* dl_dtau, int* iters,
+                            int nthreads) {
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  omp_set_dynamic(0);
+  omp_set_num_threads(nthreads);
+  std::vector<std::unique_ptr<orc::Data<T>>> datas(nthreads);
+  for (int t = 0; t < nthreads; ++t) datas[t].reset(new orc::Data<T>(m));
+  int nc = 0;
+  for (const auto& c : cms) nc += c.size();
+  const int nq = m.nq, nv = m.nv;
+  const size_t nn = (size_t)nv * nv, cn = (size_t)nc * nv;
+  std::string err;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < B; ++b) {
+    orc::Data<T>& d = *datas[omp_get_thread_num()];
+    Buf<T> bq, bv, bt;
+    bq.load(q + (size_t)b * nq, nq);
+    bv.load(v + (size_t)b * nv, nv);
+    bt.load(tau + (size_t)b * nv, nv);
+    std::vector<T> o(nv), l(nc), a1(nn), a2(nn), a3(nn), l1(cn), l2(cn), l3(cn);
+    try {
+      const orc::ProximalResult r = orc::constraint_dynamics_derivatives(
+          m, d, bq.x.data(), bv.x.data(), bt.x.data(), cms, T(mu), max_iter, T(abs_acc), T(rel_acc), o.data(),
+          l.data(), a1.data(), a2.data(), a3.data(), l1.data(), l2.data(), l3.data());
+      if (iters) iters[b] = r.iter;
+    } catch (const std::exception& e) {
+#pragma omp critical
+      err = e.what();
+      continue;
+    }
+    store(o, ddq + (size_t)b * nv, nv);
+    store(l, lam + (size_t)b * nc, nc);
+    store(a1, ddq_dq + b * nn, nn);
+    store(a2, ddq_dv + b * nn, nn);
+    store(a3, ddq_dtau + b * nn, nn);
+    store(l1, dl_dq + b * cn, cn);
+    store(l2, dl_dv + b * cn, cn);
+    store(l3, dl_dtau + b * cn, cn);
+  }
+  if (!err.empty()) throw std::invalid_argument(err);
+  return 0;
+}
+}  // namespace
+// computeConstraintDynamicsDerivatives (algorithm/constrained-dynamics-derivatives.hxx:344-1050) for
+// constraints to the world without Baumgarte gains: per instance ddq, lambda_c, ddq_dq, ddq_dv,
+// ddq_dtau (nv x nv), dlambda_dq, dlambda_dv, dlambda_dtau (nc x nv), row-major, and the iterations.
+extern "C" int orc_constraint_dynamics_derivatives(void* h, int prec, long B, int ncontacts, const double* desc,
+                                                   const double* q, const double* v, const double* tau, double mu,
+                                                   int max_iter, double abs_acc, double rel_acc, double* ddq,
+                                                   double* lambda_c, double* ddq_dq, double* ddq_dv, double* ddq_dtau,
+                                                   double* dl_dq, double* dl_dv, double* dl_dtau, int* iters, int nt) {
+  const Model& m = *static_cast<Model*>(h);
+  try {
+    const std::vector<orc::ConstraintModel> cms = constraint_models(m, ncontacts, desc);
+    if (max_iter < 1 || !(mu >= 0.0)) throw std::invalid_argument("max_iter must be >= 1 and mu >= 0");
+    return prec == 1 ? constraint_derivs_batch<long double>(m, B, cms, q, v, tau, mu, max_iter, abs_acc, rel_acc, ddq,
+                                                            lambda_c, ddq_dq, ddq_dv, ddq_dtau, dl_dq, dl_dv, dl_dtau,
+                                                            iters, nt)
+                     : constraint_derivs_batch<double>(m, B, cms, q, v, tau, mu, max_iter, abs_acc, rel_acc, ddq,
+                                                       lambda_c, ddq_dq, ddq_dv, ddq_dtau, dl_dq, dl_dv, dl_dtau,
+                                                       iters, nt);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}

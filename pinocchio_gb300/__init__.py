@@ -47,6 +47,7 @@ from .api import (  # noqa: F401
     abaInParallel,
     checkNumeric,
     computeABADerivatives,
+    computeConstraintDynamicsDerivatives,
     computeGeneralizedGravity,
     computeJointJacobians,
     computeKKTContactDynamicMatrixInverse,

@@ -58,6 +58,7 @@ EXPORTS = (
     "gb_constraint_set_destroy",
     "gb_constraint_set_dims",
     "gb_constraint_dynamics",
+    "gb_constraint_dynamics_derivatives",
     "gb_forward_kinematics",
     "gb_compute_joint_jacobians",
     "gb_integrate",
@@ -198,6 +199,7 @@ def lib():
         L.gb_constraint_set_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
         L.gb_constraint_dynamics.argtypes = [vp, i, vp, C.POINTER(ProximalSettingsC), i, l, vp, vp, vp, vp, vp, vp, vp,
                                              vp]
+        L.gb_constraint_dynamics_derivatives.argtypes = [vp, i, vp, C.POINTER(ProximalSettingsC), i, l] + [vp] * 13
         L.gb_forward_kinematics.argtypes = [vp, i, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.gb_compute_joint_jacobians.argtypes = [vp, i, i, l, vp, vp, vp]
         L.gb_batch_multi.argtypes = [C.POINTER(Task), i, i, i, vp]

@@ -435,6 +435,7 @@ def constraintDynamics(model: Model, data: Data, q, v, tau, contact_models, cont
         )
     )
     data.ddq, data.lambda_c, data.constraint_iterations, data.constraint_residuals = ddq, lam, iters, res
+    data.constraint_inputs = (qt, vt, tt, settings)
     if B:
         settings.iter = int(iters.max().item())
         settings.absolute_residual = float(res[:, 0].max().item())
@@ -448,6 +449,46 @@ def constraintDynamics(model: Model, data: Data, q, v, tau, contact_models, cont
             cd.contact_force = _ret(f, was_np, vec)
             row += n
     return _ret(ddq, was_np, vec)
+
+
+def computeConstraintDynamicsDerivatives(model: Model, data: Data, contact_models, contact_datas=None, settings=None):
+    """(ddq_dq, ddq_dv, ddq_dtau, dlambda_dq, dlambda_dv, dlambda_dtau) at the inputs of the last
+    constraintDynamics call on ``data`` (reference
+    algorithm/constrained-dynamics-derivatives.hxx:344-1050, binding
+    expose-constrained-dynamics-derivatives.cpp:23-37): batched (batch, nv, nv) and
+    (batch, constraint_dim, nv) tensors, also kept in data.  Constraints to the world without
+    Baumgarte gains (others raise)."""
+    torch = _torch()
+    inputs = getattr(data, "constraint_inputs", None)
+    if inputs is None:
+        raise RuntimeError("call constraintDynamics first")
+    qt, vt, tt, last_settings = inputs
+    settings = last_settings if settings is None else settings
+    from .constraints import stack_desc
+
+    cset = data.constraint_set
+    desc = stack_desc(contact_models)
+    if cset.desc.shape != desc.shape or not np.array_equal(cset.desc, desc):
+        raise ValueError("the constraint models differ from the last constraintDynamics call")
+    B, nv, nc = qt.shape[0], model.nv, cset.nc
+    dev = qt.device
+    ddq = torch.empty((B, nv), dtype=torch.float64, device=dev)
+    lam = torch.empty((B, nc), dtype=torch.float64, device=dev)
+    mats = [torch.empty((B, nv, nv), dtype=torch.float64, device=dev) for _ in range(3)]
+    lmats = [torch.empty((B, nc, nv), dtype=torch.float64, device=dev) for _ in range(3)]
+    iters = torch.empty(B, dtype=torch.int32, device=dev)
+    ps = _capi.ProximalSettingsC(float(settings.absolute_accuracy), float(settings.relative_accuracy),
+                                 float(settings.mu), int(settings.max_iter))
+    lp = [_ptr(t) if nc else None for t in [lam] + lmats]
+    _capi.check(
+        _capi.lib().gb_constraint_dynamics_derivatives(
+            data.dev.h, _PREC[data.precision], cset.h, C.byref(ps), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt), _ptr(vt),
+            _ptr(tt), _ptr(ddq), lp[0], *(_ptr(t) for t in mats), *lp[1:], _ptr(iters), _stream_ptr(),
+        )
+    )
+    data.ddq_dq, data.ddq_dv, data.ddq_dtau = mats
+    data.dlambda_dq, data.dlambda_dv, data.dlambda_dtau = lmats
+    return tuple(mats + lmats)
 
 
 def _constraint(x, B: int, shape: tuple, name: str):

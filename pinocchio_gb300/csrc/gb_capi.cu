@@ -360,6 +360,45 @@ int gb_constraint_dynamics(const gb_model* M, int precision, const gb_constraint
                                 residuals, (cudaStream_t)stream);
 }
 
+int gb_constraint_dynamics_derivatives(const gb_model* M, int precision, const gb_constraint_set* S,
+                                       const gb_proximal_settings* settings, int layout, long B, const double* q,
+                                       const double* v, const double* tau, double* ddq, double* lambda_c,
+                                       double* ddq_dq, double* ddq_dv, double* ddq_dtau, double* dl_dq, double* dl_dv,
+                                       double* dl_dtau, int* iterations, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (!S || !settings) return set_error(GB_ERR_INVALID_ARGUMENT, "set/settings is NULL");
+  if (S->model != M) return set_error(GB_ERR_INVALID_ARGUMENT, "the constraint set belongs to another model");
+  if (!(settings->mu >= 0.0)) return set_error(GB_ERR_INVALID_ARGUMENT, "mu has to be positive");
+  if (!(settings->absolute_accuracy >= 0.0) || !(settings->relative_accuracy >= 0.0))
+    return set_error(GB_ERR_INVALID_ARGUMENT, "Accuracy must be positive.");
+  if (settings->max_iter < 1) return set_error(GB_ERR_INVALID_ARGUMENT, "max_iter must be greater or equal to 1");
+  for (const gbi::ConstraintDev& c : S->host)
+    if (c.j2 != 0 || c.gains)
+      return set_error(GB_ERR_UNSUPPORTED,
+                       "the constraint dynamics derivatives take constraints to the world (joint2_id = 0) without "
+                       "Baumgarte gains");
+  GB_TRY(gbi::check_gravity(M));
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));
+  GB_TRY(gbi::check_ptr(ddq, "ddq"));
+  GB_TRY(gbi::check_ptr(ddq_dq, "ddq_dq")); GB_TRY(gbi::check_ptr(ddq_dv, "ddq_dv"));
+  GB_TRY(gbi::check_ptr(ddq_dtau, "ddq_dtau"));
+  if (S->nc > 0) {
+    GB_TRY(gbi::check_ptr(lambda_c, "lambda_c"));
+    GB_TRY(gbi::check_ptr(dl_dq, "dlambda_dq")); GB_TRY(gbi::check_ptr(dl_dv, "dlambda_dv"));
+    GB_TRY(gbi::check_ptr(dl_dtau, "dlambda_dtau"));
+  }
+  const long nv = M->nv, nn = nv * nv, cn = (long)S->nc * nv;
+  using gbi::arr;
+  const gbi::Arr none{nullptr, 0, 0};
+  return gbi::launch_constraint_derivs(
+      M, precision, B, S, *settings, arr(q, layout, B, M->nq), arr(v, layout, B, nv), arr(tau, layout, B, nv),
+      arr(ddq, layout, B, nv), S->nc > 0 ? arr(lambda_c, layout, B, S->nc) : none, arr(ddq_dq, layout, B, nn),
+      arr(ddq_dv, layout, B, nn), arr(ddq_dtau, layout, B, nn), S->nc > 0 ? arr(dl_dq, layout, B, cn) : none,
+      S->nc > 0 ? arr(dl_dv, layout, B, cn) : none, S->nc > 0 ? arr(dl_dtau, layout, B, cn) : none, iterations,
+      (cudaStream_t)stream);
+}
+
 int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                           const double* a, double* oMi, double* vout, double* aout, void* stream) {
   GB_TRY(gbi::check_common(M, precision, layout, B));

@@ -579,6 +579,401 @@ __global__ void __launch_bounds__(kThreads)
   }
   if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
 }
+
+// ---- computeConstraintDynamicsDerivatives for constraints to the world without Baumgarte gains ----
+// (algorithm/constrained-dynamics-derivatives.hxx:344-1050).  After constraintDynamics (ddq, lambda)
+// and before the inverse dynamics derivatives: k_cd_setup, per configuration, the world kinematics
+// at ddq, per constraint its Jacobian rows (dac_da), the derivatives of its frame acceleration
+// (dac_dq, dac_dv: getFrameAccelerationDerivatives, frames-derivatives.hxx:85-176, over
+// JointAccelerationDerivativesBackwardStep, kinematics-derivatives.hxx:285-440; point constraints:
+// PointClassicAccelerationDerivativesBackwardStep, kinematics-derivatives.hxx:700-880), the force
+// derivative term of world-aligned constraints (hxx:1000-1040) and the constraint forces as forces
+// on the constraint joints (ContactForceContribution, hxx:225-342) for the inverse dynamics
+// derivatives; then k_cd_assemble (M^-1, the operational-space inertia, the proximal recursion,
+// hxx:815-990).
+
+__device__ void translate_motion(const double* p, M6d& m) {  // linear -= p x angular
+  double w[3];
+  gb::cross3(p, m.v + 3, w);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) m.v[k] -= w[k];
+}
+__device__ void cross_lin_ang(const M6d& a, const M6d& b, double* o) {  // a.ang x b.lin + a.lin x b.ang
+  double t1[3], t2[3];
+  gb::cross3(a.v + 3, b.v, t1);
+  gb::cross3(a.v, b.v + 3, t2);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) o[k] = t1[k] + t2[k];
+}
+__device__ void cross_lin_ang_minus(const M6d& a, const M6d& b, double* o) {  // a.ang x b.lin - a.lin x b.ang
+  double t1[3], t2[3];
+  gb::cross3(a.v + 3, b.v, t1);
+  gb::cross3(a.v, b.v + 3, t2);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) o[k] = t1[k] - t2[k];
+}
+
+template <int CAP>
+__global__ void __launch_bounds__(kThreads)
+    k_cd_setup(const unsigned char* blob, int bytes, long B, Arr q, Arr v, Arr ddq, Arr lam,
+               const ConstraintDev* __restrict__ tab, int ncon, int nj_user, double* Js, double* Aqs, double* Avs,
+               double* Cqs, double* Fes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int nv = m.nv;
+  const gb::In qi{q.p + b * q.is, q.es}, vi{v.p + b * v.is, v.es}, ai{ddq.p + b * ddq.is, ddq.es};
+  const gb::In li{lam.p + b * lam.is, lam.es};
+  X3d oM[CAP];
+  M6d ov[CAP], oa[CAP];
+  gb::zero(ov[0]);
+  gb::zero(oa[0]);
+  for (int i = 1; i < m.nj; ++i) {  // world placements, velocities, accelerations at ddq
+    const int p = m.parent[i];
+    X3d X;
+    gb::joint_transform(m, i, qi, X);
+    if (p > 0) gb::compose(oM[p], X, oM[i]);
+    else oM[i] = X;
+    M6d vJ, aJ, w, t;
+    gb::joint_motion(m.jtype[i], vi, m.idx_v[i], vJ);
+    gb::joint_motion(m.jtype[i], ai, m.idx_v[i], aJ);
+    gb::act_motion(oM[i], vJ, w);
+    gb::act_motion(oM[i], aJ, t);
+    M6d x;
+    gb::cross_motion(ov[p], w, x);  // ov_p x vJ (world); zero for a root joint
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      ov[i].v[k] = ov[p].v[k] + w.v[k];
+      oa[i].v[k] = oa[p].v[k] + x.v[k] + t.v[k];
+    }
+  }
+  const Col J{Js + b, B}, Aq{Aqs + b, B}, Av{Avs + b, B}, Cq{Cqs + b, B}, Fe{Fes + b, B};
+  for (int k = 0; k < 6 * nj_user; ++k) Fe[k] = 0.0;
+  for (int e = 0; e < ncon; ++e) {
+    const ConstraintDev& c = tab[e];
+    const int n = c.type == GB_CONTACT_3D ? 3 : 6, j = c.j1, row = c.row;
+    const bool local = c.frame == GB_FRAME_LOCAL;
+    for (int k = 0; k < n; ++k)
+      for (int jj = 0; jj < nv; ++jj) {
+        const long o = (long)(row + k) * nv + jj;
+        J[o] = 0.0;
+        Aq[o] = 0.0;
+        Av[o] = 0.0;
+        Cq[o] = 0.0;
+      }
+    X3d P, oMc;
+    load_se3(c.P1, P);
+    gb::compose(oM[j], P, oMc);
+    M6d f;
+    gb::zero(f);
+    for (int k = 0; k < n; ++k) f.v[k] = li[row + k];
+    // the constraint force on joint j, in the caller's frame of that joint
+    {
+      M6d fi;
+      if (local) {
+        gb::act_force(P, f, fi);
+      } else {
+        M6d fw = f;
+        double w[3], nn[3];
+        gb::cross3(oMc.t, f.v, w);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) fw.v[3 + k] += w[k];
+        gb::mtv3(oM[j].R, fw.v, fi.v);
+        gb::cross3(oM[j].t, fw.v, w);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nn[k] = fw.v[3 + k] - w[k];
+        gb::mtv3(oM[j].R, nn, fi.v + 3);
+      }
+      M6d fu = fi;
+      if (m.fix_d) {  // the caller's frame of an unaligned joint is the kernels' frame F^T
+        gb::mv3(m.fix_d + 9 * j, fi.v, fu.v);
+        gb::mv3(m.fix_d + 9 * j, fi.v + 3, fu.v + 3);
+      }
+      const int u = m.ujoint[j];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Fe[6 * u + k] += fu.v[k];
+    }
+    const X3d& oMl = oM[j];
+    M6d vloc;  // the local velocity of joint j
+    gb::actinv_motion(oMl, ov[j], vloc);
+    M6d vl, al;  // point constraints: the contact point's spatial velocity / acceleration
+    double pacc[3], trans[3];
+    gb::actinv_motion(oMc, ov[j], vl);
+    gb::actinv_motion(oMc, oa[j], al);
+    gb::cross3(vl.v + 3, vl.v, pacc);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pacc[k] += al.v[k];
+    gb::mv3(oMl.R, P.t, trans);
+    for (int i = j; i > 0; i = m.parent[i]) {
+      const int p = m.parent[i], jt = m.jtype[i];
+      for (int k = 0; k < gb::jt_nv(jt); ++k) {
+        const int col = m.idx_v[i] + k;
+        M6d Jc, dJc;
+        gb::world_axis_column(oM[i], gb::jt_col(jt, k), Jc.v);
+        gb::cross_motion(ov[i], Jc, dJc);
+        double rj[6], rq[6], rv[6];
+        if (n == 6) {
+          M6d da, vdq, adq, adv;
+          gb::zero(vdq);
+          gb::zero(adq);
+          if (local) {
+            M6d vtmp, t;
+            gb::actinv_motion(oMl, Jc, da);
+            gb::zero(vtmp);
+            if (p > 0) {
+              gb::actinv_motion(oMl, ov[p], vtmp);
+              gb::cross_motion(vtmp, da, vdq);
+            }
+#pragma unroll
+            for (int r = 0; r < 6; ++r) vtmp.v[r] -= vloc.v[r];
+            gb::cross_motion(vtmp, da, adv);
+            gb::actinv_motion(oMl, dJc, t);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) adv.v[r] += t.v[r];
+            if (p > 0) {
+              M6d atmp, x1, x2;
+              gb::actinv_motion(oMl, oa[p], atmp);
+              gb::cross_motion(atmp, da, x1);
+              gb::cross_motion(vtmp, vdq, x2);
+#pragma unroll
+              for (int r = 0; r < 6; ++r) adq.v[r] = x1.v[r] + x2.v[r];
+            }
+          } else {
+            M6d vtmp, atmp;
+            da = Jc;
+            translate_motion(oMl.t, da);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+              vtmp.v[r] = (p > 0 ? ov[p].v[r] : 0.0) - ov[j].v[r];
+              atmp.v[r] = (p > 0 ? oa[p].v[r] : 0.0) - oa[j].v[r];
+            }
+            double w[3];
+            gb::cross3(vtmp.v + 3, oMl.t, w);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) vtmp.v[r] += w[r];
+            gb::cross3(atmp.v + 3, oMl.t, w);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) atmp.v[r] += w[r];
+            gb::cross_motion(vtmp, da, vdq);
+            adv = dJc;
+            translate_motion(oMl.t, adv);
+            gb::cross_motion(atmp, da, adq);
+            if (p > 0) {
+              M6d x;
+              gb::cross_motion(vtmp, adv, x);
+#pragma unroll
+              for (int r = 0; r < 6; ++r) adq.v[r] += x.v[r];
+            }
+#pragma unroll
+            for (int r = 0; r < 6; ++r) adv.v[r] += vdq.v[r];
+          }
+          // the frame's placement in the joint (frames-derivatives.hxx:137-172)
+          M6d* mats[3] = {&da, &adq, &adv};
+          for (int t = 0; t < 3; ++t) {
+            if (local) {
+              M6d y;
+              gb::actinv_motion(P, *mats[t], y);
+              *mats[t] = y;
+            } else {
+              translate_motion(trans, *mats[t]);
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < 6; ++r) {
+            rj[r] = da.v[r];
+            rq[r] = adq.v[r];
+            rv[r] = adv.v[r];
+          }
+        } else {
+          M6d sda, svdq, vtmp;
+          gb::actinv_motion(oMc, Jc, sda);
+          gb::zero(svdq);
+          gb::zero(vtmp);
+          double vdq[3] = {0.0, 0.0, 0.0}, adq[3] = {0.0, 0.0, 0.0}, adv[3], t1[3], t2[3];
+          if (p > 0) {
+            gb::actinv_motion(oMc, ov[p], vtmp);
+            gb::cross_motion(vtmp, sda, svdq);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) vdq[r] = svdq.v[r];
+          }
+#pragma unroll
+          for (int r = 0; r < 6; ++r) vtmp.v[r] -= vl.v[r];
+          cross_lin_ang(vtmp, sda, adv);
+          double dl[3];
+          gb::cross3(dJc.v + 3, oMc.t, t1);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) dl[r] = dJc.v[r] + t1[r];
+          gb::mtv3(oMc.R, dl, t1);
+          cross_lin_ang_minus(vl, sda, t2);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) adv[r] += t1[r] + t2[r];
+          if (p > 0) {
+            M6d atmp;
+            gb::actinv_motion(oMc, oa[p], atmp);
+            cross_lin_ang(atmp, sda, adq);
+            cross_lin_ang(vtmp, svdq, t1);
+            cross_lin_ang_minus(vl, svdq, t2);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) adq[r] += t1[r] + t2[r];
+          }
+          double ada[3] = {sda.v[0], sda.v[1], sda.v[2]};
+          if (!local) {
+            double x[3], y[3];
+            gb::cross3(sda.v + 3, pacc, x);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) x[r] += adq[r];
+            gb::mv3(oMc.R, x, adq);
+            gb::mv3(oMc.R, adv, y);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) adv[r] = y[r];
+            gb::mv3(oMc.R, ada, y);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) ada[r] = y[r];
+          }
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            rj[r] = ada[r];
+            rq[r] = adq[r];
+            rv[r] = adv[r];
+          }
+        }
+        for (int r = 0; r < n; ++r) {
+          const long o = (long)(row + r) * nv + col;
+          J[o] = rj[r];
+          Aq[o] = rq[r];
+          Av[o] = rv[r];
+        }
+        if (!local) {  // world-aligned: d(force)/dq += J.ang x f (hxx:1000-1040)
+          double w[3];
+          gb::cross3(Jc.v + 3, f.v, w);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) Cq[(long)(row + r) * nv + col] = w[r];
+          if (n == 6) {
+            gb::cross3(Jc.v + 3, f.v + 3, w);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) Cq[(long)(row + 3 + r) * nv + col] = w[r];
+          }
+        }
+      }
+    }
+  }
+}
+
+// The assembly, per configuration (FP64): M^-1 from the tree factorisation, JMinv = J M^-1,
+// osim = (J M^-1 J^T + mu I)^-1, the proximal recursion X_1 = -osim R, X_k = osim (mu X_{k-1} - R)
+// over the configuration's iteration count, then (hxx:815-990)
+//   dlambda_dtau = X(JMinv), ddq_dtau = M^-1 + JMinv^T dlambda_dtau,
+//   dlambda_dx = X(dac_dx - JMinv dtau_dx), ddq_dx = -M^-1 (dtau_dx - J^T dlambda_dx)  (x = q, v),
+//   dlambda_dq += the world-aligned force term.
+__global__ void __launch_bounds__(kThreads)
+    k_cd_assemble(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
+                  const double* Js, const double* Aqs, const double* Avs, const double* Cqs, double* dtqs,
+                  double* dtvs, const int* iters, double mu, double* Mis, double* JMs, double* Gs, double* Os,
+                  double* Rs, double* Xs, double* Ts, Arr ddq_dq, Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv,
+                  Arr dl_dtau) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int nv = m.nv, it = iters[b];
+  const Col U{const_cast<double*>(Us) + b, B}, D{const_cast<double*>(Ds) + b, B};
+  const Col J{const_cast<double*>(Js) + b, B}, Aq{const_cast<double*>(Aqs) + b, B};
+  const Col Av{const_cast<double*>(Avs) + b, B}, Cq{const_cast<double*>(Cqs) + b, B};
+  const Col Mi{Mis + b, B}, JM{JMs + b, B}, G{Gs + b, B}, O{Os + b, B}, R{Rs + b, B}, X{Xs + b, B}, T{Ts + b, B};
+  for (int c = 0; c < nv; ++c) {  // M^-1, column by column
+    const Col col{Mis + b + (long)c * B, (long)nv * B};
+    for (int k = 0; k < nv; ++k) col[k] = k == c ? 1.0 : 0.0;
+    chol_solve(m, U, D, col);
+  }
+  for (int r = 0; r < nc; ++r)
+    for (int c = 0; c < nv; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < nv; ++k) s += J[(long)r * nv + k] * Mi[(long)k * nv + c];
+      JM[(long)r * nv + c] = s;
+    }
+  for (int r = 0; r < nc; ++r)
+    for (int c = 0; c <= r; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < nv; ++k) s += JM[(long)r * nv + k] * J[(long)c * nv + k];
+      G[(long)r * nc + c] = s + (r == c ? mu : 0.0);
+    }
+  for (int jc = 0; jc < nc; ++jc) {  // LLT in place (lower)
+    double s = G[(long)jc * nc + jc];
+    for (int k = 0; k < jc; ++k) s -= G[(long)jc * nc + k] * G[(long)jc * nc + k];
+    gb::check_pivot(m, s);
+    const double l = sqrt(s);
+    G[(long)jc * nc + jc] = l;
+    for (int i = jc + 1; i < nc; ++i) {
+      double t = G[(long)i * nc + jc];
+      for (int k = 0; k < jc; ++k) t -= G[(long)i * nc + k] * G[(long)jc * nc + k];
+      G[(long)i * nc + jc] = t / l;
+    }
+  }
+  for (int c = 0; c < nc; ++c) {  // osim = G^-1, column by column
+    const Col col{Os + b + (long)c * B, (long)nc * B};
+    for (int k = 0; k < nc; ++k) col[k] = k == c ? 1.0 : 0.0;
+    llt_solve(G, nc, col);
+  }
+  auto prox = [&](const Col& Rm) {  // X <- the recursion on the right-hand side Rm (nc x nv)
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nv; ++c) {
+        double s = 0.0;
+        for (int k = 0; k < nc; ++k) s += O[(long)r * nc + k] * Rm[(long)k * nv + c];
+        X[(long)r * nv + c] = -s;
+      }
+    for (int k2 = 1; k2 < it; ++k2) {
+      for (long k = 0; k < (long)nc * nv; ++k) T[k] = mu * X[k] - Rm[k];
+      for (int r = 0; r < nc; ++r)
+        for (int c = 0; c < nv; ++c) {
+          double s = 0.0;
+          for (int k = 0; k < nc; ++k) s += O[(long)r * nc + k] * T[(long)k * nv + c];
+          X[(long)r * nv + c] = s;
+        }
+    }
+  };
+  const gb::Out odt{const_cast<double*>(ddq_dtau.p) + b * ddq_dtau.is, ddq_dtau.es};
+  const gb::Out oldt{nc > 0 ? const_cast<double*>(dl_dtau.p) + b * dl_dtau.is : nullptr, dl_dtau.es};
+  prox(JM);
+  for (long k = 0; k < (long)nc * nv; ++k) oldt[k] = X[k];
+  for (int r = 0; r < nv; ++r)
+    for (int c = 0; c < nv; ++c) {
+      double s = Mi[(long)r * nv + c];
+      for (int k = 0; k < nc; ++k) s += JM[(long)k * nv + r] * X[(long)k * nv + c];
+      odt[(long)r * nv + c] = s;
+    }
+  for (int pass = 0; pass < 2; ++pass) {
+    const Col dt{(pass == 0 ? dtqs : dtvs) + b, B};
+    const Col& A = pass == 0 ? Aq : Av;
+    const Arr& od = pass == 0 ? ddq_dq : ddq_dv;
+    const Arr& ol = pass == 0 ? dl_dq : dl_dv;
+    const gb::Out o{const_cast<double*>(od.p) + b * od.is, od.es};
+    const gb::Out l{nc > 0 ? const_cast<double*>(ol.p) + b * ol.is : nullptr, ol.es};
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nv; ++c) {
+        double s = 0.0;
+        for (int k = 0; k < nv; ++k) s += JM[(long)r * nv + k] * dt[(long)k * nv + c];
+        R[(long)r * nv + c] = A[(long)r * nv + c] - s;
+      }
+    prox(R);
+    for (int r = 0; r < nv; ++r)
+      for (int c = 0; c < nv; ++c) {
+        double s = 0.0;
+        for (int k = 0; k < nc; ++k) s += J[(long)k * nv + r] * X[(long)k * nv + c];
+        dt[(long)r * nv + c] -= s;
+      }
+    bool finite = true;
+    for (int r = 0; r < nv; ++r)
+      for (int c = 0; c < nv; ++c) {
+        double s = 0.0;
+        for (int k = 0; k < nv; ++k) s += Mi[(long)r * nv + k] * dt[(long)k * nv + c];
+        finite = finite && gb::finite_value(s);
+        o[(long)r * nv + c] = -s;
+      }
+    if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
+    for (long k = 0; k < (long)nc * nv; ++k) l[k] = X[k] + (pass == 0 ? Cq[k] : 0.0);
+  }
+}
 }  // namespace
 
 int launch_contact(const gb_model* M, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
@@ -676,6 +1071,71 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
                                                                         ddq, lam, iters, residuals);
     rc = cuda_error(cudaGetLastError(), "k_constraint_solve");
   }
+  scratch_free(scratch, st);
+  return rc;
+}
+
+int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_constraint_set* set,
+                             const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, Arr ddq_dq,
+                             Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv, Arr dl_dtau, int* iters_out,
+                             cudaStream_t st) {
+  const long nv = M->nv, nn = nv * nv, nc = set->nc, cn = nc * nv, nju = M->nj_user;
+  // scratch, [element][configuration]: M, U, M^-1, dtau_dq, dtau_dv, dM (nn); D (nv); J, dac_dq, dac_dv,
+  // the force term, JMinv, R, X, tmp (nc * nv each); G, osim (nc * nc); fext (6 per caller joint);
+  // and the iteration counts (ints)
+  const size_t doubles = (size_t)B * (6 * nn + nv + 8 * cn + 2 * nc * nc + 6 * nju);
+  void* scratch = nullptr;
+  int rc = scratch_alloc(&scratch, sizeof(double) * doubles + sizeof(int) * (size_t)B + 256, st);
+  if (rc != GB_OK) return rc;
+  double* base = static_cast<double*>(scratch);
+  double *Ms = base, *Us = Ms + nn * B, *Mis = Us + nn * B, *dtq = Mis + nn * B, *dtv = dtq + nn * B,
+         *dMs = dtv + nn * B, *Ds = dMs + nn * B, *Js = Ds + nv * B, *Aq = Js + cn * B, *Av = Aq + cn * B,
+         *Cq = Av + cn * B, *JMs = Cq + cn * B, *Rs = JMs + cn * B, *Xs = Rs + cn * B, *Ts = Xs + cn * B,
+         *Gs = Ts + cn * B, *Os = Gs + nc * nc * B, *Fe = Os + nc * nc * B;
+  int* its = reinterpret_cast<int*>(base + doubles);
+  rc = launch_constraint(M, precision, B, set, s, q, v, tau, ddq, lam, its, nullptr, st);
+  if (rc == GB_OK) rc = launch_crba(M, GB_FP64, false, B, q, Arr{Ms, 1, B}, Arr{Us, 1, B}, Arr{Ds, 1, B}, st);
+  const long grid = (B + kThreads - 1) / kThreads;
+  auto opt_in = [&](const void* kern, const char* name) -> int {
+    if (M->stage_bytes <= 48 * 1024) return GB_OK;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M->stage_bytes);
+    return e == cudaSuccess ? GB_OK : cuda_error(e, name);
+  };
+  const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
+  if (rc == GB_OK && set->n > 0) {
+    switch (M->cap) {
+#define GB_CD_SETUP(C)                                                                                       \
+  case C:                                                                                                    \
+    rc = opt_in((const void*)k_cd_setup<C>, "k_cd_setup");                                                   \
+    if (rc == GB_OK)                                                                                         \
+      k_cd_setup<C><<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, q, v, ddq, lam, \
+                                                                       tab, set->n, (int)nju, Js, Aq, Av, Cq, Fe); \
+    break;
+      GB_CD_SETUP(8)
+      GB_CD_SETUP(16)
+      GB_CD_SETUP(32)
+      GB_CD_SETUP(64)
+      GB_CD_SETUP(128)
+#undef GB_CD_SETUP
+      default:
+        rc = set_error(GB_ERR_UNSUPPORTED, "model too large");
+    }
+    if (rc == GB_OK) rc = cuda_error(cudaGetLastError(), "k_cd_setup");
+  } else if (rc == GB_OK) {
+    rc = cuda_error(cudaMemsetAsync(Fe, 0, sizeof(double) * 6 * nju * B, st), "cudaMemsetAsync");
+  }
+  if (rc == GB_OK)
+    rc = launch_rnea_derivs_fext(M, precision, B, q, v, ddq, Arr{Fe, 1, B}, Arr{dtq, 1, B}, Arr{dtv, 1, B},
+                                 Arr{dMs, 1, B}, st);
+  if (rc == GB_OK) rc = opt_in((const void*)k_cd_assemble, "k_cd_assemble");
+  if (rc == GB_OK) {
+    k_cd_assemble<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(
+        M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Aq, Av, Cq, dtq, dtv, its, s.mu, Mis, JMs, Gs, Os, Rs, Xs,
+        Ts, ddq_dq, ddq_dv, ddq_dtau, dl_dq, dl_dv, dl_dtau);
+    rc = cuda_error(cudaGetLastError(), "k_cd_assemble");
+  }
+  if (rc == GB_OK && iters_out)
+    rc = cuda_error(cudaMemcpyAsync(iters_out, its, sizeof(int) * B, cudaMemcpyDefault, st), "cudaMemcpyAsync");
   scratch_free(scratch, st);
   return rc;
 }

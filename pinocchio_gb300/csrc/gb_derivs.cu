@@ -710,13 +710,13 @@ int run_aba_derivs(const gb_model* M, long B, Arr q, Arr v, Arr tau, Arr dq, Arr
 constexpr int kMixedDfDepth = 32;
 bool mixed_df(const gb_model* M) { return M->max_depth > kMixedDfDepth; }
 
+}  // namespace
+
 int check_gravity(const gb_model* M) {
   if (M->gravity[3] != 0.0 || M->gravity[4] != 0.0 || M->gravity[5] != 0.0)
     return set_error(GB_ERR_GRAVITY, "The gravity must be a pure force vector, no angular part");
   return GB_OK;
 }
-
-}  // namespace
 
 // Per-model launch preparation (at creation, on the model's device): the warp-task plan
 // of the pipelined product kernel and its shared-memory size, when the two stages fit.
@@ -797,7 +797,14 @@ int gb_pipeline_wait_selftest(unsigned int limit_us, void* stream) {
 }  // extern "C"
 
 namespace gbi {
+int launch_rnea_derivs_fext(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr fext, Arr dq, Arr dv,
+                            Arr Mo, cudaStream_t st) {
+  if (precision == GB_FP64)
+    return run_rnea_derivs<double, true>(M, B, false, q, v, a, dq, dv, Mo, Arr{nullptr, 0, 0}, st, fext);
+  return run_rnea_derivs<float, true>(M, B, false, q, v, a, dq, dv, Mo, Arr{nullptr, 0, 0}, st, fext);
+}
 namespace {
+
 int rnea_derivs_entry(const gb_model* M, int precision, int matrix_mode, int layout, long B, const double* q,
                       const double* v, const double* a, const double* fext, double* dtau_dq, double* dtau_dv,
                       double* Mo, double* tau, void* stream) {

@@ -75,6 +75,12 @@ int launch_crba(const gb_model* m, int precision, bool symmetric, long B, Arr q,
 int launch_contact(const gb_model* m, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
                    Arr gamma, double r_coeff, double inv_damping, Arr out, Arr lam, cudaStream_t st);
 int launch_kkt_inverse(const gb_model* m, long B, int nc, Arr q, Arr J, double inv_damping, Arr K, cudaStream_t st);
+int check_gravity(const gb_model* M);  // GB_ERR_GRAVITY when the gravity has an angular part
+int launch_rnea_derivs_fext(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr fext, Arr dq, Arr dv,
+                            Arr Mo, cudaStream_t st);
+int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_constraint_set* set,
+                             const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, Arr ddq_dq,
+                             Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv, Arr dl_dtau, int* iters, cudaStream_t st);
 int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
                       const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
                       double* residuals, cudaStream_t st);

@@ -254,3 +254,78 @@ def test_argument_errors(humanoid):
     assert c.joint2_id == 0 and c.reference_frame == cs.LOCAL_WORLD_ALIGNED and c.size() == 3
     c = cs.RigidConstraintModel(cs.CONTACT_6D, model, 5, gm.SE3.Identity(), 7, gm.SE3.Identity(), cs.LOCAL)
     assert (c.joint1_id, c.joint2_id) == (5, 7)
+
+
+def _central_differences(model, om, q, v, tau, desc, h=1e-6, **kw):
+    """Central differences of constraintDynamics' (ddq, lambda_c) in q (along integrate), v and tau."""
+    B, nv = q.shape[0], model.nv
+    out = []
+    for which in ("q", "v", "tau"):
+        dd = np.zeros((B, nv, nv))
+        dl = None
+        for k in range(nv):
+            e = np.zeros((B, nv))
+            e[:, k] = h
+            if which == "q":
+                args_p, args_m = (om.integrate(q, e), v, tau), (om.integrate(q, -e), v, tau)
+            elif which == "v":
+                args_p, args_m = (q, v + e, tau), (q, v - e, tau)
+            else:
+                args_p, args_m = (q, v, tau + e), (q, v, tau - e)
+            fp = om.constraint_dynamics(*args_p, desc, **kw)
+            fm = om.constraint_dynamics(*args_m, desc, **kw)
+            dd[:, :, k] = (fp[0] - fm[0]) / (2 * h)
+            if dl is None:
+                dl = np.zeros((B, fp[1].shape[1], nv))
+            dl[:, :, k] = (fp[1] - fm[1]) / (2 * h)
+        out += [dd, dl]
+    return out  # ddq_dq, dl_dq, ddq_dv, dl_dv, ddq_dtau, dl_dtau
+
+
+@pytest.mark.parametrize("kinds", [
+    [(cs.CONTACT_6D, cs.LOCAL), (cs.CONTACT_3D, cs.LOCAL)],
+    [(cs.CONTACT_6D, cs.LOCAL_WORLD_ALIGNED), (cs.CONTACT_3D, cs.LOCAL_WORLD_ALIGNED)],
+    [(cs.CONTACT_3D, cs.LOCAL), (cs.CONTACT_6D, cs.LOCAL_WORLD_ALIGNED), (cs.CONTACT_3D, cs.LOCAL_WORLD_ALIGNED),
+     (cs.CONTACT_6D, cs.LOCAL)],
+])
+def test_constraint_dynamics_derivatives_central_differences(humanoid, kinds):
+    """computeConstraintDynamicsDerivatives (constraints to the world, no gains) against central
+    differences of constraintDynamics (the check of unittest/constrained-dynamics-derivatives.cpp)."""
+    model, om = humanoid
+    rng = np.random.default_rng(21)
+    cms = [cs.RigidConstraintModel(t, model, j, _rand_se3(rng), 0, _rand_se3(rng, 1.0), f)
+           for (t, f), j in zip(kinds, _leaves(model))]
+    q, v, x = sm.random_inputs(model, 4, 22)
+    desc = cs.stack_desc(cms)
+    got = om.constraint_dynamics_derivatives(q, v, 10 * x, desc)
+    ref = om.constraint_dynamics(q, v, 10 * x, desc)
+    assert rel_err(got[0], ref[0]) < 1e-14 and rel_err(got[1], ref[1]) < 1e-14
+    fd = _central_differences(model, om, q, v, 10 * x, desc)
+    names = ("ddq_dq", "dlambda_dq", "ddq_dv", "dlambda_dv", "ddq_dtau", "dlambda_dtau")
+    analytic = (got[2], got[5], got[3], got[6], got[4], got[7])
+    for name, a, f in zip(names, analytic, fd):
+        assert rel_err(a, f) < 1e-6, (name, rel_err(a, f))
+
+
+def test_constraint_dynamics_derivatives_proximal_and_errors(humanoid):
+    """With mu > 0 the derivatives follow the proximal recursion: at convergence they approach the
+    undamped derivatives; closed loops and Baumgarte gains are rejected."""
+    model, om = humanoid
+    rng = np.random.default_rng(23)
+    cms = [cs.RigidConstraintModel(cs.CONTACT_6D, model, j, _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL)
+           for j in _leaves(model)[:2]]
+    q, v, x = sm.random_inputs(model, 3, 24)
+    desc = cs.stack_desc(cms)
+    a = om.constraint_dynamics_derivatives(q, v, 10 * x, desc)
+    b = om.constraint_dynamics_derivatives(q, v, 10 * x, desc, mu=1e-6, max_iter=50, absolute_accuracy=0.0,
+                                           relative_accuracy=1e-14)
+    assert np.all(b[8] > 1)
+    for k in range(2, 8):
+        assert rel_err(b[k], a[k]) < 1e-6, k
+    loop = [cs.RigidConstraintModel(cs.CONTACT_6D, model, _leaves(model)[0], gm.SE3.Identity(), _leaves(model)[1],
+                                    gm.SE3.Identity(), cs.LOCAL)]
+    with pytest.raises(ValueError, match="world"):
+        om.constraint_dynamics_derivatives(q, v, x, cs.stack_desc(loop))
+    cms[0].corrector.Kp[:] = 1.0
+    with pytest.raises(ValueError, match="world"):
+        om.constraint_dynamics_derivatives(q, v, x, cs.stack_desc(cms))

@@ -231,3 +231,67 @@ def test_argument_errors():
     ps.max_iter = 1
     assert L.gb_constraint_dynamics(other.dev.h, 0, data.constraint_set.h, C.byref(ps), *args) == _capi.GB_ERR_INVALID_ARGUMENT
     assert L.gb_constraint_dynamics(data.dev.h, 0, data.constraint_set.h, C.byref(ps), *args) == _capi.GB_OK
+
+
+def _deriv_tol(om, q, v, tau, desc, **kw):
+    a = om.constraint_dynamics_derivatives(q, v, tau, desc, **kw)
+    b = om.constraint_dynamics_derivatives(q, v, tau, desc, prec=1, **kw)
+    errs = [rel_err(a[k], b[k]) for k in range(2, 8) if a[k].size]
+    return a, b, max(1e-9, 30 * max(errs))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["humanoid32", "tree32ff", "chain100", "mixedtree24ff", "unaligned20ff",
+                                  "translationtree14", "multidoftree16"])
+def test_constraint_dynamics_derivatives_match_oracle(name, precision):
+    """computeConstraintDynamicsDerivatives (constraints to the world, no gains) against the oracle:
+    ddq_dq, ddq_dv, ddq_dtau, dlambda_dq, dlambda_dv, dlambda_dtau; FP64 at 30 x the double oracle's
+    own error against long double (at least 1e-9)."""
+    model = MODELS[name]()
+    om = OracleModel(model)
+    cms = _constraints(model, 31)
+    q, v, x = sm.random_inputs(model, 129, 32)
+    v = 0.3 * v
+    tau = 10 * x
+    data = pg.createData(model, precision)
+    pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(tau), cms)
+    got = [t.cpu().numpy() for t in pg.computeConstraintDynamicsDerivatives(model, data, cms)]
+    (o, ld, tol64) = _deriv_tol(om, q, v, tau, cs.stack_desc(cms))
+    names = ("ddq_dq", "ddq_dv", "ddq_dtau", "dlambda_dq", "dlambda_dv", "dlambda_dtau")
+    for k, nm in enumerate(names):
+        if precision == "fp64":
+            assert rel_err(got[k], ld[2 + k]) < tol64, (nm, rel_err(got[k], ld[2 + k]), tol64)
+        else:
+            tol = 1e-2 if name == "chain100" else max(1e-4, 30 * tol64)
+            assert rel_err(got[k], o[2 + k]) < tol, (nm, rel_err(got[k], o[2 + k]))
+    assert pg.numericStatus(data) == 0
+
+
+def test_constraint_dynamics_derivatives_proximal_and_errors():
+    """mu > 0 with a fixed number of iterations (accuracies 0): the derivatives follow the oracle's
+    proximal recursion; no constraint gives the ABA derivatives; closed loops and Baumgarte gains are
+    refused with GB_ERR_UNSUPPORTED."""
+    model = sm.humanoid32(1)
+    om = OracleModel(model)
+    cms = _constraints(model, 33)
+    q, v, x = sm.random_inputs(model, 64, 34)
+    data = pg.createData(model)
+    st = pg.ProximalSettings(0.0, 0.0, 1e-4, 5)
+    pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms, None, st)
+    assert st.iter == 5
+    got = [t.cpu().numpy() for t in pg.computeConstraintDynamicsDerivatives(model, data, cms)]
+    o = om.constraint_dynamics_derivatives(q, v, 10 * x, cs.stack_desc(cms), mu=1e-4, max_iter=5,
+                                           absolute_accuracy=0.0, relative_accuracy=0.0)
+    for k in range(6):
+        assert rel_err(got[k], o[2 + k]) < 1e-9, k
+    pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), [])
+    d0 = [t.cpu().numpy() for t in pg.computeConstraintDynamicsDerivatives(model, data, [])]
+    _, a_dq, a_dv, a_mi = om.aba_derivatives(q, v, 10 * x)
+    assert rel_err(d0[0], a_dq) < 1e-10 and rel_err(d0[1], a_dv) < 1e-10 and rel_err(d0[2], a_mi) < 1e-10
+    lv = _leaves(model)
+    for bad in ([cs.RigidConstraintModel(cs.CONTACT_6D, model, lv[0], gm.SE3.Identity(), lv[1], gm.SE3.Identity(),
+                                         cs.LOCAL)], _constraints(model, 35, gains=True)):
+        pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), bad)
+        with pytest.raises(_capi.GBError) as e:
+            pg.computeConstraintDynamicsDerivatives(model, data, bad)
+        assert e.value.code == _capi.GB_ERR_UNSUPPORTED
