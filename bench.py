@@ -50,7 +50,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-extra", action="store_true",
                    help="skip the per-function, heterogeneous-batch and rollout measurements")
-    p.add_argument("--only", choices=["rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives"], default=None,
+    p.add_argument("--only", choices=["rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives",
+                                      "constraint_dynamics", "constraint_dynamics_derivatives"], default=None,
                    help="time one batched call on the humanoid (for profiling), print its timing and exit")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     return p.parse_args()
@@ -983,7 +984,11 @@ def run_only(args):
     q, v, x = sm.random_inputs(model, B, 0)
     qd, vd, xd = (torch.from_numpy(a).cuda() for a in (q, v, 10.0 * x))
     data = pg.createData(model, args.precision)
+    contacts = humanoid_contacts(pg, model)
     fn = {
+        "constraint_dynamics": lambda: pg.constraintDynamics(model, data, qd, vd, xd, contacts),
+        "constraint_dynamics_derivatives": lambda: (pg.constraintDynamics(model, data, qd, vd, xd, contacts),
+                                                    pg.computeConstraintDynamicsDerivatives(model, data, contacts)),
         "rnea": lambda: pg.rnea(model, data, qd, vd, xd),
         "aba": lambda: pg.aba(model, data, qd, vd, xd),
         "crba": lambda: pg.crba(model, data, qd),

@@ -974,6 +974,168 @@ __global__ void __launch_bounds__(kThreads)
     for (long k = 0; k < (long)nc * nv; ++k) l[k] = X[k] + (pass == 0 ? Cq[k] : 0.0);
   }
 }
+
+// The same assembly with one warp per configuration: lanes own columns (c = lane, lane + 32, ...),
+// the operands of a configuration sit in shared memory (rows padded to an odd stride), broadcast
+// reads along the rows.  Shared memory per warp, in doubles: M^-1 and dtau (nv rows each), J, JMinv,
+// R, X, tmp (nc rows each) at stride nv + 1, G and osim (nc x (nc + 1)).
+__host__ __device__ inline long cd_warp_doubles(int nv, int nc) {
+  return 2L * nv * (nv + 1) + 5L * nc * (nv + 1) + 2L * nc * (nc + 1) + nv;
+}
+
+// Y(r, c) for rows r < rows and the lane's columns c: Y = sum_k A(r, k) Bm(k, c), A(r, k) =
+// A[r * ars + k * acs] read by broadcast, Bm(k, c) = Bm[k * bs + c]; four rows per pass (four
+// independent accumulations per Bm load); store(r, c, value) consumes the results
+template <class F>
+__device__ void lane_gemm(int rows, int cols, int K, const double* A, int ars, int acs, const double* Bm, int bs,
+                          int lane, F store) {
+  for (int c = lane; c < cols; c += 32)
+    for (int r0 = 0; r0 < rows; r0 += 4) {
+      const int r1 = min(r0 + 1, rows - 1), r2 = min(r0 + 2, rows - 1), r3 = min(r0 + 3, rows - 1);
+      double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+      for (int k = 0; k < K; ++k) {
+        const double bk = Bm[k * bs + c];
+        t0 += A[r0 * ars + k * acs] * bk;
+        t1 += A[r1 * ars + k * acs] * bk;
+        t2 += A[r2 * ars + k * acs] * bk;
+        t3 += A[r3 * ars + k * acs] * bk;
+      }
+      store(r0, c, t0);
+      if (r0 + 1 < rows) store(r0 + 1, c, t1);
+      if (r0 + 2 < rows) store(r0 + 2, c, t2);
+      if (r0 + 3 < rows) store(r0 + 3, c, t3);
+    }
+}
+
+__global__ void __launch_bounds__(128)
+    k_cd_assemble_warp(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
+                       const double* Js, const double* Aqs, const double* Avs, const double* Cqs, Arr dtq, Arr dtv,
+                       const int* iters, double mu, Arr ddq_dq, Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv,
+                       Arr dl_dtau) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
+  const long b = (long)blockIdx.x * wpb + warp;
+  if (b >= B) return;  // whole warps leave together
+  const int nv = m.nv, sv = nv + 1, sc = nc + 1, it = iters[b];
+  double* base = reinterpret_cast<double*>(smem + ((bytes + 15) & ~15)) + (long)warp * cd_warp_doubles(nv, nc);
+  double *Mi = base, *dt = Mi + (long)nv * sv, *J = dt + (long)nv * sv, *JM = J + (long)nc * sv,
+         *R = JM + (long)nc * sv, *X = R + (long)nc * sv, *T = X + (long)nc * sv, *G = T + (long)nc * sv,
+         *O = G + (long)nc * sc, *Dv = O + (long)nc * sc;
+  // M^-1 = U^-T D^-1 U^-1 (cholesky.hxx:483-500) from U and D staged in shared memory (U in the
+  // dtau buffer, free until dtau is loaded): lane c solves column c, the rows of U read by broadcast
+  {
+    double* Uu = dt;
+    for (int e = lane; e < nv * nv; e += 32) Uu[(e / nv) * sv + e % nv] = Us[(long)e * B + b];
+    for (int k = lane; k < nv; k += 32) Dv[k] = Ds[(long)k * B + b];
+    __syncwarp();
+    for (int c = lane; c < nv; c += 32) {
+      double* x = Mi + c;  // column c, stride sv
+      for (int k = 0; k < nv; ++k) x[k * sv] = k == c ? 1.0 : 0.0;
+      for (int k = nv - 2; k >= 0; --k) {  // x <- U^-1 x
+        const int n = m.nsfr[k] - 1;
+        double t = 0.0;
+        for (int j = 1; j <= n; ++j) t += Uu[k * sv + k + j] * x[(k + j) * sv];
+        x[k * sv] -= t;
+      }
+      for (int k = 0; k < nv; ++k) x[k * sv] /= Dv[k];
+      for (int k = 0; k < nv - 1; ++k) {  // x <- U^-T x
+        const int n = m.nsfr[k] - 1;
+        const double xk = x[k * sv];
+        for (int j = 1; j <= n; ++j) x[(k + j) * sv] -= Uu[k * sv + k + j] * xk;
+      }
+    }
+  }
+  for (int e = lane; e < nc * nv; e += 32) J[(e / nv) * sv + e % nv] = Js[(long)e * B + b];
+  __syncwarp();
+  // JMinv = J M^-1
+  lane_gemm(nc, nv, nv, J, sv, 1, Mi, sv, lane, [&](int r, int c, double t) { JM[r * sv + c] = t; });
+  __syncwarp();
+  // G = JMinv J^T + mu I (Bm(k, c) = J(c, k): the transposed read is a column of J)
+  for (int c = lane; c < nc; c += 32)
+    for (int r = 0; r < nc; ++r) {
+      double t = 0.0;
+      for (int k = 0; k < nv; ++k) t += JM[r * sv + k] * J[c * sv + k];
+      G[r * sc + c] = t + (r == c ? mu : 0.0);
+    }
+  __syncwarp();
+  if (lane == 0)  // G = L L^T in place (lower)
+    for (int j = 0; j < nc; ++j) {
+      double t = G[j * sc + j];
+      for (int k = 0; k < j; ++k) t -= G[j * sc + k] * G[j * sc + k];
+      gb::check_pivot(m, t);
+      const double l = sqrt(t);
+      G[j * sc + j] = l;
+      for (int i = j + 1; i < nc; ++i) {
+        double u = G[i * sc + j];
+        for (int k = 0; k < j; ++k) u -= G[i * sc + k] * G[j * sc + k];
+        G[i * sc + j] = u / l;
+      }
+    }
+  __syncwarp();
+  for (int c = lane; c < nc; c += 32) {  // osim = G^-1: lane c solves column c
+    for (int i = 0; i < nc; ++i) {
+      double t = i == c ? 1.0 : 0.0;
+      for (int k = 0; k < i; ++k) t -= G[i * sc + k] * O[k * sc + c];
+      O[i * sc + c] = t / G[i * sc + i];
+    }
+    for (int i = nc - 1; i >= 0; --i) {
+      double t = O[i * sc + c];
+      for (int k = i + 1; k < nc; ++k) t -= G[k * sc + i] * O[k * sc + c];
+      O[i * sc + c] = t / G[i * sc + i];
+    }
+  }
+  __syncwarp();
+  auto prox = [&](const double* Rm) {  // X <- the recursion on Rm (nc x nv, stride sv)
+    lane_gemm(nc, nv, nc, O, sc, 1, Rm, sv, lane, [&](int r, int c, double t) { X[r * sv + c] = -t; });
+    for (int k2 = 1; k2 < it; ++k2) {
+      __syncwarp();
+      for (int c = lane; c < nv; c += 32)
+        for (int r = 0; r < nc; ++r) T[r * sv + c] = mu * X[r * sv + c] - Rm[r * sv + c];
+      __syncwarp();
+      lane_gemm(nc, nv, nc, O, sc, 1, T, sv, lane, [&](int r, int c, double t) { X[r * sv + c] = t; });
+    }
+    __syncwarp();
+  };
+  // the derivatives in tau
+  prox(JM);
+  {
+    const gb::Out od{const_cast<double*>(ddq_dtau.p) + b * ddq_dtau.is, ddq_dtau.es};
+    const gb::Out ol{nc > 0 ? const_cast<double*>(dl_dtau.p) + b * dl_dtau.is : nullptr, dl_dtau.es};
+    for (int e = lane; e < nc * nv; e += 32) ol[e] = X[(e / nv) * sv + e % nv];
+    // ddq_dtau = M^-1 + JMinv^T X (A(r, k) = JM(k, r))
+    lane_gemm(nv, nv, nc, JM, 1, sv, X, sv, lane,
+              [&](int r, int c, double t) { od[(long)r * nv + c] = Mi[r * sv + c] + t; });
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    const Arr& dta = pass == 0 ? dtq : dtv;
+    const double* A = pass == 0 ? Aqs : Avs;
+    const gb::In dti{dta.p + b * dta.is, dta.es};
+    __syncwarp();
+    for (int e = lane; e < nv * nv; e += 32) dt[(e / nv) * sv + e % nv] = dti[e];
+    __syncwarp();
+    // R = dac_dx - JMinv dtau_dx
+    lane_gemm(nc, nv, nv, JM, sv, 1, dt, sv, lane,
+              [&](int r, int c, double t) { R[r * sv + c] = A[(long)(r * nv + c) * B + b] - t; });
+    __syncwarp();
+    prox(R);
+    // dtau_dx -= J^T dlambda_dx (A(r, k) = J(k, r); column c is lane c's)
+    lane_gemm(nv, nv, nc, J, 1, sv, X, sv, lane, [&](int r, int c, double t) { dt[r * sv + c] -= t; });
+    __syncwarp();
+    const Arr& od = pass == 0 ? ddq_dq : ddq_dv;
+    const Arr& ol = pass == 0 ? dl_dq : dl_dv;
+    const gb::Out o{const_cast<double*>(od.p) + b * od.is, od.es};
+    const gb::Out l{nc > 0 ? const_cast<double*>(ol.p) + b * ol.is : nullptr, ol.es};
+    bool finite = true;  // ddq_dx = -M^-1 dtau_dx
+    lane_gemm(nv, nv, nv, Mi, sv, 1, dt, sv, lane, [&](int r, int c, double t) {
+      finite = finite && gb::finite_value(t);
+      o[(long)r * nv + c] = -t;
+    });
+    if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
+    for (int e = lane; e < nc * nv; e += 32)
+      l[e] = X[(e / nv) * sv + e % nv] + (pass == 0 ? Cqs[(long)e * B + b] : 0.0);
+  }
+}
 }  // namespace
 
 int launch_contact(const gb_model* M, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
@@ -1124,11 +1286,32 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
   } else if (rc == GB_OK) {
     rc = cuda_error(cudaMemsetAsync(Fe, 0, sizeof(double) * 6 * nju * B, st), "cudaMemsetAsync");
   }
+  // the warp assembly reads dtau per configuration (instance layout); the thread assembly per element
+  const long per_warp = sizeof(double) * cd_warp_doubles((int)nv, (int)nc);
+  const long stage = (M->stage_bytes + 15) & ~15L;
+  int wpb = 4;
+  while (wpb > 1 && stage + wpb * per_warp > M->smem_optin) --wpb;
+  const bool warp_kernel = stage + wpb * per_warp <= M->smem_optin;
+  const Arr dtqa = warp_kernel ? Arr{dtq, nn, 1} : Arr{dtq, 1, B}, dtva = warp_kernel ? Arr{dtv, nn, 1} : Arr{dtv, 1, B};
   if (rc == GB_OK)
-    rc = launch_rnea_derivs_fext(M, precision, B, q, v, ddq, Arr{Fe, 1, B}, Arr{dtq, 1, B}, Arr{dtv, 1, B},
-                                 Arr{dMs, 1, B}, st);
-  if (rc == GB_OK) rc = opt_in((const void*)k_cd_assemble, "k_cd_assemble");
-  if (rc == GB_OK) {
+    rc = launch_rnea_derivs_fext(M, precision, B, q, v, ddq, Arr{Fe, 1, B}, dtqa, dtva,
+                                 warp_kernel ? Arr{dMs, nn, 1} : Arr{dMs, 1, B}, st);
+  if (rc == GB_OK && warp_kernel) {
+    const size_t smem = (size_t)(stage + wpb * per_warp);
+    const cudaError_t e = cudaFuncSetAttribute((const void*)k_cd_assemble_warp,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    rc = e == cudaSuccess ? GB_OK : cuda_error(e, "k_cd_assemble_warp");
+    if (rc == GB_OK) {
+      const long g = (B + wpb - 1) / wpb;
+      k_cd_assemble_warp<<<(unsigned)g, 32 * wpb, smem, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Aq,
+                                                            Av, Cq, dtqa, dtva, its, s.mu, ddq_dq, ddq_dv, ddq_dtau,
+                                                            dl_dq, dl_dv, dl_dtau);
+      rc = cuda_error(cudaGetLastError(), "k_cd_assemble_warp");
+    }
+  } else if (rc == GB_OK) {
+    rc = opt_in((const void*)k_cd_assemble, "k_cd_assemble");
+  }
+  if (rc == GB_OK && !warp_kernel) {
     k_cd_assemble<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(
         M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Aq, Av, Cq, dtq, dtv, its, s.mu, Mis, JMs, Gs, Os, Rs, Xs,
         Ts, ddq_dq, ddq_dv, ddq_dtau, dl_dq, dl_dv, dl_dtau);
