@@ -120,13 +120,14 @@ def test_orientation_forms_and_units():
 
 
 @pytest.mark.parametrize("snippet, msg", [
-    ('<default><joint damping="1"/></default><worldbody/>', "default"),
     ('<worldbody><body name="a"><joint/><joint type="slide"/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "several"),
-    ('<worldbody><body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody>', "geom"),
+    ('<default><default><joint/></default></default><worldbody/>', "Class does not have a name"),
+    ('<worldbody><body name="a" childclass="x"><joint/></body></worldbody>', "unknown class"),
+    ('<worldbody><body name="a"><joint/><geom type="box" size="0.1 0.1 0.1" shellinertia="true"/></body></worldbody>',
+     "Shell inertia"),
     ('<worldbody><body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/>'
      '<body name="b"><freejoint/><inertial mass="1" diaginertia="1 1 1"/></body></body></worldbody>', "free"),
     ('<worldbody><body name="a" zaxis="0 1 0"><joint/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "zaxis"),
-    ('<worldbody><body name="a" childclass="x"><joint/></body></worldbody>', "class"),
     ('<worldbody><body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/>'
      '<frame pos="0 0 1"><body name="b"><joint/><inertial mass="1" diaginertia="1 1 1"/></body></frame>'
      '</body></worldbody>', "frame"),
@@ -140,10 +141,82 @@ def test_outside_the_subset_raises(snippet, msg):
         buildModelFromMJCFXML("<robot/>")
 
 
-def test_geoms_ignored_when_inertia_not_from_geoms():
-    m = buildModelFromMJCFXML("""<mujoco><compiler inertiafromgeom="false"/><worldbody>
-      <body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody></mujoco>""")
-    assert m.nv == 1 and m.inertias[1].mass == 0.0
+def test_inertia_from_geom_false_needs_an_inertial():
+    """inertiafromgeom="false" without an <inertial> is an error (mjcf-graph.cpp:416-419)."""
+    with pytest.raises(ValueError, match="no inertia was found"):
+        buildModelFromMJCFXML("""<mujoco><compiler inertiafromgeom="false"/><worldbody>
+          <body name="a"><joint/><geom type="sphere" size="0.1"/></body></worldbody></mujoco>""")
+
+
+def test_defaults_and_classes():
+    """Attribute precedence: top-level default < body childclass (inherited by nested bodies) <
+    element class < the element's own attributes; nested classes inherit from their enclosing
+    default (mjcf-graph.cpp:35-52, 239-285)."""
+    m = buildModelFromMJCFXML("""<mujoco><default>
+        <joint type="hinge" axis="0 1 0" armature="0.1"/>
+        <default class="slider"><joint type="slide" axis="1 0 0"/>
+          <default class="zslider"><joint axis="0 0 1" armature="0.3"/></default></default>
+        <default class="heavy"><joint armature="0.5"/></default></default>
+      <worldbody>
+        <body name="a"><joint/><inertial mass="1" diaginertia="1 1 1"/>
+          <body name="b" childclass="slider"><joint/><inertial mass="1" diaginertia="1 1 1"/>
+            <body name="c"><joint class="zslider"/><inertial mass="1" diaginertia="1 1 1"/>
+              <body name="d"><joint class="heavy" axis="0 0 1" type="hinge"/><inertial mass="1" diaginertia="1 1 1"/>
+              </body></body></body></body></worldbody></mujoco>""")
+    assert m.jtypes[1:] == [gm.JT_RY, gm.JT_PX, gm.JT_PZ, gm.JT_RZ]
+    assert np.allclose(m.armature, [0.1, 0.1, 0.3, 0.5])
+
+
+def _solid(kind, m, size):
+    """Solid inertias about the center (diagonal), by the textbook formulas."""
+    if kind == "sphere":
+        r = size[0]
+        return np.diag([0.4 * m * r * r] * 3)
+    if kind == "box":  # full side lengths
+        x, y, z = size
+        return np.diag([m * (y * y + z * z), m * (x * x + z * z), m * (x * x + y * y)]) / 12
+    if kind == "cylinder":  # radius, full length
+        r, L = size
+        return np.diag([m * (3 * r * r + L * L) / 12] * 2 + [m * r * r / 2])
+    raise ValueError(kind)
+
+
+def test_inertia_from_geoms():
+    """A body's inertia from its geoms (inertiafromgeom auto, no <inertial>): a sphere from its
+    density (default 1000), a box given its mass, a cylinder placed by fromto; a visual geom
+    (contype = conaffinity = 0) does not count; the geom class defaults apply."""
+    m = buildModelFromMJCFXML("""<mujoco><default><default class="vis"><geom contype="0" conaffinity="0"/></default>
+      </default><worldbody><body name="a"><joint axis="0 0 1"/>
+        <geom type="sphere" size="0.1" pos="0.2 0 0"/>
+        <geom type="box" size="0.1 0.2 0.3" mass="3" pos="0 0.5 0" euler="0 0 90"/>
+        <geom type="cylinder" size="0.05" fromto="0 0 0 0 0 0.4" density="500"/>
+        <geom class="vis" type="sphere" size="5"/></body></worldbody></mujoco>""")
+    m_s = 1000 * 4.0 / 3 * np.pi * 0.1 ** 3
+    m_c = 500 * np.pi * 0.05 ** 2 * 0.4
+    Rz = np.array([[0.0, -1, 0], [1, 0, 0], [0, 0, 1]])
+    parts = [gm.Inertia(m_s, np.zeros(3), _solid("sphere", m_s, [0.1])).se3_action(gm.SE3(np.eye(3), np.array([0.2, 0, 0]))),
+             gm.Inertia(3.0, np.zeros(3), _solid("box", 3.0, [0.2, 0.4, 0.6])).se3_action(gm.SE3(Rz, np.array([0, 0.5, 0]))),
+             gm.Inertia(m_c, np.zeros(3), _solid("cylinder", m_c, [0.05, 0.4])).se3_action(gm.SE3(np.eye(3), np.array([0, 0, 0.2])))]
+    want = parts[0] + parts[1] + parts[2]
+    got = m.inertias[1]
+    assert np.isclose(got.mass, m_s + 3.0 + m_c)
+    assert np.allclose(got.lever, want.lever, atol=1e-14)
+    assert np.allclose(got.matrix3(), want.matrix3(), atol=1e-13)
+
+
+def test_capsule_inertia_and_fromto_orientation():
+    """A capsule along x given by fromto: mass from the volume of a cylinder and two half spheres, the
+    reference's capsule inertia (spatial/inertia.hpp FromCapsule) rotated so that its axis is x."""
+    m = buildModelFromMJCFXML("""<mujoco><worldbody><body name="a"><joint axis="0 0 1"/>
+        <geom type="capsule" size="0.05" fromto="-0.2 0 0 0.2 0 0"/></body></worldbody></mujoco>""")
+    r, h = 0.05, 0.4
+    vol = np.pi * r * r * h + 4.0 / 3 * np.pi * r ** 3
+    Y = m.inertias[1]
+    assert np.isclose(Y.mass, 1000 * vol)
+    assert np.allclose(Y.lever, 0, atol=1e-15)
+    I = Y.matrix3()
+    assert np.isclose(I[1, 1], I[2, 2]) and I[0, 0] < I[1, 1]  # the symmetry axis is x
+    assert np.allclose(I - np.diag(np.diag(I)), 0, atol=1e-15)
 
 
 def test_ball_joint():
