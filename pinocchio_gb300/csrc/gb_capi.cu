@@ -306,12 +306,28 @@ int gb_constraint_set_create(const gb_model* M, int n, const gb_constraint_desc*
       for (int j = c1; j > 0; j = M->parents[j]) mark(j, 3);
     S->host.push_back(d);
   }
-  const size_t bytes = sizeof(gbi::ConstraintDev) * (size_t)n + S->sparsity.size();
+  // the dofs whose rows of U^-1 J^T can be non-zero: the ancestor closure of each constraint's
+  // columns (both joints' supports), as a mask and as a sorted list [count, dofs...]
+  std::vector<signed char> closure((size_t)n * nv, 0);
+  std::vector<short> lists((size_t)n * (nv + 1), 0);
+  for (int e = 0; e < n; ++e) {
+    signed char* cm = closure.data() + (size_t)e * nv;
+    for (int j : {S->host[e].j1, S->host[e].j2})
+      for (; j > 0; j = M->parents[j])
+        for (int k = 0; k < M->nvs[j]; ++k) cm[M->idx_v[j] + k] = 1;
+    short* L = lists.data() + (size_t)e * (nv + 1);
+    for (int k = 0; k < nv; ++k)
+      if (cm[k]) L[1 + L[0]++] = (short)k;
+  }
+  const size_t o_lists = (sizeof(gbi::ConstraintDev) * (size_t)n + 2 * S->sparsity.size() + 1) & ~(size_t)1;
+  const size_t bytes = n > 0 ? o_lists + sizeof(short) * lists.size() : 0;
   if (bytes > 0) {
-    std::vector<unsigned char> h(bytes);
-    if (n > 0) std::memcpy(h.data(), S->host.data(), sizeof(gbi::ConstraintDev) * (size_t)n);
-    if (!S->sparsity.empty()) std::memcpy(h.data() + sizeof(gbi::ConstraintDev) * (size_t)n, S->sparsity.data(),
-                                          S->sparsity.size());
+    std::vector<unsigned char> h(bytes, 0);
+    std::memcpy(h.data(), S->host.data(), sizeof(gbi::ConstraintDev) * (size_t)n);
+    unsigned char* codes = h.data() + sizeof(gbi::ConstraintDev) * (size_t)n;
+    std::memcpy(codes, S->sparsity.data(), S->sparsity.size());
+    std::memcpy(codes + S->sparsity.size(), closure.data(), closure.size());
+    std::memcpy(h.data() + o_lists, lists.data(), sizeof(short) * lists.size());
     cudaError_t e = cudaMalloc(&S->d_mem, bytes);
     if (e == cudaSuccess) e = cudaMemcpy(S->d_mem, h.data(), bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {

@@ -503,6 +503,64 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// delassus_llt on the constraint rows' supports: the rows of U^-1 J^T that can be non-zero for a
+// constraint are the ancestor closure of its columns (a sorted list per constraint, clist = [count,
+// dofs...]; cmask the same set as a mask), U^-1 keeps a vector inside such a set, and a Delassus
+// entry sums over the two constraints' common dofs only
+__device__ void delassus_llt_tree(const gb::MView& m, const Col& U, const Col& D, const gb::In& Ji, int nc,
+                                  double inv_damping, const Col& Y, const Col& G, const ConstraintDev* tab,
+                                  int ncon, const signed char* cmask, const short* clist) {
+  const int nv = m.nv;
+  for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);
+  for (int e = 0; e < ncon; ++e) {
+    const short* L = clist + (long)e * (nv + 1);
+    const int len = L[0], r0 = tab[e].row, r1 = r0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
+    for (int c = r0; c < r1; ++c) {
+      for (int p = 0; p < len; ++p) Y[(long)L[1 + p] * nc + c] = Ji[c * nv + L[1 + p]];
+      for (int p = len - 2; p >= 0; --p) {  // U^-1 restricted to the set (subtree rows k..k+nsfr-1)
+        const int k = L[1 + p], end = k + m.nsfr[k];
+        double t = 0.0;
+        for (int p2 = p + 1; p2 < len && L[1 + p2] < end; ++p2) t += U[(long)k * nv + L[1 + p2]] * Y[(long)L[1 + p2] * nc + c];
+        Y[(long)k * nc + c] -= t;
+      }
+    }
+    for (int p = 0; p < len; ++p) {
+      const int r = L[1 + p];
+      const double sd = sqrt(D[r]);
+      for (int c = r0; c < r1; ++c) Y[(long)r * nc + c] /= sd;
+    }
+  }
+  for (int ei = 0; ei < ncon; ++ei) {
+    const int i0 = tab[ei].row, i1 = i0 + (tab[ei].type == GB_CONTACT_3D ? 3 : 6);
+    const signed char* mi = cmask + (long)ei * nv;
+    for (int ej = 0; ej <= ei; ++ej) {
+      const short* L = clist + (long)ej * (nv + 1);
+      const int len = L[0], j0 = tab[ej].row, j1 = j0 + (tab[ej].type == GB_CONTACT_3D ? 3 : 6);
+      for (int i = i0; i < i1; ++i)
+        for (int j = j0; j < j1 && j <= i; ++j) {
+          double t = 0.0;
+          for (int p = 0; p < len; ++p) {
+            const int k = L[1 + p];
+            if (mi[k]) t += Y[(long)k * nc + i] * Y[(long)k * nc + j];
+          }
+          G[(long)i * nc + j] = t + (i == j ? inv_damping : 0.0);
+        }
+    }
+  }
+  for (int j = 0; j < nc; ++j) {
+    double t = G[(long)j * nc + j];
+    for (int k = 0; k < j; ++k) t -= G[(long)j * nc + k] * G[(long)j * nc + k];
+    gb::check_pivot(m, t);
+    const double ljj = sqrt(t);
+    G[(long)j * nc + j] = ljj;
+    for (int i = j + 1; i < nc; ++i) {
+      double u = G[(long)i * nc + j];
+      for (int k = 0; k < j; ++k) u -= G[(long)i * nc + k] * G[(long)j * nc + k];
+      G[(long)i * nc + j] = u / ljj;
+    }
+  }
+}
+
 // The proximal iterations (constrained-dynamics.hxx:434-486) on the factorisations M = U D U^T and
 // J M^-1 J^T + mu I = L L^T: lambda_k = L^-T L^-1 (c0 + mu lambda_{k-1}) with c0 = rhs - J M^-1 (tau -
 // nle); the reference's residuals: absolute ||(J M^-1 J^T) y - rhs||_inf and relative ||y - y_prev||_inf
@@ -511,7 +569,8 @@ __global__ void __launch_bounds__(kThreads)
     k_constraint_solve(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
                        const double* nles, double* Rs, double* Ys, double* Gs, const double* Js, const double* Rh,
                        double* C0s, double* LPs, double* Ts, Arr tau, gb_proximal_settings s, Arr ddq, Arr lam,
-                       int* iters, double* residuals) {
+                       int* iters, double* residuals, const ConstraintDev* __restrict__ tab, int ncon,
+                       const signed char* __restrict__ cmask, const short* __restrict__ clist) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -529,12 +588,16 @@ __global__ void __launch_bounds__(kThreads)
   double ar = 0.0, rr = 0.0;
   const Col L{nc > 0 ? const_cast<double*>(lam.p) + b * lam.is : nullptr, nc > 0 ? lam.es : 0};
   if (nc > 0) {
-    delassus_llt(m, U, D, Ji, nc, s.mu, Y, G);
-    for (int c = 0; c < nc; ++c) {
-      double t = 0.0;
-      for (int k = 0; k < nv; ++k) t += Ji[c * nv + k] * R[k];
-      C0[c] = Rhs[c] - t;
-      LP[c] = 0.0;
+    delassus_llt_tree(m, U, D, Ji, nc, s.mu, Y, G, tab, ncon, cmask, clist);
+    for (int e = 0; e < ncon; ++e) {
+      const short* Ls = clist + (long)e * (nv + 1);
+      const int r0 = tab[e].row, r1 = r0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
+      for (int c = r0; c < r1; ++c) {
+        double t = 0.0;
+        for (int p = 0; p < Ls[0]; ++p) t += Ji[c * nv + Ls[1 + p]] * R[Ls[1 + p]];
+        C0[c] = Rhs[c] - t;
+        LP[c] = 0.0;
+      }
     }
     while (it < s.max_iter) {
       ++it;
@@ -565,10 +628,16 @@ __global__ void __launch_bounds__(kThreads)
     residuals[2 * b + 1] = rr;
   }
   const Col A{Y.p, B};
-  for (int k = 0; k < nv; ++k) {
-    double t = 0.0;
-    for (int c = 0; c < nc; ++c) t += Ji[c * nv + k] * L[c];
-    A[k] = t;
+  for (int k = 0; k < nv; ++k) A[k] = 0.0;
+  for (int e = 0; e < ncon; ++e) {
+    const short* Ls = clist + (long)e * (nv + 1);
+    const int r0 = tab[e].row, r1 = r0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
+    for (int p = 0; p < Ls[0]; ++p) {
+      const int k = Ls[1 + p];
+      double t = 0.0;
+      for (int c = r0; c < r1; ++c) t += Ji[c * nv + k] * L[c];
+      A[k] += t;
+    }
   }
   chol_solve(m, U, D, A);
   bool finite = true;
@@ -1194,6 +1263,10 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
          *LP = C0 + nc * B, *Ts = LP + nc * B;
   const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
   const signed char* sp = reinterpret_cast<const signed char*>(tab + (set->n > 0 ? set->n : 0));
+  const signed char* cmask = sp + (long)set->n * nv;
+  const short* clist = reinterpret_cast<const short*>(
+      static_cast<const unsigned char*>(set->d_mem) +
+      ((sizeof(ConstraintDev) * (size_t)set->n + 2 * (size_t)set->n * nv + 1) & ~(size_t)1));
   rc = launch_crba(M, GB_FP64, false, B, q, Arr{Ms, 1, B}, Arr{Us, 1, B}, Arr{Ds, 1, B}, st);
   if (rc == GB_OK) {
     const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
@@ -1230,7 +1303,8 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
   if (rc == GB_OK) {
     k_constraint_solve<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds,
                                                                         nles, Rs, Ys, Gs, Js, Rh, C0, LP, Ts, tau, s,
-                                                                        ddq, lam, iters, residuals);
+                                                                        ddq, lam, iters, residuals, tab, set->n, cmask,
+                                                                        clist);
     rc = cuda_error(cudaGetLastError(), "k_constraint_solve");
   }
   scratch_free(scratch, st);
