@@ -67,10 +67,16 @@ enum {
   GB_JOINT_TRANSLATION = 10, /* JointModelTranslation (joint-translation.hpp): q = v in R^3 */
   GB_JOINT_SPHERICAL = 11,   /* JointModelSpherical (joint-spherical.hpp): q = unit quaternion
                                 (x, y, z, w), v = angular velocity in the joint frame */
-  GB_JOINT_PLANAR = 12       /* JointModelPlanar (joint-planar.hpp): q = (x, y, cos t, sin t),
+  GB_JOINT_PLANAR = 12,      /* JointModelPlanar (joint-planar.hpp): q = (x, y, cos t, sin t),
                                 v = (vx, vy, wz) in the joint frame.  Models with spherical or
                                 planar joints run one configuration per thread (gb_model_set_layout
                                 refuses the lane layouts) and are not accepted by gb_batch_multi. */
+  GB_JOINT_RUBX = 13,        /* JointModelRUBX/RUBY/RUBZ (joint-revolute-unbounded.hpp): revolute   */
+  GB_JOINT_RUBY = 14,        /* about x / y / z with q = (cos t, sin t) taken as given (not        */
+  GB_JOINT_RUBZ = 15,        /* renormalised), nq = 2, nv = 1; what the URDF "continuous" joint is */
+  GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED = 16 /* JointModelRevoluteUnboundedUnaligned
+                                (joint-revolute-unbounded-unaligned.hpp): the same about
+                                gb_model_desc.axis */
 };
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
 /* functions of a heterogeneous batch task / of a launch setting */

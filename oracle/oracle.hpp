@@ -41,8 +41,13 @@ enum JointType {
   JT_PU = 9,  // JointModelPrismaticUnaligned (multibody/joint/joint-prismatic-unaligned.hpp)
   JT_TR = 10,   // JointModelTranslation (multibody/joint/joint-translation.hpp): nq = nv = 3
   JT_SPH = 11,  // JointModelSpherical (multibody/joint/joint-spherical.hpp): quaternion, nq 4, nv 3
-  JT_PL = 12    // JointModelPlanar (multibody/joint/joint-planar.hpp): (x, y, cos, sin), nq 4, nv 3
+  JT_PL = 12,   // JointModelPlanar (multibody/joint/joint-planar.hpp): (x, y, cos, sin), nq 4, nv 3
+  // JointModelRevoluteUnboundedTpl<axis> (multibody/joint/joint-revolute-unbounded.hpp):
+  // q = (cos, sin), nq 2, nv 1; the unaligned form (joint-revolute-unbounded-unaligned.hpp)
+  JT_RUBX = 13, JT_RUBY = 14, JT_RUBZ = 15, JT_RUBU = 16
 };
+inline bool three_dof(int jt) { return jt == JT_TR || jt == JT_SPH || jt == JT_PL; }
+inline bool unbounded(int jt) { return jt >= JT_RUBX && jt <= JT_RUBU; }
 enum Convention { LOCAL = 0, WORLD = 1 };  // reference multibody/fwd.hpp:73-81
 
 // ---------------------------------------------------------------------------
@@ -72,9 +77,9 @@ struct Model {
   std::vector<int> lastChild, nvSubtree, parents_fromRow, nvSubtree_fromRow;
 
   static int joint_nq(int jt) {
-    return jt == JT_FF ? 7 : jt == JT_NONE ? 0 : jt == JT_TR ? 3 : (jt == JT_SPH || jt == JT_PL) ? 4 : 1;
+    return jt == JT_FF ? 7 : jt == JT_NONE ? 0 : jt == JT_TR ? 3 : (jt == JT_SPH || jt == JT_PL) ? 4 : unbounded(jt) ? 2 : 1;
   }
-  static int joint_nv(int jt) { return jt == JT_FF ? 6 : jt == JT_NONE ? 0 : jt >= JT_TR ? 3 : 1; }
+  static int joint_nv(int jt) { return jt == JT_FF ? 6 : jt == JT_NONE ? 0 : three_dof(jt) ? 3 : 1; }
 
   // Validates the description and fills the derived tables.
   // lastChild / nvSubtree: data.hxx:195-225 (no mimic joints).
@@ -91,8 +96,8 @@ struct Model {
         if (jtype[0] != JT_NONE) throw std::invalid_argument("joint 0 must be the universe");
         continue;
       }
-      if (jtype[i] < JT_RX || jtype[i] > JT_PL) throw std::invalid_argument("unsupported joint type");
-      if (jtype[i] == JT_RU || jtype[i] == JT_PU) {
+      if (jtype[i] < JT_RX || jtype[i] > JT_RUBU) throw std::invalid_argument("unsupported joint type");
+      if (jtype[i] == JT_RU || jtype[i] == JT_PU || jtype[i] == JT_RUBU) {
         if ((int)axis.size() != 3 * njoints) throw std::invalid_argument("unaligned joints need the axis table");
         const double n = std::sqrt(axis[3 * i] * axis[3 * i] + axis[3 * i + 1] * axis[3 * i + 1] +
                                    axis[3 * i + 2] * axis[3 * i + 2]);
@@ -599,21 +604,30 @@ template <class T> inline SE3<T> joint_transform(int jt, const T* q) {
     return M;
   }
   for (int k = 0; k < 3; ++k) M.R[4 * k] = T(1);
-  if (jt >= JT_PX) {
+  if (jt >= JT_PX && jt <= JT_PZ) {
     M.t[jt - JT_PX] = q[0];
     return M;
   }
   T s, c;
-  o_sincos(q[0], &s, &c);
-  if (jt == JT_RX) { M.R[4] = c; M.R[5] = -s; M.R[7] = s; M.R[8] = c; }
-  if (jt == JT_RY) { M.R[0] = c; M.R[2] = s; M.R[6] = -s; M.R[8] = c; }
-  if (jt == JT_RZ) { M.R[0] = c; M.R[1] = -s; M.R[3] = s; M.R[4] = c; }
+  int ax = jt - JT_RX;
+  if (unbounded(jt)) {  // the unbounded joint's (cos, sin) taken as they are (joint-revolute-unbounded.hpp:154-162)
+    c = q[0];
+    s = q[1];
+    ax = jt - JT_RUBX;
+  } else {
+    o_sincos(q[0], &s, &c);
+  }
+  if (ax == 0) { M.R[4] = c; M.R[5] = -s; M.R[7] = s; M.R[8] = c; }
+  if (ax == 1) { M.R[0] = c; M.R[2] = s; M.R[6] = -s; M.R[8] = c; }
+  if (ax == 2) { M.R[0] = c; M.R[1] = -s; M.R[3] = s; M.R[4] = c; }
   return M;
 }
 // The motion-subspace entry of a one-dof joint: the angular axis 3 + a of a
 // revolute joint (SpatialAxis<ANGULAR + axis>, joint-revolute.hpp:429-543), the
 // linear axis a of a prismatic one (SpatialAxis<LINEAR + axis>, joint-prismatic.hpp:353-461).
-inline int motion_index(int jt) { return jt >= JT_PX ? jt - JT_PX : 3 + (jt - JT_RX); }
+inline int motion_index(int jt) {
+  return unbounded(jt) ? 3 + (jt - JT_RUBX) : jt >= JT_PX ? jt - JT_PX : 3 + (jt - JT_RX);
+}
 // Column k of the joint motion subspace S (local frame).
 // The three-dof joints have unit columns too: translation the linear axes
 // (JointMotionSubspaceTranslationTpl), spherical the angular axes
@@ -623,7 +637,7 @@ inline int multi_col(int jt, int k) { return jt == JT_TR ? k : jt == JT_SPH ? 3 
 template <class T> inline Vec6<T> S_col(int jt, int k) {
   Vec6<T> s = zero6<T>();
   if (jt == JT_FF) s.v[k] = T(1);
-  else if (jt >= JT_TR) s.v[multi_col(jt, k)] = T(1);
+  else if (three_dof(jt)) s.v[multi_col(jt, k)] = T(1);
   else s.v[motion_index(jt)] = T(1);
   return s;
 }
@@ -631,7 +645,7 @@ template <class T> inline Vec6<T> S_col(int jt, int k) {
 template <class T> inline Vec6<T> joint_velocity(int jt, const T* v) {
   Vec6<T> o = zero6<T>();
   if (jt == JT_FF) for (int k = 0; k < 6; ++k) o.v[k] = v[k];
-  else if (jt >= JT_TR) for (int k = 0; k < 3; ++k) o.v[multi_col(jt, k)] = v[k];
+  else if (three_dof(jt)) for (int k = 0; k < 3; ++k) o.v[multi_col(jt, k)] = v[k];
   else o.v[motion_index(jt)] = v[0];
   return o;
 }
@@ -640,7 +654,9 @@ template <class T> inline Vec6<T> joint_velocity(int jt, const T* v) {
 //  * revolute unaligned: M = (toRotationMatrix(axis, q), 0) (joint-revolute-unaligned.hpp:668-673;
 //    math/rotation.hpp:26-73, the Eigen AngleAxis formula), S = (0, axis);
 //  * prismatic unaligned: M = (I, axis q) (joint-prismatic-unaligned.hpp:643-647), S = (axis, 0).
-inline bool unaligned(int jt) { return jt == JT_RU || jt == JT_PU; }
+inline bool unaligned(int jt) { return jt == JT_RU || jt == JT_PU || jt == JT_RUBU; }
+//  * revolute unbounded unaligned: the same rotation from (cos, sin) = q (no sincos),
+//    S = (0, axis) (joint-revolute-unbounded-unaligned.hpp).
 template <class T> inline SE3<T> joint_transform(const Model& m, int i, const T* q) {
   const int jt = m.jtype[i];
   if (!unaligned(jt)) return joint_transform<T>(jt, q);
@@ -653,7 +669,12 @@ template <class T> inline SE3<T> joint_transform(const Model& m, int i, const T*
     return M;
   }
   T s, c;
-  o_sincos(q[0], &s, &c);
+  if (jt == JT_RUBU) {
+    c = q[0];
+    s = q[1];
+  } else {
+    o_sincos(q[0], &s, &c);
+  }
   const T sa[3] = {s * a[0], s * a[1], s * a[2]};
   const T ca[3] = {(T(1) - c) * a[0], (T(1) - c) * a[1], (T(1) - c) * a[2]};
   T t = ca[0] * a[1];
@@ -669,7 +690,7 @@ template <class T> inline Vec6<T> S_col(const Model& m, int i, int k) {
   const int jt = m.jtype[i];
   if (!unaligned(jt)) return S_col<T>(jt, k);
   Vec6<T> s = zero6<T>();
-  const int o = jt == JT_RU ? 3 : 0;
+  const int o = jt == JT_PU ? 0 : 3;
   for (int r = 0; r < 3; ++r) s.v[o + r] = T(m.axis[3 * i + r]);
   return s;
 }
@@ -831,7 +852,7 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau,
             for (int k = 1; k < 6; ++k) s += UDinv[6 * r + k] * U[6 * c + k];
             Ia.a[6 * r + c] -= s;
           }
-    } else if (jt >= JT_TR) {  // calc_aba of the three-dof joints with unit columns (translation
+    } else if (three_dof(jt)) {  // calc_aba of the three-dof joints with unit columns (translation
                                // joint-translation.hpp, spherical joint-spherical.hpp:572-586, planar
                                // joint-planar.hpp:643-661): U = I S, StU = S^T U + armature, LLT inverse
       int cols[3];
@@ -858,7 +879,7 @@ void aba_local(const Model& m, Data<T>& d, const T* q, const T* v, const T* tau,
           }
     } else if (unaligned(jt)) {  // calc_aba of joint-revolute-unaligned.hpp:695-707 /
                                  // joint-prismatic-unaligned.hpp:671-683: U = I S, Dinv = 1 / (S.U + armature)
-      const int o = jt == JT_RU ? 3 : 0;
+      const int o = jt == JT_PU ? 0 : 3;
       T a[3];
       for (int k = 0; k < 3; ++k) a[k] = T(m.axis[3 * i + k]);
       for (int r = 0; r < 6; ++r) U[r] = Ia.a[6 * r + o] * a[0] + Ia.a[6 * r + o + 1] * a[1] + Ia.a[6 * r + o + 2] * a[2];
@@ -1681,6 +1702,19 @@ template <class T> void integrate_se2(const T* q, const T* v, T* out) {
   out[3] = s0 * cv + c0 * sv;
 }
 
+// SpecialOrthogonalOperationTpl<2>::integrate (liegroup/special-orthogonal.hpp:164-185): the unit
+// complex (cos, sin) turned by v, then its first-order renormalisation (3 - |z|^2) / 2
+template <class T> inline void integrate_so2(const T* q, const T* v, T* out) {
+  T sw, cw;
+  o_sincos(v[0], &sw, &cw);
+  out[0] = cw * q[0] - sw * q[1];
+  out[1] = sw * q[0] + cw * q[1];
+  const T n2 = out[0] * out[0] + out[1] * out[1];
+  const T f = (T(3) - n2) / T(2);
+  out[0] *= f;
+  out[1] *= f;
+}
+
 template <class T>
 void integrate(const Model& m, const T* q, const T* v, T* qout) {
   for (int i = 1; i < m.njoints; ++i) {
@@ -1695,6 +1729,10 @@ void integrate(const Model& m, const T* q, const T* v, T* qout) {
     }
     if (jt == JT_PL) {
       integrate_se2(q + iq, v + iv, qout + iq);
+      continue;
+    }
+    if (unbounded(jt)) {
+      integrate_so2(q + iq, v + iv, qout + iq);
       continue;
     }
     if (jt != JT_FF) {

@@ -15,6 +15,10 @@ from .model import (  # noqa: F401
     JointModelPY,
     JointModelPZ,
     JointModelRevoluteUnaligned,
+    JointModelRevoluteUnboundedUnaligned,
+    JointModelRUBX,
+    JointModelRUBY,
+    JointModelRUBZ,
     JointModelRX,
     JointModelRY,
     JointModelRZ,

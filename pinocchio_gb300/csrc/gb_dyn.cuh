@@ -104,15 +104,26 @@ template <class S> GB_HD void joint_params(int jt, S x, S* s, S* c) {
     ssincos(x, s, c);
   }
 }
-// joint_params from the FP64 configuration value; a double-float revolute angle
-// takes sincos_df (no FP64 sincos)
-template <class S> GB_HD void joint_params_q(int jt, double x, S* s, S* c) { joint_params(jt, S(x), s, c); }
-template <> GB_HD void joint_params_q<dfloat>(int jt, double x, dfloat* s, dfloat* c) {
-  if (jt_slides(jt)) {
-    *s = dfloat(x);
+// joint_params from the FP64 configuration q[iq]; a double-float revolute angle takes
+// sincos_df (no FP64 sincos); an unbounded revolute joint's (cos, sin) = (q[iq], q[iq + 1]) are
+// taken as they are (JointModelRevoluteUnboundedTpl::calc, joint-revolute-unbounded.hpp:154-162)
+template <class S> GB_HD void joint_params_q(int jt, const In& q, int iq, S* s, S* c) {
+  if (jt_unbounded(jt)) {
+    *c = S(q[iq]);
+    *s = S(q[iq + 1]);
+  } else {
+    joint_params(jt, S(q[iq]), s, c);
+  }
+}
+template <> GB_HD void joint_params_q<dfloat>(int jt, const In& q, int iq, dfloat* s, dfloat* c) {
+  if (jt_unbounded(jt)) {
+    *c = dfloat(q[iq]);
+    *s = dfloat(q[iq + 1]);
+  } else if (jt_slides(jt)) {
+    *s = dfloat(q[iq]);
     *c = dfloat(1.0f);
   } else {
-    sincos_df(x, s, c);
+    sincos_df(q[iq], s, c);
   }
 }
 // liMi = placement * M_joint of a one-dof joint from its parameters
@@ -148,7 +159,7 @@ template <class S> GB_HD void joint_transform(const MView& m, int i, const In& q
     compose(Pl, J, X);
   } else {
     S s, c;
-    joint_params_q(jt, q[iq], &s, &c);
+    joint_params_q(jt, q, iq, &s, &c);
     compose_joint(P, P + 9, jt, c, s, X);
   }
 }
@@ -327,7 +338,7 @@ GB_HD void aba_one(const MView& m, const In& q, const In& v, const In& tau, cons
       joint_transform(m, i, q, X);
     } else {
       S sn, cn;
-      joint_params_q(jt, q[m.idx_q[i]], &sn, &cn);
+      joint_params_q(jt, q, m.idx_q[i], &sn, &cn);
       const S* P = ModelScalar<S>::place(m, i);
       compose_joint(P, P + 9, jt, cn, sn, X);
       if (!kStoreX) { cs[i][0] = sn; cs[i][1] = cn; }
@@ -842,6 +853,17 @@ GB_HD void integrate_one(const MView& m, const In& q, const In& v, const Out& qo
     const int iq = m.idx_q[i], iv = m.idx_v[i];
     if (jt_three(m.jtype[i])) {
       integrate_three(m.jtype[i], q, v, iq, iv, qo);
+      continue;
+    }
+    if (jt_unbounded(m.jtype[i])) {  // SpecialOrthogonalOperationTpl<2>::integrate
+      // (liegroup/special-orthogonal.hpp:164-185): (cos, sin) turned by v, then the
+      // first-order renormalisation (3 - |z|^2) / 2
+      double sw, cw;
+      sincos(v[iv], &sw, &cw);
+      const double c = cw * q[iq] - sw * q[iq + 1], s = sw * q[iq] + cw * q[iq + 1];
+      const double f = (3.0 - (c * c + s * s)) / 2.0;
+      qo[iq] = c * f;
+      qo[iq + 1] = s * f;
       continue;
     }
     if (m.jtype[i] != JT_FF) {

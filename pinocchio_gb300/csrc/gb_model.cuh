@@ -20,15 +20,20 @@
 namespace gb {
 
 // JT_SPH / JT_PL: spherical (quaternion q, angular velocity v in the joint frame) and planar
-// ((x, y, cos, sin), (vx, vy, wz) in the joint frame) joints, the C ABI's values
-enum { JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7, JT_SPH = 11, JT_PL = 12 };
+// ((x, y, cos, sin), (vx, vy, wz) in the joint frame) joints; JT_RUX / JT_RUY / JT_RUZ: unbounded
+// revolute joints (q = (cos, sin) of the angle, nq 2, nv 1); the C ABI's values
+enum {
+  JT_NONE = 0, JT_RX = 1, JT_RY = 2, JT_RZ = 3, JT_FF = 4, JT_PX = 5, JT_PY = 6, JT_PZ = 7, JT_SPH = 11, JT_PL = 12,
+  JT_RUX = 13, JT_RUY = 14, JT_RUZ = 15
+};
 
-// One-dof joints (revolute RX/RY/RZ, prismatic PX/PY/PZ): the coordinate axis,
-// whether the joint slides along it, and its entry of the motion subspace S
+// One-dof joints (revolute RX/RY/RZ, prismatic PX/PY/PZ, unbounded revolute RUX/RUY/RUZ): the
+// coordinate axis, whether the joint slides along it, and its entry of the motion subspace S
 // (3 + axis, angular, for a revolute joint; axis, linear, for a prismatic one).
 GB_HD bool jt_slides(int jt) { return jt >= JT_PX && jt <= JT_PZ; }
-GB_HD int jt_axis(int jt) { return jt >= JT_PX ? jt - JT_PX : jt - JT_RX; }
-GB_HD int jt_sidx(int jt) { return jt >= JT_PX ? jt - JT_PX : jt + 2; }
+GB_HD bool jt_unbounded(int jt) { return jt >= JT_RUX && jt <= JT_RUZ; }
+GB_HD int jt_axis(int jt) { return jt >= JT_RUX ? jt - JT_RUX : jt >= JT_PX ? jt - JT_PX : jt - JT_RX; }
+GB_HD int jt_sidx(int jt) { return jt >= JT_RUX ? jt - JT_RUX + 3 : jt >= JT_PX ? jt - JT_PX : jt + 2; }
 // Every supported joint's motion subspace is made of unit spatial axes of its frame:
 // jt_nv(jt) dofs, dof k along spatial axis jt_col(jt, k) ([linear; angular] index):
 // the free-flyer all six (joint-free-flyer.hpp), the spherical joint the angular three

@@ -77,7 +77,9 @@ inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err)
   M->has_fix = false;
   for (int i = 1; i < nj; ++i) {
     const int jt = M->jtype[i];
-    if (jt != GB_JOINT_REVOLUTE_UNALIGNED && jt != GB_JOINT_PRISMATIC_UNALIGNED) continue;
+    if (jt != GB_JOINT_REVOLUTE_UNALIGNED && jt != GB_JOINT_PRISMATIC_UNALIGNED &&
+        jt != GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED)
+      continue;
     if (!d->axis) {
       *err = "unaligned joints need gb_model_desc.axis";
       return GB_ERR_INVALID_ARGUMENT;
@@ -91,7 +93,9 @@ inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err)
     for (double& x : a) x /= n;
     double F[9];
     rotation_to_axis(a, F);
-    M->jtype[i] = jt == GB_JOINT_REVOLUTE_UNALIGNED ? GB_JOINT_RZ : GB_JOINT_PZ;
+    M->jtype[i] = jt == GB_JOINT_REVOLUTE_UNALIGNED ? GB_JOINT_RZ
+                  : jt == GB_JOINT_PRISMATIC_UNALIGNED ? GB_JOINT_PZ
+                                                       : GB_JOINT_RUBZ;
     double* P = &M->placement[12 * (size_t)i];  // R <- R F
     double R[9];
     std::memcpy(R, P, sizeof(R));
@@ -134,7 +138,8 @@ inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err)
 // the caller's joint of internal joint i (-1 for the two intermediate ones), last_of[j] the
 // internal joint carrying the caller's joint j.
 static_assert((int)GB_JOINT_SPHERICAL == (int)gb::JT_SPH && (int)GB_JOINT_PLANAR == (int)gb::JT_PL &&
-                  (int)GB_JOINT_FREEFLYER == (int)gb::JT_FF,
+                  (int)GB_JOINT_FREEFLYER == (int)gb::JT_FF && (int)GB_JOINT_RUBX == (int)gb::JT_RUX &&
+                  (int)GB_JOINT_RUBY == (int)gb::JT_RUY && (int)GB_JOINT_RUBZ == (int)gb::JT_RUZ,
               "the kernels use the C ABI's joint codes");
 struct ExpandedTree {
   std::vector<int> parents, jtype, user_of, last_of;
@@ -213,7 +218,8 @@ inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
   for (int i = 1; i < nj; ++i) {
     const int jt = M->jtype[i], p = M->parents[i];
     const bool three = jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR;
-    if (!three && (jt < GB_JOINT_RX || jt > GB_JOINT_PRISMATIC_UNALIGNED))
+    const bool unbounded = jt >= GB_JOINT_RUBX && jt <= GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED;
+    if (!three && !unbounded && (jt < GB_JOINT_RX || jt > GB_JOINT_PRISMATIC_UNALIGNED))
       return set_error(GB_ERR_UNSUPPORTED, "joint " + std::to_string(i) + ": unsupported joint type");
     if (p < 0 || p >= i) return set_error(GB_ERR_INVALID_ARGUMENT, "parents[i] must satisfy 0 <= parents[i] < i");
     if (jt == GB_JOINT_FREEFLYER) {
@@ -224,7 +230,7 @@ inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
     M->idx_q[i] = nq;
     M->idx_v[i] = nv;
     M->nvs[i] = jt == GB_JOINT_FREEFLYER ? 6 : three ? 3 : 1;
-    nq += jt == GB_JOINT_FREEFLYER ? 7 : three ? 4 : 1;
+    nq += jt == GB_JOINT_FREEFLYER ? 7 : three ? 4 : unbounded ? 2 : 1;
     M->has_three = M->has_three || three;
     nv += M->nvs[i];
     M->depth[i] = M->depth[p] + 1;

@@ -209,7 +209,7 @@ __device__ void aba_warp_one(const gb::MView& m, const gb::In& q, const gb::In& 
       joint_transform(m, i, q, X[i]);
     } else {
       S sn, cn;
-      joint_params_q(m.jtype[i], q[m.idx_q[i]], &sn, &cn);
+      joint_params_q(m.jtype[i], q, m.idx_q[i], &sn, &cn);
       const S* P = ModelScalar<S>::place(m, i);
       compose_joint(P, P + 9, m.jtype[i], cn, sn, X[i]);
     }

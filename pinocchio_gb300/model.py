@@ -10,7 +10,8 @@ free-flyer) and flattens the tree into the plain tables the C ABI takes:
 
 * ``parents`` (int32, njoints), ``jtype`` (int32, njoints; 0 = universe,
   1/2/3 = RX/RY/RZ, 4 = free-flyer, 5/6/7 = PX/PY/PZ, 8 = revolute unaligned,
-  9 = prismatic unaligned),
+  9 = prismatic unaligned, 10 = translation, 11 = spherical, 12 = planar, 13/14/15 = unbounded
+  revolute RUBX/RUBY/RUBZ, 16 = unbounded revolute unaligned),
 * ``axis`` (njoints x 3: the unit axis of an unaligned joint, zero otherwise),
 * ``placement`` (njoints x 12: rotation row-major, then translation),
 * ``inertia`` (njoints x 10: mass, lever (COM), rotational inertia about the COM
@@ -21,10 +22,12 @@ from __future__ import annotations
 
 import numpy as np
 
-JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU, JT_TR, JT_SPH, JT_PL = range(13)
+(JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU, JT_TR, JT_SPH, JT_PL, JT_RUBX, JT_RUBY,
+ JT_RUBZ, JT_RUBU) = range(17)
 _ONE_DOF = (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)
-_JT_NQ = {JT_NONE: 0, JT_FF: 7, JT_TR: 3, JT_SPH: 4, JT_PL: 4, **{j: 1 for j in _ONE_DOF}}
-_JT_NV = {JT_NONE: 0, JT_FF: 6, JT_TR: 3, JT_SPH: 3, JT_PL: 3, **{j: 1 for j in _ONE_DOF}}
+UNBOUNDED = (JT_RUBX, JT_RUBY, JT_RUBZ, JT_RUBU)
+_JT_NQ = {JT_NONE: 0, JT_FF: 7, JT_TR: 3, JT_SPH: 4, JT_PL: 4, **{j: 1 for j in _ONE_DOF}, **{j: 2 for j in UNBOUNDED}}
+_JT_NV = {JT_NONE: 0, JT_FF: 6, JT_TR: 3, JT_SPH: 3, JT_PL: 3, **{j: 1 for j in _ONE_DOF + UNBOUNDED}}
 PRISMATIC = (JT_PX, JT_PY, JT_PZ, JT_PU)
 
 
@@ -97,6 +100,22 @@ class JointModelPlanar(JointModel):
     jtype = JT_PL
 
 
+class JointModelRUBX(JointModel):
+    """Unbounded revolute joint about x: q = (cos theta, sin theta), taken as given (reference
+    JointModelRevoluteUnboundedTpl, multibody/joint/joint-revolute-unbounded.hpp); what the URDF
+    parser makes of a ``continuous`` joint."""
+
+    jtype = JT_RUBX
+
+
+class JointModelRUBY(JointModel):
+    jtype = JT_RUBY
+
+
+class JointModelRUBZ(JointModel):
+    jtype = JT_RUBZ
+
+
 def _unit(axis) -> np.ndarray:
     a = np.asarray(axis, dtype=np.float64).reshape(3)
     n = float(np.linalg.norm(a))
@@ -109,6 +128,16 @@ class JointModelRevoluteUnaligned(JointModel):
     """Revolute joint about a unit axis of its frame (reference JointModelRevoluteUnalignedTpl)."""
 
     jtype = JT_RU
+
+    def __init__(self, axis):
+        self.axis = _unit(axis)
+
+
+class JointModelRevoluteUnboundedUnaligned(JointModel):
+    """Unbounded revolute joint about a unit axis of its frame, q = (cos theta, sin theta)
+    (reference JointModelRevoluteUnboundedUnalignedTpl)."""
+
+    jtype = JT_RUBU
 
     def __init__(self, axis):
         self.axis = _unit(axis)
@@ -293,8 +322,16 @@ class Model:
                     raise ValueError("joints are not in depth-first order")
 
     def neutral(self) -> np.ndarray:
+        """The identity configuration (reference neutral(model), liegroup neutral elements): unit
+        quaternions (0, 0, 0, 1), planar and unbounded angles (cos, sin) = (1, 0), zero elsewhere."""
         q = np.zeros(self.nq)
-        for i, (jt, iq) in enumerate(zip(self.jtypes, self.idx_qs)):
+        for jt, iq in zip(self.jtypes, self.idx_qs):
             if jt == JT_FF:
                 q[iq + 6] = 1.0
+            elif jt == JT_SPH:
+                q[iq + 3] = 1.0
+            elif jt == JT_PL:
+                q[iq + 2] = 1.0
+            elif jt in UNBOUNDED:
+                q[iq] = 1.0
         return q

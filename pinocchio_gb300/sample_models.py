@@ -33,6 +33,7 @@ from .model import (
     JT_SPH,
     JT_TR,
     PRISMATIC,
+    UNBOUNDED,
     Inertia,
     JointModelFreeFlyer,
     JointModelPX,
@@ -40,6 +41,10 @@ from .model import (
     JointModelPZ,
     JointModelPrismaticUnaligned,
     JointModelRevoluteUnaligned,
+    JointModelRevoluteUnboundedUnaligned,
+    JointModelRUBX,
+    JointModelRUBY,
+    JointModelRUBZ,
     JointModelRX,
     JointModelRY,
     JointModelRZ,
@@ -103,6 +108,17 @@ def _random_any_axis(rng: np.random.Generator):
         return _ONE_DOF[3 + int(rng.integers(0, 3))]()
     axis = rng.standard_normal(3)
     return (JointModelRevoluteUnaligned if k == 2 else JointModelPrismaticUnaligned)(axis / np.linalg.norm(axis))
+
+
+def _random_unbounded(rng: np.random.Generator):
+    """An unbounded revolute joint about x, y, z or a random axis, or (one in five) a revolute one."""
+    k = int(rng.integers(0, 5))
+    if k < 3:
+        return (JointModelRUBX, JointModelRUBY, JointModelRUBZ)[k]()
+    if k == 3:
+        axis = rng.standard_normal(3)
+        return JointModelRevoluteUnboundedUnaligned(axis / np.linalg.norm(axis))
+    return _random_revolute(rng)
 
 
 def _add_link(model: Model, rng, parent: int, joint, name: str, mass_range=(0.5, 5.0)) -> int:
@@ -203,6 +219,14 @@ def unaligned_tree(nv: int = 14, free_flyer: bool = False, seed: int = 7) -> Mod
     return model
 
 
+def unbounded_tree(nv: int = 15, free_flyer: bool = True, seed: int = 11) -> Model:
+    """``random_tree`` whose joints are mostly unbounded revolute joints (JointModelRUBX/Y/Z and
+    the unaligned form, q = (cos, sin)): what URDF ``continuous`` joints give."""
+    model = random_tree(nv, free_flyer, seed, joint=_random_unbounded)
+    model.name = f"unboundedtree{nv}{'ff' if free_flyer else ''}"
+    return model
+
+
 def translation_tree(seed: int = 9) -> Model:
     """A tree with translation joints (JointModelTranslation) at the root, inside a chain and at
     a leaf, among revolute and prismatic joints: nv 14."""
@@ -265,7 +289,8 @@ def heterogeneous_trees(seed: int = 3):
 # ---------------------------------------------------------------------------------------------
 def random_configurations(model: Model, batch: int, rng: np.random.Generator) -> np.ndarray:
     """q of shape (batch, nq): FF position N(0,1), uniform unit quaternion; revolute angles
-    U[-pi, pi]; prismatic displacements U[-0.5, 0.5] m."""
+    U[-pi, pi] (unbounded revolute joints: their cos and sin); prismatic displacements
+    U[-0.5, 0.5] m."""
     q = np.empty((batch, model.nq))
     for jt, iq in zip(model.jtypes[1:], model.idx_qs[1:]):
         if jt == JT_FF:
@@ -282,6 +307,10 @@ def random_configurations(model: Model, batch: int, rng: np.random.Generator) ->
             q[:, iq + 3] = np.sin(th)
         elif jt in PRISMATIC:
             q[:, iq] = rng.uniform(-0.5, 0.5, batch)
+        elif jt in UNBOUNDED:
+            th = rng.uniform(-np.pi, np.pi, batch)
+            q[:, iq] = np.cos(th)
+            q[:, iq + 1] = np.sin(th)
         else:
             q[:, iq] = rng.uniform(-np.pi, np.pi, batch)
     return q

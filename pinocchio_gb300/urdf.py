@@ -12,11 +12,11 @@ root link, as the reference's ``buildModel(filename, root_joint, model)`` does.
 
 Joint axes map as in the reference (UrdfVisitor::addJoint and extractCartesianAxis,
 include/pinocchio/parsers/urdf/model.hxx:438-576): an axis equal to the unit x, y or z axis (to a
-relative 1e-12) gives JointModelRX/RY/RZ (``revolute``, ``continuous``) or JointModelPX/PY/PZ
-(``prismatic``); any other axis, negative ones included, gives JointModelRevoluteUnaligned /
-JointModelPrismaticUnaligned with the normalised axis.  One difference: the reference makes a
-``continuous`` joint a JointModelRevoluteUnbounded (nq = 2, q = (cos, sin)); here it is the bounded
-revolute joint (nq = 1, q = the angle), with the same dynamics in the angle.  ``planar`` gives
+relative 1e-12) gives JointModelRX/RY/RZ (``revolute``), JointModelRUBX/RUBY/RUBZ (``continuous``:
+the unbounded revolute joint, nq = 2, q = (cos, sin)) or JointModelPX/PY/PZ (``prismatic``); any
+other axis, negative ones included, gives JointModelRevoluteUnaligned /
+JointModelRevoluteUnboundedUnaligned / JointModelPrismaticUnaligned with the normalised axis.
+``planar`` gives
 JointModelPlanar (motion in the joint frame's xy plane, the axis ignored, as the reference's
 UrdfVisitor::addJointAndBody, model.hxx:285-290); ``floating`` gives the free-flyer on the root
 link (the kernels run the free-flyer as the root joint only; a ``floating`` joint inside the tree
@@ -43,12 +43,17 @@ from .model import (
     JT_RX,
     JT_RY,
     JT_RZ,
+    JT_RUBX,
+    JT_RUBY,
+    JT_RUBZ,
+    JT_RUBU,
     Inertia,
     JointModel,
     JointModelFreeFlyer,
     JointModelPlanar,
     JointModelPrismaticUnaligned,
     JointModelRevoluteUnaligned,
+    JointModelRevoluteUnboundedUnaligned,
     Model,
     SE3,
 )
@@ -99,8 +104,9 @@ def _link_inertia(link) -> Inertia:
     return Inertia(mass, np.zeros(3), I).se3_action(_origin(inertial))
 
 
-_AXIS_JT = {"revolute": (JT_RX, JT_RY, JT_RZ), "continuous": (JT_RX, JT_RY, JT_RZ), "prismatic": (JT_PX, JT_PY, JT_PZ)}
-_UNALIGNED = {"revolute": JointModelRevoluteUnaligned, "continuous": JointModelRevoluteUnaligned,
+_AXIS_JT = {"revolute": (JT_RX, JT_RY, JT_RZ), "continuous": (JT_RUBX, JT_RUBY, JT_RUBZ),
+            "prismatic": (JT_PX, JT_PY, JT_PZ)}
+_UNALIGNED = {"revolute": JointModelRevoluteUnaligned, "continuous": JointModelRevoluteUnboundedUnaligned,
               "prismatic": JointModelPrismaticUnaligned}
 
 
@@ -210,6 +216,8 @@ def load_model(path: str) -> Model:
                 joint = JointModelRevoluteUnaligned(axis[i])
             elif jt == JT_PU:
                 joint = JointModelPrismaticUnaligned(axis[i])
+            elif jt == JT_RUBU:
+                joint = JointModelRevoluteUnboundedUnaligned(axis[i])
             else:
                 joint = _OneDof(jt)
             if jt == JT_NONE:

@@ -8,6 +8,8 @@ restated here against the oracle (reference file:line on each test):
   (unittest/rnea-derivatives.cpp:113-314, unittest/aba-derivatives.cpp:23-155),
   batch == serial bit-exact (unittest/parallel-aba.cpp:21-55, unittest/parallel-rnea.cpp:78-112).
 """
+import copy
+
 import numpy as np
 import pytest
 
@@ -17,7 +19,7 @@ from pinocchio_gb300 import sample_models as sm
 from util import MODELS, ORACLE_ONLY_MODELS, rel_err
 
 CPU_MODELS = ["manipulator6r", "humanoid32", "tree12", "tree60ff", "chain100", "mixedtree12", "mixedtree24ff",
-              "unaligned14", "unaligned20ff", "translationtree14", "multidoftree16"]
+              "unaligned14", "unaligned20ff", "translationtree14", "multidoftree16", "unbounded15ff"]
 
 
 @pytest.fixture(scope="module", params=CPU_MODELS)
@@ -94,7 +96,7 @@ def _fd(f, x0, h, k, integrate=None):
 
 
 @pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree12", "mixedtree24ff", "unaligned20ff",
-                                  "translationtree14", "multidoftree16"])
+                                  "translationtree14", "multidoftree16", "unbounded15ff"])
 def test_derivatives_vs_central_fd(name):
     model = {**MODELS, **ORACLE_ONLY_MODELS}[name]()
     om = OracleModel(model)
@@ -115,6 +117,45 @@ def test_derivatives_vs_central_fd(name):
     assert rel_err(adq, fd["aq"]) < 1e-6
     assert rel_err(adv, fd["av"]) < 1e-6
     assert rel_err(Minv, fd["at"]) < 1e-6
+
+
+def test_unbounded_revolute_is_the_revolute_joint_in_its_angle():
+    """An unbounded revolute joint at q = (cos t, sin t) (joint-revolute-unbounded.hpp) has the
+    dynamics of the revolute joint about the same axis at t, in every function and derivative
+    (both have nv = 1 and the same motion subspace); its integrate is the rotation of the unit
+    complex by v with the first-order renormalisation (special-orthogonal.hpp:164-185)."""
+    mu = MODELS["unbounded15ff"]()
+    mr = copy.deepcopy(mu)
+    to_rev = {gm.JT_RUBX: gm.JT_RX, gm.JT_RUBY: gm.JT_RY, gm.JT_RUBZ: gm.JT_RZ, gm.JT_RUBU: gm.JT_RU}
+    mr.jtypes = [to_rev.get(j, j) for j in mu.jtypes]
+    assert mr.nv == mu.nv and mu.nq == mr.nq + sum(j in to_rev for j in mu.jtypes)
+    ou, orv = OracleModel(mu), OracleModel(mr)
+    qu, v, a = sm.random_inputs(mu, 16, 21)
+    qr = np.zeros((16, mr.nq))
+    for i in range(1, mu.njoints):
+        iqu, iqr, n = mu.idx_qs[i], mr.idx_qs[i], mr.nqs[i]
+        if mu.jtypes[i] in to_rev:
+            qr[:, iqr] = np.arctan2(qu[:, iqu + 1], qu[:, iqu])
+        else:
+            qr[:, iqr : iqr + n] = qu[:, iqu : iqu + n]
+    tau = orv.rnea(qr, v, a)
+    assert rel_err(ou.rnea(qu, v, a), tau) < 1e-12
+    for conv in (LOCAL, WORLD):
+        assert rel_err(ou.aba(qu, v, tau, conv), orv.aba(qr, v, tau, conv)) < 1e-12
+    assert rel_err(ou.crba(qu), orv.crba(qr)) < 1e-12
+    for x, y in zip(ou.rnea_derivatives(qu, v, a), orv.rnea_derivatives(qr, v, a)):
+        assert rel_err(x, y) < 1e-12
+    for x, y in zip(ou.aba_derivatives(qu, v, tau), orv.aba_derivatives(qr, v, tau)):
+        assert rel_err(x, y) < 1e-11
+    # integrate: (cos, sin) turned by v and renormalised to first order
+    qn = ou.integrate(qu, v)
+    for ju, iqu, ivu in zip(mu.jtypes[1:], mu.idx_qs[1:], mu.idx_vs[1:]):
+        if ju in to_rev:
+            c, s_ = qu[:, iqu], qu[:, iqu + 1]
+            cw, sw = np.cos(v[:, ivu]), np.sin(v[:, ivu])
+            z = np.stack([cw * c - sw * s_, sw * c + cw * s_], axis=1)
+            z *= ((3.0 - (z * z).sum(axis=1)) / 2.0)[:, None]
+            assert np.allclose(qn[:, iqu : iqu + 2], z, rtol=0, atol=1e-15)
 
 
 def test_batch_equals_serial():

@@ -109,19 +109,26 @@ _TWO_LINK = """<robot name="two">
 </robot>"""
 
 
+def _unbounded_q(theta, rest):
+    return np.concatenate([np.cos(theta)[:, None], np.sin(theta)[:, None], rest], axis=1)
+
+
 def test_urdf_fixed_joint_and_negative_axis():
     """A fixed joint merges its link into the parent body and carries its origin to
-    the next joint; an axis -z gives the +z joint's dynamics with that joint's
-    coordinate negated (tau_-(q, v, a) = D tau_+(D q, D v, D a), D = diag(-1, 1))."""
+    the next joint; the continuous shoulder is an unbounded revolute joint (q = (cos, sin),
+    as the reference's JointModelRUBZ); an axis -z gives the +z joint's dynamics with that joint's
+    angle negated (tau_-(q, v, a) = D tau_+(D q, D v, D a), D = diag(-1, 1))."""
     plus = pg.buildModelFromXML(_TWO_LINK.replace("AXIS", "0 1"))
     minus = pg.buildModelFromXML(_TWO_LINK.replace("AXIS", "0 -1"))
-    assert plus.njoints == 3 and plus.jtypes[1:] == [gm.JT_RZ, gm.JT_RX]
+    assert plus.njoints == 3 and plus.jtypes[1:] == [gm.JT_RUBZ, gm.JT_RX] and (plus.nq, plus.nv) == (3, 2)
+    assert minus.jtypes[1:] == [gm.JT_RUBU, gm.JT_RX]
     assert abs(plus.inertias[1].mass - 1.9) < 1e-15  # upper + tool
     rng = np.random.default_rng(1)
-    q, v, a = (rng.standard_normal((16, 2)) for _ in range(3))
+    th, qe = rng.uniform(-np.pi, np.pi, 16), rng.standard_normal((16, 1))
+    v, a = (rng.standard_normal((16, 2)) for _ in range(2))
     D = np.array([-1.0, 1.0])
-    tp = OracleModel(plus).rnea(q * D, v * D, a * D)
-    tm = OracleModel(minus).rnea(q, v, a)
+    tp = OracleModel(plus).rnea(_unbounded_q(-th, qe), v * D, a * D)
+    tm = OracleModel(minus).rnea(_unbounded_q(th, qe), v, a)
     assert rel_err(tm, tp * D) < 1e-12
     # the same tree from the construction API: the tool merged into the shoulder body
     m = pg.Model()
@@ -133,7 +140,8 @@ def test_urdf_fixed_joint_and_negative_axis():
     elbow = pg.SE3(mount.rotation @ rpy(0, 0.5, 0), mount.rotation @ np.array([0, 0.02, -0.3]) + mount.translation)
     j2 = m.addJoint(j1, pg.JointModelRX(), elbow, "elbow")
     m.appendBodyToJoint(j2, pg.Inertia(0.8, [0, 0, -0.25], np.diag([0.01, 0.01, 0.004])))
-    assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(plus).rnea(q, v, a)) < 1e-12
+    q = np.concatenate([th[:, None], qe], axis=1)
+    assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(plus).rnea(_unbounded_q(th, qe), v, a)) < 1e-12
 
 
 def test_urdf_prismatic_negative_axis():
@@ -152,12 +160,14 @@ def test_urdf_prismatic_negative_axis():
 </robot>"""
     plus = pg.buildModelFromXML(doc.replace("AXIS", "1 0 0"))
     minus = pg.buildModelFromXML(doc.replace("AXIS", "-1 0 0"))
-    assert plus.jtypes[1:] == [gm.JT_PX, gm.JT_RY] and minus.jtypes[1:] == [gm.JT_PU, gm.JT_RY]
+    assert plus.jtypes[1:] == [gm.JT_PX, gm.JT_RUBY] and minus.jtypes[1:] == [gm.JT_PU, gm.JT_RUBY]
     rng = np.random.default_rng(2)
-    q, v, a = (rng.standard_normal((16, 2)) for _ in range(3))
+    x, th = rng.standard_normal((16, 1)), rng.uniform(-np.pi, np.pi, 16)
+    v, a = (rng.standard_normal((16, 2)) for _ in range(2))
     D = np.array([-1.0, 1.0])
-    tp = OracleModel(plus).rnea(q * D, v * D, a * D)
-    tm = OracleModel(minus).rnea(q, v, a)
+    hinge = _unbounded_q(th, np.zeros((16, 0)))
+    tp = OracleModel(plus).rnea(np.concatenate([-x, hinge], axis=1), v * D, a * D)
+    tm = OracleModel(minus).rnea(np.concatenate([x, hinge], axis=1), v, a)
     assert rel_err(tm, tp * D) < 1e-12
 
 

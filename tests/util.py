@@ -35,6 +35,7 @@ MODELS = {
     "unaligned20ff": lambda: sm.unaligned_tree(20, True, 8),
     "translationtree14": lambda: sm.translation_tree(9),
     "multidoftree16": lambda: sm.multidof_tree(10),
+    "unbounded15ff": lambda: sm.unbounded_tree(15, True, 11),
 }
 # models the oracle covers beyond the kernels (none at present)
 ORACLE_ONLY_MODELS = {}
@@ -46,7 +47,7 @@ MIXED_TOL = 1e-5
 # workload: their FP64 results meet FP64_TOL; their mixed-precision error, which scales with
 # each random model's conditioning, is held to 1e-4
 JOINT_TYPE_MODELS = ("mixedtree12", "mixedtree24ff", "unaligned14", "unaligned20ff", "translationtree14",
-                     "multidoftree16")
+                     "multidoftree16", "unbounded15ff")
 
 
 def mixed_tol(name: str) -> float:
