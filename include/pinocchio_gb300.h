@@ -94,7 +94,22 @@ typedef struct gb_pool gb_pool;
  * armature:  nv values (may be NULL for zeros); gravity: 6 values [lin; ang]
  *            (may be NULL for (0, 0, -9.81, 0, 0, 0), multibody/model.hxx:40).
  * axis:      njoints x 3, the axis of each unaligned joint (normalised on creation; the
- *            entries of other joints are ignored); may be NULL when there is none. */
+ *            entries of other joints are ignored); may be NULL when there is none.
+ * mimic:     njoints entries (may be NULL: no mimic joint): mimic[i] = j > 0 makes joint i a
+ *            mimic of joint j < i (JointModelMimic, multibody/joint/joint-mimic.hpp:557-760):
+ *            joint i keeps its own type, placement and body, adds no entry to q or v (nq and
+ *            nv count the other joints; nvExtended counts it too), and moves with
+ *            q_i = mimic_scaling[i] q_j + mimic_offset[i] (for an unbounded revolute joint:
+ *            its angle, atan2 of (sin, cos)), v_i = mimic_scaling[i] v_j; its torque adds to
+ *            joint j's (LinearAffineTransform / UnboundedRevoluteAffineTransform,
+ *            joint-common-operations.hpp:52-90).  Both joints are one-dof joints with the same
+ *            nq, joint j is no mimic itself.  Mimic joints are supported by rnea,
+ *            nonLinearEffects, computeGeneralizedGravity, crba (without the Cholesky factors),
+ *            forwardKinematics, computeJointJacobians (6 x nvExtended, the mimic joints' own
+ *            columns included, as the reference's data.J) and integrate; every other function
+ *            returns GB_ERR_UNSUPPORTED, as the reference rejects mimic joints in ABA, the
+ *            derivatives and the Cholesky (aba.hxx:250, rnea-derivatives.hxx:157,
+ *            cholesky.hxx:37).  armature has nv entries. */
 typedef struct {
   int njoints;
   const int* parents;
@@ -105,6 +120,9 @@ typedef struct {
   int nv_armature;
   const double* gravity;
   const double* axis;
+  const int* mimic;
+  const double* mimic_scaling;
+  const double* mimic_offset;
 } gb_model_desc;
 
 /* Replaces building a ModelTpl + DataTpl (multibody/model.hpp:98-220,
@@ -113,6 +131,8 @@ typedef struct {
 int gb_model_create(const gb_model_desc* desc, gb_model** out);
 int gb_model_destroy(gb_model* model);
 int gb_model_dims(const gb_model* model, int* nq, int* nv, int* njoints);
+/* nvExtended (multibody/model.hpp): nv plus one per mimic joint (= nv without mimic joints) */
+int gb_model_nv_extended(const gb_model* model, int* nv_extended);
 const char* gb_last_error(void);
 
 /* Numeric status of a model's kernels (bits of *flags), replacing the checks the

@@ -52,6 +52,10 @@ struct ModelTables {
   std::vector<double> armature;     // nv
   double gravity[6] = {0, 0, -9.81, 0, 0, 0};
   std::vector<double> axis;         // njoints x 3: axes of the unaligned joints (empty: none)
+  // mimic joints (gb_model_desc.mimic): per joint the joint it mimics (0: none), its scaling and
+  // offset; empty: none
+  std::vector<int> mimic;
+  std::vector<double> mimic_scaling, mimic_offset;
 };
 
 class Model {
@@ -67,13 +71,17 @@ class Model {
     d.nv_armature = static_cast<int>(t.armature.size());
     d.gravity = t.gravity;
     d.axis = t.axis.empty() ? nullptr : t.axis.data();
+    d.mimic = t.mimic.empty() ? nullptr : t.mimic.data();
+    d.mimic_scaling = t.mimic_scaling.empty() ? nullptr : t.mimic_scaling.data();
+    d.mimic_offset = t.mimic_offset.empty() ? nullptr : t.mimic_offset.data();
     gb_model* m = nullptr;
     check(gb_model_create(&d, &m));
     handle_.reset(m, [](gb_model* p) { gb_model_destroy(p); });
     check(gb_model_dims(m, &nq, &nv, &njoints));
+    check(gb_model_nv_extended(m, &nvExtended));
   }
   gb_model* get() const { return handle_.get(); }
-  int nq = 0, nv = 0, njoints = 0;
+  int nq = 0, nv = 0, njoints = 0, nvExtended = 0;
 
  private:
   std::shared_ptr<gb_model> handle_;

@@ -94,6 +94,8 @@ class OracleModel:
     def __init__(self, model):
         L = lib()
         t = model.tables()
+        if "mimic" in t and t["mimic"].any():
+            raise ValueError("a model with mimic joints: use MimicOracleModel")
         self._keep = t
         h = L.orc_model_new(
             int(len(t["parents"])), _ptr(t["parents"]), _ptr(t["jtype"]), _ptr(t["placement"]), _ptr(t["inertia"]),
@@ -320,3 +322,102 @@ def rollout_with_gradients(om, q0, v0, taus, dt=1e-3, nthreads=0):
         lv = lv + np.einsum("bk,bkc->bc", g, dv)
         gt[k] = np.einsum("bkc,bk->bc", Minv, g)
     return qT, vT, lq, lv, gt
+
+
+class _Tables:
+    def __init__(self, t):
+        self.t = t
+
+    def tables(self):
+        return self.t
+
+
+class MimicOracleModel:
+    """Models with mimic joints (reference JointModelMimic, multibody/joint/joint-mimic.hpp:557-760),
+    restated as the reference's own unit tests check them (unittest/rnea.cpp:350-420,
+    unittest/crba.cpp:131-170, utils/model-generator.hpp MimicTestCases): over the *full* model, in
+    which every mimic joint is a joint with its own dof, with q_full = toFull(q) (a mimic's
+    coordinate scaling * q + offset; an unbounded joint's angle, LinearAffineTransform /
+    UnboundedRevoluteAffineTransform, joint-common-operations.hpp:52-90) and v_full = G v:
+    tau = G^T (M_full G a + nle_full), M = G^T M_full G, the kinematics of the full model at
+    (toFull(q), G v, G a), data.J the full model's 6 x nvExtended Jacobian."""
+
+    def __init__(self, model):
+        t = {k: np.array(v, copy=True) for k, v in model.tables().items()}
+        self.model = model
+        self.mimic = [int(m) for m in t["mimic"]]
+        self.scaling, self.offset = t["mimic_scaling"], t["mimic_offset"]
+        nj = len(self.mimic)
+        unb = {13, 14, 15, 16}
+        full_nq = {0: 0, 4: 7, 10: 3, 11: 4, 12: 4, **{j: 2 for j in unb}}
+        full_nv = {0: 0, 4: 6, 10: 3, 11: 3, 12: 3}
+        jt = [int(j) for j in t["jtype"]]
+        self.fq = np.cumsum([0] + [full_nq.get(j, 1) for j in jt])[:-1]
+        self.fv = np.cumsum([0] + [full_nv.get(j, 1) for j in jt])[:-1]
+        self.nq_full = int(sum(full_nq.get(j, 1) for j in jt))
+        self.nv_full = int(sum(full_nv.get(j, 1) for j in jt))
+        self.rq, self.rv = model.idx_qs, model.idx_vs
+        self.nq, self.nv = model.nq, model.nv
+        self.jt, self.unb = jt, unb
+        G = np.zeros((self.nv_full, self.nv))
+        arm = np.zeros(self.nv_full)
+        for i in range(1, nj):
+            nvi = full_nv.get(jt[i], 1)
+            if self.mimic[i]:
+                G[self.fv[i], self.rv[self.mimic[i]]] = self.scaling[i]
+            else:
+                for k in range(nvi):
+                    G[self.fv[i] + k, self.rv[i] + k] = 1.0
+                    arm[self.fv[i] + k] = t["armature"][self.rv[i] + k]
+        self.G = G
+        t["mimic"][:] = 0
+        t["armature"] = arm
+        self.full = OracleModel(_Tables(t))
+
+    def to_full(self, q):
+        q = np.atleast_2d(np.asarray(q, dtype=np.float64))
+        out = np.zeros((q.shape[0], self.nq_full))
+        full_nq = lambda j: 7 if j == 4 else 3 if j == 10 else 4 if j in (11, 12) else 2 if j in self.unb else 1  # noqa: E731
+        for i in range(1, len(self.mimic)):
+            m, f = self.mimic[i], self.fq[i]
+            if not m:
+                n = full_nq(self.jt[i])
+                out[:, f : f + n] = q[:, self.rq[i] : self.rq[i] + n]
+            elif self.jt[i] in self.unb:
+                th = self.scaling[i] * np.arctan2(q[:, self.rq[m] + 1], q[:, self.rq[m]]) + self.offset[i]
+                out[:, f], out[:, f + 1] = np.cos(th), np.sin(th)
+            else:
+                out[:, f] = self.scaling[i] * q[:, self.rq[m]] + self.offset[i]
+        return out
+
+    def _gv(self, v):
+        return np.atleast_2d(np.asarray(v, dtype=np.float64)) @ self.G.T
+
+    def crba(self, q):
+        """The symmetric reduced joint-space inertia G^T M_full G."""
+        Mf = symmetrize_upper(self.full.crba(self.to_full(q)))
+        return np.einsum("ki,bkl,lj->bij", self.G, Mf, self.G)
+
+    def rnea(self, q, v, a, fext=None):
+        if fext is not None:
+            return self.full.rnea(self.to_full(q), self._gv(v), self._gv(a), fext=fext) @ self.G
+        qf, vf = self.to_full(q), self._gv(v)
+        Mf = symmetrize_upper(self.full.crba(qf))
+        nle = self.full.rnea(qf, vf, np.zeros_like(vf))
+        return np.einsum("ki,bkl,bl->bi", self.G, Mf, self._gv(a)) + nle @ self.G
+
+    def forward_kinematics(self, q, v=None, a=None):
+        return self.full.forward_kinematics(self.to_full(q), None if v is None else self._gv(v),
+                                            None if a is None else self._gv(a))
+
+    def joint_jacobians(self, q):
+        return self.full.joint_jacobians(self.to_full(q))
+
+    def integrate(self, q, v):
+        qf = self.full.integrate(self.to_full(q), self._gv(v))
+        out = np.zeros((qf.shape[0], self.nq))
+        for i in range(1, len(self.mimic)):
+            if not self.mimic[i]:
+                n = self.model.nqs[i]
+                out[:, self.rq[i] : self.rq[i] + n] = qf[:, self.fq[i] : self.fq[i] + n]
+        return out

@@ -16,6 +16,7 @@ from .model import (  # noqa: F401
     JointModelPZ,
     JointModelRevoluteUnaligned,
     JointModelRevoluteUnboundedUnaligned,
+    JointModelMimic,
     JointModelRUBX,
     JointModelRUBY,
     JointModelRUBZ,

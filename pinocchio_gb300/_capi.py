@@ -31,6 +31,7 @@ EXPORTS = (
     "gb_model_create",
     "gb_model_destroy",
     "gb_model_dims",
+    "gb_model_nv_extended",
     "gb_last_error",
     "gb_numeric_status",
     "gb_pipeline_timeouts",
@@ -103,6 +104,9 @@ class ModelDesc(C.Structure):
         ("nv_armature", C.c_int),
         ("gravity", C.c_void_p),
         ("axis", C.c_void_p),
+        ("mimic", C.c_void_p),
+        ("mimic_scaling", C.c_void_p),
+        ("mimic_offset", C.c_void_p),
     ]
 
 
@@ -146,6 +150,10 @@ def make_desc(tables: dict) -> tuple[ModelDesc, dict]:
     d.nv_armature = len(keep["armature"])
     d.gravity = keep["gravity"].ctypes.data
     d.axis = keep["axis"].ctypes.data if "axis" in keep else None
+    if "mimic" in keep and keep["mimic"].any():
+        d.mimic = keep["mimic"].ctypes.data
+        d.mimic_scaling = keep["mimic_scaling"].ctypes.data
+        d.mimic_offset = keep["mimic_offset"].ctypes.data
     return d, keep
 
 
@@ -171,6 +179,7 @@ def lib():
         L.gb_model_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(vp)]
         L.gb_model_destroy.argtypes = [vp]
         L.gb_model_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
+        L.gb_model_nv_extended.argtypes = [vp, C.POINTER(i)]
         L.gb_pipeline_timeouts.argtypes = [C.POINTER(C.c_uint), i]
         L.gb_numeric_status.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.gb_pipeline_wait_selftest.argtypes = [C.c_uint, vp]

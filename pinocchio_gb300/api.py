@@ -283,9 +283,10 @@ def forwardKinematics(model: Model, data: Data, q, v=None, a=None):
 
 def computeJointJacobians(model: Model, data: Data, q):
     """data.J = computeJointJacobians(model, data, q) (reference algorithm/jacobian.hxx:17-95):
-    (batch, 6, nv), column k the world-frame motion subspace of dof k about the world origin."""
+    (batch, 6, nvExtended), column k the world-frame motion subspace of dof k about the world
+    origin (with mimic joints, data.J has their own columns too: nvExtended = nv + their count)."""
     qt, was_np, vec = _as_batch(q, model.nq, "q")
-    B, nv = qt.shape[0], model.nv
+    B, nv = qt.shape[0], model.nvExtended
     Jc = _torch().empty((B, nv, 6), dtype=qt.dtype, device=qt.device)  # column-major 6 x nv
     _capi.check(
         _capi.lib().gb_compute_joint_jacobians(

@@ -29,13 +29,20 @@ int check_ptr(const void* p, const char* name) {
     return set_error(GB_ERR_INVALID_ARGUMENT, std::string(name) + " is not 8-byte aligned");
   return GB_OK;
 }
-int check_common(const gb_model* m, int precision, int layout, long batch) {
+int check_common_mimic(const gb_model* m, int precision, int layout, long batch) {
   if (m == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
   if (precision != GB_FP64 && precision != GB_MIXED) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown precision");
   if (layout != GB_LAYOUT_INSTANCE && layout != GB_LAYOUT_SOA)
     return set_error(GB_ERR_INVALID_ARGUMENT, "unknown layout");
   if (batch < 0) return set_error(GB_ERR_SIZE, "batch must be >= 0");
   return GB_OK;
+}
+// the reference rejects mimic joints outside RNEA, CRBA and the kinematics (MimicChecker:
+// aba.hxx:250, rnea-derivatives.hxx:157, cholesky.hxx:37)
+int check_common(const gb_model* m, int precision, int layout, long batch) {
+  const int rc = check_common_mimic(m, precision, layout, batch);
+  if (rc == GB_OK && m->has_mimic) return set_error(GB_ERR_UNSUPPORTED, "Function does not support mimic joints");
+  return rc;
 }
 
 }  // namespace gbi
@@ -69,8 +76,22 @@ int gb_model_create(const gb_model_desc* desc, gb_model** out) {
     delete M;
     return gbi::cuda_error(e, "gb_model_create");
   }
+  if (M->has_mimic) {
+    const size_t qb = sizeof(gb::MimicQ) * M->qmap.size(), vb = sizeof(gb::MimicV) * M->vmap.size();
+    e = cudaMalloc(&M->d_mimic, qb + vb);
+    if (e == cudaSuccess) e = cudaMemcpy(M->d_mimic, M->qmap.data(), qb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(static_cast<unsigned char*>(M->d_mimic) + qb, M->vmap.data(), vb, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      if (M->d_mimic) cudaFree(M->d_mimic);
+      cudaFree(M->d_blob);
+      delete M;
+      return gbi::cuda_error(e, "gb_model_create");
+    }
+  }
   rc = gbi::prepare_model_launches(M);
   if (rc != GB_OK) {
+    if (M->d_mimic) cudaFree(M->d_mimic);
     cudaFree(M->d_blob);
     delete M;
     return rc;
@@ -82,6 +103,7 @@ int gb_model_create(const gb_model_desc* desc, gb_model** out) {
 int gb_model_destroy(gb_model* M) {
   if (!M) return GB_OK;
   if (M->d_blob) cudaFree(M->d_blob);
+  if (M->d_mimic) cudaFree(M->d_mimic);
   delete M;
   return GB_OK;
 }
@@ -111,9 +133,15 @@ int gb_memcpy_async(void* dst, const void* src, size_t bytes, void* stream) {
 
 int gb_model_dims(const gb_model* M, int* nq, int* nv, int* nj) {
   if (!M) return set_error(GB_ERR_INVALID_ARGUMENT, "model is NULL");
-  if (nq) *nq = M->nq;
-  if (nv) *nv = M->nv;
+  if (nq) *nq = M->nq_red;
+  if (nv) *nv = M->nv_red;
   if (nj) *nj = M->nj_user;
+  return GB_OK;
+}
+
+int gb_model_nv_extended(const gb_model* M, int* nv_extended) {
+  if (!M || !nv_extended) return set_error(GB_ERR_INVALID_ARGUMENT, "model/nv_extended is NULL");
+  *nv_extended = M->nv;
   return GB_OK;
 }
 
@@ -125,23 +153,25 @@ int gb_model_dims(const gb_model* M, int* nq, int* nv, int* nj) {
 
 int gb_rnea(const gb_model* M, int precision, int layout, long B, const double* q, const double* v, const double* a,
             double* tau, void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(a, "a"));
   GB_TRY(gbi::check_ptr(tau, "tau"));
-  return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
-                          gbi::arr(a, layout, B, M->nv), gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
+  return (M->has_mimic ? gbi::launch_rnea_mimic : gbi::launch_rnea)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), gbi::arr(v, layout, B, M->nv_red),
+      gbi::arr(a, layout, B, M->nv_red), gbi::arr(tau, layout, B, M->nv_red), (cudaStream_t)stream);
 }
 
 int gb_rnea_fext(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                  const double* a, const double* fext, double* tau, void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(a, "a"));
   GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(tau, "tau"));
-  return gbi::launch_rnea_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
-                               gbi::arr(a, layout, B, M->nv), gbi::arr(fext, layout, B, 6L * M->nj_user),
-                               gbi::arr(tau, layout, B, M->nv), (cudaStream_t)stream);
+  return (M->has_mimic ? gbi::launch_rnea_fext_mimic : gbi::launch_rnea_fext)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), gbi::arr(v, layout, B, M->nv_red),
+      gbi::arr(a, layout, B, M->nv_red), gbi::arr(fext, layout, B, 6L * M->nj_user),
+      gbi::arr(tau, layout, B, M->nv_red), (cudaStream_t)stream);
 }
 
 // nonLinearEffects = rnea(q, v, 0) and computeGeneralizedGravity = rnea(q, 0, 0)
@@ -154,29 +184,32 @@ static gbi::Arr zero_arr(const gb_model* M) {
 
 int gb_nonlinear_effects(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                          double* nle, void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(nle, "nle"));
-  return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv), zero_arr(M),
-                          gbi::arr(nle, layout, B, M->nv), (cudaStream_t)stream);
+  return (M->has_mimic ? gbi::launch_rnea_mimic : gbi::launch_rnea)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), gbi::arr(v, layout, B, M->nv_red), zero_arr(M),
+      gbi::arr(nle, layout, B, M->nv_red), (cudaStream_t)stream);
 }
 
 int gb_generalized_gravity(const gb_model* M, int precision, int layout, long B, const double* q, double* g,
                            void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(g, "g"));
-  return gbi::launch_rnea(M, precision, B, gbi::arr(q, layout, B, M->nq), zero_arr(M), zero_arr(M),
-                          gbi::arr(g, layout, B, M->nv), (cudaStream_t)stream);
+  return (M->has_mimic ? gbi::launch_rnea_mimic : gbi::launch_rnea)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), zero_arr(M), zero_arr(M),
+      gbi::arr(g, layout, B, M->nv_red), (cudaStream_t)stream);
 }
 
 int gb_static_torque(const gb_model* M, int precision, int layout, long B, const double* q, const double* fext,
                      double* tau, void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(fext, "fext")); GB_TRY(gbi::check_ptr(tau, "tau"));
-  return gbi::launch_rnea_fext(M, precision, B, gbi::arr(q, layout, B, M->nq), zero_arr(M), zero_arr(M),
-                               gbi::arr(fext, layout, B, 6L * M->nj_user), gbi::arr(tau, layout, B, M->nv),
+  return (M->has_mimic ? gbi::launch_rnea_fext_mimic : gbi::launch_rnea_fext)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), zero_arr(M), zero_arr(M),
+      gbi::arr(fext, layout, B, 6L * M->nj_user), gbi::arr(tau, layout, B, M->nv_red),
                                (cudaStream_t)stream);
 }
 
@@ -238,6 +271,7 @@ int gb_kkt_contact_inverse(const gb_model* M, int precision, int layout, long B,
 int gb_constraint_set_create(const gb_model* M, int n, const gb_constraint_desc* cs, gb_constraint_set** out) {
   if (!M || !out) return set_error(GB_ERR_INVALID_ARGUMENT, "model/out is NULL");
   *out = nullptr;
+  if (M->has_mimic) return set_error(GB_ERR_UNSUPPORTED, "Function does not support mimic joints");
   if (n < 0 || n > 64) return set_error(GB_ERR_SIZE, "the number of constraint models must be in 0..64");
   if (n > 0 && !cs) return set_error(GB_ERR_INVALID_ARGUMENT, "constraints is NULL");
   std::vector<int> internal(M->nj_user, -1);  // the caller's joint -> the internal joint carrying it
@@ -417,7 +451,7 @@ int gb_constraint_dynamics_derivatives(const gb_model* M, int precision, const g
 
 int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, const double* q, const double* v,
                           const double* a, double* oMi, double* vout, double* aout, void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (a && !v) return set_error(GB_ERR_INVALID_ARGUMENT, "an acceleration needs a velocity");
   if ((vout && !v) || (aout && !a)) return set_error(GB_ERR_INVALID_ARGUMENT, "velocity / acceleration output without input");
   if (B == 0) return GB_OK;
@@ -427,18 +461,20 @@ int gb_forward_kinematics(const gb_model* M, int precision, int layout, long B, 
   if (vout) GB_TRY(gbi::check_ptr(vout, "v output"));
   if (aout) GB_TRY(gbi::check_ptr(aout, "a output"));
   const long nj = M->nj_user;
-  return gbi::launch_fk(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
-                        gbi::arr(a, layout, B, M->nv), gbi::arr(oMi, layout, B, 12 * nj),
-                        gbi::arr(vout, layout, B, 6 * nj), gbi::arr(aout, layout, B, 6 * nj), (cudaStream_t)stream);
+  return (M->has_mimic ? gbi::launch_fk_mimic : gbi::launch_fk)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), gbi::arr(v, layout, B, M->nv_red),
+      gbi::arr(a, layout, B, M->nv_red), gbi::arr(oMi, layout, B, 12 * nj), gbi::arr(vout, layout, B, 6 * nj),
+      gbi::arr(aout, layout, B, 6 * nj), (cudaStream_t)stream);
 }
 
 int gb_compute_joint_jacobians(const gb_model* M, int precision, int layout, long B, const double* q, double* J,
                                void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(J, "J"));
-  return gbi::launch_jacobians(M, precision, B, gbi::arr(q, layout, B, M->nq), gbi::arr(J, layout, B, 6L * M->nv),
-                               (cudaStream_t)stream);
+  // 6 x nvExtended (data.J of a model with mimic joints has their columns too)
+  return (M->has_mimic ? gbi::launch_jacobians_mimic : gbi::launch_jacobians)(
+      M, precision, B, gbi::arr(q, layout, B, M->nq_red), gbi::arr(J, layout, B, 6L * M->nv), (cudaStream_t)stream);
 }
 
 int gb_aba(const gb_model* M, int precision, int convention, int layout, long B, const double* q, const double* v,
@@ -466,7 +502,8 @@ int gb_aba_fext(const gb_model* M, int precision, int convention, int layout, lo
 
 int gb_crba(const gb_model* M, int precision, int convention, int matrix_mode, int layout, long B, const double* q,
             double* Mout, double* U, double* D, void* stream) {
-  GB_TRY(gbi::check_common(M, precision, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, precision, layout, B));
+  if (M->has_mimic && U) return set_error(GB_ERR_UNSUPPORTED, "the Cholesky decomposition does not support mimic joints");
   if (convention != GB_LOCAL && convention != GB_WORLD) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown convention");
   if (matrix_mode != GB_MATRIX_UPPER && matrix_mode != GB_MATRIX_SYMMETRIC)
     return set_error(GB_ERR_INVALID_ARGUMENT, "unknown matrix mode");
@@ -474,6 +511,9 @@ int gb_crba(const gb_model* M, int precision, int convention, int matrix_mode, i
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(Mout, "M"));
   if (U) { GB_TRY(gbi::check_ptr(U, "U")); GB_TRY(gbi::check_ptr(D, "D")); }
+  if (M->has_mimic)
+    return gbi::launch_crba_mimic(M, precision, matrix_mode == GB_MATRIX_SYMMETRIC, B, gbi::arr(q, layout, B, M->nq_red),
+                                  gbi::arr(Mout, layout, B, (long)M->nv_red * M->nv_red), (cudaStream_t)stream);
   const long nn = (long)M->nv * M->nv;
   return gbi::launch_crba(M, precision, matrix_mode == GB_MATRIX_SYMMETRIC, B, gbi::arr(q, layout, B, M->nq),
                           gbi::arr(Mout, layout, B, nn), gbi::arr(U, layout, B, nn), gbi::arr(D, layout, B, M->nv),
@@ -481,11 +521,12 @@ int gb_crba(const gb_model* M, int precision, int convention, int matrix_mode, i
 }
 
 int gb_integrate(const gb_model* M, int layout, long B, const double* q, const double* v, double* qout, void* stream) {
-  GB_TRY(gbi::check_common(M, GB_FP64, layout, B));
+  GB_TRY(gbi::check_common_mimic(M, GB_FP64, layout, B));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(qout, "qout"));
-  return gbi::launch_integrate(M, B, gbi::arr(q, layout, B, M->nq), gbi::arr(v, layout, B, M->nv),
-                               gbi::arr(qout, layout, B, M->nq), (cudaStream_t)stream);
+  return (M->has_mimic ? gbi::launch_integrate_mimic : gbi::launch_integrate)(
+      M, B, gbi::arr(q, layout, B, M->nq_red), gbi::arr(v, layout, B, M->nv_red), gbi::arr(qout, layout, B, M->nq_red),
+      (cudaStream_t)stream);
 }
 
 int gb_model_set_launch(gb_model* M, int function, int threads_per_block) {
@@ -580,7 +621,7 @@ static int in_parallel(gb_pool* P, long B, const double* q, const double* v, con
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(x, "x"));
   GB_TRY(gbi::check_ptr(out, "out"));
-  const size_t nq = M->nq, nv = M->nv;
+  const size_t nq = M->nq_red, nv = M->nv_red;
   const size_t bytes = sizeof(double) * (size_t)B * (nq + 3 * nv);
   GB_TRY(pool_buffers(P, bytes));
   double* dq = P->d_buf;
@@ -602,12 +643,13 @@ static int in_parallel(gb_pool* P, long B, const double* q, const double* v, con
 int gb_rnea_in_parallel(long num_threads, gb_pool* P, long B, const double* q, const double* v, const double* a,
                         double* tau) {
   GB_TRY(parallel_checks(num_threads, P, B));
-  return in_parallel(P, B, q, v, a, tau, gbi::launch_rnea);
+  return in_parallel(P, B, q, v, a, tau, P->model->has_mimic ? gbi::launch_rnea_mimic : gbi::launch_rnea);
 }
 
 int gb_aba_in_parallel(long num_threads, gb_pool* P, long B, const double* q, const double* v, const double* tau,
                        double* a) {
   GB_TRY(parallel_checks(num_threads, P, B));
+  if (P->model->has_mimic) return set_error(GB_ERR_UNSUPPORTED, "Function does not support mimic joints");
   return in_parallel(P, B, q, v, tau, a, gbi::launch_aba);
 }
 

@@ -54,7 +54,10 @@ inline Arr arr(const double* p, int layout, long batch, long n) {
   return layout == GB_LAYOUT_SOA ? Arr{p, 1, batch} : Arr{p, n, 1};
 }
 
+// check_common also refuses models with mimic joints (the functions that take them call
+// check_common_mimic and the *_mimic launches below)
 int check_common(const gb_model* m, int precision, int layout, long batch);
+int check_common_mimic(const gb_model* m, int precision, int layout, long batch);
 int check_ptr(const void* p, const char* name);
 
 
@@ -87,6 +90,15 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);
+// models with mimic joints (gb_mimic.cu): the caller's arrays mapped to and from the extended tree
+int launch_rnea_mimic(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr tau, cudaStream_t st);
+int launch_rnea_fext_mimic(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr fext, Arr tau,
+                           cudaStream_t st);
+int launch_crba_mimic(const gb_model* M, int precision, bool symmetric, long B, Arr q, Arr Mout, cudaStream_t st);
+int launch_fk_mimic(const gb_model* M, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vout, Arr aout,
+                    cudaStream_t st);
+int launch_jacobians_mimic(const gb_model* M, int precision, long B, Arr q, Arr J, cudaStream_t st);
+int launch_integrate_mimic(const gb_model* M, long B, Arr q, Arr v, Arr qout, cudaStream_t st);
 size_t aba_derivs_workspace_bytes(const gb_model* M, int precision, long B);
 // per-model launch preparation at creation (gb_derivs.cu)
 int prepare_model_launches(gb_model* M);

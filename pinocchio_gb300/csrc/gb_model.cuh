@@ -45,6 +45,19 @@ GB_HD int jt_col(int jt, int k) {
   return jt == JT_FF ? k : jt == JT_SPH ? 3 + k : jt == JT_PL ? (k < 2 ? k : 5) : jt_sidx(jt);
 }
 
+// Mimic joints: an entry of the extended configuration (src: the caller's entry; kind 0 copy,
+// 1 scaling * q + offset, 2 the (cos, sin) pair of an unbounded joint turned to scaling * angle +
+// offset, 3 the second entry of such a pair) and of the extended velocity (src, own: the caller's
+// own dof, g: 1 or the mimic's scaling)
+struct MimicQ {
+  int src = 0, kind = 0;
+  double scaling = 1.0, offset = 0.0;
+};
+struct MimicV {
+  int src = 0, own = 1;
+  double g = 1.0;
+};
+
 struct BlobHeader {
   int nj, nq, nv, bytes;
   int max_depth, has_ff, n_rel, nslot;

@@ -42,6 +42,17 @@ struct gb_model {
   unsigned short prod_woff[33] = {};
   unsigned short prod_task[256] = {};
   bool prod_plan_ok = false;
+  // mimic joints: the kernels run the extended tree (every mimic joint a joint with its own dof,
+  // nq / nv above are its sizes); the caller's q, v, tau, M have nq_red / nv_red entries.  Each
+  // extended configuration entry comes from a caller entry (qmap: copy, linear affine, or the
+  // (cos, sin) pair of an unbounded revolute joint) and each extended velocity entry is a caller
+  // entry times a factor (vmap: 1, or the mimic's scaling): v_ext = G v, tau = G^T tau_ext,
+  // M = G^T M_ext G
+  bool has_mimic = false;
+  int nq_red = 0, nv_red = 0;
+  std::vector<gb::MimicQ> qmap;
+  std::vector<gb::MimicV> vmap;
+  void* d_mimic = nullptr;  // device copy: qmap then vmap
 };
 
 namespace gbm {
@@ -191,6 +202,92 @@ inline int expand_translations(const gb_model_desc* d, ExpandedTree& t, std::str
   return GB_OK;
 }
 
+// Mimic joints (JointModelMimic, reference multibody/joint/joint-mimic.hpp:557-760): the
+// mimicking joint is a one-dof joint of the caller's tree whose coordinate follows another
+// one-dof joint's, q_i = scaling q_j + offset.
+inline bool mimic_capable(int jt) {
+  return (jt >= GB_JOINT_RX && jt <= GB_JOINT_RZ) || (jt >= GB_JOINT_PX && jt <= GB_JOINT_PRISMATIC_UNALIGNED) ||
+         (jt >= GB_JOINT_RUBX && jt <= GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED);
+}
+inline bool unbounded_type(int jt) { return jt >= GB_JOINT_RUBX && jt <= GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED; }
+inline int check_mimic(const gb_model_desc* d, std::string* err) {
+  if (!d->mimic) return GB_OK;
+  for (int i = 1; i < d->njoints; ++i) {
+    const int j = d->mimic[i];
+    if (j <= 0) continue;
+    std::string bad;
+    if (j >= i) bad = "a mimic joint must come after the joint it mimics";
+    else if (d->mimic[j] > 0) bad = "the mimicked joint is a mimic joint itself";
+    else if (!mimic_capable(d->jtype[i]) || !mimic_capable(d->jtype[j]))
+      bad = "mimic joints are one-dof joints mimicking one-dof joints";
+    else if (unbounded_type(d->jtype[i]) != unbounded_type(d->jtype[j]))
+      bad = "a mimic joint and its mimicked joint must have the same nq";
+    else if (!d->mimic_scaling || !d->mimic_offset)
+      bad = "mimic joints need mimic_scaling and mimic_offset";
+    if (!bad.empty()) {
+      *err = "joint " + std::to_string(i) + ": " + bad;
+      return GB_ERR_INVALID_ARGUMENT;
+    }
+  }
+  return GB_OK;
+}
+// The caller's indices (mimic joints take none: idx_q / idx_v of the joint they mimic, as the
+// reference's setMimicIndexes) and the maps from the extended tree's entries to them.
+inline void build_mimic_maps(gb_model* M, const gb_model_desc* du, const ExpandedTree& tree) {
+  const int nju = du->njoints;
+  std::vector<int> rq(nju, 0), rv(nju, 0);
+  int nq = 0, nv = 0;
+  for (int j = 1; j < nju; ++j) {
+    const int jt = du->jtype[j];
+    const int m = du->mimic ? du->mimic[j] : 0;
+    if (m > 0) {
+      rq[j] = rq[m];
+      rv[j] = rv[m];
+      M->has_mimic = true;
+      continue;
+    }
+    rq[j] = nq;
+    rv[j] = nv;
+    nq += jt == GB_JOINT_FREEFLYER ? 7 : (jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR) ? 4
+          : jt == GB_JOINT_TRANSLATION ? 3 : unbounded_type(jt) ? 2 : 1;
+    nv += jt == GB_JOINT_FREEFLYER ? 6 : (jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR ||
+                                          jt == GB_JOINT_TRANSLATION) ? 3 : 1;
+  }
+  M->nq_red = nq;
+  M->nv_red = nv;
+  M->qmap.assign(M->nq, gb::MimicQ{});
+  M->vmap.assign(M->nv, gb::MimicV{});
+  // internal joints of each caller joint: a translation joint's three, otherwise its own
+  for (int i = 1; i < M->nj; ++i) {
+    int j = tree.user_of[i];
+    int k = 0;  // position of internal joint i among its caller joint's internal joints
+    if (j < 0) {  // the first two joints of an expanded translation: the caller joint is the last's
+      int l = i;
+      while (tree.user_of[l] < 0) ++l;
+      j = tree.user_of[l];
+      k = 2 - (l - i);
+    } else if (du->jtype[j] == GB_JOINT_TRANSLATION) {
+      k = 2;
+    }
+    const int m = du->mimic ? du->mimic[j] : 0;
+    const int iq = M->idx_q[i], iv = M->idx_v[i];
+    const int nqi = M->jtype[i] == GB_JOINT_FREEFLYER ? 7 : gb::jt_three(M->jtype[i]) ? 4
+                    : gb::jt_unbounded(M->jtype[i]) ? 2 : 1;
+    if (m > 0) {
+      gb::MimicQ& e = M->qmap[iq];
+      e.src = rq[m];
+      e.kind = gb::jt_unbounded(M->jtype[i]) ? 2 : 1;
+      e.scaling = du->mimic_scaling[j];
+      e.offset = du->mimic_offset[j];
+      if (e.kind == 2) M->qmap[iq + 1] = gb::MimicQ{rq[m] + 1, 3, 0.0, 0.0};
+      M->vmap[iv] = gb::MimicV{rv[m], 0, du->mimic_scaling[j]};
+    } else {
+      for (int c = 0; c < nqi; ++c) M->qmap[iq + c] = gb::MimicQ{rq[j] + k + c, 0, 1.0, 0.0};
+      for (int c = 0; c < M->nvs[i]; ++c) M->vmap[iv + c] = gb::MimicV{rv[j] + k + c, 1, 1.0};
+    }
+  }
+}
+
 // Builds the tree tables of DataTpl (reference multibody/data.hxx:195-306) and
 // the device blob.
 inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
@@ -198,6 +295,7 @@ inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
   if (du->njoints < 2) return set_error(GB_ERR_SIZE, "model needs at least one joint besides the universe");
   ExpandedTree tree;
   if (int rc = expand_translations(du, tree, err)) return rc;
+  if (int rc = check_mimic(du, err)) return rc;
   const gb_model_desc* d = &tree.desc;
   M->nj_user = du->njoints;
   M->ujoint = tree.user_of;
@@ -240,9 +338,12 @@ inline int build_model(gb_model* M, const gb_model_desc* du, std::string* err) {
   M->nq = nq;
   M->nv = nv;
   if (int rc = fold_unaligned(M, d, err)) return rc;
-  if (d->armature && d->nv_armature != nv) return set_error(GB_ERR_SIZE, "armature must have nv entries");
-  M->armature.assign(nv, 0.0);
-  if (d->armature) M->armature.assign(d->armature, d->armature + nv);
+  build_mimic_maps(M, du, tree);
+  if (d->armature && d->nv_armature != M->nv_red) return set_error(GB_ERR_SIZE, "armature must have nv entries");
+  M->armature.assign(nv, 0.0);  // per extended dof: the caller's own dofs' entries, 0 for mimic dofs
+  if (d->armature)
+    for (int e = 0; e < nv; ++e)
+      if (M->vmap[e].own) M->armature[e] = d->armature[M->vmap[e].src];
   M->cap = cap_class(std::max(nj, nv));
   if (M->cap == 0) return set_error(GB_ERR_UNSUPPORTED, "models are limited to 128 joints and 128 dofs");
   // lastChild / nvSubtree (data.hxx:195-225)

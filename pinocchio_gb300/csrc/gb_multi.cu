@@ -126,6 +126,8 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
   for (int k = 0; k < ntasks; ++k) {
     const gb_task& t = tasks[k];
     if (t.model == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, "task model is NULL");
+    if (t.model->has_mimic)
+      return set_error(GB_ERR_UNSUPPORTED, "mimic joints: the heterogeneous launch does not take them (gb_rnea does)");
     if (t.model->has_three)
       return set_error(GB_ERR_UNSUPPORTED, "spherical and planar joints: the heterogeneous launch does not take them "
                                            "(gb_rnea / gb_aba do)");

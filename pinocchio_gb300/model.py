@@ -152,6 +152,33 @@ class JointModelPrismaticUnaligned(JointModel):
         self.axis = _unit(axis)
 
 
+class JointModelMimic(JointModel):
+    """A joint that follows another one-dof joint (reference JointModelMimicTpl,
+    multibody/joint/joint-mimic.hpp:557-760): ``JointModelMimic(joint, mimicked_joint_id, scaling,
+    offset)`` adds ``joint`` (a one-dof joint model: revolute, prismatic, unaligned or unbounded)
+    with q = scaling * q_mimicked + offset and v = scaling * v_mimicked; it has no entry in q or v
+    of its own (nq = nv = 0; nvExtended counts it).  ``mimicked_joint_id`` is the index of a joint
+    already in the model (an int, or an object with an ``id`` attribute)."""
+
+    def __init__(self, joint: JointModel, mimicked, scaling: float = 1.0, offset: float = 0.0):
+        if isinstance(joint, JointModelMimic):
+            raise ValueError("a mimic joint cannot wrap a mimic joint")
+        self.joint = joint
+        self.jtype = joint.jtype
+        self.axis = joint.axis
+        self.mimicked = int(getattr(mimicked, "id", mimicked))
+        self.scaling = float(scaling)
+        self.offset = float(offset)
+
+    @property
+    def nq(self) -> int:
+        return 0
+
+    @property
+    def nv(self) -> int:
+        return 0
+
+
 class SE3:
     """Rigid transform (R, t)."""
 
@@ -211,6 +238,9 @@ class Model:
         self.jointPlacements = [SE3.Identity()]
         self.axes = [np.zeros(3)]
         self.inertias = [Inertia.Zero()]
+        self.mimic = [0]  # per joint: the joint it mimics (0: none)
+        self.mimic_scaling = [1.0]
+        self.mimic_offset = [0.0]
         self.armature = np.zeros(0)
         self.gravity = np.array([0.0, 0.0, -9.81, 0.0, 0.0, 0.0])
         self.name = ""
@@ -219,6 +249,21 @@ class Model:
     def addJoint(self, parent_id: int, joint: JointModel, placement: SE3, name: str = "") -> int:
         if not 0 <= parent_id < self.njoints:
             raise ValueError("parent joint index out of range")
+        if isinstance(joint, JointModelMimic):
+            m = joint.mimicked
+            if not 0 < m < self.njoints or self.mimic[m] != 0:
+                raise ValueError("the mimicked joint must be a joint of the model that is no mimic itself")
+            if joint.jtype not in _ONE_DOF + UNBOUNDED or self.jtypes[m] not in _ONE_DOF + UNBOUNDED:
+                raise ValueError("mimic joints are one-dof joints mimicking one-dof joints")
+            if (joint.jtype in UNBOUNDED) != (self.jtypes[m] in UNBOUNDED):
+                raise ValueError("a mimic joint and its mimicked joint must have the same nq")
+            self.mimic.append(m)
+            self.mimic_scaling.append(joint.scaling)
+            self.mimic_offset.append(joint.offset)
+        else:
+            self.mimic.append(0)
+            self.mimic_scaling.append(1.0)
+            self.mimic_offset.append(0.0)
         self.parents.append(int(parent_id))
         self.jtypes.append(int(joint.jtype))
         self.jointPlacements.append(placement)
@@ -240,19 +285,35 @@ class Model:
 
     @property
     def nqs(self):
-        return [_JT_NQ[j] for j in self.jtypes]
+        return [0 if m else _JT_NQ[j] for j, m in zip(self.jtypes, self.mimic)]
 
     @property
     def nvs(self):
-        return [_JT_NV[j] for j in self.jtypes]
+        return [0 if m else _JT_NV[j] for j, m in zip(self.jtypes, self.mimic)]
+
+    def _indices(self, sizes):
+        # cumulative in insertion order; a mimic joint takes its mimicked joint's index
+        out, n = [], 0
+        for i, (k, m) in enumerate(zip(sizes, self.mimic)):
+            out.append(out[m] if m else n)
+            n += k
+        return out
 
     @property
     def idx_qs(self):
-        return list(np.concatenate([[0], np.cumsum(self.nqs)[:-1]]).astype(int))
+        return self._indices(self.nqs)
 
     @property
     def idx_vs(self):
-        return list(np.concatenate([[0], np.cumsum(self.nvs)[:-1]]).astype(int))
+        return self._indices(self.nvs)
+
+    @property
+    def nvExtended(self) -> int:
+        """nv plus one per mimic joint (reference ModelTpl::nvExtended)."""
+        return self.nv + sum(1 for m in self.mimic if m)
+
+    def has_mimic(self) -> bool:
+        return any(self.mimic)
 
     @property
     def nq(self) -> int:
@@ -285,6 +346,9 @@ class Model:
             armature=np.ascontiguousarray(self.armature, dtype=np.float64),
             gravity=np.ascontiguousarray(self.gravity, dtype=np.float64),
             axis=np.ascontiguousarray(np.array(self.axes, dtype=np.float64).reshape(nj, 3)),
+            mimic=np.ascontiguousarray(self.mimic, dtype=np.int32),
+            mimic_scaling=np.ascontiguousarray(self.mimic_scaling, dtype=np.float64),
+            mimic_offset=np.ascontiguousarray(self.mimic_offset, dtype=np.float64),
         )
 
     def subtree_tables(self) -> dict:
@@ -325,7 +389,9 @@ class Model:
         """The identity configuration (reference neutral(model), liegroup neutral elements): unit
         quaternions (0, 0, 0, 1), planar and unbounded angles (cos, sin) = (1, 0), zero elsewhere."""
         q = np.zeros(self.nq)
-        for jt, iq in zip(self.jtypes, self.idx_qs):
+        for jt, iq, m in zip(self.jtypes, self.idx_qs, self.mimic):
+            if m:
+                continue
             if jt == JT_FF:
                 q[iq + 6] = 1.0
             elif jt == JT_SPH:

@@ -263,6 +263,32 @@ def multidof_tree(seed: int = 10) -> Model:
     return model
 
 
+def mimic_tree(seed: int = 12) -> Model:
+    """A floating base with mimic joints (JointModelMimic): a revolute joint about x following a
+    revolute joint about z (scaling 0.5, offset 0.1), a parallel gripper (the second finger
+    -1 x the first), an unbounded wheel and an unbounded joint about x turning twice as fast
+    (offset 0.3), an unaligned revolute joint following a revolute joint (-0.7, 0.2): nv 11,
+    nvExtended 15, nq 13."""
+    from .model import JointModelMimic, JointModelRUBX, JointModelRUBZ
+
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = "mimictree"
+    base = _add_link(model, rng, 0, JointModelFreeFlyer(), "base")
+    a1 = _add_link(model, rng, base, JointModelRZ(), "a1")
+    a2 = _add_link(model, rng, a1, JointModelRY(), "a2")
+    a3 = _add_link(model, rng, a2, JointModelMimic(JointModelRX(), a1, 0.5, 0.1), "a3")
+    f1 = _add_link(model, rng, a3, JointModelPX(), "finger1")
+    _add_link(model, rng, a3, JointModelMimic(JointModelPX(), f1, -1.0, 0.0), "finger2")
+    w = _add_link(model, rng, base, JointModelRUBZ(), "wheel")
+    _add_link(model, rng, w, JointModelMimic(JointModelRUBX(), w, 2.0, 0.3), "wheel2")
+    b1 = _add_link(model, rng, base, JointModelRX(), "b1")
+    axis = rng.standard_normal(3)
+    _add_link(model, rng, b1, JointModelMimic(JointModelRevoluteUnaligned(axis / np.linalg.norm(axis)), b1, -0.7, 0.2),
+              "b2")
+    return model
+
+
 def chain(n: int = 100, seed: int = 4, mass_range=(0.1, 1.0)) -> Model:
     """Revolute serial chain of ``n`` links."""
     rng = np.random.default_rng(seed)
@@ -292,7 +318,9 @@ def random_configurations(model: Model, batch: int, rng: np.random.Generator) ->
     U[-pi, pi] (unbounded revolute joints: their cos and sin); prismatic displacements
     U[-0.5, 0.5] m."""
     q = np.empty((batch, model.nq))
-    for jt, iq in zip(model.jtypes[1:], model.idx_qs[1:]):
+    for jt, iq, m in zip(model.jtypes[1:], model.idx_qs[1:], model.mimic[1:]):
+        if m:  # a mimic joint has no entry of its own
+            continue
         if jt == JT_FF:
             q[:, iq : iq + 3] = rng.standard_normal((batch, 3))
             q[:, iq + 3 : iq + 7] = random_unit_quaternion(rng, batch)

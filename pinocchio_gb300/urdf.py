@@ -50,6 +50,7 @@ from .model import (
     Inertia,
     JointModel,
     JointModelFreeFlyer,
+    JointModelMimic,
     JointModelPlanar,
     JointModelPrismaticUnaligned,
     JointModelRevoluteUnaligned,
@@ -131,8 +132,12 @@ def _axis_joint(joint) -> JointModel:
     return _UNALIGNED[kind](ax / n)
 
 
-def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
-    """Model of a URDF document (reference pinocchio::urdf::buildModelFromXML)."""
+def buildModelFromXML(xml: str, root_joint: JointModel | None = None, mimic: bool = False) -> Model:
+    """Model of a URDF document (reference pinocchio::urdf::buildModelFromXML).  With ``mimic``, a
+    revolute or prismatic joint carrying ``<mimic joint=... multiplier=... offset=...>`` becomes a
+    JointModelMimic of that joint (the reference's ``mimic`` argument, src/parsers/urdf/model.cpp:
+    140-160, 213-230; off by default, when such joints are ordinary joints); the mimicked joint
+    must come earlier in the depth-first walk."""
     robot = ET.fromstring(xml)
     if robot.tag != "robot":
         raise ValueError("not a URDF document: the root element must be <robot>")
@@ -176,6 +181,13 @@ def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
                 visit(child, (joint_id, Pj))
             elif jt in _AXIS_JT or jt == "planar" or (jt == "floating" and joint_id == 0):
                 jm = _axis_joint(j) if jt in _AXIS_JT else JointModelPlanar() if jt == "planar" else JointModelFreeFlyer()
+                mi = j.find("mimic")
+                if mimic and mi is not None and jt in ("revolute", "prismatic"):
+                    target = mi.get("joint")
+                    if target not in model.names:
+                        raise ValueError(f"joint {j.get('name')!r} mimics {target!r}, which is not an earlier joint")
+                    jm = JointModelMimic(jm, model.names.index(target), float(mi.get("multiplier", "1")),
+                                         float(mi.get("offset", "0")))
                 new_id = model.addJoint(joint_id, jm, Pj, j.get("name"))
                 append(new_id, child, SE3.Identity())
                 visit(child, (new_id, SE3.Identity()))
@@ -187,10 +199,11 @@ def buildModelFromXML(xml: str, root_joint: JointModel | None = None) -> Model:
     return model
 
 
-def buildModelFromUrdf(path: str, root_joint: JointModel | None = None) -> Model:
-    """Model of a URDF file (reference pinocchio::urdf::buildModel(filename[, root_joint], model))."""
+def buildModelFromUrdf(path: str, root_joint: JointModel | None = None, mimic: bool = False) -> Model:
+    """Model of a URDF file (reference pinocchio::urdf::buildModel(filename[, root_joint], model[,
+    verbose, mimic]))."""
     with open(path, "r", encoding="utf-8") as f:
-        return buildModelFromXML(f.read(), root_joint)
+        return buildModelFromXML(f.read(), root_joint, mimic)
 
 
 def save_model(model: Model, path: str) -> None:
@@ -222,6 +235,9 @@ def load_model(path: str) -> Model:
                 joint = _OneDof(jt)
             if jt == JT_NONE:
                 raise ValueError("joint type 0 (universe) below the root")
+            if "mimic" in z.files and int(z["mimic"][i]) > 0:
+                joint = JointModelMimic(joint, int(z["mimic"][i]), float(z["mimic_scaling"][i]),
+                                        float(z["mimic_offset"][i]))
             P = SE3(placement[i, :9].reshape(3, 3), placement[i, 9:])
             model.addJoint(int(parents[i]), joint, P, names[i])
             model.inertias[i] = Inertia(inertia[i, 0], inertia[i, 1:4], inertia[i, 4:])
