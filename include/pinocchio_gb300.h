@@ -402,6 +402,22 @@ int gb_constraint_dynamics_derivatives(const gb_model* model, int precision, con
                                        double* dlambda_dq, double* dlambda_dv, double* dlambda_dtau,
                                        int* iterations, void* stream);
 
+/* ContactCholeskyDecomposition(model, contact_models).compute(model, data, contact_models,
+ * contact_datas, mu) at each configuration q and its accessors (algorithm/contact-cholesky.hpp:
+ * 168-265, contact-cholesky.hxx:152-304, 617-759), n = constraint dim + nv, row-major per
+ * configuration in `layout`; every output may be NULL:
+ *   kkt           n x n   matrix():  [[-mu I, J], [J^T, M]], the constraint rows first;
+ *   kkt_inverse   n x n   inverse(): [[-OSIM, OSIM J M^-1], [M^-1 J^T OSIM, M^-1 - M^-1 J^T OSIM J M^-1]];
+ *   osim_inverse  nc x nc getInverseOperationalSpaceInertiaMatrix(): J M^-1 J^T + mu I;
+ *   osim          nc x nc getOperationalSpaceInertiaMatrix(): its inverse;
+ *   minv          nv x nv getInverseMassMatrix(): M^-1;
+ *   jminv         nc x nv getJMinv(): J M^-1.
+ * J is the constraint Jacobian of the set's models at q (as constraintDynamics builds it).  The
+ * factorisation is FP64 in both precisions (the CRBA's Cholesky is). */
+int gb_contact_cholesky(const gb_model* model, int precision, const gb_constraint_set* set, double mu, int layout,
+                        long batch, const double* q, double* kkt, double* kkt_inverse, double* osim_inverse,
+                        double* osim, double* minv, double* jminv, void* stream);
+
 /* forwardKinematics(model, data, q[, v[, a]]) (reference algorithm/kinematics.hxx:42-272):
  * per instance, for every joint i = 0 .. njoints-1 (joint 0 the universe:
  * identity, zero), oMi[12 i ..] = the world placement (rotation row-major, then

@@ -2079,6 +2079,114 @@ void constraint_jacobian(const Model& m, const Data<T>& d, const ConstraintModel
   }
 }
 
+// ContactCholeskyDecomposition::compute at q (contact-cholesky.hxx:152-304: M in the bottom-right
+// block, the constraint Jacobian rows in the top-right block, the factorisation with damping mu) and
+// its accessors: matrix() = U D U^T (hxx:617-622), inverse() column by column with the strictly lower
+// triangle copied from the upper (hxx:746-759), getInverseOperationalSpaceInertiaMatrix() =
+// -U1 D1 U1^T, getOperationalSpaceInertiaMatrix() = -U1^-T D1^-1 U1^-1, getInverseMassMatrix() =
+// U4^-T D4^-1 U4^-1, getJMinv() = U2 U4^-1 (contact-cholesky.hpp:168-265).  Every output is
+// row-major and may be null.
+template <class T>
+void contact_cholesky(const Model& m, Data<T>& d, const T* q, const std::vector<ConstraintModel>& cms, T mu, T* kkt,
+                      T* kkt_inv, T* osim_inv, T* osim, T* minv, T* jminv) {
+  const int nv = m.nv;
+  for (int i = 1; i < m.njoints; ++i) {  // placements, world columns and inertias (crba.hxx:23-96)
+    const int p = m.parents[i], iq = m.idx_q[i], iv = m.idx_v[i];
+    d.liMi[i] = se3_mul(placement_of<T>(m, i), joint_transform<T>(m, i, q + iq));
+    d.oMi[i] = p > 0 ? se3_mul(d.oMi[p], d.liMi[i]) : d.liMi[i];
+    for (int k = 0; k < m.nvs[i]; ++k) set_col6(d.J, iv + k, act_motion(d.oMi[i], S_col<T>(m, i, k)));
+    d.oYcrb[i] = iner_act(d.oMi[i], inertia_of<T>(m, i));
+  }
+  std::fill(d.M.begin(), d.M.end(), T(0));
+  for (int i = m.njoints - 1; i > 0; --i) {
+    const int p = m.parents[i], iv = m.idx_v[i], nvi = m.nvs[i];
+    for (int k = 0; k < nvi; ++k) set_col6(d.dFda, iv + k, iner_mul(d.oYcrb[i], col6(d.J, iv + k)));
+    for (int r = 0; r < nvi; ++r)
+      for (int c = iv; c < iv + m.nvSubtree[i]; ++c) d.M[(size_t)(iv + r) * nv + c] = dot6(col6(d.J, iv + r), col6(d.dFda, c));
+    if (p > 0) iner_add(d.oYcrb[p], d.oYcrb[i]);
+  }
+  for (int k = 0; k < nv; ++k) d.M[(size_t)k * nv + k] += T(m.armature[k]);
+  ContactCholesky<T> ch;
+  ch.allocate(m, cms);
+  const int nc = ch.nc, n = ch.n;
+  for (int k = 0; k < nv; ++k) {
+    ch.D[nc + k] = d.M[(size_t)k * nv + k];
+    for (int c = k + 1; c < nv; ++c) ch.u(nc + k, nc + c) = d.M[(size_t)k * nv + c];
+  }
+  int row = 0;
+  for (const ConstraintModel& c : cms) {
+    const SE3<T> oMc1 = c.joint1 > 0 ? se3_mul(d.oMi[c.joint1], se3_from<T>(c.P1)) : se3_from<T>(c.P1);
+    const SE3<T> oMc2 = c.joint2 > 0 ? se3_mul(d.oMi[c.joint2], se3_from<T>(c.P2)) : se3_from<T>(c.P2);
+    constraint_jacobian(m, d, c, oMc1, oMc2, se3_actinv(oMc1, oMc2), row, ch);
+    row += c.size();
+  }
+  ch.factor(mu);
+  if (kkt)
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) {
+        T s = T(0);
+        for (int k = std::max(r, c); k < n; ++k) s += ch.u(r, k) * ch.D[k] * ch.u(c, k);
+        kkt[(size_t)r * n + c] = s;
+      }
+  if (kkt_inv) {
+    std::vector<T> x(n);
+    for (int c = 0; c < n; ++c) {
+      std::fill(x.begin(), x.end(), T(0));
+      x[c] = T(1);
+      ch.solve(x.data());
+      for (int r = 0; r <= c; ++r) kkt_inv[(size_t)r * n + c] = x[r];
+    }
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < r; ++c) kkt_inv[(size_t)r * n + c] = kkt_inv[(size_t)c * n + r];
+  }
+  if (osim_inv)
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nc; ++c) {
+        T s = T(0);
+        for (int k = std::max(r, c); k < nc; ++k) s += ch.u(r, k) * ch.D[k] * ch.u(c, k);
+        osim_inv[(size_t)r * nc + c] = -s;
+      }
+  // the inverse of a unit upper triangular block U[o.., o..] of size s: W (row-major, s x s)
+  auto unit_upper_inverse = [&](int o, int s, std::vector<T>& W) {
+    W.assign((size_t)s * s, T(0));
+    for (int c = 0; c < s; ++c) {
+      W[(size_t)c * s + c] = T(1);
+      for (int r = c - 1; r >= 0; --r) {
+        T t = T(0);
+        for (int k = r + 1; k <= c; ++k) t += ch.u(o + r, o + k) * W[(size_t)k * s + c];
+        W[(size_t)r * s + c] = -t;
+      }
+    }
+  };
+  std::vector<T> W;
+  if (osim) {
+    unit_upper_inverse(0, nc, W);
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nc; ++c) {
+        T s = T(0);
+        for (int k = 0; k <= std::min(r, c); ++k) s += W[(size_t)k * nc + r] * ch.Dinv[k] * W[(size_t)k * nc + c];
+        osim[(size_t)r * nc + c] = -s;
+      }
+  }
+  if (minv || jminv) {
+    unit_upper_inverse(nc, nv, W);
+    if (minv)
+      for (int r = 0; r < nv; ++r)
+        for (int c = 0; c < nv; ++c) {
+          T s = T(0);
+          for (int k = 0; k <= std::min(r, c); ++k) s += W[(size_t)k * nv + r] * ch.Dinv[nc + k] * W[(size_t)k * nv + c];
+          minv[(size_t)r * nv + c] = s;
+        }
+    if (jminv)
+      for (int r = 0; r < nc; ++r)
+        for (int c = 0; c < nv; ++c) {
+          T s = T(0);
+          for (int k = 0; k <= c; ++k) s += ch.u(r, nc + k) * W[(size_t)k * nv + c];
+          jminv[(size_t)r * nv + c] = s;
+        }
+  }
+}
+
 struct ProximalResult {
   int iter = 0;
   double absolute_residual = -1.0, relative_residual = -1.0;

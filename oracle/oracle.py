@@ -62,6 +62,7 @@ def lib():
                                               C.c_double, C.c_double, vp, vp, vp, vp, C.c_int]
         L.orc_constraint_dynamics_derivatives.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, C.c_double,
                                                           C.c_int, C.c_double, C.c_double] + [vp] * 9 + [C.c_int]
+        L.orc_contact_cholesky.argtypes = [vp, C.c_long, C.c_int, vp, vp, C.c_double, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_impulse_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
         L.orc_forward_kinematics.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, vp, vp, vp, C.c_int]
@@ -225,6 +226,24 @@ class OracleModel:
                                                   float(relative_accuracy), _ptr(ddq), _ptr(lam), _ptr(iters),
                                                   _ptr(res), nthreads))
         return ddq, lam, iters, res
+
+    def contact_cholesky(self, q, desc, mu=0.0, nthreads=0):
+        """ContactCholeskyDecomposition(model, contact_models).compute(model, data, contact_models,
+        contact_datas, mu) at each configuration (reference algorithm/contact-cholesky.hxx:152-304) and
+        its accessors (contact-cholesky.hpp:168-265, contact-cholesky.hxx:617-759): a dict of matrix
+        (B, n, n), inverse (B, n, n), osim_inverse (B, nc, nc), osim (B, nc, nc), minv (B, nv, nv) and
+        jminv (B, nc, nv), n = nc + nv, the constraint rows first."""
+        q = _c(q)
+        desc = _c(np.asarray(desc).reshape(-1, 46))
+        B, nv = q.shape[0], self.nv
+        nc = int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
+        n = nc + nv
+        out = dict(matrix=np.empty((B, n, n)), inverse=np.empty((B, n, n)), osim_inverse=np.empty((B, nc, nc)),
+                   osim=np.empty((B, nc, nc)), minv=np.empty((B, nv, nv)), jminv=np.empty((B, nc, nv)))
+        self._check(lib().orc_contact_cholesky(self.h, B, len(desc), _ptr(desc), _ptr(q), float(mu),
+                                               *(_ptr(out[k]) for k in ("matrix", "inverse", "osim_inverse", "osim",
+                                                                        "minv", "jminv")), nthreads))
+        return out
 
     def constraint_dynamics_derivatives(self, q, v, tau, desc, mu=0.0, max_iter=1, absolute_accuracy=1e-12,
                                         relative_accuracy=1e-12, prec=0, nthreads=0):

@@ -462,6 +462,38 @@ extern "C" int orc_constraint_dynamics(void* h, int prec, long B, int ncontacts,
   }
 }
 
+// ContactCholeskyDecomposition(model, contact_models).compute(model, data, contact_models,
+// contact_datas, mu) at each configuration and its accessors (contact-cholesky.hpp:168-265,
+// contact-cholesky.hxx:152-304, 617-759); n = constraint dim + nv; every output may be null.
+extern "C" int orc_contact_cholesky(void* h, long B, int ncontacts, const double* desc, const double* q, double mu,
+                                    double* kkt, double* kkt_inv, double* osim_inv, double* osim, double* minv,
+                                    double* jminv, int nt) {
+  const Model& m = *static_cast<Model*>(h);
+  try {
+    const std::vector<orc::ConstraintModel> cms = constraint_models(m, ncontacts, desc);
+    if (!(mu >= 0.0)) throw std::invalid_argument("mu must be positive.");
+    int nc = 0;
+    for (const auto& c : cms) nc += c.size();
+    const size_t n = (size_t)nc + m.nv, nv = m.nv;
+    if (nt <= 0) nt = omp_get_max_threads();
+    omp_set_dynamic(0);
+    omp_set_num_threads(nt);
+    std::vector<std::unique_ptr<orc::Data<double>>> datas(nt);
+    for (int t = 0; t < nt; ++t) datas[t].reset(new orc::Data<double>(m));
+#pragma omp parallel for schedule(static)
+    for (long b = 0; b < B; ++b) {
+      auto at = [&](double* p, size_t k) { return p ? p + (size_t)b * k : nullptr; };
+      orc::contact_cholesky(m, *datas[omp_get_thread_num()], q + (size_t)b * m.nq, cms, mu, at(kkt, n * n),
+                            at(kkt_inv, n * n), at(osim_inv, (size_t)nc * nc), at(osim, (size_t)nc * nc),
+                            at(minv, nv * nv), at(jminv, (size_t)nc * nv));
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
 namespace {
 template <class T>
 int constraint_derivs_batch(const Model& m, long B, const std::vector<orc::ConstraintModel>& cms, const double* q,

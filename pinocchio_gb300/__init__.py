@@ -45,6 +45,7 @@ from .constraints import (  # noqa: F401
 from .urdf import buildModelFromUrdf, buildModelFromXML, load_model, save_model  # noqa: F401
 from .mjcf import buildModelFromMJCF, buildModelFromMJCFXML  # noqa: F401
 from .api import (  # noqa: F401
+    ContactCholeskyDecomposition,
     Data,
     ModelPool,
     aba,

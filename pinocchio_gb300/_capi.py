@@ -60,6 +60,7 @@ EXPORTS = (
     "gb_constraint_set_dims",
     "gb_constraint_dynamics",
     "gb_constraint_dynamics_derivatives",
+    "gb_contact_cholesky",
     "gb_forward_kinematics",
     "gb_compute_joint_jacobians",
     "gb_integrate",
@@ -180,6 +181,7 @@ def lib():
         L.gb_model_destroy.argtypes = [vp]
         L.gb_model_dims.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
         L.gb_model_nv_extended.argtypes = [vp, C.POINTER(i)]
+        L.gb_contact_cholesky.argtypes = [vp, i, vp, C.c_double, i, C.c_long] + [vp] * 8
         L.gb_pipeline_timeouts.argtypes = [C.POINTER(C.c_uint), i]
         L.gb_numeric_status.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.gb_pipeline_wait_selftest.argtypes = [C.c_uint, vp]

@@ -391,6 +391,104 @@ class _ConstraintSet:
             self.h = None
 
 
+class ContactCholeskyDecomposition:
+    """ContactCholeskyDecomposition(model[, contact_models]) (reference algorithm/contact-cholesky.hpp:
+    107-470) over a batch.  ``compute(model, data, contact_models, contact_datas, mu=0.0[, q=])``
+    factorises the KKT matrix [[-mu I, J], [J^T, M]] (constraint rows first) at each configuration,
+    J the constraint Jacobian of the models: q defaults to the configurations of the last
+    ``crba(model, data, q)``, whose data.M the reference's compute reads.  The accessors return
+    (batch, ...) arrays: ``matrix()``, ``inverse()``, ``getInverseOperationalSpaceInertiaMatrix()``
+    (J M^-1 J^T + mu I), ``getOperationalSpaceInertiaMatrix()``, ``getInverseMassMatrix()``,
+    ``getJMinv()``, and ``solve(rhs)`` (the KKT inverse applied to (batch, n) or (batch, n, k)
+    right-hand sides); ``updateDamping(mu)`` refactorises with another damping.  FP64 (the CRBA's
+    Cholesky is FP64 in both precisions)."""
+
+    _KEYS = ("matrix", "inverse", "osim_inverse", "osim", "minv", "jminv")
+
+    def __init__(self, model: Model, contact_models=()):
+        self.nv = model.nv
+        self._nc = int(sum(c.size() for c in contact_models))
+        self._num_contacts = len(contact_models)
+        self._out = None
+
+    def compute(self, model: Model, data: Data, contact_models, contact_datas=None, mu: float = 0.0, *, q=None):
+        from .constraints import stack_desc
+
+        if not mu >= 0.0:
+            raise ValueError("mu must be positive.")
+        if q is None:
+            q = getattr(data, "crba_q", None)
+            if q is None:
+                raise ValueError("compute needs the configurations: call crba(model, data, q) first or pass q=")
+        qt, was_np, vec = _as_batch(q, model.nq, "q")
+        desc = stack_desc(contact_models)
+        cset = getattr(data, "constraint_set", None)
+        if cset is None or cset.desc.shape != desc.shape or not np.array_equal(cset.desc, desc):
+            data.constraint_set = cset = _ConstraintSet(data, desc)
+        torch = _torch()
+        B, nv, nc = qt.shape[0], model.nv, cset.nc
+        n = nv + nc
+        shapes = dict(matrix=(n, n), inverse=(n, n), osim_inverse=(nc, nc), osim=(nc, nc), minv=(nv, nv),
+                      jminv=(nc, nv))
+        out = {k: torch.empty((B,) + shapes[k], dtype=qt.dtype, device=qt.device) for k in self._KEYS}
+        _capi.check(
+            _capi.lib().gb_contact_cholesky(
+                data.dev.h, _PREC[data.precision], cset.h, float(mu), _capi.GB_LAYOUT_INSTANCE, B, _ptr(qt),
+                *(_ptr(out[k]) if out[k].numel() else None for k in self._KEYS), _stream_ptr(),
+            )
+        )
+        self._out, self._was_np, self._vec = out, was_np, vec
+        self._args = (model, data, contact_models, contact_datas, qt)
+        self._nc, self._num_contacts, self.mu = nc, len(contact_models), float(mu)
+
+    def updateDamping(self, mu: float):
+        """contact-cholesky.hxx:274-304: the same factorisation with another damping."""
+        model, data, cms, cds, qt = self._args
+        self.compute(model, data, cms, cds, mu, q=qt)
+
+    def _get(self, key):
+        if self._out is None:
+            raise ValueError("call compute first")
+        return _ret(self._out[key], self._was_np, self._vec)
+
+    def size(self) -> int:
+        return self._nc + self.nv
+
+    def constraintDim(self) -> int:
+        return self._nc
+
+    def numContacts(self) -> int:
+        return self._num_contacts
+
+    def matrix(self):
+        return self._get("matrix")
+
+    def inverse(self):
+        return self._get("inverse")
+
+    def getInverseOperationalSpaceInertiaMatrix(self):
+        return self._get("osim_inverse")
+
+    def getOperationalSpaceInertiaMatrix(self):
+        return self._get("osim")
+
+    def getInverseMassMatrix(self):
+        return self._get("minv")
+
+    def getJMinv(self):
+        return self._get("jminv")
+
+    def solve(self, rhs):
+        """KKT^-1 rhs for (batch, n) or (batch, n, k) right-hand sides (contact-cholesky.hxx:306-330)."""
+        if self._out is None:
+            raise ValueError("call compute first")
+        torch = _torch()
+        K = self._out["inverse"]
+        r = torch.as_tensor(np.asarray(rhs) if not torch.is_tensor(rhs) else rhs, dtype=K.dtype).to(K.device)
+        x = torch.matmul(K, r.unsqueeze(-1)).squeeze(-1) if r.dim() == 2 else torch.matmul(K, r)
+        return x.cpu().numpy() if not torch.is_tensor(rhs) else x
+
+
 def initConstraintDynamics(model: Model, data: Data, contact_models) -> None:
     """initConstraintDynamics(model, data, contact_models) (reference
     algorithm/constrained-dynamics.hxx:21-60): uploads the constraint models for the calls of
@@ -583,6 +681,7 @@ def crba(model: Model, data: Data, q, convention: int = Convention.LOCAL, symmet
         )
     )
     data.M = M
+    data.crba_q = qt  # the configurations data.M belongs to (ContactCholeskyDecomposition.compute reads them)
     return _ret(M, was_np, vec)
 
 

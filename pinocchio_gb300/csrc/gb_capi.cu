@@ -410,6 +410,22 @@ int gb_constraint_dynamics(const gb_model* M, int precision, const gb_constraint
                                 residuals, (cudaStream_t)stream);
 }
 
+int gb_contact_cholesky(const gb_model* M, int precision, const gb_constraint_set* S, double mu, int layout, long B,
+                        const double* q, double* kkt, double* kkt_inverse, double* osim_inverse, double* osim,
+                        double* minv, double* jminv, void* stream) {
+  GB_TRY(gbi::check_common(M, precision, layout, B));
+  if (!S) return set_error(GB_ERR_INVALID_ARGUMENT, "set is NULL");
+  if (S->model != M) return set_error(GB_ERR_INVALID_ARGUMENT, "the constraint set belongs to another model");
+  if (!(mu >= 0.0)) return set_error(GB_ERR_INVALID_ARGUMENT, "mu must be positive.");
+  if (B == 0) return GB_OK;
+  GB_TRY(gbi::check_ptr(q, "q"));
+  const long nv = M->nv, nc = S->nc, n = nv + nc;
+  auto a = [&](double* p, long k) { return p && k > 0 ? gbi::arr(p, layout, B, k) : gbi::Arr{nullptr, 0, 0}; };
+  return gbi::launch_contact_cholesky(M, B, S, mu, gbi::arr(q, layout, B, M->nq), a(kkt, n * n), a(kkt_inverse, n * n),
+                                      a(osim_inverse, nc * nc), a(osim, nc * nc), a(minv, nv * nv), a(jminv, nc * nv),
+                                      (cudaStream_t)stream);
+}
+
 int gb_constraint_dynamics_derivatives(const gb_model* M, int precision, const gb_constraint_set* S,
                                        const gb_proximal_settings* settings, int layout, long B, const double* q,
                                        const double* v, const double* tau, double* ddq, double* lambda_c,

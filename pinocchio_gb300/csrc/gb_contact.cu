@@ -1205,6 +1205,109 @@ __global__ void __launch_bounds__(128)
       l[e] = X[(e / nv) * sv + e % nv] + (pass == 0 ? Cqs[(long)e * B + b] : 0.0);
   }
 }
+// ContactCholeskyDecomposition::compute at q and its accessors (contact-cholesky.hpp:168-265,
+// contact-cholesky.hxx:152-304, 617-759), one thread per configuration, from the tree
+// factorisation M = U D U^T, the symmetric M and the constraint rows J (all [element][configuration]):
+// JMinv = J M^-1 (a tree solve per row), OSIM^-1 = J M^-1 J^T + mu I (the damped Delassus matrix),
+// OSIM its inverse (LLT), M^-1 (a tree solve per column), the KKT matrix
+// [[-mu I, J], [J^T, M]] (constraint rows first, as the reference's matrix()) and its inverse
+// [[-OSIM, OSIM J M^-1], [M^-1 J^T OSIM, M^-1 - M^-1 J^T OSIM J M^-1]].  Outputs may be null.
+__global__ void __launch_bounds__(kThreads)
+    k_contact_cholesky(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
+                       const double* Ms, const double* Js, double mu, double* Mis, double* JMs, double* Gs,
+                       double* Os, double* Ts, Arr kkt, Arr kinv, Arr oinv, Arr osim, Arr minv, Arr jminv) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int nv = m.nv, n = nc + nv;
+  const Col U{const_cast<double*>(Us) + b, B}, D{const_cast<double*>(Ds) + b, B};
+  const Col Mi{Mis + b, B}, JM{JMs + b, B}, G{Gs + b, B}, O{Os + b, B}, T{Ts + b, B};
+  const gb::In Ji{Js + b, B}, Mf{Ms + b, B};
+  auto out = [&](const Arr& a, long k) -> double& { return const_cast<double*>(a.p)[b * a.is + k * a.es]; };
+  const bool need_minv = minv.p || kinv.p, need_jm = nc > 0 && (jminv.p || oinv.p || osim.p || kinv.p);
+  for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);
+  if (need_minv)
+    for (int c = 0; c < nv; ++c) {  // column c of M^-1
+      const Col x{Mi.p + (long)c * B, (long)nv * B};
+      for (int k = 0; k < nv; ++k) x[k] = k == c ? 1.0 : 0.0;
+      chol_solve(m, U, D, x);
+    }
+  if (need_jm)
+    for (int r = 0; r < nc; ++r) {  // row r of J M^-1 = (M^-1 J_r^T)^T
+      const Col x{JM.p + (long)r * nv * B, B};
+      for (int k = 0; k < nv; ++k) x[k] = Ji[r * nv + k];
+      chol_solve(m, U, D, x);
+    }
+  if (need_jm) {
+    for (int i = 0; i < nc; ++i)  // J M^-1 J^T + mu I (lower), its LLT in G, OSIM = G^-T G^-1 in O
+      for (int j = 0; j <= i; ++j) {
+        double t = 0.0;
+        for (int k = 0; k < nv; ++k) t += JM[(long)i * nv + k] * Ji[j * nv + k];
+        G[(long)i * nc + j] = t + (i == j ? mu : 0.0);
+        if (oinv.p) {
+          out(oinv, (long)i * nc + j) = G[(long)i * nc + j];
+          out(oinv, (long)j * nc + i) = G[(long)i * nc + j];
+        }
+      }
+    if (osim.p || kinv.p) {
+      for (int j = 0; j < nc; ++j) {
+        double t = G[(long)j * nc + j];
+        for (int k = 0; k < j; ++k) t -= G[(long)j * nc + k] * G[(long)j * nc + k];
+        gb::check_pivot(m, t);
+        const double l = sqrt(t);
+        G[(long)j * nc + j] = l;
+        for (int i = j + 1; i < nc; ++i) {
+          double u = G[(long)i * nc + j];
+          for (int k = 0; k < j; ++k) u -= G[(long)i * nc + k] * G[(long)j * nc + k];
+          G[(long)i * nc + j] = u / l;
+        }
+      }
+      for (int c = 0; c < nc; ++c) {  // column c of OSIM: (L L^T)^-1 e_c
+        const Col x{O.p + (long)c * B, (long)nc * B};
+        for (int k = 0; k < nc; ++k) x[k] = k == c ? 1.0 : 0.0;
+        llt_solve(G, nc, x);
+      }
+      if (osim.p)
+        for (long k = 0; k < (long)nc * nc; ++k) out(osim, k) = O[k];
+    }
+  }
+  if (jminv.p)
+    for (long k = 0; k < (long)nc * nv; ++k) out(jminv, k) = JM[k];
+  if (minv.p)
+    for (long k = 0; k < (long)nv * nv; ++k) out(minv, k) = Mi[k];
+  if (kkt.p)
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) {
+        double x;
+        if (r < nc) x = c < nc ? (r == c ? -mu : 0.0) : Ji[r * nv + (c - nc)];
+        else x = c < nc ? Ji[c * nv + (r - nc)] : Mf[(long)(r - nc) * nv + (c - nc)];
+        out(kkt, (long)r * n + c) = x;
+      }
+  if (kinv.p) {
+    for (int r = 0; r < nc; ++r)  // T = OSIM J M^-1
+      for (int c = 0; c < nv; ++c) {
+        double t = 0.0;
+        for (int k = 0; k < nc; ++k) t += O[(long)r * nc + k] * JM[(long)k * nv + c];
+        T[(long)r * nv + c] = t;
+      }
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nc; ++c) out(kinv, (long)r * n + c) = -O[(long)r * nc + c];
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c < nv; ++c) {
+        out(kinv, (long)r * n + nc + c) = T[(long)r * nv + c];
+        out(kinv, (long)(nc + c) * n + r) = T[(long)r * nv + c];
+      }
+    for (int i = 0; i < nv; ++i)
+      for (int j = i; j < nv; ++j) {
+        double t = Mi[(long)i * nv + j];
+        for (int k = 0; k < nc; ++k) t -= JM[(long)k * nv + i] * T[(long)k * nv + j];
+        out(kinv, (long)(nc + i) * n + nc + j) = t;
+        out(kinv, (long)(nc + j) * n + nc + i) = t;
+      }
+  }
+}
+
 }  // namespace
 
 int launch_contact(const gb_model* M, int precision, bool impulse, long B, int nc, Arr q, Arr v, Arr x, Arr J,
@@ -1306,6 +1409,60 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
                                                                         ddq, lam, iters, residuals, tab, set->n, cmask,
                                                                         clist);
     rc = cuda_error(cudaGetLastError(), "k_constraint_solve");
+  }
+  scratch_free(scratch, st);
+  return rc;
+}
+
+int launch_contact_cholesky(const gb_model* M, long B, const gb_constraint_set* set, double mu, Arr q, Arr kkt,
+                            Arr kinv, Arr oinv, Arr osim, Arr minv, Arr jminv, cudaStream_t st) {
+  const long nv = M->nv, nn = nv * nv, nc = set->nc;
+  // scratch, [element][configuration]: M, U, M^-1 (nn), D (nv), J, J M^-1, OSIM J M^-1 (nc nv),
+  // the Delassus factor, OSIM (nc nc), the constraint right-hand sides (nc, unused here)
+  void* scratch = nullptr;
+  int rc = scratch_alloc(&scratch, sizeof(double) * (size_t)B * (3 * nn + nv + 3 * nc * nv + 2 * nc * nc + nc), st);
+  if (rc != GB_OK) return rc;
+  double* base = static_cast<double*>(scratch);
+  double *Ms = base, *Us = Ms + nn * B, *Mis = Us + nn * B, *Ds = Mis + nn * B, *Js = Ds + nv * B,
+         *JMs = Js + nc * nv * B, *Ts = JMs + nc * nv * B, *Gs = Ts + nc * nv * B, *Os = Gs + nc * nc * B,
+         *Rh = Os + nc * nc * B;
+  const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
+  const signed char* sp = reinterpret_cast<const signed char*>(tab + (set->n > 0 ? set->n : 0));
+  rc = launch_crba(M, GB_FP64, true, B, q, Arr{Ms, 1, B}, Arr{Us, 1, B}, Arr{Ds, 1, B}, st);
+  const long grid = (B + kThreads - 1) / kThreads;
+  auto opt_in = [&](const void* kern, const char* name) -> int {
+    if (M->stage_bytes <= 48 * 1024) return GB_OK;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M->stage_bytes);
+    return e == cudaSuccess ? GB_OK : cuda_error(e, name);
+  };
+  if (rc == GB_OK && set->n > 0) {
+    const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
+    const Arr zero{reinterpret_cast<const double*>(M->d_blob + h->o_zero), 0, 0};
+    switch (M->cap) {
+#define GB_SETUP(C)                                                                                         \
+  case C:                                                                                                   \
+    rc = opt_in((const void*)k_constraint_setup<C>, "k_constraint_setup");                                  \
+    if (rc == GB_OK)                                                                                        \
+      k_constraint_setup<C><<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, q, zero, \
+                                                                               tab, sp, set->n, Js, Rh);    \
+    break;
+      GB_SETUP(8)
+      GB_SETUP(16)
+      GB_SETUP(32)
+      GB_SETUP(64)
+      GB_SETUP(128)
+#undef GB_SETUP
+      default:
+        rc = set_error(GB_ERR_UNSUPPORTED, "model too large");
+    }
+    if (rc == GB_OK) rc = cuda_error(cudaGetLastError(), "k_constraint_setup");
+  }
+  if (rc == GB_OK) rc = opt_in((const void*)k_contact_cholesky, "k_contact_cholesky");
+  if (rc == GB_OK) {
+    k_contact_cholesky<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds,
+                                                                        Ms, Js, mu, Mis, JMs, Gs, Os, Ts, kkt, kinv,
+                                                                        oinv, osim, minv, jminv);
+    rc = cuda_error(cudaGetLastError(), "k_contact_cholesky");
   }
   scratch_free(scratch, st);
   return rc;

@@ -87,6 +87,8 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
 int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
                       const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
                       double* residuals, cudaStream_t st);
+int launch_contact_cholesky(const gb_model* M, long B, const gb_constraint_set* set, double mu, Arr q, Arr kkt,
+                            Arr kinv, Arr oinv, Arr osim, Arr minv, Arr jminv, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
 int launch_fk(const gb_model* m, int precision, long B, Arr q, Arr v, Arr a, Arr oMi, Arr vo, Arr ao, cudaStream_t st);
 int launch_jacobians(const gb_model* m, int precision, long B, Arr q, Arr J, cudaStream_t st);

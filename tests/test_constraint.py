@@ -329,3 +329,35 @@ def test_constraint_dynamics_derivatives_proximal_and_errors(humanoid):
     cms[0].corrector.Kp[:] = 1.0
     with pytest.raises(ValueError, match="world"):
         om.constraint_dynamics_derivatives(q, v, x, cs.stack_desc(cms))
+
+
+@pytest.mark.parametrize("mu", [0.0, 0.1])
+def test_contact_cholesky_accessors(humanoid, mu):
+    """ContactCholeskyDecomposition (unittest/contact-cholesky.cpp:270-420): matrix() is the KKT
+    matrix [[-mu I, J], [J^T, M]] built from the contact frames' Jacobians and M, inverse() its
+    inverse, getInverseOperationalSpaceInertiaMatrix() = J M^-1 J^T + mu I,
+    getOperationalSpaceInertiaMatrix() its inverse, getInverseMassMatrix() = M^-1, getJMinv() = J M^-1."""
+    model, om = humanoid
+    rng = np.random.default_rng(11)
+    cms = _contacts(model, rng, [(cs.CONTACT_6D, cs.LOCAL), (cs.CONTACT_3D, cs.LOCAL_WORLD_ALIGNED)])
+    q, v, x = sm.random_inputs(model, 6, 12)
+    out = om.contact_cholesky(q, cs.stack_desc(cms), mu=mu)
+    J = np.concatenate([_frame_jacobian_and_drift(model, om, q, v, c)[0] for c in cms], axis=1)
+    M = om.crba(q)
+    M = np.triu(M) + np.swapaxes(np.triu(M, 1), 1, 2)
+    nc, nv = J.shape[1], model.nv
+    H = np.zeros((6, nc + nv, nc + nv))
+    H[:, :nc, :nc] = -mu * np.eye(nc)
+    H[:, :nc, nc:] = J
+    H[:, nc:, :nc] = np.swapaxes(J, 1, 2)
+    H[:, nc:, nc:] = M
+    assert rel_err(out["matrix"], H) < 1e-12
+    eye = np.broadcast_to(np.eye(nc + nv), H.shape)
+    assert np.abs(np.einsum("bij,bjk->bik", out["inverse"], H) - eye).max() < 1e-9
+    Minv = np.linalg.inv(M)
+    JMJ = np.einsum("bij,bjk,blk->bil", J, Minv, J) + mu * np.eye(nc)
+    assert rel_err(out["osim_inverse"], JMJ) < 1e-11
+    assert rel_err(out["osim"], np.linalg.inv(JMJ)) < 1e-9
+    assert rel_err(out["minv"], Minv) < 1e-11
+    assert rel_err(out["jminv"], np.einsum("bij,bjk->bik", J, Minv)) < 1e-11
+

@@ -295,3 +295,77 @@ def test_constraint_dynamics_derivatives_proximal_and_errors():
         with pytest.raises(_capi.GBError) as e:
             pg.computeConstraintDynamicsDerivatives(model, data, bad)
         assert e.value.code == _capi.GB_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("mu", [0.0, 0.05])
+@pytest.mark.parametrize("name", [n for n in MODELS if n != "chain100"] + ["humanoid32-loop"])
+def test_contact_cholesky_matches_oracle(name, mu):
+    """ContactCholeskyDecomposition.compute and its accessors (contact-cholesky.hpp:168-265,
+    contact-cholesky.hxx:617-759) against the oracle's restatement of the reference's KKT
+    factorisation, relative to the oracle's own double / long-double gap of constraintDynamics on
+    the same case; the Python class reads the configurations of the last crba call."""
+    import torch
+
+    loop = name.endswith("-loop")
+    model = MODELS[name.replace("-loop", "")]()
+    om = OracleModel(model)
+    cms = _loop_constraints(model, 5) if loop else _constraints(model, 5)
+    desc = cs.stack_desc(cms)
+    q, v, x = sm.random_inputs(model, 64, 9)
+    ref = om.contact_cholesky(q, desc, mu=mu)
+    _, _, tol = _fp64_tol(om, q, v, 10 * x, desc, mu=mu)
+    tol = max(tol, 1e-10)
+    data = pg.createData(model)
+    pg.crba(model, data, _dev(q))
+    chol = pg.ContactCholeskyDecomposition(model, cms)
+    chol.compute(model, data, cms, [cs.RigidConstraintData(c) for c in cms], mu)
+    got = dict(matrix=chol.matrix(), inverse=chol.inverse(), osim_inverse=chol.getInverseOperationalSpaceInertiaMatrix(),
+               osim=chol.getOperationalSpaceInertiaMatrix(), minv=chol.getInverseMassMatrix(), jminv=chol.getJMinv())
+    assert chol.size() == model.nv + desc_dim(desc) and chol.constraintDim() == desc_dim(desc)
+    for k, r in ref.items():
+        assert rel_err(got[k].cpu().numpy(), r) < tol, k
+    rhs = np.random.default_rng(2).standard_normal((64, chol.size()))
+    assert rel_err(chol.solve(rhs), np.einsum("bij,bj->bi", ref["inverse"], rhs)) < tol
+    if mu == 0.0:  # updateDamping refactorises with another mu
+        chol.updateDamping(0.05)
+        r2 = om.contact_cholesky(q, desc, mu=0.05)
+        assert rel_err(chol.getInverseOperationalSpaceInertiaMatrix().cpu().numpy(), r2["osim_inverse"]) < tol
+    # the SOA layout through the C ABI gives the same bits
+    B, n, nc, nv = q.shape[0], chol.size(), chol.constraintDim(), model.nv
+    outs = [torch.empty((k, B), dtype=torch.float64, device="cuda") for k in (n * n, n * n, nc * nc, nc * nc, nv * nv, nc * nv)]
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    _capi.check(_capi.lib().gb_contact_cholesky(data.dev.h, _capi.GB_FP64, data.constraint_set.h, float(mu),
+                                                _capi.GB_LAYOUT_SOA, B, P(_dev(np.ascontiguousarray(q.T))),
+                                                *(P(o) for o in outs), None))
+    torch.cuda.synchronize()
+    for o, k in zip(outs, ("matrix", "inverse", "osim_inverse", "osim", "minv", "jminv")):
+        assert np.array_equal(o.cpu().numpy().T.reshape(got[k].shape), got[k].cpu().numpy()), k
+
+
+def desc_dim(desc):
+    return int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
+
+
+def test_contact_cholesky_without_constraints_and_errors():
+    """With no constraint the KKT matrix is M and its inverse M^-1; mu < 0 and a set of another
+    model are refused."""
+    model = MODELS["humanoid32"]()
+    om = OracleModel(model)
+    q, v, x = sm.random_inputs(model, 16, 3)
+    data = pg.createData(model)
+    chol = pg.ContactCholeskyDecomposition(model)
+    chol.compute(model, data, [], None, 0.0, q=_dev(q))
+    M = om.crba(q)
+    M = np.triu(M) + np.swapaxes(np.triu(M, 1), 1, 2)
+    assert rel_err(chol.matrix().cpu().numpy(), M) < FP64_TOL
+    assert rel_err(chol.inverse().cpu().numpy(), om.aba_derivatives(q, v, x)[3]) < 1e-11
+    with pytest.raises(ValueError):
+        chol.compute(model, data, [], None, -1.0, q=_dev(q))
+    other = pg.createData(MODELS["tree12"]())
+    pg.initConstraintDynamics(MODELS["tree12"](), other, [])
+    L = _capi.lib()
+    qq = np.ascontiguousarray(q[:2])
+    rc = L.gb_contact_cholesky(data.dev.h, _capi.GB_FP64, other.constraint_set.h, 0.0, _capi.GB_LAYOUT_INSTANCE, 2,
+                               qq.ctypes.data_as(C.c_void_p), None, None, None, None, None, None, None)
+    assert rc == _capi.GB_ERR_INVALID_ARGUMENT
+
