@@ -326,7 +326,16 @@ def _function_reference(om, fname, q, v, x, f, J, g, desc=None):
         "forward_dynamics_12rows": lambda: (om.forward_dynamics(q, v, t, J, g)[0],),
         "constraint_dynamics_18rows": lambda: (om.constraint_dynamics(q, v, t, desc)[0],),
         "constraint_dynamics_derivatives_18rows": lambda: om.constraint_dynamics_derivatives(q, v, t, desc)[2:8],
+        "contact_cholesky_18rows": lambda: tuple(om.contact_cholesky(q, desc).values()),
     }[fname]()
+
+
+def _contact_cholesky(pg, model, data, contacts, q):
+    """ContactCholeskyDecomposition.compute at q and its six accessors."""
+    chol = pg.ContactCholeskyDecomposition(model, contacts)
+    chol.compute(model, data, contacts, None, 0.0, q=q)
+    return (chol.matrix(), chol.inverse(), chol.getInverseOperationalSpaceInertiaMatrix(),
+            chol.getOperationalSpaceInertiaMatrix(), chol.getInverseMassMatrix(), chol.getJMinv())
 
 
 def humanoid_contacts(pg, model):
@@ -355,7 +364,8 @@ def measure_functions(torch, pg, sm):
     algorithms at batch 16384; RNEA, ABA and the ABA derivatives with external forces on
     every joint (the fext overloads) at the same batches; forwardDynamics with 12 constraint
     rows (two 6-D contacts) and constraintDynamics with four contacts (18 rows) at batch 65536, and
-    constraintDynamics followed by computeConstraintDynamicsDerivatives at batch 16384.  Each function's outputs are checked against the
+    constraintDynamics followed by computeConstraintDynamicsDerivatives and the contact Cholesky with
+    its six accessors at batch 16384.  Each function's outputs are checked against the
     FP64 oracle on 256 configurations strided over its batch: the max and median over those
     configurations of the relative error of every output."""
     from oracle.oracle import OracleModel
@@ -375,7 +385,8 @@ def measure_functions(torch, pg, sm):
                          ("nonlinear_effects", 65536), ("generalized_gravity", 65536),
                          ("forward_kinematics", 65536), ("joint_jacobians", 65536), ("rnea_fext", 65536),
                          ("aba_fext", 65536), ("aba_derivatives_fext", 16384), ("forward_dynamics_12rows", 65536),
-                         ("constraint_dynamics_18rows", 65536), ("constraint_dynamics_derivatives_18rows", 16384)):
+                         ("constraint_dynamics_18rows", 65536), ("constraint_dynamics_derivatives_18rows", 16384),
+                         ("contact_cholesky_18rows", 16384)):
             q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, B, 11))
             f = torch.randn((B, model.njoints, 6), dtype=torch.float64, device="cuda")
             Jc = torch.randn((B, 12, model.nv), dtype=torch.float64, device="cuda") if fname.startswith("forward_dyn") else None
@@ -400,6 +411,7 @@ def measure_functions(torch, pg, sm):
                 "constraint_dynamics_derivatives_18rows": lambda: (
                     pg.constraintDynamics(model, data, q, v, 10.0 * x, contacts),
                     pg.computeConstraintDynamicsDerivatives(model, data, contacts))[1],
+                "contact_cholesky_18rows": lambda: _contact_cholesky(pg, model, data, contacts, q),
             }[fname]
             ms = _time_call(torch, fn)
             res[fname] = {"batch": B, "ms": ms, "evals_per_s": B / ms * 1e3}
