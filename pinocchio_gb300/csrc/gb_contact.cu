@@ -1076,11 +1076,63 @@ __device__ void lane_gemm(int rows, int cols, int K, const double* A, int ars, i
     }
 }
 
-__global__ void __launch_bounds__(128)
+// Y(r0 + i, c) = sum over the constraint's dofs k of J(r0 + i, k) Bm(k, c) for the NR rows of one
+// constraint, the lane's columns c: the constraint's Jacobian rows vanish outside the ancestor
+// closure of its joints (the sorted list L = [count, dofs...]), so the sum runs over that list
+template <int NR, class F>
+__device__ void lane_jprod(const double* J, int sv, const short* L, int r0, int cols, const double* Bm, int bs,
+                           int lane, F store) {
+  const int len = L[0];
+  for (int c = lane; c < cols; c += 32) {
+    double t[NR];
+#pragma unroll
+    for (int i = 0; i < NR; ++i) t[i] = 0.0;
+    for (int p = 0; p < len; ++p) {
+      const int k = L[1 + p];
+      const double bk = Bm[k * bs + c];
+#pragma unroll
+      for (int i = 0; i < NR; ++i) t[i] += J[(r0 + i) * sv + k] * bk;
+    }
+#pragma unroll
+    for (int i = 0; i < NR; ++i) store(r0 + i, c, t[i]);
+  }
+}
+template <class F>
+__device__ void lane_jprod_all(const ConstraintDev* tab, int ncon, const short* clist, int nv, const double* J,
+                               int sv, const double* Bm, int bs, int lane, F store) {
+  for (int e = 0; e < ncon; ++e) {
+    const short* L = clist + (long)e * (nv + 1);
+    if (tab[e].type == GB_CONTACT_3D) lane_jprod<3>(J, sv, L, tab[e].row, nv, Bm, bs, lane, store);
+    else lane_jprod<6>(J, sv, L, tab[e].row, nv, Bm, bs, lane, store);
+  }
+}
+// x <- M^-1 x = U^-T D^-1 U^-1 x for one column x (stride sv) of shared memory, U and D staged
+__device__ __forceinline__ void col_minv(const gb::MView& m, const double* Uu, const double* Dv, int sv, double* x) {
+  const int nv = m.nv;
+  for (int k = nv - 2; k >= 0; --k) {  // x <- U^-1 x
+    const int n = m.nsfr[k] - 1;
+    double t = 0.0;
+    for (int j = 1; j <= n; ++j) t += Uu[k * sv + k + j] * x[(k + j) * sv];
+    x[k * sv] -= t;
+  }
+  for (int k = 0; k < nv; ++k) x[k * sv] /= Dv[k];
+  for (int k = 0; k < nv - 1; ++k) {  // x <- U^-T x
+    const int n = m.nsfr[k] - 1;
+    const double xk = x[k * sv];
+    for (int j = 1; j <= n; ++j) x[(k + j) * sv] -= Uu[k * sv + k + j] * xk;
+  }
+}
+
+// Per configuration, with W = M^-1 dtau_dx formed by tree solves (cholesky.hxx:483-500):
+// dlambda_dx = X(dac_dx - J W) and ddq_dx = -M^-1 (dtau_dx - J^T dlambda_dx) = -W + JMinv^T
+// dlambda_dx, the products with J over each constraint's dofs.  Shared memory per warp: two nv-row
+// buffers (M^-1 then dtau / W; the factor U), J, JMinv, R, X, tmp (nc rows each) at stride nv + 1,
+// G and osim (nc x (nc + 1)), D.
+__global__ void __launch_bounds__(128, 1)  // occupancy is set by shared memory: no register cap
     k_cd_assemble_warp(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
                        const double* Js, const double* Aqs, const double* Avs, const double* Cqs, Arr dtq, Arr dtv,
                        const int* iters, double mu, Arr ddq_dq, Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv,
-                       Arr dl_dtau) {
+                       Arr dl_dtau, const ConstraintDev* __restrict__ tab, int ncon, const short* __restrict__ clist) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
@@ -1088,45 +1140,34 @@ __global__ void __launch_bounds__(128)
   if (b >= B) return;  // whole warps leave together
   const int nv = m.nv, sv = nv + 1, sc = nc + 1, it = iters[b];
   double* base = reinterpret_cast<double*>(smem + ((bytes + 15) & ~15)) + (long)warp * cd_warp_doubles(nv, nc);
-  double *Mi = base, *dt = Mi + (long)nv * sv, *J = dt + (long)nv * sv, *JM = J + (long)nc * sv,
+  double *P1 = base, *Uu = P1 + (long)nv * sv, *J = Uu + (long)nv * sv, *JM = J + (long)nc * sv,
          *R = JM + (long)nc * sv, *X = R + (long)nc * sv, *T = X + (long)nc * sv, *G = T + (long)nc * sv,
          *O = G + (long)nc * sc, *Dv = O + (long)nc * sc;
-  // M^-1 = U^-T D^-1 U^-1 (cholesky.hxx:483-500) from U and D staged in shared memory (U in the
-  // dtau buffer, free until dtau is loaded): lane c solves column c, the rows of U read by broadcast
-  {
-    double* Uu = dt;
-    for (int e = lane; e < nv * nv; e += 32) Uu[(e / nv) * sv + e % nv] = Us[(long)e * B + b];
-    for (int k = lane; k < nv; k += 32) Dv[k] = Ds[(long)k * B + b];
-    __syncwarp();
-    for (int c = lane; c < nv; c += 32) {
-      double* x = Mi + c;  // column c, stride sv
-      for (int k = 0; k < nv; ++k) x[k * sv] = k == c ? 1.0 : 0.0;
-      for (int k = nv - 2; k >= 0; --k) {  // x <- U^-1 x
-        const int n = m.nsfr[k] - 1;
-        double t = 0.0;
-        for (int j = 1; j <= n; ++j) t += Uu[k * sv + k + j] * x[(k + j) * sv];
-        x[k * sv] -= t;
-      }
-      for (int k = 0; k < nv; ++k) x[k * sv] /= Dv[k];
-      for (int k = 0; k < nv - 1; ++k) {  // x <- U^-T x
-        const int n = m.nsfr[k] - 1;
-        const double xk = x[k * sv];
-        for (int j = 1; j <= n; ++j) x[(k + j) * sv] -= Uu[k * sv + k + j] * xk;
-      }
-    }
-  }
+  double* Mi = P1;  // M^-1 until ddq_dtau is written, then dtau_dx / W
+  for (int e = lane; e < nv * nv; e += 32) Uu[(e / nv) * sv + e % nv] = Us[(long)e * B + b];
+  for (int k = lane; k < nv; k += 32) Dv[k] = Ds[(long)k * B + b];
   for (int e = lane; e < nc * nv; e += 32) J[(e / nv) * sv + e % nv] = Js[(long)e * B + b];
   __syncwarp();
-  // JMinv = J M^-1
-  lane_gemm(nc, nv, nv, J, sv, 1, Mi, sv, lane, [&](int r, int c, double t) { JM[r * sv + c] = t; });
+  for (int c = lane; c < nv; c += 32) {  // M^-1: lane c solves column c
+    double* x = Mi + c;
+    for (int k = 0; k < nv; ++k) x[k * sv] = k == c ? 1.0 : 0.0;
+    col_minv(m, Uu, Dv, sv, x);
+  }
   __syncwarp();
-  // G = JMinv J^T + mu I (Bm(k, c) = J(c, k): the transposed read is a column of J)
-  for (int c = lane; c < nc; c += 32)
+  // JMinv = J M^-1 over each constraint's dofs
+  lane_jprod_all(tab, ncon, clist, nv, J, sv, Mi, sv, lane, [&](int r, int c, double t) { JM[r * sv + c] = t; });
+  __syncwarp();
+  // G = JMinv J^T + mu I (lane c: row c of J, over its constraint's dofs)
+  for (int c = lane; c < nc; c += 32) {
+    int e = 0;
+    while (e + 1 < ncon && tab[e + 1].row <= c) ++e;
+    const short* L = clist + (long)e * (nv + 1);
     for (int r = 0; r < nc; ++r) {
       double t = 0.0;
-      for (int k = 0; k < nv; ++k) t += JM[r * sv + k] * J[c * sv + k];
+      for (int p = 0; p < L[0]; ++p) t += JM[r * sv + L[1 + p]] * J[c * sv + L[1 + p]];
       G[r * sc + c] = t + (r == c ? mu : 0.0);
     }
+  }
   __syncwarp();
   if (lane == 0)  // G = L L^T in place (lower)
     for (int j = 0; j < nc; ++j) {
@@ -1176,29 +1217,30 @@ __global__ void __launch_bounds__(128)
     lane_gemm(nv, nv, nc, JM, 1, sv, X, sv, lane,
               [&](int r, int c, double t) { od[(long)r * nv + c] = Mi[r * sv + c] + t; });
   }
+  double* W = P1;
   for (int pass = 0; pass < 2; ++pass) {
     const Arr& dta = pass == 0 ? dtq : dtv;
     const double* A = pass == 0 ? Aqs : Avs;
     const gb::In dti{dta.p + b * dta.is, dta.es};
     __syncwarp();
-    for (int e = lane; e < nv * nv; e += 32) dt[(e / nv) * sv + e % nv] = dti[e];
+    for (int e = lane; e < nv * nv; e += 32) W[(e / nv) * sv + e % nv] = dti[e];
     __syncwarp();
-    // R = dac_dx - JMinv dtau_dx
-    lane_gemm(nc, nv, nv, JM, sv, 1, dt, sv, lane,
-              [&](int r, int c, double t) { R[r * sv + c] = A[(long)(r * nv + c) * B + b] - t; });
+    for (int c = lane; c < nv; c += 32) col_minv(m, Uu, Dv, sv, W + c);  // W = M^-1 dtau_dx
+    __syncwarp();
+    // R = dac_dx - J W  (= dac_dx - JMinv dtau_dx)
+    lane_jprod_all(tab, ncon, clist, nv, J, sv, W, sv, lane,
+                   [&](int r, int c, double t) { R[r * sv + c] = A[(long)(r * nv + c) * B + b] - t; });
     __syncwarp();
     prox(R);
-    // dtau_dx -= J^T dlambda_dx (A(r, k) = J(k, r); column c is lane c's)
-    lane_gemm(nv, nv, nc, J, 1, sv, X, sv, lane, [&](int r, int c, double t) { dt[r * sv + c] -= t; });
-    __syncwarp();
     const Arr& od = pass == 0 ? ddq_dq : ddq_dv;
     const Arr& ol = pass == 0 ? dl_dq : dl_dv;
     const gb::Out o{const_cast<double*>(od.p) + b * od.is, od.es};
     const gb::Out l{nc > 0 ? const_cast<double*>(ol.p) + b * ol.is : nullptr, ol.es};
-    bool finite = true;  // ddq_dx = -M^-1 dtau_dx
-    lane_gemm(nv, nv, nv, Mi, sv, 1, dt, sv, lane, [&](int r, int c, double t) {
-      finite = finite && gb::finite_value(t);
-      o[(long)r * nv + c] = -t;
+    bool finite = true;  // ddq_dx = -W + JMinv^T dlambda_dx
+    lane_gemm(nv, nv, nc, JM, 1, sv, X, sv, lane, [&](int r, int c, double t) {
+      const double y = t - W[r * sv + c];
+      finite = finite && gb::finite_value(y);
+      o[(long)r * nv + c] = y;
     });
     if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
     for (int e = lane; e < nc * nv; e += 32)
@@ -1350,6 +1392,14 @@ int launch_contact(const gb_model* M, int precision, bool impulse, long B, int n
   return rc;
 }
 
+// the constraint set's device table: the models, their side codes, the ancestor-closure masks and
+// then (2-byte aligned) the closure lists [count, dofs...] of nv + 1 entries per model
+const short* closure_lists(const gb_constraint_set* set, int nv) {
+  return reinterpret_cast<const short*>(
+      static_cast<const unsigned char*>(set->d_mem) +
+      ((sizeof(ConstraintDev) * (size_t)set->n + 2 * (size_t)set->n * nv + 1) & ~(size_t)1));
+}
+
 int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
                       const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
                       double* residuals, cudaStream_t st) {
@@ -1367,9 +1417,7 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
   const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
   const signed char* sp = reinterpret_cast<const signed char*>(tab + (set->n > 0 ? set->n : 0));
   const signed char* cmask = sp + (long)set->n * nv;
-  const short* clist = reinterpret_cast<const short*>(
-      static_cast<const unsigned char*>(set->d_mem) +
-      ((sizeof(ConstraintDev) * (size_t)set->n + 2 * (size_t)set->n * nv + 1) & ~(size_t)1));
+  const short* clist = closure_lists(set, (int)nv);
   rc = launch_crba(M, GB_FP64, false, B, q, Arr{Ms, 1, B}, Arr{Us, 1, B}, Arr{Ds, 1, B}, st);
   if (rc == GB_OK) {
     const gb::BlobHeader* h = reinterpret_cast<const gb::BlobHeader*>(M->blob.data());
@@ -1495,6 +1543,7 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
     return e == cudaSuccess ? GB_OK : cuda_error(e, name);
   };
   const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
+  const short* clist = closure_lists(set, (int)nv);
   if (rc == GB_OK && set->n > 0) {
     switch (M->cap) {
 #define GB_CD_SETUP(C)                                                                                       \
@@ -1536,7 +1585,7 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
       const long g = (B + wpb - 1) / wpb;
       k_cd_assemble_warp<<<(unsigned)g, 32 * wpb, smem, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Aq,
                                                             Av, Cq, dtqa, dtva, its, s.mu, ddq_dq, ddq_dv, ddq_dtau,
-                                                            dl_dq, dl_dv, dl_dtau);
+                                                            dl_dq, dl_dv, dl_dtau, tab, set->n, clist);
       rc = cuda_error(cudaGetLastError(), "k_cd_assemble_warp");
     }
   } else if (rc == GB_OK) {
