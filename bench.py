@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--no-extra", action="store_true",
                    help="skip the per-function, heterogeneous-batch and rollout measurements")
     p.add_argument("--only", choices=["rnea", "aba", "crba", "rnea_derivatives", "aba_derivatives",
-                                      "constraint_dynamics", "constraint_dynamics_derivatives"], default=None,
+                                      "constraint_dynamics", "constraint_dynamics_derivatives", "contact_cholesky"],
+                   default=None,
                    help="time one batched call on the humanoid (for profiling), print its timing and exit")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     return p.parse_args()
@@ -1006,6 +1007,7 @@ def run_only(args):
         "crba": lambda: pg.crba(model, data, qd),
         "rnea_derivatives": lambda: pg.computeRNEADerivatives(model, data, qd, vd, xd),
         "aba_derivatives": lambda: pg.computeABADerivatives(model, data, qd, vd, xd),
+        "contact_cholesky": lambda: _contact_cholesky(pg, model, data, contacts, qd),
     }[args.only]
     for _ in range(args.warmup):
         fn()

@@ -658,8 +658,9 @@ __global__ void __launch_bounds__(kThreads)
 // PointClassicAccelerationDerivativesBackwardStep, kinematics-derivatives.hxx:700-880), the force
 // derivative term of world-aligned constraints (hxx:1000-1040) and the constraint forces as forces
 // on the constraint joints (ContactForceContribution, hxx:225-342) for the inverse dynamics
-// derivatives; then k_cd_assemble (M^-1, the operational-space inertia, the proximal recursion,
-// hxx:815-990).
+// derivatives; then the assembly as column-parallel steps (M^-1, the operational-space inertia,
+// the proximal recursion, hxx:815-990: k_tree_solve_cols, k_jprod_rows, k_delassus, k_prox_cols,
+// k_out_rows).
 
 __device__ void translate_motion(const double* p, M6d& m) {  // linear -= p x angular
   double w[3];
@@ -929,424 +930,188 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// The assembly, per configuration (FP64): M^-1 from the tree factorisation, JMinv = J M^-1,
-// osim = (J M^-1 J^T + mu I)^-1, the proximal recursion X_1 = -osim R, X_k = osim (mu X_{k-1} - R)
-// over the configuration's iteration count, then (hxx:815-990)
-//   dlambda_dtau = X(JMinv), ddq_dtau = M^-1 + JMinv^T dlambda_dtau,
-//   dlambda_dx = X(dac_dx - JMinv dtau_dx), ddq_dx = -M^-1 (dtau_dx - J^T dlambda_dx)  (x = q, v),
-//   dlambda_dq += the world-aligned force term.
+// ---- the assembly as column-parallel steps: one thread per (configuration, column or row) ----
+// Thread t covers configuration b = t % B and column (or row) c = t / B: the 32 threads of a warp are
+// consecutive configurations of one column, so every [element][configuration] array they touch is
+// read and written in 256-byte lines, and a batch of B configurations gives B x nv threads instead
+// of B.  Element (k, c) of an m x n per-configuration matrix X sits at X[(k * n + c) * B + b].
+
+// X[:, c] <- M^-1 X[:, c] for the columns c < ncols of an nv x ncols matrix (identity: from the unit
+// columns, i.e. X = M^-1), by the tree factorisation M = U D U^T (cholesky.hxx:483-500)
 __global__ void __launch_bounds__(kThreads)
-    k_cd_assemble(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
-                  const double* Js, const double* Aqs, const double* Avs, const double* Cqs, double* dtqs,
-                  double* dtvs, const int* iters, double mu, double* Mis, double* JMs, double* Gs, double* Os,
-                  double* Rs, double* Xs, double* Ts, Arr ddq_dq, Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv,
-                  Arr dl_dtau) {
+    k_tree_solve_cols(const unsigned char* blob, int bytes, long B, int ncols, const double* Us, const double* Ds,
+                      double* X, int identity) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
-  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  const int nv = m.nv, it = iters[b];
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * ncols) return;
+  const long b = t % B;
+  const int c = (int)(t / B);
   const Col U{const_cast<double*>(Us) + b, B}, D{const_cast<double*>(Ds) + b, B};
-  const Col J{const_cast<double*>(Js) + b, B}, Aq{const_cast<double*>(Aqs) + b, B};
-  const Col Av{const_cast<double*>(Avs) + b, B}, Cq{const_cast<double*>(Cqs) + b, B};
-  const Col Mi{Mis + b, B}, JM{JMs + b, B}, G{Gs + b, B}, O{Os + b, B}, R{Rs + b, B}, X{Xs + b, B}, T{Ts + b, B};
-  for (int c = 0; c < nv; ++c) {  // M^-1, column by column
-    const Col col{Mis + b + (long)c * B, (long)nv * B};
-    for (int k = 0; k < nv; ++k) col[k] = k == c ? 1.0 : 0.0;
-    chol_solve(m, U, D, col);
-  }
-  for (int r = 0; r < nc; ++r)
-    for (int c = 0; c < nv; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < nv; ++k) s += J[(long)r * nv + k] * Mi[(long)k * nv + c];
-      JM[(long)r * nv + c] = s;
-    }
-  for (int r = 0; r < nc; ++r)
-    for (int c = 0; c <= r; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < nv; ++k) s += JM[(long)r * nv + k] * J[(long)c * nv + k];
-      G[(long)r * nc + c] = s + (r == c ? mu : 0.0);
-    }
-  for (int jc = 0; jc < nc; ++jc) {  // LLT in place (lower)
-    double s = G[(long)jc * nc + jc];
-    for (int k = 0; k < jc; ++k) s -= G[(long)jc * nc + k] * G[(long)jc * nc + k];
-    gb::check_pivot(m, s);
-    const double l = sqrt(s);
-    G[(long)jc * nc + jc] = l;
-    for (int i = jc + 1; i < nc; ++i) {
-      double t = G[(long)i * nc + jc];
-      for (int k = 0; k < jc; ++k) t -= G[(long)i * nc + k] * G[(long)jc * nc + k];
-      G[(long)i * nc + jc] = t / l;
-    }
-  }
-  for (int c = 0; c < nc; ++c) {  // osim = G^-1, column by column
-    const Col col{Os + b + (long)c * B, (long)nc * B};
-    for (int k = 0; k < nc; ++k) col[k] = k == c ? 1.0 : 0.0;
-    llt_solve(G, nc, col);
-  }
-  auto prox = [&](const Col& Rm) {  // X <- the recursion on the right-hand side Rm (nc x nv)
-    for (int r = 0; r < nc; ++r)
-      for (int c = 0; c < nv; ++c) {
-        double s = 0.0;
-        for (int k = 0; k < nc; ++k) s += O[(long)r * nc + k] * Rm[(long)k * nv + c];
-        X[(long)r * nv + c] = -s;
-      }
-    for (int k2 = 1; k2 < it; ++k2) {
-      for (long k = 0; k < (long)nc * nv; ++k) T[k] = mu * X[k] - Rm[k];
-      for (int r = 0; r < nc; ++r)
-        for (int c = 0; c < nv; ++c) {
-          double s = 0.0;
-          for (int k = 0; k < nc; ++k) s += O[(long)r * nc + k] * T[(long)k * nv + c];
-          X[(long)r * nv + c] = s;
-        }
-    }
-  };
-  const gb::Out odt{const_cast<double*>(ddq_dtau.p) + b * ddq_dtau.is, ddq_dtau.es};
-  const gb::Out oldt{nc > 0 ? const_cast<double*>(dl_dtau.p) + b * dl_dtau.is : nullptr, dl_dtau.es};
-  prox(JM);
-  for (long k = 0; k < (long)nc * nv; ++k) oldt[k] = X[k];
-  for (int r = 0; r < nv; ++r)
-    for (int c = 0; c < nv; ++c) {
-      double s = Mi[(long)r * nv + c];
-      for (int k = 0; k < nc; ++k) s += JM[(long)k * nv + r] * X[(long)k * nv + c];
-      odt[(long)r * nv + c] = s;
-    }
-  for (int pass = 0; pass < 2; ++pass) {
-    const Col dt{(pass == 0 ? dtqs : dtvs) + b, B};
-    const Col& A = pass == 0 ? Aq : Av;
-    const Arr& od = pass == 0 ? ddq_dq : ddq_dv;
-    const Arr& ol = pass == 0 ? dl_dq : dl_dv;
-    const gb::Out o{const_cast<double*>(od.p) + b * od.is, od.es};
-    const gb::Out l{nc > 0 ? const_cast<double*>(ol.p) + b * ol.is : nullptr, ol.es};
-    for (int r = 0; r < nc; ++r)
-      for (int c = 0; c < nv; ++c) {
-        double s = 0.0;
-        for (int k = 0; k < nv; ++k) s += JM[(long)r * nv + k] * dt[(long)k * nv + c];
-        R[(long)r * nv + c] = A[(long)r * nv + c] - s;
-      }
-    prox(R);
-    for (int r = 0; r < nv; ++r)
-      for (int c = 0; c < nv; ++c) {
-        double s = 0.0;
-        for (int k = 0; k < nc; ++k) s += J[(long)k * nv + r] * X[(long)k * nv + c];
-        dt[(long)r * nv + c] -= s;
-      }
-    bool finite = true;
-    for (int r = 0; r < nv; ++r)
-      for (int c = 0; c < nv; ++c) {
-        double s = 0.0;
-        for (int k = 0; k < nv; ++k) s += Mi[(long)r * nv + k] * dt[(long)k * nv + c];
-        finite = finite && gb::finite_value(s);
-        o[(long)r * nv + c] = -s;
-      }
-    if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
-    for (long k = 0; k < (long)nc * nv; ++k) l[k] = X[k] + (pass == 0 ? Cq[k] : 0.0);
-  }
+  const Col x{X + (long)c * B + b, (long)ncols * B};
+  if (identity)
+    for (int k = 0; k < m.nv; ++k) x[k] = k == c ? 1.0 : 0.0;
+  chol_solve(m, U, D, x);
 }
 
-// The same assembly with one warp per configuration: lanes own columns (c = lane, lane + 32, ...),
-// the operands of a configuration sit in shared memory (rows padded to an odd stride), broadcast
-// reads along the rows.  Shared memory per warp, in doubles: M^-1 and dtau (nv rows each), J, JMinv,
-// R, X, tmp (nc rows each) at stride nv + 1, G and osim (nc x (nc + 1)).
-__host__ __device__ inline long cd_warp_doubles(int nv, int nc) {
-  return 2L * nv * (nv + 1) + 5L * nc * (nv + 1) + 2L * nc * (nc + 1) + nv;
-}
-
-// Y(r, c) for rows r < rows and the lane's columns c: Y = sum_k A(r, k) Bm(k, c), A(r, k) =
-// A[r * ars + k * acs] read by broadcast, Bm(k, c) = Bm[k * bs + c]; four rows per pass (four
-// independent accumulations per Bm load); store(r, c, value) consumes the results
-template <class F>
-__device__ void lane_gemm(int rows, int cols, int K, const double* A, int ars, int acs, const double* Bm, int bs,
-                          int lane, F store) {
-  for (int c = lane; c < cols; c += 32)
-    for (int r0 = 0; r0 < rows; r0 += 4) {
-      const int r1 = min(r0 + 1, rows - 1), r2 = min(r0 + 2, rows - 1), r3 = min(r0 + 3, rows - 1);
-      double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
-      for (int k = 0; k < K; ++k) {
-        const double bk = Bm[k * bs + c];
-        t0 += A[r0 * ars + k * acs] * bk;
-        t1 += A[r1 * ars + k * acs] * bk;
-        t2 += A[r2 * ars + k * acs] * bk;
-        t3 += A[r3 * ars + k * acs] * bk;
-      }
-      store(r0, c, t0);
-      if (r0 + 1 < rows) store(r0 + 1, c, t1);
-      if (r0 + 2 < rows) store(r0 + 2, c, t2);
-      if (r0 + 3 < rows) store(r0 + 3, c, t3);
-    }
-}
-
-// Y(r0 + i, c) = sum over the constraint's dofs k of J(r0 + i, k) Bm(k, c) for the NR rows of one
-// constraint, the lane's columns c: the constraint's Jacobian rows vanish outside the ancestor
-// closure of its joints (the sorted list L = [count, dofs...]), so the sum runs over that list
-template <int NR, class F>
-__device__ void lane_jprod(const double* J, int sv, const short* L, int r0, int cols, const double* Bm, int bs,
-                           int lane, F store) {
+// Y(r, c) = (A(r, c) if A) + sign * sum over row r's constraint dofs k of J(r, k) S(k, c), c < ncols,
+// one thread per (configuration, row r < nc); J nc x nv, S nv x ncols, A and Y nc x ncols
+__global__ void __launch_bounds__(kThreads)
+    k_jprod_rows(long B, int nc, int nv, int ncols, const ConstraintDev* __restrict__ tab, int ncon,
+                 const short* __restrict__ clist, const double* Js, const double* S, const double* A, double sign,
+                 double* Y) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * nc) return;
+  const long b = t % B;
+  const int r = (int)(t / B);
+  int e = 0;
+  while (e + 1 < ncon && tab[e + 1].row <= r) ++e;
+  const short* L = clist + (long)e * (nv + 1);
   const int len = L[0];
-  for (int c = lane; c < cols; c += 32) {
-    double t[NR];
-#pragma unroll
-    for (int i = 0; i < NR; ++i) t[i] = 0.0;
+  for (int c = 0; c < ncols; ++c) {
+    double acc = 0.0;
     for (int p = 0; p < len; ++p) {
       const int k = L[1 + p];
-      const double bk = Bm[k * bs + c];
-#pragma unroll
-      for (int i = 0; i < NR; ++i) t[i] += J[(r0 + i) * sv + k] * bk;
+      acc += Js[((long)r * nv + k) * B + b] * S[((long)k * ncols + c) * B + b];
     }
-#pragma unroll
-    for (int i = 0; i < NR; ++i) store(r0 + i, c, t[i]);
-  }
-}
-template <class F>
-__device__ void lane_jprod_all(const ConstraintDev* tab, int ncon, const short* clist, int nv, const double* J,
-                               int sv, const double* Bm, int bs, int lane, F store) {
-  for (int e = 0; e < ncon; ++e) {
-    const short* L = clist + (long)e * (nv + 1);
-    if (tab[e].type == GB_CONTACT_3D) lane_jprod<3>(J, sv, L, tab[e].row, nv, Bm, bs, lane, store);
-    else lane_jprod<6>(J, sv, L, tab[e].row, nv, Bm, bs, lane, store);
-  }
-}
-// x <- M^-1 x = U^-T D^-1 U^-1 x for one column x (stride sv) of shared memory, U and D staged
-__device__ __forceinline__ void col_minv(const gb::MView& m, const double* Uu, const double* Dv, int sv, double* x) {
-  const int nv = m.nv;
-  for (int k = nv - 2; k >= 0; --k) {  // x <- U^-1 x
-    const int n = m.nsfr[k] - 1;
-    double t = 0.0;
-    for (int j = 1; j <= n; ++j) t += Uu[k * sv + k + j] * x[(k + j) * sv];
-    x[k * sv] -= t;
-  }
-  for (int k = 0; k < nv; ++k) x[k * sv] /= Dv[k];
-  for (int k = 0; k < nv - 1; ++k) {  // x <- U^-T x
-    const int n = m.nsfr[k] - 1;
-    const double xk = x[k * sv];
-    for (int j = 1; j <= n; ++j) x[(k + j) * sv] -= Uu[k * sv + k + j] * xk;
+    const long o = ((long)r * ncols + c) * B + b;
+    Y[o] = (A ? A[o] : 0.0) + sign * acc;
   }
 }
 
-// Per configuration, with W = M^-1 dtau_dx formed by tree solves (cholesky.hxx:483-500):
-// dlambda_dx = X(dac_dx - J W) and ddq_dx = -M^-1 (dtau_dx - J^T dlambda_dx) = -W + JMinv^T
-// dlambda_dx, the products with J over each constraint's dofs.  Shared memory per warp: two nv-row
-// buffers (M^-1 then dtau / W; the factor U), J, JMinv, R, X, tmp (nc rows each) at stride nv + 1,
-// G and osim (nc x (nc + 1)), D.
-__global__ void __launch_bounds__(128, 1)  // occupancy is set by shared memory: no register cap
-    k_cd_assemble_warp(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
-                       const double* Js, const double* Aqs, const double* Avs, const double* Cqs, Arr dtq, Arr dtv,
-                       const int* iters, double mu, Arr ddq_dq, Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv,
-                       Arr dl_dtau, const ConstraintDev* __restrict__ tab, int ncon, const short* __restrict__ clist) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const gb::MView m = stage_model(blob, bytes, smem);
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
-  const long b = (long)blockIdx.x * wpb + warp;
-  if (b >= B) return;  // whole warps leave together
-  const int nv = m.nv, sv = nv + 1, sc = nc + 1, it = iters[b];
-  double* base = reinterpret_cast<double*>(smem + ((bytes + 15) & ~15)) + (long)warp * cd_warp_doubles(nv, nc);
-  double *P1 = base, *Uu = P1 + (long)nv * sv, *J = Uu + (long)nv * sv, *JM = J + (long)nc * sv,
-         *R = JM + (long)nc * sv, *X = R + (long)nc * sv, *T = X + (long)nc * sv, *G = T + (long)nc * sv,
-         *O = G + (long)nc * sc, *Dv = O + (long)nc * sc;
-  double* Mi = P1;  // M^-1 until ddq_dtau is written, then dtau_dx / W
-  for (int e = lane; e < nv * nv; e += 32) Uu[(e / nv) * sv + e % nv] = Us[(long)e * B + b];
-  for (int k = lane; k < nv; k += 32) Dv[k] = Ds[(long)k * B + b];
-  for (int e = lane; e < nc * nv; e += 32) J[(e / nv) * sv + e % nv] = Js[(long)e * B + b];
-  __syncwarp();
-  for (int c = lane; c < nv; c += 32) {  // M^-1: lane c solves column c
-    double* x = Mi + c;
-    for (int k = 0; k < nv; ++k) x[k * sv] = k == c ? 1.0 : 0.0;
-    col_minv(m, Uu, Dv, sv, x);
-  }
-  __syncwarp();
-  // JMinv = J M^-1 over each constraint's dofs
-  lane_jprod_all(tab, ncon, clist, nv, J, sv, Mi, sv, lane, [&](int r, int c, double t) { JM[r * sv + c] = t; });
-  __syncwarp();
-  // G = JMinv J^T + mu I (lane c: row c of J, over its constraint's dofs)
-  for (int c = lane; c < nc; c += 32) {
-    int e = 0;
-    while (e + 1 < ncon && tab[e + 1].row <= c) ++e;
-    const short* L = clist + (long)e * (nv + 1);
-    for (int r = 0; r < nc; ++r) {
-      double t = 0.0;
-      for (int p = 0; p < L[0]; ++p) t += JM[r * sv + L[1 + p]] * J[c * sv + L[1 + p]];
-      G[r * sc + c] = t + (r == c ? mu : 0.0);
-    }
-  }
-  __syncwarp();
-  if (lane == 0)  // G = L L^T in place (lower)
-    for (int j = 0; j < nc; ++j) {
-      double t = G[j * sc + j];
-      for (int k = 0; k < j; ++k) t -= G[j * sc + k] * G[j * sc + k];
-      gb::check_pivot(m, t);
-      const double l = sqrt(t);
-      G[j * sc + j] = l;
-      for (int i = j + 1; i < nc; ++i) {
-        double u = G[i * sc + j];
-        for (int k = 0; k < j; ++k) u -= G[i * sc + k] * G[j * sc + k];
-        G[i * sc + j] = u / l;
-      }
-    }
-  __syncwarp();
-  for (int c = lane; c < nc; c += 32) {  // osim = G^-1: lane c solves column c
-    for (int i = 0; i < nc; ++i) {
-      double t = i == c ? 1.0 : 0.0;
-      for (int k = 0; k < i; ++k) t -= G[i * sc + k] * O[k * sc + c];
-      O[i * sc + c] = t / G[i * sc + i];
-    }
-    for (int i = nc - 1; i >= 0; --i) {
-      double t = O[i * sc + c];
-      for (int k = i + 1; k < nc; ++k) t -= G[k * sc + i] * O[k * sc + c];
-      O[i * sc + c] = t / G[i * sc + i];
-    }
-  }
-  __syncwarp();
-  auto prox = [&](const double* Rm) {  // X <- the recursion on Rm (nc x nv, stride sv)
-    lane_gemm(nc, nv, nc, O, sc, 1, Rm, sv, lane, [&](int r, int c, double t) { X[r * sv + c] = -t; });
-    for (int k2 = 1; k2 < it; ++k2) {
-      __syncwarp();
-      for (int c = lane; c < nv; c += 32)
-        for (int r = 0; r < nc; ++r) T[r * sv + c] = mu * X[r * sv + c] - Rm[r * sv + c];
-      __syncwarp();
-      lane_gemm(nc, nv, nc, O, sc, 1, T, sv, lane, [&](int r, int c, double t) { X[r * sv + c] = t; });
-    }
-    __syncwarp();
-  };
-  // the derivatives in tau
-  prox(JM);
-  {
-    const gb::Out od{const_cast<double*>(ddq_dtau.p) + b * ddq_dtau.is, ddq_dtau.es};
-    const gb::Out ol{nc > 0 ? const_cast<double*>(dl_dtau.p) + b * dl_dtau.is : nullptr, dl_dtau.es};
-    for (int e = lane; e < nc * nv; e += 32) ol[e] = X[(e / nv) * sv + e % nv];
-    // ddq_dtau = M^-1 + JMinv^T X (A(r, k) = JM(k, r))
-    lane_gemm(nv, nv, nc, JM, 1, sv, X, sv, lane,
-              [&](int r, int c, double t) { od[(long)r * nv + c] = Mi[r * sv + c] + t; });
-  }
-  double* W = P1;
-  for (int pass = 0; pass < 2; ++pass) {
-    const Arr& dta = pass == 0 ? dtq : dtv;
-    const double* A = pass == 0 ? Aqs : Avs;
-    const gb::In dti{dta.p + b * dta.is, dta.es};
-    __syncwarp();
-    for (int e = lane; e < nv * nv; e += 32) W[(e / nv) * sv + e % nv] = dti[e];
-    __syncwarp();
-    for (int c = lane; c < nv; c += 32) col_minv(m, Uu, Dv, sv, W + c);  // W = M^-1 dtau_dx
-    __syncwarp();
-    // R = dac_dx - J W  (= dac_dx - JMinv dtau_dx)
-    lane_jprod_all(tab, ncon, clist, nv, J, sv, W, sv, lane,
-                   [&](int r, int c, double t) { R[r * sv + c] = A[(long)(r * nv + c) * B + b] - t; });
-    __syncwarp();
-    prox(R);
-    const Arr& od = pass == 0 ? ddq_dq : ddq_dv;
-    const Arr& ol = pass == 0 ? dl_dq : dl_dv;
-    const gb::Out o{const_cast<double*>(od.p) + b * od.is, od.es};
-    const gb::Out l{nc > 0 ? const_cast<double*>(ol.p) + b * ol.is : nullptr, ol.es};
-    bool finite = true;  // ddq_dx = -W + JMinv^T dlambda_dx
-    lane_gemm(nv, nv, nc, JM, 1, sv, X, sv, lane, [&](int r, int c, double t) {
-      const double y = t - W[r * sv + c];
-      finite = finite && gb::finite_value(y);
-      o[(long)r * nv + c] = y;
-    });
-    if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
-    for (int e = lane; e < nc * nv; e += 32)
-      l[e] = X[(e / nv) * sv + e % nv] + (pass == 0 ? Cqs[(long)e * B + b] : 0.0);
-  }
-}
-// ContactCholeskyDecomposition::compute at q and its accessors (contact-cholesky.hpp:168-265,
-// contact-cholesky.hxx:152-304, 617-759), one thread per configuration, from the tree
-// factorisation M = U D U^T, the symmetric M and the constraint rows J (all [element][configuration]):
-// JMinv = J M^-1 (a tree solve per row), OSIM^-1 = J M^-1 J^T + mu I (the damped Delassus matrix),
-// OSIM its inverse (LLT), M^-1 (a tree solve per column), the KKT matrix
-// [[-mu I, J], [J^T, M]] (constraint rows first, as the reference's matrix()) and its inverse
-// [[-OSIM, OSIM J M^-1], [M^-1 J^T OSIM, M^-1 - M^-1 J^T OSIM J M^-1]].  Outputs may be null.
+// per configuration: G = JMinv J^T + mu I (the damped Delassus matrix; a column over its row's
+// constraint dofs), its LLT in place and O = G^-1; oinv / osim (optional) take G and O
 __global__ void __launch_bounds__(kThreads)
-    k_contact_cholesky(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
-                       const double* Ms, const double* Js, double mu, double* Mis, double* JMs, double* Gs,
-                       double* Os, double* Ts, Arr kkt, Arr kinv, Arr oinv, Arr osim, Arr minv, Arr jminv) {
+    k_delassus(const unsigned char* blob, int bytes, long B, int nc, const ConstraintDev* __restrict__ tab, int ncon,
+               const short* __restrict__ clist, const double* Js, const double* JMs, double mu, double* Gs, double* Os,
+               Arr oinv, Arr osim) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
-  const int nv = m.nv, n = nc + nv;
-  const Col U{const_cast<double*>(Us) + b, B}, D{const_cast<double*>(Ds) + b, B};
-  const Col Mi{Mis + b, B}, JM{JMs + b, B}, G{Gs + b, B}, O{Os + b, B}, T{Ts + b, B};
-  const gb::In Ji{Js + b, B}, Mf{Ms + b, B};
+  const int nv = m.nv;
+  const Col G{Gs + b, B}, O{Os + b, B};
   auto out = [&](const Arr& a, long k) -> double& { return const_cast<double*>(a.p)[b * a.is + k * a.es]; };
-  const bool need_minv = minv.p || kinv.p, need_jm = nc > 0 && (jminv.p || oinv.p || osim.p || kinv.p);
-  for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);
-  if (need_minv)
-    for (int c = 0; c < nv; ++c) {  // column c of M^-1
-      const Col x{Mi.p + (long)c * B, (long)nv * B};
-      for (int k = 0; k < nv; ++k) x[k] = k == c ? 1.0 : 0.0;
-      chol_solve(m, U, D, x);
-    }
-  if (need_jm)
-    for (int r = 0; r < nc; ++r) {  // row r of J M^-1 = (M^-1 J_r^T)^T
-      const Col x{JM.p + (long)r * nv * B, B};
-      for (int k = 0; k < nv; ++k) x[k] = Ji[r * nv + k];
-      chol_solve(m, U, D, x);
-    }
-  if (need_jm) {
-    for (int i = 0; i < nc; ++i)  // J M^-1 J^T + mu I (lower), its LLT in G, OSIM = G^-T G^-1 in O
-      for (int j = 0; j <= i; ++j) {
-        double t = 0.0;
-        for (int k = 0; k < nv; ++k) t += JM[(long)i * nv + k] * Ji[j * nv + k];
-        G[(long)i * nc + j] = t + (i == j ? mu : 0.0);
-        if (oinv.p) {
-          out(oinv, (long)i * nc + j) = G[(long)i * nc + j];
-          out(oinv, (long)j * nc + i) = G[(long)i * nc + j];
-        }
+  for (int e = 0; e < ncon; ++e) {
+    const short* L = clist + (long)e * (nv + 1);
+    const int c0 = tab[e].row, c1 = c0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
+    for (int c = c0; c < c1; ++c)
+      for (int r = c; r < nc; ++r) {
+        double acc = 0.0;
+        for (int p = 0; p < L[0]; ++p)
+          acc += JMs[((long)r * nv + L[1 + p]) * B + b] * Js[((long)c * nv + L[1 + p]) * B + b];
+        G[(long)r * nc + c] = acc + (r == c ? mu : 0.0);
       }
-    if (osim.p || kinv.p) {
-      for (int j = 0; j < nc; ++j) {
-        double t = G[(long)j * nc + j];
-        for (int k = 0; k < j; ++k) t -= G[(long)j * nc + k] * G[(long)j * nc + k];
-        gb::check_pivot(m, t);
-        const double l = sqrt(t);
-        G[(long)j * nc + j] = l;
-        for (int i = j + 1; i < nc; ++i) {
-          double u = G[(long)i * nc + j];
-          for (int k = 0; k < j; ++k) u -= G[(long)i * nc + k] * G[(long)j * nc + k];
-          G[(long)i * nc + j] = u / l;
-        }
+  }
+  if (oinv.p)
+    for (int r = 0; r < nc; ++r)
+      for (int c = 0; c <= r; ++c) {
+        out(oinv, (long)r * nc + c) = G[(long)r * nc + c];
+        out(oinv, (long)c * nc + r) = G[(long)r * nc + c];
       }
-      for (int c = 0; c < nc; ++c) {  // column c of OSIM: (L L^T)^-1 e_c
-        const Col x{O.p + (long)c * B, (long)nc * B};
-        for (int k = 0; k < nc; ++k) x[k] = k == c ? 1.0 : 0.0;
-        llt_solve(G, nc, x);
-      }
-      if (osim.p)
-        for (long k = 0; k < (long)nc * nc; ++k) out(osim, k) = O[k];
+  for (int j = 0; j < nc; ++j) {
+    double t = G[(long)j * nc + j];
+    for (int k = 0; k < j; ++k) t -= G[(long)j * nc + k] * G[(long)j * nc + k];
+    gb::check_pivot(m, t);
+    const double l = sqrt(t);
+    G[(long)j * nc + j] = l;
+    for (int i = j + 1; i < nc; ++i) {
+      double u = G[(long)i * nc + j];
+      for (int k = 0; k < j; ++k) u -= G[(long)i * nc + k] * G[(long)j * nc + k];
+      G[(long)i * nc + j] = u / l;
     }
   }
-  if (jminv.p)
-    for (long k = 0; k < (long)nc * nv; ++k) out(jminv, k) = JM[k];
-  if (minv.p)
-    for (long k = 0; k < (long)nv * nv; ++k) out(minv, k) = Mi[k];
-  if (kkt.p)
-    for (int r = 0; r < n; ++r)
-      for (int c = 0; c < n; ++c) {
-        double x;
-        if (r < nc) x = c < nc ? (r == c ? -mu : 0.0) : Ji[r * nv + (c - nc)];
-        else x = c < nc ? Ji[c * nv + (r - nc)] : Mf[(long)(r - nc) * nv + (c - nc)];
-        out(kkt, (long)r * n + c) = x;
-      }
-  if (kinv.p) {
-    for (int r = 0; r < nc; ++r)  // T = OSIM J M^-1
-      for (int c = 0; c < nv; ++c) {
-        double t = 0.0;
-        for (int k = 0; k < nc; ++k) t += O[(long)r * nc + k] * JM[(long)k * nv + c];
-        T[(long)r * nv + c] = t;
-      }
+  for (int c = 0; c < nc; ++c) {
+    const Col x{O.p + (long)c * B, (long)nc * B};
+    for (int k = 0; k < nc; ++k) x[k] = k == c ? 1.0 : 0.0;
+    llt_solve(G, nc, x);
+    if (osim.p)
+      for (int k = 0; k < nc; ++k) out(osim, (long)k * nc + c) = x[k];
+  }
+}
+
+// X[:, c] = s1 O R[:, c], then it - 1 times X[:, c] = O (mu X[:, c] - R[:, c]) (the proximal
+// recursion of the derivatives, hxx:869-990, per column); one thread per (configuration, column
+// c < ncols), O nc x nc, R, X, Tm (scratch) nc x ncols; dl (optional): X + C (C optional)
+__global__ void __launch_bounds__(kThreads)
+    k_prox_cols(long B, int nc, int ncols, const double* Os, const int* iters, double mu, double s1, const double* R,
+                double* X, double* Tm, Arr dl, const double* C) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * ncols) return;
+  const long b = t % B;
+  const int c = (int)(t / B), it = iters ? iters[b] : 1;
+  auto at = [&](int k) { return ((long)k * ncols + c) * B + b; };
+  for (int r = 0; r < nc; ++r) {
+    double acc = 0.0;
+    for (int k = 0; k < nc; ++k) acc += Os[((long)r * nc + k) * B + b] * R[at(k)];
+    X[at(r)] = s1 * acc;
+  }
+  for (int k2 = 1; k2 < it; ++k2) {
+    for (int k = 0; k < nc; ++k) Tm[at(k)] = mu * X[at(k)] - R[at(k)];
+    for (int r = 0; r < nc; ++r) {
+      double acc = 0.0;
+      for (int k = 0; k < nc; ++k) acc += Os[((long)r * nc + k) * B + b] * Tm[at(k)];
+      X[at(r)] = acc;
+    }
+  }
+  if (dl.p)
     for (int r = 0; r < nc; ++r)
-      for (int c = 0; c < nc; ++c) out(kinv, (long)r * n + c) = -O[(long)r * nc + c];
-    for (int r = 0; r < nc; ++r)
-      for (int c = 0; c < nv; ++c) {
-        out(kinv, (long)r * n + nc + c) = T[(long)r * nv + c];
-        out(kinv, (long)(nc + c) * n + r) = T[(long)r * nv + c];
-      }
-    for (int i = 0; i < nv; ++i)
-      for (int j = i; j < nv; ++j) {
-        double t = Mi[(long)i * nv + j];
-        for (int k = 0; k < nc; ++k) t -= JM[(long)k * nv + i] * T[(long)k * nv + j];
-        out(kinv, (long)(nc + i) * n + nc + j) = t;
-        out(kinv, (long)(nc + j) * n + nc + i) = t;
-      }
+      const_cast<double*>(dl.p)[b * dl.is + ((long)r * ncols + c) * dl.es] = X[at(r)] + (C ? C[at(r)] : 0.0);
+}
+
+// Out(r, c) = bsign Base(r, c) + sum_k JM(k, r) X(k, c) for c < nv: one thread per (configuration,
+// row r < nv); Base nv x nv, JM and X nc x nv; Out in the caller's layout, at column offset
+// (ro, co) of an ld-wide matrix (ld = nv for the derivative outputs)
+__global__ void __launch_bounds__(kThreads)
+    k_out_rows(const unsigned char* blob, int bytes, long B, int nc, const double* Base, double bsign,
+               const double* JMs, const double* X, Arr out, int ld, int ro, int co) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const int nv = m.nv;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * nv) return;
+  const long b = t % B;
+  const int r = (int)(t / B);
+  double* o = const_cast<double*>(out.p) + b * out.is;
+  bool finite = true;
+  for (int c = 0; c < nv; ++c) {
+    double acc = bsign * Base[((long)r * nv + c) * B + b];
+    for (int k = 0; k < nc; ++k) acc += JMs[((long)k * nv + r) * B + b] * X[((long)k * nv + c) * B + b];
+    finite = finite && gb::finite_value(acc);
+    o[((long)(ro + r) * ld + co + c) * out.es] = acc;
+  }
+  if (!finite) gb::flag_numeric(m, gb::NUM_NONFINITE);
+}
+
+// The contact Cholesky's row-wise outputs, one thread per (configuration, row r < nc + nv), from
+// M^-1, J, JMinv, osim and Tn = -osim JMinv: the KKT matrix [[-mu I, J], [J^T, M]] (constraint rows
+// first, as the reference's matrix()), the blocks of its inverse other than the bottom-right one
+// ([[-osim, osim JMinv], [M^-1 J^T osim, .]]), M^-1 and JMinv; every output optional
+__global__ void __launch_bounds__(kThreads)
+    k_cc_rows(long B, int nc, int nv, double mu, const double* Ms, const double* Mis, const double* Js,
+              const double* JMs, const double* Os, const double* Tn, Arr kkt, Arr kinv, Arr minv, Arr jminv) {
+  const int n = nc + nv;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * n) return;
+  const long b = t % B;
+  const int r = (int)(t / B);
+  auto at = [&](const double* X, int ld, int i, int j) { return X[((long)i * ld + j) * B + b]; };
+  auto put = [&](const Arr& a, long k, double x) { const_cast<double*>(a.p)[b * a.is + k * a.es] = x; };
+  if (r < nc) {
+    if (kkt.p)
+      for (int c = 0; c < n; ++c) put(kkt, (long)r * n + c, c < nc ? (r == c ? -mu : 0.0) : at(Js, nv, r, c - nc));
+    if (kinv.p)
+      for (int c = 0; c < n; ++c) put(kinv, (long)r * n + c, c < nc ? -at(Os, nc, r, c) : -at(Tn, nv, r, c - nc));
+    if (jminv.p)
+      for (int c = 0; c < nv; ++c) put(jminv, (long)r * nv + c, at(JMs, nv, r, c));
+  } else {
+    const int i = r - nc;
+    if (kkt.p)
+      for (int c = 0; c < n; ++c) put(kkt, (long)r * n + c, c < nc ? at(Js, nv, c, i) : at(Ms, nv, i, c - nc));
+    if (kinv.p)
+      for (int c = 0; c < nc; ++c) put(kinv, (long)r * n + c, -at(Tn, nv, c, i));
+    if (minv.p)
+      for (int c = 0; c < nv; ++c) put(minv, (long)i * nv + c, at(Mis, nv, i, c));
   }
 }
 
@@ -1505,12 +1270,30 @@ int launch_contact_cholesky(const gb_model* M, long B, const gb_constraint_set* 
     }
     if (rc == GB_OK) rc = cuda_error(cudaGetLastError(), "k_constraint_setup");
   }
-  if (rc == GB_OK) rc = opt_in((const void*)k_contact_cholesky, "k_contact_cholesky");
+  // M^-1 by tree solves, JMinv over each constraint's dofs, the Delassus factor (+ its matrix and
+  // osim as outputs), Tn = -osim JMinv, the row-wise outputs and the inverse's bottom-right block
+  // M^-1 + JMinv^T Tn = M^-1 - M^-1 J^T osim J M^-1
+  const unsigned gc = (unsigned)((B * nv + kThreads - 1) / kThreads), gr = (unsigned)((B * nc + kThreads - 1) / kThreads);
+  const unsigned gn = (unsigned)((B * (nv + nc) + kThreads - 1) / kThreads);
+  const short* clist = closure_lists(set, (int)nv);
+  if (rc == GB_OK) rc = opt_in((const void*)k_tree_solve_cols, "k_tree_solve_cols");
+  if (rc == GB_OK) rc = opt_in((const void*)k_delassus, "k_delassus");
+  if (rc == GB_OK) rc = opt_in((const void*)k_out_rows, "k_out_rows");
   if (rc == GB_OK) {
-    k_contact_cholesky<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds,
-                                                                        Ms, Js, mu, Mis, JMs, Gs, Os, Ts, kkt, kinv,
-                                                                        oinv, osim, minv, jminv);
-    rc = cuda_error(cudaGetLastError(), "k_contact_cholesky");
+    k_tree_solve_cols<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nv, Us, Ds, Mis, 1);
+    if (nc > 0) {
+      k_jprod_rows<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, (int)nv, tab, set->n, clist, Js, Mis, nullptr, 1.0,
+                                            JMs);
+      k_delassus<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, tab, set->n,
+                                                                  clist, Js, JMs, mu, Gs, Os, oinv, osim);
+      k_prox_cols<<<gc, kThreads, 0, st>>>(B, (int)nc, (int)nv, Os, nullptr, mu, -1.0, JMs, Ts, Rh, Arr{nullptr, 0, 0},
+                                           nullptr);
+    }
+    k_cc_rows<<<gn, kThreads, 0, st>>>(B, (int)nc, (int)nv, mu, Ms, Mis, Js, JMs, Os, Ts, kkt, kinv, minv, jminv);
+    if (kinv.p)
+      k_out_rows<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Mis, 1.0, JMs, Ts, kinv,
+                                                      (int)(nv + nc), (int)nc, (int)nc);
+    rc = cuda_error(cudaGetLastError(), "contact Cholesky kernels");
   }
   scratch_free(scratch, st);
   return rc;
@@ -1566,36 +1349,47 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
   } else if (rc == GB_OK) {
     rc = cuda_error(cudaMemsetAsync(Fe, 0, sizeof(double) * 6 * nju * B, st), "cudaMemsetAsync");
   }
-  // the warp assembly reads dtau per configuration (instance layout); the thread assembly per element
-  const long per_warp = sizeof(double) * cd_warp_doubles((int)nv, (int)nc);
-  const long stage = (M->stage_bytes + 15) & ~15L;
-  int wpb = 4;
-  while (wpb > 1 && stage + wpb * per_warp > M->smem_optin) --wpb;
-  const bool warp_kernel = stage + wpb * per_warp <= M->smem_optin;
-  const Arr dtqa = warp_kernel ? Arr{dtq, nn, 1} : Arr{dtq, 1, B}, dtva = warp_kernel ? Arr{dtv, nn, 1} : Arr{dtv, 1, B};
   if (rc == GB_OK)
-    rc = launch_rnea_derivs_fext(M, precision, B, q, v, ddq, Arr{Fe, 1, B}, dtqa, dtva,
-                                 warp_kernel ? Arr{dMs, nn, 1} : Arr{dMs, 1, B}, st);
-  if (rc == GB_OK && warp_kernel) {
-    const size_t smem = (size_t)(stage + wpb * per_warp);
-    const cudaError_t e = cudaFuncSetAttribute((const void*)k_cd_assemble_warp,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    rc = e == cudaSuccess ? GB_OK : cuda_error(e, "k_cd_assemble_warp");
-    if (rc == GB_OK) {
-      const long g = (B + wpb - 1) / wpb;
-      k_cd_assemble_warp<<<(unsigned)g, 32 * wpb, smem, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Aq,
-                                                            Av, Cq, dtqa, dtva, its, s.mu, ddq_dq, ddq_dv, ddq_dtau,
-                                                            dl_dq, dl_dv, dl_dtau, tab, set->n, clist);
-      rc = cuda_error(cudaGetLastError(), "k_cd_assemble_warp");
-    }
-  } else if (rc == GB_OK) {
-    rc = opt_in((const void*)k_cd_assemble, "k_cd_assemble");
+    rc = launch_rnea_derivs_fext(M, precision, B, q, v, ddq, Arr{Fe, 1, B}, Arr{dtq, 1, B}, Arr{dtv, 1, B},
+                                 Arr{dMs, 1, B}, st);
+  // the assembly (hxx:815-990), column-parallel: M^-1 and W = M^-1 dtau_dx by tree solves,
+  // JMinv = J M^-1 and R = dac_dx - J W over each constraint's dofs, the Delassus factor and osim,
+  // the proximal recursion per column, then ddq_dtau = M^-1 + JMinv^T dlambda_dtau and
+  // ddq_dx = -W + JMinv^T dlambda_dx (= -M^-1 (dtau_dx - J^T dlambda_dx))
+  const unsigned gc = (unsigned)((B * nv + kThreads - 1) / kThreads), gr = (unsigned)((B * nc + kThreads - 1) / kThreads);
+  if (rc == GB_OK) rc = opt_in((const void*)k_tree_solve_cols, "k_tree_solve_cols");
+  if (rc == GB_OK) rc = opt_in((const void*)k_delassus, "k_delassus");
+  if (rc == GB_OK) rc = opt_in((const void*)k_out_rows, "k_out_rows");
+  const Arr none{nullptr, 0, 0};
+  if (rc == GB_OK) {
+    k_tree_solve_cols<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nv, Us, Ds, Mis, 1);
+    k_tree_solve_cols<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nv, Us, Ds, dtq, 0);
+    k_tree_solve_cols<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nv, Us, Ds, dtv, 0);
+    rc = cuda_error(cudaGetLastError(), "k_tree_solve_cols");
   }
-  if (rc == GB_OK && !warp_kernel) {
-    k_cd_assemble<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(
-        M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Aq, Av, Cq, dtq, dtv, its, s.mu, Mis, JMs, Gs, Os, Rs, Xs,
-        Ts, ddq_dq, ddq_dv, ddq_dtau, dl_dq, dl_dv, dl_dtau);
-    rc = cuda_error(cudaGetLastError(), "k_cd_assemble");
+  if (rc == GB_OK && nc > 0) {
+    k_jprod_rows<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, (int)nv, tab, set->n, clist, Js, Mis, nullptr, 1.0, JMs);
+    k_delassus<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, tab, set->n,
+                                                                clist, Js, JMs, s.mu, Gs, Os, none, none);
+    k_prox_cols<<<gc, kThreads, 0, st>>>(B, (int)nc, (int)nv, Os, its, s.mu, -1.0, JMs, Xs, Ts, dl_dtau, nullptr);
+    rc = cuda_error(cudaGetLastError(), "k_delassus");
+  }
+  if (rc == GB_OK) {
+    k_out_rows<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Mis, 1.0, JMs, Xs,
+                                                    ddq_dtau, (int)nv, 0, 0);
+    rc = cuda_error(cudaGetLastError(), "k_out_rows");
+  }
+  for (int pass = 0; pass < 2 && rc == GB_OK; ++pass) {
+    double* W = pass == 0 ? dtq : dtv;
+    if (nc > 0) {
+      k_jprod_rows<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, (int)nv, tab, set->n, clist, Js, W,
+                                            pass == 0 ? Aq : Av, -1.0, Rs);
+      k_prox_cols<<<gc, kThreads, 0, st>>>(B, (int)nc, (int)nv, Os, its, s.mu, -1.0, Rs, Xs, Ts,
+                                           pass == 0 ? dl_dq : dl_dv, pass == 0 ? Cq : nullptr);
+    }
+    k_out_rows<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, W, -1.0, JMs, Xs,
+                                                    pass == 0 ? ddq_dq : ddq_dv, (int)nv, 0, 0);
+    rc = cuda_error(cudaGetLastError(), "k_out_rows");
   }
   if (rc == GB_OK && iters_out)
     rc = cuda_error(cudaMemcpyAsync(iters_out, its, sizeof(int) * B, cudaMemcpyDefault, st), "cudaMemcpyAsync");
