@@ -565,7 +565,7 @@ __device__ void delassus_llt_tree(const gb::MView& m, const Col& U, const Col& D
 // J M^-1 J^T + mu I = L L^T: lambda_k = L^-T L^-1 (c0 + mu lambda_{k-1}) with c0 = rhs - J M^-1 (tau -
 // nle); the reference's residuals: absolute ||(J M^-1 J^T) y - rhs||_inf and relative ||y - y_prev||_inf
 // for y = -lambda_k; then ddq = M^-1 (tau - nle + J^T lambda).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 1)  // a single wave at these batches: no register cap
     k_constraint_solve(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
                        const double* nles, double* Rs, double* Ys, double* Gs, const double* Js, const double* Rh,
                        double* C0s, double* LPs, double* Ts, Arr tau, gb_proximal_settings s, Arr ddq, Arr lam,
