@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // a single wave at these batche
 // derivative term of world-aligned constraints (hxx:1000-1040) and the constraint forces as forces
 // on the constraint joints (ContactForceContribution, hxx:225-342) for the inverse dynamics
 // derivatives; then the assembly as column-parallel steps (M^-1, the operational-space inertia,
-// the proximal recursion, hxx:815-990: k_tree_solve_cols, k_jprod_rows, k_delassus, k_prox_cols,
+// the proximal recursion, hxx:815-990: k_tree_solve_cols, k_jprod_rows, k_delassus_cols, k_llt, k_osim_cols, k_prox_cols,
 // k_out_rows).
 
 __device__ void translate_motion(const double* p, M6d& m) {  // linear -= p x angular
@@ -979,36 +979,42 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// per configuration: G = JMinv J^T + mu I (the damped Delassus matrix; a column over its row's
-// constraint dofs), its LLT in place and O = G^-1; oinv / osim (optional) take G and O
+// G(r, c) = JMinv(r, :) J(c, :)^T + mu [r == c] for r >= c (the damped Delassus matrix, lower part;
+// the sum over column c's constraint dofs): one thread per (configuration, column c < nc); oinv
+// (optional) takes the symmetric matrix
 __global__ void __launch_bounds__(kThreads)
-    k_delassus(const unsigned char* blob, int bytes, long B, int nc, const ConstraintDev* __restrict__ tab, int ncon,
-               const short* __restrict__ clist, const double* Js, const double* JMs, double mu, double* Gs, double* Os,
-               Arr oinv, Arr osim) {
+    k_delassus_cols(long B, int nc, int nv, const ConstraintDev* __restrict__ tab, int ncon,
+                    const short* __restrict__ clist, const double* Js, const double* JMs, double mu, double* Gs,
+                    Arr oinv) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * nc) return;
+  const long b = t % B;
+  const int c = (int)(t / B);
+  int e = 0;
+  while (e + 1 < ncon && tab[e + 1].row <= c) ++e;
+  const short* L = clist + (long)e * (nv + 1);
+  for (int r = c; r < nc; ++r) {
+    double acc = 0.0;
+    for (int p = 0; p < L[0]; ++p)
+      acc += JMs[((long)r * nv + L[1 + p]) * B + b] * Js[((long)c * nv + L[1 + p]) * B + b];
+    acc += r == c ? mu : 0.0;
+    Gs[((long)r * nc + c) * B + b] = acc;
+    if (oinv.p) {
+      double* o = const_cast<double*>(oinv.p) + b * oinv.is;
+      o[((long)r * nc + c) * oinv.es] = acc;
+      o[((long)c * nc + r) * oinv.es] = acc;
+    }
+  }
+}
+
+// G = L L^T in place (lower), per configuration (pivots checked)
+__global__ void __launch_bounds__(kThreads)
+    k_llt(const unsigned char* blob, int bytes, long B, int nc, double* Gs) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
-  const int nv = m.nv;
-  const Col G{Gs + b, B}, O{Os + b, B};
-  auto out = [&](const Arr& a, long k) -> double& { return const_cast<double*>(a.p)[b * a.is + k * a.es]; };
-  for (int e = 0; e < ncon; ++e) {
-    const short* L = clist + (long)e * (nv + 1);
-    const int c0 = tab[e].row, c1 = c0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
-    for (int c = c0; c < c1; ++c)
-      for (int r = c; r < nc; ++r) {
-        double acc = 0.0;
-        for (int p = 0; p < L[0]; ++p)
-          acc += JMs[((long)r * nv + L[1 + p]) * B + b] * Js[((long)c * nv + L[1 + p]) * B + b];
-        G[(long)r * nc + c] = acc + (r == c ? mu : 0.0);
-      }
-  }
-  if (oinv.p)
-    for (int r = 0; r < nc; ++r)
-      for (int c = 0; c <= r; ++c) {
-        out(oinv, (long)r * nc + c) = G[(long)r * nc + c];
-        out(oinv, (long)c * nc + r) = G[(long)r * nc + c];
-      }
+  const Col G{Gs + b, B};
   for (int j = 0; j < nc; ++j) {
     double t = G[(long)j * nc + j];
     for (int k = 0; k < j; ++k) t -= G[(long)j * nc + k] * G[(long)j * nc + k];
@@ -1021,13 +1027,23 @@ __global__ void __launch_bounds__(kThreads)
       G[(long)i * nc + j] = u / l;
     }
   }
-  for (int c = 0; c < nc; ++c) {
-    const Col x{O.p + (long)c * B, (long)nc * B};
-    for (int k = 0; k < nc; ++k) x[k] = k == c ? 1.0 : 0.0;
-    llt_solve(G, nc, x);
-    if (osim.p)
-      for (int k = 0; k < nc; ++k) out(osim, (long)k * nc + c) = x[k];
-  }
+}
+
+// O(:, c) = (L L^T)^-1 e_c (osim, the operational-space inertia): one thread per (configuration,
+// column c < nc); osim (optional) takes it
+__global__ void __launch_bounds__(kThreads)
+    k_osim_cols(long B, int nc, const double* Gs, double* Os, Arr osim) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * nc) return;
+  const long b = t % B;
+  const int c = (int)(t / B);
+  const Col G{const_cast<double*>(Gs) + b, B};
+  const Col x{Os + (long)c * B + b, (long)nc * B};
+  for (int k = 0; k < nc; ++k) x[k] = k == c ? 1.0 : 0.0;
+  llt_solve(G, nc, x);
+  if (osim.p)
+    for (int k = 0; k < nc; ++k)
+      const_cast<double*>(osim.p)[b * osim.is + ((long)k * nc + c) * osim.es] = x[k];
 }
 
 // X[:, c] = s1 O R[:, c], then it - 1 times X[:, c] = O (mu X[:, c] - R[:, c]) (the proximal
@@ -1277,15 +1293,16 @@ int launch_contact_cholesky(const gb_model* M, long B, const gb_constraint_set* 
   const unsigned gn = (unsigned)((B * (nv + nc) + kThreads - 1) / kThreads);
   const short* clist = closure_lists(set, (int)nv);
   if (rc == GB_OK) rc = opt_in((const void*)k_tree_solve_cols, "k_tree_solve_cols");
-  if (rc == GB_OK) rc = opt_in((const void*)k_delassus, "k_delassus");
+  if (rc == GB_OK) rc = opt_in((const void*)k_llt, "k_llt");
   if (rc == GB_OK) rc = opt_in((const void*)k_out_rows, "k_out_rows");
   if (rc == GB_OK) {
     k_tree_solve_cols<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nv, Us, Ds, Mis, 1);
     if (nc > 0) {
       k_jprod_rows<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, (int)nv, tab, set->n, clist, Js, Mis, nullptr, 1.0,
                                             JMs);
-      k_delassus<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, tab, set->n,
-                                                                  clist, Js, JMs, mu, Gs, Os, oinv, osim);
+      k_delassus_cols<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, tab, set->n, clist, Js, JMs, mu, Gs, oinv);
+      k_llt<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Gs);
+      k_osim_cols<<<gr, kThreads, 0, st>>>(B, (int)nc, Gs, Os, osim);
       k_prox_cols<<<gc, kThreads, 0, st>>>(B, (int)nc, (int)nv, Os, nullptr, mu, -1.0, JMs, Ts, Rh, Arr{nullptr, 0, 0},
                                            nullptr);
     }
@@ -1358,7 +1375,7 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
   // ddq_dx = -W + JMinv^T dlambda_dx (= -M^-1 (dtau_dx - J^T dlambda_dx))
   const unsigned gc = (unsigned)((B * nv + kThreads - 1) / kThreads), gr = (unsigned)((B * nc + kThreads - 1) / kThreads);
   if (rc == GB_OK) rc = opt_in((const void*)k_tree_solve_cols, "k_tree_solve_cols");
-  if (rc == GB_OK) rc = opt_in((const void*)k_delassus, "k_delassus");
+  if (rc == GB_OK) rc = opt_in((const void*)k_llt, "k_llt");
   if (rc == GB_OK) rc = opt_in((const void*)k_out_rows, "k_out_rows");
   const Arr none{nullptr, 0, 0};
   if (rc == GB_OK) {
@@ -1369,10 +1386,11 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
   }
   if (rc == GB_OK && nc > 0) {
     k_jprod_rows<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, (int)nv, tab, set->n, clist, Js, Mis, nullptr, 1.0, JMs);
-    k_delassus<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, tab, set->n,
-                                                                clist, Js, JMs, s.mu, Gs, Os, none, none);
+    k_delassus_cols<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, tab, set->n, clist, Js, JMs, s.mu, Gs, none);
+    k_llt<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Gs);
+    k_osim_cols<<<gr, kThreads, 0, st>>>(B, (int)nc, Gs, Os, none);
     k_prox_cols<<<gc, kThreads, 0, st>>>(B, (int)nc, (int)nv, Os, its, s.mu, -1.0, JMs, Xs, Ts, dl_dtau, nullptr);
-    rc = cuda_error(cudaGetLastError(), "k_delassus");
+    rc = cuda_error(cudaGetLastError(), "the Delassus kernels");
   }
   if (rc == GB_OK) {
     k_out_rows<<<gc, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Mis, 1.0, JMs, Xs,
