@@ -309,6 +309,7 @@ class Data {
   void* stream;
   DeviceMatrix tau, ddq, M, dtau_dq, dtau_dv, ddq_dq, ddq_dv, Minv;
   DeviceMatrix lambda_c, prox_residuals;  // constraintDynamics: multipliers, (absolute, relative) residuals
+  DeviceMatrix q_crba;                    // the configurations of the last crba (ContactCholeskyDecomposition::compute)
   std::shared_ptr<ConstraintSet> constraints;  // the models of initConstraintDynamics
 
   // a device pointer to the n x batch input x: x itself when it lives in device (or
@@ -368,6 +369,10 @@ const DeviceMatrix& crba(const Model& m, Data& data, const MQ& q, int convention
   data.M.resize(static_cast<long>(m.nv) * m.nv, B);
   check(gb_crba(m.get(), data.precision, convention, GB_MATRIX_UPPER, GB_LAYOUT_INSTANCE, B, Q, data.M.data(), nullptr,
                 nullptr, data.stream));
+  data.q_crba.resize(m.nq, B);
+  check_cuda(cudaMemcpyAsync(data.q_crba.data(), Q, sizeof(double) * m.nq * B, cudaMemcpyDeviceToDevice,
+                             static_cast<cudaStream_t>(data.stream)),
+             "crba");
   return data.M;
 }
 
@@ -552,6 +557,56 @@ const DeviceMatrix& constraintDynamics(const Model& m, Data& data, const MQ& q, 
   }
   return data.ddq;
 }
+
+// ContactCholeskyDecomposition(model, contact_models) (algorithm/contact-cholesky.hpp:107-470) over
+// a batch: compute(model, data, contact_models, contact_datas, mu) factorises the KKT matrix
+// [[-mu I, J], [J^T, M]] at the configurations of the last crba(model, data, q) (whose data.M the
+// reference's compute reads); the accessors are device matrices with one row-major matrix per
+// configuration (column b of the (rows * cols) x batch matrix): matrix(), inverse(),
+// getInverseOperationalSpaceInertiaMatrix(), getOperationalSpaceInertiaMatrix(),
+// getInverseMassMatrix(), getJMinv().
+class ContactCholeskyDecomposition {
+ public:
+  ContactCholeskyDecomposition(const Model& m, const std::vector<RigidConstraintModel>& contact_models)
+      : nv_(m.nv), num_contacts_(static_cast<int>(contact_models.size())) {
+    for (const auto& c : contact_models) nc_ += c.size();
+  }
+  void compute(const Model& m, Data& data, const std::vector<RigidConstraintModel>& contact_models,
+               const std::vector<RigidConstraintData>& contact_datas, double mu = 0.0) {
+    if (contact_models.size() != contact_datas.size())
+      throw std::invalid_argument("The contact models and data do not have the same vector size.");
+    if (data.q_crba.cols() == 0 && data.q_crba.rows() == 0)
+      throw std::invalid_argument("compute reads the configurations of crba(model, data, q): call it first");
+    if (!data.constraints || !data.constraints->same(contact_models)) initConstraintDynamics(m, data, contact_models);
+    const long B = data.q_crba.cols();
+    nc_ = data.constraints->dim();
+    num_contacts_ = static_cast<int>(contact_models.size());
+    const long n = nc_ + nv_;
+    kkt_.resize(n * n, B);
+    inverse_.resize(n * n, B);
+    osim_inverse_.resize(static_cast<long>(nc_) * nc_, B);
+    osim_.resize(static_cast<long>(nc_) * nc_, B);
+    minv_.resize(static_cast<long>(nv_) * nv_, B);
+    jminv_.resize(static_cast<long>(nc_) * nv_, B);
+    const bool c = nc_ > 0;
+    check(gb_contact_cholesky(m.get(), data.precision, data.constraints->get(), mu, GB_LAYOUT_INSTANCE, B,
+                              data.q_crba.data(), kkt_.data(), inverse_.data(), c ? osim_inverse_.data() : nullptr,
+                              c ? osim_.data() : nullptr, minv_.data(), c ? jminv_.data() : nullptr, data.stream));
+  }
+  int size() const { return nc_ + nv_; }
+  int constraintDim() const { return nc_; }
+  int numContacts() const { return num_contacts_; }
+  const DeviceMatrix& matrix() const { return kkt_; }
+  const DeviceMatrix& inverse() const { return inverse_; }
+  const DeviceMatrix& getInverseOperationalSpaceInertiaMatrix() const { return osim_inverse_; }
+  const DeviceMatrix& getOperationalSpaceInertiaMatrix() const { return osim_; }
+  const DeviceMatrix& getInverseMassMatrix() const { return minv_; }
+  const DeviceMatrix& getJMinv() const { return jminv_; }
+
+ private:
+  int nv_ = 0, nc_ = 0, num_contacts_ = 0;
+  DeviceMatrix kkt_, inverse_, osim_inverse_, osim_, minv_, jminv_;
+};
 
 // Throws std::runtime_error when the model's kernels recorded a numeric failure
 // (gb_numeric_status: a pivot that was not > 0, or a non-finite output); clears the record.

@@ -136,6 +136,25 @@ int main() {
     std::printf("constraint_dynamics aba %.3e prox %.3e iter %d lambda_rows %ld\n", e6, e7 / s7, ps1.iter,
                 data.lambda_c.rows());
     if (!(e6 < 1e-10 && e7 < 1e-6 * s7 && ps1.iter > 1 && data.lambda_c.rows() == 3 && cd[0].size == 3)) return 6;
+    // ContactCholeskyDecomposition at the configurations of crba: inverse() * matrix() = I and
+    // getInverseMassMatrix() * M = I
+    pinocchio_gb300::crba(model, data, q);
+    pinocchio_gb300::ContactCholeskyDecomposition chol(model, cm);
+    chol.compute(model, data, cm, cd, 1e-3);
+    const int nk = chol.size();
+    Mat K(static_cast<long>(nk) * nk, B), Ki(static_cast<long>(nk) * nk, B);
+    chol.matrix().copyToHost(K);
+    chol.inverse().copyToHost(Ki);
+    double e8 = 0.0;
+    for (long b = 0; b < B; ++b)
+      for (int r = 0; r < nk; ++r)
+        for (int c = 0; c < nk; ++c) {
+          double t = 0.0;
+          for (int k = 0; k < nk; ++k) t += Ki.d[b * nk * nk + r * nk + k] * K.d[b * nk * nk + k * nk + c];
+          e8 = std::fmax(e8, std::fabs(t - (r == c ? 1.0 : 0.0)));
+        }
+    std::printf("contact_cholesky size %d dim %d kkt_inverse %.3e\n", nk, chol.constraintDim(), e8);
+    if (!(nk == model.nv + 3 && chol.constraintDim() == 3 && e8 < 1e-8)) return 7;
     try {
       Mat bad(model.nq + 1, B);
       pinocchio_gb300::rnea(model, data, bad, v, a);
