@@ -561,6 +561,59 @@ __device__ void delassus_llt_tree(const gb::MView& m, const Col& U, const Col& D
   }
 }
 
+// The same Delassus matrix by columns, one thread per (configuration, constraint row c): Y(:, c) =
+// D^-1/2 U^-1 J(c, :)^T on the ancestor closure of row c's constraint (the entries outside it are
+// not written and not read), then G(i, c) for i >= c over the two rows' common dofs + mu [i == c]
+// (its LLT: k_llt).  Y is nv x nc and G nc x nc, [element][configuration].
+__global__ void __launch_bounds__(kThreads)
+    k_delassus_y_cols(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
+                      const double* Js, double* Ys, const ConstraintDev* __restrict__ tab, int ncon,
+                      const short* __restrict__ clist) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gb::MView m = stage_model(blob, bytes, smem);
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * nc) return;
+  const long b = t % B;
+  const int c = (int)(t / B), nv = m.nv;
+  int e = 0;
+  while (e + 1 < ncon && tab[e + 1].row <= c) ++e;
+  const short* L = clist + (long)e * (nv + 1);
+  const int len = L[0];
+  auto U = [&](int r, int k) { return Us[((long)r * nv + k) * B + b]; };
+  auto Y = [&](int k) -> double& { return Ys[((long)k * nc + c) * B + b]; };
+  for (int p = 0; p < len; ++p) Y(L[1 + p]) = Js[((long)c * nv + L[1 + p]) * B + b];
+  for (int p = len - 2; p >= 0; --p) {  // U^-1 restricted to the set (subtree rows k..k+nsfr-1)
+    const int k = L[1 + p], end = k + m.nsfr[k];
+    double acc = 0.0;
+    for (int p2 = p + 1; p2 < len && L[1 + p2] < end; ++p2) acc += U(k, L[1 + p2]) * Y(L[1 + p2]);
+    Y(k) -= acc;
+  }
+  for (int p = 0; p < len; ++p) Y(L[1 + p]) /= sqrt(Ds[(long)L[1 + p] * B + b]);
+}
+__global__ void __launch_bounds__(kThreads)
+    k_delassus_gram_cols(long B, int nc, int nv, const double* Ys, double* Gs, double mu,
+                         const ConstraintDev* __restrict__ tab, int ncon, const signed char* __restrict__ cmask,
+                         const short* __restrict__ clist) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * nc) return;
+  const long b = t % B;
+  const int c = (int)(t / B);
+  int ec = 0;
+  while (ec + 1 < ncon && tab[ec + 1].row <= c) ++ec;
+  const short* L = clist + (long)ec * (nv + 1);
+  int ei = ec;
+  for (int i = c; i < nc; ++i) {
+    while (ei + 1 < ncon && tab[ei + 1].row <= i) ++ei;
+    const signed char* mi = cmask + (long)ei * nv;
+    double acc = 0.0;
+    for (int p = 0; p < L[0]; ++p) {
+      const int k = L[1 + p];
+      if (mi[k]) acc += Ys[((long)k * nc + i) * B + b] * Ys[((long)k * nc + c) * B + b];
+    }
+    Gs[((long)i * nc + c) * B + b] = acc + (i == c ? mu : 0.0);
+  }
+}
+
 // The proximal iterations (constrained-dynamics.hxx:434-486) on the factorisations M = U D U^T and
 // J M^-1 J^T + mu I = L L^T: lambda_k = L^-T L^-1 (c0 + mu lambda_{k-1}) with c0 = rhs - J M^-1 (tau -
 // nle); the reference's residuals: absolute ||(J M^-1 J^T) y - rhs||_inf and relative ||y - y_prev||_inf
@@ -570,7 +623,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // a single wave at these batche
                        const double* nles, double* Rs, double* Ys, double* Gs, const double* Js, const double* Rh,
                        double* C0s, double* LPs, double* Ts, Arr tau, gb_proximal_settings s, Arr ddq, Arr lam,
                        int* iters, double* residuals, const ConstraintDev* __restrict__ tab, int ncon,
-                       const signed char* __restrict__ cmask, const short* __restrict__ clist) {
+                       const signed char* __restrict__ cmask, const short* __restrict__ clist, int factored) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -588,7 +641,11 @@ __global__ void __launch_bounds__(kThreads, 1)  // a single wave at these batche
   double ar = 0.0, rr = 0.0;
   const Col L{nc > 0 ? const_cast<double*>(lam.p) + b * lam.is : nullptr, nc > 0 ? lam.es : 0};
   if (nc > 0) {
-    delassus_llt_tree(m, U, D, Ji, nc, s.mu, Y, G, tab, ncon, cmask, clist);
+    if (factored) {  // Y, G and its LLT come from the column kernels
+      for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);
+    } else {
+      delassus_llt_tree(m, U, D, Ji, nc, s.mu, Y, G, tab, ncon, cmask, clist);
+    }
     for (int e = 0; e < ncon; ++e) {
       const short* Ls = clist + (long)e * (nv + 1);
       const int r0 = tab[e].row, r1 = r0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
@@ -1231,12 +1288,26 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
     }
     if (rc == GB_OK) rc = cuda_error(cudaGetLastError(), "k_constraint_setup");
   }
+  // the Delassus matrix and its factor by columns (one thread per configuration and constraint row),
+  // then the per-configuration solve: R = M^-1 (tau - nle), the proximal iterations, ddq
+  if (rc == GB_OK && nc > 0) {
+    const unsigned gr = (unsigned)((B * nc + kThreads - 1) / kThreads);
+    rc = opt_in((const void*)k_delassus_y_cols, "k_delassus_y_cols");
+    if (rc == GB_OK) rc = opt_in((const void*)k_llt, "k_llt");
+    if (rc == GB_OK) {
+      k_delassus_y_cols<<<gr, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds, Js, Ys,
+                                                             tab, set->n, clist);
+      k_delassus_gram_cols<<<gr, kThreads, 0, st>>>(B, (int)nc, (int)nv, Ys, Gs, s.mu, tab, set->n, cmask, clist);
+      k_llt<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Gs);
+      rc = cuda_error(cudaGetLastError(), "the Delassus kernels");
+    }
+  }
   if (rc == GB_OK) rc = opt_in((const void*)k_constraint_solve, "k_constraint_solve");
   if (rc == GB_OK) {
     k_constraint_solve<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds,
                                                                         nles, Rs, Ys, Gs, Js, Rh, C0, LP, Ts, tau, s,
                                                                         ddq, lam, iters, residuals, tab, set->n, cmask,
-                                                                        clist);
+                                                                        clist, 1);
     rc = cuda_error(cudaGetLastError(), "k_constraint_solve");
   }
   scratch_free(scratch, st);
