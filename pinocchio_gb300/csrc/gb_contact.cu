@@ -503,67 +503,11 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// delassus_llt on the constraint rows' supports: the rows of U^-1 J^T that can be non-zero for a
-// constraint are the ancestor closure of its columns (a sorted list per constraint, clist = [count,
-// dofs...]; cmask the same set as a mask), U^-1 keeps a vector inside such a set, and a Delassus
-// entry sums over the two constraints' common dofs only
-__device__ void delassus_llt_tree(const gb::MView& m, const Col& U, const Col& D, const gb::In& Ji, int nc,
-                                  double inv_damping, const Col& Y, const Col& G, const ConstraintDev* tab,
-                                  int ncon, const signed char* cmask, const short* clist) {
-  const int nv = m.nv;
-  for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);
-  for (int e = 0; e < ncon; ++e) {
-    const short* L = clist + (long)e * (nv + 1);
-    const int len = L[0], r0 = tab[e].row, r1 = r0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
-    for (int c = r0; c < r1; ++c) {
-      for (int p = 0; p < len; ++p) Y[(long)L[1 + p] * nc + c] = Ji[c * nv + L[1 + p]];
-      for (int p = len - 2; p >= 0; --p) {  // U^-1 restricted to the set (subtree rows k..k+nsfr-1)
-        const int k = L[1 + p], end = k + m.nsfr[k];
-        double t = 0.0;
-        for (int p2 = p + 1; p2 < len && L[1 + p2] < end; ++p2) t += U[(long)k * nv + L[1 + p2]] * Y[(long)L[1 + p2] * nc + c];
-        Y[(long)k * nc + c] -= t;
-      }
-    }
-    for (int p = 0; p < len; ++p) {
-      const int r = L[1 + p];
-      const double sd = sqrt(D[r]);
-      for (int c = r0; c < r1; ++c) Y[(long)r * nc + c] /= sd;
-    }
-  }
-  for (int ei = 0; ei < ncon; ++ei) {
-    const int i0 = tab[ei].row, i1 = i0 + (tab[ei].type == GB_CONTACT_3D ? 3 : 6);
-    const signed char* mi = cmask + (long)ei * nv;
-    for (int ej = 0; ej <= ei; ++ej) {
-      const short* L = clist + (long)ej * (nv + 1);
-      const int len = L[0], j0 = tab[ej].row, j1 = j0 + (tab[ej].type == GB_CONTACT_3D ? 3 : 6);
-      for (int i = i0; i < i1; ++i)
-        for (int j = j0; j < j1 && j <= i; ++j) {
-          double t = 0.0;
-          for (int p = 0; p < len; ++p) {
-            const int k = L[1 + p];
-            if (mi[k]) t += Y[(long)k * nc + i] * Y[(long)k * nc + j];
-          }
-          G[(long)i * nc + j] = t + (i == j ? inv_damping : 0.0);
-        }
-    }
-  }
-  for (int j = 0; j < nc; ++j) {
-    double t = G[(long)j * nc + j];
-    for (int k = 0; k < j; ++k) t -= G[(long)j * nc + k] * G[(long)j * nc + k];
-    gb::check_pivot(m, t);
-    const double ljj = sqrt(t);
-    G[(long)j * nc + j] = ljj;
-    for (int i = j + 1; i < nc; ++i) {
-      double u = G[(long)i * nc + j];
-      for (int k = 0; k < j; ++k) u -= G[(long)i * nc + k] * G[(long)j * nc + k];
-      G[(long)i * nc + j] = u / ljj;
-    }
-  }
-}
-
-// The same Delassus matrix by columns, one thread per (configuration, constraint row c): Y(:, c) =
-// D^-1/2 U^-1 J(c, :)^T on the ancestor closure of row c's constraint (the entries outside it are
-// not written and not read), then G(i, c) for i >= c over the two rows' common dofs + mu [i == c]
+// The Delassus matrix J M^-1 J^T + mu I = Y^T Y + mu I by columns, one thread per (configuration,
+// constraint row c): Y(:, c) = D^-1/2 U^-1 J(c, :)^T on the ancestor closure of row c's constraint
+// (the rows of U^-1 J^T that can be non-zero: U^-1 keeps a vector inside such a set; the entries
+// outside it are neither written nor read; clist holds the closure of each constraint as [count,
+// dofs...], cmask as a mask), then G(i, c) for i >= c over the two rows' common dofs + mu [i == c]
 // (its LLT: k_llt).  Y is nv x nc and G nc x nc, [element][configuration].
 __global__ void __launch_bounds__(kThreads)
     k_delassus_y_cols(const unsigned char* blob, int bytes, long B, int nc, const double* Us, const double* Ds,
@@ -623,7 +567,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // a single wave at these batche
                        const double* nles, double* Rs, double* Ys, double* Gs, const double* Js, const double* Rh,
                        double* C0s, double* LPs, double* Ts, Arr tau, gb_proximal_settings s, Arr ddq, Arr lam,
                        int* iters, double* residuals, const ConstraintDev* __restrict__ tab, int ncon,
-                       const signed char* __restrict__ cmask, const short* __restrict__ clist, int factored) {
+                       const short* __restrict__ clist) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gb::MView m = stage_model(blob, bytes, smem);
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -641,11 +585,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // a single wave at these batche
   double ar = 0.0, rr = 0.0;
   const Col L{nc > 0 ? const_cast<double*>(lam.p) + b * lam.is : nullptr, nc > 0 ? lam.es : 0};
   if (nc > 0) {
-    if (factored) {  // Y, G and its LLT come from the column kernels
-      for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);
-    } else {
-      delassus_llt_tree(m, U, D, Ji, nc, s.mu, Y, G, tab, ncon, cmask, clist);
-    }
+    for (int r = 0; r < nv; ++r) gb::check_pivot(m, D[r]);  // G and its LLT: the column kernels
     for (int e = 0; e < ncon; ++e) {
       const short* Ls = clist + (long)e * (nv + 1);
       const int r0 = tab[e].row, r1 = r0 + (tab[e].type == GB_CONTACT_3D ? 3 : 6);
@@ -1306,8 +1246,7 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
   if (rc == GB_OK) {
     k_constraint_solve<<<(unsigned)grid, kThreads, M->stage_bytes, st>>>(M->d_blob, M->stage_bytes, B, (int)nc, Us, Ds,
                                                                         nles, Rs, Ys, Gs, Js, Rh, C0, LP, Ts, tau, s,
-                                                                        ddq, lam, iters, residuals, tab, set->n, cmask,
-                                                                        clist, 1);
+                                                                        ddq, lam, iters, residuals, tab, set->n, clist);
     rc = cuda_error(cudaGetLastError(), "k_constraint_solve");
   }
   scratch_free(scratch, st);
