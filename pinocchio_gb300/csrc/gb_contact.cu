@@ -1180,7 +1180,7 @@ const short* closure_lists(const gb_constraint_set* set, int nv) {
 
 int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
                       const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
-                      double* residuals, cudaStream_t st) {
+                      double* residuals, cudaStream_t st, double* U_keep, double* D_keep) {
   const long nv = M->nv, nn = nv * nv, nc = set->nc;
   // scratch, [element][configuration]: M, U (nn), D, nle, r (nv), sDUiJt (nv * max(nc, 1)), G (nc * nc),
   // J (nc * nv), rhs, c0, lambda_prev, tmp (nc)
@@ -1192,6 +1192,8 @@ int launch_constraint(const gb_model* M, int precision, long B, const gb_constra
   double *Ms = base, *Us = Ms + nn * B, *Ds = Us + nn * B, *nles = Ds + nv * B, *Rs = nles + nv * B,
          *Ys = Rs + nv * B, *Gs = Ys + ny * B, *Js = Gs + ng * B, *Rh = Js + nc * nv * B, *C0 = Rh + nc * B,
          *LP = C0 + nc * B, *Ts = LP + nc * B;
+  if (U_keep) Us = U_keep;  // the caller keeps the factorisation of M ([element][configuration])
+  if (D_keep) Ds = D_keep;
   const ConstraintDev* tab = static_cast<const ConstraintDev*>(set->d_mem);
   const signed char* sp = reinterpret_cast<const signed char*>(tab + (set->n > 0 ? set->n : 0));
   const signed char* cmask = sp + (long)set->n * nv;
@@ -1344,8 +1346,8 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
          *Cq = Av + cn * B, *JMs = Cq + cn * B, *Rs = JMs + cn * B, *Xs = Rs + cn * B, *Ts = Xs + cn * B,
          *Gs = Ts + cn * B, *Os = Gs + nc * nc * B, *Fe = Os + nc * nc * B;
   int* its = reinterpret_cast<int*>(base + doubles);
-  rc = launch_constraint(M, precision, B, set, s, q, v, tau, ddq, lam, its, nullptr, st);
-  if (rc == GB_OK) rc = launch_crba(M, GB_FP64, false, B, q, Arr{Ms, 1, B}, Arr{Us, 1, B}, Arr{Ds, 1, B}, st);
+  // the constraint dynamics it differentiates, which leaves the factorisation of M in Us / Ds
+  rc = launch_constraint(M, precision, B, set, s, q, v, tau, ddq, lam, its, nullptr, st, Us, Ds);
   const long grid = (B + kThreads - 1) / kThreads;
   auto opt_in = [&](const void* kern, const char* name) -> int {
     if (M->stage_bytes <= 48 * 1024) return GB_OK;

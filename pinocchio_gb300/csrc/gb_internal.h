@@ -86,7 +86,8 @@ int launch_constraint_derivs(const gb_model* M, int precision, long B, const gb_
                              Arr ddq_dv, Arr ddq_dtau, Arr dl_dq, Arr dl_dv, Arr dl_dtau, int* iters, cudaStream_t st);
 int launch_constraint(const gb_model* M, int precision, long B, const gb_constraint_set* set,
                       const gb_proximal_settings& s, Arr q, Arr v, Arr tau, Arr ddq, Arr lam, int* iters,
-                      double* residuals, cudaStream_t st);
+                      double* residuals, cudaStream_t st,
+                      double* U_keep = nullptr, double* D_keep = nullptr);
 int launch_contact_cholesky(const gb_model* M, long B, const gb_constraint_set* set, double mu, Arr q, Arr kkt,
                             Arr kinv, Arr oinv, Arr osim, Arr minv, Arr jminv, cudaStream_t st);
 int launch_integrate(const gb_model* m, long B, Arr q, Arr v, Arr qo, cudaStream_t st);
