@@ -478,6 +478,12 @@ class ContactCholeskyDecomposition:
     def getJMinv(self):
         return self._get("jminv")
 
+    def getDelassusCholeskyExpression(self):
+        """The damped Delassus matrix J M^-1 J^T + mu I as an operator (DelassusCholeskyExpressionTpl,
+        contact-cholesky.hpp:520-620): ``expr @ x`` / ``expr.solve(x)`` for (batch, nc) or (batch, nc, k)
+        right-hand sides, ``matrix()``, ``inverse()``, ``size()``, ``updateDamping(mu)``."""
+        return _DelassusCholeskyExpression(self)
+
     def solve(self, rhs):
         """KKT^-1 rhs for (batch, n) or (batch, n, k) right-hand sides (contact-cholesky.hxx:306-330)."""
         if self._out is None:
@@ -487,6 +493,36 @@ class ContactCholeskyDecomposition:
         r = torch.as_tensor(np.asarray(rhs) if not torch.is_tensor(rhs) else rhs, dtype=K.dtype).to(K.device)
         x = torch.matmul(K, r.unsqueeze(-1)).squeeze(-1) if r.dim() == 2 else torch.matmul(K, r)
         return x.cpu().numpy() if not torch.is_tensor(rhs) else x
+
+
+class _DelassusCholeskyExpression:
+    def __init__(self, chol: ContactCholeskyDecomposition):
+        self.chol = chol
+
+    def _apply(self, key, x):
+        torch = _torch()
+        K = self.chol._out[key]
+        r = torch.as_tensor(np.asarray(x) if not torch.is_tensor(x) else x, dtype=K.dtype).to(K.device)
+        y = torch.matmul(K, r.unsqueeze(-1)).squeeze(-1) if r.dim() == 2 else torch.matmul(K, r)
+        return y.cpu().numpy() if not torch.is_tensor(x) else y
+
+    def __matmul__(self, x):  # applyOnTheRight
+        return self._apply("osim_inverse", x)
+
+    def solve(self, x):
+        return self._apply("osim", x)
+
+    def matrix(self):
+        return self.chol.getInverseOperationalSpaceInertiaMatrix()
+
+    def inverse(self):
+        return self.chol.getOperationalSpaceInertiaMatrix()
+
+    def size(self) -> int:
+        return self.chol.constraintDim()
+
+    def updateDamping(self, mu: float):
+        self.chol.updateDamping(mu)
 
 
 def initConstraintDynamics(model: Model, data: Data, contact_models) -> None:

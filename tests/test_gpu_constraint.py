@@ -326,6 +326,11 @@ def test_contact_cholesky_matches_oracle(name, mu):
         assert rel_err(got[k].cpu().numpy(), r) < tol, k
     rhs = np.random.default_rng(2).standard_normal((64, chol.size()))
     assert rel_err(chol.solve(rhs), np.einsum("bij,bj->bi", ref["inverse"], rhs)) < tol
+    if chol.constraintDim():  # the Delassus operator (DelassusCholeskyExpression) and its solve
+        dx = rhs[:, : chol.constraintDim()]
+        expr = chol.getDelassusCholeskyExpression()
+        assert rel_err(expr @ dx, np.einsum("bij,bj->bi", ref["osim_inverse"], dx)) < tol
+        assert rel_err(expr.solve(dx), np.einsum("bij,bj->bi", ref["osim"], dx)) < tol
     if mu == 0.0:  # updateDamping refactorises with another mu
         chol.updateDamping(0.05)
         r2 = om.contact_cholesky(q, desc, mu=0.05)
