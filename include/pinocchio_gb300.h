@@ -70,7 +70,7 @@ enum {
   GB_JOINT_PLANAR = 12,      /* JointModelPlanar (joint-planar.hpp): q = (x, y, cos t, sin t),
                                 v = (vx, vy, wz) in the joint frame.  Models with spherical or
                                 planar joints run one configuration per thread (gb_model_set_layout
-                                refuses the lane layouts) and are not accepted by gb_batch_multi. */
+                                refuses the lane layouts), in gb_batch_multi too. */
   GB_JOINT_RUBX = 13,        /* JointModelRUBX/RUBY/RUBZ (joint-revolute-unbounded.hpp): revolute   */
   GB_JOINT_RUBY = 14,        /* about x / y / z with q = (cos t, sin t) taken as given (not        */
   GB_JOINT_RUBZ = 15,        /* renormalised), nq = 2, nv = 1; what the URDF "continuous" joint is */

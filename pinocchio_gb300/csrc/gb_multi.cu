@@ -43,7 +43,9 @@ struct TaskTable {
   long ntiles;
 };
 
-template <class S, class SS, int CAP>
+// J3: some task's model has spherical / planar joints (the ABA's three-dof steps are compiled in
+// only then, so that the launches of the other models keep their registers)
+template <class S, class SS, int CAP, bool J3>
 __global__ void k_multi(TaskTable tab, int tile, int blob_region, int warp_region) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned char* staged = nullptr;
@@ -84,13 +86,13 @@ __global__ void k_multi(TaskTable tab, int tile, int blob_region, int warp_regio
     const gb::In q{T.q + b * T.nq, 1}, v{T.v + b * T.nv, 1}, x{T.x + b * T.nv, 1};
     const gb::Out o{T.out + b * T.nv, 1};
     if (T.function == GB_FUNC_RNEA) gb::rnea_one<S, CAP>(m, q, v, x, o);
-    else gb::aba_one<S, SS, CAP>(m, q, v, x, o);
+    else gb::aba_one<S, SS, CAP, J3>(m, q, v, x, o);
   }
 }
 
 template <class S, class SS, int CAP>
-int launch_multi_cap(const TaskTable& tab, int tile, int blob_region, int warp_region, cudaStream_t st) {
-  auto kernel = k_multi<S, SS, CAP>;
+int launch_multi_cap(const TaskTable& tab, int tile, int blob_region, int warp_region, bool j3, cudaStream_t st) {
+  auto kernel = j3 ? k_multi<S, SS, CAP, true> : k_multi<S, SS, CAP, false>;
   const int smem = blob_region + (tile / 32) * warp_region;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return cuda_error(e, "k_multi");
@@ -128,9 +130,6 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
     if (t.model == nullptr) return set_error(GB_ERR_INVALID_ARGUMENT, "task model is NULL");
     if (t.model->has_mimic)
       return set_error(GB_ERR_UNSUPPORTED, "mimic joints: the heterogeneous launch does not take them (gb_rnea does)");
-    if (t.model->has_three)
-      return set_error(GB_ERR_UNSUPPORTED, "spherical and planar joints: the heterogeneous launch does not take them "
-                                           "(gb_rnea / gb_aba do)");
     if (t.function != GB_FUNC_RNEA && t.function != GB_FUNC_ABA) return set_error(GB_ERR_INVALID_ARGUMENT, "unknown task function");
     if (t.batch < 0) return set_error(GB_ERR_SIZE, "task batch must be >= 0");
     if (t.batch > 0) {
@@ -165,6 +164,7 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
   tab.ntasks = 0;
   tab.ntiles = 0;
   int cap = 8;
+  bool j3 = false;  // spherical / planar joints in a task (they run one configuration per thread)
   for (int k : order) {
     const gb_task& t = tasks[k];
     if (t.batch == 0) continue;
@@ -180,16 +180,17 @@ extern "C" int gb_batch_multi(const gb_task* tasks, int ntasks, int precision, i
     d.nq = t.model->nq; d.nv = t.model->nv;
     tab.ntiles += (t.batch + d.per_tile - 1) / d.per_tile;
     if (!use_warp[k]) cap = std::max(cap, t.model->cap);
+    j3 = j3 || t.model->has_three;
   }
   if (tab.ntasks == 0) return GB_OK;
   cudaStream_t st = (cudaStream_t)stream;
   const int wr = (int)warp_region;
   switch (cap) {
-    case 8: return f64 ? launch_multi_cap<double, double, 8>(tab, tile, blob_region, wr, st) : launch_multi_cap<float, double, 8>(tab, tile, blob_region, wr, st);
-    case 16: return f64 ? launch_multi_cap<double, double, 16>(tab, tile, blob_region, wr, st) : launch_multi_cap<float, double, 16>(tab, tile, blob_region, wr, st);
-    case 32: return f64 ? launch_multi_cap<double, double, 32>(tab, tile, blob_region, wr, st) : launch_multi_cap<float, double, 32>(tab, tile, blob_region, wr, st);
-    case 64: return f64 ? launch_multi_cap<double, double, 64>(tab, tile, blob_region, wr, st) : launch_multi_cap<float, double, 64>(tab, tile, blob_region, wr, st);
-    case 128: return f64 ? launch_multi_cap<double, double, 128>(tab, tile, blob_region, wr, st) : launch_multi_cap<float, double, 128>(tab, tile, blob_region, wr, st);
+    case 8: return f64 ? launch_multi_cap<double, double, 8>(tab, tile, blob_region, wr, j3, st) : launch_multi_cap<float, double, 8>(tab, tile, blob_region, wr, j3, st);
+    case 16: return f64 ? launch_multi_cap<double, double, 16>(tab, tile, blob_region, wr, j3, st) : launch_multi_cap<float, double, 16>(tab, tile, blob_region, wr, j3, st);
+    case 32: return f64 ? launch_multi_cap<double, double, 32>(tab, tile, blob_region, wr, j3, st) : launch_multi_cap<float, double, 32>(tab, tile, blob_region, wr, j3, st);
+    case 64: return f64 ? launch_multi_cap<double, double, 64>(tab, tile, blob_region, wr, j3, st) : launch_multi_cap<float, double, 64>(tab, tile, blob_region, wr, j3, st);
+    case 128: return f64 ? launch_multi_cap<double, double, 128>(tab, tile, blob_region, wr, j3, st) : launch_multi_cap<float, double, 128>(tab, tile, blob_region, wr, j3, st);
     default: return set_error(GB_ERR_UNSUPPORTED, "model too large");
   }
 }

@@ -217,7 +217,8 @@ def test_autotuner_chooses_a_derivative_layout(tmp_path, monkeypatch):
 
 def test_three_dof_joints_run_per_thread(tmp_path, monkeypatch):
     """Models with spherical or planar joints run one configuration per thread: the lane
-    layouts are refused, the autotuner keeps to CTA sizes, and gb_batch_multi refuses them."""
+    layouts are refused, the autotuner keeps to CTA sizes, and gb_batch_multi runs them next to
+    other trees (the three-dof steps compiled in for that launch only)."""
     import torch
 
     from util import MODELS
@@ -235,5 +236,11 @@ def test_three_dof_joints_run_per_thread(tmp_path, monkeypatch):
     q, v, x = (torch.from_numpy(a).cuda() for a in sm.random_inputs(model, 64, 5))
     ddq_o = OracleModel(model).aba(*(t.cpu().numpy() for t in (q, v, x)), LOCAL)
     assert rel_err(pg.aba(model, data, q, v, x).cpu().numpy(), ddq_o) < FP64_TOL
-    with pytest.raises(pg._capi.GBError):
-        api.MultiBatch([(data, "aba", q, v, x)]).run()
+    other = sm.random_tree(12, False, 312)
+    d2 = pg.createData(other)
+    q2, v2, x2 = (torch.from_numpy(a).cuda() for a in sm.random_inputs(other, 96, 6))
+    outs = api.MultiBatch([(data, "aba", q, v, x), (d2, "rnea", q2, v2, x2), (data, "rnea", q, v, x)]).run()
+    outs = [o.cpu().numpy() for o in outs]
+    assert rel_err(outs[0], ddq_o) < FP64_TOL
+    assert rel_err(outs[1], OracleModel(other).rnea(*(t.cpu().numpy() for t in (q2, v2, x2)))) < FP64_TOL
+    assert rel_err(outs[2], OracleModel(model).rnea(*(t.cpu().numpy() for t in (q, v, x)))) < FP64_TOL
