@@ -2541,8 +2541,9 @@ ProximalResult constraint_dynamics_derivatives(const Model& m, Data<T>& d, const
   for (const auto& c : cms) {
     bool gains = false;
     for (int k = 0; k < 6; ++k) gains = gains || c.Kp[k] != 0.0 || c.Kd[k] != 0.0;
-    if (c.joint2 != 0 || gains)
-      throw std::invalid_argument("the derivatives take constraints to the world without Baumgarte gains");
+    if (c.joint2 != 0 || (gains && (c.type == CONTACT_6D || c.frame != RF_LOCAL)))
+      throw std::invalid_argument(
+          "the derivatives take constraints to the world, with Baumgarte gains on LOCAL point contacts only");
   }
   const int nv = m.nv;
   const ProximalResult res = constraint_dynamics(m, d, q, v, tau, cms, mu, max_iter, abs_acc, rel_acc, ddq, lambda);
@@ -2610,6 +2611,30 @@ ProximalResult constraint_dynamics_derivatives(const Model& m, Data<T>& d, const
         Aq[(size_t)(row + k) * nv + col] = adq[(size_t)stride * col + k];
         Av[(size_t)(row + k) * nv + col] = adv[(size_t)stride * col + k];
       }
+    bool gains = false;
+    for (int k = 0; k < 6; ++k) gains = gains || c.Kp[k] != 0.0 || c.Kd[k] != 0.0;
+    if (gains) {  // the corrector's derivative for a LOCAL point contact to the world (hxx:753-830):
+      // dac_dq += Kd dvc_dq + Kp dac_da + Kp pe x (R1^T J_ang) on joint 1's support (pe =
+      // -c1Mc2.translation the placement error), dac_dv += Kd dac_da.  (In LOCAL_WORLD_ALIGNED axes
+      // the reference's same terms miss the rotation of the corrector into world axes: central
+      // differences disagree, so those are refused.)
+      const SE3<T> oMc1 = se3_mul(d.oMi[c.joint1], P);
+      const SE3<T> c1Mc2 = se3_actinv(oMc1, se3_from<T>(c.P2));
+      const T pe[3] = {-c1Mc2.t[0], -c1Mc2.t[1], -c1Mc2.t[2]};
+      for (int j = m.idx_v[c.joint1] + m.nvs[c.joint1] - 1; j >= 0; j = m.parents_fromRow[j]) {
+          const Vec6<T> Jcol = col6(d.J, j);
+          T wa[3], x[3];
+          matTvec(oMc1.R, Jcol.v + 3, wa);
+          cross3(pe, wa, x);
+          for (int k = 0; k < 3; ++k) Aq[(size_t)(row + k) * nv + j] += T(c.Kp[k]) * x[k];
+        }
+      for (int k = 0; k < 3; ++k)
+        for (int col = 0; col < nv; ++col) {
+          const T da = ada[(size_t)3 * col + k];
+          Aq[(size_t)(row + k) * nv + col] += T(c.Kd[k]) * vdq[(size_t)3 * col + k] + T(c.Kp[k]) * da;
+          Av[(size_t)(row + k) * nv + col] += T(c.Kd[k]) * da;
+        }
+    }
     row += n;
   }
   // JMinv, osim = (J M^-1 J^T + mu I)^-1

@@ -732,6 +732,16 @@ __global__ void __launch_bounds__(kThreads)
     X3d P, oMc;
     load_se3(c.P1, P);
     gb::compose(oM[j], P, oMc);
+    // Baumgarte gains (LOCAL point contacts: the host refuses the others): the placement error
+    // pe = -c1Mc2.translation = -R_c^T (t_anchor - t_c) of the corrector's derivative
+    const bool gains3 = n == 3 && c.gains;
+    double pe[3] = {0.0, 0.0, 0.0};
+    if (gains3) {
+      const double dpos[3] = {c.P2[9] - oMc.t[0], c.P2[10] - oMc.t[1], c.P2[11] - oMc.t[2]};
+      gb::mtv3(oMc.R, dpos, pe);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) pe[k] = -pe[k];
+    }
     M6d f;
     gb::zero(f);
     for (int k = 0; k < n; ++k) f.v[k] = li[row + k];
@@ -903,6 +913,17 @@ __global__ void __launch_bounds__(kThreads)
             rj[r] = ada[r];
             rq[r] = adq[r];
             rv[r] = adv[r];
+          }
+          if (gains3) {  // the corrector (hxx:753-830): dac_dq += Kd dvc_dq + Kp (dac_da + pe x (R_c^T J_ang)),
+                         // dac_dv += Kd dac_da
+            double wa[3], x[3];
+            gb::mtv3(oMc.R, Jc.v + 3, wa);
+            gb::cross3(pe, wa, x);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+              rq[r] += c.Kd[r] * vdq[r] + c.Kp[r] * (ada[r] + x[r]);
+              rv[r] += c.Kd[r] * ada[r];
+            }
           }
         }
         for (int r = 0; r < n; ++r) {

@@ -307,6 +307,35 @@ def test_constraint_dynamics_derivatives_central_differences(humanoid, kinds):
         assert rel_err(a, f) < 1e-6, (name, rel_err(a, f))
 
 
+def test_constraint_dynamics_derivatives_with_point_contact_gains(humanoid):
+    """LOCAL point contacts to the world with Baumgarte gains (the corrector's derivative,
+    constrained-dynamics-derivatives.hxx:753-830) against central differences, next to a frame
+    contact without gains and a world-aligned point contact without gains; the reference's same
+    terms in LOCAL_WORLD_ALIGNED axes disagree with central differences and are refused."""
+    model, om = humanoid
+    rng = np.random.default_rng(31)
+    lv = _leaves(model)
+    cms = [cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[0], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
+           cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[2], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
+           cs.RigidConstraintModel(cs.CONTACT_6D, model, lv[1], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
+           cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[3], _rand_se3(rng), 0, _rand_se3(rng, 1.0),
+                                   cs.LOCAL_WORLD_ALIGNED)]
+    for c in cms[:2]:
+        c.corrector.Kp[:] = rng.uniform(0.5, 5.0, 3)
+        c.corrector.Kd[:] = rng.uniform(0.5, 5.0, 3)
+    q, v, x = sm.random_inputs(model, 4, 32)
+    desc = cs.stack_desc(cms)
+    got = om.constraint_dynamics_derivatives(q, v, 10 * x, desc)
+    fd = _central_differences(model, om, q, v, 10 * x, desc)
+    names = ("ddq_dq", "dlambda_dq", "ddq_dv", "dlambda_dv", "ddq_dtau", "dlambda_dtau")
+    analytic = (got[2], got[5], got[3], got[6], got[4], got[7])
+    for name, a, f in zip(names, analytic, fd):
+        assert rel_err(a, f) < 1e-6, (name, rel_err(a, f))
+    cms[3].corrector.Kp[:] = 1.0
+    with pytest.raises(ValueError):
+        om.constraint_dynamics_derivatives(q, v, 10 * x, cs.stack_desc(cms))
+
+
 def test_constraint_dynamics_derivatives_proximal_and_errors(humanoid):
     """With mu > 0 the derivatives follow the proximal recursion: at convergence they approach the
     undamped derivatives; closed loops and Baumgarte gains are rejected."""

@@ -267,6 +267,41 @@ def test_constraint_dynamics_derivatives_match_oracle(name, precision):
     assert pg.numericStatus(data) == 0
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_constraint_dynamics_derivatives_with_point_contact_gains(precision):
+    """LOCAL point contacts with Baumgarte gains (the corrector's derivative) next to a frame
+    contact and a world-aligned point contact without gains, against the oracle; gains on a
+    world-aligned point contact are refused."""
+    model = sm.humanoid32(1)
+    om = OracleModel(model)
+    rng = np.random.default_rng(41)
+    lv = _leaves(model)
+    cms = [cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[0], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
+           cs.RigidConstraintModel(cs.CONTACT_6D, model, lv[1], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
+           cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[2], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
+           cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[3], _rand_se3(rng), 0, _rand_se3(rng, 1.0),
+                                   cs.LOCAL_WORLD_ALIGNED)]
+    for c in (cms[0], cms[2]):
+        c.corrector.Kp[:] = rng.uniform(0.5, 5.0, 3)
+        c.corrector.Kd[:] = rng.uniform(0.5, 5.0, 3)
+    q, v, x = sm.random_inputs(model, 97, 42)
+    v = 0.3 * v
+    data = pg.createData(model, precision)
+    pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms)
+    got = [t.cpu().numpy() for t in pg.computeConstraintDynamicsDerivatives(model, data, cms)]
+    (o, ld, tol64) = _deriv_tol(om, q, v, 10 * x, cs.stack_desc(cms))
+    for k in range(6):
+        if precision == "fp64":
+            assert rel_err(got[k], ld[2 + k]) < tol64, (k, rel_err(got[k], ld[2 + k]), tol64)
+        else:
+            assert rel_err(got[k], o[2 + k]) < max(1e-4, 30 * tol64), (k, rel_err(got[k], o[2 + k]))
+    cms[3].corrector.Kp[:] = 1.0
+    pg.constraintDynamics(model, data, _dev(q), _dev(v), _dev(10 * x), cms)
+    with pytest.raises(_capi.GBError) as e:
+        pg.computeConstraintDynamicsDerivatives(model, data, cms)
+    assert e.value.code == _capi.GB_ERR_UNSUPPORTED
+
+
 def test_constraint_dynamics_derivatives_proximal_and_errors():
     """mu > 0 with a fixed number of iterations (accuracies 0): the derivatives follow the oracle's
     proximal recursion; no constraint gives the ABA derivatives; closed loops and Baumgarte gains are
