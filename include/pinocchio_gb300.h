@@ -393,9 +393,9 @@ int gb_constraint_dynamics(const gb_model* model, int precision, const gb_constr
  * (nv x nv, row-major per instance) and of lambda_c (constraint_dim x nv) with respect to q (in the
  * tangent space), v and tau, following the reference's proximal recursion over each instance's
  * iteration count; iterations may be NULL.  Constraints to the world (joint2_id = 0), with Baumgarte
- * gains on GB_CONTACT_3D / GB_FRAME_LOCAL constraints only (others: GB_ERR_UNSUPPORTED; the
- * reference's corrector terms in world-aligned axes disagree with central differences of its own
- * constraintDynamics); gravity without an angular part (GB_ERR_GRAVITY).
+ * gains on GB_FRAME_LOCAL constraints only (others: GB_ERR_UNSUPPORTED; the reference's corrector
+ * terms in world-aligned axes disagree with central differences of its own constraintDynamics);
+ * gravity without an angular part (GB_ERR_GRAVITY).
  * The inverse-dynamics derivatives at ddq use the precision's sweeps, the rest is FP64. */
 int gb_constraint_dynamics_derivatives(const gb_model* model, int precision, const gb_constraint_set* set,
                                        const gb_proximal_settings* settings, int layout, long batch,

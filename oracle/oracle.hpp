@@ -1921,6 +1921,70 @@ template <class T> inline Vec6<T> log6(const SE3<T>& M) {
   return o;
 }
 
+// Jlog6 (spatial/explog.hpp, Jlog6): d log6(M exp6(d)) / dd at d = 0, the inverse of SE(3)'s right
+// Jacobian at xi = log6(M) = (rho, phi) ([linear; angular]), written from the published closed form
+// (Barfoot, State Estimation for Robotics, 7.1.5; the right Jacobian is the left one at -xi):
+//   [[Jr^-1(phi), -Jr^-1(phi) Qr Jr^-1(phi)], [0, Jr^-1(phi)]], row-major 6 x 6,
+//   Jr^-1(phi) = I + phi^ / 2 + c phi^ phi^, c = 1 / t^2 - (1 + cos t) / (2 t sin t),
+//   Qr = -rho^ / 2 + a1 (phi^ rho^ + rho^ phi^ - phi^ rho^ phi^) - a2 (phi^ phi^ rho^ + rho^ phi^ phi^
+//        - 3 phi^ rho^ phi^) + a3 (phi^ rho^ phi^ phi^ + phi^ phi^ rho^ phi^),
+//   a1 = (t - sin t) / t^3, a2 = (t^2 + 2 cos t - 2) / (2 t^4), a3 = (2 t - 3 sin t + t cos t) / (2 t^5),
+// with their Taylor series for small t.
+template <class T> inline void jlog6(const SE3<T>& M, T* J) {
+  const Vec6<T> xi = log6(M);
+  const T* rho = xi.v;
+  const T* phi = xi.v + 3;
+  const T t2 = phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2], t = o_sqrt(t2);
+  T c, a1, a2, a3;
+  if (t < T(1e-3)) {
+    c = T(1) / T(12) + t2 / T(720);
+    a1 = T(1) / T(6) - t2 / T(120);
+    a2 = T(1) / T(24) - t2 / T(720);
+    a3 = T(1) / T(120) - t2 / T(2520);
+  } else {
+    T st, ct;
+    o_sincos(t, &st, &ct);
+    c = T(1) / t2 - (T(1) + ct) / (T(2) * t * st);
+    a1 = (t - st) / (t2 * t);
+    a2 = (t2 + T(2) * ct - T(2)) / (T(2) * t2 * t2);
+    a3 = (T(2) * t - T(3) * st + t * ct) / (T(2) * t2 * t2 * t);
+  }
+  auto skew = [](const T* v, T* S) {
+    S[0] = T(0); S[1] = -v[2]; S[2] = v[1];
+    S[3] = v[2]; S[4] = T(0); S[5] = -v[0];
+    S[6] = -v[1]; S[7] = v[0]; S[8] = T(0);
+  };
+  auto mul = [](const T* A, const T* B, T* C) {
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) C[3 * r + q] = A[3 * r] * B[q] + A[3 * r + 1] * B[3 + q] + A[3 * r + 2] * B[6 + q];
+  };
+  T P[9], R[9], PP[9], PR[9], RP[9], PRP[9], PPR[9], RPP[9], PRPP[9], PPRP[9], Jr[9], Q[9], tmp[9], B[9];
+  skew(phi, P);
+  skew(rho, R);
+  mul(P, P, PP);
+  mul(P, R, PR);
+  mul(R, P, RP);
+  mul(PR, P, PRP);
+  mul(PP, R, PPR);
+  mul(RP, P, RPP);
+  mul(PRP, P, PRPP);
+  mul(PPR, P, PPRP);
+  for (int k = 0; k < 9; ++k) {
+    Jr[k] = (k % 4 == 0 ? T(1) : T(0)) + T(0.5) * P[k] + c * PP[k];
+    Q[k] = -T(0.5) * R[k] + a1 * (PR[k] + RP[k] - PRP[k]) - a2 * (PPR[k] + RPP[k] - T(3) * PRP[k]) +
+           a3 * (PRPP[k] + PPRP[k]);
+  }
+  mul(Jr, Q, tmp);
+  mul(tmp, Jr, B);
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) {
+      J[6 * r + q] = Jr[3 * r + q];
+      J[6 * r + 3 + q] = -B[3 * r + q];
+      J[6 * (3 + r) + q] = T(0);
+      J[6 * (3 + r) + 3 + q] = Jr[3 * r + q];
+    }
+}
+
 // The contact Cholesky factorisation U D U^T of the KKT matrix (contact-cholesky.hxx:21-330):
 // rows / columns 0..nc-1 the constraints, nc..nc+nv-1 the dofs; U unit upper, row-major.
 template <class T> struct ContactCholesky {
@@ -2541,9 +2605,9 @@ ProximalResult constraint_dynamics_derivatives(const Model& m, Data<T>& d, const
   for (const auto& c : cms) {
     bool gains = false;
     for (int k = 0; k < 6; ++k) gains = gains || c.Kp[k] != 0.0 || c.Kd[k] != 0.0;
-    if (c.joint2 != 0 || (gains && (c.type == CONTACT_6D || c.frame != RF_LOCAL)))
+    if (c.joint2 != 0 || (gains && c.frame != RF_LOCAL))
       throw std::invalid_argument(
-          "the derivatives take constraints to the world, with Baumgarte gains on LOCAL point contacts only");
+          "the derivatives take constraints to the world, with Baumgarte gains on LOCAL contacts only");
   }
   const int nv = m.nv;
   const ProximalResult res = constraint_dynamics(m, d, q, v, tau, cms, mu, max_iter, abs_acc, rel_acc, ddq, lambda);
@@ -2613,7 +2677,25 @@ ProximalResult constraint_dynamics_derivatives(const Model& m, Data<T>& d, const
       }
     bool gains = false;
     for (int k = 0; k < 6; ++k) gains = gains || c.Kp[k] != 0.0 || c.Kd[k] != 0.0;
-    if (gains) {  // the corrector's derivative for a LOCAL point contact to the world (hxx:753-830):
+    if (gains && c.type == CONTACT_6D) {  // the corrector's derivative for a LOCAL frame contact
+      // (hxx:758-782): dac_dq += Kd dvc_dq + Kp Jlog6(c1Mc2^-1) dac_da, dac_dv += Kd dac_da
+      const SE3<T> oMc1 = se3_mul(d.oMi[c.joint1], P);
+      const SE3<T> c1Mc2 = se3_actinv(oMc1, se3_from<T>(c.P2));
+      SE3<T> c2Mc1;  // the inverse placement (R^T, -R^T t)
+      for (int r = 0; r < 3; ++r)
+        for (int q2 = 0; q2 < 3; ++q2) c2Mc1.R[3 * r + q2] = c1Mc2.R[3 * q2 + r];
+      matTvec(c1Mc2.R, c1Mc2.t, c2Mc1.t);
+      for (int r = 0; r < 3; ++r) c2Mc1.t[r] = -c2Mc1.t[r];
+      T Jl[36];
+      jlog6(c2Mc1, Jl);
+      for (int col = 0; col < nv; ++col)
+        for (int k = 0; k < 6; ++k) {
+          T acc = T(0);
+          for (int i = 0; i < 6; ++i) acc += Jl[6 * k + i] * ada[(size_t)6 * col + i];
+          Aq[(size_t)(row + k) * nv + col] += T(c.Kd[k]) * vdq[(size_t)6 * col + k] + T(c.Kp[k]) * acc;
+          Av[(size_t)(row + k) * nv + col] += T(c.Kd[k]) * ada[(size_t)6 * col + k];
+        }
+    } else if (gains) {  // the corrector's derivative for a LOCAL point contact to the world (hxx:753-830):
       // dac_dq += Kd dvc_dq + Kp dac_da + Kp pe x (R1^T J_ang) on joint 1's support (pe =
       // -c1Mc2.translation the placement error), dac_dv += Kd dac_da.  (In LOCAL_WORLD_ALIGNED axes
       // the reference's same terms miss the rotation of the corrector into world axes: central

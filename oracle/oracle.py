@@ -62,6 +62,7 @@ def lib():
                                               C.c_double, C.c_double, vp, vp, vp, vp, C.c_int]
         L.orc_constraint_dynamics_derivatives.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, vp, C.c_double,
                                                           C.c_int, C.c_double, C.c_double] + [vp] * 9 + [C.c_int]
+        L.orc_log6.argtypes = [vp, vp, vp]
         L.orc_contact_cholesky.argtypes = [vp, C.c_long, C.c_int, vp, vp, C.c_double, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_impulse_dynamics.argtypes = [vp, C.c_int, C.c_long, C.c_int, vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int]
         L.orc_integrate.argtypes = [vp, C.c_int, C.c_long, vp, vp, vp, C.c_int]
@@ -440,3 +441,13 @@ class MimicOracleModel:
                 n = self.model.nqs[i]
                 out[:, self.rq[i] : self.rq[i] + n] = qf[:, self.fq[i] : self.fq[i] + n]
         return out
+
+
+def log6(M):
+    """(log6(M), Jlog6(M)) of a placement M = (R (3, 3), t (3,)) (reference spatial/explog.hpp)."""
+    R, t = M
+    m = _c(np.concatenate([np.asarray(R, dtype=np.float64).reshape(9), np.asarray(t, dtype=np.float64)]))
+    xi, J = np.empty(6), np.empty((6, 6))
+    lib().orc_log6(_ptr(m), _ptr(xi), _ptr(J))
+    return xi, J
+

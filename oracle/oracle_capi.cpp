@@ -462,7 +462,16 @@ extern "C" int orc_constraint_dynamics(void* h, int prec, long B, int ncontacts,
   }
 }
 
-// ContactCholeskyDecomposition(model, contact_models).compute(model, data, contact_models,
+// log6 and Jlog6 of one placement M (12 doubles: R row-major, t): xi (6), J (6 x 6 row-major)
+extern "C" int orc_log6(const double* M, double* xi, double* J) {
+  orc::SE3<double> P = orc::se3_from<double>(M);
+  const orc::Vec6<double> x = orc::log6(P);
+  for (int k = 0; k < 6; ++k) xi[k] = x.v[k];
+  if (J) orc::jlog6(P, J);
+  return 0;
+}
+
+// ContactCholeskyDecomposition(model, contact_models).compute(model, data, contact_models,// ContactCholeskyDecomposition(model, contact_models).compute(model, data, contact_models,
 // contact_datas, mu) at each configuration and its accessors (contact-cholesky.hpp:168-265,
 // contact-cholesky.hxx:152-304, 617-759); n = constraint dim + nv; every output may be null.
 extern "C" int orc_contact_cholesky(void* h, long B, int ncontacts, const double* desc, const double* q, double mu,

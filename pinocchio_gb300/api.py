@@ -591,8 +591,8 @@ def computeConstraintDynamicsDerivatives(model: Model, data: Data, contact_model
     constraintDynamics call on ``data`` (reference
     algorithm/constrained-dynamics-derivatives.hxx:344-1050, binding
     expose-constrained-dynamics-derivatives.cpp:23-37): batched (batch, nv, nv) and
-    (batch, constraint_dim, nv) tensors, also kept in data.  Constraints to the world without
-    Baumgarte gains (others raise)."""
+    (batch, constraint_dim, nv) tensors, also kept in data.  Constraints to the world, with
+    Baumgarte gains on LOCAL contacts only (others raise)."""
     torch = _torch()
     inputs = getattr(data, "constraint_inputs", None)
     if inputs is None:

@@ -439,10 +439,10 @@ int gb_constraint_dynamics_derivatives(const gb_model* M, int precision, const g
     return set_error(GB_ERR_INVALID_ARGUMENT, "Accuracy must be positive.");
   if (settings->max_iter < 1) return set_error(GB_ERR_INVALID_ARGUMENT, "max_iter must be greater or equal to 1");
   for (const gbi::ConstraintDev& c : S->host)
-    if (c.j2 != 0 || (c.gains && (c.type != GB_CONTACT_3D || c.frame != GB_FRAME_LOCAL)))
+    if (c.j2 != 0 || (c.gains && c.frame != GB_FRAME_LOCAL))
       return set_error(GB_ERR_UNSUPPORTED,
                        "the constraint dynamics derivatives take constraints to the world (joint2_id = 0), with "
-                       "Baumgarte gains on LOCAL point contacts only");
+                       "Baumgarte gains on LOCAL contacts only");
   GB_TRY(gbi::check_gravity(M));
   if (B == 0) return GB_OK;
   GB_TRY(gbi::check_ptr(q, "q")); GB_TRY(gbi::check_ptr(v, "v")); GB_TRY(gbi::check_ptr(tau, "tau"));

@@ -289,6 +289,68 @@ __device__ void log6(const X3d& M, M6d& o) {
     o.v[3 + k] = w[k];
   }
 }
+
+// Jlog6 = d log6(M exp6(d)) / dd at d = 0 (row-major 6 x 6, [linear; angular]): the inverse of SE(3)'s
+// right Jacobian at (rho, phi) = log6(M), from the published closed form (Barfoot, State Estimation
+// for Robotics, 7.1.5): [[Jr^-1, -Jr^-1 Qr Jr^-1], [0, Jr^-1]] with Jr^-1 = I + phi^ / 2 + c phi^2 and
+// Qr the right-Jacobian coupling block (a1, a2, a3 below; Taylor series for small angles)
+__device__ void jlog6(const X3d& M, double* J) {
+  M6d xi;
+  log6(M, xi);
+  const double* rho = xi.v;
+  const double* phi = xi.v + 3;
+  const double t2 = phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2], t = sqrt(t2);
+  double c, a1, a2, a3;
+  if (t < 1e-3) {
+    c = 1.0 / 12.0 + t2 / 720.0;
+    a1 = 1.0 / 6.0 - t2 / 120.0;
+    a2 = 1.0 / 24.0 - t2 / 720.0;
+    a3 = 1.0 / 120.0 - t2 / 2520.0;
+  } else {
+    double st, ct;
+    sincos(t, &st, &ct);
+    c = 1.0 / t2 - (1.0 + ct) / (2.0 * t * st);
+    a1 = (t - st) / (t2 * t);
+    a2 = (t2 + 2.0 * ct - 2.0) / (2.0 * t2 * t2);
+    a3 = (2.0 * t - 3.0 * st + t * ct) / (2.0 * t2 * t2 * t);
+  }
+  auto skew = [](const double* v, double* S) {
+    S[0] = 0.0; S[1] = -v[2]; S[2] = v[1];
+    S[3] = v[2]; S[4] = 0.0; S[5] = -v[0];
+    S[6] = -v[1]; S[7] = v[0]; S[8] = 0.0;
+  };
+  auto mul = [](const double* A, const double* B, double* C) {
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) C[3 * r + q] = A[3 * r] * B[q] + A[3 * r + 1] * B[3 + q] + A[3 * r + 2] * B[6 + q];
+  };
+  double P[9], R[9], PP[9], PR[9], RP[9], PRP[9], X[9], Y[9], Jr[9], Q[9];
+  skew(phi, P);
+  skew(rho, R);
+  mul(P, P, PP);
+  mul(P, R, PR);
+  mul(R, P, RP);
+  mul(PR, P, PRP);
+  for (int k = 0; k < 9; ++k) {
+    Jr[k] = (k % 4 == 0 ? 1.0 : 0.0) + 0.5 * P[k] + c * PP[k];
+    Q[k] = -0.5 * R[k] + a1 * (PR[k] + RP[k] - PRP[k]);
+  }
+  mul(PP, R, X);  // phi^ phi^ rho^, then + rho^ phi^ phi^ - 3 phi^ rho^ phi^
+  mul(RP, P, Y);
+  for (int k = 0; k < 9; ++k) Q[k] -= a2 * (X[k] + Y[k] - 3.0 * PRP[k]);
+  mul(PRP, P, X);  // phi^ rho^ phi^ phi^ + phi^ phi^ rho^ phi^
+  mul(PP, R, Y);
+  mul(Y, P, R);
+  for (int k = 0; k < 9; ++k) Q[k] += a3 * (X[k] + R[k]);
+  mul(Jr, Q, X);
+  mul(X, Jr, Y);
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) {
+      J[6 * r + q] = Jr[3 * r + q];
+      J[6 * r + 3 + q] = -Y[3 * r + q];
+      J[6 * (3 + r) + q] = 0.0;
+      J[6 * (3 + r) + 3 + q] = Jr[3 * r + q];
+    }
+}
 // ov.ang x (ov.lin + ov.ang x p): the velocity-product part of a point's classical acceleration
 __device__ void point_drift(const M6d& ov, const double* p, double* o) {
   double wxp[3], vp[3];
@@ -732,15 +794,22 @@ __global__ void __launch_bounds__(kThreads)
     X3d P, oMc;
     load_se3(c.P1, P);
     gb::compose(oM[j], P, oMc);
-    // Baumgarte gains (LOCAL point contacts: the host refuses the others): the placement error
-    // pe = -c1Mc2.translation = -R_c^T (t_anchor - t_c) of the corrector's derivative
-    const bool gains3 = n == 3 && c.gains;
+    // Baumgarte gains (LOCAL contacts: the host refuses the others): the point contact's placement
+    // error pe = -c1Mc2.translation = -R_c^T (t_anchor - t_c), the frame contact's Jlog6(c1Mc2^-1)
+    const bool gains3 = n == 3 && c.gains, gains6 = n == 6 && c.gains;
     double pe[3] = {0.0, 0.0, 0.0};
+    double Jl[36];
     if (gains3) {
       const double dpos[3] = {c.P2[9] - oMc.t[0], c.P2[10] - oMc.t[1], c.P2[11] - oMc.t[2]};
       gb::mtv3(oMc.R, dpos, pe);
 #pragma unroll
       for (int k = 0; k < 3; ++k) pe[k] = -pe[k];
+    }
+    if (gains6) {  // c2Mc1 = anchor^-1 oMc
+      X3d A, c21;
+      load_se3(c.P2, A);
+      se3_actinv(A, oMc, c21);
+      jlog6(c21, Jl);
     }
     M6d f;
     gb::zero(f);
@@ -846,8 +915,8 @@ __global__ void __launch_bounds__(kThreads)
             for (int r = 0; r < 6; ++r) adv.v[r] += vdq.v[r];
           }
           // the frame's placement in the joint (frames-derivatives.hxx:137-172)
-          M6d* mats[3] = {&da, &adq, &adv};
-          for (int t = 0; t < 3; ++t) {
+          M6d* mats[4] = {&da, &adq, &adv, &vdq};
+          for (int t = 0; t < (gains6 ? 4 : 3); ++t) {
             if (local) {
               M6d y;
               gb::actinv_motion(P, *mats[t], y);
@@ -862,6 +931,14 @@ __global__ void __launch_bounds__(kThreads)
             rq[r] = adq.v[r];
             rv[r] = adv.v[r];
           }
+          if (gains6)  // the corrector (hxx:758-782): dac_dq += Kd dvc_dq + Kp Jlog6 dac_da, dac_dv += Kd dac_da
+            for (int r = 0; r < 6; ++r) {
+              double acc = 0.0;
+#pragma unroll
+              for (int i2 = 0; i2 < 6; ++i2) acc += Jl[6 * r + i2] * da.v[i2];
+              rq[r] += c.Kd[r] * vdq.v[r] + c.Kp[r] * acc;
+              rv[r] += c.Kd[r] * da.v[r];
+            }
         } else {
           M6d sda, svdq, vtmp;
           gb::actinv_motion(oMc, Jc, sda);

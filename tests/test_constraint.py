@@ -307,11 +307,11 @@ def test_constraint_dynamics_derivatives_central_differences(humanoid, kinds):
         assert rel_err(a, f) < 1e-6, (name, rel_err(a, f))
 
 
-def test_constraint_dynamics_derivatives_with_point_contact_gains(humanoid):
-    """LOCAL point contacts to the world with Baumgarte gains (the corrector's derivative,
-    constrained-dynamics-derivatives.hxx:753-830) against central differences, next to a frame
-    contact without gains and a world-aligned point contact without gains; the reference's same
-    terms in LOCAL_WORLD_ALIGNED axes disagree with central differences and are refused."""
+def test_constraint_dynamics_derivatives_with_local_contact_gains(humanoid):
+    """LOCAL point and frame contacts to the world with Baumgarte gains (the corrector's derivative,
+    constrained-dynamics-derivatives.hxx:753-830, with Jlog6 for the frame contact) against central
+    differences, next to a world-aligned point contact without gains; the reference's same terms in
+    LOCAL_WORLD_ALIGNED axes disagree with central differences and are refused."""
     model, om = humanoid
     rng = np.random.default_rng(31)
     lv = _leaves(model)
@@ -320,9 +320,9 @@ def test_constraint_dynamics_derivatives_with_point_contact_gains(humanoid):
            cs.RigidConstraintModel(cs.CONTACT_6D, model, lv[1], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
            cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[3], _rand_se3(rng), 0, _rand_se3(rng, 1.0),
                                    cs.LOCAL_WORLD_ALIGNED)]
-    for c in cms[:2]:
-        c.corrector.Kp[:] = rng.uniform(0.5, 5.0, 3)
-        c.corrector.Kd[:] = rng.uniform(0.5, 5.0, 3)
+    for c in cms[:3]:
+        c.corrector.Kp[:] = rng.uniform(0.5, 5.0, c.size())
+        c.corrector.Kd[:] = rng.uniform(0.5, 5.0, c.size())
     q, v, x = sm.random_inputs(model, 4, 32)
     desc = cs.stack_desc(cms)
     got = om.constraint_dynamics_derivatives(q, v, 10 * x, desc)
@@ -338,7 +338,7 @@ def test_constraint_dynamics_derivatives_with_point_contact_gains(humanoid):
 
 def test_constraint_dynamics_derivatives_proximal_and_errors(humanoid):
     """With mu > 0 the derivatives follow the proximal recursion: at convergence they approach the
-    undamped derivatives; closed loops and Baumgarte gains are rejected."""
+    undamped derivatives; closed loops and Baumgarte gains in world-aligned axes are rejected."""
     model, om = humanoid
     rng = np.random.default_rng(23)
     cms = [cs.RigidConstraintModel(cs.CONTACT_6D, model, j, _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL)
@@ -355,9 +355,11 @@ def test_constraint_dynamics_derivatives_proximal_and_errors(humanoid):
                                     gm.SE3.Identity(), cs.LOCAL)]
     with pytest.raises(ValueError, match="world"):
         om.constraint_dynamics_derivatives(q, v, x, cs.stack_desc(loop))
-    cms[0].corrector.Kp[:] = 1.0
-    with pytest.raises(ValueError, match="world"):
-        om.constraint_dynamics_derivatives(q, v, x, cs.stack_desc(cms))
+    wa = [cs.RigidConstraintModel(cs.CONTACT_6D, model, _leaves(model)[0], gm.SE3.Identity(), 0, gm.SE3.Identity(),
+                                  cs.LOCAL_WORLD_ALIGNED)]
+    wa[0].corrector.Kp[:] = 1.0
+    with pytest.raises(ValueError, match="LOCAL contacts"):
+        om.constraint_dynamics_derivatives(q, v, x, cs.stack_desc(wa))
 
 
 @pytest.mark.parametrize("mu", [0.0, 0.1])
@@ -389,4 +391,31 @@ def test_contact_cholesky_accessors(humanoid, mu):
     assert rel_err(out["osim"], np.linalg.inv(JMJ)) < 1e-9
     assert rel_err(out["minv"], Minv) < 1e-11
     assert rel_err(out["jminv"], np.einsum("bij,bjk->bik", J, Minv)) < 1e-11
+
+
+def test_jlog6_against_central_differences():
+    """Jlog6 (spatial/explog.hpp) = d log6(M exp6(d)) / dd at 0, at large, small and zero angles."""
+    from oracle.oracle import log6
+
+    def exp6(d):
+        rho, phi = d[:3], d[3:]
+        t = np.linalg.norm(phi)
+        P = np.array([[0, -phi[2], phi[1]], [phi[2], 0, -phi[0]], [-phi[1], phi[0], 0]])
+        if t < 1e-12:
+            return np.eye(3) + P, rho + P @ rho / 2
+        R = np.eye(3) + np.sin(t) / t * P + (1 - np.cos(t)) / t**2 * P @ P
+        V = np.eye(3) + (1 - np.cos(t)) / t**2 * P + (t - np.sin(t)) / t**3 * P @ P
+        return R, V @ rho
+
+    rng = np.random.default_rng(0)
+    for scale in (2.5, 1.0, 1e-4, 0.0):
+        R, t = exp6(np.concatenate([rng.standard_normal(3), scale * rng.standard_normal(3)]))
+        _, J = log6((R, t))
+        F = np.zeros((6, 6))
+        for k in range(6):
+            e = np.zeros(6)
+            e[k] = 1e-6
+            (Rp, tp), (Rm, tm) = exp6(e), exp6(-e)
+            F[:, k] = (log6((R @ Rp, R @ tp + t))[0] - log6((R @ Rm, R @ tm + t))[0]) / 2e-6
+        assert np.abs(J - F).max() < 1e-8, scale
 

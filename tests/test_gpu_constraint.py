@@ -268,10 +268,10 @@ def test_constraint_dynamics_derivatives_match_oracle(name, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_constraint_dynamics_derivatives_with_point_contact_gains(precision):
-    """LOCAL point contacts with Baumgarte gains (the corrector's derivative) next to a frame
-    contact and a world-aligned point contact without gains, against the oracle; gains on a
-    world-aligned point contact are refused."""
+def test_constraint_dynamics_derivatives_with_local_contact_gains(precision):
+    """LOCAL point and frame contacts with Baumgarte gains (the corrector's derivative, Jlog6 for the
+    frame contact) next to a world-aligned point contact without gains, against the oracle; gains on
+    a world-aligned contact are refused."""
     model = sm.humanoid32(1)
     om = OracleModel(model)
     rng = np.random.default_rng(41)
@@ -281,9 +281,9 @@ def test_constraint_dynamics_derivatives_with_point_contact_gains(precision):
            cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[2], _rand_se3(rng), 0, _rand_se3(rng, 1.0), cs.LOCAL),
            cs.RigidConstraintModel(cs.CONTACT_3D, model, lv[3], _rand_se3(rng), 0, _rand_se3(rng, 1.0),
                                    cs.LOCAL_WORLD_ALIGNED)]
-    for c in (cms[0], cms[2]):
-        c.corrector.Kp[:] = rng.uniform(0.5, 5.0, 3)
-        c.corrector.Kd[:] = rng.uniform(0.5, 5.0, 3)
+    for c in cms[:3]:
+        c.corrector.Kp[:] = rng.uniform(0.5, 5.0, c.size())
+        c.corrector.Kd[:] = rng.uniform(0.5, 5.0, c.size())
     q, v, x = sm.random_inputs(model, 97, 42)
     v = 0.3 * v
     data = pg.createData(model, precision)
