@@ -74,9 +74,12 @@ enum {
   GB_JOINT_RUBX = 13,        /* JointModelRUBX/RUBY/RUBZ (joint-revolute-unbounded.hpp): revolute   */
   GB_JOINT_RUBY = 14,        /* about x / y / z with q = (cos t, sin t) taken as given (not        */
   GB_JOINT_RUBZ = 15,        /* renormalised), nq = 2, nv = 1; what the URDF "continuous" joint is */
-  GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED = 16 /* JointModelRevoluteUnboundedUnaligned
+  GB_JOINT_REVOLUTE_UNBOUNDED_UNALIGNED = 16, /* JointModelRevoluteUnboundedUnaligned
                                 (joint-revolute-unbounded-unaligned.hpp): the same about
                                 gb_model_desc.axis */
+  GB_JOINT_SPHERICAL_ZYX = 17 /* JointModelSphericalZYX (joint-spherical-ZYX.hpp): q = the Euler
+                                angles (z, y, x), R = Rz(q0) Ry(q1) Rx(q2), v = dq/dt, nq = nv = 3,
+                                anywhere in the tree (a vector space: integrate adds v dt) */
 };
 enum { GB_MATRIX_UPPER = 0, GB_MATRIX_SYMMETRIC = 1 }; /* CRBA / RNEA-derivative M output */
 /* functions of a heterogeneous batch task / of a launch setting */

@@ -90,14 +90,62 @@ def _out(o, shape):
     return o
 
 
+JT_RX, JT_RY, JT_RZ, JT_ZYX = 1, 2, 3, 17
+
+
+def expand_spherical_zyx(t):
+    """Tables with every spherical ZYX joint (reference JointModelSphericalZYX,
+    multibody/joint/joint-spherical-ZYX.hpp:404-470: M = (Rz(q0) Ry(q1) Rx(q2), 0), S(q) the
+    angular velocity of the Euler rates in the child frame, c = dS/dt v) replaced by revolute
+    joints about z, y and x, the first at the joint's placement, the other two at the identity, the
+    body on the last: the same transform, velocity, acceleration and coordinates, a vector space
+    like the joint.  Returns (tables, rows): rows[j] the joint carrying the caller's joint j (None
+    when the model has no such joint).  The tests pin this against the reference's own known
+    answers for the joint (unittest/joint-spherical.cpp:215-300) and against the joint's closed-form
+    S(q) and c."""
+    jt = [int(j) for j in t["jtype"]]
+    if JT_ZYX not in jt:
+        return t, None
+    nj = len(jt)
+    keys = [k for k, v in t.items() if k not in ("armature", "gravity") and len(v) == nj]
+    new = {k: [] for k in keys}
+    ident = np.array([1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0, 0, 0, 0])
+    rows = []
+
+    def push(row):
+        for k in keys:
+            new[k].append(row[k])
+        return len(new["parents"]) - 1
+
+    for j in range(nj):
+        row = {k: np.array(t[k][j], copy=True) for k in keys}
+        if j > 0:
+            row["parents"] = np.int32(rows[int(t["parents"][j])])
+        if jt[j] == JT_ZYX:
+            for code in (JT_RZ, JT_RY):
+                mid = {k: np.zeros_like(v) for k, v in row.items()}
+                mid["parents"], mid["jtype"] = row["parents"], np.int32(code)
+                mid["placement"] = row["placement"] if code == JT_RZ else ident
+                row["parents"] = np.int32(push(mid))
+            row["jtype"], row["placement"] = np.int32(JT_RX), ident
+        rows.append(push(row))
+    out = dict(t)
+    for k in keys:
+        out[k] = np.ascontiguousarray(np.stack(new[k]).astype(t[k].dtype))
+    return out, np.asarray(rows)
+
+
 class OracleModel:
-    """The oracle's copy of a flattened model (from ``Model.tables()``)."""
+    """The oracle's copy of a flattened model (from ``Model.tables()``); spherical ZYX joints run as
+    the revolute chain of ``expand_spherical_zyx`` with the caller's joint indices mapped."""
 
     def __init__(self, model):
         L = lib()
         t = model.tables()
         if "mimic" in t and t["mimic"].any():
             raise ValueError("a model with mimic joints: use MimicOracleModel")
+        nj_user = int(len(t["parents"]))
+        t, self._rows = expand_spherical_zyx(t)
         self._keep = t
         h = L.orc_model_new(
             int(len(t["parents"])), _ptr(t["parents"]), _ptr(t["jtype"]), _ptr(t["placement"]), _ptr(t["inertia"]),
@@ -109,7 +157,8 @@ class OracleModel:
         nq, nv = C.c_int(), C.c_int()
         L.orc_model_dims(self.h, C.byref(nq), C.byref(nv))
         self.nq, self.nv = nq.value, nv.value
-        self.njoints = int(len(t["parents"]))
+        self.njoints = nj_user
+        self._nj_internal = int(len(t["parents"]))
         self.model = model
 
     def __del__(self):
@@ -128,7 +177,19 @@ class OracleModel:
         f = _c(fext).reshape(B, -1)
         if f.shape[1] != 6 * self.njoints:
             raise ValueError("fext must hold njoints x 6 values per instance")
+        if self._rows is not None:
+            full = np.zeros((B, self._nj_internal, 6))
+            full[:, self._rows] = f.reshape(B, self.njoints, 6)
+            return full.reshape(B, -1)
         return f
+
+    def _desc(self, desc):
+        d = _c(np.asarray(desc).reshape(-1, 46))
+        if self._rows is not None:
+            d = d.copy()
+            for c in (2, 3):
+                d[:, c] = self._rows[d[:, c].astype(np.int64)]
+        return d
 
     def rnea(self, q, v, a, prec=0, nthreads=0, fext=None, out=None):
         q, v, a = _c(q), _c(v), _c(a)
@@ -217,7 +278,7 @@ class OracleModel:
         (12), desired acceleration (6), Kp (6), Kd (6)).  Returns (ddq (B, nv), lambda_c (B, nc),
         iterations (B,), residuals (B, 2): absolute, relative)."""
         q, v, tau = _c(q), _c(v), _c(tau)
-        desc = _c(np.asarray(desc).reshape(-1, 46))
+        desc = self._desc(desc)
         B = q.shape[0]
         nc = int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
         ddq, lam = np.empty((B, self.nv)), np.empty((B, nc))
@@ -235,7 +296,7 @@ class OracleModel:
         (B, n, n), inverse (B, n, n), osim_inverse (B, nc, nc), osim (B, nc, nc), minv (B, nv, nv) and
         jminv (B, nc, nv), n = nc + nv, the constraint rows first."""
         q = _c(q)
-        desc = _c(np.asarray(desc).reshape(-1, 46))
+        desc = self._desc(desc)
         B, nv = q.shape[0], self.nv
         nc = int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
         n = nc + nv
@@ -252,7 +313,7 @@ class OracleModel:
         344-1050) for constraints to the world without Baumgarte gains.  Returns (ddq, lambda_c, ddq_dq,
         ddq_dv, ddq_dtau (B, nv, nv), dlambda_dq, dlambda_dv, dlambda_dtau (B, nc, nv), iterations)."""
         q, v, tau = _c(q), _c(v), _c(tau)
-        desc = _c(np.asarray(desc).reshape(-1, 46))
+        desc = self._desc(desc)
         B, nv = q.shape[0], self.nv
         nc = int(sum(3 if int(d[0]) == 0 else 6 for d in desc))
         ddq, lam = np.empty((B, nv)), np.empty((B, nc))
@@ -284,7 +345,7 @@ class OracleModel:
         """(oMi (B, njoints, 12): R row-major then t; v (B, njoints, 6) or None; a (B, njoints, 6) or None),
         joint 0 the identity / zero -- data.oMi, data.v, data.a after forwardKinematics(q[, v[, a]])."""
         q = _c(q)
-        B, nj = q.shape[0], self.njoints
+        B, nj = q.shape[0], self._nj_internal
         v = None if v is None else _c(v)
         a = None if (a is None or v is None) else _c(a)
         oMi = np.empty((B, nj, 12))
@@ -292,6 +353,9 @@ class OracleModel:
         ai = np.empty((B, nj, 6)) if a is not None else None
         self._check(lib().orc_forward_kinematics(self.h, prec, B, _ptr(q), _ptr(v), _ptr(a), _ptr(oMi), _ptr(vi),
                                                  _ptr(ai), nthreads))
+        if self._rows is not None:
+            pick = lambda x: None if x is None else np.ascontiguousarray(x[:, self._rows])  # noqa: E731
+            return pick(oMi), pick(vi), pick(ai)
         return oMi, vi, ai
 
     def joint_jacobians(self, q, prec=0, nthreads=0):
@@ -369,8 +433,8 @@ class MimicOracleModel:
         self.scaling, self.offset = t["mimic_scaling"], t["mimic_offset"]
         nj = len(self.mimic)
         unb = {13, 14, 15, 16}
-        full_nq = {0: 0, 4: 7, 10: 3, 11: 4, 12: 4, **{j: 2 for j in unb}}
-        full_nv = {0: 0, 4: 6, 10: 3, 11: 3, 12: 3}
+        full_nq = {0: 0, 4: 7, 10: 3, 11: 4, 12: 4, 17: 3, **{j: 2 for j in unb}}
+        full_nv = {0: 0, 4: 6, 10: 3, 11: 3, 12: 3, 17: 3}
         jt = [int(j) for j in t["jtype"]]
         self.fq = np.cumsum([0] + [full_nq.get(j, 1) for j in jt])[:-1]
         self.fv = np.cumsum([0] + [full_nv.get(j, 1) for j in jt])[:-1]
@@ -397,7 +461,7 @@ class MimicOracleModel:
     def to_full(self, q):
         q = np.atleast_2d(np.asarray(q, dtype=np.float64))
         out = np.zeros((q.shape[0], self.nq_full))
-        full_nq = lambda j: 7 if j == 4 else 3 if j == 10 else 4 if j in (11, 12) else 2 if j in self.unb else 1  # noqa: E731
+        full_nq = lambda j: 7 if j == 4 else 3 if j in (10, 17) else 4 if j in (11, 12) else 2 if j in self.unb else 1  # noqa: E731
         for i in range(1, len(self.mimic)):
             m, f = self.mimic[i], self.fq[i]
             if not m:

@@ -24,6 +24,7 @@ from .model import (  # noqa: F401
     JointModelRY,
     JointModelRZ,
     JointModelSpherical,
+    JointModelSphericalZYX,
     JointModelTranslation,
     Model,
     SE3,

@@ -148,6 +148,15 @@ inline int fold_unaligned(gb_model* M, const gb_model_desc* d, std::string* err)
 // kernels then see only one-dof joints there.  `expanded` is the internal tree; user_of[i] is
 // the caller's joint of internal joint i (-1 for the two intermediate ones), last_of[j] the
 // internal joint carrying the caller's joint j.
+//
+// Spherical ZYX joints (JointModelSphericalZYX, joint-spherical-ZYX.hpp:404-470: M = (Rz(q0)
+// Ry(q1) Rx(q2), 0), S(q) the angular velocity of the Euler rates in the child frame, c = dS/dt
+// v) become three revolute joints about z, y and x the same way: the chain's transform is the
+// product of the three rotations, the angular velocity of its last frame is the sum of the three
+// axes' rates carried into that frame (the columns of S(q)), and its acceleration adds the
+// products of those rates (the bias c), so every joint-space quantity and its derivatives in q
+// (a vector space) are the joint's.  The chain is singular where the joint is (cos q1 = 0).
+inline bool expanded_three(int jt) { return jt == GB_JOINT_TRANSLATION || jt == GB_JOINT_SPHERICAL_ZYX; }
 static_assert((int)GB_JOINT_SPHERICAL == (int)gb::JT_SPH && (int)GB_JOINT_PLANAR == (int)gb::JT_PL &&
                   (int)GB_JOINT_FREEFLYER == (int)gb::JT_FF && (int)GB_JOINT_RUBX == (int)gb::JT_RUX &&
                   (int)GB_JOINT_RUBY == (int)gb::JT_RUY && (int)GB_JOINT_RUBZ == (int)gb::JT_RUZ,
@@ -188,6 +197,10 @@ inline int expand_translations(const gb_model_desc* d, ExpandedTree& t, std::str
       const int a = push(t.last_of[pu], GB_JOINT_PX, P, kZero, nullptr, -1);
       const int b = push(a, GB_JOINT_PY, kIdentity, kZero, nullptr, -1);
       t.last_of[j] = push(b, GB_JOINT_PZ, kIdentity, Y, nullptr, j);
+    } else if (d->jtype[j] == GB_JOINT_SPHERICAL_ZYX) {
+      const int a = push(t.last_of[pu], GB_JOINT_RZ, P, kZero, nullptr, -1);
+      const int b = push(a, GB_JOINT_RY, kIdentity, kZero, nullptr, -1);
+      t.last_of[j] = push(b, GB_JOINT_RX, kIdentity, Y, nullptr, j);
     } else {
       t.last_of[j] = push(t.last_of[pu], d->jtype[j], P, Y, ax, j);
     }
@@ -249,24 +262,24 @@ inline void build_mimic_maps(gb_model* M, const gb_model_desc* du, const Expande
     rq[j] = nq;
     rv[j] = nv;
     nq += jt == GB_JOINT_FREEFLYER ? 7 : (jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR) ? 4
-          : jt == GB_JOINT_TRANSLATION ? 3 : unbounded_type(jt) ? 2 : 1;
+          : expanded_three(jt) ? 3 : unbounded_type(jt) ? 2 : 1;
     nv += jt == GB_JOINT_FREEFLYER ? 6 : (jt == GB_JOINT_SPHERICAL || jt == GB_JOINT_PLANAR ||
-                                          jt == GB_JOINT_TRANSLATION) ? 3 : 1;
+                                          expanded_three(jt)) ? 3 : 1;
   }
   M->nq_red = nq;
   M->nv_red = nv;
   M->qmap.assign(M->nq, gb::MimicQ{});
   M->vmap.assign(M->nv, gb::MimicV{});
-  // internal joints of each caller joint: a translation joint's three, otherwise its own
+  // internal joints of each caller joint: a translation or ZYX joint's three, otherwise its own
   for (int i = 1; i < M->nj; ++i) {
     int j = tree.user_of[i];
     int k = 0;  // position of internal joint i among its caller joint's internal joints
-    if (j < 0) {  // the first two joints of an expanded translation: the caller joint is the last's
+    if (j < 0) {  // the first two joints of an expanded joint: the caller joint is the last's
       int l = i;
       while (tree.user_of[l] < 0) ++l;
       j = tree.user_of[l];
       k = 2 - (l - i);
-    } else if (du->jtype[j] == GB_JOINT_TRANSLATION) {
+    } else if (expanded_three(du->jtype[j])) {
       k = 2;
     }
     const int m = du->mimic ? du->mimic[j] : 0;

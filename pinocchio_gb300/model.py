@@ -11,7 +11,7 @@ free-flyer) and flattens the tree into the plain tables the C ABI takes:
 * ``parents`` (int32, njoints), ``jtype`` (int32, njoints; 0 = universe,
   1/2/3 = RX/RY/RZ, 4 = free-flyer, 5/6/7 = PX/PY/PZ, 8 = revolute unaligned,
   9 = prismatic unaligned, 10 = translation, 11 = spherical, 12 = planar, 13/14/15 = unbounded
-  revolute RUBX/RUBY/RUBZ, 16 = unbounded revolute unaligned),
+  revolute RUBX/RUBY/RUBZ, 16 = unbounded revolute unaligned, 17 = spherical ZYX),
 * ``axis`` (njoints x 3: the unit axis of an unaligned joint, zero otherwise),
 * ``placement`` (njoints x 12: rotation row-major, then translation),
 * ``inertia`` (njoints x 10: mass, lever (COM), rotational inertia about the COM
@@ -23,11 +23,12 @@ from __future__ import annotations
 import numpy as np
 
 (JT_NONE, JT_RX, JT_RY, JT_RZ, JT_FF, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU, JT_TR, JT_SPH, JT_PL, JT_RUBX, JT_RUBY,
- JT_RUBZ, JT_RUBU) = range(17)
+ JT_RUBZ, JT_RUBU, JT_ZYX) = range(18)
 _ONE_DOF = (JT_RX, JT_RY, JT_RZ, JT_PX, JT_PY, JT_PZ, JT_RU, JT_PU)
 UNBOUNDED = (JT_RUBX, JT_RUBY, JT_RUBZ, JT_RUBU)
-_JT_NQ = {JT_NONE: 0, JT_FF: 7, JT_TR: 3, JT_SPH: 4, JT_PL: 4, **{j: 1 for j in _ONE_DOF}, **{j: 2 for j in UNBOUNDED}}
-_JT_NV = {JT_NONE: 0, JT_FF: 6, JT_TR: 3, JT_SPH: 3, JT_PL: 3, **{j: 1 for j in _ONE_DOF + UNBOUNDED}}
+_JT_NQ = {JT_NONE: 0, JT_FF: 7, JT_TR: 3, JT_ZYX: 3, JT_SPH: 4, JT_PL: 4, **{j: 1 for j in _ONE_DOF},
+          **{j: 2 for j in UNBOUNDED}}
+_JT_NV = {JT_NONE: 0, JT_FF: 6, JT_TR: 3, JT_ZYX: 3, JT_SPH: 3, JT_PL: 3, **{j: 1 for j in _ONE_DOF + UNBOUNDED}}
 PRISMATIC = (JT_PX, JT_PY, JT_PZ, JT_PU)
 
 
@@ -91,6 +92,14 @@ class JointModelSpherical(JointModel):
     frame (reference JointModelSphericalTpl, multibody/joint/joint-spherical.hpp)."""
 
     jtype = JT_SPH
+
+
+class JointModelSphericalZYX(JointModel):
+    """Rotation by the Euler angles q = (z, y, x), R = Rz(q0) Ry(q1) Rx(q2), v = dq/dt (reference
+    JointModelSphericalZYXTpl, multibody/joint/joint-spherical-ZYX.hpp); a vector space
+    (integrate adds v dt), singular where cos q1 = 0."""
+
+    jtype = JT_ZYX
 
 
 class JointModelPlanar(JointModel):

@@ -32,6 +32,7 @@ from .model import (
     JT_PL,
     JT_SPH,
     JT_TR,
+    JT_ZYX,
     PRISMATIC,
     UNBOUNDED,
     Inertia,
@@ -48,6 +49,7 @@ from .model import (
     JointModelRX,
     JointModelRY,
     JointModelRZ,
+    JointModelSphericalZYX,
     JointModelTranslation,
     Model,
     SE3,
@@ -244,6 +246,23 @@ def translation_tree(seed: int = 9) -> Model:
     return model
 
 
+def zyx_tree(seed: int = 12) -> Model:
+    """A tree with spherical ZYX joints (JointModelSphericalZYX) at the root, inside a chain and at
+    a leaf, among revolute and prismatic joints and a translation joint: nv 16."""
+    rng = np.random.default_rng(seed)
+    model = Model()
+    model.name = "zyxtree16"
+    root = _add_link(model, rng, 0, JointModelSphericalZYX(), "base")
+    a = _add_link(model, rng, root, _random_revolute(rng), "a1")
+    a = _add_link(model, rng, a, JointModelSphericalZYX(), "a2")
+    a = _add_link(model, rng, a, _random_one_dof(rng), "a3")
+    b = _add_link(model, rng, root, JointModelTranslation(), "b1")
+    b = _add_link(model, rng, b, _random_revolute(rng), "b2")
+    _add_link(model, rng, b, JointModelSphericalZYX(), "b3")
+    _add_link(model, rng, root, _random_one_dof(rng), "c1")
+    return model
+
+
 def multidof_tree(seed: int = 10) -> Model:
     """A tree with every three-dof joint type: a planar root, a spherical torso, a translation
     joint and a spherical leaf among revolute joints: nv 16."""
@@ -316,7 +335,8 @@ def heterogeneous_trees(seed: int = 3):
 def random_configurations(model: Model, batch: int, rng: np.random.Generator) -> np.ndarray:
     """q of shape (batch, nq): FF position N(0,1), uniform unit quaternion; revolute angles
     U[-pi, pi] (unbounded revolute joints: their cos and sin); prismatic displacements
-    U[-0.5, 0.5] m."""
+    U[-0.5, 0.5] m; spherical ZYX angles U[-pi, pi] with the middle one in U[-1.2, 1.2] (away
+    from the joint's singularity at +-pi/2)."""
     q = np.empty((batch, model.nq))
     for jt, iq, m in zip(model.jtypes[1:], model.idx_qs[1:], model.mimic[1:]):
         if m:  # a mimic joint has no entry of its own
@@ -326,6 +346,9 @@ def random_configurations(model: Model, batch: int, rng: np.random.Generator) ->
             q[:, iq + 3 : iq + 7] = random_unit_quaternion(rng, batch)
         elif jt == JT_TR:
             q[:, iq : iq + 3] = rng.uniform(-0.5, 0.5, (batch, 3))
+        elif jt == JT_ZYX:
+            q[:, iq : iq + 3] = rng.uniform(-np.pi, np.pi, (batch, 3))
+            q[:, iq + 1] = rng.uniform(-1.2, 1.2, batch)
         elif jt == JT_SPH:
             q[:, iq : iq + 4] = random_unit_quaternion(rng, batch)
         elif jt == JT_PL:

@@ -78,7 +78,7 @@ def test_tree_validation(L):
     # an unknown joint type code
     t = sm.manipulator6r().tables()
     t["jtype"] = t["jtype"].copy()
-    t["jtype"][3] = 17
+    t["jtype"][3] = 18
     rc, _ = _create(L, t)
     assert rc == _capi.GB_ERR_UNSUPPORTED
     # armature of the wrong size

@@ -178,3 +178,32 @@ def test_translation_joints_keep_the_callers_joint_indexing():
     oMo, vo, ao = OracleModel(model).forward_kinematics(q, v, a)
     assert oMi.shape == oMo.shape
     assert rel_err(oMi, oMo) < FP64_TOL and rel_err(vi, vo) < FP64_TOL and rel_err(ai, ao) < FP64_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_spherical_zyx_reference_known_answers(precision):
+    """One spherical ZYX joint (three revolute joints inside the kernels) with a unit mass at (0.5,
+    0, 0) and unit rotational inertia: rnea, crba and aba (M^-1 (tau - nle)) at the reference's own
+    known answers (unittest/joint-spherical.cpp:215-300); the C ABI reports the caller's joint."""
+    m = pg.Model()
+    j = m.addJoint(0, pg.JointModelSphericalZYX(), pg.SE3.Identity(), "root")
+    m.appendBodyToJoint(j, pg.Inertia(1.0, [0.5, 0.0, 0.0], np.eye(3)))
+    data = pg.createData(m, precision)
+    nq, nv, nj = C.c_int(), C.c_int(), C.c_int()
+    _capi.check(_capi.lib().gb_model_dims(data.dev.h, C.byref(nq), C.byref(nv), C.byref(nj)))
+    assert (nq.value, nv.value, nj.value) == (3, 3, 2)
+    qs = np.array([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0], [3.0, 2.0, 1.0]])
+    va = np.array([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0], [1.0, 1.0, 1.0]])
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    tau = np.asarray(pg.rnea(m, data, qs, va, va))
+    expected = np.array([[0.0, -4.905, 0.0],
+                         [-0.53611600195085, -0.74621832606188, -0.38177329067604],
+                         [0.73934458094049, 2.7804530848031, 0.50684940972146]])
+    assert np.allclose(tau, expected, rtol=0, atol=tol * 10)
+    M = np.asarray(pg.crba(m, data, qs))
+    Mexp = np.array([[[1.25, 0, 0], [0, 1.25, 0], [0, 0, 1.0]],
+                     [[1.0729816454316, 0, -0.8414709848079], [0, 1.25, 0], [-0.8414709848079, 0, 1.0]],
+                     [[1.043294547392, 0, -0.90929742682568], [0, 1.25, 0], [-0.90929742682568, 0, 1.0]]])
+    assert np.allclose(M, Mexp, rtol=0, atol=tol * 10)
+    ddq = np.asarray(pg.aba(m, data, qs, va, expected))
+    assert np.allclose(ddq, va, rtol=0, atol=tol * 100)

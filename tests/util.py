@@ -36,6 +36,7 @@ MODELS = {
     "translationtree14": lambda: sm.translation_tree(9),
     "multidoftree16": lambda: sm.multidof_tree(10),
     "unbounded15ff": lambda: sm.unbounded_tree(15, True, 11),
+    "zyxtree16": lambda: sm.zyx_tree(12),
 }
 # models the oracle covers beyond the kernels (none at present)
 ORACLE_ONLY_MODELS = {}
@@ -47,7 +48,7 @@ MIXED_TOL = 1e-5
 # workload: their FP64 results meet FP64_TOL; their mixed-precision error, which scales with
 # each random model's conditioning, is held to 1e-4
 JOINT_TYPE_MODELS = ("mixedtree12", "mixedtree24ff", "unaligned14", "unaligned20ff", "translationtree14",
-                     "multidoftree16", "unbounded15ff")
+                     "multidoftree16", "unbounded15ff", "zyxtree16")
 
 
 def mixed_tol(name: str) -> float:
