@@ -10,6 +10,13 @@ children in file order, as MjcfGraph::parseGraph / fillModel do:
   pos^-1``); ``hinge`` -> revolute, ``slide`` -> prismatic (aligned or unaligned by the axis, as the
   URDF loader maps axes), ``ball`` -> the spherical joint (mjcf-graph.cpp:946-951), ``free`` -> the
   free-flyer (root body only);
+* a ``<body>`` with several joints (the reference's composite joint, mjcf-graph.cpp:1002-1083: its
+  first component at ``body pose * pos_0``, component k at ``pos_{k-1}^-1 pos_k`` from the one
+  before, the body at ``pos_last^-1``, the joint's transform the product of the components') becomes
+  the same product as a chain of joints with massless links between them: the same q, v,
+  kinematics and dynamics, with one joint per component (the last, which carries the body and the
+  composite joint's frame, named ``Composite_<first joint's name>`` as the reference's composite
+  joint; the others by their own names); each component's armature on its dofs;
 * a body without a joint is welded to its parent: its inertia is merged into the parent's joint
   (addFixedJointAndBody);
 * body poses: ``pos`` with ``quat`` (w x y z), ``axisangle`` or ``euler`` (the compiler's
@@ -35,8 +42,8 @@ children in file order, as MjcfGraph::parseGraph / fillModel do:
   and hfield geoms keep the unit inertia the reference gives them.
 
 Outside the subset (each raises ValueError, so that no model is silently different from the
-reference's): ``<include>`` and ``<frame>``, bodies with several joints (the reference's composite
-joints), free joints below the root, ``xyaxes`` / ``zaxis`` orientations, uppercase (fixed-axis)
+reference's): ``<include>`` and ``<frame>``, a free joint among a body's several joints (the
+reference refuses it too), free joints below the root, ``xyaxes`` / ``zaxis`` orientations, uppercase (fixed-axis)
 Euler sequences, ``shellinertia`` geoms.
 """
 from __future__ import annotations
@@ -308,28 +315,35 @@ def buildModelFromMJCFXML(xml: str) -> Model:
         jattrs = {id(j): classes.attributes(j, childclass) for j in body.findall("joint")}
         joints = [("free", j) for j in body.findall("freejoint")] + [
             (jattrs[id(j)].get("type", "hinge"), j) for j in body.findall("joint")]
-        if len(joints) > 1:
-            raise ValueError(f"body {body.get('name')!r}: several joints (a composite joint) are not supported")
+        if len(joints) > 1 and any(kind == "free" for kind, _ in joints):
+            raise ValueError(f"body {body.get('name')!r}: a composite joint cannot hold a free joint")
         Y = _body_inertia(body, comp, classes, childclass)
         if not joints:  # welded to the parent body
             if parent_joint > 0 and (Y.mass > 0.0 or Y.inertia.any()):
                 model.appendBodyToJoint(parent_joint, Y, pose)
             child_frame = (parent_joint, pose)
         else:
-            kind, j = joints[0]
-            name = j.get("name") or (body.get("name", "") + "_joint")
-            jpos = SE3(np.eye(3), _floats(j.get("pos"), 3, [0, 0, 0]))
-            if kind == "free":
-                if parent_joint != 0 or j.get("pos") is not None:
-                    raise ValueError(f"joint {name!r}: a free joint is supported on a root body only")
-                jid = model.addJoint(0, JointModelFreeFlyer(), pose, name)
-            else:
-                jid = model.addJoint(parent_joint, _joint_model(j, comp, jattrs[id(j)]), _mul(pose, jpos), name)
-                arm = float(jattrs[id(j)].get("armature", "0"))
-                if arm:
-                    iv = model.idx_vs[jid]
-                    model.armature[iv:iv + model.nvs[jid]] = arm
-            body_in_joint = SE3(np.eye(3), -jpos.translation)
+            jid, prev = parent_joint, None
+            first = joints[0][1].get("name") or (body.get("name", "") + "_joint")
+            for n, (kind, j) in enumerate(joints):
+                name = j.get("name") or (body.get("name", "") + "_joint")
+                if len(joints) > 1 and n == len(joints) - 1:
+                    name = "Composite_" + first
+                jpos = _floats(j.get("pos"), 3, [0, 0, 0])
+                if kind == "free":
+                    if parent_joint != 0 or j.get("pos") is not None:
+                        raise ValueError(f"joint {name!r}: a free joint is supported on a root body only")
+                    jid = model.addJoint(0, JointModelFreeFlyer(), pose, name)
+                else:
+                    # the first component at body pose * pos_0, the next ones at pos_{k-1}^-1 pos_k
+                    place = _mul(pose, SE3(np.eye(3), jpos)) if prev is None else SE3(np.eye(3), jpos - prev)
+                    jid = model.addJoint(jid, _joint_model(j, comp, jattrs[id(j)]), place, name)
+                    arm = float(jattrs[id(j)].get("armature", "0"))
+                    if arm:
+                        iv = model.idx_vs[jid]
+                        model.armature[iv:iv + model.nvs[jid]] = arm
+                prev = jpos
+            body_in_joint = SE3(np.eye(3), -prev)
             if Y.mass > 0.0 or Y.inertia.any():
                 model.appendBodyToJoint(jid, Y, body_in_joint)
             child_frame = (jid, body_in_joint)

@@ -120,7 +120,8 @@ def test_orientation_forms_and_units():
 
 
 @pytest.mark.parametrize("snippet, msg", [
-    ('<worldbody><body name="a"><joint/><joint type="slide"/><inertial mass="1" diaginertia="1 1 1"/></body></worldbody>', "several"),
+    ('<worldbody><body name="a"><freejoint/><joint type="slide"/><inertial mass="1" diaginertia="1 1 1"/></body>'
+     '</worldbody>', "composite joint cannot hold a free joint"),
     ('<default><default><joint/></default></default><worldbody/>', "Class does not have a name"),
     ('<worldbody><body name="a" childclass="x"><joint/></body></worldbody>', "unknown class"),
     ('<worldbody><body name="a"><joint/><geom type="box" size="0.1 0.1 0.1" shellinertia="true"/></body></worldbody>',
@@ -237,3 +238,49 @@ def test_ball_joint():
     ref.armature[1:] = 0.05
     q, v, a = sm.random_inputs(m, 8, 4)
     assert rel_err(OracleModel(m).rnea(q, v, a), OracleModel(ref).rnea(q, v, a)) < 1e-14
+
+
+def _se3(R, t):
+    T = np.eye(4)
+    T[:3, :3], T[:3, 3] = R, t
+    return T
+
+
+def test_composite_joint():
+    """A body with a hinge about y at (0, 0, 0.1), an unaligned slide at (0.05, 0, 0) and a hinge about
+    x: the reference's composite joint (mjcf-graph.cpp:1002-1083) as a chain of three joints with
+    massless links, the last named Composite_<first>; the body frame placed by the composite's
+    product body pose * pos_0 * M_0(q_0) * (pos_0^-1 pos_1) * M_1(q_1) * (pos_1^-1 pos_2) * M_2(q_2),
+    the body at pos_2^-1, each component's armature on its dof."""
+    m = buildModelFromMJCFXML("""<mujoco><compiler angle="radian"/><worldbody>
+      <body name="base" pos="0 0 1"><joint name="yaw" type="hinge" axis="0 0 1"/>
+        <inertial mass="1" diaginertia="0.1 0.2 0.3"/>
+        <body name="hip" pos="0.2 0 -0.1" axisangle="0 0 1 0.4">
+          <joint name="hy" type="hinge" axis="0 1 0" pos="0 0 0.1" armature="0.02"/>
+          <joint name="ext" type="slide" axis="1 1 0" pos="0.05 0 0"/>
+          <joint name="hx" type="hinge" axis="1 0 0" armature="0.03"/>
+          <inertial pos="0 0 -0.2" mass="2" diaginertia="0.02 0.03 0.04"/>
+          <body name="foot" pos="0 0 -0.4"><joint name="ankle" type="hinge" axis="0 1 0"/>
+            <inertial mass="0.5" diaginertia="0.01 0.01 0.01"/></body>
+        </body></body></worldbody></mujoco>""")
+    assert m.names == ["universe", "yaw", "hy", "ext", "Composite_hy", "ankle"]
+    assert m.jtypes[1:] == [gm.JT_RZ, gm.JT_RY, gm.JT_PU, gm.JT_RX, gm.JT_RY]
+    assert m.parents == [0, 0, 1, 2, 3, 4] and (m.nq, m.nv) == (5, 5)
+    assert np.array_equal(m.armature, [0, 0.02, 0, 0.03, 0])
+    q = np.random.default_rng(5).uniform(-1, 1, (6, 5))
+    oMi, _, _ = OracleModel(m).forward_kinematics(q)
+    a = np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0)
+    pos = [np.array([0, 0, 0.1]), np.array([0.05, 0, 0]), np.zeros(3)]
+    for b in range(6):
+        T = _se3(np.eye(3), [0, 0, 1]) @ _se3(_rot([0, 0, 1], q[b, 0]), np.zeros(3))
+        T = T @ _se3(_rot([0, 0, 1], 0.4), [0.2, 0, -0.1]) @ _se3(np.eye(3), pos[0])
+        T = T @ _se3(_rot([0, 1, 0], q[b, 1]), np.zeros(3)) @ _se3(np.eye(3), pos[1] - pos[0])
+        T = T @ _se3(np.eye(3), a * q[b, 2]) @ _se3(np.eye(3), pos[2] - pos[1])
+        T = T @ _se3(_rot([1, 0, 0], q[b, 3]), np.zeros(3))
+        got = _se3(oMi[b, 4, :9].reshape(3, 3), oMi[b, 4, 9:])
+        assert np.allclose(got, T, atol=1e-13)
+        foot = T @ _se3(np.eye(3), -pos[2]) @ _se3(np.eye(3), [0, 0, -0.4]) @ _se3(_rot([0, 1, 0], q[b, 4]), np.zeros(3))
+        assert np.allclose(_se3(oMi[b, 5, :9].reshape(3, 3), oMi[b, 5, 9:]), foot, atol=1e-13)
+    # the body hangs from the last component: its centre of mass at pos_2^-1 * (0, 0, -0.2)
+    assert np.allclose(m.tables()["inertia"][4, :4], [2.0, 0.0, 0.0, -0.2])
+    assert m.tables()["inertia"][2:4, 0].sum() == 0.0  # massless links between the components
