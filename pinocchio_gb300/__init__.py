@@ -25,6 +25,7 @@ from .model import (  # noqa: F401
     JointModelRZ,
     JointModelSpherical,
     JointModelSphericalZYX,
+    JointModelComposite,
     JointModelTranslation,
     Model,
     SE3,

@@ -161,6 +161,36 @@ class JointModelPrismaticUnaligned(JointModel):
         self.axis = _unit(axis)
 
 
+class JointModelComposite(JointModel):
+    """A joint made of component joints, each placed relative to the frame of the one before
+    (reference JointModelCompositeTpl, multibody/joint/joint-composite.hpp:286-290 addJoint(jmodel,
+    placement); joint-composite.hxx:40-77: M = prod_k placement_k M_k(q_k), q and v the components'
+    in order).  ``Model.addJoint`` adds it as the chain of its components with massless links
+    between them: the same product, q, v, kinematics and dynamics, one model joint per component.
+    The last carries the composite's name and bodies and is the index addJoint returns; the others
+    are named ``<name>_<k>``."""
+
+    def __init__(self, joint: JointModel | None = None, placement: "SE3 | None" = None):
+        self.joints, self.placements = [], []
+        if joint is not None:
+            self.addJoint(joint, placement)
+
+    def addJoint(self, joint: JointModel, placement: "SE3 | None" = None) -> "JointModelComposite":
+        if isinstance(joint, (JointModelComposite, JointModelMimic)):
+            raise ValueError("a composite joint's components are plain joint models")
+        self.joints.append(joint)
+        self.placements.append(SE3.Identity() if placement is None else placement)
+        return self
+
+    @property
+    def nq(self) -> int:
+        return sum(j.nq for j in self.joints)
+
+    @property
+    def nv(self) -> int:
+        return sum(j.nv for j in self.joints)
+
+
 class JointModelMimic(JointModel):
     """A joint that follows another one-dof joint (reference JointModelMimicTpl,
     multibody/joint/joint-mimic.hpp:557-760): ``JointModelMimic(joint, mimicked_joint_id, scaling,
@@ -201,6 +231,9 @@ class SE3:
 
     def act_point(self, p):
         return self.rotation @ p + self.translation
+
+    def __mul__(self, other: "SE3") -> "SE3":
+        return SE3(self.rotation @ other.rotation, self.rotation @ other.translation + self.translation)
 
 
 class Inertia:
@@ -258,6 +291,13 @@ class Model:
     def addJoint(self, parent_id: int, joint: JointModel, placement: SE3, name: str = "") -> int:
         if not 0 <= parent_id < self.njoints:
             raise ValueError("parent joint index out of range")
+        if isinstance(joint, JointModelComposite):
+            if not joint.joints:
+                raise ValueError("a composite joint without components")
+            jid, n = parent_id, len(joint.joints)
+            for k, (jm, P) in enumerate(zip(joint.joints, joint.placements)):
+                jid = self.addJoint(jid, jm, placement * P if k == 0 else P, name if k == n - 1 else f"{name}_{k}")
+            return jid
         if isinstance(joint, JointModelMimic):
             m = joint.mimicked
             if not 0 < m < self.njoints or self.mimic[m] != 0:
