@@ -103,7 +103,7 @@ def test_autotuner_keeps_results(tmp_path, monkeypatch):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100", "mixedtree24ff"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100", "mixedtree24ff", "zyxtree16"])
 def test_warp_layout_matches_thread_layout_bitwise(name, precision):
     """The warp-per-instance and lane-per-branch layouts (gb_model_set_layout) give
     the thread layout's results for RNEA, ABA, nonLinearEffects and gravity -- the same bits in FP64,
@@ -155,7 +155,7 @@ def test_layout_setting_errors():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100", "mixedtree24ff"])
+@pytest.mark.parametrize("name", ["manipulator6r", "humanoid32", "tree60ff", "chain100", "mixedtree24ff", "zyxtree16"])
 def test_team_layouts_aba_derivatives(name, precision):
     """The ABA derivatives with a team of 4, 8 or 32 lanes per configuration
     (the lanes split the column loops of the sweeps) give the thread layout's
@@ -244,3 +244,26 @@ def test_three_dof_joints_run_per_thread(tmp_path, monkeypatch):
     assert rel_err(outs[0], ddq_o) < FP64_TOL
     assert rel_err(outs[1], OracleModel(other).rnea(*(t.cpu().numpy() for t in (q2, v2, x2)))) < FP64_TOL
     assert rel_err(outs[2], OracleModel(model).rnea(*(t.cpu().numpy() for t in (q, v, x)))) < FP64_TOL
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", 1e-4)])
+def test_multi_with_spherical_zyx_joints(precision, tol):
+    """A launch over the ZYX tree (its joints run as revolute chains) and the humanoid: every task
+    against the oracle and the single-model call."""
+    import torch
+
+    tasks, ref = [], []
+    for k, model in enumerate((sm.zyx_tree(), sm.humanoid32(1))):
+        q, v, x = sm.random_inputs(model, 300 + 100 * k, 30 + k)
+        data = pg.createData(model, precision)
+        d = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+        tasks += [(data, "aba", d(q), d(v), d(10.0 * x)), (data, "rnea", d(q), d(v), d(x))]
+        ref.append((model, data, q, v, x))
+    outs = [o.cpu().numpy() for o in api.MultiBatch(tasks, precision).run()]
+    for k, (model, data, q, v, x) in enumerate(ref):
+        om = OracleModel(model)
+        assert rel_err(outs[2 * k], om.aba(q, v, 10.0 * x, LOCAL)) < tol
+        assert rel_err(outs[2 * k + 1], om.rnea(q, v, x)) < tol
+        single = pg.aba(model, data, torch.from_numpy(q).cuda(), torch.from_numpy(v).cuda(),
+                        torch.from_numpy(10.0 * x).cuda())
+        assert np.array_equal(single.cpu().numpy(), outs[2 * k])
