@@ -125,3 +125,36 @@ def test_functions_without_mimic_support_are_refused(case):
     nve = C.c_int()
     _capi.check(L.gb_model_nv_extended(data.dev.h, C.byref(nve)))
     assert nve.value == model.nvExtended
+
+
+def test_mimic_with_expanded_joints():
+    """Mimic joints in a tree whose spherical ZYX and translation joints the model builder expands
+    into chains: the maps from the caller's q and v to the extended tree skip the expanded joints'
+    internal links (rnea, crba and the kinematics against the oracle)."""
+    import torch
+
+    rng = np.random.default_rng(12)
+    m = pg.Model()
+    a = m.addJoint(0, pg.JointModelSphericalZYX(), sm.random_placement(rng), "a")
+    m.appendBodyToJoint(a, sm.random_inertia(rng))
+    b = m.addJoint(a, pg.JointModelRZ(), sm.random_placement(rng), "b")
+    m.appendBodyToJoint(b, sm.random_inertia(rng))
+    c = m.addJoint(b, pg.JointModelTranslation(), sm.random_placement(rng), "c")
+    m.appendBodyToJoint(c, sm.random_inertia(rng))
+    d = m.addJoint(c, pg.JointModelMimic(pg.JointModelPY(), b, -0.7, 0.2), sm.random_placement(rng), "d")
+    m.appendBodyToJoint(d, sm.random_inertia(rng))
+    e = m.addJoint(d, pg.JointModelSphericalZYX(), sm.random_placement(rng), "e")
+    m.appendBodyToJoint(e, sm.random_inertia(rng))
+    assert (m.nq, m.nv, m.nvExtended) == (10, 10, 11)
+    om = MimicOracleModel(m)
+    q, v, x = sm.random_inputs(m, 64, 5)
+    dev = lambda t: torch.from_numpy(np.ascontiguousarray(t)).cuda()  # noqa: E731
+    data = pg.createData(m)
+    assert rel_err(pg.rnea(m, data, dev(q), dev(v), dev(x)).cpu().numpy(), om.rnea(q, v, x)) < FP64_TOL
+    assert rel_err(pg.crba(m, data, dev(q)).cpu().numpy(), om.crba(q)) < FP64_TOL
+    outs = [t.cpu().numpy() for t in pg.forwardKinematics(m, data, dev(q), dev(v), dev(x))]
+    for o, r in zip(outs, om.forward_kinematics(q, v, x)):
+        assert rel_err(o, r) < FP64_TOL
+    J = pg.computeJointJacobians(m, data, dev(q)).cpu().numpy()
+    assert rel_err(J, np.swapaxes(om.joint_jacobians(q), 1, 2)) < FP64_TOL
+    assert rel_err(pg.integrate(m, dev(q), dev(0.1 * v)).cpu().numpy(), om.integrate(q, 0.1 * v)) < 1e-15
